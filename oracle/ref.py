@@ -1,0 +1,82 @@
+"""ctypes bindings to oracle/_ref/libcrnref.so: the reference crnlib compiled from its own
+sources by oracle/Makefile (target `ref`). Test infrastructure only: used to generate and
+re-check the golden fixtures under tests/golden/. The library only exists where the reference
+tree is available (the build container); on other hosts `available()` is False."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PATH = os.path.join(_HERE, "_ref", "libcrnref.so")
+_lib = None
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_u32 = ctypes.c_uint32
+
+
+def available() -> bool:
+    return os.path.exists(_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(_PATH)
+        L.ref_compress_blocks.argtypes = [ctypes.c_void_p, _u32, _u32, _u32, _u32, ctypes.c_void_p]
+        L.ref_compress_blocks.restype = ctypes.c_int
+        L.ref_compress_blocks_mt.argtypes = [ctypes.c_void_p, _u32, _u32, _u32, _u32, ctypes.c_void_p, _u32,
+                                             ctypes.POINTER(ctypes.c_double)]
+        L.ref_compress_blocks_mt.restype = ctypes.c_int
+        L.ref_compress_texture.argtypes = [ctypes.c_void_p, _u32, _u32, _u32, _u32, _u32, _u32, _u32, _u32, _u32,
+                                           _u32, ctypes.c_void_p, _u32]
+        L.ref_compress_texture.restype = _u32
+        L.ref_unpack_level.argtypes = [ctypes.c_void_p, _u32, _u32, ctypes.c_void_p, _u32]
+        L.ref_unpack_level.restype = _u32
+        L.ref_time_unpack.argtypes = [ctypes.c_void_p, _u32, _u32, ctypes.c_void_p, _u32]
+        L.ref_time_unpack.restype = ctypes.c_double
+        _lib = L
+    return _lib
+
+
+def compress_blocks(blocks: np.ndarray, fmt: int, flags: int, dxt_quality: int = 4, threads: int = 1) -> np.ndarray:
+    """blocks: (n, 64) uint8 RGBA 4x4 blocks -> (n, bytes_per_block) uint8 DXT blocks."""
+    blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+    n = blocks.shape[0]
+    out = np.zeros(n * 16, np.uint8)
+    if threads > 1:
+        secs = ctypes.c_double()
+        bpb = lib().ref_compress_blocks_mt(blocks.ctypes.data, n, fmt, flags, dxt_quality, out.ctypes.data, threads,
+                                           ctypes.byref(secs))
+    else:
+        bpb = lib().ref_compress_blocks(blocks.ctypes.data, n, fmt, flags, dxt_quality, out.ctypes.data)
+    if bpb <= 0:
+        raise RuntimeError("reference block compressor failed")
+    return out[: n * bpb].reshape(n, bpb)
+
+
+def compress_texture(levels_faces: list[list[np.ndarray]], fmt: int, file_type: int, quality: int, flags: int,
+                     dxt_quality: int = 4, helper_threads: int = 0) -> bytes:
+    """levels_faces[f][l] = (h, w, 4) uint8 images -> .crn (file_type 0) / .dds (1) bytes."""
+    faces = len(levels_faces)
+    levels = len(levels_faces[0])
+    h, w = levels_faces[0][0].shape[:2]
+    flat = np.concatenate([np.ascontiguousarray(im).reshape(-1) for face in levels_faces for im in face])
+    cap = max(1 << 20, flat.size * 2)
+    out = np.zeros(cap, np.uint8)
+    size = lib().ref_compress_texture(flat.ctypes.data, w, h, levels, faces, fmt, file_type, quality, flags,
+                                      dxt_quality, helper_threads, out.ctypes.data, cap)
+    if size == 0 or size > cap:
+        raise RuntimeError("reference crn_compress failed")
+    return out[:size].tobytes()
+
+
+def unpack_level(crn: bytes, level: int, out_size: int) -> np.ndarray:
+    src = np.frombuffer(crn, np.uint8)
+    out = np.zeros(out_size, np.uint8)
+    n = lib().ref_unpack_level(src.ctypes.data, len(crn), level, out.ctypes.data, out_size)
+    if n == 0:
+        raise RuntimeError("reference crnd_unpack_level failed")
+    return out[:n]

@@ -1,0 +1,169 @@
+// Golden-vector harness around the reference crnlib (test infrastructure only).
+//
+// This file is compiled together with the reference's own sources by oracle/Makefile into
+// oracle/_ref/libcrnref.so. It exposes a small extern "C" surface that the golden-fixture
+// generator (tests/golden/make_golden.py) drives through ctypes. Nothing in the product
+// links or loads this library.
+//
+// Entry points used (reference file:line):
+//   crn_create_block_compressor / crn_compress_block / crn_free_block_compressor
+//       inc/crnlib.h:674-682, crnlib/crnlib.cpp:351-418 (dxt_image::set_block_pixels stack)
+//   crn_compress (comp params + mip params)   inc/crnlib.h:614, crnlib/crnlib.cpp:242-267
+//   crnd_unpack_begin / crnd_unpack_level / crnd_unpack_end   inc/crn_defs.h:174-205
+//   crnd_get_texture_info / crnd_get_level_info              inc/crn_defs.h:152-160
+#include <cstdint>
+#include <cstring>
+#include <cstdlib>
+#include <vector>
+#include <thread>
+#include <atomic>
+#include <chrono>
+
+#include "crnlib.h"
+#include "crn_defs.h"
+
+namespace {
+
+crn_comp_params make_params(uint32_t fmt, uint32_t flags, uint32_t dxt_quality) {
+  crn_comp_params p;
+  p.m_format = static_cast<crn_format>(fmt);
+  p.m_flags = flags;
+  p.m_dxt_quality = static_cast<crn_dxt_quality>(dxt_quality);
+  p.m_width = 4;
+  p.m_height = 4;
+  return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Compresses n independent 4x4 blocks (n x 16 RGBA8 pixels, row-major inside the block)
+// with one reference block-compressor context. flags are crn_comp_flags; pass
+// cCRNCompFlagDisableEndpointCaching (32) for thread-count-independent results.
+// out receives n x bytes_per_block. Returns bytes per block, or 0 on failure.
+int ref_compress_blocks(const uint8_t* rgba, uint32_t n, uint32_t fmt, uint32_t flags,
+                        uint32_t dxt_quality, uint8_t* out) {
+  crn_comp_params p = make_params(fmt, flags, dxt_quality);
+  crn_block_compressor_context_t ctx = crn_create_block_compressor(p);
+  if (!ctx) return 0;
+  const uint32_t bpb = crnd::crnd_get_bytes_per_dxt_block(p.m_format);
+  for (uint32_t i = 0; i < n; i++) {
+    crn_compress_block(ctx, reinterpret_cast<const crn_uint32*>(rgba + (size_t)i * 64), out + (size_t)i * bpb);
+  }
+  crn_free_block_compressor(ctx);
+  return (int)bpb;
+}
+
+// Same as ref_compress_blocks but splits the blocks over `threads` OS threads, one
+// block-compressor context per thread (the way the reference's block API is meant to
+// be used from several threads). Returns elapsed wall seconds through *seconds.
+int ref_compress_blocks_mt(const uint8_t* rgba, uint32_t n, uint32_t fmt, uint32_t flags,
+                           uint32_t dxt_quality, uint8_t* out, uint32_t threads, double* seconds) {
+  if (threads < 1) threads = 1;
+  crn_comp_params p = make_params(fmt, flags, dxt_quality);
+  const uint32_t bpb = crnd::crnd_get_bytes_per_dxt_block(p.m_format);
+  std::atomic<uint32_t> next(0);
+  auto t0 = std::chrono::steady_clock::now();
+  std::vector<std::thread> pool;
+  for (uint32_t t = 0; t < threads; t++) {
+    pool.emplace_back([&]() {
+      crn_block_compressor_context_t ctx = crn_create_block_compressor(p);
+      if (!ctx) return;
+      for (;;) {
+        uint32_t i0 = next.fetch_add(64);
+        if (i0 >= n) break;
+        uint32_t i1 = i0 + 64 < n ? i0 + 64 : n;
+        for (uint32_t i = i0; i < i1; i++)
+          crn_compress_block(ctx, reinterpret_cast<const crn_uint32*>(rgba + (size_t)i * 64), out + (size_t)i * bpb);
+      }
+      crn_free_block_compressor(ctx);
+    });
+  }
+  for (auto& th : pool) th.join();
+  auto t1 = std::chrono::steady_clock::now();
+  if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+  return (int)bpb;
+}
+
+// Compresses a texture given as faces x levels RGBA8 mip images (face-major; level l is
+// max(1,w>>l) x max(1,h>>l), tightly packed, concatenated) to a .crn (file_type 0) or .dds
+// (file_type 1) file in memory.
+// quality is m_quality_level (0..255). Returns the file size (0 on failure); the file is copied
+// to out when it fits in out_cap.
+uint32_t ref_compress_texture(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels, uint32_t faces,
+                              uint32_t fmt, uint32_t file_type, uint32_t quality, uint32_t flags,
+                              uint32_t dxt_quality, uint32_t helper_threads, uint8_t* out, uint32_t out_cap) {
+  crn_comp_params p;
+  p.m_file_type = file_type ? cCRNFileTypeDDS : cCRNFileTypeCRN;
+  p.m_width = width;
+  p.m_height = height;
+  p.m_levels = levels;
+  p.m_faces = faces;
+  p.m_format = static_cast<crn_format>(fmt);
+  p.m_flags = flags;
+  p.m_quality_level = quality;
+  p.m_dxt_quality = static_cast<crn_dxt_quality>(dxt_quality);
+  p.m_num_helper_threads = helper_threads;
+  size_t ofs = 0;
+  for (uint32_t f = 0; f < faces; f++) {
+    for (uint32_t l = 0; l < levels; l++) {
+      uint32_t w = width >> l ? width >> l : 1, h = height >> l ? height >> l : 1;
+      p.m_pImages[f][l] = reinterpret_cast<const crn_uint32*>(rgba_levels + ofs);
+      ofs += (size_t)w * h * 4;
+    }
+  }
+  crn_mipmap_params mp;
+  mp.m_mode = cCRNMipModeUseSourceMips;
+  crn_uint32 size = 0;
+  void* data = crn_compress(p, mp, size);
+  if (!data) return 0;
+  if (size <= out_cap && out) memcpy(out, data, size);
+  crn_free_block(data);
+  return size;
+}
+
+// Transcodes one level of a .crn file with the reference crnd unpacker into out
+// (faces x blocks_y x row_pitch bytes, row_pitch = minimal). Returns bytes written or 0.
+uint32_t ref_unpack_level(const uint8_t* crn, uint32_t crn_size, uint32_t level, uint8_t* out, uint32_t out_cap) {
+  crnd::crn_texture_info ti;
+  if (!crnd::crnd_get_texture_info(crn, crn_size, &ti)) return 0;
+  crnd::crn_level_info li;
+  if (!crnd::crnd_get_level_info(crn, crn_size, level, &li)) return 0;
+  const uint32_t pitch = li.m_blocks_x * li.m_bytes_per_block;
+  const uint32_t face_size = pitch * li.m_blocks_y;
+  if ((uint64_t)face_size * ti.m_faces > out_cap) return 0;
+  crnd::crnd_unpack_context ctx = crnd::crnd_unpack_begin(crn, crn_size);
+  if (!ctx) return 0;
+  void* faces[6];
+  for (uint32_t f = 0; f < ti.m_faces; f++) faces[f] = out + (size_t)f * face_size;
+  bool ok = crnd::crnd_unpack_level(ctx, faces, face_size, pitch, level);
+  crnd::crnd_unpack_end(ctx);
+  return ok ? face_size * ti.m_faces : 0;
+}
+
+// Times `reps` full transcodes (every level) of a .crn file on one thread; returns seconds.
+double ref_time_unpack(const uint8_t* crn, uint32_t crn_size, uint32_t reps, uint8_t* scratch, uint32_t scratch_cap) {
+  crnd::crn_texture_info ti;
+  if (!crnd::crnd_get_texture_info(crn, crn_size, &ti)) return -1.0;
+  auto t0 = std::chrono::steady_clock::now();
+  for (uint32_t r = 0; r < reps; r++) {
+    crnd::crnd_unpack_context ctx = crnd::crnd_unpack_begin(crn, crn_size);
+    if (!ctx) return -1.0;
+    for (uint32_t l = 0; l < ti.m_levels; l++) {
+      crnd::crn_level_info li;
+      crnd::crnd_get_level_info(crn, crn_size, l, &li);
+      const uint32_t pitch = li.m_blocks_x * li.m_bytes_per_block;
+      const uint32_t face_size = pitch * li.m_blocks_y;
+      if ((uint64_t)face_size * ti.m_faces > scratch_cap) return -1.0;
+      void* faces[6];
+      for (uint32_t f = 0; f < ti.m_faces; f++) faces[f] = scratch + (size_t)f * face_size;
+      crnd::crnd_unpack_level(ctx, faces, face_size, pitch, l);
+    }
+    crnd::crnd_unpack_end(ctx);
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  return std::chrono::duration<double>(t1 - t0).count();
+}
+
+}  // extern "C"

@@ -1,0 +1,150 @@
+"""Regenerates the golden fixtures in this folder from the REFERENCE crnlib.
+
+The reference is compiled from its own sources by `make -C oracle ref` (oracle/_ref/libcrnref.so,
+x86_64 build container only) and driven through its public API:
+  * crn_create_block_compressor / crn_compress_block   (inc/crnlib.h:674-682)
+  * crn_compress with source mips                       (inc/crnlib.h:614)
+  * crnd_unpack_begin / crnd_unpack_level               (inc/crn_defs.h:174-191)
+with cCRNCompFlagDisableEndpointCaching set for block encodes, so the outputs do not depend on
+thread count. Inputs come from crunch2_gb300.texgen (seeded, platform-independent) or are stored.
+
+Outputs (all small; committed):
+  blocks.npz        edge-case + texture block inputs and the reference DXT1/DXT5/DXN/DXT5A blocks
+  crn/*.crn         reference .crn files; crn/manifest.json holds per-level sha256 of the
+                    reference transcode and the generation parameters
+Run:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from crunch2_gb300 import texgen  # noqa: E402
+from oracle import ref  # noqa: E402
+
+FLAG_PERCEPTUAL = 1
+FLAG_HIERARCHICAL = 2
+FLAG_BOTH_BLOCK_TYPES = 8
+FLAG_NO_ENDPOINT_CACHING = 32
+DXT_UBER = 4
+FMT = {"DXT1": 0, "DXT5": 2, "DXN_XY": 7, "DXN_YX": 8, "DXT5A": 9}
+
+
+def edge_blocks(seed: int = 1) -> np.ndarray:
+    """Stress blocks: random 16-colour, 1..5-colour palettes, low-contrast gradients, extremes
+    (black/white/primaries, 565 boundary values), with random alpha."""
+    rng = np.random.default_rng(seed)
+    parts = [rng.integers(0, 256, (400, 64), dtype=np.uint8)]
+    for k in (1, 2, 3, 4, 5):
+        pal = rng.integers(0, 256, (160, k, 4), dtype=np.uint8)
+        idx = rng.integers(0, k, (160, 16))
+        parts.append(np.take_along_axis(pal, idx[:, :, None].repeat(4, 2), 1).reshape(160, 64))
+    base = rng.integers(0, 256, (200, 1, 4)).astype(int)
+    parts.append(np.clip(base + rng.integers(-8, 9, (200, 16, 4)), 0, 255).astype(np.uint8).reshape(200, 64))
+    ex = np.array([[0, 0, 0, 255], [255, 255, 255, 255], [255, 0, 0, 255], [0, 255, 0, 255], [0, 0, 255, 255],
+                   [8, 4, 8, 255], [247, 251, 247, 255], [4, 4, 4, 255]], np.uint8)
+    parts.append(ex[rng.integers(0, 8, (200, 16))].reshape(200, 64))
+    solid = rng.integers(0, 256, (100, 1, 4), dtype=np.uint8).repeat(16, 1).reshape(100, 64)
+    parts.append(solid)
+    b = np.concatenate(parts).reshape(-1, 16, 4)
+    b[:, :, 3] = rng.integers(0, 256, (b.shape[0], 16))
+    return np.ascontiguousarray(b.reshape(-1, 64))
+
+
+def sha(a) -> str:
+    return hashlib.sha256(bytes(a)).hexdigest()
+
+
+def make_blocks() -> None:
+    edge = edge_blocks()
+    c0 = texgen.image_blocks(texgen.colour_texture(256, 256, 0))           # config-0 texture
+    dxt5_tex = texgen.image_blocks(texgen.colour_texture(128, 128, 3, with_alpha_noise=True))
+    nrm_tex = texgen.image_blocks(texgen.normal_map(128, 128, 4))
+    out = {"edge_in": edge, "c0_in_sha": np.frombuffer(sha(c0).encode(), np.uint8),
+           "dxt5_tex_sha": np.frombuffer(sha(dxt5_tex).encode(), np.uint8),
+           "nrm_tex_sha": np.frombuffer(sha(nrm_tex).encode(), np.uint8)}
+    base = FLAG_HIERARCHICAL | FLAG_NO_ENDPOINT_CACHING
+    # DXT1, both metrics x both block-type settings, on the edge set; config-0 texture default mode
+    for perc in (1, 0):
+        for both in (1, 0):
+            flags = base | (FLAG_PERCEPTUAL if perc else 0) | (FLAG_BOTH_BLOCK_TYPES if both else 0)
+            out[f"edge_dxt1_p{perc}_b{both}"] = ref.compress_blocks(edge, FMT["DXT1"], flags, DXT_UBER)
+    out["c0_dxt1"] = ref.compress_blocks(c0, FMT["DXT1"], base | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES, DXT_UBER)
+    for name in ("DXT5", "DXN_XY", "DXN_YX", "DXT5A"):
+        for both in (1, 0):
+            flags = base | FLAG_PERCEPTUAL | (FLAG_BOTH_BLOCK_TYPES if both else 0)
+            out[f"edge_{name.lower()}_b{both}"] = ref.compress_blocks(edge, FMT[name], flags, DXT_UBER)
+    out["dxt5_tex_dxt5"] = ref.compress_blocks(dxt5_tex, FMT["DXT5"], base | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES,
+                                               DXT_UBER)
+    out["nrm_tex_dxn_xy"] = ref.compress_blocks(nrm_tex, FMT["DXN_XY"], base | FLAG_BOTH_BLOCK_TYPES, DXT_UBER)
+    # Whole-image cross-check: the block API must equal crn_compress's plain .dds output.
+    dds = np.frombuffer(ref.compress_texture([[texgen.colour_texture(256, 256, 0)]], FMT["DXT1"], 1, 255,
+                                             base | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES, DXT_UBER, 7), np.uint8)
+    assert np.array_equal(dds[128:128 + out["c0_dxt1"].size].reshape(-1, 8), out["c0_dxt1"]), "dds != block api"
+    np.savez_compressed(os.path.join(HERE, "blocks.npz"), **out)
+
+
+# (name, width, height, format, faces, content, seed)
+CRN_CASES = [
+    ("c1_dxt1_1024", 1024, 1024, "DXT1", 1, "colour", 100),   # config-1 texture, 11 levels
+    ("dxt1_256", 256, 256, "DXT1", 1, "colour", 10),
+    ("dxt1_100x60", 100, 60, "DXT1", 1, "colour", 11),        # odd block counts
+    ("dxt1_cube_64", 64, 64, "DXT1", 6, "colour", 12),        # 6 faces share decoder state
+    ("dxt5_256", 256, 256, "DXT5", 1, "colour_alpha", 13),
+    ("dxt5_cube_64x32", 64, 32, "DXT5", 6, "colour_alpha", 14),
+    ("dxn_xy_256", 256, 256, "DXN_XY", 1, "normal", 15),
+    ("dxt5a_256", 256, 256, "DXT5A", 1, "colour_alpha", 16),
+]
+
+
+def texture_levels(w, h, content, seed, faces):
+    out = []
+    for f in range(faces):
+        if content == "normal":
+            img = texgen.normal_map(w, h, seed + f)
+        else:
+            img = texgen.colour_texture(w, h, seed + f, with_alpha_noise=(content == "colour_alpha"))
+        out.append(texgen.mip_chain(img))
+    return out
+
+
+def level_bytes(w, h, level, bpb, faces):
+    w, h = max(1, w >> level), max(1, h >> level)
+    return ((w + 3) // 4) * ((h + 3) // 4) * bpb * faces
+
+
+def make_crn() -> None:
+    os.makedirs(os.path.join(HERE, "crn"), exist_ok=True)
+    manifest = {}
+    for name, w, h, fmt, faces, content, seed in CRN_CASES:
+        fl = texture_levels(w, h, content, seed, faces)
+        flags = (0 if content == "normal" else FLAG_PERCEPTUAL) | FLAG_HIERARCHICAL | FLAG_BOTH_BLOCK_TYPES
+        crn = ref.compress_texture(fl, FMT[fmt], 0, 128, flags, DXT_UBER, 7)
+        with open(os.path.join(HERE, "crn", name + ".crn"), "wb") as fh:
+            fh.write(crn)
+        bpb = 8 if fmt in ("DXT1", "DXT5A") else 16
+        levels = []
+        for lvl in range(len(fl[0])):
+            out = ref.unpack_level(crn, lvl, level_bytes(w, h, lvl, bpb, faces))
+            levels.append({"bytes": int(out.size), "sha256": sha(out)})
+        manifest[name] = {"width": w, "height": h, "format": fmt, "faces": faces, "content": content, "seed": seed,
+                          "quality": 128, "crn_sha256": sha(crn), "levels": levels,
+                          "input_sha256": sha(np.concatenate([im.reshape(-1) for f in fl for im in f]))}
+    with open(os.path.join(HERE, "crn", "manifest.json"), "w") as fh:
+        json.dump(manifest, fh, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    if not ref.available():
+        sys.exit("oracle/_ref/libcrnref.so missing: run `make -C oracle ref` where the reference tree exists")
+    make_blocks()
+    make_crn()
+    print("golden fixtures written to", HERE)
