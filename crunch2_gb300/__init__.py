@@ -1,0 +1,256 @@
+"""crunch2_gb300: GB300-native crnlib DXTn hot path (DXT1/DXT5A block encode, CRN -> DXTn transcode).
+
+The compute lives in libcrngpu.so (C ABI, include/crngpu.h; CUDA kernels for sm_103a). This module
+is a thin ctypes host mirror of the reference's interfaces for the path:
+
+  crnlib (inc/crnlib.h)                      this module
+  ---------------------------------------    ----------------------------------------------
+  dxt1_endpoint_optimizer::compute           dxt1_optimize(blocks, perceptual, use_alpha_blocks)
+  dxt5_endpoint_optimizer::compute           dxt5a_optimize(blocks, comp_index, use_both_block_types)
+  crn_compress_block (batched)               compress_blocks(blocks, fmt, flags)
+  crn_compress, quality 255 (.dds blocks)    compress_image(rgba, fmt, flags)
+  crnd_unpack_begin / _level / _end          unpack_begin / unpack_level / unpack_end
+  crn_decompress (emscripten wrapper)        crn_decompress(src, first_level, level_count)
+
+There is no CPU fallback: if the library is missing or a call fails, an exception is raised.
+Arrays may be numpy arrays (host) or torch CUDA tensors (device; the call is then asynchronous on
+the given stream).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import texgen  # noqa: F401  (seeded synthetic inputs)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libcrngpu.so")
+
+OK, E_PARAM, E_CORRUPT, E_DEVICE, E_UNSUPPORTED = 0, -1, -2, -3, -4
+MEM_HOST, MEM_DEVICE = 0, 1
+FMT_DXT1, FMT_DXT5, FMT_DXN_XY, FMT_DXN_YX, FMT_DXT5A = 0, 2, 7, 8, 9
+FLAG_PERCEPTUAL, FLAG_USE_BOTH_BLOCK_TYPES = 1, 8
+
+
+class CrnGpuError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        super().__init__(f"{where} failed ({code}): {last_error()}")
+        self.code = code
+
+
+class _Dxt1Params(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("perceptual", ctypes.c_int32),
+                ("use_alpha_blocks", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def lib():
+    """Loads libcrngpu.so (building it first if it is missing). Raises if that fails."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        from .build import build
+        build()
+    L = ctypes.CDLL(LIB_PATH)
+    vp, u32, i32, i64, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_int64, ctypes.c_uint64
+    L.crngpu_version.restype = ctypes.c_char_p
+    L.crngpu_last_error.restype = ctypes.c_char_p
+    L.crngpu_dxt1_optimize_batch.argtypes = [vp, u32, ctypes.POINTER(_Dxt1Params), vp, vp, i32, vp]
+    L.crngpu_dxt1_optimize_batch.restype = i32
+    L.crngpu_dxt5a_optimize_batch.argtypes = [vp, u32, u32, ctypes.c_int32, vp, i32, vp]
+    L.crngpu_dxt5a_optimize_batch.restype = i32
+    L.crngpu_compress_blocks.argtypes = [vp, u32, u32, u32, vp, i32, vp]
+    L.crngpu_compress_blocks.restype = i32
+    L.crngpu_compress_image.argtypes = [vp, u32, u32, u32, u32, u32, vp, u64, i32, vp]
+    L.crngpu_compress_image.restype = i64
+    L.crngpu_unpack_begin.argtypes = [vp, u32]
+    L.crngpu_unpack_begin.restype = vp
+    L.crngpu_get_info.argtypes = [vp] + [ctypes.POINTER(u32)] * 6
+    L.crngpu_get_info.restype = i32
+    L.crngpu_unpack_level.argtypes = [vp, ctypes.POINTER(vp), u32, u32, u32, i32, vp]
+    L.crngpu_unpack_level.restype = i32
+    L.crngpu_unpack_level_segmented.argtypes = [vp, vp, u32, ctypes.POINTER(vp), u32, u32, u32, i32, vp]
+    L.crngpu_unpack_level_segmented.restype = i32
+    L.crngpu_unpack_levels.argtypes = [vp, u32, u32, vp, u64, i32, vp]
+    L.crngpu_unpack_levels.restype = i64
+    L.crngpu_unpack_end.argtypes = [vp]
+    L.crngpu_unpack_end.restype = i32
+    L.crngpu_crn_decompress.argtypes = [vp, ctypes.c_uint, vp, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint]
+    L.crngpu_crn_decompress.restype = None
+    _lib = L
+    return L
+
+
+def version() -> str:
+    return lib().crngpu_version().decode()
+
+
+def last_error() -> str:
+    return (lib().crngpu_last_error() or b"").decode(errors="replace")
+
+
+def _check(rc: int, where: str) -> int:
+    if rc < 0:
+        raise CrnGpuError(rc, where)
+    return rc
+
+
+def _is_torch_cuda(x) -> bool:
+    return hasattr(x, "is_cuda") and getattr(x, "is_cuda")
+
+
+def _ptr_mem(x):
+    """(pointer, mem kind) of a numpy array or torch CUDA tensor."""
+    if _is_torch_cuda(x):
+        return x.data_ptr(), MEM_DEVICE
+    return x.ctypes.data, MEM_HOST
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    return getattr(stream, "cuda_stream", stream)
+
+
+def _out_like(inp, shape, dtype=np.uint8):
+    if _is_torch_cuda(inp):
+        import torch
+        return torch.empty(shape, dtype={np.uint8: torch.uint8, np.uint64: torch.int64}[dtype], device=inp.device)
+    return np.zeros(shape, dtype)
+
+
+# ------------------------------------------------------------------------------------------
+# Block encoders
+
+def dxt1_optimize(blocks, perceptual: bool = True, use_alpha_blocks: bool = True, with_error: bool = False,
+                  stream=None):
+    """(n, 64) RGBA8 blocks -> (n, 8) dxt1 blocks [, (n,) squared errors]."""
+    n = int(blocks.shape[0])
+    out = _out_like(blocks, (n, 8))
+    err = _out_like(blocks, (n,), np.uint64) if with_error else None
+    p = _Dxt1Params(ctypes.sizeof(_Dxt1Params), int(perceptual), int(use_alpha_blocks), 0)
+    ip, mem = _ptr_mem(blocks)
+    op, _ = _ptr_mem(out)
+    ep = _ptr_mem(err)[0] if err is not None else None
+    _check(lib().crngpu_dxt1_optimize_batch(ip, n, ctypes.byref(p), op, ep, mem, _stream_ptr(stream)),
+           "crngpu_dxt1_optimize_batch")
+    return (out, err) if with_error else out
+
+
+def dxt5a_optimize(blocks, comp_index: int = 3, use_both_block_types: bool = True, stream=None):
+    """(n, 64) RGBA8 blocks -> (n, 8) dxt5 alpha blocks of channel comp_index."""
+    n = int(blocks.shape[0])
+    out = _out_like(blocks, (n, 8))
+    ip, mem = _ptr_mem(blocks)
+    _check(lib().crngpu_dxt5a_optimize_batch(ip, n, comp_index, int(use_both_block_types), _ptr_mem(out)[0], mem,
+                                             _stream_ptr(stream)), "crngpu_dxt5a_optimize_batch")
+    return out
+
+
+def bytes_per_block(fmt: int) -> int:
+    return 8 if fmt in (FMT_DXT1, FMT_DXT5A) else 16
+
+
+def compress_blocks(blocks, fmt: int, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES, stream=None):
+    """Batched crn_compress_block: (n, 64) RGBA8 -> (n, 8|16) DXTn blocks."""
+    n = int(blocks.shape[0])
+    out = _out_like(blocks, (n, bytes_per_block(fmt)))
+    ip, mem = _ptr_mem(blocks)
+    _check(lib().crngpu_compress_blocks(ip, n, fmt, flags, _ptr_mem(out)[0], mem, _stream_ptr(stream)),
+           "crngpu_compress_blocks")
+    return out
+
+
+def compress_image(rgba, fmt: int = FMT_DXT1, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES,
+                   out=None, stream=None):
+    """Plain DXTn encode of an (h, w, 4) RGBA8 image -> (blocks_y * blocks_x, 8|16) blocks."""
+    h, w = int(rgba.shape[0]), int(rgba.shape[1])
+    n = ((w + 3) // 4) * ((h + 3) // 4)
+    if out is None:
+        out = _out_like(rgba, (n, bytes_per_block(fmt)))
+    ip, mem = _ptr_mem(rgba)
+    _check(lib().crngpu_compress_image(ip, w, h, 0, fmt, flags, _ptr_mem(out)[0], n * bytes_per_block(fmt), mem,
+                                       _stream_ptr(stream)), "crngpu_compress_image")
+    return out
+
+
+# ------------------------------------------------------------------------------------------
+# Transcoder
+
+class UnpackContext:
+    """crnd_unpack_begin .. crnd_unpack_end for one .crn file (context lives on the device)."""
+
+    def __init__(self, crn: bytes):
+        self._buf = np.frombuffer(crn, np.uint8)
+        self.handle = lib().crngpu_unpack_begin(self._buf.ctypes.data, len(crn))
+        if not self.handle:
+            raise CrnGpuError(E_CORRUPT, "crngpu_unpack_begin")
+        vals = [ctypes.c_uint32() for _ in range(6)]
+        _check(lib().crngpu_get_info(self.handle, *[ctypes.byref(v) for v in vals]), "crngpu_get_info")
+        self.width, self.height, self.levels, self.faces, self.format, self.bytes_per_block = [v.value for v in vals]
+
+    def level_dims(self, level: int):
+        w, h = max(1, self.width >> level), max(1, self.height >> level)
+        return (w + 3) // 4, (h + 3) // 4
+
+    def level_bytes(self, level: int) -> int:
+        bx, by = self.level_dims(level)
+        return bx * by * self.bytes_per_block * self.faces
+
+    def unpack_level(self, level: int, row_pitch: int = 0, out=None, stream=None):
+        """All faces of one level; returns a (faces, blocks_y * pitch) uint8 array/tensor."""
+        bx, by = self.level_dims(level)
+        pitch = row_pitch or bx * self.bytes_per_block
+        if out is None:
+            out = np.zeros((self.faces, by * pitch), np.uint8)
+        ptr, mem = _ptr_mem(out)
+        stride = by * pitch
+        faces = (ctypes.c_void_p * self.faces)(*[ptr + f * stride for f in range(self.faces)])
+        _check(lib().crngpu_unpack_level(self.handle, faces, stride, row_pitch, level, mem, _stream_ptr(stream)),
+               "crngpu_unpack_level")
+        return out
+
+    def unpack_levels(self, first: int = 0, count: int | None = None, out=None, stream=None):
+        """Levels first..first+count-1 back to back (minimal pitch); one launch pair."""
+        count = self.levels - first if count is None else count
+        total = sum(self.level_bytes(l) for l in range(first, first + count))
+        if out is None:
+            out = np.zeros(total, np.uint8)
+        ptr, mem = _ptr_mem(out)
+        _check(lib().crngpu_unpack_levels(self.handle, first, count, ptr, total, mem, _stream_ptr(stream)),
+               "crngpu_unpack_levels")
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().crngpu_unpack_end(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def unpack_begin(crn: bytes) -> UnpackContext:
+    return UnpackContext(crn)
+
+
+def crn_decompress(src: bytes, first_level: int, level_count: int, dst_size: int) -> np.ndarray:
+    """emscripten crn_decompress contract: levels back to back into one host buffer."""
+    s = np.frombuffer(src, np.uint8)
+    out = np.zeros(dst_size, np.uint8)
+    lib().crngpu_crn_decompress(s.ctypes.data, len(src), out.ctypes.data, dst_size, first_level, level_count)
+    return out

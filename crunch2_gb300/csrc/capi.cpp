@@ -1,0 +1,67 @@
+// Library-wide pieces of the C ABI: version, last-error text, device buffers.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "crngpu_internal.h"
+
+namespace crngpu {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+const char* last_error_cstr() { return g_last_error.c_str(); }
+
+int cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return CRNGPU_OK;
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return CRNGPU_E_DEVICE;
+}
+
+cudaError_t DevBuf::ensure(size_t bytes) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (ptr && cap >= bytes && dev == device) return cudaSuccess;
+  release();
+  size_t want = bytes < 256 ? 256 : bytes;
+  want = (want + want / 4 + 255) & ~(size_t)255;  // grow with headroom, 256-byte multiple
+  e = cudaMalloc(&ptr, want);
+  if (e != cudaSuccess) {
+    ptr = nullptr;
+    cap = 0;
+    return e;
+  }
+  cap = want;
+  device = dev;
+  return cudaSuccess;
+}
+
+void DevBuf::release() {
+  if (ptr) {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (device >= 0 && device != cur) cudaSetDevice(device);
+    cudaFree(ptr);
+    if (device >= 0 && device != cur && cur >= 0) cudaSetDevice(cur);
+  }
+  ptr = nullptr;
+  cap = 0;
+  device = -1;
+}
+
+// Staging buffers for host-memory calls; one set per host thread so concurrent callers on
+// different threads never share them.
+DevBuf& staging(int slot) {
+  thread_local DevBuf bufs[4];
+  return bufs[slot & 3];
+}
+
+}  // namespace crngpu
+
+extern "C" const char* crngpu_version(void) { return "crngpu 0.1 (sm_103a)"; }
+extern "C" const char* crngpu_last_error(void) { return crngpu::last_error_cstr(); }

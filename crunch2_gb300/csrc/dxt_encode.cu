@@ -1,0 +1,1280 @@
+// DXT1 / DXT5A block encoders for sm_103a, bit-exact with crnlib's uber-quality optimizers.
+//
+// DXT1 (dxt1_endpoint_optimizer, crnlib/crn_dxt1.cpp) runs in two phases inside one kernel:
+//   phase 1, lane per block: unique colours, perceptual weighting (powf), the double-precision
+//     PCA and projection bounds (handle_multicolor_block :1069-1178) and the LBG seeds of
+//     try_median4 (:1181-1308). These are scalar, FP64-heavy and tiny, so lanes work on
+//     different blocks and GB300's narrow FP64 pipe is amortised over the warp.
+//   phase 2, warp per block, lane per candidate: every candidate list of optimize_endpoints
+//     (:703-1067) in reference order. The reference accepts a candidate only if its error is
+//     strictly lower than the running best, after a plane-table prune evaluated against that
+//     running best. Here 32 candidates are evaluated at once and a ballot resolves the exact
+//     sequential outcome: the first lane that beats the current best is accepted, then the next
+//     lane after it that beats the new best, and so on. Lists whose candidates are built from
+//     the running best (lattice neighbours) are regenerated right after each acceptance.
+//     The tried-solution hash set of the reference is not needed: a repeated candidate can
+//     never be accepted (its error was already compared against an equal or larger best).
+// Distances are exact integers computed in FP32 with the expanded square
+//   w.(x-p)^2 = w.x^2 + (w.p^2 - 2 w.p.x), all terms integers below 2^24.
+// This file must be compiled with --fmad=false: the FP32/FP64 parts restate the reference's
+// expression order without fused multiply-adds (the only FMAs are the explicit fmaf of exact
+// integer terms).
+//
+// DXT5A (dxt5_endpoint_optimizer, crnlib/crn_dxt5a.cpp:40-262) is warp per block, lane per
+// candidate, with the same first-improvement resolution; its probe grid follows the moving
+// centre of the reference.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+
+#include "crngpu_internal.h"
+
+namespace crngpu {
+
+#define FULL_MASK 0xFFFFFFFFu
+
+constexpr int kBlocksPerWarp = 8;
+constexpr int kWarpsPerCta = 4;
+constexpr uint32_t kInf = 0xFFFFFFFFu;
+
+// ryg single-colour tables (crnlib/crn_ryg_dxt.cpp:58-99): [value][0]=max, [1]=min endpoint
+struct SingleColour { uint8_t m5[256][2], m6[256][2], m5_3[256][2], m6_3[256][2]; };
+__constant__ SingleColour c_sct;
+
+__constant__ int16_t c_uber_probe[15] = {0, 1, 2, 3, 5, 7, 9, 10, 13, 15, 19, 27, 43, 59, 91};
+
+// ------------------------------------------------------------------------------------------
+// small helpers
+
+__device__ __forceinline__ int exp5(int v) { return (v << 3) | (v >> 2); }
+__device__ __forceinline__ int exp6(int v) { return (v << 2) | (v >> 4); }
+__device__ __forceinline__ uint32_t pack565(int r, int g, int b) { return (uint32_t)(b | (g << 5) | (r << 11)); }
+__device__ __forceinline__ uint32_t canon_lo(uint32_t lo, uint32_t hi) { return lo < hi ? hi : lo; }
+__device__ __forceinline__ uint32_t canon_hi(uint32_t lo, uint32_t hi) { return lo < hi ? lo : hi; }
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
+// exact float (integer value in [0, 2^23)) -> uint via the 2^23 magic constant
+__device__ __forceinline__ uint32_t f2u_exact(float v) { return __float_as_uint(__fadd_rn(v, 8388608.0f)) - 0x4B000000u; }
+
+// Per-warp shared state for phase 2 (one block at a time).
+struct WarpShared {
+  float4 ucf[16];     // r, g, b as floats, X2 = weighted |x|^2
+  int ucw[16];        // weights
+  uint32_t uci[16];   // r | g << 8 | b << 16
+  uint2 lbr[32], lbg[64], lbb[32];  // plane lower bounds: .x = low, .y = high
+  uint16_t list[64];  // scratch candidate list (probes / solid / combinatorial)
+  uint16_t list2[32];
+  // phase-1 hand-off, one slot per block of the warp's chunk
+  float p1f[kBlocksPerWarp][9];     // axis[3], low[3], high[3]
+  uint32_t p1m[kBlocksPerWarp][6];  // try_median4 candidates (lo | hi << 16)
+  int p1n[kBlocksPerWarp];          // unique colour count
+  // phase-1 scratch, transposed [i][lane] so lanes never share a bank
+  uint32_t t_col[16][kBlocksPerWarp];
+  uint8_t t_w[16][kBlocksPerWarp];
+  float t_norm[3][16][kBlocksPerWarp];
+};
+
+struct Best {
+  uint32_t lo, hi, err;
+  int alpha, alt, enforce, enforced;
+};
+
+// ------------------------------------------------------------------------------------------
+// Phase 1 (one lane = one block).
+
+struct V3f { float x, y, z; };
+
+// intersection::ray_aabb against [0,1]^3 (crn_intersect.h:44-132); true on cSuccess
+__device__ bool ray_unit_box(float o[3], const float d[3], float out[3]) {
+  int quad[3];
+  float cand[3] = {0.f, 0.f, 0.f};
+  bool inside = true;
+  for (int i = 0; i < 3; i++) {
+    if (o[i] < 0.0f) { quad[i] = 1; cand[i] = 0.0f; inside = false; }
+    else if (o[i] > 1.0f) { quad[i] = 0; cand[i] = 1.0f; inside = false; }
+    else quad[i] = 2;
+  }
+  if (inside) return false;
+  float mt[3];
+  for (int i = 0; i < 3; i++) mt[i] = (quad[i] != 2 && d[i] != 0.0f) ? __fdiv_rn(__fsub_rn(cand[i], o[i]), d[i]) : -1.0f;
+  int wp = 0;
+  for (int i = 1; i < 3; i++) if (mt[wp] < mt[i]) wp = i;
+  if (mt[wp] < 0.0f) return false;
+  float c[3];
+  for (int i = 0; i < 3; i++) {
+    if (i != wp) {
+      c[i] = __fadd_rn(o[i], __fmul_rn(mt[wp], d[i]));
+      if (c[i] < 0.0f || c[i] > 1.0f) return false;
+    } else {
+      c[i] = cand[i];
+    }
+  }
+  out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
+  return true;
+}
+
+// fast_random (crnlib/crn_rand.cpp:310-405) with its default seed
+struct FastRandom {
+  uint32_t jsr = 0xABCD917Au, jcong = 0x17F3DEADu;
+  __device__ float frand(float l, float h) {
+    jsr ^= (jsr << 17); jsr ^= (jsr >> 13); jsr ^= (jsr << 5);
+    jcong = 69069u * jcong + 1234567u;
+    const uint32_t r32 = jsr ^ jcong;
+    const double t = __dmul_rn((double)r32, 1.0 / 4294967296.0);
+    float r = (float)__dadd_rn((double)l, __dmul_rn((double)__fsub_rn(h, l), t));
+    return r < l ? l : (r > h ? h : r);
+  }
+};
+
+// Runs handle_multicolor_block up to optimize_endpoints' entry, plus try_median4's seeds.
+__device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, bool perceptual) {
+  const int L = slot;
+  // unique colours in first-occurrence order (compute_internal :2113-2131)
+  int n = 0;
+  uint32_t pix[16];
+  {
+    const uint4* p4 = reinterpret_cast<const uint4*>(px);
+    for (int q = 0; q < 4; q++) {
+      const uint4 v = __ldg(p4 + q);
+      pix[4 * q] = v.x; pix[4 * q + 1] = v.y; pix[4 * q + 2] = v.z; pix[4 * q + 3] = v.w;
+    }
+  }
+  for (int p = 0; p < 16; p++) {
+    const uint32_t c = pix[p] & 0xFFFFFFu;
+    int i = 0;
+    for (; i < n; i++) if (S.t_col[i][L] == c) break;
+    if (i == n) { S.t_col[n][L] = c; S.t_w[n][L] = 1; n++; }
+    else S.t_w[i][L]++;
+  }
+  S.p1n[L] = n;
+  if (n <= 1) return;
+  const float total = 16.0f;
+  // perceptual weights (:1074-1108); powf restated as the correctly rounded float of pow()
+  int passes = 1;
+  float pw[3] = {1.0f, 1.0f, 1.0f};
+  if (perceptual) {
+    float red = 0.f, blue = 0.f, avel = 0.f;
+    for (int i = 0; i < n; i++) {
+      const uint32_t c = S.t_col[i][L];
+      const int r = c & 255, g = (c >> 8) & 255, b = c >> 16;
+      const int l = (r + g + b + 1) / 3;
+      const float lf = (float)l;
+      const float scale = __fdiv_rn((float)S.t_w[i][L], 1.0f > lf ? 1.0f : lf);
+      red = __fadd_rn(red, __fmul_rn(scale, (float)r));
+      blue = __fadd_rn(blue, __fmul_rn(scale, (float)b));
+      avel = __fadd_rn(avel, lf);
+    }
+    red = __fdiv_rn(red, total);
+    blue = __fdiv_rn(blue, total);
+    avel = __fdiv_rn(avel, total);
+    const float a16 = __fdiv_rn(__fmul_rn(avel, 16.0f), 255.0f);
+    avel = a16 < 1.0f ? a16 : 1.0f;
+    const float mx = red > blue ? red : blue;
+    float s = __fdiv_rn(__fmul_rn(mx, 1.0f), 3.0f);
+    s = s < 0.0f ? 0.0f : (s > 1.0f ? 1.0f : s);
+    const float pwr = (float)pow((double)s, 2.75);
+    const float p = __fmul_rn(avel, pwr);
+    if (!(p >= 1.0f)) {
+      passes = 2;
+      const float a0[3] = {.212f, .72f, .072f};
+      for (int k = 0; k < 3; k++) pw[k] = __fadd_rn(a0[k], __fmul_rn(__fsub_rn(pw[k], a0[k]), p));
+    }
+  }
+  float mean[3], axis[3];
+  for (int pass = 0; pass < passes; pass++) {
+    // compute_vectors :155-189
+    float meanw[3] = {0.f, 0.f, 0.f};
+    mean[0] = mean[1] = mean[2] = 0.f;
+    for (int i = 0; i < n; i++) {
+      const uint32_t c = S.t_col[i][L];
+      const float wf = (float)S.t_w[i][L];
+      const float v[3] = {__fdiv_rn((float)(c & 255), 255.0f), __fdiv_rn((float)((c >> 8) & 255), 255.0f),
+                          __fdiv_rn((float)(c >> 16), 255.0f)};
+      for (int k = 0; k < 3; k++) {
+        mean[k] = __fadd_rn(mean[k], __fmul_rn(v[k], wf));
+        meanw[k] = __fadd_rn(meanw[k], __fmul_rn(__fmul_rn(pw[k], v[k]), wf));
+      }
+    }
+    const float inv = __fdiv_rn(1.0f, total);
+    for (int k = 0; k < 3; k++) { mean[k] = __fmul_rn(mean[k], inv); meanw[k] = __fmul_rn(meanw[k], inv); }
+    // compute_pca :192-256 (double accumulation in colour order)
+    double cov[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < n; i++) {
+      const uint32_t c = S.t_col[i][L];
+      const int w = S.t_w[i][L];
+      const float v[3] = {__fdiv_rn((float)(c & 255), 255.0f), __fdiv_rn((float)((c >> 8) & 255), 255.0f),
+                          __fdiv_rn((float)(c >> 16), 255.0f)};
+      float nv[3];
+      for (int k = 0; k < 3; k++) {
+        nv[k] = __fsub_rn(v[k], mean[k]);
+        S.t_norm[k][i][L] = nv[k];
+      }
+      const float r = __fsub_rn(__fmul_rn(pw[0], v[0]), meanw[0]);
+      const float g = __fsub_rn(__fmul_rn(pw[1], v[1]), meanw[1]);
+      const float b = __fsub_rn(__fmul_rn(pw[2], v[2]), meanw[2]);
+      const float pr[6] = {__fmul_rn(r, r), __fmul_rn(r, g), __fmul_rn(r, b), __fmul_rn(g, g), __fmul_rn(g, b), __fmul_rn(b, b)};
+      if (w > 1) {
+        for (int k = 0; k < 6; k++) cov[k] = __dadd_rn(cov[k], __dmul_rn((double)pr[k], (double)w));
+      } else {
+        for (int k = 0; k < 6; k++) cov[k] = __dadd_rn(cov[k], (double)pr[k]);
+      }
+    }
+    double vf[3] = {(double).9f, (double)1.0f, (double).7f};
+    for (int it = 0; it < 8; it++) {
+      double r = __dadd_rn(__dadd_rn(__dmul_rn(vf[0], cov[0]), __dmul_rn(vf[1], cov[1])), __dmul_rn(vf[2], cov[2]));
+      double g = __dadd_rn(__dadd_rn(__dmul_rn(vf[0], cov[1]), __dmul_rn(vf[1], cov[3])), __dmul_rn(vf[2], cov[4]));
+      double b = __dadd_rn(__dadd_rn(__dmul_rn(vf[0], cov[2]), __dmul_rn(vf[1], cov[4])), __dmul_rn(vf[2], cov[5]));
+      double m = fabs(r);
+      if (fabs(g) > m) m = fabs(g);
+      if (fabs(b) > m) m = fabs(b);
+      if (m > 1e-10) {
+        m = __ddiv_rn(1.0, m);
+        r = __dmul_rn(r, m); g = __dmul_rn(g, m); b = __dmul_rn(b, m);
+      }
+      const double d0 = __dsub_rn(vf[0], r), d1 = __dsub_rn(vf[1], g), d2 = __dsub_rn(vf[2], b);
+      const double delta = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+      vf[0] = r; vf[1] = g; vf[2] = b;
+      if (it > 2 && delta < 1e-8) break;
+    }
+    const double len = __dadd_rn(__dadd_rn(__dmul_rn(vf[0], vf[0]), __dmul_rn(vf[1], vf[1])), __dmul_rn(vf[2], vf[2]));
+    if (len < 1e-10) {
+      axis[0] = .2837149f; axis[1] = 0.9540631f; axis[2] = 0.096277453f;
+    } else {
+      const double il = __ddiv_rn(1.0, __dsqrt_rn(len));
+      axis[0] = (float)__dmul_rn(vf[0], il); axis[1] = (float)__dmul_rn(vf[1], il); axis[2] = (float)__dmul_rn(vf[2], il);
+    }
+    for (int k = 0; k < 3; k++) axis[k] = __fdiv_rn(axis[k], pw[k]);
+    // vec::normalize (crn_vec.h:674-690): float squares accumulated in double
+    double nn = (double)__fmul_rn(axis[0], axis[0]);
+    nn = __dadd_rn(nn, (double)__fmul_rn(axis[1], axis[1]));
+    nn = __dadd_rn(nn, (double)__fmul_rn(axis[2], axis[2]));
+    if (nn != 0.0) {
+      const float sc = (float)__ddiv_rn(1.0, __dsqrt_rn(nn));
+      for (int k = 0; k < 3; k++) axis[k] = __fmul_rn(axis[k], sc);
+    }
+    if (passes > 1) {
+      if (fabsf(axis[0]) >= .795f) { pw[0] = .424f; pw[1] = .6f; pw[2] = .072f; }
+      else if (fabsf(axis[2]) >= .795f) { pw[0] = .212f; pw[1] = .6f; pw[2] = .212f; }
+      else break;
+    }
+  }
+  // projection bounds on the axis, then pull outside endpoints back into the unit cube
+  float lo_d = 1e+9f, hi_d = -1e+9f;
+  for (int i = 0; i < n; i++) {
+    float d = __fmul_rn(S.t_norm[0][i][L], axis[0]);
+    d = __fadd_rn(d, __fmul_rn(S.t_norm[1][i][L], axis[1]));
+    d = __fadd_rn(d, __fmul_rn(S.t_norm[2][i][L], axis[2]));
+    lo_d = d < lo_d ? d : lo_d;
+    hi_d = d > hi_d ? d : hi_d;
+  }
+  float low[3], high[3];
+  for (int k = 0; k < 3; k++) {
+    low[k] = __fadd_rn(mean[k], __fmul_rn(lo_d, axis[k]));
+    high[k] = __fadd_rn(mean[k], __fmul_rn(hi_d, axis[k]));
+  }
+  auto within = [](const float* v) {
+    for (int i = 0; i < 3; i++) if (v[i] < 0.0f || v[i] > 1.0f) return false;
+    return true;
+  };
+  if (!within(low)) {
+    float c[3];
+    if (ray_unit_box(low, axis, c)) { low[0] = c[0]; low[1] = c[1]; low[2] = c[2]; }
+  }
+  if (!within(high)) {
+    float c[3];
+    const float nd[3] = {-axis[0], -axis[1], -axis[2]};
+    if (ray_unit_box(high, nd, c)) { high[0] = c[0]; high[1] = c[1]; high[2] = c[2]; }
+  }
+  for (int k = 0; k < 3; k++) {
+    S.p1f[L][k] = axis[k];
+    S.p1f[L][3 + k] = low[k];
+    S.p1f[L][6 + k] = high[k];
+  }
+  // try_median4 seeds (:1181-1308)
+  float means[4][3];
+  if (n <= 4) {
+    for (int i = 0; i < 4; i++) {
+      const int src = i < n - 1 ? i : n - 1;
+      for (int k = 0; k < 3; k++) means[i][k] = S.t_norm[k][src][L];
+    }
+  } else {
+    for (int k = 0; k < 3; k++) {
+      means[0][k] = __fsub_rn(low[k], mean[k]);
+      means[3][k] = __fsub_rn(high[k], mean[k]);
+    }
+    for (int k = 0; k < 3; k++) {
+      means[1][k] = __fadd_rn(means[0][k], __fmul_rn(__fsub_rn(means[3][k], means[0][k]), 1.0f / 3.0f));
+      means[2][k] = __fadd_rn(means[0][k], __fmul_rn(__fsub_rn(means[3][k], means[0][k]), 2.0f / 3.0f));
+    }
+    FastRandom rm;
+    unsigned rover = 0;
+    float prev_total = 1.0e+37f;
+    for (int it = 0; it < 8; it++) {
+      float nm[4][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      float nw[4] = {0.f, 0.f, 0.f, 0.f};
+      float tot = 0.f;
+      for (int i = 0; i < n; i++) {
+        const float v[3] = {S.t_norm[0][i][L], S.t_norm[1][i][L], S.t_norm[2][i][L]};
+        float bd = 0.f;
+        int bi = 0;
+        for (int j = 0; j < 4; j++) {
+          float d2 = 0.f;
+          for (int k = 0; k < 3; k++) {
+            const float d = __fsub_rn(means[j][k], v[k]);
+            d2 = __fadd_rn(d2, __fmul_rn(d, d));
+          }
+          if (j == 0 || d2 < bd) { bd = d2; bi = j; }
+        }
+        tot = __fadd_rn(tot, bd);
+        const float wf = (float)S.t_w[i][L];
+        for (int k = 0; k < 3; k++) nm[bi][k] = __fadd_rn(nm[bi][k], __fmul_rn(v[k], wf));
+        nw[bi] = __fadd_rn(nw[bi], wf);
+      }
+      unsigned hi_idx = 0;
+      float hi_w = 0.f;
+      bool empty = false;
+      for (int j = 0; j < 4; j++) {
+        if (nw[j] > 0.0f) {
+          for (int k = 0; k < 3; k++) means[j][k] = __fdiv_rn(nm[j][k], nw[j]);
+          if (nw[j] > hi_w) { hi_w = nw[j]; hi_idx = j; }
+        } else {
+          empty = true;
+        }
+      }
+      if (!empty) {
+        if (fabsf(__fsub_rn(tot, prev_total)) < .00001f) break;
+        prev_total = tot;
+      } else {
+        prev_total = 1.0e+37f;
+      }
+      if (empty && it != 7) {
+        const unsigned ri = (hi_idx + rover) & 3;
+        rover++;
+        for (int j = 0; j < 4; j++) {
+          if (nw[j] == 0.0f) {
+            for (int k = 0; k < 3; k++) means[j][k] = means[ri][k];
+            for (int k = 0; k < 3; k++) means[j][k] = __fadd_rn(means[j][k], rm.frand(-.00196f, .00196f));
+          }
+        }
+      }
+    }
+  }
+  int slot_i = 0;
+  for (int i = 0; i < 3; i++) {
+    for (int j = i + 1; j < 4; j++) {
+      int q[2][3];
+      for (int k = 0; k < 3; k++) {
+        const float sc = k == 1 ? 63.0f : 31.0f;
+        q[0][k] = (int)floorf(__fadd_rn(.5f, __fmul_rn(__fadd_rn(means[i][k], mean[k]), sc)));
+        q[1][k] = (int)floorf(__fadd_rn(.5f, __fmul_rn(__fadd_rn(means[j][k], mean[k]), sc)));
+      }
+      uint32_t pk[2];
+      for (int e = 0; e < 2; e++) {
+        // color_quad_u8 clamps to 0..255, pack_color(scaled=false) then clamps to 31/63/31
+        const int r = min(clampi(q[e][0], 0, 255), 31), g = min(clampi(q[e][1], 0, 255), 63),
+                  b = min(clampi(q[e][2], 0, 255), 31);
+        pk[e] = pack565(r, g, b);
+      }
+      S.p1m[L][slot_i++] = canon_lo(pk[0], pk[1]) | (canon_hi(pk[0], pk[1]) << 16);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Phase 2 (one warp = one block).
+
+template <bool HC>
+struct Search {
+  WarpShared& S;
+  int n;
+  bool perceptual, use_alpha;
+  Best best;
+  Best snap;  // hc: the best at the last compute_selectors() call (selectors are lazy there)
+  float wr, wg, wb;
+  uint32_t lane;
+
+  __device__ Search(WarpShared& s, int n_, bool perc, bool alpha_blocks)
+      : S(s), n(n_), perceptual(perc), use_alpha(alpha_blocks) {
+    best.lo = best.hi = 0; best.err = kInf; best.alpha = 0; best.alt = 0; best.enforce = 0; best.enforced = 0;
+    snap = best;
+    wr = perc ? 8.f : 1.f; wg = perc ? 25.f : 1.f; wb = 1.f;
+    lane = lane_id();
+  }
+
+  // evaluate_solution's plane-table prune (crn_dxt1.cpp:1312-1322)
+  __device__ __forceinline__ uint32_t lower_bound(uint32_t lo, uint32_t hi) const {
+    const int r0 = lo >> 11, g0 = (lo >> 5) & 63, b0 = lo & 31;
+    const int r1 = hi >> 11, g1 = (hi >> 5) & 63, b1 = hi & 31;
+    const uint32_t re = r0 < r1 ? S.lbr[r0].x + S.lbr[r1].y : S.lbr[r0].y + S.lbr[r1].x;
+    const uint32_t ge = g0 < g1 ? S.lbg[g0].x + S.lbg[g1].y : S.lbg[g0].y + S.lbg[g1].x;
+    const uint32_t be = b0 < b1 ? S.lbb[b0].x + S.lbb[b1].y : S.lbb[b0].y + S.lbb[b1].x;
+    return re + ge + be;
+  }
+
+  // Palette entry k -> (q = 2 w p, P2 = w.p^2) for the expanded-square distance.
+  __device__ __forceinline__ void entry(int r, int g, int b, float4& q) const {
+    const float fr = (float)r, fg = (float)g, fb = (float)b;
+    q.x = 2.f * wr * fr; q.y = 2.f * wg * fg; q.z = 2.f * wb * fb;
+    q.w = wr * fr * fr + wg * fg * fg + wb * fb * fb;
+  }
+  __device__ __forceinline__ static float dist_part(const float4& x, const float4& q) {
+    float t = fmaf(-x.x, q.x, q.w);
+    t = fmaf(-x.y, q.y, t);
+    return fmaf(-x.z, q.z, t);
+  }
+
+  // Full error of one candidate. Uber path (evaluate_solution_uber :1370-1592): min over the
+  // 4-colour and (if allowed) 3-colour block, 4-colour preferred on ties. hc path
+  // (evaluate_solution_hc_* :1759-1835): 4-colour only.
+  __device__ __forceinline__ void eval(uint32_t lo, uint32_t hi, int alt, uint32_t& err, int& type) const {
+    const int r0 = exp5(lo >> 11), g0 = exp6((lo >> 5) & 63), b0 = exp5(lo & 31);
+    const int r1 = exp5(hi >> 11), g1 = exp6((hi >> 5) & 63), b1 = exp5(hi & 31);
+    float4 q0, q1, q2, q3, q4;
+    entry(r0, g0, b0, q0);
+    entry(r1, g1, b1, q1);
+    entry((r0 * 2 + r1 + alt) / 3, (g0 * 2 + g1 + alt) / 3, (b0 * 2 + b1 + alt) / 3, q2);
+    entry((r1 * 2 + r0 + alt) / 3, (g1 * 2 + g0 + alt) / 3, (b1 * 2 + b0 + alt) / 3, q3);
+    const bool three = !HC && use_alpha;
+    if (three) entry((r0 + r1 + alt) >> 1, (g0 + g1 + alt) >> 1, (b0 + b1 + alt) >> 1, q4);
+    uint32_t e0 = 0, e1 = 0;
+    for (int i = 0; i < n; i++) {
+      const float4 x = S.ucf[i];
+      const uint32_t w = (uint32_t)S.ucw[i];
+      const float d0 = dist_part(x, q0), d1 = dist_part(x, q1), d2 = dist_part(x, q2), d3 = dist_part(x, q3);
+      const float m01 = fminf(d0, d1);
+      const float m4 = fminf(m01, fminf(d2, d3));
+      e0 += w * f2u_exact(__fadd_rn(x.w, m4));
+      if (three) {
+        const float m3 = fminf(m01, dist_part(x, q4));
+        e1 += w * f2u_exact(__fadd_rn(x.w, m3));
+      }
+    }
+    if (three && e1 < e0) { err = e1; type = 1; }
+    else { err = e0; type = 0; }
+  }
+
+  // Selector of unique colour i for solution `s` (ties -> lowest index, as both the uber
+  // loop and compute_selectors_hc resolve them).
+  __device__ __forceinline__ int selector_of(int i, const Best& s) const {
+    if (s.enforce) return s.enforced;
+    const int r0 = exp5(s.lo >> 11), g0 = exp6((s.lo >> 5) & 63), b0 = exp5(s.lo & 31);
+    const int r1 = exp5(s.hi >> 11), g1 = exp6((s.hi >> 5) & 63), b1 = exp5(s.hi & 31);
+    float4 q[4];
+    entry(r0, g0, b0, q[0]);
+    entry(r1, g1, b1, q[1]);
+    const int a = s.alt;
+    if (s.alpha) {
+      entry((r0 + r1 + a) >> 1, (g0 + g1 + a) >> 1, (b0 + b1 + a) >> 1, q[2]);
+    } else {
+      entry((r0 * 2 + r1 + a) / 3, (g0 * 2 + g1 + a) / 3, (b0 * 2 + b1 + a) / 3, q[2]);
+      entry((r1 * 2 + r0 + a) / 3, (g1 * 2 + g0 + a) / 3, (b1 * 2 + b0 + a) / 3, q[3]);
+    }
+    const float4 x = S.ucf[i];
+    float bd = dist_part(x, q[0]);
+    int bi = 0;
+    const int nk = s.alpha ? 3 : 4;
+    for (int k = 1; k < nk; k++) {
+      const float d = dist_part(x, q[k]);
+      if (d < bd) { bd = d; bi = k; }
+    }
+    return bi;
+  }
+
+  // The selectors the reference's m_best_solution.m_selectors holds right now.
+  __device__ __forceinline__ const Best& sel_source() const { return HC ? snap : best; }
+  __device__ __forceinline__ void compute_selectors() { if (HC) snap = best; }
+
+  __device__ __forceinline__ void accept(uint32_t lo, uint32_t hi, uint32_t err, int type, int alt) {
+    best.lo = lo; best.hi = hi; best.err = err; best.alpha = type; best.alt = alt;
+    best.enforce = (!type && lo == hi) ? 1 : 0;
+    if (best.enforce) {
+      if ((best.lo & 31) != 31) { best.lo++; best.enforced = 1; }
+      else { best.hi--; best.enforced = 0; }
+    }
+  }
+
+  // Processes `count` candidates in order; gen(i, lo, hi) -> valid. Returns true if any was
+  // accepted. dependent: candidates depend on `best`, so regenerate after an acceptance.
+  template <typename Gen>
+  __device__ bool run_list(int count, bool dependent, int alt, Gen gen) {
+    bool any = false;
+    int i0 = 0;
+    while (i0 < count) {
+      const int i = i0 + (int)lane;
+      uint32_t lo = 0, hi = 0;
+      bool valid = false;
+      if (i < count) valid = gen(i, lo, hi);
+      const uint32_t lb = valid ? lower_bound(lo, hi) : kInf;
+      const bool live = valid && lb < best.err;
+      uint32_t err = kInf;
+      int type = 0;
+      if (live) eval(lo, hi, alt, err, type);
+      unsigned ok = __ballot_sync(FULL_MASK, live && err < best.err);
+      int last = -1;
+      while (ok) {
+        const int j = __ffs(ok) - 1;
+        const uint32_t jlo = __shfl_sync(FULL_MASK, lo, j), jhi = __shfl_sync(FULL_MASK, hi, j);
+        const uint32_t jerr = __shfl_sync(FULL_MASK, err, j);
+        const int jtype = __shfl_sync(FULL_MASK, type, j);
+        accept(jlo, jhi, jerr, jtype, alt);
+        any = true;
+        last = j;
+        if (dependent) break;
+        const unsigned after = j == 31 ? 0u : (FULL_MASK << (j + 1));
+        ok = __ballot_sync(FULL_MASK, valid && lb < best.err && err < best.err) & after;
+      }
+      if (dependent && last >= 0) i0 += last + 1;
+      else i0 += 32;
+    }
+    return any;
+  }
+
+  // refine_solution(1) :525-698 (least squares from the current selectors, then 2 x 27
+  // lattice neighbours of the two fitted endpoints)
+  __device__ bool refine() {
+    compute_selectors();
+    const Best& s = sel_source();
+    int a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // ak0 ak1 ak2 at1r at1g at1b at2r at2g at2b
+    if ((int)lane < n) {
+      const int step = selector_of(lane, s) ^ 1;
+      const int w = S.ucw[lane];
+      const uint32_t c = S.uci[lane];
+      const int r = (c & 255) * w, g = ((c >> 8) & 255) * w, b = (c >> 16) * w;
+      const int w1 = step == 0 ? 3 : step == 1 ? 0 : step == 2 ? 2 : 1;
+      const int p0 = step >= 2 ? 2 : 0;
+      const int p1 = step == 0 ? 0 : step == 1 ? 9 : step == 2 ? 1 : 4;
+      const int p2 = step == 0 ? 9 : step == 1 ? 0 : step == 2 ? 4 : 1;
+      a[0] = p0 * w; a[1] = p1 * w; a[2] = p2 * w;
+      a[3] = w1 * r; a[4] = w1 * g; a[5] = w1 * b;
+      a[6] = r; a[7] = g; a[8] = b;
+    }
+    for (int k = 0; k < 9; k++) a[k] = __reduce_add_sync(FULL_MASK, a[k]);
+    const long long xx = a[2], yy = a[1], xy = a[0];
+    const long long at1[3] = {a[3], a[4], a[5]};
+    const long long at2[3] = {3LL * a[6] - a[3], 3LL * a[7] - a[4], 3LL * a[8] - a[5]};
+    const long long t = xx * yy - xy * xy;
+    if (!yy || !xx || t == 0) return false;
+    // the six fitted components, one per lane, in double exactly as the reference
+    int comp = 0;
+    if (lane < 6) {
+      const int k = lane % 3;
+      const double frb = __ddiv_rn((double)__fdiv_rn(93.0f, 255.0f), (double)t);
+      const double f = k == 1 ? __dmul_rn(frb, (double)__fdiv_rn(63.0f, 31.0f)) : frb;
+      const long long num = lane < 3 ? at1[k] * yy - at2[k] * xy : at2[k] * xx - at1[k] * xy;
+      const double v = __dadd_rn(__dmul_rn((double)num, f), (double)0.5f);
+      comp = clampi(__double2int_rz(v), 0, k == 1 ? 63 : 31);
+    }
+    int e[2][3];
+    for (int k = 0; k < 6; k++) e[k / 3][k % 3] = __shfl_sync(FULL_MASK, comp, k);
+    return run_list(54, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
+      const int which = i / 27, rr = (i / 9) % 3 - 1, gr = (i / 3) % 3 - 1, br = i % 3 - 1;
+      int c[2][3] = {{e[0][0], e[0][1], e[0][2]}, {e[1][0], e[1][1], e[1][2]}};
+      c[which][0] = clampi(c[which][0] + rr, 0, 31);
+      c[which][1] = clampi(c[which][1] + gr, 0, 63);
+      c[which][2] = clampi(c[which][2] + br, 0, 31);
+      const uint32_t p0 = pack565(c[0][0], c[0][1], c[0][2]), p1 = pack565(c[1][0], c[1][1], c[1][2]);
+      lo = canon_lo(p0, p1);
+      hi = canon_hi(p0, p1);
+      return true;
+    });
+  }
+
+  __device__ bool all_selectors_equal() const {
+    const Best& s = sel_source();
+    const int mine = (int)lane < n ? selector_of(lane, s) : -1;
+    const int first = __shfl_sync(FULL_MASK, mine, 0);
+    return __all_sync(FULL_MASK, (int)lane >= n || mine == first);
+  }
+
+  // try_average_block_as_solid :93-153
+  __device__ bool try_solid() {
+    int tr = 0, tg = 0, tb = 0;
+    if ((int)lane < n) {
+      const uint32_t c = S.uci[lane];
+      const int w = S.ucw[lane];
+      tr = (c & 255) * w; tg = ((c >> 8) & 255) * w; tb = (c >> 16) * w;
+    }
+    tr = __reduce_add_sync(FULL_MASK, tr);
+    tg = __reduce_add_sync(FULL_MASK, tg);
+    tb = __reduce_add_sync(FULL_MASK, tb);
+    const int ar = (tr + 8) / 16, ag = (tg + 8) / 16, ab = (tb + 8) / 16;
+    // candidate list: (colour source, table) pairs; source 16 = the average
+    int cnt = 0;
+    if (lane == 0) {
+      S.list[cnt++] = (uint16_t)(16 << 1);
+      if (use_alpha) S.list[cnt++] = (uint16_t)((16 << 1) | 1);
+      for (int i = 0; i < n; i++) {
+        const uint32_t c = S.uci[i];
+        if ((int)(c & 255) == ar && (int)((c >> 8) & 255) == ag && (int)(c >> 16) == ab) continue;
+        S.list[cnt++] = (uint16_t)(i << 1);
+        if (use_alpha) S.list[cnt++] = (uint16_t)((i << 1) | 1);
+      }
+    }
+    cnt = __shfl_sync(FULL_MASK, cnt, 0);
+    __syncwarp();
+    return run_list(cnt, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
+      const int e = S.list[i];
+      const int src = e >> 1;
+      int r = ar, g = ag, b = ab;
+      if (src < 16) { const uint32_t c = S.uci[src]; r = c & 255; g = (c >> 8) & 255; b = c >> 16; }
+      if (e & 1) {
+        lo = pack565(c_sct.m5_3[r][0], c_sct.m6_3[g][0], c_sct.m5_3[b][0]);
+        hi = pack565(c_sct.m5_3[r][1], c_sct.m6_3[g][1], c_sct.m5_3[b][1]);
+      } else {
+        lo = pack565(c_sct.m5[r][0], c_sct.m6[g][0], c_sct.m5[b][0]);
+        hi = pack565(c_sct.m5[r][1], c_sct.m6[g][1], c_sct.m5[b][1]);
+      }
+      return true;
+    });
+  }
+
+  // compute_endpoint_component_errors :369-413, kept as closed-form quadratics
+  struct CompErr {
+    uint32_t W[4], WP2[4], WPP[4], rem[4];
+    __device__ __forceinline__ uint32_t E(int s, uint32_t p) const { return W[s] * p * p - WP2[s] * p + WPP[s]; }
+  };
+  __device__ void comp_errors(int comp, CompErr& ce) {
+    const Best& s = sel_source();
+    int sel = -1;
+    uint32_t p = 0, w = 0;
+    if ((int)lane < n) {
+      sel = selector_of(lane, s);
+      p = (S.uci[lane] >> (8 * comp)) & 255;
+      w = (uint32_t)S.ucw[lane];
+    }
+    for (int k = 0; k < 4; k++) {
+      ce.W[k] = __reduce_add_sync(FULL_MASK, sel == k ? w : 0u);
+      ce.WP2[k] = __reduce_add_sync(FULL_MASK, sel == k ? w * p * 2 : 0u);
+      ce.WPP[k] = __reduce_add_sync(FULL_MASK, sel == k ? w * p * p : 0u);
+    }
+    const int limit = comp == 1 ? 64 : 32;
+    for (int k = 0; k < 2; k++) {
+      uint32_t m = kInf;
+      for (int c = lane; c < limit; c += 32) {
+        const uint32_t pv = comp == 1 ? exp6(c) : exp5(c);
+        m = min(m, ce.E(k, pv));
+      }
+      ce.rem[k] = __reduce_min_sync(FULL_MASK, m);
+    }
+    for (int k = 2; k < 4; k++) {
+      uint32_t m = kInf;
+      for (int v = lane; v < 256; v += 32) m = min(m, ce.E(k, (uint32_t)v));
+      ce.rem[k] = __reduce_min_sync(FULL_MASK, m);
+    }
+    for (int k = 3; k > 0; k--) ce.rem[k - 1] += ce.rem[k];
+  }
+
+  // optimize_endpoint_comps :415-486
+  __device__ void optimize_comps() {
+    compute_selectors();
+    if (best.alpha || !best.err) return;
+    const int src_lo[3] = {exp5(best.lo >> 11), exp6((best.lo >> 5) & 63), exp5(best.lo & 31)};
+    const int src_hi[3] = {exp5(best.hi >> 11), exp6((best.hi >> 5) & 63), exp5(best.hi & 31)};
+    CompErr ce;
+    for (int comp = 0; comp < 3; comp++) {
+      const int p0s = src_lo[comp], p1s = src_hi[comp];
+      int lo_u[3] = {(int)(best.lo >> 11), (int)((best.lo >> 5) & 63), (int)(best.lo & 31)};
+      int hi_u[3] = {(int)(best.hi >> 11), (int)((best.hi >> 5) & 63), (int)(best.hi & 31)};
+      comp_errors(comp, ce);
+      const int limit = comp == 1 ? 64 : 32;
+      auto ex = [&](int c) { return (uint32_t)(comp == 1 ? exp6(c) : exp5(c)); };
+      uint32_t best_err = ce.E(0, ex(lo_u[comp])) + ce.E(1, ex(hi_u[comp])) + ce.E(2, (uint32_t)((p0s * 2 + p1s) / 3)) +
+                          ce.E(3, (uint32_t)((p0s + p1s * 2) / 3));
+      if (ce.rem[0] >= best_err) continue;
+      for (int c0 = 0; c0 < limit; c0++) {
+        uint32_t e0 = ce.E(0, ex(c0));
+        if (e0 + ce.rem[1] >= best_err) continue;
+        lo_u[comp] = c0;
+        const uint32_t packed_lo = pack565(lo_u[0], lo_u[1], lo_u[2]);
+        const int p0 = (int)ex(c0);
+        int start = 0;
+        while (start < limit) {
+          const int c1 = start + (int)lane;
+          bool pass = c1 < limit;
+          uint32_t lo = 0, hi = 0;
+          if (pass) {
+            uint32_t e = e0 + ce.E(1, ex(c1));
+            pass = e + ce.rem[2] < best_err;
+            const int p1 = (int)ex(c1);
+            e += ce.E(2, (uint32_t)((p0 * 2 + p1) / 3));
+            pass = pass && e + ce.rem[3] < best_err;
+            e += ce.E(3, (uint32_t)((p0 + p1 * 2) / 3));
+            pass = pass && e < best_err;
+            int h[3] = {hi_u[0], hi_u[1], hi_u[2]};
+            h[comp] = c1;
+            lo = packed_lo;
+            hi = pack565(h[0], h[1], h[2]);
+          }
+          const uint32_t lb = pass ? lower_bound(lo, hi) : kInf;
+          const bool live = pass && lb < best.err;
+          uint32_t err = kInf;
+          int type = 0;
+          if (live) eval(lo, hi, 0, err, type);
+          const unsigned ok = __ballot_sync(FULL_MASK, live && err < best.err);
+          if (!ok) { start += 32; continue; }
+          const int j = __ffs(ok) - 1;
+          accept(__shfl_sync(FULL_MASK, lo, j), __shfl_sync(FULL_MASK, hi, j), __shfl_sync(FULL_MASK, err, j),
+                 __shfl_sync(FULL_MASK, type, j), 0);
+          if (!best.err) return;
+          compute_selectors();
+          comp_errors(comp, ce);
+          const int c1j = start + j;
+          const int p1 = (int)ex(c1j);
+          best_err = ce.E(0, ex(c0)) + ce.E(1, ex(c1j)) + ce.E(2, (uint32_t)((p0 * 2 + p1) / 3)) +
+                     ce.E(3, (uint32_t)((p0 + p1 * 2) / 3));
+          e0 = ce.E(0, ex(c0));
+          if (e0 + ce.rem[1] >= best_err) break;
+          start = c1j + 1;
+        }
+      }
+    }
+  }
+
+  // try_combinatorial_encoding :1886-1997 (2..4 unique colours: endpoints of a block that was
+  // already DXT-compressed may be recovered by extrapolation)
+  __device__ void try_combinatorial() {
+    if (n < 2 || n > 4) return;
+    int m = 0;
+    if (lane == 0) {
+      int tr[48], tg[48], tb[48];
+      int cnt = 0;
+      for (int i = 0; i < n; i++) {
+        const uint32_t c = S.uci[i];
+        tr[cnt] = c & 255; tg[cnt] = (c >> 8) & 255; tb[cnt] = c >> 16; cnt++;
+      }
+      auto push = [&](int a, int b, float f, int rounding) {
+        const float r = rounding ? 1.0f : 0.0f;
+        auto one = [&](int x, int y) {
+          const float fx = (float)x, fy = (float)y;
+          const float l = __fadd_rn(fx, __fmul_rn(__fsub_rn(fy, fx), f));
+          return clampi(__float2int_rz(__fadd_rn(r, l)), 0, 255);
+        };
+        const int nr = one(tr[a], tr[b]), ng = one(tg[a], tg[b]), nb = one(tb[a], tb[b]);
+        tr[cnt] = nr; tg[cnt] = ng; tb[cnt] = nb; cnt++;
+      };
+      if (n == 2) {
+        const float fs[10] = {2.0f, 3.0f, .5f, 1.5f, -1.0f, 2.0f, -.5f, .5f, -2.0f, -1.0f};
+        for (int k = 0; k < 2; k++)
+          for (int qq = 0; qq < 2; qq++)
+            for (int f = 0; f < 10; f++) push(qq, qq ^ 1, fs[f], k);
+      } else if (n == 3) {
+        for (int i = 0; i <= 2; i++)
+          for (int j = 0; j <= 2; j++) {
+            if (i == j) continue;
+            push(i, j, 1.5f, 1);
+            push(i, j, 2.0f / 3.0f, 1);
+            push(i, j, 1.0f / 3.0f, 1);
+            push(i, j, -.5f, 1);
+          }
+      }
+      for (int i = 0; i < cnt; i++) {
+        const uint32_t ur = min(((uint32_t)tr[i] * 31u + 127u) / 255u, 31u);
+        const uint32_t ug = min(((uint32_t)tg[i] * 63u + 127u) / 255u, 63u);
+        const uint32_t ub = min(((uint32_t)tb[i] * 31u + 127u) / 255u, 31u);
+        const uint16_t pk = (uint16_t)(ub | (ug << 5) | (ur << 11));
+        bool dup = false;
+        for (int k = 0; k < m; k++) if (S.list[k] == pk) { dup = true; break; }
+        if (!dup) S.list[m++] = pk;
+      }
+    }
+    m = __shfl_sync(FULL_MASK, m, 0);
+    __syncwarp();
+    for (int i = 0; best.err && i + 1 < m; i++)
+      run_list(m - 1 - i, false, 0, [&](int k, uint32_t& lo, uint32_t& hi) {
+        lo = S.list[i]; hi = S.list[i + 1 + k]; return true;
+      });
+    const uint32_t saved = best.err;
+    if (saved) best.err = 1;
+    for (int i = 0; best.err && i + 1 < m; i++)
+      run_list(m - 1 - i, false, 1, [&](int k, uint32_t& lo, uint32_t& hi) {
+        lo = S.list[i]; hi = S.list[i + 1 + k]; return true;
+      });
+    if (best.err) best.err = saved;
+  }
+
+  // optimize_endpoints :703-1067 from the phase-1 projection bounds
+  __device__ void optimize(const float* axis, const float* low0, const float* high0, const uint32_t* med) {
+    // try_median4: the six LBG pairs, then refine(1)
+    run_list(6, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) { lo = med[i] & 0xFFFF; hi = med[i] >> 16; return true; });
+    refine();
+    float sa1[3];
+    for (int k = 0; k < 3; k++) sa1[k] = __fmul_rn(axis[k], .015625f);
+    sa1[0] = __fmul_rn(sa1[0], 31.0f); sa1[1] = __fmul_rn(sa1[1], 63.0f); sa1[2] = __fmul_rn(sa1[2], 31.0f);
+    float low[3], high[3];
+    const float lim[3] = {31.0f, 63.0f, 31.0f};
+    for (int k = 0; k < 3; k++) {
+      const float l = __fmul_rn(low0[k], lim[k]), h = __fmul_rn(high0[k], lim[k]);
+      low[k] = l < 0.0f ? 0.0f : (l > lim[k] ? lim[k] : l);
+      high[k] = h < 0.0f ? 0.0f : (h > lim[k] ? lim[k] : h);
+    }
+    for (int pass = 0; pass < 4; pass++) {
+      if (pass) {
+        low[0] = (float)(best.lo >> 11); low[1] = (float)((best.lo >> 5) & 63); low[2] = (float)(best.lo & 31);
+        high[0] = (float)(best.hi >> 11); high[1] = (float)((best.hi >> 5) & 63); high[2] = (float)(best.hi & 31);
+      }
+      const uint32_t prev = best.err;
+      if (!prev) break;
+      // sweep both endpoints along the axis (the 15-entry uber probe table, both directions)
+      int nl, nh;
+      {
+        const int k = (int)lane;
+        const int i = (k + 1) >> 1, s = (k + 1) & 1;
+        const float x = (float)c_uber_probe[i < 15 ? i : 14];
+        auto probe = [&](const float* base) {
+          int v[3];
+          for (int c = 0; c < 3; c++) {
+            const float step = s ? sa1[c] : -sa1[c];
+            const float pv = __fadd_rn(__fadd_rn(base[c], .5f), __fmul_rn(step, x));
+            v[c] = clampi((int)floorf(pv), 0, c == 1 ? 63 : 31);
+          }
+          return pack565(v[0], v[1], v[2]);
+        };
+        const uint32_t pl = probe(low), ph = probe(high);
+        const uint32_t pl2 = __shfl_up_sync(FULL_MASK, pl, 2), ph2 = __shfl_up_sync(FULL_MASK, ph, 2);
+        const bool in = k < 29;
+        const bool rl = in && (k < 2 || pl != pl2), rh = in && (k < 2 || ph != ph2);
+        const unsigned ml = __ballot_sync(FULL_MASK, rl), mh = __ballot_sync(FULL_MASK, rh);
+        const unsigned below = (1u << lane) - 1u;
+        if (rl) S.list[__popc(ml & below)] = (uint16_t)pl;
+        if (rh) S.list2[__popc(mh & below)] = (uint16_t)ph;
+        nl = __popc(ml);
+        nh = __popc(mh);
+        __syncwarp();
+      }
+      run_list(nl * nh, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
+        const int a = i / nh, b = i - a * nh;
+        const uint32_t p0 = S.list[a], p1 = S.list2[b];
+        lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
+        return true;
+      });
+      __syncwarp();
+      // lattice neighbours of the low endpoint: 26 adjacent cells, then +-2 on each axis
+      for (int side = 0; side < 2; side++) {
+        const uint32_t base = side ? best.hi : best.lo;
+        const int bc[3] = {(int)(base >> 11), (int)((base >> 5) & 63), (int)(base & 31)};
+        run_list(26, true, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
+          // g_adjacency order: x fastest, then y, then z, skipping the centre
+          const int idx = i < 13 ? i : i + 1;
+          const int dx = idx % 3 - 1, dy = (idx / 3) % 3 - 1, dz = idx / 9 - 1;
+          const int r = bc[0] + dx, g = bc[1] + dy, b = bc[2] + dz;
+          if (r < 0 || r > 31 || g < 0 || g > 63 || b < 0 || b > 31) return false;
+          const uint32_t moved = pack565(r, g, b);
+          const uint32_t p0 = side ? best.lo : moved, p1 = side ? moved : best.hi;
+          lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
+          return true;
+        });
+        const uint32_t base2 = side ? best.hi : best.lo;
+        const int bc2[3] = {(int)(base2 >> 11), (int)((base2 >> 5) & 63), (int)(base2 & 31)};
+        run_list(6, true, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
+          const int a = i >> 1, s = (i & 1) ? 2 : -2;
+          int c[3] = {bc2[0], bc2[1], bc2[2]};
+          const int q = c[a] + s;
+          if (q < 0 || q > (a == 1 ? 63 : 31)) return false;
+          c[a] = q;
+          const uint32_t moved = pack565(c[0], c[1], c[2]);
+          const uint32_t p0 = side ? best.lo : moved, p1 = side ? moved : best.hi;
+          lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
+          return true;
+        });
+      }
+      if (!best.err || (pass && best.err == prev)) break;
+      refine();
+    }
+    if (best.err) {
+      bool solid = false;
+      if (all_selectors_equal()) solid = try_solid();
+      if (!solid) optimize_comps();
+    }
+    if (best.err) try_combinatorial();
+  }
+};
+
+// Plane tables -> per-channel lower bounds (compute_internal :2133-2203), lane c handles
+// planes c (and c+32 for green).
+__device__ void build_lower_bounds(WarpShared& S, int n, bool perceptual) {
+  const int c = (int)lane_id();
+  uint32_t rw = 0, r1 = 0, r2 = 0, gw = 0, g1 = 0, g2 = 0, gw2 = 0, g12 = 0, g22 = 0, bw = 0, b1 = 0, b2 = 0;
+  uint32_t tw = 0, tr1 = 0, tr2 = 0, tg1 = 0, tg2 = 0, tb1 = 0, tb2 = 0;
+  for (int i = 0; i < n; i++) {
+    const uint32_t col = S.uci[i];
+    const uint32_t w = (uint32_t)S.ucw[i];
+    const int R = col & 255, G = (col >> 8) & 255, B = col >> 16;
+    const int pr = (R >> 3) + ((R & 7) > (R >> 5) ? 1 : 0);
+    const int pg = (G >> 2) + ((G & 3) > (G >> 6) ? 1 : 0);
+    const int pb = (B >> 3) + ((B & 7) > (B >> 5) ? 1 : 0);
+    tw += w;
+    tr1 += w * R; tr2 += w * R * R; tg1 += w * G; tg2 += w * G * G; tb1 += w * B; tb2 += w * B * B;
+    if (pr <= c) { rw += w; r1 += w * R; r2 += w * R * R; }
+    if (pg <= c) { gw += w; g1 += w * G; g2 += w * G * G; }
+    if (pg <= c + 32) { gw2 += w; g12 += w * G; g22 += w * G * G; }
+    if (pb <= c) { bw += w; b1 += w * B; b2 += w * B * B; }
+  }
+  const uint32_t kr = perceptual ? 8u : 1u, kg = perceptual ? 25u : 1u;
+  auto dist = [](uint32_t s2, uint32_t w, uint32_t s1, uint32_t C) { return s2 + C * C * w - 2u * C * s1; };
+  {
+    const uint32_t C = (uint32_t)exp5(c);
+    const uint32_t lo = kr * dist(r2, rw, r1, C);
+    S.lbr[c] = make_uint2(lo, kr * dist(tr2, tw, tr1, C) - lo);
+    const uint32_t lob = dist(b2, bw, b1, C);
+    S.lbb[c] = make_uint2(lob, dist(tb2, tw, tb1, C) - lob);
+  }
+  {
+    const uint32_t C = (uint32_t)exp6(c), C2 = (uint32_t)exp6(c + 32);
+    const uint32_t lo = kg * dist(g2, gw, g1, C), lo2 = kg * dist(g22, gw2, g12, C2);
+    S.lbg[c] = make_uint2(lo, kg * dist(tg2, tw, tg1, C) - lo);
+    S.lbg[c + 32] = make_uint2(lo2, kg * dist(tg2, tw, tg1, C2) - lo2);
+  }
+}
+
+template <bool HC>
+__device__ void phase2_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, bool perceptual,
+                             bool use_alpha, uint8_t* __restrict__ out, uint64_t* __restrict__ err_out) {
+  const uint32_t lane = lane_id();
+  // unique colours in first-occurrence order via match_any (lanes >= 16 carry sentinels)
+  uint32_t pixel = lane < 16 ? __ldg(reinterpret_cast<const uint32_t*>(px) + lane) : 0;
+  const uint32_t key = lane < 16 ? (pixel & 0xFFFFFFu) : (0x80000000u | lane);
+  const unsigned match = __match_any_sync(FULL_MASK, key);
+  const int leader = __ffs(match) - 1;
+  const bool is_leader = lane < 16 && leader == (int)lane;
+  const unsigned lmask = __ballot_sync(FULL_MASK, is_leader);
+  const int n = __popc(lmask);
+  const int uidx = __popc(lmask & ((1u << leader) - 1u));
+  const float wr = perceptual ? 8.f : 1.f, wg = perceptual ? 25.f : 1.f;
+  if (is_leader) {
+    const uint32_t c = key;
+    const float r = (float)(c & 255), g = (float)((c >> 8) & 255), b = (float)(c >> 16);
+    S.ucf[uidx] = make_float4(r, g, b, wr * r * r + wg * g * g + b * b);
+    S.ucw[uidx] = __popc(match);
+    S.uci[uidx] = c;
+  }
+  __syncwarp();
+  build_lower_bounds(S, n, perceptual);
+  __syncwarp();
+  Search<HC> srch(S, n, perceptual, use_alpha);
+  if (n == 1) {
+    const uint32_t c = S.uci[0];
+    const int r = c & 255, g = (c >> 8) & 255, b = c >> 16;
+    srch.run_list(use_alpha ? 2 : 1, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
+      if (i == 0) {
+        lo = pack565(c_sct.m5[r][0], c_sct.m6[g][0], c_sct.m5[b][0]);
+        hi = pack565(c_sct.m5[r][1], c_sct.m6[g][1], c_sct.m5[b][1]);
+      } else {
+        lo = pack565(c_sct.m5_3[r][0], c_sct.m6_3[g][0], c_sct.m5_3[b][0]);
+        hi = pack565(c_sct.m5_3[r][1], c_sct.m6_3[g][1], c_sct.m5_3[b][1]);
+      }
+      return true;
+    });
+  } else {
+    float axis[3], low[3], high[3];
+    for (int k = 0; k < 3; k++) { axis[k] = S.p1f[slot][k]; low[k] = S.p1f[slot][3 + k]; high[k] = S.p1f[slot][6 + k]; }
+    uint32_t med[6];
+    for (int k = 0; k < 6; k++) med[k] = S.p1m[slot][k];
+    srch.optimize(axis, low, high, med);
+  }
+  // return_solution :263-365
+  srch.compute_selectors();
+  const Best& b = srch.sel_source();
+  const int my_sel = (int)lane < n ? srch.selector_of(lane, b) : 0;
+  const int s = __shfl_sync(FULL_MASK, my_sel, lane < 16 ? uidx : 0);
+  const bool invert = srch.best.alpha ? srch.best.lo > srch.best.hi : srch.best.lo < srch.best.hi;
+  int sel = s;
+  if (invert) sel = srch.best.alpha ? (s < 2 ? (s ^ 1) : s) : (s ^ 1);
+  const uint32_t bits = __reduce_or_sync(FULL_MASK, lane < 16 ? ((uint32_t)sel << (2 * lane)) : 0u);
+  if (lane == 0) {
+    const uint32_t lo = invert ? srch.best.hi : srch.best.lo, hi = invert ? srch.best.lo : srch.best.hi;
+    uint2 w = make_uint2(lo | (hi << 16), bits);
+    *reinterpret_cast<uint2*>(out) = w;
+    if (err_out) *err_out = srch.best.err;
+  }
+}
+
+template <bool HC>
+__global__ void __launch_bounds__(kWarpsPerCta * 32)
+    k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, int perceptual, int use_alpha, uint8_t* __restrict__ out,
+                  uint32_t out_stride, uint64_t* __restrict__ err_out) {
+  __shared__ WarpShared smem[kWarpsPerCta];
+  WarpShared& S = smem[threadIdx.x >> 5];
+  const uint32_t lane = lane_id();
+  const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  const uint32_t nwarps = gridDim.x * kWarpsPerCta;
+  const uint32_t chunks = (n + kBlocksPerWarp - 1) / kBlocksPerWarp;
+  for (uint32_t chunk = warp_global; chunk < chunks; chunk += nwarps) {
+    const uint32_t b0 = chunk * kBlocksPerWarp;
+    const uint32_t cnt = min((uint32_t)kBlocksPerWarp, n - b0);
+    if (lane < cnt) phase1_block(S, lane, blocks + (size_t)(b0 + lane) * 64, perceptual != 0);
+    __syncwarp();
+    for (uint32_t k = 0; k < cnt; k++) {
+      const uint32_t bi = b0 + k;
+      phase2_block<HC>(S, k, blocks + (size_t)bi * 64, perceptual != 0, use_alpha != 0, out + (size_t)bi * out_stride,
+                       err_out ? err_out + bi : nullptr);
+      __syncwarp();
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// DXT5A: warp per block, lane per (low, high) candidate.
+
+struct Alpha5 {
+  int n;
+  uint32_t val[16], wt[16];
+  bool both;
+  // error of both block types for one (l, h); 8-value preferred on ties
+  __device__ __forceinline__ void eval(int l, int h, uint32_t& err, int& type) const {
+    int p8[8], p6[8];
+    p8[0] = l; p8[1] = h;
+    p8[2] = (l * 6 + h) / 7; p8[3] = (l * 5 + h * 2) / 7; p8[4] = (l * 4 + h * 3) / 7;
+    p8[5] = (l * 3 + h * 4) / 7; p8[6] = (l * 2 + h * 5) / 7; p8[7] = (l + h * 6) / 7;
+    p6[0] = l; p6[1] = h;
+    p6[2] = (l * 4 + h) / 5; p6[3] = (l * 3 + h * 2) / 5; p6[4] = (l * 2 + h * 3) / 5; p6[5] = (l + h * 4) / 5;
+    p6[6] = 0; p6[7] = 255;
+    uint32_t e8 = 0, e6 = 0;
+    for (int i = 0; i < n; i++) {
+      const int v = (int)val[i];
+      int m8 = 1 << 30, m6 = 1 << 30;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int d8 = v - p8[j], d6 = v - p6[j];
+        m8 = min(m8, d8 * d8);
+        m6 = min(m6, d6 * d6);
+      }
+      e8 += (uint32_t)m8 * wt[i];
+      e6 += (uint32_t)m6 * wt[i];
+    }
+    if (both && e6 < e8) { err = e6; type = 1; }
+    else { err = e8; type = 0; }
+  }
+};
+
+__global__ void __launch_bounds__(128)
+    k_dxt5a_encode(const uint8_t* __restrict__ blocks, uint32_t n, int comp, int both, uint8_t* __restrict__ out,
+                   uint32_t out_stride) {
+  const uint32_t lane = lane_id();
+  const uint32_t warp_global = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const uint32_t nwarps = gridDim.x * 4;
+  for (uint32_t bi = warp_global; bi < n; bi += nwarps) {
+    const uint8_t* px = blocks + (size_t)bi * 64;
+    const uint32_t v = lane < 16 ? __ldg(px + lane * 4 + comp) : 0x100u + lane;
+    const unsigned match = __match_any_sync(FULL_MASK, v);
+    const int leader = __ffs(match) - 1;
+    const bool is_leader = lane < 16 && leader == (int)lane;
+    const unsigned lmask = __ballot_sync(FULL_MASK, is_leader);
+    Alpha5 A;
+    A.n = __popc(lmask);
+    A.both = both != 0;
+    const int uidx = __popc(lmask & ((1u << leader) - 1u));
+    // every lane gets the unique values (first-occurrence order) and weights
+    {
+      unsigned m = lmask;
+      for (int i = 0; i < A.n; i++) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        A.val[i] = __shfl_sync(FULL_MASK, v, src);
+        A.wt[i] = (uint32_t)__popc(__shfl_sync(FULL_MASK, match, src));
+      }
+    }
+    uint32_t first = 0, second = 0, berr = kInf;
+    int btype = 0;
+    uint8_t* o = out + (size_t)bi * out_stride;
+    if (A.n == 1) {
+      if (lane == 0) {
+        uint2 w = make_uint2(A.val[0] | (A.val[0] << 8), 0u);
+        *reinterpret_cast<uint2*>(o) = w;
+      }
+      continue;
+    }
+    auto accept_chain = [&](bool valid, int l, int h, uint32_t err, int type, bool dependent) -> int {
+      unsigned ok = __ballot_sync(FULL_MASK, valid && err < berr);
+      int last = -1;
+      while (ok) {
+        const int j = __ffs(ok) - 1;
+        berr = __shfl_sync(FULL_MASK, err, j);
+        first = (uint32_t)__shfl_sync(FULL_MASK, l, j);
+        second = (uint32_t)__shfl_sync(FULL_MASK, h, j);
+        btype = __shfl_sync(FULL_MASK, type, j);
+        last = j;
+        if (dependent) break;
+        const unsigned after = j == 31 ? 0u : (FULL_MASK << (j + 1));
+        ok = __ballot_sync(FULL_MASK, valid && err < berr) & after;
+      }
+      return last;
+    };
+    // all unique value pairs i < j (compute :83-96)
+    const int npairs = A.n * (A.n - 1) / 2;
+    for (int p0 = 0; p0 < npairs; p0 += 32) {
+      const int p = p0 + (int)lane;
+      int l = 0, h = 0;
+      const bool valid = p < npairs;
+      if (valid) {
+        int i = 0, rem = p;
+        while (rem >= A.n - 1 - i) { rem -= A.n - 1 - i; i++; }
+        l = (int)A.val[i];
+        h = (int)A.val[i + 1 + rem];
+      }
+      uint32_t err = kInf;
+      int type = 0;
+      if (valid) A.eval(l, h, err, type);
+      accept_chain(valid, l, h, err, type, false);
+    }
+    // +-16 probe around the running best (:98-141); the centre moves with each improvement
+    if (berr) {
+      int pos = 0, row_l = (int)first - 16;
+      const int total = 33 * 33;
+      while (pos < total) {
+        const int p = pos + (int)lane;
+        const int row0 = pos / 33;
+        int l = 0, h = 0;
+        bool valid = p < total;
+        if (valid) {
+          const int r = p / 33, c = p % 33;
+          l = r == row0 ? row_l : (int)first + (r - 16);
+          h = (int)second + (c - 16);
+          valid = l >= 0 && l <= 255 && h >= 0 && h <= 255;
+        }
+        uint32_t err = kInf;
+        int type = 0;
+        if (valid) A.eval(l, h, err, type);
+        const int last = accept_chain(valid, l, h, err, type, true);
+        const int next = last >= 0 ? pos + last + 1 : pos + 32;
+        const int nrow = next / 33;
+        // the reference fixes l when a row starts: a row begun inside this batch used the
+        // centre from before the batch, unless it is the accepted candidate's own row
+        const int last_row = last >= 0 ? (pos + last) / 33 : -1;
+        if (last >= 0 && nrow == last_row) row_l = __shfl_sync(FULL_MASK, l, last);
+        else if (nrow != row0) row_l = (int)first + (nrow - 16);
+        pos = next;
+      }
+    }
+    // selectors of the winner, reorder rules (:143-185), pack (dxt5_block, crn_dxt.h:318-361)
+    int sel = 0;
+    if (lane < 16) {
+      const int l = (int)first, h = (int)second;
+      int pv[8];
+      pv[0] = l; pv[1] = h;
+      if (btype == 0) {
+        pv[2] = (l * 6 + h) / 7; pv[3] = (l * 5 + h * 2) / 7; pv[4] = (l * 4 + h * 3) / 7;
+        pv[5] = (l * 3 + h * 4) / 7; pv[6] = (l * 2 + h * 5) / 7; pv[7] = (l + h * 6) / 7;
+      } else {
+        pv[2] = (l * 4 + h) / 5; pv[3] = (l * 3 + h * 2) / 5; pv[4] = (l * 2 + h * 3) / 5; pv[5] = (l + h * 4) / 5;
+        pv[6] = 0; pv[7] = 255;
+      }
+      const int x = (int)A.val[uidx];
+      int bd = 1 << 30;
+      for (int j = 0; j < 8; j++) {
+        const int d = (x - pv[j]) * (x - pv[j]);
+        if (d < bd) { bd = d; sel = j; }
+      }
+    }
+    uint32_t f = first, s = second;
+    if (f == s) {
+      sel = 0;
+    } else if (btype) {
+      if (f > s) {
+        const uint32_t t = f; f = s; s = t;
+        const int inv6[8] = {1, 0, 5, 4, 3, 2, 6, 7};
+        sel = inv6[sel];
+      }
+    } else if (f <= s) {
+      const uint32_t t = f; f = s; s = t;
+      const int inv8[8] = {1, 0, 7, 6, 5, 4, 3, 2};
+      sel = inv8[sel];
+    }
+    const uint32_t lo_bits = __reduce_or_sync(FULL_MASK, lane < 10 ? ((uint32_t)sel << (3 * lane)) : 0u);
+    const uint32_t hi_bits = __reduce_or_sync(FULL_MASK, (lane >= 10 && lane < 16) ? ((uint32_t)sel << (3 * (lane - 10))) : 0u);
+    if (lane == 0) {
+      const uint64_t bits = (uint64_t)lo_bits | ((uint64_t)hi_bits << 30);
+      const uint64_t word = (uint64_t)f | ((uint64_t)s << 8) | (bits << 16);
+      *reinterpret_cast<uint2*>(o) = make_uint2((uint32_t)word, (uint32_t)(word >> 32));
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host side
+
+namespace {
+
+// ryg table construction (crnlib/crn_ryg_dxt.cpp:58-99,517-535), same integer algorithm
+void build_single_colour(SingleColour& t) {
+  auto build = [](uint8_t (*tab)[2], int bits, bool three) {
+    const int size = 1 << bits;
+    for (int v = 0; v < 256; v++) {
+      int best = 256;
+      for (int lo = 0; lo < size; lo++) {
+        for (int hi = 0; hi < size; hi++) {
+          const int le = bits == 5 ? (lo << 3) | (lo >> 2) : (lo << 2) | (lo >> 4);
+          const int he = bits == 5 ? (hi << 3) | (hi >> 2) : (hi << 2) | (hi >> 4);
+          const int interp = three ? ((le + he) >> 1) : ((he * 2 + le) / 3);
+          const int d = interp - v, spread = he - le;
+          const int e = (d < 0 ? -d : d) + (((spread < 0 ? -spread : spread) * 8) >> 8);
+          if (e < best) { tab[v][0] = (uint8_t)hi; tab[v][1] = (uint8_t)lo; best = e; }
+        }
+      }
+    }
+  };
+  build(t.m5, 5, false);
+  build(t.m6, 6, false);
+  build(t.m5_3, 5, true);
+  build(t.m6_3, 6, true);
+}
+
+struct DeviceInit {
+  bool done[64] = {};
+};
+
+int ensure_tables() {
+  static DeviceInit init;
+  static SingleColour* host = nullptr;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
+  if (dev < 64 && init.done[dev]) return CRNGPU_OK;
+  if (!host) {
+    host = new SingleColour;
+    build_single_colour(*host);
+  }
+  if ((e = cudaMemcpyToSymbol(c_sct, host, sizeof(SingleColour))) != cudaSuccess) return cuda_check(e, "upload tables");
+  if (dev < 64) init.done[dev] = true;
+  return CRNGPU_OK;
+}
+
+int grid_for(const void* kernel, int threads, uint32_t work_units) {
+  int dev = 0, sms = 148, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+  if (per_sm < 1) per_sm = 1;
+  const uint32_t full = (uint32_t)sms * (uint32_t)per_sm;
+  return (int)(work_units < full ? (work_units ? work_units : 1) : full);
+}
+
+}  // namespace
+
+// Device-pointer launches (no synchronization).
+int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_alpha_blocks, uint8_t* d_out,
+                uint32_t out_stride, uint64_t* d_err, cudaStream_t s) {
+  int rc = ensure_tables();
+  if (rc != CRNGPU_OK) return rc;
+  if (!n) return CRNGPU_OK;
+  const uint32_t warps_needed = (n + kBlocksPerWarp - 1) / kBlocksPerWarp;
+  const uint32_t ctas_needed = (warps_needed + kWarpsPerCta - 1) / kWarpsPerCta;
+  if (use_alpha_blocks) {
+    const int grid = grid_for((const void*)k_dxt1_encode<false>, kWarpsPerCta * 32, ctas_needed);
+    k_dxt1_encode<false><<<grid, kWarpsPerCta * 32, 0, s>>>(d_blocks, n, perceptual, 1, d_out, out_stride, d_err);
+  } else {
+    const int grid = grid_for((const void*)k_dxt1_encode<true>, kWarpsPerCta * 32, ctas_needed);
+    k_dxt1_encode<true><<<grid, kWarpsPerCta * 32, 0, s>>>(d_blocks, n, perceptual, 0, d_out, out_stride, d_err);
+  }
+  return cuda_check(cudaGetLastError(), "launch k_dxt1_encode");
+}
+
+int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint8_t* d_out, uint32_t out_stride,
+                 cudaStream_t s) {
+  if (!n) return CRNGPU_OK;
+  const int grid = grid_for((const void*)k_dxt5a_encode, 128, (n + 3) / 4);
+  k_dxt5a_encode<<<grid, 128, 0, s>>>(d_blocks, n, comp, both ? 1 : 0, d_out, out_stride);
+  return cuda_check(cudaGetLastError(), "launch k_dxt5a_encode");
+}
+
+}  // namespace crngpu

@@ -1,0 +1,193 @@
+// C ABI for the block encoders: batch entry points (dxt1_endpoint_optimizer::compute,
+// dxt5_endpoint_optimizer::compute, crn_compress_block) and the plain image path
+// (dxt_image::init, crnlib/crn_dxt_image.cpp:283-349,447-493).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "crngpu_internal.h"
+
+namespace crngpu {
+
+int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_alpha_blocks, uint8_t* d_out,
+                uint32_t out_stride, uint64_t* d_err, cudaStream_t s);
+int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint8_t* d_out, uint32_t out_stride,
+                 cudaStream_t s);
+
+namespace {
+
+// Image -> 4x4 blocks with edge clamping (init_task :334-344): texel (x, y) of block (bx, by)
+// is img[min(4by+y, h-1)][min(4bx+x, w-1)]. One thread per output texel.
+__global__ void k_gather_blocks(const uint8_t* __restrict__ img, uint32_t w, uint32_t h, uint32_t pitch,
+                                uint32_t blocks_x, uint64_t total_texels, uint32_t* __restrict__ out) {
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total_texels;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t blk = t >> 4;
+    const uint32_t tin = (uint32_t)t & 15;
+    const uint32_t by = (uint32_t)(blk / blocks_x), bx = (uint32_t)(blk - (uint64_t)by * blocks_x);
+    const uint32_t x = min(bx * 4 + (tin & 3), w - 1), y = min(by * 4 + (tin >> 2), h - 1);
+    const uint8_t* p = img + (uint64_t)y * pitch + (uint64_t)x * 4;
+    out[t] = (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+  }
+}
+
+int bytes_per_block(uint32_t fmt) {
+  switch (fmt) {
+    case CRNGPU_FMT_DXT1: case CRNGPU_FMT_DXT5A: return 8;
+    case CRNGPU_FMT_DXT5: case CRNGPU_FMT_DXT5_CCXY: case CRNGPU_FMT_DXT5_XGXR: case CRNGPU_FMT_DXT5_XGBR:
+    case CRNGPU_FMT_DXT5_AGBR: case CRNGPU_FMT_DXN_XY: case CRNGPU_FMT_DXN_YX: return 16;
+    default: return 0;
+  }
+}
+
+// Launches the element encoders of one format on device buffers (dxt_image element layout,
+// crnlib/crn_dxt_image.cpp:150-200: DXT5 = alpha block then colour block, DXN = X then Y).
+int encode_device(const uint8_t* d_in, uint32_t n, uint32_t fmt, uint32_t flags, uint8_t* d_out, cudaStream_t s) {
+  const bool perceptual = (flags & CRNGPU_FLAG_PERCEPTUAL) != 0;
+  const bool both = (flags & CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES) != 0;
+  switch (fmt) {
+    case CRNGPU_FMT_DXT1: return launch_dxt1(d_in, n, perceptual, both, d_out, 8, nullptr, s);
+    case CRNGPU_FMT_DXT5A: return launch_dxt5a(d_in, n, 3, both, d_out, 8, s);
+    case CRNGPU_FMT_DXN_XY:
+    case CRNGPU_FMT_DXN_YX: {
+      const int c0 = fmt == CRNGPU_FMT_DXN_XY ? 0 : 1;
+      int rc = launch_dxt5a(d_in, n, c0, both, d_out, 16, s);
+      if (rc == CRNGPU_OK) rc = launch_dxt5a(d_in, n, 1 - c0, both, d_out + 8, 16, s);
+      return rc;
+    }
+    default: {  // DXT5 family: alpha element, then a colour element that may not use 3-colour blocks
+      int rc = launch_dxt5a(d_in, n, 3, both, d_out, 16, s);
+      if (rc == CRNGPU_OK) rc = launch_dxt1(d_in, n, perceptual, false, d_out + 8, 16, nullptr, s);
+      return rc;
+    }
+  }
+}
+
+// Runs `fn(d_in, d_out, d_err)` with host or device buffers; host buffers are staged.
+template <typename F>
+int with_buffers(const uint8_t* in, size_t in_bytes, uint8_t* out, size_t out_bytes, uint64_t* err, size_t err_bytes,
+                 int mem, cudaStream_t s, F fn) {
+  if (mem == CRNGPU_MEM_DEVICE) {
+    if (((uintptr_t)in & 15) || ((uintptr_t)out & 7) || ((uintptr_t)err & 7)) {
+      set_error("device buffers must be 16-byte (input) / 8-byte (output) aligned");
+      return CRNGPU_E_PARAM;
+    }
+    return fn(in, out, err);
+  }
+  cudaError_t e;
+  DevBuf& bi = staging(0);
+  DevBuf& bo = staging(1);
+  DevBuf& be = staging(3);
+  if ((e = bi.ensure(in_bytes)) != cudaSuccess) return cuda_check(e, "alloc input stage");
+  if ((e = bo.ensure(out_bytes)) != cudaSuccess) return cuda_check(e, "alloc output stage");
+  if (err && (e = be.ensure(err_bytes)) != cudaSuccess) return cuda_check(e, "alloc error stage");
+  if ((e = cudaMemcpyAsync(bi.ptr, in, in_bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    return cuda_check(e, "copy input");
+  int rc = fn(static_cast<const uint8_t*>(bi.ptr), static_cast<uint8_t*>(bo.ptr),
+              err ? static_cast<uint64_t*>(be.ptr) : nullptr);
+  if (rc != CRNGPU_OK) return rc;
+  if ((e = cudaMemcpyAsync(out, bo.ptr, out_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    return cuda_check(e, "copy output");
+  if (err && (e = cudaMemcpyAsync(err, be.ptr, err_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    return cuda_check(e, "copy errors");
+  return cuda_check(cudaStreamSynchronize(s), "sync");
+}
+
+}  // namespace
+
+}  // namespace crngpu
+
+using namespace crngpu;
+
+extern "C" int crngpu_dxt1_optimize_batch(const uint8_t* rgba_blocks, uint32_t n, const crngpu_dxt1_params* params,
+                                          uint8_t* out_blocks, uint64_t* out_error, int mem, void* stream) {
+  clear_error();
+  if (!params || params->struct_size != sizeof(crngpu_dxt1_params) || (n && (!rgba_blocks || !out_blocks))) {
+    set_error("bad arguments");
+    return CRNGPU_E_PARAM;
+  }
+  if (!n) return CRNGPU_OK;
+  cudaStream_t s = as_stream(stream);
+  return with_buffers(rgba_blocks, (size_t)n * 64, out_blocks, (size_t)n * 8, out_error, (size_t)n * 8, mem, s,
+                      [&](const uint8_t* in, uint8_t* out, uint64_t* err) {
+                        return launch_dxt1(in, n, params->perceptual != 0, params->use_alpha_blocks != 0, out, 8, err,
+                                           s);
+                      });
+}
+
+extern "C" int crngpu_dxt5a_optimize_batch(const uint8_t* rgba_blocks, uint32_t n, uint32_t comp_index,
+                                           int32_t use_both_block_types, uint8_t* out_blocks, int mem, void* stream) {
+  clear_error();
+  if (comp_index > 3 || (n && (!rgba_blocks || !out_blocks))) { set_error("bad arguments"); return CRNGPU_E_PARAM; }
+  if (!n) return CRNGPU_OK;
+  cudaStream_t s = as_stream(stream);
+  return with_buffers(rgba_blocks, (size_t)n * 64, out_blocks, (size_t)n * 8, nullptr, 0, mem, s,
+                      [&](const uint8_t* in, uint8_t* out, uint64_t*) {
+                        return launch_dxt5a(in, n, (int)comp_index, use_both_block_types != 0, out, 8, s);
+                      });
+}
+
+extern "C" int crngpu_compress_blocks(const uint8_t* rgba_blocks, uint32_t n, uint32_t format, uint32_t flags,
+                                      uint8_t* out_blocks, int mem, void* stream) {
+  clear_error();
+  const int bpb = bytes_per_block(format);
+  if (!bpb) { set_error("unsupported format"); return CRNGPU_E_UNSUPPORTED; }
+  if (n && (!rgba_blocks || !out_blocks)) { set_error("bad arguments"); return CRNGPU_E_PARAM; }
+  if (!n) return bpb;
+  cudaStream_t s = as_stream(stream);
+  const int rc = with_buffers(rgba_blocks, (size_t)n * 64, out_blocks, (size_t)n * bpb, nullptr, 0, mem, s,
+                              [&](const uint8_t* in, uint8_t* out, uint64_t*) {
+                                return encode_device(in, n, format, flags, out, s);
+                              });
+  return rc == CRNGPU_OK ? bpb : rc;
+}
+
+extern "C" int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, uint32_t height, uint32_t pitch_bytes,
+                                         uint32_t format, uint32_t flags, uint8_t* out, uint64_t out_size, int mem,
+                                         void* stream) {
+  clear_error();
+  const int bpb = bytes_per_block(format);
+  if (!bpb) { set_error("unsupported format"); return CRNGPU_E_UNSUPPORTED; }
+  if (!rgba || !out || !width || !height) { set_error("bad arguments"); return CRNGPU_E_PARAM; }
+  if (!pitch_bytes) pitch_bytes = width * 4;
+  if (pitch_bytes < width * 4) { set_error("bad pitch"); return CRNGPU_E_PARAM; }
+  const uint32_t bx = (width + 3) / 4, by = (height + 3) / 4;
+  const uint64_t n = (uint64_t)bx * by;
+  const uint64_t need = n * (uint64_t)bpb;
+  if (out_size < need || n > 0xFFFFFFFFull) { set_error("output too small"); return CRNGPU_E_PARAM; }
+  cudaStream_t s = as_stream(stream);
+  cudaError_t e;
+  const size_t img_bytes = (size_t)pitch_bytes * (height - 1) + (size_t)width * 4;
+  DevBuf& blocks = staging(2);
+  if ((e = blocks.ensure(n * 64)) != cudaSuccess) return cuda_check(e, "alloc blocks");
+  const uint8_t* d_img = rgba;
+  if (mem != CRNGPU_MEM_DEVICE) {
+    DevBuf& bi = staging(0);
+    if ((e = bi.ensure(img_bytes)) != cudaSuccess) return cuda_check(e, "alloc image stage");
+    if ((e = cudaMemcpyAsync(bi.ptr, rgba, img_bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return cuda_check(e, "copy image");
+    d_img = static_cast<const uint8_t*>(bi.ptr);
+  }
+  const uint64_t texels = n * 16;
+  const uint32_t grid = (uint32_t)((texels + 255) / 256 < 65535 * 8 ? (texels + 255) / 256 : 65535 * 8);
+  k_gather_blocks<<<grid, 256, 0, s>>>(d_img, width, height, pitch_bytes, bx, texels, static_cast<uint32_t*>(blocks.ptr));
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_gather_blocks");
+  uint8_t* d_out = out;
+  DevBuf* so = nullptr;
+  if (mem != CRNGPU_MEM_DEVICE) {
+    so = &staging(1);
+    if ((e = so->ensure(need)) != cudaSuccess) return cuda_check(e, "alloc output stage");
+    d_out = static_cast<uint8_t*>(so->ptr);
+  } else if ((uintptr_t)out & 7) {
+    set_error("device output must be 8-byte aligned");
+    return CRNGPU_E_PARAM;
+  }
+  int rc = encode_device(static_cast<const uint8_t*>(blocks.ptr), (uint32_t)n, format, flags, d_out, s);
+  if (rc != CRNGPU_OK) return rc;
+  if (so) {
+    if ((e = cudaMemcpyAsync(out, so->ptr, need, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+      return cuda_check(e, "copy output");
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
+  }
+  return (int64_t)need;
+}

@@ -1,0 +1,152 @@
+/*
+ * crngpu: GB300 (sm_103a) implementation of crnlib's DXTn hot path behind a plain C ABI.
+ *
+ * Every entry point takes plain pointers and sizes. Buffers are either host or device
+ * memory, as each call's `mem` argument says; device pointers must live on the current
+ * CUDA device. `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ * Calls are asynchronous on `stream` only when every buffer is device memory; with any host
+ * buffer the call synchronizes before returning.
+ *
+ * Status codes: >= 0 success (some calls return a size), < 0 failure (CRNGPU_E_*).
+ */
+#ifndef CRNGPU_H
+#define CRNGPU_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define CRNGPU_API __attribute__((visibility("default")))
+#else
+#define CRNGPU_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CRNGPU_OK 0
+#define CRNGPU_E_PARAM (-1)        /* bad argument (size, pitch, level, format, NULL) */
+#define CRNGPU_E_CORRUPT (-2)      /* malformed .crn data (header, tables or block stream) */
+#define CRNGPU_E_DEVICE (-3)       /* CUDA error (allocation, launch, copy) */
+#define CRNGPU_E_UNSUPPORTED (-4)  /* valid request outside this library's scope */
+
+/* Memory kinds for the `mem` arguments. */
+#define CRNGPU_MEM_HOST 0
+#define CRNGPU_MEM_DEVICE 1
+
+/* crn_format values (inc/crnlib.h:71-110). */
+#define CRNGPU_FMT_DXT1 0
+#define CRNGPU_FMT_DXT5 2
+#define CRNGPU_FMT_DXT5_CCXY 3
+#define CRNGPU_FMT_DXT5_XGXR 4
+#define CRNGPU_FMT_DXT5_XGBR 5
+#define CRNGPU_FMT_DXT5_AGBR 6
+#define CRNGPU_FMT_DXN_XY 7
+#define CRNGPU_FMT_DXN_YX 8
+#define CRNGPU_FMT_DXT5A 9
+
+/* crn_comp_flags bits that the block encoders honour (inc/crnlib.h:132-185). */
+#define CRNGPU_FLAG_PERCEPTUAL 1u
+#define CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES 8u
+
+/* Library version and last-error text (thread-local). */
+CRNGPU_API const char* crngpu_version(void);
+CRNGPU_API const char* crngpu_last_error(void);
+
+/* ------------------------------------------------------------------------------------------
+ * Block encoders (quality: cCRNDXTQualityUber; endpoint caching is never used, so results do
+ * not depend on how blocks are batched).
+ * --------------------------------------------------------------------------------------- */
+
+/* Parameters of dxt1_endpoint_optimizer::params (crnlib/crn_dxt1.h:168-201) that apply to
+ * 16-texel blocks: perceptual metric and whether 3-colour (alpha) blocks may be used. */
+typedef struct crngpu_dxt1_params {
+    uint32_t struct_size;      /* sizeof(crngpu_dxt1_params) */
+    int32_t perceptual;        /* m_perceptual */
+    int32_t use_alpha_blocks;  /* m_use_alpha_blocks */
+    int32_t reserved;
+} crngpu_dxt1_params;
+
+/* Batched replacement for dxt1_endpoint_optimizer::compute (crnlib/crn_dxt1.h:223,
+ * crnlib/crn_dxt1.cpp:2234) plus the dxt1_block packing of dxt_image::set_block_pixels
+ * (crnlib/crn_dxt_image.cpp:1436-1490).
+ *   rgba_blocks: n x 64 bytes (16 RGBA8 texels, row-major within the block)
+ *   out_blocks:  n x 8 bytes (dxt1_block: LE16 low colour, LE16 high colour, 4 selector bytes)
+ *   out_error:   optional (NULL), n x uint64 squared error (results::m_error)
+ * Returns CRNGPU_OK or an error code. */
+CRNGPU_API int crngpu_dxt1_optimize_batch(const uint8_t* rgba_blocks, uint32_t n, const crngpu_dxt1_params* params,
+                               uint8_t* out_blocks, uint64_t* out_error, int mem, void* stream);
+
+/* Batched replacement for dxt5_endpoint_optimizer::compute (crnlib/crn_dxt5a.h:72,
+ * crnlib/crn_dxt5a.cpp:40-196) plus dxt5_block packing (crnlib/crn_dxt_image.cpp:1491-1522).
+ *   comp_index: channel (0..3) of each texel to encode; use_both_block_types: allow 6-value blocks
+ *   out_blocks: n x 8 bytes (dxt5_block) */
+CRNGPU_API int crngpu_dxt5a_optimize_batch(const uint8_t* rgba_blocks, uint32_t n, uint32_t comp_index,
+                                int32_t use_both_block_types, uint8_t* out_blocks, int mem, void* stream);
+
+/* Batched replacement for crn_compress_block (inc/crnlib.h:679, crnlib/crnlib.cpp:351-418):
+ * encodes n 4x4 blocks to `format` (DXT1, DXT5 family, DXN_XY/YX, DXT5A) with the block
+ * layout dxt_image produces. flags: CRNGPU_FLAG_* (crn_comp_params::m_flags).
+ * Returns bytes per block (8 or 16) or an error code. */
+CRNGPU_API int crngpu_compress_blocks(const uint8_t* rgba_blocks, uint32_t n, uint32_t format, uint32_t flags,
+                           uint8_t* out_blocks, int mem, void* stream);
+
+/* Plain (quality 255, no clustering) DXTn encode of one RGBA8 image, the dxt_image::init path
+ * (crnlib/crn_dxt_image.cpp:283-349,447-493): 4x4 blocks with edge clamping, block-row-major
+ * output, row pitch = blocks_x * bytes_per_block. pitch_bytes: source row pitch (0 = width*4).
+ * Returns the number of output bytes or an error code. */
+CRNGPU_API int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, uint32_t height, uint32_t pitch_bytes,
+                              uint32_t format, uint32_t flags, uint8_t* out, uint64_t out_size, int mem,
+                              void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * CRN -> DXTn transcoder (crnd::crn_unpacker, inc/crn_decomp.h:3498-4223; API inc/crn_defs.h:
+ * 174-205). Supported: DXT1, DXT5 family, DXN_XY/YX, DXT5A. ETC formats: CRNGPU_E_UNSUPPORTED.
+ * --------------------------------------------------------------------------------------- */
+
+typedef struct crngpu_unpack_context_s* crngpu_unpack_context;
+
+/* Replaces crnd_unpack_begin (inc/crn_defs.h:174): parses the header, Huffman models and
+ * palettes on the host and uploads the file, decode tables and palettes to the current device.
+ * The caller's buffer may be freed after this returns. NULL on failure. */
+CRNGPU_API crngpu_unpack_context crngpu_unpack_begin(const void* data, uint32_t data_size);
+
+/* Texture geometry of an open context (crnd_get_texture_info, inc/crn_defs.h:152). */
+CRNGPU_API int crngpu_get_info(crngpu_unpack_context ctx, uint32_t* width, uint32_t* height, uint32_t* levels,
+                    uint32_t* faces, uint32_t* format, uint32_t* bytes_per_block);
+
+/* Replaces crnd_unpack_level (inc/crn_defs.h:188-191, checks inc/crn_decomp.h:3569-3575):
+ * writes level `level_index` of every face to dst_faces[f] (faces pointers), each
+ * dst_size_in_bytes large, rows row_pitch_in_bytes apart (0 = minimal; else >= minimal and a
+ * multiple of 4). Returns CRNGPU_OK or an error code. */
+CRNGPU_API int crngpu_unpack_level(crngpu_unpack_context ctx, void** dst_faces, uint32_t dst_size_in_bytes,
+                        uint32_t row_pitch_in_bytes, uint32_t level_index, int mem, void* stream);
+
+/* Segmented variant (crnd_unpack_level_segmented, inc/crn_defs.h:196-200): the level's
+ * compressed bytes come from `src` instead of the file passed to crngpu_unpack_begin. */
+CRNGPU_API int crngpu_unpack_level_segmented(crngpu_unpack_context ctx, const void* src, uint32_t src_size_in_bytes,
+                                  void** dst_faces, uint32_t dst_size_in_bytes, uint32_t row_pitch_in_bytes,
+                                  uint32_t level_index, int mem, void* stream);
+
+/* Transcodes levels [first_level, first_level + level_count) in one decode launch and one
+ * expansion launch. dst: one buffer receiving the levels back to back, each level
+ * faces x blocks_y x (blocks_x * bytes_per_block) bytes (minimal pitch). Returns the total number
+ * of bytes written or an error code. */
+CRNGPU_API int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t first_level, uint32_t level_count, void* dst,
+                             uint64_t dst_size, int mem, void* stream);
+
+/* Replaces crnd_unpack_end (inc/crn_defs.h:205). Returns CRNGPU_OK, or CRNGPU_E_PARAM for NULL. */
+CRNGPU_API int crngpu_unpack_end(crngpu_unpack_context ctx);
+
+/* Same contract as the reference's extern "C" crn_decompress (emscripten/crunch_lib.cpp:40,
+ * 91-120): transcodes levels firstLevel .. firstLevel+levelCount-1 of face 0 back to back into
+ * dst (host memory), each level with minimal pitch; levels whose width or height shifts to 0
+ * are skipped without advancing dst, as in the reference. */
+CRNGPU_API void crngpu_crn_decompress(void* src, unsigned int src_size, void* dst, unsigned int dst_size,
+                           unsigned int firstLevel, unsigned int levelCount);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CRNGPU_H */

@@ -1,0 +1,200 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's golden vectors and the
+oracle (CPU restatement pinned to those vectors)."""
+import numpy as np
+import pytest
+
+import golden_util as G
+from dxt_decode import dxt1_error, rgb_rmse
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def cg():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import crunch2_gb300
+    crunch2_gb300.lib()
+    return crunch2_gb300
+
+
+@pytest.fixture(scope="module")
+def gold():
+    return G.blocks()
+
+
+def check_dxt1(out, ref, pixels, perceptual, exact_min=0.999):
+    """>= 99.9% identical blocks, no differing block with a higher error, RMSE within 0.01."""
+    same = (out == ref).all(1)
+    frac = same.mean()
+    if not same.all():
+        e_out = dxt1_error(out[~same], pixels[~same], perceptual)
+        e_ref = dxt1_error(ref[~same], pixels[~same], perceptual)
+        assert (e_out <= e_ref).all(), "a differing block has a higher error than the reference"
+    assert abs(rgb_rmse(out, pixels) - rgb_rmse(ref, pixels)) <= 0.01
+    assert frac >= exact_min, f"only {frac:.5f} of blocks identical"
+    return frac
+
+
+@pytest.mark.parametrize("perc", [1, 0])
+@pytest.mark.parametrize("both", [1, 0])
+@pytest.mark.parametrize("device", [True, False])
+def test_dxt1_edge_blocks(cg, gold, perc, both, device):
+    blocks = gold["edge_in"]
+    inp = torch.from_numpy(blocks).cuda() if device else blocks
+    out = cg.dxt1_optimize(inp, bool(perc), bool(both))
+    out = out.cpu().numpy() if device else out
+    frac = check_dxt1(out, gold[f"edge_dxt1_p{perc}_b{both}"], blocks, bool(perc))
+    print(f"edge dxt1 p{perc} b{both}: identical {frac:.5f}")
+
+
+def test_dxt1_config0_texture(cg, gold):
+    blocks = G.c0_blocks()
+    out = cg.dxt1_optimize(torch.from_numpy(blocks).cuda()).cpu().numpy()
+    check_dxt1(out, gold["c0_dxt1"], blocks, True)
+
+
+def test_dxt1_error_output_matches_oracle(cg, gold):
+    from oracle import port
+    blocks = gold["edge_in"][:512]
+    out, err = cg.dxt1_optimize(blocks, True, True, with_error=True)
+    ref, ref_err = port.dxt1_blocks(blocks, True, True)
+    same = (out == ref).all(1)
+    assert (err[same] == ref_err[same]).all()
+
+
+@pytest.mark.parametrize("name,fmt", [("dxt5", 2), ("dxn_xy", 7), ("dxn_yx", 8), ("dxt5a", 9)])
+@pytest.mark.parametrize("both", [1, 0])
+def test_alpha_formats(cg, gold, name, fmt, both):
+    flags = cg.FLAG_PERCEPTUAL | (cg.FLAG_USE_BOTH_BLOCK_TYPES if both else 0)
+    out = cg.compress_blocks(gold["edge_in"], fmt, flags)
+    ref = gold[f"edge_{name}_b{both}"]
+    same = (out == ref).all(1)
+    if fmt == 2:  # colour half goes through the float optimizer: same bar as DXT1
+        assert (out[:, :8] == ref[:, :8]).all(), "DXT5 alpha half must be bit-exact"
+        check_dxt1(out[:, 8:], ref[:, 8:], gold["edge_in"], True)
+    else:
+        assert same.all(), np.nonzero(~same)[0][:10]
+
+
+def test_dxt5_dxn_textures(cg, gold):
+    out = cg.compress_blocks(G.dxt5_tex_blocks(), 2, cg.FLAG_PERCEPTUAL | cg.FLAG_USE_BOTH_BLOCK_TYPES)
+    ref = gold["dxt5_tex_dxt5"]
+    assert (out[:, :8] == ref[:, :8]).all()
+    check_dxt1(out[:, 8:], ref[:, 8:], G.dxt5_tex_blocks(), True)
+    nrm = cg.compress_blocks(G.nrm_tex_blocks(), 7, cg.FLAG_USE_BOTH_BLOCK_TYPES)
+    assert (nrm == gold["nrm_tex_dxn_xy"]).all()
+
+
+def test_compress_image_edge_clamp(cg):
+    from crunch2_gb300 import texgen
+    from oracle import port
+    img = texgen.colour_texture(37, 22, 5)  # ragged: 10 x 6 blocks with clamped edges
+    out = cg.compress_image(img, cg.FMT_DXT1)
+    ref, _ = port.dxt1_blocks(texgen.image_blocks(img), True, True)
+    assert (out == ref).all(1).mean() >= 0.999
+    dev = cg.compress_image(torch.from_numpy(img).cuda(), cg.FMT_DXT1).cpu().numpy()
+    assert (dev == out).all()
+
+
+def test_empty_batch(cg):
+    out = cg.dxt1_optimize(np.zeros((0, 64), np.uint8))
+    assert out.shape == (0, 8)
+
+
+# ------------------------------------------------------------------------------------------
+# transcoder
+
+@pytest.mark.parametrize("name", sorted(G.manifest().keys()))
+def test_transcode_levels_bit_exact(cg, name):
+    m = G.manifest()[name]
+    crn = G.crn_bytes(name)
+    with cg.unpack_begin(crn) as ctx:
+        assert (ctx.width, ctx.height, ctx.faces) == (m["width"], m["height"], m["faces"])
+        for lvl, info in enumerate(m["levels"]):
+            out = ctx.unpack_level(lvl)
+            assert G.sha(out.reshape(-1)) == info["sha256"], (name, lvl)
+            dev = torch.zeros(out.size, dtype=torch.uint8, device="cuda")
+            ctx.unpack_level(lvl, out=dev.view(ctx.faces, -1))
+            assert G.sha(dev.cpu().numpy()) == info["sha256"], (name, lvl, "device")
+        allv = ctx.unpack_levels()
+        pos = 0
+        for lvl, info in enumerate(m["levels"]):
+            assert G.sha(allv[pos:pos + info["bytes"]]) == info["sha256"]
+            pos += info["bytes"]
+
+
+def test_transcode_row_pitch_padding(cg):
+    crn = G.crn_bytes("dxt5_256")
+    with cg.unpack_begin(crn) as ctx:
+        bx, by = ctx.level_dims(1)
+        pitch = bx * 16 + 20  # multiple of 4, not 16: exercises the scalar store path
+        out = np.full((1, by * pitch), 0xAB, np.uint8)
+        ctx.unpack_level(1, row_pitch=pitch, out=out)
+        tight = ctx.unpack_level(1).reshape(by, bx * 16)
+        rows = out.reshape(by, pitch)
+        assert (rows[:, :bx * 16] == tight).all()
+        assert (rows[:, bx * 16:] == 0xAB).all()
+
+
+def test_transcode_segmented(cg):
+    import struct
+    crn = G.crn_bytes("dxt1_256")
+    ofs = [struct.unpack(">I", crn[70 + 4 * l:74 + 4 * l])[0] for l in range(9)]
+    with cg.unpack_begin(crn) as ctx:
+        for lvl in (0, 3, 8):
+            end = ofs[lvl + 1] if lvl + 1 < 9 else len(crn)
+            seg = np.frombuffer(crn[ofs[lvl]:end], np.uint8).copy()
+            bx, by = ctx.level_dims(lvl)
+            out = np.zeros(bx * by * 8, np.uint8)
+            faces = (cg.ctypes.c_void_p * 1)(out.ctypes.data)
+            rc = cg.lib().crngpu_unpack_level_segmented(ctx.handle, seg.ctypes.data, seg.size, faces, out.size, 0,
+                                                        lvl, cg.MEM_HOST, None)
+            assert rc == 0
+            assert (out == ctx.unpack_level(lvl).reshape(-1)).all()
+
+
+def test_crn_decompress_contract(cg):
+    crn = G.crn_bytes("c1_dxt1_1024")
+    m = G.manifest()["c1_dxt1_1024"]
+    total = sum(l["bytes"] for l in m["levels"][2:6])
+    out = cg.crn_decompress(crn, 2, 4, total)
+    pos = 0
+    for info in m["levels"][2:6]:
+        assert G.sha(out[pos:pos + info["bytes"]]) == info["sha256"]
+        pos += info["bytes"]
+
+
+def test_transcode_rejects_bad_input(cg):
+    crn = bytearray(G.crn_bytes("dxt1_256"))
+    with pytest.raises(cg.CrnGpuError):
+        cg.unpack_begin(bytes(crn[:60]))
+    bad = bytearray(crn)
+    bad[0] ^= 0xFF
+    with pytest.raises(cg.CrnGpuError):
+        cg.unpack_begin(bytes(bad))
+    with cg.unpack_begin(bytes(crn)) as ctx:
+        with pytest.raises(cg.CrnGpuError):
+            ctx.unpack_level(0, row_pitch=6)
+        with pytest.raises(cg.CrnGpuError):
+            ctx.unpack_level(99)
+
+
+def test_transcode_corrupt_stream_reports_error(cg):
+    """Random garbage in a level's block stream must come back as an error or as some output,
+    never as a hang or a fault; the device decoder bounds every table and palette index."""
+    import struct
+    crn = bytearray(G.crn_bytes("dxt5_256"))
+    lvl0 = struct.unpack(">I", bytes(crn[70:74]))[0]
+    rng = np.random.default_rng(7)
+    for trial in range(8):
+        bad = bytearray(crn)
+        pos = lvl0 + int(rng.integers(0, 64))
+        bad[pos:pos + 64] = rng.integers(0, 256, 64, dtype=np.uint8).tobytes()
+        with cg.unpack_begin(bytes(bad)) as ctx:
+            try:
+                ctx.unpack_level(0)
+            except cg.CrnGpuError as e:
+                assert e.code == cg.E_CORRUPT
