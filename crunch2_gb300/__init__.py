@@ -82,6 +82,8 @@ def lib():
     L.crngpu_unpack_end.restype = i32
     L.crngpu_crn_decompress.argtypes = [vp, ctypes.c_uint, vp, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint]
     L.crngpu_crn_decompress.restype = None
+    L.crngpu_profile_counters.argtypes = [i32, ctypes.POINTER(ctypes.c_uint64), vp]
+    L.crngpu_profile_counters.restype = i32
     _lib = L
     return L
 
@@ -92,6 +94,14 @@ def version() -> str:
 
 def last_error() -> str:
     return (lib().crngpu_last_error() or b"").decode(errors="replace")
+
+
+def profile_counters(enable: bool, stream=None) -> int:
+    """Returns the DXT1 candidate x colour evaluations counted since the last call and turns
+    counting on or off (profiling hook; counting is off by default)."""
+    v = ctypes.c_uint64(0)
+    _check(lib().crngpu_profile_counters(int(enable), ctypes.byref(v), _stream_ptr(stream)), "crngpu_profile_counters")
+    return int(v.value)
 
 
 def _check(rc: int, where: str) -> int:
@@ -105,9 +115,9 @@ def _is_torch_cuda(x) -> bool:
 
 
 def _ptr_mem(x):
-    """(pointer, mem kind) of a numpy array or torch CUDA tensor."""
-    if _is_torch_cuda(x):
-        return x.data_ptr(), MEM_DEVICE
+    """(pointer, mem kind) of a numpy array or a torch tensor (CUDA = device, CPU = host)."""
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr(), (MEM_DEVICE if x.is_cuda else MEM_HOST)
     return x.ctypes.data, MEM_HOST
 
 
@@ -118,9 +128,12 @@ def _stream_ptr(stream):
 
 
 def _out_like(inp, shape, dtype=np.uint8):
-    if _is_torch_cuda(inp):
+    if hasattr(inp, "data_ptr"):
         import torch
-        return torch.empty(shape, dtype={np.uint8: torch.uint8, np.uint64: torch.int64}[dtype], device=inp.device)
+        tdt = {np.uint8: torch.uint8, np.uint64: torch.int64}[dtype]
+        if inp.is_cuda:
+            return torch.empty(shape, dtype=tdt, device=inp.device)
+        return torch.empty(shape, dtype=tdt, pin_memory=inp.is_pinned())
     return np.zeros(shape, dtype)
 
 

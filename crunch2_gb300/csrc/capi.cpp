@@ -63,5 +63,20 @@ DevBuf& staging(int slot) {
 
 }  // namespace crngpu
 
+namespace crngpu {
+int set_work_counter(bool on, cudaStream_t s);
+int read_work_counter(uint64_t* value, cudaStream_t s);
+}
+
+extern "C" int crngpu_profile_counters(int enable, uint64_t* dxt1_evaluations, void* stream) {
+  crngpu::clear_error();
+  cudaStream_t s = crngpu::as_stream(stream);
+  if (dxt1_evaluations) {
+    const int rc = crngpu::read_work_counter(dxt1_evaluations, s);
+    if (rc != CRNGPU_OK) return rc;
+  }
+  return crngpu::set_work_counter(enable != 0, s);
+}
+
 extern "C" const char* crngpu_version(void) { return "crngpu 0.1 (sm_103a)"; }
 extern "C" const char* crngpu_last_error(void) { return crngpu::last_error_cstr(); }

@@ -57,26 +57,35 @@ constexpr int kMaxRowBlocks = 1024;  // 4096 px / 4, already even
 
 // ------------------------------------------------------------------------------------------
 // Bit reader: MSB-first 64-bit window; bytes past the end of the stream read as zero, as in
-// symbol_codec::get_bits / decode (inc/crn_decomp.h:3162-3214).
+// symbol_codec::get_bits / decode (inc/crn_decomp.h:3162-3214). After a byte-wise head the
+// stream is read as aligned 32-bit words (byte-swapped to MSB-first) with an L1 prefetch a few
+// lines ahead, so the lone decoding thread rarely waits on memory.
 struct Bits {
-  const uint8_t* p;
-  uint32_t pos, end;
+  const uint8_t* p;   // stream start
+  uint32_t pos, end;  // next byte to load, stream size
   uint64_t buf;
   int n;
   __device__ __forceinline__ void init(const uint8_t* src, uint32_t size) {
     p = src; pos = 0; end = size; buf = 0; n = 0;
+    // head: bytes up to the first 4-byte aligned address
+    while (((uintptr_t)(p + pos) & 3) && n <= 56) {
+      const uint32_t v = pos < end ? (uint32_t)__ldg(p + pos) : 0u;
+      buf |= (uint64_t)v << (56 - n);
+      n += 8;
+      pos++;
+    }
   }
   __device__ __forceinline__ void refill() {
     if (n <= 32) {
       uint32_t w;
       if (pos + 4 <= end) {
-        w = ((uint32_t)__ldg(p + pos) << 24) | ((uint32_t)__ldg(p + pos + 1) << 16) |
-            ((uint32_t)__ldg(p + pos + 2) << 8) | (uint32_t)__ldg(p + pos + 3);
+        w = __byte_perm(__ldg(reinterpret_cast<const uint32_t*>(p + pos)), 0, 0x0123);
+        if ((pos & 127) == 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(p + pos + 1024));
+      } else if (pos < end) {
+        w = __byte_perm(__ldg(reinterpret_cast<const uint32_t*>(p + pos)), 0, 0x0123);
+        w &= 0xFFFFFFFFu << (8 * (4 - (end - pos)));  // zero the bytes past the end
       } else {
         w = 0;
-#pragma unroll
-        for (int k = 0; k < 4; k++)
-          if (pos + k < end) w |= (uint32_t)__ldg(p + pos + k) << (24 - 8 * k);
       }
       pos += 4;
       buf |= (uint64_t)w << (32 - n);
@@ -85,12 +94,12 @@ struct Bits {
   }
 };
 
-// Canonical prefix decode (symbol_codec::decode, inc/crn_decomp.h:3186-3253): 11-bit table,
-// then a walk over left-aligned per-length limits. Returns -1 for a pattern that is no code.
-__device__ __forceinline__ int decode_sym(Bits& b, const DevModel* __restrict__ m) {
+// Canonical prefix decode (symbol_codec::decode, inc/crn_decomp.h:3186-3253): 11-bit table in
+// shared memory, then a walk over left-aligned per-length limits. -1: no such code.
+__device__ __forceinline__ int decode_sym(Bits& b, const uint32_t* __restrict__ lut, const DevModel* __restrict__ m) {
   b.refill();
   const uint32_t v = (uint32_t)(b.buf >> 48);
-  const uint32_t e = __ldg(&m->lut[v >> (16 - kLutBits)]);
+  const uint32_t e = lut[v >> (16 - kLutBits)];
   uint32_t s, len;
   if (e != kLutLong) {
     s = e & 0xFFFFu;
@@ -115,13 +124,30 @@ __device__ __forceinline__ uint32_t rb_a(uint32_t e) { return (e >> 2) & 0x1FFFu
 __device__ __forceinline__ uint32_t rb_b(uint32_t e) { return (e >> 15) & 0x1FFFu; }
 
 // KIND: 0 DXT1, 1 DXT5 (colour + alpha), 2 DXN (two alpha), 3 DXT5A
+// Number of prefix models a format reads: ref + (colour ep, sel) + (alpha ep, sel).
+template <int KIND>
+__host__ __device__ constexpr int models_used() { return KIND == 1 ? 5 : 3; }
+
 template <int KIND>
 __global__ void __launch_bounds__(32) k_crn_decode(const DecodeJob* __restrict__ jobs, int njobs,
                                                     const DevModel* __restrict__ models, DevPalettes pal,
                                                     void* __restrict__ records, uint32_t* __restrict__ status) {
   __shared__ uint32_t row[kMaxRowBlocks];
+  extern __shared__ uint32_t luts[];  // models_used<KIND>() x 2^kLutBits entries
   const int job_i = blockIdx.x;
-  if (job_i >= njobs || threadIdx.x != 0) return;
+  if (job_i >= njobs) return;
+  // the warp copies the first-level tables this format needs into shared memory
+  {
+    const int slots[5] = {kMRef, KIND == 0 || KIND == 1 ? kMEp0 : kMEp1, KIND == 0 || KIND == 1 ? kMSel0 : kMSel1,
+                          kMEp1, kMSel1};
+    for (int t = 0; t < models_used<KIND>(); t++) {
+      const uint4* src = reinterpret_cast<const uint4*>(models[slots[t]].lut);
+      uint4* dst = reinterpret_cast<uint4*>(luts + t * (1 << kLutBits));
+      for (int k = threadIdx.x; k < (1 << kLutBits) / 4; k += 32) dst[k] = __ldg(src + k);
+    }
+    __syncwarp();
+  }
+  if (threadIdx.x != 0) return;
   const DecodeJob job = jobs[job_i];
   const bool colour = KIND == 0 || KIND == 1;
   const int nalpha = KIND == 2 ? 2 : (KIND == 0 ? 0 : 1);
@@ -130,6 +156,11 @@ __global__ void __launch_bounds__(32) k_crn_decode(const DecodeJob* __restrict__
   const DevModel* m_sel0 = models + kMSel0;
   const DevModel* m_ep1 = models + kMEp1;
   const DevModel* m_sel1 = models + kMSel1;
+  const uint32_t* l_ref = luts;
+  const uint32_t* l_ep0 = luts + (1 << kLutBits);      // colour models (DXT1, DXT5) ...
+  const uint32_t* l_sel0 = luts + 2 * (1 << kLutBits);
+  const uint32_t* l_ep1 = KIND == 1 ? luts + 3 * (1 << kLutBits) : l_ep0;   // ... or alpha models
+  const uint32_t* l_sel1 = KIND == 1 ? luts + 4 * (1 << kLutBits) : l_sel0;
   const uint32_t W = (job.bx + 1) & ~1u, H = (job.by + 1) & ~1u;
   for (uint32_t x = 0; x < W; x++) row[x] = 0;
   Bits b;
@@ -147,7 +178,7 @@ __global__ void __launch_bounds__(32) k_crn_decode(const DecodeJob* __restrict__
         uint32_t ref;
         if (!(y & 1)) {
           if (!(x & 1)) {
-            const int g = decode_sym(b, m_ref);
+            const int g = decode_sym(b, l_ref, m_ref);
             if (g < 0) { err = kStBadCode; break; }
             group = (uint32_t)g & 0xFFu;  // reference_group is a uint8
           }
@@ -160,21 +191,21 @@ __global__ void __launch_bounds__(32) k_crn_decode(const DecodeJob* __restrict__
         // endpoint A = colour (DXT1/DXT5) or alpha0 (DXN/DXT5A); B = alpha0 (DXT5) or alpha1 (DXN)
         if (ref == 0) {
           if (colour) {
-            const int d = decode_sym(b, m_ep0);
+            const int d = decode_sym(b, l_ep0, m_ep0);
             if (d < 0) { err = kStBadCode; break; }
             cep += (uint32_t)d;
             if (cep >= pal.n_cep) cep -= pal.n_cep;
             if (cep >= pal.n_cep) { err = kStBadIndex; break; }
           }
           if (nalpha >= 1) {
-            const int d = decode_sym(b, m_ep1);
+            const int d = decode_sym(b, l_ep1, m_ep1);
             if (d < 0) { err = kStBadCode; break; }
             a0 += (uint32_t)d;
             if (a0 >= pal.n_aep) a0 -= pal.n_aep;
             if (a0 >= pal.n_aep) { err = kStBadIndex; break; }
           }
           if (nalpha == 2) {
-            const int d = decode_sym(b, m_ep1);
+            const int d = decode_sym(b, l_ep1, m_ep1);
             if (d < 0) { err = kStBadCode; break; }
             a1 += (uint32_t)d;
             if (a1 >= pal.n_aep) a1 -= pal.n_aep;
@@ -193,19 +224,19 @@ __global__ void __launch_bounds__(32) k_crn_decode(const DecodeJob* __restrict__
         row[x] = e;
         uint32_t cs = 0, s0 = 0, s1 = 0;
         if (colour) {
-          const int s = decode_sym(b, m_sel0);
+          const int s = decode_sym(b, l_sel0, m_sel0);
           if (s < 0) { err = kStBadCode; break; }
           if ((uint32_t)s >= pal.n_csel) { err = kStBadIndex; break; }
           cs = (uint32_t)s;
         }
         if (nalpha >= 1) {
-          const int s = decode_sym(b, m_sel1);
+          const int s = decode_sym(b, l_sel1, m_sel1);
           if (s < 0) { err = kStBadCode; break; }
           if ((uint32_t)s >= pal.n_asel) { err = kStBadIndex; break; }
           s0 = (uint32_t)s;
         }
         if (nalpha == 2) {
-          const int s = decode_sym(b, m_sel1);
+          const int s = decode_sym(b, l_sel1, m_sel1);
           if (s < 0) { err = kStBadCode; break; }
           if ((uint32_t)s >= pal.n_asel) { err = kStBadIndex; break; }
           s1 = (uint32_t)s;
@@ -305,7 +336,7 @@ int upload_context(UnpackContext* c, const uint8_t* data, uint32_t size) {
   cudaError_t e = cudaGetDevice(&c->device);
   if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
   // file bytes, padded so word reads near the end stay inside the allocation
-  if ((e = c->d_file.ensure(size + 16)) != cudaSuccess) return cuda_check(e, "alloc file");
+  if ((e = c->d_file.ensure(size + 64)) != cudaSuccess) return cuda_check(e, "alloc file");
   if ((e = cudaMemcpy(c->d_file.ptr, data, size, cudaMemcpyHostToDevice)) != cudaSuccess)
     return cuda_check(e, "copy file");
   std::unique_ptr<DevModel[]> models(new DevModel[kNumModels]);
@@ -351,7 +382,8 @@ int upload_context(UnpackContext* c, const uint8_t* data, uint32_t size) {
 
 template <int K>
 void launch_decode(const DecodeJob* jobs, int njobs, UnpackContext* c, void* rec, uint32_t* st, cudaStream_t s) {
-  k_crn_decode<K><<<njobs, 32, 0, s>>>(jobs, njobs, static_cast<const DevModel*>(c->d_models.ptr), c->pal, rec, st);
+  const size_t smem = sizeof(uint32_t) * (1 << kLutBits) * models_used<K>();  // <= 40 KB, no opt-in needed
+  k_crn_decode<K><<<njobs, 32, smem, s>>>(jobs, njobs, static_cast<const DevModel*>(c->d_models.ptr), c->pal, rec, st);
 }
 template <int K>
 void launch_expand(const ExpandJob* jobs, int njobs, uint32_t ctas, UnpackContext* c, const void* rec, int vec,
@@ -468,7 +500,7 @@ int unpack_one(UnpackContext* c, const uint8_t* host_src, const uint8_t* dev_src
   if (dev_src) { o.src = dev_src; o.src_size = src_size; }
   else if (host_src) {
     DevBuf& sb = staging(2);
-    if ((e = sb.ensure(src_size + 16)) != cudaSuccess) return cuda_check(e, "alloc segment");
+    if ((e = sb.ensure(src_size + 64)) != cudaSuccess) return cuda_check(e, "alloc segment");
     if ((e = cudaMemcpyAsync(sb.ptr, host_src, src_size, cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return cuda_check(e, "copy segment");
     o.src = static_cast<const uint8_t*>(sb.ptr);

@@ -57,14 +57,50 @@ __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 // exact float (integer value in [0, 2^23)) -> uint via the 2^23 magic constant
 __device__ __forceinline__ uint32_t f2u_exact(float v) { return __float_as_uint(__fadd_rn(v, 8388608.0f)) - 0x4B000000u; }
 
-// Per-warp shared state for phase 2 (one block at a time).
+constexpr int kHashBits = 11;
+constexpr int kHashSize = 1 << kHashBits;
+constexpr int kHashProbe = 8;
+
+// A DXT1 solution (dxt1_endpoint_optimizer::potential_solution, crn_dxt1.h:272-311) minus its
+// selectors, which are recomputed from it when needed.
+struct Sol {
+  uint32_t lo, hi, err;
+  int alpha, alt, enforce, enforced;
+};
+
+// Warp-uniform search state.
+struct State {
+  Sol best, snap;  // snap: the best at the last compute_selectors() (hc path)
+  int n, hc, three;
+  float wr, wg;
+};
+
+// Candidate list kinds consumed by run_list (the reference's candidate loops).
+enum : int { LK_TABLE = 0, LK_PAIRS, LK_NEIGH, LK_MOVE2, LK_REFINE, LK_COMB, LK_COMPS };
+
+struct ListDesc {
+  int kind, count, dependent, alt, stop_on_accept;
+  int side, nh, row;
+  int base[3];  // NEIGH/MOVE2: centre; COMPS: unpacked high endpoint
+  int e[6];     // REFINE: fitted endpoints (At1 triple, At2 triple)
+  // COMPS: per-component error tables and running bounds
+  int comp, p0;
+  uint32_t packed_lo, e0, best_err;
+  uint32_t W[4], WP2[4], WPP[4], rem[4];
+};
+
+// Per-warp shared state: phase-1 hand-off for the warp's blocks plus phase-2 working set.
 struct WarpShared {
   float4 ucf[16];     // r, g, b as floats, X2 = weighted |x|^2
   int ucw[16];        // weights
   uint32_t uci[16];   // r | g << 8 | b << 16
   uint2 lbr[32], lbg[64], lbb[32];  // plane lower bounds: .x = low, .y = high
-  uint16_t list[64];  // scratch candidate list (probes / solid / combinatorial)
-  uint16_t list2[32];
+  uint16_t list[64];  // low-endpoint probes / combinatorial endpoints
+  uint16_t list2[32]; // high-endpoint probes
+  uint32_t cand[64];  // table candidates (lo | hi << 16) / combinatorial scratch colours
+  State st;
+  ListDesc d;
+  __align__(16) uint32_t hset[kHashSize];  // tried-solution keys (lo | hi << 16), kInf = empty
   // phase-1 hand-off, one slot per block of the warp's chunk
   float p1f[kBlocksPerWarp][9];     // axis[3], low[3], high[3]
   uint32_t p1m[kBlocksPerWarp][6];  // try_median4 candidates (lo | hi << 16)
@@ -73,11 +109,6 @@ struct WarpShared {
   uint32_t t_col[16][kBlocksPerWarp];
   uint8_t t_w[16][kBlocksPerWarp];
   float t_norm[3][16][kBlocksPerWarp];
-};
-
-struct Best {
-  uint32_t lo, hi, err;
-  int alpha, alt, enforce, enforced;
 };
 
 // ------------------------------------------------------------------------------------------
@@ -382,516 +413,599 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
 }
 
 // ------------------------------------------------------------------------------------------
-// Phase 2 (one warp = one block).
+// Phase 2 (one warp = one block). All search state that is uniform across the warp (running
+// best, list descriptor, candidate tables, tried-set) lives in the warp's shared memory, and a
+// single non-inlined list runner holds the one copy of the candidate evaluation loop, so the
+// hot loop stays small enough for the instruction cache.
 
-template <bool HC>
-struct Search {
-  WarpShared& S;
-  int n;
-  bool perceptual, use_alpha;
-  Best best;
-  Best snap;  // hc: the best at the last compute_selectors() call (selectors are lazy there)
-  float wr, wg, wb;
-  uint32_t lane;
-
-  __device__ Search(WarpShared& s, int n_, bool perc, bool alpha_blocks)
-      : S(s), n(n_), perceptual(perc), use_alpha(alpha_blocks) {
-    best.lo = best.hi = 0; best.err = kInf; best.alpha = 0; best.alt = 0; best.enforce = 0; best.enforced = 0;
-    snap = best;
-    wr = perc ? 8.f : 1.f; wg = perc ? 25.f : 1.f; wb = 1.f;
-    lane = lane_id();
-  }
-
+__device__ __forceinline__ uint32_t lower_bound(const WarpShared& S, uint32_t lo, uint32_t hi) {
   // evaluate_solution's plane-table prune (crn_dxt1.cpp:1312-1322)
-  __device__ __forceinline__ uint32_t lower_bound(uint32_t lo, uint32_t hi) const {
-    const int r0 = lo >> 11, g0 = (lo >> 5) & 63, b0 = lo & 31;
-    const int r1 = hi >> 11, g1 = (hi >> 5) & 63, b1 = hi & 31;
-    const uint32_t re = r0 < r1 ? S.lbr[r0].x + S.lbr[r1].y : S.lbr[r0].y + S.lbr[r1].x;
-    const uint32_t ge = g0 < g1 ? S.lbg[g0].x + S.lbg[g1].y : S.lbg[g0].y + S.lbg[g1].x;
-    const uint32_t be = b0 < b1 ? S.lbb[b0].x + S.lbb[b1].y : S.lbb[b0].y + S.lbb[b1].x;
-    return re + ge + be;
-  }
+  const int r0 = lo >> 11, g0 = (lo >> 5) & 63, b0 = lo & 31;
+  const int r1 = hi >> 11, g1 = (hi >> 5) & 63, b1 = hi & 31;
+  const uint32_t re = r0 < r1 ? S.lbr[r0].x + S.lbr[r1].y : S.lbr[r0].y + S.lbr[r1].x;
+  const uint32_t ge = g0 < g1 ? S.lbg[g0].x + S.lbg[g1].y : S.lbg[g0].y + S.lbg[g1].x;
+  const uint32_t be = b0 < b1 ? S.lbb[b0].x + S.lbb[b1].y : S.lbb[b0].y + S.lbb[b1].x;
+  return re + ge + be;
+}
 
-  // Palette entry k -> (q = 2 w p, P2 = w.p^2) for the expanded-square distance.
-  __device__ __forceinline__ void entry(int r, int g, int b, float4& q) const {
-    const float fr = (float)r, fg = (float)g, fb = (float)b;
-    q.x = 2.f * wr * fr; q.y = 2.f * wg * fg; q.z = 2.f * wb * fb;
-    q.w = wr * fr * fr + wg * fg * fg + wb * fb * fb;
-  }
-  __device__ __forceinline__ static float dist_part(const float4& x, const float4& q) {
-    float t = fmaf(-x.x, q.x, q.w);
-    t = fmaf(-x.y, q.y, t);
-    return fmaf(-x.z, q.z, t);
-  }
+// Palette entry -> (q = 2 w p, P2 = w.p^2) for the expanded-square distance.
+__device__ __forceinline__ float4 entry(float wr, float wg, int r, int g, int b) {
+  const float fr = (float)r, fg = (float)g, fb = (float)b;
+  return make_float4(2.f * wr * fr, 2.f * wg * fg, 2.f * fb, wr * fr * fr + wg * fg * fg + fb * fb);
+}
+__device__ __forceinline__ float dist_part(const float4& x, const float4& q) {
+  float t = fmaf(-x.x, q.x, q.w);
+  t = fmaf(-x.y, q.y, t);
+  return fmaf(-x.z, q.z, t);
+}
 
-  // Full error of one candidate. Uber path (evaluate_solution_uber :1370-1592): min over the
-  // 4-colour and (if allowed) 3-colour block, 4-colour preferred on ties. hc path
-  // (evaluate_solution_hc_* :1759-1835): 4-colour only.
-  __device__ __forceinline__ void eval(uint32_t lo, uint32_t hi, int alt, uint32_t& err, int& type) const {
-    const int r0 = exp5(lo >> 11), g0 = exp6((lo >> 5) & 63), b0 = exp5(lo & 31);
-    const int r1 = exp5(hi >> 11), g1 = exp6((hi >> 5) & 63), b1 = exp5(hi & 31);
-    float4 q0, q1, q2, q3, q4;
-    entry(r0, g0, b0, q0);
-    entry(r1, g1, b1, q1);
-    entry((r0 * 2 + r1 + alt) / 3, (g0 * 2 + g1 + alt) / 3, (b0 * 2 + b1 + alt) / 3, q2);
-    entry((r1 * 2 + r0 + alt) / 3, (g1 * 2 + g0 + alt) / 3, (b1 * 2 + b0 + alt) / 3, q3);
-    const bool three = !HC && use_alpha;
-    if (three) entry((r0 + r1 + alt) >> 1, (g0 + g1 + alt) >> 1, (b0 + b1 + alt) >> 1, q4);
-    uint32_t e0 = 0, e1 = 0;
-    for (int i = 0; i < n; i++) {
-      const float4 x = S.ucf[i];
-      const uint32_t w = (uint32_t)S.ucw[i];
-      const float d0 = dist_part(x, q0), d1 = dist_part(x, q1), d2 = dist_part(x, q2), d3 = dist_part(x, q3);
-      const float m01 = fminf(d0, d1);
-      const float m4 = fminf(m01, fminf(d2, d3));
-      e0 += w * f2u_exact(__fadd_rn(x.w, m4));
-      if (three) {
-        const float m3 = fminf(m01, dist_part(x, q4));
-        e1 += w * f2u_exact(__fadd_rn(x.w, m3));
-      }
-    }
-    if (three && e1 < e0) { err = e1; type = 1; }
-    else { err = e0; type = 0; }
+// Selector of unique colour i for solution s; ties go to the lowest index, which is how both
+// the uber trial loop and compute_selectors_hc (crn_dxt1.cpp:1845-1869) resolve them.
+__device__ __noinline__ int selector_of(const WarpShared& S, int i, const Sol& s) {
+  if (s.enforce) return s.enforced;
+  const float wr = S.st.wr, wg = S.st.wg;
+  const int r0 = exp5(s.lo >> 11), g0 = exp6((s.lo >> 5) & 63), b0 = exp5(s.lo & 31);
+  const int r1 = exp5(s.hi >> 11), g1 = exp6((s.hi >> 5) & 63), b1 = exp5(s.hi & 31);
+  const int a = s.alt;
+  float4 q[4];
+  q[0] = entry(wr, wg, r0, g0, b0);
+  q[1] = entry(wr, wg, r1, g1, b1);
+  if (s.alpha) {
+    q[2] = entry(wr, wg, (r0 + r1 + a) >> 1, (g0 + g1 + a) >> 1, (b0 + b1 + a) >> 1);
+  } else {
+    q[2] = entry(wr, wg, (r0 * 2 + r1 + a) / 3, (g0 * 2 + g1 + a) / 3, (b0 * 2 + b1 + a) / 3);
+    q[3] = entry(wr, wg, (r1 * 2 + r0 + a) / 3, (g1 * 2 + g0 + a) / 3, (b1 * 2 + b0 + a) / 3);
   }
-
-  // Selector of unique colour i for solution `s` (ties -> lowest index, as both the uber
-  // loop and compute_selectors_hc resolve them).
-  __device__ __forceinline__ int selector_of(int i, const Best& s) const {
-    if (s.enforce) return s.enforced;
-    const int r0 = exp5(s.lo >> 11), g0 = exp6((s.lo >> 5) & 63), b0 = exp5(s.lo & 31);
-    const int r1 = exp5(s.hi >> 11), g1 = exp6((s.hi >> 5) & 63), b1 = exp5(s.hi & 31);
-    float4 q[4];
-    entry(r0, g0, b0, q[0]);
-    entry(r1, g1, b1, q[1]);
-    const int a = s.alt;
-    if (s.alpha) {
-      entry((r0 + r1 + a) >> 1, (g0 + g1 + a) >> 1, (b0 + b1 + a) >> 1, q[2]);
-    } else {
-      entry((r0 * 2 + r1 + a) / 3, (g0 * 2 + g1 + a) / 3, (b0 * 2 + b1 + a) / 3, q[2]);
-      entry((r1 * 2 + r0 + a) / 3, (g1 * 2 + g0 + a) / 3, (b1 * 2 + b0 + a) / 3, q[3]);
-    }
-    const float4 x = S.ucf[i];
-    float bd = dist_part(x, q[0]);
-    int bi = 0;
-    const int nk = s.alpha ? 3 : 4;
-    for (int k = 1; k < nk; k++) {
-      const float d = dist_part(x, q[k]);
-      if (d < bd) { bd = d; bi = k; }
-    }
-    return bi;
+  const float4 x = S.ucf[i];
+  float bd = dist_part(x, q[0]);
+  int bi = 0;
+  const int nk = s.alpha ? 3 : 4;
+  for (int k = 1; k < nk; k++) {
+    const float d = dist_part(x, q[k]);
+    if (d < bd) { bd = d; bi = k; }
   }
+  return bi;
+}
 
-  // The selectors the reference's m_best_solution.m_selectors holds right now.
-  __device__ __forceinline__ const Best& sel_source() const { return HC ? snap : best; }
-  __device__ __forceinline__ void compute_selectors() { if (HC) snap = best; }
+// The selectors m_best_solution.m_selectors holds right now: the best itself on the uber path,
+// the best at the last compute_selectors() call on the hc path (selectors are lazy there).
+__device__ __forceinline__ const Sol& sel_source(const WarpShared& S) { return S.st.hc ? S.st.snap : S.st.best; }
+__device__ __forceinline__ void compute_selectors(WarpShared& S) {
+  if (S.st.hc && lane_id() == 0) S.st.snap = S.st.best;
+  __syncwarp();
+}
 
-  __device__ __forceinline__ void accept(uint32_t lo, uint32_t hi, uint32_t err, int type, int alt) {
-    best.lo = lo; best.hi = hi; best.err = err; best.alpha = type; best.alt = alt;
-    best.enforce = (!type && lo == hi) ? 1 : 0;
-    if (best.enforce) {
-      if ((best.lo & 31) != 31) { best.lo++; best.enforced = 1; }
-      else { best.hi--; best.enforced = 0; }
+__device__ __forceinline__ void accept(WarpShared& S, uint32_t lo, uint32_t hi, uint32_t err, int type, int alt) {
+  if (lane_id() == 0) {
+    Sol& b = S.st.best;
+    b.lo = lo; b.hi = hi; b.err = err; b.alpha = type; b.alt = alt;
+    b.enforce = (!type && lo == hi) ? 1 : 0;
+    if (b.enforce) {
+      if ((b.lo & 31) != 31) { b.lo++; b.enforced = 1; }
+      else { b.hi--; b.enforced = 0; }
     }
   }
+  __syncwarp();
+}
 
-  // Processes `count` candidates in order; gen(i, lo, hi) -> valid. Returns true if any was
-  // accepted. dependent: candidates depend on `best`, so regenerate after an acceptance.
-  template <typename Gen>
-  __device__ bool run_list(int count, bool dependent, int alt, Gen gen) {
-    bool any = false;
-    int i0 = 0;
-    while (i0 < count) {
-      const int i = i0 + (int)lane;
-      uint32_t lo = 0, hi = 0;
-      bool valid = false;
-      if (i < count) valid = gen(i, lo, hi);
-      const uint32_t lb = valid ? lower_bound(lo, hi) : kInf;
-      const bool live = valid && lb < best.err;
-      uint32_t err = kInf;
-      int type = 0;
-      if (live) eval(lo, hi, alt, err, type);
-      unsigned ok = __ballot_sync(FULL_MASK, live && err < best.err);
-      int last = -1;
-      while (ok) {
-        const int j = __ffs(ok) - 1;
-        const uint32_t jlo = __shfl_sync(FULL_MASK, lo, j), jhi = __shfl_sync(FULL_MASK, hi, j);
-        const uint32_t jerr = __shfl_sync(FULL_MASK, err, j);
-        const int jtype = __shfl_sync(FULL_MASK, type, j);
-        accept(jlo, jhi, jerr, jtype, alt);
-        any = true;
-        last = j;
-        if (dependent) break;
-        const unsigned after = j == 31 ? 0u : (FULL_MASK << (j + 1));
-        ok = __ballot_sync(FULL_MASK, valid && lb < best.err && err < best.err) & after;
-      }
-      if (dependent && last >= 0) i0 += last + 1;
-      else i0 += 32;
-    }
-    return any;
+// Tried-solution set (m_solutions_tried, crn_dxt1.cpp:1323-1330): open addressing in shared
+// memory. A hit may only be reported for a key that was really evaluated before; a miss (or a
+// full probe window) just means the candidate is evaluated again, which cannot change results.
+__device__ __forceinline__ uint32_t hslot(uint32_t key) { return (key * 0x9E3779B1u) >> (32 - kHashBits); }
+__device__ __forceinline__ bool hset_find(const WarpShared& S, uint32_t key) {
+  if (key == kInf) return false;  // the empty marker is never stored as a key
+  uint32_t h = hslot(key);
+  for (int k = 0; k < kHashProbe; k++) {
+    const uint32_t v = S.hset[(h + k) & (kHashSize - 1)];
+    if (v == key) return true;
+    if (v == kInf) return false;
   }
+  return false;
+}
+__device__ __forceinline__ void hset_insert(WarpShared& S, uint32_t key) {
+  if (key == kInf) return;
+  uint32_t h = hslot(key);
+  for (int k = 0; k < kHashProbe; k++) {
+    uint32_t* p = &S.hset[(h + k) & (kHashSize - 1)];
+    const uint32_t old = atomicCAS(p, kInf, key);
+    if (old == kInf || old == key) return;
+  }
+}
 
-  // refine_solution(1) :525-698 (least squares from the current selectors, then 2 x 27
-  // lattice neighbours of the two fitted endpoints)
-  __device__ bool refine() {
-    compute_selectors();
-    const Best& s = sel_source();
-    int a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // ak0 ak1 ak2 at1r at1g at1b at2r at2g at2b
-    if ((int)lane < n) {
-      const int step = selector_of(lane, s) ^ 1;
-      const int w = S.ucw[lane];
-      const uint32_t c = S.uci[lane];
-      const int r = (c & 255) * w, g = ((c >> 8) & 255) * w, b = (c >> 16) * w;
-      const int w1 = step == 0 ? 3 : step == 1 ? 0 : step == 2 ? 2 : 1;
-      const int p0 = step >= 2 ? 2 : 0;
-      const int p1 = step == 0 ? 0 : step == 1 ? 9 : step == 2 ? 1 : 4;
-      const int p2 = step == 0 ? 9 : step == 1 ? 0 : step == 2 ? 4 : 1;
-      a[0] = p0 * w; a[1] = p1 * w; a[2] = p2 * w;
-      a[3] = w1 * r; a[4] = w1 * g; a[5] = w1 * b;
-      a[6] = r; a[7] = g; a[8] = b;
-    }
-    for (int k = 0; k < 9; k++) a[k] = __reduce_add_sync(FULL_MASK, a[k]);
-    const long long xx = a[2], yy = a[1], xy = a[0];
-    const long long at1[3] = {a[3], a[4], a[5]};
-    const long long at2[3] = {3LL * a[6] - a[3], 3LL * a[7] - a[4], 3LL * a[8] - a[5]};
-    const long long t = xx * yy - xy * xy;
-    if (!yy || !xx || t == 0) return false;
-    // the six fitted components, one per lane, in double exactly as the reference
-    int comp = 0;
-    if (lane < 6) {
-      const int k = lane % 3;
-      const double frb = __ddiv_rn((double)__fdiv_rn(93.0f, 255.0f), (double)t);
-      const double f = k == 1 ? __dmul_rn(frb, (double)__fdiv_rn(63.0f, 31.0f)) : frb;
-      const long long num = lane < 3 ? at1[k] * yy - at2[k] * xy : at2[k] * xx - at1[k] * xy;
-      const double v = __dadd_rn(__dmul_rn((double)num, f), (double)0.5f);
-      comp = clampi(__double2int_rz(v), 0, k == 1 ? 63 : 31);
-    }
-    int e[2][3];
-    for (int k = 0; k < 6; k++) e[k / 3][k % 3] = __shfl_sync(FULL_MASK, comp, k);
-    return run_list(54, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
-      const int which = i / 27, rr = (i / 9) % 3 - 1, gr = (i / 3) % 3 - 1, br = i % 3 - 1;
-      int c[2][3] = {{e[0][0], e[0][1], e[0][2]}, {e[1][0], e[1][1], e[1][2]}};
-      c[which][0] = clampi(c[which][0] + rr, 0, 31);
-      c[which][1] = clampi(c[which][1] + gr, 0, 63);
-      c[which][2] = clampi(c[which][2] + br, 0, 31);
-      const uint32_t p0 = pack565(c[0][0], c[0][1], c[0][2]), p1 = pack565(c[1][0], c[1][1], c[1][2]);
-      lo = canon_lo(p0, p1);
-      hi = canon_hi(p0, p1);
+// Candidate i of the current list (descriptor in S.d); false when the reference skips it.
+__device__ __forceinline__ bool gen_candidate(const WarpShared& S, const ListDesc& d, int i, uint32_t& lo, uint32_t& hi) {
+  switch (d.kind) {
+    case LK_TABLE: {
+      const uint32_t v = S.cand[i];
+      lo = v & 0xFFFFu; hi = v >> 16;
       return true;
-    });
-  }
-
-  __device__ bool all_selectors_equal() const {
-    const Best& s = sel_source();
-    const int mine = (int)lane < n ? selector_of(lane, s) : -1;
-    const int first = __shfl_sync(FULL_MASK, mine, 0);
-    return __all_sync(FULL_MASK, (int)lane >= n || mine == first);
-  }
-
-  // try_average_block_as_solid :93-153
-  __device__ bool try_solid() {
-    int tr = 0, tg = 0, tb = 0;
-    if ((int)lane < n) {
-      const uint32_t c = S.uci[lane];
-      const int w = S.ucw[lane];
-      tr = (c & 255) * w; tg = ((c >> 8) & 255) * w; tb = (c >> 16) * w;
     }
-    tr = __reduce_add_sync(FULL_MASK, tr);
-    tg = __reduce_add_sync(FULL_MASK, tg);
-    tb = __reduce_add_sync(FULL_MASK, tb);
-    const int ar = (tr + 8) / 16, ag = (tg + 8) / 16, ab = (tb + 8) / 16;
-    // candidate list: (colour source, table) pairs; source 16 = the average
-    int cnt = 0;
-    if (lane == 0) {
-      S.list[cnt++] = (uint16_t)(16 << 1);
-      if (use_alpha) S.list[cnt++] = (uint16_t)((16 << 1) | 1);
-      for (int i = 0; i < n; i++) {
-        const uint32_t c = S.uci[i];
-        if ((int)(c & 255) == ar && (int)((c >> 8) & 255) == ag && (int)(c >> 16) == ab) continue;
-        S.list[cnt++] = (uint16_t)(i << 1);
-        if (use_alpha) S.list[cnt++] = (uint16_t)((i << 1) | 1);
-      }
+    case LK_PAIRS: {
+      const int a = i / d.nh, b = i - a * d.nh;
+      const uint32_t p0 = S.list[a], p1 = S.list2[b];
+      lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
+      return true;
     }
-    cnt = __shfl_sync(FULL_MASK, cnt, 0);
-    __syncwarp();
-    return run_list(cnt, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
-      const int e = S.list[i];
-      const int src = e >> 1;
-      int r = ar, g = ag, b = ab;
-      if (src < 16) { const uint32_t c = S.uci[src]; r = c & 255; g = (c >> 8) & 255; b = c >> 16; }
-      if (e & 1) {
-        lo = pack565(c_sct.m5_3[r][0], c_sct.m6_3[g][0], c_sct.m5_3[b][0]);
-        hi = pack565(c_sct.m5_3[r][1], c_sct.m6_3[g][1], c_sct.m5_3[b][1]);
+    case LK_NEIGH:
+    case LK_MOVE2: {
+      int c[3] = {d.base[0], d.base[1], d.base[2]};
+      if (d.kind == LK_NEIGH) {
+        // g_adjacency order (crn_dxt1.cpp:489-522): x fastest, then y, then z, centre skipped
+        const int idx = i < 13 ? i : i + 1;
+        c[0] += idx % 3 - 1; c[1] += (idx / 3) % 3 - 1; c[2] += idx / 9 - 1;
+        if (c[0] < 0 || c[0] > 31 || c[1] < 0 || c[1] > 63 || c[2] < 0 || c[2] > 31) return false;
       } else {
-        lo = pack565(c_sct.m5[r][0], c_sct.m6[g][0], c_sct.m5[b][0]);
-        hi = pack565(c_sct.m5[r][1], c_sct.m6[g][1], c_sct.m5[b][1]);
+        const int a = i >> 1;
+        c[a] += (i & 1) ? 2 : -2;
+        if (c[a] < 0 || c[a] > (a == 1 ? 63 : 31)) return false;
       }
+      const uint32_t moved = pack565(c[0], c[1], c[2]);
+      const uint32_t p0 = d.side ? S.st.best.lo : moved, p1 = d.side ? moved : S.st.best.hi;
+      lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
       return true;
-    });
+    }
+    case LK_REFINE: {
+      const int which = i / 27, rr = (i / 9) % 3 - 1, gr = (i / 3) % 3 - 1, br = i % 3 - 1;
+      int c[6] = {d.e[0], d.e[1], d.e[2], d.e[3], d.e[4], d.e[5]};
+      const int o = which * 3;
+      c[o] = clampi(c[o] + rr, 0, 31);
+      c[o + 1] = clampi(c[o + 1] + gr, 0, 63);
+      c[o + 2] = clampi(c[o + 2] + br, 0, 31);
+      const uint32_t p0 = pack565(c[0], c[1], c[2]), p1 = pack565(c[3], c[4], c[5]);
+      lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
+      return true;
+    }
+    case LK_COMB:
+      lo = S.list[d.row];
+      hi = S.list[d.row + 1 + i];
+      return true;
+    default: {  // LK_COMPS: optimize_endpoint_comps inner loop with its table prune (:440-470)
+      const int c1 = i;
+      const uint32_t p1 = (uint32_t)(d.comp == 1 ? exp6(c1) : exp5(c1));
+      const uint32_t p0 = (uint32_t)d.p0;
+      auto E = [&](int s, uint32_t p) { return d.W[s] * p * p - d.WP2[s] * p + d.WPP[s]; };
+      uint32_t e = d.e0 + E(1, p1);
+      if (e + d.rem[2] >= d.best_err) return false;
+      e += E(2, (p0 * 2 + p1) / 3);
+      if (e + d.rem[3] >= d.best_err) return false;
+      e += E(3, (p0 + p1 * 2) / 3);
+      if (e >= d.best_err) return false;
+      int h[3] = {d.base[0], d.base[1], d.base[2]};
+      h[d.comp] = c1;
+      lo = d.packed_lo;
+      hi = pack565(h[0], h[1], h[2]);
+      return true;
+    }
   }
+}
 
-  // compute_endpoint_component_errors :369-413, kept as closed-form quadratics
-  struct CompErr {
-    uint32_t W[4], WP2[4], WPP[4], rem[4];
-    __device__ __forceinline__ uint32_t E(int s, uint32_t p) const { return W[s] * p * p - WP2[s] * p + WPP[s]; }
-  };
-  __device__ void comp_errors(int comp, CompErr& ce) {
-    const Best& s = sel_source();
-    int sel = -1;
-    uint32_t p = 0, w = 0;
-    if ((int)lane < n) {
-      sel = selector_of(lane, s);
-      p = (S.uci[lane] >> (8 * comp)) & 255;
-      w = (uint32_t)S.ucw[lane];
+// Runs the list described by S.d from position `start` with the reference's sequential
+// semantics; see the file comment. Returns, for stop_on_accept lists, the position of the
+// first accepted candidate (or -1); otherwise 1 if anything was accepted, else 0.
+__device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
+  const ListDesc& d = S.d;
+  const uint32_t lane = lane_id();
+  const int n = S.st.n;
+  const bool three = S.st.three != 0;
+  const float wr = S.st.wr, wg = S.st.wg;
+  bool any = false;
+  int i0 = start;
+  while (i0 < d.count) {
+    const int i = i0 + (int)lane;
+    uint32_t lo = 0, hi = 0;
+    bool valid = i < d.count && gen_candidate(S, d, i, lo, hi);
+    const uint32_t lb = valid ? lower_bound(S, lo, hi) : kInf;
+    const uint32_t B0 = S.st.best.err;
+    bool live = valid && lb < B0;
+    const uint32_t key = lo | (hi << 16);
+    if (!d.alt) {
+      // a repeated candidate can never win: keep the first copy in the batch, drop keys tried before
+      const unsigned same = __match_any_sync(FULL_MASK, key);
+      const unsigned live_mask = __ballot_sync(FULL_MASK, live);
+      const unsigned grp = same & live_mask;
+      live = live && (int)lane == __ffs(grp) - 1;
+      live = live && !hset_find(S, key);
     }
-    for (int k = 0; k < 4; k++) {
-      ce.W[k] = __reduce_add_sync(FULL_MASK, sel == k ? w : 0u);
-      ce.WP2[k] = __reduce_add_sync(FULL_MASK, sel == k ? w * p * 2 : 0u);
-      ce.WPP[k] = __reduce_add_sync(FULL_MASK, sel == k ? w * p * p : 0u);
-    }
-    const int limit = comp == 1 ? 64 : 32;
-    for (int k = 0; k < 2; k++) {
-      uint32_t m = kInf;
-      for (int c = lane; c < limit; c += 32) {
-        const uint32_t pv = comp == 1 ? exp6(c) : exp5(c);
-        m = min(m, ce.E(k, pv));
-      }
-      ce.rem[k] = __reduce_min_sync(FULL_MASK, m);
-    }
-    for (int k = 2; k < 4; k++) {
-      uint32_t m = kInf;
-      for (int v = lane; v < 256; v += 32) m = min(m, ce.E(k, (uint32_t)v));
-      ce.rem[k] = __reduce_min_sync(FULL_MASK, m);
-    }
-    for (int k = 3; k > 0; k--) ce.rem[k - 1] += ce.rem[k];
-  }
-
-  // optimize_endpoint_comps :415-486
-  __device__ void optimize_comps() {
-    compute_selectors();
-    if (best.alpha || !best.err) return;
-    const int src_lo[3] = {exp5(best.lo >> 11), exp6((best.lo >> 5) & 63), exp5(best.lo & 31)};
-    const int src_hi[3] = {exp5(best.hi >> 11), exp6((best.hi >> 5) & 63), exp5(best.hi & 31)};
-    CompErr ce;
-    for (int comp = 0; comp < 3; comp++) {
-      const int p0s = src_lo[comp], p1s = src_hi[comp];
-      int lo_u[3] = {(int)(best.lo >> 11), (int)((best.lo >> 5) & 63), (int)(best.lo & 31)};
-      int hi_u[3] = {(int)(best.hi >> 11), (int)((best.hi >> 5) & 63), (int)(best.hi & 31)};
-      comp_errors(comp, ce);
-      const int limit = comp == 1 ? 64 : 32;
-      auto ex = [&](int c) { return (uint32_t)(comp == 1 ? exp6(c) : exp5(c)); };
-      uint32_t best_err = ce.E(0, ex(lo_u[comp])) + ce.E(1, ex(hi_u[comp])) + ce.E(2, (uint32_t)((p0s * 2 + p1s) / 3)) +
-                          ce.E(3, (uint32_t)((p0s + p1s * 2) / 3));
-      if (ce.rem[0] >= best_err) continue;
-      for (int c0 = 0; c0 < limit; c0++) {
-        uint32_t e0 = ce.E(0, ex(c0));
-        if (e0 + ce.rem[1] >= best_err) continue;
-        lo_u[comp] = c0;
-        const uint32_t packed_lo = pack565(lo_u[0], lo_u[1], lo_u[2]);
-        const int p0 = (int)ex(c0);
-        int start = 0;
-        while (start < limit) {
-          const int c1 = start + (int)lane;
-          bool pass = c1 < limit;
-          uint32_t lo = 0, hi = 0;
-          if (pass) {
-            uint32_t e = e0 + ce.E(1, ex(c1));
-            pass = e + ce.rem[2] < best_err;
-            const int p1 = (int)ex(c1);
-            e += ce.E(2, (uint32_t)((p0 * 2 + p1) / 3));
-            pass = pass && e + ce.rem[3] < best_err;
-            e += ce.E(3, (uint32_t)((p0 + p1 * 2) / 3));
-            pass = pass && e < best_err;
-            int h[3] = {hi_u[0], hi_u[1], hi_u[2]};
-            h[comp] = c1;
-            lo = packed_lo;
-            hi = pack565(h[0], h[1], h[2]);
-          }
-          const uint32_t lb = pass ? lower_bound(lo, hi) : kInf;
-          const bool live = pass && lb < best.err;
-          uint32_t err = kInf;
-          int type = 0;
-          if (live) eval(lo, hi, 0, err, type);
-          const unsigned ok = __ballot_sync(FULL_MASK, live && err < best.err);
-          if (!ok) { start += 32; continue; }
-          const int j = __ffs(ok) - 1;
-          accept(__shfl_sync(FULL_MASK, lo, j), __shfl_sync(FULL_MASK, hi, j), __shfl_sync(FULL_MASK, err, j),
-                 __shfl_sync(FULL_MASK, type, j), 0);
-          if (!best.err) return;
-          compute_selectors();
-          comp_errors(comp, ce);
-          const int c1j = start + j;
-          const int p1 = (int)ex(c1j);
-          best_err = ce.E(0, ex(c0)) + ce.E(1, ex(c1j)) + ce.E(2, (uint32_t)((p0 * 2 + p1) / 3)) +
-                     ce.E(3, (uint32_t)((p0 + p1 * 2) / 3));
-          e0 = ce.E(0, ex(c0));
-          if (e0 + ce.rem[1] >= best_err) break;
-          start = c1j + 1;
+    // evaluate every lane's candidate (uber: 4- and 3-colour; hc: 4-colour), stopping early once
+    // no live lane can still beat the running best
+    uint32_t e0 = 0, e1 = 0;
+    {
+      const int a = d.alt;
+      const int r0 = exp5(lo >> 11), g0 = exp6((lo >> 5) & 63), b0 = exp5(lo & 31);
+      const int r1 = exp5(hi >> 11), g1 = exp6((hi >> 5) & 63), b1 = exp5(hi & 31);
+      const float4 q0 = entry(wr, wg, r0, g0, b0), q1 = entry(wr, wg, r1, g1, b1);
+      const float4 q2 = entry(wr, wg, (r0 * 2 + r1 + a) / 3, (g0 * 2 + g1 + a) / 3, (b0 * 2 + b1 + a) / 3);
+      const float4 q3 = entry(wr, wg, (r1 * 2 + r0 + a) / 3, (g1 * 2 + g0 + a) / 3, (b1 * 2 + b0 + a) / 3);
+      const float4 q4 = entry(wr, wg, (r0 + r1 + a) >> 1, (g0 + g1 + a) >> 1, (b0 + b1 + a) >> 1);
+      if (__any_sync(FULL_MASK, live)) {
+        int k = 0;
+        for (; k < n; k++) {
+          const float4 x = S.ucf[k];
+          const uint32_t w = (uint32_t)S.ucw[k];
+          const float m01 = fminf(dist_part(x, q0), dist_part(x, q1));
+          e0 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, fminf(dist_part(x, q2), dist_part(x, q3)))));
+          if (three) e1 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, dist_part(x, q4))));
+          if ((k & 3) == 3 && __all_sync(FULL_MASK, !live || (three ? min(e0, e1) : e0) >= B0)) { k++; break; }
         }
+        if (live) work += (uint32_t)k;
       }
     }
-  }
-
-  // try_combinatorial_encoding :1886-1997 (2..4 unique colours: endpoints of a block that was
-  // already DXT-compressed may be recovered by extrapolation)
-  __device__ void try_combinatorial() {
-    if (n < 2 || n > 4) return;
-    int m = 0;
-    if (lane == 0) {
-      int tr[48], tg[48], tb[48];
-      int cnt = 0;
-      for (int i = 0; i < n; i++) {
-        const uint32_t c = S.uci[i];
-        tr[cnt] = c & 255; tg[cnt] = (c >> 8) & 255; tb[cnt] = c >> 16; cnt++;
-      }
-      auto push = [&](int a, int b, float f, int rounding) {
-        const float r = rounding ? 1.0f : 0.0f;
-        auto one = [&](int x, int y) {
-          const float fx = (float)x, fy = (float)y;
-          const float l = __fadd_rn(fx, __fmul_rn(__fsub_rn(fy, fx), f));
-          return clampi(__float2int_rz(__fadd_rn(r, l)), 0, 255);
-        };
-        const int nr = one(tr[a], tr[b]), ng = one(tg[a], tg[b]), nb = one(tb[a], tb[b]);
-        tr[cnt] = nr; tg[cnt] = ng; tb[cnt] = nb; cnt++;
-      };
-      if (n == 2) {
-        const float fs[10] = {2.0f, 3.0f, .5f, 1.5f, -1.0f, 2.0f, -.5f, .5f, -2.0f, -1.0f};
-        for (int k = 0; k < 2; k++)
-          for (int qq = 0; qq < 2; qq++)
-            for (int f = 0; f < 10; f++) push(qq, qq ^ 1, fs[f], k);
-      } else if (n == 3) {
-        for (int i = 0; i <= 2; i++)
-          for (int j = 0; j <= 2; j++) {
-            if (i == j) continue;
-            push(i, j, 1.5f, 1);
-            push(i, j, 2.0f / 3.0f, 1);
-            push(i, j, 1.0f / 3.0f, 1);
-            push(i, j, -.5f, 1);
-          }
-      }
-      for (int i = 0; i < cnt; i++) {
-        const uint32_t ur = min(((uint32_t)tr[i] * 31u + 127u) / 255u, 31u);
-        const uint32_t ug = min(((uint32_t)tg[i] * 63u + 127u) / 255u, 63u);
-        const uint32_t ub = min(((uint32_t)tb[i] * 31u + 127u) / 255u, 31u);
-        const uint16_t pk = (uint16_t)(ub | (ug << 5) | (ur << 11));
-        bool dup = false;
-        for (int k = 0; k < m; k++) if (S.list[k] == pk) { dup = true; break; }
-        if (!dup) S.list[m++] = pk;
-      }
+    const uint32_t err = (three && e1 < e0) ? e1 : e0;
+    const int type = (three && e1 < e0) ? 1 : 0;
+    // resolve the sequential outcome of the batch
+    unsigned ok = __ballot_sync(FULL_MASK, live && err < B0);
+    int last = -1, cut = 31;
+    while (ok) {
+      const int j = __ffs(ok) - 1;
+      accept(S, __shfl_sync(FULL_MASK, lo, j), __shfl_sync(FULL_MASK, hi, j), __shfl_sync(FULL_MASK, err, j),
+             __shfl_sync(FULL_MASK, type, j), d.alt);
+      any = true;
+      last = j;
+      if (d.dependent) { cut = j; break; }
+      const uint32_t B = S.st.best.err;
+      const unsigned after = j == 31 ? 0u : (FULL_MASK << (j + 1));
+      ok = __ballot_sync(FULL_MASK, live && lb < B && err < B) & after;
     }
-    m = __shfl_sync(FULL_MASK, m, 0);
+    // lanes past an accepted candidate of a dependent list were generated from a stale best:
+    // only candidates up to the cut count as tried
+    if (!d.alt && live && (int)lane <= cut) hset_insert(S, key);
     __syncwarp();
-    for (int i = 0; best.err && i + 1 < m; i++)
-      run_list(m - 1 - i, false, 0, [&](int k, uint32_t& lo, uint32_t& hi) {
-        lo = S.list[i]; hi = S.list[i + 1 + k]; return true;
-      });
-    const uint32_t saved = best.err;
-    if (saved) best.err = 1;
-    for (int i = 0; best.err && i + 1 < m; i++)
-      run_list(m - 1 - i, false, 1, [&](int k, uint32_t& lo, uint32_t& hi) {
-        lo = S.list[i]; hi = S.list[i + 1 + k]; return true;
-      });
-    if (best.err) best.err = saved;
-  }
-
-  // optimize_endpoints :703-1067 from the phase-1 projection bounds
-  __device__ void optimize(const float* axis, const float* low0, const float* high0, const uint32_t* med) {
-    // try_median4: the six LBG pairs, then refine(1)
-    run_list(6, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) { lo = med[i] & 0xFFFF; hi = med[i] >> 16; return true; });
-    refine();
-    float sa1[3];
-    for (int k = 0; k < 3; k++) sa1[k] = __fmul_rn(axis[k], .015625f);
-    sa1[0] = __fmul_rn(sa1[0], 31.0f); sa1[1] = __fmul_rn(sa1[1], 63.0f); sa1[2] = __fmul_rn(sa1[2], 31.0f);
-    float low[3], high[3];
-    const float lim[3] = {31.0f, 63.0f, 31.0f};
-    for (int k = 0; k < 3; k++) {
-      const float l = __fmul_rn(low0[k], lim[k]), h = __fmul_rn(high0[k], lim[k]);
-      low[k] = l < 0.0f ? 0.0f : (l > lim[k] ? lim[k] : l);
-      high[k] = h < 0.0f ? 0.0f : (h > lim[k] ? lim[k] : h);
+    if (d.dependent && last >= 0) {
+      if (d.stop_on_accept) return i0 + last;
+      i0 += last + 1;
+    } else {
+      i0 += 32;
     }
-    for (int pass = 0; pass < 4; pass++) {
-      if (pass) {
-        low[0] = (float)(best.lo >> 11); low[1] = (float)((best.lo >> 5) & 63); low[2] = (float)(best.lo & 31);
-        high[0] = (float)(best.hi >> 11); high[1] = (float)((best.hi >> 5) & 63); high[2] = (float)(best.hi & 31);
+  }
+  return d.stop_on_accept ? -1 : (any ? 1 : 0);
+}
+
+__device__ __forceinline__ void set_list(WarpShared& S, int kind, int count, int dependent, int alt) {
+  if (lane_id() == 0) {
+    S.d.kind = kind; S.d.count = count; S.d.dependent = dependent; S.d.alt = alt; S.d.stop_on_accept = 0;
+  }
+}
+
+// refine_solution(1) :525-698: least-squares endpoints from the current selectors, then the
+// 2 x 27 lattice neighbours of the two fitted endpoints.
+__device__ bool refine(WarpShared& S, uint32_t& work) {
+  compute_selectors(S);
+  const uint32_t lane = lane_id();
+  const int n = S.st.n;
+  int a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // ak0 ak1 ak2 at1r at1g at1b at2r at2g at2b
+  if ((int)lane < n) {
+    const int step = selector_of(S, lane, sel_source(S)) ^ 1;
+    const int w = S.ucw[lane];
+    const uint32_t c = S.uci[lane];
+    const int r = (c & 255) * w, g = ((c >> 8) & 255) * w, b = (c >> 16) * w;
+    const int w1 = step == 0 ? 3 : step == 1 ? 0 : step == 2 ? 2 : 1;
+    const int p0 = step >= 2 ? 2 : 0;
+    const int p1 = step == 0 ? 0 : step == 1 ? 9 : step == 2 ? 1 : 4;
+    const int p2 = step == 0 ? 9 : step == 1 ? 0 : step == 2 ? 4 : 1;
+    a[0] = p0 * w; a[1] = p1 * w; a[2] = p2 * w;
+    a[3] = w1 * r; a[4] = w1 * g; a[5] = w1 * b;
+    a[6] = r; a[7] = g; a[8] = b;
+  }
+  for (int k = 0; k < 9; k++) a[k] = __reduce_add_sync(FULL_MASK, a[k]);
+  const long long xx = a[2], yy = a[1], xy = a[0];
+  const long long t = xx * yy - xy * xy;
+  if (!yy || !xx || t == 0) return false;
+  int comp = 0;
+  if (lane < 6) {  // the six fitted components, one per lane, in double exactly as the reference
+    const int k = lane % 3;
+    const long long at1 = a[3 + k], at2 = 3LL * a[6 + k] - a[3 + k];
+    const double frb = __ddiv_rn((double)__fdiv_rn(93.0f, 255.0f), (double)t);
+    const double f = k == 1 ? __dmul_rn(frb, (double)__fdiv_rn(63.0f, 31.0f)) : frb;
+    const long long num = lane < 3 ? at1 * yy - at2 * xy : at2 * xx - at1 * xy;
+    const double v = __dadd_rn(__dmul_rn((double)num, f), (double)0.5f);
+    comp = clampi(__double2int_rz(v), 0, k == 1 ? 63 : 31);
+  }
+  const int mine = comp;
+  for (int k = 0; k < 6; k++) {
+    const int v = __shfl_sync(FULL_MASK, mine, k);
+    if (lane == 0) S.d.e[k] = v;
+  }
+  set_list(S, LK_REFINE, 54, 0, 0);
+  __syncwarp();
+  return run_list(S, 0, work) != 0;
+}
+
+__device__ bool all_selectors_equal(const WarpShared& S) {
+  const uint32_t lane = lane_id();
+  const int n = S.st.n;
+  const int mine = (int)lane < n ? selector_of(S, lane, sel_source(S)) : -1;
+  const int first = __shfl_sync(FULL_MASK, mine, 0);
+  return __all_sync(FULL_MASK, (int)lane >= n || mine == first);
+}
+
+__device__ __forceinline__ uint32_t solid_coords(int r, int g, int b, bool three) {
+  const uint32_t lo = three ? pack565(c_sct.m5_3[r][0], c_sct.m6_3[g][0], c_sct.m5_3[b][0])
+                            : pack565(c_sct.m5[r][0], c_sct.m6[g][0], c_sct.m5[b][0]);
+  const uint32_t hi = three ? pack565(c_sct.m5_3[r][1], c_sct.m6_3[g][1], c_sct.m5_3[b][1])
+                            : pack565(c_sct.m5[r][1], c_sct.m6[g][1], c_sct.m5[b][1]);
+  return lo | (hi << 16);
+}
+
+// try_average_block_as_solid :93-153
+__device__ bool try_solid(WarpShared& S, uint32_t& work) {
+  const uint32_t lane = lane_id();
+  const int n = S.st.n;
+  int tr = 0, tg = 0, tb = 0;
+  if ((int)lane < n) {
+    const uint32_t c = S.uci[lane];
+    const int w = S.ucw[lane];
+    tr = (c & 255) * w; tg = ((c >> 8) & 255) * w; tb = (c >> 16) * w;
+  }
+  tr = __reduce_add_sync(FULL_MASK, tr);
+  tg = __reduce_add_sync(FULL_MASK, tg);
+  tb = __reduce_add_sync(FULL_MASK, tb);
+  const int ar = (tr + 8) / 16, ag = (tg + 8) / 16, ab = (tb + 8) / 16;
+  const bool three = S.st.three != 0;
+  if (lane == 0) {
+    int cnt = 0;
+    S.cand[cnt++] = solid_coords(ar, ag, ab, false);
+    if (three) S.cand[cnt++] = solid_coords(ar, ag, ab, true);
+    for (int i = 0; i < n; i++) {
+      const uint32_t c = S.uci[i];
+      const int r = c & 255, g = (c >> 8) & 255, b = c >> 16;
+      if (r == ar && g == ag && b == ab) continue;
+      S.cand[cnt++] = solid_coords(r, g, b, false);
+      if (three) S.cand[cnt++] = solid_coords(r, g, b, true);
+    }
+    S.d.count = cnt;
+  }
+  __syncwarp();
+  set_list(S, LK_TABLE, S.d.count, 0, 0);
+  __syncwarp();
+  return run_list(S, 0, work) != 0;
+}
+
+// compute_endpoint_component_errors :369-413 as closed-form quadratics; fills S.d.W/WP2/WPP/rem
+__device__ void comp_errors(WarpShared& S, int comp) {
+  const uint32_t lane = lane_id();
+  const int n = S.st.n;
+  int sel = -1;
+  uint32_t p = 0, w = 0;
+  if ((int)lane < n) {
+    sel = selector_of(S, lane, sel_source(S));
+    p = (S.uci[lane] >> (8 * comp)) & 255;
+    w = (uint32_t)S.ucw[lane];
+  }
+  uint32_t W[4], WP2[4], WPP[4], rem[4];
+  for (int k = 0; k < 4; k++) {
+    W[k] = __reduce_add_sync(FULL_MASK, sel == k ? w : 0u);
+    WP2[k] = __reduce_add_sync(FULL_MASK, sel == k ? w * p * 2 : 0u);
+    WPP[k] = __reduce_add_sync(FULL_MASK, sel == k ? w * p * p : 0u);
+  }
+  const int limit = comp == 1 ? 64 : 32;
+  for (int k = 0; k < 4; k++) {
+    uint32_t m = kInf;
+    if (k < 2) {
+      for (int c = lane; c < limit; c += 32) {
+        const uint32_t pv = (uint32_t)(comp == 1 ? exp6(c) : exp5(c));
+        m = min(m, W[k] * pv * pv - WP2[k] * pv + WPP[k]);
       }
-      const uint32_t prev = best.err;
-      if (!prev) break;
-      // sweep both endpoints along the axis (the 15-entry uber probe table, both directions)
-      int nl, nh;
-      {
-        const int k = (int)lane;
-        const int i = (k + 1) >> 1, s = (k + 1) & 1;
-        const float x = (float)c_uber_probe[i < 15 ? i : 14];
-        auto probe = [&](const float* base) {
-          int v[3];
-          for (int c = 0; c < 3; c++) {
-            const float step = s ? sa1[c] : -sa1[c];
-            const float pv = __fadd_rn(__fadd_rn(base[c], .5f), __fmul_rn(step, x));
-            v[c] = clampi((int)floorf(pv), 0, c == 1 ? 63 : 31);
-          }
-          return pack565(v[0], v[1], v[2]);
-        };
-        const uint32_t pl = probe(low), ph = probe(high);
-        const uint32_t pl2 = __shfl_up_sync(FULL_MASK, pl, 2), ph2 = __shfl_up_sync(FULL_MASK, ph, 2);
-        const bool in = k < 29;
-        const bool rl = in && (k < 2 || pl != pl2), rh = in && (k < 2 || ph != ph2);
-        const unsigned ml = __ballot_sync(FULL_MASK, rl), mh = __ballot_sync(FULL_MASK, rh);
-        const unsigned below = (1u << lane) - 1u;
-        if (rl) S.list[__popc(ml & below)] = (uint16_t)pl;
-        if (rh) S.list2[__popc(mh & below)] = (uint16_t)ph;
-        nl = __popc(ml);
-        nh = __popc(mh);
-        __syncwarp();
+    } else {
+      for (uint32_t v = lane; v < 256; v += 32) m = min(m, W[k] * v * v - WP2[k] * v + WPP[k]);
+    }
+    rem[k] = __reduce_min_sync(FULL_MASK, m);
+  }
+  for (int k = 3; k > 0; k--) rem[k - 1] += rem[k];
+  if (lane == 0) {
+    for (int k = 0; k < 4; k++) { S.d.W[k] = W[k]; S.d.WP2[k] = WP2[k]; S.d.WPP[k] = WPP[k]; S.d.rem[k] = rem[k]; }
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ uint32_t comp_E(const ListDesc& d, int s, uint32_t p) {
+  return d.W[s] * p * p - d.WP2[s] * p + d.WPP[s];
+}
+
+// optimize_endpoint_comps :415-486
+__device__ void optimize_comps(WarpShared& S, uint32_t& work) {
+  compute_selectors(S);
+  if (S.st.best.alpha || !S.st.best.err) return;
+  const uint32_t blo = S.st.best.lo, bhi = S.st.best.hi;
+  const int src_lo[3] = {exp5(blo >> 11), exp6((blo >> 5) & 63), exp5(blo & 31)};
+  const int src_hi[3] = {exp5(bhi >> 11), exp6((bhi >> 5) & 63), exp5(bhi & 31)};
+  const uint32_t lane = lane_id();
+  for (int comp = 0; comp < 3; comp++) {
+    const int p0s = src_lo[comp], p1s = src_hi[comp];
+    const uint32_t clo = S.st.best.lo, chi = S.st.best.hi;
+    int lo_u[3] = {(int)(clo >> 11), (int)((clo >> 5) & 63), (int)(clo & 31)};
+    const int hi_u[3] = {(int)(chi >> 11), (int)((chi >> 5) & 63), (int)(chi & 31)};
+    comp_errors(S, comp);
+    const int limit = comp == 1 ? 64 : 32;
+    auto ex = [&](int c) { return (uint32_t)(comp == 1 ? exp6(c) : exp5(c)); };
+    uint32_t best_err = comp_E(S.d, 0, ex(lo_u[comp])) + comp_E(S.d, 1, ex(hi_u[comp])) +
+                        comp_E(S.d, 2, (uint32_t)((p0s * 2 + p1s) / 3)) + comp_E(S.d, 3, (uint32_t)((p0s + p1s * 2) / 3));
+    if (S.d.rem[0] >= best_err) continue;
+    for (int c0 = 0; c0 < limit; c0++) {
+      uint32_t e0 = comp_E(S.d, 0, ex(c0));
+      if (e0 + S.d.rem[1] >= best_err) continue;
+      lo_u[comp] = c0;
+      if (lane == 0) {
+        S.d.kind = LK_COMPS; S.d.count = limit; S.d.dependent = 1; S.d.alt = 0; S.d.stop_on_accept = 1;
+        S.d.comp = comp; S.d.p0 = (int)ex(c0); S.d.e0 = e0; S.d.best_err = best_err;
+        S.d.packed_lo = pack565(lo_u[0], lo_u[1], lo_u[2]);
+        S.d.base[0] = hi_u[0]; S.d.base[1] = hi_u[1]; S.d.base[2] = hi_u[2];
       }
-      run_list(nl * nh, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
-        const int a = i / nh, b = i - a * nh;
-        const uint32_t p0 = S.list[a], p1 = S.list2[b];
-        lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
-        return true;
-      });
       __syncwarp();
-      // lattice neighbours of the low endpoint: 26 adjacent cells, then +-2 on each axis
-      for (int side = 0; side < 2; side++) {
-        const uint32_t base = side ? best.hi : best.lo;
-        const int bc[3] = {(int)(base >> 11), (int)((base >> 5) & 63), (int)(base & 31)};
-        run_list(26, true, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
-          // g_adjacency order: x fastest, then y, then z, skipping the centre
-          const int idx = i < 13 ? i : i + 1;
-          const int dx = idx % 3 - 1, dy = (idx / 3) % 3 - 1, dz = idx / 9 - 1;
-          const int r = bc[0] + dx, g = bc[1] + dy, b = bc[2] + dz;
-          if (r < 0 || r > 31 || g < 0 || g > 63 || b < 0 || b > 31) return false;
-          const uint32_t moved = pack565(r, g, b);
-          const uint32_t p0 = side ? best.lo : moved, p1 = side ? moved : best.hi;
-          lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
-          return true;
-        });
-        const uint32_t base2 = side ? best.hi : best.lo;
-        const int bc2[3] = {(int)(base2 >> 11), (int)((base2 >> 5) & 63), (int)(base2 & 31)};
-        run_list(6, true, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
-          const int a = i >> 1, s = (i & 1) ? 2 : -2;
-          int c[3] = {bc2[0], bc2[1], bc2[2]};
-          const int q = c[a] + s;
-          if (q < 0 || q > (a == 1 ? 63 : 31)) return false;
-          c[a] = q;
-          const uint32_t moved = pack565(c[0], c[1], c[2]);
-          const uint32_t p0 = side ? best.lo : moved, p1 = side ? moved : best.hi;
-          lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
-          return true;
-        });
+      int start = 0;
+      while (start < limit) {
+        const int c1 = run_list(S, start, work);
+        if (c1 < 0) break;
+        if (!S.st.best.err) return;
+        compute_selectors(S);
+        comp_errors(S, comp);
+        const uint32_t p0 = (uint32_t)S.d.p0, p1 = ex(c1);
+        best_err = comp_E(S.d, 0, ex(c0)) + comp_E(S.d, 1, p1) + comp_E(S.d, 2, (p0 * 2 + p1) / 3) +
+                   comp_E(S.d, 3, (p0 + p1 * 2) / 3);
+        e0 = comp_E(S.d, 0, ex(c0));
+        if (lane == 0) { S.d.e0 = e0; S.d.best_err = best_err; }
+        __syncwarp();
+        if (e0 + S.d.rem[1] >= best_err) break;
+        start = c1 + 1;
       }
-      if (!best.err || (pass && best.err == prev)) break;
-      refine();
     }
-    if (best.err) {
-      bool solid = false;
-      if (all_selectors_equal()) solid = try_solid();
-      if (!solid) optimize_comps();
-    }
-    if (best.err) try_combinatorial();
   }
-};
+}
 
-// Plane tables -> per-channel lower bounds (compute_internal :2133-2203), lane c handles
-// planes c (and c+32 for green).
+// try_combinatorial_encoding :1886-1997: blocks of 2..4 colours that were DXT-compressed
+// before may have their original endpoints recovered by extrapolation.
+__device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
+  const int n = S.st.n;
+  if (n < 2 || n > 4) return;
+  const uint32_t lane = lane_id();
+  if (lane == 0) {
+    // temporary colours (r | g << 8 | b << 16) in S.cand, unique packed endpoints in S.list
+    int cnt = 0;
+    for (int i = 0; i < n; i++) S.cand[cnt++] = S.uci[i];
+    auto push = [&](int a, int b, float f, int rounding) {
+      const float r = rounding ? 1.0f : 0.0f;
+      uint32_t out = 0;
+      for (int ch = 0; ch < 3; ch++) {
+        const float fx = (float)((S.cand[a] >> (8 * ch)) & 255), fy = (float)((S.cand[b] >> (8 * ch)) & 255);
+        const float l = __fadd_rn(fx, __fmul_rn(__fsub_rn(fy, fx), f));
+        out |= (uint32_t)clampi(__float2int_rz(__fadd_rn(r, l)), 0, 255) << (8 * ch);
+      }
+      S.cand[cnt++] = out;
+    };
+    if (n == 2) {
+      const float fs[10] = {2.0f, 3.0f, .5f, 1.5f, -1.0f, 2.0f, -.5f, .5f, -2.0f, -1.0f};
+      for (int k = 0; k < 2; k++)
+        for (int q = 0; q < 2; q++)
+          for (int f = 0; f < 10; f++) push(q, q ^ 1, fs[f], k);
+    } else if (n == 3) {
+      for (int i = 0; i <= 2; i++)
+        for (int j = 0; j <= 2; j++) {
+          if (i == j) continue;
+          push(i, j, 1.5f, 1);
+          push(i, j, 2.0f / 3.0f, 1);
+          push(i, j, 1.0f / 3.0f, 1);
+          push(i, j, -.5f, 1);
+        }
+    }
+    int m = 0;
+    for (int i = 0; i < cnt; i++) {
+      const uint32_t c = S.cand[i];
+      const uint32_t ur = min(((c & 255) * 31u + 127u) / 255u, 31u);
+      const uint32_t ug = min((((c >> 8) & 255) * 63u + 127u) / 255u, 63u);
+      const uint32_t ub = min(((c >> 16) * 31u + 127u) / 255u, 31u);
+      const uint16_t pk = (uint16_t)(ub | (ug << 5) | (ur << 11));
+      bool dup = false;
+      for (int k = 0; k < m; k++) if (S.list[k] == pk) { dup = true; break; }
+      if (!dup) S.list[m++] = pk;
+    }
+    S.d.nh = m;
+  }
+  __syncwarp();
+  const int m = S.d.nh;
+  for (int alt = 0; alt < 2; alt++) {
+    uint32_t saved = 0;
+    if (alt) {
+      saved = S.st.best.err;
+      if (lane == 0 && saved) S.st.best.err = 1;
+      __syncwarp();
+    }
+    for (int i = 0; S.st.best.err && i + 1 < m; i++) {
+      if (lane == 0) {
+        S.d.kind = LK_COMB; S.d.count = m - 1 - i; S.d.dependent = 0; S.d.alt = alt; S.d.stop_on_accept = 0;
+        S.d.row = i;
+      }
+      __syncwarp();
+      run_list(S, 0, work);
+    }
+    if (alt) {
+      if (lane == 0 && S.st.best.err) S.st.best.err = saved;
+      __syncwarp();
+    }
+  }
+}
+
+// optimize_endpoints :703-1067 from the phase-1 projection bounds
+__device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
+  const uint32_t lane = lane_id();
+  // try_median4: the six LBG pairs, then refine(1)
+  if (lane < 6) S.cand[lane] = S.p1m[slot][lane];
+  set_list(S, LK_TABLE, 6, 0, 0);
+  __syncwarp();
+  run_list(S, 0, work);
+  refine(S, work);
+  float sa1[3], low[3], high[3];
+  const float lim[3] = {31.0f, 63.0f, 31.0f};
+  for (int k = 0; k < 3; k++) {
+    sa1[k] = __fmul_rn(S.p1f[slot][k], .015625f);
+    const float l = __fmul_rn(S.p1f[slot][3 + k], lim[k]), h = __fmul_rn(S.p1f[slot][6 + k], lim[k]);
+    low[k] = l < 0.0f ? 0.0f : (l > lim[k] ? lim[k] : l);
+    high[k] = h < 0.0f ? 0.0f : (h > lim[k] ? lim[k] : h);
+  }
+  sa1[0] = __fmul_rn(sa1[0], 31.0f); sa1[1] = __fmul_rn(sa1[1], 63.0f); sa1[2] = __fmul_rn(sa1[2], 31.0f);
+  for (int pass = 0; pass < 4; pass++) {
+    if (pass) {
+      const uint32_t blo = S.st.best.lo, bhi = S.st.best.hi;
+      low[0] = (float)(blo >> 11); low[1] = (float)((blo >> 5) & 63); low[2] = (float)(blo & 31);
+      high[0] = (float)(bhi >> 11); high[1] = (float)((bhi >> 5) & 63); high[2] = (float)(bhi & 31);
+    }
+    const uint32_t prev = S.st.best.err;
+    if (!prev) break;
+    // sweep both endpoints along the axis with the 15-entry uber probe table, both directions;
+    // lane k holds probe (i, s) = ((k+1)/2, (k+1)&1) in the reference's loop order
+    {
+      const int k = (int)lane;
+      const int i = (k + 1) >> 1, s = (k + 1) & 1;
+      const float x = (float)c_uber_probe[i < 15 ? i : 14];
+      uint32_t pl, ph;
+      {
+        int v[3], w[3];
+        for (int c = 0; c < 3; c++) {
+          const float step = s ? sa1[c] : -sa1[c];
+          v[c] = clampi((int)floorf(__fadd_rn(__fadd_rn(low[c], .5f), __fmul_rn(step, x))), 0, c == 1 ? 63 : 31);
+          w[c] = clampi((int)floorf(__fadd_rn(__fadd_rn(high[c], .5f), __fmul_rn(step, x))), 0, c == 1 ? 63 : 31);
+        }
+        pl = pack565(v[0], v[1], v[2]);
+        ph = pack565(w[0], w[1], w[2]);
+      }
+      const uint32_t pl2 = __shfl_up_sync(FULL_MASK, pl, 2), ph2 = __shfl_up_sync(FULL_MASK, ph, 2);
+      const bool in = k < 29;
+      const bool rl = in && (k < 2 || pl != pl2), rh = in && (k < 2 || ph != ph2);
+      const unsigned ml = __ballot_sync(FULL_MASK, rl), mh = __ballot_sync(FULL_MASK, rh);
+      const unsigned below = (1u << lane) - 1u;
+      if (rl) S.list[__popc(ml & below)] = (uint16_t)pl;
+      if (rh) S.list2[__popc(mh & below)] = (uint16_t)ph;
+      if (lane == 0) {
+        S.d.kind = LK_PAIRS; S.d.count = __popc(ml) * __popc(mh); S.d.dependent = 0; S.d.alt = 0;
+        S.d.stop_on_accept = 0; S.d.nh = __popc(mh);
+      }
+      __syncwarp();
+    }
+    run_list(S, 0, work);
+    // lattice neighbours: low endpoint (26 adjacent cells, then +-2 per axis), then high
+    for (int side = 0; side < 2; side++) {
+      for (int kind = LK_NEIGH; kind <= LK_MOVE2; kind++) {
+        if (lane == 0) {
+          const uint32_t base = side ? S.st.best.hi : S.st.best.lo;
+          S.d.base[0] = (int)(base >> 11); S.d.base[1] = (int)((base >> 5) & 63); S.d.base[2] = (int)(base & 31);
+          S.d.kind = kind; S.d.count = kind == LK_NEIGH ? 26 : 6; S.d.dependent = 1; S.d.alt = 0;
+          S.d.stop_on_accept = 0; S.d.side = side;
+        }
+        __syncwarp();
+        run_list(S, 0, work);
+      }
+    }
+    if (!S.st.best.err || (pass && S.st.best.err == prev)) break;
+    refine(S, work);
+  }
+  if (S.st.best.err) {
+    bool solid = false;
+    if (all_selectors_equal(S)) solid = try_solid(S, work);
+    if (!solid) optimize_comps(S, work);
+  }
+  if (S.st.best.err) try_combinatorial(S, work);
+}
+
+// Plane tables -> per-channel lower bounds (compute_internal :2133-2203); lane c handles
+// planes c (and c + 32 for green).
 __device__ void build_lower_bounds(WarpShared& S, int n, bool perceptual) {
   const int c = (int)lane_id();
   uint32_t rw = 0, r1 = 0, r2 = 0, gw = 0, g1 = 0, g2 = 0, gw2 = 0, g12 = 0, g22 = 0, bw = 0, b1 = 0, b2 = 0;
@@ -927,12 +1041,11 @@ __device__ void build_lower_bounds(WarpShared& S, int n, bool perceptual) {
   }
 }
 
-template <bool HC>
-__device__ void phase2_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, bool perceptual,
-                             bool use_alpha, uint8_t* __restrict__ out, uint64_t* __restrict__ err_out) {
+__device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, bool perceptual,
+                                 bool hc, bool use_alpha, uint8_t* __restrict__ out, uint64_t* __restrict__ err_out) {
   const uint32_t lane = lane_id();
   // unique colours in first-occurrence order via match_any (lanes >= 16 carry sentinels)
-  uint32_t pixel = lane < 16 ? __ldg(reinterpret_cast<const uint32_t*>(px) + lane) : 0;
+  const uint32_t pixel = lane < 16 ? __ldg(reinterpret_cast<const uint32_t*>(px) + lane) : 0;
   const uint32_t key = lane < 16 ? (pixel & 0xFFFFFFu) : (0x80000000u | lane);
   const unsigned match = __match_any_sync(FULL_MASK, key);
   const int leader = __ffs(match) - 1;
@@ -942,63 +1055,62 @@ __device__ void phase2_block(WarpShared& S, int slot, const uint8_t* __restrict_
   const int uidx = __popc(lmask & ((1u << leader) - 1u));
   const float wr = perceptual ? 8.f : 1.f, wg = perceptual ? 25.f : 1.f;
   if (is_leader) {
-    const uint32_t c = key;
-    const float r = (float)(c & 255), g = (float)((c >> 8) & 255), b = (float)(c >> 16);
+    const float r = (float)(key & 255), g = (float)((key >> 8) & 255), b = (float)(key >> 16);
     S.ucf[uidx] = make_float4(r, g, b, wr * r * r + wg * g * g + b * b);
     S.ucw[uidx] = __popc(match);
-    S.uci[uidx] = c;
+    S.uci[uidx] = key;
+  }
+  // clear the tried-set
+  for (int k = lane; k < kHashSize / 4; k += 32) reinterpret_cast<uint4*>(S.hset)[k] = make_uint4(kInf, kInf, kInf, kInf);
+  if (lane == 0) {
+    Sol z;
+    z.lo = z.hi = 0; z.err = kInf; z.alpha = 0; z.alt = 0; z.enforce = 0; z.enforced = 0;
+    S.st.best = z; S.st.snap = z;
+    S.st.n = n; S.st.hc = hc ? 1 : 0; S.st.three = (!hc && use_alpha) ? 1 : 0; S.st.wr = wr; S.st.wg = wg;
   }
   __syncwarp();
   build_lower_bounds(S, n, perceptual);
   __syncwarp();
-  Search<HC> srch(S, n, perceptual, use_alpha);
+  uint32_t work = 0;
   if (n == 1) {
     const uint32_t c = S.uci[0];
     const int r = c & 255, g = (c >> 8) & 255, b = c >> 16;
-    srch.run_list(use_alpha ? 2 : 1, false, 0, [&](int i, uint32_t& lo, uint32_t& hi) {
-      if (i == 0) {
-        lo = pack565(c_sct.m5[r][0], c_sct.m6[g][0], c_sct.m5[b][0]);
-        hi = pack565(c_sct.m5[r][1], c_sct.m6[g][1], c_sct.m5[b][1]);
-      } else {
-        lo = pack565(c_sct.m5_3[r][0], c_sct.m6_3[g][0], c_sct.m5_3[b][0]);
-        hi = pack565(c_sct.m5_3[r][1], c_sct.m6_3[g][1], c_sct.m5_3[b][1]);
-      }
-      return true;
-    });
+    if (lane == 0) { S.cand[0] = solid_coords(r, g, b, false); S.cand[1] = solid_coords(r, g, b, true); }
+    set_list(S, LK_TABLE, use_alpha ? 2 : 1, 0, 0);
+    __syncwarp();
+    run_list(S, 0, work);
   } else {
-    float axis[3], low[3], high[3];
-    for (int k = 0; k < 3; k++) { axis[k] = S.p1f[slot][k]; low[k] = S.p1f[slot][3 + k]; high[k] = S.p1f[slot][6 + k]; }
-    uint32_t med[6];
-    for (int k = 0; k < 6; k++) med[k] = S.p1m[slot][k];
-    srch.optimize(axis, low, high, med);
+    optimize(S, slot, work);
   }
   // return_solution :263-365
-  srch.compute_selectors();
-  const Best& b = srch.sel_source();
-  const int my_sel = (int)lane < n ? srch.selector_of(lane, b) : 0;
+  compute_selectors(S);
+  const Sol best = S.st.best;
+  const int my_sel = (int)lane < n ? selector_of(S, lane, sel_source(S)) : 0;
   const int s = __shfl_sync(FULL_MASK, my_sel, lane < 16 ? uidx : 0);
-  const bool invert = srch.best.alpha ? srch.best.lo > srch.best.hi : srch.best.lo < srch.best.hi;
+  const bool invert = best.alpha ? best.lo > best.hi : best.lo < best.hi;
   int sel = s;
-  if (invert) sel = srch.best.alpha ? (s < 2 ? (s ^ 1) : s) : (s ^ 1);
+  if (invert) sel = best.alpha ? (s < 2 ? (s ^ 1) : s) : (s ^ 1);
   const uint32_t bits = __reduce_or_sync(FULL_MASK, lane < 16 ? ((uint32_t)sel << (2 * lane)) : 0u);
   if (lane == 0) {
-    const uint32_t lo = invert ? srch.best.hi : srch.best.lo, hi = invert ? srch.best.lo : srch.best.hi;
-    uint2 w = make_uint2(lo | (hi << 16), bits);
-    *reinterpret_cast<uint2*>(out) = w;
-    if (err_out) *err_out = srch.best.err;
+    const uint32_t lo = invert ? best.hi : best.lo, hi = invert ? best.lo : best.hi;
+    *reinterpret_cast<uint2*>(out) = make_uint2(lo | (hi << 16), bits);
+    if (err_out) *err_out = best.err;
   }
+  __syncwarp();
+  return work;
 }
 
-template <bool HC>
-__global__ void __launch_bounds__(kWarpsPerCta * 32)
-    k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, int perceptual, int use_alpha, uint8_t* __restrict__ out,
-                  uint32_t out_stride, uint64_t* __restrict__ err_out) {
-  __shared__ WarpShared smem[kWarpsPerCta];
-  WarpShared& S = smem[threadIdx.x >> 5];
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 3)
+    k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, int perceptual, int hc, int use_alpha,
+                  uint8_t* __restrict__ out, uint32_t out_stride, uint64_t* __restrict__ err_out,
+                  unsigned long long* __restrict__ work_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpShared& S = reinterpret_cast<WarpShared*>(smem_raw)[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
   const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const uint32_t nwarps = gridDim.x * kWarpsPerCta;
   const uint32_t chunks = (n + kBlocksPerWarp - 1) / kBlocksPerWarp;
+  unsigned long long work = 0;
   for (uint32_t chunk = warp_global; chunk < chunks; chunk += nwarps) {
     const uint32_t b0 = chunk * kBlocksPerWarp;
     const uint32_t cnt = min((uint32_t)kBlocksPerWarp, n - b0);
@@ -1006,10 +1118,13 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32)
     __syncwarp();
     for (uint32_t k = 0; k < cnt; k++) {
       const uint32_t bi = b0 + k;
-      phase2_block<HC>(S, k, blocks + (size_t)bi * 64, perceptual != 0, use_alpha != 0, out + (size_t)bi * out_stride,
-                       err_out ? err_out + bi : nullptr);
-      __syncwarp();
+      work += phase2_block(S, k, blocks + (size_t)bi * 64, perceptual != 0, hc != 0, use_alpha != 0,
+                           out + (size_t)bi * out_stride, err_out ? err_out + bi : nullptr);
     }
+  }
+  if (work_out) {
+    for (int o = 16; o > 0; o >>= 1) work += __shfl_xor_sync(FULL_MASK, work, o);
+    if (lane == 0 && work) atomicAdd(work_out, work);
   }
 }
 
@@ -1252,6 +1367,27 @@ int grid_for(const void* kernel, int threads, uint32_t work_units) {
 }  // namespace
 
 // Device-pointer launches (no synchronization).
+// Opt-in work counter (profiling hook): candidate x unique-colour evaluations of the DXT1 search.
+namespace {
+bool g_count = false;
+DevBuf g_count_buf;
+}
+
+int set_work_counter(bool on, cudaStream_t s) {
+  g_count = on;
+  if (!on) return CRNGPU_OK;
+  cudaError_t e = g_count_buf.ensure(16);
+  if (e != cudaSuccess) return cuda_check(e, "alloc counter");
+  return cuda_check(cudaMemsetAsync(g_count_buf.ptr, 0, 16, s), "clear counter");
+}
+
+int read_work_counter(uint64_t* value, cudaStream_t s) {
+  if (!g_count_buf.ptr) { *value = 0; return CRNGPU_OK; }
+  cudaError_t e = cudaMemcpyAsync(value, g_count_buf.ptr, 8, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return cuda_check(e, "read counter");
+}
+
 int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_alpha_blocks, uint8_t* d_out,
                 uint32_t out_stride, uint64_t* d_err, cudaStream_t s) {
   int rc = ensure_tables();
@@ -1259,13 +1395,24 @@ int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_a
   if (!n) return CRNGPU_OK;
   const uint32_t warps_needed = (n + kBlocksPerWarp - 1) / kBlocksPerWarp;
   const uint32_t ctas_needed = (warps_needed + kWarpsPerCta - 1) / kWarpsPerCta;
-  if (use_alpha_blocks) {
-    const int grid = grid_for((const void*)k_dxt1_encode<false>, kWarpsPerCta * 32, ctas_needed);
-    k_dxt1_encode<false><<<grid, kWarpsPerCta * 32, 0, s>>>(d_blocks, n, perceptual, 1, d_out, out_stride, d_err);
-  } else {
-    const int grid = grid_for((const void*)k_dxt1_encode<true>, kWarpsPerCta * 32, ctas_needed);
-    k_dxt1_encode<true><<<grid, kWarpsPerCta * 32, 0, s>>>(d_blocks, n, perceptual, 0, d_out, out_stride, d_err);
+  unsigned long long* work = g_count ? static_cast<unsigned long long*>(g_count_buf.ptr) : nullptr;
+  const size_t smem = sizeof(WarpShared) * kWarpsPerCta;
+  static bool attr_done[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !attr_done[dev]) {
+    cudaError_t ae = cudaFuncSetAttribute(k_dxt1_encode, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (ae != cudaSuccess) return cuda_check(ae, "set smem attribute");
+    attr_done[dev] = true;
   }
+  int per_sm = 1, sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dxt1_encode, kWarpsPerCta * 32, smem);
+  if (per_sm < 1) per_sm = 1;
+  const uint32_t full = (uint32_t)sms * (uint32_t)per_sm;
+  const int grid = (int)(ctas_needed < full ? ctas_needed : full);
+  k_dxt1_encode<<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, perceptual, use_alpha_blocks ? 0 : 1,
+                                                       use_alpha_blocks ? 1 : 0, d_out, out_stride, d_err, work);
   return cuda_check(cudaGetLastError(), "launch k_dxt1_encode");
 }
 

@@ -53,6 +53,12 @@ extern "C" {
 CRNGPU_API const char* crngpu_version(void);
 CRNGPU_API const char* crngpu_last_error(void);
 
+/* Profiling hook (the counterpart of the reference's timing/statistics output, crn_timer.h:43-50):
+ * when enabled, DXT1 encodes count candidate x unique-colour evaluations, the algorithmic work
+ * unit of the endpoint search. Reads the count accumulated since the last call into
+ * *dxt1_evaluations (if not NULL), then enables (1) or disables (0) counting and clears it. */
+CRNGPU_API int crngpu_profile_counters(int enable, uint64_t* dxt1_evaluations, void* stream);
+
 /* ------------------------------------------------------------------------------------------
  * Block encoders (quality: cCRNDXTQualityUber; endpoint caching is never used, so results do
  * not depend on how blocks are batched).
