@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "crn_file.h"
@@ -660,4 +661,175 @@ extern "C" void crngpu_crn_decompress(void* src, unsigned int src_size, void* ds
     height >>= 1;
   }
   crngpu_unpack_end(ctx);
+}
+
+// ------------------------------------------------------------------------------------------
+// Allocation-free transcode of one level.
+//
+// For callers that must not allocate GPU memory while they run: engines and streaming systems
+// that reserve their whole VRAM budget up front and forbid untracked allocations afterwards, and
+// real-time loops where cudaMalloc/cudaFree would block until the device is idle and stall other
+// work. crngpu_unpack_level_noalloc transcodes from a .crn in host memory into the caller's
+// device buffers and keeps everything else it needs -- decode tables, palettes, the level's
+// compressed bytes, the per-block index records, launch descriptors and the status word -- in
+// the fixed array below, which every GPU that loads this library holds until the process exits.
+// It never calls cudaMalloc, cudaFree or any allocating library routine on the device side; the
+// host side only parses the file into ordinary heap memory.
+//
+// All calls share this one array and it keeps the contents of the last call: the status word is
+// cleared on every call, and calls whose work overlaps on the GPU (other threads or streams)
+// race on it, so callers serialise them.
+namespace crngpu {
+
+constexpr size_t kNoAllocScratchBytes = 16u << 20;  // 16 MiB: tables, palettes, stream, records
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+// Device address of g_noalloc_scratch, looked up once per device with that device current (in
+// host code the array's name is only a host-side stand-in, not a device address).
+int noalloc_scratch_ptr(unsigned char** out) {
+  static unsigned char* ptrs[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) { set_error("device index out of range"); return CRNGPU_E_PARAM; }
+  if (!ptrs[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_check(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    ptrs[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = ptrs[dev];
+  return CRNGPU_OK;
+}
+
+}  // namespace
+
+}  // namespace crngpu
+
+extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_size, void** dst_faces,
+                                           uint32_t dst_size_in_bytes, uint32_t row_pitch_in_bytes,
+                                           uint32_t level_index, void* stream) {
+  using namespace crngpu;
+  clear_error();
+  if (!crn_data || !dst_faces || dst_size_in_bytes < 8) { set_error("bad arguments"); return CRNGPU_E_PARAM; }
+  CrnFile F;
+  if (!F.parse(static_cast<const uint8_t*>(crn_data), crn_size)) { set_error(F.error); return CRNGPU_E_CORRUPT; }
+  if (level_index >= F.levels) { set_error("level out of range"); return CRNGPU_E_PARAM; }
+  const LevelInfo& li = F.level[level_index];
+  const uint32_t minimal = li.blocks_x * F.bytes_per_block;
+  uint32_t pitch = row_pitch_in_bytes ? row_pitch_in_bytes : minimal;
+  if (pitch < minimal || (pitch & 3)) { set_error("bad row pitch"); return CRNGPU_E_PARAM; }
+  const uint64_t face_bytes = (uint64_t)pitch * li.blocks_y;
+  if (dst_size_in_bytes < face_bytes) { set_error("destination too small"); return CRNGPU_E_PARAM; }
+  for (uint32_t f = 0; f < F.faces; f++)
+    if (!dst_faces[f]) { set_error("NULL face pointer"); return CRNGPU_E_PARAM; }
+
+  // scratch layout: [status | jobs][models][palettes][level stream][records]
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  const size_t n_cep = F.colour_ep.size(), n_csel = F.colour_sel.size();
+  const size_t n_aep = F.alpha_ep.size(), n_asel = F.alpha_sel.size() / 3;
+  const size_t o_jobs = 256, o_models = 4096;
+  const size_t o_cep = o_models + al(sizeof(DevModel) * kNumModels);
+  const size_t o_csel = o_cep + al(n_cep * 4), o_asel = o_csel + al(n_csel * 4), o_aep = o_asel + al(n_asel * 8);
+  const size_t o_src = o_aep + al(n_aep * 2);
+  const size_t o_rec = o_src + al((size_t)li.size + 64);
+  const size_t rec_bytes = (size_t)li.blocks_x * li.blocks_y * F.faces *
+                           ((F.kind == Kind::DXT1 || F.kind == Kind::DXT5A) ? 4u : 8u);
+  const size_t need = o_rec + al(rec_bytes);
+  if (need > kNoAllocScratchBytes) {
+    set_error("level needs " + std::to_string(need) + " bytes of scratch; the allocation-free entry point has " +
+              std::to_string(kNoAllocScratchBytes));
+    return CRNGPU_E_PARAM;
+  }
+  unsigned char* base = nullptr;
+  int rc = noalloc_scratch_ptr(&base);
+  if (rc != CRNGPU_OK) return rc;
+  cudaStream_t s = as_stream(stream);
+  cudaError_t e;
+  // host images of the tables, palettes and launch descriptors (ordinary heap, copied below)
+  std::vector<DevModel> models(kNumModels);
+  F.ref_dm.to_device(models[kMRef]);
+  F.ep_dm[0].to_device(models[kMEp0]);
+  F.sel_dm[0].to_device(models[kMSel0]);
+  F.ep_dm[1].to_device(models[kMEp1]);
+  F.sel_dm[1].to_device(models[kMSel1]);
+  std::vector<uint64_t> asel64(n_asel);
+  for (size_t i = 0; i < n_asel; i++)
+    asel64[i] = (uint64_t)F.alpha_sel[3 * i] | ((uint64_t)F.alpha_sel[3 * i + 1] << 16) |
+                ((uint64_t)F.alpha_sel[3 * i + 2] << 32);
+  DevPalettes pal;
+  pal.colour_ep = reinterpret_cast<const uint32_t*>(base + o_cep);
+  pal.colour_sel = reinterpret_cast<const uint32_t*>(base + o_csel);
+  pal.alpha_sel = reinterpret_cast<const uint64_t*>(base + o_asel);
+  pal.alpha_ep = reinterpret_cast<const uint16_t*>(base + o_aep);
+  pal.n_cep = (uint32_t)n_cep; pal.n_csel = (uint32_t)n_csel; pal.n_aep = (uint32_t)n_aep; pal.n_asel = (uint32_t)n_asel;
+  DecodeJob dj{base + o_src, li.size, li.blocks_x, li.blocks_y, F.faces, 0};
+  ExpandJob ej[6];
+  const uint32_t chunk_blocks = F.bytes_per_block == 8 ? 2 : 1;
+  const uint32_t per_row = ((li.blocks_x + chunk_blocks - 1) / chunk_blocks + kExpandThreads - 1) / kExpandThreads;
+  int vec_ok = 1;
+  for (uint32_t f = 0; f < F.faces; f++) {
+    ej[f].dst = static_cast<uint8_t*>(dst_faces[f]);
+    ej[f].face_stride = 0;
+    ej[f].rec_ofs = (uint64_t)f * li.blocks_x * li.blocks_y;
+    ej[f].bx = li.blocks_x; ej[f].by = li.blocks_y; ej[f].faces = 1; ej[f].pitch = pitch;
+    ej[f].cta_begin = f * per_row * li.blocks_y;
+    ej[f].ctas_per_row = per_row;
+    if (((uintptr_t)dst_faces[f] | pitch) & 15) vec_ok = 0;
+  }
+  unsigned char jobs[sizeof(DecodeJob) + 6 * sizeof(ExpandJob)];
+  std::memcpy(jobs, &dj, sizeof(dj));
+  std::memcpy(jobs + sizeof(dj), ej, sizeof(ExpandJob) * F.faces);
+  uint32_t* status = reinterpret_cast<uint32_t*>(base);
+  const DecodeJob* d_dj = reinterpret_cast<const DecodeJob*>(base + o_jobs);
+  const ExpandJob* d_ej = reinterpret_cast<const ExpandJob*>(base + o_jobs + sizeof(DecodeJob));
+  struct Copy { size_t ofs; const void* src; size_t bytes; };
+  const Copy copies[] = {
+      {o_jobs, jobs, sizeof(DecodeJob) + sizeof(ExpandJob) * F.faces},
+      {o_models, models.data(), sizeof(DevModel) * kNumModels},
+      {o_cep, F.colour_ep.data(), n_cep * 4},
+      {o_csel, F.colour_sel.data(), n_csel * 4},
+      {o_asel, asel64.data(), n_asel * 8},
+      {o_aep, F.alpha_ep.data(), n_aep * 2},
+      {o_src, static_cast<const uint8_t*>(crn_data) + li.ofs, li.size},
+  };
+  for (const Copy& c : copies) {
+    if (!c.bytes) continue;
+    if ((e = cudaMemcpyAsync(base + c.ofs, c.src, c.bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return cuda_check(e, "copy into the fixed scratch");
+  }
+  if ((e = cudaMemsetAsync(status, 0, 4, s)) != cudaSuccess) return cuda_check(e, "clear status");
+  const DevModel* d_models = reinterpret_cast<const DevModel*>(base + o_models);
+  void* records = base + o_rec;
+  const uint32_t ctas = per_row * li.blocks_y * F.faces;
+  switch (F.kind) {
+    case Kind::DXT1:
+      k_crn_decode<0><<<1, 32, sizeof(uint32_t) * (1 << kLutBits) * models_used<0>(), s>>>(d_dj, 1, d_models, pal, records, status);
+      k_crn_expand<0><<<ctas, kExpandThreads, 0, s>>>(d_ej, (int)F.faces, pal, records, vec_ok);
+      break;
+    case Kind::DXT5:
+      k_crn_decode<1><<<1, 32, sizeof(uint32_t) * (1 << kLutBits) * models_used<1>(), s>>>(d_dj, 1, d_models, pal, records, status);
+      k_crn_expand<1><<<ctas, kExpandThreads, 0, s>>>(d_ej, (int)F.faces, pal, records, vec_ok);
+      break;
+    case Kind::DXN:
+      k_crn_decode<2><<<1, 32, sizeof(uint32_t) * (1 << kLutBits) * models_used<2>(), s>>>(d_dj, 1, d_models, pal, records, status);
+      k_crn_expand<2><<<ctas, kExpandThreads, 0, s>>>(d_ej, (int)F.faces, pal, records, vec_ok);
+      break;
+    case Kind::DXT5A:
+      k_crn_decode<3><<<1, 32, sizeof(uint32_t) * (1 << kLutBits) * models_used<3>(), s>>>(d_dj, 1, d_models, pal, records, status);
+      k_crn_expand<3><<<ctas, kExpandThreads, 0, s>>>(d_ej, (int)F.faces, pal, records, vec_ok);
+      break;
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch transcode kernels");
+  uint32_t st = 0;
+  if ((e = cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read status");
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
+  if (st) {
+    set_error(st == kStBadCode ? "corrupt block stream (no such prefix code)"
+                               : "corrupt block stream (palette index out of range)");
+    return CRNGPU_E_CORRUPT;
+  }
+  return CRNGPU_OK;
 }

@@ -141,6 +141,24 @@ CRNGPU_API int crngpu_unpack_level_segmented(crngpu_unpack_context ctx, const vo
 CRNGPU_API int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t first_level, uint32_t level_count, void* dst,
                              uint64_t dst_size, int mem, void* stream);
 
+/* Allocation-free transcode of one level. No counterpart in the reference: it exists for
+ * callers that cannot allocate GPU memory while they run -- engines that reserve their whole
+ * VRAM budget up front and forbid untracked allocations, and real-time loops in which
+ * cudaMalloc/cudaFree would wait for the device to go idle and stall other work.
+ * crn_data (crn_size bytes) is the .crn file in host memory; dst_faces holds one device
+ * pointer per face; size, pitch and level rules are those of crngpu_unpack_level. Everything
+ * else the kernels need lives in one fixed 16 MiB device array that every GPU loading this
+ * library holds until the process exits; a level that needs more (tables + palettes + its
+ * compressed bytes + 4 or 8 bytes per block) is rejected with CRNGPU_E_PARAM and a message.
+ * The call makes no cudaMalloc/cudaFree or other device allocation. The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture. All calls share the array and it keeps the last call's contents,
+ * so calls that overlap on the GPU (from other threads or streams) race: serialise them.
+ * The call returns after the level is written (it reads back a status word). */
+CRNGPU_API int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_size, void** dst_faces,
+                                           uint32_t dst_size_in_bytes, uint32_t row_pitch_in_bytes,
+                                           uint32_t level_index, void* stream);
+
 /* Replaces crnd_unpack_end (inc/crn_defs.h:205). Returns CRNGPU_OK, or CRNGPU_E_PARAM for NULL. */
 CRNGPU_API int crngpu_unpack_end(crngpu_unpack_context ctx);
 
