@@ -171,6 +171,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
       pix[4 * q] = v.x; pix[4 * q + 1] = v.y; pix[4 * q + 2] = v.z; pix[4 * q + 3] = v.w;
     }
   }
+  #pragma unroll 1
   for (int p = 0; p < 16; p++) {
     const uint32_t c = pix[p] & 0xFFFFFFu;
     int i = 0;
@@ -186,6 +187,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
   float pw[3] = {1.0f, 1.0f, 1.0f};
   if (perceptual) {
     float red = 0.f, blue = 0.f, avel = 0.f;
+    #pragma unroll 1
     for (int i = 0; i < n; i++) {
       const uint32_t c = S.t_col[i][L];
       const int r = c & 255, g = (c >> 8) & 255, b = c >> 16;
@@ -213,10 +215,12 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
     }
   }
   float mean[3], axis[3];
+  #pragma unroll 1
   for (int pass = 0; pass < passes; pass++) {
     // compute_vectors :155-189
     float meanw[3] = {0.f, 0.f, 0.f};
     mean[0] = mean[1] = mean[2] = 0.f;
+    #pragma unroll 1
     for (int i = 0; i < n; i++) {
       const uint32_t c = S.t_col[i][L];
       const float wf = (float)S.t_w[i][L];
@@ -231,6 +235,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
     for (int k = 0; k < 3; k++) { mean[k] = __fmul_rn(mean[k], inv); meanw[k] = __fmul_rn(meanw[k], inv); }
     // compute_pca :192-256 (double accumulation in colour order)
     double cov[6] = {0, 0, 0, 0, 0, 0};
+    #pragma unroll 1
     for (int i = 0; i < n; i++) {
       const uint32_t c = S.t_col[i][L];
       const int w = S.t_w[i][L];
@@ -252,6 +257,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
       }
     }
     double vf[3] = {(double).9f, (double)1.0f, (double).7f};
+    #pragma unroll 1
     for (int it = 0; it < 8; it++) {
       double r = __dadd_rn(__dadd_rn(__dmul_rn(vf[0], cov[0]), __dmul_rn(vf[1], cov[1])), __dmul_rn(vf[2], cov[2]));
       double g = __dadd_rn(__dadd_rn(__dmul_rn(vf[0], cov[1]), __dmul_rn(vf[1], cov[3])), __dmul_rn(vf[2], cov[4]));
@@ -292,6 +298,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
   }
   // projection bounds on the axis, then pull outside endpoints back into the unit cube
   float lo_d = 1e+9f, hi_d = -1e+9f;
+  #pragma unroll 1
   for (int i = 0; i < n; i++) {
     float d = __fmul_rn(S.t_norm[0][i][L], axis[0]);
     d = __fadd_rn(d, __fmul_rn(S.t_norm[1][i][L], axis[1]));
@@ -341,10 +348,12 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
     FastRandom rm;
     unsigned rover = 0;
     float prev_total = 1.0e+37f;
+    #pragma unroll 1
     for (int it = 0; it < 8; it++) {
       float nm[4][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
       float nw[4] = {0.f, 0.f, 0.f, 0.f};
       float tot = 0.f;
+      #pragma unroll 1
       for (int i = 0; i < n; i++) {
         const float v[3] = {S.t_norm[0][i][L], S.t_norm[1][i][L], S.t_norm[2][i][L]};
         float bd = 0.f;
@@ -392,6 +401,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
     }
   }
   int slot_i = 0;
+  #pragma unroll 1
   for (int i = 0; i < 3; i++) {
     for (int j = i + 1; j < 4; j++) {
       int q[2][3];
@@ -597,6 +607,10 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
     const uint32_t lb = valid ? lower_bound(S, lo, hi) : kInf;
     const uint32_t B0 = S.st.best.err;
     bool live = valid && lb < B0;
+    if (!__any_sync(FULL_MASK, live)) {  // the whole batch is pruned: nothing tried, nothing to insert
+      i0 += 32;
+      continue;
+    }
     const uint32_t key = lo | (hi << 16);
     if (!d.alt) {
       // a repeated candidate can never win: keep the first copy in the batch, drop keys tried before
@@ -745,6 +759,7 @@ __device__ bool try_solid(WarpShared& S, uint32_t& work) {
     int cnt = 0;
     S.cand[cnt++] = solid_coords(ar, ag, ab, false);
     if (three) S.cand[cnt++] = solid_coords(ar, ag, ab, true);
+    #pragma unroll 1
     for (int i = 0; i < n; i++) {
       const uint32_t c = S.uci[i];
       const int r = c & 255, g = (c >> 8) & 255, b = c >> 16;
@@ -778,6 +793,7 @@ __device__ void comp_errors(WarpShared& S, int comp) {
     WPP[k] = __reduce_add_sync(FULL_MASK, sel == k ? w * p * p : 0u);
   }
   const int limit = comp == 1 ? 64 : 32;
+  #pragma unroll 1
   for (int k = 0; k < 4; k++) {
     uint32_t m = kInf;
     if (k < 2) {
@@ -809,6 +825,7 @@ __device__ void optimize_comps(WarpShared& S, uint32_t& work) {
   const int src_lo[3] = {exp5(blo >> 11), exp6((blo >> 5) & 63), exp5(blo & 31)};
   const int src_hi[3] = {exp5(bhi >> 11), exp6((bhi >> 5) & 63), exp5(bhi & 31)};
   const uint32_t lane = lane_id();
+  #pragma unroll 1
   for (int comp = 0; comp < 3; comp++) {
     const int p0s = src_lo[comp], p1s = src_hi[comp];
     const uint32_t clo = S.st.best.lo, chi = S.st.best.hi;
@@ -820,6 +837,7 @@ __device__ void optimize_comps(WarpShared& S, uint32_t& work) {
     uint32_t best_err = comp_E(S.d, 0, ex(lo_u[comp])) + comp_E(S.d, 1, ex(hi_u[comp])) +
                         comp_E(S.d, 2, (uint32_t)((p0s * 2 + p1s) / 3)) + comp_E(S.d, 3, (uint32_t)((p0s + p1s * 2) / 3));
     if (S.d.rem[0] >= best_err) continue;
+    #pragma unroll 1
     for (int c0 = 0; c0 < limit; c0++) {
       uint32_t e0 = comp_E(S.d, 0, ex(c0));
       if (e0 + S.d.rem[1] >= best_err) continue;
@@ -831,6 +849,13 @@ __device__ void optimize_comps(WarpShared& S, uint32_t& work) {
         S.d.base[0] = hi_u[0]; S.d.base[1] = hi_u[1]; S.d.base[2] = hi_u[2];
       }
       __syncwarp();
+      {
+        // cheap pre-check: does any c1 pass the component-table prune for this c0?
+        uint32_t tlo, thi;
+        const bool p0ok = (int)lane < limit && gen_candidate(S, S.d, lane, tlo, thi);
+        const bool p1ok = (int)lane + 32 < limit && gen_candidate(S, S.d, lane + 32, tlo, thi);
+        if (!__any_sync(FULL_MASK, p0ok || p1ok)) continue;
+      }
       int start = 0;
       while (start < limit) {
         const int c1 = run_list(S, start, work);
@@ -873,10 +898,12 @@ __device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
     };
     if (n == 2) {
       const float fs[10] = {2.0f, 3.0f, .5f, 1.5f, -1.0f, 2.0f, -.5f, .5f, -2.0f, -1.0f};
+      #pragma unroll 1
       for (int k = 0; k < 2; k++)
         for (int q = 0; q < 2; q++)
           for (int f = 0; f < 10; f++) push(q, q ^ 1, fs[f], k);
     } else if (n == 3) {
+      #pragma unroll 1
       for (int i = 0; i <= 2; i++)
         for (int j = 0; j <= 2; j++) {
           if (i == j) continue;
@@ -887,6 +914,7 @@ __device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
         }
     }
     int m = 0;
+    #pragma unroll 1
     for (int i = 0; i < cnt; i++) {
       const uint32_t c = S.cand[i];
       const uint32_t ur = min(((c & 255) * 31u + 127u) / 255u, 31u);
@@ -901,6 +929,7 @@ __device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
   }
   __syncwarp();
   const int m = S.d.nh;
+  #pragma unroll 1
   for (int alt = 0; alt < 2; alt++) {
     uint32_t saved = 0;
     if (alt) {
@@ -908,6 +937,7 @@ __device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
       if (lane == 0 && saved) S.st.best.err = 1;
       __syncwarp();
     }
+    #pragma unroll 1
     for (int i = 0; S.st.best.err && i + 1 < m; i++) {
       if (lane == 0) {
         S.d.kind = LK_COMB; S.d.count = m - 1 - i; S.d.dependent = 0; S.d.alt = alt; S.d.stop_on_accept = 0;
@@ -941,6 +971,7 @@ __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
     high[k] = h < 0.0f ? 0.0f : (h > lim[k] ? lim[k] : h);
   }
   sa1[0] = __fmul_rn(sa1[0], 31.0f); sa1[1] = __fmul_rn(sa1[1], 63.0f); sa1[2] = __fmul_rn(sa1[2], 31.0f);
+  #pragma unroll 1
   for (int pass = 0; pass < 4; pass++) {
     if (pass) {
       const uint32_t blo = S.st.best.lo, bhi = S.st.best.hi;
@@ -981,6 +1012,7 @@ __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
     }
     run_list(S, 0, work);
     // lattice neighbours: low endpoint (26 adjacent cells, then +-2 per axis), then high
+    #pragma unroll 1
     for (int side = 0; side < 2; side++) {
       for (int kind = LK_NEIGH; kind <= LK_MOVE2; kind++) {
         if (lane == 0) {
@@ -1010,6 +1042,7 @@ __device__ void build_lower_bounds(WarpShared& S, int n, bool perceptual) {
   const int c = (int)lane_id();
   uint32_t rw = 0, r1 = 0, r2 = 0, gw = 0, g1 = 0, g2 = 0, gw2 = 0, g12 = 0, g22 = 0, bw = 0, b1 = 0, b2 = 0;
   uint32_t tw = 0, tr1 = 0, tr2 = 0, tg1 = 0, tg2 = 0, tb1 = 0, tb2 = 0;
+  #pragma unroll 1
   for (int i = 0; i < n; i++) {
     const uint32_t col = S.uci[i];
     const uint32_t w = (uint32_t)S.ucw[i];
@@ -1100,7 +1133,7 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
   return work;
 }
 
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 3)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
     k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, int perceptual, int hc, int use_alpha,
                   uint8_t* __restrict__ out, uint32_t out_stride, uint64_t* __restrict__ err_out,
                   unsigned long long* __restrict__ work_out) {
@@ -1116,6 +1149,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 3)
     const uint32_t cnt = min((uint32_t)kBlocksPerWarp, n - b0);
     if (lane < cnt) phase1_block(S, lane, blocks + (size_t)(b0 + lane) * 64, perceptual != 0);
     __syncwarp();
+    #pragma unroll 1
     for (uint32_t k = 0; k < cnt; k++) {
       const uint32_t bi = b0 + k;
       work += phase2_block(S, k, blocks + (size_t)bi * 64, perceptual != 0, hc != 0, use_alpha != 0,
