@@ -26,6 +26,7 @@ UNITS = [
     ("crn_transcode.cu", []),
     ("encode_api.cu", []),
     ("dxt_encode.cu", ["--fmad=false"]),
+    ("mlp.cu", []),
 ]
 
 

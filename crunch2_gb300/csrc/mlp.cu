@@ -1,0 +1,744 @@
+// Learned DXT1 endpoint proposal: a 48 -> 256 (GELU) -> 256 (GELU) -> 8 MLP trained and run on
+// the 5th-generation tensor cores (tcgen05.mma, BF16 operands from shared memory, FP32
+// accumulators in tensor memory). This part has no counterpart in the reference; it replaces
+// the initial guess and most of the refinement of dxt1_endpoint_optimizer (crnlib/crn_dxt1.cpp)
+// for blocks where it is good enough, and the exact optimizer stays the fallback and the judge.
+//
+// Inputs: 16 texels x RGB scaled to [0, 1]. Outputs: y[0..5] = low/high endpoint (r/31, g/63,
+// b/31) of the plain optimizer's 4-colour solution, y[6] = log2(1 + block error)/16, the
+// network's prediction of the error the plain optimizer reaches (the fallback bound); y[7] unused.
+//
+// All GEMMs go through k_gemm_tc: C[M x N] = sum_k A(m, k) B(n, k), a 128 x BN tile per CTA,
+// K staged 64 at a time into shared memory in the no-swizzle K-major core-matrix layout
+// (8 x 8 BF16 core matrices, 128 bytes each), four K=16 MMAs per stage issued by one thread,
+// completion through tcgen05.commit on an mbarrier (bounded wait), epilogue from TMEM with
+// tcgen05.ld. Operands are fp32, bf16 or raw RGBA8 blocks with arbitrary strides, so the
+// transposed products of the backward pass need no separate transpose kernels.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "crngpu_internal.h"
+
+namespace crngpu {
+
+int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_alpha_blocks, uint8_t* d_out,
+                uint32_t out_stride, uint64_t* d_err, cudaStream_t s);
+
+namespace mlp {
+
+constexpr int kIn = 48, kHid = 256, kOut = 8, kOutPad = 16;
+constexpr int BM = 128, BK = 64;
+constexpr int kTmemCols = 128;
+constexpr uint32_t kWaitLimit = 1u << 24;  // bounded mbarrier polls (~ tens of ms), then error
+
+enum OpKind : int { OP_F32 = 0, OP_BF16 = 1, OP_PIXELS = 2 };
+// epilogues
+enum Epi : int {
+  EPI_STORE = 0,       // C = acc (+ bias)
+  EPI_BIAS_GELU = 1,   // Cpre = acc + bias (fp32), Cb = bf16(gelu(Cpre))
+  EPI_GELU_GRAD = 2,   // Cb = bf16(acc * gelu'(pre)), C (fp32) = same value
+};
+
+struct Operand {
+  const void* p;
+  int kind;
+  long long s_row, s_k;  // element (row, k) at p[row * s_row + k * s_k]; OP_PIXELS: see load_op
+  int pix_sample_is_row; // OP_PIXELS: 1 -> row = sample, k = feature; 0 -> row = feature, k = sample
+};
+
+struct GemmArgs {
+  Operand a, b;
+  int M, N, K;
+  int epi;
+  float* C;              // fp32 out (row-major, ldc)
+  __nv_bfloat16* Cb;     // bf16 out (row-major, ldc)
+  const float* pre;      // EPI_GELU_GRAD: pre-activation (row-major, ldc)
+  const float* bias;     // per column
+  int ldc;
+  uint32_t* err;         // set to 1 if an mbarrier wait timed out
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (r, k) of a tile with `kt` K-columns in the no-swizzle K-major layout
+__device__ __forceinline__ uint32_t kmaj_off(int r, int k, int kt) {
+  return (uint32_t)((r >> 3) * ((kt >> 3) * 128) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// tcgen05 shared-memory matrix descriptor: start, leading (K) and stride (8-row) byte offsets,
+// descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ float gelu(float x) {
+  const float c = 0.7978845608f;  // sqrt(2/pi), tanh form
+  return 0.5f * x * (1.f + tanhf(c * (x + 0.044715f * x * x * x)));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float c = 0.7978845608f;
+  const float t = tanhf(c * (x + 0.044715f * x * x * x));
+  return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * c * (1.f + 3.f * 0.044715f * x * x);
+}
+
+__device__ __forceinline__ float load_op(const Operand& o, int row, int k, int rows, int ks) {
+  if (row >= rows || k >= ks) return 0.f;
+  switch (o.kind) {
+    case OP_F32: return reinterpret_cast<const float*>(o.p)[row * o.s_row + k * o.s_k];
+    case OP_BF16: return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(o.p)[row * o.s_row + k * o.s_k]);
+    default: {
+      const int s = o.pix_sample_is_row ? row : k, f = o.pix_sample_is_row ? k : row;
+      const uint8_t* px = reinterpret_cast<const uint8_t*>(o.p);
+      return (float)px[(long long)s * 64 + (f / 3) * 4 + f % 3] * (1.0f / 255.0f);
+    }
+  }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  uint32_t done = 0;
+  for (uint32_t it = 0; it < kWaitLimit && !done; it++) {
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity));
+  }
+  return done != 0;
+}
+
+// C tile (blockIdx.x: 128 rows of M, blockIdx.y: BN columns of N) = A x B^T over all of K.
+template <int BN>
+__global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
+  __shared__ __align__(1024) unsigned char sa[BM * BK * 2];
+  __shared__ __align__(1024) unsigned char sb[BN * BK * 2];
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "n"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base;
+  const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+  uint32_t phase = 0;
+  bool ok = true;
+  const int nk = (g.K + BK - 1) / BK;
+  for (int kc = 0; kc < nk; kc++) {
+    const int k0 = kc * BK;
+    // stage A (BM x BK) and B (BN x BK); the faster-varying index follows the operand's
+    // contiguous dimension so global reads coalesce
+    for (int e = tid; e < BM * BK; e += 128) {
+      int r, k;
+      if (g.a.kind != OP_PIXELS && g.a.s_row == 1) { r = e % BM; k = e / BM; } else { k = e % BK; r = e / BK; }
+      const float v = load_op(g.a, m0 + r, k0 + k, g.M, g.K);
+      *reinterpret_cast<__nv_bfloat16*>(sa + kmaj_off(r, k, BK)) = __float2bfloat16(v);
+    }
+    for (int e = tid; e < BN * BK; e += 128) {
+      int r, k;
+      if (g.b.kind != OP_PIXELS && g.b.s_row == 1) { r = e % BN; k = e / BN; } else { k = e % BK; r = e / BK; }
+      const float v = load_op(g.b, n0 + r, k0 + k, g.N, g.K);
+      *reinterpret_cast<__nv_bfloat16*>(sb + kmaj_off(r, k, BK)) = __float2bfloat16(v);
+    }
+    asm volatile("fence.proxy.async.shared::cta;");  // generic-proxy smem writes -> tensor core reads
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int ks = 0; ks < BK / 16; ks++) {
+        const uint64_t ad = make_desc(smem_u32(sa) + ks * 256, 128, (BK / 8) * 128);
+        const uint64_t bd = make_desc(smem_u32(sb) + ks * 256, 128, (BK / 8) * 128);
+        const uint32_t acc = (kc > 0 || ks > 0) ? 1u : 0u;
+        asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                     "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&mbar)));
+    }
+    // the MMAs read shared memory asynchronously: wait before restaging it
+    const bool done = mbar_wait(smem_u32(&mbar), phase);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    ok = __syncthreads_and(done) != 0;  // uniform across the CTA
+    if (!ok) {
+      // give the in-flight MMAs a second bounded chance to finish before TMEM is released
+      mbar_wait(smem_u32(&mbar), phase);
+      break;
+    }
+    phase ^= 1;
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(g.err, 1u);
+  } else {
+    // epilogue: warp w owns rows 32w..32w+31 of the tile, 16 columns per tcgen05.ld
+    const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;");
+      if (row < g.M) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int col = n0 + c0 + j;
+          if (col >= g.N) continue;
+          float v = __uint_as_float(r[j]);
+          const long long o = (long long)row * g.ldc + col;
+          if (g.epi == EPI_STORE) {
+            if (g.bias) v += g.bias[col];
+            if (g.C) g.C[o] = v;
+            if (g.Cb) g.Cb[o] = __float2bfloat16(v);
+          } else if (g.epi == EPI_BIAS_GELU) {
+            v += g.bias[col];
+            g.C[o] = v;
+            g.Cb[o] = __float2bfloat16(gelu(v));
+          } else {
+            v *= gelu_grad(g.pre[o]);
+            if (g.C) g.C[o] = v;
+            g.Cb[o] = __float2bfloat16(v);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kTmemCols));
+}
+
+// ------------------------------------------------------------------------------------------
+// elementwise / reduction kernels
+
+// dY = 2 (y - t) / B on the 7 trained outputs; loss partial sums
+__global__ void k_loss_grad(const float* __restrict__ y, const float* __restrict__ t, int B, float* __restrict__ dy,
+                            float* __restrict__ loss) {
+  float acc = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B * kOutPad; i += gridDim.x * blockDim.x) {
+    const int s = i / kOutPad, c = i % kOutPad;
+    float g = 0.f;
+    if (c < 7) {
+      const float d = y[(long long)s * kOutPad + c] - t[(long long)s * kOut + c];
+      acc += d * d;
+      g = 2.f * d / (float)B;
+    }
+    dy[i] = g;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xFFFFFFFFu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, acc / (float)B);
+}
+
+// column sums of a row-major [rows x cols] fp32 matrix -> out[cols]
+__global__ void k_colsum(const float* __restrict__ x, int rows, int cols, float* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.f;
+  for (int r = 0; r < rows; r++) s += x[(long long)r * cols + c];
+  out[c] = s;
+}
+
+// AdamW on fp32 master weights; refreshes the bf16 copy. mask: parameters that stay zero.
+__global__ void k_adamw(float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                        __nv_bfloat16* __restrict__ wb, int n, float lr, float b1, float b2, float eps, float wd,
+                        float bc1, float bc2, int rows_live, int row_len) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (i / row_len >= rows_live) { w[i] = 0.f; if (wb) wb[i] = __float2bfloat16(0.f); continue; }
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    float wi = w[i] * (1.f - lr * wd);
+    wi -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16(wi);
+  }
+}
+
+// Training targets from the plain optimizer's blocks: endpoints of the 4-colour solution in
+// [0, 1] units, and log2(1 + error) / 16.
+__global__ void k_make_targets(const uint8_t* __restrict__ blocks8, const uint64_t* __restrict__ err, int n,
+                               float* __restrict__ t) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const uint8_t* b = blocks8 + (long long)i * 8;
+    uint32_t lo = b[0] | (b[1] << 8), hi = b[2] | (b[3] << 8);
+    if (lo <= hi) { const uint32_t x = lo; lo = hi; hi = x; }  // 3-colour blocks: order as 4-colour
+    float* o = t + (long long)i * kOut;
+    o[0] = (float)(lo >> 11) / 31.f; o[1] = (float)((lo >> 5) & 63) / 63.f; o[2] = (float)(lo & 31) / 31.f;
+    o[3] = (float)(hi >> 11) / 31.f; o[4] = (float)((hi >> 5) & 63) / 63.f; o[5] = (float)(hi & 31) / 31.f;
+    o[6] = log2f(1.f + (float)err[i]) / 16.f;
+    o[7] = 0.f;
+  }
+}
+
+// Learned encode, per block: quantise the predicted endpoints, choose selectors, refit the
+// endpoints by least squares from those selectors (refine_solution level 0,
+// crnlib/crn_dxt1.cpp:525-600), choose selectors again, and keep the block unless its error is
+// above 1.5x the network's predicted bound; those blocks are queued for the exact optimizer.
+__device__ __forceinline__ int q565(float v, int hi) {
+  int x = __float2int_rn(v * (float)hi);
+  return x < 0 ? 0 : (x > hi ? hi : x);
+}
+__device__ uint32_t block_error(const uint32_t* px, uint32_t lo, uint32_t hi, bool perceptual, uint32_t* sel_out) {
+  int c[4][3];
+  const int r0 = ((lo >> 11) << 3) | (lo >> 13), g0 = (((lo >> 5) & 63) << 2) | (((lo >> 5) & 63) >> 4),
+            b0 = ((lo & 31) << 3) | ((lo & 31) >> 2);
+  const int r1 = ((hi >> 11) << 3) | (hi >> 13), g1 = (((hi >> 5) & 63) << 2) | (((hi >> 5) & 63) >> 4),
+            b1 = ((hi & 31) << 3) | ((hi & 31) >> 2);
+  c[0][0] = r0; c[0][1] = g0; c[0][2] = b0;
+  c[1][0] = r1; c[1][1] = g1; c[1][2] = b1;
+  for (int k = 0; k < 3; k++) {
+    c[2][k] = (c[0][k] * 2 + c[1][k]) / 3;
+    c[3][k] = (c[1][k] * 2 + c[0][k]) / 3;
+  }
+  const int wr = perceptual ? 8 : 1, wg = perceptual ? 25 : 1;
+  uint32_t err = 0, sel = 0;
+  for (int p = 0; p < 16; p++) {
+    const int r = px[p] & 255, g = (px[p] >> 8) & 255, b = (px[p] >> 16) & 255;
+    uint32_t best = 0xFFFFFFFFu;
+    int bi = 0;
+    for (int k = 0; k < 4; k++) {
+      const int dr = r - c[k][0], dg = g - c[k][1], db = b - c[k][2];
+      const uint32_t d = (uint32_t)(wr * dr * dr + wg * dg * dg + db * db);
+      if (d < best) { best = d; bi = k; }
+    }
+    err += best;
+    sel |= (uint32_t)bi << (2 * p);
+  }
+  *sel_out = sel;
+  return err;
+}
+
+__global__ void k_learned_refit(const uint8_t* __restrict__ blocks, const float* __restrict__ y, int n, int perceptual,
+                                uint8_t* __restrict__ out, uint32_t* __restrict__ fallback, uint32_t* __restrict__ nfall,
+                                float threshold) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    uint32_t px[16];
+    const uint4* p4 = reinterpret_cast<const uint4*>(blocks + (long long)i * 64);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const uint4 v = __ldg(p4 + q);
+      px[4 * q] = v.x; px[4 * q + 1] = v.y; px[4 * q + 2] = v.z; px[4 * q + 3] = v.w;
+    }
+    const float* yi = y + (long long)i * kOutPad;
+    uint32_t lo = (uint32_t)((q565(yi[0], 31) << 11) | (q565(yi[1], 63) << 5) | q565(yi[2], 31));
+    uint32_t hi = (uint32_t)((q565(yi[3], 31) << 11) | (q565(yi[4], 63) << 5) | q565(yi[5], 31));
+    uint32_t sel;
+    uint32_t err = block_error(px, lo, hi, perceptual != 0, &sel);
+    // least-squares refit from the selectors (points at 0, 1/3, 2/3, 1 between low and high)
+    {
+      float aa = 0.f, ab = 0.f, bb = 0.f, ax[3] = {0, 0, 0}, bx[3] = {0, 0, 0};
+      static const float wlow[4] = {1.f, 0.f, 2.f / 3.f, 1.f / 3.f};
+      for (int p = 0; p < 16; p++) {
+        const int s = (sel >> (2 * p)) & 3;
+        const float a = wlow[s], b = 1.f - a;
+        aa += a * a; ab += a * b; bb += b * b;
+        const float x[3] = {(float)(px[p] & 255), (float)((px[p] >> 8) & 255), (float)((px[p] >> 16) & 255)};
+        for (int k = 0; k < 3; k++) { ax[k] += a * x[k]; bx[k] += b * x[k]; }
+      }
+      const float det = aa * bb - ab * ab;
+      if (fabsf(det) > 1e-6f) {
+        const float inv = 1.f / det;
+        float e0[3], e1[3];
+        for (int k = 0; k < 3; k++) {
+          e0[k] = (ax[k] * bb - bx[k] * ab) * inv;
+          e1[k] = (bx[k] * aa - ax[k] * ab) * inv;
+        }
+        const uint32_t nlo = (uint32_t)((q565(e0[0] / 255.f, 31) << 11) | (q565(e0[1] / 255.f, 63) << 5) |
+                                        q565(e0[2] / 255.f, 31));
+        const uint32_t nhi = (uint32_t)((q565(e1[0] / 255.f, 31) << 11) | (q565(e1[1] / 255.f, 63) << 5) |
+                                        q565(e1[2] / 255.f, 31));
+        uint32_t nsel;
+        const uint32_t nerr = block_error(px, nlo, nhi, perceptual != 0, &nsel);
+        if (nerr < err) { err = nerr; lo = nlo; hi = nhi; sel = nsel; }
+      }
+    }
+    // a 4-colour block needs low > high; swap (and remap selectors 0<->1, 2<->3) or break ties
+    if (lo < hi) {
+      const uint32_t t = lo; lo = hi; hi = t;
+      sel ^= 0x55555555u;
+    } else if (lo == hi) {
+      if ((lo & 31) != 31) { lo++; sel = 0x55555555u; } else { hi--; sel = 0; }
+      err = block_error(px, lo, hi, perceptual != 0, &sel);
+    }
+    const float bound = exp2f(yi[6] * 16.f) - 1.f;
+    uint2 w = make_uint2(lo | (hi << 16), sel);
+    *reinterpret_cast<uint2*>(out + (long long)i * 8) = w;
+    if ((float)err > threshold * fmaxf(bound, 1.f)) {
+      const uint32_t at = atomicAdd(nfall, 1u);
+      fallback[at] = (uint32_t)i;
+    }
+  }
+}
+
+__global__ void k_gather_idx(const uint8_t* __restrict__ blocks, const uint32_t* __restrict__ idx,
+                             const uint32_t* __restrict__ count, uint8_t* __restrict__ out) {
+  const uint32_t n = *count;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < n * 4; t += gridDim.x * blockDim.x) {
+    const uint32_t i = t >> 2, q = t & 3;
+    reinterpret_cast<uint4*>(out)[t] = reinterpret_cast<const uint4*>(blocks + (long long)idx[i] * 64)[q];
+  }
+}
+__global__ void k_scatter_idx(const uint8_t* __restrict__ enc, const uint32_t* __restrict__ idx,
+                              const uint32_t* __restrict__ count, uint8_t* __restrict__ out) {
+  const uint32_t n = *count;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    *reinterpret_cast<uint2*>(out + (long long)idx[i] * 8) = reinterpret_cast<const uint2*>(enc)[i];
+}
+
+// ------------------------------------------------------------------------------------------
+// Host side
+
+struct Param {
+  int rows, cols, rows_live;
+  DevBuf w, g, m, v, wb;  // fp32 master, grad, Adam moments, bf16 copy (weights only)
+  size_t n() const { return (size_t)rows * cols; }
+};
+
+struct Net {
+  uint32_t magic = 0x4D4C5030u;
+  int device = -1;
+  Param W1, b1, W2, b2, W3, b3;
+  int step = 0;
+  // activations / scratch sized for the largest batch seen
+  int cap = 0;
+  DevBuf pre1, h1, pre2, h2, y, dy, dpre2, dpre1, dh_b, dh_b1, targets, loss, errflag;
+  // learned encode scratch
+  DevBuf fb_idx, fb_count, fb_in, fb_out, chunk_y;
+  std::vector<Param*> params() { return {&W1, &b1, &W2, &b2, &W3, &b3}; }
+};
+
+int alloc_param(Param& p, int rows, int cols, int rows_live, bool bf16) {
+  p.rows = rows; p.cols = cols; p.rows_live = rows_live;
+  cudaError_t e;
+  if ((e = p.w.ensure(p.n() * 4)) != cudaSuccess) return cuda_check(e, "alloc weights");
+  if ((e = p.g.ensure(p.n() * 4)) != cudaSuccess) return cuda_check(e, "alloc grads");
+  if ((e = p.m.ensure(p.n() * 4)) != cudaSuccess) return cuda_check(e, "alloc adam m");
+  if ((e = p.v.ensure(p.n() * 4)) != cudaSuccess) return cuda_check(e, "alloc adam v");
+  cudaMemset(p.m.ptr, 0, p.n() * 4);
+  cudaMemset(p.v.ptr, 0, p.n() * 4);
+  cudaMemset(p.g.ptr, 0, p.n() * 4);
+  if (bf16 && (e = p.wb.ensure(p.n() * 2)) != cudaSuccess) return cuda_check(e, "alloc bf16 weights");
+  return CRNGPU_OK;
+}
+
+int upload(Param& p, const std::vector<float>& host) {
+  cudaError_t e = cudaMemcpy(p.w.ptr, host.data(), p.n() * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_check(e, "upload weights");
+  if (p.wb.ptr) {
+    std::vector<__nv_bfloat16> hb(p.n());
+    for (size_t i = 0; i < p.n(); i++) hb[i] = __float2bfloat16(host[i]);
+    if ((e = cudaMemcpy(p.wb.ptr, hb.data(), p.n() * 2, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return cuda_check(e, "upload bf16 weights");
+  }
+  return CRNGPU_OK;
+}
+
+int ensure_batch(Net& net, int B) {
+  if (B <= net.cap) return CRNGPU_OK;
+  cudaError_t e;
+  const size_t hid = (size_t)B * kHid;
+  DevBuf* f32[] = {&net.pre1, &net.pre2, &net.dpre2, &net.dpre1};
+  for (DevBuf* b : f32)
+    if ((e = b->ensure(hid * 4)) != cudaSuccess) return cuda_check(e, "alloc activations");
+  DevBuf* b16[] = {&net.h1, &net.h2, &net.dh_b, &net.dh_b1};
+  for (DevBuf* b : b16)
+    if ((e = b->ensure(hid * 2)) != cudaSuccess) return cuda_check(e, "alloc activations");
+  if ((e = net.y.ensure((size_t)B * kOutPad * 4)) != cudaSuccess) return cuda_check(e, "alloc outputs");
+  if ((e = net.dy.ensure((size_t)B * kOutPad * 4)) != cudaSuccess) return cuda_check(e, "alloc output grads");
+  if ((e = net.targets.ensure((size_t)B * kOut * 4)) != cudaSuccess) return cuda_check(e, "alloc targets");
+  if ((e = net.loss.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc loss");
+  if ((e = net.errflag.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc flag");
+  net.cap = B;
+  return CRNGPU_OK;
+}
+
+Operand op_f32(const float* p, long long s_row, long long s_k) { return Operand{p, OP_F32, s_row, s_k, 0}; }
+Operand op_bf16(const __nv_bfloat16* p, long long s_row, long long s_k) { return Operand{p, OP_BF16, s_row, s_k, 0}; }
+Operand op_pixels(const uint8_t* p, bool sample_is_row) { return Operand{p, OP_PIXELS, 0, 0, sample_is_row ? 1 : 0}; }
+
+// Each CTA allocates kTmemCols of the SM's 512 tensor-memory columns; an unused dynamic
+// shared-memory reservation brings every CTA to about 57 KB so at most 4 CTAs share an SM and
+// the allocations never wait on each other.
+int gemm(const GemmArgs& g, cudaStream_t s) {
+  static bool attr_done[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !attr_done[dev]) {  // > 48 KB per CTA in total needs the opt-in
+    cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 40 << 10);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, 36 << 10);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 24 << 10);
+    if (e != cudaSuccess) return cuda_check(e, "set k_gemm_tc shared memory");
+    attr_done[dev] = true;
+  }
+  const unsigned gx = (g.M + BM - 1) / BM;
+  if (g.N <= 16) {
+    k_gemm_tc<16><<<dim3(gx, (g.N + 15) / 16), 128, 40 << 10, s>>>(g);
+  } else if (g.N <= 48) {
+    k_gemm_tc<48><<<dim3(gx, (g.N + 47) / 48), 128, 36 << 10, s>>>(g);
+  } else {
+    k_gemm_tc<128><<<dim3(gx, (g.N + 127) / 128), 128, 24 << 10, s>>>(g);
+  }
+  return cuda_check(cudaGetLastError(), "launch k_gemm_tc");
+}
+
+GemmArgs args(Operand a, Operand b, int M, int N, int K, int epi, float* C, __nv_bfloat16* Cb, const float* pre,
+              const float* bias, int ldc, Net& net) {
+  GemmArgs g;
+  g.a = a; g.b = b; g.M = M; g.N = N; g.K = K; g.epi = epi; g.C = C; g.Cb = Cb; g.pre = pre; g.bias = bias; g.ldc = ldc;
+  g.err = static_cast<uint32_t*>(net.errflag.ptr);
+  return g;
+}
+
+// forward over B samples whose pixels are `blocks` (device); y -> net.y [B x 16]
+int forward(Net& net, const uint8_t* blocks, int B, cudaStream_t s) {
+  int rc;
+  float* pre1 = static_cast<float*>(net.pre1.ptr);
+  float* pre2 = static_cast<float*>(net.pre2.ptr);
+  __nv_bfloat16* h1 = static_cast<__nv_bfloat16*>(net.h1.ptr);
+  __nv_bfloat16* h2 = static_cast<__nv_bfloat16*>(net.h2.ptr);
+  // L1: pre1 = X W1^T + b1, h1 = gelu(pre1)
+  if ((rc = gemm(args(op_pixels(blocks, true), op_bf16(static_cast<__nv_bfloat16*>(net.W1.wb.ptr), kIn, 1), B, kHid,
+                      kIn, EPI_BIAS_GELU, pre1, h1, nullptr, static_cast<float*>(net.b1.w.ptr), kHid, net),
+                 s)) != CRNGPU_OK)
+    return rc;
+  if ((rc = gemm(args(op_bf16(h1, kHid, 1), op_bf16(static_cast<__nv_bfloat16*>(net.W2.wb.ptr), kHid, 1), B, kHid,
+                      kHid, EPI_BIAS_GELU, pre2, h2, nullptr, static_cast<float*>(net.b2.w.ptr), kHid, net),
+                 s)) != CRNGPU_OK)
+    return rc;
+  return gemm(args(op_bf16(h2, kHid, 1), op_bf16(static_cast<__nv_bfloat16*>(net.W3.wb.ptr), kHid, 1), B, kOutPad, kHid,
+                   EPI_STORE, static_cast<float*>(net.y.ptr), nullptr, nullptr, static_cast<float*>(net.b3.w.ptr),
+                   kOutPad, net),
+              s);
+}
+
+// gradients of the mean squared error for targets in net.targets; loss -> net.loss
+int backward(Net& net, const uint8_t* blocks, int B, cudaStream_t s) {
+  int rc;
+  float* dy = static_cast<float*>(net.dy.ptr);
+  float* dpre2 = static_cast<float*>(net.dpre2.ptr);
+  float* dpre1 = static_cast<float*>(net.dpre1.ptr);
+  __nv_bfloat16* dhb = static_cast<__nv_bfloat16*>(net.dh_b.ptr);    // bf16 dpre2
+  __nv_bfloat16* dhb1 = static_cast<__nv_bfloat16*>(net.dh_b1.ptr);  // bf16 dpre1 (own buffer: dhb is read meanwhile)
+  cudaMemsetAsync(net.loss.ptr, 0, 4, s);
+  k_loss_grad<<<256, 256, 0, s>>>(static_cast<float*>(net.y.ptr), static_cast<float*>(net.targets.ptr), B, dy,
+                                  static_cast<float*>(net.loss.ptr));
+  // dW3 [16 x 256] = dY^T H2 ; db3 = colsum(dY)
+  if ((rc = gemm(args(op_f32(dy, 1, kOutPad), op_bf16(static_cast<__nv_bfloat16*>(net.h2.ptr), 1, kHid), kOutPad, kHid,
+                      B, EPI_STORE, static_cast<float*>(net.W3.g.ptr), nullptr, nullptr, nullptr, kHid, net),
+                 s)) != CRNGPU_OK)
+    return rc;
+  k_colsum<<<1, kOutPad, 0, s>>>(dy, B, kOutPad, static_cast<float*>(net.b3.g.ptr));
+  // dpre2 = (dY W3) * gelu'(pre2)
+  if ((rc = gemm(args(op_f32(dy, kOutPad, 1), op_f32(static_cast<float*>(net.W3.w.ptr), 1, kHid), B, kHid, kOutPad,
+                      EPI_GELU_GRAD, dpre2, dhb, static_cast<float*>(net.pre2.ptr), nullptr, kHid, net),
+                 s)) != CRNGPU_OK)
+    return rc;
+  // dW2 [256 x 256] = dpre2^T H1 ; db2
+  if ((rc = gemm(args(op_bf16(dhb, 1, kHid), op_bf16(static_cast<__nv_bfloat16*>(net.h1.ptr), 1, kHid), kHid, kHid, B,
+                      EPI_STORE, static_cast<float*>(net.W2.g.ptr), nullptr, nullptr, nullptr, kHid, net),
+                 s)) != CRNGPU_OK)
+    return rc;
+  k_colsum<<<(kHid + 127) / 128, 128, 0, s>>>(dpre2, B, kHid, static_cast<float*>(net.b2.g.ptr));
+  // dpre1 = (dpre2 W2) * gelu'(pre1)
+  if ((rc = gemm(args(op_bf16(dhb, kHid, 1), op_f32(static_cast<float*>(net.W2.w.ptr), 1, kHid), B, kHid, kHid,
+                      EPI_GELU_GRAD, dpre1, dhb1, static_cast<float*>(net.pre1.ptr), nullptr, kHid, net),
+                 s)) != CRNGPU_OK)
+    return rc;
+  // dW1 [256 x 48] = dpre1^T X ; db1
+  if ((rc = gemm(args(op_bf16(dhb1, 1, kHid), op_pixels(blocks, false), kHid, kIn, B, EPI_STORE,
+                      static_cast<float*>(net.W1.g.ptr), nullptr, nullptr, nullptr, kIn, net),
+                 s)) != CRNGPU_OK)
+    return rc;
+  k_colsum<<<(kHid + 127) / 128, 128, 0, s>>>(dpre1, B, kHid, static_cast<float*>(net.b1.g.ptr));
+  return cuda_check(cudaGetLastError(), "backward kernels");
+}
+
+int check_flag(Net& net, cudaStream_t s) {
+  uint32_t f = 0;
+  cudaError_t e = cudaMemcpyAsync(&f, net.errflag.ptr, 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_check(e, "read mma status");
+  if (f) { set_error("tensor-core wait timed out"); return CRNGPU_E_DEVICE; }
+  return CRNGPU_OK;
+}
+
+}  // namespace mlp
+}  // namespace crngpu
+
+using namespace crngpu;
+using namespace crngpu::mlp;
+
+extern "C" void* crngpu_mlp_create(uint64_t seed) {
+  clear_error();
+  Net* net = new Net();
+  cudaGetDevice(&net->device);
+  std::mt19937_64 rng(seed);
+  auto init = [&](Param& p, int rows, int cols, int rows_live, bool is_bias, int fan_in) {
+    if (alloc_param(p, rows, cols, rows_live, !is_bias) != CRNGPU_OK) return false;
+    std::vector<float> h(p.n(), 0.f);
+    if (!is_bias) {
+      const float bound = std::sqrt(6.0f / (float)fan_in) * 0.5f;
+      std::uniform_real_distribution<float> u(-bound, bound);
+      for (int r = 0; r < rows_live; r++)
+        for (int c = 0; c < cols; c++) h[(size_t)r * cols + c] = u(rng);
+    }
+    return upload(p, h) == CRNGPU_OK;
+  };
+  if (!init(net->W1, kHid, kIn, kHid, false, kIn) || !init(net->b1, 1, kHid, 1, true, 1) ||
+      !init(net->W2, kHid, kHid, kHid, false, kHid) || !init(net->b2, 1, kHid, 1, true, 1) ||
+      !init(net->W3, kOutPad, kHid, 7, false, kHid) || !init(net->b3, 1, kOutPad, 1, true, 1)) {
+    delete net;
+    return nullptr;
+  }
+  cudaDeviceSynchronize();
+  return net;
+}
+
+extern "C" int crngpu_mlp_destroy(void* h) {
+  Net* net = static_cast<Net*>(h);
+  if (!net || net->magic != 0x4D4C5030u) return CRNGPU_E_PARAM;
+  net->magic = 0;
+  delete net;
+  return CRNGPU_OK;
+}
+
+// Parameter access for checkpoints and gradient checks. which: 0 W1, 1 b1, 2 W2, 3 b2, 4 W3, 5 b3;
+// what: 0 weights, 1 gradients. count = number of floats in the buffer.
+extern "C" int crngpu_mlp_param(void* h, int which, int what, float* host, uint32_t count, int write) {
+  Net* net = static_cast<Net*>(h);
+  if (!net || net->magic != 0x4D4C5030u || which < 0 || which > 5 || !host) return CRNGPU_E_PARAM;
+  Param* p = net->params()[which];
+  if (count != p->n()) { set_error("size mismatch"); return CRNGPU_E_PARAM; }
+  void* dev = what ? p->g.ptr : p->w.ptr;
+  if (write) {
+    std::vector<float> v(host, host + count);
+    if (what == 0) return upload(*p, v);
+    return cuda_check(cudaMemcpy(dev, host, count * 4, cudaMemcpyHostToDevice), "write param");
+  }
+  return cuda_check(cudaMemcpy(host, dev, count * 4, cudaMemcpyDeviceToHost), "read param");
+}
+
+// Forward pass over n blocks (device RGBA8, n x 64) -> y (device, n x 16 fp32).
+extern "C" int crngpu_mlp_forward(void* h, const uint8_t* d_blocks, uint32_t n, float* d_y, void* stream) {
+  clear_error();
+  Net* net = static_cast<Net*>(h);
+  if (!net || net->magic != 0x4D4C5030u || !d_blocks || !d_y) return CRNGPU_E_PARAM;
+  cudaStream_t s = as_stream(stream);
+  int rc = ensure_batch(*net, (int)n);
+  if (rc != CRNGPU_OK) return rc;
+  cudaMemsetAsync(net->errflag.ptr, 0, 4, s);
+  if ((rc = forward(*net, d_blocks, (int)n, s)) != CRNGPU_OK) return rc;
+  cudaMemcpyAsync(d_y, net->y.ptr, (size_t)n * kOutPad * 4, cudaMemcpyDeviceToDevice, s);
+  return check_flag(*net, s);
+}
+
+// Gradients of the loss for n blocks and targets (device, n x 8 fp32) into the gradient buffers;
+// *loss (host) receives the loss. Does not update the weights.
+extern "C" int crngpu_mlp_gradients(void* h, const uint8_t* d_blocks, const float* d_targets, uint32_t n, float* loss,
+                                    void* stream) {
+  clear_error();
+  Net* net = static_cast<Net*>(h);
+  if (!net || net->magic != 0x4D4C5030u || !d_blocks || !d_targets || !n) return CRNGPU_E_PARAM;
+  cudaStream_t s = as_stream(stream);
+  int rc = ensure_batch(*net, (int)n);
+  if (rc != CRNGPU_OK) return rc;
+  cudaMemsetAsync(net->errflag.ptr, 0, 4, s);
+  cudaMemcpyAsync(net->targets.ptr, d_targets, (size_t)n * kOut * 4, cudaMemcpyDeviceToDevice, s);
+  if ((rc = forward(*net, d_blocks, (int)n, s)) != CRNGPU_OK) return rc;
+  if ((rc = backward(*net, d_blocks, (int)n, s)) != CRNGPU_OK) return rc;
+  if (loss) cudaMemcpyAsync(loss, net->loss.ptr, 4, cudaMemcpyDeviceToHost, s);
+  return check_flag(*net, s);
+}
+
+// One AdamW step (betas 0.9/0.999, eps 1e-8) on a batch: forward, backward, update.
+extern "C" int crngpu_mlp_train_step(void* h, const uint8_t* d_blocks, const float* d_targets, uint32_t n, float lr,
+                                     float weight_decay, float* loss, void* stream) {
+  int rc = crngpu_mlp_gradients(h, d_blocks, d_targets, n, loss, stream);
+  if (rc != CRNGPU_OK) return rc;
+  Net* net = static_cast<Net*>(h);
+  cudaStream_t s = as_stream(stream);
+  net->step++;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float bc1 = 1.f - std::pow(b1, (float)net->step), bc2 = 1.f - std::pow(b2, (float)net->step);
+  for (Param* p : net->params()) {
+    const bool is_bias = p->rows == 1;
+    k_adamw<<<64, 256, 0, s>>>(static_cast<float*>(p->w.ptr), static_cast<float*>(p->g.ptr),
+                               static_cast<float*>(p->m.ptr), static_cast<float*>(p->v.ptr),
+                               static_cast<__nv_bfloat16*>(p->wb.ptr), (int)p->n(), lr, b1, b2, 1e-8f,
+                               is_bias ? 0.f : weight_decay, bc1, bc2, is_bias ? 1 : p->rows_live, p->cols);
+  }
+  return cuda_check(cudaGetLastError(), "launch k_adamw");
+}
+
+// Training targets from plain-optimizer output (device): blocks8 (n x 8) + errors (n) -> n x 8.
+extern "C" int crngpu_mlp_make_targets(const uint8_t* d_blocks8, const uint64_t* d_err, uint32_t n, float* d_targets,
+                                       void* stream) {
+  if (!d_blocks8 || !d_err || !d_targets) return CRNGPU_E_PARAM;
+  k_make_targets<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, as_stream(stream)>>>(d_blocks8, d_err,
+                                                                                                  (int)n, d_targets);
+  return cuda_check(cudaGetLastError(), "launch k_make_targets");
+}
+
+// Learned DXT1 encode of n blocks (device RGBA8 in, device dxt1 out): MLP proposal, one
+// selector refit, and the exact optimizer for blocks whose error exceeds threshold x the
+// predicted bound. *fallbacks (host, optional) receives how many blocks fell back.
+extern "C" int crngpu_dxt1_learned(void* h, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
+                                   uint8_t* d_out, uint32_t* fallbacks, void* stream) {
+  clear_error();
+  Net* net = static_cast<Net*>(h);
+  if (!net || net->magic != 0x4D4C5030u || !d_blocks || !d_out) return CRNGPU_E_PARAM;
+  if (!n) return CRNGPU_OK;
+  cudaStream_t s = as_stream(stream);
+  const uint32_t chunk = 1u << 18;
+  int rc = ensure_batch(*net, (int)(n < chunk ? n : chunk));
+  if (rc != CRNGPU_OK) return rc;
+  cudaError_t e;
+  if ((e = net->fb_idx.ensure((size_t)(n < chunk ? n : chunk) * 4)) != cudaSuccess) return cuda_check(e, "alloc fallback list");
+  if ((e = net->fb_count.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc fallback count");
+  cudaMemsetAsync(net->fb_count.ptr, 0, 4, s);
+  cudaMemsetAsync(net->errflag.ptr, 0, 4, s);
+  if (fallbacks) *fallbacks = 0;
+  for (uint32_t c0 = 0; c0 < n; c0 += chunk) {
+    const uint32_t cn = n - c0 < chunk ? n - c0 : chunk;
+    const uint8_t* in = d_blocks + (size_t)c0 * 64;
+    uint8_t* out = d_out + (size_t)c0 * 8;
+    uint32_t* idx = static_cast<uint32_t*>(net->fb_idx.ptr);
+    uint32_t* cnt_d = static_cast<uint32_t*>(net->fb_count.ptr);
+    cudaMemsetAsync(cnt_d, 0, 4, s);
+    if ((rc = forward(*net, in, (int)cn, s)) != CRNGPU_OK) return rc;
+    k_learned_refit<<<(cn + 127) / 128, 128, 0, s>>>(in, static_cast<float*>(net->y.ptr), (int)cn, perceptual, out,
+                                                      idx, cnt_d, threshold);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_learned_refit");
+    uint32_t cnt = 0;
+    if ((e = cudaMemcpyAsync(&cnt, cnt_d, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+      return cuda_check(e, "read fallback count");
+    if (fallbacks) *fallbacks += cnt;
+    if (!cnt) continue;
+    // blocks above the bound: the exact optimizer, on a compacted copy, scattered back
+    if ((e = net->fb_in.ensure((size_t)cnt * 64)) != cudaSuccess) return cuda_check(e, "alloc fallback blocks");
+    if ((e = net->fb_out.ensure((size_t)cnt * 8)) != cudaSuccess) return cuda_check(e, "alloc fallback out");
+    k_gather_idx<<<(cnt * 4 + 255) / 256, 256, 0, s>>>(in, idx, cnt_d, static_cast<uint8_t*>(net->fb_in.ptr));
+    if ((rc = launch_dxt1(static_cast<uint8_t*>(net->fb_in.ptr), cnt, perceptual != 0, true,
+                          static_cast<uint8_t*>(net->fb_out.ptr), 8, nullptr, s)) != CRNGPU_OK)
+      return rc;
+    k_scatter_idx<<<(cnt + 255) / 256, 256, 0, s>>>(static_cast<uint8_t*>(net->fb_out.ptr), idx, cnt_d, out);
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "learned encode kernels");
+  return check_flag(*net, s);
+}

@@ -143,3 +143,59 @@ def image_blocks(img: np.ndarray) -> np.ndarray:
     xs = np.minimum(np.arange(bx * 4), w - 1)
     full = img[ys][:, xs]
     return np.ascontiguousarray(full.reshape(by, 4, bx, 4, 4).transpose(0, 2, 1, 3, 4).reshape(by * bx, 64))
+
+
+def colour_texture_torch(w: int, h: int, seed: int, device="cuda"):
+    """Same recipe as colour_texture (4-octave value noise, period 64, + 40 flat rectangles,
+    alpha 255) computed on the GPU in float32 for large training/evaluation sets. Seeded and
+    deterministic on a given device; not bit-identical to the numpy version."""
+    import torch
+    M = 0xFFFFFFFF
+
+    def h32(*keys):
+        x = torch.full_like(keys[-1], 0x9E3779B9) if torch.is_tensor(keys[-1]) else torch.tensor(0x9E3779B9)
+        for k in keys:
+            k = k if torch.is_tensor(k) else torch.tensor(k, dtype=torch.int64, device=device)
+            x = (x ^ (k & M)) & M
+            x = (x * 0x85EBCA6B) & M
+            x = x ^ (x >> 13)
+            x = (x * 0xC2B2AE35) & M
+            x = x ^ (x >> 16)
+        return x
+
+    ys = torch.arange(h, device=device, dtype=torch.int64).view(h, 1).expand(h, w)
+    xs = torch.arange(w, device=device, dtype=torch.int64).view(1, w).expand(h, w)
+    img = torch.empty((h, w, 4), dtype=torch.uint8, device=device)
+    for c in range(3):
+        total = torch.zeros((h, w), dtype=torch.float32, device=device)
+        amp, norm, p = 1.0, 0.0, 64.0
+        for o in range(4):
+            fx, fy = xs.float() / p, ys.float() / p
+            ix, iy = fx.floor().long(), fy.floor().long()
+            tx, ty = fx - ix, fy - iy
+            tx = tx * tx * (3 - 2 * tx)
+            ty = ty * ty * (3 - 2 * ty)
+            u = lambda a, b: h32(seed, c, o, a, b).float() / 4294967296.0
+            v00, v10, v01, v11 = u(ix, iy), u(ix + 1, iy), u(ix, iy + 1), u(ix + 1, iy + 1)
+            a = v00 + (v10 - v00) * tx
+            b = v01 + (v11 - v01) * tx
+            total += amp * (a + (b - a) * ty)
+            norm += amp
+            amp *= 0.5
+            p = max(p / 2, 1.0)
+        img[:, :, c] = (total / norm * 255 + 0.5).floor().clamp(0, 255).to(torch.uint8)
+    img[:, :, 3] = 255
+    r = h32(seed, 1000 + torch.arange(40 * 7, device=device)).view(40, 7).cpu().tolist()
+    for i in range(40):
+        rw, rh = 4 + r[i][0] % 61, 4 + r[i][1] % 61
+        x0, y0 = r[i][2] % w, r[i][3] % h
+        img[y0:y0 + rh, x0:x0 + rw, 0] = r[i][4] & 255
+        img[y0:y0 + rh, x0:x0 + rw, 1] = r[i][5] & 255
+        img[y0:y0 + rh, x0:x0 + rw, 2] = r[i][6] & 255
+    return img
+
+
+def image_blocks_torch(img):
+    """(h, w, 4) uint8 torch tensor (dimensions multiples of 4) -> (n, 64) blocks, row-major."""
+    h, w = img.shape[0], img.shape[1]
+    return img.view(h // 4, 4, w // 4, 4, 4).permute(0, 2, 1, 3, 4).reshape(-1, 64).contiguous()

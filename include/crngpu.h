@@ -106,6 +106,43 @@ CRNGPU_API int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, ui
                               void* stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Learned DXT1 endpoint proposal (no counterpart in the reference). A 48 -> 256 -> 256 -> 8 MLP
+ * (GELU, BF16 weights, FP32 accumulation on tcgen05 tensor cores) predicts the endpoints the
+ * plain optimizer would choose and the error it would reach; the learned encode keeps the
+ * prediction after one selector refit unless its error exceeds threshold x that predicted bound,
+ * in which case the block goes through crngpu_dxt1_optimize_batch's exact search.
+ * All block/target/output pointers are device memory.
+ * --------------------------------------------------------------------------------------- */
+
+/* Creates a network with seeded random weights on the current device; NULL on failure. */
+CRNGPU_API void* crngpu_mlp_create(uint64_t seed);
+CRNGPU_API int crngpu_mlp_destroy(void* net);
+
+/* Reads (write = 0) or writes (write = 1) parameter `which` (0 W1[256x48], 1 b1[256], 2 W2[256x256],
+ * 3 b2[256], 4 W3[16x256] (rows 7..15 stay zero), 5 b3[16]); what: 0 = weights, 1 = gradients. */
+CRNGPU_API int crngpu_mlp_param(void* net, int which, int what, float* host, uint32_t count, int write);
+
+/* Forward pass: n RGBA8 blocks (n x 64) -> outputs y (n x 16 fp32; columns 0..6 used). */
+CRNGPU_API int crngpu_mlp_forward(void* net, const uint8_t* d_blocks, uint32_t n, float* d_y, void* stream);
+
+/* Training targets from plain-optimizer results: blocks8 (n x 8) and errors (n) -> n x 8 fp32. */
+CRNGPU_API int crngpu_mlp_make_targets(const uint8_t* d_blocks8, const uint64_t* d_err, uint32_t n,
+                                       float* d_targets, void* stream);
+
+/* Mean-squared-error gradients for a batch into the gradient buffers; *loss (host) gets the loss. */
+CRNGPU_API int crngpu_mlp_gradients(void* net, const uint8_t* d_blocks, const float* d_targets, uint32_t n,
+                                    float* loss, void* stream);
+
+/* One AdamW step (betas 0.9/0.999, eps 1e-8, decoupled weight decay) on a batch. */
+CRNGPU_API int crngpu_mlp_train_step(void* net, const uint8_t* d_blocks, const float* d_targets, uint32_t n,
+                                     float lr, float weight_decay, float* loss, void* stream);
+
+/* Learned DXT1 encode of n blocks (4-colour blocks; fallback blocks use the exact optimizer).
+ * *fallbacks (host, optional) receives the number of blocks that fell back. */
+CRNGPU_API int crngpu_dxt1_learned(void* net, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
+                                   uint8_t* d_out, uint32_t* fallbacks, void* stream);
+
+/* ------------------------------------------------------------------------------------------
  * CRN -> DXTn transcoder (crnd::crn_unpacker, inc/crn_decomp.h:3498-4223; API inc/crn_defs.h:
  * 174-205). Supported: DXT1, DXT5 family, DXN_XY/YX, DXT5A. ETC formats: CRNGPU_E_UNSUPPORTED.
  * --------------------------------------------------------------------------------------- */
