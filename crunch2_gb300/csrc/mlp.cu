@@ -8,7 +8,9 @@
 // b/31) of the plain optimizer's 4-colour solution, y[6] = log2(1 + block error)/16, the
 // network's prediction of the error the plain optimizer reaches (the fallback bound); y[7] unused.
 //
-// All GEMMs go through k_gemm_tc: C[M x N] = sum_k A(m, k) B(n, k), a 128 x BN tile per CTA,
+// Inference (crngpu_mlp_forward, the learned encode) runs as one fused persistent kernel,
+// k_mlp_infer: weights resident in shared memory, activations kept on the SM.
+// Training GEMMs go through k_gemm_tc: C[M x N] = sum_k A(m, k) B(n, k), a 128 x BN tile per CTA,
 // K staged 64 at a time into shared memory in the no-swizzle K-major core-matrix layout
 // (8 x 8 BF16 core matrices, 128 bytes each), four K=16 MMAs per stage issued by one thread,
 // completion through tcgen05.commit on an mbarrier (bounded wait), epilogue from TMEM with
@@ -222,6 +224,211 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
 }
 
 // ------------------------------------------------------------------------------------------
+// Fused inference: the whole 48 -> 256 -> 256 -> 16 forward pass of 128 blocks per tile in one
+// persistent CTA per SM. All weights stay in shared memory in the K-major core-matrix layout
+// (W2 128 KB, W1 24 KB, W3 8 KB); the activations of a tile never leave the SM: input features
+// and hidden layers go through one 64 KB shared-memory tile (features alias its first 12 KB),
+// accumulators through 256 TMEM columns reused by all three layers. Same arithmetic as the
+// training forward (bf16 operands, fp32 accumulation, bias + tanh-GELU in fp32, bf16 hidden).
+constexpr int kInferThreads = 256;
+constexpr uint32_t kSmW2 = 0, kSmW1 = kSmW2 + kHid * kHid * 2, kSmW3 = kSmW1 + kHid * kIn * 2,
+                   kSmH = kSmW3 + kOutPad * kHid * 2, kSmB1 = kSmH + BM * kHid * 2, kSmB2 = kSmB1 + kHid * 4,
+                   kSmB3 = kSmB2 + kHid * 4, kSmBar = kSmB3 + kOutPad * 4, kSmTmem = kSmBar + 8,
+                   kInferSmem = kSmTmem + 8;
+static_assert(kInferSmem <= 232448, "fused forward exceeds the 227 KB shared-memory limit");
+
+// byte offset of the 16-byte row segment (row r, K-group kg) in a K-major tile with kt K-columns
+__device__ __forceinline__ uint32_t kseg(int r, int kg, int kt) {
+  return (uint32_t)((r >> 3) * ((kt >> 3) * 128) + kg * 128 + (r & 7) * 16);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+  asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+               "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+               "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;");
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);  // .x = a (low half), .y = b
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// hidden-layer epilogue: TMEM accumulators of this thread's row, columns [c_lo, c_lo + 128),
+// + bias, GELU, bf16 into the K-major hidden tile
+__device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int quarter, int row, int c_lo, const float* bias,
+                                                unsigned char* sH) {
+#pragma unroll 1
+  for (int c0 = c_lo; c0 < c_lo + 128; c0 += 16) {
+    uint32_t r[16];
+    tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0, r);
+    uint32_t w[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const float a = gelu(__uint_as_float(r[2 * j]) + bias[c0 + 2 * j]);
+      const float b = gelu(__uint_as_float(r[2 * j + 1]) + bias[c0 + 2 * j + 1]);
+      w[j] = pack_bf16(a, b);
+    }
+    *reinterpret_cast<uint4*>(sH + kseg(row, c0 >> 3, kHid)) = make_uint4(w[0], w[1], w[2], w[3]);
+    *reinterpret_cast<uint4*>(sH + kseg(row, (c0 >> 3) + 1, kHid)) = make_uint4(w[4], w[5], w[6], w[7]);
+  }
+}
+
+// Waits for the tcgen05.commit of this phase; false (uniform across the CTA) on timeout, after a
+// second bounded wait so the tensor core is done with shared memory and TMEM before the caller exits.
+__device__ __forceinline__ bool tile_wait(uint32_t bar, uint32_t phase) {
+  const bool done = mbar_wait(bar, phase);
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  if (__syncthreads_and(done)) return true;
+  mbar_wait(bar, phase);
+  return false;
+}
+
+__global__ void __launch_bounds__(kInferThreads, 1)
+    k_mlp_infer(const uint8_t* __restrict__ blocks, int n, const __nv_bfloat16* __restrict__ W1,
+                const __nv_bfloat16* __restrict__ W2, const __nv_bfloat16* __restrict__ W3,
+                const float* __restrict__ b1, const float* __restrict__ b2, const float* __restrict__ b3,
+                float* __restrict__ y, uint32_t* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char* sW1 = sm + kSmW1;
+  unsigned char* sW2 = sm + kSmW2;
+  unsigned char* sW3 = sm + kSmW3;
+  unsigned char* sH = sm + kSmH;  // features (first 12 KB) / hidden layer of the current tile
+  float* sB1 = reinterpret_cast<float*>(sm + kSmB1);
+  float* sB2 = reinterpret_cast<float*>(sm + kSmB2);
+  float* sB3 = reinterpret_cast<float*>(sm + kSmB3);
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + kSmBar);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + kSmTmem);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  // weights (row-major bf16 [rows x K]) -> K-major core matrices, 16 bytes at a time
+  for (int e = tid; e < kHid * (kHid / 8); e += kInferThreads) {
+    const int r = e >> 5, kg = e & 31;
+    *reinterpret_cast<uint4*>(sW2 + kseg(r, kg, kHid)) = __ldg(reinterpret_cast<const uint4*>(W2 + r * kHid + kg * 8));
+  }
+  for (int e = tid; e < kHid * (kIn / 8); e += kInferThreads) {
+    const int r = e / (kIn / 8), kg = e % (kIn / 8);
+    *reinterpret_cast<uint4*>(sW1 + kseg(r, kg, kIn)) = __ldg(reinterpret_cast<const uint4*>(W1 + r * kIn + kg * 8));
+  }
+  for (int e = tid; e < kOutPad * (kHid / 8); e += kInferThreads) {
+    const int r = e >> 5, kg = e & 31;
+    *reinterpret_cast<uint4*>(sW3 + kseg(r, kg, kHid)) = __ldg(reinterpret_cast<const uint4*>(W3 + r * kHid + kg * 8));
+  }
+  for (int e = tid; e < kHid; e += kInferThreads) { sB1[e] = b1[e]; sB2[e] = b2[e]; }
+  if (tid < kOutPad) sB3[tid] = b3[tid];
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;" ::"r"(smem_u32(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)));
+  asm volatile("fence.proxy.async.shared::cta;");
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t bar = smem_u32(mbar);
+  const uint32_t id256 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kHid >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+  const uint32_t id16 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kOutPad >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+  const uint32_t aH = smem_u32(sH), aW1 = smem_u32(sW1), aW2 = smem_u32(sW2), aW3 = smem_u32(sW3);
+  const int quarter = warp & 3, half = warp >> 2;
+  const int erow = quarter * 32 + lane;  // the tile row whose accumulators this thread reads
+  uint32_t phase = 0;
+  bool ok = true;
+  const int ntiles = (n + BM - 1) / BM;
+#pragma unroll 1
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long row0 = (long long)tile * BM;
+    {  // features: thread (row, half) converts texels 8*half .. 8*half+7 (24 features, 3 K-groups)
+      const int r = tid & (BM - 1), hf = tid >> 7;
+      uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
+      if (row0 + r < n) {
+        const uint4* src = reinterpret_cast<const uint4*>(blocks + (row0 + r) * 64 + hf * 32);
+        v0 = __ldg(src);
+        v1 = __ldg(src + 1);
+      }
+      const uint32_t px[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+      float f[24];
+#pragma unroll
+      for (int t = 0; t < 8; t++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) f[t * 3 + c] = (float)((px[t] >> (8 * c)) & 255u) * (1.0f / 255.0f);
+#pragma unroll
+      for (int g = 0; g < 3; g++)
+        *reinterpret_cast<uint4*>(sH + kseg(r, hf * 3 + g, kIn)) =
+            make_uint4(pack_bf16(f[g * 8], f[g * 8 + 1]), pack_bf16(f[g * 8 + 2], f[g * 8 + 3]),
+                       pack_bf16(f[g * 8 + 4], f[g * 8 + 5]), pack_bf16(f[g * 8 + 6], f[g * 8 + 7]));
+    }
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid == 0) {  // layer 1: [128 x 48] x [48 x 256]
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int ks = 0; ks < kIn / 16; ks++)
+        mma_bf16(tmem, make_desc(aH + ks * 256, 128, (kIn / 8) * 128), make_desc(aW1 + ks * 256, 128, (kIn / 8) * 128),
+                 id256, ks > 0);
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
+    }
+    if (!(ok = tile_wait(bar, phase))) break;
+    phase ^= 1;
+    hidden_epilogue(tmem, quarter, erow, half * 128, sB1, sH);
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid == 0) {  // layer 2: [128 x 256] x [256 x 256]
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int ks = 0; ks < kHid / 16; ks++)
+        mma_bf16(tmem, make_desc(aH + ks * 256, 128, (kHid / 8) * 128), make_desc(aW2 + ks * 256, 128, (kHid / 8) * 128),
+                 id256, ks > 0);
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
+    }
+    if (!(ok = tile_wait(bar, phase))) break;
+    phase ^= 1;
+    hidden_epilogue(tmem, quarter, erow, half * 128, sB2, sH);
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (tid == 0) {  // layer 3: [128 x 256] x [256 x 16]
+      asm volatile("tcgen05.fence::after_thread_sync;");
+#pragma unroll
+      for (int ks = 0; ks < kHid / 16; ks++)
+        mma_bf16(tmem, make_desc(aH + ks * 256, 128, (kHid / 8) * 128), make_desc(aW3 + ks * 256, 128, (kHid / 8) * 128),
+                 id16, ks > 0);
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar));
+    }
+    if (!(ok = tile_wait(bar, phase))) break;
+    phase ^= 1;
+    if (half == 0) {
+      uint32_t r[16];
+      tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16), r);
+      if (row0 + erow < n) {
+        float4* dst = reinterpret_cast<float4*>(y + (row0 + erow) * kOutPad);
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+          dst[q] = make_float4(__uint_as_float(r[4 * q]) + sB3[4 * q], __uint_as_float(r[4 * q + 1]) + sB3[4 * q + 1],
+                               __uint_as_float(r[4 * q + 2]) + sB3[4 * q + 2],
+                               __uint_as_float(r[4 * q + 3]) + sB3[4 * q + 3]);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();  // TMEM columns and the feature tile are reused by the next tile
+  }
+  if (!ok && tid == 0) atomicExch(err, 1u);
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tmem));
+}
+
+// ------------------------------------------------------------------------------------------
 // elementwise / reduction kernels
 
 // dY = 2 (y - t) / B on the 7 trained outputs; loss partial sums
@@ -287,31 +494,41 @@ __global__ void k_make_targets(const uint8_t* __restrict__ blocks8, const uint64
 
 // Learned encode, per block: quantise the predicted endpoints, choose selectors, refit the
 // endpoints by least squares from those selectors (refine_solution level 0,
-// crnlib/crn_dxt1.cpp:525-600), choose selectors again, and keep the block unless its error is
-// above 1.5x the network's predicted bound; those blocks are queued for the exact optimizer.
+// crnlib/crn_dxt1.cpp:525-600), polish with a short greedy search of +-1 steps on the six
+// endpoint components, check the 3-colour block on the same endpoints, and keep the block unless
+// its error is above `threshold` x the network's predicted bound; those blocks are queued for the
+// exact optimizer.
 __device__ __forceinline__ int q565(float v, int hi) {
   int x = __float2int_rn(v * (float)hi);
   return x < 0 ? 0 : (x > hi ? hi : x);
 }
-__device__ uint32_t block_error(const uint32_t* px, uint32_t lo, uint32_t hi, bool perceptual, uint32_t* sel_out) {
+__device__ __forceinline__ void expand565(uint32_t c, int* o) {
+  const int r = c >> 11, g = (c >> 5) & 63, b = c & 31;
+  o[0] = (r << 3) | (r >> 2); o[1] = (g << 2) | (g >> 4); o[2] = (b << 3) | (b >> 2);
+}
+// error of the 4-colour (three = false) or 3-colour palette of (lo, hi); selectors in 2-bit slots
+__device__ uint32_t block_error(const uint32_t* px, uint32_t lo, uint32_t hi, bool perceptual, bool three,
+                                uint32_t* sel_out) {
   int c[4][3];
-  const int r0 = ((lo >> 11) << 3) | (lo >> 13), g0 = (((lo >> 5) & 63) << 2) | (((lo >> 5) & 63) >> 4),
-            b0 = ((lo & 31) << 3) | ((lo & 31) >> 2);
-  const int r1 = ((hi >> 11) << 3) | (hi >> 13), g1 = (((hi >> 5) & 63) << 2) | (((hi >> 5) & 63) >> 4),
-            b1 = ((hi & 31) << 3) | ((hi & 31) >> 2);
-  c[0][0] = r0; c[0][1] = g0; c[0][2] = b0;
-  c[1][0] = r1; c[1][1] = g1; c[1][2] = b1;
+  expand565(lo, c[0]);
+  expand565(hi, c[1]);
   for (int k = 0; k < 3; k++) {
-    c[2][k] = (c[0][k] * 2 + c[1][k]) / 3;
-    c[3][k] = (c[1][k] * 2 + c[0][k]) / 3;
+    if (three) {
+      c[2][k] = (c[0][k] + c[1][k]) >> 1;
+    } else {
+      c[2][k] = (c[0][k] * 2 + c[1][k]) / 3;
+      c[3][k] = (c[1][k] * 2 + c[0][k]) / 3;
+    }
   }
+  const int nk = three ? 3 : 4;
   const int wr = perceptual ? 8 : 1, wg = perceptual ? 25 : 1;
   uint32_t err = 0, sel = 0;
+#pragma unroll 4
   for (int p = 0; p < 16; p++) {
     const int r = px[p] & 255, g = (px[p] >> 8) & 255, b = (px[p] >> 16) & 255;
     uint32_t best = 0xFFFFFFFFu;
     int bi = 0;
-    for (int k = 0; k < 4; k++) {
+    for (int k = 0; k < nk; k++) {
       const int dr = r - c[k][0], dg = g - c[k][1], db = b - c[k][2];
       const uint32_t d = (uint32_t)(wr * dr * dr + wg * dg * dg + db * db);
       if (d < best) { best = d; bi = k; }
@@ -323,29 +540,31 @@ __device__ uint32_t block_error(const uint32_t* px, uint32_t lo, uint32_t hi, bo
   return err;
 }
 
-__global__ void k_learned_refit(const uint8_t* __restrict__ blocks, const float* __restrict__ y, int n, int perceptual,
-                                uint8_t* __restrict__ out, uint32_t* __restrict__ fallback, uint32_t* __restrict__ nfall,
-                                float threshold) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+// y holds the proposals of blocks base .. base + n - 1; indices written to `fallback` are batch-wide
+__global__ void k_learned_refit(const uint8_t* __restrict__ blocks, const float* __restrict__ y, uint32_t base, int n,
+                                int perceptual, uint8_t* __restrict__ out, uint32_t* __restrict__ fallback,
+                                uint32_t* __restrict__ nfall, float threshold) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const long long i = (long long)base + j;
     uint32_t px[16];
-    const uint4* p4 = reinterpret_cast<const uint4*>(blocks + (long long)i * 64);
+    const uint4* p4 = reinterpret_cast<const uint4*>(blocks + i * 64);
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       const uint4 v = __ldg(p4 + q);
       px[4 * q] = v.x; px[4 * q + 1] = v.y; px[4 * q + 2] = v.z; px[4 * q + 3] = v.w;
     }
-    const float* yi = y + (long long)i * kOutPad;
-    uint32_t lo = (uint32_t)((q565(yi[0], 31) << 11) | (q565(yi[1], 63) << 5) | q565(yi[2], 31));
-    uint32_t hi = (uint32_t)((q565(yi[3], 31) << 11) | (q565(yi[4], 63) << 5) | q565(yi[5], 31));
+    const bool perc = perceptual != 0;
+    const float* yi = y + (long long)j * kOutPad;
+    int e[6] = {q565(yi[0], 31), q565(yi[1], 63), q565(yi[2], 31), q565(yi[3], 31), q565(yi[4], 63), q565(yi[5], 31)};
+    auto pk = [](const int* v) { return (uint32_t)((v[0] << 11) | (v[1] << 5) | v[2]); };
     uint32_t sel;
-    uint32_t err = block_error(px, lo, hi, perceptual != 0, &sel);
-    // least-squares refit from the selectors (points at 0, 1/3, 2/3, 1 between low and high)
+    uint32_t err = block_error(px, pk(e), pk(e + 3), perc, false, &sel);
+    // least-squares refit from the selectors (points at 1, 0, 2/3, 1/3 of the low endpoint)
     {
       float aa = 0.f, ab = 0.f, bb = 0.f, ax[3] = {0, 0, 0}, bx[3] = {0, 0, 0};
-      static const float wlow[4] = {1.f, 0.f, 2.f / 3.f, 1.f / 3.f};
+      const float wlow[4] = {1.f, 0.f, 2.f / 3.f, 1.f / 3.f};
       for (int p = 0; p < 16; p++) {
-        const int s = (sel >> (2 * p)) & 3;
-        const float a = wlow[s], b = 1.f - a;
+        const float a = wlow[(sel >> (2 * p)) & 3], b = 1.f - a;
         aa += a * a; ab += a * b; bb += b * b;
         const float x[3] = {(float)(px[p] & 255), (float)((px[p] >> 8) & 255), (float)((px[p] >> 16) & 255)};
         for (int k = 0; k < 3; k++) { ax[k] += a * x[k]; bx[k] += b * x[k]; }
@@ -353,32 +572,59 @@ __global__ void k_learned_refit(const uint8_t* __restrict__ blocks, const float*
       const float det = aa * bb - ab * ab;
       if (fabsf(det) > 1e-6f) {
         const float inv = 1.f / det;
-        float e0[3], e1[3];
+        const int lim[3] = {31, 63, 31};
+        int f[6];
         for (int k = 0; k < 3; k++) {
-          e0[k] = (ax[k] * bb - bx[k] * ab) * inv;
-          e1[k] = (bx[k] * aa - ax[k] * ab) * inv;
+          f[k] = q565((ax[k] * bb - bx[k] * ab) * inv / 255.f, lim[k]);
+          f[3 + k] = q565((bx[k] * aa - ax[k] * ab) * inv / 255.f, lim[k]);
         }
-        const uint32_t nlo = (uint32_t)((q565(e0[0] / 255.f, 31) << 11) | (q565(e0[1] / 255.f, 63) << 5) |
-                                        q565(e0[2] / 255.f, 31));
-        const uint32_t nhi = (uint32_t)((q565(e1[0] / 255.f, 31) << 11) | (q565(e1[1] / 255.f, 63) << 5) |
-                                        q565(e1[2] / 255.f, 31));
         uint32_t nsel;
-        const uint32_t nerr = block_error(px, nlo, nhi, perceptual != 0, &nsel);
-        if (nerr < err) { err = nerr; lo = nlo; hi = nhi; sel = nsel; }
+        const uint32_t nerr = block_error(px, pk(f), pk(f + 3), perc, false, &nsel);
+        if (nerr < err) { err = nerr; sel = nsel; for (int k = 0; k < 6; k++) e[k] = f[k]; }
       }
     }
-    // a 4-colour block needs low > high; swap (and remap selectors 0<->1, 2<->3) or break ties
+    // greedy polish: two rounds of the best single +-1 move over the six components
+#pragma unroll 1
+    for (int round = 0; round < 2; round++) {
+      int best_k = -1, best_d = 0;
+      uint32_t best_err = err, best_sel = sel;
+#pragma unroll 1
+      for (int k = 0; k < 6; k++) {
+        const int lim = (k % 3) == 1 ? 63 : 31;
+        for (int d = -1; d <= 1; d += 2) {
+          const int v = e[k] + d;
+          if (v < 0 || v > lim) continue;
+          int f[6] = {e[0], e[1], e[2], e[3], e[4], e[5]};
+          f[k] = v;
+          uint32_t nsel;
+          const uint32_t nerr = block_error(px, pk(f), pk(f + 3), perc, false, &nsel);
+          if (nerr < best_err) { best_err = nerr; best_sel = nsel; best_k = k; best_d = d; }
+        }
+      }
+      if (best_k < 0) break;
+      e[best_k] += best_d;
+      err = best_err;
+      sel = best_sel;
+    }
+    uint32_t lo = pk(e), hi = pk(e + 3);
+    // 4-colour blocks need low > high (swap and remap selectors 0<->1, 2<->3); equal endpoints
+    // are nudged apart as the reference does (crnlib/crn_dxt1.cpp:1563-1583)
     if (lo < hi) {
       const uint32_t t = lo; lo = hi; hi = t;
       sel ^= 0x55555555u;
     } else if (lo == hi) {
-      if ((lo & 31) != 31) { lo++; sel = 0x55555555u; } else { hi--; sel = 0; }
-      err = block_error(px, lo, hi, perceptual != 0, &sel);
+      if ((lo & 31) != 31) lo++; else hi--;
+      err = block_error(px, lo, hi, perc, false, &sel);
+    }
+    // the 3-colour block on the same endpoints (low <= high, mid-point palette)
+    {
+      uint32_t sel3;
+      const uint32_t err3 = block_error(px, hi, lo, perc, true, &sel3);
+      if (err3 < err) { err = err3; sel = sel3; const uint32_t t = lo; lo = hi; hi = t; }
     }
     const float bound = exp2f(yi[6] * 16.f) - 1.f;
-    uint2 w = make_uint2(lo | (hi << 16), sel);
-    *reinterpret_cast<uint2*>(out + (long long)i * 8) = w;
-    if ((float)err > threshold * fmaxf(bound, 1.f)) {
+    *reinterpret_cast<uint2*>(out + i * 8) = make_uint2(lo | (hi << 16), sel);
+    if (!(threshold > 0.f) || (float)err > threshold * fmaxf(bound, 1.f)) {  // threshold <= 0: all exact
       const uint32_t at = atomicAdd(nfall, 1u);
       fallback[at] = (uint32_t)i;
     }
@@ -526,6 +772,31 @@ int forward(Net& net, const uint8_t* blocks, int B, cudaStream_t s) {
               s);
 }
 
+// inference over n blocks (device) -> y [n x 16] with the fused kernel, one persistent CTA per SM
+int infer(Net& net, const uint8_t* blocks, uint32_t n, float* y, cudaStream_t s) {
+  static bool attr_done[64] = {};
+  static int sms[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) { set_error("device index out of range"); return CRNGPU_E_DEVICE; }
+  if (!attr_done[dev]) {
+    e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_check(e, "set up k_mlp_infer");
+    attr_done[dev] = true;
+  }
+  if ((e = net.errflag.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc flag");
+  if (!n) return CRNGPU_OK;
+  const uint32_t tiles = (n + BM - 1) / BM;
+  const uint32_t grid = tiles < (uint32_t)sms[dev] ? tiles : (uint32_t)sms[dev];
+  k_mlp_infer<<<grid, kInferThreads, kInferSmem, s>>>(
+      blocks, (int)n, static_cast<__nv_bfloat16*>(net.W1.wb.ptr), static_cast<__nv_bfloat16*>(net.W2.wb.ptr),
+      static_cast<__nv_bfloat16*>(net.W3.wb.ptr), static_cast<float*>(net.b1.w.ptr), static_cast<float*>(net.b2.w.ptr),
+      static_cast<float*>(net.b3.w.ptr), y, static_cast<uint32_t*>(net.errflag.ptr));
+  return cuda_check(cudaGetLastError(), "launch k_mlp_infer");
+}
+
 // gradients of the mean squared error for targets in net.targets; loss -> net.loss
 int backward(Net& net, const uint8_t* blocks, int B, cudaStream_t s) {
   int rc;
@@ -638,12 +909,13 @@ extern "C" int crngpu_mlp_forward(void* h, const uint8_t* d_blocks, uint32_t n, 
   clear_error();
   Net* net = static_cast<Net*>(h);
   if (!net || net->magic != 0x4D4C5030u || !d_blocks || !d_y) return CRNGPU_E_PARAM;
+  if (n > (1u << 28)) { set_error("crngpu_mlp_forward: at most 2^28 blocks per call"); return CRNGPU_E_PARAM; }
   cudaStream_t s = as_stream(stream);
-  int rc = ensure_batch(*net, (int)n);
-  if (rc != CRNGPU_OK) return rc;
+  cudaError_t e = net->errflag.ensure(16);
+  if (e != cudaSuccess) return cuda_check(e, "alloc flag");
   cudaMemsetAsync(net->errflag.ptr, 0, 4, s);
-  if ((rc = forward(*net, d_blocks, (int)n, s)) != CRNGPU_OK) return rc;
-  cudaMemcpyAsync(d_y, net->y.ptr, (size_t)n * kOutPad * 4, cudaMemcpyDeviceToDevice, s);
+  int rc = infer(*net, d_blocks, n, d_y, s);
+  if (rc != CRNGPU_OK) return rc;
   return check_flag(*net, s);
 }
 
@@ -703,41 +975,46 @@ extern "C" int crngpu_dxt1_learned(void* h, const uint8_t* d_blocks, uint32_t n,
   Net* net = static_cast<Net*>(h);
   if (!net || net->magic != 0x4D4C5030u || !d_blocks || !d_out) return CRNGPU_E_PARAM;
   if (!n) return CRNGPU_OK;
+  if (n > (1u << 28)) { set_error("crngpu_dxt1_learned: at most 2^28 blocks per call"); return CRNGPU_E_PARAM; }
   cudaStream_t s = as_stream(stream);
-  const uint32_t chunk = 1u << 18;
-  int rc = ensure_batch(*net, (int)(n < chunk ? n : chunk));
-  if (rc != CRNGPU_OK) return rc;
+  const uint32_t chunk = 1u << 20;
+  int rc;
   cudaError_t e;
-  if ((e = net->fb_idx.ensure((size_t)(n < chunk ? n : chunk) * 4)) != cudaSuccess) return cuda_check(e, "alloc fallback list");
+  if ((e = net->errflag.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc flag");
+  if ((e = net->chunk_y.ensure((size_t)(n < chunk ? n : chunk) * kOutPad * 4)) != cudaSuccess)
+    return cuda_check(e, "alloc proposals");
+  if ((e = net->fb_idx.ensure((size_t)n * 4)) != cudaSuccess) return cuda_check(e, "alloc fallback list");
   if ((e = net->fb_count.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc fallback count");
-  cudaMemsetAsync(net->fb_count.ptr, 0, 4, s);
+  uint32_t* idx = static_cast<uint32_t*>(net->fb_idx.ptr);
+  uint32_t* cnt_d = static_cast<uint32_t*>(net->fb_count.ptr);
+  cudaMemsetAsync(cnt_d, 0, 4, s);
   cudaMemsetAsync(net->errflag.ptr, 0, 4, s);
   if (fallbacks) *fallbacks = 0;
+  // proposals for every block (chunked to bound the activation buffers); blocks above the bound
+  // are appended to one list of indices into the whole batch
   for (uint32_t c0 = 0; c0 < n; c0 += chunk) {
     const uint32_t cn = n - c0 < chunk ? n - c0 : chunk;
-    const uint8_t* in = d_blocks + (size_t)c0 * 64;
-    uint8_t* out = d_out + (size_t)c0 * 8;
-    uint32_t* idx = static_cast<uint32_t*>(net->fb_idx.ptr);
-    uint32_t* cnt_d = static_cast<uint32_t*>(net->fb_count.ptr);
-    cudaMemsetAsync(cnt_d, 0, 4, s);
-    if ((rc = forward(*net, in, (int)cn, s)) != CRNGPU_OK) return rc;
-    k_learned_refit<<<(cn + 127) / 128, 128, 0, s>>>(in, static_cast<float*>(net->y.ptr), (int)cn, perceptual, out,
-                                                      idx, cnt_d, threshold);
+    if ((rc = infer(*net, d_blocks + (size_t)c0 * 64, cn, static_cast<float*>(net->chunk_y.ptr), s)) != CRNGPU_OK)
+      return rc;
+    k_learned_refit<<<(cn + 127) / 128, 128, 0, s>>>(d_blocks, static_cast<float*>(net->chunk_y.ptr), c0, (int)cn,
+                                                      perceptual, d_out, idx, cnt_d, threshold);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_learned_refit");
-    uint32_t cnt = 0;
-    if ((e = cudaMemcpyAsync(&cnt, cnt_d, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(s)) != cudaSuccess)
-      return cuda_check(e, "read fallback count");
-    if (fallbacks) *fallbacks += cnt;
-    if (!cnt) continue;
+  }
+  uint32_t cnt = 0;
+  if ((e = cudaMemcpyAsync(&cnt, cnt_d, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return cuda_check(e, "read fallback count");
+  if (cnt > n) { set_error("crngpu_dxt1_learned: fallback count out of range"); return CRNGPU_E_DEVICE; }
+  if (fallbacks) *fallbacks = cnt;
+  if (cnt) {
     // blocks above the bound: the exact optimizer, on a compacted copy, scattered back
     if ((e = net->fb_in.ensure((size_t)cnt * 64)) != cudaSuccess) return cuda_check(e, "alloc fallback blocks");
     if ((e = net->fb_out.ensure((size_t)cnt * 8)) != cudaSuccess) return cuda_check(e, "alloc fallback out");
-    k_gather_idx<<<(cnt * 4 + 255) / 256, 256, 0, s>>>(in, idx, cnt_d, static_cast<uint8_t*>(net->fb_in.ptr));
+    k_gather_idx<<<(cnt * 4 + 255) / 256, 256, 0, s>>>(d_blocks, idx, cnt_d, static_cast<uint8_t*>(net->fb_in.ptr));
     if ((rc = launch_dxt1(static_cast<uint8_t*>(net->fb_in.ptr), cnt, perceptual != 0, true,
                           static_cast<uint8_t*>(net->fb_out.ptr), 8, nullptr, s)) != CRNGPU_OK)
       return rc;
-    k_scatter_idx<<<(cnt + 255) / 256, 256, 0, s>>>(static_cast<uint8_t*>(net->fb_out.ptr), idx, cnt_d, out);
+    k_scatter_idx<<<(cnt + 255) / 256, 256, 0, s>>>(static_cast<uint8_t*>(net->fb_out.ptr), idx, cnt_d, d_out);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "learned encode kernels");
   return check_flag(*net, s);

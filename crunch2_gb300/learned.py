@@ -2,7 +2,8 @@
 
 The network (48 -> 256 -> 256 -> 8, GELU, BF16 tensor-core GEMMs with FP32 accumulation) is
 trained on blocks the plain GPU optimizer labels (its endpoints and its error); the learned
-encode keeps a prediction after one selector refit unless its error is above 1.5x the
+encode keeps a refined prediction (selector fit, least-squares refit, +-1 search, 3-colour check)
+unless its error is above a threshold (1.5x by default) times the
 predicted bound, and sends the rest to the exact optimizer.
 """
 from __future__ import annotations
@@ -152,3 +153,123 @@ def train(net: EndpointNet, d_blocks, d_targets, steps: int, batch: int = 8192, 
         if log_every and step % log_every == 0:
             print(f"step {step} loss {loss:.6f}")
     return losses
+
+
+def rgb_rmse_torch(blocks8, pixels):
+    """'RGB Average' RMSE (crnlib/crn_image_utils.cpp:1048-1139) of DXT1 blocks vs RGBA8 blocks,
+    computed on the device in chunks."""
+    import torch
+    total = 0.0
+    n = int(pixels.shape[0])
+    for c0 in range(0, n, 1 << 21):
+        b = blocks8[c0:c0 + (1 << 21)].to(torch.int64)
+        px = pixels[c0:c0 + (1 << 21)].view(-1, 16, 4)[:, :, :3].to(torch.int64)
+        lo = b[:, 0] | (b[:, 1] << 8)
+        hi = b[:, 2] | (b[:, 3] << 8)
+
+        def exp565(c):
+            r, g, bb = (c >> 11) & 31, (c >> 5) & 63, c & 31
+            return torch.stack([(r << 3) | (r >> 2), (g << 2) | (g >> 4), (bb << 3) | (bb >> 2)], -1)
+        c0_, c1_ = exp565(lo), exp565(hi)
+        four = (lo > hi).unsqueeze(-1)
+        c2 = torch.where(four, (2 * c0_ + c1_) // 3, (c0_ + c1_) >> 1)
+        c3 = torch.where(four, (c0_ + 2 * c1_) // 3, torch.zeros_like(c0_))
+        pal = torch.stack([c0_, c1_, c2, c3], 1)
+        sel = torch.stack([(b[:, 4 + (i >> 2)] >> (2 * (i & 3))) & 3 for i in range(16)], 1)
+        dec = torch.gather(pal, 1, sel.unsqueeze(-1).expand(-1, -1, 3))
+        total += float(((dec - px) ** 2).sum())
+    return (total / (n * 16 * 3)) ** 0.5
+
+
+def config4(train_textures=64, train_size=2048, eval_textures=32, eval_size=4096, steps=2048, batch=8192,
+            lr=1e-3, threshold=1.5, log_every=256, seed=0, weights=None):
+    """Learned endpoint proposal end to end: GPU-labelled training set, GPU training, and learned
+    vs plain DXT1 encode on held-out textures (different seed range). `threshold` may be a list
+    (or a comma-separated string) to report several fallback thresholds from one trained net;
+    `weights` loads a saved state instead of training. Returns a metrics dict."""
+    import time
+    import torch
+    ev = lambda: torch.cuda.Event(enable_timing=True)
+    net = EndpointNet(seed=seed)
+    res = {}
+    if weights:
+        net.load(dict(np.load(weights)))
+        res["weights"] = str(weights)
+    else:
+        t0 = time.perf_counter()
+        train_blocks = training_blocks(train_textures, train_size, seed0=1000)
+        targets, _ = make_targets(train_blocks)
+        torch.cuda.synchronize()
+        t_label = time.perf_counter() - t0
+        t1 = time.perf_counter()
+        losses = train(net, train_blocks, targets, steps=steps, batch=batch, lr=lr, log_every=log_every)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t1
+        del train_blocks, targets
+        res.update({"train_blocks": train_textures * (train_size // 4) ** 2, "train_steps": steps, "batch": batch,
+                    "label_s": round(t_label, 3), "train_s": round(t_train, 3), "loss_first": losses[0],
+                    "loss_last": float(np.mean(losses[-32:]))})
+    if isinstance(threshold, str):
+        threshold = [float(t) for t in threshold.split(",")]
+    ths = list(threshold) if isinstance(threshold, (list, tuple)) else [float(threshold)]
+    tot = {"plain_ms": 0.0, "forward_ms": 0.0, "blocks": 0, "se_plain": 0.0}
+    per = [{"learned_ms": 0.0, "fallbacks": 0, "se": 0.0} for _ in ths]
+    from .texgen import colour_texture_torch, image_blocks_torch
+    from . import dxt1_optimize
+    for i in range(eval_textures):
+        blocks = image_blocks_torch(colour_texture_torch(eval_size, eval_size, 50000 + i))
+        n = int(blocks.shape[0])
+        out_p = torch.empty((n, 8), dtype=torch.uint8, device=blocks.device)
+        out_l = torch.empty_like(out_p)
+        dxt1_optimize(blocks)  # warm
+        a, b = ev(), ev()
+        a.record(); out_p = dxt1_optimize(blocks); b.record(); torch.cuda.synchronize()
+        tot["plain_ms"] += a.elapsed_time(b)
+        net.forward(blocks)
+        a, b = ev(), ev()
+        a.record(); net.forward(blocks); b.record(); torch.cuda.synchronize()
+        tot["forward_ms"] += a.elapsed_time(b)
+        tot["blocks"] += n
+        tot["se_plain"] += rgb_rmse_torch(out_p, blocks) ** 2 * n
+        for th, acc in zip(ths, per):
+            a, b = ev(), ev()
+            a.record(); out_l, fb = net.encode(blocks, threshold=th, out=out_l); b.record(); torch.cuda.synchronize()
+            acc["learned_ms"] += a.elapsed_time(b)
+            acc["fallbacks"] += fb
+            acc["se"] += rgb_rmse_torch(out_l, blocks) ** 2 * n
+    texels = tot["blocks"] * 16
+    res.update({"eval_textures": eval_textures, "eval_size": eval_size, "eval_blocks": tot["blocks"],
+                "plain_mtexel_s": texels / (tot["plain_ms"] / 1e3) / 1e6,
+                "rmse_plain": (tot["se_plain"] / tot["blocks"]) ** 0.5,
+                "forward_ms_per_mblock": tot["forward_ms"] / (tot["blocks"] / 1e6)})
+    res["learned"] = [{"threshold": th,
+                       "learned_mtexel_s": texels / (acc["learned_ms"] / 1e3) / 1e6,
+                       "speedup": tot["plain_ms"] / acc["learned_ms"],
+                       "rmse_learned": (acc["se"] / tot["blocks"]) ** 0.5,
+                       "fallback_frac": acc["fallbacks"] / tot["blocks"]} for th, acc in zip(ths, per)]
+    res["state"] = net.state()
+    return res
+
+
+if __name__ == "__main__":
+    # python -m crunch2_gb300.learned [key=value ...] [out=weights.npz]
+    import json
+    import sys
+    kw, out = {}, None
+    for a in sys.argv[1:]:
+        k, v = a.split("=", 1)
+        if k == "out":
+            out = v
+        else:
+            try:
+                kw[k] = int(v)
+            except ValueError:
+                try:
+                    kw[k] = float(v)
+                except ValueError:
+                    kw[k] = v
+    r = config4(**kw)
+    st = r.pop("state")
+    if out:
+        np.savez(out, **st)
+    print(json.dumps(r))

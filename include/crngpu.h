@@ -108,9 +108,11 @@ CRNGPU_API int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, ui
 /* ------------------------------------------------------------------------------------------
  * Learned DXT1 endpoint proposal (no counterpart in the reference). A 48 -> 256 -> 256 -> 8 MLP
  * (GELU, BF16 weights, FP32 accumulation on tcgen05 tensor cores) predicts the endpoints the
- * plain optimizer would choose and the error it would reach; the learned encode keeps the
- * prediction after one selector refit unless its error exceeds threshold x that predicted bound,
- * in which case the block goes through crngpu_dxt1_optimize_batch's exact search.
+ * plain optimizer would choose and the error it would reach; the learned encode refines the
+ * prediction (selector fit, least-squares endpoint refit, a short +-1 search on the six endpoint
+ * components, the 3-colour block on the same endpoints) and keeps it unless its error exceeds
+ * threshold x that predicted bound, in which case the block goes through
+ * crngpu_dxt1_optimize_batch's exact search.
  * All block/target/output pointers are device memory.
  * --------------------------------------------------------------------------------------- */
 
@@ -137,8 +139,10 @@ CRNGPU_API int crngpu_mlp_gradients(void* net, const uint8_t* d_blocks, const fl
 CRNGPU_API int crngpu_mlp_train_step(void* net, const uint8_t* d_blocks, const float* d_targets, uint32_t n,
                                      float lr, float weight_decay, float* loss, void* stream);
 
-/* Learned DXT1 encode of n blocks (4-colour blocks; fallback blocks use the exact optimizer).
- * *fallbacks (host, optional) receives the number of blocks that fell back. */
+/* Learned DXT1 encode of n blocks (n <= 2^28; fallback blocks use the exact optimizer with both
+ * block types). threshold <= 0 sends every block to the exact optimizer. *fallbacks (host,
+ * optional) receives the number of blocks that fell back. Synchronises `stream` once, to read the
+ * fallback count. */
 CRNGPU_API int crngpu_dxt1_learned(void* net, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
                                    uint8_t* d_out, uint32_t* fallbacks, void* stream);
 

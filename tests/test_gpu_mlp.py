@@ -41,6 +41,22 @@ def test_forward_matches_oracle(L, batch):
     assert np.abs(y[:, 7:]).max() < 1e-6  # padded outputs stay zero
 
 
+def test_fused_forward_many_tiles(L):
+    """The persistent inference kernel loops over tiles: more tiles than SMs and a ragged tail."""
+    from oracle import mlp_oracle
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    n = sms * 128 * 2 + 37
+    rng = np.random.default_rng(11)
+    blocks = rng.integers(0, 256, size=(n, 64), dtype=np.uint8)
+    net = L.EndpointNet(seed=9)
+    y = net.forward(torch.from_numpy(blocks).cuda()).cpu().numpy().astype(np.float64)
+    idx = np.concatenate([np.arange(0, 256), np.arange(n - 300, n)])   # first tiles and the tail
+    ref, _ = mlp_oracle.forward(net.state(), blocks[idx])
+    assert rel_err(y[idx, :7], ref[:, :7]) < 1e-2
+    assert np.isfinite(y).all()
+    assert np.abs(y[:, 7:]).max() < 1e-6
+
+
 def test_gradients_match_oracle(L, batch):
     from oracle import mlp_oracle
     blocks, targets = batch
