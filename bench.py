@@ -4,6 +4,8 @@ synthetic texture (value noise + 40 flat rectangles, seed 100; 11 box-filtered l
 
 One JSON line on stdout (rank 0):
   value      whole-job DXT1 encode Mtexel/s, inputs resident in HBM, device time of K steps
+  learned    the learned-proposal encode of the same blocks (shipped weights): Mtexel/s, RGB
+             RMSE beside the plain encode's, fallback fraction
   e2e        the same encode through the C ABI with pinned host buffers (H2D + encode + D2H)
   transcode  CRN -> DXT1 transcode of the reference-encoded .crn of the same texture (q128)
   roofline   the encoder kernel: ALU issue roofline (candidate x colour evaluations counted on
@@ -290,6 +292,35 @@ def main():
     e2e_value = world * texels * args.steps / e2e_s / 1e6
     e2e_parity = float((host_outs[0].numpy() == d_out[:host_outs[0].shape[0]].cpu().numpy()).all())
 
+    # ---- learned endpoint proposal (shipped weights) on the same blocks, against the plain result
+    from crunch2_gb300 import learned as LR
+    net = LR.default_net()
+    d_learned = torch.empty_like(d_out)
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        net.encode(d_blocks, threshold=LR.DEFAULT_THRESHOLD, out=d_learned, stream=stream)
+    torch.cuda.synchronize()
+    ln_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ln_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    fallbacks = 0
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        ln_start[i].record(stream)
+        _, fallbacks = net.encode(d_blocks, threshold=LR.DEFAULT_THRESHOLD, out=d_learned, stream=stream)
+        ln_end[i].record(stream)
+    torch.cuda.synchronize()
+    ln_ms = sum(s.elapsed_time(e) for s, e in zip(ln_start, ln_end)) / args.steps
+    rmse_plain = LR.rgb_rmse_torch(d_out, d_blocks)
+    rmse_learned = LR.rgb_rmse_torch(d_learned, d_blocks)
+    learned = {"value": round(texels / (ln_ms / 1e3) / 1e6, 3), "unit": "Mtexel/s", "ms_per_step": round(ln_ms, 4),
+               "speedup_vs_plain": round(kernel_ms / ln_ms, 3), "rmse_plain": round(rmse_plain, 4),
+               "rmse_learned": round(rmse_learned, 4), "rmse_delta": round(rmse_learned - rmse_plain, 4),
+               "fallback_frac": round(fallbacks / n_blocks, 4), "threshold": LR.DEFAULT_THRESHOLD,
+               "weights": "crunch2_gb300/weights/dxt1_endpoint_net.npz",
+               "path": "crngpu_dxt1_learned: fused MLP (k_mlp_infer) + refit (k_learned_refit) + exact "
+                       "optimizer on fallback blocks; one host sync per call"}
+    del net
+
     # ---- CRN -> DXT1 transcode of the same texture (all 11 levels, device output)
     with open(CRN_FIXTURE, "rb") as fh:
         crn = fh.read()
@@ -343,7 +374,7 @@ def main():
                 "parity_vs_oracle_sample": parity, "e2e_parity": e2e_parity,
                 "e2e": {"value": round(e2e_value, 3), "unit": "Mtexel/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "path": "crngpu_compress_image per level, pinned host buffers"},
-                "transcode": transcode, "roofline": roofline, "cpu_baseline": cpu,
+                "learned": learned, "transcode": transcode, "roofline": roofline, "cpu_baseline": cpu,
                 "gpu_launches": args.steps * 1, "clocks": clk, "wall_s_timed": round(wall, 4)}
         print(json.dumps(line))
 

@@ -14,7 +14,14 @@ import numpy as np
 
 from . import lib, _check, CrnGpuError, E_PARAM, dxt1_optimize
 
+import os
+
 PARAM_SHAPES = [(256, 48), (256,), (256, 256), (256,), (16, 256), (16,)]
+# Trained network shipped with the package: `python -m crunch2_gb300.learned out=<this path>`
+# (16,777,216 training blocks from 64 seeded 2048x2048 colour textures, labels from the plain
+# GPU optimizer, 2048 AdamW steps of 8192 blocks, lr 1e-3, weight decay 0.01, init seed 0).
+WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "dxt1_endpoint_net.npz")
+DEFAULT_THRESHOLD = 1.5
 PARAM_NAMES = ["W1", "b1", "W2", "b2", "W3", "b3"]
 
 
@@ -100,7 +107,7 @@ class EndpointNet:
                "crngpu_mlp_train_step")
         return float(loss.value)
 
-    def encode(self, d_blocks, perceptual: bool = True, threshold: float = 1.5, out=None, stream=None):
+    def encode(self, d_blocks, perceptual: bool = True, threshold: float = DEFAULT_THRESHOLD, out=None, stream=None):
         """Learned DXT1 encode; returns (blocks (n, 8) uint8 device tensor, fallback count)."""
         import torch
         n = int(d_blocks.shape[0])
@@ -110,6 +117,13 @@ class EndpointNet:
         _check(self.L.crngpu_dxt1_learned(self.h, d_blocks.data_ptr(), n, int(perceptual), threshold, out.data_ptr(),
                                           ctypes.byref(fb), _sp(stream)), "crngpu_dxt1_learned")
         return out, int(fb.value)
+
+
+def default_net(path: str = WEIGHTS) -> EndpointNet:
+    """The shipped trained network on the current device."""
+    net = EndpointNet(seed=0)
+    net.load(dict(np.load(path)))
+    return net
 
 
 def make_targets(d_blocks, perceptual: bool = True, stream=None):
