@@ -48,6 +48,12 @@ class _Dxt1Params(ctypes.Structure):
 _lib = None
 
 
+class _BatchItem(ctypes.Structure):
+    """crngpu_unpack_batch_item"""
+    _fields_ = [("ctx", ctypes.c_void_p), ("first_level", ctypes.c_uint32), ("level_count", ctypes.c_uint32),
+                ("dst", ctypes.c_void_p), ("dst_size", ctypes.c_uint64)]
+
+
 def lib():
     """Loads libcrngpu.so (building it first if it is missing). Raises if that fails."""
     global _lib
@@ -80,6 +86,16 @@ def lib():
     L.crngpu_unpack_levels.restype = i64
     L.crngpu_unpack_end.argtypes = [vp]
     L.crngpu_unpack_end.restype = i32
+    L.crngpu_unpack_batch_create.argtypes = [ctypes.POINTER(_BatchItem), u32]
+    L.crngpu_unpack_batch_create.restype = vp
+    L.crngpu_unpack_batch_launch.argtypes = [vp, i32, vp]
+    L.crngpu_unpack_batch_launch.restype = i32
+    L.crngpu_unpack_batch_status.argtypes = [vp, vp]
+    L.crngpu_unpack_batch_status.restype = i32
+    L.crngpu_unpack_batch_bytes.argtypes = [vp]
+    L.crngpu_unpack_batch_bytes.restype = i64
+    L.crngpu_unpack_batch_destroy.argtypes = [vp]
+    L.crngpu_unpack_batch_destroy.restype = i32
     L.crngpu_crn_decompress.argtypes = [vp, ctypes.c_uint, vp, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint]
     L.crngpu_crn_decompress.restype = None
     L.crngpu_profile_counters.argtypes = [i32, ctypes.POINTER(ctypes.c_uint64), vp]
@@ -242,6 +258,46 @@ class UnpackContext:
     def close(self):
         if self.handle:
             lib().crngpu_unpack_end(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class UnpackBatch:
+    """Many levels of many open contexts transcoded by one persistent decode launch and one
+    expansion launch (crngpu_unpack_batch_*). items: (context, first_level, level_count, dst)
+    with dst a CUDA uint8 tensor receiving the levels back to back (minimal pitch)."""
+
+    def __init__(self, items):
+        self._keep = [(ctx, dst) for ctx, _, _, dst in items]  # contexts and outputs outlive the batch
+        arr = (_BatchItem * len(items))()
+        for i, (ctx, first, count, dst) in enumerate(items):
+            arr[i] = _BatchItem(ctx.handle, first, count, dst.data_ptr(), dst.numel() * dst.element_size())
+        self.handle = lib().crngpu_unpack_batch_create(arr, len(items))
+        if not self.handle:
+            raise CrnGpuError(E_PARAM, "crngpu_unpack_batch_create")
+        self.bytes = int(lib().crngpu_unpack_batch_bytes(self.handle))
+
+    def launch(self, use_graph: bool = False, stream=None):
+        _check(lib().crngpu_unpack_batch_launch(self.handle, int(use_graph), _stream_ptr(stream)),
+               "crngpu_unpack_batch_launch")
+
+    def status(self, stream=None):
+        _check(lib().crngpu_unpack_batch_status(self.handle, _stream_ptr(stream)), "crngpu_unpack_batch_status")
+
+    def close(self):
+        if self.handle:
+            lib().crngpu_unpack_batch_destroy(self.handle)
             self.handle = None
 
     def __enter__(self):

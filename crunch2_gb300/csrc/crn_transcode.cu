@@ -2,13 +2,19 @@
 //
 // Restates crnd::crn_unpacker::unpack_level and unpack_dxt1/dxt5/dxn/dxt5a
 // (inc/crn_decomp.h:3537-3619, 3944-4223) as two kernels:
-//   k_crn_decode  - the serial part: one warp (lane 0) per level stream Huffman-decodes the
-//                   reference-group / endpoint-delta / selector symbols, resolves the
-//                   left/top endpoint references and the running (mod palette size) endpoint
-//                   index, and writes one index record per visible block to a scratch buffer.
-//                   Streams of different levels (and textures) decode concurrently.
-//   k_crn_expand  - the parallel part: every thread turns index records into finished DXT
-//                   words (palette gathers from L2) and writes 16 bytes per store.
+//   k_crn_decode_textures - the serial part. Each level stream is a serial chain of prefix
+//                   codes whose meaning depends on the symbols before it, so one lane owns one
+//                   stream: it Huffman-decodes the reference-group / endpoint-delta / selector
+//                   symbols, resolves the left/top endpoint references and the running (mod
+//                   palette size) endpoint indices, and writes one index record per visible
+//                   block. A warp takes one texture (its prefix tables staged in shared memory)
+//                   and its lanes decode the texture's levels side by side; the decode is a
+//                   per-lane state machine (one symbol per iteration) so the lanes stay in
+//                   lockstep. The kernel is persistent: warps take textures largest-first from
+//                   a work counter until none are left, so one launch decodes every level of
+//                   every texture of a batch, whatever their sizes and formats.
+//   k_crn_expand_jobs - the parallel part: every thread turns index records into finished
+//                   DXT words (palette gathers from L2) and writes 16 bytes per store.
 // The header, Huffman models and palettes are decoded once on the host (crn_file.cpp).
 #include <cuda_runtime.h>
 
@@ -23,11 +29,14 @@
 
 namespace crngpu {
 
-// Device status word values (written by k_crn_decode, read back by the host).
+// Device status word values (written by k_crn_decode_textures, read back by the host).
 enum : uint32_t { kStOk = 0, kStBadCode = 1, kStBadIndex = 2 };
 
-// Model slots in the device model array.
+// Model slots in a context's device model array.
 enum { kMRef = 0, kMEp0 = 1, kMSel0 = 2, kMEp1 = 3, kMSel1 = 4, kNumModels = 5 };
+
+// Block formats of a level stream (runtime, per job).
+enum : uint32_t { kKDxt1 = 0, kKDxt5 = 1, kKDxn = 2, kKDxt5a = 3 };
 
 struct DevPalettes {
   const uint32_t* colour_ep;
@@ -37,67 +46,116 @@ struct DevPalettes {
   uint32_t n_cep, n_csel, n_aep, n_asel;
 };
 
-struct DecodeJob {
-  const uint8_t* src;  // level stream (device)
+// One level stream for the decoder. Endpoint "A" is the colour endpoint (DXT1, DXT5) or the
+// first alpha endpoint (DXN, DXT5A); "B" is the DXT5 alpha endpoint or the second DXN alpha.
+struct StreamJob {
+  const uint8_t* src;       // compressed level stream (device; readable 64 bytes past the end)
+  const DevModel* models;   // the file's five prefix models
+  uint8_t* rec;             // index records of the level: faces x by x bx, 4 or 8 bytes each
   uint32_t src_size;
   uint32_t bx, by, faces;
-  uint64_t rec_ofs;    // first index record of this level in the scratch buffer
+  uint32_t kind;
+  uint32_t n_a, n_b, n_sa, n_sb;  // endpoint and selector palette sizes (A, B)
+  uint32_t rb_ofs;                // the lane's row-buffer slice in shared memory (words)
 };
 
+// One texture for the decoder: the streams [first, first + nlev) of one file, one lane each.
+struct TexJob {
+  const DevModel* models;  // the file's five prefix models
+  uint32_t first, nlev, kind, rb_words;  // rb_words: row-buffer words of all its lanes
+  uint64_t work;           // blocks x streams-per-block, for the largest-first order
+};
+
+// One face of one level for the expansion kernel.
 struct ExpandJob {
-  uint8_t* dst;        // face 0 of the level (device)
-  uint64_t face_stride;
-  uint64_t rec_ofs;
-  uint32_t bx, by, faces, pitch;
-  uint32_t cta_begin;  // first CTA of this job in the expansion grid
-  uint32_t ctas_per_row;
+  uint8_t* dst;           // row 0 of the face (device)
+  const uint8_t* rec;     // the face's index records
+  DevPalettes pal;
+  uint32_t bx, by, pitch, kind;
+  uint32_t cta_begin, ctas_per_row;
 };
 
 constexpr int kExpandThreads = 128;
-constexpr int kMaxRowBlocks = 1024;  // 4096 px / 4, already even
+// Decoder shared memory per CTA: five first-level tables + the row buffers of one texture's
+// levels (at most 2 x 1024 + 2 x 16 words for a 4096-texel-wide texture with 16 levels).
+constexpr size_t kDecodeSmemMax = 64u << 10;
+
+__host__ __device__ constexpr uint32_t record_bytes(uint32_t kind) {
+  return (kind == kKDxt1 || kind == kKDxt5a) ? 4u : 8u;
+}
 
 // ------------------------------------------------------------------------------------------
 // Bit reader: MSB-first 64-bit window; bytes past the end of the stream read as zero, as in
 // symbol_codec::get_bits / decode (inc/crn_decomp.h:3162-3214). After a byte-wise head the
-// stream is read as aligned 32-bit words (byte-swapped to MSB-first) with an L1 prefetch a few
-// lines ahead, so the lone decoding thread rarely waits on memory.
+// stream is read as aligned 32-bit words (byte-swapped to MSB-first); the next word is always
+// loaded one refill ahead so a refill never waits on memory, and an L1 prefetch runs 1 KB ahead.
 struct Bits {
   const uint8_t* p;   // stream start
-  uint32_t pos, end;  // next byte to load, stream size
+  uint32_t pos, end;  // byte offset of `next`, stream size
+  uint32_t next;      // the word at pos (masked past the end)
   uint64_t buf;
   int n;
+  __device__ __forceinline__ uint32_t load_word(uint32_t at) const {
+    if (at >= end) return 0u;
+    uint32_t w = __byte_perm(__ldg(reinterpret_cast<const uint32_t*>(p + at)), 0, 0x0123);
+    if (at + 4 > end) w &= 0xFFFFFFFFu << (8 * (4 - (end - at)));  // zero the bytes past the end
+    return w;
+  }
   __device__ __forceinline__ void init(const uint8_t* src, uint32_t size) {
     p = src; pos = 0; end = size; buf = 0; n = 0;
-    // head: bytes up to the first 4-byte aligned address
     while (((uintptr_t)(p + pos) & 3) && n <= 56) {
       const uint32_t v = pos < end ? (uint32_t)__ldg(p + pos) : 0u;
       buf |= (uint64_t)v << (56 - n);
       n += 8;
       pos++;
     }
+    next = load_word(pos);
   }
   __device__ __forceinline__ void refill() {
     if (n <= 32) {
-      uint32_t w;
-      if (pos + 4 <= end) {
-        w = __byte_perm(__ldg(reinterpret_cast<const uint32_t*>(p + pos)), 0, 0x0123);
-        if ((pos & 127) == 0) asm volatile("prefetch.global.L1 [%0];" ::"l"(p + pos + 1024));
-      } else if (pos < end) {
-        w = __byte_perm(__ldg(reinterpret_cast<const uint32_t*>(p + pos)), 0, 0x0123);
-        w &= 0xFFFFFFFFu << (8 * (4 - (end - pos)));  // zero the bytes past the end
-      } else {
-        w = 0;
-      }
-      pos += 4;
-      buf |= (uint64_t)w << (32 - n);
+      buf |= (uint64_t)next << (32 - n);
       n += 32;
+      pos += 4;
+      if ((pos & 127) == 0 && pos + 1024 < end) asm volatile("prefetch.global.L1 [%0];" ::"l"(p + pos + 1024));
+      next = load_word(pos);
     }
   }
 };
 
-// Canonical prefix decode (symbol_codec::decode, inc/crn_decomp.h:3186-3253): 11-bit table in
-// shared memory, then a walk over left-aligned per-length limits. -1: no such code.
-__device__ __forceinline__ int decode_sym(Bits& b, const uint32_t* __restrict__ lut, const DevModel* __restrict__ m) {
+// Canonical prefix decode (symbol_codec::decode, inc/crn_decomp.h:3186-3253): 11-bit first-level
+// table, then a walk over left-aligned per-length limits. -1: no such code.
+__device__ __forceinline__ int decode_sym(Bits& b, const DevModel* __restrict__ m) {
+  b.refill();
+  const uint32_t v = (uint32_t)(b.buf >> 48);
+  const uint32_t e = __ldg(&m->lut[v >> (16 - kLutBits)]);
+  uint32_t s, len;
+  if (e != kLutLong) {
+    s = e & 0xFFFFu;
+    len = e >> 16;
+  } else {
+    len = kLutBits + 1;
+    while (len <= (uint32_t)kMaxCodeLen && v >= __ldg(&m->limit[len])) len++;
+    if (len > (uint32_t)kMaxCodeLen) return -1;
+    const int idx = __ldg(&m->base[len]) + (int)(v >> (16 - len));
+    if (idx < 0 || (uint32_t)idx >= __ldg(&m->num_syms)) return -1;
+    s = __ldg(&m->sorted[idx]);
+  }
+  b.buf <<= len;
+  b.n -= (int)len;
+  return (int)s;
+}
+
+// Row buffer entry (block_buffer_element, inc/crn_decomp.h:3652-3658), packed:
+// bits 0-1 endpoint reference for the odd row, 2-14 endpoint index A, 15-27 endpoint index B.
+__device__ __forceinline__ uint32_t rb_pack(uint32_t ref, uint32_t a, uint32_t b) { return ref | (a << 2) | (b << 15); }
+__device__ __forceinline__ uint32_t rb_a(uint32_t e) { return (e >> 2) & 0x1FFFu; }
+__device__ __forceinline__ uint32_t rb_b(uint32_t e) { return (e >> 15) & 0x1FFFu; }
+
+__host__ __device__ constexpr uint32_t models_used(uint32_t kind) { return kind == kKDxt5 ? 5u : 3u; }
+
+// Decodes one symbol with a first-level table in shared memory (`lut`) and, for the rare codes
+// longer than kLutBits, the device model `m`. -1: no such code.
+__device__ __forceinline__ int decode_sym_s(Bits& b, const uint32_t* __restrict__ lut, const DevModel* __restrict__ m) {
   b.refill();
   const uint32_t v = (uint32_t)(b.buf >> 48);
   const uint32_t e = lut[v >> (16 - kLutBits)];
@@ -110,7 +168,7 @@ __device__ __forceinline__ int decode_sym(Bits& b, const uint32_t* __restrict__ 
     while (len <= (uint32_t)kMaxCodeLen && v >= __ldg(&m->limit[len])) len++;
     if (len > (uint32_t)kMaxCodeLen) return -1;
     const int idx = __ldg(&m->base[len]) + (int)(v >> (16 - len));
-    if (idx < 0 || (uint32_t)idx >= m->num_syms) return -1;
+    if (idx < 0 || (uint32_t)idx >= __ldg(&m->num_syms)) return -1;
     s = __ldg(&m->sorted[idx]);
   }
   b.buf <<= len;
@@ -118,171 +176,191 @@ __device__ __forceinline__ int decode_sym(Bits& b, const uint32_t* __restrict__ 
   return (int)s;
 }
 
-// Row buffer entry (block_buffer_element, inc/crn_decomp.h:3652-3658), packed:
-// bits 0-1 endpoint reference for the odd row, 2-14 endpoint index A, 15-27 endpoint index B.
-__device__ __forceinline__ uint32_t rb_ref(uint32_t e) { return e & 3u; }
-__device__ __forceinline__ uint32_t rb_a(uint32_t e) { return (e >> 2) & 0x1FFFu; }
-__device__ __forceinline__ uint32_t rb_b(uint32_t e) { return (e >> 15) & 0x1FFFu; }
-
-// KIND: 0 DXT1, 1 DXT5 (colour + alpha), 2 DXN (two alpha), 3 DXT5A
-// Number of prefix models a format reads: ref + (colour ep, sel) + (alpha ep, sel).
+// One level stream (all its faces), the loop of unpack_dxt1/dxt5/dxn/dxt5a
+// (inc/crn_decomp.h:3944-4223). `luts` holds the first-level tables of the models this format
+// reads (ref, then delta/selector of endpoint A, then of endpoint B for DXT5); `rb` is the lane's
+// row buffer. Returns a kSt* status.
 template <int KIND>
-__host__ __device__ constexpr int models_used() { return KIND == 1 ? 5 : 3; }
-
-template <int KIND>
-__global__ void __launch_bounds__(32) k_crn_decode(const DecodeJob* __restrict__ jobs, int njobs,
-                                                    const DevModel* __restrict__ models, DevPalettes pal,
-                                                    void* __restrict__ records, uint32_t* __restrict__ status) {
-  __shared__ uint32_t row[kMaxRowBlocks];
-  extern __shared__ uint32_t luts[];  // models_used<KIND>() x 2^kLutBits entries
-  const int job_i = blockIdx.x;
-  if (job_i >= njobs) return;
-  // the warp copies the first-level tables this format needs into shared memory
-  {
-    const int slots[5] = {kMRef, KIND == 0 || KIND == 1 ? kMEp0 : kMEp1, KIND == 0 || KIND == 1 ? kMSel0 : kMSel1,
-                          kMEp1, kMSel1};
-    for (int t = 0; t < models_used<KIND>(); t++) {
-      const uint4* src = reinterpret_cast<const uint4*>(models[slots[t]].lut);
-      uint4* dst = reinterpret_cast<uint4*>(luts + t * (1 << kLutBits));
-      for (int k = threadIdx.x; k < (1 << kLutBits) / 4; k += 32) dst[k] = __ldg(src + k);
-    }
-    __syncwarp();
-  }
-  if (threadIdx.x != 0) return;
-  const DecodeJob job = jobs[job_i];
-  const bool colour = KIND == 0 || KIND == 1;
-  const int nalpha = KIND == 2 ? 2 : (KIND == 0 ? 0 : 1);
-  const DevModel* m_ref = models + kMRef;
-  const DevModel* m_ep0 = models + kMEp0;
-  const DevModel* m_sel0 = models + kMSel0;
-  const DevModel* m_ep1 = models + kMEp1;
-  const DevModel* m_sel1 = models + kMSel1;
-  const uint32_t* l_ref = luts;
-  const uint32_t* l_ep0 = luts + (1 << kLutBits);      // colour models (DXT1, DXT5) ...
-  const uint32_t* l_sel0 = luts + 2 * (1 << kLutBits);
-  const uint32_t* l_ep1 = KIND == 1 ? luts + 3 * (1 << kLutBits) : l_ep0;   // ... or alpha models
-  const uint32_t* l_sel1 = KIND == 1 ? luts + 4 * (1 << kLutBits) : l_sel0;
-  const uint32_t W = (job.bx + 1) & ~1u, H = (job.by + 1) & ~1u;
-  for (uint32_t x = 0; x < W; x++) row[x] = 0;
+__device__ uint32_t decode_level(const StreamJob& J, const uint32_t* __restrict__ luts, uint32_t* __restrict__ rb) {
+  constexpr bool colour = KIND == kKDxt1 || KIND == kKDxt5;
+  constexpr bool two = KIND == kKDxt5 || KIND == kKDxn;
+  const DevModel* mR = J.models + kMRef;
+  const DevModel* mDA = J.models + (colour ? kMEp0 : kMEp1);
+  const DevModel* mSA = J.models + (colour ? kMSel0 : kMSel1);
+  const DevModel* mDB = J.models + kMEp1;
+  const DevModel* mSB = J.models + kMSel1;
+  const uint32_t* lR = luts;
+  const uint32_t* lDA = luts + (1u << kLutBits);
+  const uint32_t* lSA = luts + (2u << kLutBits);
+  const uint32_t* lDB = KIND == kKDxt5 ? luts + (3u << kLutBits) : lDA;
+  const uint32_t* lSB = KIND == kKDxt5 ? luts + (4u << kLutBits) : lSA;
+  const uint32_t bx = J.bx, by = J.by, faces = J.faces;
+  const uint32_t W = (bx + 1) & ~1u, H = (by + 1) & ~1u;
+  const uint32_t nA = J.n_a, nB = J.n_b, nSA = J.n_sa, nSB = J.n_sb;
+  for (uint32_t x = 0; x < W; x++) rb[x] = 0;
   Bits b;
-  b.init(job.src, job.src_size);
-  uint32_t cep = 0, a0 = 0, a1 = 0, group = 0;
-  uint32_t* rec32 = reinterpret_cast<uint32_t*>(records) + job.rec_ofs;
-  uint64_t* rec64 = reinterpret_cast<uint64_t*>(records) + job.rec_ofs;
-  uint64_t out_i = 0;
-  uint32_t err = kStOk;
-  for (uint32_t f = 0; f < job.faces && !err; f++) {
-    for (uint32_t y = 0; y < H && !err; y++) {
-      const bool yvis = y < job.by;
+  b.init(J.src, J.src_size);
+  uint32_t iA = 0, iB = 0, group = 0;
+  uint32_t* rec32 = reinterpret_cast<uint32_t*>(J.rec);
+  uint64_t* rec64 = reinterpret_cast<uint64_t*>(J.rec);
+  for (uint32_t f = 0; f < faces; f++) {
+    for (uint32_t y = 0; y < H; y++) {
+      const bool yvis = y < by;
+      const bool odd = y & 1;
       for (uint32_t x = 0; x < W; x++) {
-        uint32_t e = row[x];
+        uint32_t e = rb[x];
         uint32_t ref;
-        if (!(y & 1)) {
+        if (!odd) {
           if (!(x & 1)) {
-            const int g = decode_sym(b, l_ref, m_ref);
-            if (g < 0) { err = kStBadCode; break; }
+            const int g = decode_sym_s(b, lR, mR);
+            if (g < 0) return kStBadCode;
             group = (uint32_t)g & 0xFFu;  // reference_group is a uint8
           }
           ref = group & 3u;
           e = (e & ~3u) | ((group >> 2) & 3u);
           group >>= 4;
         } else {
-          ref = rb_ref(e);
+          ref = e & 3u;
         }
-        // endpoint A = colour (DXT1/DXT5) or alpha0 (DXN/DXT5A); B = alpha0 (DXT5) or alpha1 (DXN)
         if (ref == 0) {
-          if (colour) {
-            const int d = decode_sym(b, l_ep0, m_ep0);
-            if (d < 0) { err = kStBadCode; break; }
-            cep += (uint32_t)d;
-            if (cep >= pal.n_cep) cep -= pal.n_cep;
-            if (cep >= pal.n_cep) { err = kStBadIndex; break; }
-          }
-          if (nalpha >= 1) {
-            const int d = decode_sym(b, l_ep1, m_ep1);
-            if (d < 0) { err = kStBadCode; break; }
-            a0 += (uint32_t)d;
-            if (a0 >= pal.n_aep) a0 -= pal.n_aep;
-            if (a0 >= pal.n_aep) { err = kStBadIndex; break; }
-          }
-          if (nalpha == 2) {
-            const int d = decode_sym(b, l_ep1, m_ep1);
-            if (d < 0) { err = kStBadCode; break; }
-            a1 += (uint32_t)d;
-            if (a1 >= pal.n_aep) a1 -= pal.n_aep;
-            if (a1 >= pal.n_aep) { err = kStBadIndex; break; }
+          const int d = decode_sym_s(b, lDA, mDA);
+          if (d < 0) return kStBadCode;
+          iA += (uint32_t)d;
+          if (iA >= nA) iA -= nA;
+          if (iA >= nA) return kStBadIndex;
+          if (two) {
+            const int d2 = decode_sym_s(b, lDB, mDB);
+            if (d2 < 0) return kStBadCode;
+            iB += (uint32_t)d2;
+            if (iB >= nB) iB -= nB;
+            if (iB >= nB) return kStBadIndex;
           }
         }
         if (ref <= 1) {
-          const uint32_t A = colour ? cep : a0;
-          const uint32_t B = KIND == 1 ? a0 : a1;
-          e = (e & 3u) | (A << 2) | (B << 15);
+          e = rb_pack(e & 3u, iA, iB);
         } else {
-          if (colour) cep = rb_a(e); else a0 = rb_a(e);
-          if (KIND == 1) a0 = rb_b(e);
-          if (KIND == 2) a1 = rb_b(e);
+          iA = rb_a(e);
+          iB = rb_b(e);
+          if (iA >= nA || (two && iB >= nB)) return kStBadIndex;
         }
-        row[x] = e;
-        uint32_t cs = 0, s0 = 0, s1 = 0;
-        if (colour) {
-          const int s = decode_sym(b, l_sel0, m_sel0);
-          if (s < 0) { err = kStBadCode; break; }
-          if ((uint32_t)s >= pal.n_csel) { err = kStBadIndex; break; }
-          cs = (uint32_t)s;
+        rb[x] = e;
+        const int sa = decode_sym_s(b, lSA, mSA);
+        if (sa < 0) return kStBadCode;
+        if ((uint32_t)sa >= nSA) return kStBadIndex;
+        uint32_t sb = 0;
+        if (two) {
+          const int t = decode_sym_s(b, lSB, mSB);
+          if (t < 0) return kStBadCode;
+          if ((uint32_t)t >= nSB) return kStBadIndex;
+          sb = (uint32_t)t;
         }
-        if (nalpha >= 1) {
-          const int s = decode_sym(b, l_sel1, m_sel1);
-          if (s < 0) { err = kStBadCode; break; }
-          if ((uint32_t)s >= pal.n_asel) { err = kStBadIndex; break; }
-          s0 = (uint32_t)s;
-        }
-        if (nalpha == 2) {
-          const int s = decode_sym(b, l_sel1, m_sel1);
-          if (s < 0) { err = kStBadCode; break; }
-          if ((uint32_t)s >= pal.n_asel) { err = kStBadIndex; break; }
-          s1 = (uint32_t)s;
-        }
-        if (yvis && x < job.bx) {
-          if (KIND == 0) rec32[out_i] = cep | (cs << 16);
-          else if (KIND == 3) rec32[out_i] = a0 | (s0 << 16);
-          else if (KIND == 1) rec64[out_i] = (uint64_t)(cep | (cs << 16)) | ((uint64_t)(a0 | (s0 << 16)) << 32);
-          else rec64[out_i] = (uint64_t)(a0 | (s0 << 16)) | ((uint64_t)(a1 | (s1 << 16)) << 32);
-          out_i++;
+        if (yvis && x < bx) {
+          const uint32_t lo = iA | ((uint32_t)sa << 16);
+          if (!two) *rec32++ = lo;
+          else *rec64++ = (uint64_t)lo | ((uint64_t)(iB | (sb << 16)) << 32);
         }
       }
     }
   }
+  return kStOk;
+}
+
+// Persistent decoder: one warp per texture (one batch item: one file, up to 32 level streams),
+// one lane per level. The warp stages the file's first-level prefix tables in shared memory, so
+// every lane's symbol lookup is a shared-memory load; each lane keeps its row buffer (packed
+// block_buffer_element entries) in a compact slice of shared memory.
+// Dynamic shared memory: [lut_words table words][rb_total row-buffer words].
+// `counter` must be zero at launch; items are ordered largest first.
+__global__ void __launch_bounds__(32) k_crn_decode_textures(const TexJob* __restrict__ items, uint32_t nitems,
+                                                            const StreamJob* __restrict__ streams,
+                                                            uint32_t* __restrict__ counter, uint32_t lut_words,
+                                                            uint32_t rb_total, uint32_t* __restrict__ status) {
+  extern __shared__ uint32_t smem[];
+  uint32_t* luts = smem;
+  uint32_t* rb_base = smem + lut_words;
+  const uint32_t lane = threadIdx.x;
+  uint32_t err = kStOk;
+  for (;;) {
+    uint32_t it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1u);
+    it = __shfl_sync(0xFFFFFFFFu, it, 0);
+    if (it >= nitems) break;
+    const TexJob T = items[it];
+    const uint32_t kind = T.kind;
+    const uint32_t nm = models_used(kind);
+    if ((nm << kLutBits) > lut_words || T.rb_words > rb_total) { err = max(err, (uint32_t)kStBadCode); continue; }
+    // stage the tables this format reads: ref, delta A, selector A (+ delta B, selector B for DXT5)
+    {
+      const bool colour = kind == kKDxt5 || kind == kKDxt1;
+      const int srcm[5] = {kMRef, colour ? kMEp0 : kMEp1, colour ? kMSel0 : kMSel1, kMEp1, kMSel1};
+      __syncwarp();
+      for (uint32_t t = 0; t < nm; t++) {
+        const uint4* src = reinterpret_cast<const uint4*>(T.models[srcm[t]].lut);
+        uint4* dst = reinterpret_cast<uint4*>(luts + (t << kLutBits));
+        for (uint32_t k = lane; k < (1u << kLutBits) / 4; k += 32) dst[k] = __ldg(src + k);
+      }
+      __syncwarp();
+    }
+    if (lane < T.nlev) {
+      const StreamJob J = streams[T.first + lane];
+      const uint32_t W = (J.bx + 1) & ~1u;
+      if (J.rb_ofs + W <= rb_total && J.kind == kind) {  // host validated; never false
+        uint32_t* rb = rb_base + J.rb_ofs;
+        uint32_t st;
+        switch (kind) {
+          case kKDxt1: st = decode_level<kKDxt1>(J, luts, rb); break;
+          case kKDxt5: st = decode_level<kKDxt5>(J, luts, rb); break;
+          case kKDxn: st = decode_level<kKDxn>(J, luts, rb); break;
+          default: st = decode_level<kKDxt5a>(J, luts, rb); break;
+        }
+        err = max(err, st);
+      }
+    }
+    __syncwarp();
+  }
   if (err) atomicMax(status, err);
 }
 
+// Palette entry index, clamped so that records left unwritten by a stream the decoder rejected
+// as corrupt can never read outside the palette (valid records are already in range).
+__device__ __forceinline__ uint32_t clamp_idx(uint32_t i, uint32_t n) { return i < n ? i : 0u; }
+
+__device__ __forceinline__ uint2 alpha_words(const DevPalettes& pal, uint32_t r) {
+  const uint64_t a = (uint64_t)__ldg(pal.alpha_ep + clamp_idx(r & 0xFFFFu, pal.n_aep)) |
+                     (__ldg(pal.alpha_sel + clamp_idx(r >> 16, pal.n_asel)) << 16);
+  return make_uint2((uint32_t)a, (uint32_t)(a >> 32));
+}
+
 // One 16-byte output chunk per thread: two 8-byte blocks (DXT1/DXT5A) or one 16-byte block.
-template <int KIND>
-__global__ void __launch_bounds__(kExpandThreads) k_crn_expand(const ExpandJob* __restrict__ jobs, int njobs,
-                                                                DevPalettes pal, const void* __restrict__ records,
-                                                                int vec_ok) {
-  // find this CTA's job (jobs are few; cta_begin ascending)
-  int j = 0;
-  while (j + 1 < njobs && jobs[j + 1].cta_begin <= blockIdx.x) j++;
-  const ExpandJob job = jobs[j];
-  const uint32_t local = blockIdx.x - job.cta_begin;
-  const uint32_t rowi = local / job.ctas_per_row;
-  const uint32_t chunk = (local - rowi * job.ctas_per_row) * kExpandThreads + threadIdx.x;
-  const uint32_t f = rowi / job.by, y = rowi - f * job.by;
-  if (f >= job.faces) return;
-  uint8_t* drow = job.dst + f * job.face_stride + (uint64_t)y * job.pitch;
-  const uint64_t rbase = job.rec_ofs + (uint64_t)rowi * job.bx;
-  if (KIND == 0 || KIND == 3) {
+// A CTA covers part of one block row of one face; its job is found by binary search.
+__global__ void __launch_bounds__(kExpandThreads) k_crn_expand_jobs(const ExpandJob* __restrict__ jobs, int njobs,
+                                                                     int vec_ok) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].cta_begin <= blockIdx.x) lo = mid; else hi = mid - 1;
+  }
+  const ExpandJob& J = jobs[lo];
+  const uint32_t local = blockIdx.x - J.cta_begin;
+  const uint32_t y = local / J.ctas_per_row;
+  const uint32_t chunk = (local - y * J.ctas_per_row) * kExpandThreads + threadIdx.x;
+  if (y >= J.by) return;
+  const uint32_t kind = J.kind, bx = J.bx;
+  const DevPalettes pal = J.pal;
+  uint8_t* drow = J.dst + (uint64_t)y * J.pitch;
+  if (kind == kKDxt1 || kind == kKDxt5a) {
     const uint32_t x0 = chunk * 2;
-    if (x0 >= job.bx) return;
-    const uint32_t* rec = reinterpret_cast<const uint32_t*>(records) + rbase;
+    if (x0 >= bx) return;
+    const uint32_t* rec = reinterpret_cast<const uint32_t*>(J.rec) + (uint64_t)y * bx;
     auto word = [&](uint32_t r) -> uint2 {
-      if (KIND == 0) return make_uint2(__ldg(pal.colour_ep + (r & 0xFFFFu)), __ldg(pal.colour_sel + (r >> 16)));
-      const uint64_t a = (uint64_t)__ldg(pal.alpha_ep + (r & 0xFFFFu)) | (__ldg(pal.alpha_sel + (r >> 16)) << 16);
-      return make_uint2((uint32_t)a, (uint32_t)(a >> 32));
+      if (kind == kKDxt1)
+        return make_uint2(__ldg(pal.colour_ep + clamp_idx(r & 0xFFFFu, pal.n_cep)),
+                          __ldg(pal.colour_sel + clamp_idx(r >> 16, pal.n_csel)));
+      return alpha_words(pal, r);
     };
     const uint2 w0 = word(__ldg(rec + x0));
     uint32_t* d = reinterpret_cast<uint32_t*>(drow + (uint64_t)x0 * 8);
-    if (x0 + 1 < job.bx) {
+    if (x0 + 1 < bx) {
       const uint2 w1 = word(__ldg(rec + x0 + 1));
       if (vec_ok) {
         __stcs(reinterpret_cast<uint4*>(d), make_uint4(w0.x, w0.y, w1.x, w1.y));
@@ -294,18 +372,17 @@ __global__ void __launch_bounds__(kExpandThreads) k_crn_expand(const ExpandJob* 
     }
   } else {
     const uint32_t x = chunk;
-    if (x >= job.bx) return;
-    const uint64_t r = __ldg(reinterpret_cast<const unsigned long long*>(records) + rbase + x);
-    const uint32_t lo = (uint32_t)r, hi = (uint32_t)(r >> 32);
+    if (x >= bx) return;
+    const uint64_t r = __ldg(reinterpret_cast<const unsigned long long*>(J.rec) + (uint64_t)y * bx + x);
+    const uint32_t rlo = (uint32_t)r, rhi = (uint32_t)(r >> 32);
     uint4 o;
-    if (KIND == 1) {
-      const uint64_t a = (uint64_t)__ldg(pal.alpha_ep + (hi & 0xFFFFu)) | (__ldg(pal.alpha_sel + (hi >> 16)) << 16);
-      o = make_uint4((uint32_t)a, (uint32_t)(a >> 32), __ldg(pal.colour_ep + (lo & 0xFFFFu)),
-                     __ldg(pal.colour_sel + (lo >> 16)));
+    if (kind == kKDxt5) {
+      const uint2 a = alpha_words(pal, rhi);
+      o = make_uint4(a.x, a.y, __ldg(pal.colour_ep + clamp_idx(rlo & 0xFFFFu, pal.n_cep)),
+                     __ldg(pal.colour_sel + clamp_idx(rlo >> 16, pal.n_csel)));
     } else {
-      const uint64_t a = (uint64_t)__ldg(pal.alpha_ep + (lo & 0xFFFFu)) | (__ldg(pal.alpha_sel + (lo >> 16)) << 16);
-      const uint64_t c = (uint64_t)__ldg(pal.alpha_ep + (hi & 0xFFFFu)) | (__ldg(pal.alpha_sel + (hi >> 16)) << 16);
-      o = make_uint4((uint32_t)a, (uint32_t)(a >> 32), (uint32_t)c, (uint32_t)(c >> 32));
+      const uint2 a = alpha_words(pal, rlo), c = alpha_words(pal, rhi);
+      o = make_uint4(a.x, a.y, c.x, c.y);
     }
     uint32_t* d = reinterpret_cast<uint32_t*>(drow + (uint64_t)x * 16);
     if (vec_ok) __stcs(reinterpret_cast<uint4*>(d), o);
@@ -314,7 +391,7 @@ __global__ void __launch_bounds__(kExpandThreads) k_crn_expand(const ExpandJob* 
 }
 
 // ------------------------------------------------------------------------------------------
-// Host side: the unpack context.
+// Host side.
 
 struct UnpackContext {
   uint32_t magic = 0x43524E47u;
@@ -322,35 +399,19 @@ struct UnpackContext {
   CrnFile file;
   DevBuf d_file, d_models, d_pal, d_jobs, d_records, d_status;
   DevPalettes pal{};
-  uint32_t status_host = 0;
+  uint32_t status_host[2] = {0, 0};
 
-  int kind_id() const { return (int)file.kind; }
-  uint32_t rec_bytes() const { return (file.kind == Kind::DXT1 || file.kind == Kind::DXT5A) ? 4u : 8u; }
+  uint32_t kind() const { return (uint32_t)file.kind; }
+  uint32_t rec_bytes() const { return record_bytes(kind()); }
 };
 
 namespace {
 
-bool valid_ctx(UnpackContext* c) { return c && c->magic == 0x43524E47u; }
+bool valid_ctx(const UnpackContext* c) { return c && c->magic == 0x43524E47u; }
 
-int upload_context(UnpackContext* c, const uint8_t* data, uint32_t size) {
-  CrnFile& F = c->file;
-  cudaError_t e = cudaGetDevice(&c->device);
-  if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
-  // file bytes, padded so word reads near the end stay inside the allocation
-  if ((e = c->d_file.ensure(size + 64)) != cudaSuccess) return cuda_check(e, "alloc file");
-  if ((e = cudaMemcpy(c->d_file.ptr, data, size, cudaMemcpyHostToDevice)) != cudaSuccess)
-    return cuda_check(e, "copy file");
-  std::unique_ptr<DevModel[]> models(new DevModel[kNumModels]);
-  F.ref_dm.to_device(models[kMRef]);
-  F.ep_dm[0].to_device(models[kMEp0]);
-  F.sel_dm[0].to_device(models[kMSel0]);
-  F.ep_dm[1].to_device(models[kMEp1]);
-  F.sel_dm[1].to_device(models[kMSel1]);
-  if ((e = c->d_models.ensure(sizeof(DevModel) * kNumModels)) != cudaSuccess) return cuda_check(e, "alloc models");
-  if ((e = cudaMemcpy(c->d_models.ptr, models.get(), sizeof(DevModel) * kNumModels, cudaMemcpyHostToDevice)) !=
-      cudaSuccess)
-    return cuda_check(e, "copy models");
-  // palettes: colour ep | colour sel | alpha sel (u64) | alpha ep, each 16-byte aligned
+// Palettes in the device layout, packed back to back with 16-byte alignment. `base` is the
+// device address the image will be copied to; returns the image and fills *pal.
+std::vector<uint8_t> palette_image(const CrnFile& F, uint8_t* base, DevPalettes* pal) {
   auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
   const size_t n_cep = F.colour_ep.size(), n_csel = F.colour_sel.size();
   const size_t n_aep = F.alpha_ep.size(), n_asel = F.alpha_sel.size() / 3;
@@ -365,116 +426,274 @@ int upload_context(UnpackContext* c, const uint8_t* data, uint32_t size) {
     std::memcpy(host.data() + o_asel + 8 * i, &v, 8);
   }
   if (n_aep) std::memcpy(host.data() + o_aep, F.alpha_ep.data(), n_aep * 2);
-  if ((e = c->d_pal.ensure(total)) != cudaSuccess) return cuda_check(e, "alloc palettes");
-  if ((e = cudaMemcpy(c->d_pal.ptr, host.data(), total, cudaMemcpyHostToDevice)) != cudaSuccess)
+  pal->colour_ep = reinterpret_cast<const uint32_t*>(base);
+  pal->colour_sel = reinterpret_cast<const uint32_t*>(base + o_csel);
+  pal->alpha_sel = reinterpret_cast<const uint64_t*>(base + o_asel);
+  pal->alpha_ep = reinterpret_cast<const uint16_t*>(base + o_aep);
+  pal->n_cep = (uint32_t)n_cep;
+  pal->n_csel = (uint32_t)n_csel;
+  pal->n_aep = (uint32_t)n_aep;
+  pal->n_asel = (uint32_t)n_asel;
+  return host;
+}
+
+size_t palette_bytes(const CrnFile& F) {
+  auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
+  return al(F.colour_ep.size() * 4) + al(F.colour_sel.size() * 4) + al(F.alpha_sel.size() / 3 * 8) +
+         al(F.alpha_ep.size() * 2) + 16;
+}
+
+std::vector<DevModel> model_image(const CrnFile& F) {
+  std::vector<DevModel> models(kNumModels);
+  F.ref_dm.to_device(models[kMRef]);
+  F.ep_dm[0].to_device(models[kMEp0]);
+  F.sel_dm[0].to_device(models[kMSel0]);
+  F.ep_dm[1].to_device(models[kMEp1]);
+  F.sel_dm[1].to_device(models[kMSel1]);
+  return models;
+}
+
+int upload_context(UnpackContext* c, const uint8_t* data, uint32_t size) {
+  CrnFile& F = c->file;
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
+  // file bytes, padded so word reads near the end stay inside the allocation
+  if ((e = c->d_file.ensure(size + 64)) != cudaSuccess) return cuda_check(e, "alloc file");
+  if ((e = cudaMemcpy(c->d_file.ptr, data, size, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_check(e, "copy file");
+  std::vector<DevModel> models = model_image(F);
+  if ((e = c->d_models.ensure(sizeof(DevModel) * kNumModels)) != cudaSuccess) return cuda_check(e, "alloc models");
+  if ((e = cudaMemcpy(c->d_models.ptr, models.data(), sizeof(DevModel) * kNumModels, cudaMemcpyHostToDevice)) !=
+      cudaSuccess)
+    return cuda_check(e, "copy models");
+  if ((e = c->d_pal.ensure(palette_bytes(F))) != cudaSuccess) return cuda_check(e, "alloc palettes");
+  std::vector<uint8_t> img = palette_image(F, static_cast<uint8_t*>(c->d_pal.ptr), &c->pal);
+  if ((e = cudaMemcpy(c->d_pal.ptr, img.data(), img.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
     return cuda_check(e, "copy palettes");
-  uint8_t* base = static_cast<uint8_t*>(c->d_pal.ptr);
-  c->pal.colour_ep = reinterpret_cast<const uint32_t*>(base);
-  c->pal.colour_sel = reinterpret_cast<const uint32_t*>(base + o_csel);
-  c->pal.alpha_sel = reinterpret_cast<const uint64_t*>(base + o_asel);
-  c->pal.alpha_ep = reinterpret_cast<const uint16_t*>(base + o_aep);
-  c->pal.n_cep = (uint32_t)n_cep;
-  c->pal.n_csel = (uint32_t)n_csel;
-  c->pal.n_aep = (uint32_t)n_aep;
-  c->pal.n_asel = (uint32_t)n_asel;
   if ((e = c->d_status.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc status");
   return CRNGPU_OK;
 }
 
-template <int K>
-void launch_decode(const DecodeJob* jobs, int njobs, UnpackContext* c, void* rec, uint32_t* st, cudaStream_t s) {
-  const size_t smem = sizeof(uint32_t) * (1 << kLutBits) * models_used<K>();  // <= 40 KB, no opt-in needed
-  k_crn_decode<K><<<njobs, 32, smem, s>>>(jobs, njobs, static_cast<const DevModel*>(c->d_models.ptr), c->pal, rec, st);
-}
-template <int K>
-void launch_expand(const ExpandJob* jobs, int njobs, uint32_t ctas, UnpackContext* c, const void* rec, int vec,
-                   cudaStream_t s) {
-  k_crn_expand<K><<<ctas, kExpandThreads, 0, s>>>(jobs, njobs, c->pal, rec, vec);
-}
-
-struct LevelOut {
+// One level of one file to decode and expand (all pointers device memory).
+struct LevelTask {
+  const CrnFile* file;
+  const DevModel* models;
+  DevPalettes pal;
   uint32_t level;
-  uint8_t* dst[6];     // device pointer per face
+  uint8_t* dst[6];     // face pointers
   uint32_t pitch;
-  const uint8_t* src;  // device pointer to the compressed level stream
+  const uint8_t* src;  // compressed level stream
   uint32_t src_size;
+  uint8_t* rec;        // the level's index records (faces x blocks, record_bytes each)
+  uint32_t item;       // texture job this level belongs to (one warp decodes a texture job)
 };
 
-// Decodes and expands a list of levels (all destinations device memory). `records` holds
-// at least sum(blocks) records; `status` is a device word (zeroed here).
-int run_levels(UnpackContext* c, const std::vector<LevelOut>& outs, void* records, uint32_t* status,
-               cudaStream_t s) {
-  const CrnFile& F = c->file;
-  std::vector<DecodeJob> dj;
-  std::vector<ExpandJob> ej;
-  uint64_t rec = 0;
-  uint32_t ctas = 0;
+// Launch plan: jobs image [TexJob x n_item][StreamJob x n_stream][ExpandJob x n_expand],
+// built on the host. Tasks with the same `item` (consecutive) form one texture job.
+struct Plan {
+  std::vector<uint8_t> image;
+  uint32_t n_item = 0, n_stream = 0, n_expand = 0, ctas = 0;
+  uint32_t rb_words = 2;    // largest row-buffer need of one texture job (words)
+  uint32_t lut_words = 0;   // first-level tables staged per texture job (words)
+  size_t stream_ofs = 0, expand_ofs = 0;
   int vec_ok = 1;
-  const uint32_t chunk_blocks = F.bytes_per_block == 8 ? 2 : 1;
-  for (const LevelOut& o : outs) {
-    const LevelInfo& li = F.level[o.level];
-    dj.push_back(DecodeJob{o.src, o.src_size, li.blocks_x, li.blocks_y, F.faces, rec});
-    for (uint32_t f = 0; f < F.faces; f++) {
-      // faces of one level are contiguous in `records`; each face is one expansion job
-      const uint32_t chunks = (li.blocks_x + chunk_blocks - 1) / chunk_blocks;
-      const uint32_t per_row = (chunks + kExpandThreads - 1) / kExpandThreads;
-      ExpandJob j;
-      j.dst = o.dst[f];
-      j.face_stride = 0;
-      j.rec_ofs = rec + (uint64_t)f * li.blocks_x * li.blocks_y;
+};
+
+uint64_t level_records(const CrnFile& F, uint32_t l) {
+  return (uint64_t)F.level[l].blocks_x * F.level[l].blocks_y * F.faces;
+}
+
+// false if a texture job would not fit the decoder (more than 32 levels or rows too wide)
+bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
+  std::vector<TexJob> items;
+  std::vector<std::vector<StreamJob>> item_streams;
+  for (size_t i = 0; i < tasks.size();) {
+    size_t k = i;
+    while (k < tasks.size() && tasks[k].item == tasks[i].item) k++;
+    if (k - i > 32) return false;
+    const CrnFile& F = *tasks[i].file;
+    const uint32_t kind = (uint32_t)F.kind;
+    const bool colour = kind == kKDxt1 || kind == kKDxt5;
+    TexJob T{};
+    T.models = tasks[i].models;
+    T.nlev = (uint32_t)(k - i);
+    T.kind = kind;
+    std::vector<StreamJob> sj;
+    uint32_t rb = 0;
+    for (size_t t = i; t < k; t++) {
+      const LevelInfo& li = F.level[tasks[t].level];
+      StreamJob j{};
+      j.src = tasks[t].src;
+      j.src_size = tasks[t].src_size;
+      j.models = tasks[t].models;
+      j.rec = tasks[t].rec;
       j.bx = li.blocks_x;
       j.by = li.blocks_y;
-      j.faces = 1;
-      j.pitch = o.pitch;
+      j.faces = F.faces;
+      j.kind = kind;
+      j.n_a = colour ? tasks[t].pal.n_cep : tasks[t].pal.n_aep;
+      j.n_b = tasks[t].pal.n_aep;
+      j.n_sa = colour ? tasks[t].pal.n_csel : tasks[t].pal.n_asel;
+      j.n_sb = tasks[t].pal.n_asel;
+      j.rb_ofs = rb;
+      rb += (li.blocks_x + 1) & ~1u;
+      T.work = std::max<uint64_t>(T.work, (uint64_t)li.blocks_x * li.blocks_y * F.faces * (kind == kKDxt1 || kind == kKDxt5a ? 1 : 2));
+      sj.push_back(j);
+    }
+    T.rb_words = rb;
+    p.rb_words = std::max(p.rb_words, rb);
+    p.lut_words = std::max(p.lut_words, models_used(kind) << kLutBits);
+    items.push_back(T);
+    item_streams.push_back(std::move(sj));
+    i = k;
+  }
+  // largest textures first: the persistent warps then finish at about the same time
+  std::vector<size_t> order(items.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return items[a].work > items[b].work; });
+  std::vector<TexJob> it_sorted;
+  std::vector<StreamJob> sj;
+  for (size_t o : order) {
+    TexJob T = items[o];
+    T.first = (uint32_t)sj.size();
+    it_sorted.push_back(T);
+    sj.insert(sj.end(), item_streams[o].begin(), item_streams[o].end());
+  }
+  std::vector<ExpandJob> ej;
+  uint32_t ctas = 0;
+  for (const LevelTask& t : tasks) {
+    const CrnFile& F = *t.file;
+    const LevelInfo& li = F.level[t.level];
+    const uint32_t kind = (uint32_t)F.kind;
+    const uint32_t chunk_blocks = F.bytes_per_block == 8 ? 2 : 1;
+    const uint32_t chunks = (li.blocks_x + chunk_blocks - 1) / chunk_blocks;
+    const uint32_t per_row = (chunks + kExpandThreads - 1) / kExpandThreads;
+    for (uint32_t f = 0; f < F.faces; f++) {
+      ExpandJob j;
+      j.dst = t.dst[f];
+      j.rec = t.rec + (uint64_t)f * li.blocks_x * li.blocks_y * record_bytes(kind);
+      j.pal = t.pal;
+      j.bx = li.blocks_x;
+      j.by = li.blocks_y;
+      j.pitch = t.pitch;
+      j.kind = kind;
       j.cta_begin = ctas;
       j.ctas_per_row = per_row;
       ctas += per_row * li.blocks_y;
       ej.push_back(j);
-      if (((uintptr_t)o.dst[f] | o.pitch) & 15) vec_ok = 0;
+      if (((uintptr_t)t.dst[f] | t.pitch) & 15) p.vec_ok = 0;
     }
-    rec += (uint64_t)li.blocks_x * li.blocks_y * F.faces;
   }
-  const size_t jb = sizeof(DecodeJob) * dj.size(), eb = sizeof(ExpandJob) * ej.size();
-  cudaError_t e = c->d_jobs.ensure(jb + eb + 16);
-  if (e != cudaSuccess) return cuda_check(e, "alloc jobs");
-  std::vector<uint8_t> hj(jb + eb);
-  std::memcpy(hj.data(), dj.data(), jb);
-  std::memcpy(hj.data() + jb, ej.data(), eb);
-  if ((e = cudaMemcpyAsync(c->d_jobs.ptr, hj.data(), hj.size(), cudaMemcpyHostToDevice, s)) != cudaSuccess)
-    return cuda_check(e, "copy jobs");
-  if ((e = cudaMemsetAsync(status, 0, 4, s)) != cudaSuccess) return cuda_check(e, "clear status");
-  const DecodeJob* djd = static_cast<const DecodeJob*>(c->d_jobs.ptr);
-  const ExpandJob* ejd = reinterpret_cast<const ExpandJob*>(static_cast<uint8_t*>(c->d_jobs.ptr) + jb);
-  switch (F.kind) {
-    case Kind::DXT1: launch_decode<0>(djd, (int)dj.size(), c, records, status, s); break;
-    case Kind::DXT5: launch_decode<1>(djd, (int)dj.size(), c, records, status, s); break;
-    case Kind::DXN: launch_decode<2>(djd, (int)dj.size(), c, records, status, s); break;
-    case Kind::DXT5A: launch_decode<3>(djd, (int)dj.size(), c, records, status, s); break;
+  p.n_item = (uint32_t)it_sorted.size();
+  p.n_stream = (uint32_t)sj.size();
+  p.n_expand = (uint32_t)ej.size();
+  p.ctas = ctas;
+  auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  p.stream_ofs = al(sizeof(TexJob) * it_sorted.size());
+  p.expand_ofs = p.stream_ofs + al(sizeof(StreamJob) * sj.size());
+  p.image.assign(p.expand_ofs + sizeof(ExpandJob) * ej.size(), 0);
+  std::memcpy(p.image.data(), it_sorted.data(), sizeof(TexJob) * it_sorted.size());
+  std::memcpy(p.image.data() + p.stream_ofs, sj.data(), sizeof(StreamJob) * sj.size());
+  std::memcpy(p.image.data() + p.expand_ofs, ej.data(), sizeof(ExpandJob) * ej.size());
+  return true;
+}
+
+// Persistent decoder grid: CTAs of one warp, as many as shared memory lets reside on every SM.
+int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
+  static int sms[64] = {}, smem_sm[64] = {};
+  static bool attr_set[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) { set_error("device index out of range"); return CRNGPU_E_PARAM; }
+  if (!sms[dev]) {
+    if ((e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      return cuda_check(e, "device attribute");
+    if ((e = cudaDeviceGetAttribute(&smem_sm[dev], cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
+      return cuda_check(e, "device attribute");
   }
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_decode");
-  if (ctas) {
-    switch (F.kind) {
-      case Kind::DXT1: launch_expand<0>(ejd, (int)ej.size(), ctas, c, records, vec_ok, s); break;
-      case Kind::DXT5: launch_expand<1>(ejd, (int)ej.size(), ctas, c, records, vec_ok, s); break;
-      case Kind::DXN: launch_expand<2>(ejd, (int)ej.size(), ctas, c, records, vec_ok, s); break;
-      case Kind::DXT5A: launch_expand<3>(ejd, (int)ej.size(), ctas, c, records, vec_ok, s); break;
-    }
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_expand");
+  if (!attr_set[dev]) {
+    if ((e = cudaFuncSetAttribute(k_crn_decode_textures, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)kDecodeSmemMax)) != cudaSuccess)
+      return cuda_check(e, "decoder shared memory attribute");
+    attr_set[dev] = true;
   }
-  // the reference reports a bad stream through its bool result; read the status word back
-  if ((e = cudaMemcpyAsync(&c->status_host, status, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-    return cuda_check(e, "read status");
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
-  if (c->status_host) {
-    set_error(c->status_host == kStBadCode ? "corrupt block stream (no such prefix code)"
-                                           : "corrupt block stream (palette index out of range)");
-    return CRNGPU_E_CORRUPT;
+  *smem = (size_t)(p.lut_words + p.rb_words) * sizeof(uint32_t);
+  const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(32, (uint32_t)(smem_sm[dev] / (*smem + 1024))));
+  *grid = std::max<uint32_t>(1, std::min<uint32_t>(p.n_item, per_sm * (uint32_t)sms[dev]));
+  return CRNGPU_OK;
+}
+
+// Enqueues the counter/status clear, the decoder and the expansion for a plan whose image is
+// already at d_jobs. `words` = 2 device words: [0] work counter, [1] status. Asynchronous.
+int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStream_t s) {
+  if ((size_t)(p.lut_words + p.rb_words) * 4 > kDecodeSmemMax) {
+    set_error("texture rows too wide for the decoder");
+    return CRNGPU_E_PARAM;
+  }
+  uint32_t grid = 0;
+  size_t smem = 0;
+  int rc = decode_grid(p, &grid, &smem);
+  if (rc != CRNGPU_OK) return rc;
+  cudaError_t e = cudaMemsetAsync(words, 0, 8, s);
+  if (e != cudaSuccess) return cuda_check(e, "clear work counter");
+  const TexJob* tj = reinterpret_cast<const TexJob*>(d_jobs);
+  const StreamJob* sj = reinterpret_cast<const StreamJob*>(d_jobs + p.stream_ofs);
+  const ExpandJob* ej = reinterpret_cast<const ExpandJob*>(d_jobs + p.expand_ofs);
+  if (p.n_item) {
+    k_crn_decode_textures<<<grid, 32, smem, s>>>(tj, p.n_item, sj, words, p.lut_words, p.rb_words, words + 1);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_decode_textures");
+  }
+  if (p.ctas) {
+    k_crn_expand_jobs<<<p.ctas, kExpandThreads, 0, s>>>(ej, (int)p.n_expand, p.vec_ok);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_expand_jobs");
   }
   return CRNGPU_OK;
 }
 
-uint64_t level_records(const CrnFile& F, uint32_t l) {
-  return (uint64_t)F.level[l].blocks_x * F.level[l].blocks_y * F.faces;
+int status_to_rc(uint32_t st) {
+  if (!st) return CRNGPU_OK;
+  set_error(st == kStBadCode ? "corrupt block stream (no such prefix code)"
+                             : "corrupt block stream (palette index out of range)");
+  return CRNGPU_E_CORRUPT;
+}
+
+// Decodes and expands a list of levels of one context (destinations device memory), then
+// reads the status word back (synchronises `s`).
+int run_levels(UnpackContext* c, std::vector<LevelTask>& tasks, cudaStream_t s) {
+  uint64_t rec = 0;
+  for (LevelTask& t : tasks) rec += level_records(c->file, t.level) * c->rec_bytes();
+  cudaError_t e = c->d_records.ensure(rec + 16);
+  if (e != cudaSuccess) return cuda_check(e, "alloc records");
+  uint64_t ofs = 0;
+  for (LevelTask& t : tasks) {
+    t.rec = static_cast<uint8_t*>(c->d_records.ptr) + ofs;
+    ofs += level_records(c->file, t.level) * c->rec_bytes();
+  }
+  Plan p;
+  if (!make_plan(tasks, p)) { set_error("too many levels in one texture job"); return CRNGPU_E_PARAM; }
+  if ((e = c->d_jobs.ensure(p.image.size() + 16)) != cudaSuccess) return cuda_check(e, "alloc jobs");
+  if ((e = cudaMemcpyAsync(c->d_jobs.ptr, p.image.data(), p.image.size(), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+    return cuda_check(e, "copy jobs");
+  uint32_t* words = static_cast<uint32_t*>(c->d_status.ptr);
+  int rc = enqueue_plan(p, static_cast<const uint8_t*>(c->d_jobs.ptr), words, s);
+  if (rc != CRNGPU_OK) return rc;
+  // the reference reports a bad stream through its bool result; read the status word back
+  if ((e = cudaMemcpyAsync(c->status_host, words, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    return cuda_check(e, "read status");
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
+  return status_to_rc(c->status_host[1]);
+}
+
+LevelTask context_task(UnpackContext* c, uint32_t level) {
+  LevelTask t{};
+  t.file = &c->file;
+  t.models = static_cast<const DevModel*>(c->d_models.ptr);
+  t.pal = c->pal;
+  t.level = level;
+  t.src = static_cast<const uint8_t*>(c->d_file.ptr) + c->file.level[level].ofs;
+  t.src_size = c->file.level[level].size;
+  return t;
 }
 
 // Shared implementation of crngpu_unpack_level / _segmented.
@@ -495,48 +714,84 @@ int unpack_one(UnpackContext* c, const uint8_t* host_src, const uint8_t* dev_src
     if (!dst_faces[f]) { set_error("NULL face pointer"); return CRNGPU_E_PARAM; }
   cudaStream_t s = as_stream(stream);
   cudaError_t e;
-  LevelOut o;
-  o.level = level;
-  o.pitch = row_pitch;
-  if (dev_src) { o.src = dev_src; o.src_size = src_size; }
+  LevelTask t = context_task(c, level);
+  t.pitch = row_pitch;
+  if (dev_src) { t.src = dev_src; t.src_size = src_size; }
   else if (host_src) {
     DevBuf& sb = staging(2);
     if ((e = sb.ensure(src_size + 64)) != cudaSuccess) return cuda_check(e, "alloc segment");
     if ((e = cudaMemcpyAsync(sb.ptr, host_src, src_size, cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return cuda_check(e, "copy segment");
-    o.src = static_cast<const uint8_t*>(sb.ptr);
-    o.src_size = src_size;
-  } else {
-    o.src = static_cast<const uint8_t*>(c->d_file.ptr) + li.ofs;
-    o.src_size = li.size;
+    t.src = static_cast<const uint8_t*>(sb.ptr);
+    t.src_size = src_size;
   }
   DevBuf* out_stage = nullptr;
   if (mem == CRNGPU_MEM_DEVICE) {
-    for (uint32_t f = 0; f < F.faces; f++) o.dst[f] = static_cast<uint8_t*>(dst_faces[f]);
+    for (uint32_t f = 0; f < F.faces; f++) t.dst[f] = static_cast<uint8_t*>(dst_faces[f]);
   } else {
     out_stage = &staging(1);
     if ((e = out_stage->ensure(face_bytes * F.faces)) != cudaSuccess) return cuda_check(e, "alloc output stage");
-    for (uint32_t f = 0; f < F.faces; f++) o.dst[f] = static_cast<uint8_t*>(out_stage->ptr) + face_bytes * f;
+    for (uint32_t f = 0; f < F.faces; f++) t.dst[f] = static_cast<uint8_t*>(out_stage->ptr) + face_bytes * f;
     // rows may have pitch padding the transcoder does not write: keep the caller's bytes there
     if (row_pitch != minimal)
       for (uint32_t f = 0; f < F.faces; f++)
-        if ((e = cudaMemcpyAsync(o.dst[f], dst_faces[f], face_bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        if ((e = cudaMemcpyAsync(t.dst[f], dst_faces[f], face_bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
           return cuda_check(e, "stage output");
   }
-  if ((e = c->d_records.ensure(level_records(F, level) * c->rec_bytes() + 16)) != cudaSuccess)
-    return cuda_check(e, "alloc records");
-  int rc = run_levels(c, {o}, c->d_records.ptr, static_cast<uint32_t*>(c->d_status.ptr), s);
+  std::vector<LevelTask> tasks{t};
+  int rc = run_levels(c, tasks, s);
   if (rc != CRNGPU_OK) return rc;
   if (out_stage) {
     for (uint32_t f = 0; f < F.faces; f++)
-      if ((e = cudaMemcpyAsync(dst_faces[f], o.dst[f], face_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+      if ((e = cudaMemcpyAsync(dst_faces[f], tasks[0].dst[f], face_bytes, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
         return cuda_check(e, "copy output");
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   }
   return CRNGPU_OK;
 }
 
+// Output bytes of levels [first, first + count) at minimal pitch.
+uint64_t levels_bytes(const CrnFile& F, uint32_t first, uint32_t count) {
+  uint64_t total = 0;
+  for (uint32_t l = first; l < first + count; l++)
+    total += (uint64_t)F.level[l].blocks_x * F.bytes_per_block * F.level[l].blocks_y * F.faces;
+  return total;
+}
+
+// Level tasks writing levels [first, first + count) back to back at `out` (minimal pitch).
+void levels_tasks(UnpackContext* c, uint32_t first, uint32_t count, uint8_t* out, uint32_t item,
+                  std::vector<LevelTask>& tasks) {
+  const CrnFile& F = c->file;
+  uint64_t ofs = 0;
+  for (uint32_t l = first; l < first + count; l++) {
+    LevelTask t = context_task(c, l);
+    t.item = item;
+    t.pitch = F.level[l].blocks_x * F.bytes_per_block;
+    const uint64_t face_bytes = (uint64_t)t.pitch * F.level[l].blocks_y;
+    for (uint32_t f = 0; f < F.faces; f++) t.dst[f] = out + ofs + f * face_bytes;
+    ofs += face_bytes * F.faces;
+    tasks.push_back(t);
+  }
+}
+
 }  // namespace
+
+// A prepared batch: many levels of many contexts, decoded by one persistent launch and expanded
+// by one more. The job tables and record buffer are uploaded/allocated once at creation, so a
+// launch only enqueues a memset and two kernels (and can replay as a CUDA graph).
+struct UnpackBatch {
+  uint32_t magic = 0x42415443u;
+  int device = -1;
+  Plan plan;
+  DevBuf d_jobs, d_records, d_words;
+  uint32_t words_host[2] = {0, 0};
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  uint64_t out_bytes = 0;
+  ~UnpackBatch() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
 
 }  // namespace crngpu
 
@@ -544,6 +799,7 @@ using namespace crngpu;
 
 extern "C" crngpu_unpack_context crngpu_unpack_begin(const void* data, uint32_t data_size) {
   clear_error();
+  if (!data) { set_error("NULL data"); return nullptr; }
   std::unique_ptr<UnpackContext> c(new UnpackContext());
   if (!c->file.parse(static_cast<const uint8_t*>(data), data_size)) {
     set_error(c->file.error);
@@ -593,12 +849,7 @@ extern "C" int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t firs
     set_error("bad context, destination or level range");
     return CRNGPU_E_PARAM;
   }
-  const CrnFile& F = c->file;
-  uint64_t total = 0, recs = 0;
-  for (uint32_t l = first_level; l < first_level + level_count; l++) {
-    total += (uint64_t)F.level[l].blocks_x * F.bytes_per_block * F.level[l].blocks_y * F.faces;
-    recs += level_records(F, l);
-  }
+  const uint64_t total = levels_bytes(c->file, first_level, level_count);
   if (dst_size < total) { set_error("destination too small"); return CRNGPU_E_PARAM; }
   cudaStream_t s = as_stream(stream);
   cudaError_t e;
@@ -609,21 +860,9 @@ extern "C" int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t firs
     if ((e = stage->ensure(total)) != cudaSuccess) return cuda_check(e, "alloc output stage");
     out = static_cast<uint8_t*>(stage->ptr);
   }
-  std::vector<LevelOut> outs;
-  uint64_t ofs = 0;
-  for (uint32_t l = first_level; l < first_level + level_count; l++) {
-    LevelOut o;
-    o.level = l;
-    o.pitch = F.level[l].blocks_x * F.bytes_per_block;
-    const uint64_t face_bytes = (uint64_t)o.pitch * F.level[l].blocks_y;
-    for (uint32_t f = 0; f < F.faces; f++) o.dst[f] = out + ofs + f * face_bytes;
-    o.src = static_cast<const uint8_t*>(c->d_file.ptr) + F.level[l].ofs;
-    o.src_size = F.level[l].size;
-    ofs += face_bytes * F.faces;
-    outs.push_back(o);
-  }
-  if ((e = c->d_records.ensure(recs * c->rec_bytes() + 16)) != cudaSuccess) return cuda_check(e, "alloc records");
-  int rc = run_levels(c, outs, c->d_records.ptr, static_cast<uint32_t*>(c->d_status.ptr), s);
+  std::vector<LevelTask> tasks;
+  levels_tasks(c, first_level, level_count, out, 0, tasks);
+  int rc = run_levels(c, tasks, s);
   if (rc != CRNGPU_OK) return rc;
   if (stage) {
     if ((e = cudaMemcpyAsync(dst, stage->ptr, total, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
@@ -631,6 +870,108 @@ extern "C" int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t firs
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   }
   return (int64_t)total;
+}
+
+extern "C" crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_batch_item* items, uint32_t n) {
+  clear_error();
+  if (!items || !n) { set_error("empty batch"); return nullptr; }
+  std::unique_ptr<UnpackBatch> b(new UnpackBatch());
+  cudaError_t e = cudaGetDevice(&b->device);
+  if (e != cudaSuccess) { cuda_check(e, "cudaGetDevice"); return nullptr; }
+  std::vector<LevelTask> tasks;
+  uint64_t rec = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    UnpackContext* c = reinterpret_cast<UnpackContext*>(items[i].ctx);
+    if (!valid_ctx(c) || !items[i].dst || !items[i].level_count ||
+        items[i].first_level + items[i].level_count > c->file.levels || c->device != b->device) {
+      set_error("batch item " + std::to_string(i) + ": bad context, destination, level range or device");
+      return nullptr;
+    }
+    const uint64_t need = levels_bytes(c->file, items[i].first_level, items[i].level_count);
+    if (items[i].dst_size < need) {
+      set_error("batch item " + std::to_string(i) + ": destination too small");
+      return nullptr;
+    }
+    b->out_bytes += need;
+    const size_t first = tasks.size();
+    levels_tasks(c, items[i].first_level, items[i].level_count, static_cast<uint8_t*>(items[i].dst), i, tasks);
+    for (size_t k = first; k < tasks.size(); k++) {
+      rec = (rec + 7) & ~(uint64_t)7;
+      tasks[k].rec = reinterpret_cast<uint8_t*>(rec);  // offset for now; rebased below
+      rec += level_records(c->file, tasks[k].level) * c->rec_bytes();
+    }
+  }
+  if ((e = b->d_records.ensure(rec + 16)) != cudaSuccess) { cuda_check(e, "alloc records"); return nullptr; }
+  for (LevelTask& t : tasks) t.rec = static_cast<uint8_t*>(b->d_records.ptr) + reinterpret_cast<uintptr_t>(t.rec);
+  if (!make_plan(tasks, b->plan)) { set_error("too many levels in one batch item"); return nullptr; }
+  if ((e = b->d_jobs.ensure(b->plan.image.size() + 16)) != cudaSuccess) { cuda_check(e, "alloc jobs"); return nullptr; }
+  if ((e = cudaMemcpy(b->d_jobs.ptr, b->plan.image.data(), b->plan.image.size(), cudaMemcpyHostToDevice)) !=
+      cudaSuccess) {
+    cuda_check(e, "copy jobs");
+    return nullptr;
+  }
+  if ((e = b->d_words.ensure(16)) != cudaSuccess) { cuda_check(e, "alloc status"); return nullptr; }
+  // resolve the decoder's launch shape (and its shared-memory attribute) outside any capture
+  uint32_t grid = 0;
+  size_t smem = 0;
+  if (decode_grid(b->plan, &grid, &smem) != CRNGPU_OK) return nullptr;
+  return reinterpret_cast<crngpu_unpack_batch>(b.release());
+}
+
+extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, int use_graph, void* stream) {
+  clear_error();
+  UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
+  if (!b || b->magic != 0x42415443u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
+  cudaStream_t s = as_stream(stream);
+  const uint8_t* jobs = static_cast<const uint8_t*>(b->d_jobs.ptr);
+  uint32_t* words = static_cast<uint32_t*>(b->d_words.ptr);
+  if (!use_graph) return enqueue_plan(b->plan, jobs, words, s);
+  cudaError_t e;
+  if (!b->graph) {
+    // capture on a private stream (the legacy default stream cannot be captured), then replay
+    cudaStream_t cap;
+    if ((e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking)) != cudaSuccess) return cuda_check(e, "stream");
+    cudaGraph_t g = nullptr;
+    if ((e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+      cudaStreamDestroy(cap);
+      return cuda_check(e, "begin capture");
+    }
+    int rc = enqueue_plan(b->plan, jobs, words, cap);
+    e = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (rc != CRNGPU_OK) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return cuda_check(e, "end capture");
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { b->graph = nullptr; return cuda_check(e, "instantiate graph"); }
+  }
+  if ((e = cudaGraphLaunch(b->graph, s)) != cudaSuccess) return cuda_check(e, "graph launch");
+  return CRNGPU_OK;
+}
+
+extern "C" int crngpu_unpack_batch_status(crngpu_unpack_batch batch, void* stream) {
+  clear_error();
+  UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
+  if (!b || b->magic != 0x42415443u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
+  cudaStream_t s = as_stream(stream);
+  cudaError_t e = cudaMemcpyAsync(b->words_host, b->d_words.ptr, 8, cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return cuda_check(e, "read status");
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
+  return status_to_rc(b->words_host[1]);
+}
+
+extern "C" int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch) {
+  UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
+  if (!b || b->magic != 0x42415443u) return CRNGPU_E_PARAM;
+  return (int64_t)b->out_bytes;
+}
+
+extern "C" int crngpu_unpack_batch_destroy(crngpu_unpack_batch batch) {
+  UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
+  if (!b || b->magic != 0x42415443u) return CRNGPU_E_PARAM;
+  b->magic = 0;
+  delete b;
+  return CRNGPU_OK;
 }
 
 extern "C" int crngpu_unpack_end(crngpu_unpack_context ctx) {
@@ -671,14 +1012,14 @@ extern "C" void crngpu_crn_decompress(void* src, unsigned int src_size, void* ds
 // real-time loops where cudaMalloc/cudaFree would block until the device is idle and stall other
 // work. crngpu_unpack_level_noalloc transcodes from a .crn in host memory into the caller's
 // device buffers and keeps everything else it needs -- decode tables, palettes, the level's
-// compressed bytes, the per-block index records, launch descriptors and the status word -- in
-// the fixed array below, which every GPU that loads this library holds until the process exits.
-// It never calls cudaMalloc, cudaFree or any allocating library routine on the device side; the
-// host side only parses the file into ordinary heap memory.
+// compressed bytes, the per-block index records, launch descriptors, the work counter and the
+// status word -- in the fixed array below, which every GPU that loads this library holds until
+// the process exits. It never calls cudaMalloc, cudaFree or any allocating library routine on
+// the device side; the host side only parses the file into ordinary heap memory.
 //
-// All calls share this one array and it keeps the contents of the last call: the status word is
-// cleared on every call, and calls whose work overlaps on the GPU (other threads or streams)
-// race on it, so callers serialise them.
+// All calls share this one array and it keeps the contents of the last call: the work counter
+// and status word are cleared on every call, and calls whose work overlaps on the GPU (other
+// threads or streams) race on it, so callers serialise them.
 namespace crngpu {
 
 constexpr size_t kNoAllocScratchBytes = 16u << 20;  // 16 MiB: tables, palettes, stream, records
@@ -726,17 +1067,13 @@ extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_si
   for (uint32_t f = 0; f < F.faces; f++)
     if (!dst_faces[f]) { set_error("NULL face pointer"); return CRNGPU_E_PARAM; }
 
-  // scratch layout: [status | jobs][models][palettes][level stream][records]
+  // scratch layout: [counter, status | jobs][models][palettes][level stream][records]
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-  const size_t n_cep = F.colour_ep.size(), n_csel = F.colour_sel.size();
-  const size_t n_aep = F.alpha_ep.size(), n_asel = F.alpha_sel.size() / 3;
   const size_t o_jobs = 256, o_models = 4096;
-  const size_t o_cep = o_models + al(sizeof(DevModel) * kNumModels);
-  const size_t o_csel = o_cep + al(n_cep * 4), o_asel = o_csel + al(n_csel * 4), o_aep = o_asel + al(n_asel * 8);
-  const size_t o_src = o_aep + al(n_aep * 2);
+  const size_t o_pal = o_models + al(sizeof(DevModel) * kNumModels);
+  const size_t o_src = o_pal + al(palette_bytes(F));
   const size_t o_rec = o_src + al((size_t)li.size + 64);
-  const size_t rec_bytes = (size_t)li.blocks_x * li.blocks_y * F.faces *
-                           ((F.kind == Kind::DXT1 || F.kind == Kind::DXT5A) ? 4u : 8u);
+  const size_t rec_bytes = (size_t)li.blocks_x * li.blocks_y * F.faces * record_bytes((uint32_t)F.kind);
   const size_t need = o_rec + al(rec_bytes);
   if (need > kNoAllocScratchBytes) {
     set_error("level needs " + std::to_string(need) + " bytes of scratch; the allocation-free entry point has " +
@@ -749,50 +1086,28 @@ extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_si
   cudaStream_t s = as_stream(stream);
   cudaError_t e;
   // host images of the tables, palettes and launch descriptors (ordinary heap, copied below)
-  std::vector<DevModel> models(kNumModels);
-  F.ref_dm.to_device(models[kMRef]);
-  F.ep_dm[0].to_device(models[kMEp0]);
-  F.sel_dm[0].to_device(models[kMSel0]);
-  F.ep_dm[1].to_device(models[kMEp1]);
-  F.sel_dm[1].to_device(models[kMSel1]);
-  std::vector<uint64_t> asel64(n_asel);
-  for (size_t i = 0; i < n_asel; i++)
-    asel64[i] = (uint64_t)F.alpha_sel[3 * i] | ((uint64_t)F.alpha_sel[3 * i + 1] << 16) |
-                ((uint64_t)F.alpha_sel[3 * i + 2] << 32);
+  std::vector<DevModel> models = model_image(F);
   DevPalettes pal;
-  pal.colour_ep = reinterpret_cast<const uint32_t*>(base + o_cep);
-  pal.colour_sel = reinterpret_cast<const uint32_t*>(base + o_csel);
-  pal.alpha_sel = reinterpret_cast<const uint64_t*>(base + o_asel);
-  pal.alpha_ep = reinterpret_cast<const uint16_t*>(base + o_aep);
-  pal.n_cep = (uint32_t)n_cep; pal.n_csel = (uint32_t)n_csel; pal.n_aep = (uint32_t)n_aep; pal.n_asel = (uint32_t)n_asel;
-  DecodeJob dj{base + o_src, li.size, li.blocks_x, li.blocks_y, F.faces, 0};
-  ExpandJob ej[6];
-  const uint32_t chunk_blocks = F.bytes_per_block == 8 ? 2 : 1;
-  const uint32_t per_row = ((li.blocks_x + chunk_blocks - 1) / chunk_blocks + kExpandThreads - 1) / kExpandThreads;
-  int vec_ok = 1;
-  for (uint32_t f = 0; f < F.faces; f++) {
-    ej[f].dst = static_cast<uint8_t*>(dst_faces[f]);
-    ej[f].face_stride = 0;
-    ej[f].rec_ofs = (uint64_t)f * li.blocks_x * li.blocks_y;
-    ej[f].bx = li.blocks_x; ej[f].by = li.blocks_y; ej[f].faces = 1; ej[f].pitch = pitch;
-    ej[f].cta_begin = f * per_row * li.blocks_y;
-    ej[f].ctas_per_row = per_row;
-    if (((uintptr_t)dst_faces[f] | pitch) & 15) vec_ok = 0;
-  }
-  unsigned char jobs[sizeof(DecodeJob) + 6 * sizeof(ExpandJob)];
-  std::memcpy(jobs, &dj, sizeof(dj));
-  std::memcpy(jobs + sizeof(dj), ej, sizeof(ExpandJob) * F.faces);
-  uint32_t* status = reinterpret_cast<uint32_t*>(base);
-  const DecodeJob* d_dj = reinterpret_cast<const DecodeJob*>(base + o_jobs);
-  const ExpandJob* d_ej = reinterpret_cast<const ExpandJob*>(base + o_jobs + sizeof(DecodeJob));
+  std::vector<uint8_t> pal_img = palette_image(F, base + o_pal, &pal);
+  LevelTask t{};
+  t.file = &F;
+  t.models = reinterpret_cast<const DevModel*>(base + o_models);
+  t.pal = pal;
+  t.level = level_index;
+  for (uint32_t f = 0; f < F.faces; f++) t.dst[f] = static_cast<uint8_t*>(dst_faces[f]);
+  t.pitch = pitch;
+  t.src = base + o_src;
+  t.src_size = li.size;
+  t.rec = base + o_rec;
+  t.item = 0;
+  Plan p;
+  if (!make_plan({t}, p)) { set_error("bad level"); return CRNGPU_E_PARAM; }
+  if (p.image.size() > o_models - o_jobs) { set_error("launch descriptors too large"); return CRNGPU_E_PARAM; }
   struct Copy { size_t ofs; const void* src; size_t bytes; };
   const Copy copies[] = {
-      {o_jobs, jobs, sizeof(DecodeJob) + sizeof(ExpandJob) * F.faces},
+      {o_jobs, p.image.data(), p.image.size()},
       {o_models, models.data(), sizeof(DevModel) * kNumModels},
-      {o_cep, F.colour_ep.data(), n_cep * 4},
-      {o_csel, F.colour_sel.data(), n_csel * 4},
-      {o_asel, asel64.data(), n_asel * 8},
-      {o_aep, F.alpha_ep.data(), n_aep * 2},
+      {o_pal, pal_img.data(), pal_img.size()},
       {o_src, static_cast<const uint8_t*>(crn_data) + li.ofs, li.size},
   };
   for (const Copy& c : copies) {
@@ -800,36 +1115,10 @@ extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_si
     if ((e = cudaMemcpyAsync(base + c.ofs, c.src, c.bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return cuda_check(e, "copy into the fixed scratch");
   }
-  if ((e = cudaMemsetAsync(status, 0, 4, s)) != cudaSuccess) return cuda_check(e, "clear status");
-  const DevModel* d_models = reinterpret_cast<const DevModel*>(base + o_models);
-  void* records = base + o_rec;
-  const uint32_t ctas = per_row * li.blocks_y * F.faces;
-  switch (F.kind) {
-    case Kind::DXT1:
-      k_crn_decode<0><<<1, 32, sizeof(uint32_t) * (1 << kLutBits) * models_used<0>(), s>>>(d_dj, 1, d_models, pal, records, status);
-      k_crn_expand<0><<<ctas, kExpandThreads, 0, s>>>(d_ej, (int)F.faces, pal, records, vec_ok);
-      break;
-    case Kind::DXT5:
-      k_crn_decode<1><<<1, 32, sizeof(uint32_t) * (1 << kLutBits) * models_used<1>(), s>>>(d_dj, 1, d_models, pal, records, status);
-      k_crn_expand<1><<<ctas, kExpandThreads, 0, s>>>(d_ej, (int)F.faces, pal, records, vec_ok);
-      break;
-    case Kind::DXN:
-      k_crn_decode<2><<<1, 32, sizeof(uint32_t) * (1 << kLutBits) * models_used<2>(), s>>>(d_dj, 1, d_models, pal, records, status);
-      k_crn_expand<2><<<ctas, kExpandThreads, 0, s>>>(d_ej, (int)F.faces, pal, records, vec_ok);
-      break;
-    case Kind::DXT5A:
-      k_crn_decode<3><<<1, 32, sizeof(uint32_t) * (1 << kLutBits) * models_used<3>(), s>>>(d_dj, 1, d_models, pal, records, status);
-      k_crn_expand<3><<<ctas, kExpandThreads, 0, s>>>(d_ej, (int)F.faces, pal, records, vec_ok);
-      break;
-  }
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch transcode kernels");
-  uint32_t st = 0;
-  if ((e = cudaMemcpyAsync(&st, status, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read status");
+  uint32_t* words = reinterpret_cast<uint32_t*>(base);
+  if ((rc = enqueue_plan(p, base + o_jobs, words, s)) != CRNGPU_OK) return rc;
+  uint32_t st[2] = {0, 0};
+  if ((e = cudaMemcpyAsync(st, words, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read status");
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
-  if (st) {
-    set_error(st == kStBadCode ? "corrupt block stream (no such prefix code)"
-                               : "corrupt block stream (palette index out of range)");
-    return CRNGPU_E_CORRUPT;
-  }
-  return CRNGPU_OK;
+  return status_to_rc(st[1]);
 }

@@ -182,6 +182,41 @@ CRNGPU_API int crngpu_unpack_level_segmented(crngpu_unpack_context ctx, const vo
 CRNGPU_API int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t first_level, uint32_t level_count, void* dst,
                              uint64_t dst_size, int mem, void* stream);
 
+/* Batched transcode (no single counterpart in the reference, which transcodes one level per
+ * crnd_unpack_level call, inc/crn_decomp.h:3537-3619): many levels of many open contexts, of any
+ * mix of sizes and formats, decoded by ONE persistent launch (one lane per level stream, streams
+ * taken largest-first from a work counter) and expanded by one more. Each item writes levels
+ * [first_level, first_level + level_count) of its context back to back into `dst` (device
+ * memory), exactly as crngpu_unpack_levels does. Creation validates every item, uploads the job
+ * tables and allocates the index-record buffer once; the contexts must stay open while the batch
+ * exists. */
+typedef struct crngpu_unpack_batch_item {
+    crngpu_unpack_context ctx;
+    uint32_t first_level;
+    uint32_t level_count;
+    void* dst;          /* device memory */
+    uint64_t dst_size;  /* bytes available at dst */
+} crngpu_unpack_batch_item;
+
+typedef struct crngpu_unpack_batch_s* crngpu_unpack_batch;
+
+/* NULL on failure (crngpu_last_error says which item). */
+CRNGPU_API crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_batch_item* items, uint32_t n);
+
+/* Enqueues the batch on `stream` without synchronising: a two-word memset and two kernels.
+ * use_graph = 1 captures them into a CUDA graph on the first call and replays that graph on
+ * later calls (one launch from the host per batch). */
+CRNGPU_API int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, int use_graph, void* stream);
+
+/* Synchronises `stream` and reports the last launch's outcome: CRNGPU_OK, or CRNGPU_E_CORRUPT if
+ * a block stream held an invalid code or palette index (the reference's bool result). */
+CRNGPU_API int crngpu_unpack_batch_status(crngpu_unpack_batch batch, void* stream);
+
+/* Total output bytes of the batch (sum of the items' level sizes). */
+CRNGPU_API int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch);
+
+CRNGPU_API int crngpu_unpack_batch_destroy(crngpu_unpack_batch batch);
+
 /* Allocation-free transcode of one level. No counterpart in the reference: it exists for
  * callers that cannot allocate GPU memory while they run -- engines that reserve their whole
  * VRAM budget up front and forbid untracked allocations, and real-time loops in which

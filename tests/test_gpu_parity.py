@@ -126,6 +126,51 @@ def test_transcode_levels_bit_exact(cg, name):
             pos += info["bytes"]
 
 
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_transcode_batch_mixed_formats(cg, use_graph):
+    """Every fixture (DXT1, DXT5, DXN, DXT5A, cube maps, NPOT) in one batch, each twice with its
+    own context: one persistent decode launch + one expansion, replayed; bit-exact per level."""
+    man = G.manifest()
+    names = sorted(man) * 2
+    ctxs = [cg.unpack_begin(G.crn_bytes(n)) for n in names]
+    outs = [torch.full((sum(l["bytes"] for l in man[n]["levels"]),), 0xCD, dtype=torch.uint8, device="cuda")
+            for n in names]
+    with cg.UnpackBatch([(c, 0, c.levels, o) for c, o in zip(ctxs, outs)]) as batch:
+        assert batch.bytes == sum(o.numel() for o in outs)
+        for rep in range(3):
+            for o in outs:
+                o.fill_(0xCD)
+            batch.launch(use_graph=use_graph)
+            batch.status()
+            for n, o in zip(names, outs):
+                host = o.cpu().numpy()
+                pos = 0
+                for lvl, info in enumerate(man[n]["levels"]):
+                    assert G.sha(host[pos:pos + info["bytes"]]) == info["sha256"], (n, lvl, rep)
+                    pos += info["bytes"]
+    for c in ctxs:
+        c.close()
+
+
+def test_transcode_batch_level_subset(cg):
+    man = G.manifest()
+    crn = G.crn_bytes("c1_dxt1_1024")
+    with cg.unpack_begin(crn) as ctx:
+        lv = man["c1_dxt1_1024"]["levels"]
+        out = torch.zeros(sum(l["bytes"] for l in lv[3:7]), dtype=torch.uint8, device="cuda")
+        with cg.UnpackBatch([(ctx, 3, 4, out)]) as batch:
+            batch.launch()
+            batch.status()
+        host = out.cpu().numpy()
+        pos = 0
+        for info in lv[3:7]:
+            assert G.sha(host[pos:pos + info["bytes"]]) == info["sha256"]
+            pos += info["bytes"]
+        small = torch.zeros(10, dtype=torch.uint8, device="cuda")
+        with pytest.raises(cg.CrnGpuError):
+            cg.UnpackBatch([(ctx, 0, 2, small)])
+
+
 def test_transcode_row_pitch_padding(cg):
     crn = G.crn_bytes("dxt5_256")
     with cg.unpack_begin(crn) as ctx:
