@@ -7,7 +7,10 @@ One JSON line on stdout (rank 0):
   learned    the learned-proposal encode of the same blocks (shipped weights): Mtexel/s, RGB
              RMSE beside the plain encode's, fallback fraction
   e2e        the same encode through the C ABI with pinned host buffers (H2D + encode + D2H)
-  transcode  CRN -> DXT1 transcode of the reference-encoded .crn of the same texture (q128)
+  transcode  CRN -> DXT1 transcode GB/s: a batch of 1024 textures (each with its own context holding
+             the reference-encoded .crn of the same texture, q128) in one persistent decode launch
+             and one expansion launch (CUDA graph); the expansion kernel's HBM roofline; the
+             single-texture latency; the oracle on all host cores over the same .crn
   roofline   the encoder kernel: ALU issue roofline (candidate x colour evaluations counted on
              the device x lane-ops per evaluation, over the peak lane-op rate)
   cpu_baseline  the oracle (CPU restatement of the reference, bit-identical outputs) on all
@@ -37,6 +40,7 @@ TEXTURE_SEED = 100
 CRN_FIXTURE = os.path.join(ROOT, "tests", "golden", "crn", "c1_dxt1_1024.crn")
 METRIC = "DXT1 encode Mtexel/s at matched RMSE, learned vs plain; CRN→DXT1 transcode GB/s"
 L2_FLUSH_BYTES = 256 << 20
+TX_BATCH = 1024  # textures per transcode batch
 LANE_OPS_PER_EVAL = 27  # uber inner loop per candidate x colour: 15 FFMA, 4 FMNMX, 4 FADD, 2 IADD, 2 IMAD
 
 
@@ -321,29 +325,77 @@ def main():
                        "optimizer on fallback blocks; one host sync per call"}
     del net
 
-    # ---- CRN -> DXT1 transcode of the same texture (all 11 levels, device output)
+    # ---- CRN -> DXT1 transcode: a batch of TX_BATCH textures (each its own context, i.e. its own
+    # tables and palettes, holding the reference-encoded .crn of the same texture, q128, 11 levels)
+    # in one persistent decode launch + one expansion launch, replayed as a CUDA graph
     with open(CRN_FIXTURE, "rb") as fh:
         crn = fh.read()
-    ctx = cg.unpack_begin(crn)
-    tx_bytes = sum(ctx.level_bytes(l) for l in range(ctx.levels))
+    ctx0 = cg.unpack_begin(crn)
+    tx_bytes = sum(ctx0.level_bytes(l) for l in range(ctx0.levels))
+    tx_blocks = tx_bytes // 8
     d_tx = torch.empty(tx_bytes, dtype=torch.uint8, device=dev)
+
+    def timed(fn, steps):
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for i in range(steps):
+            flush.fill_(i & 0xFF)
+            st[i].record(stream)
+            fn()
+            en[i].record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in zip(st, en)) / steps
+
     for _ in range(args.warmup):
-        ctx.unpack_levels(out=d_tx, stream=stream)
-    torch.cuda.synchronize()
-    tx_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    tx_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    for i in range(args.steps):
-        flush.fill_(i & 0xFF)
-        tx_start[i].record(stream)
-        ctx.unpack_levels(out=d_tx, stream=stream)
-        tx_end[i].record(stream)
-    torch.cuda.synchronize()
-    tx_ms = sum(s.elapsed_time(e) for s, e in zip(tx_start, tx_end)) / args.steps
-    ctx.close()
-    transcode = {"value": round(tx_bytes / (tx_ms / 1e3) / 1e9, 4), "unit": "GB/s",
-                 "mtexel_s": round(texels / (tx_ms / 1e3) / 1e6, 2), "ms_per_transcode": round(tx_ms, 4),
-                 "output_bytes": tx_bytes, "crn_bytes": len(crn),
-                 "note": "11 level streams decode concurrently (one warp each), then one 16-byte-store expansion"}
+        ctx0.unpack_levels(out=d_tx, stream=stream)
+    single_ms = timed(lambda: ctx0.unpack_levels(out=d_tx, stream=stream), args.steps)
+    ctxs = [cg.unpack_begin(crn) for _ in range(TX_BATCH)]
+    outs = [torch.empty(tx_bytes, dtype=torch.uint8, device=dev) for _ in range(TX_BATCH)]
+    batch = cg.UnpackBatch([(c, 0, c.levels, o) for c, o in zip(ctxs, outs)])
+    for _ in range(args.warmup):
+        batch.launch(use_graph=True, stream=stream)
+    batch.status(stream=stream)
+    tx_parity = bool((outs[-1].cpu().numpy() == ctx0.unpack_levels()).all())
+    batch_ms = timed(lambda: batch.launch(use_graph=True, stream=stream), args.steps)
+    batch.status(stream=stream)
+    expand_ms = timed(lambda: batch.launch(expand_only=True, stream=stream), args.steps)
+    # end to end through the C ABI: the batch plus the copy of every texture's DXT1 levels to
+    # pinned host memory (the .crn files are uploaded once, by crngpu_unpack_begin)
+    host_tx = torch.empty((TX_BATCH, tx_bytes), dtype=torch.uint8).pin_memory()
+
+    def tx_e2e():
+        batch.launch(use_graph=True, stream=stream)
+        for i, o in enumerate(outs):
+            host_tx[i].copy_(o, non_blocking=True)
+        batch.status(stream=stream)
+
+    tx_e2e()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        tx_e2e()
+    tx_e2e_s = (time.perf_counter() - t0) / args.steps
+    batch.close()
+    for c in ctxs:
+        c.close()
+    del outs
+    ctx0.close()
+    exp_bytes = TX_BATCH * tx_blocks * 12  # 4-byte index record read + 8-byte DXT1 block written
+    transcode = {"value": round(TX_BATCH * tx_bytes / (batch_ms / 1e3) / 1e9, 3), "unit": "GB/s",
+                 "mtexel_s": round(TX_BATCH * texels / (batch_ms / 1e3) / 1e6, 1),
+                 "ms_per_batch": round(batch_ms, 4), "textures_per_batch": TX_BATCH,
+                 "output_bytes_per_batch": TX_BATCH * tx_bytes, "crn_bytes_per_texture": len(crn),
+                 "parity_vs_single_context": tx_parity,
+                 "e2e": {"value": round(TX_BATCH * tx_bytes / tx_e2e_s / 1e9, 3), "unit": "GB/s",
+                         "h2d_bytes_per_step": 0, "d2h_bytes_per_step": TX_BATCH * tx_bytes,
+                         "path": "crngpu_unpack_batch_launch (graph) + D2H of every level to pinned host memory"},
+                 "single_texture": {"ms": round(single_ms, 4), "GB/s": round(tx_bytes / (single_ms / 1e3) / 1e9, 4),
+                                    "note": "one texture = 11 level streams on 11 lanes of one warp; the 1024x1024 "
+                                            "level is one serial prefix-code chain, so this is its latency"},
+                 "expand_roofline": None,
+                 "workload": f"{TX_BATCH} contexts of the 1024x1024 q128 DXT1 .crn (11 levels, {len(crn)} bytes)"}
+    expand = {"kernel": "k_crn_expand_tiles", "bound": "hbm", "unit": "GB/s",
+              "ms": round(expand_ms, 4), "bytes_algorithmic": exp_bytes,
+              "achieved": round(exp_bytes / (expand_ms / 1e3) / 1e9, 1)}
 
     peaks, peak_kind = measured_peaks()
     clk = clocks.summary()
@@ -356,11 +408,16 @@ def main():
                 "traffic": None, "peak_source": f"SMs x 128 lanes x max SM clock ({peak_kind} clock)",
                 "evals_per_launch": evals, "lane_ops_per_eval": LANE_OPS_PER_EVAL,
                 "kernel_ms": round(kernel_ms, 4), "hbm_bytes_algorithmic": n_blocks * 72}
+    expand["peak"] = peaks["hbm_gbs"]
+    expand["frac"] = round(expand["achieved"] / peaks["hbm_gbs"], 4)
+    expand["peak_source"] = f"{peak_kind} HBM copy bandwidth"
+    transcode["expand_roofline"] = expand
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_encode_baseline(blocks, texels / n_blocks)
         transcode["cpu_baseline"] = cpu_transcode_baseline(crn, tx_bytes)
+        transcode["vs_cpu"] = round(transcode["value"] / transcode["cpu_baseline"]["value"], 2)
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mtexel/s", "n_gpus": world,

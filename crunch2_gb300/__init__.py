@@ -88,7 +88,7 @@ def lib():
     L.crngpu_unpack_end.restype = i32
     L.crngpu_unpack_batch_create.argtypes = [ctypes.POINTER(_BatchItem), u32]
     L.crngpu_unpack_batch_create.restype = vp
-    L.crngpu_unpack_batch_launch.argtypes = [vp, i32, vp]
+    L.crngpu_unpack_batch_launch.argtypes = [vp, u32, vp]
     L.crngpu_unpack_batch_launch.restype = i32
     L.crngpu_unpack_batch_status.argtypes = [vp, vp]
     L.crngpu_unpack_batch_status.restype = i32
@@ -288,8 +288,9 @@ class UnpackBatch:
             raise CrnGpuError(E_PARAM, "crngpu_unpack_batch_create")
         self.bytes = int(lib().crngpu_unpack_batch_bytes(self.handle))
 
-    def launch(self, use_graph: bool = False, stream=None):
-        _check(lib().crngpu_unpack_batch_launch(self.handle, int(use_graph), _stream_ptr(stream)),
+    def launch(self, use_graph: bool = False, expand_only: bool = False, stream=None):
+        flags = (1 if use_graph else 0) | (2 if expand_only else 0)
+        _check(lib().crngpu_unpack_batch_launch(self.handle, flags, _stream_ptr(stream)),
                "crngpu_unpack_batch_launch")
 
     def status(self, stream=None):

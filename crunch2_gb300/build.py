@@ -27,6 +27,7 @@ UNITS = [
     ("encode_api.cu", []),
     ("dxt_encode.cu", ["--fmad=false"]),
     ("mlp.cu", []),
+    ("hc_encode.cu", []),
 ]
 
 

@@ -13,7 +13,7 @@
 //                   lockstep. The kernel is persistent: warps take textures largest-first from
 //                   a work counter until none are left, so one launch decodes every level of
 //                   every texture of a batch, whatever their sizes and formats.
-//   k_crn_expand_jobs - the parallel part: every thread turns index records into finished
+//   k_crn_expand_tiles - the parallel part: every thread turns index records into finished
 //                   DXT words (palette gathers from L2) and writes 16 bytes per store.
 // The header, Huffman models and palettes are decoded once on the host (crn_file.cpp).
 #include <cuda_runtime.h>
@@ -72,10 +72,13 @@ struct ExpandJob {
   const uint8_t* rec;     // the face's index records
   DevPalettes pal;
   uint32_t bx, by, pitch, kind;
-  uint32_t cta_begin, ctas_per_row;
+  uint32_t flat;          // pitch == bx * bytes per block: the face is one contiguous block array
+  uint32_t vec;           // 16-byte stores are aligned (dst, and pitch unless flat)
 };
 
-constexpr int kExpandThreads = 128;
+constexpr uint32_t kExpandThreads = 256;
+constexpr uint32_t kTileBlocks = 4096;  // blocks per expansion tile (16 per thread)
+constexpr uint32_t kStageMin = 1024;    // DXT1 tiles at least this large stage their palettes
 // Decoder shared memory per CTA: five first-level tables + the row buffers of one texture's
 // levels (at most 2 x 1024 + 2 x 16 words for a 4096-texel-wide texture with 16 levels).
 constexpr size_t kDecodeSmemMax = 64u << 10;
@@ -331,62 +334,128 @@ __device__ __forceinline__ uint2 alpha_words(const DevPalettes& pal, uint32_t r)
   return make_uint2((uint32_t)a, (uint32_t)(a >> 32));
 }
 
-// One 16-byte output chunk per thread: two 8-byte blocks (DXT1/DXT5A) or one 16-byte block.
-// A CTA covers part of one block row of one face; its job is found by binary search.
-__global__ void __launch_bounds__(kExpandThreads) k_crn_expand_jobs(const ExpandJob* __restrict__ jobs, int njobs,
-                                                                     int vec_ok) {
-  int lo = 0, hi = njobs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (jobs[mid].cta_begin <= blockIdx.x) lo = mid; else hi = mid - 1;
-  }
-  const ExpandJob& J = jobs[lo];
-  const uint32_t local = blockIdx.x - J.cta_begin;
-  const uint32_t y = local / J.ctas_per_row;
-  const uint32_t chunk = (local - y * J.ctas_per_row) * kExpandThreads + threadIdx.x;
-  if (y >= J.by) return;
+// The expansion works on tiles of kTileBlocks consecutive blocks of one face of one level; each
+// CTA takes one tile from a table built on the host (no per-CTA search). A thread handles
+// kTileBlocks / kExpandThreads blocks: it first loads all its index records, then gathers the
+// palette words, then stores, so each thread keeps many loads in flight. For DXT1 tiles of at
+// least kStageMin blocks the CTA first copies the two colour palettes into shared memory, so the
+// per-block gathers hit shared memory instead of costing a 32-byte L2 sector per 4-byte word.
+template <bool WIDE>  // WIDE: 16-byte blocks (DXT5, DXN); else 8-byte blocks (DXT1, DXT5A)
+__device__ __forceinline__ void expand_tile(const ExpandJob& J, uint32_t first, const uint32_t* s_ep,
+                                            const uint32_t* s_sel) {
+  constexpr uint32_t kPer = kTileBlocks / kExpandThreads;  // blocks per thread
   const uint32_t kind = J.kind, bx = J.bx;
+  const uint32_t nblk = bx * J.by;
   const DevPalettes pal = J.pal;
-  uint8_t* drow = J.dst + (uint64_t)y * J.pitch;
-  if (kind == kKDxt1 || kind == kKDxt5a) {
-    const uint32_t x0 = chunk * 2;
-    if (x0 >= bx) return;
-    const uint32_t* rec = reinterpret_cast<const uint32_t*>(J.rec) + (uint64_t)y * bx;
-    auto word = [&](uint32_t r) -> uint2 {
-      if (kind == kKDxt1)
-        return make_uint2(__ldg(pal.colour_ep + clamp_idx(r & 0xFFFFu, pal.n_cep)),
-                          __ldg(pal.colour_sel + clamp_idx(r >> 16, pal.n_csel)));
-      return alpha_words(pal, r);
-    };
-    const uint2 w0 = word(__ldg(rec + x0));
-    uint32_t* d = reinterpret_cast<uint32_t*>(drow + (uint64_t)x0 * 8);
-    if (x0 + 1 < bx) {
-      const uint2 w1 = word(__ldg(rec + x0 + 1));
-      if (vec_ok) {
-        __stcs(reinterpret_cast<uint4*>(d), make_uint4(w0.x, w0.y, w1.x, w1.y));
+  const bool flat = J.flat;  // minimal pitch: the face is one contiguous array of blocks
+  if (!WIDE) {
+    // pairs of blocks: thread t handles blocks first + 2 * (k * threads + t) and the next one
+    uint32_t r[kPer];
+    const uint32_t* rec = reinterpret_cast<const uint32_t*>(J.rec);
+    const bool rec8 = ((uintptr_t)rec & 7) == 0;  // pairs of records (b0 even) are 8-byte aligned
+#pragma unroll
+    for (uint32_t k = 0; k < kPer / 2; k++) {
+      const uint32_t b0 = first + 2 * (k * kExpandThreads + threadIdx.x);
+      if (b0 + 1 < nblk && rec8) {
+        const uint2 v = __ldg(reinterpret_cast<const uint2*>(rec + b0));
+        r[2 * k] = v.x;
+        r[2 * k + 1] = v.y;
+      } else if (b0 + 1 < nblk) {
+        r[2 * k] = __ldg(rec + b0);
+        r[2 * k + 1] = __ldg(rec + b0 + 1);
       } else {
-        d[0] = w0.x; d[1] = w0.y; d[2] = w1.x; d[3] = w1.y;
+        r[2 * k] = b0 < nblk ? __ldg(rec + b0) : 0u;
+        r[2 * k + 1] = 0u;
       }
-    } else {
-      d[0] = w0.x; d[1] = w0.y;
+    }
+    uint2 w[kPer];
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; k++) {
+      if (kind == kKDxt1) {
+        const uint32_t ei = clamp_idx(r[k] & 0xFFFFu, pal.n_cep), si = clamp_idx(r[k] >> 16, pal.n_csel);
+        w[k] = s_ep ? make_uint2(s_ep[ei], s_sel[si]) : make_uint2(__ldg(pal.colour_ep + ei), __ldg(pal.colour_sel + si));
+      } else {
+        w[k] = alpha_words(pal, r[k]);
+      }
+    }
+#pragma unroll
+    for (uint32_t k = 0; k < kPer / 2; k++) {
+      const uint32_t b0 = first + 2 * (k * kExpandThreads + threadIdx.x);
+      if (b0 >= nblk) break;
+      if (flat && J.vec && b0 + 1 < nblk) {
+        __stcs(reinterpret_cast<uint4*>(J.dst + (uint64_t)b0 * 8),
+               make_uint4(w[2 * k].x, w[2 * k].y, w[2 * k + 1].x, w[2 * k + 1].y));
+      } else {
+        for (uint32_t q = 0; q < 2 && b0 + q < nblk; q++) {
+          const uint32_t bb = b0 + q, y = bb / bx, x = bb - y * bx;
+          uint32_t* d = reinterpret_cast<uint32_t*>(J.dst + (uint64_t)y * J.pitch + (uint64_t)x * 8);
+          d[0] = w[2 * k + q].x;
+          d[1] = w[2 * k + q].y;
+        }
+      }
     }
   } else {
-    const uint32_t x = chunk;
-    if (x >= bx) return;
-    const uint64_t r = __ldg(reinterpret_cast<const unsigned long long*>(J.rec) + (uint64_t)y * bx + x);
-    const uint32_t rlo = (uint32_t)r, rhi = (uint32_t)(r >> 32);
-    uint4 o;
-    if (kind == kKDxt5) {
-      const uint2 a = alpha_words(pal, rhi);
-      o = make_uint4(a.x, a.y, __ldg(pal.colour_ep + clamp_idx(rlo & 0xFFFFu, pal.n_cep)),
-                     __ldg(pal.colour_sel + clamp_idx(rlo >> 16, pal.n_csel)));
-    } else {
-      const uint2 a = alpha_words(pal, rlo), c = alpha_words(pal, rhi);
-      o = make_uint4(a.x, a.y, c.x, c.y);
+    constexpr uint32_t kPerW = kPer / 2;  // 16-byte blocks: half as many per thread per pass
+#pragma unroll 1
+    for (uint32_t pass = 0; pass < 2; pass++) {
+      const uint32_t base = first + pass * kPerW * kExpandThreads;
+      uint64_t r[kPerW];
+      const unsigned long long* rec = reinterpret_cast<const unsigned long long*>(J.rec);
+#pragma unroll
+      for (uint32_t k = 0; k < kPerW; k++) {
+        const uint32_t bb = base + k * kExpandThreads + threadIdx.x;
+        r[k] = bb < nblk ? __ldg(rec + bb) : 0ull;
+      }
+      uint4 o[kPerW];
+#pragma unroll
+      for (uint32_t k = 0; k < kPerW; k++) {
+        const uint32_t rlo = (uint32_t)r[k], rhi = (uint32_t)(r[k] >> 32);
+        if (kind == kKDxt5) {
+          const uint2 a = alpha_words(pal, rhi);
+          o[k] = make_uint4(a.x, a.y, __ldg(pal.colour_ep + clamp_idx(rlo & 0xFFFFu, pal.n_cep)),
+                            __ldg(pal.colour_sel + clamp_idx(rlo >> 16, pal.n_csel)));
+        } else {
+          const uint2 a = alpha_words(pal, rlo), c = alpha_words(pal, rhi);
+          o[k] = make_uint4(a.x, a.y, c.x, c.y);
+        }
+      }
+#pragma unroll
+      for (uint32_t k = 0; k < kPerW; k++) {
+        const uint32_t bb = base + k * kExpandThreads + threadIdx.x;
+        if (bb >= nblk) break;
+        const uint32_t y = flat ? 0u : bb / bx, x = flat ? bb : bb - y * bx;
+        uint32_t* d = reinterpret_cast<uint32_t*>(J.dst + (uint64_t)y * J.pitch + (uint64_t)x * 16);
+        if (J.vec) __stcs(reinterpret_cast<uint4*>(d), o[k]);
+        else { d[0] = o[k].x; d[1] = o[k].y; d[2] = o[k].z; d[3] = o[k].w; }
+      }
     }
-    uint32_t* d = reinterpret_cast<uint32_t*>(drow + (uint64_t)x * 16);
-    if (vec_ok) __stcs(reinterpret_cast<uint4*>(d), o);
-    else { d[0] = o.x; d[1] = o.y; d[2] = o.z; d[3] = o.w; }
+  }
+}
+
+// Dynamic shared memory: the staged DXT1 colour palettes, smem_words = the largest
+// n_cep + n_csel of the launch's DXT1 jobs (0 when none is staged).
+__global__ void __launch_bounds__(kExpandThreads) k_crn_expand_tiles(const ExpandJob* __restrict__ jobs,
+                                                                      const uint2* __restrict__ tiles,
+                                                                      uint32_t smem_words) {
+  extern __shared__ uint32_t s_pal[];
+  const uint2 t = tiles[blockIdx.x];  // (job, first block)
+  const ExpandJob& J = jobs[t.x];
+  if (J.kind == kKDxt1) {
+    const uint32_t nblk = J.bx * J.by;
+    const uint32_t n_ep = J.pal.n_cep, n_sel = J.pal.n_csel;
+    const bool stage = nblk - t.y >= kStageMin && n_ep + n_sel <= smem_words;  // uniform per CTA
+    if (stage) {
+      for (uint32_t i = threadIdx.x; i < n_ep; i += kExpandThreads) s_pal[i] = __ldg(J.pal.colour_ep + i);
+      for (uint32_t i = threadIdx.x; i < n_sel; i += kExpandThreads) s_pal[n_ep + i] = __ldg(J.pal.colour_sel + i);
+      __syncthreads();
+      expand_tile<false>(J, t.y, s_pal, s_pal + n_ep);
+    } else {
+      expand_tile<false>(J, t.y, nullptr, nullptr);
+    }
+  } else if (J.kind == kKDxt5a) {
+    expand_tile<false>(J, t.y, nullptr, nullptr);
+  } else {
+    expand_tile<true>(J, t.y, nullptr, nullptr);
   }
 }
 
@@ -495,8 +564,8 @@ struct Plan {
   uint32_t n_item = 0, n_stream = 0, n_expand = 0, ctas = 0;
   uint32_t rb_words = 2;    // largest row-buffer need of one texture job (words)
   uint32_t lut_words = 0;   // first-level tables staged per texture job (words)
-  size_t stream_ofs = 0, expand_ofs = 0;
-  int vec_ok = 1;
+  size_t stream_ofs = 0, expand_ofs = 0, tile_ofs = 0;
+  uint32_t pal_words = 0;   // shared memory of the expansion: largest staged DXT1 palette pair
 };
 
 uint64_t level_records(const CrnFile& F, uint32_t l) {
@@ -560,41 +629,42 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
     sj.insert(sj.end(), item_streams[o].begin(), item_streams[o].end());
   }
   std::vector<ExpandJob> ej;
-  uint32_t ctas = 0;
+  std::vector<uint2> tiles;
   for (const LevelTask& t : tasks) {
     const CrnFile& F = *t.file;
     const LevelInfo& li = F.level[t.level];
     const uint32_t kind = (uint32_t)F.kind;
-    const uint32_t chunk_blocks = F.bytes_per_block == 8 ? 2 : 1;
-    const uint32_t chunks = (li.blocks_x + chunk_blocks - 1) / chunk_blocks;
-    const uint32_t per_row = (chunks + kExpandThreads - 1) / kExpandThreads;
+    const uint32_t nblk = li.blocks_x * li.blocks_y;
     for (uint32_t f = 0; f < F.faces; f++) {
       ExpandJob j;
       j.dst = t.dst[f];
-      j.rec = t.rec + (uint64_t)f * li.blocks_x * li.blocks_y * record_bytes(kind);
+      j.rec = t.rec + (uint64_t)f * nblk * record_bytes(kind);
       j.pal = t.pal;
       j.bx = li.blocks_x;
       j.by = li.blocks_y;
       j.pitch = t.pitch;
       j.kind = kind;
-      j.cta_begin = ctas;
-      j.ctas_per_row = per_row;
-      ctas += per_row * li.blocks_y;
+      j.flat = t.pitch == li.blocks_x * F.bytes_per_block ? 1u : 0u;
+      j.vec = (((uintptr_t)t.dst[f] & 15) == 0 && (j.flat || (t.pitch & 15) == 0)) ? 1u : 0u;
+      for (uint32_t b = 0; b < nblk; b += kTileBlocks) tiles.push_back(make_uint2((uint32_t)ej.size(), b));
+      if (kind == kKDxt1 && nblk >= kStageMin)
+        p.pal_words = std::max(p.pal_words, t.pal.n_cep + t.pal.n_csel);
       ej.push_back(j);
-      if (((uintptr_t)t.dst[f] | t.pitch) & 15) p.vec_ok = 0;
     }
   }
   p.n_item = (uint32_t)it_sorted.size();
   p.n_stream = (uint32_t)sj.size();
   p.n_expand = (uint32_t)ej.size();
-  p.ctas = ctas;
+  p.ctas = (uint32_t)tiles.size();
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
   p.stream_ofs = al(sizeof(TexJob) * it_sorted.size());
   p.expand_ofs = p.stream_ofs + al(sizeof(StreamJob) * sj.size());
-  p.image.assign(p.expand_ofs + sizeof(ExpandJob) * ej.size(), 0);
+  p.tile_ofs = p.expand_ofs + al(sizeof(ExpandJob) * ej.size());
+  p.image.assign(p.tile_ofs + sizeof(uint2) * tiles.size(), 0);
   std::memcpy(p.image.data(), it_sorted.data(), sizeof(TexJob) * it_sorted.size());
   std::memcpy(p.image.data() + p.stream_ofs, sj.data(), sizeof(StreamJob) * sj.size());
   std::memcpy(p.image.data() + p.expand_ofs, ej.data(), sizeof(ExpandJob) * ej.size());
+  std::memcpy(p.image.data() + p.tile_ofs, tiles.data(), sizeof(uint2) * tiles.size());
   return true;
 }
 
@@ -616,6 +686,9 @@ int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
     if ((e = cudaFuncSetAttribute(k_crn_decode_textures, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDecodeSmemMax)) != cudaSuccess)
       return cuda_check(e, "decoder shared memory attribute");
+    if ((e = cudaFuncSetAttribute(k_crn_expand_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(2 * kMaxSyms * sizeof(uint32_t)))) != cudaSuccess)
+      return cuda_check(e, "expansion shared memory attribute");
     attr_set[dev] = true;
   }
   *smem = (size_t)(p.lut_words + p.rb_words) * sizeof(uint32_t);
@@ -626,7 +699,7 @@ int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
 
 // Enqueues the counter/status clear, the decoder and the expansion for a plan whose image is
 // already at d_jobs. `words` = 2 device words: [0] work counter, [1] status. Asynchronous.
-int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStream_t s) {
+int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStream_t s, bool decode = true) {
   if ((size_t)(p.lut_words + p.rb_words) * 4 > kDecodeSmemMax) {
     set_error("texture rows too wide for the decoder");
     return CRNGPU_E_PARAM;
@@ -635,18 +708,19 @@ int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStre
   size_t smem = 0;
   int rc = decode_grid(p, &grid, &smem);
   if (rc != CRNGPU_OK) return rc;
-  cudaError_t e = cudaMemsetAsync(words, 0, 8, s);
-  if (e != cudaSuccess) return cuda_check(e, "clear work counter");
+  cudaError_t e;
   const TexJob* tj = reinterpret_cast<const TexJob*>(d_jobs);
   const StreamJob* sj = reinterpret_cast<const StreamJob*>(d_jobs + p.stream_ofs);
   const ExpandJob* ej = reinterpret_cast<const ExpandJob*>(d_jobs + p.expand_ofs);
-  if (p.n_item) {
+  if (decode && p.n_item) {
+    if ((e = cudaMemsetAsync(words, 0, 8, s)) != cudaSuccess) return cuda_check(e, "clear work counter");
     k_crn_decode_textures<<<grid, 32, smem, s>>>(tj, p.n_item, sj, words, p.lut_words, p.rb_words, words + 1);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_decode_textures");
   }
   if (p.ctas) {
-    k_crn_expand_jobs<<<p.ctas, kExpandThreads, 0, s>>>(ej, (int)p.n_expand, p.vec_ok);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_expand_jobs");
+    const uint2* tiles = reinterpret_cast<const uint2*>(d_jobs + p.tile_ofs);
+    k_crn_expand_tiles<<<p.ctas, kExpandThreads, (size_t)p.pal_words * 4, s>>>(ej, tiles, p.pal_words);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_expand_tiles");
   }
   return CRNGPU_OK;
 }
@@ -661,14 +735,15 @@ int status_to_rc(uint32_t st) {
 // Decodes and expands a list of levels of one context (destinations device memory), then
 // reads the status word back (synchronises `s`).
 int run_levels(UnpackContext* c, std::vector<LevelTask>& tasks, cudaStream_t s) {
+  // one record buffer for all levels, each level's records starting on a 16-byte boundary
   uint64_t rec = 0;
-  for (LevelTask& t : tasks) rec += level_records(c->file, t.level) * c->rec_bytes();
+  for (LevelTask& t : tasks) rec += (level_records(c->file, t.level) * c->rec_bytes() + 15) & ~(uint64_t)15;
   cudaError_t e = c->d_records.ensure(rec + 16);
   if (e != cudaSuccess) return cuda_check(e, "alloc records");
   uint64_t ofs = 0;
   for (LevelTask& t : tasks) {
     t.rec = static_cast<uint8_t*>(c->d_records.ptr) + ofs;
-    ofs += level_records(c->file, t.level) * c->rec_bytes();
+    ofs += (level_records(c->file, t.level) * c->rec_bytes() + 15) & ~(uint64_t)15;
   }
   Plan p;
   if (!make_plan(tasks, p)) { set_error("too many levels in one texture job"); return CRNGPU_E_PARAM; }
@@ -786,7 +861,7 @@ struct UnpackBatch {
   DevBuf d_jobs, d_records, d_words;
   uint32_t words_host[2] = {0, 0};
   cudaGraphExec_t graph = nullptr;
-  cudaStream_t graph_stream = nullptr;
+  bool decoded = false;
   uint64_t out_bytes = 0;
   ~UnpackBatch() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -896,7 +971,7 @@ extern "C" crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_ba
     const size_t first = tasks.size();
     levels_tasks(c, items[i].first_level, items[i].level_count, static_cast<uint8_t*>(items[i].dst), i, tasks);
     for (size_t k = first; k < tasks.size(); k++) {
-      rec = (rec + 7) & ~(uint64_t)7;
+      rec = (rec + 15) & ~(uint64_t)15;
       tasks[k].rec = reinterpret_cast<uint8_t*>(rec);  // offset for now; rebased below
       rec += level_records(c->file, tasks[k].level) * c->rec_bytes();
     }
@@ -918,14 +993,20 @@ extern "C" crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_ba
   return reinterpret_cast<crngpu_unpack_batch>(b.release());
 }
 
-extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, int use_graph, void* stream) {
+extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t flags, void* stream) {
   clear_error();
   UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
   if (!b || b->magic != 0x42415443u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
+  if (flags & ~(uint32_t)(CRNGPU_BATCH_GRAPH | CRNGPU_BATCH_EXPAND_ONLY)) { set_error("unknown flags"); return CRNGPU_E_PARAM; }
   cudaStream_t s = as_stream(stream);
   const uint8_t* jobs = static_cast<const uint8_t*>(b->d_jobs.ptr);
   uint32_t* words = static_cast<uint32_t*>(b->d_words.ptr);
-  if (!use_graph) return enqueue_plan(b->plan, jobs, words, s);
+  if (flags & CRNGPU_BATCH_EXPAND_ONLY) {
+    if (!b->decoded) { set_error("no decode has run on this batch"); return CRNGPU_E_PARAM; }
+    return enqueue_plan(b->plan, jobs, words, s, false);
+  }
+  b->decoded = true;
+  if (!(flags & CRNGPU_BATCH_GRAPH)) return enqueue_plan(b->plan, jobs, words, s);
   cudaError_t e;
   if (!b->graph) {
     // capture on a private stream (the legacy default stream cannot be captured), then replay

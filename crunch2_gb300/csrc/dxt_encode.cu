@@ -1372,6 +1372,15 @@ struct DeviceInit {
   bool done[64] = {};
 };
 
+SingleColour* single_colour_host_tables() {
+  static SingleColour* host = nullptr;
+  if (!host) {
+    host = new SingleColour;
+    build_single_colour(*host);
+  }
+  return host;
+}
+
 int ensure_tables() {
   static DeviceInit init;
   static SingleColour* host = nullptr;
@@ -1379,14 +1388,18 @@ int ensure_tables() {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
   if (dev < 64 && init.done[dev]) return CRNGPU_OK;
-  if (!host) {
-    host = new SingleColour;
-    build_single_colour(*host);
-  }
+  if (!host) host = single_colour_host_tables();
   if ((e = cudaMemcpyToSymbol(c_sct, host, sizeof(SingleColour))) != cudaSuccess) return cuda_check(e, "upload tables");
   if (dev < 64) init.done[dev] = true;
   return CRNGPU_OK;
 }
+
+}  // namespace
+
+// ryg single-colour tables on the host: m5[256][2], m6[256][2] (then the 3-colour variants)
+const void* single_colour_tables_host() { return single_colour_host_tables(); }
+
+namespace {
 
 int grid_for(const void* kernel, int threads, uint32_t work_units) {
   int dev = 0, sms = 148, per_sm = 1;

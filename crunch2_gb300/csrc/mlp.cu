@@ -431,17 +431,25 @@ __global__ void __launch_bounds__(kInferThreads, 1)
 // ------------------------------------------------------------------------------------------
 // elementwise / reduction kernels
 
-// dY = 2 (y - t) / B on the 7 trained outputs; loss partial sums
+// Loss gradient dY and loss partial sums. Outputs 0..5 (endpoints): squared error, dY = 2 (y - t) / B.
+// Output 6 (the error bound): squared error when tau <= 0; otherwise the quantile (pinball) loss
+// bw * max(tau (t - y), (1 - tau) (y - t)), whose minimiser is the tau-quantile of the plain
+// optimizer's error given the block, i.e. an upper bound that holds for a fraction tau of blocks.
 __global__ void k_loss_grad(const float* __restrict__ y, const float* __restrict__ t, int B, float* __restrict__ dy,
-                            float* __restrict__ loss) {
+                            float* __restrict__ loss, float tau, float bw) {
   float acc = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B * kOutPad; i += gridDim.x * blockDim.x) {
     const int s = i / kOutPad, c = i % kOutPad;
     float g = 0.f;
     if (c < 7) {
       const float d = y[(long long)s * kOutPad + c] - t[(long long)s * kOut + c];
-      acc += d * d;
-      g = 2.f * d / (float)B;
+      if (c == 6 && tau > 0.f) {
+        acc += bw * (d > 0.f ? (1.f - tau) * d : -tau * d);
+        g = bw * (d > 0.f ? (1.f - tau) : -tau) / (float)B;
+      } else {
+        acc += d * d;
+        g = 2.f * d / (float)B;
+      }
     }
     dy[i] = g;
   }
@@ -583,9 +591,9 @@ __global__ void k_learned_refit(const uint8_t* __restrict__ blocks, const float*
         if (nerr < err) { err = nerr; sel = nsel; for (int k = 0; k < 6; k++) e[k] = f[k]; }
       }
     }
-    // greedy polish: two rounds of the best single +-1 move over the six components
+    // greedy polish: up to three rounds of the best single +-1 move over the six components
 #pragma unroll 1
-    for (int round = 0; round < 2; round++) {
+    for (int round = 0; round < 3; round++) {
       int best_k = -1, best_d = 0;
       uint32_t best_err = err, best_sel = sel;
 #pragma unroll 1
@@ -660,6 +668,7 @@ struct Net {
   int device = -1;
   Param W1, b1, W2, b2, W3, b3;
   int step = 0;
+  float bound_tau = 0.f, bound_weight = 1.f;  // loss of the error-bound output (see k_loss_grad)
   // activations / scratch sized for the largest batch seen
   int cap = 0;
   DevBuf pre1, h1, pre2, h2, y, dy, dpre2, dpre1, dh_b, dh_b1, targets, loss, errflag;
@@ -807,7 +816,7 @@ int backward(Net& net, const uint8_t* blocks, int B, cudaStream_t s) {
   __nv_bfloat16* dhb1 = static_cast<__nv_bfloat16*>(net.dh_b1.ptr);  // bf16 dpre1 (own buffer: dhb is read meanwhile)
   cudaMemsetAsync(net.loss.ptr, 0, 4, s);
   k_loss_grad<<<256, 256, 0, s>>>(static_cast<float*>(net.y.ptr), static_cast<float*>(net.targets.ptr), B, dy,
-                                  static_cast<float*>(net.loss.ptr));
+                                  static_cast<float*>(net.loss.ptr), net.bound_tau, net.bound_weight);
   // dW3 [16 x 256] = dY^T H2 ; db3 = colsum(dY)
   if ((rc = gemm(args(op_f32(dy, 1, kOutPad), op_bf16(static_cast<__nv_bfloat16*>(net.h2.ptr), 1, kHid), kOutPad, kHid,
                       B, EPI_STORE, static_cast<float*>(net.W3.g.ptr), nullptr, nullptr, nullptr, kHid, net),
@@ -902,6 +911,16 @@ extern "C" int crngpu_mlp_param(void* h, int which, int what, float* host, uint3
     return cuda_check(cudaMemcpy(dev, host, count * 4, cudaMemcpyHostToDevice), "write param");
   }
   return cuda_check(cudaMemcpy(host, dev, count * 4, cudaMemcpyDeviceToHost), "read param");
+}
+
+// Loss of the error-bound output: tau <= 0 squared error (weight ignored); 0 < tau < 1 the
+// tau-quantile (pinball) loss scaled by `weight`.
+extern "C" int crngpu_mlp_set_bound_loss(void* h, float tau, float weight) {
+  Net* net = static_cast<Net*>(h);
+  if (!net || net->magic != 0x4D4C5030u || !(tau < 1.f) || !(weight > 0.f)) return CRNGPU_E_PARAM;
+  net->bound_tau = tau > 0.f ? tau : 0.f;
+  net->bound_weight = weight;
+  return CRNGPU_OK;
 }
 
 // Forward pass over n blocks (device RGBA8, n x 64) -> y (device, n x 16 fp32).

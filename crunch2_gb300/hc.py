@@ -1,0 +1,121 @@
+"""Clustered (CRN-style) DXT1 compression through the crngpu C ABI: crn_comp's block layout and
+codebook sizes (crnlib/crn_comp.cpp:424-463, 541-577, 713-741) around crngpu_hc_compress_dxt1,
+the GPU restatement of dxt_hc::compress (crnlib/crn_dxt_hc.cpp:97-316)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import lib, _check, CrnGpuError, E_PARAM, FMT_DXT1
+
+
+class HcParams(ctypes.Structure):
+    class _Level(ctypes.Structure):
+        _fields_ = [("first_block", ctypes.c_uint32), ("num_blocks", ctypes.c_uint32),
+                    ("block_width", ctypes.c_uint32), ("weight", ctypes.c_float)]
+    _fields_ = [("struct_size", ctypes.c_uint32), ("num_blocks", ctypes.c_uint32), ("num_levels", ctypes.c_uint32),
+                ("num_faces", ctypes.c_uint32), ("perceptual", ctypes.c_int32),
+                ("color_endpoint_codebook_size", ctypes.c_uint32), ("color_selector_codebook_size", ctypes.c_uint32),
+                ("adaptive_tile_color_psnr_derating", ctypes.c_float), ("levels", _Level * 16)]
+
+
+class HcStats(ctypes.Structure):
+    _fields_ = [("color_endpoints", ctypes.c_uint32), ("color_selectors", ctypes.c_uint32),
+                ("tiles", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+def _bind():
+    L = lib()
+    if getattr(L, "_hc_bound", False):
+        return L
+    vp = ctypes.c_void_p
+    L.crngpu_hc_compress_dxt1.argtypes = [vp, ctypes.POINTER(HcParams), vp, vp, vp, vp, vp, ctypes.POINTER(HcStats), vp]
+    L.crngpu_hc_compress_dxt1.restype = ctypes.c_int
+    L.crngpu_hc_codebook_sizes.argtypes = [ctypes.c_uint32] * 4 + [ctypes.POINTER(ctypes.c_uint32)]
+    L.crngpu_hc_codebook_sizes.restype = ctypes.c_int
+    L._hc_bound = True
+    return L
+
+
+def codebook_sizes(width: int, height: int, quality: int, fmt: int = FMT_DXT1):
+    """(colour endpoints, colour selectors, alpha endpoints, alpha selectors) for a quality level."""
+    out = (ctypes.c_uint32 * 4)()
+    _check(_bind().crngpu_hc_codebook_sizes(width, height, quality, fmt, out), "crngpu_hc_codebook_sizes")
+    return tuple(int(v) for v in out)
+
+
+def crn_layout(faces_levels):
+    """faces_levels[face][level] RGBA8 images -> (blocks (n, 64) uint8 in crn_comp's order, per-level
+    (first_block, num_blocks, block_width), per-level visible (blocks_x, blocks_y, padded width)).
+    Each level is padded to a multiple of 8 texels by edge clamping (crnlib/crn_comp.cpp:454-463,
+    717-741); faces of a level are consecutive."""
+    from .texgen import image_blocks
+    nlev = len(faces_levels[0])
+    parts, levels, vis = [], [], []
+    first = 0
+    for l in range(nlev):
+        h, w = faces_levels[0][l].shape[:2]
+        pw, ph = (w + 7) & ~7, (h + 7) & ~7
+        level_blocks = []
+        for f in range(len(faces_levels)):
+            img = faces_levels[f][l]
+            pad = np.pad(img, ((0, ph - h), (0, pw - w), (0, 0)), mode="edge")
+            level_blocks.append(image_blocks(pad))
+        lb = np.concatenate(level_blocks)
+        parts.append(lb)
+        levels.append((first, lb.shape[0], pw // 4))
+        vis.append(((w + 3) // 4, (h + 3) // 4, pw // 4))
+        first += lb.shape[0]
+    return np.ascontiguousarray(np.concatenate(parts)), levels, vis
+
+
+def compress_dxt1(faces_levels, quality: int = 128, perceptual: bool = True, stream=None, with_indices=False):
+    """Clustered DXT1 of a mip chain (faces_levels[face][level]): returns (per level, per face, the
+    visible DXT1 blocks (by, bx, 8)), stats dict[, index arrays])."""
+    import torch
+    L = _bind()
+    blocks, levels, vis = crn_layout(faces_levels)
+    h0, w0 = faces_levels[0][0].shape[:2]
+    ce, cs, _, _ = codebook_sizes(w0, h0, quality)
+    p = HcParams()
+    p.struct_size = ctypes.sizeof(HcParams)
+    p.num_blocks = blocks.shape[0]
+    p.num_levels = len(levels)
+    p.num_faces = len(faces_levels)
+    p.perceptual = int(perceptual)
+    p.color_endpoint_codebook_size = ce
+    p.color_selector_codebook_size = cs
+    p.adaptive_tile_color_psnr_derating = 2.0
+    for i, (fb, nb, bw) in enumerate(levels):
+        p.levels[i].first_block, p.levels[i].num_blocks, p.levels[i].block_width = fb, nb, bw
+        p.levels[i].weight = min(12.0, 1.3 ** i)
+    d_blocks = torch.from_numpy(blocks).cuda()
+    n = blocks.shape[0]
+    out = torch.empty((n, 8), dtype=torch.uint8, device="cuda")
+    idx = None
+    ptrs = [None] * 4
+    if with_indices:
+        idx = {"endpoint_index": torch.empty(n, dtype=torch.int16, device="cuda"),
+               "selector_index": torch.empty(n, dtype=torch.int16, device="cuda"),
+               "endpoints": torch.empty(8192, dtype=torch.int32, device="cuda"),
+               "selectors": torch.empty(8192, dtype=torch.int32, device="cuda")}
+        ptrs = [v.data_ptr() for v in idx.values()]
+    st = HcStats()
+    sp = None if stream is None else getattr(stream, "cuda_stream", stream)
+    _check(L.crngpu_hc_compress_dxt1(d_blocks.data_ptr(), ctypes.byref(p), out.data_ptr(), *ptrs, ctypes.byref(st), sp),
+           "crngpu_hc_compress_dxt1")
+    host = out.cpu().numpy()
+    res = []
+    for (fb, nb, bw), (bx, by, _) in zip(levels, vis):
+        faces = []
+        per_face = nb // len(faces_levels)
+        for f in range(len(faces_levels)):
+            g = host[fb + f * per_face: fb + (f + 1) * per_face].reshape(-1, bw, 8)
+            faces.append(g[:by, :bx])
+        res.append(faces)
+    stats = {"color_endpoints": st.color_endpoints, "color_selectors": st.color_selectors, "tiles": st.tiles,
+             "codebook_request": (ce, cs), "blocks": n}
+    if with_indices:
+        return res, stats, {k: v.cpu().numpy() for k, v in idx.items()}
+    return res, stats

@@ -3,8 +3,9 @@
 The network (48 -> 256 -> 256 -> 8, GELU, BF16 tensor-core GEMMs with FP32 accumulation) is
 trained on blocks the plain GPU optimizer labels (its endpoints and its error); the learned
 encode keeps a refined prediction (selector fit, least-squares refit, +-1 search, 3-colour check)
-unless its error is above a threshold (1.5x by default) times the
-predicted bound, and sends the rest to the exact optimizer.
+unless its error is above a threshold (1.5x by default) times the predicted bound -- the
+network's 0.75-quantile estimate of the error the plain optimizer reaches -- and sends the rest
+to the exact optimizer.
 """
 from __future__ import annotations
 
@@ -17,9 +18,12 @@ from . import lib, _check, CrnGpuError, E_PARAM, dxt1_optimize
 import os
 
 PARAM_SHAPES = [(256, 48), (256,), (256, 256), (256,), (16, 256), (16,)]
-# Trained network shipped with the package: `python -m crunch2_gb300.learned out=<this path>`
+# Trained network shipped with the package:
+#   python -m crunch2_gb300.learned steps=16384 tau=0.75 bound_weight=0.25 out=<this path>
 # (16,777,216 training blocks from 64 seeded 2048x2048 colour textures, labels from the plain
-# GPU optimizer, 2048 AdamW steps of 8192 blocks, lr 1e-3, weight decay 0.01, init seed 0).
+# GPU optimizer, 16384 AdamW steps of 8192 blocks (8 epochs), lr 1e-3, weight decay 0.01, init
+# seed 0; endpoint outputs trained on squared error, the error-bound output on the 0.75-quantile
+# pinball loss so that it is an upper bound of the plain optimizer's error for 75% of blocks).
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "dxt1_endpoint_net.npz")
 DEFAULT_THRESHOLD = 1.5
 PARAM_NAMES = ["W1", "b1", "W2", "b2", "W3", "b3"]
@@ -39,8 +43,9 @@ def _bind():
     L.crngpu_mlp_gradients.argtypes = [vp, vp, vp, u32, ctypes.POINTER(f32), vp]
     L.crngpu_mlp_train_step.argtypes = [vp, vp, vp, u32, f32, f32, ctypes.POINTER(f32), vp]
     L.crngpu_dxt1_learned.argtypes = [vp, vp, u32, i32, f32, vp, ctypes.POINTER(u32), vp]
+    L.crngpu_mlp_set_bound_loss.argtypes = [vp, f32, f32]
     for fn in ("crngpu_mlp_destroy", "crngpu_mlp_param", "crngpu_mlp_forward", "crngpu_mlp_make_targets",
-               "crngpu_mlp_gradients", "crngpu_mlp_train_step", "crngpu_dxt1_learned"):
+               "crngpu_mlp_gradients", "crngpu_mlp_train_step", "crngpu_dxt1_learned", "crngpu_mlp_set_bound_loss"):
         getattr(L, fn).restype = i32
     L._mlp_bound = True
     return L
@@ -84,6 +89,10 @@ class EndpointNet:
     def load(self, state: dict):
         for i, nm in enumerate(PARAM_NAMES):
             self.set(i, state[nm])
+
+    def set_bound_loss(self, tau: float, weight: float = 1.0):
+        """tau <= 0: squared error on the bound output; 0 < tau < 1: tau-quantile (pinball) loss."""
+        _check(self.L.crngpu_mlp_set_bound_loss(self.h, tau, weight), "crngpu_mlp_set_bound_loss")
 
     # compute ---------------------------------------------------------------------------------
     def forward(self, d_blocks, stream=None):
@@ -196,16 +205,20 @@ def rgb_rmse_torch(blocks8, pixels):
 
 
 def config4(train_textures=64, train_size=2048, eval_textures=32, eval_size=4096, steps=2048, batch=8192,
-            lr=1e-3, threshold=1.5, log_every=256, seed=0, weights=None):
+            lr=1e-3, threshold=1.5, log_every=256, seed=0, weights=None, tau=0.0, bound_weight=1.0):
     """Learned endpoint proposal end to end: GPU-labelled training set, GPU training, and learned
     vs plain DXT1 encode on held-out textures (different seed range). `threshold` may be a list
     (or a comma-separated string) to report several fallback thresholds from one trained net;
-    `weights` loads a saved state instead of training. Returns a metrics dict."""
+    `weights` loads a saved state instead of training; tau > 0 trains the error-bound output as
+    the tau-quantile of the plain optimizer's error (pinball loss, scaled by bound_weight).
+    Returns a metrics dict."""
     import time
     import torch
     ev = lambda: torch.cuda.Event(enable_timing=True)
     net = EndpointNet(seed=seed)
-    res = {}
+    res = {"tau": tau, "bound_weight": bound_weight}
+    if tau > 0:
+        net.set_bound_loss(tau, bound_weight)
     if weights:
         net.load(dict(np.load(weights)))
         res["weights"] = str(weights)

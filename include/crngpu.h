@@ -106,6 +106,51 @@ CRNGPU_API int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, ui
                               void* stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Clustered (CRN-style) DXT1 compression: dxt_hc::compress (crnlib/crn_dxt_hc.cpp:97-316) for
+ * cDXT1 on the GPU -- adaptive tiles, endpoint codebook VQ, per-cluster endpoint optimisation,
+ * selector codebook VQ. The reference's clusterizer is not thread-count deterministic, so this
+ * path is judged on quality (RGB RMSE at the same codebook sizes), not bit-exactness.
+ * --------------------------------------------------------------------------------------- */
+
+/* dxt_hc::params (crnlib/crn_dxt_hc.h:113-173) for DXT1. Blocks are in the crn_comp layout
+ * (crnlib/crn_comp.cpp:454-463, 717-741): per level, per face, rows of block_width blocks, each
+ * level padded to a multiple of 8 texels so that block_width and the row count are even. */
+typedef struct crngpu_hc_params {
+    uint32_t struct_size;                   /* sizeof(crngpu_hc_params) */
+    uint32_t num_blocks;                    /* m_num_blocks */
+    uint32_t num_levels, num_faces;         /* m_num_levels (1..16), m_num_faces */
+    int32_t perceptual;                     /* m_perceptual */
+    uint32_t color_endpoint_codebook_size;  /* m_color_endpoint_codebook_size */
+    uint32_t color_selector_codebook_size;  /* m_color_selector_codebook_size */
+    float adaptive_tile_color_psnr_derating; /* m_adaptive_tile_color_psnr_derating (2.0) */
+    struct {
+        uint32_t first_block, num_blocks, block_width;
+        float weight;                       /* min(12, 1.3^level) in crn_comp */
+    } levels[16];
+} crngpu_hc_params;
+
+typedef struct crngpu_hc_stats {
+    uint32_t color_endpoints;  /* endpoint codebook entries produced */
+    uint32_t color_selectors;  /* selector codebook entries produced */
+    uint32_t tiles;            /* tiles the adaptive tiling chose */
+    uint32_t reserved;
+} crngpu_hc_stats;
+
+/* d_blocks: num_blocks x 64 bytes (device); d_out: num_blocks x 8 bytes of DXT1 (device).
+ * Optional device outputs (NULL to skip): per-block endpoint / selector codebook indices
+ * (uint16), the endpoint codebook (uint32 first | second << 16, first > second) and the selector
+ * codebook (uint32, 2-bit linear selectors, pixel p at bits 2p). stats (host) may be NULL.
+ * Synchronises `stream`. */
+CRNGPU_API int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_params* params, uint8_t* d_out,
+                                       uint16_t* d_endpoint_idx, uint16_t* d_selector_idx, uint32_t* d_endpoints,
+                                       uint32_t* d_selectors, crngpu_hc_stats* stats, void* stream);
+
+/* Codebook sizes for a quality level (crn_comp::quantize_images, crnlib/crn_comp.cpp:541-577):
+ * sizes4 = colour endpoints, colour selectors, alpha endpoints, alpha selectors. */
+CRNGPU_API int crngpu_hc_codebook_sizes(uint32_t width, uint32_t height, uint32_t quality_level, uint32_t format,
+                                        uint32_t* sizes4);
+
+/* ------------------------------------------------------------------------------------------
  * Learned DXT1 endpoint proposal (no counterpart in the reference). A 48 -> 256 -> 256 -> 8 MLP
  * (GELU, BF16 weights, FP32 accumulation on tcgen05 tensor cores) predicts the endpoints the
  * plain optimizer would choose and the error it would reach; the learned encode refines the
@@ -131,7 +176,12 @@ CRNGPU_API int crngpu_mlp_forward(void* net, const uint8_t* d_blocks, uint32_t n
 CRNGPU_API int crngpu_mlp_make_targets(const uint8_t* d_blocks8, const uint64_t* d_err, uint32_t n,
                                        float* d_targets, void* stream);
 
-/* Mean-squared-error gradients for a batch into the gradient buffers; *loss (host) gets the loss. */
+/* Loss of the error-bound output y[6]: tau <= 0 squared error (the default); 0 < tau < 1 the
+ * tau-quantile (pinball) loss times `weight`, so y[6] learns an upper bound of the plain
+ * optimizer's error that holds for a fraction tau of blocks. Endpoint outputs keep squared error. */
+CRNGPU_API int crngpu_mlp_set_bound_loss(void* net, float tau, float weight);
+
+/* Loss gradients for a batch into the gradient buffers; *loss (host) gets the loss. */
 CRNGPU_API int crngpu_mlp_gradients(void* net, const uint8_t* d_blocks, const float* d_targets, uint32_t n,
                                     float* loss, void* stream);
 
@@ -204,9 +254,13 @@ typedef struct crngpu_unpack_batch_s* crngpu_unpack_batch;
 CRNGPU_API crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_batch_item* items, uint32_t n);
 
 /* Enqueues the batch on `stream` without synchronising: a two-word memset and two kernels.
- * use_graph = 1 captures them into a CUDA graph on the first call and replays that graph on
- * later calls (one launch from the host per batch). */
-CRNGPU_API int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, int use_graph, void* stream);
+ * flags: CRNGPU_BATCH_GRAPH captures them into a CUDA graph on the first call and replays that
+ * graph on later calls (one launch from the host per batch); CRNGPU_BATCH_EXPAND_ONLY re-runs
+ * only the expansion kernel from the index records of the last decode (the destinations are
+ * rewritten; used to time the HBM-bound expansion on its own). */
+#define CRNGPU_BATCH_GRAPH 1u
+#define CRNGPU_BATCH_EXPAND_ONLY 2u
+CRNGPU_API int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t flags, void* stream);
 
 /* Synchronises `stream` and reports the last launch's outcome: CRNGPU_OK, or CRNGPU_E_CORRUPT if
  * a block stream held an invalid code or palette index (the reference's bool result). */

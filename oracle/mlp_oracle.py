@@ -5,7 +5,8 @@ The GPU computes GEMMs from BF16 operands with FP32 accumulation; this oracle ro
 BF16 at the same points (inputs, weights, hidden activations, the backward operands) and
 accumulates in float64, so the comparison isolates accumulation order and transcendental ulps.
 Architecture: y = W3 g(W2 g(W1 x + b1) + b2) + b3, g = tanh-form GELU; loss = mean over samples
-of the sum over outputs 0..6 of (y - t)^2.
+of the sum over outputs 0..5 of (y - t)^2 plus, for output 6, (y - t)^2 or (tau > 0) the pinball
+loss bw * max(tau (t - y), (1 - tau) (y - t)).
 """
 from __future__ import annotations
 
@@ -48,13 +49,18 @@ def forward(p: dict, blocks: np.ndarray):
     return y, (x, pre1, h1, pre2, h2)
 
 
-def gradients(p: dict, blocks: np.ndarray, targets: np.ndarray):
+def gradients(p: dict, blocks: np.ndarray, targets: np.ndarray, tau: float = 0.0, bw: float = 1.0):
     y, (x, pre1, h1, pre2, h2) = forward(p, blocks)
     B = y.shape[0]
     d = np.zeros_like(y)
     d[:, :7] = y[:, :7] - targets[:, :7]
-    loss = float((d[:, :7] ** 2).sum() / B)
     dy = 2 * d / B
+    if tau > 0:
+        r = d[:, 6]
+        loss = float(((d[:, :6] ** 2).sum() + (bw * np.where(r > 0, (1 - tau) * r, -tau * r)).sum()) / B)
+        dy[:, 6] = bw * np.where(r > 0, 1 - tau, -tau) / B
+    else:
+        loss = float((d[:, :7] ** 2).sum() / B)
     g = {}
     g["W3"] = bf16(dy).T @ h2
     g["b3"] = dy.sum(0)

@@ -1,0 +1,92 @@
+"""Clustered (CRN-style) DXT1 on the GPU against the reference's own clustered output: the
+reference's q128 .crn of the same texture (committed fixture), transcoded, gives the RGB RMSE the
+GPU path must match at the same codebook sizes. The reference's clusterizer is not thread-count
+deterministic, so the comparison is on quality, not on bits."""
+import numpy as np
+import pytest
+
+import golden_util as G
+from dxt_decode import rgb_rmse
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def hc():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from crunch2_gb300 import hc
+    hc._bind()
+    return hc
+
+
+def reference_rmse(name, levels):
+    """RMSE of the reference's clustered encode: its .crn transcoded by the oracle, all levels."""
+    from oracle import port
+    from crunch2_gb300 import texgen
+    crn = G.crn_bytes(name)
+    m = G.manifest()[name]
+    dec, src = [], []
+    for l, img in enumerate(levels):
+        dec.append(port.unpack_level(crn, l, m["levels"][l]["bytes"]).reshape(-1, 8))
+        src.append(texgen.image_blocks(img))
+    return rgb_rmse(np.concatenate(dec), np.concatenate(src))
+
+
+def gpu_rmse(out, levels):
+    from crunch2_gb300 import texgen
+    dec = np.concatenate([out[l][0].reshape(-1, 8) for l in range(len(levels))])
+    src = np.concatenate([texgen.image_blocks(img) for img in levels])
+    return rgb_rmse(dec, src)
+
+
+@pytest.mark.parametrize("name,size,seed", [("dxt1_256", 256, 10), ("c1_dxt1_1024", 1024, 100)])
+def test_clustered_dxt1_matches_reference_quality(hc, name, size, seed):
+    from crunch2_gb300 import texgen
+    levels = texgen.mip_chain(texgen.colour_texture(size, size, seed))
+    out, stats = hc.compress_dxt1([levels], quality=128)
+    ce, cs = stats["codebook_request"]
+    assert (ce, cs) == hc.codebook_sizes(size, size, 128)[:2]
+    m = G.manifest()[name]
+    assert 0 < stats["color_endpoints"] <= min(ce, stats["tiles"])
+    assert 0 < stats["color_selectors"] <= cs
+    ours, ref = gpu_rmse(out, levels), reference_rmse(name, levels)
+    print(f"{name}: GPU clustered RMSE {ours:.4f}, reference q128 .crn {ref:.4f}, stats {stats}")
+    assert ours <= 1.10 * ref, (ours, ref)
+
+
+def test_clustered_dxt1_indices_reproduce_blocks(hc):
+    """The endpoint/selector codebooks and per-block indices (what a .crn stores) rebuild exactly
+    the DXT1 blocks the call returned."""
+    from crunch2_gb300 import texgen
+    levels = texgen.mip_chain(texgen.colour_texture(128, 128, 21))
+    out, stats, idx = hc.compress_dxt1([levels], quality=128, with_indices=True)
+    blocks, lv, vis = hc.crn_layout([levels])
+    ei = idx["endpoint_index"].astype(np.uint16).astype(np.int64)
+    si = idx["selector_index"].astype(np.uint16).astype(np.int64)
+    eps = idx["endpoints"].astype(np.uint32)[:stats["color_endpoints"]]
+    sels = idx["selectors"].astype(np.uint32)[:stats["color_selectors"]]
+    assert ei.max() < len(eps) and si.max() < len(sels)
+    first, second = eps & 0xFFFF, eps >> 16
+    assert (first > second).all()  # 4-colour order
+    from_linear = np.array([0, 2, 3, 1], np.uint32)
+    lin = sels[si]
+    dxt = np.zeros_like(lin)
+    for p in range(16):
+        dxt |= from_linear[(lin >> (2 * p)) & 3] << (2 * p)
+    rebuilt = np.stack([eps[ei], dxt], 1).astype("<u4").view(np.uint8).reshape(-1, 8)
+    fb, nb, bw = lv[0]
+    bx, by, _ = vis[0]
+    assert (rebuilt[fb:fb + nb].reshape(-1, bw, 8)[:by, :bx] == out[0][0]).all()
+
+
+def test_codebook_sizes_follow_quality(hc):
+    # crn_comp::quantize_images: 1024x1024 at q128 (the config-1 sizes) and the clamps at 0 / 255
+    ce, cs, ae, as_ = hc.codebook_sizes(1024, 1024, 128)
+    assert (ce, cs) == (2415, 2692)
+    lo = hc.codebook_sizes(1024, 1024, 0)
+    assert lo[0] == 64 and lo[1] == 96
+    hi = hc.codebook_sizes(64, 64, 255)
+    assert hi[0] == 256 and hi[1] == 256

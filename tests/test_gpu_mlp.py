@@ -71,6 +71,21 @@ def test_gradients_match_oracle(L, batch):
         assert e < 3e-2 and cos > 0.999, (name, e, cos)
 
 
+def test_quantile_bound_gradients_match_oracle(L, batch):
+    from oracle import mlp_oracle
+    blocks, targets = batch
+    net = L.EndpointNet(seed=4)
+    net.set_bound_loss(0.9, 0.25)
+    loss = net.gradients(torch.from_numpy(blocks).cuda(), torch.from_numpy(targets).cuda())
+    ref_loss, ref = mlp_oracle.gradients(net.state(), blocks, targets, tau=0.9, bw=0.25)
+    assert abs(loss - ref_loss) / ref_loss < 1e-2
+    for i, name in enumerate(L.PARAM_NAMES):
+        g = net.get(i, grad=True).astype(np.float64)
+        e = rel_err(g, ref[name])
+        cos = float((g * ref[name]).sum() / (np.linalg.norm(g) * np.linalg.norm(ref[name]) + 1e-30))
+        assert e < 3e-2 and cos > 0.999, (name, e, cos)
+
+
 @pytest.fixture(scope="module")
 def trained(L):
     blocks = L.training_blocks(4, 256, seed0=1000)          # 16,384 training blocks
