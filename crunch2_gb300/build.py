@@ -1,7 +1,8 @@
 """Builds libcrngpu.so (the C-ABI library) in-tree for sm_103a with nvcc.
 
-Translation units are compiled in parallel; dxt_encode.cu is compiled with --fmad=false
-because its float/double code must round exactly like the reference's (no contraction).
+Translation units are compiled in parallel; dxt_encode.cu and hc_encode.cu are compiled with
+--fmad=false because their float/double code must round exactly like the reference's (no
+contraction): the tile errors of the clustered path decide its tile layouts.
 Usage: python -m crunch2_gb300.build   (or crunch2_gb300.build.build())
 """
 from __future__ import annotations
@@ -27,7 +28,7 @@ UNITS = [
     ("encode_api.cu", []),
     ("dxt_encode.cu", ["--fmad=false"]),
     ("mlp.cu", []),
-    ("hc_encode.cu", []),
+    ("hc_encode.cu", ["--fmad=false"]),
 ]
 
 

@@ -9,8 +9,8 @@
 //   k_vq_split<D>     tree_clusterizer (crnlib/crn_tree_clusterizer.h:89-570): a node is split by
 //                     furthest/opposite seeds, a 10-step power iteration for its principal axis and
 //                     a 2-means loop. Instead of the reference's one-node-at-a-time priority queue,
-//                     every round splits all leaves of the current top-variance set at once, one CTA
-//                     per node, until the codebook size is reached.
+//                     a round splits the top quarter of the leaves by variance at once, one CTA per
+//                     node, until the codebook size is reached.
 //   k_nearest_vec6    tile -> nearest endpoint codebook entry (determine_color_endpoint_clusters_task,
 //                     :836-886).
 //   k_cluster_fit     per endpoint cluster, over all pixels of its tiles: principal-axis start, least-
@@ -51,25 +51,25 @@ struct Level {
 // ------------------------------------------------------------------------------------------
 // small helpers
 
-__device__ __forceinline__ int exp5(int v) { return (v << 3) | (v >> 2); }
-__device__ __forceinline__ int exp6(int v) { return (v << 2) | (v >> 4); }
-__device__ __forceinline__ void unpack565(uint32_t c, int* o) {
+__host__ __device__ __forceinline__ int exp5(int v) { return (v << 3) | (v >> 2); }
+__host__ __device__ __forceinline__ int exp6(int v) { return (v << 2) | (v >> 4); }
+__host__ __device__ __forceinline__ void unpack565(uint32_t c, int* o) {
   o[0] = exp5((c >> 11) & 31); o[1] = exp6((c >> 5) & 63); o[2] = exp5(c & 31);
 }
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
-__device__ __forceinline__ uint32_t px_r(uint32_t p) { return p & 255u; }
-__device__ __forceinline__ uint32_t px_g(uint32_t p) { return (p >> 8) & 255u; }
-__device__ __forceinline__ uint32_t px_b(uint32_t p) { return (p >> 16) & 255u; }
+__host__ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+__host__ __device__ __forceinline__ uint32_t px_r(uint32_t p) { return p & 255u; }
+__host__ __device__ __forceinline__ uint32_t px_g(uint32_t p) { return (p >> 8) & 255u; }
+__host__ __device__ __forceinline__ uint32_t px_b(uint32_t p) { return (p >> 16) & 255u; }
 
 // color::color_distance (crnlib/crn_color.h:728-745) for RGB: weights 8/25/1 (perceptual) or 1/1/1.
-__device__ __forceinline__ uint32_t cdist(bool perc, int r0, int g0, int b0, int r1, int g1, int b1) {
+__host__ __device__ __forceinline__ uint32_t cdist(bool perc, int r0, int g0, int b0, int r1, int g1, int b1) {
   const int dr = r0 - r1, dg = g0 - g1, db = b0 - b1;
   return perc ? (uint32_t)(dr * dr * 8 + dg * dg * 25 + db * db) : (uint32_t)(dr * dr + dg * dg + db * db);
 }
 
 // 4-colour palette of (first, second) in DXT order (dxt1_block::get_block_colors4,
 // crnlib/crn_dxt.cpp:247-260): c0, c1, (2 c0 + c1) / 3, (c0 + 2 c1) / 3.
-__device__ __forceinline__ void colors4(uint32_t c0, uint32_t c1, int (*c)[3]) {
+__host__ __device__ __forceinline__ void colors4(uint32_t c0, uint32_t c1, int (*c)[3]) {
   unpack565(c0, c[0]);
   unpack565(c1, c[1]);
   for (int k = 0; k < 3; k++) {
@@ -88,19 +88,19 @@ __constant__ uint8_t c_to_linear[4] = {0, 3, 1, 2};
 
 struct SolidTables { uint8_t m5[256][2], m6[256][2]; };
 
-__device__ __forceinline__ int mul_8bit(int a, int b) {
+__host__ __device__ __forceinline__ int mul_8bit(int a, int b) {
   const int t = a * b + 128;
   return (t + (t >> 8)) >> 8;
 }
-__device__ __forceinline__ uint32_t fast_pack(int r, int g, int b) {
+__host__ __device__ __forceinline__ uint32_t fast_pack(int r, int g, int b) {
   return (uint32_t)((mul_8bit(r, 31) << 11) + (mul_8bit(g, 63) << 5) + mul_8bit(b, 31));
 }
 
 // eval_colors (:76-96): color[0] = c0, color[1] = c1, color[2] = (2 c0 + c1) / 3, color[3] = (2 c1 + c0) / 3
-__device__ __forceinline__ void fast_eval(uint32_t c0, uint32_t c1, int (*col)[3]) { colors4(c0, c1, col); }
+__host__ __device__ __forceinline__ void fast_eval(uint32_t c0, uint32_t c1, int (*col)[3]) { colors4(c0, c1, col); }
 
 // match_block_colors (:99-148); false if all selectors are equal
-__device__ bool fast_match(int n, const uint32_t* px, int (*col)[3], uint8_t* sel) {
+__host__ __device__ bool fast_match(int n, const uint32_t* px, int (*col)[3], uint8_t* sel) {
   const int dirr = col[0][0] - col[1][0], dirg = col[0][1] - col[1][1], dirb = col[0][2] - col[1][2];
   int stops[4];
   for (int i = 0; i < 4; i++) stops[i] = col[i][0] * dirr + col[i][1] * dirg + col[i][2] * dirb;
@@ -119,7 +119,7 @@ __device__ bool fast_match(int n, const uint32_t* px, int (*col)[3], uint8_t* se
 }
 
 // optimize_block_colors (:151-286): principal axis by power iteration, extreme pixels along it
-__device__ bool fast_optimize(int n, const uint32_t* px, uint32_t& max16, uint32_t& min16, int* ave) {
+__host__ __device__ bool fast_optimize(int n, const uint32_t* px, uint32_t& max16, uint32_t& min16, int* ave) {
   int mn[3], mx[3];
   for (int ch = 0; ch < 3; ch++) {
     long long mu = 0;
@@ -127,8 +127,8 @@ __device__ bool fast_optimize(int n, const uint32_t* px, uint32_t& max16, uint32
     for (int i = 0; i < n; i++) {
       const int v = (px[i] >> (8 * ch)) & 255;
       mu += v;
-      lo = min(lo, v);
-      hi = max(hi, v);
+      lo = lo < v ? lo : v;
+      hi = hi > v ? hi : v;
     }
     ave[ch] = (int)((mu + (n / 2)) / n);
     mn[ch] = lo;
@@ -170,7 +170,7 @@ __device__ bool fast_optimize(int n, const uint32_t* px, uint32_t& max16, uint32
 }
 
 // refine_block (:288-335): least-squares endpoints from the selectors (Cramer's rule)
-__device__ bool fast_refine(int n, const uint32_t* px, uint32_t& max16, uint32_t& min16, const uint8_t* sel) {
+__host__ __device__ bool fast_refine(int n, const uint32_t* px, uint32_t& max16, uint32_t& min16, const uint8_t* sel) {
   const int w1Tab[4] = {3, 0, 2, 1};
   const int prods_0[4] = {0x00, 0x00, 0x02, 0x02};
   const int prods_1[4] = {0x00, 0x09, 0x01, 0x04};
@@ -202,7 +202,7 @@ __device__ bool fast_refine(int n, const uint32_t* px, uint32_t& max16, uint32_t
 
 // compress_color_block (:725-764, refine = false) and the squared RGB error of the result against
 // get_block_colors4 (crn_dxt_hc.cpp:459-472)
-__device__ uint32_t fast_tile_error(int n, const uint32_t* px, const SolidTables* __restrict__ st) {
+__host__ __device__ uint32_t fast_tile_error(int n, const uint32_t* px, const SolidTables* __restrict__ st) {
   uint8_t sel[64];
   uint32_t lo16, hi16;
   int ave[3];
@@ -252,7 +252,7 @@ __device__ uint32_t fast_tile_error(int n, const uint32_t* px, const SolidTables
 // ------------------------------------------------------------------------------------------
 // split_vectors (crnlib/crn_tree_clusterizer.h:573-753) for up to 64 weighted vec3: the two
 // centroids of a 2-means split seeded by furthest/opposite points and the principal axis.
-__device__ void split_vec3(const float (*v)[3], const uint32_t* w, int size, float* res) {
+__host__ __device__ void split_vec3(const float (*v)[3], const uint32_t* w, int size, float* res) {
   float cen[3] = {0, 0, 0};
   double ttsum = 0;
   uint64_t tw = 0;
@@ -335,13 +335,14 @@ __device__ void split_vec3(const float (*v)[3], const uint32_t* w, int size, flo
 // Tiles: one thread per 2x2-block chunk.
 
 // tile t of a chunk: offset into the 128-pixel chunk image and size (crn_dxt_hc.cpp:389-390)
-__constant__ uint8_t c_tile_ofs[9] = {0, 16, 32, 48, 0, 32, 64, 96, 64};
+#define HC_TILE_OFS {0, 16, 32, 48, 0, 32, 64, 96, 64}
 // tiles of each layout, in layout order (crn_dxt_hc.cpp:390)
-__constant__ uint8_t c_layout_tiles[8][4] = {{8}, {6, 7}, {4, 5}, {6, 1, 3}, {7, 0, 2}, {4, 2, 3}, {5, 0, 1}, {0, 2, 1, 3}};
-__constant__ uint8_t c_layout_ntiles[8] = {1, 2, 2, 3, 3, 3, 3, 4};
+#define HC_LAYOUT_TILES {{8, 0, 0, 0}, {6, 7, 0, 0}, {4, 5, 0, 0}, {6, 1, 3, 0}, {7, 0, 2, 0}, {4, 2, 3, 0}, {5, 0, 1, 0}, {0, 2, 1, 3}}
+#define HC_LAYOUT_NTILES {1, 2, 2, 3, 3, 3, 3, 4}
 // tile (within the layout) covering each block of the chunk, [layout][by][bx] (g_tile_map, :36-45)
-__constant__ uint8_t c_tile_map[8][2][2] = {{{0, 0}, {0, 0}}, {{0, 0}, {1, 1}}, {{0, 1}, {0, 1}}, {{0, 0}, {1, 2}},
-                                            {{1, 2}, {0, 0}}, {{0, 1}, {0, 2}}, {{1, 0}, {2, 0}}, {{0, 1}, {2, 3}}};
+#define HC_TILE_MAP {{{0, 0}, {0, 0}}, {{0, 0}, {1, 1}}, {{0, 1}, {0, 1}}, {{0, 0}, {1, 2}}, \
+                     {{1, 2}, {0, 0}}, {{0, 1}, {0, 2}}, {{1, 0}, {2, 0}}, {{0, 1}, {2, 3}}}
+__constant__ uint8_t c_tile_ofs[9] = HC_TILE_OFS;
 
 struct Chunk {
   uint32_t b;      // first (top-left) block
@@ -357,21 +358,29 @@ struct Tile {
   float v[6];      // palettize_color result
 };
 
-__device__ __forceinline__ void chunk_pixels(const uint32_t* __restrict__ blocks, uint32_t b, uint32_t width,
-                                             uint32_t* px /* 128 */) {
+__host__ __device__ __forceinline__ uint32_t ld_px(const uint32_t* p) {
+#ifdef __CUDA_ARCH__
+  return __ldg(p);
+#else
+  return *p;
+#endif
+}
+
+__host__ __device__ __forceinline__ void chunk_pixels(const uint32_t* __restrict__ blocks, uint32_t b, uint32_t width,
+                                                      uint32_t* px /* 128 */) {
   const uint32_t bl[4] = {b, b + width, b + 1, b + width + 1};  // [0..63]: TL, BL, TR, BR blocks
   for (int q = 0; q < 4; q++)
-    for (int i = 0; i < 16; i++) px[q * 16 + i] = __ldg(blocks + (size_t)bl[q] * 16 + i);
+    for (int i = 0; i < 16; i++) px[q * 16 + i] = ld_px(blocks + (size_t)bl[q] * 16 + i);
   // [64..127]: top 8x4 then bottom 8x4, row-major (t & 32: lower blocks, t & 4: right block)
   for (int t = 0; t < 64; t += 4) {
     const uint32_t blk = b + ((t & 32) ? width : 0) + ((t & 4) ? 1 : 0);
     const int row = (t >> 1) & 12;
-    for (int i = 0; i < 4; i++) px[64 + t + i] = __ldg(blocks + (size_t)blk * 16 + row + i);
+    for (int i = 0; i < 4; i++) px[64 + t + i] = ld_px(blocks + (size_t)blk * 16 + row + i);
   }
 }
 
 // palettize_color (crn_dxt_hc.cpp:318-351): unique colours (perceptual: r * 0.5, b * 0.25) split in two
-__device__ void palettize(const uint32_t* px, int n, bool perc, float* out6) {
+__host__ __device__ void palettize(const uint32_t* px, int n, bool perc, float* out6) {
   uint32_t col[64];
   for (int i = 0; i < n; i++) col[i] = (px_r(px[i]) << 16) | (px_g(px[i]) << 8) | px_b(px[i]);
   for (int i = 1; i < n; i++) {  // insertion sort (n <= 64)
@@ -406,23 +415,25 @@ __device__ void palettize(const uint32_t* px, int n, bool perc, float* out6) {
   for (int k = 0; k < 6; k++) out6[k] = res[k];
 }
 
-__global__ void __launch_bounds__(64) k_hc_tiles(const uint32_t* __restrict__ blocks, const Chunk* __restrict__ chunks,
-                                                 uint32_t nchunks, const float* __restrict__ derating /* [level][8] */,
-                                                 const float* __restrict__ level_weight, int perceptual,
-                                                 const SolidTables* __restrict__ st, Tile* __restrict__ tiles,
-                                                 uint32_t* __restrict__ block_tile, uint8_t* __restrict__ block_enc) {
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nchunks) return;
-  const Chunk ch = chunks[c];
+// One chunk of determine_tiles_task (crn_dxt_hc.cpp:386-561): tile errors, layout choice, the
+// chosen tiles' vec6, and each block's tile slot and layout. Returns the layout.
+__host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint32_t c, const Chunk& ch,
+                                      const float* __restrict__ derating, const float* __restrict__ level_weight,
+                                      bool perceptual, const SolidTables* __restrict__ st, Tile* __restrict__ tiles,
+                                      uint32_t* __restrict__ block_tile, uint8_t* __restrict__ block_enc) {
+  const uint8_t tile_ofs[9] = HC_TILE_OFS;
+  const uint8_t layout_tiles[8][4] = HC_LAYOUT_TILES;
+  const uint8_t layout_ntiles[8] = HC_LAYOUT_NTILES;
+  const uint8_t tile_map[8][2][2] = HC_TILE_MAP;
   uint32_t px[128];
   chunk_pixels(blocks, ch.b, ch.width, px);
   uint32_t terr[9];
-  for (int t = 0; t < 9; t++) terr[t] = fast_tile_error(16 << (t >> 2), px + c_tile_ofs[t], st);
+  for (int t = 0; t < 9; t++) terr[t] = fast_tile_error(16 << (t >> 2), px + tile_ofs[t], st);
   float best_q = 0.0f;
   int best_e = 0;
   for (int e = 0; e < 8; e++) {
     uint32_t tot = 0;
-    for (int k = 0; k < c_layout_ntiles[e]; k++) tot += terr[c_layout_tiles[e][k]];
+    for (int k = 0; k < layout_ntiles[e]; k++) tot += terr[layout_tiles[e][k]];
     const double psnr = tot ? log10((double)255.0f / sqrt(tot / 192.0)) * (double)20.0f : (double)999999.0f;
     const float q = (float)fmax(psnr - (double)derating[ch.level * 8 + e], 0.0);
     if (q > best_q) { best_q = q; best_e = e; }
@@ -430,26 +441,38 @@ __global__ void __launch_bounds__(64) k_hc_tiles(const uint32_t* __restrict__ bl
   const float lw = level_weight[ch.level];
   for (int k = 0; k < 4; k++) {
     Tile& T = tiles[4 * c + k];
-    if (k >= c_layout_ntiles[best_e]) { T.kind = 0xFFu; T.chunk = c; T.weight = 0; continue; }
-    const int t = c_layout_tiles[best_e][k];
+    if (k >= layout_ntiles[best_e]) { T.kind = 0xFFu; T.chunk = c; T.weight = 0; continue; }
+    const int t = layout_tiles[best_e][k];
     const int n = 16 << (t >> 2);
     T.chunk = c;
     T.kind = (uint32_t)t;
     T.weight = (float)n * lw;
-    palettize(px + c_tile_ofs[t], n, perceptual != 0, T.v);
+    palettize(px + tile_ofs[t], n, perceptual, T.v);
   }
   for (int by = 0; by < 2; by++)
     for (int bx = 0; bx < 2; bx++) {
       const uint32_t blk = ch.b + (by ? ch.width : 0) + bx;
-      block_tile[blk] = 4 * c + c_tile_map[best_e][by][bx];
+      block_tile[blk] = 4 * c + tile_map[best_e][by][bx];
       block_enc[blk] = (uint8_t)best_e;
     }
+  return best_e;
+}
+
+__global__ void __launch_bounds__(64) k_hc_tiles(const uint32_t* __restrict__ blocks, const Chunk* __restrict__ chunks,
+                                                 uint32_t nchunks, const float* __restrict__ derating /* [level][8] */,
+                                                 const float* __restrict__ level_weight, int perceptual,
+                                                 const SolidTables* __restrict__ st, Tile* __restrict__ tiles,
+                                                 uint32_t* __restrict__ block_tile, uint8_t* __restrict__ block_enc) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nchunks) return;
+  hc_tile_chunk(blocks, c, chunks[c], derating, level_weight, perceptual != 0, st, tiles, block_tile, block_enc);
 }
 
 // ------------------------------------------------------------------------------------------
 // Tree clusterizer, batched: one CTA per node to split.
 
 constexpr int kVqThreads = 512;
+constexpr uint32_t kDefaultRoundFraction = 4;  // a VQ round splits at most leaves / 4 nodes
 
 template <int D>
 struct VqNode {
@@ -738,8 +761,8 @@ __global__ void k_iota(uint32_t* p, uint32_t n) {
 // Host driver of the batched tree clusterizer: returns the codebook (leaf centroids) on the device
 // as K x D floats in `codebook` and the leaf count in *k_out.
 template <int D>
-int tree_vq(const float* d_vec, const uint32_t* d_w, uint32_t n, uint32_t max_entries, DevBuf& codebook,
-            uint32_t* k_out, cudaStream_t s) {
+int tree_vq(const float* d_vec, const uint32_t* d_w, uint32_t n, uint32_t max_entries, uint32_t round_fraction,
+            DevBuf& codebook, uint32_t* k_out, cudaStream_t s) {
   using Node = VqNode<D>;
   *k_out = 0;
   if (!n) return CRNGPU_OK;
@@ -771,7 +794,11 @@ int tree_vq(const float* d_vec, const uint32_t* d_w, uint32_t n, uint32_t max_en
     }
     if (cand.empty()) break;
     std::stable_sort(cand.begin(), cand.end(), [&](int a, int b) { return h[a].variance > h[b].variance; });
+    // the reference splits one node at a time, always the leaf of largest variance; a round here
+    // splits the top 1/round_fraction of the splittable leaves by variance (at least one), which
+    // keeps the greedy order's preference for high-variance regions while giving the GPU a batch
     size_t take = std::min(cand.size(), (size_t)max_entries - leaves.size());
+    take = std::min(take, std::max<size_t>(1, leaves.size() / round_fraction));
     take = std::min(take, (max_nodes - used) / 2);
     if (!take) break;
     std::vector<SplitJob> jobs(take);
@@ -883,6 +910,55 @@ struct FitAcc {
   float err;
 };
 
+
+// Unique colours of a cluster in shared memory (open addressing on the packed RGB, count per
+// colour); a cluster with more than kUniqCap / 2 distinct colours skips the probe search.
+constexpr int kUniqCap = 4096;
+constexpr int kMaxCand = 1024;
+__constant__ int16_t c_probe[15] = {0, 1, 2, 3, 5, 7, 9, 10, 13, 15, 19, 27, 43, 59, 91};  // g_uber_probe_table
+
+// Squared error (perceptual or RGB weights) of the 4-colour block (lo, hi) over the unique colours,
+// each pixel on its nearest colour; one warp, result on every lane.
+__device__ __forceinline__ unsigned long long warp_pair_error(uint32_t lo, uint32_t hi, const uint32_t* ucol,
+                                                               const uint32_t* ucnt, int U, bool perc) {
+  int col[4][3];
+  colors4(lo, hi, col);
+  unsigned long long e = 0;
+  for (int i = (int)(threadIdx.x & 31); i < U; i += 32) {
+    const uint32_t c = ucol[i];
+    const int r = (int)(c & 255), g = (int)((c >> 8) & 255), b = (int)((c >> 16) & 255);
+    uint32_t bd = cdist(perc, r, g, b, col[0][0], col[0][1], col[0][2]);
+    bd = min(bd, cdist(perc, r, g, b, col[1][0], col[1][1], col[1][2]));
+    bd = min(bd, cdist(perc, r, g, b, col[2][0], col[2][1], col[2][2]));
+    bd = min(bd, cdist(perc, r, g, b, col[3][0], col[3][1], col[3][2]));
+    e += (unsigned long long)bd * ucnt[i];
+  }
+  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xFFFFFFFFu, e, o);
+  return e;
+}
+
+// Evaluates the candidate pairs cand[0..n) (lo | hi << 16), warp per candidate; returns the best
+// (lowest error, then lowest index) to every thread through shared memory.
+__device__ void best_candidate(const uint32_t* cand, int n, const uint32_t* ucol, const uint32_t* ucnt, int U, bool perc,
+                               unsigned long long* s_be, uint32_t* s_bi, unsigned long long& err, uint32_t& pair) {
+  const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned long long be = ~0ull;
+  uint32_t bi = 0xFFFFFFFFu;
+  for (int i = warp; i < n; i += nw) {
+    const unsigned long long e = warp_pair_error(cand[i] & 0xFFFFu, cand[i] >> 16, ucol, ucnt, U, perc);
+    if (e < be) { be = e; bi = (uint32_t)i; }
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { s_be[warp] = be; s_bi[warp] = bi; }
+  __syncthreads();
+  be = s_be[0]; bi = s_bi[0];
+  for (int w = 1; w < nw; w++)
+    if (s_be[w] < be || (s_be[w] == be && s_bi[w] < bi)) { be = s_be[w]; bi = s_bi[w]; }
+  err = be;
+  pair = bi < (uint32_t)n ? cand[bi] : 0;
+  __syncthreads();
+}
+
 __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __restrict__ blocks,
                                                              const Chunk* __restrict__ chunks,
                                                              const Tile* __restrict__ tiles,
@@ -968,56 +1044,212 @@ __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __r
               bi = clampi((int)floorf(b * 31.f / 255.f + .5f), 0, 31);
     return (uint32_t)((ri << 11) | (gi << 5) | bi);
   };
-  uint32_t e0 = q565(mean[0] + pr[1] * axis[0], mean[1] + pr[1] * axis[1], mean[2] + pr[1] * axis[2]);
-  uint32_t e1 = q565(mean[0] + pr[0] * axis[0], mean[1] + pr[0] * axis[1], mean[2] + pr[0] * axis[2]);
-  // 3. selector fit + least-squares refit, keep the best (error evaluated with nearest-colour selectors)
-  uint32_t best0 = e0, best1 = e1;
+  // spread of the pixels along the axis (unweighted covariance projected on it)
+  const double c_rr = acc[4] / cnt - mean[0] * mean[0], c_rg = acc[5] / cnt - mean[0] * mean[1],
+               c_rb = acc[6] / cnt - mean[0] * mean[2], c_gg = acc[7] / cnt - mean[1] * mean[1],
+               c_gb = acc[8] / cnt - mean[1] * mean[2], c_bb = acc[9] / cnt - mean[2] * mean[2];
+  const double var_ax = axis[0] * axis[0] * c_rr + axis[1] * axis[1] * c_gg + axis[2] * axis[2] * c_bb +
+                        2 * (axis[0] * axis[1] * c_rg + axis[0] * axis[2] * c_rb + axis[1] * axis[2] * c_gb);
+  const float sd = (float)sqrt(fmax(var_ax, 0.0)) * 1.25f;
+  // 3. two starts -- the extreme projections and mean +- 1.25 sigma -- each refined by alternating
+  // nearest-colour selectors and least-squares endpoints; keep the lowest (perceptual) error
+  uint32_t best0 = 0, best1 = 0;
   float best_err = 3.4e38f;
-  for (int it = 0; it < 6; it++) {
-    int col[4][3];
-    colors4(e0, e1, col);  // DXT order
-    float a[10];
-    for (int i = 0; i < 10; i++) a[i] = 0.f;
-    for_pixels([&](uint32_t p) {
-      const int r = px_r(p), g = px_g(p), b = px_b(p);
-      uint32_t bd = 0xFFFFFFFFu;
-      int bs = 0;
-      for (int s = 0; s < 4; s++) {
-        const uint32_t d = cdist(perc, r, g, b, col[s][0], col[s][1], col[s][2]);
-        if (d < bd) { bd = d; bs = s; }
+  for (int start = 0; start < 2; start++) {
+    const float hi_t = start ? fminf(pr[1], sd) : pr[1], lo_t = start ? fmaxf(pr[0], -sd) : pr[0];
+    uint32_t e0 = q565(mean[0] + hi_t * axis[0], mean[1] + hi_t * axis[1], mean[2] + hi_t * axis[2]);
+    uint32_t e1 = q565(mean[0] + lo_t * axis[0], mean[1] + lo_t * axis[1], mean[2] + lo_t * axis[2]);
+    for (int it = 0; it < 8; it++) {
+      int col[4][3];
+      colors4(e0, e1, col);  // DXT order
+      float a[10];
+      for (int i = 0; i < 10; i++) a[i] = 0.f;
+      for_pixels([&](uint32_t p) {
+        const int r = px_r(p), g = px_g(p), b = px_b(p);
+        uint32_t bd = 0xFFFFFFFFu;
+        int bs = 0;
+        for (int q = 0; q < 4; q++) {
+          const uint32_t d = cdist(perc, r, g, b, col[q][0], col[q][1], col[q][2]);
+          if (d < bd) { bd = d; bs = q; }
+        }
+        // weight of the first endpoint at DXT selector q: 1, 0, 2/3, 1/3
+        const float wa = bs == 0 ? 1.f : bs == 1 ? 0.f : bs == 2 ? (2.f / 3.f) : (1.f / 3.f), wb = 1.f - wa;
+        a[0] += wa * wa; a[1] += wa * wb; a[2] += wb * wb;
+        a[3] += wa * r; a[4] += wa * g; a[5] += wa * b;
+        a[6] += wb * r; a[7] += wb * g; a[8] += wb * b;
+        a[9] += (float)bd;
+      });
+      block_sum<10>(a, red);
+      if (a[9] < best_err) { best_err = a[9]; best0 = e0; best1 = e1; }
+      const float det = a[0] * a[2] - a[1] * a[1];
+      if (fabsf(det) < 1e-6f) break;
+      const float inv = 1.f / det;
+      float f0[3], f1[3];
+      for (int c = 0; c < 3; c++) {
+        f0[c] = (a[3 + c] * a[2] - a[6 + c] * a[1]) * inv;
+        f1[c] = (a[6 + c] * a[0] - a[3 + c] * a[1]) * inv;
       }
-      // weight of the first endpoint at DXT selector s: 1, 0, 2/3, 1/3
-      const float wa = bs == 0 ? 1.f : bs == 1 ? 0.f : bs == 2 ? (2.f / 3.f) : (1.f / 3.f), wb = 1.f - wa;
-      a[0] += wa * wa; a[1] += wa * wb; a[2] += wb * wb;
-      a[3] += wa * r; a[4] += wa * g; a[5] += wa * b;
-      a[6] += wb * r; a[7] += wb * g; a[8] += wb * b;
-      a[9] += (float)bd;
-    });
-    block_sum<10>(a, red);
-    if (a[9] < best_err) { best_err = a[9]; best0 = e0; best1 = e1; }
-    const float det = a[0] * a[2] - a[1] * a[1];
-    if (fabsf(det) < 1e-6f) break;
-    const float inv = 1.f / det;
-    float f0[3], f1[3];
-    for (int c = 0; c < 3; c++) {
-      f0[c] = (a[3 + c] * a[2] - a[6 + c] * a[1]) * inv;
-      f1[c] = (a[6 + c] * a[0] - a[3 + c] * a[1]) * inv;
+      const uint32_t n0 = q565(f0[0], f0[1], f0[2]), n1 = q565(f1[0], f1[1], f1[2]);
+      if (n0 == e0 && n1 == e1) break;
+      e0 = n0; e1 = n1;
     }
-    const uint32_t n0 = q565(f0[0], f0[1], f0[2]), n1 = q565(f1[0], f1[1], f1[2]);
-    if (n0 == e0 && n1 == e1) break;
-    e0 = n0; e1 = n1;
+  }
+  // 3b. the uber probe search of dxt1_endpoint_optimizer::optimize_endpoints (crnlib/crn_dxt1.cpp:703-1028)
+  // over the cluster's unique colours: low and high endpoints probed along the principal axis
+  // (g_uber_probe_table steps of 1/64), every low x high pair, then the 26 lattice neighbours and
+  // +-2 axis moves of each endpoint of the best pair; up to four passes.
+  {
+    __shared__ uint32_t s_key[kUniqCap], s_cnt[kUniqCap];
+    __shared__ uint32_t s_cand[kMaxCand];
+    __shared__ unsigned long long s_be[kFitThreads / 32];
+    __shared__ uint32_t s_bi[kFitThreads / 32];
+    __shared__ uint32_t s_nu, s_overflow;
+    __syncthreads();
+    for (int i = threadIdx.x; i < kUniqCap; i += blockDim.x) { s_key[i] = 0; s_cnt[i] = 0; }
+    if (threadIdx.x == 0) { s_nu = 0; s_overflow = 0; }
+    __syncthreads();
+    for_pixels([&](uint32_t p) {
+      const uint32_t key = (p & 0xFFFFFFu) + 1u;  // 0 marks an empty slot
+      uint32_t h = (key * 2654435761u) >> 20;      // 12-bit slot
+      for (int probe_n = 0; probe_n < kUniqCap; probe_n++) {
+        const uint32_t prev = atomicCAS(&s_key[h], 0u, key);
+        if (prev == 0u || prev == key) { atomicAdd(&s_cnt[h], 1u); return; }
+        h = (h + 1) & (kUniqCap - 1);
+      }
+      s_overflow = 1;
+    });
+    __syncthreads();
+    // compact the table in place (slot order); count distinct colours
+    __shared__ uint32_t s_wcnt[kFitThreads / 32 + 1];
+    uint32_t mine_key[kUniqCap / kFitThreads], mine_cnt[kUniqCap / kFitThreads];
+    int nm = 0;
+    for (int i = threadIdx.x * (kUniqCap / kFitThreads); i < (int)((threadIdx.x + 1) * (kUniqCap / kFitThreads)); i++)
+      if (s_key[i]) { mine_key[nm] = s_key[i] - 1u; mine_cnt[nm] = s_cnt[i]; nm++; }
+    {
+      // exclusive scan of nm over the CTA
+      int incl = nm;
+      for (int o = 1; o < 32; o <<= 1) { const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o); if ((threadIdx.x & 31) >= o) incl += v; }
+      if ((threadIdx.x & 31) == 31) s_wcnt[threadIdx.x >> 5] = incl;
+      __syncthreads();
+      int base = 0;
+      for (int w = 0; w < (int)(threadIdx.x >> 5); w++) base += s_wcnt[w];
+      const int at = base + incl - nm;
+      __syncthreads();
+      for (int j = 0; j < nm; j++) { s_key[at + j] = mine_key[j]; s_cnt[at + j] = mine_cnt[j]; }
+      if (threadIdx.x == blockDim.x - 1) s_nu = (uint32_t)(at + nm);
+    }
+    __syncthreads();
+    const int U = (int)s_nu;
+    if (!s_overflow && U > 0 && U <= kUniqCap / 2) {
+      // best so far: the least-squares fit
+      uint32_t bl = best0, bh = best1;
+      unsigned long long berr;
+      {
+        uint32_t pair;
+        if (threadIdx.x == 0) s_cand[0] = bl | (bh << 16);
+        __syncthreads();
+        best_candidate(s_cand, 1, s_key, s_cnt, U, perc, s_be, s_bi, berr, pair);
+      }
+      // low / high colours from the axis projection bounds, in 565 units
+      float lowc[3], highc[3];
+      const float lim[3] = {31.f, 63.f, 31.f};
+      for (int c = 0; c < 3; c++) {
+        lowc[c] = fminf(fmaxf((mean[c] + pr[0] * axis[c]) / 255.f * lim[c], 0.f), lim[c]);
+        highc[c] = fminf(fmaxf((mean[c] + pr[1] * axis[c]) / 255.f * lim[c], 0.f), lim[c]);
+      }
+      float sax[3];
+      for (int c = 0; c < 3; c++) sax[c] = axis[c] * .015625f * lim[c];
+      for (int pass = 0; pass < 4 && berr; pass++) {
+        const unsigned long long prev_err = berr;
+        if (pass) {
+          int cl[3], ch[3];
+          unpack565(bl, cl);
+          unpack565(bh, ch);
+          for (int c = 0; c < 3; c++) { lowc[c] = (float)cl[c] / 255.f * lim[c]; highc[c] = (float)ch[c] / 255.f * lim[c]; }
+        }
+        // probe lists (thread 0), then every low x high pair
+        __shared__ uint32_t s_pl[32], s_ph[32], s_npl, s_nph;
+        if (threadIdx.x == 0) {
+          for (int which = 0; which < 2; which++) {
+            const float* base = which ? highc : lowc;
+            uint32_t* outp = which ? s_ph : s_pl;
+            int prev[2] = {-1, -1}, n = 0;
+            for (int i = 0; i < 15; i++) {
+              const int x = c_probe[i];
+              for (int sg = i ? 0 : 1; sg < 2; sg++) {
+                const float f = sg ? 1.f : -1.f;
+                const int r = clampi((int)floorf(base[0] + .5f + f * sax[0] * (float)x), 0, 31);
+                const int g = clampi((int)floorf(base[1] + .5f + f * sax[1] * (float)x), 0, 63);
+                const int b = clampi((int)floorf(base[2] + .5f + f * sax[2] * (float)x), 0, 31);
+                const int pc = b | (g << 5) | (r << 11);
+                if (pc != prev[sg]) { outp[n++] = (uint32_t)pc; prev[sg] = pc; }
+              }
+            }
+            if (which) s_nph = (uint32_t)n; else s_npl = (uint32_t)n;
+          }
+        }
+        __syncthreads();
+        const int npl = (int)s_npl, nph = (int)s_nph;
+        for (int i = threadIdx.x; i < npl * nph; i += blockDim.x) s_cand[i] = s_pl[i / nph] | (s_ph[i % nph] << 16);
+        __syncthreads();
+        {
+          unsigned long long e;
+          uint32_t pair;
+          best_candidate(s_cand, npl * nph, s_key, s_cnt, U, perc, s_be, s_bi, e, pair);
+          if (e < berr) { berr = e; bl = pair & 0xFFFFu; bh = pair >> 16; }
+        }
+        // lattice neighbours (26) and +-2 axis moves of the low endpoint, then of the high one
+        for (int which = 0; which < 2; which++) {
+          if (threadIdx.x == 0) {
+            int n = 0;
+            const uint32_t E = which ? bh : bl, O2 = which ? bl : bh;
+            const int r0 = (E >> 11) & 31, g0 = (E >> 5) & 63, b0 = E & 31;
+            for (int dr = -1; dr <= 1; dr++)
+              for (int dg = -1; dg <= 1; dg++)
+                for (int db = -1; db <= 1; db++) {
+                  if (!dr && !dg && !db) continue;
+                  const int r = r0 + dr, g = g0 + dg, b = b0 + db;
+                  if (r < 0 || r > 31 || g < 0 || g > 63 || b < 0 || b > 31) continue;
+                  const uint32_t X = (uint32_t)((r << 11) | (g << 5) | b);
+                  s_cand[n++] = which ? (O2 | (X << 16)) : (X | (O2 << 16));
+                }
+            const int d6[6][3] = {{-2, 0, 0}, {2, 0, 0}, {0, -2, 0}, {0, 2, 0}, {0, 0, -2}, {0, 0, 2}};
+            for (int q = 0; q < 6; q++) {
+              const int r = r0 + d6[q][0], g = g0 + d6[q][1], b = b0 + d6[q][2];
+              if (r < 0 || r > 31 || g < 0 || g > 63 || b < 0 || b > 31) continue;
+              const uint32_t X = (uint32_t)((r << 11) | (g << 5) | b);
+              s_cand[n++] = which ? (O2 | (X << 16)) : (X | (O2 << 16));
+            }
+            s_npl = (uint32_t)n;
+          }
+          __syncthreads();
+          const int n = (int)s_npl;
+          unsigned long long e;
+          uint32_t pair;
+          best_candidate(s_cand, n, s_key, s_cnt, U, perc, s_be, s_bi, e, pair);
+          if (e < berr) { berr = e; bl = pair & 0xFFFFu; bh = pair >> 16; }
+        }
+        if (pass && berr == prev_err) break;
+      }
+      best0 = bl;
+      best1 = bh;
+    }
+    __syncthreads();
   }
   // 4. dxt_endpoint_refiner::optimize_dxt1 (crn_dxt_endpoint_refiner.cpp:203-302): histogram
-  // statistics of the selectors (linear order) and a lattice walk on both endpoints
+  // statistics of the current selectors and a lattice walk on both endpoints; repeated with the
+  // selectors re-chosen for the walk's result while the true error keeps falling
+  __shared__ unsigned long long s_stat[29];  // hist[4], D2[4][3], DD[4][3] (exact integers), error
+  __shared__ uint32_t s_LH[2];
   uint32_t L0 = best0 > best1 ? best0 : best1, H0 = best0 > best1 ? best1 : best0;
   if (L0 == H0) { if (L0 < 0xFFFFu) L0++; else H0--; }
-  __shared__ unsigned long long s_stat[28];  // hist[4], D2[4][3], DD[4][3] (exact integers)
-  double hist[4], D2[4][3], DD[4][3];
-  {
+  uint32_t keepL = L0, keepH = H0;
+  unsigned long long keep_err = ~0ull;
+  for (int outer = 0; outer < 4; outer++) {
     int col[4][3];
     colors4(L0, H0, col);
     __syncthreads();
-    if (threadIdx.x < 28) s_stat[threadIdx.x] = 0;
+    if (threadIdx.x < 29) s_stat[threadIdx.x] = 0;
     __syncthreads();
     for_pixels([&](uint32_t p) {
       const int r = px_r(p), g = px_g(p), b = px_b(p);
@@ -1033,68 +1265,85 @@ __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __r
         atomicAdd(&s_stat[4 + bs * 3 + c], (unsigned long long)(2 * rgb[c]));
         atomicAdd(&s_stat[16 + bs * 3 + c], (unsigned long long)(rgb[c] * rgb[c]));
       }
+      atomicAdd(&s_stat[28], (unsigned long long)bd);
     });
     __syncthreads();
-    for (int q = 0; q < 4; q++) {
-      hist[q] = (double)s_stat[q];
-      for (int c = 0; c < 3; c++) { D2[q][c] = (double)s_stat[4 + q * 3 + c]; DD[q][c] = (double)s_stat[16 + q * 3 + c]; }
+    const unsigned long long true_err = s_stat[28];
+    if (true_err >= keep_err) break;  // uniform: every thread reads the same shared value
+    keep_err = true_err;
+    keepL = L0;
+    keepH = H0;
+    if (threadIdx.x == 0) {
+      double hist[4], D2[4][3], DD[4][3];
+      for (int q = 0; q < 4; q++) {
+        hist[q] = (double)s_stat[q];
+        for (int c = 0; c < 3; c++) { D2[q][c] = (double)s_stat[4 + q * 3 + c]; DD[q][c] = (double)s_stat[16 + q * 3 + c]; }
+      }
+      auto err_of = [&](uint32_t L, uint32_t H) {
+        int cc[4][3];
+        colors4(L, H, cc);
+        double er = 0;
+        for (int q = 0; q < 4; q++) {
+          double d[3];
+          for (int c = 0; c < 3; c++) d[c] = hist[q] * cc[q][c] * cc[q][c] - D2[q][c] * cc[q][c] + DD[q][c];
+          er += perc ? d[0] * 8 + d[1] * 25 + d[2] : d[0] + d[1] + d[2];
+        }
+        return er;
+      };
+      uint32_t wL = L0, wH = H0;
+      double best = err_of(wL, wH);
+      const bool preserveL = hist[0] + hist[2] > hist[1] + hist[3];
+      bool improved = true;
+      for (int iters = 8; improved && iters; iters--) {
+        improved = false;
+        uint32_t sol[54];
+        int ns = 0;
+        for (int which = 0; which < 2; which++) {
+          const uint32_t E = which ? wH : wL, O2 = which ? wL : wH;
+          const int b0 = E & 31, g0 = (E >> 5) & 63, r0 = (E >> 11) & 31;
+          for (int b = b0 ? b0 - 1 : b0; b <= b0 + 1 && b <= 31; b++)
+            for (int g = g0 ? g0 - 1 : g0; g <= g0 + 1 && g <= 63; g++)
+              for (int r = r0 ? r0 - 1 : r0; r <= r0 + 1 && r <= 31; r++) {
+                const uint32_t X = (uint32_t)((r << 11) | (g << 5) | b);
+                if (X != E) sol[ns++] = X > O2 ? (X | (O2 << 16)) : (O2 | (X << 16));
+              }
+        }
+        for (int i = 1; i < ns; i++) {  // sorted, as the reference evaluates them
+          const uint32_t x = sol[i];
+          int j = i - 1;
+          while (j >= 0 && sol[j] > x) { sol[j + 1] = sol[j]; j--; }
+          sol[j + 1] = x;
+        }
+        for (int i = 0; i < ns; i++) {
+          if (i && sol[i] == sol[i - 1]) continue;
+          uint32_t L = sol[i] & 0xFFFFu, H = sol[i] >> 16;
+          if (L == H) {
+            L += !preserveL ? ((~L & 0x1F) ? 0x1 : (~L & 0xF800) ? 0x800 : (~L & 0x7E0) ? 0x20 : 0) : (!L ? 0x1 : 0);
+            H -= preserveL ? ((H & 0x1F) ? 0x1 : (H & 0xF800) ? 0x800 : (H & 0x7E0) ? 0x20 : 0) : (H == 0xFFFF ? 0x1 : 0);
+            L &= 0xFFFFu; H &= 0xFFFFu;
+          }
+          const double er = err_of(L, H);
+          if (er < best) { best = er; wL = L; wH = H; improved = true; }
+        }
+        if (best == 0) break;
+      }
+      if (wL <= wH) {  // keep 4-colour order (first > second)
+        if (wL == wH) { if (wL < 0xFFFFu) wL++; else wH--; }
+        else { const uint32_t t = wL; wL = wH; wH = t; }
+      }
+      s_LH[0] = wL;
+      s_LH[1] = wH;
     }
+    __syncthreads();
+    if (s_LH[0] == L0 && s_LH[1] == H0) break;
+    L0 = s_LH[0];
+    H0 = s_LH[1];
   }
   if (threadIdx.x == 0) {
-    auto err_of = [&](uint32_t L, uint32_t H) {
-      int col[4][3];
-      colors4(L, H, col);
-      double er = 0;
-      for (int s = 0; s < 4; s++) {
-        double d[3];
-        for (int c = 0; c < 3; c++) d[c] = hist[s] * col[s][c] * col[s][c] - D2[s][c] * col[s][c] + DD[s][c];
-        er += perc ? d[0] * 8 + d[1] * 25 + d[2] : d[0] + d[1] + d[2];
-      }
-      return er;
-    };
-    double best = err_of(L0, H0);
-    const bool preserveL = hist[0] + hist[2] > hist[1] + hist[3];
-    bool improved = true;
-    for (int iters = 8; improved && iters; iters--) {
-      improved = false;
-      uint32_t sol[54];
-      int ns = 0;
-      for (int which = 0; which < 2; which++) {
-        const uint32_t E = which ? H0 : L0, O2 = which ? L0 : H0;
-        const int b0 = E & 31, g0 = (E >> 5) & 63, r0 = (E >> 11) & 31;
-        for (int b = b0 ? b0 - 1 : b0; b <= b0 + 1 && b <= 31; b++)
-          for (int g = g0 ? g0 - 1 : g0; g <= g0 + 1 && g <= 63; g++)
-            for (int r = r0 ? r0 - 1 : r0; r <= r0 + 1 && r <= 31; r++) {
-              const uint32_t X = (uint32_t)((r << 11) | (g << 5) | b);
-              if (X != E) sol[ns++] = X > O2 ? (X | (O2 << 16)) : (O2 | (X << 16));
-            }
-      }
-      for (int i = 1; i < ns; i++) {  // sort (order of evaluation follows the reference)
-        const uint32_t x = sol[i];
-        int j = i - 1;
-        while (j >= 0 && sol[j] > x) { sol[j + 1] = sol[j]; j--; }
-        sol[j + 1] = x;
-      }
-      for (int i = 0; i < ns; i++) {
-        if (i && sol[i] == sol[i - 1]) continue;
-        uint32_t L = sol[i] & 0xFFFFu, H = sol[i] >> 16;
-        if (L == H) {
-          L += !preserveL ? ((~L & 0x1F) ? 0x1 : (~L & 0xF800) ? 0x800 : (~L & 0x7E0) ? 0x20 : 0) : (!L ? 0x1 : 0);
-          H -= preserveL ? ((H & 0x1F) ? 0x1 : (H & 0xF800) ? 0x800 : (H & 0x7E0) ? 0x20 : 0) : (H == 0xFFFF ? 0x1 : 0);
-          L &= 0xFFFFu; H &= 0xFFFFu;
-        }
-        const double er = err_of(L, H);
-        if (er < best) { best = er; L0 = L; H0 = H; improved = true; if (best == 0) { improved = false; break; } }
-      }
-    }
-    if (L0 <= H0) {  // keep 4-colour order (first > second)
-      if (L0 == H0) { if (L0 < 0xFFFFu) L0++; else H0--; }
-      else { const uint32_t t = L0; L0 = H0; H0 = t; }
-    }
-    O.first = L0;
-    O.second = H0;
+    O.first = keepL;
+    O.second = keepH;
     int col[4][3];
-    colors4(L0, H0, col);
+    colors4(keepL, keepH, col);
     for (int i = 0; i < 4; i++)
       for (int c = 0; c < 3; c++) O.col[i][c] = col[c_from_linear[i]][c];
   }
@@ -1107,7 +1356,8 @@ __global__ void k_block_selectors(const uint32_t* __restrict__ blocks, uint32_t 
                                   const uint32_t* __restrict__ block_tile, const uint32_t* __restrict__ tile_cluster,
                                   const uint8_t* __restrict__ block_enc, const float* __restrict__ block_weight,
                                   const ClusterOut* __restrict__ cl, int perceptual, uint32_t* __restrict__ block_cluster,
-                                  float* __restrict__ sel_vec /* n x 16 */, uint32_t* __restrict__ sel_w) {
+                                  float* __restrict__ sel_vec /* n x 16 */, uint32_t* __restrict__ sel_w,
+                                  unsigned long long* __restrict__ sse) {
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nblocks) return;
   const bool perc = perceptual != 0;
@@ -1119,6 +1369,7 @@ __global__ void k_block_selectors(const uint32_t* __restrict__ blocks, uint32_t 
   float wf = (float)ew * block_weight[b];
   wf = wf < 1.f ? 1.f : (wf > 2048.f ? 2048.f : wf);
   const uint32_t weight = (uint32_t)((float)(uint32_t)wf * enc_w);
+  uint32_t rgb_sse = 0;
   for (int p = 0; p < 16; p++) {
     const uint32_t px = __ldg(blocks + (size_t)b * 16 + p);
     uint32_t bd = 0xFFFFFFFFu;
@@ -1129,8 +1380,10 @@ __global__ void k_block_selectors(const uint32_t* __restrict__ blocks, uint32_t 
       if (d < bd) { bd = d; bs = s; }
     }
     sel_vec[(size_t)b * 16 + p] = ((float)bs + 0.5f) * 0.25f;  // vector component v[s] = (s + 0.5) / 4
+    rgb_sse += cdist(false, px_r(px), px_g(px), px_b(px), C.col[bs][0], C.col[bs][1], C.col[bs][2]);
   }
   sel_w[b] = weight;
+  atomicAdd(sse, (unsigned long long)rgb_sse);
 }
 
 // codebook vectors -> 2-bit linear selectors (crn_dxt_hc.cpp:1468-1476)
@@ -1201,16 +1454,22 @@ __global__ void k_selector_finalise(const unsigned long long* __restrict__ entry
 }
 
 // finished DXT1 blocks: cluster endpoints + codebook selectors (linear -> DXT order)
-__global__ void k_hc_emit(uint32_t nblocks, const uint32_t* __restrict__ block_cluster, const ClusterOut* __restrict__ cl,
-                          const uint32_t* __restrict__ block_sel, const uint32_t* __restrict__ cbsel,
-                          uint2* __restrict__ out) {
+__global__ void k_hc_emit(const uint32_t* __restrict__ blocks, uint32_t nblocks, const uint32_t* __restrict__ block_cluster,
+                          const ClusterOut* __restrict__ cl, const uint32_t* __restrict__ block_sel,
+                          const uint32_t* __restrict__ cbsel, uint2* __restrict__ out, unsigned long long* __restrict__ sse) {
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nblocks) return;
   const ClusterOut& C = cl[block_cluster[b]];
   const uint32_t lin = cbsel[block_sel[b]];
-  uint32_t dxt = 0;
-  for (int p = 0; p < 16; p++) dxt |= (uint32_t)c_from_linear[(lin >> (2 * p)) & 3] << (2 * p);
+  uint32_t dxt = 0, rgb_sse = 0;
+  for (int p = 0; p < 16; p++) {
+    const uint32_t l = (lin >> (2 * p)) & 3;
+    dxt |= (uint32_t)c_from_linear[l] << (2 * p);
+    const uint32_t px = __ldg(blocks + (size_t)b * 16 + p);
+    rgb_sse += cdist(false, px_r(px), px_g(px), px_b(px), C.col[l][0], C.col[l][1], C.col[l][2]);
+  }
   out[b] = make_uint2(C.first | (C.second << 16), dxt);
+  atomicAdd(sse, (unsigned long long)rgb_sse);
 }
 
 // cluster membership: count tiles per cluster (CSR built on the host from the counts)
@@ -1261,7 +1520,7 @@ namespace {
 struct HcBuffers {
   DevBuf chunks, derating, lweight, st, tiles, block_tile, block_enc, vec6, w6, count, cb6, tile_cluster, ccount,
       cstart, clist, clusters, bweight, block_cluster, selvec, selw, cb16, cbsel, block_sel, entry_err, entry_used,
-      levels, flags, iota, used, keys, keys2, cub_tmp;
+      levels, flags, iota, used, keys, keys2, cub_tmp, sse;
 };
 
 }  // namespace
@@ -1355,8 +1614,9 @@ extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_
   k_tile_vectors<<<(nused + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused,
                                                       static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr));
   uint32_t K = 0;
+  const uint32_t frac = P.vq_round_fraction ? P.vq_round_fraction : kDefaultRoundFraction;
   int rc = tree_vq<6>(static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr), nused,
-                      std::min(nused, P.color_endpoint_codebook_size), B.cb6, &K, s);
+                      std::min(nused, P.color_endpoint_codebook_size), frac, B.cb6, &K, s);
   if (rc != CRNGPU_OK) return rc;
   if ((e = B.tile_cluster.ensure(4 * ntiles)) != cudaSuccess) return cuda_check(e, "alloc tile clusters");
   k_nearest_vec6<<<(ntiles + 255) / 256, 256, 0, s>>>(tiles, ntiles, static_cast<float*>(B.cb6.ptr), K,
@@ -1400,16 +1660,19 @@ extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_
   if ((e = B.bweight.ensure(4 * N)) != cudaSuccess || (e = B.block_cluster.ensure(4 * N)) != cudaSuccess ||
       (e = B.selvec.ensure(sizeof(float) * 16 * N)) != cudaSuccess || (e = B.selw.ensure(4 * N)) != cudaSuccess)
     return cuda_check(e, "alloc selectors");
+  if ((e = B.sse.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc sse");
+  cudaMemsetAsync(B.sse.ptr, 0, 16, s);
   k_block_weights<<<(N + 255) / 256, 256, 0, s>>>(static_cast<Level*>(B.levels.ptr), P.num_levels, N, static_cast<float*>(B.bweight.ptr));
   k_block_selectors<<<(N + 127) / 128, 128, 0, s>>>(blocks, N, static_cast<uint32_t*>(B.block_tile.ptr),
                                                      static_cast<uint32_t*>(B.tile_cluster.ptr),
                                                      static_cast<uint8_t*>(B.block_enc.ptr), static_cast<float*>(B.bweight.ptr),
                                                      cl, P.perceptual, static_cast<uint32_t*>(B.block_cluster.ptr),
-                                                     static_cast<float*>(B.selvec.ptr), static_cast<uint32_t*>(B.selw.ptr));
+                                                     static_cast<float*>(B.selvec.ptr), static_cast<uint32_t*>(B.selw.ptr),
+                                                     static_cast<unsigned long long*>(B.sse.ptr));
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_block_selectors");
   uint32_t KS = 0;
   rc = tree_vq<16>(static_cast<float*>(B.selvec.ptr), static_cast<uint32_t*>(B.selw.ptr), N,
-                   std::min(N, P.color_selector_codebook_size), B.cb16, &KS, s);
+                   std::min(N, P.color_selector_codebook_size), frac, B.cb16, &KS, s);
   if (rc != CRNGPU_OK) return rc;
   if ((e = B.cbsel.ensure(4 * KS)) != cudaSuccess || (e = B.block_sel.ensure(4 * N)) != cudaSuccess ||
       (e = B.entry_err.ensure(8 * 64 * (size_t)KS)) != cudaSuccess || (e = B.entry_used.ensure(4 * KS)) != cudaSuccess)
@@ -1423,8 +1686,9 @@ extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_
       static_cast<uint32_t*>(B.block_sel.ptr), static_cast<unsigned long long*>(B.entry_err.ptr),
       static_cast<uint32_t*>(B.entry_used.ptr));
   k_selector_finalise<<<(KS + 255) / 256, 256, 0, s>>>(static_cast<unsigned long long*>(B.entry_err.ptr), KS, cbsel);
-  k_hc_emit<<<(N + 255) / 256, 256, 0, s>>>(N, static_cast<uint32_t*>(B.block_cluster.ptr), cl,
-                                            static_cast<uint32_t*>(B.block_sel.ptr), cbsel, reinterpret_cast<uint2*>(d_out));
+  k_hc_emit<<<(N + 255) / 256, 256, 0, s>>>(blocks, N, static_cast<uint32_t*>(B.block_cluster.ptr), cl,
+                                            static_cast<uint32_t*>(B.block_sel.ptr), cbsel, reinterpret_cast<uint2*>(d_out),
+                                            static_cast<unsigned long long*>(B.sse.ptr) + 1);
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch hc selector kernels");
   // optional index outputs
   if (d_endpoint_idx || d_selector_idx || d_endpoints || d_selectors) {
@@ -1445,9 +1709,14 @@ extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_
     if (d_selectors) cudaMemcpyAsync(d_selectors, cbsel, 4 * KS, cudaMemcpyDeviceToDevice, s);
   }
   if (stats) {
+    unsigned long long sse[2] = {0, 0};
+    if ((e = cudaMemcpyAsync(sse, B.sse.ptr, 16, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read sse");
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
     stats->color_endpoints = K;
     stats->color_selectors = KS;
     stats->tiles = nused;
+    stats->sse_endpoints = (double)sse[0];
+    stats->sse_final = (double)sse[1];
   }
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   return CRNGPU_OK;

@@ -17,12 +17,14 @@ class HcParams(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("num_blocks", ctypes.c_uint32), ("num_levels", ctypes.c_uint32),
                 ("num_faces", ctypes.c_uint32), ("perceptual", ctypes.c_int32),
                 ("color_endpoint_codebook_size", ctypes.c_uint32), ("color_selector_codebook_size", ctypes.c_uint32),
-                ("adaptive_tile_color_psnr_derating", ctypes.c_float), ("levels", _Level * 16)]
+                ("adaptive_tile_color_psnr_derating", ctypes.c_float), ("vq_round_fraction", ctypes.c_uint32),
+                ("levels", _Level * 16)]
 
 
 class HcStats(ctypes.Structure):
     _fields_ = [("color_endpoints", ctypes.c_uint32), ("color_selectors", ctypes.c_uint32),
-                ("tiles", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("tiles", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("sse_endpoints", ctypes.c_double),
+                ("sse_final", ctypes.c_double)]
 
 
 def _bind():
@@ -70,14 +72,15 @@ def crn_layout(faces_levels):
     return np.ascontiguousarray(np.concatenate(parts)), levels, vis
 
 
-def compress_dxt1(faces_levels, quality: int = 128, perceptual: bool = True, stream=None, with_indices=False):
+def compress_dxt1(faces_levels, quality: int = 128, perceptual: bool = True, stream=None, with_indices=False,
+                  codebook=None, vq_round_fraction: int = 0):
     """Clustered DXT1 of a mip chain (faces_levels[face][level]): returns (per level, per face, the
     visible DXT1 blocks (by, bx, 8)), stats dict[, index arrays])."""
     import torch
     L = _bind()
     blocks, levels, vis = crn_layout(faces_levels)
     h0, w0 = faces_levels[0][0].shape[:2]
-    ce, cs, _, _ = codebook_sizes(w0, h0, quality)
+    ce, cs = codebook if codebook else codebook_sizes(w0, h0, quality)[:2]
     p = HcParams()
     p.struct_size = ctypes.sizeof(HcParams)
     p.num_blocks = blocks.shape[0]
@@ -87,6 +90,7 @@ def compress_dxt1(faces_levels, quality: int = 128, perceptual: bool = True, str
     p.color_endpoint_codebook_size = ce
     p.color_selector_codebook_size = cs
     p.adaptive_tile_color_psnr_derating = 2.0
+    p.vq_round_fraction = vq_round_fraction
     for i, (fb, nb, bw) in enumerate(levels):
         p.levels[i].first_block, p.levels[i].num_blocks, p.levels[i].block_width = fb, nb, bw
         p.levels[i].weight = min(12.0, 1.3 ** i)
@@ -115,7 +119,9 @@ def compress_dxt1(faces_levels, quality: int = 128, perceptual: bool = True, str
             faces.append(g[:by, :bx])
         res.append(faces)
     stats = {"color_endpoints": st.color_endpoints, "color_selectors": st.color_selectors, "tiles": st.tiles,
-             "codebook_request": (ce, cs), "blocks": n}
+             "codebook_request": (ce, cs), "blocks": n,
+             "rmse_endpoints_all_blocks": (st.sse_endpoints / (n * 48)) ** 0.5,
+             "rmse_final_all_blocks": (st.sse_final / (n * 48)) ** 0.5}
     if with_indices:
         return res, stats, {k: v.cpu().numpy() for k, v in idx.items()}
     return res, stats

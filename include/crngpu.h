@@ -123,6 +123,9 @@ typedef struct crngpu_hc_params {
     uint32_t color_endpoint_codebook_size;  /* m_color_endpoint_codebook_size */
     uint32_t color_selector_codebook_size;  /* m_color_selector_codebook_size */
     float adaptive_tile_color_psnr_derating; /* m_adaptive_tile_color_psnr_derating (2.0) */
+    uint32_t vq_round_fraction;             /* codebook tree: a round splits the top 1/this of the
+                                               leaves by variance (0 = 4; larger = closer to the
+                                               reference's one-at-a-time order, more rounds) */
     struct {
         uint32_t first_block, num_blocks, block_width;
         float weight;                       /* min(12, 1.3^level) in crn_comp */
@@ -134,6 +137,9 @@ typedef struct crngpu_hc_stats {
     uint32_t color_selectors;  /* selector codebook entries produced */
     uint32_t tiles;            /* tiles the adaptive tiling chose */
     uint32_t reserved;
+    double sse_endpoints;      /* RGB squared error over all blocks with the codebook endpoints and
+                                  each pixel's best selector (before the selector codebook) */
+    double sse_final;          /* RGB squared error of the output blocks */
 } crngpu_hc_stats;
 
 /* d_blocks: num_blocks x 64 bytes (device); d_out: num_blocks x 8 bytes of DXT1 (device).

@@ -37,6 +37,9 @@ def lib():
         L.ref_unpack_level.restype = _u32
         L.ref_time_unpack.argtypes = [ctypes.c_void_p, _u32, _u32, ctypes.c_void_p, _u32]
         L.ref_time_unpack.restype = ctypes.c_double
+        L.ref_dxt_hc_dxt1.argtypes = [ctypes.c_void_p, _u32, _u32, ctypes.c_void_p, _u32, _u32, _u32, ctypes.c_int,
+                                      _u32, ctypes.c_void_p, ctypes.c_void_p]
+        L.ref_dxt_hc_dxt1.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -80,3 +83,19 @@ def unpack_level(crn: bytes, level: int, out_size: int) -> np.ndarray:
     if n == 0:
         raise RuntimeError("reference crnd_unpack_level failed")
     return out[:n]
+
+
+def dxt_hc_dxt1(blocks: np.ndarray, levels, faces: int, endpoint_codebook: int, selector_codebook: int,
+                perceptual: bool = True, threads: int = 8):
+    """The reference's dxt_hc::compress for DXT1 on blocks in crn_comp's layout.
+    levels: (first_block, num_blocks, block_width) per level. Returns ((n, 8) DXT1 blocks,
+    {tiles, endpoints, selectors})."""
+    blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+    n = blocks.shape[0]
+    info = np.array([v for lv in levels for v in lv], np.uint32)
+    out = np.zeros(n * 8, np.uint8)
+    stats = np.zeros(4, np.uint32)
+    if not lib().ref_dxt_hc_dxt1(blocks.ctypes.data, n, len(levels), info.ctypes.data, faces, endpoint_codebook,
+                                 selector_codebook, int(perceptual), threads, out.ctypes.data, stats.ctypes.data):
+        raise RuntimeError("reference dxt_hc failed")
+    return out.reshape(n, 8), {"tiles": int(stats[0]), "endpoints": int(stats[1]), "selectors": int(stats[2])}

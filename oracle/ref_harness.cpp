@@ -11,6 +11,7 @@
 //   crn_compress (comp params + mip params)   inc/crnlib.h:614, crnlib/crnlib.cpp:242-267
 //   crnd_unpack_begin / crnd_unpack_level / crnd_unpack_end   inc/crn_defs.h:174-205
 //   crnd_get_texture_info / crnd_get_level_info              inc/crn_defs.h:152-160
+//   crnlib::dxt_hc::compress (clustered DXT1)                 crnlib/crn_dxt_hc.cpp:97-316
 #include <cstdint>
 #include <cstring>
 #include <cstdlib>
@@ -21,6 +22,9 @@
 
 #include "crnlib.h"
 #include "crn_defs.h"
+#include "crn_dxt_hc.h"
+#include "crn_dxt_fast.h"
+#include "crn_threading.h"
 
 namespace {
 
@@ -164,6 +168,72 @@ double ref_time_unpack(const uint8_t* crn, uint32_t crn_size, uint32_t reps, uin
   }
   auto t1 = std::chrono::steady_clock::now();
   return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// The reference's clustered DXT1 compressor (crnlib::dxt_hc::compress, crnlib/crn_dxt_hc.cpp:97-316)
+// run directly on blocks in crn_comp's layout (crnlib/crn_comp.cpp:717-741), with crn_comp's level
+// weights. level_info: first_block, num_blocks, block_width per level. Writes the DXT1 blocks the
+// returned codebooks and indices describe (endpoints as stored, linear selectors converted to DXT
+// order) to out (n x 8) and stats[0..2] = tiles, endpoint entries, selector entries. Returns 1.
+int ref_dxt_hc_dxt1(const uint8_t* rgba_blocks, uint32_t n, uint32_t nlevels, const uint32_t* level_info,
+                    uint32_t faces, uint32_t endpoint_codebook, uint32_t selector_codebook, int perceptual,
+                    uint32_t threads, uint8_t* out, uint32_t* stats) {
+  crnlib::task_pool pool;
+  if (!pool.init(threads > 1 ? threads - 1 : 0)) return 0;
+  crnlib::dxt_hc::params p;
+  p.m_num_blocks = n;
+  p.m_num_levels = nlevels;
+  p.m_num_faces = faces;
+  p.m_format = crnlib::cDXT1;
+  p.m_perceptual = perceptual != 0;
+  p.m_hierarchical = true;
+  p.m_color_endpoint_codebook_size = endpoint_codebook;
+  p.m_color_selector_codebook_size = selector_codebook;
+  p.m_pTask_pool = &pool;
+  for (uint32_t l = 0; l < nlevels; l++) {
+    p.m_levels[l].m_first_block = level_info[3 * l];
+    p.m_levels[l].m_num_blocks = level_info[3 * l + 1];
+    p.m_levels[l].m_block_width = level_info[3 * l + 2];
+    p.m_levels[l].m_weight = crnlib::math::minimum(12.0f, powf(1.3f, (float)l));
+  }
+  std::vector<uint8_t> copy(rgba_blocks, rgba_blocks + (size_t)n * 64);
+  crnlib::vector<crnlib::dxt_hc::endpoint_indices_details> ei;
+  crnlib::vector<crnlib::dxt_hc::selector_indices_details> si;
+  crnlib::vector<crnlib::uint32> ce, ae, cs;
+  crnlib::vector<crnlib::uint64> as;
+  crnlib::dxt_hc hc;
+  if (!hc.compress(reinterpret_cast<crnlib::color_quad_u8(*)[16]>(copy.data()), ei, si, ce, ae, cs, as, p)) return 0;
+  static const uint8_t from_linear[4] = {0, 2, 3, 1};
+  for (uint32_t b = 0; b < n; b++) {
+    const uint32_t ep = ce[ei[b].color], lin = cs[si[b].color];
+    uint32_t dxt = 0;
+    for (int q = 0; q < 16; q++) dxt |= (uint32_t)from_linear[(lin >> (2 * q)) & 3] << (2 * q);
+    memcpy(out + (size_t)b * 8, &ep, 4);
+    memcpy(out + (size_t)b * 8 + 4, &dxt, 4);
+  }
+  stats[0] = hc.m_num_tiles;
+  stats[1] = ce.size();
+  stats[2] = cs.size();
+  pool.deinit();
+  return 1;
+}
+
+// Squared RGB error of dxt_fast::compress_color_block on n pixels (n = 16, 32 or 64), measured
+// against the 4-colour palette as dxt_hc::determine_tiles_task does (crnlib/crn_dxt_hc.cpp:459-472).
+uint32_t ref_dxt_fast_tile_error(const uint8_t* rgba, uint32_t n) {
+  uint8_t sel[64];
+  crnlib::uint low16, high16;
+  const crnlib::color_quad_u8* px = reinterpret_cast<const crnlib::color_quad_u8*>(rgba);
+  crnlib::dxt_fast::compress_color_block(n, px, low16, high16, sel);
+  crnlib::color_quad_u8 colors[4];
+  crnlib::dxt1_block::get_block_colors4(colors, (crnlib::uint16)low16, (crnlib::uint16)high16);
+  uint32_t err = 0;
+  for (uint32_t p = 0; p < n; p++)
+    for (int c = 0; c < 3; c++) {
+      const uint32_t d = px[p][c] - colors[sel[p]][c];
+      err += d * d;
+    }
+  return err;
 }
 
 }  // extern "C"

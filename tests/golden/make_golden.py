@@ -142,9 +142,36 @@ def make_crn() -> None:
         json.dump(manifest, fh, indent=1, sort_keys=True)
 
 
+HC_CASES = [("dxt1_256", 256, 10), ("c1_dxt1_1024", 1024, 100), ("hc_128", 128, 21)]
+
+
+def make_hc() -> None:
+    """The reference's clustered DXT1 compressor (crnlib::dxt_hc::compress, run directly on blocks in
+    crn_comp's layout at q128 codebook sizes): its tile count, codebook sizes and RGB RMSE, the
+    quality bar of the GPU clustered path."""
+    from crunch2_gb300 import hc
+    from crunch2_gb300.hc import crn_layout
+    sys.path.insert(0, os.path.dirname(HERE))
+    from dxt_decode import rgb_rmse
+    out = {}
+    for name, size, seed in HC_CASES:
+        levels = texgen.mip_chain(texgen.colour_texture(size, size, seed))
+        blocks, lv, vis = crn_layout([levels])
+        ce, cs = hc.codebook_sizes(size, size, 128)[:2]
+        dxt, st = ref.dxt_hc_dxt1(blocks, lv, 1, ce, cs, True, threads=8)
+        rows = [dxt[fb:fb + nb].reshape(-1, bw, 8)[:by, :bx].reshape(-1, 8) for (fb, nb, bw), (bx, by, _) in zip(lv, vis)]
+        src = np.concatenate([texgen.image_blocks(im) for im in levels])
+        out[name] = {"size": size, "seed": seed, "quality": 128, "codebook_request": [ce, cs], "tiles": st["tiles"],
+                     "endpoints": st["endpoints"], "selectors": st["selectors"],
+                     "rmse_visible": rgb_rmse(np.concatenate(rows), src), "rmse_all_blocks": rgb_rmse(dxt, blocks)}
+    with open(os.path.join(HERE, "hc_reference.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
 if __name__ == "__main__":
     if not ref.available():
         sys.exit("oracle/_ref/libcrnref.so missing: run `make -C oracle ref` where the reference tree exists")
     make_blocks()
     make_crn()
+    make_hc()
     print("golden fixtures written to", HERE)
