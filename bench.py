@@ -7,6 +7,8 @@ One JSON line on stdout (rank 0):
   learned    the learned-proposal encode of the same blocks (shipped weights): Mtexel/s, RGB
              RMSE beside the plain encode's, fallback fraction
   e2e        the same encode through the C ABI with pinned host buffers (H2D + encode + D2H)
+  clustered  clustered (CRN-style, quality 128) DXT1 of the same mip chain on the GPU: Mtexel/s
+             and RGB RMSE beside the reference dxt_hc's RMSE on the same blocks
   transcode  CRN -> DXT1 transcode GB/s: a batch of 1024 textures (each with its own context holding
              the reference-encoded .crn of the same texture, q128) in one persistent decode launch
              and one expansion launch (CUDA graph); the expansion kernel's HBM roofline; the
@@ -355,6 +357,7 @@ def main():
     for _ in range(args.warmup):
         batch.launch(use_graph=True, stream=stream)
     batch.status(stream=stream)
+    tune_variant, tune_ms = batch.tuning()
     tx_parity = bool((outs[-1].cpu().numpy() == ctx0.unpack_levels()).all())
     batch_ms = timed(lambda: batch.launch(use_graph=True, stream=stream), args.steps)
     batch.status(stream=stream)
@@ -392,10 +395,36 @@ def main():
                                     "note": "one texture = 11 level streams on 11 lanes of one warp; the 1024x1024 "
                                             "level is one serial prefix-code chain, so this is its latency"},
                  "expand_roofline": None,
+                 "expand_autotune": {"variant": tune_variant, "ms_per_variant": tune_ms,
+                                     "variants": "tile of 1024 << (v >> 1) blocks; DXT1 palettes staged in "
+                                                 "shared memory when v is odd"},
                  "workload": f"{TX_BATCH} contexts of the 1024x1024 q128 DXT1 .crn (11 levels, {len(crn)} bytes)"}
     expand = {"kernel": "k_crn_expand_tiles", "bound": "hbm", "unit": "GB/s",
               "ms": round(expand_ms, 4), "bytes_algorithmic": exp_bytes,
               "achieved": round(exp_bytes / (expand_ms / 1e3) / 1e9, 1)}
+
+    # ---- clustered (CRN-style) DXT1 of the same mip chain at quality 128: dxt_hc on the GPU,
+    # quality against the reference's own dxt_hc on the same blocks (committed fixture)
+    from crunch2_gb300 import hc as HC
+    from crunch2_gb300.texgen import image_blocks
+    HC.compress_dxt1([levels], quality=128)  # warm-up (allocations, tables)
+    hc_times = []
+    for _ in range(max(1, min(args.steps, 5))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hc_out, hc_stats = HC.compress_dxt1([levels], quality=128)
+        hc_times.append(time.perf_counter() - t0)
+    hc_s = statistics.median(hc_times)
+    dec = np.concatenate([hc_out[l][0].reshape(-1, 8) for l in range(len(levels))])
+    with open(os.path.join(ROOT, "tests", "golden", "hc_reference.json")) as fh:
+        hc_ref = json.load(fh)["c1_dxt1_1024"]
+    hc_rmse = LR.rgb_rmse_torch(torch.from_numpy(dec).to(dev), torch.from_numpy(blocks).to(dev))
+    clustered = {"value": round(texels / hc_s / 1e6, 3), "unit": "Mtexel/s", "s_per_texture": round(hc_s, 4),
+                 "quality": 128, "rmse": round(hc_rmse, 4), "rmse_reference_dxt_hc": round(hc_ref["rmse_visible"], 4),
+                 "codebooks": [hc_stats["color_endpoints"], hc_stats["color_selectors"]],
+                 "tiles": hc_stats["tiles"], "tiles_reference": hc_ref["tiles"],
+                 "path": "crngpu_hc_compress_dxt1 from host RGBA8 (H2D of the blocks, every stage on the GPU, "
+                         "D2H of the DXT1 blocks), wall time of the call"}
 
     peaks, peak_kind = measured_peaks()
     clk = clocks.summary()
@@ -431,7 +460,8 @@ def main():
                 "parity_vs_oracle_sample": parity, "e2e_parity": e2e_parity,
                 "e2e": {"value": round(e2e_value, 3), "unit": "Mtexel/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "path": "crngpu_compress_image per level, pinned host buffers"},
-                "learned": learned, "transcode": transcode, "roofline": roofline, "cpu_baseline": cpu,
+                "learned": learned, "transcode": transcode, "clustered": clustered, "roofline": roofline,
+                "cpu_baseline": cpu,
                 "gpu_launches": args.steps * 1, "clocks": clk, "wall_s_timed": round(wall, 4)}
         print(json.dumps(line))
 

@@ -94,10 +94,14 @@ def lib():
     L.crngpu_unpack_batch_status.restype = i32
     L.crngpu_unpack_batch_bytes.argtypes = [vp]
     L.crngpu_unpack_batch_bytes.restype = i64
+    L.crngpu_unpack_batch_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float), u32]
+    L.crngpu_unpack_batch_tuning.restype = i32
     L.crngpu_unpack_batch_destroy.argtypes = [vp]
     L.crngpu_unpack_batch_destroy.restype = i32
     L.crngpu_crn_decompress.argtypes = [vp, ctypes.c_uint, vp, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint]
     L.crngpu_crn_decompress.restype = None
+    L.crngpu_crn_pack.argtypes = [vp, u32, u32, u32, u32, u32, vp, u64]
+    L.crngpu_crn_pack.restype = i64
     L.crngpu_profile_counters.argtypes = [i32, ctypes.POINTER(ctypes.c_uint64), vp]
     L.crngpu_profile_counters.restype = i32
     _lib = L
@@ -296,6 +300,13 @@ class UnpackBatch:
     def status(self, stream=None):
         _check(lib().crngpu_unpack_batch_status(self.handle, _stream_ptr(stream)), "crngpu_unpack_batch_status")
 
+    def tuning(self):
+        """(chosen expansion variant, measured ms per variant) of the autotuner (first launch)."""
+        v = ctypes.c_int32(-1)
+        ms = (ctypes.c_float * 16)()
+        n = lib().crngpu_unpack_batch_tuning(self.handle, ctypes.byref(v), ms, 16)
+        return int(v.value), [round(float(ms[i]), 4) for i in range(max(n, 0))]
+
     def close(self):
         if self.handle:
             lib().crngpu_unpack_batch_destroy(self.handle)
@@ -324,3 +335,27 @@ def crn_decompress(src: bytes, first_level: int, level_count: int, dst_size: int
     out = np.zeros(dst_size, np.uint8)
     lib().crngpu_crn_decompress(s.ctypes.data, len(src), out.ctypes.data, dst_size, first_level, level_count)
     return out
+
+
+def crn_pack(blocks, width: int, height: int, levels: int, faces: int, fmt: int) -> bytes:
+    """DXTn blocks in crn_comp's layout (numpy, host) -> .crn bytes (crngpu_crn_pack)."""
+    b = np.ascontiguousarray(blocks, dtype=np.uint8)
+    size = _check(int(lib().crngpu_crn_pack(b.ctypes.data, width, height, levels, faces, fmt, None, 0)),
+                  "crngpu_crn_pack")
+    out = np.zeros(size, np.uint8)
+    _check(int(lib().crngpu_crn_pack(b.ctypes.data, width, height, levels, faces, fmt, out.ctypes.data, size)),
+           "crngpu_crn_pack")
+    return out.tobytes()
+
+
+def crn_layout_from_levels(level_blocks, width: int, height: int, faces: int, bpb: int):
+    """Visible blocks per level ([level][face] -> (by, bx, bpb)) -> crn_comp's padded layout, the
+    blocks outside the image filled with the nearest edge block."""
+    parts = []
+    for l, fl in enumerate(level_blocks):
+        w, h = max(1, width >> l), max(1, height >> l)
+        W, H = ((w + 7) & ~7) >> 2, ((h + 7) & ~7) >> 2
+        for f in range(faces):
+            v = np.asarray(fl[f]).reshape((h + 3) // 4, (w + 3) // 4, bpb)
+            parts.append(np.pad(v, ((0, H - v.shape[0]), (0, W - v.shape[1]), (0, 0)), mode="edge").reshape(-1, bpb))
+    return np.concatenate(parts)

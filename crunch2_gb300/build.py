@@ -23,6 +23,7 @@ NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompi
 
 UNITS = [
     ("crn_file.cpp", []),
+    ("crn_pack.cpp", []),
     ("capi.cpp", []),
     ("crn_transcode.cu", []),
     ("encode_api.cu", []),

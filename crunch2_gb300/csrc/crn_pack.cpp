@@ -1,0 +1,470 @@
+// .crn writer: the serial tail of crn_comp (crnlib/crn_comp.cpp:295-422, 1356-1611) after the
+// clustered encode. It packs DXTn blocks in crn_comp's block layout into a .crn file that
+// crnd::crn_unpacker (inc/crn_decomp.h) and this library's transcoder decode back to exactly
+// those blocks:
+//   * palettes = the distinct endpoint pairs and selector words of the blocks (at most 8192 of
+//     each, the decoder's limit), in first-use order, delta coded as crn_comp::pack_color_endpoints /
+//     pack_color_selectors / pack_alpha_endpoints / pack_alpha_selectors do;
+//   * per level, the block stream of crn_comp::pack_blocks: one reference group per 2x2 blocks
+//     (left / top endpoint reuse), endpoint index deltas modulo the palette size, selector
+//     indices;
+//   * static canonical Huffman models (code lengths limited to 16 bits), transmitted with the
+//     21-symbol code-length code of symbol_codec (run-length codes 17-20);
+//   * the header (inc/crn_defs.h:286-339) with its two CRC16s.
+// The reference additionally reorders its palettes to shrink the deltas (crn_comp::optimize_color
+// / optimize_alpha); this writer keeps first-use order, which changes the file size, not the
+// decoded blocks.
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <queue>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "crn_file.h"
+#include "crngpu_internal.h"
+
+namespace crngpu {
+namespace {
+
+class BitWriter {
+ public:
+  void put(uint32_t v, uint32_t bits) {
+    for (int i = (int)bits - 1; i >= 0; i--) {
+      acc_ = (acc_ << 1) | ((v >> i) & 1u);
+      if (++n_ == 8) { out_.push_back((uint8_t)acc_); acc_ = 0; n_ = 0; }
+    }
+  }
+  std::vector<uint8_t> finish() {
+    if (n_) { out_.push_back((uint8_t)(acc_ << (8 - n_))); acc_ = 0; n_ = 0; }
+    return std::move(out_);
+  }
+
+ private:
+  std::vector<uint8_t> out_;
+  uint32_t acc_ = 0;
+  int n_ = 0;
+};
+
+// Huffman code lengths for a histogram, limited to `limit` bits (frequencies are halved until the
+// tree fits). Unused symbols get 0; a single used symbol gets length 1.
+std::vector<uint8_t> code_lengths(const std::vector<uint32_t>& freq_in, int limit) {
+  const size_t n = freq_in.size();
+  std::vector<uint8_t> len(n, 0);
+  std::vector<uint64_t> freq(freq_in.begin(), freq_in.end());
+  size_t used = 0, last = 0;
+  for (size_t i = 0; i < n; i++)
+    if (freq[i]) { used++; last = i; }
+  if (!used) return len;
+  if (used == 1) { len[last] = 1; return len; }
+  for (;;) {
+    // nodes: leaves 0..n-1, internal n..; (weight, id) min-heap with id tie-break for determinism
+    std::vector<int> parent(2 * n, -1);
+    using Item = std::pair<uint64_t, int>;
+    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> q;
+    for (size_t i = 0; i < n; i++)
+      if (freq[i]) q.push({freq[i], (int)i});
+    int next = (int)n;
+    while (q.size() > 1) {
+      const Item a = q.top(); q.pop();
+      const Item b = q.top(); q.pop();
+      parent[a.second] = next;
+      parent[b.second] = next;
+      q.push({a.first + b.first, next++});
+    }
+    int maxl = 0;
+    for (size_t i = 0; i < n; i++) {
+      if (!freq[i]) continue;
+      int d = 0;
+      for (int p = (int)i; parent[p] >= 0; p = parent[p]) d++;
+      len[i] = (uint8_t)d;
+      maxl = std::max(maxl, d);
+    }
+    if (maxl <= limit) return len;
+    for (auto& f : freq)
+      if (f) f = (f + 1) >> 1;
+  }
+}
+
+// Canonical codes (the decoder's convention, inc/crn_decomp.h:2150-2326): symbols ordered by
+// (length, index), consecutive codes within a length.
+std::vector<uint32_t> canonical_codes(const std::vector<uint8_t>& len) {
+  uint32_t count[17] = {}, next_code[17] = {};
+  for (uint8_t l : len)
+    if (l) count[l]++;
+  uint32_t code = 0;
+  for (int l = 1; l <= 16; l++) {
+    next_code[l] = code;
+    code = (code + count[l]) << 1;
+  }
+  std::vector<uint32_t> codes(len.size(), 0);
+  for (size_t s = 0; s < len.size(); s++)
+    if (len[s]) codes[s] = next_code[len[s]]++;
+  return codes;
+}
+
+struct Huff {
+  std::vector<uint8_t> len;
+  std::vector<uint32_t> code;
+  void build(const std::vector<uint32_t>& freq, int limit) {
+    len = code_lengths(freq, limit);
+    code = canonical_codes(len);
+  }
+  void put(BitWriter& bw, uint32_t sym) const { bw.put(code[sym], len[sym]); }
+};
+
+// symbol_codec's static model transmission, the inverse of
+// decode_receive_static_data_model (inc/crn_decomp.h:3044-3123): 14-bit symbol count, the 21
+// code-length-code lengths in transmission order (3 bits each), then the code lengths coded with
+// literals 0-16, zero runs (17: 3-10, 18: 11-138) and repeats of the previous length (19: 3-6,
+// 20: 7-70).
+void send_model(BitWriter& bw, const Huff& h) {
+  static const uint8_t kOrder[21] = {17, 18, 19, 20, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15, 16};
+  const std::vector<uint8_t>& len = h.len;
+  const uint32_t total = (uint32_t)len.size();
+  bw.put(total, 14);
+  if (!total) return;
+  struct Sym { uint8_t s; uint32_t extra; int bits; };
+  std::vector<Sym> syms;
+  for (uint32_t i = 0; i < total;) {
+    const uint8_t l = len[i];
+    if (!l) {
+      uint32_t r = 1;
+      while (i + r < total && !len[i + r] && r < 138) r++;
+      if (r >= 11) syms.push_back({18, r - 11, 7});
+      else if (r >= 3) syms.push_back({17, r - 3, 3});
+      else for (uint32_t k = 0; k < r; k++) syms.push_back({0, 0, 0});
+      i += r;
+    } else {
+      syms.push_back({l, 0, 0});
+      i++;
+      uint32_t r = 0;
+      while (i + r < total && len[i + r] == l && r < 70) r++;
+      if (r >= 7) { syms.push_back({20, r - 7, 6}); i += r; }
+      else if (r >= 3) { syms.push_back({19, r - 3, 2}); i += r; }
+    }
+  }
+  std::vector<uint32_t> cf(21, 0);
+  for (const Sym& s : syms) cf[s.s]++;
+  Huff cl;
+  cl.build(cf, 7);
+  int ncl = 21;
+  while (ncl > 1 && !cl.len[kOrder[ncl - 1]]) ncl--;
+  bw.put((uint32_t)ncl, 5);
+  for (int i = 0; i < ncl; i++) bw.put(cl.len[kOrder[i]], 3);
+  for (const Sym& s : syms) {
+    cl.put(bw, s.s);
+    if (s.bits) bw.put(s.extra, (uint32_t)s.bits);
+  }
+}
+
+// histogram with at least one used symbol (a model the format requires must not be empty)
+void ensure_used(std::vector<uint32_t>& f) {
+  for (uint32_t v : f)
+    if (v) return;
+  if (!f.empty()) f[0] = 1;
+}
+
+void put_be(std::vector<uint8_t>& d, size_t at, uint32_t v, int bytes) {
+  for (int i = bytes - 1; i >= 0; i--) d[at + (size_t)(bytes - 1 - i)] = (uint8_t)(v >> (8 * i));
+}
+
+struct Palette {
+  std::vector<uint64_t> values;               // distinct values in first-use order
+  std::unordered_map<uint64_t, uint32_t> index;
+  uint32_t add(uint64_t v) {
+    auto it = index.find(v);
+    if (it != index.end()) return it->second;
+    const uint32_t i = (uint32_t)values.size();
+    index.emplace(v, i);
+    values.push_back(v);
+    return i;
+  }
+};
+
+// DXT order -> linear order selectors (g_dxt1_to_linear, g_dxt5_to_linear, crnlib/crn_dxt.cpp:35-39)
+uint32_t dxt1_sel_to_linear(uint32_t dxt) {
+  static const uint8_t t[4] = {0, 3, 1, 2};
+  uint32_t lin = 0;
+  for (int p = 0; p < 16; p++) lin |= (uint32_t)t[(dxt >> (2 * p)) & 3] << (2 * p);
+  return lin;
+}
+uint64_t dxt5_sel_to_linear(uint64_t dxt) {
+  static const uint8_t t[8] = {0, 7, 1, 2, 3, 4, 5, 6};
+  uint64_t lin = 0;
+  for (int p = 0; p < 16; p++) lin |= (uint64_t)t[(dxt >> (3 * p)) & 7] << (3 * p);
+  return lin;
+}
+
+}  // namespace
+}  // namespace crngpu
+
+using namespace crngpu;
+
+extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32_t height, uint32_t levels,
+                                   uint32_t faces, uint32_t format, void* out, uint64_t out_capacity) {
+  clear_error();
+  if (!blocks || !width || !height || width > 4096 || height > 4096 || !levels || levels > 16 ||
+      (faces != 1 && faces != 6)) {
+    set_error("crngpu_crn_pack: bad dimensions, level or face count");
+    return CRNGPU_E_PARAM;
+  }
+  int nalpha;
+  bool colour;
+  uint32_t bpb;
+  switch (format) {
+    case CRNGPU_FMT_DXT1: colour = true; nalpha = 0; bpb = 8; break;
+    case CRNGPU_FMT_DXT5: case CRNGPU_FMT_DXT5_CCXY: case CRNGPU_FMT_DXT5_XGXR: case CRNGPU_FMT_DXT5_XGBR:
+    case CRNGPU_FMT_DXT5_AGBR: colour = true; nalpha = 1; bpb = 16; break;
+    case CRNGPU_FMT_DXN_XY: case CRNGPU_FMT_DXN_YX: colour = false; nalpha = 2; bpb = 16; break;
+    case CRNGPU_FMT_DXT5A: colour = false; nalpha = 1; bpb = 8; break;
+    default: set_error("crngpu_crn_pack: unsupported format"); return CRNGPU_E_UNSUPPORTED;
+  }
+  if (levels > 1) {
+    uint32_t full = 1;
+    while ((width >> full) || (height >> full)) full++;
+    if (levels > full) { set_error("crngpu_crn_pack: more levels than the mip chain has"); return CRNGPU_E_PARAM; }
+  }
+  // level geometry (crn_comp::alias_images, crnlib/crn_comp.cpp:454-463)
+  struct Lv { uint32_t W, H, first; };
+  std::vector<Lv> lv(levels);
+  uint64_t nblocks = 0;
+  for (uint32_t l = 0; l < levels; l++) {
+    const uint32_t w = std::max(1u, width >> l), h = std::max(1u, height >> l);
+    lv[l] = Lv{((w + 7) & ~7u) >> 2, ((h + 7) & ~7u) >> 2, (uint32_t)nblocks};
+    nblocks += (uint64_t)lv[l].W * lv[l].H * faces;
+  }
+  // per block: endpoint / selector palette indices of each component (colour, alpha0, alpha1)
+  Palette cep, csel, aep, asel;
+  const int ncomp = (colour ? 1 : 0) + nalpha;
+  std::vector<uint32_t> eidx((size_t)nblocks * ncomp), sidx((size_t)nblocks * ncomp);
+  for (uint64_t b = 0; b < nblocks; b++) {
+    const uint8_t* blk = blocks + b * bpb;
+    int c = 0;
+    if (colour) {
+      const uint8_t* cb = blk + (bpb == 16 ? 8 : 0);
+      uint32_t ep, sel;
+      std::memcpy(&ep, cb, 4);
+      std::memcpy(&sel, cb + 4, 4);
+      eidx[b * ncomp + c] = cep.add(ep);
+      sidx[b * ncomp + c] = csel.add(dxt1_sel_to_linear(sel));
+      c++;
+    }
+    for (int a = 0; a < nalpha; a++, c++) {
+      const uint8_t* ab = blk + 8 * a;
+      uint64_t sel = 0;
+      for (int k = 0; k < 6; k++) sel |= (uint64_t)ab[2 + k] << (8 * k);
+      eidx[b * ncomp + c] = aep.add((uint64_t)ab[0] | ((uint64_t)ab[1] << 8));
+      sidx[b * ncomp + c] = asel.add(dxt5_sel_to_linear(sel));
+    }
+  }
+  if (cep.values.size() > (size_t)kMaxSyms || csel.values.size() > (size_t)kMaxSyms ||
+      aep.values.size() > (size_t)kMaxSyms || asel.values.size() > (size_t)kMaxSyms) {
+    set_error("crngpu_crn_pack: more than 8192 distinct endpoints or selectors (cluster the blocks first)");
+    return CRNGPU_E_PARAM;
+  }
+  // reference groups and symbol streams (crn_comp::pack_blocks, crnlib/crn_comp.cpp:295-422): the
+  // histograms first, then the coded streams
+  std::vector<uint32_t> h_ref(256, 0), h_ep[2], h_sel[2];
+  if (colour) { h_ep[0].assign(cep.values.size(), 0); h_sel[0].assign(csel.values.size(), 0); }
+  if (nalpha) { h_ep[1].assign(aep.values.size(), 0); h_sel[1].assign(asel.values.size(), 0); }
+  // references of every block: 0 new (delta), 1 same as the previous block in decode order, 2 same
+  // as the block above (the faces of a level are one tall image to the decoder's row buffer)
+  auto refs_of = [&](const Lv& L, uint32_t f, uint32_t y, uint32_t x) -> uint32_t {
+    const uint64_t b = L.first + ((uint64_t)f * L.H + y) * L.W + x;
+    const uint32_t row = f * L.H + y;
+    bool left = row || x, top = row != 0;
+    for (int c = 0; c < ncomp; c++) {
+      const uint32_t e = eidx[b * ncomp + c];
+      if (left) left = e == eidx[(b - 1) * ncomp + c];
+      if (top) top = e == eidx[(b - L.W) * ncomp + c];
+    }
+    return left ? 1u : top ? 2u : 0u;
+  };
+  Huff m_ref, m_ep[2], m_sel[2];
+  std::vector<std::vector<uint8_t>> level_data(levels);
+  for (int pass = 0; pass < 2; pass++) {
+    if (pass == 1) {
+      ensure_used(h_ref);
+      m_ref.build(h_ref, 16);
+      for (int m = 0; m < 2; m++) {
+        if (h_ep[m].empty()) continue;
+        ensure_used(h_ep[m]);
+        ensure_used(h_sel[m]);
+        m_ep[m].build(h_ep[m], 16);
+        m_sel[m].build(h_sel[m], 16);
+      }
+    }
+    for (uint32_t l = 0; l < levels; l++) {
+      const Lv& L = lv[l];
+      BitWriter bw;
+      uint32_t prev[3] = {0, 0, 0};
+      for (uint32_t f = 0; f < faces; f++)
+        for (uint32_t y = 0; y < L.H; y++)
+          for (uint32_t x = 0; x < L.W; x++) {
+            if (!(y & 1) && !(x & 1)) {
+              const uint32_t g = refs_of(L, f, y, x) | (refs_of(L, f, y + 1, x) << 2) | (refs_of(L, f, y, x + 1) << 4) |
+                                 (refs_of(L, f, y + 1, x + 1) << 6);
+              if (pass) m_ref.put(bw, g); else h_ref[g]++;
+            }
+            const uint32_t ref = refs_of(L, f, y, x);
+            const uint64_t b = L.first + ((uint64_t)f * L.H + y) * L.W + x;
+            for (int c = 0; c < ncomp; c++) {
+              const int m = (colour && c == 0) ? 0 : 1;
+              const uint32_t e = eidx[b * ncomp + c];
+              if (ref == 0) {
+                const uint32_t n = (uint32_t)(m ? aep.values.size() : cep.values.size());
+                const uint32_t d = (e + n - prev[c]) % n;
+                if (pass) m_ep[m].put(bw, d); else h_ep[m][d]++;
+              }
+              prev[c] = e;
+            }
+            for (int c = 0; c < ncomp; c++) {
+              const int m = (colour && c == 0) ? 0 : 1;
+              const uint32_t s = sidx[b * ncomp + c];
+              if (pass) m_sel[m].put(bw, s); else h_sel[m][s]++;
+            }
+          }
+      if (pass) level_data[l] = bw.finish();
+    }
+  }
+  // palettes (crn_comp::pack_color_endpoints etc.; the inverse of crn_unpacker::decode_palettes,
+  // inc/crn_decomp.h:3715-3851)
+  std::vector<uint8_t> pal[4];
+  if (colour) {
+    // endpoints: six running component deltas, 5-bit model for red/blue, 6-bit for green
+    std::vector<uint32_t> f5(32, 0), f6(64, 0);
+    auto comps = [](uint32_t v, uint32_t* c) {
+      c[0] = (v >> 11) & 31; c[1] = (v >> 5) & 63; c[2] = v & 31;
+      c[3] = (v >> 27) & 31; c[4] = (v >> 21) & 63; c[5] = (v >> 16) & 31;
+    };
+    static const uint32_t kMask[6] = {31, 63, 31, 31, 63, 31};
+    static const int kModel[6] = {0, 1, 0, 0, 1, 0};
+    for (int pass = 0; pass < 2; pass++) {
+      Huff h5, h6;
+      BitWriter bw;
+      if (pass) {
+        ensure_used(f5); ensure_used(f6);
+        h5.build(f5, 16); h6.build(f6, 16);
+        send_model(bw, h5);
+        send_model(bw, h6);
+      }
+      uint32_t prev[6] = {0, 0, 0, 0, 0, 0};
+      for (uint64_t v : cep.values) {
+        uint32_t c[6];
+        comps((uint32_t)v, c);
+        for (int k = 0; k < 6; k++) {
+          const uint32_t d = (c[k] - prev[k]) & kMask[k];
+          prev[k] = c[k];
+          if (pass) (kModel[k] ? h6 : h5).put(bw, d);
+          else (kModel[k] ? f6 : f5)[d]++;
+        }
+      }
+      if (pass) pal[0] = bw.finish();
+    }
+    // selectors: XOR deltas of the linear words, 4 bits at a time
+    std::vector<uint32_t> fs(16, 0);
+    for (int pass = 0; pass < 2; pass++) {
+      Huff hs;
+      BitWriter bw;
+      if (pass) { ensure_used(fs); hs.build(fs, 16); send_model(bw, hs); }
+      uint32_t prev = 0;
+      for (uint64_t v : csel.values) {
+        const uint32_t d = (uint32_t)v ^ prev;
+        prev = (uint32_t)v;
+        for (int j = 0; j < 32; j += 4) {
+          const uint32_t x = (d >> j) & 15u;
+          if (pass) hs.put(bw, x); else fs[x]++;
+        }
+      }
+      if (pass) pal[1] = bw.finish();
+    }
+  }
+  if (nalpha) {
+    // endpoints: two running 8-bit deltas
+    std::vector<uint32_t> fa(256, 0);
+    for (int pass = 0; pass < 2; pass++) {
+      Huff ha;
+      BitWriter bw;
+      if (pass) { ensure_used(fa); ha.build(fa, 16); send_model(bw, ha); }
+      uint32_t pa = 0, pb = 0;
+      for (uint64_t v : aep.values) {
+        const uint32_t a = (uint32_t)v & 255u, b = (uint32_t)(v >> 8) & 255u;
+        const uint32_t d0 = (a - pa) & 255u, d1 = (b - pb) & 255u;
+        pa = a; pb = b;
+        if (pass) { ha.put(bw, d0); ha.put(bw, d1); } else { fa[d0]++; fa[d1]++; }
+      }
+      if (pass) pal[2] = bw.finish();
+    }
+    // selectors: XOR deltas of the two 24-bit linear halves, 6 bits at a time
+    std::vector<uint32_t> fs(64, 0);
+    for (int pass = 0; pass < 2; pass++) {
+      Huff hs;
+      BitWriter bw;
+      if (pass) { ensure_used(fs); hs.build(fs, 16); send_model(bw, hs); }
+      uint32_t prev[2] = {0, 0};
+      for (uint64_t v : asel.values) {
+        for (int h = 0; h < 2; h++) {
+          const uint32_t half = (uint32_t)(v >> (24 * h)) & 0xFFFFFFu;
+          const uint32_t d = half ^ prev[h];
+          prev[h] = half;
+          for (int j = 0; j < 24; j += 6) {
+            const uint32_t x = (d >> j) & 63u;
+            if (pass) hs.put(bw, x); else fs[x]++;
+          }
+        }
+      }
+      if (pass) pal[3] = bw.finish();
+    }
+  }
+  // the block-stream models (crn_comp::pack_data_models)
+  std::vector<uint8_t> tables;
+  {
+    BitWriter bw;
+    send_model(bw, m_ref);
+    if (colour) { send_model(bw, m_ep[0]); send_model(bw, m_sel[0]); }
+    if (nalpha) { send_model(bw, m_ep[1]); send_model(bw, m_sel[1]); }
+    tables = bw.finish();
+  }
+  if (tables.size() > 0xFFFF) { set_error("crngpu_crn_pack: model tables too large"); return CRNGPU_E_PARAM; }
+  // file: header | palettes | tables | levels (crn_comp::create_comp_data, crnlib/crn_comp.cpp:1414-1496)
+  const uint32_t header_size = 74 + 4 * (levels - 1);
+  std::vector<uint8_t> d(header_size, 0);
+  uint32_t pal_ofs[4] = {0, 0, 0, 0};
+  for (int p = 0; p < 4; p++) {
+    if (pal[p].empty()) continue;
+    pal_ofs[p] = (uint32_t)d.size();
+    d.insert(d.end(), pal[p].begin(), pal[p].end());
+  }
+  const uint32_t tables_ofs = (uint32_t)d.size();
+  d.insert(d.end(), tables.begin(), tables.end());
+  std::vector<uint32_t> level_ofs(levels);
+  for (uint32_t l = 0; l < levels; l++) {
+    level_ofs[l] = (uint32_t)d.size();
+    d.insert(d.end(), level_data[l].begin(), level_data[l].end());
+  }
+  if (d.size() > 0xFFFFFFu) { set_error("crngpu_crn_pack: file larger than the format's 24-bit offsets"); return CRNGPU_E_PARAM; }
+  put_be(d, 0, ('H' << 8) | 'x', 2);
+  put_be(d, 2, header_size, 2);
+  put_be(d, 6, (uint32_t)d.size(), 4);
+  put_be(d, 12, width, 2);
+  put_be(d, 14, height, 2);
+  d[16] = (uint8_t)levels;
+  d[17] = (uint8_t)faces;
+  d[18] = (uint8_t)format;
+  const size_t nums[4] = {cep.values.size(), csel.values.size(), aep.values.size(), asel.values.size()};
+  for (int p = 0; p < 4; p++) {
+    if (pal[p].empty()) continue;
+    put_be(d, 33 + 8 * p, pal_ofs[p], 3);
+    put_be(d, 36 + 8 * p, (uint32_t)pal[p].size(), 3);
+    put_be(d, 39 + 8 * p, (uint32_t)nums[p], 2);
+  }
+  put_be(d, 65, (uint32_t)tables.size(), 2);
+  put_be(d, 67, tables_ofs, 3);
+  for (uint32_t l = 0; l < levels; l++) put_be(d, 70 + 4 * l, level_ofs[l], 4);
+  put_be(d, 10, crc16(d.data() + header_size, (uint32_t)(d.size() - header_size)), 2);
+  put_be(d, 4, crc16(d.data() + 6, header_size - 6), 2);
+  if (out && out_capacity >= d.size()) std::memcpy(out, d.data(), d.size());
+  return (int64_t)d.size();
+}

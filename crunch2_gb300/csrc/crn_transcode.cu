@@ -77,8 +77,12 @@ struct ExpandJob {
 };
 
 constexpr uint32_t kExpandThreads = 256;
-constexpr uint32_t kTileBlocks = 4096;  // blocks per expansion tile (16 per thread)
-constexpr uint32_t kStageMin = 1024;    // DXT1 tiles at least this large stage their palettes
+// Expansion variants: tile of 1024 << kTileShift[v] blocks, DXT1 palettes staged or not. The
+// autotuner (crngpu_unpack_batch_launch, first launch) times all of them and keeps the fastest.
+constexpr int kTileSizes = 6;           // 1024 .. 32768 blocks per tile, processed 2048 at a time
+constexpr uint32_t kSubBlocks = 2048;   // blocks per pass of a CTA over its tile (8 per thread)
+constexpr int kExpandVariants = 2 * kTileSizes;
+constexpr uint32_t kStageMin = 1024;    // DXT1 tiles at least this large may stage their palettes
 // Decoder shared memory per CTA: five first-level tables + the row buffers of one texture's
 // levels (at most 2 x 1024 + 2 x 16 words for a 4096-texel-wide texture with 16 levels).
 constexpr size_t kDecodeSmemMax = 64u << 10;
@@ -334,16 +338,16 @@ __device__ __forceinline__ uint2 alpha_words(const DevPalettes& pal, uint32_t r)
   return make_uint2((uint32_t)a, (uint32_t)(a >> 32));
 }
 
-// The expansion works on tiles of kTileBlocks consecutive blocks of one face of one level; each
-// CTA takes one tile from a table built on the host (no per-CTA search). A thread handles
-// kTileBlocks / kExpandThreads blocks: it first loads all its index records, then gathers the
-// palette words, then stores, so each thread keeps many loads in flight. For DXT1 tiles of at
-// least kStageMin blocks the CTA first copies the two colour palettes into shared memory, so the
-// per-block gathers hit shared memory instead of costing a 32-byte L2 sector per 4-byte word.
-template <bool WIDE>  // WIDE: 16-byte blocks (DXT5, DXN); else 8-byte blocks (DXT1, DXT5A)
+// The expansion works on tiles of TILE consecutive blocks of one face of one level; each CTA
+// takes one tile from a table built on the host (no per-CTA search). A thread handles
+// TILE / kExpandThreads blocks: it first loads all its index records, then gathers the palette
+// words, then stores, so each thread keeps several loads in flight. With STAGE, DXT1 tiles of at
+// least kStageMin blocks first copy the two colour palettes into shared memory, so the per-block
+// gathers hit shared memory instead of costing a 32-byte L2 sector per 4-byte word.
+template <bool WIDE, uint32_t TILE>  // WIDE: 16-byte blocks (DXT5, DXN); else 8-byte blocks (DXT1, DXT5A)
 __device__ __forceinline__ void expand_tile(const ExpandJob& J, uint32_t first, const uint32_t* s_ep,
                                             const uint32_t* s_sel) {
-  constexpr uint32_t kPer = kTileBlocks / kExpandThreads;  // blocks per thread
+  constexpr uint32_t kPer = TILE / kExpandThreads;  // blocks per thread and pass
   const uint32_t kind = J.kind, bx = J.bx;
   const uint32_t nblk = bx * J.by;
   const DevPalettes pal = J.pal;
@@ -432,32 +436,45 @@ __device__ __forceinline__ void expand_tile(const ExpandJob& J, uint32_t first, 
   }
 }
 
-// Dynamic shared memory: the staged DXT1 colour palettes, smem_words = the largest
-// n_cep + n_csel of the launch's DXT1 jobs (0 when none is staged).
+// Dynamic shared memory (STAGE): the staged DXT1 colour palettes, smem_words = the largest
+// n_cep + n_csel of the launch's DXT1 jobs. A CTA covers TILE blocks in passes of up to
+// kSubBlocks, so a large tile pays for the palette copy once.
+template <uint32_t TILE, bool STAGE>
 __global__ void __launch_bounds__(kExpandThreads) k_crn_expand_tiles(const ExpandJob* __restrict__ jobs,
                                                                       const uint2* __restrict__ tiles,
                                                                       uint32_t smem_words) {
   extern __shared__ uint32_t s_pal[];
+  constexpr uint32_t kSub = TILE < kSubBlocks ? TILE : kSubBlocks;
   const uint2 t = tiles[blockIdx.x];  // (job, first block)
   const ExpandJob& J = jobs[t.x];
+  const uint32_t nblk = J.bx * J.by;
+  const uint32_t end = min(nblk, t.y + TILE);
   if (J.kind == kKDxt1) {
-    const uint32_t nblk = J.bx * J.by;
     const uint32_t n_ep = J.pal.n_cep, n_sel = J.pal.n_csel;
-    const bool stage = nblk - t.y >= kStageMin && n_ep + n_sel <= smem_words;  // uniform per CTA
+    const bool stage = STAGE && end - t.y >= kStageMin && n_ep + n_sel <= smem_words;  // uniform per CTA
     if (stage) {
       for (uint32_t i = threadIdx.x; i < n_ep; i += kExpandThreads) s_pal[i] = __ldg(J.pal.colour_ep + i);
       for (uint32_t i = threadIdx.x; i < n_sel; i += kExpandThreads) s_pal[n_ep + i] = __ldg(J.pal.colour_sel + i);
       __syncthreads();
-      expand_tile<false>(J, t.y, s_pal, s_pal + n_ep);
+      for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, s_pal, s_pal + n_ep);
     } else {
-      expand_tile<false>(J, t.y, nullptr, nullptr);
+      for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, nullptr, nullptr);
     }
   } else if (J.kind == kKDxt5a) {
-    expand_tile<false>(J, t.y, nullptr, nullptr);
+    for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, nullptr, nullptr);
   } else {
-    expand_tile<true>(J, t.y, nullptr, nullptr);
+    for (uint32_t f = t.y; f < end; f += kSub) expand_tile<true, kSub>(J, f, nullptr, nullptr);
   }
 }
+
+// variant v: tile size 1024 << (v >> 1), palettes staged when v is odd
+typedef void (*ExpandKernel)(const ExpandJob*, const uint2*, uint32_t);
+const ExpandKernel kExpandKernels[kExpandVariants] = {
+    k_crn_expand_tiles<1024, false>,  k_crn_expand_tiles<1024, true>,  k_crn_expand_tiles<2048, false>,
+    k_crn_expand_tiles<2048, true>,   k_crn_expand_tiles<4096, false>, k_crn_expand_tiles<4096, true>,
+    k_crn_expand_tiles<8192, false>,  k_crn_expand_tiles<8192, true>,  k_crn_expand_tiles<16384, false>,
+    k_crn_expand_tiles<16384, true>,  k_crn_expand_tiles<32768, false>, k_crn_expand_tiles<32768, true>};
+int g_expand_variant[64] = {};  // per device: the autotuner's last choice (0 until tuned)
 
 // ------------------------------------------------------------------------------------------
 // Host side.
@@ -564,7 +581,9 @@ struct Plan {
   uint32_t n_item = 0, n_stream = 0, n_expand = 0, ctas = 0;
   uint32_t rb_words = 2;    // largest row-buffer need of one texture job (words)
   uint32_t lut_words = 0;   // first-level tables staged per texture job (words)
-  size_t stream_ofs = 0, expand_ofs = 0, tile_ofs = 0;
+  size_t stream_ofs = 0, expand_ofs = 0;
+  size_t tile_ofs[kTileSizes] = {};
+  uint32_t tile_ctas[kTileSizes] = {};
   uint32_t pal_words = 0;   // shared memory of the expansion: largest staged DXT1 palette pair
 };
 
@@ -629,7 +648,7 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
     sj.insert(sj.end(), item_streams[o].begin(), item_streams[o].end());
   }
   std::vector<ExpandJob> ej;
-  std::vector<uint2> tiles;
+  std::vector<uint2> tiles[kTileSizes];
   for (const LevelTask& t : tasks) {
     const CrnFile& F = *t.file;
     const LevelInfo& li = F.level[t.level];
@@ -646,7 +665,8 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
       j.kind = kind;
       j.flat = t.pitch == li.blocks_x * F.bytes_per_block ? 1u : 0u;
       j.vec = (((uintptr_t)t.dst[f] & 15) == 0 && (j.flat || (t.pitch & 15) == 0)) ? 1u : 0u;
-      for (uint32_t b = 0; b < nblk; b += kTileBlocks) tiles.push_back(make_uint2((uint32_t)ej.size(), b));
+      for (int ts = 0; ts < kTileSizes; ts++)
+        for (uint32_t b = 0; b < nblk; b += 1024u << ts) tiles[ts].push_back(make_uint2((uint32_t)ej.size(), b));
       if (kind == kKDxt1 && nblk >= kStageMin)
         p.pal_words = std::max(p.pal_words, t.pal.n_cep + t.pal.n_csel);
       ej.push_back(j);
@@ -655,16 +675,22 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
   p.n_item = (uint32_t)it_sorted.size();
   p.n_stream = (uint32_t)sj.size();
   p.n_expand = (uint32_t)ej.size();
-  p.ctas = (uint32_t)tiles.size();
+  p.ctas = (uint32_t)tiles[0].size();
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
   p.stream_ofs = al(sizeof(TexJob) * it_sorted.size());
   p.expand_ofs = p.stream_ofs + al(sizeof(StreamJob) * sj.size());
-  p.tile_ofs = p.expand_ofs + al(sizeof(ExpandJob) * ej.size());
-  p.image.assign(p.tile_ofs + sizeof(uint2) * tiles.size(), 0);
+  size_t end = p.expand_ofs + al(sizeof(ExpandJob) * ej.size());
+  for (int ts = 0; ts < kTileSizes; ts++) {
+    p.tile_ofs[ts] = end;
+    p.tile_ctas[ts] = (uint32_t)tiles[ts].size();
+    end += al(sizeof(uint2) * tiles[ts].size());
+  }
+  p.image.assign(end, 0);
   std::memcpy(p.image.data(), it_sorted.data(), sizeof(TexJob) * it_sorted.size());
   std::memcpy(p.image.data() + p.stream_ofs, sj.data(), sizeof(StreamJob) * sj.size());
   std::memcpy(p.image.data() + p.expand_ofs, ej.data(), sizeof(ExpandJob) * ej.size());
-  std::memcpy(p.image.data() + p.tile_ofs, tiles.data(), sizeof(uint2) * tiles.size());
+  for (int ts = 0; ts < kTileSizes; ts++)
+    std::memcpy(p.image.data() + p.tile_ofs[ts], tiles[ts].data(), sizeof(uint2) * tiles[ts].size());
   return true;
 }
 
@@ -686,9 +712,10 @@ int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
     if ((e = cudaFuncSetAttribute(k_crn_decode_textures, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDecodeSmemMax)) != cudaSuccess)
       return cuda_check(e, "decoder shared memory attribute");
-    if ((e = cudaFuncSetAttribute(k_crn_expand_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(2 * kMaxSyms * sizeof(uint32_t)))) != cudaSuccess)
-      return cuda_check(e, "expansion shared memory attribute");
+    for (int v = 1; v < kExpandVariants; v += 2)
+      if ((e = cudaFuncSetAttribute(kExpandKernels[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(2 * kMaxSyms * sizeof(uint32_t)))) != cudaSuccess)
+        return cuda_check(e, "expansion shared memory attribute");
     attr_set[dev] = true;
   }
   *smem = (size_t)(p.lut_words + p.rb_words) * sizeof(uint32_t);
@@ -699,7 +726,8 @@ int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
 
 // Enqueues the counter/status clear, the decoder and the expansion for a plan whose image is
 // already at d_jobs. `words` = 2 device words: [0] work counter, [1] status. Asynchronous.
-int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStream_t s, bool decode = true) {
+int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStream_t s, bool decode = true,
+                 int variant = -1) {
   if ((size_t)(p.lut_words + p.rb_words) * 4 > kDecodeSmemMax) {
     set_error("texture rows too wide for the decoder");
     return CRNGPU_E_PARAM;
@@ -718,8 +746,13 @@ int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStre
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_decode_textures");
   }
   if (p.ctas) {
-    const uint2* tiles = reinterpret_cast<const uint2*>(d_jobs + p.tile_ofs);
-    k_crn_expand_tiles<<<p.ctas, kExpandThreads, (size_t)p.pal_words * 4, s>>>(ej, tiles, p.pal_words);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int v = variant >= 0 ? variant : g_expand_variant[dev & 63];
+    const int ts = v >> 1;
+    const uint2* tiles = reinterpret_cast<const uint2*>(d_jobs + p.tile_ofs[ts]);
+    const size_t smem = (v & 1) ? (size_t)p.pal_words * 4 : 0;
+    kExpandKernels[v]<<<p.tile_ctas[ts], kExpandThreads, smem, s>>>(ej, tiles, p.pal_words);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_expand_tiles");
   }
   return CRNGPU_OK;
@@ -862,6 +895,8 @@ struct UnpackBatch {
   uint32_t words_host[2] = {0, 0};
   cudaGraphExec_t graph = nullptr;
   bool decoded = false;
+  int variant = -1;          // expansion variant chosen by the autotuner
+  float variant_ms[kExpandVariants] = {};
   uint64_t out_bytes = 0;
   ~UnpackBatch() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -1001,12 +1036,45 @@ extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t fl
   cudaStream_t s = as_stream(stream);
   const uint8_t* jobs = static_cast<const uint8_t*>(b->d_jobs.ptr);
   uint32_t* words = static_cast<uint32_t*>(b->d_words.ptr);
+  if (b->variant < 0) {
+    // autotuner: decode once, then time every expansion variant on the real records (each writes
+    // the same, correct output) and keep the fastest for this batch and as the device default
+    int rc = enqueue_plan(b->plan, jobs, words, s, true, 0);
+    if (rc != CRNGPU_OK) return rc;
+    cudaEvent_t ev[2];
+    cudaError_t e;
+    if ((e = cudaEventCreate(&ev[0])) != cudaSuccess || (e = cudaEventCreate(&ev[1])) != cudaSuccess)
+      return cuda_check(e, "events");
+    float best = 3.4e38f;
+    int bv = 0;
+    for (int v = 0; v < kExpandVariants; v++) {
+      float tot = 0.f;
+      for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(ev[0], s);
+        if ((rc = enqueue_plan(b->plan, jobs, words, s, false, v)) != CRNGPU_OK) break;
+        cudaEventRecord(ev[1], s);
+        cudaEventSynchronize(ev[1]);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ev[0], ev[1]);
+        if (rep) tot += ms;  // the first run of each variant warms it up
+      }
+      if (rc != CRNGPU_OK) break;
+      b->variant_ms[v] = tot / 2;
+      if (tot < best) { best = tot; bv = v; }
+    }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (rc != CRNGPU_OK) return rc;
+    b->variant = bv;
+    g_expand_variant[b->device & 63] = bv;
+    b->decoded = true;
+  }
   if (flags & CRNGPU_BATCH_EXPAND_ONLY) {
     if (!b->decoded) { set_error("no decode has run on this batch"); return CRNGPU_E_PARAM; }
-    return enqueue_plan(b->plan, jobs, words, s, false);
+    return enqueue_plan(b->plan, jobs, words, s, false, b->variant);
   }
   b->decoded = true;
-  if (!(flags & CRNGPU_BATCH_GRAPH)) return enqueue_plan(b->plan, jobs, words, s);
+  if (!(flags & CRNGPU_BATCH_GRAPH)) return enqueue_plan(b->plan, jobs, words, s, true, b->variant);
   cudaError_t e;
   if (!b->graph) {
     // capture on a private stream (the legacy default stream cannot be captured), then replay
@@ -1017,7 +1085,7 @@ extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t fl
       cudaStreamDestroy(cap);
       return cuda_check(e, "begin capture");
     }
-    int rc = enqueue_plan(b->plan, jobs, words, cap);
+    int rc = enqueue_plan(b->plan, jobs, words, cap, true, b->variant);
     e = cudaStreamEndCapture(cap, &g);
     cudaStreamDestroy(cap);
     if (rc != CRNGPU_OK) { if (g) cudaGraphDestroy(g); return rc; }
@@ -1039,6 +1107,14 @@ extern "C" int crngpu_unpack_batch_status(crngpu_unpack_batch batch, void* strea
   if (e != cudaSuccess) return cuda_check(e, "read status");
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   return status_to_rc(b->words_host[1]);
+}
+
+extern "C" int crngpu_unpack_batch_tuning(crngpu_unpack_batch batch, int32_t* variant, float* ms, uint32_t n) {
+  UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
+  if (!b || b->magic != 0x42415443u) return CRNGPU_E_PARAM;
+  if (variant) *variant = b->variant;
+  for (uint32_t i = 0; ms && i < n && i < (uint32_t)kExpandVariants; i++) ms[i] = b->variant_ms[i];
+  return kExpandVariants;
 }
 
 extern "C" int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch) {

@@ -356,7 +356,126 @@ struct Tile {
   uint32_t kind;   // 0..8 (tile within the chunk image), 0xFF: unused slot
   float weight;    // pixels x level weight
   float v[6];      // palettize_color result
+  float va[2][2];  // palettize_alpha result per alpha channel (low <= high)
 };
+
+// Which channels the clustered format carries (dxt_hc::compress, crn_dxt_hc.cpp:104-118).
+struct TileCfg {
+  int has_color;        // DXT1, DXT5
+  int num_alpha;        // 0 (DXT1), 1 (DXT5, DXT5A), 2 (DXN)
+  int comp[2];          // m_alpha_component_indices
+  float ratio;          // m_adaptive_tile_color_alpha_weighting_ratio
+  float alpha_derating[8];
+};
+
+// dxt5_endpoint_optimizer::compute at quality Normal with 8-value blocks only, for the tile
+// decision (crn_dxt_hc.cpp:475-490): the smallest error over all pairs of the tile's unique
+// values (crnlib/crn_dxt5a.cpp:40-100, 198-262).
+__host__ __device__ uint32_t alpha_tile_error(int n, const uint32_t* px, int comp) {
+  uint8_t uv[64];
+  uint32_t uw[64];
+  int U = 0;
+  for (int i = 0; i < n; i++) {
+    const uint8_t a = (uint8_t)((px[i] >> (8 * comp)) & 255u);
+    int k = 0;
+    while (k < U && uv[k] != a) k++;
+    if (k == U) { uv[U] = a; uw[U] = 0; U++; }
+    uw[k]++;
+  }
+  if (U == 1) return 0;
+  unsigned long long best = ~0ull;
+  for (int i = 0; i < U - 1; i++) {
+    for (int j = i + 1; j < U; j++) {
+      const int l = uv[i], h = uv[j];
+      const int v[8] = {l, h, (l * 6 + h) / 7, (l * 5 + h * 2) / 7, (l * 4 + h * 3) / 7, (l * 3 + h * 4) / 7,
+                        (l * 2 + h * 5) / 7, (l + h * 6) / 7};
+      unsigned long long e = 0;
+      for (int u = 0; u < U && e <= best; u++) {
+        int bd = 0x7FFFFFFF;
+        for (int k = 0; k < 8; k++) {
+          const int d = (int)uv[u] - v[k];
+          bd = min(bd, d * d);
+        }
+        e += (unsigned long long)bd * uw[u];
+      }
+      if (e < best) best = e;
+    }
+  }
+  return (uint32_t)best;
+}
+
+// split_vectors<vec1F> (crn_tree_clusterizer.h:573-753) for up to 64 weighted values: the two
+// centroids of a 1-D 2-means split seeded by the furthest/opposite values.
+__host__ __device__ void split_vec1(const float* v, const uint32_t* w, int size, float* res) {
+  float cen = 0.f;
+  double ttsum = 0;
+  uint64_t tw = 0;
+  for (int i = 0; i < size; i++) { cen += v[i] * (float)w[i]; tw += w[i]; ttsum += (double)(v[i] * v[i]) * w[i]; }
+  const float variance = (float)(ttsum - (double)(cen * cen) / (double)tw);
+  cen *= 1.0f / (float)tw;
+  res[0] = res[1] = cen;
+  if (variance <= 0.0f || size == 1) return;
+  int fi = 0, oi = 0;
+  float fd = -1.f, od = -1.f;
+  for (int i = 0; i < size; i++) { const float d = (v[i] - cen) * (v[i] - cen); if (d > fd) { fd = d; fi = i; } }
+  for (int i = 0; i < size; i++) { const float d = (v[i] - v[fi]) * (v[i] - v[fi]); if (d > od) { od = d; oi = i; } }
+  float L = (v[fi] + cen) * .5f, R = (v[oi] + cen) * .5f;
+  if (size > 2) {
+    // the 1-D principal axis is +1: split at the centroid
+    float nl = 0.f, nr = 0.f;
+    double lw = 0, rw = 0;
+    for (int i = 0; i < size; i++) {
+      if ((double)(v[i] - cen) < 0.0) { nl += v[i] * (float)w[i]; lw += w[i]; }
+      else { nr += v[i] * (float)w[i]; rw += w[i]; }
+    }
+    if (lw > 0 && rw > 0) { L = nl * (float)(1.0 / lw); R = nr * (float)(1.0 / rw); }
+  }
+  float prev = 1e10f;
+  for (int loop = 0; loop < 1024; loop++) {
+    float nl = 0.f, nr = 0.f;
+    double lt = 0, rt = 0;
+    uint64_t lw = 0, rw = 0;
+    for (int i = 0; i < size; i++) {
+      const float vv = v[i] * v[i] * (float)w[i];
+      if ((L - v[i]) * (L - v[i]) < (R - v[i]) * (R - v[i])) { nl += v[i] * (float)w[i]; lt += vv; lw += w[i]; }
+      else { nr += v[i] * (float)w[i]; rt += vv; rw += w[i]; }
+    }
+    if (!lw || !rw) return;
+    const float lv = (float)(lt - (double)(nl * nl) / (double)lw), rv = (float)(rt - (double)(nr * nr) / (double)rw);
+    L = nl * (1.0f / (float)lw);
+    R = nr * (1.0f / (float)rw);
+    const float tv = lv + rv;
+    if (tv < .00001f) break;
+    if ((prev - tv) / tv < .00001f) break;
+    prev = tv;
+  }
+  res[0] = L;
+  res[1] = R;
+}
+
+// palettize_alpha (crn_dxt_hc.cpp:353-384): the tile's values of one channel split in two, sorted
+__host__ __device__ void palettize_alpha(const uint32_t* px, int n, int comp, float* out2) {
+  uint8_t a[64];
+  for (int i = 0; i < n; i++) a[i] = (uint8_t)((px[i] >> (8 * comp)) & 255u);
+  for (int i = 1; i < n; i++) {
+    const uint8_t x = a[i];
+    int j = i - 1;
+    while (j >= 0 && a[j] > x) { a[j + 1] = a[j]; j--; }
+    a[j + 1] = x;
+  }
+  float v[64];
+  uint32_t w[64];
+  int size = 0;
+  for (int i = 0; i < n; i++) {
+    if (!i || a[i] != a[i - 1]) { v[size] = (float)a[i] * (1.0f / 255.0f); w[size] = 1; size++; }
+    else w[size - 1]++;
+  }
+  float r[2];
+  split_vec1(v, w, size, r);
+  if (r[0] > r[1]) { const float t = r[0]; r[0] = r[1]; r[1] = t; }
+  out2[0] = r[0];
+  out2[1] = r[1];
+}
 
 __host__ __device__ __forceinline__ uint32_t ld_px(const uint32_t* p) {
 #ifdef __CUDA_ARCH__
@@ -416,26 +535,41 @@ __host__ __device__ void palettize(const uint32_t* px, int n, bool perc, float* 
 }
 
 // One chunk of determine_tiles_task (crn_dxt_hc.cpp:386-561): tile errors, layout choice, the
-// chosen tiles' vec6, and each block's tile slot and layout. Returns the layout.
+// chosen tiles' colour vec6 / alpha vec2, and each block's tile slot and layout. Returns the layout.
 __host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint32_t c, const Chunk& ch,
                                       const float* __restrict__ derating, const float* __restrict__ level_weight,
-                                      bool perceptual, const SolidTables* __restrict__ st, Tile* __restrict__ tiles,
-                                      uint32_t* __restrict__ block_tile, uint8_t* __restrict__ block_enc) {
+                                      bool perceptual, const SolidTables* __restrict__ st, const TileCfg& cfg,
+                                      Tile* __restrict__ tiles, uint32_t* __restrict__ block_tile,
+                                      uint8_t* __restrict__ block_enc) {
   const uint8_t tile_ofs[9] = HC_TILE_OFS;
   const uint8_t layout_tiles[8][4] = HC_LAYOUT_TILES;
   const uint8_t layout_ntiles[8] = HC_LAYOUT_NTILES;
   const uint8_t tile_map[8][2][2] = HC_TILE_MAP;
   uint32_t px[128];
   chunk_pixels(blocks, ch.b, ch.width, px);
-  uint32_t terr[9];
-  for (int t = 0; t < 9; t++) terr[t] = fast_tile_error(16 << (t >> 2), px + tile_ofs[t], st);
+  uint32_t terr[3][9];
+  for (int t = 0; t < 9; t++) {
+    const int n = 16 << (t >> 2);
+    if (cfg.has_color) terr[0][t] = fast_tile_error(n, px + tile_ofs[t], st);
+    for (int a = 0; a < cfg.num_alpha; a++) terr[1 + a][t] = alpha_tile_error(n, px + tile_ofs[t], cfg.comp[a]);
+  }
   float best_q = 0.0f;
   int best_e = 0;
   for (int e = 0; e < 8; e++) {
-    uint32_t tot = 0;
-    for (int k = 0; k < layout_ntiles[e]; k++) tot += terr[layout_tiles[e][k]];
-    const double psnr = tot ? log10((double)255.0f / sqrt(tot / 192.0)) * (double)20.0f : (double)999999.0f;
-    const float q = (float)fmax(psnr - (double)derating[ch.level * 8 + e], 0.0);
+    float q = 0.0f;
+    if (cfg.has_color) {
+      uint32_t tot = 0;
+      for (int k = 0; k < layout_ntiles[e]; k++) tot += terr[0][layout_tiles[e][k]];
+      const double psnr = tot ? log10((double)255.0f / sqrt(tot / 192.0)) * (double)20.0f : (double)999999.0f;
+      q = (float)fmax(psnr - (double)derating[ch.level * 8 + e], 0.0);
+      if (cfg.num_alpha) q *= cfg.ratio;
+    }
+    for (int a = 0; a < cfg.num_alpha; a++) {
+      uint32_t tot = 0;
+      for (int k = 0; k < layout_ntiles[e]; k++) tot += terr[1 + a][layout_tiles[e][k]];
+      const double psnr = tot ? log10((double)255.0f / sqrt(tot / 64.0)) * (double)20.0f : (double)999999.0f;
+      q += (float)fmax(psnr - (double)cfg.alpha_derating[e], 0.0);
+    }
     if (q > best_q) { best_q = q; best_e = e; }
   }
   const float lw = level_weight[ch.level];
@@ -447,7 +581,8 @@ __host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint3
     T.chunk = c;
     T.kind = (uint32_t)t;
     T.weight = (float)n * lw;
-    palettize(px + tile_ofs[t], n, perceptual, T.v);
+    if (cfg.has_color) palettize(px + tile_ofs[t], n, perceptual, T.v);
+    for (int a = 0; a < cfg.num_alpha; a++) palettize_alpha(px + tile_ofs[t], n, cfg.comp[a], T.va[a]);
   }
   for (int by = 0; by < 2; by++)
     for (int bx = 0; bx < 2; bx++) {
@@ -461,11 +596,11 @@ __host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint3
 __global__ void __launch_bounds__(64) k_hc_tiles(const uint32_t* __restrict__ blocks, const Chunk* __restrict__ chunks,
                                                  uint32_t nchunks, const float* __restrict__ derating /* [level][8] */,
                                                  const float* __restrict__ level_weight, int perceptual,
-                                                 const SolidTables* __restrict__ st, Tile* __restrict__ tiles,
+                                                 const SolidTables* __restrict__ st, TileCfg cfg, Tile* __restrict__ tiles,
                                                  uint32_t* __restrict__ block_tile, uint8_t* __restrict__ block_enc) {
   const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nchunks) return;
-  hc_tile_chunk(blocks, c, chunks[c], derating, level_weight, perceptual != 0, st, tiles, block_tile, block_enc);
+  hc_tile_chunk(blocks, c, chunks[c], derating, level_weight, perceptual != 0, st, cfg, tiles, block_tile, block_enc);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1456,7 +1591,8 @@ __global__ void k_selector_finalise(const unsigned long long* __restrict__ entry
 // finished DXT1 blocks: cluster endpoints + codebook selectors (linear -> DXT order)
 __global__ void k_hc_emit(const uint32_t* __restrict__ blocks, uint32_t nblocks, const uint32_t* __restrict__ block_cluster,
                           const ClusterOut* __restrict__ cl, const uint32_t* __restrict__ block_sel,
-                          const uint32_t* __restrict__ cbsel, uint2* __restrict__ out, unsigned long long* __restrict__ sse) {
+                          const uint32_t* __restrict__ cbsel, uint8_t* __restrict__ out, uint32_t bpb, uint32_t ofs,
+                          unsigned long long* __restrict__ sse) {
   const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nblocks) return;
   const ClusterOut& C = cl[block_cluster[b]];
@@ -1468,7 +1604,7 @@ __global__ void k_hc_emit(const uint32_t* __restrict__ blocks, uint32_t nblocks,
     const uint32_t px = __ldg(blocks + (size_t)b * 16 + p);
     rgb_sse += cdist(false, px_r(px), px_g(px), px_b(px), C.col[l][0], C.col[l][1], C.col[l][2]);
   }
-  out[b] = make_uint2(C.first | (C.second << 16), dxt);
+  *reinterpret_cast<uint2*>(out + (size_t)b * bpb + ofs) = make_uint2(C.first | (C.second << 16), dxt);
   atomicAdd(sse, (unsigned long long)rgb_sse);
 }
 
@@ -1511,6 +1647,386 @@ __global__ void k_block_weights(const Level* __restrict__ lv, uint32_t nlev, uin
   bw[b] = w;
 }
 
+
+// ------------------------------------------------------------------------------------------
+// Alpha channels (DXT5 alpha, DXT5A, the two DXN channels): vec2 endpoint VQ over the tiles'
+// palettize_alpha pairs, per-cluster dxt5_endpoint_optimizer + dxt_endpoint_refiner::optimize_dxt5,
+// 3-bit selector codebook (crn_dxt_hc.cpp:1014-1300, 1506-1720).
+
+__constant__ uint8_t c_from_linear8[8] = {0, 2, 3, 4, 5, 6, 7, 1};  // g_dxt5_from_linear
+__constant__ uint8_t c_to_linear8[8] = {0, 7, 1, 2, 3, 4, 5, 6};    // g_dxt5_to_linear
+
+// dxt5_block::get_block_values8 / 6 (crnlib/crn_dxt.cpp:369-431)
+__host__ __device__ __forceinline__ void alpha_values8(int l, int h, int* v) {
+  v[0] = l; v[1] = h;
+  v[2] = (l * 6 + h) / 7; v[3] = (l * 5 + h * 2) / 7; v[4] = (l * 4 + h * 3) / 7;
+  v[5] = (l * 3 + h * 4) / 7; v[6] = (l * 2 + h * 5) / 7; v[7] = (l + h * 6) / 7;
+}
+__host__ __device__ __forceinline__ void alpha_values(int l, int h, int* v) {
+  if (l > h) { alpha_values8(l, h, v); return; }
+  v[0] = l; v[1] = h;
+  v[2] = (l * 4 + h) / 5; v[3] = (l * 3 + h * 2) / 5; v[4] = (l * 2 + h * 3) / 5; v[5] = (l + h * 4) / 5;
+  v[6] = 0; v[7] = 255;
+}
+
+struct AlphaCluster {
+  uint32_t first, second;  // final endpoints (first > second: 8-value block), after the refiner
+  int vals[8];             // linear-order values of the optimizer's endpoints (block selectors, search)
+  int rvals[8];            // linear-order values of the final endpoints (error accumulation)
+  uint32_t endpoint_weight;
+};
+
+// tile -> nearest alpha codebook entry per channel (determine_alpha_endpoint_clusters_task, :1132-1163)
+__global__ void k_nearest_vec2(const Tile* __restrict__ tiles, const uint32_t* __restrict__ used, uint32_t nused,
+                               int num_alpha, const float* __restrict__ cb, uint32_t K, uint32_t* __restrict__ tile_ac) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nused * (uint32_t)num_alpha) return;
+  const uint32_t a = i / nused, t = used[i - a * nused];
+  const float v0 = tiles[t].va[a][0], v1 = tiles[t].va[a][1];
+  float best = 3.4e38f;
+  uint32_t bi = 0;
+  for (uint32_t k = 0; k < K; k++) {
+    const float d = (cb[2 * k] - v0) * (cb[2 * k] - v0) + (cb[2 * k + 1] - v1) * (cb[2 * k + 1] - v1);
+    if (d < best) { best = d; bi = k; if (best == 0.0f) break; }
+  }
+  tile_ac[2 * t + a] = bi;
+}
+
+// alpha VQ input: (channel-major) the used tiles' vec2 with their pixel counts as weights
+__global__ void k_alpha_vectors(const Tile* __restrict__ tiles, const uint32_t* __restrict__ used, uint32_t nused,
+                                int num_alpha, float* __restrict__ vec, uint32_t* __restrict__ w, uint32_t* __restrict__ key_item) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nused * (uint32_t)num_alpha) return;
+  const uint32_t a = i / nused, t = used[i - a * nused];
+  vec[2 * i] = tiles[t].va[a][0];
+  vec[2 * i + 1] = tiles[t].va[a][1];
+  w[i] = tile_npix(tiles[t].kind);
+  key_item[i] = 2 * t + a;
+}
+__global__ void k_alpha_keys(const uint32_t* __restrict__ items, uint32_t n, const uint32_t* __restrict__ tile_ac,
+                             uint32_t* __restrict__ key, uint32_t* __restrict__ counts) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  key[i] = tile_ac[items[i]];
+  atomicAdd(counts + key[i], 1u);
+}
+
+constexpr int kAFitThreads = 256;
+
+// error of the 8-value block (l, h) over a value histogram, each value on its nearest palette
+// value, from prefix sums P0 (count), P1 (sum v), P2 (sum v^2) of 257 entries
+__device__ __forceinline__ unsigned long long alpha_pair_error(int l, int h, const unsigned long long* P0,
+                                                               const unsigned long long* P1, const unsigned long long* P2) {
+  int q[8];
+  alpha_values8(l, h, q);
+  for (int i = 1; i < 8; i++) {  // sort the 8 values ascending
+    const int x = q[i];
+    int j = i - 1;
+    while (j >= 0 && q[j] > x) { q[j + 1] = q[j]; j--; }
+    q[j + 1] = x;
+  }
+  long long e = 0;
+  int lo = 0;
+  for (int k = 0; k < 8; k++) {
+    const int hi = k < 7 ? (q[k] + q[k + 1]) >> 1 : 255;
+    if (hi >= lo) {
+      const long long s0 = (long long)(P0[hi + 1] - P0[lo]), s1 = (long long)(P1[hi + 1] - P1[lo]),
+                      s2 = (long long)(P2[hi + 1] - P2[lo]);
+      e += s2 - 2 * (long long)q[k] * s1 + (long long)q[k] * q[k] * s0;
+      lo = hi + 1;
+    }
+  }
+  return (unsigned long long)e;
+}
+
+// CTA-wide minimum of (error, key)
+__device__ __forceinline__ void block_min_pair(unsigned long long& e, uint32_t& key, unsigned long long* se, uint32_t* sk) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long oe = __shfl_xor_sync(0xFFFFFFFFu, e, o);
+    const uint32_t ok = __shfl_xor_sync(0xFFFFFFFFu, key, o);
+    if (oe < e || (oe == e && ok < key)) { e = oe; key = ok; }
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) { se[threadIdx.x >> 5] = e; sk[threadIdx.x >> 5] = key; }
+  __syncthreads();
+  e = se[0]; key = sk[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); w++)
+    if (se[w] < e || (se[w] == e && sk[w] < key)) { e = se[w]; key = sk[w]; }
+  __syncthreads();
+}
+
+// Per alpha cluster (determine_alpha_endpoint_codebook_task, :1014-1130): the histogram of the
+// cluster's values, dxt5_endpoint_optimizer at uber quality with 8-value blocks (all pairs of
+// unique values, then the +-16 grid around the best, crnlib/crn_dxt5a.cpp:40-196) evaluated
+// exactly through prefix sums, then dxt_endpoint_refiner::optimize_dxt5
+// (crnlib/crn_dxt_endpoint_refiner.cpp:36-201).
+__global__ void __launch_bounds__(kAFitThreads) k_alpha_cluster_fit(const uint32_t* __restrict__ blocks,
+                                                                     const Chunk* __restrict__ chunks,
+                                                                     const Tile* __restrict__ tiles, TileCfg cfg,
+                                                                     const uint32_t* __restrict__ start,
+                                                                     const uint32_t* __restrict__ members,
+                                                                     AlphaCluster* __restrict__ out) {
+  __shared__ uint32_t hist[256];
+  __shared__ unsigned long long P0[257], P1[257], P2[257];
+  __shared__ uint8_t uv[256];
+  __shared__ uint32_t s_nu;
+  __shared__ unsigned long long se[kAFitThreads / 32];
+  __shared__ uint32_t sk[kAFitThreads / 32];
+  const uint32_t k = blockIdx.x;
+  const uint32_t m0 = start[k], m1 = start[k + 1];
+  AlphaCluster& O = out[k];
+  if (m0 == m1) {
+    if (threadIdx.x == 0) { O.first = O.second = 0; for (int i = 0; i < 8; i++) O.vals[i] = O.rvals[i] = 0; O.endpoint_weight = 1; }
+    return;
+  }
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  for (uint32_t m = m0 + (threadIdx.x >> 6); m < m1; m += blockDim.x >> 6) {  // 64 threads per member tile
+    const uint32_t item = members[m], t = item >> 1, a = item & 1;
+    const Tile& T = tiles[t];
+    const uint32_t j = threadIdx.x & 63;
+    if (j < tile_npix(T.kind)) {
+      const uint32_t v = (tile_pixel(blocks, chunks[T.chunk], T.kind, j) >> (8 * cfg.comp[a])) & 255u;
+      atomicAdd(&hist[v], 1u);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    P0[0] = P1[0] = P2[0] = 0;
+    uint32_t nu = 0;
+    for (int v = 0; v < 256; v++) {
+      P0[v + 1] = P0[v] + hist[v];
+      P1[v + 1] = P1[v] + (unsigned long long)hist[v] * v;
+      P2[v + 1] = P2[v] + (unsigned long long)hist[v] * v * v;
+      if (hist[v]) uv[nu++] = (uint8_t)v;
+    }
+    s_nu = nu;
+  }
+  __syncthreads();
+  const int U = (int)s_nu;
+  int first, second;
+  unsigned long long best;
+  if (U == 1) {
+    first = second = uv[0];
+    best = 0;
+  } else {
+    // all pairs of unique values
+    unsigned long long be = ~0ull;
+    uint32_t bk = 0xFFFFFFFFu;
+    for (int i = threadIdx.x; i < U - 1; i += blockDim.x)
+      for (int j = i + 1; j < U; j++) {
+        const unsigned long long e = alpha_pair_error(uv[i], uv[j], P0, P1, P2);
+        const uint32_t key = (uint32_t)(i * 256 + j);
+        if (e < be || (e == be && key < bk)) { be = e; bk = key; }
+      }
+    block_min_pair(be, bk, se, sk);
+    first = uv[bk >> 8];
+    second = uv[bk & 255];
+    best = be;
+    if (best) {
+      // +-16 probe grid around the best pair
+      unsigned long long ge = best;
+      uint32_t gk = 0xFFFFFFFFu;
+      for (int i = threadIdx.x; i < 33 * 33; i += blockDim.x) {
+        const int l = first + i / 33 - 16, h = second + i % 33 - 16;
+        if (l < 0 || l > 255 || h < 0 || h > 255) continue;
+        const unsigned long long e = alpha_pair_error(l, h, P0, P1, P2);
+        if (e < ge || (e == ge && (uint32_t)i < gk)) { ge = e; gk = (uint32_t)i; }
+      }
+      block_min_pair(ge, gk, se, sk);
+      if (gk != 0xFFFFFFFFu && ge < best) {
+        best = ge;
+        const int l = first + (int)(gk / 33) - 16, h = second + (int)(gk % 33) - 16;
+        first = l;
+        second = h;
+      }
+    }
+  }
+  // 8-value blocks need first > second (the reference swaps and inverts the selectors)
+  if (first <= second) { const int t = first; first = second; second = t; }
+  if (threadIdx.x == 0) {
+    int bv[8];
+    alpha_values(first, second, bv);
+    for (int i = 0; i < 8; i++) O.vals[i] = bv[c_from_linear8[i]];
+    const int delta = first - second;
+    O.endpoint_weight = (uint32_t)min(max((delta * delta) >> 3, 1), 2048);
+    // refiner: least squares from the DXT-order selectors of every value, then the +-11 grid
+    uint32_t L = (uint32_t)first, H = (uint32_t)second;
+    if (U > 1 && best) {
+      double a2 = 0, b2 = 0, ab = 0, ax = 0, bx = 0;
+      double hs[8] = {0, 0, 0, 0, 0, 0, 0, 0}, d2[8] = {0, 0, 0, 0, 0, 0, 0, 0}, dd[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      double first_x = uv[0] / 255.0;
+      for (int u = 0; u < U; u++) {
+        const int v = uv[u];
+        const double c = hist[v];
+        int bs = 0, bd = 0x7FFFFFFF;
+        for (int j = 0; j < 8; j++) { const int d = (v - bv[j]) * (v - bv[j]); if (d < bd) { bd = d; bs = j; } }
+        const double kk = (double)c_to_linear8[bs] * (double)(1.0f / 7.0f);
+        const double al = 1.0 - kk, be2 = kk, x = (double)((float)v * (1.0f / 255.0f));
+        a2 += c * al * al; b2 += c * be2 * be2; ab += c * al * be2; ax += c * al * x; bx += c * be2 * x;
+        hs[bs] += c; d2[bs] += c * 2 * v; dd[bs] += c * v * v;
+      }
+      double ea, eb;
+      if (b2 == 0.0) { ea = ax / a2; eb = 0; }
+      else if (a2 == 0.0) { ea = 0; eb = bx / b2; }
+      else {
+        const double f = a2 * b2 - ab * ab;
+        if (f != 0.0) { ea = (ax * b2 - bx * ab) / f; eb = (bx * a2 - ax * ab) / f; }
+        else { ea = eb = first_x; }
+      }
+      const float lf = fminf(fmaxf((float)ea, 0.f), 1.f), hf = fminf(fmaxf((float)eb, 0.f), 1.f);
+      const int L0 = clampi((int)(lf * 256.0f), 0, 255), H0 = clampi((int)(hf * 256.0f), 0, 255);
+      auto norm = [](int l, int h) -> uint32_t {
+        return l == h ? (h ? ((uint32_t)(h - 1) << 8 | (uint32_t)l) : 1u) : (l > h ? ((uint32_t)h << 8 | (uint32_t)l) : ((uint32_t)l << 8 | (uint32_t)h));
+      };
+      unsigned long long rbest = ~0ull;
+      uint32_t rsol = 0;
+      auto eval = [&](uint32_t sol) {
+        int v[8];
+        alpha_values8((int)(sol & 255), (int)(sol >> 8), v);
+        double er = 0;
+        for (int q = 0; q < 8; q++) er += hs[q] * v[q] * v[q] - d2[q] * v[q] + dd[q];
+        const unsigned long long e = (unsigned long long)(er + 0.5);
+        if (e < rbest) { rbest = e; rsol = sol; }
+      };
+      eval(norm(L0, H0));
+      const int minL = L0 <= 11 ? 0 : L0 - 11, maxL = L0 >= 244 ? 255 : L0 + 11;
+      const int minH = H0 <= 11 ? 0 : H0 - 11, maxH = H0 >= 244 ? 255 : H0 + 11;
+      for (int l = minL; l <= maxL && rbest; l++)
+        for (int h = minH; h <= maxH && rbest; h++)
+          if ((maxH < l || l <= h || h < minL) && (l != L0 || h != H0) && (l != H0 || h != L0)) eval(norm(l, h));
+      if (rbest < best) { L = rsol & 255; H = rsol >> 8; }
+    }
+    O.first = L;
+    O.second = H;
+    int rv[8];
+    alpha_values((int)L, (int)H, rv);
+    for (int i = 0; i < 8; i++) O.rvals[i] = rv[c_from_linear8[i]];
+  }
+}
+
+// Per (block, channel): 3-bit linear selectors against the cluster's values (absolute error, DXT
+// order first-min) and the selector codebook weight (crn_dxt_hc.cpp:1076-1100); item = a * N + b.
+__global__ void k_alpha_block_selectors(const uint32_t* __restrict__ blocks, uint32_t N, int num_alpha, TileCfg cfg,
+                                        const uint32_t* __restrict__ block_tile, const uint32_t* __restrict__ tile_ac,
+                                        const uint8_t* __restrict__ block_enc, const AlphaCluster* __restrict__ ac,
+                                        uint32_t* __restrict__ item_cluster, float* __restrict__ sel_vec,
+                                        uint32_t* __restrict__ sel_w) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N * (uint32_t)num_alpha) return;
+  const uint32_t a = i / N, b = i - a * N;
+  const uint32_t k = tile_ac[2 * block_tile[b] + a];
+  item_cluster[i] = k;
+  const AlphaCluster& C = ac[k];
+  const float ew = 1.15f + (1.0f - 1.15f) * ((float)block_enc[b] / 7.0f);
+  sel_w[i] = (uint32_t)((float)C.endpoint_weight * ew);
+  for (int p = 0; p < 16; p++) {
+    const int v = (int)((__ldg(blocks + (size_t)b * 16 + p) >> (8 * cfg.comp[a])) & 255u);
+    int bd = 0x7FFFFFFF, bs = 0;
+    for (int t = 0; t < 8; t++) {
+      const int s = c_to_linear8[t];
+      const int d = abs(v - C.vals[s]);
+      if (d < bd) { bd = d; bs = s; }
+    }
+    sel_vec[(size_t)i * 16 + p] = ((float)bs + 0.5f) * 0.125f;
+  }
+}
+
+__global__ void k_alpha_selector_quantise(const float* __restrict__ cb, uint32_t K, unsigned long long* __restrict__ sel) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K) return;
+  unsigned long long s = 0;
+  for (int j = 0; j < 16; j++) s |= (unsigned long long)min(7, max(0, (int)(cb[(size_t)i * 16 + j] * 8.0f))) << (3 * j);
+  sel[i] = s;
+}
+
+// Best alpha selector-codebook entry per (block, channel) through E3/E6 tables
+// (create_alpha_selector_codebook_task, :1516-1580); per-entry tables accumulate with the final
+// (refined) values. One warp per item.
+constexpr int kASelWarps = 8;
+__global__ void __launch_bounds__(kASelWarps * 32) k_alpha_selector_assign(
+    const uint32_t* __restrict__ blocks, uint32_t N, int num_alpha, TileCfg cfg, const uint32_t* __restrict__ item_cluster,
+    const AlphaCluster* __restrict__ ac, const unsigned long long* __restrict__ cbsel, uint32_t K,
+    uint32_t* __restrict__ item_sel, unsigned long long* __restrict__ entry_err /* K x 128 */) {
+  __shared__ uint32_t s_E6[kASelWarps][8][64];
+  __shared__ uint32_t s_E3[kASelWarps][16][8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t i = blockIdx.x * kASelWarps + warp;
+  if (i >= N * (uint32_t)num_alpha) return;
+  const uint32_t a = i / N, b = i - a * N;
+  const AlphaCluster& C = ac[item_cluster[i]];
+  for (int q = lane; q < 128; q += 32) {
+    const int p = q >> 3, sidx = q & 7;
+    const int v = (int)((__ldg(blocks + (size_t)b * 16 + p) >> (8 * cfg.comp[a])) & 255u);
+    s_E3[warp][p][sidx] = (uint32_t)((v - C.vals[sidx]) * (v - C.vals[sidx]));
+  }
+  __syncwarp();
+  for (int q = lane; q < 512; q += 32) {
+    const int p = q >> 6, sv = q & 63;
+    s_E6[warp][p][sv] = s_E3[warp][2 * p][sv & 7] + s_E3[warp][2 * p + 1][sv >> 3];
+  }
+  __syncwarp();
+  uint32_t best = 0xFFFFFFFFu, bi = 0;
+  for (uint32_t e = lane; e < K; e += 32) {
+    const unsigned long long sel = __ldg(cbsel + e);
+    uint32_t er = 0;
+#pragma unroll
+    for (int p = 0; p < 8; p++) er += s_E6[warp][p][(sel >> (6 * p)) & 63];
+    if (er < best) { best = er; bi = e; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const uint32_t ob = __shfl_xor_sync(0xFFFFFFFFu, best, o), oi = __shfl_xor_sync(0xFFFFFFFFu, bi, o);
+    if (ob < best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+  }
+  if (lane == 0) item_sel[i] = bi;
+  for (int q = lane; q < 128; q += 32) {
+    const int p = q >> 3, sidx = q & 7;
+    const int v = (int)((__ldg(blocks + (size_t)b * 16 + p) >> (8 * cfg.comp[a])) & 255u);
+    atomicAdd(entry_err + (size_t)bi * 128 + q, (unsigned long long)((v - C.rvals[sidx]) * (v - C.rvals[sidx])));
+  }
+}
+
+// per entry: each pixel's selector minimising the accumulated error (crn_dxt_hc.cpp:1700-1715)
+__global__ void k_alpha_selector_finalise(const unsigned long long* __restrict__ entry_err, uint32_t K,
+                                          unsigned long long* __restrict__ sel) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K) return;
+  unsigned long long s = 0;
+  for (int p = 0; p < 16; p++) {
+    const unsigned long long* e = entry_err + (size_t)i * 128 + p * 8;
+    const int s07 = e[7] < e[0] ? 7 : 0, s12 = e[2] < e[1] ? 2 : 1, s34 = e[4] < e[3] ? 4 : 3, s56 = e[6] < e[5] ? 6 : 5;
+    const int s02 = e[s12] < e[s07] ? s12 : s07, s36 = e[s56] < e[s34] ? s56 : s34;
+    s |= (unsigned long long)(e[s36] < e[s02] ? s36 : s02) << (3 * p);
+  }
+  sel[i] = s;
+}
+
+// finished alpha blocks: endpoints + codebook selectors (linear -> DXT5 order) at byte offset
+// 8 * slot of each output block; squared error of the result into *sse
+__global__ void k_alpha_emit(const uint32_t* __restrict__ blocks, uint32_t N, int num_alpha, TileCfg cfg,
+                             const uint32_t* __restrict__ item_cluster, const AlphaCluster* __restrict__ ac,
+                             const uint32_t* __restrict__ item_sel, const unsigned long long* __restrict__ cbsel,
+                             uint8_t* __restrict__ out, uint32_t bpb, int slot0, unsigned long long* __restrict__ sse) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N * (uint32_t)num_alpha) return;
+  const uint32_t a = i / N, b = i - a * N;
+  const AlphaCluster& C = ac[item_cluster[i]];
+  const unsigned long long lin = cbsel[item_sel[i]];
+  unsigned long long dxt = 0;
+  uint32_t err = 0;
+  for (int p = 0; p < 16; p++) {
+    const uint32_t l = (uint32_t)((lin >> (3 * p)) & 7);
+    dxt |= (unsigned long long)c_from_linear8[l] << (3 * p);
+    const int v = (int)((__ldg(blocks + (size_t)b * 16 + p) >> (8 * cfg.comp[a])) & 255u);
+    err += (uint32_t)((v - C.rvals[l]) * (v - C.rvals[l]));
+  }
+  uint8_t* o = out + (size_t)b * bpb + 8 * (slot0 + (int)a);
+  o[0] = (uint8_t)C.first;
+  o[1] = (uint8_t)C.second;
+  for (int k = 0; k < 6; k++) o[2 + k] = (uint8_t)(dxt >> (8 * k));
+  atomicAdd(sse, (unsigned long long)err);
+}
+
 }  // namespace hc
 
 const void* single_colour_tables_host();
@@ -1520,7 +2036,8 @@ namespace {
 struct HcBuffers {
   DevBuf chunks, derating, lweight, st, tiles, block_tile, block_enc, vec6, w6, count, cb6, tile_cluster, ccount,
       cstart, clist, clusters, bweight, block_cluster, selvec, selw, cb16, cbsel, block_sel, entry_err, entry_used,
-      levels, flags, iota, used, keys, keys2, cub_tmp, sse;
+      levels, flags, iota, used, keys, keys2, cub_tmp, sse, avec, aw, aitems, tile_ac, cb2, acount, alist, astart,
+      aclusters, aitem_cluster, aselvec, aselw, acb16, acbsel, aitem_sel, aentry_err;
 };
 
 }  // namespace
@@ -1530,30 +2047,38 @@ struct HcBuffers {
 using namespace crngpu;
 using namespace crngpu::hc;
 
-// Clustered DXT1 encode (dxt_hc::compress for cDXT1). See include/crngpu.h.
-extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_params* params, uint8_t* d_out,
-                                       uint16_t* d_endpoint_idx, uint16_t* d_selector_idx, uint32_t* d_endpoints,
-                                       uint32_t* d_selectors, crngpu_hc_stats* stats, void* stream) {
-  clear_error();
-  if (!d_blocks || !params || !d_out || params->struct_size != sizeof(crngpu_hc_params) || !params->num_blocks ||
-      params->num_levels < 1 || params->num_levels > 16) {
-    set_error("crngpu_hc_compress_dxt1: bad arguments");
-    return CRNGPU_E_PARAM;
-  }
-  const crngpu_hc_params& P = *params;
+namespace crngpu {
+namespace {
+
+// dxt_hc::compress (crnlib/crn_dxt_hc.cpp:97-316) for DXT1, DXT5, DXN_XY/YX and DXT5A.
+int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_t format, uint8_t* d_out,
+                     uint16_t* d_endpoint_idx, uint16_t* d_selector_idx, uint32_t* d_endpoints, uint32_t* d_selectors,
+                     crngpu_hc_stats* stats, cudaStream_t s) {
   const uint32_t N = P.num_blocks;
-  cudaStream_t s = as_stream(stream);
   cudaError_t e;
   HcBuffers B;
+  TileCfg cfg{};
+  uint32_t bpb = 8, color_ofs = 0;
+  int alpha_slot0 = 0;
+  switch (format) {
+    case CRNGPU_FMT_DXT1: cfg.has_color = 1; cfg.num_alpha = 0; break;
+    case CRNGPU_FMT_DXT5: cfg.has_color = 1; cfg.num_alpha = 1; cfg.comp[0] = (int)(P.alpha_component & 3); bpb = 16; color_ofs = 8; break;
+    case CRNGPU_FMT_DXN_XY: cfg.num_alpha = 2; cfg.comp[0] = 0; cfg.comp[1] = 1; bpb = 16; break;
+    case CRNGPU_FMT_DXN_YX: cfg.num_alpha = 2; cfg.comp[0] = 1; cfg.comp[1] = 0; bpb = 16; break;
+    case CRNGPU_FMT_DXT5A: cfg.num_alpha = 1; cfg.comp[0] = (int)(P.alpha_component & 3); break;
+    default: set_error("clustered compression supports DXT1, DXT5, DXN_XY/YX and DXT5A"); return CRNGPU_E_UNSUPPORTED;
+  }
+  cfg.ratio = P.color_alpha_weighting_ratio > 0.f ? P.color_alpha_weighting_ratio : 3.0f;
+  const int tile_derating[8] = {0, 1, 1, 2, 2, 2, 2, 3};
+  for (int k = 0; k < 8; k++) cfg.alpha_derating[k] = P.adaptive_tile_alpha_psnr_derating * ((float)tile_derating[k] / 3.0f);
   // chunks of every level (block rows are processed in pairs; widths and heights are even)
   std::vector<Chunk> chunks;
   std::vector<float> derating(16 * 8), lweight(16);
-  const int tile_derating[8] = {0, 1, 1, 2, 2, 2, 2, 3};
   std::vector<Level> lv(P.num_levels);
   for (uint32_t l = 0; l < P.num_levels; l++) {
     const auto& L = P.levels[l];
     if (!L.block_width || (L.block_width & 1) || L.num_blocks % (2 * L.block_width) || L.first_block + L.num_blocks > N) {
-      set_error("crngpu_hc_compress_dxt1: level " + std::to_string(l) + " is not a whole number of 2x2 chunks");
+      set_error("clustered compression: level " + std::to_string(l) + " is not a whole number of 2x2 chunks");
       return CRNGPU_E_PARAM;
     }
     lv[l] = Level{L.first_block, L.num_blocks, L.block_width, L.weight};
@@ -1586,23 +2111,20 @@ extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_
   Tile* tiles = static_cast<Tile*>(B.tiles.ptr);
   k_hc_tiles<<<(nchunks + 63) / 64, 64, 0, s>>>(blocks, static_cast<Chunk*>(B.chunks.ptr), nchunks,
                                                  static_cast<float*>(B.derating.ptr), static_cast<float*>(B.lweight.ptr),
-                                                 P.perceptual, static_cast<SolidTables*>(B.st.ptr), tiles,
+                                                 P.perceptual, static_cast<SolidTables*>(B.st.ptr), cfg, tiles,
                                                  static_cast<uint32_t*>(B.block_tile.ptr), static_cast<uint8_t*>(B.block_enc.ptr));
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_hc_tiles");
-  // endpoint VQ over the used tiles' vec6 (compacted in tile order, so the result is reproducible)
-  if ((e = B.vec6.ensure(sizeof(float) * 6 * ntiles)) != cudaSuccess || (e = B.w6.ensure(4 * ntiles)) != cudaSuccess ||
-      (e = B.count.ensure(16)) != cudaSuccess || (e = B.flags.ensure(ntiles)) != cudaSuccess ||
+  // the used tiles, compacted in tile order (so the result is reproducible)
+  if ((e = B.count.ensure(16)) != cudaSuccess || (e = B.flags.ensure(ntiles)) != cudaSuccess ||
       (e = B.iota.ensure(4 * ntiles)) != cudaSuccess || (e = B.used.ensure(4 * ntiles)) != cudaSuccess ||
-      (e = B.keys.ensure(4 * ntiles)) != cudaSuccess || (e = B.keys2.ensure(4 * ntiles)) != cudaSuccess)
-    return cuda_check(e, "alloc vq input");
+      (e = B.keys.ensure(8 * ntiles)) != cudaSuccess || (e = B.keys2.ensure(8 * ntiles)) != cudaSuccess)
+    return cuda_check(e, "alloc tile lists");
   k_tile_flags<<<(ntiles + 255) / 256, 256, 0, s>>>(tiles, ntiles, static_cast<uint8_t*>(B.flags.ptr),
                                                      static_cast<uint32_t*>(B.iota.ptr));
-  size_t tmp_bytes = 0, tmp2 = 0;
+  size_t tmp_bytes = 0;
   cub::DeviceSelect::Flagged(nullptr, tmp_bytes, static_cast<uint32_t*>(B.iota.ptr), static_cast<uint8_t*>(B.flags.ptr),
                              static_cast<uint32_t*>(B.used.ptr), static_cast<uint32_t*>(B.count.ptr), (int)ntiles, s);
-  cub::DeviceRadixSort::SortPairs(nullptr, tmp2, static_cast<uint32_t*>(B.keys.ptr), static_cast<uint32_t*>(B.keys2.ptr),
-                                  static_cast<uint32_t*>(B.used.ptr), static_cast<uint32_t*>(B.iota.ptr), (int)ntiles, 0, 32, s);
-  if ((e = B.cub_tmp.ensure(std::max(tmp_bytes, tmp2) + 256)) != cudaSuccess) return cuda_check(e, "alloc cub scratch");
+  if ((e = B.cub_tmp.ensure(tmp_bytes + 256)) != cudaSuccess) return cuda_check(e, "alloc cub scratch");
   tmp_bytes = B.cub_tmp.cap;
   if ((e = cub::DeviceSelect::Flagged(B.cub_tmp.ptr, tmp_bytes, static_cast<uint32_t*>(B.iota.ptr),
                                       static_cast<uint8_t*>(B.flags.ptr), static_cast<uint32_t*>(B.used.ptr),
@@ -1611,115 +2133,225 @@ extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_
   uint32_t nused = 0;
   if ((e = cudaMemcpyAsync(&nused, B.count.ptr, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read count");
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
-  k_tile_vectors<<<(nused + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused,
-                                                      static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr));
-  uint32_t K = 0;
   const uint32_t frac = P.vq_round_fraction ? P.vq_round_fraction : kDefaultRoundFraction;
-  int rc = tree_vq<6>(static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr), nused,
-                      std::min(nused, P.color_endpoint_codebook_size), frac, B.cb6, &K, s);
-  if (rc != CRNGPU_OK) return rc;
-  if ((e = B.tile_cluster.ensure(4 * ntiles)) != cudaSuccess) return cuda_check(e, "alloc tile clusters");
-  k_nearest_vec6<<<(ntiles + 255) / 256, 256, 0, s>>>(tiles, ntiles, static_cast<float*>(B.cb6.ptr), K,
-                                                       static_cast<uint32_t*>(B.tile_cluster.ptr));
-  // cluster -> tiles (CSR): used tiles sorted by cluster (stable radix sort keeps tile order)
-  if ((e = B.ccount.ensure(4 * (K + 1))) != cudaSuccess || (e = B.cstart.ensure(4 * (K + 1))) != cudaSuccess ||
-      (e = B.clist.ensure(4 * ntiles)) != cudaSuccess)
-    return cuda_check(e, "alloc cluster lists");
-  cudaMemsetAsync(B.ccount.ptr, 0, 4 * (K + 1), s);
-  k_count_clusters<<<(ntiles + 255) / 256, 256, 0, s>>>(static_cast<uint32_t*>(B.tile_cluster.ptr), ntiles,
-                                                         static_cast<uint32_t*>(B.ccount.ptr));
-  k_used_clusters<<<(nused + 255) / 256, 256, 0, s>>>(static_cast<uint32_t*>(B.used.ptr), nused,
-                                                       static_cast<uint32_t*>(B.tile_cluster.ptr), static_cast<uint32_t*>(B.keys.ptr));
-  int key_bits = 1;
-  while ((1u << key_bits) < K) key_bits++;
-  tmp_bytes = 0;
-  cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, static_cast<uint32_t*>(B.keys.ptr), static_cast<uint32_t*>(B.keys2.ptr),
-                                  static_cast<uint32_t*>(B.used.ptr), static_cast<uint32_t*>(B.clist.ptr), (int)nused, 0,
-                                  key_bits, s);
-  if ((e = B.cub_tmp.ensure(tmp_bytes + 256)) != cudaSuccess) return cuda_check(e, "alloc cub scratch");
-  tmp_bytes = B.cub_tmp.cap;
-  if ((e = cub::DeviceRadixSort::SortPairs(B.cub_tmp.ptr, tmp_bytes, static_cast<uint32_t*>(B.keys.ptr),
-                                           static_cast<uint32_t*>(B.keys2.ptr), static_cast<uint32_t*>(B.used.ptr),
-                                           static_cast<uint32_t*>(B.clist.ptr), (int)nused, 0, key_bits, s)) != cudaSuccess)
-    return cuda_check(e, "sort tiles by cluster");
-  std::vector<uint32_t> cnt(K + 1), start(K + 1);
-  if ((e = cudaMemcpyAsync(cnt.data(), B.ccount.ptr, 4 * K, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read counts");
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
-  uint32_t run = 0;
-  for (uint32_t k = 0; k < K; k++) { start[k] = run; run += cnt[k]; }
-  start[K] = run;
-  if ((e = cudaMemcpyAsync(B.cstart.ptr, start.data(), 4 * (K + 1), cudaMemcpyHostToDevice, s)) != cudaSuccess)
-    return cuda_check(e, "copy cluster starts");
-  if ((e = B.clusters.ensure(sizeof(ClusterOut) * K)) != cudaSuccess) return cuda_check(e, "alloc clusters");
-  ClusterOut* cl = static_cast<ClusterOut*>(B.clusters.ptr);
-  k_cluster_fit<<<K, kFitThreads, 0, s>>>(blocks, static_cast<Chunk*>(B.chunks.ptr), tiles,
-                                           static_cast<uint32_t*>(B.cstart.ptr), static_cast<uint32_t*>(B.clist.ptr),
-                                           P.perceptual, cl);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_cluster_fit");
-  // per-block selectors and weights -> selector VQ
-  if ((e = B.bweight.ensure(4 * N)) != cudaSuccess || (e = B.block_cluster.ensure(4 * N)) != cudaSuccess ||
-      (e = B.selvec.ensure(sizeof(float) * 16 * N)) != cudaSuccess || (e = B.selw.ensure(4 * N)) != cudaSuccess)
-    return cuda_check(e, "alloc selectors");
-  if ((e = B.sse.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc sse");
-  cudaMemsetAsync(B.sse.ptr, 0, 16, s);
+  if ((e = B.sse.ensure(32)) != cudaSuccess) return cuda_check(e, "alloc sse");
+  cudaMemsetAsync(B.sse.ptr, 0, 32, s);
+  // sorts `n` (key, value) pairs with keys below 2^bits (stable: equal keys keep value order)
+  auto sort_pairs = [&](uint32_t* keys, uint32_t* keys_out, uint32_t* vals, uint32_t* vals_out, uint32_t n,
+                        int bits) -> int {
+    size_t need = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, need, keys, keys_out, vals, vals_out, (int)n, 0, bits, s);
+    cudaError_t r = B.cub_tmp.ensure(need + 256);
+    if (r != cudaSuccess) return cuda_check(r, "alloc cub scratch");
+    size_t have = B.cub_tmp.cap;
+    r = cub::DeviceRadixSort::SortPairs(B.cub_tmp.ptr, have, keys, keys_out, vals, vals_out, (int)n, 0, bits, s);
+    return r == cudaSuccess ? CRNGPU_OK : cuda_check(r, "radix sort");
+  };
+  // CSR starts from per-cluster counts (device) -> start (device), host round trip of K words
+  auto csr_starts = [&](DevBuf& counts, DevBuf& starts, uint32_t K) -> int {
+    std::vector<uint32_t> cnt(K + 1), st(K + 1);
+    cudaError_t r = cudaMemcpyAsync(cnt.data(), counts.ptr, 4 * K, cudaMemcpyDeviceToHost, s);
+    if (r != cudaSuccess) return cuda_check(r, "read counts");
+    if ((r = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(r, "sync");
+    uint32_t run = 0;
+    for (uint32_t k = 0; k < K; k++) { st[k] = run; run += cnt[k]; }
+    st[K] = run;
+    if ((r = starts.ensure(4 * (K + 1))) != cudaSuccess) return cuda_check(r, "alloc starts");
+    r = cudaMemcpyAsync(starts.ptr, st.data(), 4 * (K + 1), cudaMemcpyHostToDevice, s);
+    return r == cudaSuccess ? CRNGPU_OK : cuda_check(r, "copy starts");
+  };
+  uint32_t K = 0, KS = 0, KA = 0, KAS = 0;
+  int rc;
+  if ((e = B.bweight.ensure(4 * N)) != cudaSuccess) return cuda_check(e, "alloc block weights");
   k_block_weights<<<(N + 255) / 256, 256, 0, s>>>(static_cast<Level*>(B.levels.ptr), P.num_levels, N, static_cast<float*>(B.bweight.ptr));
-  k_block_selectors<<<(N + 127) / 128, 128, 0, s>>>(blocks, N, static_cast<uint32_t*>(B.block_tile.ptr),
-                                                     static_cast<uint32_t*>(B.tile_cluster.ptr),
-                                                     static_cast<uint8_t*>(B.block_enc.ptr), static_cast<float*>(B.bweight.ptr),
-                                                     cl, P.perceptual, static_cast<uint32_t*>(B.block_cluster.ptr),
-                                                     static_cast<float*>(B.selvec.ptr), static_cast<uint32_t*>(B.selw.ptr),
-                                                     static_cast<unsigned long long*>(B.sse.ptr));
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_block_selectors");
-  uint32_t KS = 0;
-  rc = tree_vq<16>(static_cast<float*>(B.selvec.ptr), static_cast<uint32_t*>(B.selw.ptr), N,
-                   std::min(N, P.color_selector_codebook_size), frac, B.cb16, &KS, s);
-  if (rc != CRNGPU_OK) return rc;
-  if ((e = B.cbsel.ensure(4 * KS)) != cudaSuccess || (e = B.block_sel.ensure(4 * N)) != cudaSuccess ||
-      (e = B.entry_err.ensure(8 * 64 * (size_t)KS)) != cudaSuccess || (e = B.entry_used.ensure(4 * KS)) != cudaSuccess)
-    return cuda_check(e, "alloc selector codebook");
-  uint32_t* cbsel = static_cast<uint32_t*>(B.cbsel.ptr);
-  k_selector_quantise<<<(KS + 255) / 256, 256, 0, s>>>(static_cast<float*>(B.cb16.ptr), KS, cbsel);
-  cudaMemsetAsync(B.entry_err.ptr, 0, 8 * 64 * (size_t)KS, s);
-  cudaMemsetAsync(B.entry_used.ptr, 0, 4 * KS, s);
-  k_selector_assign<<<(N + kSelWarps - 1) / kSelWarps, kSelWarps * 32, 0, s>>>(
-      blocks, N, static_cast<uint32_t*>(B.block_cluster.ptr), cl, P.perceptual, cbsel, KS,
-      static_cast<uint32_t*>(B.block_sel.ptr), static_cast<unsigned long long*>(B.entry_err.ptr),
-      static_cast<uint32_t*>(B.entry_used.ptr));
-  k_selector_finalise<<<(KS + 255) / 256, 256, 0, s>>>(static_cast<unsigned long long*>(B.entry_err.ptr), KS, cbsel);
-  k_hc_emit<<<(N + 255) / 256, 256, 0, s>>>(blocks, N, static_cast<uint32_t*>(B.block_cluster.ptr), cl,
-                                            static_cast<uint32_t*>(B.block_sel.ptr), cbsel, reinterpret_cast<uint2*>(d_out),
-                                            static_cast<unsigned long long*>(B.sse.ptr) + 1);
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch hc selector kernels");
-  // optional index outputs
-  if (d_endpoint_idx || d_selector_idx || d_endpoints || d_selectors) {
-    std::vector<uint32_t> bc(N), bs(N);
-    std::vector<ClusterOut> hcl(K);
-    if ((e = cudaMemcpyAsync(bc.data(), B.block_cluster.ptr, 4 * N, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(bs.data(), B.block_sel.ptr, 4 * N, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(hcl.data(), cl, sizeof(ClusterOut) * K, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-      return cuda_check(e, "read indices");
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
-    std::vector<uint16_t> ei(N), si(N);
-    std::vector<uint32_t> eps(K);
-    for (uint32_t k = 0; k < K; k++) eps[k] = hcl[k].first | (hcl[k].second << 16);
-    for (uint32_t b = 0; b < N; b++) { ei[b] = (uint16_t)bc[b]; si[b] = (uint16_t)bs[b]; }
-    if (d_endpoint_idx) cudaMemcpyAsync(d_endpoint_idx, ei.data(), 2 * N, cudaMemcpyHostToDevice, s);
-    if (d_selector_idx) cudaMemcpyAsync(d_selector_idx, si.data(), 2 * N, cudaMemcpyHostToDevice, s);
-    if (d_endpoints) cudaMemcpyAsync(d_endpoints, eps.data(), 4 * K, cudaMemcpyHostToDevice, s);
-    if (d_selectors) cudaMemcpyAsync(d_selectors, cbsel, 4 * KS, cudaMemcpyDeviceToDevice, s);
+  if (cfg.has_color) {
+    // colour endpoint VQ over the used tiles' vec6
+    if ((e = B.vec6.ensure(sizeof(float) * 6 * ntiles)) != cudaSuccess || (e = B.w6.ensure(4 * ntiles)) != cudaSuccess)
+      return cuda_check(e, "alloc vq input");
+    k_tile_vectors<<<(nused + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused,
+                                                        static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr));
+    if ((rc = tree_vq<6>(static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr), nused,
+                         std::min(nused, P.color_endpoint_codebook_size), frac, B.cb6, &K, s)) != CRNGPU_OK)
+      return rc;
+    if ((e = B.tile_cluster.ensure(4 * ntiles)) != cudaSuccess) return cuda_check(e, "alloc tile clusters");
+    k_nearest_vec6<<<(ntiles + 255) / 256, 256, 0, s>>>(tiles, ntiles, static_cast<float*>(B.cb6.ptr), K,
+                                                         static_cast<uint32_t*>(B.tile_cluster.ptr));
+    // cluster -> tiles (CSR): used tiles sorted by cluster (stable radix sort keeps tile order)
+    if ((e = B.ccount.ensure(4 * (K + 1))) != cudaSuccess || (e = B.clist.ensure(4 * ntiles)) != cudaSuccess)
+      return cuda_check(e, "alloc cluster lists");
+    cudaMemsetAsync(B.ccount.ptr, 0, 4 * (K + 1), s);
+    k_count_clusters<<<(ntiles + 255) / 256, 256, 0, s>>>(static_cast<uint32_t*>(B.tile_cluster.ptr), ntiles,
+                                                           static_cast<uint32_t*>(B.ccount.ptr));
+    k_used_clusters<<<(nused + 255) / 256, 256, 0, s>>>(static_cast<uint32_t*>(B.used.ptr), nused,
+                                                         static_cast<uint32_t*>(B.tile_cluster.ptr), static_cast<uint32_t*>(B.keys.ptr));
+    int key_bits = 1;
+    while ((1u << key_bits) < K) key_bits++;
+    if ((rc = sort_pairs(static_cast<uint32_t*>(B.keys.ptr), static_cast<uint32_t*>(B.keys2.ptr),
+                         static_cast<uint32_t*>(B.used.ptr), static_cast<uint32_t*>(B.clist.ptr), nused, key_bits)) != CRNGPU_OK)
+      return rc;
+    if ((rc = csr_starts(B.ccount, B.cstart, K)) != CRNGPU_OK) return rc;
+    if ((e = B.clusters.ensure(sizeof(ClusterOut) * K)) != cudaSuccess) return cuda_check(e, "alloc clusters");
+    ClusterOut* cl = static_cast<ClusterOut*>(B.clusters.ptr);
+    k_cluster_fit<<<K, kFitThreads, 0, s>>>(blocks, static_cast<Chunk*>(B.chunks.ptr), tiles,
+                                             static_cast<uint32_t*>(B.cstart.ptr), static_cast<uint32_t*>(B.clist.ptr),
+                                             P.perceptual, cl);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_cluster_fit");
+    // per-block selectors and weights -> selector VQ
+    if ((e = B.block_cluster.ensure(4 * N)) != cudaSuccess || (e = B.selvec.ensure(sizeof(float) * 16 * N)) != cudaSuccess ||
+        (e = B.selw.ensure(4 * N)) != cudaSuccess)
+      return cuda_check(e, "alloc selectors");
+    k_block_selectors<<<(N + 127) / 128, 128, 0, s>>>(blocks, N, static_cast<uint32_t*>(B.block_tile.ptr),
+                                                       static_cast<uint32_t*>(B.tile_cluster.ptr),
+                                                       static_cast<uint8_t*>(B.block_enc.ptr), static_cast<float*>(B.bweight.ptr),
+                                                       cl, P.perceptual, static_cast<uint32_t*>(B.block_cluster.ptr),
+                                                       static_cast<float*>(B.selvec.ptr), static_cast<uint32_t*>(B.selw.ptr),
+                                                       static_cast<unsigned long long*>(B.sse.ptr));
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_block_selectors");
+    if ((rc = tree_vq<16>(static_cast<float*>(B.selvec.ptr), static_cast<uint32_t*>(B.selw.ptr), N,
+                          std::min(N, P.color_selector_codebook_size), frac, B.cb16, &KS, s)) != CRNGPU_OK)
+      return rc;
+    if ((e = B.cbsel.ensure(4 * KS)) != cudaSuccess || (e = B.block_sel.ensure(4 * N)) != cudaSuccess ||
+        (e = B.entry_err.ensure(8 * 64 * (size_t)KS)) != cudaSuccess || (e = B.entry_used.ensure(4 * KS)) != cudaSuccess)
+      return cuda_check(e, "alloc selector codebook");
+    uint32_t* cbsel = static_cast<uint32_t*>(B.cbsel.ptr);
+    k_selector_quantise<<<(KS + 255) / 256, 256, 0, s>>>(static_cast<float*>(B.cb16.ptr), KS, cbsel);
+    cudaMemsetAsync(B.entry_err.ptr, 0, 8 * 64 * (size_t)KS, s);
+    cudaMemsetAsync(B.entry_used.ptr, 0, 4 * KS, s);
+    k_selector_assign<<<(N + kSelWarps - 1) / kSelWarps, kSelWarps * 32, 0, s>>>(
+        blocks, N, static_cast<uint32_t*>(B.block_cluster.ptr), cl, P.perceptual, cbsel, KS,
+        static_cast<uint32_t*>(B.block_sel.ptr), static_cast<unsigned long long*>(B.entry_err.ptr),
+        static_cast<uint32_t*>(B.entry_used.ptr));
+    k_selector_finalise<<<(KS + 255) / 256, 256, 0, s>>>(static_cast<unsigned long long*>(B.entry_err.ptr), KS, cbsel);
+    k_hc_emit<<<(N + 255) / 256, 256, 0, s>>>(blocks, N, static_cast<uint32_t*>(B.block_cluster.ptr), cl,
+                                              static_cast<uint32_t*>(B.block_sel.ptr), cbsel, d_out, bpb, color_ofs,
+                                              static_cast<unsigned long long*>(B.sse.ptr) + 1);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch hc selector kernels");
+    // optional index outputs (colour)
+    if (d_endpoint_idx || d_selector_idx || d_endpoints || d_selectors) {
+      std::vector<uint32_t> bc(N), bs(N);
+      std::vector<ClusterOut> hcl(K);
+      if ((e = cudaMemcpyAsync(bc.data(), B.block_cluster.ptr, 4 * N, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(bs.data(), B.block_sel.ptr, 4 * N, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+          (e = cudaMemcpyAsync(hcl.data(), cl, sizeof(ClusterOut) * K, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+        return cuda_check(e, "read indices");
+      if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
+      std::vector<uint16_t> ei(N), si(N);
+      std::vector<uint32_t> eps(K);
+      for (uint32_t k = 0; k < K; k++) eps[k] = hcl[k].first | (hcl[k].second << 16);
+      for (uint32_t b = 0; b < N; b++) { ei[b] = (uint16_t)bc[b]; si[b] = (uint16_t)bs[b]; }
+      if (d_endpoint_idx) cudaMemcpyAsync(d_endpoint_idx, ei.data(), 2 * N, cudaMemcpyHostToDevice, s);
+      if (d_selector_idx) cudaMemcpyAsync(d_selector_idx, si.data(), 2 * N, cudaMemcpyHostToDevice, s);
+      if (d_endpoints) cudaMemcpyAsync(d_endpoints, eps.data(), 4 * K, cudaMemcpyHostToDevice, s);
+      if (d_selectors) cudaMemcpyAsync(d_selectors, cbsel, 4 * KS, cudaMemcpyDeviceToDevice, s);
+      if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
+    }
   }
+  if (cfg.num_alpha) {
+    const uint32_t na = (uint32_t)cfg.num_alpha, nitem_t = nused * na, nitem_b = N * na;
+    // alpha endpoint VQ over the tiles' vec2 (both DXN channels share one codebook)
+    if ((e = B.avec.ensure(sizeof(float) * 2 * nitem_t)) != cudaSuccess || (e = B.aw.ensure(4 * nitem_t)) != cudaSuccess ||
+        (e = B.aitems.ensure(4 * nitem_t)) != cudaSuccess || (e = B.tile_ac.ensure(8 * ntiles)) != cudaSuccess)
+      return cuda_check(e, "alloc alpha vq input");
+    k_alpha_vectors<<<(nitem_t + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused, cfg.num_alpha,
+                                                          static_cast<float*>(B.avec.ptr), static_cast<uint32_t*>(B.aw.ptr),
+                                                          static_cast<uint32_t*>(B.aitems.ptr));
+    if ((rc = tree_vq<2>(static_cast<float*>(B.avec.ptr), static_cast<uint32_t*>(B.aw.ptr), nitem_t,
+                         std::min(nused, P.alpha_endpoint_codebook_size), frac, B.cb2, &KA, s)) != CRNGPU_OK)
+      return rc;
+    k_nearest_vec2<<<(nitem_t + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused, cfg.num_alpha,
+                                                          static_cast<float*>(B.cb2.ptr), KA, static_cast<uint32_t*>(B.tile_ac.ptr));
+    // alpha cluster -> (tile, channel) members
+    if ((e = B.acount.ensure(4 * (KA + 1))) != cudaSuccess || (e = B.alist.ensure(4 * nitem_t)) != cudaSuccess)
+      return cuda_check(e, "alloc alpha lists");
+    cudaMemsetAsync(B.acount.ptr, 0, 4 * (KA + 1), s);
+    k_alpha_keys<<<(nitem_t + 255) / 256, 256, 0, s>>>(static_cast<uint32_t*>(B.aitems.ptr), nitem_t,
+                                                       static_cast<uint32_t*>(B.tile_ac.ptr), static_cast<uint32_t*>(B.keys.ptr),
+                                                       static_cast<uint32_t*>(B.acount.ptr));
+    int key_bits = 1;
+    while ((1u << key_bits) < KA) key_bits++;
+    if ((rc = sort_pairs(static_cast<uint32_t*>(B.keys.ptr), static_cast<uint32_t*>(B.keys2.ptr),
+                         static_cast<uint32_t*>(B.aitems.ptr), static_cast<uint32_t*>(B.alist.ptr), nitem_t, key_bits)) != CRNGPU_OK)
+      return rc;
+    if ((rc = csr_starts(B.acount, B.astart, KA)) != CRNGPU_OK) return rc;
+    if ((e = B.aclusters.ensure(sizeof(AlphaCluster) * KA)) != cudaSuccess) return cuda_check(e, "alloc alpha clusters");
+    AlphaCluster* ac = static_cast<AlphaCluster*>(B.aclusters.ptr);
+    k_alpha_cluster_fit<<<KA, kAFitThreads, 0, s>>>(blocks, static_cast<Chunk*>(B.chunks.ptr), tiles, cfg,
+                                                     static_cast<uint32_t*>(B.astart.ptr), static_cast<uint32_t*>(B.alist.ptr), ac);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_alpha_cluster_fit");
+    // block selectors -> alpha selector VQ -> assignment -> finalise -> emit
+    if ((e = B.aitem_cluster.ensure(4 * nitem_b)) != cudaSuccess || (e = B.aselvec.ensure(sizeof(float) * 16 * nitem_b)) != cudaSuccess ||
+        (e = B.aselw.ensure(4 * nitem_b)) != cudaSuccess)
+      return cuda_check(e, "alloc alpha selectors");
+    k_alpha_block_selectors<<<(nitem_b + 127) / 128, 128, 0, s>>>(
+        blocks, N, cfg.num_alpha, cfg, static_cast<uint32_t*>(B.block_tile.ptr), static_cast<uint32_t*>(B.tile_ac.ptr),
+        static_cast<uint8_t*>(B.block_enc.ptr), ac, static_cast<uint32_t*>(B.aitem_cluster.ptr),
+        static_cast<float*>(B.aselvec.ptr), static_cast<uint32_t*>(B.aselw.ptr));
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_alpha_block_selectors");
+    if ((rc = tree_vq<16>(static_cast<float*>(B.aselvec.ptr), static_cast<uint32_t*>(B.aselw.ptr), nitem_b,
+                          std::min(nitem_b, P.alpha_selector_codebook_size), frac, B.acb16, &KAS, s)) != CRNGPU_OK)
+      return rc;
+    if ((e = B.acbsel.ensure(8 * KAS)) != cudaSuccess || (e = B.aitem_sel.ensure(4 * nitem_b)) != cudaSuccess ||
+        (e = B.aentry_err.ensure(8 * 128 * (size_t)KAS)) != cudaSuccess)
+      return cuda_check(e, "alloc alpha selector codebook");
+    unsigned long long* acbsel = static_cast<unsigned long long*>(B.acbsel.ptr);
+    k_alpha_selector_quantise<<<(KAS + 255) / 256, 256, 0, s>>>(static_cast<float*>(B.acb16.ptr), KAS, acbsel);
+    cudaMemsetAsync(B.aentry_err.ptr, 0, 8 * 128 * (size_t)KAS, s);
+    k_alpha_selector_assign<<<(nitem_b + kASelWarps - 1) / kASelWarps, kASelWarps * 32, 0, s>>>(
+        blocks, N, cfg.num_alpha, cfg, static_cast<uint32_t*>(B.aitem_cluster.ptr), ac, acbsel, KAS,
+        static_cast<uint32_t*>(B.aitem_sel.ptr), static_cast<unsigned long long*>(B.aentry_err.ptr));
+    k_alpha_selector_finalise<<<(KAS + 255) / 256, 256, 0, s>>>(static_cast<unsigned long long*>(B.aentry_err.ptr), KAS, acbsel);
+    k_alpha_emit<<<(nitem_b + 255) / 256, 256, 0, s>>>(blocks, N, cfg.num_alpha, cfg,
+                                                       static_cast<uint32_t*>(B.aitem_cluster.ptr), ac,
+                                                       static_cast<uint32_t*>(B.aitem_sel.ptr), acbsel, d_out, bpb,
+                                                       alpha_slot0, static_cast<unsigned long long*>(B.sse.ptr) + 2);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch alpha selector kernels");
+  }
+  unsigned long long sse[3] = {0, 0, 0};
+  if ((e = cudaMemcpyAsync(sse, B.sse.ptr, 24, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read sse");
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   if (stats) {
-    unsigned long long sse[2] = {0, 0};
-    if ((e = cudaMemcpyAsync(sse, B.sse.ptr, 16, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read sse");
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
     stats->color_endpoints = K;
     stats->color_selectors = KS;
     stats->tiles = nused;
+    stats->alpha_endpoints = KA;
+    stats->alpha_selectors = KAS;
     stats->sse_endpoints = (double)sse[0];
     stats->sse_final = (double)sse[1];
+    stats->sse_alpha = (double)sse[2];
   }
-  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   return CRNGPU_OK;
+}
+
+bool hc_params_ok(const crngpu_hc_params* params) {
+  return params && params->struct_size == sizeof(crngpu_hc_params) && params->num_blocks && params->num_levels >= 1 &&
+         params->num_levels <= 16;
+}
+
+}  // namespace
+}  // namespace crngpu
+
+// Clustered DXT1 encode with the colour codebooks and indices (dxt_hc::compress for cDXT1).
+extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_params* params, uint8_t* d_out,
+                                       uint16_t* d_endpoint_idx, uint16_t* d_selector_idx, uint32_t* d_endpoints,
+                                       uint32_t* d_selectors, crngpu_hc_stats* stats, void* stream) {
+  clear_error();
+  if (!d_blocks || !d_out || !hc_params_ok(params)) {
+    set_error("crngpu_hc_compress_dxt1: bad arguments");
+    return CRNGPU_E_PARAM;
+  }
+  return hc_compress_impl(d_blocks, *params, CRNGPU_FMT_DXT1, d_out, d_endpoint_idx, d_selector_idx, d_endpoints,
+                          d_selectors, stats, as_stream(stream));
+}
+
+// Clustered encode of any supported format (dxt_hc::compress). See include/crngpu.h.
+extern "C" int crngpu_hc_compress(const uint8_t* d_blocks, const crngpu_hc_params* params, uint32_t format,
+                                  uint8_t* d_out, crngpu_hc_stats* stats, void* stream) {
+  clear_error();
+  if (!d_blocks || !d_out || !hc_params_ok(params)) {
+    set_error("crngpu_hc_compress: bad arguments");
+    return CRNGPU_E_PARAM;
+  }
+  return hc_compress_impl(d_blocks, *params, format, d_out, nullptr, nullptr, nullptr, nullptr, stats, as_stream(stream));
 }
 
 // Codebook sizes of crn_comp::quantize_images (crnlib/crn_comp.cpp:541-577) for a quality level.

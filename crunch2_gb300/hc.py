@@ -7,7 +7,7 @@ import ctypes
 
 import numpy as np
 
-from . import lib, _check, CrnGpuError, E_PARAM, FMT_DXT1
+from . import lib, _check, CrnGpuError, E_PARAM, FMT_DXT1, FMT_DXT5, FMT_DXN_XY, FMT_DXN_YX, FMT_DXT5A
 
 
 class HcParams(ctypes.Structure):
@@ -18,13 +18,16 @@ class HcParams(ctypes.Structure):
                 ("num_faces", ctypes.c_uint32), ("perceptual", ctypes.c_int32),
                 ("color_endpoint_codebook_size", ctypes.c_uint32), ("color_selector_codebook_size", ctypes.c_uint32),
                 ("adaptive_tile_color_psnr_derating", ctypes.c_float), ("vq_round_fraction", ctypes.c_uint32),
-                ("levels", _Level * 16)]
+                ("alpha_endpoint_codebook_size", ctypes.c_uint32), ("alpha_selector_codebook_size", ctypes.c_uint32),
+                ("adaptive_tile_alpha_psnr_derating", ctypes.c_float), ("color_alpha_weighting_ratio", ctypes.c_float),
+                ("alpha_component", ctypes.c_uint32), ("levels", _Level * 16)]
 
 
 class HcStats(ctypes.Structure):
     _fields_ = [("color_endpoints", ctypes.c_uint32), ("color_selectors", ctypes.c_uint32),
                 ("tiles", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("sse_endpoints", ctypes.c_double),
-                ("sse_final", ctypes.c_double)]
+                ("sse_final", ctypes.c_double), ("alpha_endpoints", ctypes.c_uint32), ("alpha_selectors", ctypes.c_uint32),
+                ("sse_alpha", ctypes.c_double)]
 
 
 def _bind():
@@ -34,6 +37,8 @@ def _bind():
     vp = ctypes.c_void_p
     L.crngpu_hc_compress_dxt1.argtypes = [vp, ctypes.POINTER(HcParams), vp, vp, vp, vp, vp, ctypes.POINTER(HcStats), vp]
     L.crngpu_hc_compress_dxt1.restype = ctypes.c_int
+    L.crngpu_hc_compress.argtypes = [vp, ctypes.POINTER(HcParams), ctypes.c_uint32, vp, ctypes.POINTER(HcStats), vp]
+    L.crngpu_hc_compress.restype = ctypes.c_int
     L.crngpu_hc_codebook_sizes.argtypes = [ctypes.c_uint32] * 4 + [ctypes.POINTER(ctypes.c_uint32)]
     L.crngpu_hc_codebook_sizes.restype = ctypes.c_int
     L._hc_bound = True
@@ -124,4 +129,57 @@ def compress_dxt1(faces_levels, quality: int = 128, perceptual: bool = True, str
              "rmse_final_all_blocks": (st.sse_final / (n * 48)) ** 0.5}
     if with_indices:
         return res, stats, {k: v.cpu().numpy() for k, v in idx.items()}
+    return res, stats
+
+
+def _params(blocks, levels, nfaces, perceptual, sizes, vq_round_fraction=0, alpha_component=3):
+    p = HcParams()
+    p.struct_size = ctypes.sizeof(HcParams)
+    p.num_blocks = blocks.shape[0]
+    p.num_levels = len(levels)
+    p.num_faces = nfaces
+    p.perceptual = int(perceptual)
+    p.color_endpoint_codebook_size, p.color_selector_codebook_size = sizes[0], sizes[1]
+    p.alpha_endpoint_codebook_size, p.alpha_selector_codebook_size = sizes[2], sizes[3]
+    p.adaptive_tile_color_psnr_derating = 2.0
+    p.adaptive_tile_alpha_psnr_derating = 2.0
+    p.color_alpha_weighting_ratio = 3.0
+    p.alpha_component = alpha_component
+    p.vq_round_fraction = vq_round_fraction
+    for i, (fb, nb, bw) in enumerate(levels):
+        p.levels[i].first_block, p.levels[i].num_blocks, p.levels[i].block_width = fb, nb, bw
+        p.levels[i].weight = min(12.0, 1.3 ** i)
+    return p
+
+
+def compress(faces_levels, fmt: int, quality: int = 128, perceptual=None, stream=None, codebook=None,
+             vq_round_fraction: int = 0, alpha_component: int = 3):
+    """Clustered encode (crn_comp's dxt_hc stage) of a mip chain in DXT1, DXT5, DXN_XY/YX or DXT5A.
+    perceptual defaults to crn_comp's choice (on for DXT1/DXT5, off for DXN/DXT5A). Returns (per
+    level, per face, the visible blocks (by, bx, bytes per block)), stats dict)."""
+    import torch
+    L = _bind()
+    blocks, levels, vis = crn_layout(faces_levels)
+    h0, w0 = faces_levels[0][0].shape[:2]
+    sizes = codebook if codebook else codebook_sizes(w0, h0, quality, fmt)
+    if perceptual is None:
+        perceptual = fmt in (FMT_DXT1, FMT_DXT5)
+    p = _params(blocks, levels, len(faces_levels), perceptual, sizes, vq_round_fraction, alpha_component)
+    bpb = 8 if fmt in (FMT_DXT1, FMT_DXT5A) else 16
+    d_blocks = torch.from_numpy(blocks).cuda()
+    n = blocks.shape[0]
+    out = torch.empty((n, bpb), dtype=torch.uint8, device="cuda")
+    st = HcStats()
+    sp = None if stream is None else getattr(stream, "cuda_stream", stream)
+    _check(L.crngpu_hc_compress(d_blocks.data_ptr(), ctypes.byref(p), fmt, out.data_ptr(), ctypes.byref(st), sp),
+           "crngpu_hc_compress")
+    host = out.cpu().numpy()
+    res = []
+    for (fb, nb, bw), (bx, by, _) in zip(levels, vis):
+        per_face = nb // len(faces_levels)
+        res.append([host[fb + f * per_face: fb + (f + 1) * per_face].reshape(-1, bw, bpb)[:by, :bx]
+                    for f in range(len(faces_levels))])
+    stats = {"color_endpoints": st.color_endpoints, "color_selectors": st.color_selectors, "tiles": st.tiles,
+             "alpha_endpoints": st.alpha_endpoints, "alpha_selectors": st.alpha_selectors,
+             "codebook_request": tuple(sizes), "blocks": n}
     return res, stats

@@ -147,11 +147,18 @@ def make_targets(d_blocks, perceptual: bool = True, stream=None):
     return t, plain
 
 
-def training_blocks(n_textures: int, size: int, seed0: int, device="cuda"):
-    """Blocks of seeded config-0-style textures generated on the GPU."""
+def training_blocks(n_textures: int, size: int, seed0: int, device="cuda", mips: bool = False):
+    """Blocks of seeded config-0-style textures generated on the GPU; with mips, also the blocks of
+    every box-filtered mip level down to 4x4 (mip chains are what real textures are encoded as)."""
     import torch
-    from .texgen import colour_texture_torch, image_blocks_torch
-    parts = [image_blocks_torch(colour_texture_torch(size, size, seed0 + i, device)) for i in range(n_textures)]
+    from .texgen import colour_texture_torch, image_blocks_torch, box_mip_torch
+    parts = []
+    for i in range(n_textures):
+        img = colour_texture_torch(size, size, seed0 + i, device)
+        parts.append(image_blocks_torch(img))
+        while mips and img.shape[0] >= 8 and img.shape[1] >= 8:
+            img = box_mip_torch(img)
+            parts.append(image_blocks_torch(img))
     return torch.cat(parts)
 
 
@@ -205,7 +212,7 @@ def rgb_rmse_torch(blocks8, pixels):
 
 
 def config4(train_textures=64, train_size=2048, eval_textures=32, eval_size=4096, steps=2048, batch=8192,
-            lr=1e-3, threshold=1.5, log_every=256, seed=0, weights=None, tau=0.0, bound_weight=1.0):
+            lr=1e-3, threshold=1.5, log_every=256, seed=0, weights=None, tau=0.0, bound_weight=1.0, mips=0):
     """Learned endpoint proposal end to end: GPU-labelled training set, GPU training, and learned
     vs plain DXT1 encode on held-out textures (different seed range). `threshold` may be a list
     (or a comma-separated string) to report several fallback thresholds from one trained net;
@@ -224,7 +231,8 @@ def config4(train_textures=64, train_size=2048, eval_textures=32, eval_size=4096
         res["weights"] = str(weights)
     else:
         t0 = time.perf_counter()
-        train_blocks = training_blocks(train_textures, train_size, seed0=1000)
+        train_blocks = training_blocks(train_textures, train_size, seed0=1000, mips=bool(mips))
+        n_train = int(train_blocks.shape[0])
         targets, _ = make_targets(train_blocks)
         torch.cuda.synchronize()
         t_label = time.perf_counter() - t0
@@ -233,7 +241,8 @@ def config4(train_textures=64, train_size=2048, eval_textures=32, eval_size=4096
         torch.cuda.synchronize()
         t_train = time.perf_counter() - t1
         del train_blocks, targets
-        res.update({"train_blocks": train_textures * (train_size // 4) ** 2, "train_steps": steps, "batch": batch,
+        res.update({"train_blocks": n_train, "train_mips": bool(mips), "train_steps": steps,
+                    "batch": batch,
                     "label_s": round(t_label, 3), "train_s": round(t_train, 3), "loss_first": losses[0],
                     "loss_last": float(np.mean(losses[-32:]))})
     if isinstance(threshold, str):
@@ -269,6 +278,15 @@ def config4(train_textures=64, train_size=2048, eval_textures=32, eval_size=4096
                 "plain_mtexel_s": texels / (tot["plain_ms"] / 1e3) / 1e6,
                 "rmse_plain": (tot["se_plain"] / tot["blocks"]) ** 0.5,
                 "forward_ms_per_mblock": tot["forward_ms"] / (tot["blocks"] / 1e6)})
+    # the mip chain of a 1024x1024 texture (seed 100, box-filtered levels): plain vs learned
+    from .texgen import colour_texture, mip_chain, image_blocks
+    chain = torch.from_numpy(np.concatenate([image_blocks(l) for l in mip_chain(colour_texture(1024, 1024, 100))])).cuda()
+    out_p = dxt1_optimize(chain)
+    res["mip_chain_1024"] = {"rmse_plain": rgb_rmse_torch(out_p, chain)}
+    for th in ths:
+        out_l, fb = net.encode(chain, threshold=th)
+        res["mip_chain_1024"][f"rmse_learned@{th}"] = rgb_rmse_torch(out_l, chain)
+        res["mip_chain_1024"][f"fallback@{th}"] = fb / chain.shape[0]
     res["learned"] = [{"threshold": th,
                        "learned_mtexel_s": texels / (acc["learned_ms"] / 1e3) / 1e6,
                        "speedup": tot["plain_ms"] / acc["learned_ms"],

@@ -195,6 +195,13 @@ def colour_texture_torch(w: int, h: int, seed: int, device="cuda"):
     return img
 
 
+def box_mip_torch(img):
+    """box_mip on a (h, w, 4) uint8 torch tensor with even dimensions."""
+    x = img.to(dtype=img.new_empty(0, dtype=__import__("torch").int32).dtype)
+    s = x[0::2, 0::2] + x[0::2, 1::2] + x[1::2, 0::2] + x[1::2, 1::2]
+    return ((s + 2) >> 2).to(img.dtype)
+
+
 def image_blocks_torch(img):
     """(h, w, 4) uint8 torch tensor (dimensions multiples of 4) -> (n, 64) blocks, row-major."""
     h, w = img.shape[0], img.shape[1]

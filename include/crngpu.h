@@ -126,6 +126,11 @@ typedef struct crngpu_hc_params {
     uint32_t vq_round_fraction;             /* codebook tree: a round splits the top 1/this of the
                                                leaves by variance (0 = 4; larger = closer to the
                                                reference's one-at-a-time order, more rounds) */
+    uint32_t alpha_endpoint_codebook_size;  /* m_alpha_endpoint_codebook_size */
+    uint32_t alpha_selector_codebook_size;  /* m_alpha_selector_codebook_size */
+    float adaptive_tile_alpha_psnr_derating; /* m_adaptive_tile_alpha_psnr_derating (2.0) */
+    float color_alpha_weighting_ratio;      /* m_adaptive_tile_color_alpha_weighting_ratio (3.0) */
+    uint32_t alpha_component;               /* DXT5 / DXT5A: the channel encoded as alpha (3) */
     struct {
         uint32_t first_block, num_blocks, block_width;
         float weight;                       /* min(12, 1.3^level) in crn_comp */
@@ -140,6 +145,9 @@ typedef struct crngpu_hc_stats {
     double sse_endpoints;      /* RGB squared error over all blocks with the codebook endpoints and
                                   each pixel's best selector (before the selector codebook) */
     double sse_final;          /* RGB squared error of the output blocks */
+    uint32_t alpha_endpoints;  /* alpha endpoint codebook entries produced */
+    uint32_t alpha_selectors;  /* alpha selector codebook entries produced */
+    double sse_alpha;          /* squared error of the output alpha channels (all channels summed) */
 } crngpu_hc_stats;
 
 /* d_blocks: num_blocks x 64 bytes (device); d_out: num_blocks x 8 bytes of DXT1 (device).
@@ -150,6 +158,25 @@ typedef struct crngpu_hc_stats {
 CRNGPU_API int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_params* params, uint8_t* d_out,
                                        uint16_t* d_endpoint_idx, uint16_t* d_selector_idx, uint32_t* d_endpoints,
                                        uint32_t* d_selectors, crngpu_hc_stats* stats, void* stream);
+
+/* Clustered encode of DXT1, DXT5 (colour + alpha = params->alpha_component), DXN_XY/YX (two
+ * alpha channels, X = red / Y = green) or DXT5A: dxt_hc::compress for those formats, including the
+ * alpha endpoint VQ (vec2), the per-cluster dxt5_endpoint_optimizer + refiner and the 3-bit
+ * selector codebook (crnlib/crn_dxt_hc.cpp:1014-1300, 1506-1720). d_out: num_blocks x 8 (DXT1,
+ * DXT5A) or x 16 (DXT5: alpha then colour; DXN: X then Y) bytes. Synchronises `stream`. */
+CRNGPU_API int crngpu_hc_compress(const uint8_t* d_blocks, const crngpu_hc_params* params, uint32_t format,
+                                  uint8_t* d_out, crngpu_hc_stats* stats, void* stream);
+
+/* .crn writer: the tail of crn_comp (crnlib/crn_comp.cpp:295-422, 1356-1611; palettes
+ * crn_comp::pack_color_endpoints .. pack_alpha_selectors, block streams crn_comp::pack_blocks,
+ * models crn_comp::pack_data_models, header crn_comp::create_comp_data). Host code, no GPU needed.
+ * blocks: host memory, DXTn blocks of every level in crn_comp's layout (per level, per face, rows
+ * of ((w + 7) & ~7) / 4 blocks, ((h + 7) & ~7) / 4 rows; the blocks outside the image are stored
+ * but never output), 8 or 16 bytes each as `format` says. Palettes are the distinct endpoint
+ * pairs and selector words (at most 8192 of each: cluster first, e.g. crngpu_hc_compress).
+ * Returns the file size (the file is copied to `out` when out_capacity suffices) or an error. */
+CRNGPU_API int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32_t height, uint32_t levels,
+                                   uint32_t faces, uint32_t format, void* out, uint64_t out_capacity);
 
 /* Codebook sizes for a quality level (crn_comp::quantize_images, crnlib/crn_comp.cpp:541-577):
  * sizes4 = colour endpoints, colour selectors, alpha endpoints, alpha selectors. */
@@ -263,7 +290,8 @@ CRNGPU_API crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_ba
  * flags: CRNGPU_BATCH_GRAPH captures them into a CUDA graph on the first call and replays that
  * graph on later calls (one launch from the host per batch); CRNGPU_BATCH_EXPAND_ONLY re-runs
  * only the expansion kernel from the index records of the last decode (the destinations are
- * rewritten; used to time the HBM-bound expansion on its own). */
+ * rewritten; used to time the HBM-bound expansion on its own). The first launch of a batch also
+ * runs the expansion autotuner (see crngpu_unpack_batch_tuning) and synchronises once. */
 #define CRNGPU_BATCH_GRAPH 1u
 #define CRNGPU_BATCH_EXPAND_ONLY 2u
 CRNGPU_API int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t flags, void* stream);
@@ -271,6 +299,13 @@ CRNGPU_API int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t fl
 /* Synchronises `stream` and reports the last launch's outcome: CRNGPU_OK, or CRNGPU_E_CORRUPT if
  * a block stream held an invalid code or palette index (the reference's bool result). */
 CRNGPU_API int crngpu_unpack_batch_status(crngpu_unpack_batch batch, void* stream);
+
+/* Autotuner result: the first launch of a batch decodes, then times each expansion variant
+ * (tile of 1024 << (v >> 1) blocks; DXT1 palettes staged in shared memory when v is odd) and keeps
+ * the fastest for the batch and as the device's default for later single-texture calls.
+ * *variant (-1 before the first launch) and up to n measured times in ms; returns the number of
+ * variants. */
+CRNGPU_API int crngpu_unpack_batch_tuning(crngpu_unpack_batch batch, int32_t* variant, float* ms, uint32_t n);
 
 /* Total output bytes of the batch (sum of the items' level sizes). */
 CRNGPU_API int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch);

@@ -40,6 +40,9 @@ def lib():
         L.ref_dxt_hc_dxt1.argtypes = [ctypes.c_void_p, _u32, _u32, ctypes.c_void_p, _u32, _u32, _u32, ctypes.c_int,
                                       _u32, ctypes.c_void_p, ctypes.c_void_p]
         L.ref_dxt_hc_dxt1.restype = ctypes.c_int
+        L.ref_dxt_hc_alpha.argtypes = [ctypes.c_void_p, _u32, _u32, ctypes.c_void_p, _u32, _u32, ctypes.c_void_p,
+                                       ctypes.c_int, _u32, ctypes.c_void_p, ctypes.c_void_p]
+        L.ref_dxt_hc_alpha.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -99,3 +102,22 @@ def dxt_hc_dxt1(blocks: np.ndarray, levels, faces: int, endpoint_codebook: int, 
                                  selector_codebook, int(perceptual), threads, out.ctypes.data, stats.ctypes.data):
         raise RuntimeError("reference dxt_hc failed")
     return out.reshape(n, 8), {"tiles": int(stats[0]), "endpoints": int(stats[1]), "selectors": int(stats[2])}
+
+
+def dxt_hc_alpha(blocks: np.ndarray, levels, faces: int, fmt: str, codebooks, perceptual: bool = True, threads: int = 8):
+    """The reference's dxt_hc::compress for DXT5 (alpha = channel 3), DXN_XY, DXN_YX or DXT5A.
+    Returns ((n, 16 or 8) blocks, stats)."""
+    code = {"DXT5": 0, "DXN_XY": 1, "DXN_YX": 2, "DXT5A": 3}[fmt]
+    blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+    n = blocks.shape[0]
+    info = np.array([v for lv in levels for v in lv], np.uint32)
+    cb = np.array(codebooks, np.uint32)
+    out = np.zeros(n * 16, np.uint8)
+    stats = np.zeros(8, np.uint32)
+    bpb = lib().ref_dxt_hc_alpha(blocks.ctypes.data, n, len(levels), info.ctypes.data, faces, code, cb.ctypes.data,
+                                 int(perceptual), threads, out.ctypes.data, stats.ctypes.data)
+    if bpb <= 0:
+        raise RuntimeError("reference dxt_hc failed")
+    return out[: n * bpb].reshape(n, bpb), {"tiles": int(stats[0]), "color_endpoints": int(stats[1]),
+                                            "color_selectors": int(stats[2]), "alpha_endpoints": int(stats[3]),
+                                            "alpha_selectors": int(stats[4])}

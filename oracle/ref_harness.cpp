@@ -218,6 +218,77 @@ int ref_dxt_hc_dxt1(const uint8_t* rgba_blocks, uint32_t n, uint32_t nlevels, co
   return 1;
 }
 
+// The reference's clustered compressor for an alpha-carrying format (fmt: 0 DXT5 with alpha
+// channel 3, 1 DXN_XY, 2 DXN_YX, 3 DXT5A on channel 3), same layout and weights as
+// ref_dxt_hc_dxt1. codebooks: colour endpoints, colour selectors, alpha endpoints, alpha selectors.
+// Writes n x 16 bytes (DXT5, DXN) or n x 8 (DXT5A): alpha blocks are endpoints (first, second)
+// then 16 3-bit selectors converted from linear to DXT5 order. stats[0..4] = tiles, colour
+// endpoints, colour selectors, alpha endpoints, alpha selectors. Returns bytes per block.
+int ref_dxt_hc_alpha(const uint8_t* rgba_blocks, uint32_t n, uint32_t nlevels, const uint32_t* level_info,
+                     uint32_t faces, uint32_t fmt, const uint32_t* codebooks, int perceptual, uint32_t threads,
+                     uint8_t* out, uint32_t* stats) {
+  crnlib::task_pool pool;
+  if (!pool.init(threads > 1 ? threads - 1 : 0)) return 0;
+  crnlib::dxt_hc::params p;
+  p.m_num_blocks = n;
+  p.m_num_levels = nlevels;
+  p.m_num_faces = faces;
+  p.m_format = fmt == 0 ? crnlib::cDXT5 : fmt == 1 ? crnlib::cDXN_XY : fmt == 2 ? crnlib::cDXN_YX : crnlib::cDXT5A;
+  p.m_perceptual = perceptual != 0;
+  p.m_hierarchical = true;
+  p.m_color_endpoint_codebook_size = codebooks[0];
+  p.m_color_selector_codebook_size = codebooks[1];
+  p.m_alpha_endpoint_codebook_size = codebooks[2];
+  p.m_alpha_selector_codebook_size = codebooks[3];
+  if (fmt == 0 || fmt == 3) p.m_alpha_component_indices[0] = 3;
+  else if (fmt == 1) { p.m_alpha_component_indices[0] = 0; p.m_alpha_component_indices[1] = 1; }
+  else { p.m_alpha_component_indices[0] = 1; p.m_alpha_component_indices[1] = 0; }
+  p.m_pTask_pool = &pool;
+  for (uint32_t l = 0; l < nlevels; l++) {
+    p.m_levels[l].m_first_block = level_info[3 * l];
+    p.m_levels[l].m_num_blocks = level_info[3 * l + 1];
+    p.m_levels[l].m_block_width = level_info[3 * l + 2];
+    p.m_levels[l].m_weight = crnlib::math::minimum(12.0f, powf(1.3f, (float)l));
+  }
+  std::vector<uint8_t> copy(rgba_blocks, rgba_blocks + (size_t)n * 64);
+  crnlib::vector<crnlib::dxt_hc::endpoint_indices_details> ei;
+  crnlib::vector<crnlib::dxt_hc::selector_indices_details> si;
+  crnlib::vector<crnlib::uint32> ce, ae, cs;
+  crnlib::vector<crnlib::uint64> as;
+  crnlib::dxt_hc hc;
+  if (!hc.compress(reinterpret_cast<crnlib::color_quad_u8(*)[16]>(copy.data()), ei, si, ce, ae, cs, as, p)) return 0;
+  static const uint8_t from_linear[4] = {0, 2, 3, 1};
+  static const uint8_t from_linear8[8] = {0, 2, 3, 4, 5, 6, 7, 1};
+  const uint32_t nalpha = (fmt == 1 || fmt == 2) ? 2 : 1;
+  const uint32_t bpb = fmt == 3 ? 8 : 16;
+  for (uint32_t b = 0; b < n; b++) {
+    uint8_t* o = out + (size_t)b * bpb;
+    for (uint32_t a = 0; a < nalpha; a++) {
+      const uint32_t ep = ae[ei[b].component[1 + a]];
+      const uint64_t lin = as[si[b].component[1 + a]];
+      uint64_t dxt = 0;
+      for (int q = 0; q < 16; q++) dxt |= (uint64_t)from_linear8[(lin >> (3 * q)) & 7] << (3 * q);
+      o[8 * a] = (uint8_t)(ep & 255);
+      o[8 * a + 1] = (uint8_t)((ep >> 8) & 255);
+      for (int k = 0; k < 6; k++) o[8 * a + 2 + k] = (uint8_t)(dxt >> (8 * k));
+    }
+    if (fmt == 0) {
+      const uint32_t ep = ce[ei[b].color], lin = cs[si[b].color];
+      uint32_t dxt = 0;
+      for (int q = 0; q < 16; q++) dxt |= (uint32_t)from_linear[(lin >> (2 * q)) & 3] << (2 * q);
+      memcpy(o + 8, &ep, 4);
+      memcpy(o + 12, &dxt, 4);
+    }
+  }
+  stats[0] = hc.m_num_tiles;
+  stats[1] = ce.size();
+  stats[2] = cs.size();
+  stats[3] = ae.size();
+  stats[4] = as.size();
+  pool.deinit();
+  return (int)bpb;
+}
+
 // Squared RGB error of dxt_fast::compress_color_block on n pixels (n = 16, 32 or 64), measured
 // against the 4-colour palette as dxt_hc::determine_tiles_task does (crnlib/crn_dxt_hc.cpp:459-472).
 uint32_t ref_dxt_fast_tile_error(const uint8_t* rgba, uint32_t n) {

@@ -143,6 +143,8 @@ def make_crn() -> None:
 
 
 HC_CASES = [("dxt1_256", 256, 10), ("c1_dxt1_1024", 1024, 100), ("hc_128", 128, 21)]
+# (name, format, crn format code, size, seed, content)
+HC_ALPHA_CASES = [("dxt5_256", "DXT5", 2, 256, 13, "colour_alpha"), ("dxn_xy_256", "DXN_XY", 7, 256, 15, "normal")]
 
 
 def make_hc() -> None:
@@ -164,6 +166,30 @@ def make_hc() -> None:
         out[name] = {"size": size, "seed": seed, "quality": 128, "codebook_request": [ce, cs], "tiles": st["tiles"],
                      "endpoints": st["endpoints"], "selectors": st["selectors"],
                      "rmse_visible": rgb_rmse(np.concatenate(rows), src), "rmse_all_blocks": rgb_rmse(dxt, blocks)}
+    # alpha-carrying formats: DXT5 (colour + alpha noise, perceptual) and DXN_XY (normal map)
+    from dxt_decode import dxt5a_values
+    for name, fmt, code, size, seed, content in HC_ALPHA_CASES:
+        img = texgen.normal_map(size, size, seed) if content == "normal" else \
+            texgen.colour_texture(size, size, seed, with_alpha_noise=True)
+        levels = texgen.mip_chain(img)
+        blocks, lv, vis = crn_layout([levels])
+        sizes = hc.codebook_sizes(size, size, 128, code)
+        dxt, st = ref.dxt_hc_alpha(blocks, lv, 1, fmt, sizes, content != "normal", threads=8)
+        rows = [dxt[fb:fb + nb].reshape(-1, bw, dxt.shape[1])[:by, :bx].reshape(-1, dxt.shape[1])
+                for (fb, nb, bw), (bx, by, _) in zip(lv, vis)]
+        dec = np.concatenate(rows)
+        src = np.concatenate([texgen.image_blocks(im) for im in levels]).reshape(-1, 16, 4).astype(np.int64)
+        rec = {"size": size, "seed": seed, "quality": 128, "format": fmt, "content": content,
+               "codebook_request": list(sizes), **st}
+        if fmt == "DXT5":
+            rec["rmse_color_visible"] = rgb_rmse(dec[:, 8:], src.reshape(-1, 64).astype(np.uint8))
+            a = dxt5a_values(dec[:, :8])
+            rec["rmse_alpha_visible"] = float(np.sqrt(((a - src[:, :, 3]) ** 2).mean()))
+        else:
+            x, y = dxt5a_values(dec[:, :8]), dxt5a_values(dec[:, 8:])
+            rec["rmse_alpha_visible"] = float(np.sqrt((((x - src[:, :, 0]) ** 2).sum() + ((y - src[:, :, 1]) ** 2).sum())
+                                                      / (2 * x.size)))
+        out[name] = rec
     with open(os.path.join(HERE, "hc_reference.json"), "w") as fh:
         json.dump(out, fh, indent=1, sort_keys=True)
 

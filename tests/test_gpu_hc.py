@@ -103,3 +103,38 @@ def test_codebook_sizes_follow_quality(hc):
     assert lo[0] == 64 and lo[1] == 96
     hi = hc.codebook_sizes(64, 64, 255)
     assert hi[0] == 256 and hi[1] == 256
+
+
+@pytest.mark.parametrize("name", ["dxt5_256", "dxn_xy_256"])
+def test_clustered_alpha_formats_match_reference_quality(hc, name):
+    """DXT5 (colour + alpha) and DXN (two alpha channels) through crngpu_hc_compress against the
+    reference dxt_hc on the same blocks: same tile count (the alpha tile errors are restated
+    exactly), RGB and alpha RMSE within a few percent."""
+    from crunch2_gb300 import texgen
+    import crunch2_gb300 as cg
+    from dxt_decode import dxt5a_values
+    R = hc_reference()[name]
+    size, seed = R["size"], R["seed"]
+    img = texgen.normal_map(size, size, seed) if R["content"] == "normal" else \
+        texgen.colour_texture(size, size, seed, with_alpha_noise=True)
+    levels = texgen.mip_chain(img)
+    fmt = cg.FMT_DXT5 if R["format"] == "DXT5" else cg.FMT_DXN_XY
+    out, stats = hc.compress([levels], fmt, quality=128)
+    assert list(stats["codebook_request"]) == R["codebook_request"]
+    assert stats["tiles"] == R["tiles"]
+    assert 0 < stats["alpha_endpoints"] <= R["codebook_request"][2]
+    assert 0 < stats["alpha_selectors"] <= R["codebook_request"][3]
+    dec = np.concatenate([out[l][0].reshape(-1, 16) for l in range(len(levels))])
+    src = np.concatenate([texgen.image_blocks(im) for im in levels]).reshape(-1, 16, 4).astype(np.int64)
+    if fmt == cg.FMT_DXT5:
+        rc = rgb_rmse(dec[:, 8:], src.reshape(-1, 64).astype(np.uint8))
+        a = dxt5a_values(dec[:, :8])
+        ra = float(np.sqrt(((a - src[:, :, 3]) ** 2).mean()))
+        print(f"{name}: colour RMSE {rc:.4f} (reference {R['rmse_color_visible']:.4f}), alpha {ra:.4f} "
+              f"(reference {R['rmse_alpha_visible']:.4f}), stats {stats}")
+        assert rc <= 1.03 * R["rmse_color_visible"]
+    else:
+        x, y = dxt5a_values(dec[:, :8]), dxt5a_values(dec[:, 8:])
+        ra = float(np.sqrt((((x - src[:, :, 0]) ** 2).sum() + ((y - src[:, :, 1]) ** 2).sum()) / (2 * x.size)))
+        print(f"{name}: alpha RMSE {ra:.4f} (reference {R['rmse_alpha_visible']:.4f}), stats {stats}")
+    assert ra <= max(1.05 * R["rmse_alpha_visible"], R["rmse_alpha_visible"] + 0.02)
