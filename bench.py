@@ -7,8 +7,8 @@ One JSON line on stdout (rank 0):
   learned    the learned-proposal encode of the same blocks (shipped weights): Mtexel/s, RGB
              RMSE beside the plain encode's, fallback fraction
   e2e        the same encode through the C ABI with pinned host buffers (H2D + encode + D2H)
-  clustered  clustered (CRN-style, quality 128) DXT1 of the same mip chain on the GPU: Mtexel/s
-             and RGB RMSE beside the reference dxt_hc's RMSE on the same blocks
+  clustered  crn_compress of the same mip chain to .crn at quality 128 (DXT1): Mtexel/s, bits per
+             texel and RGB RMSE beside the reference's own .crn of the texture
   transcode  CRN -> DXT1 transcode GB/s: a batch of 1024 textures (each with its own context holding
              the reference-encoded .crn of the same texture, q128) in one persistent decode launch
              and one expansion launch (CUDA graph); the expansion kernel's HBM roofline; the
@@ -403,28 +403,30 @@ def main():
               "ms": round(expand_ms, 4), "bytes_algorithmic": exp_bytes,
               "achieved": round(exp_bytes / (expand_ms / 1e3) / 1e9, 1)}
 
-    # ---- clustered (CRN-style) DXT1 of the same mip chain at quality 128: dxt_hc on the GPU,
-    # quality against the reference's own dxt_hc on the same blocks (committed fixture)
-    from crunch2_gb300 import hc as HC
-    from crunch2_gb300.texgen import image_blocks
-    HC.compress_dxt1([levels], quality=128)  # warm-up (allocations, tables)
-    hc_times = []
+    # ---- crn_compress of the same mip chain at quality 128 (DXT1): clustered encode on the GPU
+    # (crngpu_hc_compress) + the .crn writer (host); quality and size beside the reference's own
+    # .crn of this texture (committed fixture), both decoded by the GPU transcoder
+    cg.compress_crn([levels], cg.FMT_DXT1, quality=128)  # warm-up (allocations, tables)
+    crn_times = []
     for _ in range(max(1, min(args.steps, 5))):
-        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        hc_out, hc_stats = HC.compress_dxt1([levels], quality=128)
-        hc_times.append(time.perf_counter() - t0)
-    hc_s = statistics.median(hc_times)
-    dec = np.concatenate([hc_out[l][0].reshape(-1, 8) for l in range(len(levels))])
-    with open(os.path.join(ROOT, "tests", "golden", "hc_reference.json")) as fh:
-        hc_ref = json.load(fh)["c1_dxt1_1024"]
-    hc_rmse = LR.rgb_rmse_torch(torch.from_numpy(dec).to(dev), torch.from_numpy(blocks).to(dev))
-    clustered = {"value": round(texels / hc_s / 1e6, 3), "unit": "Mtexel/s", "s_per_texture": round(hc_s, 4),
-                 "quality": 128, "rmse": round(hc_rmse, 4), "rmse_reference_dxt_hc": round(hc_ref["rmse_visible"], 4),
-                 "codebooks": [hc_stats["color_endpoints"], hc_stats["color_selectors"]],
-                 "tiles": hc_stats["tiles"], "tiles_reference": hc_ref["tiles"],
-                 "path": "crngpu_hc_compress_dxt1 from host RGBA8 (H2D of the blocks, every stage on the GPU, "
-                         "D2H of the DXT1 blocks), wall time of the call"}
+        our_crn = cg.compress_crn([levels], cg.FMT_DXT1, quality=128)
+        crn_times.append(time.perf_counter() - t0)
+    crn_s = statistics.median(crn_times)
+
+    def crn_rmse(data):
+        with cg.unpack_begin(data) as c:
+            dec = c.unpack_levels()
+        return LR.rgb_rmse_torch(torch.from_numpy(dec.reshape(-1, 8)).to(dev), torch.from_numpy(blocks).to(dev))
+
+    with open(CRN_FIXTURE, "rb") as fh:
+        ref_crn = fh.read()
+    clustered = {"value": round(texels / crn_s / 1e6, 3), "unit": "Mtexel/s", "s_per_texture": round(crn_s, 4),
+                 "quality": 128, "rmse": round(crn_rmse(our_crn), 4), "rmse_reference_crn": round(crn_rmse(ref_crn), 4),
+                 "bits_per_texel": round(len(our_crn) * 8 / texels, 4),
+                 "bits_per_texel_reference": round(len(ref_crn) * 8 / texels, 4),
+                 "path": "crngpu_compress_crn: host RGBA8 mip chain -> crn_comp block gather (host) -> H2D -> "
+                         "clustered encode (every dxt_hc stage on the GPU) -> D2H -> .crn writer (host); wall time"}
 
     peaks, peak_kind = measured_peaks()
     clk = clocks.summary()

@@ -100,6 +100,8 @@ def lib():
     L.crngpu_unpack_batch_destroy.restype = i32
     L.crngpu_crn_decompress.argtypes = [vp, ctypes.c_uint, vp, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint]
     L.crngpu_crn_decompress.restype = None
+    L.crngpu_compress_crn.argtypes = [vp, u32, u32, u32, u32, u32, u32, u32, vp, u64]
+    L.crngpu_compress_crn.restype = i64
     L.crngpu_crn_pack.argtypes = [vp, u32, u32, u32, u32, u32, vp, u64]
     L.crngpu_crn_pack.restype = i64
     L.crngpu_profile_counters.argtypes = [i32, ctypes.POINTER(ctypes.c_uint64), vp]
@@ -359,3 +361,21 @@ def crn_layout_from_levels(level_blocks, width: int, height: int, faces: int, bp
             v = np.asarray(fl[f]).reshape((h + 3) // 4, (w + 3) // 4, bpb)
             parts.append(np.pad(v, ((0, H - v.shape[0]), (0, W - v.shape[1]), (0, 0)), mode="edge").reshape(-1, bpb))
     return np.concatenate(parts)
+
+
+def compress_crn(faces_levels, fmt: int = FMT_DXT1, quality: int = 128, flags: int = FLAG_PERCEPTUAL) -> bytes:
+    """crn_compress to a .crn with source mips: faces_levels[face][level] RGBA8 images."""
+    h, w = faces_levels[0][0].shape[:2]
+    flat = np.concatenate([np.ascontiguousarray(im, dtype=np.uint8).reshape(-1) for face in faces_levels for im in face])
+    L = lib()
+    args = (flat.ctypes.data, w, h, len(faces_levels[0]), len(faces_levels), fmt, quality, flags)
+    # a .crn is smaller than its DXT blocks (at most ~3 prefix codes of <= 16 bits per block)
+    # plus palettes (<= 8192 entries x 12 bytes) and models
+    bpb = 8 if fmt in (FMT_DXT1, FMT_DXT5A) else 16
+    cap = sum(((max(1, w >> l) + 7) // 8 * 2) * ((max(1, h >> l) + 7) // 8 * 2) * bpb
+              for l in range(len(faces_levels[0]))) * len(faces_levels) + (1 << 20)
+    out = np.zeros(cap, np.uint8)
+    size = _check(int(L.crngpu_compress_crn(*args, out.ctypes.data, cap)), "crngpu_compress_crn")
+    if size > cap:
+        raise CrnGpuError(E_PARAM, "crngpu_compress_crn: output larger than expected")
+    return out[:size].tobytes()

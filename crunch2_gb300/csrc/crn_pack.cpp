@@ -11,14 +11,18 @@
 //   * static canonical Huffman models (code lengths limited to 16 bits), transmitted with the
 //     21-symbol code-length code of symbol_codec (run-length codes 17-20);
 //   * the header (inc/crn_defs.h:286-339) with its two CRC16s.
-// The reference additionally reorders its palettes to shrink the deltas (crn_comp::optimize_color
-// / optimize_alpha); this writer keeps first-use order, which changes the file size, not the
-// decoded blocks.
+//   * palette order chosen as crn_comp::optimize_color / optimize_alpha do
+//     (crnlib/crn_comp.cpp:767-1321): selectors as a nearest-neighbour chain under an XOR-delta
+//     cost; endpoints by four trials (a nearest-neighbour chain, and three two-ended chains grown
+//     from the most frequent endpoint by similarity times co-occurrence in the block stream),
+//     keeping the trial whose palette plus index stream codes in the fewest bits.
+// The order changes the file size only, never the decoded blocks.
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <queue>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -40,6 +44,7 @@ class BitWriter {
     if (n_) { out_.push_back((uint8_t)(acc_ << (8 - n_))); acc_ = 0; n_ = 0; }
     return std::move(out_);
   }
+  uint64_t bits() const { return (uint64_t)out_.size() * 8 + (uint64_t)n_; }
 
  private:
   std::vector<uint8_t> out_;
@@ -197,6 +202,222 @@ uint64_t dxt5_sel_to_linear(uint64_t dxt) {
   return lin;
 }
 
+// ---- palettes (crn_comp::pack_color_endpoints / pack_color_selectors / pack_alpha_endpoints /
+// pack_alpha_selectors; the inverse of crn_unpacker::decode_palettes, inc/crn_decomp.h:3715-3851).
+// Each codes its symbols twice: a histogram pass, then the Huffman-coded pass behind its model.
+
+// colour endpoints: six running component deltas, a 5-bit model for red/blue, 6-bit for green
+std::vector<uint8_t> pack_colour_endpoints(const std::vector<uint64_t>& values) {
+  std::vector<uint32_t> f5(32, 0), f6(64, 0);
+  static const uint32_t kMask[6] = {31, 63, 31, 31, 63, 31};
+  static const int kModel[6] = {0, 1, 0, 0, 1, 0};
+  static const int kShift[6] = {11, 5, 0, 27, 21, 16};
+  std::vector<uint8_t> outb;
+  for (int pass = 0; pass < 2; pass++) {
+    Huff h5, h6;
+    BitWriter bw;
+    if (pass) {
+      ensure_used(f5); ensure_used(f6);
+      h5.build(f5, 16); h6.build(f6, 16);
+      send_model(bw, h5);
+      send_model(bw, h6);
+    }
+    uint32_t prev[6] = {0, 0, 0, 0, 0, 0};
+    for (uint64_t v : values)
+      for (int k = 0; k < 6; k++) {
+        const uint32_t c = ((uint32_t)v >> kShift[k]) & kMask[k];
+        const uint32_t d = (c - prev[k]) & kMask[k];
+        prev[k] = c;
+        if (pass) (kModel[k] ? h6 : h5).put(bw, d);
+        else (kModel[k] ? f6 : f5)[d]++;
+      }
+    if (pass) outb = bw.finish();
+  }
+  return outb;
+}
+
+// colour selectors: XOR deltas of the linear words, 4 bits at a time
+std::vector<uint8_t> pack_colour_selectors(const std::vector<uint64_t>& values) {
+  std::vector<uint32_t> fs(16, 0);
+  std::vector<uint8_t> outb;
+  for (int pass = 0; pass < 2; pass++) {
+    Huff hs;
+    BitWriter bw;
+    if (pass) { ensure_used(fs); hs.build(fs, 16); send_model(bw, hs); }
+    uint32_t prev = 0;
+    for (uint64_t v : values) {
+      const uint32_t d = (uint32_t)v ^ prev;
+      prev = (uint32_t)v;
+      for (int j = 0; j < 32; j += 4) {
+        const uint32_t x = (d >> j) & 15u;
+        if (pass) hs.put(bw, x); else fs[x]++;
+      }
+    }
+    if (pass) outb = bw.finish();
+  }
+  return outb;
+}
+
+// alpha endpoints: two running 8-bit deltas
+std::vector<uint8_t> pack_alpha_endpoints(const std::vector<uint64_t>& values) {
+  std::vector<uint32_t> fa(256, 0);
+  std::vector<uint8_t> outb;
+  for (int pass = 0; pass < 2; pass++) {
+    Huff ha;
+    BitWriter bw;
+    if (pass) { ensure_used(fa); ha.build(fa, 16); send_model(bw, ha); }
+    uint32_t pa = 0, pb = 0;
+    for (uint64_t v : values) {
+      const uint32_t a = (uint32_t)v & 255u, b = (uint32_t)(v >> 8) & 255u;
+      const uint32_t d0 = (a - pa) & 255u, d1 = (b - pb) & 255u;
+      pa = a; pb = b;
+      if (pass) { ha.put(bw, d0); ha.put(bw, d1); } else { fa[d0]++; fa[d1]++; }
+    }
+    if (pass) outb = bw.finish();
+  }
+  return outb;
+}
+
+// alpha selectors: XOR deltas of the two 24-bit linear halves, 6 bits at a time
+std::vector<uint8_t> pack_alpha_selectors(const std::vector<uint64_t>& values) {
+  std::vector<uint32_t> fs(64, 0);
+  std::vector<uint8_t> outb;
+  for (int pass = 0; pass < 2; pass++) {
+    Huff hs;
+    BitWriter bw;
+    if (pass) { ensure_used(fs); hs.build(fs, 16); send_model(bw, hs); }
+    uint32_t prev[2] = {0, 0};
+    for (uint64_t v : values)
+      for (int h = 0; h < 2; h++) {
+        const uint32_t half = (uint32_t)(v >> (24 * h)) & 0xFFFFFFu;
+        const uint32_t d = half ^ prev[h];
+        prev[h] = half;
+        for (int j = 0; j < 24; j += 6) {
+          const uint32_t x = (d >> j) & 63u;
+          if (pass) hs.put(bw, x); else fs[x]++;
+        }
+      }
+    if (pass) outb = bw.finish();
+  }
+  return outb;
+}
+
+// ---- palette ordering ----
+
+// Estimated coded size of an XOR delta between two linear selector words (optimize_color_selectors
+// and optimize_alpha_selectors, crnlib/crn_comp.cpp:921-975, 1236-1282): a per-field cost of the
+// XOR of corresponding 2-bit (colour) or 3-bit (alpha) selectors, costs {0, 5, 14, 10} and
+// {0, 2, 3, 3, 5, 5, 4, 4}.
+inline uint32_t colour_selector_cost(uint64_t a, uint64_t b) {
+  const uint32_t x = (uint32_t)(a ^ b);
+  const uint32_t lo = x & 0x55555555u, hi = (x >> 1) & 0x55555555u;
+  return 5u * (uint32_t)__builtin_popcount(lo & ~hi) + 14u * (uint32_t)__builtin_popcount(hi & ~lo) +
+         10u * (uint32_t)__builtin_popcount(lo & hi);
+}
+inline uint32_t alpha_selector_cost(uint64_t a, uint64_t b) {
+  static const uint8_t kCost[8] = {0, 2, 3, 3, 5, 5, 4, 4};
+  uint64_t x = a ^ b;
+  uint32_t c = 0;
+  for (int k = 0; k < 16; k++, x >>= 3) c += kCost[x & 7];
+  return c;
+}
+
+// Nearest-neighbour chain: starting from `start_cost(i)` (the distance of entry i from an
+// all-zero entry), repeatedly take the closest remaining entry to the last one taken
+// (sort_color_endpoints / sort_alpha_endpoints / the selector sorts). Returns each entry's rank.
+template <class Start, class Dist>
+std::vector<uint32_t> nearest_chain(uint32_t n, Start start_cost, Dist dist) {
+  std::vector<uint32_t> rank(n), rem(n);
+  for (uint32_t i = 0; i < n; i++) rem[i] = i;
+  int64_t cur = -1;
+  for (uint32_t left = n; left; left--) {
+    uint32_t best = 0, best_cost = UINT32_MAX;
+    for (uint32_t i = 0; i < left; i++) {
+      const uint32_t c = cur < 0 ? start_cost(rem[i]) : dist(rem[i], (uint32_t)cur);
+      if (c < best_cost) { best_cost = c; best = i; }
+    }
+    cur = rem[best];
+    rank[rem[best]] = n - left;
+    rem[best] = rem[left - 1];
+  }
+  return rank;
+}
+
+// Symmetric counts of consecutive endpoint indices in the coded stream, as compressed rows.
+struct Adjacency {
+  std::vector<uint32_t> start, nb, count;
+  std::vector<uint32_t> total;  // per entry: sum of its row
+};
+
+// Two-ended chain grown from `first` (remap_color_endpoints / remap_alpha_endpoints,
+// crnlib/crn_comp.cpp:800-873, 1094-1158). Each remaining entry carries its accumulated
+// co-occurrence with the entries taken so far and its similarity (base - min(cap, distance)) to
+// the two ends of the chain; the entry with the largest max(similarity) * (co-occurrence +
+// normaliser) is taken next, and joins the end whose half of the chain it co-occurs with more
+// (weighted toward the ends). The normaliser is the taken entry's co-occurrence << shift.
+template <class Dist>
+std::vector<uint32_t> grow_chain(uint32_t n, const Adjacency& adj, uint32_t first, uint32_t base, uint32_t cap,
+                                 int shift, Dist dist) {
+  std::vector<uint32_t> rem, freq(n, 0), sim_f(n, 0), sim_b(n, 0), row(n, 0), pos(n, UINT32_MAX), chain(2 * n + 1);
+  rem.reserve(n);
+  for (uint32_t i = 0; i < n; i++)
+    if (i != first) rem.push_back(i);
+  uint32_t lo = n, hi = n;
+  chain[n] = first;
+  pos[first] = n;
+  auto load = [&](uint32_t s, bool on) {
+    for (uint32_t k = adj.start[s]; k < adj.start[s + 1]; k++) row[adj.nb[k]] = on ? adj.count[k] : 0;
+  };
+  load(first, true);
+  uint32_t last = first, front = first, back = first;
+  bool front_new = true, back_new = true;
+  uint64_t normaliser = 0;
+  while (!rem.empty()) {
+    uint64_t best_val = 0;
+    size_t best = 0;
+    for (size_t i = 0; i < rem.size(); i++) {
+      const uint32_t e = rem[i];
+      freq[e] += row[e];
+      if (front_new) sim_f[e] = base - std::min(cap, dist(e, front));
+      if (back_new) sim_b[e] = base - std::min(cap, dist(e, back));
+      const uint64_t v = (uint64_t)std::max(sim_f[e], sim_b[e]) * ((uint64_t)freq[e] + normaliser) + 1;
+      if (v > best_val || (v == best_val && e < rem[best])) { best_val = v; best = i; }
+    }
+    const uint32_t s = rem[best];
+    load(last, false);
+    load(s, true);
+    last = s;
+    // co-occurrence of s with each half of the chain, weighted (L-1-2k) by distance k from that end
+    const int64_t L = (int64_t)hi - lo + 1;
+    uint64_t w_front = 0, w_back = 0;
+    for (uint32_t k = adj.start[s]; k < adj.start[s + 1]; k++) {
+      const uint32_t p = pos[adj.nb[k]];
+      if (p == UINT32_MAX) continue;
+      const int64_t wf = L - 1 - 2 * ((int64_t)p - lo), wb = L - 1 - 2 * ((int64_t)hi - p);
+      if (wf > 0) w_front += (uint64_t)wf * adj.count[k];
+      if (wb > 0) w_back += (uint64_t)wb * adj.count[k];
+    }
+    normaliser = (uint64_t)freq[s] << shift;
+    if ((uint64_t)sim_f[s] * w_front > (uint64_t)sim_b[s] * w_back) {
+      chain[--lo] = s; pos[s] = lo; front = s; front_new = true; back_new = false;
+    } else {
+      chain[++hi] = s; pos[s] = hi; back = s; back_new = true; front_new = false;
+    }
+    rem[best] = rem.back();
+    rem.pop_back();
+  }
+  std::vector<uint32_t> rank(n);
+  for (uint32_t p = lo; p <= hi; p++) rank[chain[p]] = p - lo;
+  return rank;
+}
+
+template <class T>
+std::vector<T> permuted(const std::vector<T>& v, const std::vector<uint32_t>& rank) {
+  std::vector<T> out(v.size());
+  for (size_t i = 0; i < v.size(); i++) out[rank[i]] = v[i];
+  return out;
+}
+
 }  // namespace
 }  // namespace crngpu
 
@@ -264,23 +485,164 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
     set_error("crngpu_crn_pack: more than 8192 distinct endpoints or selectors (cluster the blocks first)");
     return CRNGPU_E_PARAM;
   }
-  // reference groups and symbol streams (crn_comp::pack_blocks, crnlib/crn_comp.cpp:295-422): the
-  // histograms first, then the coded streams
+  // references of every block (crn_comp::pack_blocks, crnlib/crn_comp.cpp:295-422): 0 new (an
+  // endpoint delta per component), 1 same endpoints as the previous block in decode order, 2 same
+  // as the block above (the faces of a level are one tall image to the decoder's row buffer)
+  std::vector<uint8_t> ref(nblocks, 0);
+  for (uint32_t l = 0; l < levels; l++) {
+    const Lv& L = lv[l];
+    for (uint32_t row = 0; row < faces * L.H; row++)
+      for (uint32_t x = 0; x < L.W; x++) {
+        const uint64_t b = L.first + (uint64_t)row * L.W + x;
+        bool left = row || x, top = row != 0;
+        for (int c = 0; c < ncomp; c++) {
+          const uint32_t e = eidx[b * ncomp + c];
+          if (left) left = e == eidx[(b - 1) * ncomp + c];
+          if (top) top = e == eidx[(b - L.W) * ncomp + c];
+        }
+        ref[b] = left ? 1 : top ? 2 : 0;
+      }
+  }
+  // palette order. Model 0 = colour (component 0 when present), model 1 = alpha (the rest).
+  const int comp_lo[2] = {0, colour ? 1 : 0}, comp_hi[2] = {colour ? 1 : 0, ncomp};
+  Palette* ep_pal[2] = {&cep, &aep};
+  Palette* sel_pal[2] = {&csel, &asel};
+  std::vector<uint32_t> ep_rank[2], sel_rank[2];
+  {
+    std::vector<std::thread> workers;
+    // the endpoint trials of model m: coded size of the palette plus the index deltas
+    auto stream_bits = [&](int m, const std::vector<uint32_t>& rank) -> uint64_t {
+      const uint32_t n = (uint32_t)rank.size();
+      std::vector<uint32_t> h(n, 0);
+      for (uint32_t l = 0; l < levels; l++) {
+        uint32_t prev[3] = {0, 0, 0};
+        const uint64_t end = lv[l].first + (uint64_t)lv[l].W * lv[l].H * faces;
+        for (uint64_t b = lv[l].first; b < end; b++)
+          for (int c = comp_lo[m]; c < comp_hi[m]; c++) {
+            const uint32_t e = rank[eidx[b * ncomp + c]];
+            if (!ref[b]) h[(e + n - prev[c]) % n]++;
+            prev[c] = e;
+          }
+      }
+      ensure_used(h);
+      Huff hf;
+      hf.build(h, 16);
+      uint64_t bits = 0;
+      for (uint32_t k = 0; k < n; k++) bits += (uint64_t)h[k] * hf.len[k];
+      BitWriter bw;
+      send_model(bw, hf);
+      const std::vector<uint64_t> vals = permuted(ep_pal[m]->values, rank);
+      return bits + bw.bits() + 8 * (m ? pack_alpha_endpoints(vals) : pack_colour_endpoints(vals)).size();
+    };
+    for (int m = 0; m < 2; m++) {
+      if (comp_lo[m] == comp_hi[m]) continue;
+      const uint32_t n = (uint32_t)ep_pal[m]->values.size();
+      // selectors: nearest-neighbour chain under the XOR-delta cost
+      workers.emplace_back([&, m] {
+        const std::vector<uint64_t>& v = sel_pal[m]->values;
+        if (m) sel_rank[m] = nearest_chain((uint32_t)v.size(), [&](uint32_t i) { return alpha_selector_cost(v[i], 0); },
+                                           [&](uint32_t i, uint32_t j) { return alpha_selector_cost(v[i], v[j]); });
+        else sel_rank[m] = nearest_chain((uint32_t)v.size(), [&](uint32_t i) { return colour_selector_cost(v[i], 0); },
+                                         [&](uint32_t i, uint32_t j) { return colour_selector_cost(v[i], v[j]); });
+      });
+      workers.emplace_back([&, m, n] {
+        // endpoints, unpacked to 8-bit components: colour (r, g, b) of both endpoints, or the two alphas
+        std::vector<int32_t> u((size_t)n * 6);
+        for (uint32_t i = 0; i < n; i++) {
+          const uint32_t v = (uint32_t)ep_pal[m]->values[i];
+          int32_t* c = &u[(size_t)i * 6];
+          if (m) { c[0] = (int32_t)(v & 255u); c[1] = (int32_t)((v >> 8) & 255u); c[2] = c[3] = c[4] = c[5] = 0; continue; }
+          for (int e = 0; e < 2; e++) {
+            const uint32_t q = v >> (16 * e), r = (q >> 11) & 31, g = (q >> 5) & 63, bl = q & 31;
+            c[3 * e + 0] = (int32_t)((r << 3) | (r >> 2));
+            c[3 * e + 1] = (int32_t)((g << 2) | (g >> 4));
+            c[3 * e + 2] = (int32_t)((bl << 3) | (bl >> 2));
+          }
+        }
+        auto dist = [&](uint32_t i, uint32_t j) {
+          const int32_t* a = &u[(size_t)i * 6];
+          const int32_t* b = &u[(size_t)j * 6];
+          uint32_t d = 0;
+          for (int k = 0; k < 6; k++) d += (uint32_t)((a[k] - b[k]) * (a[k] - b[k]));
+          return d;
+        };
+        auto start = [&](uint32_t i) {
+          const int32_t* a = &u[(size_t)i * 6];
+          uint32_t d = 0;
+          for (int k = 0; k < 6; k++) d += (uint32_t)(a[k] * a[k]);
+          return d;
+        };
+        // co-occurrence of consecutive endpoints in the delta-coded blocks, both directions,
+        // sorted and run-length counted into rows
+        std::vector<uint64_t> pairs;
+        for (uint32_t l = 0; l < levels; l++) {
+          uint32_t prev[3] = {0, 0, 0};
+          const uint64_t end = lv[l].first + (uint64_t)lv[l].W * lv[l].H * faces;
+          for (uint64_t b = lv[l].first; b < end; b++)
+            for (int c = comp_lo[m]; c < comp_hi[m]; c++) {
+              const uint32_t e = eidx[b * ncomp + c];
+              if (!ref[b] && e != prev[c]) {
+                pairs.push_back(((uint64_t)e << 32) | prev[c]);
+                pairs.push_back(((uint64_t)prev[c] << 32) | e);
+              }
+              prev[c] = e;
+            }
+        }
+        std::sort(pairs.begin(), pairs.end());
+        Adjacency adj;
+        adj.start.assign(n + 1, 0);
+        adj.total.assign(n, 0);
+        for (size_t k = 0; k < pairs.size();) {
+          size_t r = k + 1;
+          while (r < pairs.size() && pairs[r] == pairs[k]) r++;
+          const uint32_t i = (uint32_t)(pairs[k] >> 32);
+          adj.nb.push_back((uint32_t)pairs[k]);
+          adj.count.push_back((uint32_t)(r - k));
+          adj.start[i + 1]++;
+          adj.total[i] += (uint32_t)(r - k);
+          k = r;
+        }
+        for (uint32_t i = 0; i < n; i++) adj.start[i + 1] += adj.start[i];
+        uint32_t first = 0;
+        for (uint32_t i = 0; i < n; i++)
+          if (adj.total[i] > adj.total[first]) first = i;
+        // four trials, run side by side: the nearest-neighbour chain and three grown chains
+        const uint32_t unit = m ? 1000u : 4000u;
+        const float weights[3] = {0.0f, 1.0f / 6.0f, 0.5f};
+        std::vector<uint32_t> trial[4];
+        uint64_t bits[4];
+        std::vector<std::thread> tw;
+        tw.emplace_back([&] { trial[0] = nearest_chain(n, start, dist); bits[0] = stream_bits(m, trial[0]); });
+        for (int t = 0; t < 3; t++)
+          tw.emplace_back([&, t] {
+            trial[t + 1] = grow_chain(n, adj, first, (uint32_t)((float)unit * (1.0f + weights[t])), unit, m ? 0 : 3, dist);
+            bits[t + 1] = stream_bits(m, trial[t + 1]);
+          });
+        for (auto& w : tw) w.join();
+        int best = 0;
+        for (int t = 1; t < 4; t++)
+          if (bits[t] < bits[best]) best = t;
+        ep_rank[m] = std::move(trial[best]);
+      });
+    }
+    for (auto& w : workers) w.join();
+  }
+  for (int m = 0; m < 2; m++) {
+    if (comp_lo[m] == comp_hi[m]) continue;
+    ep_pal[m]->values = permuted(ep_pal[m]->values, ep_rank[m]);
+    sel_pal[m]->values = permuted(sel_pal[m]->values, sel_rank[m]);
+    for (uint64_t b = 0; b < nblocks; b++)
+      for (int c = comp_lo[m]; c < comp_hi[m]; c++) {
+        eidx[b * ncomp + c] = ep_rank[m][eidx[b * ncomp + c]];
+        sidx[b * ncomp + c] = sel_rank[m][sidx[b * ncomp + c]];
+      }
+  }
+  // block streams: the histograms first, then the coded streams
   std::vector<uint32_t> h_ref(256, 0), h_ep[2], h_sel[2];
   if (colour) { h_ep[0].assign(cep.values.size(), 0); h_sel[0].assign(csel.values.size(), 0); }
   if (nalpha) { h_ep[1].assign(aep.values.size(), 0); h_sel[1].assign(asel.values.size(), 0); }
-  // references of every block: 0 new (delta), 1 same as the previous block in decode order, 2 same
-  // as the block above (the faces of a level are one tall image to the decoder's row buffer)
-  auto refs_of = [&](const Lv& L, uint32_t f, uint32_t y, uint32_t x) -> uint32_t {
-    const uint64_t b = L.first + ((uint64_t)f * L.H + y) * L.W + x;
-    const uint32_t row = f * L.H + y;
-    bool left = row || x, top = row != 0;
-    for (int c = 0; c < ncomp; c++) {
-      const uint32_t e = eidx[b * ncomp + c];
-      if (left) left = e == eidx[(b - 1) * ncomp + c];
-      if (top) top = e == eidx[(b - L.W) * ncomp + c];
-    }
-    return left ? 1u : top ? 2u : 0u;
+  auto ref_at = [&](const Lv& L, uint32_t f, uint32_t y, uint32_t x) -> uint32_t {
+    return ref[L.first + ((uint64_t)f * L.H + y) * L.W + x];
   };
   Huff m_ref, m_ep[2], m_sel[2];
   std::vector<std::vector<uint8_t>> level_data(levels);
@@ -304,16 +666,15 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         for (uint32_t y = 0; y < L.H; y++)
           for (uint32_t x = 0; x < L.W; x++) {
             if (!(y & 1) && !(x & 1)) {
-              const uint32_t g = refs_of(L, f, y, x) | (refs_of(L, f, y + 1, x) << 2) | (refs_of(L, f, y, x + 1) << 4) |
-                                 (refs_of(L, f, y + 1, x + 1) << 6);
+              const uint32_t g = ref_at(L, f, y, x) | (ref_at(L, f, y + 1, x) << 2) | (ref_at(L, f, y, x + 1) << 4) |
+                                 (ref_at(L, f, y + 1, x + 1) << 6);
               if (pass) m_ref.put(bw, g); else h_ref[g]++;
             }
-            const uint32_t ref = refs_of(L, f, y, x);
             const uint64_t b = L.first + ((uint64_t)f * L.H + y) * L.W + x;
             for (int c = 0; c < ncomp; c++) {
               const int m = (colour && c == 0) ? 0 : 1;
               const uint32_t e = eidx[b * ncomp + c];
-              if (ref == 0) {
+              if (ref[b] == 0) {
                 const uint32_t n = (uint32_t)(m ? aep.values.size() : cep.values.size());
                 const uint32_t d = (e + n - prev[c]) % n;
                 if (pass) m_ep[m].put(bw, d); else h_ep[m][d]++;
@@ -329,94 +690,14 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
       if (pass) level_data[l] = bw.finish();
     }
   }
-  // palettes (crn_comp::pack_color_endpoints etc.; the inverse of crn_unpacker::decode_palettes,
-  // inc/crn_decomp.h:3715-3851)
   std::vector<uint8_t> pal[4];
   if (colour) {
-    // endpoints: six running component deltas, 5-bit model for red/blue, 6-bit for green
-    std::vector<uint32_t> f5(32, 0), f6(64, 0);
-    auto comps = [](uint32_t v, uint32_t* c) {
-      c[0] = (v >> 11) & 31; c[1] = (v >> 5) & 63; c[2] = v & 31;
-      c[3] = (v >> 27) & 31; c[4] = (v >> 21) & 63; c[5] = (v >> 16) & 31;
-    };
-    static const uint32_t kMask[6] = {31, 63, 31, 31, 63, 31};
-    static const int kModel[6] = {0, 1, 0, 0, 1, 0};
-    for (int pass = 0; pass < 2; pass++) {
-      Huff h5, h6;
-      BitWriter bw;
-      if (pass) {
-        ensure_used(f5); ensure_used(f6);
-        h5.build(f5, 16); h6.build(f6, 16);
-        send_model(bw, h5);
-        send_model(bw, h6);
-      }
-      uint32_t prev[6] = {0, 0, 0, 0, 0, 0};
-      for (uint64_t v : cep.values) {
-        uint32_t c[6];
-        comps((uint32_t)v, c);
-        for (int k = 0; k < 6; k++) {
-          const uint32_t d = (c[k] - prev[k]) & kMask[k];
-          prev[k] = c[k];
-          if (pass) (kModel[k] ? h6 : h5).put(bw, d);
-          else (kModel[k] ? f6 : f5)[d]++;
-        }
-      }
-      if (pass) pal[0] = bw.finish();
-    }
-    // selectors: XOR deltas of the linear words, 4 bits at a time
-    std::vector<uint32_t> fs(16, 0);
-    for (int pass = 0; pass < 2; pass++) {
-      Huff hs;
-      BitWriter bw;
-      if (pass) { ensure_used(fs); hs.build(fs, 16); send_model(bw, hs); }
-      uint32_t prev = 0;
-      for (uint64_t v : csel.values) {
-        const uint32_t d = (uint32_t)v ^ prev;
-        prev = (uint32_t)v;
-        for (int j = 0; j < 32; j += 4) {
-          const uint32_t x = (d >> j) & 15u;
-          if (pass) hs.put(bw, x); else fs[x]++;
-        }
-      }
-      if (pass) pal[1] = bw.finish();
-    }
+    pal[0] = pack_colour_endpoints(cep.values);
+    pal[1] = pack_colour_selectors(csel.values);
   }
   if (nalpha) {
-    // endpoints: two running 8-bit deltas
-    std::vector<uint32_t> fa(256, 0);
-    for (int pass = 0; pass < 2; pass++) {
-      Huff ha;
-      BitWriter bw;
-      if (pass) { ensure_used(fa); ha.build(fa, 16); send_model(bw, ha); }
-      uint32_t pa = 0, pb = 0;
-      for (uint64_t v : aep.values) {
-        const uint32_t a = (uint32_t)v & 255u, b = (uint32_t)(v >> 8) & 255u;
-        const uint32_t d0 = (a - pa) & 255u, d1 = (b - pb) & 255u;
-        pa = a; pb = b;
-        if (pass) { ha.put(bw, d0); ha.put(bw, d1); } else { fa[d0]++; fa[d1]++; }
-      }
-      if (pass) pal[2] = bw.finish();
-    }
-    // selectors: XOR deltas of the two 24-bit linear halves, 6 bits at a time
-    std::vector<uint32_t> fs(64, 0);
-    for (int pass = 0; pass < 2; pass++) {
-      Huff hs;
-      BitWriter bw;
-      if (pass) { ensure_used(fs); hs.build(fs, 16); send_model(bw, hs); }
-      uint32_t prev[2] = {0, 0};
-      for (uint64_t v : asel.values) {
-        for (int h = 0; h < 2; h++) {
-          const uint32_t half = (uint32_t)(v >> (24 * h)) & 0xFFFFFFu;
-          const uint32_t d = half ^ prev[h];
-          prev[h] = half;
-          for (int j = 0; j < 24; j += 6) {
-            const uint32_t x = (d >> j) & 63u;
-            if (pass) hs.put(bw, x); else fs[x]++;
-          }
-        }
-      }
-      if (pass) pal[3] = bw.finish();
-    }
+    pal[2] = pack_alpha_endpoints(aep.values);
+    pal[3] = pack_alpha_selectors(asel.values);
   }
   // the block-stream models (crn_comp::pack_data_models)
   std::vector<uint8_t> tables;

@@ -2377,3 +2377,84 @@ extern "C" int crngpu_hc_codebook_sizes(uint32_t width, uint32_t height, uint32_
   sizes4[3] = size(48, powf(quality, 1.65f * amul));  // alpha selectors
   return CRNGPU_OK;
 }
+
+// crn_compress with m_file_type = cCRNFileTypeCRN and source mips (inc/crnlib.h:614,
+// crnlib/crnlib.cpp:242-267 -> crn_comp::compress_internal, crnlib/crn_comp.cpp:1515-1611):
+// crn_comp's block gather (edge clamped, levels padded to 8 texels, crn_comp.cpp:717-741), the
+// clustered encode on the GPU, then the .crn writer on the host.
+extern "C" int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels,
+                                       uint32_t faces, uint32_t format, uint32_t quality_level, uint32_t flags,
+                                       void* out, uint64_t out_capacity) {
+  using namespace crngpu;
+  using namespace crngpu::hc;
+  clear_error();
+  if (!rgba_levels || !width || !height || width > 4096 || height > 4096 || !levels || levels > 16 ||
+      (faces != 1 && faces != 6) || quality_level > 255) {
+    set_error("crngpu_compress_crn: bad dimensions, level, face count or quality");
+    return CRNGPU_E_PARAM;
+  }
+  uint32_t full = 1;
+  while ((width >> full) || (height >> full)) full++;
+  if (levels > full) { set_error("crngpu_compress_crn: more levels than the mip chain has"); return CRNGPU_E_PARAM; }
+  // gather blocks: per level, per face, rows of the padded block width
+  crngpu_hc_params P;
+  std::memset(&P, 0, sizeof(P));
+  P.struct_size = sizeof(P);
+  std::vector<uint32_t> blocks;
+  std::vector<size_t> img_ofs((size_t)faces * levels);
+  size_t ofs = 0;
+  for (uint32_t f = 0; f < faces; f++)
+    for (uint32_t l = 0; l < levels; l++) {
+      img_ofs[(size_t)f * levels + l] = ofs;
+      ofs += (size_t)std::max(1u, width >> l) * std::max(1u, height >> l) * 4;
+    }
+  for (uint32_t l = 0; l < levels; l++) {
+    const uint32_t w = std::max(1u, width >> l), h = std::max(1u, height >> l);
+    const uint32_t W = ((w + 7) & ~7u) >> 2, H = ((h + 7) & ~7u) >> 2;
+    P.levels[l].first_block = (uint32_t)(blocks.size() / 16);
+    P.levels[l].num_blocks = W * H * faces;
+    P.levels[l].block_width = W;
+    P.levels[l].weight = std::min(12.0f, powf(1.3f, (float)l));
+    for (uint32_t f = 0; f < faces; f++) {
+      const uint32_t* img = reinterpret_cast<const uint32_t*>(rgba_levels + img_ofs[(size_t)f * levels + l]);
+      for (uint32_t by = 0; by < H; by++)
+        for (uint32_t bx = 0; bx < W; bx++)
+          for (uint32_t dy = 0; dy < 4; dy++)
+            for (uint32_t dx = 0; dx < 4; dx++) {
+              const uint32_t x = std::min(bx * 4 + dx, w - 1), y = std::min(by * 4 + dy, h - 1);
+              uint32_t px;
+              std::memcpy(&px, img + (size_t)y * w + x, 4);
+              blocks.push_back(px);
+            }
+    }
+  }
+  P.num_blocks = (uint32_t)(blocks.size() / 16);
+  P.num_levels = levels;
+  P.num_faces = faces;
+  const bool colour_fmt = format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5;
+  P.perceptual = colour_fmt && (flags & CRNGPU_FLAG_PERCEPTUAL) ? 1 : 0;
+  uint32_t sizes[4];
+  if (crngpu_hc_codebook_sizes(width, height, quality_level, format, sizes) != CRNGPU_OK) return CRNGPU_E_PARAM;
+  P.color_endpoint_codebook_size = sizes[0];
+  P.color_selector_codebook_size = sizes[1];
+  P.alpha_endpoint_codebook_size = sizes[2];
+  P.alpha_selector_codebook_size = sizes[3];
+  P.adaptive_tile_color_psnr_derating = 2.0f;
+  P.adaptive_tile_alpha_psnr_derating = 2.0f;
+  P.color_alpha_weighting_ratio = 3.0f;
+  P.alpha_component = 3;
+  const uint32_t bpb = (format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5A) ? 8 : 16;
+  DevBuf d_in, d_out;
+  cudaError_t e;
+  if ((e = d_in.ensure(blocks.size() * 4)) != cudaSuccess || (e = d_out.ensure((size_t)P.num_blocks * bpb)) != cudaSuccess)
+    return cuda_check(e, "alloc blocks");
+  if ((e = cudaMemcpy(d_in.ptr, blocks.data(), blocks.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+    return cuda_check(e, "copy blocks");
+  int rc = crngpu_hc_compress(static_cast<const uint8_t*>(d_in.ptr), &P, format, static_cast<uint8_t*>(d_out.ptr),
+                              nullptr, nullptr);
+  if (rc != CRNGPU_OK) return rc;
+  std::vector<uint8_t> dxt((size_t)P.num_blocks * bpb);
+  if ((e = cudaMemcpy(dxt.data(), d_out.ptr, dxt.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_check(e, "copy result");
+  return crngpu_crn_pack(dxt.data(), width, height, levels, faces, format, out, out_capacity);
+}

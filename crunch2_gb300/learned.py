@@ -19,11 +19,12 @@ import os
 
 PARAM_SHAPES = [(256, 48), (256,), (256, 256), (256,), (16, 256), (16,)]
 # Trained network shipped with the package:
-#   python -m crunch2_gb300.learned steps=16384 tau=0.75 bound_weight=0.25 out=<this path>
-# (16,777,216 training blocks from 64 seeded 2048x2048 colour textures, labels from the plain
-# GPU optimizer, 16384 AdamW steps of 8192 blocks (8 epochs), lr 1e-3, weight decay 0.01, init
-# seed 0; endpoint outputs trained on squared error, the error-bound output on the 0.75-quantile
-# pinball loss so that it is an upper bound of the plain optimizer's error for 75% of blocks).
+#   python -m crunch2_gb300.learned steps=16384 tau=0.75 bound_weight=0.25 mips=1 out=<this path>
+# (22,369,600 training blocks: 64 seeded 2048x2048 colour textures and their box-filtered mip
+# levels, labels from the plain GPU optimizer, 16384 AdamW steps of 8192 blocks, lr 1e-3, weight
+# decay 0.01, init seed 0; endpoint outputs trained on squared error, the error-bound output on
+# the 0.75-quantile pinball loss so that it is an upper bound of the plain optimizer's error for
+# 75% of blocks).
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights", "dxt1_endpoint_net.npz")
 DEFAULT_THRESHOLD = 1.5
 PARAM_NAMES = ["W1", "b1", "W2", "b2", "W3", "b3"]

@@ -178,6 +178,17 @@ CRNGPU_API int crngpu_hc_compress(const uint8_t* d_blocks, const crngpu_hc_param
 CRNGPU_API int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32_t height, uint32_t levels,
                                    uint32_t faces, uint32_t format, void* out, uint64_t out_capacity);
 
+/* Replaces crn_compress for .crn output with source mips (inc/crnlib.h:614, crnlib/crnlib.cpp:
+ * 242-267, m_file_type = cCRNFileTypeCRN, cCRNMipModeUseSourceMips): rgba_levels holds faces x
+ * levels RGBA8 images, face-major, level l being max(1, w >> l) x max(1, h >> l) texels, tightly
+ * packed and concatenated (the order of crn_comp_params::m_pImages[face][level]). format: DXT1,
+ * DXT5 (alpha = channel 3), DXN_XY/YX, DXT5A; quality_level 0..255 sets the codebook sizes;
+ * flags: CRNGPU_FLAG_PERCEPTUAL for the colour formats. Clustered encode on the GPU, .crn written
+ * on the host. Returns the file size (copied to `out` when out_capacity suffices) or an error. */
+CRNGPU_API int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels,
+                                       uint32_t faces, uint32_t format, uint32_t quality_level, uint32_t flags,
+                                       void* out, uint64_t out_capacity);
+
 /* Codebook sizes for a quality level (crn_comp::quantize_images, crnlib/crn_comp.cpp:541-577):
  * sizes4 = colour endpoints, colour selectors, alpha endpoints, alpha selectors. */
 CRNGPU_API int crngpu_hc_codebook_sizes(uint32_t width, uint32_t height, uint32_t quality_level, uint32_t format,

@@ -1,7 +1,8 @@
 """The .crn writer (crngpu_crn_pack, host code) against the decoders: every committed fixture is
 decoded, repacked by this library and decoded again -- by the oracle (the CPU restatement pinned
 to the reference) and, where it is built, by the reference's own crnd -- and must give back
-exactly the same DXTn blocks. No GPU needed."""
+exactly the same DXTn blocks, in a file no more than 1% larger than the reference's. No GPU
+needed."""
 import numpy as np
 import pytest
 
@@ -48,6 +49,8 @@ def test_repacked_fixture_decodes_to_the_same_blocks(cg, name):
             assert np.array_equal(ref.unpack_level(packed, l, info["bytes"]),
                                   np.concatenate([x.reshape(-1) for x in levels[l]])), (name, l, "reference crnd")
     print(f"{name}: reference .crn {len(crn)} bytes, repacked {len(packed)} bytes")
+    # palette ordering as crn_comp's: the same blocks code in about the reference's size
+    assert len(packed) <= 1.01 * len(crn), (name, len(packed), len(crn))
 
 
 def test_pack_rejects_unclusterable_and_bad_input(cg):

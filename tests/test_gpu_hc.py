@@ -138,3 +138,53 @@ def test_clustered_alpha_formats_match_reference_quality(hc, name):
         ra = float(np.sqrt((((x - src[:, :, 0]) ** 2).sum() + ((y - src[:, :, 1]) ** 2).sum()) / (2 * x.size)))
         print(f"{name}: alpha RMSE {ra:.4f} (reference {R['rmse_alpha_visible']:.4f}), stats {stats}")
     assert ra <= max(1.05 * R["rmse_alpha_visible"], R["rmse_alpha_visible"] + 0.02)
+
+
+@pytest.mark.parametrize("name", ["c1_dxt1_1024", "dxt5_256", "dxn_xy_256", "dxt1_cube_64"])
+def test_compress_crn_round_trip(hc, name):
+    """crngpu_compress_crn (crn_compress with source mips -> .crn): the file transcodes on the GPU
+    and in the oracle to the same blocks, at the reference's quality and a comparable size."""
+    import crunch2_gb300 as cg
+    from crunch2_gb300 import texgen
+    from oracle import port
+    from dxt_decode import dxt5a_values
+    m = G.manifest()[name]
+    w, h, faces = m["width"], m["height"], m["faces"]
+    fmt = {"DXT1": cg.FMT_DXT1, "DXT5": cg.FMT_DXT5, "DXN_XY": cg.FMT_DXN_XY}[m["format"]]
+    fl = []
+    for f in range(faces):
+        img = texgen.normal_map(w, h, m["seed"] + f) if m["content"] == "normal" else \
+            texgen.colour_texture(w, h, m["seed"] + f, with_alpha_noise=(m["content"] == "colour_alpha"))
+        fl.append(texgen.mip_chain(img))
+    flags = 0 if m["content"] == "normal" else cg.FLAG_PERCEPTUAL
+    crn = cg.compress_crn(fl, fmt, quality=128, flags=flags)
+    ref_crn = G.crn_bytes(name)
+    bpb = G.bytes_per_block(m["format"])
+    ours_se = ref_se = 0.0
+    with cg.unpack_begin(crn) as ctx:
+        assert (ctx.width, ctx.height, ctx.levels, ctx.faces) == (w, h, len(fl[0]), faces)
+        for l, info in enumerate(m["levels"]):
+            gpu = ctx.unpack_level(l).reshape(-1)
+            assert np.array_equal(gpu, port.unpack_level(crn, l, info["bytes"])), (name, l)
+            ref = port.unpack_level(ref_crn, l, info["bytes"])
+            src = np.concatenate([texgen.image_blocks(fl[f][l]) for f in range(faces)]).reshape(-1, 16, 4).astype(np.int64)
+            for dec, acc in ((gpu, "ours"), (ref, "ref")):
+                d = dec.reshape(-1, bpb)
+                if m["format"] == "DXT1":
+                    from dxt_decode import dxt1_colours
+                    se = float(((dxt1_colours(d) - src[:, :, :3]) ** 2).sum())
+                elif m["format"] == "DXT5":
+                    from dxt_decode import dxt1_colours
+                    se = float(((dxt1_colours(d[:, 8:]) - src[:, :, :3]) ** 2).sum() +
+                               ((dxt5a_values(d[:, :8]) - src[:, :, 3]) ** 2).sum())
+                else:
+                    se = float(((dxt5a_values(d[:, :8]) - src[:, :, 0]) ** 2).sum() +
+                               ((dxt5a_values(d[:, 8:]) - src[:, :, 1]) ** 2).sum())
+                if acc == "ours":
+                    ours_se += se
+                else:
+                    ref_se += se
+    print(f"{name}: .crn {len(crn)} bytes (reference {len(ref_crn)}), squared error {ours_se:.0f} "
+          f"(reference {ref_se:.0f})")
+    assert ours_se <= 1.06 * ref_se
+    assert len(crn) <= 1.4 * len(ref_crn)
