@@ -35,10 +35,13 @@
 #include <memory>
 #include <vector>
 
+#include <cooperative_groups.h>
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_select.cuh>
 
 #include "crngpu_internal.h"
+
+namespace cg = cooperative_groups;
 
 namespace crngpu {
 namespace hc {
@@ -604,10 +607,15 @@ __global__ void __launch_bounds__(64) k_hc_tiles(const uint32_t* __restrict__ bl
 }
 
 // ------------------------------------------------------------------------------------------
-// Tree clusterizer, batched: one CTA per node to split.
+// Tree clusterizer, batched: one thread-block cluster per node to split. The node's vectors lie
+// contiguously (a split moves them, with their weights, into the other of two buffers: lefts, then
+// rights, each in their previous order), so every pass over a node is a coalesced stream; large
+// nodes get up to 16 CTAs on as many SMs, whose partial sums meet through distributed shared
+// memory.
 
 constexpr int kVqThreads = 512;
 constexpr uint32_t kDefaultRoundFraction = 4;  // a VQ round splits at most leaves / 4 nodes
+constexpr uint32_t kVqPerCta = 2048;            // vectors per CTA below which a node gets fewer CTAs
 
 template <int D>
 struct VqNode {
@@ -616,7 +624,8 @@ struct VqNode {
   float variance;     // weighted variance (sum of squared deviations)
   uint32_t begin, end;
   int32_t left, right;  // children (-1: leaf)
-  uint32_t unsplittable;
+  uint32_t unsplittable;  // 1: this node cannot be split; 2 (on a left child): its parent could not
+  uint32_t buf;           // which of the two vector buffers holds this node's range
 };
 
 struct SplitJob { int32_t parent, left, right; };
@@ -657,6 +666,97 @@ __device__ __forceinline__ void block_argmax(float& v, uint32_t& pos, float* rv,
     if (rv[w] > v || (rv[w] == v && rp[w] < pos)) { v = rv[w]; pos = rp[w]; }
 }
 
+// Cluster-wide exchange slots: each reduction writes its CTA's partial into slot[phase] and flips
+// the phase, so a slot is rewritten only after a later cluster barrier, by which time every CTA has
+// read it.
+constexpr int kVqSlot = 40;
+struct VqShared {
+  float red[kVqSlot * 16];
+  float rv[16];
+  uint32_t rp[16];
+  float part[2][kVqSlot];
+  uint32_t upart[2][2];
+  float tot[kVqSlot];
+  float stage[16][kVqSlot];
+  uint32_t ustage[16][2];
+  uint32_t scan[2][kVqThreads / 32 + 1];
+};
+
+// cluster-wide sum of N floats per thread; every CTA adds the partials in rank order, so all of
+// them hold bit-identical totals and take the same branches. Warps reduce by shuffles; N threads
+// add the warps' partials; the CTAs' partials are fetched through distributed shared memory in one
+// parallel round trip and added by N threads.
+template <int N>
+__device__ __forceinline__ void cluster_sum(float* vals, VqShared& sh, int& phase, cg::cluster_group& cl) {
+  static_assert(N <= kVqSlot, "cluster_sum slot");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < N; k++)
+    for (int o = 16; o > 0; o >>= 1) vals[k] += __shfl_xor_sync(0xFFFFFFFFu, vals[k], o);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < N; k++) sh.red[k * 16 + warp] = vals[k];
+  __syncthreads();
+  if (threadIdx.x < N) {
+    float t = 0.f;
+    for (int wi = 0; wi < nw; wi++) t += sh.red[threadIdx.x * 16 + wi];
+    sh.part[phase][threadIdx.x] = t;
+  }
+  cl.sync();
+  const unsigned C = cl.num_blocks();
+  for (unsigned t = threadIdx.x; t < N * C; t += blockDim.x)
+    sh.stage[t / N][t % N] = cl.map_shared_rank(&sh.part[phase][0], t / N)[t % N];
+  __syncthreads();
+  if (threadIdx.x < N) {
+    float t = 0.f;
+    for (unsigned q = 0; q < C; q++) t += sh.stage[q][threadIdx.x];
+    sh.tot[threadIdx.x] = t;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < N; k++) vals[k] = sh.tot[k];
+  phase ^= 1;
+}
+
+__device__ __forceinline__ void cluster_argmax(float& v, uint32_t& pos, VqShared& sh, int& phase, cg::cluster_group& cl) {
+  block_argmax(v, pos, sh.rv, sh.rp);
+  if (threadIdx.x == 0) { sh.part[phase][0] = v; sh.upart[phase][0] = pos; }
+  cl.sync();
+  const unsigned C = cl.num_blocks();
+  if (threadIdx.x < C) {
+    sh.stage[threadIdx.x][0] = cl.map_shared_rank(&sh.part[phase][0], threadIdx.x)[0];
+    sh.ustage[threadIdx.x][0] = cl.map_shared_rank(&sh.upart[phase][0], threadIdx.x)[0];
+  }
+  __syncthreads();
+  for (unsigned q = 0; q < C; q++) {
+    const float qv = sh.stage[q][0];
+    const uint32_t qp = sh.ustage[q][0];
+    if (qv > v || (qv == v && qp < pos)) { v = qv; pos = qp; }
+  }
+  __syncthreads();
+  phase ^= 1;
+}
+
+template <int D>
+__device__ __forceinline__ void load_vec(const float* __restrict__ p, float* v) {
+  if constexpr (D % 4 == 0) {
+#pragma unroll
+    for (int k = 0; k < D; k += 4) {
+      const float4 q = __ldg(reinterpret_cast<const float4*>(p + k));
+      v[k] = q.x; v[k + 1] = q.y; v[k + 2] = q.z; v[k + 3] = q.w;
+    }
+  } else if constexpr (D % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < D; k += 2) {
+      const float2 q = __ldg(reinterpret_cast<const float2*>(p + k));
+      v[k] = q.x; v[k + 1] = q.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < D; k++) v[k] = __ldg(p + k);
+  }
+}
+
 template <int D>
 __device__ __forceinline__ float dist2(const float* a, const float* b) {
   float s = 0.f;
@@ -665,20 +765,29 @@ __device__ __forceinline__ float dist2(const float* a, const float* b) {
   return s;
 }
 
-// Splits node `parent` of the perm range [begin, end) into two children (tree_clusterizer::split_node,
-// crn_tree_clusterizer.h:265-570). vec: N x D floats, w: weights, perm/tmp: index permutations.
+// Splits each job's parent node into two children (tree_clusterizer::split_node,
+// crn_tree_clusterizer.h:265-570): furthest / opposite seeds, the principal axis by 10 steps of
+// power iteration on the weighted covariance, the axis split as the 2-means start, then 2-means
+// until the variance stops falling. vec[2] / w[2]: the two buffers (N x D floats, N weights).
+// One cluster of CTAs per job; CTA r of C works on the r-th contiguous slice of the node's range.
 template <int D>
-__global__ void __launch_bounds__(kVqThreads) k_vq_split(const float* __restrict__ vec, const uint32_t* __restrict__ w,
-                                                         uint32_t* __restrict__ perm, uint32_t* __restrict__ tmp,
+__global__ void __launch_bounds__(kVqThreads) k_vq_split(float* __restrict__ vec0, float* __restrict__ vec1,
+                                                         float* __restrict__ w0, float* __restrict__ w1,
                                                          VqNode<D>* __restrict__ nodes, const SplitJob* __restrict__ jobs) {
-  __shared__ float red[(2 * D + 4) * 16];
-  __shared__ float rv[16];
-  __shared__ uint32_t rp[16];
+  __shared__ VqShared sh;
   __shared__ float s_c[D];
-  __shared__ uint32_t s_scan[kVqThreads / 32 + 1];
-  const SplitJob job = jobs[blockIdx.x];
+  cg::cluster_group cl = cg::this_cluster();
+  const unsigned C = cl.num_blocks(), r = cl.block_rank();
+  int phase = 0;
+  const SplitJob job = jobs[blockIdx.x / C];
   VqNode<D>& P = nodes[job.parent];
-  const uint32_t b0 = P.begin, b1 = P.end;
+  const uint32_t b0 = P.begin, b1 = P.end, src = P.buf;
+  const float* __restrict__ vec = src ? vec1 : vec0;
+  const float* __restrict__ w = src ? w1 : w0;
+  float* __restrict__ dvec = src ? vec0 : vec1;
+  float* __restrict__ dw = src ? w0 : w1;
+  const uint32_t per = (b1 - b0 + C - 1) / C;
+  const uint32_t s0 = min(b1, b0 + r * per), s1 = min(b1, s0 + per);  // this CTA's slice
   if (threadIdx.x < D) s_c[threadIdx.x] = P.c[threadIdx.x];
   __syncthreads();
   float c[D];
@@ -687,28 +796,36 @@ __global__ void __launch_bounds__(kVqThreads) k_vq_split(const float* __restrict
   // furthest from the centroid, then the point furthest from that
   float fv = -1.f;
   uint32_t fp = 0xFFFFFFFFu;
-  for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-    const float d = dist2<D>(vec + (size_t)perm[i] * D, c);
+  for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+    float v[D];
+    load_vec<D>(vec + (size_t)i * D, v);
+    const float d = dist2<D>(v, c);
     if (d > fv) { fv = d; fp = i; }
   }
-  block_argmax(fv, fp, rv, rp);
+  cluster_argmax(fv, fp, sh, phase, cl);
+  if (fp >= b1) fp = b0;  // only if every distance were NaN
   float fur[D];
-#pragma unroll
-  for (int k = 0; k < D; k++) fur[k] = vec[(size_t)perm[fp] * D + k];
+  load_vec<D>(vec + (size_t)fp * D, fur);
   float ov = -1.f;
   uint32_t op = 0xFFFFFFFFu;
-  for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-    const float d = dist2<D>(vec + (size_t)perm[i] * D, fur);
+  for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+    float v[D];
+    load_vec<D>(vec + (size_t)i * D, v);
+    const float d = dist2<D>(v, fur);
     if (d > ov) { ov = d; op = i; }
   }
-  block_argmax(ov, op, rv, rp);
+  cluster_argmax(ov, op, sh, phase, cl);
+  if (op >= b1) op = b0;
   float L[D], R[D];
+  {
+    float opp[D];
+    load_vec<D>(vec + (size_t)op * D, opp);
 #pragma unroll
-  for (int k = 0; k < D; k++) {
-    L[k] = (fur[k] + c[k]) * 0.5f;
-    R[k] = (vec[(size_t)perm[op] * D + k] + c[k]) * 0.5f;
+    for (int k = 0; k < D; k++) {
+      L[k] = (fur[k] + c[k]) * 0.5f;
+      R[k] = (opp[k] + c[k]) * 0.5f;
+    }
   }
-  const double tw = P.weight;
   if (b0 + 2 < b1) {
     // principal axis by power iteration on the weighted covariance, applied implicitly:
     // x = Cov a = sum_i w_i (v_i - c) ((v_i - c) . a) / W, normalised by its largest component
@@ -719,16 +836,16 @@ __global__ void __launch_bounds__(kVqThreads) k_vq_split(const float* __restrict
       float acc[D];
 #pragma unroll
       for (int k = 0; k < D; k++) acc[k] = 0.f;
-      for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-        const float* v = vec + (size_t)perm[i] * D;
+      for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
         float d[D], dot = 0.f;
+        load_vec<D>(vec + (size_t)i * D, d);
 #pragma unroll
-        for (int k = 0; k < D; k++) { d[k] = v[k] - c[k]; dot += d[k] * axis[k]; }
-        const float ww = (float)w[perm[i]] * dot;
+        for (int k = 0; k < D; k++) { d[k] -= c[k]; dot += d[k] * axis[k]; }
+        const float ww = w[i] * dot;
 #pragma unroll
         for (int k = 0; k < D; k++) acc[k] += d[k] * ww;
       }
-      block_sum<D>(acc, red);
+      cluster_sum<D>(acc, sh, phase, cl);
       float mx = acc[0];
 #pragma unroll
       for (int k = 1; k < D; k++) mx = fmaxf(mx, acc[k]);
@@ -751,46 +868,304 @@ __global__ void __launch_bounds__(kVqThreads) k_vq_split(const float* __restrict
     float acc[2 * D + 2];
 #pragma unroll
     for (int k = 0; k < 2 * D + 2; k++) acc[k] = 0.f;
-    for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-      const float* v = vec + (size_t)perm[i] * D;
+    for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+      float v[D];
+      load_vec<D>(vec + (size_t)i * D, v);
       float t = 0.f;
 #pragma unroll
       for (int k = 0; k < D; k++) t += (v[k] - c[k]) * axis[k];
-      const float ww = (float)w[perm[i]];
-      const int side = t < 0.f ? 0 : 1;
+      const float ww = w[i];
+      const float wl = t < 0.f ? ww : 0.f, wr = t < 0.f ? 0.f : ww;
 #pragma unroll
-      for (int k = 0; k < D; k++) acc[side * D + k] += v[k] * ww;
-      acc[2 * D + side] += ww;
+      for (int k = 0; k < D; k++) { acc[k] += v[k] * wl; acc[D + k] += v[k] * wr; }
+      acc[2 * D] += wl;
+      acc[2 * D + 1] += wr;
     }
-    block_sum<2 * D + 2>(acc, red);
+    cluster_sum<2 * D + 2>(acc, sh, phase, cl);
     if (acc[2 * D] > 0.f && acc[2 * D + 1] > 0.f) {
 #pragma unroll
       for (int k = 0; k < D; k++) { L[k] = acc[k] / acc[2 * D]; R[k] = acc[D + k] / acc[2 * D + 1]; }
     }
   }
-  // 2-means; the partition is the last assignment (made with the centroids before their update)
+  // 2-means; the partition is the last assignment (made with the centroids before their update).
+  // The updated centroids live in shared memory; the assignment centroids in registers.
+  __shared__ float s_L[D], s_R[D];
+#pragma unroll
+  for (int k = 0; k < D; k++)
+    if (threadIdx.x == k) { s_L[k] = L[k]; s_R[k] = R[k]; }
   float prev = 1e10f, lvar = 0.f, rvar = 0.f, lw = 0.f, rw = 0.f;
   float AL[D], AR[D];  // centroids of the last assignment
   for (int loop = 0; loop < 1024; loop++) {
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < D; k++) { AL[k] = s_L[k]; AR[k] = s_R[k]; }
     float acc[2 * D + 4];
 #pragma unroll
     for (int k = 0; k < 2 * D + 4; k++) acc[k] = 0.f;
-#pragma unroll
-    for (int k = 0; k < D; k++) { AL[k] = L[k]; AR[k] = R[k]; }
-    for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-      const float* v = vec + (size_t)perm[i] * D;
+    for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
       float vv[D];
-#pragma unroll
-      for (int k = 0; k < D; k++) vv[k] = v[k];
-      const float ww = (float)w[perm[i]];
-      const int side = dist2<D>(AL, vv) < dist2<D>(AR, vv) ? 0 : 1;
+      load_vec<D>(vec + (size_t)i * D, vv);
+      const float ww = w[i];
+      const bool left = dist2<D>(AL, vv) < dist2<D>(AR, vv);
+      const float wl = left ? ww : 0.f, wr = left ? 0.f : ww;
       float sq = 0.f;
 #pragma unroll
-      for (int k = 0; k < D; k++) { acc[side * D + k] += vv[k] * ww; sq += vv[k] * vv[k]; }
-      acc[2 * D + side] += ww;
-      acc[2 * D + 2 + side] += sq * ww;
+      for (int k = 0; k < D; k++) { acc[k] += vv[k] * wl; acc[D + k] += vv[k] * wr; sq += vv[k] * vv[k]; }
+      acc[2 * D] += wl;
+      acc[2 * D + 1] += wr;
+      acc[2 * D + 2] += sq * wl;
+      acc[2 * D + 3] += sq * wr;
     }
-    block_sum<2 * D + 4>(acc, red);
+    cluster_sum<2 * D + 4>(acc, sh, phase, cl);
+    lw = acc[2 * D]; rw = acc[2 * D + 1];
+    if (!(lw > 0.f) || !(rw > 0.f)) break;
+    float ll = 0.f, rr = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; k++) { ll += acc[k] * acc[k]; rr += acc[D + k] * acc[D + k]; }
+    lvar = acc[2 * D + 2] - ll / lw;
+    rvar = acc[2 * D + 3] - rr / rw;
+    // every thread read s_L / s_R before cluster_sum's barriers
+#pragma unroll
+    for (int k = 0; k < D; k++)
+      if (threadIdx.x == k) { s_L[k] = acc[k] / lw; s_R[k] = acc[D + k] / rw; }
+    const float tv = lvar + rvar;
+    if (tv < .00001f) break;
+    if ((prev - tv) / tv < .00001f) break;
+    prev = tv;
+  }
+  __syncthreads();
+  if (!(lw > 0.f) || !(rw > 0.f)) {
+    if (r == 0 && threadIdx.x == 0) {
+      P.unsplittable = 1;
+      nodes[job.left].unsplittable = 2;
+    }
+    cl.sync();  // no CTA leaves while another may still read its shared memory
+    return;
+  }
+  // stable partition of the node by the last assignment into the other buffer: lefts first, then
+  // rights, each keeping its order. Count this slice's lefts, exchange the counts, then place.
+  uint32_t my_left = 0;
+  for (uint32_t base = s0; base < s1; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    bool left = false;
+    if (i < s1) {
+      float vv[D];
+      load_vec<D>(vec + (size_t)i * D, vv);
+      left = dist2<D>(AL, vv) < dist2<D>(AR, vv);
+    }
+    my_left += (uint32_t)__syncthreads_count(left);
+  }
+  if (threadIdx.x == 0) { sh.upart[phase][0] = my_left; sh.upart[phase][1] = s1 - s0; }
+  cl.sync();
+  if (threadIdx.x < 2 * C) sh.ustage[threadIdx.x >> 1][threadIdx.x & 1] = cl.map_shared_rank(&sh.upart[phase][0], threadIdx.x >> 1)[threadIdx.x & 1];
+  __syncthreads();
+  uint32_t left_before = 0, right_before = 0, left_total = 0;
+  for (unsigned q = 0; q < C; q++) {
+    const uint32_t ql = sh.ustage[q][0], qn = sh.ustage[q][1];
+    left_total += ql;
+    if (q < r) { left_before += ql; right_before += qn - ql; }
+  }
+  phase ^= 1;
+  uint32_t lrun = b0 + left_before, rrun = b0 + left_total + right_before;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int sb = 0;
+  for (uint32_t base = s0; base < s1; base += blockDim.x) {
+    const uint32_t i = base + threadIdx.x;
+    const bool live = i < s1;
+    float vv[D];
+    bool left = false;
+    if (live) {
+      load_vec<D>(vec + (size_t)i * D, vv);
+      left = dist2<D>(AL, vv) < dist2<D>(AR, vv);
+    }
+    const uint32_t bl = __ballot_sync(0xFFFFFFFFu, live && left), br = __ballot_sync(0xFFFFFFFFu, live && !left);
+    if (lane == 0) { sh.scan[sb][warp] = __popc(bl); sh.scan[sb][warp] |= (uint32_t)__popc(br) << 16; }
+    __syncthreads();
+    uint32_t lpre = 0, rpre = 0, ltot = 0, rtot = 0;
+    for (int wi = 0; wi < nw; wi++) {
+      const uint32_t t = sh.scan[sb][wi];
+      if (wi < warp) { lpre += t & 0xFFFFu; rpre += t >> 16; }
+      ltot += t & 0xFFFFu;
+      rtot += t >> 16;
+    }
+    if (live) {
+      const uint32_t dst = left ? lrun + lpre + __popc(bl & ((1u << lane) - 1u)) : rrun + rpre + __popc(br & ((1u << lane) - 1u));
+#pragma unroll
+      for (int k = 0; k < D; k++) dvec[(size_t)dst * D + k] = vv[k];
+      dw[dst] = w[i];
+    }
+    lrun += ltot;
+    rrun += rtot;
+    sb ^= 1;  // the next window's counts go to the other slot; this one is rewritten after a barrier
+  }
+  if (r == 0 && threadIdx.x == 0) {
+    VqNode<D>& A = nodes[job.left];
+    VqNode<D>& B = nodes[job.right];
+    for (int k = 0; k < D; k++) { A.c[k] = s_L[k]; B.c[k] = s_R[k]; }
+    A.weight = lw; B.weight = rw;
+    A.variance = lvar; B.variance = rvar;
+    A.begin = b0; A.end = b0 + left_total;
+    B.begin = b0 + left_total; B.end = b1;
+    A.left = A.right = B.left = B.right = -1;
+    A.unsplittable = B.unsplittable = 0;
+    A.buf = B.buf = src ^ 1u;
+    P.left = job.left;
+    P.right = job.right;
+  }
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+// The same split for small nodes, one warp per job (8 jobs per CTA): the reductions are warp
+// butterflies, which leave bit-identical totals in every lane, and no CTA-wide barrier is needed.
+constexpr uint32_t kVqWarpMax = 256;  // nodes up to this many vectors take the warp kernel
+
+template <int N>
+__device__ __forceinline__ void warp_sum(float* vals) {
+#pragma unroll
+  for (int k = 0; k < N; k++)
+    for (int o = 16; o > 0; o >>= 1) vals[k] += __shfl_xor_sync(0xFFFFFFFFu, vals[k], o);
+}
+
+__device__ __forceinline__ void warp_argmax(float& v, uint32_t& pos) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const float ov = __shfl_xor_sync(0xFFFFFFFFu, v, o);
+    const uint32_t op = __shfl_xor_sync(0xFFFFFFFFu, pos, o);
+    if (ov > v || (ov == v && op < pos)) { v = ov; pos = op; }
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256, 2) k_vq_split_warp(float* __restrict__ vec0, float* __restrict__ vec1,
+                                                       float* __restrict__ w0, float* __restrict__ w1,
+                                                       VqNode<D>* __restrict__ nodes, const SplitJob* __restrict__ jobs,
+                                                       uint32_t njobs) {
+  const uint32_t jid = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (jid >= njobs) return;  // whole warps only
+  const uint32_t lane = threadIdx.x & 31;
+  const SplitJob job = jobs[jid];
+  VqNode<D>& P = nodes[job.parent];
+  const uint32_t b0 = P.begin, b1 = P.end, src = P.buf;
+  const float* __restrict__ vec = src ? vec1 : vec0;
+  const float* __restrict__ w = src ? w1 : w0;
+  float* __restrict__ dvec = src ? vec0 : vec1;
+  float* __restrict__ dw = src ? w0 : w1;
+  float c[D];
+#pragma unroll
+  for (int k = 0; k < D; k++) c[k] = P.c[k];
+  float fv = -1.f;
+  uint32_t fp = 0xFFFFFFFFu;
+  for (uint32_t i = b0 + lane; i < b1; i += 32) {
+    float v[D];
+    load_vec<D>(vec + (size_t)i * D, v);
+    const float d = dist2<D>(v, c);
+    if (d > fv) { fv = d; fp = i; }
+  }
+  warp_argmax(fv, fp);
+  if (fp >= b1) fp = b0;  // only if every distance were NaN
+  float fur[D];
+  load_vec<D>(vec + (size_t)fp * D, fur);
+  float ov = -1.f;
+  uint32_t op = 0xFFFFFFFFu;
+  for (uint32_t i = b0 + lane; i < b1; i += 32) {
+    float v[D];
+    load_vec<D>(vec + (size_t)i * D, v);
+    const float d = dist2<D>(v, fur);
+    if (d > ov) { ov = d; op = i; }
+  }
+  warp_argmax(ov, op);
+  if (op >= b1) op = b0;
+  float L[D], R[D];
+  {
+    float opp[D];
+    load_vec<D>(vec + (size_t)op * D, opp);
+#pragma unroll
+    for (int k = 0; k < D; k++) {
+      L[k] = (fur[k] + c[k]) * 0.5f;
+      R[k] = (opp[k] + c[k]) * 0.5f;
+    }
+  }
+  if (b0 + 2 < b1) {
+    float axis[D];
+#pragma unroll
+    for (int k = 0; k < D; k++) axis[k] = 1.0f;
+    for (int it = 0; it < 10; it++) {
+      float acc[D];
+#pragma unroll
+      for (int k = 0; k < D; k++) acc[k] = 0.f;
+      for (uint32_t i = b0 + lane; i < b1; i += 32) {
+        float d[D], dot = 0.f;
+        load_vec<D>(vec + (size_t)i * D, d);
+#pragma unroll
+        for (int k = 0; k < D; k++) { d[k] -= c[k]; dot += d[k] * axis[k]; }
+        const float ww = w[i] * dot;
+#pragma unroll
+        for (int k = 0; k < D; k++) acc[k] += d[k] * ww;
+      }
+      warp_sum<D>(acc);
+      float mx = acc[0];
+#pragma unroll
+      for (int k = 1; k < D; k++) mx = fmaxf(mx, acc[k]);
+      if (mx != 0.f) {
+#pragma unroll
+        for (int k = 0; k < D; k++) axis[k] = acc[k] * (1.0f / mx);
+      } else {
+#pragma unroll
+        for (int k = 0; k < D; k++) axis[k] = acc[k];
+      }
+    }
+    float len = 0.f;
+#pragma unroll
+    for (int k = 0; k < D; k++) len += axis[k] * axis[k];
+    len = sqrtf(len);
+    if (len > 0.f) {
+#pragma unroll
+      for (int k = 0; k < D; k++) axis[k] /= len;
+    }
+    float acc[2 * D + 2];
+#pragma unroll
+    for (int k = 0; k < 2 * D + 2; k++) acc[k] = 0.f;
+    for (uint32_t i = b0 + lane; i < b1; i += 32) {
+      float v[D];
+      load_vec<D>(vec + (size_t)i * D, v);
+      float t = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; k++) t += (v[k] - c[k]) * axis[k];
+      const float ww = w[i];
+      const float wl = t < 0.f ? ww : 0.f, wr = t < 0.f ? 0.f : ww;
+#pragma unroll
+      for (int k = 0; k < D; k++) { acc[k] += v[k] * wl; acc[D + k] += v[k] * wr; }
+      acc[2 * D] += wl;
+      acc[2 * D + 1] += wr;
+    }
+    warp_sum<2 * D + 2>(acc);
+    if (acc[2 * D] > 0.f && acc[2 * D + 1] > 0.f) {
+#pragma unroll
+      for (int k = 0; k < D; k++) { L[k] = acc[k] / acc[2 * D]; R[k] = acc[D + k] / acc[2 * D + 1]; }
+    }
+  }
+  float prev = 1e10f, lvar = 0.f, rvar = 0.f, lw = 0.f, rw = 0.f;
+  float AL[D], AR[D];
+  for (int loop = 0; loop < 1024; loop++) {
+#pragma unroll
+    for (int k = 0; k < D; k++) { AL[k] = L[k]; AR[k] = R[k]; }
+    float acc[2 * D + 4];
+#pragma unroll
+    for (int k = 0; k < 2 * D + 4; k++) acc[k] = 0.f;
+    for (uint32_t i = b0 + lane; i < b1; i += 32) {
+      float vv[D];
+      load_vec<D>(vec + (size_t)i * D, vv);
+      const float ww = w[i];
+      const bool left = dist2<D>(AL, vv) < dist2<D>(AR, vv);
+      const float wl = left ? ww : 0.f, wr = left ? 0.f : ww;
+      float sq = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; k++) { acc[k] += vv[k] * wl; acc[D + k] += vv[k] * wr; sq += vv[k] * vv[k]; }
+      acc[2 * D] += wl;
+      acc[2 * D + 1] += wr;
+      acc[2 * D + 2] += sq * wl;
+      acc[2 * D + 3] += sq * wr;
+    }
+    warp_sum<2 * D + 4>(acc);
     lw = acc[2 * D]; rw = acc[2 * D + 1];
     if (!(lw > 0.f) || !(rw > 0.f)) break;
     float ll = 0.f, rr = 0.f;
@@ -806,91 +1181,149 @@ __global__ void __launch_bounds__(kVqThreads) k_vq_split(const float* __restrict
     prev = tv;
   }
   if (!(lw > 0.f) || !(rw > 0.f)) {
-    if (threadIdx.x == 0) P.unsplittable = 1;
+    if (lane == 0) {
+      P.unsplittable = 1;
+      nodes[job.left].unsplittable = 2;
+    }
     return;
   }
-  // stable partition of perm[b0, b1) by the last assignment: lefts first (pass 0), then rights (pass 1)
-  uint32_t nleft_total = 0, nright_done = 0;
-  for (int pass = 0; pass < 2; pass++) {
-    for (uint32_t base = b0; base < b1; base += blockDim.x) {
-      const uint32_t i = base + threadIdx.x;
-      bool take = false;
-      uint32_t pi = 0;
-      if (i < b1) {
-        pi = perm[i];
-        float vv[D];
-#pragma unroll
-        for (int k = 0; k < D; k++) vv[k] = vec[(size_t)pi * D + k];
-        const bool left = dist2<D>(AL, vv) < dist2<D>(AR, vv);
-        take = pass == 0 ? left : !left;
-      }
-      const uint32_t ballot = __ballot_sync(0xFFFFFFFFu, take);
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-      __syncthreads();
-      if (lane == 0) s_scan[warp] = __popc(ballot);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        uint32_t run = 0;
-        for (int wi = 0; wi < (int)(blockDim.x >> 5); wi++) { const uint32_t t = s_scan[wi]; s_scan[wi] = run; run += t; }
-        s_scan[kVqThreads / 32] = run;
-      }
-      __syncthreads();
-      const uint32_t rank = s_scan[warp] + __popc(ballot & ((1u << lane) - 1u));
-      if (take) tmp[b0 + (pass == 0 ? nleft_total : nleft_total + nright_done) + rank] = pi;
-      if (pass == 0) nleft_total += s_scan[kVqThreads / 32];
-      else nright_done += s_scan[kVqThreads / 32];
+  uint32_t left_total = 0;
+  for (uint32_t base = b0; base < b1; base += 32) {
+    const uint32_t i = base + lane;
+    bool left = false;
+    if (i < b1) {
+      float vv[D];
+      load_vec<D>(vec + (size_t)i * D, vv);
+      left = dist2<D>(AL, vv) < dist2<D>(AR, vv);
     }
+    left_total += (uint32_t)__popc(__ballot_sync(0xFFFFFFFFu, left));
   }
-  __syncthreads();
-  for (uint32_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) perm[i] = tmp[i];
-  if (threadIdx.x == 0) {
+  uint32_t lrun = b0, rrun = b0 + left_total;
+  for (uint32_t base = b0; base < b1; base += 32) {
+    const uint32_t i = base + lane;
+    const bool live = i < b1;
+    float vv[D];
+    bool left = false;
+    if (live) {
+      load_vec<D>(vec + (size_t)i * D, vv);
+      left = dist2<D>(AL, vv) < dist2<D>(AR, vv);
+    }
+    const uint32_t bl = __ballot_sync(0xFFFFFFFFu, live && left), br = __ballot_sync(0xFFFFFFFFu, live && !left);
+    if (live) {
+      const uint32_t below = (1u << lane) - 1u;
+      const uint32_t dst = left ? lrun + __popc(bl & below) : rrun + __popc(br & below);
+#pragma unroll
+      for (int k = 0; k < D; k++) dvec[(size_t)dst * D + k] = vv[k];
+      dw[dst] = w[i];
+    }
+    lrun += __popc(bl);
+    rrun += __popc(br);
+  }
+  if (lane == 0) {
     VqNode<D>& A = nodes[job.left];
     VqNode<D>& B = nodes[job.right];
     for (int k = 0; k < D; k++) { A.c[k] = L[k]; B.c[k] = R[k]; }
     A.weight = lw; B.weight = rw;
     A.variance = lvar; B.variance = rvar;
-    A.begin = b0; A.end = b0 + nleft_total;
-    B.begin = b0 + nleft_total; B.end = b1;
+    A.begin = b0; A.end = b0 + left_total;
+    B.begin = b0 + left_total; B.end = b1;
     A.left = A.right = B.left = B.right = -1;
     A.unsplittable = B.unsplittable = 0;
+    A.buf = B.buf = src ^ 1u;
     P.left = job.left;
     P.right = job.right;
   }
-  (void)tw;
 }
 
-// Root node statistics: centroid, weight and variance of all vectors (one CTA).
+// Root node statistics (centroid, weight, variance of all vectors) and the first buffer: the
+// caller's vectors and integer weights copied as floats. One cluster over all vectors.
 template <int D>
 __global__ void __launch_bounds__(kVqThreads) k_vq_root(const float* __restrict__ vec, const uint32_t* __restrict__ w,
-                                                        uint32_t n, VqNode<D>* __restrict__ nodes) {
-  __shared__ float red[(D + 2) * 16];
+                                                        uint32_t n, float* __restrict__ vec0, float* __restrict__ w0,
+                                                        VqNode<D>* __restrict__ nodes) {
+  __shared__ VqShared sh;
+  cg::cluster_group cl = cg::this_cluster();
+  const unsigned C = cl.num_blocks(), r = cl.block_rank();
+  int phase = 0;
+  const uint32_t per = (n + C - 1) / C;
+  const uint32_t s0 = min(n, r * per), s1 = min(n, s0 + per);
   float acc[D + 2];
 #pragma unroll
   for (int k = 0; k < D + 2; k++) acc[k] = 0.f;
-  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+  for (uint32_t i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
     const float ww = (float)w[i];
+    float v[D];
+    load_vec<D>(vec + (size_t)i * D, v);
     float sq = 0.f;
 #pragma unroll
-    for (int k = 0; k < D; k++) { const float v = vec[(size_t)i * D + k]; acc[k] += v * ww; sq += v * v; }
+    for (int k = 0; k < D; k++) { acc[k] += v[k] * ww; sq += v[k] * v[k]; vec0[(size_t)i * D + k] = v[k]; }
+    w0[i] = ww;
     acc[D] += ww;
     acc[D + 1] += sq * ww;
   }
-  block_sum<D + 2>(acc, red);
-  if (threadIdx.x == 0) {
-    VqNode<D>& r = nodes[0];
+  cluster_sum<D + 2>(acc, sh, phase, cl);
+  if (r == 0 && threadIdx.x == 0) {
+    VqNode<D>& rt = nodes[0];
     float cc = 0.f;
     for (int k = 0; k < D; k++) cc += acc[k] * acc[k];
-    r.variance = acc[D] > 0.f ? acc[D + 1] - cc / acc[D] : 0.f;
-    for (int k = 0; k < D; k++) r.c[k] = acc[D] > 0.f ? acc[k] / acc[D] : 0.f;
-    r.weight = acc[D];
-    r.begin = 0; r.end = n;
-    r.left = r.right = -1;
-    r.unsplittable = 0;
+    rt.variance = acc[D] > 0.f ? acc[D + 1] - cc / acc[D] : 0.f;
+    for (int k = 0; k < D; k++) rt.c[k] = acc[D] > 0.f ? acc[k] / acc[D] : 0.f;
+    rt.weight = acc[D];
+    rt.begin = 0; rt.end = n;
+    rt.left = rt.right = -1;
+    rt.unsplittable = 0;
+    rt.buf = 0;
   }
+  cl.sync();
 }
 
-__global__ void k_iota(uint32_t* p, uint32_t n) {
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = i;
+// CTAs per cluster for nodes of up to `size` vectors: one CTA per kVqPerCta vectors, a power of
+// two, at most 16 (8 where the device cannot co-schedule 16-CTA clusters of this kernel).
+inline unsigned vq_cluster_size(uint32_t size, unsigned max_cluster) {
+  unsigned c = 1;
+  while (c < max_cluster && (uint64_t)c * kVqPerCta < size) c <<= 1;
+  return c;
+}
+
+template <class K, class... Args>
+cudaError_t launch_clustered(K kernel, unsigned grid, unsigned cluster, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kVqThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+// Largest cluster (16 or 8) the device co-schedules for this kernel.
+template <class K>
+unsigned max_vq_cluster(K kernel) {
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return 8;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(16);
+  cfg.blockDim = dim3(kVqThreads);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 16;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, kernel, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 8;
+  }
+  return nclusters >= 1 ? 16u : 8u;
 }
 
 // Host driver of the batched tree clusterizer: returns the codebook (leaf centroids) on the device
@@ -905,15 +1338,26 @@ int tree_vq(const float* d_vec, const uint32_t* d_w, uint32_t n, uint32_t max_en
   // every split attempt takes two node slots; a node fails at most once (it is then marked
   // unsplittable), so attempts <= (max_entries - 1) successes + at most 2 * max_entries failures
   const size_t max_nodes = 6 * (size_t)max_entries + 8;
-  DevBuf d_nodes, d_perm, d_tmp, d_jobs;
+  static const unsigned max_split_cluster = max_vq_cluster(k_vq_split<D>);
+  static const unsigned max_root_cluster = max_vq_cluster(k_vq_root<D>);
+  DevBuf d_nodes, d_v[2], d_wt[2], d_jobs;
   cudaError_t e;
   if ((e = d_nodes.ensure(sizeof(Node) * max_nodes)) != cudaSuccess) return cuda_check(e, "alloc vq nodes");
-  if ((e = d_perm.ensure(sizeof(uint32_t) * n)) != cudaSuccess) return cuda_check(e, "alloc vq perm");
-  if ((e = d_tmp.ensure(sizeof(uint32_t) * n)) != cudaSuccess) return cuda_check(e, "alloc vq tmp");
+  for (int b = 0; b < 2; b++) {
+    if ((e = d_v[b].ensure(sizeof(float) * D * (size_t)n)) != cudaSuccess) return cuda_check(e, "alloc vq vectors");
+    if ((e = d_wt[b].ensure(sizeof(float) * (size_t)n)) != cudaSuccess) return cuda_check(e, "alloc vq weights");
+  }
   if ((e = d_jobs.ensure(sizeof(SplitJob) * max_entries)) != cudaSuccess) return cuda_check(e, "alloc vq jobs");
   Node* nodes = static_cast<Node*>(d_nodes.ptr);
-  k_iota<<<256, 256, 0, s>>>(static_cast<uint32_t*>(d_perm.ptr), n);
-  k_vq_root<D><<<1, kVqThreads, 0, s>>>(d_vec, d_w, n, nodes);
+  float* v0 = static_cast<float*>(d_v[0].ptr);
+  float* v1 = static_cast<float*>(d_v[1].ptr);
+  float* w0 = static_cast<float*>(d_wt[0].ptr);
+  float* w1 = static_cast<float*>(d_wt[1].ptr);
+  {
+    const unsigned C = vq_cluster_size(n, max_root_cluster);
+    if ((e = launch_clustered(k_vq_root<D>, C, C, s, d_vec, d_w, n, v0, w0, nodes)) != cudaSuccess)
+      return cuda_check(e, "launch k_vq_root");
+  }
   std::vector<Node> h(max_nodes);
   if ((e = cudaMemcpyAsync(h.data(), nodes, sizeof(Node), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
     return cuda_check(e, "read vq root");
@@ -936,26 +1380,52 @@ int tree_vq(const float* d_vec, const uint32_t* d_w, uint32_t n, uint32_t max_en
     take = std::min(take, std::max<size_t>(1, leaves.size() / round_fraction));
     take = std::min(take, (max_nodes - used) / 2);
     if (!take) break;
-    std::vector<SplitJob> jobs(take);
-    for (size_t i = 0; i < take; i++) {
-      jobs[i].parent = cand[i];
-      jobs[i].left = (int)used++;
-      jobs[i].right = (int)used++;
-    }
+    // large nodes first in the job list (one CTA cluster each), then small ones (a warp each)
+    std::vector<SplitJob> jobs;
+    jobs.reserve(take);
+    uint32_t largest = 0;
+    const size_t first_new = used;
+    for (int pass = 0; pass < 2; pass++)
+      for (size_t i = 0; i < take; i++) {
+        const uint32_t size = h[cand[i]].end - h[cand[i]].begin;
+        if ((size > kVqWarpMax) != (pass == 0)) continue;
+        jobs.push_back(SplitJob{cand[i], (int)used, (int)used + 1});
+        used += 2;
+        if (!pass) largest = std::max(largest, size);
+      }
+    size_t nbig = 0;
+    while (nbig < jobs.size() && h[jobs[nbig].parent].end - h[jobs[nbig].parent].begin > kVqWarpMax) nbig++;
     if ((e = cudaMemcpyAsync(d_jobs.ptr, jobs.data(), sizeof(SplitJob) * take, cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return cuda_check(e, "copy vq jobs");
-    k_vq_split<D><<<(unsigned)take, kVqThreads, 0, s>>>(d_vec, d_w, static_cast<uint32_t*>(d_perm.ptr),
-                                                         static_cast<uint32_t*>(d_tmp.ptr), nodes,
-                                                         static_cast<const SplitJob*>(d_jobs.ptr));
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_vq_split");
-    if ((e = cudaMemcpyAsync(h.data(), nodes, sizeof(Node) * used, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    const SplitJob* dj = static_cast<const SplitJob*>(d_jobs.ptr);
+    if (nbig) {
+      const unsigned C = vq_cluster_size(largest, max_split_cluster);
+      if ((e = launch_clustered(k_vq_split<D>, (unsigned)nbig * C, C, s, v0, v1, w0, w1, nodes, dj)) != cudaSuccess)
+        return cuda_check(e, "launch k_vq_split");
+    }
+    if (nbig < take) {
+      const uint32_t nsmall = (uint32_t)(take - nbig);
+      k_vq_split_warp<D><<<(nsmall + 7) / 8, 256, 0, s>>>(v0, v1, w0, w1, nodes, dj + nbig, nsmall);
+      if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_vq_split_warp");
+    }
+    // only the new children are read back; a failed split is flagged on its left child
+    if ((e = cudaMemcpyAsync(h.data() + first_new, nodes + first_new, sizeof(Node) * (used - first_new),
+                             cudaMemcpyDeviceToHost, s)) != cudaSuccess)
       return cuda_check(e, "read vq nodes");
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
     std::vector<int> next;
     bool progressed = false;
     std::vector<char> split(used, 0);
-    for (const SplitJob& j : jobs)
-      if (!h[j.parent].unsplittable) { split[j.parent] = 1; progressed = true; }
+    for (const SplitJob& j : jobs) {
+      if (h[j.left].unsplittable == 2) {
+        h[j.parent].unsplittable = 1;
+      } else {
+        h[j.parent].left = j.left;
+        h[j.parent].right = j.right;
+        split[j.parent] = 1;
+        progressed = true;
+      }
+    }
     for (int l : leaves) {
       if (split[l]) { next.push_back(h[l].left); next.push_back(h[l].right); }
       else next.push_back(l);

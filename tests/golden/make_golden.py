@@ -194,10 +194,60 @@ def make_hc() -> None:
         json.dump(out, fh, indent=1, sort_keys=True)
 
 
+# 2048x2048 DXT5 (colour + alpha noise) and DXN_XY (normal map) mip chains at quality 128
+CONFIG2_CASES = [("dxt5_2048", "DXT5", 2, 2048, 200, "colour_alpha"), ("dxn_xy_2048", "DXN_XY", 7, 2048, 201, "normal")]
+
+
+def level_quality(dxt_levels, src_levels, fmt):
+    """RMSEs of decoded blocks against the source mip chain (all levels, visible blocks): RGB and
+    alpha for DXT5, the two channels together for DXN."""
+    sys.path.insert(0, os.path.dirname(HERE))
+    from dxt_decode import rgb_rmse, dxt5a_values
+    dec = np.concatenate(dxt_levels)
+    src = np.concatenate([texgen.image_blocks(im) for im in src_levels]).reshape(-1, 16, 4).astype(np.int64)
+    if fmt == "DXT5":
+        a = dxt5a_values(dec[:, :8])
+        return {"rmse_color": rgb_rmse(dec[:, 8:], src.reshape(-1, 64).astype(np.uint8)),
+                "rmse_alpha": float(np.sqrt(((a - src[:, :, 3]) ** 2).mean()))}
+    x, y = dxt5a_values(dec[:, :8]), dxt5a_values(dec[:, 8:])
+    return {"rmse_xy": float(np.sqrt((((x - src[:, :, 0]) ** 2).sum() + ((y - src[:, :, 1]) ** 2).sum()) / (2 * x.size)))}
+
+
+def make_config2() -> None:
+    """The reference's crn_compress (.crn, q128, its default flags) on the 2048x2048 DXT5 and DXN
+    textures: file size and the RMSEs of its crnd-decoded blocks, the bar for the GPU path at that
+    size (the .crn files themselves are too large to commit)."""
+    import time
+    out = {}
+    for name, fmt, code, size, seed, content in CONFIG2_CASES:
+        fl = texture_levels(size, size, content, seed, 1)
+        flags = (0 if content == "normal" else FLAG_PERCEPTUAL) | FLAG_HIERARCHICAL | FLAG_BOTH_BLOCK_TYPES
+        t = time.time()
+        crn = ref.compress_texture(fl, code, 0, 128, flags, DXT_UBER, 7)
+        secs = time.time() - t
+        bpb = 16
+        dxt = []
+        for lvl in range(len(fl[0])):
+            w, h = max(1, size >> lvl), max(1, size >> lvl)
+            dxt.append(ref.unpack_level(crn, lvl, level_bytes(size, size, lvl, bpb, 1)).reshape(-1, bpb))
+        texels = sum(im.shape[0] * im.shape[1] for im in fl[0])
+        out[name] = {"size": size, "seed": seed, "format": fmt, "content": content, "quality": 128,
+                     "levels": len(fl[0]), "bytes": len(crn), "bits_per_texel": 8 * len(crn) / texels,
+                     "crn_sha256": sha(crn), "seconds_8_threads_x86": round(secs, 2),
+                     **level_quality(dxt, fl[0], fmt)}
+        print(name, out[name], flush=True)
+    with open(os.path.join(HERE, "config2_reference.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
 if __name__ == "__main__":
     if not ref.available():
         sys.exit("oracle/_ref/libcrnref.so missing: run `make -C oracle ref` where the reference tree exists")
+    if sys.argv[1:] == ["config2"]:
+        make_config2()
+        sys.exit(0)
     make_blocks()
     make_crn()
     make_hc()
+    make_config2()
     print("golden fixtures written to", HERE)
