@@ -9,6 +9,8 @@ One JSON line on stdout (rank 0):
   e2e        the same encode through the C ABI with pinned host buffers (H2D + encode + D2H)
   clustered  crn_compress of the same mip chain to .crn at quality 128 (DXT1): Mtexel/s, bits per
              texel and RGB RMSE beside the reference's own .crn of the texture
+  clustered_2048  the same for 2048x2048 DXT5 (colour + alpha noise) and DXN_XY (normal map) mip
+             chains: colour / alpha / XY RMSE and bits per texel beside the reference's
   transcode  CRN -> DXT1 transcode GB/s: a batch of 1024 textures (each with its own context holding
              the reference-encoded .crn of the same texture, q128) in one persistent decode launch
              and one expansion launch (CUDA graph); the expansion kernel's HBM roofline; the
@@ -53,6 +55,50 @@ def workload():
     blocks = np.concatenate([texgen.image_blocks(l) for l in levels])
     texels = sum(l.shape[0] * l.shape[1] for l in levels)
     return levels, blocks, texels
+
+
+CONFIG2_REFERENCE = os.path.join(ROOT, "tests", "golden", "config2_reference.json")
+
+
+def clustered_2048_leg(cg, dev, steps: int) -> dict:
+    """crn_compress of 2048x2048 DXT5 and DXN_XY mip chains (12 levels) at q128; quality of the
+    GPU-decoded blocks against the source, beside the reference's own .crn of each texture."""
+    import torch
+    from crunch2_gb300 import quality as Q
+    from crunch2_gb300 import texgen
+    with open(CONFIG2_REFERENCE) as fh:
+        refs = json.load(fh)
+    out = {}
+    for name, fmt_name, fmt in (("dxt5_2048", "DXT5", cg.FMT_DXT5), ("dxn_xy_2048", "DXN_XY", cg.FMT_DXN_XY)):
+        r = refs[name]
+        size = r["size"]
+        img = texgen.normal_map(size, size, r["seed"]) if r["content"] == "normal" else \
+            texgen.colour_texture(size, size, r["seed"], with_alpha_noise=True)
+        levels = texgen.mip_chain(img)
+        texels = sum(l.shape[0] * l.shape[1] for l in levels)
+        flags = 0 if r["content"] == "normal" else cg.FLAG_PERCEPTUAL
+        cg.compress_crn([levels], fmt, quality=128, flags=flags)  # warm-up
+        times = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            crn = cg.compress_crn([levels], fmt, quality=128, flags=flags)
+            times.append(time.perf_counter() - t0)
+        secs = statistics.median(times)
+        with cg.unpack_begin(crn) as c:
+            dec = c.unpack_levels()
+        src = torch.from_numpy(np.concatenate([texgen.image_blocks(l) for l in levels])).to(dev)
+        q = Q.block_rmse(torch.from_numpy(dec.reshape(-1, 16)).to(dev), src, fmt_name)
+        rec = {"mtexel_s": round(texels / secs / 1e6, 3), "s_per_texture": round(secs, 4), "texels": texels,
+               "bits_per_texel": round(8 * len(crn) / texels, 4),
+               "bits_per_texel_reference": round(r["bits_per_texel"], 4)}
+        for k, v in q.items():
+            rec[k] = round(v, 4)
+            rec[k + "_reference"] = round(r[k], 4)
+        rec["reference_seconds_8_threads_x86"] = r["seconds_8_threads_x86"]
+        out[name] = rec
+    out["path"] = ("crngpu_compress_crn (host RGBA8 mip chain -> .crn), decoded by the GPU transcoder; the "
+                   "reference's figures are its own crn_compress output of the same texture, decoded by crnd")
+    return out
 
 
 def cpu_threads() -> int:
@@ -428,6 +474,11 @@ def main():
                  "path": "crngpu_compress_crn: host RGBA8 mip chain -> crn_comp block gather (host) -> H2D -> "
                          "clustered encode (every dxt_hc stage on the GPU) -> D2H -> .crn writer (host); wall time"}
 
+    # ---- the 2048x2048 DXT5 (colour + alpha noise) and DXN_XY (normal map) mip chains at quality
+    # 128: crn_compress wall time, and the RMSEs of the GPU-decoded result beside those of the
+    # reference's own .crn of the same textures (reference numbers committed with the fixtures)
+    clustered_2048 = clustered_2048_leg(cg, dev, steps=max(1, min(args.steps, 3)))
+
     peaks, peak_kind = measured_peaks()
     clk = clocks.summary()
     sm_max = clk.get("sm_max_mhz") or peaks.get("sm_max_mhz", 2070.0)
@@ -462,7 +513,8 @@ def main():
                 "parity_vs_oracle_sample": parity, "e2e_parity": e2e_parity,
                 "e2e": {"value": round(e2e_value, 3), "unit": "Mtexel/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "path": "crngpu_compress_image per level, pinned host buffers"},
-                "learned": learned, "transcode": transcode, "clustered": clustered, "roofline": roofline,
+                "learned": learned, "transcode": transcode, "clustered": clustered,
+                "clustered_2048": clustered_2048, "roofline": roofline,
                 "cpu_baseline": cpu,
                 "gpu_launches": args.steps * 1, "clocks": clk, "wall_s_timed": round(wall, 4)}
         print(json.dumps(line))

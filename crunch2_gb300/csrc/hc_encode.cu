@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -1522,36 +1523,57 @@ constexpr int kUniqCap = 4096;
 constexpr int kMaxCand = 1024;
 __constant__ int16_t c_probe[15] = {0, 1, 2, 3, 5, 7, 9, 10, 13, 15, 19, 27, 43, 59, 91};  // g_uber_probe_table
 
-// Squared error (perceptual or RGB weights) of the 4-colour block (lo, hi) over the unique colours,
-// each pixel on its nearest colour; one warp, result on every lane.
-__device__ __forceinline__ unsigned long long warp_pair_error(uint32_t lo, uint32_t hi, const uint32_t* ucol,
-                                                               const uint32_t* ucnt, int U, bool perc) {
-  int col[4][3];
-  colors4(lo, hi, col);
-  unsigned long long e = 0;
-  for (int i = (int)(threadIdx.x & 31); i < U; i += 32) {
-    const uint32_t c = ucol[i];
-    const int r = (int)(c & 255), g = (int)((c >> 8) & 255), b = (int)((c >> 16) & 255);
-    uint32_t bd = cdist(perc, r, g, b, col[0][0], col[0][1], col[0][2]);
-    bd = min(bd, cdist(perc, r, g, b, col[1][0], col[1][1], col[1][2]));
-    bd = min(bd, cdist(perc, r, g, b, col[2][0], col[2][1], col[2][2]));
-    bd = min(bd, cdist(perc, r, g, b, col[3][0], col[3][1], col[3][2]));
-    e += (unsigned long long)bd * ucnt[i];
-  }
-  for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xFFFFFFFFu, e, o);
-  return e;
+// The probe search's colour table: per unique colour u, {-2 w_r r, -2 w_g g, -2 w_b b, xx} with
+// xx = w_r r^2 + w_g g^2 + w_b b^2 (w = 8, 25, 1 perceptual, else 1), and its pixel count. For a
+// palette colour p with pp = sum w p^2, the weighted squared distance is xx + pp + a . p, so a
+// pixel's error against the 4-colour palette is xx + min_k (pp_k + a . p_k): three multiply-adds
+// per palette colour, exactly the integer error of cdist.
+__device__ __forceinline__ int4 probe_entry(uint32_t rgb, bool perc) {
+  const int r = (int)(rgb & 255), g = (int)((rgb >> 8) & 255), b = (int)((rgb >> 16) & 255);
+  const int wr = perc ? 8 : 1, wg = perc ? 25 : 1;
+  return make_int4(-2 * wr * r, -2 * wg * g, -2 * b, wr * r * r + wg * g * g + b * b);
 }
 
-// Evaluates the candidate pairs cand[0..n) (lo | hi << 16), warp per candidate; returns the best
-// (lowest error, then lowest index) to every thread through shared memory.
-__device__ void best_candidate(const uint32_t* cand, int n, const uint32_t* ucol, const uint32_t* ucnt, int U, bool perc,
-                               unsigned long long* s_be, uint32_t* s_bi, unsigned long long& err, uint32_t& pair) {
+// Error of the 4-colour block (lo, hi) over the unique colours, abandoned (returning ~0) as soon as
+// its running sum reaches `bound` (a candidate that cannot win); one thread.
+__device__ __forceinline__ unsigned long long pair_error(uint32_t lo, uint32_t hi, const int4* ut, const uint32_t* uc,
+                                                        int U, bool perc, unsigned long long bound) {
+  int col[4][3];
+  colors4(lo, hi, col);
+  const int wr = perc ? 8 : 1, wg = perc ? 25 : 1;
+  int pp[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) pp[k] = wr * col[k][0] * col[k][0] + wg * col[k][1] * col[k][1] + col[k][2] * col[k][2];
+  unsigned long long e = 0;
+  for (int i = 0; i < U; i++) {
+    const int4 t = ut[i];
+    int m = pp[0] + t.x * col[0][0] + t.y * col[0][1] + t.z * col[0][2];
+#pragma unroll
+    for (int k = 1; k < 4; k++) m = min(m, pp[k] + t.x * col[k][0] + t.y * col[k][1] + t.z * col[k][2]);
+    e += (unsigned long long)(uint32_t)(t.w + m) * uc[i];
+    if ((i & 15) == 15 && e >= bound) return ~0ull;
+  }
+  return e < bound ? e : ~0ull;
+}
+
+// Evaluates the candidate pairs cand[0..n) (lo | hi << 16), one thread per candidate, and returns
+// to every thread the best (lowest error, then lowest index) among those below `bound`; err = ~0
+// and pair = 0 when none is.
+__device__ void best_candidate(const uint32_t* cand, int n, const int4* ut, const uint32_t* uc, int U, bool perc,
+                               unsigned long long bound, unsigned long long* s_be, uint32_t* s_bi,
+                               unsigned long long& err, uint32_t& pair) {
   const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   unsigned long long be = ~0ull;
   uint32_t bi = 0xFFFFFFFFu;
-  for (int i = warp; i < n; i += nw) {
-    const unsigned long long e = warp_pair_error(cand[i] & 0xFFFFu, cand[i] >> 16, ucol, ucnt, U, perc);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    // a later candidate must beat this thread's best strictly (ties go to the lower index)
+    const unsigned long long e = pair_error(cand[i] & 0xFFFFu, cand[i] >> 16, ut, uc, U, perc, min(bound, be));
     if (e < be) { be = e; bi = (uint32_t)i; }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long oe = __shfl_xor_sync(0xFFFFFFFFu, be, o);
+    const uint32_t oi = __shfl_xor_sync(0xFFFFFFFFu, bi, o);
+    if (oe < be || (oe == be && oi < bi)) { be = oe; bi = oi; }
   }
   __syncthreads();
   if ((threadIdx.x & 31) == 0) { s_be[warp] = be; s_bi[warp] = bi; }
@@ -1704,7 +1726,13 @@ __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __r
   // (g_uber_probe_table steps of 1/64), every low x high pair, then the 26 lattice neighbours and
   // +-2 axis moves of each endpoint of the best pair; up to four passes.
   {
-    __shared__ uint32_t s_key[kUniqCap], s_cnt[kUniqCap];
+    // hashing: keys in s_raw[0, kUniqCap), counts in s_raw[kUniqCap, 2 kUniqCap); once compacted (at
+    // most kUniqCap / 2 colours): the int4 probe table in s_raw[0, 2 kUniqCap), counts after it
+    __shared__ __align__(16) uint32_t s_raw[2 * kUniqCap + kUniqCap / 2];
+    uint32_t* s_key = s_raw;
+    uint32_t* s_cnt = s_raw + kUniqCap;
+    int4* s_ut = reinterpret_cast<int4*>(s_raw);
+    uint32_t* s_uc = s_raw + 2 * kUniqCap;
     __shared__ uint32_t s_cand[kMaxCand];
     __shared__ unsigned long long s_be[kFitThreads / 32];
     __shared__ uint32_t s_bi[kFitThreads / 32];
@@ -1740,7 +1768,8 @@ __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __r
       for (int w = 0; w < (int)(threadIdx.x >> 5); w++) base += s_wcnt[w];
       const int at = base + incl - nm;
       __syncthreads();
-      for (int j = 0; j < nm; j++) { s_key[at + j] = mine_key[j]; s_cnt[at + j] = mine_cnt[j]; }
+      for (int j = 0; j < nm; j++)
+        if (at + j < kUniqCap / 2) { s_ut[at + j] = probe_entry(mine_key[j], perc); s_uc[at + j] = mine_cnt[j]; }
       if (threadIdx.x == blockDim.x - 1) s_nu = (uint32_t)(at + nm);
     }
     __syncthreads();
@@ -1753,7 +1782,7 @@ __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __r
         uint32_t pair;
         if (threadIdx.x == 0) s_cand[0] = bl | (bh << 16);
         __syncthreads();
-        best_candidate(s_cand, 1, s_key, s_cnt, U, perc, s_be, s_bi, berr, pair);
+        best_candidate(s_cand, 1, s_ut, s_uc, U, perc, ~0ull, s_be, s_bi, berr, pair);
       }
       // low / high colours from the axis projection bounds, in 565 units
       float lowc[3], highc[3];
@@ -1800,7 +1829,7 @@ __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __r
         {
           unsigned long long e;
           uint32_t pair;
-          best_candidate(s_cand, npl * nph, s_key, s_cnt, U, perc, s_be, s_bi, e, pair);
+          best_candidate(s_cand, npl * nph, s_ut, s_uc, U, perc, berr, s_be, s_bi, e, pair);
           if (e < berr) { berr = e; bl = pair & 0xFFFFu; bh = pair >> 16; }
         }
         // lattice neighbours (26) and +-2 axis moves of the low endpoint, then of the high one
@@ -1831,7 +1860,7 @@ __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __r
           const int n = (int)s_npl;
           unsigned long long e;
           uint32_t pair;
-          best_candidate(s_cand, n, s_key, s_cnt, U, perc, s_be, s_bi, e, pair);
+          best_candidate(s_cand, n, s_ut, s_uc, U, perc, berr, s_be, s_bi, e, pair);
           if (e < berr) { berr = e; bl = pair & 0xFFFFu; bh = pair >> 16; }
         }
         if (pass && berr == prev_err) break;
@@ -1846,6 +1875,7 @@ __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __r
   // selectors re-chosen for the walk's result while the true error keeps falling
   __shared__ unsigned long long s_stat[29];  // hist[4], D2[4][3], DD[4][3] (exact integers), error
   __shared__ uint32_t s_LH[2];
+  __shared__ uint32_t s_sol[54], s_nsol;
   uint32_t L0 = best0 > best1 ? best0 : best1, H0 = best0 > best1 ? best1 : best0;
   if (L0 == H0) { if (L0 < 0xFFFFu) L0++; else H0--; }
   uint32_t keepL = L0, keepH = H0;
@@ -1878,66 +1908,95 @@ __global__ void __launch_bounds__(kFitThreads) k_cluster_fit(const uint32_t* __r
     keep_err = true_err;
     keepL = L0;
     keepH = H0;
-    if (threadIdx.x == 0) {
-      double hist[4], D2[4][3], DD[4][3];
+    if (threadIdx.x < 32) {
+      // the walk runs on warp 0: lane 0 lists the moves, the lanes score them, exactly in 64-bit
+      // integers (the histogram sums are exact, so the reference's double sums are these values)
+      const int lane = threadIdx.x;
+      long long hist[4], D2[4][3], DD[4][3];
       for (int q = 0; q < 4; q++) {
-        hist[q] = (double)s_stat[q];
-        for (int c = 0; c < 3; c++) { D2[q][c] = (double)s_stat[4 + q * 3 + c]; DD[q][c] = (double)s_stat[16 + q * 3 + c]; }
+        hist[q] = (long long)s_stat[q];
+        for (int c = 0; c < 3; c++) { D2[q][c] = (long long)s_stat[4 + q * 3 + c]; DD[q][c] = (long long)s_stat[16 + q * 3 + c]; }
       }
       auto err_of = [&](uint32_t L, uint32_t H) {
         int cc[4][3];
         colors4(L, H, cc);
-        double er = 0;
+        long long er = 0;
         for (int q = 0; q < 4; q++) {
-          double d[3];
+          long long d[3];
           for (int c = 0; c < 3; c++) d[c] = hist[q] * cc[q][c] * cc[q][c] - D2[q][c] * cc[q][c] + DD[q][c];
           er += perc ? d[0] * 8 + d[1] * 25 + d[2] : d[0] + d[1] + d[2];
         }
         return er;
       };
       uint32_t wL = L0, wH = H0;
-      double best = err_of(wL, wH);
+      long long best = err_of(wL, wH);
       const bool preserveL = hist[0] + hist[2] > hist[1] + hist[3];
       bool improved = true;
       for (int iters = 8; improved && iters; iters--) {
         improved = false;
-        uint32_t sol[54];
-        int ns = 0;
-        for (int which = 0; which < 2; which++) {
-          const uint32_t E = which ? wH : wL, O2 = which ? wL : wH;
-          const int b0 = E & 31, g0 = (E >> 5) & 63, r0 = (E >> 11) & 31;
-          for (int b = b0 ? b0 - 1 : b0; b <= b0 + 1 && b <= 31; b++)
-            for (int g = g0 ? g0 - 1 : g0; g <= g0 + 1 && g <= 63; g++)
-              for (int r = r0 ? r0 - 1 : r0; r <= r0 + 1 && r <= 31; r++) {
-                const uint32_t X = (uint32_t)((r << 11) | (g << 5) | b);
-                if (X != E) sol[ns++] = X > O2 ? (X | (O2 << 16)) : (O2 | (X << 16));
-              }
+        if (lane == 0) {
+          int ns = 0;
+          for (int which = 0; which < 2; which++) {
+            const uint32_t E = which ? wH : wL, O2 = which ? wL : wH;
+            const int b0 = E & 31, g0 = (E >> 5) & 63, r0 = (E >> 11) & 31;
+            for (int b = b0 ? b0 - 1 : b0; b <= b0 + 1 && b <= 31; b++)
+              for (int g = g0 ? g0 - 1 : g0; g <= g0 + 1 && g <= 63; g++)
+                for (int r = r0 ? r0 - 1 : r0; r <= r0 + 1 && r <= 31; r++) {
+                  const uint32_t X = (uint32_t)((r << 11) | (g << 5) | b);
+                  if (X != E) s_sol[ns++] = X > O2 ? (X | (O2 << 16)) : (O2 | (X << 16));
+                }
+          }
+          for (int i = 1; i < ns; i++) {  // sorted, as the reference evaluates them
+            const uint32_t x = s_sol[i];
+            int j = i - 1;
+            while (j >= 0 && s_sol[j] > x) { s_sol[j + 1] = s_sol[j]; j--; }
+            s_sol[j + 1] = x;
+          }
+          s_nsol = (uint32_t)ns;
         }
-        for (int i = 1; i < ns; i++) {  // sorted, as the reference evaluates them
-          const uint32_t x = sol[i];
-          int j = i - 1;
-          while (j >= 0 && sol[j] > x) { sol[j + 1] = sol[j]; j--; }
-          sol[j + 1] = x;
-        }
-        for (int i = 0; i < ns; i++) {
-          if (i && sol[i] == sol[i - 1]) continue;
-          uint32_t L = sol[i] & 0xFFFFu, H = sol[i] >> 16;
+        __syncwarp();
+        const int ns = (int)s_nsol;
+        // the first strictly better move in sorted order wins ties: (error, index) minimum
+        long long le = LLONG_MAX;
+        int li = 0x7FFFFFFF;
+        for (int i = lane; i < ns; i += 32) {
+          if (i && s_sol[i] == s_sol[i - 1]) continue;
+          uint32_t L = s_sol[i] & 0xFFFFu, H = s_sol[i] >> 16;
           if (L == H) {
             L += !preserveL ? ((~L & 0x1F) ? 0x1 : (~L & 0xF800) ? 0x800 : (~L & 0x7E0) ? 0x20 : 0) : (!L ? 0x1 : 0);
             H -= preserveL ? ((H & 0x1F) ? 0x1 : (H & 0xF800) ? 0x800 : (H & 0x7E0) ? 0x20 : 0) : (H == 0xFFFF ? 0x1 : 0);
             L &= 0xFFFFu; H &= 0xFFFFu;
           }
-          const double er = err_of(L, H);
-          if (er < best) { best = er; wL = L; wH = H; improved = true; }
+          const long long er = err_of(L, H);
+          if (er < le) { le = er; li = i; }
         }
+        for (int o = 16; o > 0; o >>= 1) {
+          const long long oe = __shfl_xor_sync(0xFFFFFFFFu, le, o);
+          const int oi = __shfl_xor_sync(0xFFFFFFFFu, li, o);
+          if (oe < le || (oe == le && oi < li)) { le = oe; li = oi; }
+        }
+        if (le < best) {
+          best = le;
+          uint32_t L = s_sol[li] & 0xFFFFu, H = s_sol[li] >> 16;
+          if (L == H) {
+            L += !preserveL ? ((~L & 0x1F) ? 0x1 : (~L & 0xF800) ? 0x800 : (~L & 0x7E0) ? 0x20 : 0) : (!L ? 0x1 : 0);
+            H -= preserveL ? ((H & 0x1F) ? 0x1 : (H & 0xF800) ? 0x800 : (H & 0x7E0) ? 0x20 : 0) : (H == 0xFFFF ? 0x1 : 0);
+            L &= 0xFFFFu; H &= 0xFFFFu;
+          }
+          wL = L; wH = H;
+          improved = true;
+        }
+        __syncwarp();  // s_sol is rewritten by lane 0 in the next step
         if (best == 0) break;
       }
       if (wL <= wH) {  // keep 4-colour order (first > second)
         if (wL == wH) { if (wL < 0xFFFFu) wL++; else wH--; }
         else { const uint32_t t = wL; wL = wH; wH = t; }
       }
-      s_LH[0] = wL;
-      s_LH[1] = wH;
+      if (lane == 0) {
+        s_LH[0] = wL;
+        s_LH[1] = wH;
+      }
     }
     __syncthreads();
     if (s_LH[0] == L0 && s_LH[1] == H0) break;

@@ -38,8 +38,11 @@ def _unit(h: np.ndarray) -> np.ndarray:
 
 def value_noise(w: int, h: int, period: int, octaves: int, seed: int, channel: int,
                 persistence: float = 0.5) -> np.ndarray:
-    """Sum of `octaves` smoothstep-interpolated lattice noises, normalised to [0, 1]."""
-    ys, xs = np.mgrid[0:h, 0:w]
+    """Sum of `octaves` smoothstep-interpolated lattice noises, normalised to [0, 1]. The lattice
+    values are hashed once per lattice point and gathered per pixel; the per-pixel arithmetic is
+    the same sequence of float64 operations at every pixel."""
+    xs = np.arange(w, dtype=np.int64)
+    ys = np.arange(h, dtype=np.int64)
     total = np.zeros((h, w), np.float64)
     amp, norm = 1.0, 0.0
     p = float(period)
@@ -52,13 +55,17 @@ def value_noise(w: int, h: int, period: int, octaves: int, seed: int, channel: i
         ty = fy - iy
         tx = tx * tx * (3.0 - 2.0 * tx)
         ty = ty * ty * (3.0 - 2.0 * ty)
-        v00 = _unit(_hash32(seed, channel, o, ix, iy))
-        v10 = _unit(_hash32(seed, channel, o, ix + 1, iy))
-        v01 = _unit(_hash32(seed, channel, o, ix, iy + 1))
-        v11 = _unit(_hash32(seed, channel, o, ix + 1, iy + 1))
-        a = v00 + (v10 - v00) * tx
-        b = v01 + (v11 - v01) * tx
-        total += amp * (a + (b - a) * ty)
+        gx = np.arange(int(ix[0]), int(ix[-1]) + 2, dtype=np.int64)
+        gy = np.arange(int(iy[0]), int(iy[-1]) + 2, dtype=np.int64)
+        lat = _unit(_hash32(seed, channel, o, gx[None, :], gy[:, None]))  # lat[y, x]
+        cx, cy = ix - gx[0], iy - gy[0]
+        v00 = lat[cy][:, cx]
+        v10 = lat[cy][:, cx + 1]
+        v01 = lat[cy + 1][:, cx]
+        v11 = lat[cy + 1][:, cx + 1]
+        a = v00 + (v10 - v00) * tx[None, :]
+        b = v01 + (v11 - v01) * tx[None, :]
+        total += amp * (a + (b - a) * ty[:, None])
         norm += amp
         amp *= persistence
         p = max(p / 2.0, 1.0)
