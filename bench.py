@@ -11,6 +11,8 @@ One JSON line on stdout (rank 0):
              texel and RGB RMSE beside the reference's own .crn of the texture
   clustered_2048  the same for 2048x2048 DXT5 (colour + alpha noise) and DXN_XY (normal map) mip
              chains: colour / alpha / XY RMSE and bits per texel beside the reference's
+  mixed_batch  512 textures of uneven sizes and mixed formats: batched plain encode (CUDA graph),
+             their .crn through crn_compress, and the batched transcode of those files
   transcode  CRN -> DXT1 transcode GB/s: a batch of 1024 textures (each with its own context holding
              the reference-encoded .crn of the same texture, q128) in one persistent decode launch
              and one expansion launch (CUDA graph); the expansion kernel's HBM roofline; the
@@ -99,6 +101,98 @@ def clustered_2048_leg(cg, dev, steps: int) -> dict:
     out["path"] = ("crngpu_compress_crn (host RGBA8 mip chain -> .crn), decoded by the GPU transcoder; the "
                    "reference's figures are its own crn_compress output of the same texture, decoded by crnd")
     return out
+
+
+MIXED_TEXTURES = 512
+MIXED_SEED = 3000
+
+
+def mixed_batch_workload(cg, dev):
+    """512 textures: width and height drawn independently and log-uniformly from the powers of two
+    32..2048, full mip chains, formats 60% DXT1 / 25% DXT5 / 15% DXN_XY, content as the colour
+    recipe (DXT5 with alpha noise) or the normal-map recipe, per-texture seeds; generated on the
+    GPU. Returns [(levels (device tensors), width, height, format)]."""
+    from crunch2_gb300 import texgen
+    rng = np.random.default_rng(MIXED_SEED)
+    out = []
+    for i in range(MIXED_TEXTURES):
+        w, h = 1 << int(rng.integers(5, 12)), 1 << int(rng.integers(5, 12))
+        u = float(rng.random())
+        fmt = cg.FMT_DXT1 if u < 0.60 else cg.FMT_DXT5 if u < 0.85 else cg.FMT_DXN_XY
+        seed = MIXED_SEED + i
+        img = texgen.normal_map_torch(w, h, seed, device=dev) if fmt == cg.FMT_DXN_XY else \
+            texgen.colour_texture_torch(w, h, seed, device=dev, with_alpha_noise=(fmt == cg.FMT_DXT5))
+        out.append((texgen.mip_chain_torch(img), w, h, fmt))
+    return out
+
+
+def mixed_batch_leg(cg, dev, stream, timed, steps: int, warmup: int) -> dict:
+    import torch
+    tex = mixed_batch_workload(cg, dev)
+    names = {cg.FMT_DXT1: "DXT1", cg.FMT_DXT5: "DXT5", cg.FMT_DXN_XY: "DXN_XY"}
+    items = []
+    for levels, w, h, fmt in tex:
+        rgba = torch.cat([l.reshape(-1) for l in levels])
+        out = torch.empty(cg.mip_chain_blocks(w, h, len(levels)) * cg.bytes_per_block(fmt), dtype=torch.uint8,
+                          device=dev)
+        items.append((rgba, out, w, h, len(levels), fmt))
+    flags = cg.FLAG_PERCEPTUAL | cg.FLAG_USE_BOTH_BLOCK_TYPES
+    enc = cg.EncodeBatch(items, flags)
+    for _ in range(warmup):
+        enc.launch(use_graph=True, stream=stream)
+    torch.cuda.synchronize()
+    grids, tune_ms = enc.tuning()
+    # parity: every 64th texture against the single-image path, level by level
+    parity = True
+    for (rgba, out, w, h, n, fmt), (levels, *_) in list(zip(items, tex))[::64]:
+        got, ofs = out.cpu().numpy(), 0
+        for l in levels:
+            ref = cg.compress_image(l.cpu().numpy(), fmt, flags).reshape(-1)
+            parity &= bool(np.array_equal(got[ofs:ofs + ref.size], ref))
+            ofs += ref.size
+    enc_ms = timed(lambda: enc.launch(use_graph=True, stream=stream), steps)
+    texels, blocks = enc.texels, enc.blocks
+    enc.close()
+    counts = {names[f]: sum(1 for *_, f2 in tex if f2 == f) for f in names}
+    # .crn of every texture (clustered, q128) through crn_compress, one texture after another
+    host = [([l.cpu().numpy() for l in levels], w, h, fmt) for levels, w, h, fmt in tex]
+    del items
+    t0 = time.perf_counter()
+    crns = [cg.compress_crn([lv], fmt, quality=128, flags=0 if fmt == cg.FMT_DXN_XY else cg.FLAG_PERCEPTUAL)
+            for lv, w, h, fmt in host]
+    crn_s = time.perf_counter() - t0
+    # batched transcode of those files
+    ctxs = [cg.unpack_begin(c) for c in crns]
+    outs = [torch.empty(sum(c.level_bytes(l) for l in range(c.levels)), dtype=torch.uint8, device=dev) for c in ctxs]
+    tb = cg.UnpackBatch([(c, 0, c.levels, o) for c, o in zip(ctxs, outs)])
+    for _ in range(warmup):
+        tb.launch(use_graph=True, stream=stream)
+    tb.status(stream=stream)
+    tx_parity = all(bool((outs[i].cpu().numpy() == ctxs[i].unpack_levels()).all()) for i in range(0, len(ctxs), 64))
+    tx_ms = timed(lambda: tb.launch(use_graph=True, stream=stream), steps)
+    tb.status(stream=stream)
+    exp_ms = timed(lambda: tb.launch(expand_only=True, stream=stream), steps)
+    tx_bytes = tb.bytes
+    variant, _ = tb.tuning()
+    tb.close()
+    for c in ctxs:
+        c.close()
+    return {"textures": MIXED_TEXTURES, "formats": counts, "texels": texels, "blocks": blocks,
+            "workload": "512 textures, W and H log-uniform over 32..2048 (powers of two), full mip chains, "
+                        "60/25/15% DXT1/DXT5/DXN_XY, generated on the GPU (seeded)",
+            "encode": {"value": round(texels / (enc_ms / 1e3) / 1e6, 1), "unit": "Mtexel/s",
+                       "ms_per_batch": round(enc_ms, 3), "parity_vs_single_image": parity,
+                       "grids": {"colour": grids[0], "alpha": grids[1]}, "tuning_ms": tune_ms,
+                       "path": "crngpu_encode_batch (CUDA graph: gather + persistent colour and alpha encoders "
+                               "on two streams), uber, perceptual, inputs resident in HBM (larger than L2)"},
+            "crn_encode": {"value": round(texels / crn_s / 1e6, 2), "unit": "Mtexel/s", "s_total": round(crn_s, 3),
+                           "bytes": sum(len(c) for c in crns),
+                           "path": "crngpu_compress_crn per texture (host RGBA8 in, .crn out), q128"},
+            "transcode": {"value": round(tx_bytes / (tx_ms / 1e3) / 1e9, 3), "unit": "GB/s", "ms_per_batch": round(tx_ms, 3),
+                          "output_bytes": tx_bytes, "expand_ms": round(exp_ms, 4),
+                          "expand_gb_s_output": round(tx_bytes / (exp_ms / 1e3) / 1e9, 1),
+                          "parity_vs_single_context": tx_parity, "expand_variant": variant,
+                          "path": "crngpu_unpack_batch (CUDA graph) over the 512 .crn files"}}
 
 
 def cpu_threads() -> int:
@@ -479,6 +573,11 @@ def main():
     # reference's own .crn of the same textures (reference numbers committed with the fixtures)
     clustered_2048 = clustered_2048_leg(cg, dev, steps=max(1, min(args.steps, 3)))
 
+    # ---- 512 textures of uneven sizes and mixed formats: batched plain encode (one gather + two
+    # persistent encoder launches, CUDA graph), their .crn through crn_compress, and the batched
+    # transcode of those .crn files (one persistent decode + one expansion launch, CUDA graph)
+    mixed_batch = mixed_batch_leg(cg, dev, stream, timed, steps=args.steps, warmup=args.warmup)
+
     peaks, peak_kind = measured_peaks()
     clk = clocks.summary()
     sm_max = clk.get("sm_max_mhz") or peaks.get("sm_max_mhz", 2070.0)
@@ -514,7 +613,7 @@ def main():
                 "e2e": {"value": round(e2e_value, 3), "unit": "Mtexel/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "path": "crngpu_compress_image per level, pinned host buffers"},
                 "learned": learned, "transcode": transcode, "clustered": clustered,
-                "clustered_2048": clustered_2048, "roofline": roofline,
+                "clustered_2048": clustered_2048, "mixed_batch": mixed_batch, "roofline": roofline,
                 "cpu_baseline": cpu,
                 "gpu_launches": args.steps * 1, "clocks": clk, "wall_s_timed": round(wall, 4)}
         print(json.dumps(line))

@@ -54,6 +54,11 @@ class _BatchItem(ctypes.Structure):
                 ("dst", ctypes.c_void_p), ("dst_size", ctypes.c_uint64)]
 
 
+class _EncodeItem(ctypes.Structure):
+    _fields_ = [("rgba", ctypes.c_void_p), ("out", ctypes.c_void_p), ("width", ctypes.c_uint32),
+                ("height", ctypes.c_uint32), ("levels", ctypes.c_uint32), ("format", ctypes.c_uint32)]
+
+
 def lib():
     """Loads libcrngpu.so (building it first if it is missing). Raises if that fails."""
     global _lib
@@ -104,6 +109,16 @@ def lib():
     L.crngpu_compress_crn.restype = i64
     L.crngpu_crn_pack.argtypes = [vp, u32, u32, u32, u32, u32, vp, u64]
     L.crngpu_crn_pack.restype = i64
+    L.crngpu_encode_batch_create.argtypes = [ctypes.POINTER(_EncodeItem), u32, u32]
+    L.crngpu_encode_batch_create.restype = vp
+    L.crngpu_encode_batch_launch.argtypes = [vp, u32, vp]
+    L.crngpu_encode_batch_launch.restype = i32
+    L.crngpu_encode_batch_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float), u32]
+    L.crngpu_encode_batch_tuning.restype = i32
+    L.crngpu_encode_batch_size.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64)]
+    L.crngpu_encode_batch_size.restype = i64
+    L.crngpu_encode_batch_destroy.argtypes = [vp]
+    L.crngpu_encode_batch_destroy.restype = i32
     L.crngpu_profile_counters.argtypes = [i32, ctypes.POINTER(ctypes.c_uint64), vp]
     L.crngpu_profile_counters.restype = i32
     _lib = L
@@ -137,10 +152,21 @@ def _is_torch_cuda(x) -> bool:
 
 
 def _ptr_mem(x):
-    """(pointer, mem kind) of a numpy array or a torch tensor (CUDA = device, CPU = host)."""
+    """(pointer, mem kind) of a C-contiguous numpy array or torch tensor (CUDA = device, CPU = host)."""
     if hasattr(x, "data_ptr"):
+        if not x.is_contiguous():
+            raise CrnGpuError(E_PARAM, "tensor must be contiguous")
         return x.data_ptr(), (MEM_DEVICE if x.is_cuda else MEM_HOST)
+    if not x.flags["C_CONTIGUOUS"]:
+        raise CrnGpuError(E_PARAM, "array must be C-contiguous")
     return x.ctypes.data, MEM_HOST
+
+
+def _contiguous(x):
+    """x itself when already C-contiguous, else a C-contiguous copy (numpy or torch)."""
+    if hasattr(x, "data_ptr"):
+        return x.contiguous()
+    return np.ascontiguousarray(x)
 
 
 def _stream_ptr(stream):
@@ -165,6 +191,7 @@ def _out_like(inp, shape, dtype=np.uint8):
 def dxt1_optimize(blocks, perceptual: bool = True, use_alpha_blocks: bool = True, with_error: bool = False,
                   stream=None):
     """(n, 64) RGBA8 blocks -> (n, 8) dxt1 blocks [, (n,) squared errors]."""
+    blocks = _contiguous(blocks)
     n = int(blocks.shape[0])
     out = _out_like(blocks, (n, 8))
     err = _out_like(blocks, (n,), np.uint64) if with_error else None
@@ -179,6 +206,7 @@ def dxt1_optimize(blocks, perceptual: bool = True, use_alpha_blocks: bool = True
 
 def dxt5a_optimize(blocks, comp_index: int = 3, use_both_block_types: bool = True, stream=None):
     """(n, 64) RGBA8 blocks -> (n, 8) dxt5 alpha blocks of channel comp_index."""
+    blocks = _contiguous(blocks)
     n = int(blocks.shape[0])
     out = _out_like(blocks, (n, 8))
     ip, mem = _ptr_mem(blocks)
@@ -193,6 +221,7 @@ def bytes_per_block(fmt: int) -> int:
 
 def compress_blocks(blocks, fmt: int, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES, stream=None):
     """Batched crn_compress_block: (n, 64) RGBA8 -> (n, 8|16) DXTn blocks."""
+    blocks = _contiguous(blocks)
     n = int(blocks.shape[0])
     out = _out_like(blocks, (n, bytes_per_block(fmt)))
     ip, mem = _ptr_mem(blocks)
@@ -204,6 +233,7 @@ def compress_blocks(blocks, fmt: int, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BO
 def compress_image(rgba, fmt: int = FMT_DXT1, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES,
                    out=None, stream=None):
     """Plain DXTn encode of an (h, w, 4) RGBA8 image -> (blocks_y * blocks_x, 8|16) blocks."""
+    rgba = _contiguous(rgba)
     h, w = int(rgba.shape[0]), int(rgba.shape[1])
     n = ((w + 3) // 4) * ((h + 3) // 4)
     if out is None:
@@ -212,6 +242,61 @@ def compress_image(rgba, fmt: int = FMT_DXT1, flags: int = FLAG_PERCEPTUAL | FLA
     _check(lib().crngpu_compress_image(ip, w, h, 0, fmt, flags, _ptr_mem(out)[0], n * bytes_per_block(fmt), mem,
                                        _stream_ptr(stream)), "crngpu_compress_image")
     return out
+
+
+def mip_chain_blocks(width: int, height: int, levels: int) -> int:
+    """Blocks of a mip chain's levels (each level max(1, w >> l) x max(1, h >> l))."""
+    return sum(((max(1, width >> l) + 3) // 4) * ((max(1, height >> l) + 3) // 4) for l in range(levels))
+
+
+class EncodeBatch:
+    """Plain DXTn encode of many textures' mip chains, mixed sizes and formats, in one gather
+    launch and two persistent encoder launches (crngpu_encode_batch_*). items: (rgba, out, width,
+    height, levels, fmt) with rgba a CUDA uint8 tensor holding the levels' texels back to back and
+    out a CUDA uint8 tensor receiving every level's blocks back to back."""
+
+    def __init__(self, items, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES):
+        self._keep = [(rgba, out) for rgba, out, *_ in items]  # buffers outlive the batch
+        arr = (_EncodeItem * len(items))()
+        for i, (rgba, out, w, h, levels, fmt) in enumerate(items):
+            need = mip_chain_blocks(w, h, levels) * bytes_per_block(fmt)
+            if out.numel() * out.element_size() < need:
+                raise CrnGpuError(E_PARAM, f"EncodeBatch: item {i} output smaller than {need} bytes")
+            arr[i] = _EncodeItem(rgba.data_ptr(), out.data_ptr(), w, h, levels, fmt)
+        self.handle = lib().crngpu_encode_batch_create(arr, len(items), flags)
+        if not self.handle:
+            raise CrnGpuError(E_PARAM, "crngpu_encode_batch_create: " + last_error())
+        tex = ctypes.c_uint64(0)
+        self.blocks = int(lib().crngpu_encode_batch_size(self.handle, ctypes.byref(tex)))
+        self.texels = int(tex.value)
+
+    def launch(self, use_graph: bool = False, stream=None):
+        _check(lib().crngpu_encode_batch_launch(self.handle, 1 if use_graph else 0, _stream_ptr(stream)),
+               "crngpu_encode_batch_launch")
+
+    def tuning(self):
+        """((colour grid, alpha grid), measured ms of the colour then the alpha variants)."""
+        g = (ctypes.c_int32 * 2)()
+        ms = (ctypes.c_float * 16)()
+        n = lib().crngpu_encode_batch_tuning(self.handle, g, ms, 16)
+        return (int(g[0]), int(g[1])), [round(float(ms[i]), 4) for i in range(max(n, 0))]
+
+    def close(self):
+        if self.handle:
+            lib().crngpu_encode_batch_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ------------------------------------------------------------------------------------------

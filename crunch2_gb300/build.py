@@ -27,6 +27,7 @@ UNITS = [
     ("capi.cpp", []),
     ("crn_transcode.cu", []),
     ("encode_api.cu", []),
+    ("encode_batch.cu", []),
     ("dxt_encode.cu", ["--fmad=false"]),
     ("mlp.cu", []),
     ("hc_encode.cu", ["--fmad=false"]),

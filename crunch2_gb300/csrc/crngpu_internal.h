@@ -32,4 +32,24 @@ DevBuf& staging(int slot);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Batched block encoding (many textures, mixed formats). A segment is one element of one texture
+// over its gathered blocks [first_block, first_block + count): the colour half of DXT1/DXT5, the
+// alpha of DXT5/DXT5A or one DXN channel; block b's 8 bytes go to out + (b - first_block) * stride.
+struct EncodeSegment {
+  uint8_t* out;
+  uint32_t first_block, count, stride, options;
+};
+constexpr uint32_t kSegPerceptual = 1u, kSegThreeColour = 2u, kSegBothTypes = 4u, kSegCompShift = 8u;
+// a run of consecutive blocks of one segment, the unit a warp takes
+struct EncodeChunk {
+  uint32_t first, count, segment;
+};
+constexpr uint32_t kColourChunkBlocks = 8;  // blocks per DXT1 chunk (the encoder's blocks per warp)
+int dxt1_chunks_max_grid();
+int dxt5a_chunks_max_grid();
+int launch_dxt1_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,
+                       const EncodeSegment* d_segs, int grid, cudaStream_t s);
+int launch_dxt5a_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,
+                        const EncodeSegment* d_segs, int grid, cudaStream_t s);
+
 }  // namespace crngpu

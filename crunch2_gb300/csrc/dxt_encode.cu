@@ -1133,6 +1133,23 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
   return work;
 }
 
+// cnt (<= kBlocksPerWarp) consecutive blocks from b0 on one warp; block k's result goes to
+// out + k * out_stride (and err_out[k]). Returns the candidate x colour evaluation count.
+__device__ __forceinline__ unsigned long long dxt1_chunk(WarpShared& S, const uint8_t* __restrict__ blocks, uint32_t b0,
+                                                         uint32_t cnt, bool perceptual, bool hc, bool use_alpha,
+                                                         uint8_t* __restrict__ out, uint32_t out_stride,
+                                                         uint64_t* __restrict__ err_out) {
+  const uint32_t lane = lane_id();
+  unsigned long long work = 0;
+  if (lane < cnt) phase1_block(S, lane, blocks + (size_t)(b0 + lane) * 64, perceptual);
+  __syncwarp();
+  #pragma unroll 1
+  for (uint32_t k = 0; k < cnt; k++)
+    work += phase2_block(S, k, blocks + (size_t)(b0 + k) * 64, perceptual, hc, use_alpha, out + (size_t)k * out_stride,
+                         err_out ? err_out + k : nullptr);
+  return work;
+}
+
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
     k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, int perceptual, int hc, int use_alpha,
                   uint8_t* __restrict__ out, uint32_t out_stride, uint64_t* __restrict__ err_out,
@@ -1147,14 +1164,8 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
   for (uint32_t chunk = warp_global; chunk < chunks; chunk += nwarps) {
     const uint32_t b0 = chunk * kBlocksPerWarp;
     const uint32_t cnt = min((uint32_t)kBlocksPerWarp, n - b0);
-    if (lane < cnt) phase1_block(S, lane, blocks + (size_t)(b0 + lane) * 64, perceptual != 0);
-    __syncwarp();
-    #pragma unroll 1
-    for (uint32_t k = 0; k < cnt; k++) {
-      const uint32_t bi = b0 + k;
-      work += phase2_block(S, k, blocks + (size_t)bi * 64, perceptual != 0, hc != 0, use_alpha != 0,
-                           out + (size_t)bi * out_stride, err_out ? err_out + bi : nullptr);
-    }
+    work += dxt1_chunk(S, blocks, b0, cnt, perceptual != 0, hc != 0, use_alpha != 0, out + (size_t)b0 * out_stride,
+                       out_stride, err_out ? err_out + b0 : nullptr);
   }
   if (work_out) {
     for (int o = 16; o > 0; o >>= 1) work += __shfl_xor_sync(FULL_MASK, work, o);
@@ -1196,145 +1207,188 @@ struct Alpha5 {
   }
 };
 
-__global__ void __launch_bounds__(128)
-    k_dxt5a_encode(const uint8_t* __restrict__ blocks, uint32_t n, int comp, int both, uint8_t* __restrict__ out,
-                   uint32_t out_stride) {
+// One DXT5A element (dxt5_endpoint_optimizer::compute, crnlib/crn_dxt5a.cpp:40-196) of the 4x4
+// RGBA8 block px on channel comp, written as 8 bytes to o; a whole warp, lane per candidate.
+__device__ __forceinline__ void alpha_block(const uint8_t* __restrict__ px, int comp, int both, uint8_t* __restrict__ o) {
   const uint32_t lane = lane_id();
-  const uint32_t warp_global = blockIdx.x * 4 + (threadIdx.x >> 5);
-  const uint32_t nwarps = gridDim.x * 4;
-  for (uint32_t bi = warp_global; bi < n; bi += nwarps) {
-    const uint8_t* px = blocks + (size_t)bi * 64;
-    const uint32_t v = lane < 16 ? __ldg(px + lane * 4 + comp) : 0x100u + lane;
-    const unsigned match = __match_any_sync(FULL_MASK, v);
-    const int leader = __ffs(match) - 1;
-    const bool is_leader = lane < 16 && leader == (int)lane;
-    const unsigned lmask = __ballot_sync(FULL_MASK, is_leader);
-    Alpha5 A;
-    A.n = __popc(lmask);
-    A.both = both != 0;
-    const int uidx = __popc(lmask & ((1u << leader) - 1u));
-    // every lane gets the unique values (first-occurrence order) and weights
-    {
-      unsigned m = lmask;
-      for (int i = 0; i < A.n; i++) {
-        const int src = __ffs(m) - 1;
-        m &= m - 1;
-        A.val[i] = __shfl_sync(FULL_MASK, v, src);
-        A.wt[i] = (uint32_t)__popc(__shfl_sync(FULL_MASK, match, src));
-      }
+  const uint32_t v = lane < 16 ? __ldg(px + lane * 4 + comp) : 0x100u + lane;
+  const unsigned match = __match_any_sync(FULL_MASK, v);
+  const int leader = __ffs(match) - 1;
+  const bool is_leader = lane < 16 && leader == (int)lane;
+  const unsigned lmask = __ballot_sync(FULL_MASK, is_leader);
+  Alpha5 A;
+  A.n = __popc(lmask);
+  A.both = both != 0;
+  const int uidx = __popc(lmask & ((1u << leader) - 1u));
+  // every lane gets the unique values (first-occurrence order) and weights
+  {
+    unsigned m = lmask;
+    for (int i = 0; i < A.n; i++) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      A.val[i] = __shfl_sync(FULL_MASK, v, src);
+      A.wt[i] = (uint32_t)__popc(__shfl_sync(FULL_MASK, match, src));
     }
-    uint32_t first = 0, second = 0, berr = kInf;
-    int btype = 0;
-    uint8_t* o = out + (size_t)bi * out_stride;
-    if (A.n == 1) {
-      if (lane == 0) {
-        uint2 w = make_uint2(A.val[0] | (A.val[0] << 8), 0u);
-        *reinterpret_cast<uint2*>(o) = w;
-      }
-      continue;
+  }
+  uint32_t first = 0, second = 0, berr = kInf;
+  int btype = 0;
+  if (A.n == 1) {
+    if (lane == 0) {
+      uint2 w = make_uint2(A.val[0] | (A.val[0] << 8), 0u);
+      *reinterpret_cast<uint2*>(o) = w;
     }
-    auto accept_chain = [&](bool valid, int l, int h, uint32_t err, int type, bool dependent) -> int {
-      unsigned ok = __ballot_sync(FULL_MASK, valid && err < berr);
-      int last = -1;
-      while (ok) {
-        const int j = __ffs(ok) - 1;
-        berr = __shfl_sync(FULL_MASK, err, j);
-        first = (uint32_t)__shfl_sync(FULL_MASK, l, j);
-        second = (uint32_t)__shfl_sync(FULL_MASK, h, j);
-        btype = __shfl_sync(FULL_MASK, type, j);
-        last = j;
-        if (dependent) break;
-        const unsigned after = j == 31 ? 0u : (FULL_MASK << (j + 1));
-        ok = __ballot_sync(FULL_MASK, valid && err < berr) & after;
-      }
-      return last;
-    };
-    // all unique value pairs i < j (compute :83-96)
-    const int npairs = A.n * (A.n - 1) / 2;
-    for (int p0 = 0; p0 < npairs; p0 += 32) {
-      const int p = p0 + (int)lane;
+    return;
+  }
+  auto accept_chain = [&](bool valid, int l, int h, uint32_t err, int type, bool dependent) -> int {
+    unsigned ok = __ballot_sync(FULL_MASK, valid && err < berr);
+    int last = -1;
+    while (ok) {
+      const int j = __ffs(ok) - 1;
+      berr = __shfl_sync(FULL_MASK, err, j);
+      first = (uint32_t)__shfl_sync(FULL_MASK, l, j);
+      second = (uint32_t)__shfl_sync(FULL_MASK, h, j);
+      btype = __shfl_sync(FULL_MASK, type, j);
+      last = j;
+      if (dependent) break;
+      const unsigned after = j == 31 ? 0u : (FULL_MASK << (j + 1));
+      ok = __ballot_sync(FULL_MASK, valid && err < berr) & after;
+    }
+    return last;
+  };
+  // all unique value pairs i < j (compute :83-96)
+  const int npairs = A.n * (A.n - 1) / 2;
+  for (int p0 = 0; p0 < npairs; p0 += 32) {
+    const int p = p0 + (int)lane;
+    int l = 0, h = 0;
+    const bool valid = p < npairs;
+    if (valid) {
+      int i = 0, rem = p;
+      while (rem >= A.n - 1 - i) { rem -= A.n - 1 - i; i++; }
+      l = (int)A.val[i];
+      h = (int)A.val[i + 1 + rem];
+    }
+    uint32_t err = kInf;
+    int type = 0;
+    if (valid) A.eval(l, h, err, type);
+    accept_chain(valid, l, h, err, type, false);
+  }
+  // +-16 probe around the running best (:98-141); the centre moves with each improvement
+  if (berr) {
+    int pos = 0, row_l = (int)first - 16;
+    const int total = 33 * 33;
+    while (pos < total) {
+      const int p = pos + (int)lane;
+      const int row0 = pos / 33;
       int l = 0, h = 0;
-      const bool valid = p < npairs;
+      bool valid = p < total;
       if (valid) {
-        int i = 0, rem = p;
-        while (rem >= A.n - 1 - i) { rem -= A.n - 1 - i; i++; }
-        l = (int)A.val[i];
-        h = (int)A.val[i + 1 + rem];
+        const int r = p / 33, c = p % 33;
+        l = r == row0 ? row_l : (int)first + (r - 16);
+        h = (int)second + (c - 16);
+        valid = l >= 0 && l <= 255 && h >= 0 && h <= 255;
       }
       uint32_t err = kInf;
       int type = 0;
       if (valid) A.eval(l, h, err, type);
-      accept_chain(valid, l, h, err, type, false);
+      const int last = accept_chain(valid, l, h, err, type, true);
+      const int next = last >= 0 ? pos + last + 1 : pos + 32;
+      const int nrow = next / 33;
+      // the reference fixes l when a row starts: a row begun inside this batch used the
+      // centre from before the batch, unless it is the accepted candidate's own row
+      const int last_row = last >= 0 ? (pos + last) / 33 : -1;
+      if (last >= 0 && nrow == last_row) row_l = __shfl_sync(FULL_MASK, l, last);
+      else if (nrow != row0) row_l = (int)first + (nrow - 16);
+      pos = next;
     }
-    // +-16 probe around the running best (:98-141); the centre moves with each improvement
-    if (berr) {
-      int pos = 0, row_l = (int)first - 16;
-      const int total = 33 * 33;
-      while (pos < total) {
-        const int p = pos + (int)lane;
-        const int row0 = pos / 33;
-        int l = 0, h = 0;
-        bool valid = p < total;
-        if (valid) {
-          const int r = p / 33, c = p % 33;
-          l = r == row0 ? row_l : (int)first + (r - 16);
-          h = (int)second + (c - 16);
-          valid = l >= 0 && l <= 255 && h >= 0 && h <= 255;
-        }
-        uint32_t err = kInf;
-        int type = 0;
-        if (valid) A.eval(l, h, err, type);
-        const int last = accept_chain(valid, l, h, err, type, true);
-        const int next = last >= 0 ? pos + last + 1 : pos + 32;
-        const int nrow = next / 33;
-        // the reference fixes l when a row starts: a row begun inside this batch used the
-        // centre from before the batch, unless it is the accepted candidate's own row
-        const int last_row = last >= 0 ? (pos + last) / 33 : -1;
-        if (last >= 0 && nrow == last_row) row_l = __shfl_sync(FULL_MASK, l, last);
-        else if (nrow != row0) row_l = (int)first + (nrow - 16);
-        pos = next;
-      }
+  }
+  // selectors of the winner, reorder rules (:143-185), pack (dxt5_block, crn_dxt.h:318-361)
+  int sel = 0;
+  if (lane < 16) {
+    const int l = (int)first, h = (int)second;
+    int pv[8];
+    pv[0] = l; pv[1] = h;
+    if (btype == 0) {
+      pv[2] = (l * 6 + h) / 7; pv[3] = (l * 5 + h * 2) / 7; pv[4] = (l * 4 + h * 3) / 7;
+      pv[5] = (l * 3 + h * 4) / 7; pv[6] = (l * 2 + h * 5) / 7; pv[7] = (l + h * 6) / 7;
+    } else {
+      pv[2] = (l * 4 + h) / 5; pv[3] = (l * 3 + h * 2) / 5; pv[4] = (l * 2 + h * 3) / 5; pv[5] = (l + h * 4) / 5;
+      pv[6] = 0; pv[7] = 255;
     }
-    // selectors of the winner, reorder rules (:143-185), pack (dxt5_block, crn_dxt.h:318-361)
-    int sel = 0;
-    if (lane < 16) {
-      const int l = (int)first, h = (int)second;
-      int pv[8];
-      pv[0] = l; pv[1] = h;
-      if (btype == 0) {
-        pv[2] = (l * 6 + h) / 7; pv[3] = (l * 5 + h * 2) / 7; pv[4] = (l * 4 + h * 3) / 7;
-        pv[5] = (l * 3 + h * 4) / 7; pv[6] = (l * 2 + h * 5) / 7; pv[7] = (l + h * 6) / 7;
-      } else {
-        pv[2] = (l * 4 + h) / 5; pv[3] = (l * 3 + h * 2) / 5; pv[4] = (l * 2 + h * 3) / 5; pv[5] = (l + h * 4) / 5;
-        pv[6] = 0; pv[7] = 255;
-      }
-      const int x = (int)A.val[uidx];
-      int bd = 1 << 30;
-      for (int j = 0; j < 8; j++) {
-        const int d = (x - pv[j]) * (x - pv[j]);
-        if (d < bd) { bd = d; sel = j; }
-      }
+    const int x = (int)A.val[uidx];
+    int bd = 1 << 30;
+    for (int j = 0; j < 8; j++) {
+      const int d = (x - pv[j]) * (x - pv[j]);
+      if (d < bd) { bd = d; sel = j; }
     }
-    uint32_t f = first, s = second;
-    if (f == s) {
-      sel = 0;
-    } else if (btype) {
-      if (f > s) {
-        const uint32_t t = f; f = s; s = t;
-        const int inv6[8] = {1, 0, 5, 4, 3, 2, 6, 7};
-        sel = inv6[sel];
-      }
-    } else if (f <= s) {
+  }
+  uint32_t f = first, s = second;
+  if (f == s) {
+    sel = 0;
+  } else if (btype) {
+    if (f > s) {
       const uint32_t t = f; f = s; s = t;
-      const int inv8[8] = {1, 0, 7, 6, 5, 4, 3, 2};
-      sel = inv8[sel];
+      const int inv6[8] = {1, 0, 5, 4, 3, 2, 6, 7};
+      sel = inv6[sel];
     }
-    const uint32_t lo_bits = __reduce_or_sync(FULL_MASK, lane < 10 ? ((uint32_t)sel << (3 * lane)) : 0u);
-    const uint32_t hi_bits = __reduce_or_sync(FULL_MASK, (lane >= 10 && lane < 16) ? ((uint32_t)sel << (3 * (lane - 10))) : 0u);
-    if (lane == 0) {
-      const uint64_t bits = (uint64_t)lo_bits | ((uint64_t)hi_bits << 30);
-      const uint64_t word = (uint64_t)f | ((uint64_t)s << 8) | (bits << 16);
-      *reinterpret_cast<uint2*>(o) = make_uint2((uint32_t)word, (uint32_t)(word >> 32));
+  } else if (f <= s) {
+    const uint32_t t = f; f = s; s = t;
+    const int inv8[8] = {1, 0, 7, 6, 5, 4, 3, 2};
+    sel = inv8[sel];
+  }
+  const uint32_t lo_bits = __reduce_or_sync(FULL_MASK, lane < 10 ? ((uint32_t)sel << (3 * lane)) : 0u);
+  const uint32_t hi_bits = __reduce_or_sync(FULL_MASK, (lane >= 10 && lane < 16) ? ((uint32_t)sel << (3 * (lane - 10))) : 0u);
+  if (lane == 0) {
+    const uint64_t bits = (uint64_t)lo_bits | ((uint64_t)hi_bits << 30);
+    const uint64_t word = (uint64_t)f | ((uint64_t)s << 8) | (bits << 16);
+    *reinterpret_cast<uint2*>(o) = make_uint2((uint32_t)word, (uint32_t)(word >> 32));
+  }
+}
+
+__global__ void __launch_bounds__(128)
+    k_dxt5a_encode(const uint8_t* __restrict__ blocks, uint32_t n, int comp, int both, uint8_t* __restrict__ out,
+                   uint32_t out_stride) {
+  const uint32_t warp_global = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const uint32_t nwarps = gridDim.x * 4;
+  for (uint32_t bi = warp_global; bi < n; bi += nwarps)
+    alpha_block(blocks + (size_t)bi * 64, comp, both, out + (size_t)bi * out_stride);
+}
+
+// ------------------------------------------------------------------------------------------
+// Batched (many textures, mixed formats): persistent warps over a chunk table. A chunk is a run of
+// consecutive blocks of one segment (one element of one texture: its DXT1 colour, DXT5 colour or
+// alpha, a DXN channel); the segment gives the output base, stride and encoder options.
+
+static_assert(kColourChunkBlocks <= (uint32_t)kBlocksPerWarp, "a colour chunk must fit one warp's block slots");
+
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
+    k_dxt1_encode_chunks(const uint8_t* __restrict__ blocks, const EncodeChunk* __restrict__ chunks, uint32_t nchunks,
+                         const EncodeSegment* __restrict__ segs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpShared& S = reinterpret_cast<WarpShared*>(smem_raw)[threadIdx.x >> 5];
+  const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  const uint32_t nwarps = gridDim.x * kWarpsPerCta;
+  for (uint32_t c = warp_global; c < nchunks; c += nwarps) {
+    const EncodeChunk ch = chunks[c];
+    const EncodeSegment sg = segs[ch.segment];
+    const bool use_alpha = (sg.options & kSegThreeColour) != 0;
+    dxt1_chunk(S, blocks, ch.first, ch.count, (sg.options & kSegPerceptual) != 0, !use_alpha, use_alpha,
+               sg.out + (size_t)(ch.first - sg.first_block) * sg.stride, sg.stride, nullptr);
+  }
+}
+
+__global__ void __launch_bounds__(128)
+    k_dxt5a_encode_chunks(const uint8_t* __restrict__ blocks, const EncodeChunk* __restrict__ chunks, uint32_t nchunks,
+                          const EncodeSegment* __restrict__ segs) {
+  const uint32_t warp_global = blockIdx.x * 4 + (threadIdx.x >> 5);
+  const uint32_t nwarps = gridDim.x * 4;
+  for (uint32_t c = warp_global; c < nchunks; c += nwarps) {
+    const EncodeChunk ch = chunks[c];
+    const EncodeSegment sg = segs[ch.segment];
+    const int comp = (int)((sg.options >> kSegCompShift) & 3u);
+    const int both = (sg.options & kSegBothTypes) ? 1 : 0;
+    for (uint32_t k = 0; k < ch.count; k++) {
+      const uint32_t b = ch.first + k;
+      alpha_block(blocks + (size_t)b * 64, comp, both, sg.out + (size_t)(b - sg.first_block) * sg.stride);
     }
   }
 }
@@ -1461,6 +1515,42 @@ int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_a
   k_dxt1_encode<<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, perceptual, use_alpha_blocks ? 0 : 1,
                                                        use_alpha_blocks ? 1 : 0, d_out, out_stride, d_err, work);
   return cuda_check(cudaGetLastError(), "launch k_dxt1_encode");
+}
+
+int dxt1_chunks_max_grid() {
+  const size_t smem = sizeof(WarpShared) * kWarpsPerCta;
+  int dev = 0, per_sm = 1, sms = 148;
+  cudaGetDevice(&dev);
+  if (cudaFuncSetAttribute(k_dxt1_encode_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return -1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dxt1_encode_chunks, kWarpsPerCta * 32, smem);
+  return sms * (per_sm < 1 ? 1 : per_sm);
+}
+
+int dxt5a_chunks_max_grid() {
+  int dev = 0, per_sm = 1, sms = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dxt5a_encode_chunks, 128, 0);
+  return sms * (per_sm < 1 ? 1 : per_sm);
+}
+
+int launch_dxt1_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,
+                       const EncodeSegment* d_segs, int grid, cudaStream_t s) {
+  int rc = ensure_tables();
+  if (rc != CRNGPU_OK) return rc;
+  if (!nchunks) return CRNGPU_OK;
+  const size_t smem = sizeof(WarpShared) * kWarpsPerCta;
+  k_dxt1_encode_chunks<<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, d_chunks, nchunks, d_segs);
+  return cuda_check(cudaGetLastError(), "launch k_dxt1_encode_chunks");
+}
+
+int launch_dxt5a_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,
+                        const EncodeSegment* d_segs, int grid, cudaStream_t s) {
+  if (!nchunks) return CRNGPU_OK;
+  k_dxt5a_encode_chunks<<<grid, 128, 0, s>>>(d_blocks, d_chunks, nchunks, d_segs);
+  return cuda_check(cudaGetLastError(), "launch k_dxt5a_encode_chunks");
 }
 
 int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint8_t* d_out, uint32_t out_stride,

@@ -122,7 +122,7 @@ def box_mip(img: np.ndarray) -> np.ndarray:
     xs0 = np.minimum(np.arange(nw) * 2, w - 1)
     xs1 = np.minimum(np.arange(nw) * 2 + 1, w - 1)
     s = (img[ys0][:, xs0].astype(np.uint32) + img[ys0][:, xs1] + img[ys1][:, xs0] + img[ys1][:, xs1])
-    return ((s + 2) >> 2).astype(np.uint8)
+    return np.ascontiguousarray(((s + 2) >> 2).astype(np.uint8))
 
 
 def mip_chain(img: np.ndarray, levels: int | None = None) -> list[np.ndarray]:
@@ -152,47 +152,60 @@ def image_blocks(img: np.ndarray) -> np.ndarray:
     return np.ascontiguousarray(full.reshape(by, 4, bx, 4, 4).transpose(0, 2, 1, 3, 4).reshape(by * bx, 64))
 
 
-def colour_texture_torch(w: int, h: int, seed: int, device="cuda"):
-    """Same recipe as colour_texture (4-octave value noise, period 64, + 40 flat rectangles,
-    alpha 255) computed on the GPU in float32 for large training/evaluation sets. Seeded and
-    deterministic on a given device; not bit-identical to the numpy version."""
+def _h32_torch(device, *keys):
+    """_hash32 on int64 torch tensors (same 32-bit arithmetic)."""
     import torch
     M = 0xFFFFFFFF
+    x = torch.full_like(keys[-1], 0x9E3779B9) if torch.is_tensor(keys[-1]) else torch.tensor(0x9E3779B9)
+    for k in keys:
+        k = k if torch.is_tensor(k) else torch.tensor(k, dtype=torch.int64, device=device)
+        x = (x ^ (k & M)) & M
+        x = (x * 0x85EBCA6B) & M
+        x = x ^ (x >> 13)
+        x = (x * 0xC2B2AE35) & M
+        x = x ^ (x >> 16)
+    return x
 
-    def h32(*keys):
-        x = torch.full_like(keys[-1], 0x9E3779B9) if torch.is_tensor(keys[-1]) else torch.tensor(0x9E3779B9)
-        for k in keys:
-            k = k if torch.is_tensor(k) else torch.tensor(k, dtype=torch.int64, device=device)
-            x = (x ^ (k & M)) & M
-            x = (x * 0x85EBCA6B) & M
-            x = x ^ (x >> 13)
-            x = (x * 0xC2B2AE35) & M
-            x = x ^ (x >> 16)
-        return x
 
+def value_noise_torch(w: int, h: int, period: int, octaves: int, seed: int, channel: int, device="cuda"):
+    """value_noise in float32 on the GPU: the same lattice hashes, float32 interpolation."""
+    import torch
     ys = torch.arange(h, device=device, dtype=torch.int64).view(h, 1).expand(h, w)
     xs = torch.arange(w, device=device, dtype=torch.int64).view(1, w).expand(h, w)
+    total = torch.zeros((h, w), dtype=torch.float32, device=device)
+    amp, norm, p = 1.0, 0.0, float(period)
+    for o in range(octaves):
+        fx, fy = xs.float() / p, ys.float() / p
+        ix, iy = fx.floor().long(), fy.floor().long()
+        tx, ty = fx - ix, fy - iy
+        tx = tx * tx * (3 - 2 * tx)
+        ty = ty * ty * (3 - 2 * ty)
+        u = lambda a, b: _h32_torch(device, seed, channel, o, a, b).float() / 4294967296.0
+        v00, v10, v01, v11 = u(ix, iy), u(ix + 1, iy), u(ix, iy + 1), u(ix + 1, iy + 1)
+        a = v00 + (v10 - v00) * tx
+        b = v01 + (v11 - v01) * tx
+        total += amp * (a + (b - a) * ty)
+        norm += amp
+        amp *= 0.5
+        p = max(p / 2, 1.0)
+    return total / norm
+
+
+def colour_texture_torch(w: int, h: int, seed: int, device="cuda", with_alpha_noise: bool = False):
+    """Same recipe as colour_texture (4-octave value noise, period 64, + 40 flat rectangles; alpha
+    255 or 3-octave noise of period 128) computed on the GPU in float32 for large training,
+    evaluation and batch sets. Seeded and deterministic on a given device; not bit-identical to the
+    numpy version."""
+    import torch
     img = torch.empty((h, w, 4), dtype=torch.uint8, device=device)
     for c in range(3):
-        total = torch.zeros((h, w), dtype=torch.float32, device=device)
-        amp, norm, p = 1.0, 0.0, 64.0
-        for o in range(4):
-            fx, fy = xs.float() / p, ys.float() / p
-            ix, iy = fx.floor().long(), fy.floor().long()
-            tx, ty = fx - ix, fy - iy
-            tx = tx * tx * (3 - 2 * tx)
-            ty = ty * ty * (3 - 2 * ty)
-            u = lambda a, b: h32(seed, c, o, a, b).float() / 4294967296.0
-            v00, v10, v01, v11 = u(ix, iy), u(ix + 1, iy), u(ix, iy + 1), u(ix + 1, iy + 1)
-            a = v00 + (v10 - v00) * tx
-            b = v01 + (v11 - v01) * tx
-            total += amp * (a + (b - a) * ty)
-            norm += amp
-            amp *= 0.5
-            p = max(p / 2, 1.0)
-        img[:, :, c] = (total / norm * 255 + 0.5).floor().clamp(0, 255).to(torch.uint8)
-    img[:, :, 3] = 255
-    r = h32(seed, 1000 + torch.arange(40 * 7, device=device)).view(40, 7).cpu().tolist()
+        total = value_noise_torch(w, h, 64, 4, seed, c, device)
+        img[:, :, c] = (total * 255 + 0.5).floor().clamp(0, 255).to(torch.uint8)
+    if with_alpha_noise:
+        img[:, :, 3] = (value_noise_torch(w, h, 128, 3, seed, 7, device) * 255 + 0.5).floor().clamp(0, 255).to(torch.uint8)
+    else:
+        img[:, :, 3] = 255
+    r = _h32_torch(device, seed, 1000 + torch.arange(40 * 7, device=device)).view(40, 7).cpu().tolist()
     for i in range(40):
         rw, rh = 4 + r[i][0] % 61, 4 + r[i][1] % 61
         x0, y0 = r[i][2] % w, r[i][3] % h
@@ -200,6 +213,48 @@ def colour_texture_torch(w: int, h: int, seed: int, device="cuda"):
         img[y0:y0 + rh, x0:x0 + rw, 1] = r[i][5] & 255
         img[y0:y0 + rh, x0:x0 + rw, 2] = r[i][6] & 255
     return img
+
+
+def normal_map_torch(w: int, h: int, seed: int, strength: float = 4.0, device="cuda"):
+    """normal_map's recipe (fBm height, 5 octaves, period 256, Sobel, unit normal, XY in RG) in
+    float32 on the GPU; not bit-identical to the numpy version."""
+    import torch
+    hgt = value_noise_torch(w, h, 256, 5, seed, 11, device)
+    p = torch.nn.functional.pad(hgt[None, None], (1, 1, 1, 1), mode="replicate")[0, 0]
+    gx = (p[0:-2, 2:] + 2.0 * p[1:-1, 2:] + p[2:, 2:]) - (p[0:-2, 0:-2] + 2.0 * p[1:-1, 0:-2] + p[2:, 0:-2])
+    gy = (p[2:, 0:-2] + 2.0 * p[2:, 1:-1] + p[2:, 2:]) - (p[0:-2, 0:-2] + 2.0 * p[0:-2, 1:-1] + p[0:-2, 2:])
+    nx, ny = -gx * strength, -gy * strength
+    inv = torch.rsqrt(nx * nx + ny * ny + 1.0)
+    img = torch.zeros((h, w, 4), dtype=torch.uint8, device=device)
+    img[:, :, 0] = ((nx * inv) * 0.5 + 0.5).mul(255).add(0.5).floor().clamp(0, 255).to(torch.uint8)
+    img[:, :, 1] = ((ny * inv) * 0.5 + 0.5).mul(255).add(0.5).floor().clamp(0, 255).to(torch.uint8)
+    img[:, :, 3] = 255
+    return img
+
+
+def mip_chain_torch(img, levels: int | None = None):
+    """mip_chain on a (h, w, 4) uint8 torch tensor: the same 2x2 box filter with edge reuse for odd
+    or unit dimensions."""
+    import torch
+    h, w = int(img.shape[0]), int(img.shape[1])
+    full = 1
+    while (w >> full) or (h >> full):
+        full += 1
+    n = full if levels is None else min(levels, full)
+    out = [img]
+    for _ in range(n - 1):
+        cur = out[-1]
+        ch, cw = int(cur.shape[0]), int(cur.shape[1])
+        nh, nw = max(1, ch >> 1), max(1, cw >> 1)
+        dev = cur.device
+        ys0 = torch.clamp(torch.arange(nh, device=dev) * 2, max=ch - 1)
+        ys1 = torch.clamp(torch.arange(nh, device=dev) * 2 + 1, max=ch - 1)
+        xs0 = torch.clamp(torch.arange(nw, device=dev) * 2, max=cw - 1)
+        xs1 = torch.clamp(torch.arange(nw, device=dev) * 2 + 1, max=cw - 1)
+        x = cur.to(torch.int32)
+        s = x[ys0][:, xs0] + x[ys0][:, xs1] + x[ys1][:, xs0] + x[ys1][:, xs1]
+        out.append(((s + 2) >> 2).to(torch.uint8))
+    return out
 
 
 def box_mip_torch(img):

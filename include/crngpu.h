@@ -323,6 +323,41 @@ CRNGPU_API int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch);
 
 CRNGPU_API int crngpu_unpack_batch_destroy(crngpu_unpack_batch batch);
 
+/* Batched plain encode (no single counterpart in the reference, whose dxt_image::init encodes one
+ * image at a time, crnlib/crn_dxt_image.cpp:447-493): the mip chains of many textures of any mix
+ * of sizes and formats (DXT1, the DXT5 family, DXN_XY/YX, DXT5A) in one gather launch and two
+ * persistent encoder launches (colour elements; alpha and DXN channel elements) running side by
+ * side. Every block's result equals crngpu_compress_image's on its level with the same flags. */
+typedef struct crngpu_encode_item {
+    const uint8_t* rgba;  /* device: the levels' RGBA8 texels back to back, level l being
+                             max(1, width >> l) x max(1, height >> l), tightly packed (4-byte aligned) */
+    uint8_t* out;         /* device: every level's blocks back to back, row-major at minimal pitch
+                             (8-byte aligned) */
+    uint32_t width, height, levels, format;
+} crngpu_encode_item;
+
+typedef struct crngpu_encode_batch_s* crngpu_encode_batch;
+
+/* flags: CRNGPU_FLAG_PERCEPTUAL, CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES (as crngpu_compress_image).
+ * Validates every item, uploads the gather and work tables and allocates the gathered-block
+ * buffer (64 bytes per block) once. NULL on failure (crngpu_last_error says which item). */
+CRNGPU_API crngpu_encode_batch crngpu_encode_batch_create(const crngpu_encode_item* items, uint32_t n, uint32_t flags);
+
+/* Enqueues the batch on `stream` without synchronising. The first launch runs the autotuner (each
+ * encoder timed at several CTAs-per-SM launch shapes on the real blocks; synchronises once).
+ * flags: CRNGPU_BATCH_GRAPH captures the launches into a CUDA graph on the first call and replays
+ * it on later calls. The items' input and output buffers must stay valid while the batch exists. */
+CRNGPU_API int crngpu_encode_batch_launch(crngpu_encode_batch batch, uint32_t flags, void* stream);
+
+/* grids[0], grids[1]: the tuned colour / alpha grid sizes (0 before the first launch); ms: the
+ * measured times of the colour variants then the alpha variants. Returns the number of variants. */
+CRNGPU_API int crngpu_encode_batch_tuning(crngpu_encode_batch batch, int32_t* grids, float* ms, uint32_t n);
+
+/* Number of blocks in the batch; *texels (optional) gets the visible texels. */
+CRNGPU_API int64_t crngpu_encode_batch_size(crngpu_encode_batch batch, uint64_t* texels);
+
+CRNGPU_API int crngpu_encode_batch_destroy(crngpu_encode_batch batch);
+
 /* Allocation-free transcode of one level. No counterpart in the reference: it exists for
  * callers that cannot allocate GPU memory while they run -- engines that reserve their whole
  * VRAM budget up front and forbid untracked allocations, and real-time loops in which

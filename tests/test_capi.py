@@ -40,3 +40,16 @@ def test_host_mirror_names_follow_the_reference():
     for name in ("dxt1_optimize", "dxt5a_optimize", "compress_blocks", "compress_image", "unpack_begin",
                  "crn_decompress", "UnpackContext"):
         assert hasattr(cg, name)
+
+
+def test_pointer_helpers_refuse_strided_buffers():
+    """The C ABI takes plain pointers: a strided numpy view (such as a transposed mip level) must
+    be copied to C order by the wrappers, never passed as is."""
+    import numpy as np
+    import crunch2_gb300 as cg
+    a = np.arange(4 * 6 * 4, dtype=np.uint8).reshape(4, 6, 4).transpose(1, 0, 2)
+    with pytest.raises(cg.CrnGpuError):
+        cg._ptr_mem(a)
+    c = cg._contiguous(a)
+    assert c.flags["C_CONTIGUOUS"] and np.array_equal(c, a)
+    assert cg._ptr_mem(c)[1] == cg.MEM_HOST
