@@ -59,6 +59,35 @@ def workload():
     return levels, blocks, texels
 
 
+def clustered_leg(cg, dev, levels, blocks, texels, steps: int) -> dict:
+    """crn_compress of the 1024x1024 mip chain at q128 (DXT1), median wall time of up to 5 calls;
+    RMSE and bits per texel beside the reference's own .crn of the texture (committed fixture),
+    both decoded by the GPU transcoder."""
+    import torch
+    from crunch2_gb300 import learned as LR
+    cg.compress_crn([levels], cg.FMT_DXT1, quality=128)  # warm-up (allocations, tables)
+    crn_times = []
+    for _ in range(max(1, min(steps, 5))):
+        t0 = time.perf_counter()
+        our_crn = cg.compress_crn([levels], cg.FMT_DXT1, quality=128)
+        crn_times.append(time.perf_counter() - t0)
+    crn_s = statistics.median(crn_times)
+
+    def crn_rmse(data):
+        with cg.unpack_begin(data) as c:
+            dec = c.unpack_levels()
+        return LR.rgb_rmse_torch(torch.from_numpy(dec.reshape(-1, 8)).to(dev), torch.from_numpy(blocks).to(dev))
+
+    with open(CRN_FIXTURE, "rb") as fh:
+        ref_crn = fh.read()
+    return {"value": round(texels / crn_s / 1e6, 3), "unit": "Mtexel/s", "s_per_texture": round(crn_s, 4),
+            "quality": 128, "rmse": round(crn_rmse(our_crn), 4), "rmse_reference_crn": round(crn_rmse(ref_crn), 4),
+            "bits_per_texel": round(len(our_crn) * 8 / texels, 4),
+            "bits_per_texel_reference": round(len(ref_crn) * 8 / texels, 4),
+            "path": "crngpu_compress_crn: host RGBA8 mip chain -> crn_comp block gather (host) -> H2D -> "
+                    "clustered encode (every dxt_hc stage on the GPU) -> D2H -> .crn writer (host); wall time"}
+
+
 CONFIG2_REFERENCE = os.path.join(ROOT, "tests", "golden", "config2_reference.json")
 
 
@@ -352,7 +381,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--skip", default="", help="comma-separated legs to leave out of the run (their keys are "
+                                               "null): clustered, clustered_2048, mixed")
     args = ap.parse_args()
+    skip = set(x for x in args.skip.split(",") if x)
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -546,37 +578,19 @@ def main():
     # ---- crn_compress of the same mip chain at quality 128 (DXT1): clustered encode on the GPU
     # (crngpu_hc_compress) + the .crn writer (host); quality and size beside the reference's own
     # .crn of this texture (committed fixture), both decoded by the GPU transcoder
-    cg.compress_crn([levels], cg.FMT_DXT1, quality=128)  # warm-up (allocations, tables)
-    crn_times = []
-    for _ in range(max(1, min(args.steps, 5))):
-        t0 = time.perf_counter()
-        our_crn = cg.compress_crn([levels], cg.FMT_DXT1, quality=128)
-        crn_times.append(time.perf_counter() - t0)
-    crn_s = statistics.median(crn_times)
-
-    def crn_rmse(data):
-        with cg.unpack_begin(data) as c:
-            dec = c.unpack_levels()
-        return LR.rgb_rmse_torch(torch.from_numpy(dec.reshape(-1, 8)).to(dev), torch.from_numpy(blocks).to(dev))
-
-    with open(CRN_FIXTURE, "rb") as fh:
-        ref_crn = fh.read()
-    clustered = {"value": round(texels / crn_s / 1e6, 3), "unit": "Mtexel/s", "s_per_texture": round(crn_s, 4),
-                 "quality": 128, "rmse": round(crn_rmse(our_crn), 4), "rmse_reference_crn": round(crn_rmse(ref_crn), 4),
-                 "bits_per_texel": round(len(our_crn) * 8 / texels, 4),
-                 "bits_per_texel_reference": round(len(ref_crn) * 8 / texels, 4),
-                 "path": "crngpu_compress_crn: host RGBA8 mip chain -> crn_comp block gather (host) -> H2D -> "
-                         "clustered encode (every dxt_hc stage on the GPU) -> D2H -> .crn writer (host); wall time"}
+    clustered = None if "clustered" in skip else clustered_leg(cg, dev, levels, blocks, texels, args.steps)
 
     # ---- the 2048x2048 DXT5 (colour + alpha noise) and DXN_XY (normal map) mip chains at quality
     # 128: crn_compress wall time, and the RMSEs of the GPU-decoded result beside those of the
     # reference's own .crn of the same textures (reference numbers committed with the fixtures)
-    clustered_2048 = clustered_2048_leg(cg, dev, steps=max(1, min(args.steps, 3)))
+    clustered_2048 = None if "clustered_2048" in skip else \
+        clustered_2048_leg(cg, dev, steps=max(1, min(args.steps, 3)))
 
     # ---- 512 textures of uneven sizes and mixed formats: batched plain encode (one gather + two
     # persistent encoder launches, CUDA graph), their .crn through crn_compress, and the batched
     # transcode of those .crn files (one persistent decode + one expansion launch, CUDA graph)
-    mixed_batch = mixed_batch_leg(cg, dev, stream, timed, steps=args.steps, warmup=args.warmup)
+    mixed_batch = None if "mixed" in skip else \
+        mixed_batch_leg(cg, dev, stream, timed, steps=args.steps, warmup=args.warmup)
 
     peaks, peak_kind = measured_peaks()
     clk = clocks.summary()
