@@ -533,7 +533,8 @@ def main():
     tx_parity = bool((outs[-1].cpu().numpy() == ctx0.unpack_levels()).all())
     batch_ms = timed(lambda: batch.launch(use_graph=True, stream=stream), args.steps)
     batch.status(stream=stream)
-    expand_ms = timed(lambda: batch.launch(expand_only=True, stream=stream), args.steps)
+    with torch.cuda.nvtx.range("expand_only"):  # lets a profiler select these launches
+        expand_ms = timed(lambda: batch.launch(expand_only=True, stream=stream), args.steps)
     # end to end through the C ABI: the batch plus the copy of every texture's DXT1 levels to
     # pinned host memory (the .crn files are uploaded once, by crngpu_unpack_begin)
     host_tx = torch.empty((TX_BATCH, tx_bytes), dtype=torch.uint8).pin_memory()
@@ -568,8 +569,10 @@ def main():
                                             "level is one serial prefix-code chain, so this is its latency"},
                  "expand_roofline": None,
                  "expand_autotune": {"variant": tune_variant, "ms_per_variant": tune_ms,
-                                     "variants": "tile of 1024 << (v >> 1) blocks; DXT1 palettes staged in "
-                                                 "shared memory when v is odd"},
+                                     "variants": "0-11: tile of 1024 << (v >> 1) blocks, DXT1 palettes staged "
+                                                 "in shared memory when v is odd; 12-15: 8192/16384-block tiles "
+                                                 "with the next pass's records loaded ahead (staged when odd); "
+                                                 "16, 17: 16384/32768-block tiles, pipelined, 4096-block passes"},
                  "workload": f"{TX_BATCH} contexts of the 1024x1024 q128 DXT1 .crn (11 levels, {len(crn)} bytes)"}
     expand = {"kernel": "k_crn_expand_tiles", "bound": "hbm", "unit": "GB/s",
               "ms": round(expand_ms, 4), "bytes_algorithmic": exp_bytes,

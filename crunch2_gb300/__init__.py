@@ -107,6 +107,9 @@ def lib():
     L.crngpu_crn_decompress.restype = None
     L.crngpu_compress_crn.argtypes = [vp, u32, u32, u32, u32, u32, u32, u32, vp, u64]
     L.crngpu_compress_crn.restype = i64
+    L.crngpu_compress_crn_bitrate.argtypes = [vp, u32, u32, u32, u32, u32, ctypes.c_float, u32, vp, u64,
+                                              ctypes.POINTER(u32), ctypes.POINTER(ctypes.c_float)]
+    L.crngpu_compress_crn_bitrate.restype = i64
     L.crngpu_crn_pack.argtypes = [vp, u32, u32, u32, u32, u32, vp, u64]
     L.crngpu_crn_pack.restype = i64
     L.crngpu_encode_batch_create.argtypes = [ctypes.POINTER(_EncodeItem), u32, u32]
@@ -390,8 +393,8 @@ class UnpackBatch:
     def tuning(self):
         """(chosen expansion variant, measured ms per variant) of the autotuner (first launch)."""
         v = ctypes.c_int32(-1)
-        ms = (ctypes.c_float * 16)()
-        n = lib().crngpu_unpack_batch_tuning(self.handle, ctypes.byref(v), ms, 16)
+        ms = (ctypes.c_float * 32)()
+        n = lib().crngpu_unpack_batch_tuning(self.handle, ctypes.byref(v), ms, 32)
         return int(v.value), [round(float(ms[i]), 4) for i in range(max(n, 0))]
 
     def close(self):
@@ -446,6 +449,26 @@ def crn_layout_from_levels(level_blocks, width: int, height: int, faces: int, bp
             v = np.asarray(fl[f]).reshape((h + 3) // 4, (w + 3) // 4, bpb)
             parts.append(np.pad(v, ((0, H - v.shape[0]), (0, W - v.shape[1]), (0, 0)), mode="edge").reshape(-1, bpb))
     return np.concatenate(parts)
+
+
+def compress_crn_bitrate(faces_levels, target_bitrate: float, fmt: int = FMT_DXT1, flags: int = FLAG_PERCEPTUAL):
+    """crn_compress with m_target_bitrate: (.crn bytes, chosen quality level, its bitrate in bits
+    per texel over all faces and levels)."""
+    h, w = faces_levels[0][0].shape[:2]
+    flat = np.concatenate([np.ascontiguousarray(im, dtype=np.uint8).reshape(-1) for face in faces_levels for im in face])
+    L = lib()
+    q, br = ctypes.c_uint32(0), ctypes.c_float(0)
+    args = (flat.ctypes.data, w, h, len(faces_levels[0]), len(faces_levels), fmt, ctypes.c_float(target_bitrate), flags)
+    bpb = 8 if fmt in (FMT_DXT1, FMT_DXT5A) else 16
+    cap = sum(((max(1, w >> l) + 7) // 8 * 2) * ((max(1, h >> l) + 7) // 8 * 2) * bpb
+              for l in range(len(faces_levels[0]))) * len(faces_levels) + (1 << 20)
+    out = np.zeros(cap, np.uint8)
+    size = _check(int(L.crngpu_compress_crn_bitrate(*args, out.ctypes.data, cap, ctypes.byref(q), ctypes.byref(br))),
+                  "crngpu_compress_crn_bitrate")
+    if size > cap:
+        raise CrnGpuError(E_PARAM, "crngpu_compress_crn_bitrate: output larger than expected")
+    out = out[:size]
+    return out.tobytes(), int(q.value), float(br.value)
 
 
 def compress_crn(faces_levels, fmt: int = FMT_DXT1, quality: int = 128, flags: int = FLAG_PERCEPTUAL) -> bytes:

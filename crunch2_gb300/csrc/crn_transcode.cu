@@ -81,7 +81,7 @@ constexpr uint32_t kExpandThreads = 256;
 // autotuner (crngpu_unpack_batch_launch, first launch) times all of them and keeps the fastest.
 constexpr int kTileSizes = 6;           // 1024 .. 32768 blocks per tile, processed 2048 at a time
 constexpr uint32_t kSubBlocks = 2048;   // blocks per pass of a CTA over its tile (8 per thread)
-constexpr int kExpandVariants = 2 * kTileSizes;
+constexpr int kExpandVariants = 2 * kTileSizes + 6;  // + pipelined tiles (2048 or 4096 blocks per pass)
 constexpr uint32_t kStageMin = 1024;    // DXT1 tiles at least this large may stage their palettes
 // Decoder shared memory per CTA: five first-level tables + the row buffers of one texture's
 // levels (at most 2 x 1024 + 2 x 16 words for a 4096-texel-wide texture with 16 levels).
@@ -344,6 +344,83 @@ __device__ __forceinline__ uint2 alpha_words(const DevPalettes& pal, uint32_t r)
 // words, then stores, so each thread keeps several loads in flight. With STAGE, DXT1 tiles of at
 // least kStageMin blocks first copy the two colour palettes into shared memory, so the per-block
 // gathers hit shared memory instead of costing a 32-byte L2 sector per 4-byte word.
+// 8-byte blocks (DXT1, DXT5A), pairs of blocks: thread t handles blocks first + 2 * (k * threads +
+// t) and the next one. narrow_load reads the pass's index records, narrow_emit gathers the palette
+// words and stores the blocks.
+template <uint32_t kPer>
+__device__ __forceinline__ void narrow_load(const ExpandJob& J, uint32_t first, uint32_t nblk, uint32_t (&r)[kPer]) {
+  const uint32_t* rec = reinterpret_cast<const uint32_t*>(J.rec);
+  const bool rec8 = ((uintptr_t)rec & 7) == 0;  // pairs of records (b0 even) are 8-byte aligned
+#pragma unroll
+  for (uint32_t k = 0; k < kPer / 2; k++) {
+    const uint32_t b0 = first + 2 * (k * kExpandThreads + threadIdx.x);
+    if (b0 + 1 < nblk && rec8) {
+      const uint2 v = __ldg(reinterpret_cast<const uint2*>(rec + b0));
+      r[2 * k] = v.x;
+      r[2 * k + 1] = v.y;
+    } else if (b0 + 1 < nblk) {
+      r[2 * k] = __ldg(rec + b0);
+      r[2 * k + 1] = __ldg(rec + b0 + 1);
+    } else {
+      r[2 * k] = b0 < nblk ? __ldg(rec + b0) : 0u;
+      r[2 * k + 1] = 0u;
+    }
+  }
+}
+
+template <uint32_t kPer>
+__device__ __forceinline__ void narrow_emit(const ExpandJob& J, uint32_t first, uint32_t nblk, const uint32_t (&r)[kPer],
+                                            const uint32_t* s_ep, const uint32_t* s_sel) {
+  const uint32_t kind = J.kind, bx = J.bx;
+  const DevPalettes pal = J.pal;
+  const bool flat = J.flat;
+  uint2 w[kPer];
+#pragma unroll
+  for (uint32_t k = 0; k < kPer; k++) {
+    if (kind == kKDxt1) {
+      const uint32_t ei = clamp_idx(r[k] & 0xFFFFu, pal.n_cep), si = clamp_idx(r[k] >> 16, pal.n_csel);
+      w[k] = s_ep ? make_uint2(s_ep[ei], s_sel[si]) : make_uint2(__ldg(pal.colour_ep + ei), __ldg(pal.colour_sel + si));
+    } else {
+      w[k] = alpha_words(pal, r[k]);
+    }
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < kPer / 2; k++) {
+    const uint32_t b0 = first + 2 * (k * kExpandThreads + threadIdx.x);
+    if (b0 >= nblk) break;
+    if (flat && J.vec && b0 + 1 < nblk) {
+      __stcs(reinterpret_cast<uint4*>(J.dst + (uint64_t)b0 * 8),
+             make_uint4(w[2 * k].x, w[2 * k].y, w[2 * k + 1].x, w[2 * k + 1].y));
+    } else {
+      for (uint32_t q = 0; q < 2 && b0 + q < nblk; q++) {
+        const uint32_t bb = b0 + q, y = bb / bx, x = bb - y * bx;
+        uint32_t* d = reinterpret_cast<uint32_t*>(J.dst + (uint64_t)y * J.pitch + (uint64_t)x * 8);
+        d[0] = w[2 * k + q].x;
+        d[1] = w[2 * k + q].y;
+      }
+    }
+  }
+}
+
+// 8-byte blocks over [first, end) in passes of SUB blocks, the next pass's records loaded before
+// this pass's palette gathers and stores, so two dependent round trips overlap.
+template <uint32_t SUB>
+__device__ __forceinline__ void narrow_pipelined(const ExpandJob& J, uint32_t first, uint32_t end, const uint32_t* s_ep,
+                                                 const uint32_t* s_sel) {
+  constexpr uint32_t kPer = SUB / kExpandThreads;
+  const uint32_t nblk = J.bx * J.by;
+  uint32_t ra[kPer], rb[kPer];
+  narrow_load<kPer>(J, first, nblk, ra);
+  for (uint32_t f = first; f < end; f += SUB) {
+    const bool more = f + SUB < end;
+    if (more) narrow_load<kPer>(J, f + SUB, nblk, rb);
+    narrow_emit<kPer>(J, f, nblk, ra, s_ep, s_sel);
+    if (!more) break;
+#pragma unroll
+    for (uint32_t k = 0; k < kPer; k++) ra[k] = rb[k];
+  }
+}
+
 template <bool WIDE, uint32_t TILE>  // WIDE: 16-byte blocks (DXT5, DXN); else 8-byte blocks (DXT1, DXT5A)
 __device__ __forceinline__ void expand_tile(const ExpandJob& J, uint32_t first, const uint32_t* s_ep,
                                             const uint32_t* s_sel) {
@@ -353,51 +430,10 @@ __device__ __forceinline__ void expand_tile(const ExpandJob& J, uint32_t first, 
   const DevPalettes pal = J.pal;
   const bool flat = J.flat;  // minimal pitch: the face is one contiguous array of blocks
   if (!WIDE) {
-    // pairs of blocks: thread t handles blocks first + 2 * (k * threads + t) and the next one
     uint32_t r[kPer];
-    const uint32_t* rec = reinterpret_cast<const uint32_t*>(J.rec);
-    const bool rec8 = ((uintptr_t)rec & 7) == 0;  // pairs of records (b0 even) are 8-byte aligned
-#pragma unroll
-    for (uint32_t k = 0; k < kPer / 2; k++) {
-      const uint32_t b0 = first + 2 * (k * kExpandThreads + threadIdx.x);
-      if (b0 + 1 < nblk && rec8) {
-        const uint2 v = __ldg(reinterpret_cast<const uint2*>(rec + b0));
-        r[2 * k] = v.x;
-        r[2 * k + 1] = v.y;
-      } else if (b0 + 1 < nblk) {
-        r[2 * k] = __ldg(rec + b0);
-        r[2 * k + 1] = __ldg(rec + b0 + 1);
-      } else {
-        r[2 * k] = b0 < nblk ? __ldg(rec + b0) : 0u;
-        r[2 * k + 1] = 0u;
-      }
-    }
-    uint2 w[kPer];
-#pragma unroll
-    for (uint32_t k = 0; k < kPer; k++) {
-      if (kind == kKDxt1) {
-        const uint32_t ei = clamp_idx(r[k] & 0xFFFFu, pal.n_cep), si = clamp_idx(r[k] >> 16, pal.n_csel);
-        w[k] = s_ep ? make_uint2(s_ep[ei], s_sel[si]) : make_uint2(__ldg(pal.colour_ep + ei), __ldg(pal.colour_sel + si));
-      } else {
-        w[k] = alpha_words(pal, r[k]);
-      }
-    }
-#pragma unroll
-    for (uint32_t k = 0; k < kPer / 2; k++) {
-      const uint32_t b0 = first + 2 * (k * kExpandThreads + threadIdx.x);
-      if (b0 >= nblk) break;
-      if (flat && J.vec && b0 + 1 < nblk) {
-        __stcs(reinterpret_cast<uint4*>(J.dst + (uint64_t)b0 * 8),
-               make_uint4(w[2 * k].x, w[2 * k].y, w[2 * k + 1].x, w[2 * k + 1].y));
-      } else {
-        for (uint32_t q = 0; q < 2 && b0 + q < nblk; q++) {
-          const uint32_t bb = b0 + q, y = bb / bx, x = bb - y * bx;
-          uint32_t* d = reinterpret_cast<uint32_t*>(J.dst + (uint64_t)y * J.pitch + (uint64_t)x * 8);
-          d[0] = w[2 * k + q].x;
-          d[1] = w[2 * k + q].y;
-        }
-      }
-    }
+    narrow_load<kPer>(J, first, nblk, r);
+    narrow_emit<kPer>(J, first, nblk, r, s_ep, s_sel);
+    (void)kind; (void)bx; (void)pal; (void)flat;
   } else {
     constexpr uint32_t kPerW = kPer / 2;  // 16-byte blocks: half as many per thread per pass
 #pragma unroll 1
@@ -439,12 +475,12 @@ __device__ __forceinline__ void expand_tile(const ExpandJob& J, uint32_t first, 
 // Dynamic shared memory (STAGE): the staged DXT1 colour palettes, smem_words = the largest
 // n_cep + n_csel of the launch's DXT1 jobs. A CTA covers TILE blocks in passes of up to
 // kSubBlocks, so a large tile pays for the palette copy once.
-template <uint32_t TILE, bool STAGE>
+template <uint32_t TILE, bool STAGE, bool PIPE, uint32_t SUB = kSubBlocks>
 __global__ void __launch_bounds__(kExpandThreads) k_crn_expand_tiles(const ExpandJob* __restrict__ jobs,
                                                                       const uint2* __restrict__ tiles,
                                                                       uint32_t smem_words) {
   extern __shared__ uint32_t s_pal[];
-  constexpr uint32_t kSub = TILE < kSubBlocks ? TILE : kSubBlocks;
+  constexpr uint32_t kSub = TILE < SUB ? TILE : SUB;
   const uint2 t = tiles[blockIdx.x];  // (job, first block)
   const ExpandJob& J = jobs[t.x];
   const uint32_t nblk = J.bx * J.by;
@@ -456,24 +492,39 @@ __global__ void __launch_bounds__(kExpandThreads) k_crn_expand_tiles(const Expan
       for (uint32_t i = threadIdx.x; i < n_ep; i += kExpandThreads) s_pal[i] = __ldg(J.pal.colour_ep + i);
       for (uint32_t i = threadIdx.x; i < n_sel; i += kExpandThreads) s_pal[n_ep + i] = __ldg(J.pal.colour_sel + i);
       __syncthreads();
-      for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, s_pal, s_pal + n_ep);
+      if (PIPE) narrow_pipelined<kSub>(J, t.y, end, s_pal, s_pal + n_ep);
+      else for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, s_pal, s_pal + n_ep);
     } else {
-      for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, nullptr, nullptr);
+      if (PIPE) narrow_pipelined<kSub>(J, t.y, end, nullptr, nullptr);
+      else for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, nullptr, nullptr);
     }
   } else if (J.kind == kKDxt5a) {
-    for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, nullptr, nullptr);
+    if (PIPE) narrow_pipelined<kSub>(J, t.y, end, nullptr, nullptr);
+    else for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, nullptr, nullptr);
   } else {
     for (uint32_t f = t.y; f < end; f += kSub) expand_tile<true, kSub>(J, f, nullptr, nullptr);
   }
 }
 
-// variant v: tile size 1024 << (v >> 1), palettes staged when v is odd
+// variant v < 12: tile of 1024 << (v >> 1) blocks, palettes staged when v is odd; v = 12..15: the
+// 8192- and 16384-block tiles with the next pass's records loaded ahead (staged when v is odd);
+// v = 16, 17: 16384- and 32768-block tiles, pipelined, 4096-block passes (16 blocks per thread)
 typedef void (*ExpandKernel)(const ExpandJob*, const uint2*, uint32_t);
 const ExpandKernel kExpandKernels[kExpandVariants] = {
-    k_crn_expand_tiles<1024, false>,  k_crn_expand_tiles<1024, true>,  k_crn_expand_tiles<2048, false>,
-    k_crn_expand_tiles<2048, true>,   k_crn_expand_tiles<4096, false>, k_crn_expand_tiles<4096, true>,
-    k_crn_expand_tiles<8192, false>,  k_crn_expand_tiles<8192, true>,  k_crn_expand_tiles<16384, false>,
-    k_crn_expand_tiles<16384, true>,  k_crn_expand_tiles<32768, false>, k_crn_expand_tiles<32768, true>};
+    k_crn_expand_tiles<1024, false, false>,  k_crn_expand_tiles<1024, true, false>,
+    k_crn_expand_tiles<2048, false, false>,  k_crn_expand_tiles<2048, true, false>,
+    k_crn_expand_tiles<4096, false, false>,  k_crn_expand_tiles<4096, true, false>,
+    k_crn_expand_tiles<8192, false, false>,  k_crn_expand_tiles<8192, true, false>,
+    k_crn_expand_tiles<16384, false, false>, k_crn_expand_tiles<16384, true, false>,
+    k_crn_expand_tiles<32768, false, false>, k_crn_expand_tiles<32768, true, false>,
+    k_crn_expand_tiles<8192, false, true>,   k_crn_expand_tiles<8192, true, true>,
+    k_crn_expand_tiles<16384, false, true>,  k_crn_expand_tiles<16384, true, true>,
+    k_crn_expand_tiles<16384, false, true, 4096>, k_crn_expand_tiles<32768, false, true, 4096>};
+// the tile-table index (tile of 1024 << i blocks) of each variant
+constexpr int kVariantTile[kExpandVariants] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 3, 3, 4, 4, 4, 5};
+// whether a variant stages the DXT1 palettes in dynamic shared memory
+constexpr bool kVariantStage[kExpandVariants] = {false, true, false, true, false, true, false, true, false,
+                                                 true,  false, true, false, true, false, true, false, false};
 int g_expand_variant[64] = {};  // per device: the autotuner's last choice (0 until tuned)
 
 // ------------------------------------------------------------------------------------------
@@ -712,8 +763,8 @@ int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
     if ((e = cudaFuncSetAttribute(k_crn_decode_textures, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDecodeSmemMax)) != cudaSuccess)
       return cuda_check(e, "decoder shared memory attribute");
-    for (int v = 1; v < kExpandVariants; v += 2)
-      if ((e = cudaFuncSetAttribute(kExpandKernels[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+    for (int v = 0; v < kExpandVariants; v++)
+      if (kVariantStage[v] && (e = cudaFuncSetAttribute(kExpandKernels[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)(2 * kMaxSyms * sizeof(uint32_t)))) != cudaSuccess)
         return cuda_check(e, "expansion shared memory attribute");
     attr_set[dev] = true;
@@ -749,9 +800,9 @@ int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStre
     int dev = 0;
     cudaGetDevice(&dev);
     const int v = variant >= 0 ? variant : g_expand_variant[dev & 63];
-    const int ts = v >> 1;
+    const int ts = kVariantTile[v];
     const uint2* tiles = reinterpret_cast<const uint2*>(d_jobs + p.tile_ofs[ts]);
-    const size_t smem = (v & 1) ? (size_t)p.pal_words * 4 : 0;
+    const size_t smem = kVariantStage[v] ? (size_t)p.pal_words * 4 : 0;
     kExpandKernels[v]<<<p.tile_ctas[ts], kExpandThreads, smem, s>>>(ej, tiles, p.pal_words);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_expand_tiles");
   }

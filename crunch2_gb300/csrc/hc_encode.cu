@@ -2911,79 +2911,189 @@ extern "C" int crngpu_hc_codebook_sizes(uint32_t width, uint32_t height, uint32_
 // crnlib/crnlib.cpp:242-267 -> crn_comp::compress_internal, crnlib/crn_comp.cpp:1515-1611):
 // crn_comp's block gather (edge clamped, levels padded to 8 texels, crn_comp.cpp:717-741), the
 // clustered encode on the GPU, then the .crn writer on the host.
+namespace crngpu {
+namespace {
+
+// The quality-independent part of crn_compress: the blocks of every level and face in crn_comp's
+// layout (crn_comp::alias_images / quantize_images, crnlib/crn_comp.cpp:454-463, 717-741),
+// gathered on the host with edge clamping and uploaded once; a pass per quality level then runs
+// the clustered encode and the writer.
+struct CrnSource {
+  crngpu_hc_params P;
+  uint32_t width = 0, height = 0, levels = 0, faces = 0, format = 0, bpb = 0;
+  uint64_t texels = 0;
+  DevBuf d_in, d_out;
+
+  int prepare(const uint8_t* rgba_levels, uint32_t w, uint32_t h, uint32_t nl, uint32_t nf, uint32_t fmt,
+              uint32_t flags, const char* who) {
+    if (!rgba_levels || !w || !h || w > 4096 || h > 4096 || !nl || nl > 16 || (nf != 1 && nf != 6)) {
+      set_error(std::string(who) + ": bad dimensions, level or face count");
+      return CRNGPU_E_PARAM;
+    }
+    uint32_t full = 1;
+    while ((w >> full) || (h >> full)) full++;
+    if (nl > full) { set_error(std::string(who) + ": more levels than the mip chain has"); return CRNGPU_E_PARAM; }
+    width = w; height = h; levels = nl; faces = nf; format = fmt;
+    std::memset(&P, 0, sizeof(P));
+    P.struct_size = sizeof(P);
+    std::vector<uint32_t> blocks;
+    std::vector<size_t> img_ofs((size_t)faces * levels);
+    size_t ofs = 0;
+    for (uint32_t f = 0; f < faces; f++)
+      for (uint32_t l = 0; l < levels; l++) {
+        img_ofs[(size_t)f * levels + l] = ofs;
+        ofs += (size_t)std::max(1u, width >> l) * std::max(1u, height >> l) * 4;
+        texels += (uint64_t)std::max(1u, width >> l) * std::max(1u, height >> l);
+      }
+    for (uint32_t l = 0; l < levels; l++) {
+      const uint32_t lw = std::max(1u, width >> l), lh = std::max(1u, height >> l);
+      const uint32_t W = ((lw + 7) & ~7u) >> 2, H = ((lh + 7) & ~7u) >> 2;
+      P.levels[l].first_block = (uint32_t)(blocks.size() / 16);
+      P.levels[l].num_blocks = W * H * faces;
+      P.levels[l].block_width = W;
+      P.levels[l].weight = std::min(12.0f, powf(1.3f, (float)l));
+      for (uint32_t f = 0; f < faces; f++) {
+        const uint32_t* img = reinterpret_cast<const uint32_t*>(rgba_levels + img_ofs[(size_t)f * levels + l]);
+        for (uint32_t by = 0; by < H; by++)
+          for (uint32_t bx = 0; bx < W; bx++)
+            for (uint32_t dy = 0; dy < 4; dy++)
+              for (uint32_t dx = 0; dx < 4; dx++) {
+                const uint32_t x = std::min(bx * 4 + dx, lw - 1), y = std::min(by * 4 + dy, lh - 1);
+                uint32_t px;
+                std::memcpy(&px, img + (size_t)y * lw + x, 4);
+                blocks.push_back(px);
+              }
+      }
+    }
+    P.num_blocks = (uint32_t)(blocks.size() / 16);
+    P.num_levels = levels;
+    P.num_faces = faces;
+    const bool colour_fmt = format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5;
+    P.perceptual = colour_fmt && (flags & CRNGPU_FLAG_PERCEPTUAL) ? 1 : 0;
+    P.adaptive_tile_color_psnr_derating = 2.0f;
+    P.adaptive_tile_alpha_psnr_derating = 2.0f;
+    P.color_alpha_weighting_ratio = 3.0f;
+    P.alpha_component = 3;
+    bpb = (format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5A) ? 8 : 16;
+    cudaError_t e;
+    if ((e = d_in.ensure(blocks.size() * 4)) != cudaSuccess || (e = d_out.ensure((size_t)P.num_blocks * bpb)) != cudaSuccess)
+      return cuda_check(e, "alloc blocks");
+    if ((e = cudaMemcpy(d_in.ptr, blocks.data(), blocks.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return cuda_check(e, "copy blocks");
+    return CRNGPU_OK;
+  }
+
+  // One compress pass at `quality`: the .crn bytes into `file`.
+  int pass(uint32_t quality, std::vector<uint8_t>& file) {
+    uint32_t sizes[4];
+    if (crngpu_hc_codebook_sizes(width, height, quality, format, sizes) != CRNGPU_OK) return CRNGPU_E_PARAM;
+    P.color_endpoint_codebook_size = sizes[0];
+    P.color_selector_codebook_size = sizes[1];
+    P.alpha_endpoint_codebook_size = sizes[2];
+    P.alpha_selector_codebook_size = sizes[3];
+    int rc = crngpu_hc_compress(static_cast<const uint8_t*>(d_in.ptr), &P, format, static_cast<uint8_t*>(d_out.ptr),
+                                nullptr, nullptr);
+    if (rc != CRNGPU_OK) return rc;
+    std::vector<uint8_t> dxt((size_t)P.num_blocks * bpb);
+    cudaError_t e;
+    if ((e = cudaMemcpy(dxt.data(), d_out.ptr, dxt.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+      return cuda_check(e, "copy result");
+    // a .crn is smaller than its DXT blocks plus palettes (8192 entries of at most 8 bytes each,
+    // twice) and the models; grow once if not
+    file.resize(dxt.size() + (1u << 18));
+    int64_t n = crngpu_crn_pack(dxt.data(), width, height, levels, faces, format, file.data(), file.size());
+    if (n > (int64_t)file.size()) {
+      file.resize((size_t)n);
+      n = crngpu_crn_pack(dxt.data(), width, height, levels, faces, format, file.data(), file.size());
+    }
+    if (n < 0) return (int)n;
+    file.resize((size_t)n);
+    return CRNGPU_OK;
+  }
+};
+
+int64_t deliver(const std::vector<uint8_t>& file, void* out, uint64_t out_capacity) {
+  if (out && out_capacity >= file.size()) std::memcpy(out, file.data(), file.size());
+  return (int64_t)file.size();
+}
+
+}  // namespace
+}  // namespace crngpu
+
 extern "C" int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels,
                                        uint32_t faces, uint32_t format, uint32_t quality_level, uint32_t flags,
                                        void* out, uint64_t out_capacity) {
   using namespace crngpu;
-  using namespace crngpu::hc;
   clear_error();
-  if (!rgba_levels || !width || !height || width > 4096 || height > 4096 || !levels || levels > 16 ||
-      (faces != 1 && faces != 6) || quality_level > 255) {
-    set_error("crngpu_compress_crn: bad dimensions, level, face count or quality");
-    return CRNGPU_E_PARAM;
-  }
-  uint32_t full = 1;
-  while ((width >> full) || (height >> full)) full++;
-  if (levels > full) { set_error("crngpu_compress_crn: more levels than the mip chain has"); return CRNGPU_E_PARAM; }
-  // gather blocks: per level, per face, rows of the padded block width
-  crngpu_hc_params P;
-  std::memset(&P, 0, sizeof(P));
-  P.struct_size = sizeof(P);
-  std::vector<uint32_t> blocks;
-  std::vector<size_t> img_ofs((size_t)faces * levels);
-  size_t ofs = 0;
-  for (uint32_t f = 0; f < faces; f++)
-    for (uint32_t l = 0; l < levels; l++) {
-      img_ofs[(size_t)f * levels + l] = ofs;
-      ofs += (size_t)std::max(1u, width >> l) * std::max(1u, height >> l) * 4;
-    }
-  for (uint32_t l = 0; l < levels; l++) {
-    const uint32_t w = std::max(1u, width >> l), h = std::max(1u, height >> l);
-    const uint32_t W = ((w + 7) & ~7u) >> 2, H = ((h + 7) & ~7u) >> 2;
-    P.levels[l].first_block = (uint32_t)(blocks.size() / 16);
-    P.levels[l].num_blocks = W * H * faces;
-    P.levels[l].block_width = W;
-    P.levels[l].weight = std::min(12.0f, powf(1.3f, (float)l));
-    for (uint32_t f = 0; f < faces; f++) {
-      const uint32_t* img = reinterpret_cast<const uint32_t*>(rgba_levels + img_ofs[(size_t)f * levels + l]);
-      for (uint32_t by = 0; by < H; by++)
-        for (uint32_t bx = 0; bx < W; bx++)
-          for (uint32_t dy = 0; dy < 4; dy++)
-            for (uint32_t dx = 0; dx < 4; dx++) {
-              const uint32_t x = std::min(bx * 4 + dx, w - 1), y = std::min(by * 4 + dy, h - 1);
-              uint32_t px;
-              std::memcpy(&px, img + (size_t)y * w + x, 4);
-              blocks.push_back(px);
-            }
-    }
-  }
-  P.num_blocks = (uint32_t)(blocks.size() / 16);
-  P.num_levels = levels;
-  P.num_faces = faces;
-  const bool colour_fmt = format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5;
-  P.perceptual = colour_fmt && (flags & CRNGPU_FLAG_PERCEPTUAL) ? 1 : 0;
-  uint32_t sizes[4];
-  if (crngpu_hc_codebook_sizes(width, height, quality_level, format, sizes) != CRNGPU_OK) return CRNGPU_E_PARAM;
-  P.color_endpoint_codebook_size = sizes[0];
-  P.color_selector_codebook_size = sizes[1];
-  P.alpha_endpoint_codebook_size = sizes[2];
-  P.alpha_selector_codebook_size = sizes[3];
-  P.adaptive_tile_color_psnr_derating = 2.0f;
-  P.adaptive_tile_alpha_psnr_derating = 2.0f;
-  P.color_alpha_weighting_ratio = 3.0f;
-  P.alpha_component = 3;
-  const uint32_t bpb = (format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5A) ? 8 : 16;
-  DevBuf d_in, d_out;
-  cudaError_t e;
-  if ((e = d_in.ensure(blocks.size() * 4)) != cudaSuccess || (e = d_out.ensure((size_t)P.num_blocks * bpb)) != cudaSuccess)
-    return cuda_check(e, "alloc blocks");
-  if ((e = cudaMemcpy(d_in.ptr, blocks.data(), blocks.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
-    return cuda_check(e, "copy blocks");
-  int rc = crngpu_hc_compress(static_cast<const uint8_t*>(d_in.ptr), &P, format, static_cast<uint8_t*>(d_out.ptr),
-                              nullptr, nullptr);
+  if (quality_level > 255) { set_error("crngpu_compress_crn: quality above 255"); return CRNGPU_E_PARAM; }
+  CrnSource src;
+  int rc = src.prepare(rgba_levels, width, height, levels, faces, format, flags, "crngpu_compress_crn");
   if (rc != CRNGPU_OK) return rc;
-  std::vector<uint8_t> dxt((size_t)P.num_blocks * bpb);
-  if ((e = cudaMemcpy(dxt.data(), d_out.ptr, dxt.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
-    return cuda_check(e, "copy result");
-  return crngpu_crn_pack(dxt.data(), width, height, levels, faces, format, out, out_capacity);
+  std::vector<uint8_t> file;
+  if ((rc = src.pass(quality_level, file)) != CRNGPU_OK) return rc;
+  return deliver(file, out, out_capacity);
+}
+
+extern "C" int64_t crngpu_compress_crn_bitrate(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
+                                               uint32_t levels, uint32_t faces, uint32_t format, float target_bitrate,
+                                               uint32_t flags, void* out, uint64_t out_capacity,
+                                               uint32_t* quality_out, float* bitrate_out) {
+  using namespace crngpu;
+  clear_error();
+  if (!(target_bitrate > 0.0f)) { set_error("crngpu_compress_crn_bitrate: target bitrate must be positive"); return CRNGPU_E_PARAM; }
+  CrnSource src;
+  int rc = src.prepare(rgba_levels, width, height, levels, faces, format, flags, "crngpu_compress_crn_bitrate");
+  if (rc != CRNGPU_OK) return rc;
+  // interpolative search over the quality levels (create_compressed_texture,
+  // crnlib/crn_texture_comp.cpp:120-245): each trial's bitrate is cached; after the first trial the
+  // next quality is interpolated between the nearest tried levels that bracket the target (or taken
+  // a third of the way up the open range); after 8 trials the search is a plain bisection. The
+  // closest bitrate at or below the target wins, else the closest above; a result within 0.005 bpp
+  // below the target ends the search.
+  const int kLowest = 0, kHighest = 255, kMaxIterations = 8;
+  float cached[256];
+  for (float& c : cached) c = -1.0f;
+  int low = kLowest, high = kHighest, best_q = -1;
+  float best_rate = 1e10f;
+  std::vector<uint8_t> best_file, file;
+  bool force_bisection = false;
+  for (int iter = 0; low <= high; iter++) {
+    int trial = (low + high) / 2;
+    if (iter && !force_bisection) {
+      int bl = trial;
+      while (cached[bl] < 0 && bl > kLowest) bl--;
+      if (cached[bl] < 0) {
+        trial = (int)((float)low + ((float)high - (float)low) * .33f);
+      } else {
+        int bh = trial + 1;
+        if (bh <= kHighest) {
+          while (cached[bh] < 0 && bh < kHighest) bh++;
+          if (cached[bh] >= 0) {
+            const float lr = cached[bl], hr = cached[bh];
+            if (lr < hr && lr < target_bitrate && hr >= target_bitrate) {
+              const int q = low + (int)(((target_bitrate - lr) * (float)(high - low)) / (hr - lr));
+              if (q >= low && q <= high) trial = q;
+            }
+          }
+        }
+      }
+    }
+    if ((rc = src.pass((uint32_t)trial, file)) != CRNGPU_OK) return rc;
+    const float rate = (float)file.size() * 8.0f / (float)src.texels;
+    cached[trial] = rate;
+    if (best_q < 0 || (rate <= target_bitrate && best_rate > target_bitrate) ||
+        ((rate <= target_bitrate || best_rate > target_bitrate) &&
+         std::fabs(rate - target_bitrate) < std::fabs(best_rate - target_bitrate))) {
+      best_rate = rate;
+      best_q = trial;
+      best_file.swap(file);
+      if (best_rate <= target_bitrate && std::fabs(best_rate - target_bitrate) < .005f) break;
+    }
+    if (rate > target_bitrate) high = trial - 1;
+    else low = trial + 1;
+    if (iter + 1 > kMaxIterations) force_bisection = true;
+  }
+  if (quality_out) *quality_out = (uint32_t)best_q;
+  if (bitrate_out) *bitrate_out = best_rate;
+  return deliver(best_file, out, out_capacity);
 }

@@ -189,6 +189,20 @@ CRNGPU_API int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t widt
                                        uint32_t faces, uint32_t format, uint32_t quality_level, uint32_t flags,
                                        void* out, uint64_t out_capacity);
 
+/* crn_compress with a target bitrate instead of a quality level (crn_comp_params::m_target_bitrate,
+ * inc/crnlib.h:254; the search of create_compressed_texture, crnlib/crn_texture_comp.cpp:120-245):
+ * the reference's interpolative search over quality levels 0..255, each trial a full clustered
+ * encode and .crn write (bitrate = file bits / texels over all faces and levels), keeping the
+ * closest bitrate at or below the target (else the closest above). The blocks are gathered and
+ * uploaded once for all trials. The reference's retry without adaptive tiles is not made: its
+ * clustered encoder ignores that flag (dxt_hc::params::m_hierarchical is never read), so the retry
+ * repeats the same search. *quality_out / *bitrate_out (optional) get the chosen level and its
+ * bitrate. Returns the chosen file's size (copied to `out` when out_capacity suffices) or an error. */
+CRNGPU_API int64_t crngpu_compress_crn_bitrate(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
+                                               uint32_t levels, uint32_t faces, uint32_t format, float target_bitrate,
+                                               uint32_t flags, void* out, uint64_t out_capacity,
+                                               uint32_t* quality_out, float* bitrate_out);
+
 /* Codebook sizes for a quality level (crn_comp::quantize_images, crnlib/crn_comp.cpp:541-577):
  * sizes4 = colour endpoints, colour selectors, alpha endpoints, alpha selectors. */
 CRNGPU_API int crngpu_hc_codebook_sizes(uint32_t width, uint32_t height, uint32_t quality_level, uint32_t format,
@@ -311,11 +325,13 @@ CRNGPU_API int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t fl
  * a block stream held an invalid code or palette index (the reference's bool result). */
 CRNGPU_API int crngpu_unpack_batch_status(crngpu_unpack_batch batch, void* stream);
 
-/* Autotuner result: the first launch of a batch decodes, then times each expansion variant
- * (tile of 1024 << (v >> 1) blocks; DXT1 palettes staged in shared memory when v is odd) and keeps
- * the fastest for the batch and as the device's default for later single-texture calls.
- * *variant (-1 before the first launch) and up to n measured times in ms; returns the number of
- * variants. */
+/* Autotuner result: the first launch of a batch decodes, then times each expansion variant and
+ * keeps the fastest for the batch and as the device's default for later single-texture calls.
+ * Variants 0..11: tiles of 1024 << (v >> 1) blocks, DXT1 palettes staged in shared memory when v
+ * is odd; 12..15: 8192- and 16384-block tiles whose next pass of index records is loaded before the
+ * current pass's palette gathers (staged when v is odd); 16, 17: 16384- and 32768-block tiles,
+ * pipelined, 4096-block passes. *variant (-1 before the first launch) and up to n measured times in
+ * ms; returns the number of variants. */
 CRNGPU_API int crngpu_unpack_batch_tuning(crngpu_unpack_batch batch, int32_t* variant, float* ms, uint32_t n);
 
 /* Total output bytes of the batch (sum of the items' level sizes). */

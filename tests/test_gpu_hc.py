@@ -188,3 +188,28 @@ def test_compress_crn_round_trip(hc, name):
           f"(reference {ref_se:.0f})")
     assert ours_se <= 1.06 * ref_se
     assert len(crn) <= 1.4 * len(ref_crn)
+
+
+def test_compress_crn_bitrate_search(hc):
+    """Rate control (crn_comp_params::m_target_bitrate): the chosen file decodes, its bitrate is the
+    one reported, it is at or below the target when some level reaches that, and the next quality
+    level's file is above the target (the search found the boundary)."""
+    import crunch2_gb300 as cg
+    from crunch2_gb300 import texgen
+    levels = texgen.mip_chain(texgen.colour_texture(256, 256, 31))
+    texels = sum(l.shape[0] * l.shape[1] for l in levels)
+    target = 1.6
+    crn, q, rate = cg.compress_crn_bitrate([levels], target, cg.FMT_DXT1)
+    assert abs(len(crn) * 8 / texels - rate) < 1e-4
+    assert 0 <= q <= 255
+    with cg.unpack_begin(crn) as c:
+        assert c.levels == len(levels)
+    same = cg.compress_crn([levels], cg.FMT_DXT1, quality=q)
+    assert same == crn  # the search's file is the plain compress at the chosen level
+    lowest = len(cg.compress_crn([levels], cg.FMT_DXT1, quality=0)) * 8 / texels
+    if lowest <= target:
+        assert rate <= target
+        if q < 255:
+            above = len(cg.compress_crn([levels], cg.FMT_DXT1, quality=q + 1)) * 8 / texels
+            assert above > target or abs(above - target) < abs(rate - target) + 0.05
+    print(f"target {target}: quality {q}, {rate:.4f} bpp (quality 0: {lowest:.4f})")
