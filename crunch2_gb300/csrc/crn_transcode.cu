@@ -100,7 +100,7 @@ struct Bits {
   const uint8_t* p;   // stream start
   uint32_t pos, end;  // byte offset of `next`, stream size
   uint32_t next;      // the word at pos (masked past the end)
-  uint64_t buf;
+  uint32_t hi, lo;    // the next n <= 64 stream bits, MSB first in hi:lo; the bits past them are zero
   int n;
   __device__ __forceinline__ uint32_t load_word(uint32_t at) const {
     if (at >= end) return 0u;
@@ -109,10 +109,10 @@ struct Bits {
     return w;
   }
   __device__ __forceinline__ void init(const uint8_t* src, uint32_t size) {
-    p = src; pos = 0; end = size; buf = 0; n = 0;
-    while (((uintptr_t)(p + pos) & 3) && n <= 56) {
+    p = src; pos = 0; end = size; hi = 0; lo = 0; n = 0;
+    while (((uintptr_t)(p + pos) & 3) && n <= 24) {  // at most 3 bytes up to word alignment
       const uint32_t v = pos < end ? (uint32_t)__ldg(p + pos) : 0u;
-      buf |= (uint64_t)v << (56 - n);
+      hi |= v << (24 - n);
       n += 8;
       pos++;
     }
@@ -120,12 +120,20 @@ struct Bits {
   }
   __device__ __forceinline__ void refill() {
     if (n <= 32) {
-      buf |= (uint64_t)next << (32 - n);
+      const uint64_t w = (uint64_t)next << (32 - n);  // the word's bits at positions n .. n + 31
+      hi |= (uint32_t)(w >> 32);
+      lo = (uint32_t)w;
       n += 32;
       pos += 4;
       if ((pos & 127) == 0 && pos + 1024 < end) asm volatile("prefetch.global.L1 [%0];" ::"l"(p + pos + 1024));
       next = load_word(pos);
     }
+  }
+  __device__ __forceinline__ uint32_t peek16() const { return hi >> 16; }
+  __device__ __forceinline__ void consume(uint32_t len) {  // len <= 16
+    hi = __funnelshift_l(lo, hi, len);
+    lo <<= len;
+    n -= (int)len;
   }
 };
 
@@ -133,7 +141,7 @@ struct Bits {
 // table, then a walk over left-aligned per-length limits. -1: no such code.
 __device__ __forceinline__ int decode_sym(Bits& b, const DevModel* __restrict__ m) {
   b.refill();
-  const uint32_t v = (uint32_t)(b.buf >> 48);
+  const uint32_t v = b.peek16();
   const uint32_t e = __ldg(&m->lut[v >> (16 - kLutBits)]);
   uint32_t s, len;
   if (e != kLutLong) {
@@ -147,8 +155,7 @@ __device__ __forceinline__ int decode_sym(Bits& b, const DevModel* __restrict__ 
     if (idx < 0 || (uint32_t)idx >= __ldg(&m->num_syms)) return -1;
     s = __ldg(&m->sorted[idx]);
   }
-  b.buf <<= len;
-  b.n -= (int)len;
+  b.consume(len);
   return (int)s;
 }
 
@@ -161,10 +168,12 @@ __device__ __forceinline__ uint32_t rb_b(uint32_t e) { return (e >> 15) & 0x1FFF
 __host__ __device__ constexpr uint32_t models_used(uint32_t kind) { return kind == kKDxt5 ? 5u : 3u; }
 
 // Decodes one symbol with a first-level table in shared memory (`lut`) and, for the rare codes
-// longer than kLutBits, the device model `m`. -1: no such code.
-__device__ __forceinline__ int decode_sym_s(Bits& b, const uint32_t* __restrict__ lut, const DevModel* __restrict__ m) {
+// longer than kLutBits, the device model `m`. An invalid code sets `bad` and yields symbol 0 after
+// consuming kMaxCodeLen bits, so a corrupt stream still ends after its block count.
+__device__ __forceinline__ uint32_t decode_sym(Bits& b, const uint32_t* __restrict__ lut,
+                                               const DevModel* __restrict__ m, uint32_t& bad) {
   b.refill();
-  const uint32_t v = (uint32_t)(b.buf >> 48);
+  const uint32_t v = b.peek16();
   const uint32_t e = lut[v >> (16 - kLutBits)];
   uint32_t s, len;
   if (e != kLutLong) {
@@ -173,20 +182,26 @@ __device__ __forceinline__ int decode_sym_s(Bits& b, const uint32_t* __restrict_
   } else {
     len = kLutBits + 1;
     while (len <= (uint32_t)kMaxCodeLen && v >= __ldg(&m->limit[len])) len++;
-    if (len > (uint32_t)kMaxCodeLen) return -1;
-    const int idx = __ldg(&m->base[len]) + (int)(v >> (16 - len));
-    if (idx < 0 || (uint32_t)idx >= __ldg(&m->num_syms)) return -1;
-    s = __ldg(&m->sorted[idx]);
+    s = 0;
+    if (len > (uint32_t)kMaxCodeLen) {
+      bad |= 1u;
+      len = kMaxCodeLen;
+    } else {
+      const int idx = __ldg(&m->base[len]) + (int)(v >> (16 - len));
+      if (idx < 0 || (uint32_t)idx >= __ldg(&m->num_syms)) bad |= 1u;
+      else s = __ldg(&m->sorted[idx]);
+    }
   }
-  b.buf <<= len;
-  b.n -= (int)len;
-  return (int)s;
+  b.consume(len);
+  return s;
 }
 
 // One level stream (all its faces), the loop of unpack_dxt1/dxt5/dxn/dxt5a
 // (inc/crn_decomp.h:3944-4223). `luts` holds the first-level tables of the models this format
 // reads (ref, then delta/selector of endpoint A, then of endpoint B for DXT5); `rb` is the lane's
-// row buffer. Returns a kSt* status.
+// row buffer. Returns a kSt* status. Errors do not leave the loop: invalid codes are flagged as they
+// occur, out-of-range palette indices through the largest index seen, and the stream runs to its
+// block count, which keeps the loop free of early exits.
 template <int KIND>
 __device__ uint32_t decode_level(const StreamJob& J, const uint32_t* __restrict__ luts, uint32_t* __restrict__ rb) {
   constexpr bool colour = KIND == kKDxt1 || KIND == kKDxt5;
@@ -207,69 +222,65 @@ __device__ uint32_t decode_level(const StreamJob& J, const uint32_t* __restrict_
   for (uint32_t x = 0; x < W; x++) rb[x] = 0;
   Bits b;
   b.init(J.src, J.src_size);
-  uint32_t iA = 0, iB = 0, group = 0;
+  uint32_t iA = 0, iB = 0, bad = 0;
+  // the largest endpoint / selector index seen: a stream is corrupt if it ever leaves a palette
+  // (the expansion clamps every index, so the records of such a stream stay in bounds)
+  uint32_t max_a = 0, max_b = 0, max_sa = 0, max_sb = 0;
   uint32_t* rec32 = reinterpret_cast<uint32_t*>(J.rec);
   uint64_t* rec64 = reinterpret_cast<uint64_t*>(J.rec);
+  // one block given its reference kind and its row-buffer word (whose low bits are already the
+  // reference of the block below, on even rows)
+  auto block = [&](uint32_t ref, uint32_t e, uint32_t x, bool vis) {
+    if (ref == 0) {
+      iA += decode_sym(b, lDA, mDA, bad);
+      iA -= iA >= nA ? nA : 0u;
+      if (two) {
+        iB += decode_sym(b, lDB, mDB, bad);
+        iB -= iB >= nB ? nB : 0u;
+      }
+    }
+    if (ref <= 1) {
+      e = rb_pack(e & 3u, iA, iB);
+    } else {
+      iA = rb_a(e);
+      iB = rb_b(e);
+    }
+    max_a = max(max_a, iA);
+    rb[x] = e;
+    const uint32_t sa = decode_sym(b, lSA, mSA, bad);
+    max_sa = max(max_sa, sa);
+    uint32_t sb = 0;
+    if (two) {
+      max_b = max(max_b, iB);
+      sb = decode_sym(b, lSB, mSB, bad);
+      max_sb = max(max_sb, sb);
+    }
+    if (vis) {
+      const uint32_t lo = iA | (sa << 16);
+      if (!two) *rec32++ = lo;
+      else *rec64++ = (uint64_t)lo | ((uint64_t)(iB | (sb << 16)) << 32);
+    }
+  };
   for (uint32_t f = 0; f < faces; f++) {
-    for (uint32_t y = 0; y < H; y++) {
-      const bool yvis = y < by;
-      const bool odd = y & 1;
+    for (uint32_t y = 0; y < H; y += 2) {
+      // even row: one reference group per 2x2 chunk gives this block's and the one below's
+      // reference for the left and the right column
+      const bool vis0 = y < by;
+      for (uint32_t x = 0; x < W; x += 2) {
+        const uint32_t g = decode_sym(b, lR, mR, bad) & 0xFFu;  // reference_group is a uint8
+        block(g & 3u, (rb[x] & ~3u) | ((g >> 2) & 3u), x, vis0 && x < bx);
+        block((g >> 4) & 3u, (rb[x + 1] & ~3u) | ((g >> 6) & 3u), x + 1, vis0 && x + 1 < bx);
+      }
+      // odd row: the references stored by the row above
+      const bool vis1 = y + 1 < by;
       for (uint32_t x = 0; x < W; x++) {
-        uint32_t e = rb[x];
-        uint32_t ref;
-        if (!odd) {
-          if (!(x & 1)) {
-            const int g = decode_sym_s(b, lR, mR);
-            if (g < 0) return kStBadCode;
-            group = (uint32_t)g & 0xFFu;  // reference_group is a uint8
-          }
-          ref = group & 3u;
-          e = (e & ~3u) | ((group >> 2) & 3u);
-          group >>= 4;
-        } else {
-          ref = e & 3u;
-        }
-        if (ref == 0) {
-          const int d = decode_sym_s(b, lDA, mDA);
-          if (d < 0) return kStBadCode;
-          iA += (uint32_t)d;
-          if (iA >= nA) iA -= nA;
-          if (iA >= nA) return kStBadIndex;
-          if (two) {
-            const int d2 = decode_sym_s(b, lDB, mDB);
-            if (d2 < 0) return kStBadCode;
-            iB += (uint32_t)d2;
-            if (iB >= nB) iB -= nB;
-            if (iB >= nB) return kStBadIndex;
-          }
-        }
-        if (ref <= 1) {
-          e = rb_pack(e & 3u, iA, iB);
-        } else {
-          iA = rb_a(e);
-          iB = rb_b(e);
-          if (iA >= nA || (two && iB >= nB)) return kStBadIndex;
-        }
-        rb[x] = e;
-        const int sa = decode_sym_s(b, lSA, mSA);
-        if (sa < 0) return kStBadCode;
-        if ((uint32_t)sa >= nSA) return kStBadIndex;
-        uint32_t sb = 0;
-        if (two) {
-          const int t = decode_sym_s(b, lSB, mSB);
-          if (t < 0) return kStBadCode;
-          if ((uint32_t)t >= nSB) return kStBadIndex;
-          sb = (uint32_t)t;
-        }
-        if (yvis && x < bx) {
-          const uint32_t lo = iA | ((uint32_t)sa << 16);
-          if (!two) *rec32++ = lo;
-          else *rec64++ = (uint64_t)lo | ((uint64_t)(iB | (sb << 16)) << 32);
-        }
+        const uint32_t e = rb[x];
+        block(e & 3u, e, x, vis1 && x < bx);
       }
     }
   }
-  return kStOk;
+  if (max_a >= nA || max_sa >= nSA || (two && (max_b >= nB || max_sb >= nSB))) bad |= 2u;
+  return (bad & 1u) ? kStBadCode : (bad & 2u) ? kStBadIndex : kStOk;
 }
 
 // Persistent decoder: one warp per texture (one batch item: one file, up to 32 level streams),
@@ -278,19 +289,24 @@ __device__ uint32_t decode_level(const StreamJob& J, const uint32_t* __restrict_
 // block_buffer_element entries) in a compact slice of shared memory.
 // Dynamic shared memory: [lut_words table words][rb_total row-buffer words].
 // `counter` must be zero at launch; items are ordered largest first.
-__global__ void __launch_bounds__(32) k_crn_decode_textures(const TexJob* __restrict__ items, uint32_t nitems,
-                                                            const StreamJob* __restrict__ streams,
-                                                            uint32_t* __restrict__ counter, uint32_t lut_words,
-                                                            uint32_t rb_total, uint32_t* __restrict__ status) {
+constexpr uint32_t kDecodeWarps = 4;
+__global__ void __launch_bounds__(kDecodeWarps * 32) k_crn_decode_textures(const TexJob* __restrict__ items,
+                                                                          uint32_t nitems,
+                                                                          const StreamJob* __restrict__ streams,
+                                                                          uint32_t* __restrict__ counter,
+                                                                          uint32_t lut_words, uint32_t rb_total,
+                                                                          uint32_t* __restrict__ status) {
   extern __shared__ uint32_t smem[];
+  __shared__ uint32_t s_item;
   uint32_t* luts = smem;
   uint32_t* rb_base = smem + lut_words;
-  const uint32_t lane = threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t err = kStOk;
   for (;;) {
-    uint32_t it = 0;
-    if (lane == 0) it = atomicAdd(counter, 1u);
-    it = __shfl_sync(0xFFFFFFFFu, it, 0);
+    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    __syncthreads();  // every thread has read s_item before it is rewritten
     if (it >= nitems) break;
     const TexJob T = items[it];
     const uint32_t kind = T.kind;
@@ -300,16 +316,18 @@ __global__ void __launch_bounds__(32) k_crn_decode_textures(const TexJob* __rest
     {
       const bool colour = kind == kKDxt5 || kind == kKDxt1;
       const int srcm[5] = {kMRef, colour ? kMEp0 : kMEp1, colour ? kMSel0 : kMSel1, kMEp1, kMSel1};
-      __syncwarp();
       for (uint32_t t = 0; t < nm; t++) {
         const uint4* src = reinterpret_cast<const uint4*>(T.models[srcm[t]].lut);
         uint4* dst = reinterpret_cast<uint4*>(luts + (t << kLutBits));
-        for (uint32_t k = lane; k < (1u << kLutBits) / 4; k += 32) dst[k] = __ldg(src + k);
+        for (uint32_t k = threadIdx.x; k < (1u << kLutBits) / 4; k += blockDim.x) dst[k] = __ldg(src + k);
       }
-      __syncwarp();
     }
-    if (lane < T.nlev) {
-      const StreamJob J = streams[T.first + lane];
+    __syncthreads();
+    // level streams, largest first: stream w < kDecodeWarps - 1 alone on lane 0 of warp w, the
+    // rest on the lanes of the last warp, so the longest streams share no warp with others
+    const uint32_t si = warp + 1 < kDecodeWarps ? (lane == 0 ? warp : 0xFFFFFFFFu) : (kDecodeWarps - 1 + lane);
+    if (si < T.nlev) {
+      const StreamJob J = streams[T.first + si];
       const uint32_t W = (J.bx + 1) & ~1u;
       if (J.rb_ofs + W <= rb_total && J.kind == kind) {  // host validated; never false
         uint32_t* rb = rb_base + J.rb_ofs;
@@ -323,7 +341,7 @@ __global__ void __launch_bounds__(32) k_crn_decode_textures(const TexJob* __rest
         err = max(err, st);
       }
     }
-    __syncwarp();
+    __syncthreads();  // the texture's streams are done before its tables are replaced
   }
   if (err) atomicMax(status, err);
 }
@@ -679,6 +697,9 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
       T.work = std::max<uint64_t>(T.work, (uint64_t)li.blocks_x * li.blocks_y * F.faces * (kind == kKDxt1 || kind == kKDxt5a ? 1 : 2));
       sj.push_back(j);
     }
+    // the texture's longest streams first: the decoder gives each of the first few its own warp
+    std::stable_sort(sj.begin(), sj.end(),
+                     [](const StreamJob& a, const StreamJob& b) { return a.bx * a.by > b.bx * b.by; });
     T.rb_words = rb;
     p.rb_words = std::max(p.rb_words, rb);
     p.lut_words = std::max(p.lut_words, models_used(kind) << kLutBits);
@@ -770,7 +791,9 @@ int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
     attr_set[dev] = true;
   }
   *smem = (size_t)(p.lut_words + p.rb_words) * sizeof(uint32_t);
-  const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(32, (uint32_t)(smem_sm[dev] / (*smem + 1024))));
+  // CTAs of kDecodeWarps warps: at most 2048 / (32 kDecodeWarps) per SM, fewer if shared memory binds
+  const uint32_t per_sm = std::max<uint32_t>(
+      1, std::min<uint32_t>(2048 / (32 * kDecodeWarps), (uint32_t)(smem_sm[dev] / (*smem + 1024))));
   *grid = std::max<uint32_t>(1, std::min<uint32_t>(p.n_item, per_sm * (uint32_t)sms[dev]));
   return CRNGPU_OK;
 }
@@ -793,7 +816,8 @@ int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStre
   const ExpandJob* ej = reinterpret_cast<const ExpandJob*>(d_jobs + p.expand_ofs);
   if (decode && p.n_item) {
     if ((e = cudaMemsetAsync(words, 0, 8, s)) != cudaSuccess) return cuda_check(e, "clear work counter");
-    k_crn_decode_textures<<<grid, 32, smem, s>>>(tj, p.n_item, sj, words, p.lut_words, p.rb_words, words + 1);
+    k_crn_decode_textures<<<grid, kDecodeWarps * 32, smem, s>>>(tj, p.n_item, sj, words, p.lut_words, p.rb_words,
+                                                             words + 1);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_decode_textures");
   }
   if (p.ctas) {
