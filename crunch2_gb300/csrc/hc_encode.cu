@@ -1327,11 +1327,17 @@ unsigned max_vq_cluster(K kernel) {
   return nclusters >= 1 ? 16u : 8u;
 }
 
+// Device scratch of the tree clusterizer (nodes, the two vector / weight buffers, the job list),
+// kept across calls by the caller's workspace.
+struct VqScratch {
+  DevBuf nodes, v[2], wt[2], jobs;
+};
+
 // Host driver of the batched tree clusterizer: returns the codebook (leaf centroids) on the device
 // as K x D floats in `codebook` and the leaf count in *k_out.
 template <int D>
 int tree_vq(const float* d_vec, const uint32_t* d_w, uint32_t n, uint32_t max_entries, uint32_t round_fraction,
-            DevBuf& codebook, uint32_t* k_out, cudaStream_t s) {
+            DevBuf& codebook, uint32_t* k_out, cudaStream_t s, VqScratch& scr) {
   using Node = VqNode<D>;
   *k_out = 0;
   if (!n) return CRNGPU_OK;
@@ -1341,7 +1347,10 @@ int tree_vq(const float* d_vec, const uint32_t* d_w, uint32_t n, uint32_t max_en
   const size_t max_nodes = 6 * (size_t)max_entries + 8;
   static const unsigned max_split_cluster = max_vq_cluster(k_vq_split<D>);
   static const unsigned max_root_cluster = max_vq_cluster(k_vq_root<D>);
-  DevBuf d_nodes, d_v[2], d_wt[2], d_jobs;
+  DevBuf& d_nodes = scr.nodes;
+  DevBuf* d_v = scr.v;
+  DevBuf* d_wt = scr.wt;
+  DevBuf& d_jobs = scr.jobs;
   cudaError_t e;
   if ((e = d_nodes.ensure(sizeof(Node) * max_nodes)) != cudaSuccess) return cuda_check(e, "alloc vq nodes");
   for (int b = 0; b < 2; b++) {
@@ -2567,7 +2576,26 @@ struct HcBuffers {
       cstart, clist, clusters, bweight, block_cluster, selvec, selw, cb16, cbsel, block_sel, entry_err, entry_used,
       levels, flags, iota, used, keys, keys2, cub_tmp, sse, avec, aw, aitems, tile_ac, cb2, acount, alist, astart,
       aclusters, aitem_cluster, aselvec, aselw, acb16, acbsel, aitem_sel, aentry_err;
+  hc::VqScratch vq;
+  bool clean = true;  // the last call ended with its stream synchronised
 };
+
+// The clustered encoder's device buffers, one set per host thread and device, kept between calls
+// (they only grow): a call then allocates nothing once the texture sizes have been seen. Every
+// successful call ends by synchronising its stream, so the next call may reuse them on any stream;
+// after a failed call the device is synchronised first.
+HcBuffers& hc_workspace() {
+  static thread_local std::unique_ptr<HcBuffers> ws[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::unique_ptr<HcBuffers>& w = ws[dev & 63];
+  if (!w) w.reset(new HcBuffers);
+  if (!w->clean) {
+    cudaDeviceSynchronize();
+    w->clean = true;
+  }
+  return *w;
+}
 
 }  // namespace
 
@@ -2585,7 +2613,8 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
                      crngpu_hc_stats* stats, cudaStream_t s) {
   const uint32_t N = P.num_blocks;
   cudaError_t e;
-  HcBuffers B;
+  HcBuffers& B = hc_workspace();
+  B.clean = false;
   TileCfg cfg{};
   uint32_t bpb = 8, color_ofs = 0;
   int alpha_slot0 = 0;
@@ -2700,7 +2729,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
     k_tile_vectors<<<(nused + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused,
                                                         static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr));
     if ((rc = tree_vq<6>(static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr), nused,
-                         std::min(nused, P.color_endpoint_codebook_size), frac, B.cb6, &K, s)) != CRNGPU_OK)
+                         std::min(nused, P.color_endpoint_codebook_size), frac, B.cb6, &K, s, B.vq)) != CRNGPU_OK)
       return rc;
     if ((e = B.tile_cluster.ensure(4 * ntiles)) != cudaSuccess) return cuda_check(e, "alloc tile clusters");
     k_nearest_vec6<<<(ntiles + 255) / 256, 256, 0, s>>>(tiles, ntiles, static_cast<float*>(B.cb6.ptr), K,
@@ -2737,7 +2766,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
                                                        static_cast<unsigned long long*>(B.sse.ptr));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_block_selectors");
     if ((rc = tree_vq<16>(static_cast<float*>(B.selvec.ptr), static_cast<uint32_t*>(B.selw.ptr), N,
-                          std::min(N, P.color_selector_codebook_size), frac, B.cb16, &KS, s)) != CRNGPU_OK)
+                          std::min(N, P.color_selector_codebook_size), frac, B.cb16, &KS, s, B.vq)) != CRNGPU_OK)
       return rc;
     if ((e = B.cbsel.ensure(4 * KS)) != cudaSuccess || (e = B.block_sel.ensure(4 * N)) != cudaSuccess ||
         (e = B.entry_err.ensure(8 * 64 * (size_t)KS)) != cudaSuccess || (e = B.entry_used.ensure(4 * KS)) != cudaSuccess)
@@ -2785,7 +2814,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
                                                           static_cast<float*>(B.avec.ptr), static_cast<uint32_t*>(B.aw.ptr),
                                                           static_cast<uint32_t*>(B.aitems.ptr));
     if ((rc = tree_vq<2>(static_cast<float*>(B.avec.ptr), static_cast<uint32_t*>(B.aw.ptr), nitem_t,
-                         std::min(nused, P.alpha_endpoint_codebook_size), frac, B.cb2, &KA, s)) != CRNGPU_OK)
+                         std::min(nused, P.alpha_endpoint_codebook_size), frac, B.cb2, &KA, s, B.vq)) != CRNGPU_OK)
       return rc;
     k_nearest_vec2<<<(nitem_t + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused, cfg.num_alpha,
                                                           static_cast<float*>(B.cb2.ptr), KA, static_cast<uint32_t*>(B.tile_ac.ptr));
@@ -2817,7 +2846,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
         static_cast<float*>(B.aselvec.ptr), static_cast<uint32_t*>(B.aselw.ptr));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_alpha_block_selectors");
     if ((rc = tree_vq<16>(static_cast<float*>(B.aselvec.ptr), static_cast<uint32_t*>(B.aselw.ptr), nitem_b,
-                          std::min(nitem_b, P.alpha_selector_codebook_size), frac, B.acb16, &KAS, s)) != CRNGPU_OK)
+                          std::min(nitem_b, P.alpha_selector_codebook_size), frac, B.acb16, &KAS, s, B.vq)) != CRNGPU_OK)
       return rc;
     if ((e = B.acbsel.ensure(8 * KAS)) != cudaSuccess || (e = B.aitem_sel.ensure(4 * nitem_b)) != cudaSuccess ||
         (e = B.aentry_err.ensure(8 * 128 * (size_t)KAS)) != cudaSuccess)
@@ -2838,6 +2867,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
   unsigned long long sse[3] = {0, 0, 0};
   if ((e = cudaMemcpyAsync(sse, B.sse.ptr, 24, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read sse");
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
+  B.clean = true;
   if (stats) {
     stats->color_endpoints = K;
     stats->color_selectors = KS;
