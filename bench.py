@@ -13,6 +13,7 @@ One JSON line on stdout (rank 0):
              chains: colour / alpha / XY RMSE and bits per texel beside the reference's
   mixed_batch  512 textures of uneven sizes and mixed formats: batched plain encode (CUDA graph),
              their .crn through crn_compress, and the batched transcode of those files
+  mips       crunch's default mip generation (Kaiser, gamma filtering) of a 4096x4096 texture
   transcode  CRN -> DXT1 transcode GB/s: a batch of 1024 textures (each with its own context holding
              the reference-encoded .crn of the same texture, q128) in one persistent decode launch
              and one expansion launch (CUDA graph); the expansion kernel's HBM roofline; the
@@ -224,6 +225,21 @@ def mixed_batch_leg(cg, dev, stream, timed, steps: int, warmup: int) -> dict:
                           "path": "crngpu_unpack_batch (CUDA graph) over the 512 .crn files"}}
 
 
+def mips_leg(cg, dev, stream, timed, steps: int, warmup: int) -> dict:
+    import torch
+    from crunch2_gb300 import texgen
+    size = 4096
+    img = texgen.colour_texture_torch(size, size, 4096, device=dev, with_alpha_noise=True)
+    out_texels = sum(max(1, size >> l) ** 2 for l in range(1, 13))
+    for _ in range(warmup):
+        cg.generate_mipmaps(img, stream=stream)
+    ms = timed(lambda: cg.generate_mipmaps(img, stream=stream), steps)
+    return {"value": round(out_texels / (ms / 1e3) / 1e6, 1), "unit": "Mtexel/s (generated levels)",
+            "ms_per_chain": round(ms, 3), "levels": 13, "size": size,
+            "path": "crngpu_generate_mipmaps (Kaiser, blurriness 0.9, gamma 2.2, alpha), device buffers; "
+                    "bit-identical to crnlib's generate_mipmaps on the committed fixtures"}
+
+
 def cpu_threads() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -382,7 +398,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip", default="", help="comma-separated legs to leave out of the run (their keys are "
-                                               "null): clustered, clustered_2048, mixed")
+                                               "null): clustered, clustered_2048, mixed, mips")
     args = ap.parse_args()
     skip = set(x for x in args.skip.split(",") if x)
     args.warmup = max(args.warmup, 3)
@@ -595,6 +611,10 @@ def main():
     mixed_batch = None if "mixed" in skip else \
         mixed_batch_leg(cg, dev, stream, timed, steps=args.steps, warmup=args.warmup)
 
+    # ---- mip generation (crunch's defaults: Kaiser, blurriness 0.9, gamma filtering, alpha) of a
+    # 4096x4096 RGBA8 texture on the device: every level resampled from level 0
+    mips = None if "mips" in skip else mips_leg(cg, dev, stream, timed, steps=args.steps, warmup=args.warmup)
+
     peaks, peak_kind = measured_peaks()
     clk = clocks.summary()
     sm_max = clk.get("sm_max_mhz") or peaks.get("sm_max_mhz", 2070.0)
@@ -630,7 +650,7 @@ def main():
                 "e2e": {"value": round(e2e_value, 3), "unit": "Mtexel/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "path": "crngpu_compress_image per level, pinned host buffers"},
                 "learned": learned, "transcode": transcode, "clustered": clustered,
-                "clustered_2048": clustered_2048, "mixed_batch": mixed_batch, "roofline": roofline,
+                "clustered_2048": clustered_2048, "mixed_batch": mixed_batch, "mips": mips, "roofline": roofline,
                 "cpu_baseline": cpu,
                 "gpu_launches": args.steps * 1, "clocks": clk, "wall_s_timed": round(wall, 4)}
         print(json.dumps(line))

@@ -122,6 +122,8 @@ def lib():
     L.crngpu_encode_batch_size.restype = i64
     L.crngpu_encode_batch_destroy.argtypes = [vp]
     L.crngpu_encode_batch_destroy.restype = i32
+    L.crngpu_generate_mipmaps.argtypes = [vp, u32, u32, u32, u32, ctypes.c_float, u32, vp, u64, i32, vp]
+    L.crngpu_generate_mipmaps.restype = i64
     L.crngpu_profile_counters.argtypes = [i32, ctypes.POINTER(ctypes.c_uint64), vp]
     L.crngpu_profile_counters.restype = i32
     _lib = L
@@ -245,6 +247,35 @@ def compress_image(rgba, fmt: int = FMT_DXT1, flags: int = FLAG_PERCEPTUAL | FLA
     _check(lib().crngpu_compress_image(ip, w, h, 0, fmt, flags, _ptr_mem(out)[0], n * bytes_per_block(fmt), mem,
                                        _stream_ptr(stream)), "crngpu_compress_image")
     return out
+
+
+MIP_FILTERS = {"box": 0, "tent": 1, "lanczos4": 2, "mitchell": 3, "kaiser": 4}
+MIP_SRGB, MIP_WRAP, MIP_ALPHA = 1, 2, 4
+
+
+def generate_mipmaps(rgba, filt: str = "kaiser", filter_scale: float = 0.9, srgb: bool = True, wrap: bool = False,
+                     alpha: bool = True, levels: int = 0, stream=None):
+    """crnlib's mip generation on the GPU (crngpu_generate_mipmaps): (h, w, 4) RGBA8 level 0, numpy
+    or torch (CUDA tensors stay on the device) -> the list of levels, level 0 first. Defaults are
+    crunch's: Kaiser filter, blurriness 0.9, gamma filtering."""
+    rgba = _contiguous(rgba)
+    h, w = int(rgba.shape[0]), int(rgba.shape[1])
+    full = 1
+    while (w >> full) or (h >> full):
+        full += 1
+    n = levels or full
+    dims = [(max(1, h >> l), max(1, w >> l)) for l in range(n)]
+    need = sum(a * b * 4 for a, b in dims)
+    out = _out_like(rgba, (need,))
+    ip, mem = _ptr_mem(rgba)
+    flags = (MIP_SRGB if srgb else 0) | (MIP_WRAP if wrap else 0) | (MIP_ALPHA if alpha else 0)
+    _check(int(lib().crngpu_generate_mipmaps(ip, w, h, n, MIP_FILTERS[filt], filter_scale, flags, _ptr_mem(out)[0],
+                                              need, mem, _stream_ptr(stream))), "crngpu_generate_mipmaps")
+    res, ofs = [], 0
+    for a, b in dims:
+        res.append(out[ofs:ofs + a * b * 4].reshape(a, b, 4))
+        ofs += a * b * 4
+    return res
 
 
 def mip_chain_blocks(width: int, height: int, levels: int) -> int:

@@ -31,6 +31,7 @@ UNITS = [
     ("dxt_encode.cu", ["--fmad=false"]),
     ("mlp.cu", []),
     ("hc_encode.cu", ["--fmad=false"]),
+    ("mip_gen.cu", ["--fmad=false"]),
 ]
 
 

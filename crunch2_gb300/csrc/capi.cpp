@@ -57,8 +57,8 @@ void DevBuf::release() {
 // Staging buffers for host-memory calls; one set per host thread so concurrent callers on
 // different threads never share them.
 DevBuf& staging(int slot) {
-  thread_local DevBuf bufs[4];
-  return bufs[slot & 3];
+  thread_local DevBuf bufs[8];
+  return bufs[slot & 7];
 }
 
 }  // namespace crngpu

@@ -27,7 +27,8 @@ struct DevBuf {
   ~DevBuf() { release(); }
 };
 
-// Per-device scratch for host-memory calls (input/output staging).
+// Per-thread scratch for host-memory calls (input/output staging), slots 0..7: 0-3 the encoders,
+// 4-6 mip generation.
 DevBuf& staging(int slot);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }

@@ -339,6 +339,28 @@ CRNGPU_API int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch);
 
 CRNGPU_API int crngpu_unpack_batch_destroy(crngpu_unpack_batch batch);
 
+/* Mip generation (mipmapped_texture::generate_mipmaps, crnlib/crn_mipmapped_texture.cpp:2140-2215,
+ * with the resampler of image_utils::resample_multithreaded, crnlib/crn_image_utils.cpp:662-874):
+ * level 0 (width x height RGBA8, tightly packed) is copied, and every further level l is resampled
+ * from level 0 to max(1, width >> l) x max(1, height >> l). filter: the crn_mip_filter order
+ * (CRNGPU_MIP_FILTER_BOX .. _KAISER; crunch's default is Kaiser); filter_scale: the mip
+ * "blurriness" (crunch's default 0.9); flags: CRNGPU_MIP_SRGB filters R, G, B in linear light with
+ * gamma 2.2 (crunch's default), CRNGPU_MIP_WRAP wraps at the edges instead of clamping (tiled
+ * textures), CRNGPU_MIP_ALPHA filters alpha too (else alpha is 255, as for an image without an
+ * alpha channel). levels: 0 = the full chain. out receives the levels back to back. Host or
+ * device buffers (mem). Returns the bytes written or an error. */
+#define CRNGPU_MIP_FILTER_BOX 0u
+#define CRNGPU_MIP_FILTER_TENT 1u
+#define CRNGPU_MIP_FILTER_LANCZOS4 2u
+#define CRNGPU_MIP_FILTER_MITCHELL 3u
+#define CRNGPU_MIP_FILTER_KAISER 4u
+#define CRNGPU_MIP_SRGB 1u
+#define CRNGPU_MIP_WRAP 2u
+#define CRNGPU_MIP_ALPHA 4u
+CRNGPU_API int64_t crngpu_generate_mipmaps(const uint8_t* rgba, uint32_t width, uint32_t height, uint32_t levels,
+                                           uint32_t filter, float filter_scale, uint32_t flags, uint8_t* out,
+                                           uint64_t out_size, int mem, void* stream);
+
 /* Batched plain encode (no single counterpart in the reference, whose dxt_image::init encodes one
  * image at a time, crnlib/crn_dxt_image.cpp:447-493): the mip chains of many textures of any mix
  * of sizes and formats (DXT1, the DXT5 family, DXN_XY/YX, DXT5A) in one gather launch and two

@@ -43,6 +43,9 @@ def lib():
         L.ref_dxt_hc_alpha.argtypes = [ctypes.c_void_p, _u32, _u32, ctypes.c_void_p, _u32, _u32, ctypes.c_void_p,
                                        ctypes.c_int, _u32, ctypes.c_void_p, ctypes.c_void_p]
         L.ref_dxt_hc_alpha.restype = ctypes.c_int
+        L.ref_resample.argtypes = [ctypes.c_void_p, _u32, _u32, _u32, _u32, ctypes.c_char_p, ctypes.c_float,
+                                   ctypes.c_int, ctypes.c_int, _u32, ctypes.c_void_p]
+        L.ref_resample.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -121,3 +124,27 @@ def dxt_hc_alpha(blocks: np.ndarray, levels, faces: int, fmt: str, codebooks, pe
     return out[: n * bpb].reshape(n, bpb), {"tiles": int(stats[0]), "color_endpoints": int(stats[1]),
                                             "color_selectors": int(stats[2]), "alpha_endpoints": int(stats[3]),
                                             "alpha_selectors": int(stats[4])}
+
+
+def resample(rgba: np.ndarray, dst_w: int, dst_h: int, filt: str, filter_scale: float, srgb: bool, wrap: bool,
+             num_comps: int) -> np.ndarray:
+    """The reference's image_utils::resample_multithreaded: (h, w, 4) uint8 -> (dst_h, dst_w, 4)."""
+    src = np.ascontiguousarray(rgba, dtype=np.uint8)
+    out = np.zeros((dst_h, dst_w, 4), np.uint8)
+    ok = lib().ref_resample(src.ctypes.data, src.shape[1], src.shape[0], dst_w, dst_h, filt.encode(), filter_scale,
+                            int(srgb), int(wrap), num_comps, out.ctypes.data)
+    if not ok:
+        raise RuntimeError("reference resample failed")
+    return out
+
+
+def generate_mipmaps(rgba: np.ndarray, filt: str, filter_scale: float, srgb: bool, wrap: bool, num_comps: int):
+    """mipmapped_texture::generate_mipmaps (crnlib/crn_mipmapped_texture.cpp:2140-2215): every level
+    resampled from the level-0 image down to 1x1 (min mip size 1)."""
+    h, w = rgba.shape[:2]
+    levels = [np.ascontiguousarray(rgba)]
+    l = 1
+    while (w >> (l - 1)) > 1 or (h >> (l - 1)) > 1:
+        levels.append(resample(rgba, max(1, w >> l), max(1, h >> l), filt, filter_scale, srgb, wrap, num_comps))
+        l += 1
+    return levels

@@ -12,6 +12,7 @@
 //   crnd_unpack_begin / crnd_unpack_level / crnd_unpack_end   inc/crn_defs.h:174-205
 //   crnd_get_texture_info / crnd_get_level_info              inc/crn_defs.h:152-160
 //   crnlib::dxt_hc::compress (clustered DXT1)                 crnlib/crn_dxt_hc.cpp:97-316
+//   crnlib::image_utils::resample_multithreaded (mip levels)   crnlib/crn_image_utils.cpp:662-874
 #include <cstdint>
 #include <cstring>
 #include <cstdlib>
@@ -25,6 +26,8 @@
 #include "crn_dxt_hc.h"
 #include "crn_dxt_fast.h"
 #include "crn_threading.h"
+#include "crn_image.h"
+#include "crn_image_utils.h"
 
 namespace {
 
@@ -305,6 +308,30 @@ uint32_t ref_dxt_fast_tile_error(const uint8_t* rgba, uint32_t n) {
       err += d * d;
     }
   return err;
+}
+
+// crnlib::image_utils::resample_multithreaded (crnlib/crn_image_utils.cpp:662-874), the resampler
+// mipmapped_texture::generate_mipmaps (crnlib/crn_mipmapped_texture.cpp:2140-2215) runs for every
+// mip level from the level-0 image: the filter by name, filter scale (the mip "blurriness"), sRGB
+// gamma filtering, wrap or clamp addressing, 3 or 4 components. Returns 1 on success.
+int ref_resample(const uint8_t* rgba, uint32_t w, uint32_t h, uint32_t dst_w, uint32_t dst_h, const char* filter,
+                 float filter_scale, int srgb, int wrap, uint32_t num_comps, uint8_t* out) {
+  crnlib::image_u8 src(w, h);
+  for (uint32_t y = 0; y < h; y++) std::memcpy(src.get_scanline(y), rgba + (size_t)y * w * 4, (size_t)w * 4);
+  crnlib::image_u8 dst;
+  crnlib::image_utils::resample_params rp;
+  rp.m_dst_width = dst_w;
+  rp.m_dst_height = dst_h;
+  rp.m_pFilter = filter;
+  rp.m_filter_scale = filter_scale;
+  rp.m_srgb = srgb != 0;
+  rp.m_wrapping = wrap != 0;
+  rp.m_first_comp = 0;
+  rp.m_num_comps = num_comps;
+  rp.m_multithreaded = true;
+  if (!crnlib::image_utils::resample_multithreaded(src, dst, rp)) return 0;
+  for (uint32_t y = 0; y < dst_h; y++) std::memcpy(out + (size_t)y * dst_w * 4, dst.get_scanline(y), (size_t)dst_w * 4);
+  return 1;
 }
 
 }  // extern "C"

@@ -194,6 +194,34 @@ def make_hc() -> None:
         json.dump(out, fh, indent=1, sort_keys=True)
 
 
+# mip generation cases: (name, width, height, content, seed, filter, filter scale, sRGB, wrap, comps)
+MIP_CASES = [("kaiser_64x48_rgba", 64, 48, "colour_alpha", 40, "kaiser", 0.9, True, False, 4),
+             ("lanczos4_37x20_rgb", 37, 20, "colour", 41, "lanczos4", 1.0, True, False, 3),
+             ("box_32x32_linear", 32, 32, "colour_alpha", 42, "box", 1.0, False, False, 4),
+             ("tent_50x64_wrap", 50, 64, "colour_alpha", 43, "tent", 1.0, True, True, 4),
+             ("mitchell_16x40_linear_rgb", 16, 40, "colour", 44, "mitchell", 0.9, False, False, 3),
+             ("kaiser_1x64", 1, 64, "colour_alpha", 45, "kaiser", 0.9, True, False, 4),
+             ("kaiser_128x128_normal", 128, 128, "normal", 46, "kaiser", 0.9, False, True, 3)]
+
+
+def make_mips() -> None:
+    """The reference's mip generation (mipmapped_texture::generate_mipmaps with its resampler) on
+    small seeded images: every level for each of the five mip filters, gamma on and off, clamp and
+    wrap addressing, 3 and 4 components, a 1-texel-wide image."""
+    arrays, meta = {}, {}
+    for name, w, h, content, seed, filt, scale, srgb, wrap, comps in MIP_CASES:
+        img = texgen.normal_map(w, h, seed) if content == "normal" else \
+            texgen.colour_texture(w, h, seed, with_alpha_noise=(content == "colour_alpha"))
+        levels = ref.generate_mipmaps(img, filt, scale, srgb, wrap, comps)
+        arrays[name + "_base"] = img
+        arrays[name + "_levels"] = np.concatenate([l.reshape(-1) for l in levels[1:]])
+        meta[name] = {"width": w, "height": h, "filter": filt, "filter_scale": scale, "srgb": srgb, "wrap": wrap,
+                      "comps": comps, "levels": len(levels)}
+    np.savez_compressed(os.path.join(HERE, "mips.npz"), **arrays)
+    with open(os.path.join(HERE, "mips.json"), "w") as fh:
+        json.dump(meta, fh, indent=1, sort_keys=True)
+
+
 # 2048x2048 DXT5 (colour + alpha noise) and DXN_XY (normal map) mip chains at quality 128
 CONFIG2_CASES = [("dxt5_2048", "DXT5", 2, 2048, 200, "colour_alpha"), ("dxn_xy_2048", "DXN_XY", 7, 2048, 201, "normal")]
 
@@ -246,8 +274,12 @@ if __name__ == "__main__":
     if sys.argv[1:] == ["config2"]:
         make_config2()
         sys.exit(0)
+    if sys.argv[1:] == ["mips"]:
+        make_mips()
+        sys.exit(0)
     make_blocks()
     make_crn()
     make_hc()
     make_config2()
+    make_mips()
     print("golden fixtures written to", HERE)
