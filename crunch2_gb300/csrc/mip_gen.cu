@@ -21,6 +21,10 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "crngpu_internal.h"
@@ -252,6 +256,34 @@ __global__ void k_mip_resample_y(const float4* __restrict__ tmp, uint32_t dst_w,
   }
 }
 
+// Contributor lists and gamma tables depend only on their parameters: computed once per process.
+const Contribs* cached_contribs(int src, int dst, uint32_t filter, float filter_scale, bool wrap) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, uint32_t, float, bool>, std::unique_ptr<Contribs>> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_tuple(src, dst, filter, filter_scale, wrap);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second.get();
+  std::unique_ptr<Contribs> c(new Contribs);
+  if (!make_contribs(src, dst, kFilters[filter], filter_scale, wrap, *c)) return nullptr;
+  return (cache[key] = std::move(c)).get();
+}
+
+struct GammaTables {
+  float to_linear[256];
+  uint8_t to_srgb[8192];
+  GammaTables() {
+    // resample_multithreaded's tables with the source gamma generate_mipmaps leaves at 2.2
+    const float gamma = 2.2f;
+    for (int i = 0; i < 256; ++i) to_linear[i] = (float)std::pow(i * 1.0f / 255.0f, gamma);
+    const float inv_size = 1.0f / 8192, inv_gamma = 1.0f / gamma;
+    for (int i = 0; i < 8192; ++i) {
+      const int k = (int)(255.0f * std::pow(i * inv_size, inv_gamma) + .5f);
+      to_srgb[i] = (uint8_t)(k < 0 ? 0 : k > 255 ? 255 : k);
+    }
+  }
+};
+
 unsigned grid_for(uint64_t work) {
   const uint64_t g = (work + 255) / 256;
   return (unsigned)(g < 65535ull * 16 ? (g ? g : 1) : 65535ull * 16);
@@ -282,18 +314,9 @@ extern "C" int64_t crngpu_generate_mipmaps(const uint8_t* rgba, uint32_t width, 
   const bool srgb = (flags & CRNGPU_MIP_SRGB) != 0, wrap = (flags & CRNGPU_MIP_WRAP) != 0,
              alpha = (flags & CRNGPU_MIP_ALPHA) != 0;
   cudaStream_t s = as_stream(stream);
-  // gamma tables (resample_multithreaded): source gamma 2.2 as generate_mipmaps leaves it
-  const float gamma = 2.2f;
-  float to_linear[256];
-  for (int i = 0; i < 256; ++i) to_linear[i] = (float)std::pow(i * 1.0f / 255.0f, gamma);
-  uint8_t to_srgb[8192];
-  {
-    const float inv_size = 1.0f / 8192, inv_gamma = 1.0f / gamma;
-    for (int i = 0; i < 8192; ++i) {
-      int k = (int)(255.0f * std::pow(i * inv_size, inv_gamma) + .5f);
-      to_srgb[i] = (uint8_t)(k < 0 ? 0 : k > 255 ? 255 : k);
-    }
-  }
+  static const GammaTables gt;
+  const float* to_linear = gt.to_linear;
+  const uint8_t* to_srgb = gt.to_srgb;
   // contributor lists of every level, both axes, in one upload
   struct Axis { uint32_t ofs_first, ofs_pix, count; };
   std::vector<uint32_t> firsts, ns, pixels;
@@ -303,11 +326,12 @@ extern "C" int64_t crngpu_generate_mipmaps(const uint8_t* rgba, uint32_t width, 
     for (int a = 0; a < 2; a++) {
       const int src = a ? (int)height : (int)width;
       const int dst = std::max(1, src >> l);
-      Contribs c;
-      if (!make_contribs(src, dst, kFilters[filter], filter_scale, wrap, c)) {
+      const Contribs* cp = cached_contribs(src, dst, filter, filter_scale, wrap);
+      if (!cp) {
         set_error("crngpu_generate_mipmaps: filter has no contributors");
         return CRNGPU_E_PARAM;
       }
+      const Contribs& c = *cp;
       Axis& A = ax[2 * l + a];
       A.ofs_first = (uint32_t)firsts.size();
       A.ofs_pix = (uint32_t)pixels.size();
@@ -329,8 +353,8 @@ extern "C" int64_t crngpu_generate_mipmaps(const uint8_t* rgba, uint32_t width, 
   std::vector<uint8_t> host(tab_bytes, 0);
   size_t o = 0;
   auto put = [&](const void* p, size_t bytes) { std::memcpy(host.data() + o, p, bytes); o += (bytes + 15) & ~(size_t)15; };
-  const size_t o_lin = o; put(to_linear, sizeof(to_linear));
-  const size_t o_srgb = o; put(to_srgb, sizeof(to_srgb));
+  const size_t o_lin = o; put(to_linear, sizeof(gt.to_linear));
+  const size_t o_srgb = o; put(to_srgb, sizeof(gt.to_srgb));
   const size_t o_first = o; put(firsts.data(), firsts.size() * 4);
   const size_t o_n = o; put(ns.data(), ns.size() * 4);
   const size_t o_pix = o; put(pixels.data(), pixels.size() * 4);
