@@ -54,6 +54,13 @@ class _BatchItem(ctypes.Structure):
                 ("dst", ctypes.c_void_p), ("dst_size", ctypes.c_uint64)]
 
 
+class _CrnBatchItem(ctypes.Structure):
+    _fields_ = [("rgba_levels", ctypes.c_void_p), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("levels", ctypes.c_uint32), ("faces", ctypes.c_uint32), ("format", ctypes.c_uint32),
+                ("quality_level", ctypes.c_uint32), ("flags", ctypes.c_uint32), ("out", ctypes.c_void_p),
+                ("out_capacity", ctypes.c_uint64), ("result", ctypes.c_int64)]
+
+
 class _EncodeItem(ctypes.Structure):
     _fields_ = [("rgba", ctypes.c_void_p), ("out", ctypes.c_void_p), ("width", ctypes.c_uint32),
                 ("height", ctypes.c_uint32), ("levels", ctypes.c_uint32), ("format", ctypes.c_uint32)]
@@ -107,6 +114,8 @@ def lib():
     L.crngpu_crn_decompress.restype = None
     L.crngpu_compress_crn.argtypes = [vp, u32, u32, u32, u32, u32, u32, u32, vp, u64]
     L.crngpu_compress_crn.restype = i64
+    L.crngpu_compress_crn_batch.argtypes = [ctypes.POINTER(_CrnBatchItem), u32, u32]
+    L.crngpu_compress_crn_batch.restype = i32
     L.crngpu_compress_crn_bitrate.argtypes = [vp, u32, u32, u32, u32, u32, ctypes.c_float, u32, vp, u64,
                                               ctypes.POINTER(u32), ctypes.POINTER(ctypes.c_float)]
     L.crngpu_compress_crn_bitrate.restype = i64
@@ -500,6 +509,35 @@ def compress_crn_bitrate(faces_levels, target_bitrate: float, fmt: int = FMT_DXT
         raise CrnGpuError(E_PARAM, "crngpu_compress_crn_bitrate: output larger than expected")
     out = out[:size]
     return out.tobytes(), int(q.value), float(br.value)
+
+
+def compress_crn_batch(items, threads: int = 4):
+    """Many compress_crn calls at once (crngpu_compress_crn_batch): items are (faces_levels, fmt,
+    quality, flags); returns the .crn bytes of each, in order."""
+    arr = (_CrnBatchItem * len(items))()
+    keep = []
+    for i, (faces_levels, fmt, quality, flags) in enumerate(items):
+        h, w = faces_levels[0][0].shape[:2]
+        flat = np.concatenate([np.ascontiguousarray(im, dtype=np.uint8).reshape(-1) for face in faces_levels
+                               for im in face])
+        bpb = 8 if fmt in (FMT_DXT1, FMT_DXT5A) else 16
+        cap = sum(((max(1, w >> l) + 7) // 8 * 2) * ((max(1, h >> l) + 7) // 8 * 2) * bpb
+                  for l in range(len(faces_levels[0]))) * len(faces_levels) + (1 << 20)
+        out = np.zeros(cap, np.uint8)
+        keep.append((flat, out))
+        arr[i] = _CrnBatchItem(flat.ctypes.data, w, h, len(faces_levels[0]), len(faces_levels), fmt, quality, flags,
+                               out.ctypes.data, cap, 0)
+    rc = int(lib().crngpu_compress_crn_batch(arr, len(items), threads))
+    res = []
+    for i, (flat, out) in enumerate(keep):
+        r = int(arr[i].result)
+        if r < 0:
+            raise CrnGpuError(r, f"crngpu_compress_crn_batch item {i}: " + last_error())
+        if r > out.size:
+            raise CrnGpuError(E_PARAM, "crngpu_compress_crn_batch: output larger than expected")
+        res.append(out[:r].tobytes())
+    _check(rc, "crngpu_compress_crn_batch")
+    return res
 
 
 def compress_crn(faces_levels, fmt: int = FMT_DXT1, quality: int = 128, flags: int = FLAG_PERCEPTUAL) -> bytes:

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 #include <cstring>
 
 #include "crngpu_internal.h"
@@ -1427,23 +1428,24 @@ struct DeviceInit {
 };
 
 SingleColour* single_colour_host_tables() {
-  static SingleColour* host = nullptr;
-  if (!host) {
-    host = new SingleColour;
-    build_single_colour(*host);
-  }
+  static SingleColour* host = [] {  // initialised once, thread-safely
+    SingleColour* t = new SingleColour;
+    build_single_colour(*t);
+    return t;
+  }();
   return host;
 }
 
 int ensure_tables() {
   static DeviceInit init;
-  static SingleColour* host = nullptr;
+  static std::mutex mu;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
+  std::lock_guard<std::mutex> lock(mu);
   if (dev < 64 && init.done[dev]) return CRNGPU_OK;
-  if (!host) host = single_colour_host_tables();
-  if ((e = cudaMemcpyToSymbol(c_sct, host, sizeof(SingleColour))) != cudaSuccess) return cuda_check(e, "upload tables");
+  if ((e = cudaMemcpyToSymbol(c_sct, single_colour_host_tables(), sizeof(SingleColour))) != cudaSuccess)
+    return cuda_check(e, "upload tables");
   if (dev < 64) init.done[dev] = true;
   return CRNGPU_OK;
 }

@@ -35,6 +35,8 @@
 #include <cstring>
 #include <memory>
 #include <vector>
+#include <atomic>
+#include <thread>
 
 #include <cooperative_groups.h>
 #include <cub/device/device_radix_sort.cuh>
@@ -2948,11 +2950,25 @@ namespace {
 // layout (crn_comp::alias_images / quantize_images, crnlib/crn_comp.cpp:454-463, 717-741),
 // gathered on the host with edge clamping and uploaded once; a pass per quality level then runs
 // the clustered encode and the writer.
+// per host thread: the gathered blocks and the encoded blocks on the device, kept between calls
+struct CrnDeviceBuffers {
+  DevBuf in, out;
+};
+CrnDeviceBuffers& crn_buffers() {
+  static thread_local std::unique_ptr<CrnDeviceBuffers> b[64];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!b[dev & 63]) b[dev & 63].reset(new CrnDeviceBuffers);
+  return *b[dev & 63];
+}
+
 struct CrnSource {
   crngpu_hc_params P;
   uint32_t width = 0, height = 0, levels = 0, faces = 0, format = 0, bpb = 0;
   uint64_t texels = 0;
-  DevBuf d_in, d_out;
+  cudaStream_t stream = nullptr;
+  DevBuf& d_in = crn_buffers().in;
+  DevBuf& d_out = crn_buffers().out;
 
   int prepare(const uint8_t* rgba_levels, uint32_t w, uint32_t h, uint32_t nl, uint32_t nf, uint32_t fmt,
               uint32_t flags, const char* who) {
@@ -3008,8 +3024,9 @@ struct CrnSource {
     cudaError_t e;
     if ((e = d_in.ensure(blocks.size() * 4)) != cudaSuccess || (e = d_out.ensure((size_t)P.num_blocks * bpb)) != cudaSuccess)
       return cuda_check(e, "alloc blocks");
-    if ((e = cudaMemcpy(d_in.ptr, blocks.data(), blocks.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+    if ((e = cudaMemcpyAsync(d_in.ptr, blocks.data(), blocks.size() * 4, cudaMemcpyHostToDevice, stream)) != cudaSuccess)
       return cuda_check(e, "copy blocks");
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_check(e, "sync");  // `blocks` is freed next
     return CRNGPU_OK;
   }
 
@@ -3022,12 +3039,13 @@ struct CrnSource {
     P.alpha_endpoint_codebook_size = sizes[2];
     P.alpha_selector_codebook_size = sizes[3];
     int rc = crngpu_hc_compress(static_cast<const uint8_t*>(d_in.ptr), &P, format, static_cast<uint8_t*>(d_out.ptr),
-                                nullptr, nullptr);
+                                nullptr, stream);
     if (rc != CRNGPU_OK) return rc;
     std::vector<uint8_t> dxt((size_t)P.num_blocks * bpb);
     cudaError_t e;
-    if ((e = cudaMemcpy(dxt.data(), d_out.ptr, dxt.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    if ((e = cudaMemcpyAsync(dxt.data(), d_out.ptr, dxt.size(), cudaMemcpyDeviceToHost, stream)) != cudaSuccess)
       return cuda_check(e, "copy result");
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_check(e, "sync");
     // a .crn is smaller than its DXT blocks plus palettes (8192 entries of at most 8 bytes each,
     // twice) and the models; grow once if not
     file.resize(dxt.size() + (1u << 18));
@@ -3062,6 +3080,43 @@ extern "C" int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t widt
   std::vector<uint8_t> file;
   if ((rc = src.pass(quality_level, file)) != CRNGPU_OK) return rc;
   return deliver(file, out, out_capacity);
+}
+
+extern "C" int crngpu_compress_crn_batch(crngpu_crn_batch_item* items, uint32_t n, uint32_t threads) {
+  using namespace crngpu;
+  clear_error();
+  if (!items && n) { set_error("crngpu_compress_crn_batch: no items"); return CRNGPU_E_PARAM; }
+  if (!n) return CRNGPU_OK;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  threads = std::max(1u, std::min(threads ? threads : 4u, std::min(n, 32u)));
+  std::atomic<uint32_t> next{0};
+  std::atomic<int> failed{0};
+  auto worker = [&]() {
+    cudaSetDevice(dev);
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) { failed = 1; return; }
+    std::vector<uint8_t> file;
+    for (uint32_t i = next++; i < n; i = next++) {
+      crngpu_crn_batch_item& it = items[i];
+      CrnSource src;
+      src.stream = s;
+      int rc = it.quality_level > 255 ? (int)CRNGPU_E_PARAM
+                                      : src.prepare(it.rgba_levels, it.width, it.height, it.levels, it.faces,
+                                                    it.format, it.flags, "crngpu_compress_crn_batch");
+      if (rc == CRNGPU_OK) rc = src.pass(it.quality_level, file);
+      it.result = rc == CRNGPU_OK ? deliver(file, it.out, it.out_capacity) : (int64_t)rc;
+      if (rc != CRNGPU_OK) failed = 1;
+    }
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  };
+  std::vector<std::thread> pool;
+  for (uint32_t t = 1; t < threads; t++) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
+  if (failed) set_error("crngpu_compress_crn_batch: some items failed (see their result)");
+  return failed ? CRNGPU_E_PARAM : CRNGPU_OK;
 }
 
 extern "C" int64_t crngpu_compress_crn_bitrate(const uint8_t* rgba_levels, uint32_t width, uint32_t height,

@@ -189,6 +189,21 @@ CRNGPU_API int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t widt
                                        uint32_t faces, uint32_t format, uint32_t quality_level, uint32_t flags,
                                        void* out, uint64_t out_capacity);
 
+/* Many crn_compress calls at once (no counterpart in the reference, which compresses one texture
+ * per call): `threads` host threads (0 = 4), each with its own CUDA stream and device buffers, take
+ * items in turn, so one texture's host work (block gather, .crn writer) overlaps other textures'
+ * GPU work. Each item is exactly crngpu_compress_crn's call; its `result` gets the file size (the
+ * file is copied to `out` when out_capacity suffices) or an error code. Returns CRNGPU_OK when every
+ * item succeeded. */
+typedef struct crngpu_crn_batch_item {
+    const uint8_t* rgba_levels;
+    uint32_t width, height, levels, faces, format, quality_level, flags;
+    void* out;
+    uint64_t out_capacity;
+    int64_t result;
+} crngpu_crn_batch_item;
+CRNGPU_API int crngpu_compress_crn_batch(crngpu_crn_batch_item* items, uint32_t n, uint32_t threads);
+
 /* crn_compress with a target bitrate instead of a quality level (crn_comp_params::m_target_bitrate,
  * inc/crnlib.h:254; the search of create_compressed_texture, crnlib/crn_texture_comp.cpp:120-245):
  * the reference's interpolative search over quality levels 0..255, each trial a full clustered

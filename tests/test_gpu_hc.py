@@ -213,3 +213,20 @@ def test_compress_crn_bitrate_search(hc):
             above = len(cg.compress_crn([levels], cg.FMT_DXT1, quality=q + 1)) * 8 / texels
             assert above > target or abs(above - target) < abs(rate - target) + 0.05
     print(f"target {target}: quality {q}, {rate:.4f} bpp (quality 0: {lowest:.4f})")
+
+
+def test_compress_crn_batch_equals_single_calls(hc):
+    """crngpu_compress_crn_batch (several host threads, one stream each) writes, for every item,
+    exactly the file crngpu_compress_crn writes for it alone."""
+    import crunch2_gb300 as cg
+    from crunch2_gb300 import texgen
+    items = []
+    for i, (w, h, fmt, content) in enumerate([(64, 64, cg.FMT_DXT1, "colour"), (128, 32, cg.FMT_DXT5, "colour_alpha"),
+                                              (48, 80, cg.FMT_DXN_XY, "normal"), (256, 256, cg.FMT_DXT1, "colour"),
+                                              (16, 16, cg.FMT_DXT5A, "colour_alpha"), (100, 60, cg.FMT_DXT1, "colour")]):
+        img = texgen.normal_map(w, h, 70 + i) if content == "normal" else \
+            texgen.colour_texture(w, h, 70 + i, with_alpha_noise=content == "colour_alpha")
+        items.append(([texgen.mip_chain(img)], fmt, 100 + 20 * i, 0 if content == "normal" else cg.FLAG_PERCEPTUAL))
+    batch = cg.compress_crn_batch(items, threads=3)
+    for it, got in zip(items, batch):
+        assert got == cg.compress_crn(*it)
