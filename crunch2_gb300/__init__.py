@@ -114,6 +114,8 @@ def lib():
     L.crngpu_crn_decompress.restype = None
     L.crngpu_compress_crn.argtypes = [vp, u32, u32, u32, u32, u32, u32, u32, vp, u64]
     L.crngpu_compress_crn.restype = i64
+    L.crngpu_compress_dds_clustered.argtypes = [vp, u32, u32, u32, u32, u32, u32, u32, vp, u64]
+    L.crngpu_compress_dds_clustered.restype = i64
     L.crngpu_compress_crn_batch.argtypes = [ctypes.POINTER(_CrnBatchItem), u32, u32]
     L.crngpu_compress_crn_batch.restype = i32
     L.crngpu_compress_crn_bitrate.argtypes = [vp, u32, u32, u32, u32, u32, ctypes.c_float, u32, vp, u64,
@@ -509,6 +511,20 @@ def compress_crn_bitrate(faces_levels, target_bitrate: float, fmt: int = FMT_DXT
         raise CrnGpuError(E_PARAM, "crngpu_compress_crn_bitrate: output larger than expected")
     out = out[:size]
     return out.tobytes(), int(q.value), float(br.value)
+
+
+def compress_dds_clustered(faces_levels, quality: int = 128, flags: int = FLAG_PERCEPTUAL, fmt: int = FMT_DXT1):
+    """Clustered DDS (the reference's QDXT path, crngpu_compress_dds_clustered): the DXT1 blocks of
+    every face's mip chain, per level its visible blocks (numpy (n, 8))."""
+    h, w = faces_levels[0][0].shape[:2]
+    flat = np.concatenate([np.ascontiguousarray(im, dtype=np.uint8).reshape(-1) for face in faces_levels for im in face])
+    L = lib()
+    args = (flat.ctypes.data, w, h, len(faces_levels[0]), len(faces_levels), fmt, quality, flags)
+    need = len(faces_levels) * sum(((max(1, w >> l) + 3) // 4) * ((max(1, h >> l) + 3) // 4) * 8
+                                   for l in range(len(faces_levels[0])))
+    out = np.zeros(need, np.uint8)
+    _check(int(L.crngpu_compress_dds_clustered(*args, out.ctypes.data, need)), "crngpu_compress_dds_clustered")
+    return out.reshape(-1, 8)
 
 
 def compress_crn_batch(items, threads: int = 4):

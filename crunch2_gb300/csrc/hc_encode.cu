@@ -208,9 +208,8 @@ __host__ __device__ bool fast_refine(int n, const uint32_t* px, uint32_t& max16,
 
 // compress_color_block (:725-764, refine = false) and the squared RGB error of the result against
 // get_block_colors4 (crn_dxt_hc.cpp:459-472)
-__host__ __device__ uint32_t fast_tile_error(int n, const uint32_t* px, const SolidTables* __restrict__ st) {
-  uint8_t sel[64];
-  uint32_t lo16, hi16;
+__host__ __device__ void fast_compress(int n, const uint32_t* px, const SolidTables* __restrict__ st, uint32_t& lo16,
+                                       uint32_t& hi16, uint8_t* sel) {
   int ave[3];
   bool solid = false;
   if (!fast_optimize(n, px, lo16, hi16, ave)) {
@@ -244,6 +243,12 @@ __host__ __device__ uint32_t fast_tile_error(int n, const uint32_t* px, const So
     const uint32_t t = lo16; lo16 = hi16; hi16 = t;
     for (int i = 0; i < n; i++) sel[i] ^= 1;
   }
+}
+
+__host__ __device__ uint32_t fast_tile_error(int n, const uint32_t* px, const SolidTables* __restrict__ st) {
+  uint8_t sel[64];
+  uint32_t lo16, hi16;
+  fast_compress(n, px, st, lo16, hi16, sel);
   int col[4][3];
   colors4(lo16, hi16, col);
   uint32_t err = 0;
@@ -253,6 +258,60 @@ __host__ __device__ uint32_t fast_tile_error(int n, const uint32_t* px, const So
     err += (uint32_t)(dr * dr + dg * dg + db * db);
   }
   return err;
+}
+
+// dxt_fast::find_representative_colors (crnlib/crn_dxt_fast.cpp:855-994): the rounded mean, the
+// pixel furthest from it and the one furthest from that, both pulled halfway to the mean, then up to
+// four 2-means refinements along their axis; the darker colour first.
+__host__ __device__ void find_rep_colors(int n, const uint32_t* px, int* lo, int* hi) {
+  uint64_t s64[3] = {0, 0, 0};
+  for (int i = 0; i < n; i++) { s64[0] += px_r(px[i]); s64[1] += px_g(px[i]); s64[2] += px_b(px[i]); }
+  int ave[3];
+  for (int c = 0; c < 3; c++) ave[c] = (int)((s64[c] + (uint64_t)(n / 2)) / (uint64_t)n);
+  auto comp = [&](int i, int c) { return c == 0 ? (int)px_r(px[i]) : c == 1 ? (int)px_g(px[i]) : (int)px_b(px[i]); };
+  int fd = -1, fi = 0;
+  for (int i = 0; i < n; i++) {
+    const int r = comp(i, 0) - ave[0], g = comp(i, 1) - ave[1], b = comp(i, 2) - ave[2];
+    const int d = r * r + g * g + b * b;
+    if (d > fd) { fd = d; fi = i; }
+  }
+  int l[3] = {comp(fi, 0), comp(fi, 1), comp(fi, 2)};
+  int od = -1, oi = 0;
+  for (int i = 0; i < n; i++) {
+    const int r = comp(i, 0) - l[0], g = comp(i, 1) - l[1], b = comp(i, 2) - l[2];
+    const int d = r * r + g * g + b * b;
+    if (d > od) { od = d; oi = i; }
+  }
+  int h[3] = {comp(oi, 0), comp(oi, 1), comp(oi, 2)};
+  for (int c = 0; c < 3; c++) { l[c] = (l[c] + ave[c]) >> 1; h[c] = (h[c] + ave[c]) >> 1; }
+  for (int iter = 0; iter < 4; iter++) {
+    if (l[0] == h[0] && l[1] == h[1] && l[2] == h[2]) break;
+    uint64_t nc[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    uint32_t w[2] = {0, 0};
+    int vr = h[0] - l[0], vg = h[1] - l[1], vb = h[2] - l[2];
+    const int lo_dot = vr * l[0] + vg * l[1] + vb * l[2], hi_dot = vr * h[0] + vg * h[1] + vb * h[2];
+    const int mid = lo_dot + hi_dot;
+    vr *= 2; vg *= 2; vb *= 2;
+    for (int i = 0; i < n; i++) {
+      const int dot = comp(i, 0) * vr + comp(i, 1) * vg + comp(i, 2) * vb;
+      const int m = dot > mid ? 1 : 0;
+      for (int c = 0; c < 3; c++) nc[m][c] += (uint64_t)comp(i, c);
+      w[m]++;
+    }
+    if (!w[0] || !w[1]) break;
+    int n8[2][3];
+    for (int j = 0; j < 2; j++)
+      for (int c = 0; c < 3; c++) n8[j][c] = (int)(uint8_t)((nc[j][c] + (w[j] / 2)) / w[j]);
+    if (n8[0][0] == l[0] && n8[0][1] == l[1] && n8[0][2] == l[2] && n8[1][0] == h[0] && n8[1][1] == h[1] &&
+        n8[1][2] == h[2])
+      break;
+    for (int c = 0; c < 3; c++) { l[c] = n8[0][c]; h[c] = n8[1][c]; }
+  }
+  const int e0 = l[0] * l[0] + l[1] * l[1] + l[2] * l[2], e1 = h[0] * h[0] + h[1] * h[1] + h[2] * h[2];
+  for (int c = 0; c < 3; c++) {
+    lo[c] = e0 > e1 ? h[c] : l[c];
+    hi[c] = e0 > e1 ? l[c] : h[c];
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -372,6 +431,7 @@ struct TileCfg {
   int comp[2];          // m_alpha_component_indices
   float ratio;          // m_adaptive_tile_color_alpha_weighting_ratio
   float alpha_derating[8];
+  int qdxt;             // qdxt1::init's tiling (crnlib/crn_qdxt1.cpp:100-330) instead of dxt_hc's
 };
 
 // dxt5_endpoint_optimizer::compute at quality Normal with 8-value blocks only, for the tile
@@ -561,7 +621,21 @@ __host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint3
   }
   float best_q = 0.0f;
   int best_e = 0;
-  for (int e = 0; e < 8; e++) {
+  if (cfg.qdxt) {
+    // qdxt1::init: PSNR clamped to [0, 500] (999999 for no error) minus the layout's derating,
+    // the largest wins
+    double best = -1.0;
+    for (int e = 0; e < 8; e++) {
+      uint32_t tot = 0;
+      for (int k = 0; k < layout_ntiles[e]; k++) tot += terr[0][layout_tiles[e][k]];
+      const double ms = tot * (1.0f / (64.0f * 3.0f));
+      double psnr = 999999.0f;
+      if (ms) psnr = fmin(fmax(log10(255.0f / sqrt(ms)) * 20.0f, 0.0), 500.0);
+      psnr = psnr - (double)derating[ch.level * 8 + e];
+      if (psnr > best) { best = psnr; best_e = e; }
+    }
+  }
+  for (int e = 0; e < 8 && !cfg.qdxt; e++) {
     float q = 0.0f;
     if (cfg.has_color) {
       uint32_t tot = 0;
@@ -587,6 +661,18 @@ __host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint3
     T.chunk = c;
     T.kind = (uint32_t)t;
     T.weight = (float)n * lw;
+    if (cfg.qdxt) {
+      // representative colours as the training vector of each of the tile's blocks, weighted by
+      // their distance (squared RGB / 5000, 1..8)
+      int lo[3], hi[3];
+      find_rep_colors(n, px + tile_ofs[t], lo, hi);
+      const int d0 = lo[0] - hi[0], d1 = lo[1] - hi[1], d2 = lo[2] - hi[2];
+      const uint32_t dist = (uint32_t)(d0 * d0 + d1 * d1 + d2 * d2);
+      const uint32_t w = dist / 5000u < 1u ? 1u : dist / 5000u > 8u ? 8u : dist / 5000u;
+      for (int k2 = 0; k2 < 3; k2++) { T.v[k2] = (float)lo[k2]; T.v[3 + k2] = (float)hi[k2]; }
+      T.weight = (float)(w * (uint32_t)(n / 16));
+      continue;
+    }
     if (cfg.has_color) palettize(px + tile_ofs[t], n, perceptual, T.v);
     for (int a = 0; a < cfg.num_alpha; a++) palettize_alpha(px + tile_ofs[t], n, cfg.comp[a], T.va[a]);
   }
@@ -597,6 +683,21 @@ __host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint3
       block_enc[blk] = (uint8_t)best_e;
     }
   return best_e;
+}
+
+// the dxt_fast selector word of every block (qdxt1::init's distinct-selector count)
+__global__ void k_fast_selector_words(const uint32_t* __restrict__ blocks, uint32_t n,
+                                      const SolidTables* __restrict__ st, uint32_t* __restrict__ words) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  uint32_t px[16];
+  for (int i = 0; i < 16; i++) px[i] = blocks[(size_t)b * 16 + i];
+  uint8_t sel[16];
+  uint32_t lo16, hi16;
+  fast_compress(16, px, st, lo16, hi16, sel);
+  uint32_t w = 0;
+  for (int i = 0; i < 16; i++) w |= (uint32_t)sel[i] << (2 * i);
+  words[b] = w;
 }
 
 __global__ void __launch_bounds__(64) k_hc_tiles(const uint32_t* __restrict__ blocks, const Chunk* __restrict__ chunks,
@@ -2610,9 +2711,18 @@ namespace crngpu {
 namespace {
 
 // dxt_hc::compress (crnlib/crn_dxt_hc.cpp:97-316) for DXT1, DXT5, DXN_XY/YX and DXT5A.
+// Variant of the clustered encode: dxt_hc's (the .crn path) or qdxt1's (clustered DDS): its
+// tiling, training vectors and codebook sizes from the full codebook and selector counts.
+struct HcMode {
+  bool qdxt = false;
+  float quality = 1.0f;        // qdxt: quality level / 255
+  float power_mul = 1.0f;      // qdxt: codebook-size curve exponent multiplier
+  uint32_t selector_base = 0;  // qdxt: distinct dxt_fast selector words + 128
+};
+
 int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_t format, uint8_t* d_out,
                      uint16_t* d_endpoint_idx, uint16_t* d_selector_idx, uint32_t* d_endpoints, uint32_t* d_selectors,
-                     crngpu_hc_stats* stats, cudaStream_t s) {
+                     crngpu_hc_stats* stats, cudaStream_t s, const HcMode& mode = HcMode()) {
   const uint32_t N = P.num_blocks;
   cudaError_t e;
   HcBuffers& B = hc_workspace();
@@ -2629,6 +2739,22 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
     default: set_error("clustered compression supports DXT1, DXT5, DXN_XY/YX and DXT5A"); return CRNGPU_E_UNSUPPORTED;
   }
   cfg.ratio = P.color_alpha_weighting_ratio > 0.f ? P.color_alpha_weighting_ratio : 3.0f;
+  cfg.qdxt = mode.qdxt ? 1 : 0;
+  // codebook sizes: the caller's (dxt_hc), or qdxt1::pack's curves (crnlib/crn_qdxt1.cpp:925-935):
+  // the full endpoint codebook (one entry per distinct training vector, at most 65535) scaled by
+  // quality^(1.8 m), at least 96; the selector base scaled by quality^(1.65 m), at least 128
+  auto ce_request = [&](uint32_t nvec) -> uint32_t {
+    if (!mode.qdxt) return std::min(nvec, P.color_endpoint_codebook_size);
+    const uint32_t cb = std::min<uint32_t>(nvec, 65535u);
+    const uint32_t k = (uint32_t)(cb * powf(mode.quality, 1.8f * mode.power_mul));
+    return std::max(std::min(k, cb), std::min(96u, cb));
+  };
+  auto cs_request = [&](uint32_t nvec) -> uint32_t {
+    if (!mode.qdxt) return std::min(nvec, P.color_selector_codebook_size);
+    const uint32_t sb = mode.selector_base;
+    const uint32_t k = (uint32_t)(sb * powf(mode.quality, 1.65f * mode.power_mul));
+    return std::min(nvec, std::max(std::min(k, sb), std::min(128u, sb)));
+  };
   const int tile_derating[8] = {0, 1, 1, 2, 2, 2, 2, 3};
   for (int k = 0; k < 8; k++) cfg.alpha_derating[k] = P.adaptive_tile_alpha_psnr_derating * ((float)tile_derating[k] / 3.0f);
   // chunks of every level (block rows are processed in pairs; widths and heights are even)
@@ -2645,7 +2771,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
     lweight[l] = L.weight;
     // crn_dxt_hc.cpp:121-134: colour derating per level and layout
     float d = P.adaptive_tile_color_psnr_derating;
-    if (l && d > .25f) d = std::max(.25f, d / powf(3.0f, (float)l));
+    if (l && d > .25f) d = std::max(.25f, d / powf(mode.qdxt ? 3.1f : 3.0f, (float)l));  // qdxt1: 3.1
     for (int k = 0; k < 8; k++) derating[l * 8 + k] = 0.0f + (d - 0.0f) * ((float)tile_derating[k] / 3.0f);
     const uint32_t rows = L.num_blocks / L.block_width;
     for (uint32_t y = 0; y < rows; y += 2)
@@ -2731,7 +2857,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
     k_tile_vectors<<<(nused + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused,
                                                         static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr));
     if ((rc = tree_vq<6>(static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr), nused,
-                         std::min(nused, P.color_endpoint_codebook_size), frac, B.cb6, &K, s, B.vq)) != CRNGPU_OK)
+                         ce_request(nused), frac, B.cb6, &K, s, B.vq)) != CRNGPU_OK)
       return rc;
     if ((e = B.tile_cluster.ensure(4 * ntiles)) != cudaSuccess) return cuda_check(e, "alloc tile clusters");
     k_nearest_vec6<<<(ntiles + 255) / 256, 256, 0, s>>>(tiles, ntiles, static_cast<float*>(B.cb6.ptr), K,
@@ -2768,7 +2894,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
                                                        static_cast<unsigned long long*>(B.sse.ptr));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_block_selectors");
     if ((rc = tree_vq<16>(static_cast<float*>(B.selvec.ptr), static_cast<uint32_t*>(B.selw.ptr), N,
-                          std::min(N, P.color_selector_codebook_size), frac, B.cb16, &KS, s, B.vq)) != CRNGPU_OK)
+                          cs_request(N), frac, B.cb16, &KS, s, B.vq)) != CRNGPU_OK)
       return rc;
     if ((e = B.cbsel.ensure(4 * KS)) != cudaSuccess || (e = B.block_sel.ensure(4 * N)) != cudaSuccess ||
         (e = B.entry_err.ensure(8 * 64 * (size_t)KS)) != cudaSuccess || (e = B.entry_used.ensure(4 * KS)) != cudaSuccess)
@@ -2952,7 +3078,7 @@ namespace {
 // the clustered encode and the writer.
 // per host thread: the gathered blocks and the encoded blocks on the device, kept between calls
 struct CrnDeviceBuffers {
-  DevBuf in, out;
+  DevBuf in, out, st, words;
 };
 CrnDeviceBuffers& crn_buffers() {
   static thread_local std::unique_ptr<CrnDeviceBuffers> b[64];
@@ -3080,6 +3206,82 @@ extern "C" int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t widt
   std::vector<uint8_t> file;
   if ((rc = src.pass(quality_level, file)) != CRNGPU_OK) return rc;
   return deliver(file, out, out_capacity);
+}
+
+extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
+                                                 uint32_t levels, uint32_t faces, uint32_t format,
+                                                 uint32_t quality_level, uint32_t flags, void* out,
+                                                 uint64_t out_capacity) {
+  using namespace crngpu;
+  using namespace crngpu::hc;
+  clear_error();
+  if (format != CRNGPU_FMT_DXT1) {
+    set_error("crngpu_compress_dds_clustered: the clustered DDS path is built for DXT1");
+    return CRNGPU_E_UNSUPPORTED;
+  }
+  if (quality_level > 255) { set_error("crngpu_compress_dds_clustered: quality above 255"); return CRNGPU_E_PARAM; }
+  CrnSource src;
+  int rc = src.prepare(rgba_levels, width, height, levels, faces, format, flags, "crngpu_compress_dds_clustered");
+  if (rc != CRNGPU_OK) return rc;
+  uint64_t need = 0;
+  for (uint32_t l = 0; l < levels; l++)
+    need += (uint64_t)((std::max(1u, width >> l) + 3) / 4) * ((std::max(1u, height >> l) + 3) / 4) * 8 * faces;
+  const uint32_t N = src.P.num_blocks;
+  cudaError_t e;
+  if (quality_level >= 255) {
+    // qdxt1::pack at full quality: every block its own cluster, i.e. the plain block encoder
+    const int r = crngpu_compress_blocks(static_cast<const uint8_t*>(src.d_in.ptr), N, CRNGPU_FMT_DXT1,
+                                         flags | CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES, static_cast<uint8_t*>(src.d_out.ptr),
+                                         CRNGPU_MEM_DEVICE, nullptr);
+    if (r < 0) return r;
+  } else {
+    // qdxt1::init's selector count: distinct dxt_fast selector words of the blocks, plus 128
+    CrnDeviceBuffers& cb = crn_buffers();
+    if ((e = cb.st.ensure(sizeof(SolidTables))) != cudaSuccess || (e = cb.words.ensure(4ull * N)) != cudaSuccess)
+      return cuda_check(e, "alloc selector words");
+    if ((e = cudaMemcpy(cb.st.ptr, single_colour_tables_host(), sizeof(SolidTables), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return cuda_check(e, "upload tables");
+    k_fast_selector_words<<<(N + 255) / 256, 256>>>(static_cast<const uint32_t*>(src.d_in.ptr), N,
+                                                    static_cast<const SolidTables*>(cb.st.ptr),
+                                                    static_cast<uint32_t*>(cb.words.ptr));
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "k_fast_selector_words");
+    std::vector<uint32_t> words(N);
+    if ((e = cudaMemcpy(words.data(), cb.words.ptr, 4ull * N, cudaMemcpyDeviceToHost)) != cudaSuccess)
+      return cuda_check(e, "read selector words");
+    std::sort(words.begin(), words.end());
+    const uint32_t distinct = (uint32_t)(std::unique(words.begin(), words.end()) - words.begin());
+    HcMode mode;
+    mode.qdxt = true;
+    mode.quality = quality_level / 255.0f;
+    mode.power_mul = 1.0f;
+    mode.selector_base = distinct + 128;
+    src.P.adaptive_tile_color_psnr_derating = 1.5f;  // qdxt1::init
+    src.P.color_endpoint_codebook_size = 65535;
+    src.P.color_selector_codebook_size = 65535;
+    if ((rc = hc_compress_impl(static_cast<const uint8_t*>(src.d_in.ptr), src.P, CRNGPU_FMT_DXT1,
+                               static_cast<uint8_t*>(src.d_out.ptr), nullptr, nullptr, nullptr, nullptr, nullptr,
+                               nullptr, mode)) != CRNGPU_OK)
+      return rc;
+  }
+  if (!out || out_capacity < need) return (int64_t)need;
+  std::vector<uint8_t> dxt((size_t)N * 8);
+  if ((e = cudaMemcpy(dxt.data(), src.d_out.ptr, dxt.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+    return cuda_check(e, "copy result");
+  // DDS order: every face's mip chain, each level's visible blocks row by row
+  uint8_t* o = static_cast<uint8_t*>(out);
+  for (uint32_t f = 0; f < faces; f++)
+    for (uint32_t l = 0; l < levels; l++) {
+      const uint32_t lw = std::max(1u, width >> l), lh = std::max(1u, height >> l);
+      const uint32_t bx = (lw + 3) / 4, by = (lh + 3) / 4;
+      const auto& L = src.P.levels[l];
+      const uint32_t H = L.num_blocks / (L.block_width * faces);
+      for (uint32_t y = 0; y < by; y++) {
+        const size_t row = (size_t)L.first_block + ((size_t)f * H + y) * L.block_width;
+        std::memcpy(o, dxt.data() + row * 8, (size_t)bx * 8);
+        o += (size_t)bx * 8;
+      }
+    }
+  return (int64_t)need;
 }
 
 extern "C" int crngpu_compress_crn_batch(crngpu_crn_batch_item* items, uint32_t n, uint32_t threads) {

@@ -189,6 +189,20 @@ CRNGPU_API int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t widt
                                        uint32_t faces, uint32_t format, uint32_t quality_level, uint32_t flags,
                                        void* out, uint64_t out_capacity);
 
+/* Clustered DDS, the reference's QDXT path (crn_compress with m_file_type = cCRNFileTypeDDS and
+ * quality_level < 255: dds_comp -> mipmapped_texture::qdxt_pack -> qdxt1, crnlib/crn_dds_comp.cpp:
+ * 150-205, crnlib/crn_qdxt1.cpp:81-1027) for DXT1: qdxt1's adaptive tiling (PSNR clamped to
+ * [0, 500], derating 1.5 / 3.1^level), its representative-colour training vectors weighted by
+ * endpoint distance, its codebook-size curves (endpoints: the full codebook x (q/255)^1.8, >= 96;
+ * selectors: distinct selector words + 128, x (q/255)^1.65, >= 128), on this library's GPU
+ * clusterizer, cluster fit and selector codebook. quality_level 255 is the plain block encoder, as
+ * in the reference. Output: the DXT1 blocks of every face's mip chain, each level's visible blocks
+ * row by row (the DDS data layout); returns their size (written when out_capacity suffices). */
+CRNGPU_API int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
+                                                 uint32_t levels, uint32_t faces, uint32_t format,
+                                                 uint32_t quality_level, uint32_t flags, void* out,
+                                                 uint64_t out_capacity);
+
 /* Many crn_compress calls at once (no counterpart in the reference, which compresses one texture
  * per call): `threads` host threads (0 = 4), each with its own CUDA stream and device buffers, take
  * items in turn, so one texture's host work (block gather, .crn writer) overlaps other textures'

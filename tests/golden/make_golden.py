@@ -194,6 +194,38 @@ def make_hc() -> None:
         json.dump(out, fh, indent=1, sort_keys=True)
 
 
+# clustered DDS (QDXT) cases: (name, size, seed, quality)
+QDXT_CASES = [("qdxt_256_q128", 256, 10, 128), ("qdxt_256_q64", 256, 10, 64), ("qdxt_1024_q128", 1024, 100, 128)]
+
+
+def make_qdxt() -> None:
+    """The reference's clustered DDS (crn_compress with a DDS file type and quality < 255: its
+    QDXT path) on colour mip chains: RGB RMSE of its DXT1 blocks over every level, the bar for the
+    GPU path (which is judged on quality, like the .crn clustering)."""
+    import time
+    sys.path.insert(0, os.path.dirname(HERE))
+    from dxt_decode import rgb_rmse
+    out = {}
+    for name, size, seed, q in QDXT_CASES:
+        levels = texgen.mip_chain(texgen.colour_texture(size, size, seed))
+        t = time.time()
+        dds = ref.compress_texture([levels], FMT["DXT1"], 1, q, FLAG_PERCEPTUAL | FLAG_HIERARCHICAL | FLAG_BOTH_BLOCK_TYPES,
+                                   DXT_UBER, 7)
+        secs = time.time() - t
+        assert dds[:4] == b"DDS ", "not a DDS file"
+        blocks = np.frombuffer(dds[128:], np.uint8).reshape(-1, 8)
+        src = np.concatenate([texgen.image_blocks(im) for im in levels])
+        assert blocks.shape[0] == src.shape[0], (blocks.shape, src.shape)
+        out[name] = {"size": size, "seed": seed, "quality": q, "blocks": int(src.shape[0]),
+                     "rmse": rgb_rmse(blocks, src), "seconds_8_threads_x86": round(secs, 2),
+                     "distinct_endpoints": int(np.unique(blocks[:, :4].copy().view(np.uint32)).size),
+                     "distinct_selectors": int(np.unique(blocks[:, 4:].copy().view(np.uint32)).size),
+                     "blocks_sha256": sha(blocks)}
+        print(name, out[name], flush=True)
+    with open(os.path.join(HERE, "qdxt_reference.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
 # mip generation cases: (name, width, height, content, seed, filter, filter scale, sRGB, wrap, comps)
 MIP_CASES = [("kaiser_64x48_rgba", 64, 48, "colour_alpha", 40, "kaiser", 0.9, True, False, 4),
              ("lanczos4_37x20_rgb", 37, 20, "colour", 41, "lanczos4", 1.0, True, False, 3),
@@ -277,9 +309,13 @@ if __name__ == "__main__":
     if sys.argv[1:] == ["mips"]:
         make_mips()
         sys.exit(0)
+    if sys.argv[1:] == ["qdxt"]:
+        make_qdxt()
+        sys.exit(0)
     make_blocks()
     make_crn()
     make_hc()
     make_config2()
     make_mips()
+    make_qdxt()
     print("golden fixtures written to", HERE)

@@ -230,3 +230,41 @@ def test_compress_crn_batch_equals_single_calls(hc):
     batch = cg.compress_crn_batch(items, threads=3)
     for it, got in zip(items, batch):
         assert got == cg.compress_crn(*it)
+
+
+def qdxt_reference():
+    with open(os.path.join(G.GOLDEN, "qdxt_reference.json")) as fh:
+        return json.load(fh)
+
+
+@pytest.mark.parametrize("name", ["qdxt_256_q128", "qdxt_256_q64", "qdxt_1024_q128"])
+def test_clustered_dds_matches_reference_quality(hc, name):
+    """Clustered DDS (crnlib's QDXT1 path: crn_compress to DDS below quality 255) against the
+    reference's own output on the same mip chain (tests/golden/qdxt_reference.json): RGB RMSE within
+    5% of the reference's, and the block data clustered like the reference's (distinct endpoint
+    and selector words of the same order, far fewer than the blocks)."""
+    import crunch2_gb300 as cg
+    from crunch2_gb300 import texgen
+    R = qdxt_reference()[name]
+    levels = texgen.mip_chain(texgen.colour_texture(R["size"], R["size"], R["seed"]))
+    blocks = cg.compress_dds_clustered([levels], quality=R["quality"])
+    src = np.concatenate([texgen.image_blocks(im) for im in levels])
+    assert blocks.shape == (R["blocks"], 8) == src.shape[:1] + (8,)
+    ours = rgb_rmse(blocks, src)
+    de = np.unique(blocks[:, :4].copy().view(np.uint32)).size
+    ds = np.unique(blocks[:, 4:].copy().view(np.uint32)).size
+    print(f"{name}: GPU RMSE {ours:.4f} (reference {R['rmse']:.4f}); distinct endpoints {de} "
+          f"(reference {R['distinct_endpoints']}), selectors {ds} (reference {R['distinct_selectors']})")
+    assert ours <= 1.05 * R["rmse"], (ours, R["rmse"])
+    assert de <= 1.5 * R["distinct_endpoints"] and ds <= 1.5 * R["distinct_selectors"], (de, ds)
+
+
+def test_clustered_dds_full_quality_is_the_block_encoder(hc):
+    """At quality 255 the clustered DDS path is the plain block encoder on every level."""
+    import crunch2_gb300 as cg
+    from crunch2_gb300 import texgen
+    levels = texgen.mip_chain(texgen.colour_texture(64, 48, 5))
+    got = cg.compress_dds_clustered([levels], quality=255)
+    want = np.concatenate([cg.compress_image(im, cg.FMT_DXT1, cg.FLAG_PERCEPTUAL | cg.FLAG_USE_BOTH_BLOCK_TYPES)
+                           .reshape(-1, 8) for im in levels])
+    assert np.array_equal(got, want)
