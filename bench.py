@@ -89,6 +89,36 @@ def clustered_leg(cg, dev, levels, blocks, texels, steps: int) -> dict:
                     "clustered encode (every dxt_hc stage on the GPU) -> D2H -> .crn writer (host); wall time"}
 
 
+QDXT_REFERENCE = os.path.join(ROOT, "tests", "golden", "qdxt_reference.json")
+
+
+def qdxt_leg(cg, dev, levels, blocks, texels, steps: int) -> dict:
+    """Clustered DDS of the 1024x1024 mip chain at q128 (crn_compress to DDS below quality 255,
+    the reference's QDXT1 path), median wall time of up to 5 calls; RMSE and distinct endpoint and
+    selector words beside the reference's output on the same chain (committed with the fixtures)."""
+    import torch
+    from crunch2_gb300 import learned as LR
+    with open(QDXT_REFERENCE) as fh:
+        ref = json.load(fh)["qdxt_1024_q128"]
+    cg.compress_dds_clustered([levels], quality=128)  # warm-up
+    times = []
+    for _ in range(max(1, min(steps, 5))):
+        t0 = time.perf_counter()
+        out = cg.compress_dds_clustered([levels], quality=128)
+        times.append(time.perf_counter() - t0)
+    s = statistics.median(times)
+    return {"value": round(texels / s / 1e6, 3), "unit": "Mtexel/s", "s_per_texture": round(s, 4), "quality": 128,
+            "rmse": round(LR.rgb_rmse_torch(torch.from_numpy(out).to(dev), torch.from_numpy(blocks).to(dev)), 4),
+            "rmse_reference": round(ref["rmse"], 4),
+            "distinct_endpoints": int(np.unique(out[:, :4].copy().view(np.uint32)).size),
+            "distinct_selectors": int(np.unique(out[:, 4:].copy().view(np.uint32)).size),
+            "distinct_endpoints_reference": ref["distinct_endpoints"],
+            "distinct_selectors_reference": ref["distinct_selectors"],
+            "reference_s_8_threads_x86": ref["seconds_8_threads_x86"],
+            "path": "crngpu_compress_dds_clustered: host RGBA8 mip chain -> H2D -> qdxt1 tiling, clustering and "
+                    "block refit on the GPU -> D2H of the DDS blocks; wall time"}
+
+
 CONFIG2_REFERENCE = os.path.join(ROOT, "tests", "golden", "config2_reference.json")
 
 
@@ -602,6 +632,9 @@ def main():
     # .crn of this texture (committed fixture), both decoded by the GPU transcoder
     clustered = None if "clustered" in skip else clustered_leg(cg, dev, levels, blocks, texels, args.steps)
 
+    # ---- clustered DDS (the reference's QDXT1 path) of the same mip chain at quality 128
+    qdxt = None if "qdxt" in skip else qdxt_leg(cg, dev, levels, blocks, texels, args.steps)
+
     # ---- the 2048x2048 DXT5 (colour + alpha noise) and DXN_XY (normal map) mip chains at quality
     # 128: crn_compress wall time, and the RMSEs of the GPU-decoded result beside those of the
     # reference's own .crn of the same textures (reference numbers committed with the fixtures)
@@ -652,7 +685,7 @@ def main():
                 "parity_vs_oracle_sample": parity, "e2e_parity": e2e_parity,
                 "e2e": {"value": round(e2e_value, 3), "unit": "Mtexel/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h, "path": "crngpu_compress_image per level, pinned host buffers"},
-                "learned": learned, "transcode": transcode, "clustered": clustered,
+                "learned": learned, "transcode": transcode, "clustered": clustered, "clustered_dds": qdxt,
                 "clustered_2048": clustered_2048, "mixed_batch": mixed_batch, "mips": mips, "roofline": roofline,
                 "cpu_baseline": cpu,
                 "gpu_launches": args.steps * 1, "clocks": clk, "wall_s_timed": round(wall, 4)}
