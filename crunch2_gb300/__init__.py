@@ -513,18 +513,21 @@ def compress_crn_bitrate(faces_levels, target_bitrate: float, fmt: int = FMT_DXT
     return out.tobytes(), int(q.value), float(br.value)
 
 
-def compress_dds_clustered(faces_levels, quality: int = 128, flags: int = FLAG_PERCEPTUAL, fmt: int = FMT_DXT1):
-    """Clustered DDS (the reference's QDXT path, crngpu_compress_dds_clustered): the DXT1 blocks of
-    every face's mip chain, per level its visible blocks (numpy (n, 8))."""
+def compress_dds_clustered(faces_levels, quality: int = 128, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES,
+                           fmt: int = FMT_DXT1):
+    """The block data of a DDS written by crn_compress (crngpu_compress_dds_clustered): clustered
+    (the reference's QDXT path, DXT1) below quality 255, the plain encoder at 255 (any format); every
+    face's mip chain, per level its visible blocks (numpy (n, bytes per block))."""
     h, w = faces_levels[0][0].shape[:2]
     flat = np.concatenate([np.ascontiguousarray(im, dtype=np.uint8).reshape(-1) for face in faces_levels for im in face])
     L = lib()
+    bpb = bytes_per_block(fmt)
     args = (flat.ctypes.data, w, h, len(faces_levels[0]), len(faces_levels), fmt, quality, flags)
-    need = len(faces_levels) * sum(((max(1, w >> l) + 3) // 4) * ((max(1, h >> l) + 3) // 4) * 8
+    need = len(faces_levels) * sum(((max(1, w >> l) + 3) // 4) * ((max(1, h >> l) + 3) // 4) * bpb
                                    for l in range(len(faces_levels[0])))
     out = np.zeros(need, np.uint8)
     _check(int(L.crngpu_compress_dds_clustered(*args, out.ctypes.data, need)), "crngpu_compress_dds_clustered")
-    return out.reshape(-1, 8)
+    return out.reshape(-1, bpb)
 
 
 def compress_crn_batch(items, threads: int = 4):

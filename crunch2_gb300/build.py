@@ -32,6 +32,7 @@ UNITS = [
     ("mlp.cu", []),
     ("hc_encode.cu", ["--fmad=false"]),
     ("mip_gen.cu", ["--fmad=false"]),
+    ("crnlib_compat.cpp", []),
 ]
 
 
@@ -46,7 +47,8 @@ def _stale(obj: str, src: str) -> bool:
     if not os.path.exists(obj):
         return True
     deps = [src] + [os.path.join(SRC, h) for h in os.listdir(SRC) if h.endswith(".h")]
-    deps.append(os.path.join(os.path.dirname(HERE), "include", "crngpu.h"))
+    for h in ("crngpu.h", "crnlib_compat.h"):
+        deps.append(os.path.join(os.path.dirname(HERE), "include", h))
     t = os.path.getmtime(obj)
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 

@@ -178,6 +178,7 @@ bool CrnFile::parse(const uint8_t* d, uint32_t size) {
   levels = d[16];
   faces = d[17];
   format = d[18];
+  segmented = (be(d + 19, 2) & 1u) != 0;
   if (!width || !height || width > 4096 || height > 4096) { error = "bad dimensions"; return false; }
   if (faces != 1 && faces != 6) { error = "bad face count"; return false; }
   if (!levels || levels > 16 || kLevelOfs + 4 * levels > header_size) { error = "bad level count"; return false; }
@@ -203,6 +204,7 @@ bool CrnFile::parse(const uint8_t* d, uint32_t size) {
     li.blocks_x = (li.width + 3) >> 2;
     li.blocks_y = (li.height + 3) >> 2;
     li.ofs = be(d + kLevelOfs + 4 * l, 4);
+    if (segmented) { li.size = 0; continue; }  // level data lives outside this buffer
     const uint32_t next = l + 1 < levels ? be(d + kLevelOfs + 4 * (l + 1), 4) : size;
     if (next <= li.ofs || !in_file(li.ofs, next - li.ofs)) { error = "bad level offsets"; return false; }
     li.size = next - li.ofs;

@@ -46,6 +46,9 @@ enum class Kind { DXT1, DXT5, DXN, DXT5A };
 struct CrnFile {
   uint32_t width = 0, height = 0, levels = 0, faces = 0, format = 0, bytes_per_block = 0;
   uint32_t data_size = 0;
+  // cCRNHeaderFlagSegmented (inc/crn_defs.h:296): the level data is not in the file; each level
+  // comes with its own buffer (crnd_unpack_level_segmented)
+  bool segmented = false;
   Kind kind = Kind::DXT1;
   LevelInfo level[16];
   Model ref_dm, ep_dm[2], sel_dm[2];

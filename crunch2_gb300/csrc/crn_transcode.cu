@@ -897,6 +897,10 @@ int unpack_one(UnpackContext* c, const uint8_t* host_src, const uint8_t* dev_src
     if (!dst_faces[f]) { set_error("NULL face pointer"); return CRNGPU_E_PARAM; }
   cudaStream_t s = as_stream(stream);
   cudaError_t e;
+  if (F.segmented && !dev_src && !host_src) {
+    set_error("segmented file: pass the level data (crngpu_unpack_level_segmented)");
+    return CRNGPU_E_PARAM;
+  }
   LevelTask t = context_task(c, level);
   t.pitch = row_pitch;
   if (dev_src) { t.src = dev_src; t.src_size = src_size; }
@@ -1030,8 +1034,8 @@ extern "C" int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t firs
                                         void* dst, uint64_t dst_size, int mem, void* stream) {
   clear_error();
   UnpackContext* c = reinterpret_cast<UnpackContext*>(ctx);
-  if (!valid_ctx(c) || !dst || !level_count || first_level + level_count > c->file.levels) {
-    set_error("bad context, destination or level range");
+  if (!valid_ctx(c) || !dst || !level_count || first_level + level_count > c->file.levels || c->file.segmented) {
+    set_error("bad context, destination or level range (or a segmented file)");
     return CRNGPU_E_PARAM;
   }
   const uint64_t total = levels_bytes(c->file, first_level, level_count);
@@ -1068,8 +1072,9 @@ extern "C" crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_ba
   for (uint32_t i = 0; i < n; i++) {
     UnpackContext* c = reinterpret_cast<UnpackContext*>(items[i].ctx);
     if (!valid_ctx(c) || !items[i].dst || !items[i].level_count ||
-        items[i].first_level + items[i].level_count > c->file.levels || c->device != b->device) {
-      set_error("batch item " + std::to_string(i) + ": bad context, destination, level range or device");
+        items[i].first_level + items[i].level_count > c->file.levels || c->device != b->device ||
+        c->file.segmented) {
+      set_error("batch item " + std::to_string(i) + ": bad context, destination, level range, device or a segmented file");
       return nullptr;
     }
     const uint64_t need = levels_bytes(c->file, items[i].first_level, items[i].level_count);
@@ -1290,6 +1295,7 @@ extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_si
   CrnFile F;
   if (!F.parse(static_cast<const uint8_t*>(crn_data), crn_size)) { set_error(F.error); return CRNGPU_E_CORRUPT; }
   if (level_index >= F.levels) { set_error("level out of range"); return CRNGPU_E_PARAM; }
+  if (F.segmented) { set_error("segmented file: its level data is not in the buffer"); return CRNGPU_E_PARAM; }
   const LevelInfo& li = F.level[level_index];
   const uint32_t minimal = li.blocks_x * F.bytes_per_block;
   uint32_t pitch = row_pitch_in_bytes ? row_pitch_in_bytes : minimal;

@@ -3045,7 +3045,7 @@ extern "C" int crngpu_hc_compress(const uint8_t* d_blocks, const crngpu_hc_param
 extern "C" int crngpu_hc_codebook_sizes(uint32_t width, uint32_t height, uint32_t quality_level, uint32_t format,
                                         uint32_t* sizes4) {
   if (!sizes4 || !width || !height) return CRNGPU_E_PARAM;
-  const uint32_t kMin = 32, kMax = 8192;  // cCRNMinPaletteSize, cCRNMaxPaletteSize (inc/crnlib.h:117-118)
+  const uint32_t kMin = 8, kMax = 8192;  // cCRNMinPaletteSize, cCRNMaxPaletteSize (inc/crnlib.h:118-119)
   uint32_t max_entries = ((width + 3) / 4) * ((height + 3) / 4);
   max_entries = std::min(std::max(max_entries, kMin), kMax);
   const float quality = std::min(std::max((float)quality_level / 255.0f, 0.0f), 1.0f);
@@ -3090,6 +3090,9 @@ CrnDeviceBuffers& crn_buffers() {
 
 struct CrnSource {
   crngpu_hc_params P;
+  // crn_comp_params fields beyond quality (crnlib/crn_comp.cpp:527-577): deratings, alpha
+  // channel and, when palette_sizes[0] is nonzero, manual palette sizes
+  crngpu_crn_options opt = {sizeof(crngpu_crn_options), 2.0f, 2.0f, 3u, {0u, 0u, 0u, 0u}};
   uint32_t width = 0, height = 0, levels = 0, faces = 0, format = 0, bpb = 0;
   uint64_t texels = 0;
   cudaStream_t stream = nullptr;
@@ -3133,7 +3136,7 @@ struct CrnSource {
                 const uint32_t x = std::min(bx * 4 + dx, lw - 1), y = std::min(by * 4 + dy, lh - 1);
                 uint32_t px;
                 std::memcpy(&px, img + (size_t)y * lw + x, 4);
-                blocks.push_back(px);
+                blocks.push_back(cook_texel(format, px));
               }
       }
     }
@@ -3142,10 +3145,12 @@ struct CrnSource {
     P.num_faces = faces;
     const bool colour_fmt = format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5;
     P.perceptual = colour_fmt && (flags & CRNGPU_FLAG_PERCEPTUAL) ? 1 : 0;
-    P.adaptive_tile_color_psnr_derating = 2.0f;
-    P.adaptive_tile_alpha_psnr_derating = 2.0f;
+    P.adaptive_tile_color_psnr_derating = opt.colour_psnr_derating;
+    P.adaptive_tile_alpha_psnr_derating = opt.alpha_psnr_derating;
+    if (format == CRNGPU_FMT_DXT5_CCXY && !opt.palette_sizes[0])
+      P.adaptive_tile_color_psnr_derating = 5.0f;  // crn_comp.cpp:553-558
     P.color_alpha_weighting_ratio = 3.0f;
-    P.alpha_component = 3;
+    P.alpha_component = opt.alpha_component;
     bpb = (format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5A) ? 8 : 16;
     cudaError_t e;
     if ((e = d_in.ensure(blocks.size() * 4)) != cudaSuccess || (e = d_out.ensure((size_t)P.num_blocks * bpb)) != cudaSuccess)
@@ -3159,7 +3164,11 @@ struct CrnSource {
   // One compress pass at `quality`: the .crn bytes into `file`.
   int pass(uint32_t quality, std::vector<uint8_t>& file) {
     uint32_t sizes[4];
-    if (crngpu_hc_codebook_sizes(width, height, quality, format, sizes) != CRNGPU_OK) return CRNGPU_E_PARAM;
+    if (opt.palette_sizes[0]) {
+      for (int k = 0; k < 4; k++) sizes[k] = std::min(std::max(opt.palette_sizes[k], 8u), 8192u);  // crn_comp.cpp:532-538
+    } else if (crngpu_hc_codebook_sizes(width, height, quality, format, sizes) != CRNGPU_OK) {
+      return CRNGPU_E_PARAM;
+    }
     P.color_endpoint_codebook_size = sizes[0];
     P.color_selector_codebook_size = sizes[1];
     P.alpha_endpoint_codebook_size = sizes[2];
@@ -3215,24 +3224,26 @@ extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uin
   using namespace crngpu;
   using namespace crngpu::hc;
   clear_error();
-  if (format != CRNGPU_FMT_DXT1) {
-    set_error("crngpu_compress_dds_clustered: the clustered DDS path is built for DXT1");
+  if (format != CRNGPU_FMT_DXT1 && quality_level < 255) {
+    set_error("crngpu_compress_dds_clustered: the clustered DDS path (quality below 255) is built for DXT1");
     return CRNGPU_E_UNSUPPORTED;
   }
   if (quality_level > 255) { set_error("crngpu_compress_dds_clustered: quality above 255"); return CRNGPU_E_PARAM; }
+  if (format_is_non_srgb(format)) flags &= ~CRNGPU_FLAG_PERCEPTUAL;
   CrnSource src;
   int rc = src.prepare(rgba_levels, width, height, levels, faces, format, flags, "crngpu_compress_dds_clustered");
   if (rc != CRNGPU_OK) return rc;
+  const uint32_t bpb = src.bpb;
   uint64_t need = 0;
   for (uint32_t l = 0; l < levels; l++)
-    need += (uint64_t)((std::max(1u, width >> l) + 3) / 4) * ((std::max(1u, height >> l) + 3) / 4) * 8 * faces;
+    need += (uint64_t)((std::max(1u, width >> l) + 3) / 4) * ((std::max(1u, height >> l) + 3) / 4) * bpb * faces;
   const uint32_t N = src.P.num_blocks;
   cudaError_t e;
   if (quality_level >= 255) {
-    // qdxt1::pack at full quality: every block its own cluster, i.e. the plain block encoder
-    const int r = crngpu_compress_blocks(static_cast<const uint8_t*>(src.d_in.ptr), N, CRNGPU_FMT_DXT1,
-                                         flags | CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES, static_cast<uint8_t*>(src.d_out.ptr),
-                                         CRNGPU_MEM_DEVICE, nullptr);
+    // dds_comp at quality 255 (crnlib/crn_dds_comp.cpp:150-157): the plain encoder on every block
+    // of the cooked source (as qdxt1::pack at full quality: every block its own cluster)
+    const int r = crngpu_compress_blocks(static_cast<const uint8_t*>(src.d_in.ptr), N, format, flags,
+                                         static_cast<uint8_t*>(src.d_out.ptr), CRNGPU_MEM_DEVICE, nullptr);
     if (r < 0) return r;
   } else {
     // qdxt1::init's selector count: distinct dxt_fast selector words of the blocks, plus 128
@@ -3264,7 +3275,7 @@ extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uin
       return rc;
   }
   if (!out || out_capacity < need) return (int64_t)need;
-  std::vector<uint8_t> dxt((size_t)N * 8);
+  std::vector<uint8_t> dxt((size_t)N * bpb);
   if ((e = cudaMemcpy(dxt.data(), src.d_out.ptr, dxt.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
     return cuda_check(e, "copy result");
   // DDS order: every face's mip chain, each level's visible blocks row by row
@@ -3277,8 +3288,8 @@ extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uin
       const uint32_t H = L.num_blocks / (L.block_width * faces);
       for (uint32_t y = 0; y < by; y++) {
         const size_t row = (size_t)L.first_block + ((size_t)f * H + y) * L.block_width;
-        std::memcpy(o, dxt.data() + row * 8, (size_t)bx * 8);
-        o += (size_t)bx * 8;
+        std::memcpy(o, dxt.data() + row * bpb, (size_t)bx * bpb);
+        o += (size_t)bx * bpb;
       }
     }
   return (int64_t)need;
@@ -3321,28 +3332,23 @@ extern "C" int crngpu_compress_crn_batch(crngpu_crn_batch_item* items, uint32_t 
   return failed ? CRNGPU_E_PARAM : CRNGPU_OK;
 }
 
-extern "C" int64_t crngpu_compress_crn_bitrate(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
-                                               uint32_t levels, uint32_t faces, uint32_t format, float target_bitrate,
-                                               uint32_t flags, void* out, uint64_t out_capacity,
-                                               uint32_t* quality_out, float* bitrate_out) {
-  using namespace crngpu;
-  clear_error();
-  if (!(target_bitrate > 0.0f)) { set_error("crngpu_compress_crn_bitrate: target bitrate must be positive"); return CRNGPU_E_PARAM; }
-  CrnSource src;
-  int rc = src.prepare(rgba_levels, width, height, levels, faces, format, flags, "crngpu_compress_crn_bitrate");
-  if (rc != CRNGPU_OK) return rc;
-  // interpolative search over the quality levels (create_compressed_texture,
-  // crnlib/crn_texture_comp.cpp:120-245): each trial's bitrate is cached; after the first trial the
-  // next quality is interpolated between the nearest tried levels that bracket the target (or taken
-  // a third of the way up the open range); after 8 trials the search is a plain bisection. The
-  // closest bitrate at or below the target wins, else the closest above; a result within 0.005 bpp
-  // below the target ends the search.
+namespace crngpu {
+namespace {
+
+// The interpolative search over quality levels of create_compressed_texture
+// (crnlib/crn_texture_comp.cpp:120-245): each trial's bitrate is cached; after the first trial the
+// next quality is interpolated between the nearest tried levels that bracket the target (or taken
+// a third of the way up the open range); after 8 trials the search is a plain bisection. The
+// closest bitrate at or below the target wins, else the closest above; a result within 0.005 bpp
+// below the target ends the search.
+int bitrate_search(CrnSource& src, float target_bitrate, std::vector<uint8_t>& best_file, uint32_t* quality_out,
+                   float* bitrate_out) {
   const int kLowest = 0, kHighest = 255, kMaxIterations = 8;
   float cached[256];
   for (float& c : cached) c = -1.0f;
-  int low = kLowest, high = kHighest, best_q = -1;
+  int low = kLowest, high = kHighest, best_q = -1, rc;
   float best_rate = 1e10f;
-  std::vector<uint8_t> best_file, file;
+  std::vector<uint8_t> file;
   bool force_bisection = false;
   for (int iter = 0; low <= high; iter++) {
     int trial = (low + high) / 2;
@@ -3382,5 +3388,57 @@ extern "C" int64_t crngpu_compress_crn_bitrate(const uint8_t* rgba_levels, uint3
   }
   if (quality_out) *quality_out = (uint32_t)best_q;
   if (bitrate_out) *bitrate_out = best_rate;
-  return deliver(best_file, out, out_capacity);
+  return CRNGPU_OK;
+}
+
+}  // namespace
+}  // namespace crngpu
+
+extern "C" int64_t crngpu_compress_crn_bitrate(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
+                                               uint32_t levels, uint32_t faces, uint32_t format, float target_bitrate,
+                                               uint32_t flags, void* out, uint64_t out_capacity,
+                                               uint32_t* quality_out, float* bitrate_out) {
+  if (!(target_bitrate > 0.0f)) {
+    crngpu::set_error("crngpu_compress_crn_bitrate: target bitrate must be positive");
+    return CRNGPU_E_PARAM;
+  }
+  return crngpu_compress_crn_ex(rgba_levels, width, height, levels, faces, format, 0, target_bitrate, flags, nullptr,
+                                out, out_capacity, quality_out, bitrate_out);
+}
+
+extern "C" int64_t crngpu_compress_crn_ex(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
+                                          uint32_t levels, uint32_t faces, uint32_t format, uint32_t quality_level,
+                                          float target_bitrate, uint32_t flags, const crngpu_crn_options* options,
+                                          void* out, uint64_t out_capacity, uint32_t* quality_out,
+                                          float* bitrate_out) {
+  using namespace crngpu;
+  clear_error();
+  if (quality_out) *quality_out = 0;
+  if (bitrate_out) *bitrate_out = 0.0f;
+  if (target_bitrate < 0.0f || target_bitrate != target_bitrate) {
+    set_error("crngpu_compress_crn_ex: negative target bitrate");
+    return CRNGPU_E_PARAM;
+  }
+  if (quality_level > 255) { set_error("crngpu_compress_crn_ex: quality above 255"); return CRNGPU_E_PARAM; }
+  CrnSource src;
+  if (options) {
+    if (options->struct_size != sizeof(crngpu_crn_options) || options->alpha_component > 3 ||
+        !(options->colour_psnr_derating >= 0.0f) || !(options->alpha_psnr_derating >= 0.0f)) {
+      set_error("crngpu_compress_crn_ex: bad options");
+      return CRNGPU_E_PARAM;
+    }
+    src.opt = *options;
+  }
+  int rc = src.prepare(rgba_levels, width, height, levels, faces, format, flags, "crngpu_compress_crn_ex");
+  if (rc != CRNGPU_OK) return rc;
+  std::vector<uint8_t> file;
+  // manual palette sizes turn the bitrate search off (crnlib/crn_texture_comp.cpp:85)
+  if (target_bitrate > 0.0f && !src.opt.palette_sizes[0]) {
+    if ((rc = bitrate_search(src, target_bitrate, file, quality_out, bitrate_out)) != CRNGPU_OK) return rc;
+  } else {
+    if ((rc = src.pass(quality_level, file)) != CRNGPU_OK) return rc;
+    if (quality_out && !(target_bitrate > 0.0f)) *quality_out = quality_level;
+    if (bitrate_out) *bitrate_out = (float)file.size() * 8.0f / (float)src.texels;
+  }
+  return deliver(file, out, out_capacity);
 }

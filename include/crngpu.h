@@ -182,8 +182,9 @@ CRNGPU_API int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
  * 242-267, m_file_type = cCRNFileTypeCRN, cCRNMipModeUseSourceMips): rgba_levels holds faces x
  * levels RGBA8 images, face-major, level l being max(1, w >> l) x max(1, h >> l) texels, tightly
  * packed and concatenated (the order of crn_comp_params::m_pImages[face][level]). format: DXT1,
- * DXT5 (alpha = channel 3), DXN_XY/YX, DXT5A; quality_level 0..255 sets the codebook sizes;
- * flags: CRNGPU_FLAG_PERCEPTUAL for the colour formats. Clustered encode on the GPU, .crn written
+ * the DXT5 family (alpha = channel 3; the swizzled variants get the reference's source
+ * conversions, crn_comp.cpp:440-452), DXN_XY/YX, DXT5A; quality_level 0..255 sets the codebook
+ * sizes; flags: CRNGPU_FLAG_PERCEPTUAL for DXT1 / DXT5. Clustered encode on the GPU, .crn written
  * on the host. Returns the file size (copied to `out` when out_capacity suffices) or an error. */
 CRNGPU_API int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels,
                                        uint32_t faces, uint32_t format, uint32_t quality_level, uint32_t flags,
@@ -195,9 +196,11 @@ CRNGPU_API int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t widt
  * [0, 500], derating 1.5 / 3.1^level), its representative-colour training vectors weighted by
  * endpoint distance, its codebook-size curves (endpoints: the full codebook x (q/255)^1.8, >= 96;
  * selectors: distinct selector words + 128, x (q/255)^1.65, >= 128), on this library's GPU
- * clusterizer, cluster fit and selector codebook. quality_level 255 is the plain block encoder, as
- * in the reference. Output: the DXT1 blocks of every face's mip chain, each level's visible blocks
- * row by row (the DDS data layout); returns their size (written when out_capacity suffices). */
+ * clusterizer, cluster fit and selector codebook. quality_level 255 is dds_comp's plain path for
+ * every format (DXT1, the DXT5 family with the reference's source swizzles, DXN_XY/YX, DXT5A;
+ * the perceptual flag is dropped for the non-sRGB formats, as crn_compress does). Output: the
+ * blocks of every face's mip chain, each level's visible blocks row by row (the DDS data layout,
+ * without the 128-byte header); returns their size (written when out_capacity suffices). */
 CRNGPU_API int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
                                                  uint32_t levels, uint32_t faces, uint32_t format,
                                                  uint32_t quality_level, uint32_t flags, void* out,
@@ -231,6 +234,30 @@ CRNGPU_API int64_t crngpu_compress_crn_bitrate(const uint8_t* rgba_levels, uint3
                                                uint32_t levels, uint32_t faces, uint32_t format, float target_bitrate,
                                                uint32_t flags, void* out, uint64_t out_capacity,
                                                uint32_t* quality_out, float* bitrate_out);
+
+/* crn_compress for .crn output with every crn_comp_params field this library honours
+ * (crnlib/crn_texture_comp.cpp:48-245, crnlib/crn_comp.cpp:524-590): quality_level, or, when
+ * target_bitrate > 0 and no manual palette sizes are given, the bitrate search of
+ * crngpu_compress_crn_bitrate; options (NULL = crunch's defaults) carry the adaptive-tile PSNR
+ * deratings (m_crn_adaptive_tile_color/alpha_psnr_derating, 2.0 each; DXT5_CCxY uses 5.0 for
+ * colour unless palette sizes are manual), the alpha channel (m_alpha_component, 3) and manual
+ * palette sizes (cCRNCompFlagManualPaletteSizes with m_crn_*_palette_size, clamped to [8, 8192];
+ * palette_sizes[0] == 0 = sizes from the quality level). *quality_out gets the quality level of
+ * the file (the search's choice when it ran; 0 when manual palette sizes overrode a target
+ * bitrate, as in the reference), *bitrate_out the file's bits per texel. Returns the file size (copied to `out` when out_capacity
+ * suffices) or an error. */
+typedef struct crngpu_crn_options {
+    uint32_t struct_size;        /* sizeof(crngpu_crn_options) */
+    float colour_psnr_derating;  /* m_crn_adaptive_tile_color_psnr_derating */
+    float alpha_psnr_derating;   /* m_crn_adaptive_tile_alpha_psnr_derating */
+    uint32_t alpha_component;    /* m_alpha_component (0..3) */
+    uint32_t palette_sizes[4];   /* colour endpoints, colour selectors, alpha endpoints, alpha selectors */
+} crngpu_crn_options;
+CRNGPU_API int64_t crngpu_compress_crn_ex(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
+                                          uint32_t levels, uint32_t faces, uint32_t format, uint32_t quality_level,
+                                          float target_bitrate, uint32_t flags, const crngpu_crn_options* options,
+                                          void* out, uint64_t out_capacity, uint32_t* quality_out,
+                                          float* bitrate_out);
 
 /* Codebook sizes for a quality level (crn_comp::quantize_images, crnlib/crn_comp.cpp:541-577):
  * sizes4 = colour endpoints, colour selectors, alpha endpoints, alpha selectors. */

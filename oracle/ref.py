@@ -46,6 +46,13 @@ def lib():
         L.ref_resample.argtypes = [ctypes.c_void_p, _u32, _u32, _u32, _u32, ctypes.c_char_p, ctypes.c_float,
                                    ctypes.c_int, ctypes.c_int, _u32, ctypes.c_void_p]
         L.ref_resample.restype = ctypes.c_int
+        L.ref_compress_mips.argtypes = [ctypes.c_void_p, _u32, _u32, _u32, _u32, _u32, _u32, _u32, _u32, _u32,
+                                        ctypes.c_float, _u32, _u32, _u32, _u32, ctypes.c_void_p, _u32]
+        L.ref_compress_mips.restype = _u32
+        L.ref_crn_to_dds.argtypes = [ctypes.c_void_p, _u32, ctypes.c_void_p, _u32]
+        L.ref_crn_to_dds.restype = _u32
+        L.ref_crnd_probe.argtypes = [ctypes.c_void_p, _u32, ctypes.c_void_p, ctypes.c_void_p, _u32]
+        L.ref_crnd_probe.restype = _u32
         _lib = L
     return _lib
 
@@ -148,3 +155,40 @@ def generate_mipmaps(rgba: np.ndarray, filt: str, filter_scale: float, srgb: boo
         levels.append(resample(rgba, max(1, w >> l), max(1, h >> l), filt, filter_scale, srgb, wrap, num_comps))
         l += 1
     return levels
+
+
+def compress_mips(faces_top: list[np.ndarray], fmt: int, file_type: int, quality: int, flags: int, mip_mode: int = 2,
+                  filt: int = 4, blurriness: float = 0.9, gamma_filtering: bool = True, tiled: bool = False,
+                  max_levels: int = 16, min_mip_size: int = 1) -> bytes:
+    """crn_compress with crn_mipmap_params from the top level of each face -> .crn / .dds bytes."""
+    h, w = faces_top[0].shape[:2]
+    flat = np.concatenate([np.ascontiguousarray(im, dtype=np.uint8).reshape(-1) for im in faces_top])
+    cap = max(1 << 20, flat.size * 2)
+    out = np.zeros(cap, np.uint8)
+    size = lib().ref_compress_mips(flat.ctypes.data, w, h, len(faces_top), fmt, file_type, quality, flags, mip_mode,
+                                   filt, blurriness, int(gamma_filtering), int(tiled), max_levels, min_mip_size,
+                                   out.ctypes.data, cap)
+    if size == 0 or size > cap:
+        raise RuntimeError("reference crn_compress (mip params) failed")
+    return out[:size].tobytes()
+
+
+def crn_to_dds(crn: bytes) -> bytes:
+    buf = np.frombuffer(crn, np.uint8)
+    cap = 64 << 20
+    out = np.zeros(cap, np.uint8)
+    size = lib().ref_crn_to_dds(buf.ctypes.data, len(crn), out.ctypes.data, cap)
+    if size == 0 or size > cap:
+        raise RuntimeError("reference crn_decompress_crn_to_dds failed")
+    return out[:size].tobytes()
+
+
+def crnd_probe(crn: bytes):
+    """(values, segmented base file) from the reference's crnd header API (ref_crnd_probe)."""
+    buf = np.frombuffer(crn, np.uint8)
+    info = np.zeros(4096, np.uint32)
+    seg = np.zeros(len(crn), np.uint8)
+    n = lib().ref_crnd_probe(buf.ctypes.data, len(crn), info.ctypes.data, seg.ctypes.data, len(crn))
+    values = [int(v) for v in info[:n]]
+    base = values[-2]
+    return values, seg[:base].tobytes() if values[-1] else b""

@@ -13,6 +13,8 @@
 //   crnd_get_texture_info / crnd_get_level_info              inc/crn_defs.h:152-160
 //   crnlib::dxt_hc::compress (clustered DXT1)                 crnlib/crn_dxt_hc.cpp:97-316
 //   crnlib::image_utils::resample_multithreaded (mip levels)   crnlib/crn_image_utils.cpp:662-874
+//   crn_compress with crn_mipmap_params, crn_decompress_crn_to_dds   inc/crnlib.h:614-620
+//   crnd_validate_file / _get_level_data / segmented files        inc/crn_defs.h:153-221
 #include <cstdint>
 #include <cstring>
 #include <cstdlib>
@@ -332,6 +334,93 @@ int ref_resample(const uint8_t* rgba, uint32_t w, uint32_t h, uint32_t dst_w, ui
   if (!crnlib::image_utils::resample_multithreaded(src, dst, rp)) return 0;
   for (uint32_t y = 0; y < dst_h; y++) std::memcpy(out + (size_t)y * dst_w * 4, dst.get_scanline(y), (size_t)dst_w * 4);
   return 1;
+}
+
+// crn_compress with mip parameters (inc/crnlib.h:614, crnlib/crn_texture_comp.cpp:580-613):
+// faces top-level RGBA8 images (w x h each, face after face) and the crn_mipmap_params fields that
+// mip generation reads. Returns the file size (0 on failure); copied to out when it fits.
+uint32_t ref_compress_mips(const uint8_t* rgba_faces, uint32_t width, uint32_t height, uint32_t faces, uint32_t fmt,
+                           uint32_t file_type, uint32_t quality, uint32_t flags, uint32_t mip_mode, uint32_t filter,
+                           float blurriness, uint32_t gamma_filtering, uint32_t tiled, uint32_t max_levels,
+                           uint32_t min_mip_size, uint8_t* out, uint32_t out_cap) {
+  crn_comp_params p;
+  p.m_file_type = file_type ? cCRNFileTypeDDS : cCRNFileTypeCRN;
+  p.m_width = width;
+  p.m_height = height;
+  p.m_levels = 1;
+  p.m_faces = faces;
+  p.m_format = static_cast<crn_format>(fmt);
+  p.m_flags = flags;
+  p.m_quality_level = quality;
+  for (uint32_t f = 0; f < faces; f++)
+    p.m_pImages[f][0] = reinterpret_cast<const crn_uint32*>(rgba_faces + (size_t)f * width * height * 4);
+  crn_mipmap_params mp;
+  mp.m_mode = static_cast<crn_mip_mode>(mip_mode);
+  mp.m_filter = static_cast<crn_mip_filter>(filter);
+  mp.m_blurriness = blurriness;
+  mp.m_gamma_filtering = gamma_filtering;
+  mp.m_tiled = tiled;
+  mp.m_max_levels = max_levels;
+  mp.m_min_mip_size = min_mip_size;
+  crn_uint32 size = 0;
+  void* data = crn_compress(p, mp, size);
+  if (!data) return 0;
+  if (size <= out_cap && out) memcpy(out, data, size);
+  crn_free_block(data);
+  return size;
+}
+
+// crn_decompress_crn_to_dds (inc/crnlib.h:620, crnlib/crnlib.cpp:269-292). Returns the .dds size
+// (0 on failure); copied to out when it fits.
+uint32_t ref_crn_to_dds(const uint8_t* crn, uint32_t crn_size, uint8_t* out, uint32_t out_cap) {
+  crn_uint32 size = crn_size;
+  void* data = crn_decompress_crn_to_dds(crn, size);
+  if (!data) return 0;
+  if (size <= out_cap && out) memcpy(out, data, size);
+  crn_free_block(data);
+  return size;
+}
+
+// The crnd header API on one file (inc/crn_defs.h:139-221): writes to info[] the validate result
+// and every crn_file_info field, every crn_texture_info field, each level's crn_level_info fields
+// and crnd_get_level_data size, crnd_get_segmented_file_size and the crnd_create_segmented_file
+// result; the segmented base file goes to seg (when it fits in seg_cap). Returns the number of
+// values written.
+uint32_t ref_crnd_probe(const uint8_t* crn, uint32_t crn_size, uint32_t* info, uint8_t* seg, uint32_t seg_cap) {
+  uint32_t n = 0;
+  crnd::crn_file_info fi;
+  info[n++] = crnd::crnd_validate_file(crn, crn_size, &fi) ? 1u : 0u;
+  const uint32_t* f = reinterpret_cast<const uint32_t*>(&fi);
+  for (size_t k = 0; k < sizeof(fi) / 4; k++) info[n++] = f[k];
+  crnd::crn_texture_info ti;
+  info[n++] = crnd::crnd_get_texture_info(crn, crn_size, &ti) ? 1u : 0u;
+  info[n++] = ti.m_width;
+  info[n++] = ti.m_height;
+  info[n++] = ti.m_levels;
+  info[n++] = ti.m_faces;
+  info[n++] = ti.m_bytes_per_block;
+  info[n++] = ti.m_userdata0;
+  info[n++] = ti.m_userdata1;
+  info[n++] = (uint32_t)ti.m_format;
+  for (uint32_t l = 0; l < ti.m_levels; l++) {
+    crnd::crn_level_info li;
+    info[n++] = crnd::crnd_get_level_info(crn, crn_size, l, &li) ? 1u : 0u;
+    info[n++] = li.m_width;
+    info[n++] = li.m_height;
+    info[n++] = li.m_faces;
+    info[n++] = li.m_blocks_x;
+    info[n++] = li.m_blocks_y;
+    info[n++] = li.m_bytes_per_block;
+    info[n++] = (uint32_t)li.m_format;
+    crn_uint32 sz = 0;
+    const void* p = crnd::crnd_get_level_data(crn, crn_size, l, &sz);
+    info[n++] = p ? (uint32_t)(static_cast<const uint8_t*>(p) - crn) : 0xFFFFFFFFu;
+    info[n++] = sz;
+  }
+  const uint32_t base = crnd::crnd_get_segmented_file_size(crn, crn_size);
+  info[n++] = base;
+  info[n++] = (base <= seg_cap && crnd::crnd_create_segmented_file(crn, crn_size, seg, seg_cap)) ? 1u : 0u;
+  return n;
 }
 
 }  // extern "C"

@@ -226,6 +226,77 @@ def make_qdxt() -> None:
         json.dump(out, fh, indent=1, sort_keys=True)
 
 
+# crnlib-compatible API cases: (name, width, height, format, faces, content, seed, quality). The DDS
+# files are written by the reference's crn_compress at quality 255 (plain encode, endpoint caching
+# off so the blocks do not depend on encode order) and compared whole; at quality 128 (clustered
+# DXT1) only the header and size are pinned.
+FMT_ALL = dict(FMT, DXT5_CCxY=3, DXT5_xGxR=4, DXT5_xGBR=5, DXT5_AGBR=6)
+COMPAT_DDS_CASES = [
+    ("dds_dxt1_256", 256, 256, "DXT1", 1, "colour", 10, 255),
+    ("dds_dxt1_100x60", 100, 60, "DXT1", 1, "colour", 11, 255),
+    ("dds_dxt1_cube_32", 32, 32, "DXT1", 6, "colour", 12, 255),
+    ("dds_dxt5_128", 128, 128, "DXT5", 1, "colour_alpha", 13, 255),
+    ("dds_dxn_xy_128", 128, 128, "DXN_XY", 1, "normal", 15, 255),
+    ("dds_dxn_yx_64", 64, 64, "DXN_YX", 1, "normal", 17, 255),
+    ("dds_dxt5a_128", 128, 128, "DXT5A", 1, "colour_alpha", 16, 255),
+    ("dds_ccxy_64", 64, 64, "DXT5_CCxY", 1, "colour_alpha", 18, 255),
+    ("dds_xgxr_64", 64, 64, "DXT5_xGxR", 1, "normal", 19, 255),
+    ("dds_xgbr_64", 64, 64, "DXT5_xGBR", 1, "colour_alpha", 20, 255),
+    ("dds_agbr_64", 64, 64, "DXT5_AGBR", 1, "colour_alpha", 21, 255),
+    ("dds_qdxt_dxt1_256", 256, 256, "DXT1", 1, "colour", 10, 128),
+]
+# crn_compress with crn_mipmap_params, mips generated from the top level: (name, w, h, format,
+# content, seed, file type, quality, mip mode, filter, blurriness, gamma filtering, tiled, max levels,
+# min mip size)
+COMPAT_MIP_CASES = [
+    ("mips_dds_dxt1_kaiser_256", 256, 256, "DXT1", "colour", 30, 1, 255, 2, 4, 0.9, True, False, 16, 1),
+    ("mips_dds_dxt5_box_wrap_128x64", 128, 64, "DXT5", "colour_alpha", 31, 1, 255, 0, 0, 1.0, False, True, 5, 1),
+    ("mips_dds_dxt1_tent_min8_96", 96, 96, "DXT1", "colour", 32, 1, 255, 0, 1, 0.9, True, False, 16, 8),
+    ("mips_crn_dxt1_kaiser_128", 128, 128, "DXT1", "colour", 33, 0, 128, 2, 4, 0.9, True, False, 16, 1),
+]
+
+
+def dds_flags(content: str, quality: int) -> int:
+    base = FLAG_HIERARCHICAL | FLAG_BOTH_BLOCK_TYPES | FLAG_NO_ENDPOINT_CACHING
+    return base | (0 if content == "normal" else FLAG_PERCEPTUAL)
+
+
+def make_compat() -> None:
+    """Reference outputs for the crnlib-compatible C++ API: whole .dds files of crn_compress (plain
+    path, all formats incl. the swizzled DXT5 ones; cube and odd sizes), the clustered DDS header,
+    crn_compress with generated mips, crn_decompress_crn_to_dds of every committed .crn, and the
+    crnd header API (validate, texture / level info, level data, segmented files) on them."""
+    out = {"dds": {}, "mips": {}, "crn_to_dds": {}, "crnd": {}}
+    for name, w, h, fmt, faces, content, seed, q in COMPAT_DDS_CASES:
+        fl = texture_levels(w, h, content, seed, faces)
+        dds = ref.compress_texture(fl, FMT_ALL[fmt], 1, q, dds_flags(content, q), DXT_UBER, 7)
+        out["dds"][name] = {"width": w, "height": h, "format": fmt, "faces": faces, "content": content, "seed": seed,
+                            "quality": q, "flags": dds_flags(content, q), "size": len(dds),
+                            "header": dds[:128].hex(), "sha256": sha(np.frombuffer(dds, np.uint8)),
+                            "input_sha256": sha(np.concatenate([im.reshape(-1) for f in fl for im in f]))}
+        print(name, len(dds), flush=True)
+    for name, w, h, fmt, content, seed, ft, q, mode, filt, blur, gamma, tiled, maxl, minsz in COMPAT_MIP_CASES:
+        top = texture_levels(w, h, content, seed, 1)[0][0]
+        flags = dds_flags(content, q)
+        data = ref.compress_mips([top], FMT_ALL[fmt], ft, q, flags, mode, filt, blur, gamma, tiled, maxl, minsz)
+        out["mips"][name] = {"width": w, "height": h, "format": fmt, "content": content, "seed": seed, "file_type": ft,
+                             "quality": q, "flags": flags, "mip_mode": mode, "filter": filt, "blurriness": blur,
+                             "gamma_filtering": gamma, "tiled": tiled, "max_levels": maxl, "min_mip_size": minsz,
+                             "size": len(data), "sha256": sha(np.frombuffer(data, np.uint8)),
+                             "header": data[:128].hex() if ft == 1 else None}
+        print(name, len(data), flush=True)
+    for name in sorted(CASE[0] for CASE in CRN_CASES):
+        with open(os.path.join(HERE, "crn", name + ".crn"), "rb") as fh:
+            crn = fh.read()
+        dds = ref.crn_to_dds(crn)
+        out["crn_to_dds"][name] = {"size": len(dds), "sha256": sha(np.frombuffer(dds, np.uint8)),
+                                   "header": dds[:128].hex()}
+        values, seg = ref.crnd_probe(crn)
+        out["crnd"][name] = {"values": values, "segmented_sha256": sha(np.frombuffer(seg, np.uint8)) if seg else None}
+    with open(os.path.join(HERE, "compat_reference.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
 # mip generation cases: (name, width, height, content, seed, filter, filter scale, sRGB, wrap, comps)
 MIP_CASES = [("kaiser_64x48_rgba", 64, 48, "colour_alpha", 40, "kaiser", 0.9, True, False, 4),
              ("lanczos4_37x20_rgb", 37, 20, "colour", 41, "lanczos4", 1.0, True, False, 3),
@@ -312,10 +383,14 @@ if __name__ == "__main__":
     if sys.argv[1:] == ["qdxt"]:
         make_qdxt()
         sys.exit(0)
+    if sys.argv[1:] == ["compat"]:
+        make_compat()
+        sys.exit(0)
     make_blocks()
     make_crn()
     make_hc()
     make_config2()
     make_mips()
     make_qdxt()
+    make_compat()
     print("golden fixtures written to", HERE)

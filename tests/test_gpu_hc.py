@@ -103,6 +103,10 @@ def test_codebook_sizes_follow_quality(hc):
     assert lo[0] == 64 and lo[1] == 96
     hi = hc.codebook_sizes(64, 64, 255)
     assert hi[0] == 256 and hi[1] == 256
+    # the clamps use cCRNMinPaletteSize = 8: alpha endpoints reach 24 at quality 0, and an 8x8
+    # texture (4 blocks) gets the minimum of 8 entries everywhere at full quality
+    assert hc.codebook_sizes(1024, 1024, 0, hc.FMT_DXT5)[2:] == (24, 48)
+    assert hc.codebook_sizes(8, 8, 255) == (8, 8, 8, 8)
 
 
 @pytest.mark.parametrize("name", ["dxt5_256", "dxn_xy_256"])
