@@ -147,16 +147,19 @@ HC_CASES = [("dxt1_256", 256, 10), ("c1_dxt1_1024", 1024, 100), ("hc_128", 128, 
 HC_ALPHA_CASES = [("dxt5_256", "DXT5", 2, 256, 13, "colour_alpha"), ("dxn_xy_256", "DXN_XY", 7, 256, 15, "normal")]
 
 
-def make_hc() -> None:
+def make_hc(alpha_only: bool = False) -> None:
     """The reference's clustered DXT1 compressor (crnlib::dxt_hc::compress, run directly on blocks in
     crn_comp's layout at q128 codebook sizes): its tile count, codebook sizes and RGB RMSE, the
-    quality bar of the GPU clustered path."""
+    quality bar of the GPU clustered path. alpha_only rewrites only the alpha-format entries."""
     from crunch2_gb300 import hc
     from crunch2_gb300.hc import crn_layout
     sys.path.insert(0, os.path.dirname(HERE))
     from dxt_decode import rgb_rmse
     out = {}
-    for name, size, seed in HC_CASES:
+    if alpha_only:
+        with open(os.path.join(HERE, "hc_reference.json")) as fh:
+            out = {k: v for k, v in json.load(fh).items() if k in dict((c[0], c) for c in HC_CASES)}
+    for name, size, seed in ([] if alpha_only else HC_CASES):
         levels = texgen.mip_chain(texgen.colour_texture(size, size, seed))
         blocks, lv, vis = crn_layout([levels])
         ce, cs = hc.codebook_sizes(size, size, 128)[:2]
@@ -385,6 +388,9 @@ if __name__ == "__main__":
         sys.exit(0)
     if sys.argv[1:] == ["compat"]:
         make_compat()
+        sys.exit(0)
+    if sys.argv[1:] == ["hc_alpha"]:
+        make_hc(alpha_only=True)
         sys.exit(0)
     make_blocks()
     make_crn()
