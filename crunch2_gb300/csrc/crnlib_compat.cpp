@@ -13,6 +13,7 @@
 //   block compressor             crnlib/crnlib.cpp:351-418
 //   format helpers, strings      crnlib/crnlib.cpp:70-198, inc/crn_decomp.h:2567-2654
 //   crnd_* (transcoder API)      inc/crn_decomp.h:2657-2880, 4404-4487
+//   emscripten C exports         emscripten/crunch_lib.cpp:32-120
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -739,3 +740,38 @@ bool crnd_create_segmented_file(const void* pData, uint32 data_size, void* pBase
 }
 
 }  // namespace crnd
+
+// =============================================================================================
+// emscripten/crunch_lib.cpp's C exports. Geometry comes from crnd_get_texture_info (zeros when
+// the header is not a .crn); sizes use width >> level without the minimum of 1, as the wrapper
+// does.
+
+namespace {
+crnd::crn_texture_info wrapper_info(void* src, unsigned int src_size) {
+  crnd::crn_texture_info ti;
+  if (!crnd::crnd_get_texture_info(src, src_size, &ti)) {
+    std::memset(&ti, 0, sizeof(ti));
+    ti.m_struct_size = sizeof(ti);
+  }
+  return ti;
+}
+}  // namespace
+
+extern "C" unsigned int crn_get_width(void* src, unsigned int src_size) { return wrapper_info(src, src_size).m_width; }
+extern "C" unsigned int crn_get_height(void* src, unsigned int src_size) { return wrapper_info(src, src_size).m_height; }
+extern "C" unsigned int crn_get_levels(void* src, unsigned int src_size) { return wrapper_info(src, src_size).m_levels; }
+extern "C" unsigned int crn_get_dxt_format(void* src, unsigned int src_size) {
+  return (unsigned int)wrapper_info(src, src_size).m_format;
+}
+extern "C" unsigned int crn_get_bytes_per_block(void* src, unsigned int src_size) {
+  return crnd::crnd_get_bytes_per_dxt_block(wrapper_info(src, src_size).m_format);
+}
+extern "C" unsigned int crn_get_uncompressed_size(void* src, unsigned int src_size, unsigned int level) {
+  const crnd::crn_texture_info ti = wrapper_info(src, src_size);
+  const unsigned int w = level < 32 ? ti.m_width >> level : 0, h = level < 32 ? ti.m_height >> level : 0;
+  return ((w + 3) >> 2) * ((h + 3) >> 2) * crnd::crnd_get_bytes_per_dxt_block(ti.m_format);
+}
+extern "C" void crn_decompress(void* src, unsigned int src_size, void* dst, unsigned int dst_size,
+                               unsigned int firstLevel, unsigned int levelCount) {
+  crngpu_crn_decompress(src, src_size, dst, dst_size, firstLevel, levelCount);
+}

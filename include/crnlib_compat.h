@@ -317,6 +317,20 @@ CRN_EXPORT int crn_get_version_major();
 CRN_EXPORT int crn_get_version_minor();
 CRN_EXPORT int crn_get_version_patch();
 
+/* The emscripten wrapper's C exports (emscripten/crunch_lib.cpp:32-41), for JavaScript / WASM
+ * bindings and any other C FFI: texture geometry from the .crn header, and crn_decompress, which
+ * transcodes levels firstLevel .. firstLevel + levelCount - 1 of face 0 back to back into dst. */
+extern "C" {
+CRN_EXPORT unsigned int crn_get_width(void* src, unsigned int src_size);
+CRN_EXPORT unsigned int crn_get_height(void* src, unsigned int src_size);
+CRN_EXPORT unsigned int crn_get_levels(void* src, unsigned int src_size);
+CRN_EXPORT unsigned int crn_get_dxt_format(void* src, unsigned int src_size);
+CRN_EXPORT unsigned int crn_get_bytes_per_block(void* src, unsigned int src_size);
+CRN_EXPORT unsigned int crn_get_uncompressed_size(void* src, unsigned int src_size, unsigned int level);
+CRN_EXPORT void crn_decompress(void* src, unsigned int src_size, void* dst, unsigned int dst_size,
+                               unsigned int firstLevel, unsigned int levelCount);
+}
+
 namespace crnd {
 
 typedef unsigned char uint8;

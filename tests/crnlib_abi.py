@@ -110,6 +110,14 @@ SYMBOLS = {
                                     [vp, vp, u32, vp, u32, u32, u32]),
     "crnd_unpack_end": ("_ZN4crnd15crnd_unpack_endEPv", ctypes.c_bool, [vp]),
     "crnd_crn_format_to_fourcc": ("_ZN4crnd25crnd_crn_format_to_fourccE10crn_format", u32, [ctypes.c_int64]),
+    # emscripten/crunch_lib.cpp's extern "C" exports
+    "crn_get_width": ("crn_get_width", u32, [vp, u32]),
+    "crn_get_height": ("crn_get_height", u32, [vp, u32]),
+    "crn_get_levels": ("crn_get_levels", u32, [vp, u32]),
+    "crn_get_dxt_format": ("crn_get_dxt_format", u32, [vp, u32]),
+    "crn_get_bytes_per_block": ("crn_get_bytes_per_block", u32, [vp, u32]),
+    "crn_get_uncompressed_size": ("crn_get_uncompressed_size", u32, [vp, u32, u32]),
+    "crn_decompress": ("crn_decompress", None, [vp, u32, vp, u32, u32, u32]),
 }
 
 

@@ -103,6 +103,16 @@ def test_program_written_against_reference_headers_links(tmp_path, libpath):
     src.write_text(r"""
 #include "crnlib.h"
 #include "crn_defs.h"
+extern "C" {  // emscripten/crunch_lib.cpp:32-41
+unsigned int crn_get_width(void* src, unsigned int src_size);
+unsigned int crn_get_height(void* src, unsigned int src_size);
+unsigned int crn_get_levels(void* src, unsigned int src_size);
+unsigned int crn_get_dxt_format(void* src, unsigned int src_size);
+unsigned int crn_get_bytes_per_block(void* src, unsigned int src_size);
+unsigned int crn_get_uncompressed_size(void* p, unsigned int size, unsigned int level);
+void crn_decompress(void* src, unsigned int src_size, void* dst, unsigned int dst_size, unsigned int firstLevel,
+                    unsigned int levelCount);
+}
 typedef void* (*compress_a)(const crn_comp_params&, crn_uint32&, crn_uint32*, float*);
 typedef void* (*compress_b)(const crn_comp_params&, const crn_mipmap_params&, crn_uint32&, crn_uint32*, float*);
 void* volatile sink;
@@ -124,6 +134,9 @@ int main() {
   sink = (void*)&crnd::crnd_unpack_level_segmented; sink = (void*)&crnd::crnd_unpack_end;
   sink = (void*)&crnd::crnd_get_level_data; sink = (void*)&crnd::crnd_get_segmented_file_size;
   sink = (void*)&crnd::crnd_create_segmented_file;
+  sink = (void*)&crn_get_width; sink = (void*)&crn_get_height; sink = (void*)&crn_get_levels;
+  sink = (void*)&crn_get_dxt_format; sink = (void*)&crn_get_bytes_per_block; sink = (void*)&crn_get_uncompressed_size;
+  sink = (void*)&crn_decompress;
   return 0;
 }
 """)
@@ -175,3 +188,19 @@ def test_crnd_validate_rejects_corruption(api):
     assert not api.crnd_validate_file(buf, len(crn), None)
     fi.m_struct_size = 12  # wrong struct size is refused before any read
     assert not api.crnd_validate_file(buf, len(crn), ctypes.byref(fi))
+
+
+@pytest.mark.parametrize("name", sorted(G.manifest()))
+def test_emscripten_wrapper_geometry(api, name):
+    """emscripten/crunch_lib.cpp's C exports report the committed files' geometry."""
+    m = G.manifest()[name]
+    crn = G.crn_bytes(name)
+    fmt = {"DXT1": 0, "DXT5": 2, "DXN_XY": 7, "DXT5A": 9}[m["format"]]
+    assert api.crn_get_width(crn, len(crn)) == m["width"] and api.crn_get_height(crn, len(crn)) == m["height"]
+    assert api.crn_get_levels(crn, len(crn)) == len(m["levels"]) and api.crn_get_dxt_format(crn, len(crn)) == fmt
+    bpb = G.bytes_per_block(m["format"])
+    assert api.crn_get_bytes_per_block(crn, len(crn)) == bpb
+    for l, L in enumerate(m["levels"]):
+        w, h = m["width"] >> l, m["height"] >> l
+        assert api.crn_get_uncompressed_size(crn, len(crn), l) == ((w + 3) // 4) * ((h + 3) // 4) * bpb
+    assert api.crn_get_width(b"not a crn file at all, just bytes" * 4, 136) == 0

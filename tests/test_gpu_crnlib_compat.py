@@ -279,3 +279,21 @@ def test_block_compressor(api):
             api.crn_compress_block(ctx, src.ctypes.data, out[i].ctypes.data)
         api.crn_free_block_compressor(ctx)
         assert np.array_equal(out, cg.compress_blocks(blocks, fmt, flags).reshape(len(blocks), bpb))
+
+
+@pytest.mark.parametrize("name", ["c1_dxt1_1024", "dxt5_256", "dxn_xy_256", "dxt1_100x60"])
+def test_emscripten_crn_decompress(api, name):
+    """crn_decompress (the emscripten wrapper's transcode entry, by its own C name): levels of face
+    0 back to back, each the committed golden level."""
+    m = G.manifest()[name]
+    crn = G.crn_bytes(name)
+    first, count = 1, len(m["levels"]) - 1
+    sizes = [api.crn_get_uncompressed_size(crn, len(crn), l) for l in range(first, first + count)]
+    dst = np.zeros(sum(sizes), np.uint8)
+    api.crn_decompress(crn, len(crn), dst.ctypes.data, dst.size, first, count)
+    ofs = 0
+    for l, n in zip(range(first, first + count), sizes):
+        L = m["levels"][l]
+        if n:
+            assert n == L["bytes"] and G.sha(dst[ofs:ofs + n]) == L["sha256"], (name, l)
+        ofs += n
