@@ -110,7 +110,14 @@ struct WarpShared {
   uint32_t t_col[16][kBlocksPerWarp];
   uint8_t t_w[16][kBlocksPerWarp];
   float t_norm[3][16][kBlocksPerWarp];
+  // the chunk's 4x4 blocks (RGBA8, 64 bytes each), staged by one bulk copy (TMA) that completes
+  // on `bar`; the next chunk's copy is issued once phase 1 has read this one
+  __align__(16) uint8_t stage[kBlocksPerWarp * 64];
+  uint64_t bar;
 };
+
+// four CTAs of four warps per SM: 4 x (the CTA's warps + 1 KB reserved) within 228 KB
+static_assert(sizeof(WarpShared) * kWarpsPerCta + 1024 <= 57 * 1024, "DXT1 encoder shared memory per CTA");
 
 // ------------------------------------------------------------------------------------------
 // Phase 1 (one lane = one block).
@@ -166,9 +173,9 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
   int n = 0;
   uint32_t pix[16];
   {
-    const uint4* p4 = reinterpret_cast<const uint4*>(px);
+    const uint4* p4 = reinterpret_cast<const uint4*>(px);  // the staged copy in shared memory
     for (int q = 0; q < 4; q++) {
-      const uint4 v = __ldg(p4 + q);
+      const uint4 v = p4[q];
       pix[4 * q] = v.x; pix[4 * q + 1] = v.y; pix[4 * q + 2] = v.z; pix[4 * q + 3] = v.w;
     }
   }
@@ -1134,16 +1141,99 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
   return work;
 }
 
+// ---- TMA staging of a warp's chunk: cp.async.bulk global -> shared completing on an mbarrier.
+// The copy is 64 * cnt bytes from a 64-byte aligned block, so source, destination and size meet
+// the bulk copy's 16-byte rules. Waits are bounded: after kStageWaitLimit polls the warp stops
+// using the stage and reads its blocks from global memory (the results do not change), and the
+// event is counted in g_stage_timeouts.
+constexpr uint32_t kStageWaitLimit = 1u << 22;
+__device__ unsigned int g_stage_timeouts;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void stage_init(WarpShared& S) {
+  if (lane_id() == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+}
+
+// lane 0: announce the byte count and start the copy of cnt blocks from src into S.stage
+__device__ __forceinline__ void stage_issue(WarpShared& S, const uint8_t* src, uint32_t cnt) {
+  if (lane_id() == 0) {
+    const uint32_t bytes = cnt * 64u, bar = smem_u32(&S.bar);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier generic reads of the stage
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(S.stage)), "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+  }
+}
+
+// every lane: wait for the copy of the given phase parity; false after the poll limit
+__device__ __forceinline__ bool stage_wait(WarpShared& S, uint32_t parity) {
+  const uint32_t bar = smem_u32(&S.bar);
+  for (uint32_t i = 0; i < kStageWaitLimit; i++) {
+    uint32_t done;
+    asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    if (__all_sync(FULL_MASK, done != 0)) return true;
+  }
+  if (lane_id() == 0) atomicAdd(&g_stage_timeouts, 1u);
+  return false;
+}
+
+// A warp's sequence of chunks with the blocks of each staged in shared memory: the copy for chunk
+// i + 1 is issued as soon as phase 1 of chunk i has read the stage, so it overlaps phase 2.
+struct ChunkStager {
+  uint32_t parity = 0;
+  bool live = true;   // false after a timed-out wait: blocks are then read from global memory
+  bool pending = false;
+  __device__ void start(WarpShared& S, const uint8_t* src, uint32_t cnt) {
+    stage_init(S);
+    stage_issue(S, src, cnt);
+    pending = true;
+  }
+  // the staged blocks of the current chunk (or src itself when staging was abandoned)
+  __device__ const uint8_t* acquire(WarpShared& S, const uint8_t* src) {
+    if (live && pending) {
+      live = stage_wait(S, parity);
+      if (live) { parity ^= 1u; pending = false; }
+    }
+    return live ? S.stage : src;
+  }
+  __device__ void next(WarpShared& S, const uint8_t* src, uint32_t cnt) {
+    if (!live) return;
+    __syncwarp();  // every lane has read the stage
+    stage_issue(S, src, cnt);
+    pending = true;
+  }
+  // before the warp exits: a copy still in flight must land first (bounded)
+  __device__ void finish(WarpShared& S) {
+    if (pending) stage_wait(S, parity);
+  }
+};
+
 // cnt (<= kBlocksPerWarp) consecutive blocks from b0 on one warp; block k's result goes to
-// out + k * out_stride (and err_out[k]). Returns the candidate x colour evaluation count.
+// out + k * out_stride (and err_out[k]). staged holds the cnt blocks (shared memory, or the
+// global blocks themselves); after phase 1 has read them, issue_next() starts the next chunk's
+// copy. Returns the candidate x colour evaluation count.
+template <typename IssueNext>
 __device__ __forceinline__ unsigned long long dxt1_chunk(WarpShared& S, const uint8_t* __restrict__ blocks, uint32_t b0,
-                                                         uint32_t cnt, bool perceptual, bool hc, bool use_alpha,
+                                                         uint32_t cnt, const uint8_t* staged, IssueNext issue_next,
+                                                         bool perceptual, bool hc, bool use_alpha,
                                                          uint8_t* __restrict__ out, uint32_t out_stride,
                                                          uint64_t* __restrict__ err_out) {
   const uint32_t lane = lane_id();
   unsigned long long work = 0;
-  if (lane < cnt) phase1_block(S, lane, blocks + (size_t)(b0 + lane) * 64, perceptual);
+  if (lane < cnt) phase1_block(S, lane, staged + (size_t)lane * 64, perceptual);
   __syncwarp();
+  issue_next();
   #pragma unroll 1
   for (uint32_t k = 0; k < cnt; k++)
     work += phase2_block(S, k, blocks + (size_t)(b0 + k) * 64, perceptual, hc, use_alpha, out + (size_t)k * out_stride,
@@ -1162,12 +1252,24 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
   const uint32_t nwarps = gridDim.x * kWarpsPerCta;
   const uint32_t chunks = (n + kBlocksPerWarp - 1) / kBlocksPerWarp;
   unsigned long long work = 0;
+  auto chunk_count = [&](uint32_t chunk) { return min((uint32_t)kBlocksPerWarp, n - chunk * kBlocksPerWarp); };
+  ChunkStager st;
+  if (warp_global < chunks)
+    st.start(S, blocks + (size_t)warp_global * kBlocksPerWarp * 64, chunk_count(warp_global));
   for (uint32_t chunk = warp_global; chunk < chunks; chunk += nwarps) {
     const uint32_t b0 = chunk * kBlocksPerWarp;
-    const uint32_t cnt = min((uint32_t)kBlocksPerWarp, n - b0);
-    work += dxt1_chunk(S, blocks, b0, cnt, perceptual != 0, hc != 0, use_alpha != 0, out + (size_t)b0 * out_stride,
-                       out_stride, err_out ? err_out + b0 : nullptr);
+    const uint32_t cnt = chunk_count(chunk);
+    const uint8_t* staged = st.acquire(S, blocks + (size_t)b0 * 64);
+    const uint32_t nxt = chunk + nwarps;
+    work += dxt1_chunk(
+        S, blocks, b0, cnt, staged,
+        [&]() {
+          if (nxt < chunks) st.next(S, blocks + (size_t)nxt * kBlocksPerWarp * 64, chunk_count(nxt));
+        },
+        perceptual != 0, hc != 0, use_alpha != 0, out + (size_t)b0 * out_stride, out_stride,
+        err_out ? err_out + b0 : nullptr);
   }
+  st.finish(S);
   if (work_out) {
     for (int o = 16; o > 0; o >>= 1) work += __shfl_xor_sync(FULL_MASK, work, o);
     if (lane == 0 && work) atomicAdd(work_out, work);
@@ -1368,13 +1470,29 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
   WarpShared& S = reinterpret_cast<WarpShared*>(smem_raw)[threadIdx.x >> 5];
   const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const uint32_t nwarps = gridDim.x * kWarpsPerCta;
+  ChunkStager st;
+  if (warp_global < nchunks) {
+    const EncodeChunk c0 = chunks[warp_global];
+    st.start(S, blocks + (size_t)c0.first * 64, c0.count);
+  }
   for (uint32_t c = warp_global; c < nchunks; c += nwarps) {
     const EncodeChunk ch = chunks[c];
     const EncodeSegment sg = segs[ch.segment];
     const bool use_alpha = (sg.options & kSegThreeColour) != 0;
-    dxt1_chunk(S, blocks, ch.first, ch.count, (sg.options & kSegPerceptual) != 0, !use_alpha, use_alpha,
-               sg.out + (size_t)(ch.first - sg.first_block) * sg.stride, sg.stride, nullptr);
+    const uint8_t* staged = st.acquire(S, blocks + (size_t)ch.first * 64);
+    const uint32_t nxt = c + nwarps;
+    dxt1_chunk(
+        S, blocks, ch.first, ch.count, staged,
+        [&]() {
+          if (nxt < nchunks) {
+            const EncodeChunk cn = chunks[nxt];
+            st.next(S, blocks + (size_t)cn.first * 64, cn.count);
+          }
+        },
+        (sg.options & kSegPerceptual) != 0, !use_alpha, use_alpha,
+        sg.out + (size_t)(ch.first - sg.first_block) * sg.stride, sg.stride, nullptr);
   }
+  st.finish(S);
 }
 
 __global__ void __launch_bounds__(128)
