@@ -108,6 +108,8 @@ def lib():
     L.crngpu_unpack_batch_bytes.restype = i64
     L.crngpu_unpack_batch_tuning.argtypes = [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float), u32]
     L.crngpu_unpack_batch_tuning.restype = i32
+    L.crngpu_unpack_batch_set_variant.argtypes = [vp, i32]
+    L.crngpu_unpack_batch_set_variant.restype = i32
     L.crngpu_unpack_batch_destroy.argtypes = [vp]
     L.crngpu_unpack_batch_destroy.restype = i32
     L.crngpu_crn_decompress.argtypes = [vp, ctypes.c_uint, vp, ctypes.c_uint, ctypes.c_uint, ctypes.c_uint]
@@ -431,6 +433,10 @@ class UnpackBatch:
 
     def status(self, stream=None):
         _check(lib().crngpu_unpack_batch_status(self.handle, _stream_ptr(stream)), "crngpu_unpack_batch_status")
+
+    def set_variant(self, variant: int):
+        """Forces the expansion variant of later launches (-1: autotune again)."""
+        _check(lib().crngpu_unpack_batch_set_variant(self.handle, variant), "crngpu_unpack_batch_set_variant")
 
     def tuning(self):
         """(chosen expansion variant, measured ms per variant) of the autotuner (first launch)."""

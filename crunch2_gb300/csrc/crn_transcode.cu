@@ -81,7 +81,8 @@ constexpr uint32_t kExpandThreads = 256;
 // autotuner (crngpu_unpack_batch_launch, first launch) times all of them and keeps the fastest.
 constexpr int kTileSizes = 6;           // 1024 .. 32768 blocks per tile, processed 2048 at a time
 constexpr uint32_t kSubBlocks = 2048;   // blocks per pass of a CTA over its tile (8 per thread)
-constexpr int kExpandVariants = 2 * kTileSizes + 6;  // + pipelined tiles (2048 or 4096 blocks per pass)
+constexpr int kExpandVariants = 2 * kTileSizes + 9;  // + pipelined tiles, + TMA-staged records
+constexpr uint32_t kTmaSub = 2048;      // blocks per pass of the TMA variants (records staged per pass)
 constexpr uint32_t kStageMin = 1024;    // DXT1 tiles at least this large may stage their palettes
 // Decoder shared memory per CTA: five first-level tables + the row buffers of one texture's
 // levels (at most 2 x 1024 + 2 x 16 words for a 4096-texel-wide texture with 16 levels).
@@ -420,6 +421,115 @@ __device__ __forceinline__ void narrow_emit(const ExpandJob& J, uint32_t first, 
   }
 }
 
+// 8-byte blocks over [first, end) in passes of SUB blocks, the records of each pass brought into
+// shared memory by one bulk TMA copy (cp.async.bulk on an mbarrier, two buffers: the copy for
+// pass i + 1 is in flight while pass i gathers and stores). A copy starts at the pass's first
+// record rounded down to 16 bytes (the face's records may start mid-line; the up to three records
+// before it belong to the previous face of the same buffer) and ends at its last record rounded
+// down to 16 bytes; the up to three records after that are read from global memory. Waits are
+// bounded: a CTA whose wait runs out reads its records from global memory from then on (same
+// output) and counts the event in g_expand_stage_timeouts.
+__device__ unsigned int g_expand_stage_timeouts;
+constexpr uint32_t kExpandWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t shared_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+template <uint32_t SUB>
+__device__ __forceinline__ void narrow_tma(const ExpandJob& J, uint32_t first, uint32_t end, const uint32_t* s_ep,
+                                           const uint32_t* s_sel, uint32_t* s_rec, uint64_t* bars) {
+  constexpr uint32_t kPer = SUB / kExpandThreads;
+  constexpr uint32_t kBuf = SUB + 4;  // words per buffer: a pass plus up to 3 leading records
+  const uint32_t nblk = J.bx * J.by;
+  const uint32_t* rec = reinterpret_cast<const uint32_t*>(J.rec);
+  // [A, B): the 16-byte aligned byte range staged for the pass starting at f
+  auto range = [&](uint32_t f, uintptr_t& A, uintptr_t& B) {
+    A = reinterpret_cast<uintptr_t>(rec + f) & ~(uintptr_t)15;
+    B = reinterpret_cast<uintptr_t>(rec + min(end, f + SUB)) & ~(uintptr_t)15;
+    if (B < A) B = A;
+  };
+  auto issue = [&](uint32_t f, uint32_t buf) {
+    uintptr_t A, B;
+    range(f, A, B);
+    const uint32_t bytes = (uint32_t)(B - A), bar = shared_u32(&bars[buf]);
+    if (!bytes) return;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     shared_u32(s_rec + buf * kBuf)), "l"(A), "r"(bytes), "r"(bar)
+                 : "memory");
+  };
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(shared_u32(&bars[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(shared_u32(&bars[1])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t issued0 = 0, issued1 = 0, waited0 = 0, waited1 = 0;  // copies per buffer (same in every thread)
+  auto staged_bytes = [&](uint32_t f) {
+    uintptr_t A, B;
+    range(f, A, B);
+    return (uint32_t)(B - A);
+  };
+  if (threadIdx.x == 0) issue(first, 0);
+  if (staged_bytes(first)) issued0++;
+  bool live = true;
+  uint32_t i = 0;
+  for (uint32_t f = first; f < end; f += SUB, i++) {
+    const uint32_t buf = i & 1u;
+    const uint32_t nf = f + SUB;
+    if (live && nf < end) {
+      if (threadIdx.x == 0) issue(nf, buf ^ 1u);
+      if (staged_bytes(nf)) { if (buf) issued0++; else issued1++; }
+    }
+    uintptr_t A, B;
+    range(f, A, B);
+    if (live && B > A) {
+      bool done = false;
+      const uint32_t bar = shared_u32(&bars[buf]), parity = (buf ? waited1 : waited0) & 1u;
+      for (uint32_t k = 0; k < kExpandWaitLimit && !done; k++) {
+        uint32_t d;
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(d)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        done = d != 0;
+      }
+      live = __syncthreads_and(done) != 0;
+      if (live) { if (buf) waited1++; else waited0++; }
+      else if (threadIdx.x == 0) atomicAdd(&g_expand_stage_timeouts, 1u);
+    }
+    // records of this pass: staged words for [A, B), global memory for the rest
+    const uint32_t* st = s_rec + buf * kBuf;
+    uint32_t r[kPer];
+#pragma unroll
+    for (uint32_t k = 0; k < kPer / 2; k++) {
+#pragma unroll
+      for (uint32_t q = 0; q < 2; q++) {
+        const uint32_t b = f + 2 * (k * kExpandThreads + threadIdx.x) + q;
+        const uintptr_t addr = reinterpret_cast<uintptr_t>(rec + b);
+        uint32_t v = 0;
+        if (b < nblk) v = (live && addr >= A && addr < B) ? st[(addr - A) >> 2] : __ldg(rec + b);
+        r[2 * k + q] = v;
+      }
+    }
+    narrow_emit<kPer>(J, f, nblk, r, s_ep, s_sel);
+    __syncthreads();  // this buffer is read by all threads before it is refilled
+  }
+  // copies still in flight (only after a timed-out wait) land before the CTA exits (bounded)
+  for (uint32_t b = 0; b < 2; b++)
+    if ((b ? issued1 > waited1 : issued0 > waited0) && threadIdx.x == 0) {
+      const uint32_t bar = shared_u32(&bars[b]), parity = ((b ? issued1 : issued0) - 1) & 1u;
+      for (uint32_t k = 0; k < kExpandWaitLimit; k++) {
+        uint32_t d;
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(d)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (d) break;
+      }
+    }
+}
+
 // 8-byte blocks over [first, end) in passes of SUB blocks, the next pass's records loaded before
 // this pass's palette gathers and stores, so two dependent round trips overlap.
 template <uint32_t SUB>
@@ -493,12 +603,17 @@ __device__ __forceinline__ void expand_tile(const ExpandJob& J, uint32_t first, 
 // Dynamic shared memory (STAGE): the staged DXT1 colour palettes, smem_words = the largest
 // n_cep + n_csel of the launch's DXT1 jobs. A CTA covers TILE blocks in passes of up to
 // kSubBlocks, so a large tile pays for the palette copy once.
-template <uint32_t TILE, bool STAGE, bool PIPE, uint32_t SUB = kSubBlocks>
-__global__ void __launch_bounds__(kExpandThreads) k_crn_expand_tiles(const ExpandJob* __restrict__ jobs,
+template <uint32_t TILE, bool STAGE, bool PIPE, uint32_t SUB = kSubBlocks, bool TMA = false>
+__global__ void __launch_bounds__(kExpandThreads, TMA ? 4 : 1) k_crn_expand_tiles(const ExpandJob* __restrict__ jobs,
                                                                       const uint2* __restrict__ tiles,
                                                                       uint32_t smem_words) {
-  extern __shared__ uint32_t s_pal[];
+  // dynamic shared memory: [TMA: 2 record buffers of SUB + 4 words, 2 mbarriers][STAGE: palettes]
+  extern __shared__ __align__(16) uint32_t s_dyn[];
   constexpr uint32_t kSub = TILE < SUB ? TILE : SUB;
+  constexpr uint32_t kTmaWords = TMA ? 2 * (kSub + 4) + 4 : 0;
+  uint32_t* s_rec = s_dyn;
+  uint64_t* s_bars = reinterpret_cast<uint64_t*>(s_dyn + (TMA ? 2 * (kSub + 4) : 0));
+  uint32_t* s_pal = s_dyn + kTmaWords;
   const uint2 t = tiles[blockIdx.x];  // (job, first block)
   const ExpandJob& J = jobs[t.x];
   const uint32_t nblk = J.bx * J.by;
@@ -510,14 +625,17 @@ __global__ void __launch_bounds__(kExpandThreads) k_crn_expand_tiles(const Expan
       for (uint32_t i = threadIdx.x; i < n_ep; i += kExpandThreads) s_pal[i] = __ldg(J.pal.colour_ep + i);
       for (uint32_t i = threadIdx.x; i < n_sel; i += kExpandThreads) s_pal[n_ep + i] = __ldg(J.pal.colour_sel + i);
       __syncthreads();
-      if (PIPE) narrow_pipelined<kSub>(J, t.y, end, s_pal, s_pal + n_ep);
+      if (TMA) narrow_tma<kSub>(J, t.y, end, s_pal, s_pal + n_ep, s_rec, s_bars);
+      else if (PIPE) narrow_pipelined<kSub>(J, t.y, end, s_pal, s_pal + n_ep);
       else for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, s_pal, s_pal + n_ep);
     } else {
-      if (PIPE) narrow_pipelined<kSub>(J, t.y, end, nullptr, nullptr);
+      if (TMA) narrow_tma<kSub>(J, t.y, end, nullptr, nullptr, s_rec, s_bars);
+      else if (PIPE) narrow_pipelined<kSub>(J, t.y, end, nullptr, nullptr);
       else for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, nullptr, nullptr);
     }
   } else if (J.kind == kKDxt5a) {
-    if (PIPE) narrow_pipelined<kSub>(J, t.y, end, nullptr, nullptr);
+    if (TMA) narrow_tma<kSub>(J, t.y, end, nullptr, nullptr, s_rec, s_bars);
+    else if (PIPE) narrow_pipelined<kSub>(J, t.y, end, nullptr, nullptr);
     else for (uint32_t f = t.y; f < end; f += kSub) expand_tile<false, kSub>(J, f, nullptr, nullptr);
   } else {
     for (uint32_t f = t.y; f < end; f += kSub) expand_tile<true, kSub>(J, f, nullptr, nullptr);
@@ -526,7 +644,9 @@ __global__ void __launch_bounds__(kExpandThreads) k_crn_expand_tiles(const Expan
 
 // variant v < 12: tile of 1024 << (v >> 1) blocks, palettes staged when v is odd; v = 12..15: the
 // 8192- and 16384-block tiles with the next pass's records loaded ahead (staged when v is odd);
-// v = 16, 17: 16384- and 32768-block tiles, pipelined, 4096-block passes (16 blocks per thread)
+// v = 16, 17: 16384- and 32768-block tiles, pipelined, 4096-block passes (16 blocks per thread);
+// v = 18..20: 16384-block tiles (palettes staged when v = 19) and 32768-block tiles whose records
+// come into shared memory by double-buffered TMA copies, 2048-block passes
 typedef void (*ExpandKernel)(const ExpandJob*, const uint2*, uint32_t);
 const ExpandKernel kExpandKernels[kExpandVariants] = {
     k_crn_expand_tiles<1024, false, false>,  k_crn_expand_tiles<1024, true, false>,
@@ -537,12 +657,18 @@ const ExpandKernel kExpandKernels[kExpandVariants] = {
     k_crn_expand_tiles<32768, false, false>, k_crn_expand_tiles<32768, true, false>,
     k_crn_expand_tiles<8192, false, true>,   k_crn_expand_tiles<8192, true, true>,
     k_crn_expand_tiles<16384, false, true>,  k_crn_expand_tiles<16384, true, true>,
-    k_crn_expand_tiles<16384, false, true, 4096>, k_crn_expand_tiles<32768, false, true, 4096>};
+    k_crn_expand_tiles<16384, false, true, 4096>, k_crn_expand_tiles<32768, false, true, 4096>,
+    k_crn_expand_tiles<16384, false, false, kTmaSub, true>, k_crn_expand_tiles<16384, true, false, kTmaSub, true>,
+    k_crn_expand_tiles<32768, false, false, kTmaSub, true>};
 // the tile-table index (tile of 1024 << i blocks) of each variant
-constexpr int kVariantTile[kExpandVariants] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 3, 3, 4, 4, 4, 5};
+constexpr int kVariantTile[kExpandVariants] = {0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 3, 3, 4, 4, 4, 5, 4, 4, 5};
 // whether a variant stages the DXT1 palettes in dynamic shared memory
-constexpr bool kVariantStage[kExpandVariants] = {false, true, false, true, false, true, false, true, false,
-                                                 true,  false, true, false, true, false, true, false, false};
+constexpr bool kVariantStage[kExpandVariants] = {false, true, false, true, false, true,  false, true, false, true, false,
+                                                 true,  false, true, false, true, false, false, false, true, false};
+// dynamic shared memory of a variant's TMA record buffers and barriers (bytes)
+constexpr uint32_t kVariantTmaBytes[kExpandVariants] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
+                                                        (2 * (kTmaSub + 4) + 4) * 4, (2 * (kTmaSub + 4) + 4) * 4,
+                                                        (2 * (kTmaSub + 4) + 4) * 4};
 int g_expand_variant[64] = {};  // per device: the autotuner's last choice (0 until tuned)
 
 // ------------------------------------------------------------------------------------------
@@ -785,8 +911,10 @@ int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
                                   (int)kDecodeSmemMax)) != cudaSuccess)
       return cuda_check(e, "decoder shared memory attribute");
     for (int v = 0; v < kExpandVariants; v++)
-      if (kVariantStage[v] && (e = cudaFuncSetAttribute(kExpandKernels[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)(2 * kMaxSyms * sizeof(uint32_t)))) != cudaSuccess)
+      if ((kVariantStage[v] || kVariantTmaBytes[v]) &&
+          (e = cudaFuncSetAttribute(kExpandKernels[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(kVariantTmaBytes[v] + (kVariantStage[v] ? 2 * kMaxSyms * sizeof(uint32_t) : 0)))) !=
+              cudaSuccess)
         return cuda_check(e, "expansion shared memory attribute");
     attr_set[dev] = true;
   }
@@ -826,7 +954,7 @@ int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStre
     const int v = variant >= 0 ? variant : g_expand_variant[dev & 63];
     const int ts = kVariantTile[v];
     const uint2* tiles = reinterpret_cast<const uint2*>(d_jobs + p.tile_ofs[ts]);
-    const size_t smem = kVariantStage[v] ? (size_t)p.pal_words * 4 : 0;
+    const size_t smem = kVariantTmaBytes[v] + (kVariantStage[v] ? (size_t)p.pal_words * 4 : 0);
     kExpandKernels[v]<<<p.tile_ctas[ts], kExpandThreads, smem, s>>>(ej, tiles, p.pal_words);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_expand_tiles");
   }
@@ -1175,6 +1303,19 @@ extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t fl
     if (e != cudaSuccess) { b->graph = nullptr; return cuda_check(e, "instantiate graph"); }
   }
   if ((e = cudaGraphLaunch(b->graph, s)) != cudaSuccess) return cuda_check(e, "graph launch");
+  return CRNGPU_OK;
+}
+
+extern "C" int crngpu_unpack_batch_set_variant(crngpu_unpack_batch batch, int32_t variant) {
+  clear_error();
+  UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
+  if (!b || b->magic != 0x42415443u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
+  if (variant < -1 || variant >= kExpandVariants) { set_error("no such expansion variant"); return CRNGPU_E_PARAM; }
+  b->variant = variant;  // -1: autotune again at the next launch
+  if (b->graph) {        // a captured graph holds the old variant's launch
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
   return CRNGPU_OK;
 }
 

@@ -386,9 +386,16 @@ CRNGPU_API int crngpu_unpack_batch_status(crngpu_unpack_batch batch, void* strea
  * Variants 0..11: tiles of 1024 << (v >> 1) blocks, DXT1 palettes staged in shared memory when v
  * is odd; 12..15: 8192- and 16384-block tiles whose next pass of index records is loaded before the
  * current pass's palette gathers (staged when v is odd); 16, 17: 16384- and 32768-block tiles,
- * pipelined, 4096-block passes. *variant (-1 before the first launch) and up to n measured times in
- * ms; returns the number of variants. */
+ * pipelined, 4096-block passes; 18..20: 16384-block (palettes staged when v = 19) and 32768-block
+ * tiles whose index records are brought into shared memory by double-buffered TMA bulk copies,
+ * 2048-block passes. *variant (-1 before the first launch) and up to n measured times in ms;
+ * returns the number of variants. */
 CRNGPU_API int crngpu_unpack_batch_tuning(crngpu_unpack_batch batch, int32_t* variant, float* ms, uint32_t n);
+
+/* Forces the expansion variant of later launches (0 .. number of variants - 1; -1 runs the
+ * autotuner again at the next launch); drops a captured graph. Every variant writes the same
+ * output: this exists to time and test them one by one. */
+CRNGPU_API int crngpu_unpack_batch_set_variant(crngpu_unpack_batch batch, int32_t variant);
 
 /* Total output bytes of the batch (sum of the items' level sizes). */
 CRNGPU_API int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch);

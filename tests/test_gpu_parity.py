@@ -152,6 +152,37 @@ def test_transcode_batch_mixed_formats(cg, use_graph):
         c.close()
 
 
+def test_transcode_batch_every_expansion_variant(cg):
+    """Every expansion variant (tile sizes, staged palettes, pipelined passes, TMA-staged records)
+    writes the golden levels of every fixture, cube faces whose records start mid-line included."""
+    man = G.manifest()
+    names = sorted(man)
+    ctxs = [cg.unpack_begin(G.crn_bytes(n)) for n in names]
+    outs = [torch.full((sum(l["bytes"] for l in man[n]["levels"]),), 0xCD, dtype=torch.uint8, device="cuda")
+            for n in names]
+    with cg.UnpackBatch([(c, 0, c.levels, o) for c, o in zip(ctxs, outs)]) as batch:
+        batch.launch()
+        batch.status()
+        nvar = len(batch.tuning()[1])
+        assert nvar == 21
+        for v in range(nvar):
+            batch.set_variant(v)
+            for o in outs:
+                o.fill_(0xCD)
+            batch.launch(use_graph=(v % 2 == 1))
+            batch.status()
+            for n, o in zip(names, outs):
+                host = o.cpu().numpy()
+                pos = 0
+                for lvl, info in enumerate(man[n]["levels"]):
+                    assert G.sha(host[pos:pos + info["bytes"]]) == info["sha256"], (v, n, lvl)
+                    pos += info["bytes"]
+        with pytest.raises(cg.CrnGpuError):
+            batch.set_variant(nvar)
+    for c in ctxs:
+        c.close()
+
+
 def test_transcode_batch_level_subset(cg):
     man = G.manifest()
     crn = G.crn_bytes("c1_dxt1_1024")
