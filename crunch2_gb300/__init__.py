@@ -522,8 +522,9 @@ def compress_crn_bitrate(faces_levels, target_bitrate: float, fmt: int = FMT_DXT
 def compress_dds_clustered(faces_levels, quality: int = 128, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES,
                            fmt: int = FMT_DXT1):
     """The block data of a DDS written by crn_compress (crngpu_compress_dds_clustered): clustered
-    (the reference's QDXT path, DXT1) below quality 255, the plain encoder at 255 (any format); every
-    face's mip chain, per level its visible blocks (numpy (n, bytes per block))."""
+    (the reference's QDXT path: qdxt1 on colour, qdxt5 on alpha / DXN channels) below quality 255,
+    the plain encoder at 255; every face's mip chain, per level its visible blocks (numpy (n, bytes
+    per block))."""
     h, w = faces_levels[0][0].shape[:2]
     flat = np.concatenate([np.ascontiguousarray(im, dtype=np.uint8).reshape(-1) for face in faces_levels for im in face])
     L = lib()

@@ -434,6 +434,41 @@ struct TileCfg {
   int qdxt;             // qdxt1::init's tiling (crnlib/crn_qdxt1.cpp:100-330) instead of dxt_hc's
 };
 
+// dxt_fast::compress_alpha_block (crnlib/crn_dxt_fast.cpp:788-826): endpoints max / min of the
+// channel, selectors from the scaled distance to the minimum in three compare-and-subtract steps;
+// returns the squared error against dxt5_block::get_block_values of (max, min), the tile error of
+// qdxt5::init (crnlib/crn_qdxt5.cpp:180-200). sel48 (optional) gets the 16 3-bit selectors.
+__host__ __device__ uint32_t fast_alpha_error(int n, const uint32_t* px, int comp, uint64_t* sel48 = nullptr) {
+  auto chan = [&](int i) { return (int)((px[i] >> (8 * comp)) & 255u); };
+  int mn = chan(0), mx = mn;
+  for (int i = 1; i < n; i++) { mn = min(mn, chan(i)); mx = max(mx, chan(i)); }
+  const int l = mx, h = mn;
+  int c[8];
+  c[0] = l; c[1] = h;
+  if (l > h) {
+    for (int k = 1; k <= 6; k++) c[1 + k] = (l * (7 - k) + h * k) / 7;
+  } else {
+    for (int k = 1; k <= 4; k++) c[1 + k] = (l * (5 - k) + h * k) / 5;
+    c[6] = 0; c[7] = 255;
+  }
+  const int dist = mx - mn, bias = mn * 7 - (dist >> 1), dist4 = dist * 4, dist2 = dist * 2;
+  uint32_t err = 0;
+  uint64_t bits = 0;
+  for (int i = 0; i < n; i++) {
+    int a = chan(i) * 7 - bias, ind, t;
+    t = (dist4 - a) >> 31; ind = t & 4; a -= dist4 & t;
+    t = (dist2 - a) >> 31; ind += t & 2; a -= dist2 & t;
+    t = (dist - a) >> 31; ind += t & 1;
+    ind = -ind & 7;
+    ind ^= (2 > ind) ? 1 : 0;
+    const int d = chan(i) - c[ind];
+    err += (uint32_t)(d * d);
+    if (i < 16) bits |= (uint64_t)ind << (3 * i);
+  }
+  if (sel48) *sel48 = bits;
+  return err;
+}
+
 // dxt5_endpoint_optimizer::compute at quality Normal with 8-value blocks only, for the tile
 // decision (crn_dxt_hc.cpp:475-490): the smallest error over all pairs of the tile's unique
 // values (crnlib/crn_dxt5a.cpp:40-100, 198-262).
@@ -617,11 +652,25 @@ __host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint3
   for (int t = 0; t < 9; t++) {
     const int n = 16 << (t >> 2);
     if (cfg.has_color) terr[0][t] = fast_tile_error(n, px + tile_ofs[t], st);
-    for (int a = 0; a < cfg.num_alpha; a++) terr[1 + a][t] = alpha_tile_error(n, px + tile_ofs[t], cfg.comp[a]);
+    for (int a = 0; a < cfg.num_alpha; a++)
+      terr[1 + a][t] = cfg.qdxt ? fast_alpha_error(n, px + tile_ofs[t], cfg.comp[a])
+                                : alpha_tile_error(n, px + tile_ofs[t], cfg.comp[a]);
   }
   float best_q = 0.0f;
   int best_e = 0;
-  if (cfg.qdxt) {
+  if (cfg.qdxt && !cfg.has_color) {
+    // qdxt5::init (crnlib/crn_qdxt5.cpp:202-240): the same choice over the channel's 64 values
+    double best = -1.0;
+    for (int e = 0; e < 8; e++) {
+      uint32_t tot = 0;
+      for (int k = 0; k < layout_ntiles[e]; k++) tot += terr[1][layout_tiles[e][k]];
+      const double ms = tot * (1.0f / 64.0f);
+      double psnr = 999999.0f;
+      if (ms) psnr = fmin(fmax(log10(255.0f / sqrt(ms)) * 20.0f, 0.0), 500.0);
+      psnr = psnr - (double)derating[ch.level * 8 + e];
+      if (psnr > best) { best = psnr; best_e = e; }
+    }
+  } else if (cfg.qdxt) {
     // qdxt1::init: PSNR clamped to [0, 500] (999999 for no error) minus the layout's derating,
     // the largest wins
     double best = -1.0;
@@ -661,6 +710,20 @@ __host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint3
     T.chunk = c;
     T.kind = (uint32_t)t;
     T.weight = (float)n * lw;
+    if (cfg.qdxt && !cfg.has_color) {
+      // qdxt5: the representative pair of the channel's values (as grey pixels), weighted by the
+      // squared distance / 8, 1..8
+      uint32_t grey[64];
+      for (int i = 0; i < n; i++) grey[i] = ((px[tile_ofs[t] + i] >> (8 * cfg.comp[0])) & 255u) * 0x010101u;
+      int lo[3], hi[3];
+      find_rep_colors(n, grey, lo, hi);
+      const uint32_t dist = (uint32_t)((lo[0] - hi[0]) * (lo[0] - hi[0]));
+      const uint32_t w = dist / 8u < 1u ? 1u : dist / 8u > 8u ? 8u : dist / 8u;
+      T.va[0][0] = (float)lo[0];
+      T.va[0][1] = (float)hi[0];
+      T.weight = (float)(w * (uint32_t)(n / 16));
+      continue;
+    }
     if (cfg.qdxt) {
       // representative colours as the training vector of each of the tile's blocks, weighted by
       // their distance (squared RGB / 5000, 1..8)
@@ -683,6 +746,19 @@ __host__ __device__ int hc_tile_chunk(const uint32_t* __restrict__ blocks, uint3
       block_enc[blk] = (uint8_t)best_e;
     }
   return best_e;
+}
+
+// the dxt_fast alpha selectors of every block's channel comp (qdxt5::init's distinct-selector
+// count, crnlib/crn_qdxt5.cpp:400-422)
+__global__ void k_fast_alpha_selector_words(const uint32_t* __restrict__ blocks, uint32_t n, int comp,
+                                            unsigned long long* __restrict__ words) {
+  const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  uint32_t px[16];
+  for (int i = 0; i < 16; i++) px[i] = blocks[(size_t)b * 16 + i];
+  uint64_t w = 0;
+  fast_alpha_error(16, px, comp, &w);
+  words[b] = (unsigned long long)w;
 }
 
 // the dxt_fast selector word of every block (qdxt1::init's distinct-selector count)
@@ -2334,14 +2410,16 @@ __global__ void k_nearest_vec2(const Tile* __restrict__ tiles, const uint32_t* _
 }
 
 // alpha VQ input: (channel-major) the used tiles' vec2 with their pixel counts as weights
+// qdxt: the tile's training weight (qdxt5's distance weight x its blocks); else its pixel count
 __global__ void k_alpha_vectors(const Tile* __restrict__ tiles, const uint32_t* __restrict__ used, uint32_t nused,
-                                int num_alpha, float* __restrict__ vec, uint32_t* __restrict__ w, uint32_t* __restrict__ key_item) {
+                                int num_alpha, int qdxt, float* __restrict__ vec, uint32_t* __restrict__ w,
+                                uint32_t* __restrict__ key_item) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nused * (uint32_t)num_alpha) return;
   const uint32_t a = i / nused, t = used[i - a * nused];
   vec[2 * i] = tiles[t].va[a][0];
   vec[2 * i + 1] = tiles[t].va[a][1];
-  w[i] = tile_npix(tiles[t].kind);
+  w[i] = qdxt ? (uint32_t)tiles[t].weight : tile_npix(tiles[t].kind);
   key_item[i] = 2 * t + a;
 }
 __global__ void k_alpha_keys(const uint32_t* __restrict__ items, uint32_t n, const uint32_t* __restrict__ tile_ac,
@@ -2718,7 +2796,28 @@ struct HcMode {
   float quality = 1.0f;        // qdxt: quality level / 255
   float power_mul = 1.0f;      // qdxt: codebook-size curve exponent multiplier
   uint32_t selector_base = 0;  // qdxt: distinct dxt_fast selector words + 128
+  float derate_div = 3.1f;     // qdxt: per-level derating divisor (qdxt1 3.1, qdxt5 3.0)
 };
+
+// The number of distinct D-float training vectors (the size of the full codebook qdxt's tree
+// clusterizer reaches before it runs out of splits, crnlib/crn_qdxt1.cpp:335-345,
+// crnlib/crn_qdxt5.cpp:384-392); at most 65535 (cMaxEndpointClusters).
+uint32_t distinct_vectors(const float* d_vec, uint32_t n, int D, cudaStream_t s) {
+  std::vector<float> v((size_t)n * D);
+  if (!n || cudaMemcpyAsync(v.data(), d_vec, v.size() * sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return n;
+  std::vector<uint32_t> idx(n);
+  for (uint32_t i = 0; i < n; i++) idx[i] = i;
+  auto less = [&](uint32_t a, uint32_t b) {
+    return std::lexicographical_compare(&v[(size_t)a * D], &v[(size_t)a * D + D], &v[(size_t)b * D], &v[(size_t)b * D + D]);
+  };
+  std::sort(idx.begin(), idx.end(), less);
+  uint32_t d = n ? 1 : 0;
+  for (uint32_t i = 1; i < n; i++)
+    if (less(idx[i - 1], idx[i])) d++;
+  return std::min<uint32_t>(d, 65535u);
+}
 
 int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_t format, uint8_t* d_out,
                      uint16_t* d_endpoint_idx, uint16_t* d_selector_idx, uint32_t* d_endpoints, uint32_t* d_selectors,
@@ -2755,6 +2854,20 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
     const uint32_t k = (uint32_t)(sb * powf(mode.quality, 1.65f * mode.power_mul));
     return std::min(nvec, std::max(std::min(k, sb), std::min(128u, sb)));
   };
+  // qdxt5::pack (crnlib/crn_qdxt5.cpp:845-850): endpoints quality^2.1 of the full codebook, at
+  // least 16; selectors quality^1.65 of the distinct dxt_fast alpha selectors + 128, at least 32
+  auto ae_request = [&](uint32_t nvec) -> uint32_t {
+    if (!mode.qdxt) return std::min(nvec, P.alpha_endpoint_codebook_size);
+    const uint32_t cb = std::min<uint32_t>(nvec, 65535u);
+    const uint32_t k = (uint32_t)(cb * powf(mode.quality, 2.1f));
+    return std::max(std::min(k, cb), std::min(16u, cb));
+  };
+  auto as_request = [&](uint32_t nvec) -> uint32_t {
+    if (!mode.qdxt) return std::min(nvec, P.alpha_selector_codebook_size);
+    const uint32_t sb = mode.selector_base;
+    const uint32_t k = (uint32_t)(sb * powf(mode.quality, 1.65f));
+    return std::min(nvec, std::max(std::min(k, sb), std::min(32u, sb)));
+  };
   const int tile_derating[8] = {0, 1, 1, 2, 2, 2, 2, 3};
   for (int k = 0; k < 8; k++) cfg.alpha_derating[k] = P.adaptive_tile_alpha_psnr_derating * ((float)tile_derating[k] / 3.0f);
   // chunks of every level (block rows are processed in pairs; widths and heights are even)
@@ -2771,7 +2884,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
     lweight[l] = L.weight;
     // crn_dxt_hc.cpp:121-134: colour derating per level and layout
     float d = P.adaptive_tile_color_psnr_derating;
-    if (l && d > .25f) d = std::max(.25f, d / powf(mode.qdxt ? 3.1f : 3.0f, (float)l));  // qdxt1: 3.1
+    if (l && d > .25f) d = std::max(.25f, d / powf(mode.qdxt ? mode.derate_div : 3.0f, (float)l));
     for (int k = 0; k < 8; k++) derating[l * 8 + k] = 0.0f + (d - 0.0f) * ((float)tile_derating[k] / 3.0f);
     const uint32_t rows = L.num_blocks / L.block_width;
     for (uint32_t y = 0; y < rows; y += 2)
@@ -2856,8 +2969,9 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
       return cuda_check(e, "alloc vq input");
     k_tile_vectors<<<(nused + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused,
                                                         static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr));
+    const uint32_t ce_base = mode.qdxt ? distinct_vectors(static_cast<float*>(B.vec6.ptr), nused, 6, s) : nused;
     if ((rc = tree_vq<6>(static_cast<float*>(B.vec6.ptr), static_cast<uint32_t*>(B.w6.ptr), nused,
-                         ce_request(nused), frac, B.cb6, &K, s, B.vq)) != CRNGPU_OK)
+                         ce_request(ce_base), frac, B.cb6, &K, s, B.vq)) != CRNGPU_OK)
       return rc;
     if ((e = B.tile_cluster.ensure(4 * ntiles)) != cudaSuccess) return cuda_check(e, "alloc tile clusters");
     k_nearest_vec6<<<(ntiles + 255) / 256, 256, 0, s>>>(tiles, ntiles, static_cast<float*>(B.cb6.ptr), K,
@@ -2939,10 +3053,11 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
         (e = B.aitems.ensure(4 * nitem_t)) != cudaSuccess || (e = B.tile_ac.ensure(8 * ntiles)) != cudaSuccess)
       return cuda_check(e, "alloc alpha vq input");
     k_alpha_vectors<<<(nitem_t + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused, cfg.num_alpha,
-                                                          static_cast<float*>(B.avec.ptr), static_cast<uint32_t*>(B.aw.ptr),
+                                                          cfg.qdxt, static_cast<float*>(B.avec.ptr), static_cast<uint32_t*>(B.aw.ptr),
                                                           static_cast<uint32_t*>(B.aitems.ptr));
     if ((rc = tree_vq<2>(static_cast<float*>(B.avec.ptr), static_cast<uint32_t*>(B.aw.ptr), nitem_t,
-                         std::min(nused, P.alpha_endpoint_codebook_size), frac, B.cb2, &KA, s, B.vq)) != CRNGPU_OK)
+                         ae_request(mode.qdxt ? distinct_vectors(static_cast<float*>(B.avec.ptr), nitem_t, 2, s) : nused),
+                         frac, B.cb2, &KA, s, B.vq)) != CRNGPU_OK)
       return rc;
     k_nearest_vec2<<<(nitem_t + 255) / 256, 256, 0, s>>>(tiles, static_cast<uint32_t*>(B.used.ptr), nused, cfg.num_alpha,
                                                           static_cast<float*>(B.cb2.ptr), KA, static_cast<uint32_t*>(B.tile_ac.ptr));
@@ -2974,7 +3089,7 @@ int hc_compress_impl(const uint8_t* d_blocks, const crngpu_hc_params& P, uint32_
         static_cast<float*>(B.aselvec.ptr), static_cast<uint32_t*>(B.aselw.ptr));
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_alpha_block_selectors");
     if ((rc = tree_vq<16>(static_cast<float*>(B.aselvec.ptr), static_cast<uint32_t*>(B.aselw.ptr), nitem_b,
-                          std::min(nitem_b, P.alpha_selector_codebook_size), frac, B.acb16, &KAS, s, B.vq)) != CRNGPU_OK)
+                          as_request(nitem_b), frac, B.acb16, &KAS, s, B.vq)) != CRNGPU_OK)
       return rc;
     if ((e = B.acbsel.ensure(8 * KAS)) != cudaSuccess || (e = B.aitem_sel.ensure(4 * nitem_b)) != cudaSuccess ||
         (e = B.aentry_err.ensure(8 * 128 * (size_t)KAS)) != cudaSuccess)
@@ -3224,10 +3339,6 @@ extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uin
   using namespace crngpu;
   using namespace crngpu::hc;
   clear_error();
-  if (format != CRNGPU_FMT_DXT1 && quality_level < 255) {
-    set_error("crngpu_compress_dds_clustered: the clustered DDS path (quality below 255) is built for DXT1");
-    return CRNGPU_E_UNSUPPORTED;
-  }
   if (quality_level > 255) { set_error("crngpu_compress_dds_clustered: quality above 255"); return CRNGPU_E_PARAM; }
   if (format_is_non_srgb(format)) flags &= ~CRNGPU_FLAG_PERCEPTUAL;
   CrnSource src;
@@ -3239,6 +3350,16 @@ extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uin
     need += (uint64_t)((std::max(1u, width >> l) + 3) / 4) * ((std::max(1u, height >> l) + 3) / 4) * bpb * faces;
   const uint32_t N = src.P.num_blocks;
   cudaError_t e;
+  // elements of a block, each an 8-byte DXT1 or DXT5A element: (kind, channel, byte offset)
+  struct Element { uint32_t fmt; int comp; uint32_t ofs; };
+  std::vector<Element> elems;
+  switch (format) {
+    case CRNGPU_FMT_DXT1: elems = {{CRNGPU_FMT_DXT1, 0, 0}}; break;
+    case CRNGPU_FMT_DXT5A: elems = {{CRNGPU_FMT_DXT5A, 3, 0}}; break;
+    case CRNGPU_FMT_DXN_XY: elems = {{CRNGPU_FMT_DXT5A, 0, 0}, {CRNGPU_FMT_DXT5A, 1, 8}}; break;
+    case CRNGPU_FMT_DXN_YX: elems = {{CRNGPU_FMT_DXT5A, 1, 0}, {CRNGPU_FMT_DXT5A, 0, 8}}; break;
+    default: elems = {{CRNGPU_FMT_DXT5A, 3, 0}, {CRNGPU_FMT_DXT1, 0, 8}}; break;  // the DXT5 family
+  }
   if (quality_level >= 255) {
     // dds_comp at quality 255 (crnlib/crn_dds_comp.cpp:150-157): the plain encoder on every block
     // of the cooked source (as qdxt1::pack at full quality: every block its own cluster)
@@ -3246,38 +3367,70 @@ extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uin
                                          static_cast<uint8_t*>(src.d_out.ptr), CRNGPU_MEM_DEVICE, nullptr);
     if (r < 0) return r;
   } else {
-    // qdxt1::init's selector count: distinct dxt_fast selector words of the blocks, plus 128
+    // mipmapped_texture::qdxt_pack (crnlib/crn_mipmapped_texture.cpp:2330-2560): qdxt1 on the
+    // colour element, qdxt5 on each alpha / DXN element, each with its own tiling and codebooks;
+    // element k is written to d_out + k * N * 8 and interleaved below
     CrnDeviceBuffers& cb = crn_buffers();
-    if ((e = cb.st.ensure(sizeof(SolidTables))) != cudaSuccess || (e = cb.words.ensure(4ull * N)) != cudaSuccess)
+    if ((e = cb.st.ensure(sizeof(SolidTables))) != cudaSuccess || (e = cb.words.ensure(8ull * N)) != cudaSuccess)
       return cuda_check(e, "alloc selector words");
     if ((e = cudaMemcpy(cb.st.ptr, single_colour_tables_host(), sizeof(SolidTables), cudaMemcpyHostToDevice)) != cudaSuccess)
       return cuda_check(e, "upload tables");
-    k_fast_selector_words<<<(N + 255) / 256, 256>>>(static_cast<const uint32_t*>(src.d_in.ptr), N,
-                                                    static_cast<const SolidTables*>(cb.st.ptr),
-                                                    static_cast<uint32_t*>(cb.words.ptr));
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "k_fast_selector_words");
-    std::vector<uint32_t> words(N);
-    if ((e = cudaMemcpy(words.data(), cb.words.ptr, 4ull * N, cudaMemcpyDeviceToHost)) != cudaSuccess)
-      return cuda_check(e, "read selector words");
-    std::sort(words.begin(), words.end());
-    const uint32_t distinct = (uint32_t)(std::unique(words.begin(), words.end()) - words.begin());
-    HcMode mode;
-    mode.qdxt = true;
-    mode.quality = quality_level / 255.0f;
-    mode.power_mul = 1.0f;
-    mode.selector_base = distinct + 128;
-    src.P.adaptive_tile_color_psnr_derating = 1.5f;  // qdxt1::init
-    src.P.color_endpoint_codebook_size = 65535;
-    src.P.color_selector_codebook_size = 65535;
-    if ((rc = hc_compress_impl(static_cast<const uint8_t*>(src.d_in.ptr), src.P, CRNGPU_FMT_DXT1,
-                               static_cast<uint8_t*>(src.d_out.ptr), nullptr, nullptr, nullptr, nullptr, nullptr,
-                               nullptr, mode)) != CRNGPU_OK)
-      return rc;
+    for (size_t k = 0; k < elems.size(); k++) {
+      const Element& el = elems[k];
+      const bool colour = el.fmt == CRNGPU_FMT_DXT1;
+      // the distinct dxt_fast selector words of the blocks, plus 128 (qdxt1::init / qdxt5::init)
+      uint32_t distinct = 0;
+      if (colour) {
+        k_fast_selector_words<<<(N + 255) / 256, 256>>>(static_cast<const uint32_t*>(src.d_in.ptr), N,
+                                                        static_cast<const SolidTables*>(cb.st.ptr),
+                                                        static_cast<uint32_t*>(cb.words.ptr));
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "k_fast_selector_words");
+        std::vector<uint32_t> words(N);
+        if ((e = cudaMemcpy(words.data(), cb.words.ptr, 4ull * N, cudaMemcpyDeviceToHost)) != cudaSuccess)
+          return cuda_check(e, "read selector words");
+        std::sort(words.begin(), words.end());
+        distinct = (uint32_t)(std::unique(words.begin(), words.end()) - words.begin());
+      } else {
+        k_fast_alpha_selector_words<<<(N + 255) / 256, 256>>>(static_cast<const uint32_t*>(src.d_in.ptr), N, el.comp,
+                                                              static_cast<unsigned long long*>(cb.words.ptr));
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "k_fast_alpha_selector_words");
+        std::vector<unsigned long long> words(N);
+        if ((e = cudaMemcpy(words.data(), cb.words.ptr, 8ull * N, cudaMemcpyDeviceToHost)) != cudaSuccess)
+          return cuda_check(e, "read selector words");
+        std::sort(words.begin(), words.end());
+        distinct = (uint32_t)(std::unique(words.begin(), words.end()) - words.begin());
+      }
+      HcMode mode;
+      mode.qdxt = true;
+      mode.quality = quality_level / 255.0f;
+      // codebook curves of the colour element: deeper for DXT5's colour (favoured over alpha) and
+      // shallower for DXT5_CCxY's chroma (crnlib/crn_mipmapped_texture.cpp:2530-2544)
+      mode.power_mul = !colour ? 1.0f : format == CRNGPU_FMT_DXT5 ? .75f : format == CRNGPU_FMT_DXT5_CCXY ? 1.5f : 1.0f;
+      mode.selector_base = distinct + 128;
+      mode.derate_div = colour ? 3.1f : 3.0f;
+      crngpu_hc_params P = src.P;
+      // qdxt1::init derates colour layouts by 1.5, qdxt5::init alpha layouts by 2.4
+      P.adaptive_tile_color_psnr_derating = colour ? 1.5f : 2.4f;
+      P.color_endpoint_codebook_size = P.color_selector_codebook_size = 65535;
+      P.alpha_endpoint_codebook_size = P.alpha_selector_codebook_size = 65535;
+      P.alpha_component = (uint32_t)el.comp;
+      P.perceptual = colour ? src.P.perceptual : 0;
+      if ((rc = hc_compress_impl(static_cast<const uint8_t*>(src.d_in.ptr), P, el.fmt,
+                                 static_cast<uint8_t*>(src.d_out.ptr) + k * (size_t)N * 8, nullptr, nullptr, nullptr,
+                                 nullptr, nullptr, nullptr, mode)) != CRNGPU_OK)
+        return rc;
+    }
   }
   if (!out || out_capacity < need) return (int64_t)need;
   std::vector<uint8_t> dxt((size_t)N * bpb);
   if ((e = cudaMemcpy(dxt.data(), src.d_out.ptr, dxt.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
     return cuda_check(e, "copy result");
+  if (quality_level < 255 && elems.size() == 2) {  // element planes -> 16-byte blocks
+    std::vector<uint8_t> planes(dxt);
+    for (uint32_t b = 0; b < N; b++)
+      for (size_t k = 0; k < 2; k++)
+        std::memcpy(dxt.data() + (size_t)b * 16 + elems[k].ofs, planes.data() + (k * (size_t)N + b) * 8, 8);
+  }
   // DDS order: every face's mip chain, each level's visible blocks row by row
   uint8_t* o = static_cast<uint8_t*>(out);
   for (uint32_t f = 0; f < faces; f++)

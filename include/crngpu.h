@@ -190,17 +190,20 @@ CRNGPU_API int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t widt
                                        uint32_t faces, uint32_t format, uint32_t quality_level, uint32_t flags,
                                        void* out, uint64_t out_capacity);
 
-/* Clustered DDS, the reference's QDXT path (crn_compress with m_file_type = cCRNFileTypeDDS and
- * quality_level < 255: dds_comp -> mipmapped_texture::qdxt_pack -> qdxt1, crnlib/crn_dds_comp.cpp:
- * 150-205, crnlib/crn_qdxt1.cpp:81-1027) for DXT1: qdxt1's adaptive tiling (PSNR clamped to
- * [0, 500], derating 1.5 / 3.1^level), its representative-colour training vectors weighted by
- * endpoint distance, its codebook-size curves (endpoints: the full codebook x (q/255)^1.8, >= 96;
- * selectors: distinct selector words + 128, x (q/255)^1.65, >= 128), on this library's GPU
- * clusterizer, cluster fit and selector codebook. quality_level 255 is dds_comp's plain path for
- * every format (DXT1, the DXT5 family with the reference's source swizzles, DXN_XY/YX, DXT5A;
- * the perceptual flag is dropped for the non-sRGB formats, as crn_compress does). Output: the
- * blocks of every face's mip chain, each level's visible blocks row by row (the DDS data layout,
- * without the 128-byte header); returns their size (written when out_capacity suffices). */
+/* crn_compress to DDS (m_file_type = cCRNFileTypeDDS; dds_comp, crnlib/crn_dds_comp.cpp:150-205).
+ * quality_level 255: the plain encoder for every format (DXT1, the DXT5 family with the reference's
+ * source swizzles, DXN_XY/YX, DXT5A; the perceptual flag is dropped for the non-sRGB formats, as
+ * crn_compress does). Below 255, clustered DDS (mipmapped_texture::qdxt_pack,
+ * crnlib/crn_mipmapped_texture.cpp:2300-2600): qdxt1 (crnlib/crn_qdxt1.cpp:81-1027) on the colour
+ * element and qdxt5 (crnlib/crn_qdxt5.cpp:82-939) on each alpha / DXN element, each with its own
+ * adaptive tiling (PSNR clamped to [0, 500]; derating 1.5 / 3.1^level for colour, 2.4 / 3^level
+ * for alpha), representative-pair training vectors weighted by endpoint distance, and codebook
+ * curves (endpoints: the distinct training vectors x (q/255)^(1.8 m) >= 96 for colour, ^2.1 >= 16
+ * for alpha; selectors: the distinct dxt_fast selector words + 128, x (q/255)^(1.65 m) >= 128 for
+ * colour, >= 32 for alpha; m = .75 for DXT5's colour, 1.5 for DXT5_CCxY's, else 1), on this
+ * library's GPU clusterizer, cluster fit and selector codebooks. Output: the blocks of every
+ * face's mip chain, each level's visible blocks row by row (the DDS data layout, without the
+ * 128-byte header); returns their size (written when out_capacity suffices). */
 CRNGPU_API int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
                                                  uint32_t levels, uint32_t faces, uint32_t format,
                                                  uint32_t quality_level, uint32_t flags, void* out,

@@ -17,7 +17,6 @@
  *
  * Behaviour that differs from crnlib (all reported by returning NULL / false):
  *   - ETC formats, DXT3 and cCRNCompFlagDXT1AForTransparency are not encoded;
- *   - clustered DDS (quality < 255) is built for DXT1 only;
  *   - a target bitrate with DDS output is refused (crnlib estimates DDS bitrates with LZMA);
  *   - mip generation: gamma 2.2 only; no rescaling, cropping, clamping or renormalisation.
  * Plain encodes are always uber quality without endpoint caching, so m_dxt_quality and

@@ -199,6 +199,10 @@ def make_hc(alpha_only: bool = False) -> None:
 
 # clustered DDS (QDXT) cases: (name, size, seed, quality)
 QDXT_CASES = [("qdxt_256_q128", 256, 10, 128), ("qdxt_256_q64", 256, 10, 64), ("qdxt_1024_q128", 1024, 100, 128)]
+QDXT_ALPHA_CASES = [("qdxt_dxt5_256_q128", "DXT5", 256, 13, "colour_alpha", 128),
+                    ("qdxt_dxn_xy_256_q128", "DXN_XY", 256, 15, "normal", 128),
+                    ("qdxt_dxt5a_256_q128", "DXT5A", 256, 16, "colour_alpha", 128),
+                    ("qdxt_dxt5_256_q64", "DXT5", 256, 13, "colour_alpha", 64)]
 
 
 def make_qdxt() -> None:
@@ -225,6 +229,32 @@ def make_qdxt() -> None:
                      "distinct_selectors": int(np.unique(blocks[:, 4:].copy().view(np.uint32)).size),
                      "blocks_sha256": sha(blocks)}
         print(name, out[name], flush=True)
+    # the alpha-carrying formats (qdxt5 on each alpha / DXN element, qdxt1 on DXT5's colour)
+    import torch
+    from crunch2_gb300 import quality as Q
+    for name, fmt, size, seed, content, q in QDXT_ALPHA_CASES:
+        levels = texture_levels(size, size, content, seed, 1)[0]
+        flags = (0 if content == "normal" else FLAG_PERCEPTUAL) | FLAG_HIERARCHICAL | FLAG_BOTH_BLOCK_TYPES
+        t = time.time()
+        dds = ref.compress_texture([levels], FMT[fmt], 1, q, flags, DXT_UBER, 7)
+        secs = time.time() - t
+        bpb = 8 if fmt == "DXT5A" else 16
+        blocks = np.frombuffer(dds[128:], np.uint8).reshape(-1, bpb)
+        src = np.concatenate([texgen.image_blocks(im) for im in levels])
+        rec = {"size": size, "seed": seed, "quality": q, "format": fmt, "content": content, "flags": flags,
+               "blocks": int(src.shape[0]), "seconds_8_threads_x86": round(secs, 2)}
+        rec.update(Q.block_rmse(torch.from_numpy(blocks.copy()), torch.from_numpy(src), fmt))
+        for k in range(bpb // 8):
+            el = blocks[:, 8 * k:8 * k + 8].copy()
+            if fmt == "DXT5" and k == 1:
+                rec["distinct_colour_endpoints"] = int(np.unique(el[:, :4].view(np.uint32)).size)
+                rec["distinct_colour_selectors"] = int(np.unique(el[:, 4:].view(np.uint32)).size)
+            else:
+                rec[f"distinct_alpha_endpoints_{k}"] = int(np.unique(el[:, :2].view(np.uint16)).size)
+                sel = np.concatenate([el[:, 2:], np.zeros((el.shape[0], 2), np.uint8)], axis=1).view(np.uint64)
+                rec[f"distinct_alpha_selectors_{k}"] = int(np.unique(sel).size)
+        out[name] = rec
+        print(name, rec, flush=True)
     with open(os.path.join(HERE, "qdxt_reference.json"), "w") as fh:
         json.dump(out, fh, indent=1, sort_keys=True)
 

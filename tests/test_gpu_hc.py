@@ -272,3 +272,38 @@ def test_clustered_dds_full_quality_is_the_block_encoder(hc):
     want = np.concatenate([cg.compress_image(im, cg.FMT_DXT1, cg.FLAG_PERCEPTUAL | cg.FLAG_USE_BOTH_BLOCK_TYPES)
                            .reshape(-1, 8) for im in levels])
     assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("name", ["qdxt_dxt5_256_q128", "qdxt_dxn_xy_256_q128", "qdxt_dxt5a_256_q128",
+                                  "qdxt_dxt5_256_q64"])
+def test_clustered_dds_alpha_formats_match_reference_quality(hc, name):
+    """Clustered DDS for DXT5 (qdxt1 on the colour element, qdxt5 on alpha), DXN (qdxt5 on each
+    channel) and DXT5A against the reference's output on the same chain: per-element RMSE within
+    5% (+0.02 for the near-lossless alpha channels) and codebook sizes of the same order."""
+    import crunch2_gb300 as cg
+    from crunch2_gb300 import texgen
+    from crunch2_gb300 import quality as Q
+    R = qdxt_reference()[name]
+    img = texgen.normal_map(R["size"], R["size"], R["seed"]) if R["content"] == "normal" else \
+        texgen.colour_texture(R["size"], R["size"], R["seed"], with_alpha_noise=True)
+    levels = texgen.mip_chain(img)
+    fmt = {"DXT5": cg.FMT_DXT5, "DXN_XY": cg.FMT_DXN_XY, "DXT5A": cg.FMT_DXT5A}[R["format"]]
+    blocks = cg.compress_dds_clustered([levels], quality=R["quality"], flags=R["flags"] & 9, fmt=fmt)
+    src = np.concatenate([texgen.image_blocks(im) for im in levels])
+    assert blocks.shape[0] == R["blocks"] == src.shape[0]
+    ours = Q.block_rmse(torch.from_numpy(blocks.copy()), torch.from_numpy(src), R["format"])
+    stats = {}
+    for k in range(blocks.shape[1] // 8):
+        el = blocks[:, 8 * k:8 * k + 8].copy()
+        if R["format"] == "DXT5" and k == 1:
+            stats["distinct_colour_endpoints"] = int(np.unique(el[:, :4].view(np.uint32)).size)
+            stats["distinct_colour_selectors"] = int(np.unique(el[:, 4:].view(np.uint32)).size)
+        else:
+            stats[f"distinct_alpha_endpoints_{k}"] = int(np.unique(el[:, :2].view(np.uint16)).size)
+            sel = np.concatenate([el[:, 2:], np.zeros((el.shape[0], 2), np.uint8)], axis=1).view(np.uint64)
+            stats[f"distinct_alpha_selectors_{k}"] = int(np.unique(sel).size)
+    print(f"{name}: GPU {ours} {stats}; reference", {k: R[k] for k in list(ours) + list(stats)})
+    for key, v in ours.items():
+        assert v <= 1.05 * R[key] + (0.02 if key != "rmse_color" else 0.0), (key, v, R[key])
+    for key, v in stats.items():
+        assert v <= 2 * R[key] + 16, (key, v, R[key])
