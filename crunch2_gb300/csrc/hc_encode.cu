@@ -2807,6 +2807,19 @@ uint32_t distinct_vectors(const float* d_vec, uint32_t n, int D, cudaStream_t s)
   if (!n || cudaMemcpyAsync(v.data(), d_vec, v.size() * sizeof(float), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return n;
+  // qdxt's training vectors are 8-bit endpoint components: packed into one 64-bit key each
+  bool bytes = D <= 8;
+  for (size_t i = 0; i < v.size() && bytes; i++) bytes = v[i] >= 0.0f && v[i] <= 255.0f && v[i] == (float)(int)v[i];
+  if (bytes) {
+    std::vector<uint64_t> keys(n);
+    for (uint32_t i = 0; i < n; i++) {
+      uint64_t k = 0;
+      for (int c = 0; c < D; c++) k = (k << 8) | (uint64_t)(int)v[(size_t)i * D + c];
+      keys[i] = k;
+    }
+    std::sort(keys.begin(), keys.end());
+    return std::min<uint32_t>((uint32_t)(std::unique(keys.begin(), keys.end()) - keys.begin()), 65535u);
+  }
   std::vector<uint32_t> idx(n);
   for (uint32_t i = 0; i < n; i++) idx[i] = i;
   auto less = [&](uint32_t a, uint32_t b) {
