@@ -314,33 +314,67 @@ inline uint32_t colour_selector_cost(uint64_t a, uint64_t b) {
   return 5u * (uint32_t)__builtin_popcount(lo & ~hi) + 14u * (uint32_t)__builtin_popcount(hi & ~lo) +
          10u * (uint32_t)__builtin_popcount(lo & hi);
 }
+// the XOR-delta cost of four 3-bit selectors at once, {0, 2, 3, 3, 5, 5, 4, 4} per selector
+struct AlphaCost4 {
+  uint8_t t[4096];
+  AlphaCost4() {
+    static const uint8_t kCost[8] = {0, 2, 3, 3, 5, 5, 4, 4};
+    for (uint32_t x = 0; x < 4096; x++) t[x] = (uint8_t)(kCost[x & 7] + kCost[(x >> 3) & 7] + kCost[(x >> 6) & 7] + kCost[x >> 9]);
+  }
+};
 inline uint32_t alpha_selector_cost(uint64_t a, uint64_t b) {
-  static const uint8_t kCost[8] = {0, 2, 3, 3, 5, 5, 4, 4};
-  uint64_t x = a ^ b;
-  uint32_t c = 0;
-  for (int k = 0; k < 16; k++, x >>= 3) c += kCost[x & 7];
-  return c;
+  static const AlphaCost4 tab;
+  const uint64_t x = a ^ b;
+  return (uint32_t)tab.t[x & 4095] + tab.t[(x >> 12) & 4095] + tab.t[(x >> 24) & 4095] + tab.t[(x >> 36) & 4095];
 }
 
-// Nearest-neighbour chain: starting from `start_cost(i)` (the distance of entry i from an
-// all-zero entry), repeatedly take the closest remaining entry to the last one taken
-// (sort_color_endpoints / sort_alpha_endpoints / the selector sorts). Returns each entry's rank.
-template <class Start, class Dist>
-std::vector<uint32_t> nearest_chain(uint32_t n, Start start_cost, Dist dist) {
-  std::vector<uint32_t> rank(n), rem(n);
-  for (uint32_t i = 0; i < n; i++) rem[i] = i;
-  int64_t cur = -1;
+// Nearest-neighbour chain over payload values: starting from the entry with the smallest
+// start_cost (its distance from an all-zero entry), repeatedly take the remaining entry closest
+// (cost) to the last one taken (sort_color_endpoints / sort_alpha_endpoints / the selector
+// sorts). Returns each entry's rank.
+template <class T, class Start, class Cost>
+std::vector<uint32_t> nearest_chain(const std::vector<T>& payload, Start start_cost, Cost cost) {
+  // the remaining entries' ids and payloads are kept dense, in the order a swap-with-last removal
+  // leaves them, so the scan (and its first-minimum tie-break) visits them in that order
+  const uint32_t n = (uint32_t)payload.size();
+  std::vector<uint32_t> rank(n), id(n);
+  std::vector<T> val(payload);
+  for (uint32_t i = 0; i < n; i++) id[i] = i;
+  T cur{};
   for (uint32_t left = n; left; left--) {
     uint32_t best = 0, best_cost = UINT32_MAX;
-    for (uint32_t i = 0; i < left; i++) {
-      const uint32_t c = cur < 0 ? start_cost(rem[i]) : dist(rem[i], (uint32_t)cur);
-      if (c < best_cost) { best_cost = c; best = i; }
+    if (left == n) {
+      for (uint32_t i = 0; i < left; i++) {
+        const uint32_t c = start_cost(val[i]);
+        if (c < best_cost) { best_cost = c; best = i; }
+      }
+    } else {
+      for (uint32_t i = 0; i < left; i++) {
+        const uint32_t c = cost(val[i], cur);
+        if (c < best_cost) { best_cost = c; best = i; }
+      }
     }
-    cur = rem[best];
-    rank[rem[best]] = n - left;
-    rem[best] = rem[left - 1];
+    cur = val[best];
+    rank[id[best]] = n - left;
+    id[best] = id[left - 1];
+    val[best] = val[left - 1];
   }
   return rank;
+}
+
+// An endpoint as 8-bit components: (r, g, b) of both colour endpoints, or the two alphas.
+struct Comps {
+  int32_t c[6];
+};
+inline uint32_t comps_dist(const Comps& a, const Comps& b) {
+  uint32_t d = 0;
+  for (int k = 0; k < 6; k++) d += (uint32_t)((a.c[k] - b.c[k]) * (a.c[k] - b.c[k]));
+  return d;
+}
+inline uint32_t comps_norm(const Comps& a) {
+  uint32_t d = 0;
+  for (int k = 0; k < 6; k++) d += (uint32_t)(a.c[k] * a.c[k]);
+  return d;
 }
 
 // Symmetric counts of consecutive endpoint indices in the coded stream, as compressed rows.
@@ -355,13 +389,22 @@ struct Adjacency {
 // the two ends of the chain; the entry with the largest max(similarity) * (co-occurrence +
 // normaliser) is taken next, and joins the end whose half of the chain it co-occurs with more
 // (weighted toward the ends). The normaliser is the taken entry's co-occurrence << shift.
-template <class Dist>
-std::vector<uint32_t> grow_chain(uint32_t n, const Adjacency& adj, uint32_t first, uint32_t base, uint32_t cap,
-                                 int shift, Dist dist) {
-  std::vector<uint32_t> rem, freq(n, 0), sim_f(n, 0), sim_b(n, 0), row(n, 0), pos(n, UINT32_MAX), chain(2 * n + 1);
-  rem.reserve(n);
+std::vector<uint32_t> grow_chain(const std::vector<Comps>& u, const Adjacency& adj, uint32_t first, uint32_t base,
+                                 uint32_t cap, int shift) {
+  // per remaining entry (dense slots, swap-with-last removal): id, accumulated co-occurrence,
+  // similarity to the front and to the back of the chain, components
+  const uint32_t n = (uint32_t)u.size();
+  std::vector<uint32_t> id, freq, sim_f, sim_b, row(n, 0), pos(n, UINT32_MAX), chain(2 * n + 1);
+  std::vector<int32_t> cc[6];  // components, one array each, so the distance loops vectorise
+  id.reserve(n);
   for (uint32_t i = 0; i < n; i++)
-    if (i != first) rem.push_back(i);
+    if (i != first) {
+      id.push_back(i);
+      for (int k = 0; k < 6; k++) cc[k].push_back(u[i].c[k]);
+    }
+  freq.assign(id.size(), 0);
+  sim_f.assign(id.size(), 0);
+  sim_b.assign(id.size(), 0);
   uint32_t lo = n, hi = n;
   chain[n] = first;
   pos[first] = n;
@@ -369,21 +412,34 @@ std::vector<uint32_t> grow_chain(uint32_t n, const Adjacency& adj, uint32_t firs
     for (uint32_t k = adj.start[s]; k < adj.start[s + 1]; k++) row[adj.nb[k]] = on ? adj.count[k] : 0;
   };
   load(first, true);
-  uint32_t last = first, front = first, back = first;
+  uint32_t last = first;
+  Comps front = u[first], back = u[first];
   bool front_new = true, back_new = true;
   uint64_t normaliser = 0;
-  while (!rem.empty()) {
+  // similarity of every remaining entry to a new chain end
+  auto similarity = [&](const Comps& end, uint32_t* sim, size_t m) {
+    const int32_t e0 = end.c[0], e1 = end.c[1], e2 = end.c[2], e3 = end.c[3], e4 = end.c[4], e5 = end.c[5];
+    const int32_t *c0 = cc[0].data(), *c1 = cc[1].data(), *c2 = cc[2].data(), *c3 = cc[3].data(), *c4 = cc[4].data(),
+                  *c5 = cc[5].data();
+    for (size_t i = 0; i < m; i++) {
+      const int32_t d0 = c0[i] - e0, d1 = c1[i] - e1, d2 = c2[i] - e2, d3 = c3[i] - e3, d4 = c4[i] - e4, d5 = c5[i] - e5;
+      const uint32_t d = (uint32_t)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5);
+      sim[i] = base - (d < cap ? d : cap);
+    }
+  };
+  while (!id.empty()) {
+    const size_t m = id.size();
+    for (size_t i = 0; i < m; i++) freq[i] += row[id[i]];
+    if (front_new) similarity(front, sim_f.data(), m);
+    if (back_new) similarity(back, sim_b.data(), m);
     uint64_t best_val = 0;
     size_t best = 0;
-    for (size_t i = 0; i < rem.size(); i++) {
-      const uint32_t e = rem[i];
-      freq[e] += row[e];
-      if (front_new) sim_f[e] = base - std::min(cap, dist(e, front));
-      if (back_new) sim_b[e] = base - std::min(cap, dist(e, back));
-      const uint64_t v = (uint64_t)std::max(sim_f[e], sim_b[e]) * ((uint64_t)freq[e] + normaliser) + 1;
-      if (v > best_val || (v == best_val && e < rem[best])) { best_val = v; best = i; }
+    for (size_t i = 0; i < m; i++) {
+      const uint64_t v = (uint64_t)std::max(sim_f[i], sim_b[i]) * ((uint64_t)freq[i] + normaliser) + 1;
+      if (v > best_val || (v == best_val && id[i] < id[best])) { best_val = v; best = i; }
     }
-    const uint32_t s = rem[best];
+    const uint32_t s = id[best];
+    const uint32_t sf = sim_f[best], sb = sim_b[best], fs = freq[best];
     load(last, false);
     load(s, true);
     last = s;
@@ -397,14 +453,17 @@ std::vector<uint32_t> grow_chain(uint32_t n, const Adjacency& adj, uint32_t firs
       if (wf > 0) w_front += (uint64_t)wf * adj.count[k];
       if (wb > 0) w_back += (uint64_t)wb * adj.count[k];
     }
-    normaliser = (uint64_t)freq[s] << shift;
-    if ((uint64_t)sim_f[s] * w_front > (uint64_t)sim_b[s] * w_back) {
-      chain[--lo] = s; pos[s] = lo; front = s; front_new = true; back_new = false;
+    normaliser = (uint64_t)fs << shift;
+    if ((uint64_t)sf * w_front > (uint64_t)sb * w_back) {
+      chain[--lo] = s; pos[s] = lo; front = u[s]; front_new = true; back_new = false;
     } else {
-      chain[++hi] = s; pos[s] = hi; back = s; back_new = true; front_new = false;
+      chain[++hi] = s; pos[s] = hi; back = u[s]; back_new = true; front_new = false;
     }
-    rem[best] = rem.back();
-    rem.pop_back();
+    id[best] = id.back(); id.pop_back();
+    for (int k = 0; k < 6; k++) { cc[k][best] = cc[k].back(); cc[k].pop_back(); }
+    freq[best] = freq[m - 1]; freq.pop_back();
+    sim_f[best] = sim_f[m - 1]; sim_f.pop_back();
+    sim_b[best] = sim_b[m - 1]; sim_b.pop_back();
   }
   std::vector<uint32_t> rank(n);
   for (uint32_t p = lo; p <= hi; p++) rank[chain[p]] = p - lo;
@@ -540,17 +599,17 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
       // selectors: nearest-neighbour chain under the XOR-delta cost
       workers.emplace_back([&, m] {
         const std::vector<uint64_t>& v = sel_pal[m]->values;
-        if (m) sel_rank[m] = nearest_chain((uint32_t)v.size(), [&](uint32_t i) { return alpha_selector_cost(v[i], 0); },
-                                           [&](uint32_t i, uint32_t j) { return alpha_selector_cost(v[i], v[j]); });
-        else sel_rank[m] = nearest_chain((uint32_t)v.size(), [&](uint32_t i) { return colour_selector_cost(v[i], 0); },
-                                         [&](uint32_t i, uint32_t j) { return colour_selector_cost(v[i], v[j]); });
+        if (m) sel_rank[m] = nearest_chain(v, [](uint64_t a) { return alpha_selector_cost(a, 0); },
+                                           [](uint64_t a, uint64_t b) { return alpha_selector_cost(a, b); });
+        else sel_rank[m] = nearest_chain(v, [](uint64_t a) { return colour_selector_cost(a, 0); },
+                                         [](uint64_t a, uint64_t b) { return colour_selector_cost(a, b); });
       });
       workers.emplace_back([&, m, n] {
         // endpoints, unpacked to 8-bit components: colour (r, g, b) of both endpoints, or the two alphas
-        std::vector<int32_t> u((size_t)n * 6);
+        std::vector<Comps> u(n);
         for (uint32_t i = 0; i < n; i++) {
           const uint32_t v = (uint32_t)ep_pal[m]->values[i];
-          int32_t* c = &u[(size_t)i * 6];
+          int32_t* c = u[i].c;
           if (m) { c[0] = (int32_t)(v & 255u); c[1] = (int32_t)((v >> 8) & 255u); c[2] = c[3] = c[4] = c[5] = 0; continue; }
           for (int e = 0; e < 2; e++) {
             const uint32_t q = v >> (16 * e), r = (q >> 11) & 31, g = (q >> 5) & 63, bl = q & 31;
@@ -559,19 +618,6 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
             c[3 * e + 2] = (int32_t)((bl << 3) | (bl >> 2));
           }
         }
-        auto dist = [&](uint32_t i, uint32_t j) {
-          const int32_t* a = &u[(size_t)i * 6];
-          const int32_t* b = &u[(size_t)j * 6];
-          uint32_t d = 0;
-          for (int k = 0; k < 6; k++) d += (uint32_t)((a[k] - b[k]) * (a[k] - b[k]));
-          return d;
-        };
-        auto start = [&](uint32_t i) {
-          const int32_t* a = &u[(size_t)i * 6];
-          uint32_t d = 0;
-          for (int k = 0; k < 6; k++) d += (uint32_t)(a[k] * a[k]);
-          return d;
-        };
         // co-occurrence of consecutive endpoints in the delta-coded blocks, both directions,
         // sorted and run-length counted into rows
         std::vector<uint64_t> pairs;
@@ -612,10 +658,10 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         std::vector<uint32_t> trial[4];
         uint64_t bits[4];
         std::vector<std::thread> tw;
-        tw.emplace_back([&] { trial[0] = nearest_chain(n, start, dist); bits[0] = stream_bits(m, trial[0]); });
+        tw.emplace_back([&] { trial[0] = nearest_chain(u, comps_norm, comps_dist); bits[0] = stream_bits(m, trial[0]); });
         for (int t = 0; t < 3; t++)
           tw.emplace_back([&, t] {
-            trial[t + 1] = grow_chain(n, adj, first, (uint32_t)((float)unit * (1.0f + weights[t])), unit, m ? 0 : 3, dist);
+            trial[t + 1] = grow_chain(u, adj, first, (uint32_t)((float)unit * (1.0f + weights[t])), unit, m ? 0 : 3);
             bits[t + 1] = stream_bits(m, trial[t + 1]);
           });
         for (auto& w : tw) w.join();
