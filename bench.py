@@ -658,7 +658,9 @@ def main():
                                      "variants": "0-11: tile of 1024 << (v >> 1) blocks, DXT1 palettes staged "
                                                  "in shared memory when v is odd; 12-15: 8192/16384-block tiles "
                                                  "with the next pass's records loaded ahead (staged when odd); "
-                                                 "16, 17: 16384/32768-block tiles, pipelined, 4096-block passes"},
+                                                 "16, 17: 16384/32768-block tiles, pipelined, 4096-block passes; "
+                                                 "18-20: 16384/32768-block tiles, records staged by TMA bulk "
+                                                 "copies (palettes staged when v = 19), 2048-block passes"},
                  "workload": f"{TX_BATCH} contexts of the 1024x1024 q128 DXT1 .crn (11 levels, {len(crn)} bytes)"}
     expand = {"kernel": "k_crn_expand_tiles", "bound": "hbm", "unit": "GB/s",
               "ms": round(expand_ms, 4), "bytes_algorithmic": exp_bytes,
