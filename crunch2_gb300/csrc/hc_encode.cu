@@ -25,7 +25,7 @@
 //                     error tables; k_selector_finalise re-optimises each entry from them.
 //   k_hc_emit         the finished DXT1 blocks and per-block endpoint / selector indices.
 // The ETC paths of dxt_hc are out of scope. The reference is not bit-reproducible here (its
-// clusterizer result depends on the thread count), so this path is judged on quality.
+// clusterizer result depends on the thread count), so this path is compared on quality.
 #include <cuda_runtime.h>
 
 #include <algorithm>

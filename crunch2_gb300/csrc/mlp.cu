@@ -2,7 +2,7 @@
 // the 5th-generation tensor cores (tcgen05.mma, BF16 operands from shared memory, FP32
 // accumulators in tensor memory). This part has no counterpart in the reference; it replaces
 // the initial guess and most of the refinement of dxt1_endpoint_optimizer (crnlib/crn_dxt1.cpp)
-// for blocks where it is good enough, and the exact optimizer stays the fallback and the judge.
+// for blocks where it is good enough, and the exact optimizer stays the fallback and the arbiter of that error.
 //
 // Inputs: 16 texels x RGB scaled to [0, 1]. Outputs: y[0..5] = low/high endpoint (r/31, g/63,
 // b/31) of the plain optimizer's 4-colour solution, y[6] = log2(1 + block error)/16, the

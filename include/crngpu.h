@@ -109,7 +109,7 @@ CRNGPU_API int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, ui
  * Clustered (CRN-style) DXT1 compression: dxt_hc::compress (crnlib/crn_dxt_hc.cpp:97-316) for
  * cDXT1 on the GPU -- adaptive tiles, endpoint codebook VQ, per-cluster endpoint optimisation,
  * selector codebook VQ. The reference's clusterizer is not thread-count deterministic, so this
- * path is judged on quality (RGB RMSE at the same codebook sizes), not bit-exactness.
+ * path is compared on quality (RGB RMSE at the same codebook sizes), not bit-exactness.
  * --------------------------------------------------------------------------------------- */
 
 /* dxt_hc::params (crnlib/crn_dxt_hc.h:113-173) for DXT1. Blocks are in the crn_comp layout

@@ -208,7 +208,7 @@ QDXT_ALPHA_CASES = [("qdxt_dxt5_256_q128", "DXT5", 256, 13, "colour_alpha", 128)
 def make_qdxt() -> None:
     """The reference's clustered DDS (crn_compress with a DDS file type and quality < 255: its
     QDXT path) on colour mip chains: RGB RMSE of its DXT1 blocks over every level, the bar for the
-    GPU path (which is judged on quality, like the .crn clustering)."""
+    GPU path (which is compared on quality, like the .crn clustering)."""
     import time
     sys.path.insert(0, os.path.dirname(HERE))
     from dxt_decode import rgb_rmse

@@ -118,7 +118,7 @@ def test_crn_compress_with_generated_mips(api, name):
         assert data[:128].hex() == R["header"]
         assert size == R["size"] and sha(data) == R["sha256"]
     else:
-        # .crn: the clusterizer is judged on quality elsewhere; here the level chain and the file
+        # .crn: the clusterizer is compared on quality elsewhere; here the level chain and the file
         # must be exactly those of the C ABI fed with the GPU-generated chain
         import crunch2_gb300 as cg
         ti = A.CrnTextureInfo()
