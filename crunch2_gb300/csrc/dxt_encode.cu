@@ -1161,15 +1161,24 @@ __device__ __forceinline__ void stage_init(WarpShared& S) {
   __syncwarp();
 }
 
-// lane 0: announce the byte count and start the copy of cnt blocks from src into S.stage
-__device__ __forceinline__ void stage_issue(WarpShared& S, const uint8_t* src, uint32_t cnt) {
+// lane 0: announce the byte count and start the copy of cnt blocks into S.stage: block k comes
+// from src + k * stride blocks (stride 1: one copy of the whole run; else one 64-byte copy each)
+__device__ __forceinline__ void stage_issue(WarpShared& S, const uint8_t* src, uint32_t cnt, uint32_t stride = 1) {
   if (lane_id() == 0) {
-    const uint32_t bytes = cnt * 64u, bar = smem_u32(&S.bar);
+    const uint32_t bytes = cnt * 64u, bar = smem_u32(&S.bar), dst = smem_u32(S.stage);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier generic reads of the stage
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(S.stage)), "l"(src), "r"(bytes), "r"(bar)
-                 : "memory");
+    if (stride == 1) {
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                   "l"(src), "r"(bytes), "r"(bar)
+                   : "memory");
+    } else {
+      for (uint32_t k = 0; k < cnt; k++)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], 64, [%2];" ::"r"(
+                         dst + 64u * k),
+                     "l"(src + (size_t)k * stride * 64), "r"(bar)
+                     : "memory");
+    }
   }
 }
 
@@ -1194,23 +1203,24 @@ struct ChunkStager {
   uint32_t parity = 0;
   bool live = true;   // false after a timed-out wait: blocks are then read from global memory
   bool pending = false;
-  __device__ void start(WarpShared& S, const uint8_t* src, uint32_t cnt) {
+  __device__ void start(WarpShared& S, const uint8_t* src, uint32_t cnt, uint32_t stride = 1) {
     stage_init(S);
-    stage_issue(S, src, cnt);
+    stage_issue(S, src, cnt, stride);
     pending = true;
   }
-  // the staged blocks of the current chunk (or src itself when staging was abandoned)
-  __device__ const uint8_t* acquire(WarpShared& S, const uint8_t* src) {
+  // the staged blocks of the current chunk, or nullptr once staging was abandoned (the caller then
+  // reads the blocks from global memory)
+  __device__ const uint8_t* acquire(WarpShared& S) {
     if (live && pending) {
       live = stage_wait(S, parity);
       if (live) { parity ^= 1u; pending = false; }
     }
-    return live ? S.stage : src;
+    return live ? S.stage : nullptr;
   }
-  __device__ void next(WarpShared& S, const uint8_t* src, uint32_t cnt) {
+  __device__ void next(WarpShared& S, const uint8_t* src, uint32_t cnt, uint32_t stride = 1) {
     if (!live) return;
     __syncwarp();  // every lane has read the stage
-    stage_issue(S, src, cnt);
+    stage_issue(S, src, cnt, stride);
     pending = true;
   }
   // before the warp exits: a copy still in flight must land first (bounded)
@@ -1225,19 +1235,23 @@ struct ChunkStager {
 // copy. Returns the candidate x colour evaluation count.
 template <typename IssueNext>
 __device__ __forceinline__ unsigned long long dxt1_chunk(WarpShared& S, const uint8_t* __restrict__ blocks, uint32_t b0,
-                                                         uint32_t cnt, const uint8_t* staged, IssueNext issue_next,
-                                                         bool perceptual, bool hc, bool use_alpha,
+                                                         uint32_t bstride, uint32_t cnt, const uint8_t* staged,
+                                                         IssueNext issue_next, bool perceptual, bool hc, bool use_alpha,
                                                          uint8_t* __restrict__ out, uint32_t out_stride,
                                                          uint64_t* __restrict__ err_out) {
+  // the chunk's blocks are b0, b0 + bstride, ...; out and err_out point at block b0's result;
+  // staged holds them packed (nullptr: read them from global memory)
   const uint32_t lane = lane_id();
   unsigned long long work = 0;
-  if (lane < cnt) phase1_block(S, lane, staged + (size_t)lane * 64, perceptual);
+  if (lane < cnt)
+    phase1_block(S, lane, staged ? staged + (size_t)lane * 64 : blocks + ((size_t)b0 + (size_t)lane * bstride) * 64,
+                 perceptual);
   __syncwarp();
   issue_next();
   #pragma unroll 1
   for (uint32_t k = 0; k < cnt; k++)
-    work += phase2_block(S, k, blocks + (size_t)(b0 + k) * 64, perceptual, hc, use_alpha, out + (size_t)k * out_stride,
-                         err_out ? err_out + k : nullptr);
+    work += phase2_block(S, k, blocks + ((size_t)b0 + (size_t)k * bstride) * 64, perceptual, hc, use_alpha,
+                         out + (size_t)k * bstride * out_stride, err_out ? err_out + (size_t)k * bstride : nullptr);
   return work;
 }
 
@@ -1250,21 +1264,23 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
   const uint32_t lane = lane_id();
   const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const uint32_t nwarps = gridDim.x * kWarpsPerCta;
-  const uint32_t chunks = (n + kBlocksPerWarp - 1) / kBlocksPerWarp;
+  // warp w takes blocks w, w + nwarps, w + 2 nwarps, ... (every warp's count within one of the
+  // others', block costs interleaved across warps), eight at a time
+  const uint32_t mine = warp_global < n ? (n - warp_global + nwarps - 1) / nwarps : 0;
   unsigned long long work = 0;
-  auto chunk_count = [&](uint32_t chunk) { return min((uint32_t)kBlocksPerWarp, n - chunk * kBlocksPerWarp); };
+  auto chunk_count = [&](uint32_t k0) { return min((uint32_t)kBlocksPerWarp, mine - k0); };
+  auto first_block = [&](uint32_t k0) { return warp_global + k0 * nwarps; };
   ChunkStager st;
-  if (warp_global < chunks)
-    st.start(S, blocks + (size_t)warp_global * kBlocksPerWarp * 64, chunk_count(warp_global));
-  for (uint32_t chunk = warp_global; chunk < chunks; chunk += nwarps) {
-    const uint32_t b0 = chunk * kBlocksPerWarp;
-    const uint32_t cnt = chunk_count(chunk);
-    const uint8_t* staged = st.acquire(S, blocks + (size_t)b0 * 64);
-    const uint32_t nxt = chunk + nwarps;
+  if (mine) st.start(S, blocks + (size_t)first_block(0) * 64, chunk_count(0), nwarps);
+  for (uint32_t k0 = 0; k0 < mine; k0 += kBlocksPerWarp) {
+    const uint32_t b0 = first_block(k0);
+    const uint32_t cnt = chunk_count(k0);
+    const uint8_t* staged = st.acquire(S);
+    const uint32_t k1 = k0 + kBlocksPerWarp;
     work += dxt1_chunk(
-        S, blocks, b0, cnt, staged,
+        S, blocks, b0, nwarps, cnt, staged,
         [&]() {
-          if (nxt < chunks) st.next(S, blocks + (size_t)nxt * kBlocksPerWarp * 64, chunk_count(nxt));
+          if (k1 < mine) st.next(S, blocks + (size_t)first_block(k1) * 64, chunk_count(k1), nwarps);
         },
         perceptual != 0, hc != 0, use_alpha != 0, out + (size_t)b0 * out_stride, out_stride,
         err_out ? err_out + b0 : nullptr);
@@ -1479,10 +1495,10 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
     const EncodeChunk ch = chunks[c];
     const EncodeSegment sg = segs[ch.segment];
     const bool use_alpha = (sg.options & kSegThreeColour) != 0;
-    const uint8_t* staged = st.acquire(S, blocks + (size_t)ch.first * 64);
+    const uint8_t* staged = st.acquire(S);
     const uint32_t nxt = c + nwarps;
     dxt1_chunk(
-        S, blocks, ch.first, ch.count, staged,
+        S, blocks, ch.first, 1, ch.count, staged,
         [&]() {
           if (nxt < nchunks) {
             const EncodeChunk cn = chunks[nxt];
