@@ -61,6 +61,13 @@ class _CrnBatchItem(ctypes.Structure):
                 ("out_capacity", ctypes.c_uint64), ("result", ctypes.c_int64)]
 
 
+class _WaitStats(ctypes.Structure):
+    """crngpu_wait_stats"""
+    _fields_ = [("encode_stage_timeouts", ctypes.c_uint32), ("encode_drain_failures", ctypes.c_uint32),
+                ("expand_stage_timeouts", ctypes.c_uint32), ("expand_drain_failures", ctypes.c_uint32),
+                ("mma_wait_timeouts", ctypes.c_uint32)]
+
+
 class _EncodeItem(ctypes.Structure):
     _fields_ = [("rgba", ctypes.c_void_p), ("out", ctypes.c_void_p), ("width", ctypes.c_uint32),
                 ("height", ctypes.c_uint32), ("levels", ctypes.c_uint32), ("format", ctypes.c_uint32)]
@@ -139,6 +146,10 @@ def lib():
     L.crngpu_generate_mipmaps.restype = i64
     L.crngpu_profile_counters.argtypes = [i32, ctypes.POINTER(ctypes.c_uint64), vp]
     L.crngpu_profile_counters.restype = i32
+    L.crngpu_wait_counters.argtypes = [ctypes.POINTER(_WaitStats), i32]
+    L.crngpu_wait_counters.restype = i32
+    L.crngpu_force_wait_timeouts.argtypes = [i32]
+    L.crngpu_force_wait_timeouts.restype = i32
     _lib = L
     return L
 
@@ -157,6 +168,20 @@ def profile_counters(enable: bool, stream=None) -> int:
     v = ctypes.c_uint64(0)
     _check(lib().crngpu_profile_counters(int(enable), ctypes.byref(v), _stream_ptr(stream)), "crngpu_profile_counters")
     return int(v.value)
+
+
+def wait_counters(reset: bool = False) -> dict:
+    """How often the kernels' bounded waits ran out on the current device (crngpu_wait_counters):
+    staging waits fall back to global memory, MMA waits make the call fail, drains that ran out
+    mean a CTA exited with a copy in flight."""
+    st = _WaitStats()
+    _check(lib().crngpu_wait_counters(ctypes.byref(st), int(reset)), "crngpu_wait_counters")
+    return {name: int(getattr(st, name)) for name, _ in _WaitStats._fields_}
+
+
+def force_wait_timeouts(on: bool) -> None:
+    """Test hook: every first bounded wait gives up at once (on) or the normal bounds apply (off)."""
+    _check(lib().crngpu_force_wait_timeouts(int(on)), "crngpu_force_wait_timeouts")
 
 
 def _check(rc: int, where: str) -> int:

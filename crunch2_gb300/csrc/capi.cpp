@@ -12,6 +12,11 @@ namespace {
 thread_local std::string g_last_error;
 }
 
+std::mutex& device_setup_mutex() {
+  static std::mutex mu;
+  return mu;
+}
+
 void set_error(const std::string& msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
 const char* last_error_cstr() { return g_last_error.c_str(); }
@@ -66,6 +71,37 @@ DevBuf& staging(int slot) {
 namespace crngpu {
 int set_work_counter(bool on, cudaStream_t s);
 int read_work_counter(uint64_t* value, cudaStream_t s);
+int set_stage_wait_polls(uint32_t polls);
+int stage_wait_counters(uint32_t out[2], bool reset);
+int set_expand_wait_polls(uint32_t polls);
+int expand_wait_counters(uint32_t out[2], bool reset);
+int set_mma_wait_polls(uint32_t polls);
+int mma_wait_counter(uint32_t* out, bool reset);
+}
+
+extern "C" int crngpu_force_wait_timeouts(int on) {
+  crngpu::clear_error();
+  const uint32_t stage = on ? 0u : (1u << 22), mma = on ? 0u : (1u << 24);
+  int rc = crngpu::set_stage_wait_polls(stage);
+  if (rc == CRNGPU_OK) rc = crngpu::set_expand_wait_polls(stage);
+  if (rc == CRNGPU_OK) rc = crngpu::set_mma_wait_polls(mma);
+  return rc;
+}
+
+extern "C" int crngpu_wait_counters(crngpu_wait_stats* out, int reset) {
+  crngpu::clear_error();
+  if (!out) { crngpu::set_error("NULL output"); return CRNGPU_E_PARAM; }
+  uint32_t st[2] = {0, 0}, ex[2] = {0, 0}, mma = 0;
+  int rc = crngpu::stage_wait_counters(st, reset != 0);
+  if (rc == CRNGPU_OK) rc = crngpu::expand_wait_counters(ex, reset != 0);
+  if (rc == CRNGPU_OK) rc = crngpu::mma_wait_counter(&mma, reset != 0);
+  if (rc != CRNGPU_OK) return rc;
+  out->encode_stage_timeouts = st[0];
+  out->encode_drain_failures = st[1];
+  out->expand_stage_timeouts = ex[0];
+  out->expand_drain_failures = ex[1];
+  out->mma_wait_timeouts = mma;
+  return CRNGPU_OK;
 }
 
 extern "C" int crngpu_profile_counters(int enable, uint64_t* dxt1_evaluations, void* stream) {

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -428,9 +429,14 @@ __device__ __forceinline__ void narrow_emit(const ExpandJob& J, uint32_t first, 
 // before it belong to the previous face of the same buffer) and ends at its last record rounded
 // down to 16 bytes; the up to three records after that are read from global memory. Waits are
 // bounded: a CTA whose wait runs out reads its records from global memory from then on (same
-// output) and counts the event in g_expand_stage_timeouts.
-__device__ unsigned int g_expand_stage_timeouts;
+// output) and counts the event in g_expand_stage_timeouts. Copies still in flight when the CTA is
+// done are drained with a separate, much longer bound (kExpandDrainPolls) that the test hook does
+// not change; a drain that runs out is counted in g_expand_drain_failures.
 constexpr uint32_t kExpandWaitLimit = 1u << 22;
+constexpr uint32_t kExpandDrainPolls = 1u << 26;
+__device__ uint32_t g_expand_wait_polls = kExpandWaitLimit;
+__device__ unsigned int g_expand_stage_timeouts;
+__device__ unsigned int g_expand_drain_failures;
 
 __device__ __forceinline__ uint32_t shared_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -486,7 +492,8 @@ __device__ __forceinline__ void narrow_tma(const ExpandJob& J, uint32_t first, u
     if (live && B > A) {
       bool done = false;
       const uint32_t bar = shared_u32(&bars[buf]), parity = (buf ? waited1 : waited0) & 1u;
-      for (uint32_t k = 0; k < kExpandWaitLimit && !done; k++) {
+      const uint32_t polls = g_expand_wait_polls;
+      for (uint32_t k = 0; k < polls && !done; k++) {
         uint32_t d;
         asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
                      : "=r"(d)
@@ -519,14 +526,16 @@ __device__ __forceinline__ void narrow_tma(const ExpandJob& J, uint32_t first, u
   for (uint32_t b = 0; b < 2; b++)
     if ((b ? issued1 > waited1 : issued0 > waited0) && threadIdx.x == 0) {
       const uint32_t bar = shared_u32(&bars[b]), parity = ((b ? issued1 : issued0) - 1) & 1u;
-      for (uint32_t k = 0; k < kExpandWaitLimit; k++) {
+      bool landed = false;
+      for (uint32_t k = 0; k < kExpandDrainPolls && !landed; k++) {
         uint32_t d;
         asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
                      : "=r"(d)
                      : "r"(bar), "r"(parity)
                      : "memory");
-        if (d) break;
+        landed = d != 0;
       }
+      if (!landed) atomicAdd(&g_expand_drain_failures, 1u);
     }
 }
 
@@ -669,7 +678,9 @@ constexpr bool kVariantStage[kExpandVariants] = {false, true, false, true, false
 constexpr uint32_t kVariantTmaBytes[kExpandVariants] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
                                                         (2 * (kTmaSub + 4) + 4) * 4, (2 * (kTmaSub + 4) + 4) * 4,
                                                         (2 * (kTmaSub + 4) + 4) * 4};
-int g_expand_variant[64] = {};  // per device: the autotuner's last choice (0 until tuned)
+// per device: the autotuner's last choice (0 until tuned); atomic, as batches on several host
+// threads read and write it
+std::atomic<int> g_expand_variant[64] = {};
 
 // ------------------------------------------------------------------------------------------
 // Host side.
@@ -900,6 +911,7 @@ int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
   if (dev < 0 || dev >= 64) { set_error("device index out of range"); return CRNGPU_E_PARAM; }
+  std::lock_guard<std::mutex> lock(device_setup_mutex());
   if (!sms[dev]) {
     if ((e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
       return cuda_check(e, "device attribute");
@@ -951,7 +963,7 @@ int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStre
   if (p.ctas) {
     int dev = 0;
     cudaGetDevice(&dev);
-    const int v = variant >= 0 ? variant : g_expand_variant[dev & 63];
+    const int v = variant >= 0 ? variant : g_expand_variant[dev & 63].load(std::memory_order_relaxed);
     const int ts = kVariantTile[v];
     const uint2* tiles = reinterpret_cast<const uint2*>(d_jobs + p.tile_ofs[ts]);
     const size_t smem = kVariantTmaBytes[v] + (kVariantStage[v] ? (size_t)p.pal_words * 4 : 0);
@@ -1090,6 +1102,24 @@ void levels_tasks(UnpackContext* c, uint32_t first, uint32_t count, uint8_t* out
 }
 
 }  // namespace
+
+// Test hook for the expansion's staging waits: polls per wait (drains are not affected).
+int set_expand_wait_polls(uint32_t polls) {
+  return cuda_check(cudaMemcpyToSymbol(g_expand_wait_polls, &polls, sizeof(polls)), "set expansion wait polls");
+}
+
+// out[0]: staging waits that ran out, out[1]: drains that ran out; reset clears both.
+int expand_wait_counters(uint32_t out[2], bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(&out[0], g_expand_stage_timeouts, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(&out[1], g_expand_drain_failures, sizeof(uint32_t));
+  if (e == cudaSuccess && reset) {
+    const uint32_t z = 0;
+    e = cudaMemcpyToSymbol(g_expand_stage_timeouts, &z, sizeof(z));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_expand_drain_failures, &z, sizeof(z));
+  }
+  return cuda_check(e, "read expansion wait counters");
+}
+
 
 // A prepared batch: many levels of many contexts, decoded by one persistent launch and expanded
 // by one more. The job tables and record buffer are uploaded/allocated once at creation, so a
@@ -1274,7 +1304,7 @@ extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t fl
     cudaEventDestroy(ev[1]);
     if (rc != CRNGPU_OK) return rc;
     b->variant = bv;
-    g_expand_variant[b->device & 63] = bv;
+    g_expand_variant[b->device & 63].store(bv, std::memory_order_relaxed);
     b->decoded = true;
   }
   if (flags & CRNGPU_BATCH_EXPAND_ONLY) {
@@ -1406,13 +1436,15 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 namespace {
 
 // Device address of g_noalloc_scratch, looked up once per device with that device current (in
-// host code the array's name is only a host-side stand-in, not a device address).
+// host code the array's name is only a host-side stand-in, not a device address). The lookup is
+// made under the library's set-up mutex, so first calls from several host threads do not race.
 int noalloc_scratch_ptr(unsigned char** out) {
   static unsigned char* ptrs[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
   if (dev < 0 || dev >= 64) { set_error("device index out of range"); return CRNGPU_E_PARAM; }
+  std::lock_guard<std::mutex> lock(device_setup_mutex());
   if (!ptrs[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -1446,17 +1478,18 @@ extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_si
   for (uint32_t f = 0; f < F.faces; f++)
     if (!dst_faces[f]) { set_error("NULL face pointer"); return CRNGPU_E_PARAM; }
 
-  // scratch layout: [counter, status | jobs][models][palettes][level stream][records]
+  // scratch layout: [counter, status][models][palettes][level stream][records][launch descriptors]
+  // The descriptors go last: their size depends on the plan, which needs the record address.
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
-  const size_t o_jobs = 256, o_models = 4096;
+  const size_t o_models = 256;
   const size_t o_pal = o_models + al(sizeof(DevModel) * kNumModels);
   const size_t o_src = o_pal + al(palette_bytes(F));
   const size_t o_rec = o_src + al((size_t)li.size + 64);
   const size_t rec_bytes = (size_t)li.blocks_x * li.blocks_y * F.faces * record_bytes((uint32_t)F.kind);
-  const size_t need = o_rec + al(rec_bytes);
-  if (need > kNoAllocScratchBytes) {
-    set_error("level needs " + std::to_string(need) + " bytes of scratch; the allocation-free entry point has " +
-              std::to_string(kNoAllocScratchBytes));
+  const size_t o_jobs = o_rec + al(rec_bytes);
+  if (o_jobs > kNoAllocScratchBytes) {
+    set_error("level needs at least " + std::to_string(o_jobs) +
+              " bytes of scratch; the allocation-free entry point has " + std::to_string(kNoAllocScratchBytes));
     return CRNGPU_E_PARAM;
   }
   unsigned char* base = nullptr;
@@ -1481,7 +1514,12 @@ extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_si
   t.item = 0;
   Plan p;
   if (!make_plan({t}, p)) { set_error("bad level"); return CRNGPU_E_PARAM; }
-  if (p.image.size() > o_models - o_jobs) { set_error("launch descriptors too large"); return CRNGPU_E_PARAM; }
+  const size_t need = o_jobs + al(p.image.size());
+  if (need > kNoAllocScratchBytes) {
+    set_error("level needs " + std::to_string(need) + " bytes of scratch; the allocation-free entry point has " +
+              std::to_string(kNoAllocScratchBytes));
+    return CRNGPU_E_PARAM;
+  }
   struct Copy { size_t ofs; const void* src; size_t bytes; };
   const Copy copies[] = {
       {o_jobs, p.image.data(), p.image.size()},

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include "../../include/crngpu.h"
@@ -47,6 +48,11 @@ inline bool format_is_non_srgb(uint32_t format) {
 void set_error(const std::string& msg);
 void clear_error();
 const char* last_error_cstr();
+
+// Guards every lazily filled per-device cache of the library (function attributes, symbol
+// addresses, uploaded tables, SM counts): first calls on one device from several host threads
+// would otherwise race on them.
+std::mutex& device_setup_mutex();
 
 // Records `what` + the CUDA error string and returns CRNGPU_E_DEVICE when e != cudaSuccess.
 int cuda_check(cudaError_t e, const char* what);

@@ -1143,11 +1143,16 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
 
 // ---- TMA staging of a warp's chunk: cp.async.bulk global -> shared completing on an mbarrier.
 // The copy is 64 * cnt bytes from a 64-byte aligned block, so source, destination and size meet
-// the bulk copy's 16-byte rules. Waits are bounded: after kStageWaitLimit polls the warp stops
+// the bulk copy's 16-byte rules. Waits are bounded: after g_stage_wait_polls polls the warp stops
 // using the stage and reads its blocks from global memory (the results do not change), and the
-// event is counted in g_stage_timeouts.
+// event is counted in g_stage_timeouts. Before the warp exits, a copy still in flight is drained
+// with a separate, much longer bound (kStageDrainPolls) that the test hook does not change; a
+// drain that runs out is counted in g_stage_drain_failures.
 constexpr uint32_t kStageWaitLimit = 1u << 22;
+constexpr uint32_t kStageDrainPolls = 1u << 26;
+__device__ uint32_t g_stage_wait_polls = kStageWaitLimit;
 __device__ unsigned int g_stage_timeouts;
+__device__ unsigned int g_stage_drain_failures;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -1182,10 +1187,10 @@ __device__ __forceinline__ void stage_issue(WarpShared& S, const uint8_t* src, u
   }
 }
 
-// every lane: wait for the copy of the given phase parity; false after the poll limit
-__device__ __forceinline__ bool stage_wait(WarpShared& S, uint32_t parity) {
+// every lane: wait for the copy of the given phase parity; false after `polls` polls
+__device__ __forceinline__ bool stage_poll(WarpShared& S, uint32_t parity, uint32_t polls) {
   const uint32_t bar = smem_u32(&S.bar);
-  for (uint32_t i = 0; i < kStageWaitLimit; i++) {
+  for (uint32_t i = 0; i < polls; i++) {
     uint32_t done;
     asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
                  : "=r"(done)
@@ -1193,6 +1198,11 @@ __device__ __forceinline__ bool stage_wait(WarpShared& S, uint32_t parity) {
                  : "memory");
     if (__all_sync(FULL_MASK, done != 0)) return true;
   }
+  return false;
+}
+
+__device__ __forceinline__ bool stage_wait(WarpShared& S, uint32_t parity) {
+  if (stage_poll(S, parity, g_stage_wait_polls)) return true;
   if (lane_id() == 0) atomicAdd(&g_stage_timeouts, 1u);
   return false;
 }
@@ -1223,9 +1233,9 @@ struct ChunkStager {
     stage_issue(S, src, cnt, stride);
     pending = true;
   }
-  // before the warp exits: a copy still in flight must land first (bounded)
+  // before the warp exits: a copy still in flight must land first (bounded by the drain limit)
   __device__ void finish(WarpShared& S) {
-    if (pending) stage_wait(S, parity);
+    if (pending && !stage_poll(S, parity, kStageDrainPolls) && lane_id() == 0) atomicAdd(&g_stage_drain_failures, 1u);
   }
 };
 
@@ -1637,10 +1647,13 @@ int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_a
   static bool attr_done[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev < 64 && !attr_done[dev]) {
-    cudaError_t ae = cudaFuncSetAttribute(k_dxt1_encode, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (ae != cudaSuccess) return cuda_check(ae, "set smem attribute");
-    attr_done[dev] = true;
+  {
+    std::lock_guard<std::mutex> lock(device_setup_mutex());
+    if (dev < 64 && !attr_done[dev]) {
+      cudaError_t ae = cudaFuncSetAttribute(k_dxt1_encode, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (ae != cudaSuccess) return cuda_check(ae, "set smem attribute");
+      attr_done[dev] = true;
+    }
   }
   int per_sm = 1, sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1687,6 +1700,23 @@ int launch_dxt5a_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, ui
   if (!nchunks) return CRNGPU_OK;
   k_dxt5a_encode_chunks<<<grid, 128, 0, s>>>(d_blocks, d_chunks, nchunks, d_segs);
   return cuda_check(cudaGetLastError(), "launch k_dxt5a_encode_chunks");
+}
+
+// Test hook for the staging waits: polls per wait (drains are not affected).
+int set_stage_wait_polls(uint32_t polls) {
+  return cuda_check(cudaMemcpyToSymbol(g_stage_wait_polls, &polls, sizeof(polls)), "set stage wait polls");
+}
+
+// out[0]: staging waits that ran out, out[1]: drains that ran out; reset clears both.
+int stage_wait_counters(uint32_t out[2], bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(&out[0], g_stage_timeouts, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemcpyFromSymbol(&out[1], g_stage_drain_failures, sizeof(uint32_t));
+  if (e == cudaSuccess && reset) {
+    const uint32_t z = 0;
+    e = cudaMemcpyToSymbol(g_stage_timeouts, &z, sizeof(z));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_stage_drain_failures, &z, sizeof(z));
+  }
+  return cuda_check(e, "read stage wait counters");
 }
 
 int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint8_t* d_out, uint32_t out_stride,

@@ -103,9 +103,16 @@ __device__ __forceinline__ float load_op(const Operand& o, int row, int k, int r
   }
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Polls of a first wait on a tcgen05.commit (a test hook can lower it to force the timeout path);
+// after a timeout the in-flight MMAs are drained with kDrainPolls, which the hook does not change,
+// so TMEM and shared memory are never released under a running MMA. Timeouts are counted.
+constexpr uint32_t kDrainPolls = 1u << 26;
+__device__ uint32_t g_mma_wait_polls = kWaitLimit;
+__device__ unsigned int g_mma_wait_timeouts;
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_t polls) {
   uint32_t done = 0;
-  for (uint32_t it = 0; it < kWaitLimit && !done; it++) {
+  for (uint32_t it = 0; it < polls && !done; it++) {
     asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
                  : "=r"(done)
                  : "r"(bar), "r"(parity));
@@ -169,12 +176,14 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
           smem_u32(&mbar)));
     }
     // the MMAs read shared memory asynchronously: wait before restaging it
-    const bool done = mbar_wait(smem_u32(&mbar), phase);
+    const bool done = mbar_wait(smem_u32(&mbar), phase, g_mma_wait_polls);
     asm volatile("tcgen05.fence::after_thread_sync;");
     ok = __syncthreads_and(done) != 0;  // uniform across the CTA
     if (!ok) {
-      // give the in-flight MMAs a second bounded chance to finish before TMEM is released
-      mbar_wait(smem_u32(&mbar), phase);
+      // drain the in-flight MMAs (long bound) before TMEM is released
+      if (tid == 0) atomicAdd(&g_mma_wait_timeouts, 1u);
+      mbar_wait(smem_u32(&mbar), phase, kDrainPolls);
+      asm volatile("tcgen05.fence::after_thread_sync;");
       break;
     }
     phase ^= 1;
@@ -285,10 +294,12 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tmem, int quarter, int 
 // Waits for the tcgen05.commit of this phase; false (uniform across the CTA) on timeout, after a
 // second bounded wait so the tensor core is done with shared memory and TMEM before the caller exits.
 __device__ __forceinline__ bool tile_wait(uint32_t bar, uint32_t phase) {
-  const bool done = mbar_wait(bar, phase);
+  const bool done = mbar_wait(bar, phase, g_mma_wait_polls);
   asm volatile("tcgen05.fence::after_thread_sync;");
   if (__syncthreads_and(done)) return true;
-  mbar_wait(bar, phase);
+  if (threadIdx.x == 0) atomicAdd(&g_mma_wait_timeouts, 1u);
+  mbar_wait(bar, phase, kDrainPolls);
+  asm volatile("tcgen05.fence::after_thread_sync;");
   return false;
 }
 
@@ -733,12 +744,15 @@ int gemm(const GemmArgs& g, cudaStream_t s) {
   static bool attr_done[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev >= 0 && dev < 64 && !attr_done[dev]) {  // > 48 KB per CTA in total needs the opt-in
-    cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 40 << 10);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, 36 << 10);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 24 << 10);
-    if (e != cudaSuccess) return cuda_check(e, "set k_gemm_tc shared memory");
-    attr_done[dev] = true;
+  {
+    std::lock_guard<std::mutex> lock(device_setup_mutex());
+    if (dev >= 0 && dev < 64 && !attr_done[dev]) {  // > 48 KB per CTA in total needs the opt-in
+      cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 40 << 10);
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<48>, cudaFuncAttributeMaxDynamicSharedMemorySize, 36 << 10);
+      if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, 24 << 10);
+      if (e != cudaSuccess) return cuda_check(e, "set k_gemm_tc shared memory");
+      attr_done[dev] = true;
+    }
   }
   const unsigned gx = (g.M + BM - 1) / BM;
   if (g.N <= 16) {
@@ -789,11 +803,14 @@ int infer(Net& net, const uint8_t* blocks, uint32_t n, float* y, cudaStream_t s)
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
   if (dev < 0 || dev >= 64) { set_error("device index out of range"); return CRNGPU_E_DEVICE; }
-  if (!attr_done[dev]) {
-    e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess) return cuda_check(e, "set up k_mlp_infer");
-    attr_done[dev] = true;
+  {
+    std::lock_guard<std::mutex> lock(device_setup_mutex());
+    if (!attr_done[dev]) {
+      e = cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return cuda_check(e, "set up k_mlp_infer");
+      attr_done[dev] = true;
+    }
   }
   if ((e = net.errflag.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc flag");
   if (!n) return CRNGPU_OK;
@@ -858,6 +875,21 @@ int check_flag(Net& net, cudaStream_t s) {
 }
 
 }  // namespace mlp
+// Test hook for the tcgen05 commit waits: polls per first wait (drains are not affected).
+int set_mma_wait_polls(uint32_t polls) {
+  return cuda_check(cudaMemcpyToSymbol(mlp::g_mma_wait_polls, &polls, sizeof(polls)), "set mma wait polls");
+}
+
+// Number of first waits that ran out since the last reset.
+int mma_wait_counter(uint32_t* out, bool reset) {
+  cudaError_t e = cudaMemcpyFromSymbol(out, mlp::g_mma_wait_timeouts, sizeof(uint32_t));
+  if (e == cudaSuccess && reset) {
+    const uint32_t z = 0;
+    e = cudaMemcpyToSymbol(mlp::g_mma_wait_timeouts, &z, sizeof(z));
+  }
+  return cuda_check(e, "read mma wait counter");
+}
+
 }  // namespace crngpu
 
 using namespace crngpu;

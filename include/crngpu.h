@@ -59,6 +59,25 @@ CRNGPU_API const char* crngpu_last_error(void);
  * *dxt1_evaluations (if not NULL), then enables (1) or disables (0) counting and clears it. */
 CRNGPU_API int crngpu_profile_counters(int enable, uint64_t* dxt1_evaluations, void* stream);
 
+/* Bounded waits inside the kernels (no counterpart in the reference, whose code runs on the CPU).
+ * Every wait on an mbarrier is bounded. A staging wait of the DXT1 encoders or of the TMA
+ * expansion variants that runs out falls back to reading global memory (the output does not
+ * change); a wait on a tcgen05 MMA of the MLP kernels that runs out makes the call return
+ * CRNGPU_E_DEVICE. In-flight copies and MMAs are always drained, with a much longer bound, before
+ * a CTA exits. crngpu_wait_counters reads how often each happened on the current device (and
+ * clears the counts if reset != 0): a non-zero drain count means a CTA exited with a copy still
+ * in flight. crngpu_force_wait_timeouts(1) makes every first wait give up at once (a test hook
+ * for the fallback paths); crngpu_force_wait_timeouts(0) restores the normal bounds. */
+typedef struct crngpu_wait_stats {
+    uint32_t encode_stage_timeouts;   /* DXT1 encoders: staging waits that ran out */
+    uint32_t encode_drain_failures;   /* DXT1 encoders: drains that ran out */
+    uint32_t expand_stage_timeouts;   /* transcode expansion: staging waits that ran out */
+    uint32_t expand_drain_failures;   /* transcode expansion: drains that ran out */
+    uint32_t mma_wait_timeouts;       /* MLP kernels: MMA waits that ran out */
+} crngpu_wait_stats;
+CRNGPU_API int crngpu_wait_counters(crngpu_wait_stats* out, int reset);
+CRNGPU_API int crngpu_force_wait_timeouts(int on);
+
 /* ------------------------------------------------------------------------------------------
  * Block encoders (quality: cCRNDXTQualityUber; endpoint caching is never used, so results do
  * not depend on how blocks are batched).

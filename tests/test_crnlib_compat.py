@@ -17,7 +17,9 @@ import golden_util as G
 import crnlib_abi as A
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_INC = "/root/reference/inc"
+# the reference's headers (CRN_REFERENCE_DIR, else the container's copy); tests that compile
+# against them skip where the tree is absent
+REF_INC = os.path.join(os.environ.get("CRN_REFERENCE_DIR", "/root/reference"), "inc")
 
 
 def compat():
