@@ -23,12 +23,29 @@ extern "C" {
 int oracle_dxt1_blocks(const uint8_t* blocks, uint32_t n, int perceptual, int use_alpha_blocks,
                        uint8_t* out, uint64_t* err, int threads);
 
+// The DXT1 block encoder with every parameter the reference's block compressor passes to the
+// optimizer (dxt_image::set_block_pixels, crn_dxt_image.cpp:1436-1490):
+//   quality: crn_dxt_quality, 0 superfast .. 4 uber (crnlib.h:88-97)
+//   grayscale: cCRNCompFlagGrayscaleSampling (luma distance, perceptual off)
+//   dxt1a: DXT1A: a block with a texel whose alpha is below alpha_threshold has transparent texels
+//   transparent_black: cCRNCompFlagUseTransparentIndicesForBlack (try_alpha_as_black_optimization)
+typedef struct oracle_dxt1_opts {
+  int perceptual, use_alpha_blocks, quality, grayscale, dxt1a, alpha_threshold, transparent_black;
+} oracle_dxt1_opts;
+int oracle_dxt1_blocks_ex(const uint8_t* blocks, uint32_t n, const oracle_dxt1_opts* o, uint8_t* out,
+                          uint64_t* err, int threads);
+
 // DXT5A (single channel) endpoint optimizer over 4x4 blocks
 // (dxt5_endpoint_optimizer::compute, crnlib/crn_dxt5a.cpp:40-196), uber quality.
 //   comp: channel index 0..3;  use_both_block_types: allow 6-value blocks
 //   out: n x 8 bytes (dxt5_block layout, crn_dxt.h:266-406)
 int oracle_dxt5a_blocks(const uint8_t* blocks, uint32_t n, int comp, int use_both_block_types,
                         uint8_t* out, int threads);
+
+// The same at a given crn_dxt_quality (0 superfast .. 4 uber): the +-16 / +-8 probe grid runs at
+// Uber / Better only (crn_dxt5a.cpp:105-141).
+int oracle_dxt5a_blocks_q(const uint8_t* blocks, uint32_t n, int comp, int use_both_block_types, int quality,
+                          uint8_t* out);
 
 // Whole-format block encode the way dxt_image packs each element
 // (crn_dxt_image.cpp:1430-1530): fmt 0 = DXT1 (8 B), 2 = DXT5 (alpha + colour, 16 B),

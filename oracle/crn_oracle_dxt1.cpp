@@ -1,6 +1,7 @@
-// CPU restatement of the reference DXT1 endpoint optimizer (uber quality, endpoint caching
-// off). TEST INFRASTRUCTURE ONLY: the oracle that the CUDA path is checked against, and the
-// CPU baseline. Every stage cites the reference function it restates (crnlib/crn_dxt1.cpp
+// CPU restatement of the reference DXT1 endpoint optimizer (every crn_dxt_quality level,
+// perceptual / uniform / grayscale metrics, DXT1A transparency and the transparent-black trial;
+// endpoint caching off). TEST INFRASTRUCTURE ONLY: the oracle that the CUDA path is checked
+// against, and the CPU baseline. Every stage cites the reference function it restates (crnlib/crn_dxt1.cpp
 // unless noted). Float/double expression order and types follow the reference exactly;
 // build with -ffp-contract=off.
 #include "crn_oracle.h"
@@ -87,6 +88,19 @@ inline unsigned cdist(bool perceptual, const RGB& a, const RGB& b) {
   return (unsigned)(dr * dr + dg * dg + db * db);
 }
 
+// color::RGB_to_Y (crn_color.h:792-796): fixed-point luma
+inline int luma(const RGB& c) { return (c.r * 19595 + c.g * 38470 + c.b * 7471 + 32768) >> 16; }
+
+// dxt1_endpoint_optimizer::color_distance (crnlib/crn_dxt1.cpp:1342-1368): the grayscale-sampling
+// metric when the perceptual one is off
+inline unsigned mdist(bool perceptual, bool gray, const RGB& a, const RGB& b) {
+  if (!perceptual && gray) {
+    const int yd = luma(a) - luma(b);
+    return (unsigned)(yd * yd);
+  }
+  return cdist(perceptual, a, b);
+}
+
 struct V3 { float x[3]; float& operator[](int i) { return x[i]; } float operator[](int i) const { return x[i]; } };
 
 struct Coords {
@@ -102,7 +116,12 @@ struct Solution {
   uint8_t enforced = 0;
 };
 
+// probe tables per quality (crn_dxt1.cpp:43-53)
+const int16_t kFastProbe[4] = {0, 1, 2, 3};
+const int16_t kNormalProbe[5] = {0, 1, 3, 5, 7};
+const int16_t kBetterProbe[10] = {0, 1, 2, 3, 5, 9, 15, 19, 27, 43};
 const int16_t kUberProbe[15] = {0, 1, 2, 3, 5, 7, 9, 10, 13, 15, 19, 27, 43, 59, 91};
+enum { kSuperFast = 0, kFast = 1, kNormal = 2, kBetter = 3, kUber = 4 };
 const int8_t kAdj[26][3] = {
     {-1, -1, -1}, {0, -1, -1}, {1, -1, -1}, {-1, 0, -1}, {0, 0, -1}, {1, 0, -1}, {-1, 1, -1}, {0, 1, -1},
     {1, 1, -1},   {-1, -1, 0}, {0, -1, 0},  {1, -1, 0},  {-1, 0, 0}, {1, 0, 0},  {-1, 1, 0},  {0, 1, 0},
@@ -123,14 +142,32 @@ struct FastRandom {
   }
 };
 
+// dxt1_endpoint_optimizer::params (crn_dxt1.h:168-201) as dxt_image::set_block_pixels fills them
+struct Dxt1Params {
+  bool perceptual = true, use_alpha_blocks = true, grayscale = false, pixels_have_alpha = false;
+  bool transparent_black = false;
+  int quality = kUber;
+  int alpha_threshold = 128;
+};
+
 class Dxt1Search {
  public:
-  // One block (or cluster) of pixels in, one dxt1 solution out.
+  // One block (or cluster) of pixels in, one dxt1 solution out (compute :2234-2245).
+  void run(const uint8_t* px, uint32_t n_px, const Dxt1Params& p, uint16_t& out_lo, uint16_t& out_hi,
+           uint8_t* out_sel, uint64_t& out_err);
   void run(const uint8_t* px, uint32_t n_px, bool perceptual, bool use_alpha_blocks, uint16_t& out_lo,
-           uint16_t& out_hi, uint8_t* out_sel, uint64_t& out_err);
+           uint16_t& out_hi, uint8_t* out_sel, uint64_t& out_err) {
+    Dxt1Params p;
+    p.perceptual = perceptual;
+    p.use_alpha_blocks = use_alpha_blocks;
+    run(px, n_px, p, out_lo, out_hi, out_sel, out_err);
+  }
 
  private:
-  bool perceptual_ = true, use_alpha_ = true, hc_ = false;
+  void compute_internal(const uint8_t* px, uint32_t n_px, const Dxt1Params& p, uint16_t& out_lo, uint16_t& out_hi,
+                        uint8_t* out_sel, uint64_t& out_err);
+  bool perceptual_ = true, use_alpha_ = true, hc_ = false, gray_ = false, have_alpha_ = false;
+  int quality_ = kUber;
   std::vector<RGB> uc_;
   std::vector<uint32_t> w_;
   std::unordered_map<uint32_t, uint32_t> index_;
@@ -144,6 +181,7 @@ class Dxt1Search {
 
   bool evaluate(Coords c, bool alt = false);
   bool evaluate_uber(Coords c, bool alt);
+  bool evaluate_fast(Coords c, bool alt);
   bool evaluate_hc(Coords c, bool alt);
   void compute_selectors();
   void compute_vectors(const V3& pw);
@@ -173,7 +211,8 @@ bool Dxt1Search::evaluate(Coords c, bool alt) {
   if (!alt) {
     if (!tried_.insert((uint32_t)c.lo | ((uint32_t)c.hi << 16)).second) return false;
   }
-  return hc_ ? evaluate_hc(c, alt) : evaluate_uber(c, alt);
+  if (hc_) return evaluate_hc(c, alt);
+  return quality_ >= kBetter ? evaluate_uber(c, alt) : evaluate_fast(c, alt);
 }
 
 // evaluate_solution_uber :1370-1592
@@ -188,8 +227,9 @@ bool Dxt1Search::evaluate_uber(Coords c, bool alt) {
   col[0] = unpack565(c.lo, true);
   col[1] = unpack565(c.hi, true);
   const int a = alt ? 1 : 0;
-  const int last_type = use_alpha_ ? 1 : 0;
-  for (int type = 0; type <= last_type; type++) {
+  const int first_type = have_alpha_ ? 1 : 0;
+  const int last_type = (have_alpha_ || use_alpha_) ? 1 : 0;
+  for (int type = first_type; type <= last_type; type++) {
     uint64_t terr = 0;
     int ncol;
     if (type == 0) {
@@ -201,10 +241,10 @@ bool Dxt1Search::evaluate_uber(Coords c, bool alt) {
       ncol = 3;
     }
     for (int i = n - 1; i >= 0; i--) {
-      unsigned be = cdist(perceptual_, uc_[i], col[0]);
+      unsigned be = mdist(perceptual_, gray_, uc_[i], col[0]);
       int bi = 0;
       for (int k = 1; k < ncol; k++) {
-        unsigned e = cdist(perceptual_, uc_[i], col[k]);
+        unsigned e = mdist(perceptual_, gray_, uc_[i], col[k]);
         if (e < be) { be = e; bi = k; }
       }
       terr += (uint64_t)be * w_[i];
@@ -225,6 +265,78 @@ bool Dxt1Search::evaluate_uber(Coords c, bool alt) {
     else { trial_.c.hi--; s = 0; }
     for (int i = 0; i < n; i++) trial_.sel[i] = s;
     trial_.enforced = s;
+  }
+  if (trial_.error < best_.error) {
+    best_ = trial_;
+    return true;
+  }
+  return false;
+}
+
+// evaluate_solution_fast :1594-1757: selectors by projection onto the endpoint axis, then the
+// distance to the chosen colour. It leaves m_alternate_rounding and m_enforce_selector alone, so
+// the bumped equal-endpoint case keeps the flags of the trial before it (never set below Better).
+bool Dxt1Search::evaluate_fast(Coords c, bool alt) {
+  const int n = (int)uc_.size();
+  trial_.c = c;
+  trial_.sel.resize(n);
+  trial_.error = best_.error;
+  trial_.alpha_block = false;
+  trial_sel_.resize(n);
+  RGB col[4];
+  col[0] = unpack565(c.lo, true);
+  col[1] = unpack565(c.hi, true);
+  int vr = col[1].r - col[0].r, vg = col[1].g - col[0].g, vb = col[1].b - col[0].b;
+  if (perceptual_) {
+    vr *= 8;
+    vg *= 24;
+  }
+  auto dot = [&](const RGB& q) { return q.r * vr + q.g * vg + q.b * vb; };
+  int stops[4];
+  stops[0] = dot(col[0]);
+  stops[1] = dot(col[1]);
+  const int dr = vr * 2, dg = vg * 2, db = vb * 2;
+  const int a = alt ? 1 : 0;
+  const int first_type = have_alpha_ ? 1 : 0;
+  const int last_type = (have_alpha_ || use_alpha_) ? 1 : 0;
+  for (int type = first_type; type <= last_type; type++) {
+    uint64_t terr = 0;
+    if (type == 0) {
+      col[2] = {(col[0].r * 2 + col[1].r + a) / 3, (col[0].g * 2 + col[1].g + a) / 3, (col[0].b * 2 + col[1].b + a) / 3};
+      col[3] = {(col[1].r * 2 + col[0].r + a) / 3, (col[1].g * 2 + col[0].g + a) / 3, (col[1].b * 2 + col[0].b + a) / 3};
+      stops[2] = dot(col[2]);
+      stops[3] = dot(col[3]);
+      const int c0p = stops[1] + stops[3], halfp = stops[3] + stops[2], c3p = stops[2] + stops[0];
+      for (int i = n - 1; i >= 0; i--) {
+        const int d = uc_[i].r * dr + uc_[i].g * dg + uc_[i].b * db;
+        const int bi = d >= halfp ? (d < c0p ? 3 : 1) : (d < c3p ? 0 : 2);
+        terr += (uint64_t)mdist(perceptual_, gray_, uc_[i], col[bi]) * w_[i];
+        if (terr >= trial_.error) break;
+        trial_sel_[i] = (uint8_t)bi;
+      }
+    } else {
+      col[2] = {(col[0].r + col[1].r + a) >> 1, (col[0].g + col[1].g + a) >> 1, (col[0].b + col[1].b + a) >> 1};
+      stops[2] = dot(col[2]);
+      const int c02 = stops[0] + stops[2], c21 = stops[2] + stops[1];
+      for (int i = n - 1; i >= 0; i--) {
+        const int d = uc_[i].r * dr + uc_[i].g * dg + uc_[i].b * db;
+        const int bi = d < c02 ? 0 : (d < c21 ? 2 : 1);
+        terr += (uint64_t)mdist(perceptual_, gray_, uc_[i], col[bi]) * w_[i];
+        if (terr >= trial_.error) break;
+        trial_sel_[i] = (uint8_t)bi;
+      }
+    }
+    if (terr < trial_.error) {
+      trial_.error = terr;
+      trial_.alpha_block = type != 0;
+      trial_.sel = trial_sel_;
+    }
+  }
+  if (!trial_.alpha_block && trial_.c.lo == trial_.c.hi) {
+    uint8_t s;
+    if ((trial_.c.lo & 31) != 31) { trial_.c.lo++; s = 1; }
+    else { trial_.c.hi--; s = 0; }
+    for (int i = 0; i < n; i++) trial_.sel[i] = s;
   }
   if (trial_.error < best_.error) {
     best_ = trial_;
@@ -538,7 +650,7 @@ bool Dxt1Search::try_median4(const V3& low, const V3& high) {
       improved |= evaluate(sc.canon());
     }
   }
-  improved |= refine(1);
+  improved |= refine(quality_ == kUber ? 1 : 0);
   return improved;
 }
 
@@ -626,6 +738,7 @@ bool Dxt1Search::try_average_block_as_solid() {
   };
   bool improved = evaluate(solid4(ar, ag, ab));
   if (use_alpha_ && best_.error) improved |= evaluate(solid3(ar, ag, ab));
+  if (quality_ != kUber) return improved;
   for (size_t i = 0; i < uc_.size(); i++) {
     const unsigned r = uc_[i].r, g = uc_[i].g, b = uc_[i].b;
     if (r == ar && g == ag && b == ab) continue;
@@ -763,11 +876,21 @@ void Dxt1Search::try_combinatorial() {
   if (best_.error) best_.error = saved;
 }
 
-// optimize_endpoints :703-1067 (uber: 15-entry probe table, <= 4 passes)
+// optimize_endpoints :703-1067: the probe table, probe spacing and pass count of the quality
+// level, then the lattice moves (Normal and up; +-2 moves and per-pass refines at Uber only)
 void Dxt1Search::optimize_endpoints(V3 low, V3 high) {
   const V3 orig_low = low, orig_high = high;
-  try_median4(orig_low, orig_high);
-  const float dist_per_trial = .015625f;
+  const int16_t* table = kUberProbe;
+  int probe_range = 15, passes = 4;
+  float dist_per_trial = .015625f;
+  switch (quality_) {
+    case kSuperFast: table = kFastProbe; probe_range = 4; dist_per_trial = .027063293f; passes = 1; break;
+    case kFast: table = kFastProbe; probe_range = 4; dist_per_trial = .027063293f; passes = 2; break;
+    case kNormal: table = kNormalProbe; probe_range = 5; dist_per_trial = .027063293f; passes = 2; break;
+    case kBetter: table = kBetterProbe; probe_range = 10; passes = 2; break;
+    default: break;
+  }
+  if (quality_ >= kBetter) try_median4(orig_low, orig_high);
   V3 sa[2];
   for (int k = 0; k < 3; k++) sa[1][k] = axis_[k] * dist_per_trial;
   sa[1][0] *= 31.0f; sa[1][1] *= 63.0f; sa[1][2] *= 31.0f;
@@ -776,7 +899,7 @@ void Dxt1Search::optimize_endpoints(V3 low, V3 high) {
   low[0] = clampf(low[0] * 31.0f, 31.0f); low[1] = clampf(low[1] * 63.0f, 63.0f); low[2] = clampf(low[2] * 31.0f, 31.0f);
   high[0] = clampf(high[0] * 31.0f, 31.0f); high[1] = clampf(high[1] * 63.0f, 63.0f); high[2] = clampf(high[2] * 31.0f, 31.0f);
 
-  for (int pass = 0; pass < 4; pass++) {
+  for (int pass = 0; pass < passes; pass++) {
     if (pass) {
       RGB lo = unpack565(best_.c.lo, false), hi = unpack565(best_.c.hi, false);
       low[0] = (float)lo.r; low[1] = (float)lo.g; low[2] = (float)lo.b;
@@ -789,8 +912,8 @@ void Dxt1Search::optimize_endpoints(V3 low, V3 high) {
       int cnt = 0;
       V3 init;
       for (int k = 0; k < 3; k++) init[k] = base[k] + .5f;
-      for (int i = 0; i < 15; i++) {
-        const int x = kUberProbe[i];
+      for (int i = 0; i < probe_range; i++) {
+        const int x = table[i];
         for (int s = i ? 0 : 1; s < 2; s++) {
           float pr = init[0] + sa[s][0] * (float)x, pg = init[1] + sa[s][1] * (float)x, pb = init[2] + sa[s][2] * (float)x;
           int r = std::min(std::max((int)std::floor(pr), 0), 31);
@@ -807,66 +930,104 @@ void Dxt1Search::optimize_endpoints(V3 low, V3 high) {
     for (int i = 0; i < nl; i++)
       for (int j = 0; j < nh; j++) evaluate(Coords{pl[i], ph[j]}.canon());
 
-    // low endpoint: 26 lattice neighbours, then +-2 along each axis
-    RGB lc = unpack565(best_.c.lo, false);
-    for (int i = 0; i < 26; i++) {
-      int r = lc.r + kAdj[i][0], g = lc.g + kAdj[i][1], b = lc.b + kAdj[i][2];
-      if (r < 0 || r > 31 || g < 0 || g > 63 || b < 0 || b > 31) continue;
-      evaluate(Coords{pack565(r, g, b), best_.c.hi}.canon());
-    }
-    lc = unpack565(best_.c.lo, false);
-    for (int a = 0; a < 3; a++) {
-      const int limit = a == 1 ? 63 : 31;
-      for (int s = -2; s <= 2; s += 4) {
-        int c[3] = {lc.r, lc.g, lc.b};
-        const int qv = c[a] + s;
-        if (qv < 0 || qv > limit) continue;
-        c[a] = qv;
-        evaluate(Coords{pack565(c[0], c[1], c[2]), best_.c.hi}.canon());
-      }
-    }
-    RGB hc = unpack565(best_.c.hi, false);
-    for (int i = 0; i < 26; i++) {
-      int r = hc.r + kAdj[i][0], g = hc.g + kAdj[i][1], b = hc.b + kAdj[i][2];
-      if (r < 0 || r > 31 || g < 0 || g > 63 || b < 0 || b > 31) continue;
-      evaluate(Coords{best_.c.lo, pack565(r, g, b)}.canon());
-    }
-    hc = unpack565(best_.c.hi, false);
-    for (int a = 0; a < 3; a++) {
-      const int limit = a == 1 ? 63 : 31;
-      for (int s = -2; s <= 2; s += 4) {
-        int c[3] = {hc.r, hc.g, hc.b};
-        const int qv = c[a] + s;
-        if (qv < 0 || qv > limit) continue;
-        c[a] = qv;
-        evaluate(Coords{best_.c.lo, pack565(c[0], c[1], c[2])}.canon());
+    if (quality_ >= kNormal) {
+      // low endpoint: 26 lattice neighbours, then (Uber) +-2 along each axis; then the high one
+      for (int side = 0; side < 2; side++) {
+        RGB base = unpack565(side ? best_.c.hi : best_.c.lo, false);
+        for (int i = 0; i < 26; i++) {
+          int r = base.r + kAdj[i][0], g = base.g + kAdj[i][1], b = base.b + kAdj[i][2];
+          if (r < 0 || r > 31 || g < 0 || g > 63 || b < 0 || b > 31) continue;
+          const uint16_t m = pack565(r, g, b);
+          evaluate((side ? Coords{best_.c.lo, m} : Coords{m, best_.c.hi}).canon());
+        }
+        if (quality_ == kUber) {
+          base = unpack565(side ? best_.c.hi : best_.c.lo, false);
+          for (int a = 0; a < 3; a++) {
+            const int limit = a == 1 ? 63 : 31;
+            for (int s = -2; s <= 2; s += 4) {
+              int c[3] = {base.r, base.g, base.b};
+              const int qv = c[a] + s;
+              if (qv < 0 || qv > limit) continue;
+              c[a] = qv;
+              const uint16_t m = pack565(c[0], c[1], c[2]);
+              evaluate((side ? Coords{best_.c.lo, m} : Coords{m, best_.c.hi}).canon());
+            }
+          }
+        }
       }
     }
     if (!best_.error || (pass && best_.error == prev_best)) break;
-    refine(1);
+    if (quality_ >= kUber) refine(1);
   }
-  if (best_.error) {
-    bool solid = false;
-    if (all_selectors_equal()) solid = try_average_block_as_solid();
-    if (!solid) optimize_endpoint_comps();
+  if (quality_ >= kNormal) {
+    if (best_.error && !have_alpha_) {
+      bool solid = false;
+      if (all_selectors_equal()) solid = try_average_block_as_solid();
+      if (!solid && quality_ == kUber) optimize_endpoint_comps();
+    }
+    if (quality_ == kUber && best_.error) try_combinatorial();
   }
-  if (best_.error) try_combinatorial();
+}
+
+// compute :2234-2245: compute_internal, then (DXT1 with 3-colour blocks allowed, no real
+// transparency) try_alpha_as_black_optimization :2001-2079, which re-encodes the block with its
+// near-black texels (every channel <= 4) made transparent and keeps that 3-colour encoding when
+// its error over all texels (black for selector 3) is lower
+void Dxt1Search::run(const uint8_t* px, uint32_t n_px, const Dxt1Params& p, uint16_t& out_lo, uint16_t& out_hi,
+                     uint8_t* out_sel, uint64_t& out_err) {
+  compute_internal(px, n_px, p, out_lo, out_hi, out_sel, out_err);
+  if (!(p.use_alpha_blocks && p.transparent_black && !p.pixels_have_alpha)) return;
+  size_t dark = 0;
+  for (const RGB& c : uc_) dark += (c.r <= 4 && c.g <= 4 && c.b <= 4) ? 1 : 0;
+  if (!dark || dark == uc_.size()) return;
+  std::vector<uint8_t> trial(px, px + (size_t)n_px * 4);
+  for (uint32_t i = 0; i < n_px; i++)
+    if (trial[i * 4] <= 4 && trial[i * 4 + 1] <= 4 && trial[i * 4 + 2] <= 4) trial[i * 4 + 3] = 0;
+  Dxt1Params tp = p;
+  tp.pixels_have_alpha = true;
+  uint16_t tlo, thi;
+  std::vector<uint8_t> tsel(n_px);
+  uint64_t terr_opt;
+  compute_internal(trial.data(), n_px, tp, tlo, thi, tsel.data(), terr_opt);
+  // dxt1_block::get_block_colors3 (crn_dxt.cpp:234-245)
+  RGB c[4];
+  c[0] = unpack565(tlo, true);
+  c[1] = unpack565(thi, true);
+  c[2] = {(c[0].r + c[1].r) >> 1, (c[0].g + c[1].g) >> 1, (c[0].b + c[1].b) >> 1};
+  c[3] = {0, 0, 0};
+  uint64_t terr = 0;
+  for (uint32_t i = 0; i < n_px; i++)
+    terr += mdist(perceptual_, gray_, RGB{trial[i * 4], trial[i * 4 + 1], trial[i * 4 + 2]}, c[tsel[i]]);
+  if (terr < out_err) {
+    out_err = terr;
+    out_lo = tlo;
+    out_hi = thi;
+    std::memcpy(out_sel, tsel.data(), n_px);
+  }
 }
 
 // compute_internal :2081-2232 + return_solution :263-365
-void Dxt1Search::run(const uint8_t* px, uint32_t n_px, bool perceptual, bool use_alpha_blocks, uint16_t& out_lo,
-                     uint16_t& out_hi, uint8_t* out_sel, uint64_t& out_err) {
-  perceptual_ = perceptual;
-  use_alpha_ = use_alpha_blocks;
-  hc_ = !use_alpha_blocks;
+void Dxt1Search::compute_internal(const uint8_t* px, uint32_t n_px, const Dxt1Params& p, uint16_t& out_lo,
+                                  uint16_t& out_hi, uint8_t* out_sel, uint64_t& out_err) {
+  gray_ = p.grayscale;
+  perceptual_ = p.perceptual && !p.grayscale;
+  use_alpha_ = p.use_alpha_blocks;
+  have_alpha_ = p.pixels_have_alpha;
+  quality_ = p.quality;
+  hc_ = quality_ == kUber && !have_alpha_ && !use_alpha_ && !gray_;
   uc_.clear();
   w_.clear();
   index_.clear();
   tried_.clear();
   best_ = Solution();
   total_w_ = 0;
+  const uint32_t kTransparent = 0xFFFFFFFFu;
   std::vector<uint32_t> px_index(n_px);
   for (uint32_t i = 0; i < n_px; i++) {
+    if (have_alpha_ && px[i * 4 + 3] < p.alpha_threshold) {
+      px_index[i] = kTransparent;
+      continue;
+    }
     const uint32_t key = (uint32_t)px[i * 4] | ((uint32_t)px[i * 4 + 1] << 8) | ((uint32_t)px[i * 4 + 2] << 16);
     auto it = index_.find(key);
     if (it == index_.end()) {
@@ -880,6 +1041,7 @@ void Dxt1Search::run(const uint8_t* px, uint32_t n_px, bool perceptual, bool use
     }
     total_w_++;
   }
+  const bool has_transparent = total_w_ != n_px;
   // plane tables -> per-channel lower bounds on the endpoint error
   uint64_t plane[3][64][3];
   std::memset(plane, 0, sizeof(plane));
@@ -913,7 +1075,14 @@ void Dxt1Search::run(const uint8_t* px, uint32_t n_px, bool perceptual, bool use
     gdist_[c][0] = plane[1][c][2] + C * C * plane[1][c][0] - 2 * C * plane[1][c][1];
     gdist_[c][1] = plane[1][63][2] + C * C * plane[1][63][0] - 2 * C * plane[1][63][1] - gdist_[c][0];
   }
-  if (uc_.size() == 1) {
+  if (uc_.empty()) {
+    // every texel transparent: a 3-colour block of black endpoints, all selectors 3
+    out_lo = out_hi = 0;
+    std::memset(out_sel, 3, n_px);
+    out_err = 0;
+    return;
+  }
+  if (uc_.size() == 1 && !has_transparent) {
     const SingleColourTables& T = sct();
     const int r = uc_[0].r, g = uc_[0].g, b = uc_[0].b;
     evaluate(Coords{(uint16_t)((T.m5[r][0] << 11) | (T.m6[g][0] << 5) | T.m5[b][0]),
@@ -924,14 +1093,14 @@ void Dxt1Search::run(const uint8_t* px, uint32_t n_px, bool perceptual, bool use
   } else {
     handle_multicolor();
   }
-  // return_solution
+  // return_solution: transparent texels take selector 3
   compute_selectors();
   bool invert = best_.alpha_block ? best_.c.lo > best_.c.hi : best_.c.lo < best_.c.hi;
   static const uint8_t inv_null[4] = {0, 1, 2, 3}, inv_alpha[4] = {1, 0, 2, 3}, inv_colour[4] = {1, 0, 3, 2};
   const uint8_t* inv = invert ? (best_.alpha_block ? inv_alpha : inv_colour) : inv_null;
   out_lo = invert ? best_.c.hi : best_.c.lo;
   out_hi = invert ? best_.c.lo : best_.c.hi;
-  for (uint32_t i = 0; i < n_px; i++) out_sel[i] = inv[best_.sel[px_index[i]]];
+  for (uint32_t i = 0; i < n_px; i++) out_sel[i] = px_index[i] == kTransparent ? 3 : inv[best_.sel[px_index[i]]];
   out_err = best_.error;
 }
 
@@ -959,7 +1128,7 @@ void parallel_for(uint32_t n, int threads, F f) {
 
 // Restated DXT5A optimizer lives in crn_oracle_dxt5a.cpp.
 namespace crn_oracle_detail {
-void dxt5a_block(const uint8_t* px16, int comp, bool both, uint8_t* out8);
+void dxt5a_block(const uint8_t* px16, int comp, bool both, uint8_t* out8, int quality);
 }
 
 extern "C" int oracle_dxt1_blocks(const uint8_t* blocks, uint32_t n, int perceptual, int use_alpha_blocks,
@@ -976,6 +1145,41 @@ extern "C" int oracle_dxt1_blocks(const uint8_t* blocks, uint32_t n, int percept
       o[0] = lo & 0xFF; o[1] = lo >> 8; o[2] = hi & 0xFF; o[3] = hi >> 8;
       for (int y = 0; y < 4; y++)
         o[4 + y] = (uint8_t)(sel[y * 4] | (sel[y * 4 + 1] << 2) | (sel[y * 4 + 2] << 4) | (sel[y * 4 + 3] << 6));
+      if (err) err[i] = e;
+    }
+  });
+  return 0;
+}
+
+// The DXT1 block encode of dxt_image::set_block_pixels (crn_dxt_image.cpp:1436-1490) with every
+// parameter of the block compressor: for DXT1A, pixels_have_alpha is set per block when a texel's
+// alpha is below the threshold.
+extern "C" int oracle_dxt1_blocks_ex(const uint8_t* blocks, uint32_t n, const oracle_dxt1_opts* o, uint8_t* out,
+                                     uint64_t* err, int threads) {
+  if (!o || o->quality < 0 || o->quality > 4) return -1;
+  sct();
+  parallel_for(n, threads, [&](uint32_t i0, uint32_t i1) {
+    Dxt1Search s;
+    for (uint32_t i = i0; i < i1; i++) {
+      const uint8_t* px = blocks + (size_t)i * 64;
+      Dxt1Params p;
+      p.perceptual = o->perceptual != 0;
+      p.use_alpha_blocks = o->use_alpha_blocks != 0;
+      p.quality = o->quality;
+      p.grayscale = o->grayscale != 0;
+      p.transparent_black = o->transparent_black != 0;
+      p.alpha_threshold = o->alpha_threshold;
+      p.pixels_have_alpha = false;
+      if (o->dxt1a)
+        for (int k = 0; k < 16; k++) p.pixels_have_alpha |= px[k * 4 + 3] < o->alpha_threshold;
+      uint16_t lo, hi;
+      uint8_t sel[16];
+      uint64_t e;
+      s.run(px, 16, p, lo, hi, sel, e);
+      uint8_t* ob = out + (size_t)i * 8;
+      ob[0] = lo & 0xFF; ob[1] = lo >> 8; ob[2] = hi & 0xFF; ob[3] = hi >> 8;
+      for (int y = 0; y < 4; y++)
+        ob[4 + y] = (uint8_t)(sel[y * 4] | (sel[y * 4 + 1] << 2) | (sel[y * 4 + 2] << 4) | (sel[y * 4 + 3] << 6));
       if (err) err[i] = e;
     }
   });
@@ -1009,18 +1213,18 @@ extern "C" int oracle_encode_blocks(const uint8_t* blocks, uint32_t n, int fmt, 
       switch (fmt) {
         case 0: colour(o, use_both_block_types != 0); break;
         case 2:
-          crn_oracle_detail::dxt5a_block(px, 3, use_both_block_types != 0, o);
+          crn_oracle_detail::dxt5a_block(px, 3, use_both_block_types != 0, o, 4);
           colour(o + 8, false);
           break;
         case 7:
-          crn_oracle_detail::dxt5a_block(px, 0, use_both_block_types != 0, o);
-          crn_oracle_detail::dxt5a_block(px, 1, use_both_block_types != 0, o + 8);
+          crn_oracle_detail::dxt5a_block(px, 0, use_both_block_types != 0, o, 4);
+          crn_oracle_detail::dxt5a_block(px, 1, use_both_block_types != 0, o + 8, 4);
           break;
         case 8:
-          crn_oracle_detail::dxt5a_block(px, 1, use_both_block_types != 0, o);
-          crn_oracle_detail::dxt5a_block(px, 0, use_both_block_types != 0, o + 8);
+          crn_oracle_detail::dxt5a_block(px, 1, use_both_block_types != 0, o, 4);
+          crn_oracle_detail::dxt5a_block(px, 0, use_both_block_types != 0, o + 8, 4);
           break;
-        case 9: crn_oracle_detail::dxt5a_block(px, 3, use_both_block_types != 0, o); break;
+        case 9: crn_oracle_detail::dxt5a_block(px, 3, use_both_block_types != 0, o, 4); break;
       }
     }
   });

@@ -1,5 +1,5 @@
 // CPU restatement of the reference single-channel (DXT5 alpha / DXT5A / DXN channel) endpoint
-// optimizer, uber quality. TEST INFRASTRUCTURE ONLY (oracle + CPU baseline).
+// optimizer, every crn_dxt_quality level. TEST INFRASTRUCTURE ONLY (oracle + CPU baseline).
 // Restates dxt5_endpoint_optimizer::compute / evaluate_solution (crnlib/crn_dxt5a.cpp:40-262)
 // and the dxt5_block packing done by dxt_image::set_block_pixels (crn_dxt_image.cpp:1491-1522).
 #include "crn_oracle.h"
@@ -72,7 +72,7 @@ struct Alpha {
 }  // namespace
 
 // compute :40-196, then the selector packing of dxt5_block (crn_dxt.h:318-361)
-void dxt5a_block(const uint8_t* px16, int comp, bool both, uint8_t* out8) {
+void dxt5a_block(const uint8_t* px16, int comp, bool both, uint8_t* out8, int quality) {
   Alpha a;
   a.both = both;
   int map[256];
@@ -95,15 +95,17 @@ void dxt5a_block(const uint8_t* px16, int comp, bool both, uint8_t* out8) {
   } else {
     for (int i = 0; i + 1 < a.n; i++)
       for (int j = i + 1; j < a.n; j++) a.evaluate(a.vals[i], a.vals[j]);
-    if (a.err) {
-      // +-16 probe around the running best (the centre moves when the best improves)
+    if (quality >= 3 && a.err) {
+      // +-16 (Uber) or +-8 (Better) probe around the running best (the centre moves when the
+      // best improves); none below Better (:105-141)
+      const int amount = quality == 4 ? 16 : 8;
       static thread_local std::vector<uint8_t> flags;
       flags.assign(256 * 256, 0);
-      for (int ld = -16; ld <= 16; ld++) {
+      for (int ld = -amount; ld <= amount; ld++) {
         const int l = (int)a.first + ld;
         if (l < 0) continue;
         if (l > 255) break;
-        for (int hd = -16; hd <= 16; hd++) {
+        for (int hd = -amount; hd <= amount; hd++) {
           const int h = (int)a.second + hd;
           if (h < 0) continue;
           if (h > 255) break;
@@ -145,6 +147,15 @@ extern "C" int oracle_dxt5a_blocks(const uint8_t* blocks, uint32_t n, int comp, 
                                    uint8_t* out, int threads) {
   (void)threads;
   for (uint32_t i = 0; i < n; i++)
-    crn_oracle_detail::dxt5a_block(blocks + (size_t)i * 64, comp, use_both_block_types != 0, out + (size_t)i * 8);
+    crn_oracle_detail::dxt5a_block(blocks + (size_t)i * 64, comp, use_both_block_types != 0, out + (size_t)i * 8, 4);
+  return 0;
+}
+
+extern "C" int oracle_dxt5a_blocks_q(const uint8_t* blocks, uint32_t n, int comp, int use_both_block_types,
+                                     int quality, uint8_t* out) {
+  if (quality < 0 || quality > 4) return -1;
+  for (uint32_t i = 0; i < n; i++)
+    crn_oracle_detail::dxt5a_block(blocks + (size_t)i * 64, comp, use_both_block_types != 0, out + (size_t)i * 8,
+                                   quality);
   return 0;
 }

@@ -13,6 +13,12 @@ _PATH = os.path.join(_HERE, "_build", "libcrnoracle.so")
 _lib = None
 
 
+class Dxt1Opts(ctypes.Structure):
+    """oracle_dxt1_opts (crn_oracle.h)"""
+    _fields_ = [(n, ctypes.c_int) for n in ("perceptual", "use_alpha_blocks", "quality", "grayscale", "dxt1a",
+                                            "alpha_threshold", "transparent_black")]
+
+
 def build() -> str:
     """Compiles the restatement (make port); returns the library path."""
     subprocess.run(["make", "-s", "-C", _HERE, "port"], check=True)
@@ -30,6 +36,10 @@ def lib():
         L.oracle_dxt1_blocks.restype = i32
         L.oracle_dxt5a_blocks.argtypes = [vp, u32, i32, i32, vp, i32]
         L.oracle_dxt5a_blocks.restype = i32
+        L.oracle_dxt1_blocks_ex.argtypes = [vp, u32, ctypes.POINTER(Dxt1Opts), vp, vp, i32]
+        L.oracle_dxt1_blocks_ex.restype = i32
+        L.oracle_dxt5a_blocks_q.argtypes = [vp, u32, i32, i32, i32, vp]
+        L.oracle_dxt5a_blocks_q.restype = i32
         L.oracle_encode_blocks.argtypes = [vp, u32, i32, i32, i32, vp, i32]
         L.oracle_encode_blocks.restype = i32
         L.oracle_unpack_level.argtypes = [vp, u32, u32, vp, u32, u32]
@@ -48,6 +58,32 @@ def dxt1_blocks(blocks: np.ndarray, perceptual: bool = True, use_alpha_blocks: b
     lib().oracle_dxt1_blocks(blocks.ctypes.data, n, int(perceptual), int(use_alpha_blocks), out.ctypes.data,
                              err.ctypes.data, threads)
     return out, err
+
+
+def dxt1_blocks_ex(blocks: np.ndarray, perceptual: bool = True, use_alpha_blocks: bool = True, quality: int = 4,
+                   grayscale: bool = False, dxt1a: bool = False, alpha_threshold: int = 128,
+                   transparent_black: bool = False, threads: int = 1):
+    """DXT1 blocks with every block-compressor parameter (quality 0 superfast .. 4 uber)."""
+    blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+    n = blocks.shape[0]
+    out = np.zeros((n, 8), np.uint8)
+    err = np.zeros(n, np.uint64)
+    o = Dxt1Opts(int(perceptual), int(use_alpha_blocks), int(quality), int(grayscale), int(dxt1a),
+                 int(alpha_threshold), int(transparent_black))
+    if lib().oracle_dxt1_blocks_ex(blocks.ctypes.data, n, ctypes.byref(o), out.ctypes.data, err.ctypes.data,
+                                   threads) != 0:
+        raise ValueError("bad DXT1 options")
+    return out, err
+
+
+def dxt5a_blocks(blocks: np.ndarray, comp: int, use_both_block_types: bool = True, quality: int = 4) -> np.ndarray:
+    blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+    n = blocks.shape[0]
+    out = np.zeros((n, 8), np.uint8)
+    if lib().oracle_dxt5a_blocks_q(blocks.ctypes.data, n, comp, int(use_both_block_types), quality,
+                                   out.ctypes.data) != 0:
+        raise ValueError("bad quality")
+    return out
 
 
 def encode_blocks(blocks: np.ndarray, fmt: int, perceptual: bool = True, use_both_block_types: bool = True,

@@ -10,6 +10,8 @@ thread count. Inputs come from crunch2_gb300.texgen (seeded, platform-independen
 
 Outputs (all small; committed):
   blocks.npz        edge-case + texture block inputs and the reference DXT1/DXT5/DXN/DXT5A blocks
+  blocks_quality.npz  the same below Uber quality, with grayscale sampling, DXT1A transparency and
+                    transparent indices for black
   crn/*.crn         reference .crn files; crn/manifest.json holds per-level sha256 of the
                     reference transcode and the generation parameters
 Run:  python tests/golden/make_golden.py
@@ -90,6 +92,75 @@ def make_blocks() -> None:
                                              base | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES, DXT_UBER, 7), np.uint8)
     assert np.array_equal(dds[128:128 + out["c0_dxt1"].size].reshape(-1, 8), out["c0_dxt1"]), "dds != block api"
     np.savez_compressed(os.path.join(HERE, "blocks.npz"), **out)
+
+
+FLAG_TRANSPARENT_BLACK = 16
+FLAG_DXT1A = 128
+FLAG_GRAYSCALE = 256
+QUALITIES = (0, 1, 2, 3)  # superfast, fast, normal, better (uber is in blocks.npz)
+
+
+def alpha_blocks(seed: int = 2) -> np.ndarray:
+    """DXT1A inputs: the edge blocks with 0..4 texels below the 128 alpha threshold, fully
+    transparent blocks, and single-colour blocks with a few transparent texels."""
+    rng = np.random.default_rng(seed)
+    b = edge_blocks(seed).reshape(-1, 16, 4).copy()
+    b[:, :, 3] = 255
+    for i in range(b.shape[0]):
+        k = int(rng.integers(0, 5))
+        b[i, rng.choice(16, k, replace=False), 3] = rng.integers(0, 128, k)
+    clear = rng.integers(0, 256, (40, 16, 4), dtype=np.uint8)
+    clear[:, :, 3] = rng.integers(0, 128, (40, 16))
+    solid = rng.integers(0, 256, (80, 1, 4), dtype=np.uint8).repeat(16, 1)
+    solid[:, :, 3] = 255
+    for i in range(solid.shape[0]):
+        solid[i, rng.choice(16, 1 + i % 6, replace=False), 3] = 0
+    return np.ascontiguousarray(np.concatenate([b, clear, solid]).reshape(-1, 64))
+
+
+def dark_blocks(seed: int = 3) -> np.ndarray:
+    """Inputs for the transparent-black trial: blocks mixing near-black texels (every channel
+    <= 4) with other colours, plus the edge set."""
+    rng = np.random.default_rng(seed)
+    n = 600
+    b = rng.integers(0, 256, (n, 16, 4), dtype=np.uint8)
+    for i in range(n):
+        if i % 3 == 0:  # a few colours in the block, as textures with dark outlines have
+            pal = rng.integers(0, 256, (3, 4), dtype=np.uint8)
+            b[i] = pal[rng.integers(0, 3, 16)]
+        k = int(rng.integers(1, 16))
+        b[i, rng.choice(16, k, replace=False), :3] = rng.integers(0, 5, (k, 3))
+    return np.ascontiguousarray(np.concatenate([b.reshape(n, 64), edge_blocks(seed)]))
+
+
+def make_quality() -> None:
+    """The reference block compressor below Uber quality, with grayscale sampling, DXT1A
+    transparency and transparent indices for black: blocks_quality.npz."""
+    edge, alpha, dark = edge_blocks(), alpha_blocks(), dark_blocks()
+    out = {"alpha_in": alpha, "dark_in": dark}
+    base = FLAG_HIERARCHICAL | FLAG_NO_ENDPOINT_CACHING
+    for q in QUALITIES:
+        for perc in (1, 0):
+            for both in (1, 0):
+                flags = base | (FLAG_PERCEPTUAL if perc else 0) | (FLAG_BOTH_BLOCK_TYPES if both else 0)
+                out[f"dxt1_q{q}_p{perc}_b{both}"] = ref.compress_blocks(edge, FMT["DXT1"], flags, q)
+        for name in ("DXT5", "DXN_XY", "DXT5A"):
+            for both in (1, 0):
+                flags = base | FLAG_PERCEPTUAL | (FLAG_BOTH_BLOCK_TYPES if both else 0)
+                out[f"{name.lower()}_q{q}_b{both}"] = ref.compress_blocks(edge, FMT[name], flags, q)
+    for q in (4, 3, 1):
+        for both in (1, 0):
+            flags = base | FLAG_PERCEPTUAL | FLAG_GRAYSCALE | (FLAG_BOTH_BLOCK_TYPES if both else 0)
+            out[f"gray_q{q}_b{both}"] = ref.compress_blocks(edge, FMT["DXT1"], flags, q)
+        for perc in (1, 0):
+            for both in (1, 0):
+                flags = base | FLAG_DXT1A | (FLAG_PERCEPTUAL if perc else 0) | (FLAG_BOTH_BLOCK_TYPES if both else 0)
+                out[f"dxt1a_q{q}_p{perc}_b{both}"] = ref.compress_blocks(alpha, FMT["DXT1"], flags, q)
+            flags = base | FLAG_TRANSPARENT_BLACK | FLAG_BOTH_BLOCK_TYPES | (FLAG_PERCEPTUAL if perc else 0)
+            out[f"black_q{q}_p{perc}"] = ref.compress_blocks(dark, FMT["DXT1"], flags, q)
+        flags = base | FLAG_TRANSPARENT_BLACK | FLAG_BOTH_BLOCK_TYPES | FLAG_GRAYSCALE
+        out[f"black_gray_q{q}"] = ref.compress_blocks(dark, FMT["DXT1"], flags, q)
+    np.savez_compressed(os.path.join(HERE, "blocks_quality.npz"), **out)
 
 
 # (name, width, height, format, faces, content, seed)
@@ -407,6 +478,9 @@ def make_config2() -> None:
 if __name__ == "__main__":
     if not ref.available():
         sys.exit("oracle/_ref/libcrnref.so missing: run `make -C oracle ref` where the reference tree exists")
+    if sys.argv[1:] == ["quality"]:
+        make_quality()
+        sys.exit(0)
     if sys.argv[1:] == ["config2"]:
         make_config2()
         sys.exit(0)
@@ -423,6 +497,7 @@ if __name__ == "__main__":
         make_hc(alpha_only=True)
         sys.exit(0)
     make_blocks()
+    make_quality()
     make_crn()
     make_hc()
     make_config2()

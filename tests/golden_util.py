@@ -16,6 +16,13 @@ def blocks() -> dict:
         return {k: z[k] for k in z.files}
 
 
+def blocks_quality() -> dict:
+    """The reference block compressor below Uber, with grayscale sampling, DXT1A transparency and
+    transparent indices for black (tests/golden/make_golden.py quality)."""
+    with np.load(os.path.join(GOLDEN, "blocks_quality.npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
 def manifest() -> dict:
     with open(os.path.join(GOLDEN, "crn", "manifest.json")) as fh:
         return json.load(fh)

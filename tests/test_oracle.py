@@ -70,3 +70,64 @@ def test_transcode_rejects_bad_input():
     assert port.unpack_level(crn, 0, size - 8) is None           # destination too small
     assert port.unpack_level(crn, 0, size, row_pitch=6) is None  # pitch not a multiple of 4
     assert port.unpack_level(crn, 99, size) is None              # level out of range
+
+
+# ------------------------------------------------------------------------------------------
+# below Uber quality, grayscale sampling, DXT1A transparency, transparent indices for black
+# (tests/golden/blocks_quality.npz, made by the reference block compressor)
+
+@pytest.fixture(scope="module")
+def goldq():
+    return G.blocks_quality()
+
+
+@pytest.mark.parametrize("q", [0, 1, 2, 3])
+@pytest.mark.parametrize("perc", [1, 0])
+@pytest.mark.parametrize("both", [1, 0])
+def test_dxt1_quality_levels(gold, goldq, q, perc, both):
+    out, _ = port.dxt1_blocks_ex(gold["edge_in"], bool(perc), bool(both), quality=q, threads=4)
+    ref = goldq[f"dxt1_q{q}_p{perc}_b{both}"]
+    assert np.array_equal(out, ref), np.nonzero((out != ref).any(1))[0][:10]
+
+
+@pytest.mark.parametrize("q", [0, 1, 2, 3])
+@pytest.mark.parametrize("name", ["dxt5", "dxn_xy", "dxt5a"])
+@pytest.mark.parametrize("both", [1, 0])
+def test_alpha_formats_quality_levels(gold, goldq, q, name, both):
+    edge = gold["edge_in"]
+    ref = goldq[f"{name}_q{q}_b{both}"]
+    if name == "dxt5":
+        alpha = port.dxt5a_blocks(edge, 3, bool(both), q)
+        colour, _ = port.dxt1_blocks_ex(edge, True, False, quality=q, threads=4)
+        out = np.concatenate([alpha, colour], 1)
+    elif name == "dxn_xy":
+        out = np.concatenate([port.dxt5a_blocks(edge, 0, bool(both), q), port.dxt5a_blocks(edge, 1, bool(both), q)], 1)
+    else:
+        out = port.dxt5a_blocks(edge, 3, bool(both), q)
+    assert np.array_equal(out, ref), np.nonzero((out != ref).any(1))[0][:10]
+
+
+@pytest.mark.parametrize("q", [4, 3, 1])
+@pytest.mark.parametrize("both", [1, 0])
+def test_dxt1_grayscale_sampling(gold, goldq, q, both):
+    out, _ = port.dxt1_blocks_ex(gold["edge_in"], True, bool(both), quality=q, grayscale=True, threads=4)
+    ref = goldq[f"gray_q{q}_b{both}"]
+    assert np.array_equal(out, ref), np.nonzero((out != ref).any(1))[0][:10]
+
+
+@pytest.mark.parametrize("q", [4, 3, 1])
+@pytest.mark.parametrize("perc", [1, 0])
+@pytest.mark.parametrize("both", [1, 0])
+def test_dxt1a_transparency(goldq, q, perc, both):
+    out, _ = port.dxt1_blocks_ex(goldq["alpha_in"], bool(perc), bool(both), quality=q, dxt1a=True, threads=4)
+    ref = goldq[f"dxt1a_q{q}_p{perc}_b{both}"]
+    assert np.array_equal(out, ref), np.nonzero((out != ref).any(1))[0][:10]
+
+
+@pytest.mark.parametrize("q", [4, 3, 1])
+@pytest.mark.parametrize("mode", ["p1", "p0", "gray"])
+def test_dxt1_transparent_indices_for_black(goldq, q, mode):
+    out, _ = port.dxt1_blocks_ex(goldq["dark_in"], mode == "p1", True, quality=q, grayscale=(mode == "gray"),
+                                 transparent_black=True, threads=4)
+    ref = goldq[f"black_q{q}_{mode}" if mode != "gray" else f"black_gray_q{q}"]
+    assert np.array_equal(out, ref), np.nonzero((out != ref).any(1))[0][:10]
