@@ -32,6 +32,9 @@ OK, E_PARAM, E_CORRUPT, E_DEVICE, E_UNSUPPORTED = 0, -1, -2, -3, -4
 MEM_HOST, MEM_DEVICE = 0, 1
 FMT_DXT1, FMT_DXT5, FMT_DXN_XY, FMT_DXN_YX, FMT_DXT5A = 0, 2, 7, 8, 9
 FLAG_PERCEPTUAL, FLAG_USE_BOTH_BLOCK_TYPES = 1, 8
+FLAG_TRANSPARENT_BLACK, FLAG_DXT1A, FLAG_GRAYSCALE = 16, 128, 256
+# crn_dxt_quality
+DXT_SUPERFAST, DXT_FAST, DXT_NORMAL, DXT_BETTER, DXT_UBER = 0, 1, 2, 3, 4
 
 
 class CrnGpuError(RuntimeError):
@@ -41,8 +44,17 @@ class CrnGpuError(RuntimeError):
 
 
 class _Dxt1Params(ctypes.Structure):
+    """crngpu_dxt1_params"""
     _fields_ = [("struct_size", ctypes.c_uint32), ("perceptual", ctypes.c_int32),
-                ("use_alpha_blocks", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("use_alpha_blocks", ctypes.c_int32), ("reserved", ctypes.c_int32), ("dxt_quality", ctypes.c_uint32),
+                ("grayscale_sampling", ctypes.c_int32), ("dxt1a", ctypes.c_int32),
+                ("dxt1a_alpha_threshold", ctypes.c_uint32), ("use_transparent_indices_for_black", ctypes.c_int32)]
+
+
+class _BlockOptions(ctypes.Structure):
+    """crngpu_block_options"""
+    _fields_ = [("struct_size", ctypes.c_uint32), ("dxt_quality", ctypes.c_uint32),
+                ("dxt1a_alpha_threshold", ctypes.c_uint32)]
 
 
 _lib = None
@@ -93,6 +105,11 @@ def lib():
     L.crngpu_compress_blocks.restype = i32
     L.crngpu_compress_image.argtypes = [vp, u32, u32, u32, u32, u32, vp, u64, i32, vp]
     L.crngpu_compress_image.restype = i64
+    L.crngpu_compress_blocks_ex.argtypes = [vp, u32, u32, u32, ctypes.POINTER(_BlockOptions), vp, i32, vp]
+    L.crngpu_compress_blocks_ex.restype = i32
+    L.crngpu_compress_image_ex.argtypes = [vp, u32, u32, u32, u32, u32, ctypes.POINTER(_BlockOptions), vp, u64, i32,
+                                           vp]
+    L.crngpu_compress_image_ex.restype = i64
     L.crngpu_unpack_begin.argtypes = [vp, u32]
     L.crngpu_unpack_begin.restype = vp
     L.crngpu_get_info.argtypes = [vp] + [ctypes.POINTER(u32)] * 6
@@ -232,13 +249,17 @@ def _out_like(inp, shape, dtype=np.uint8):
 # Block encoders
 
 def dxt1_optimize(blocks, perceptual: bool = True, use_alpha_blocks: bool = True, with_error: bool = False,
-                  stream=None):
-    """(n, 64) RGBA8 blocks -> (n, 8) dxt1 blocks [, (n,) squared errors]."""
+                  stream=None, quality: int = DXT_UBER, grayscale: bool = False, dxt1a: bool = False,
+                  alpha_threshold: int = 128, transparent_black: bool = False):
+    """(n, 64) RGBA8 blocks -> (n, 8) dxt1 blocks [, (n,) squared errors]: dxt1_endpoint_optimizer
+    at crn_dxt_quality `quality`, optionally with grayscale sampling, DXT1A transparency (texels
+    with alpha below alpha_threshold) and transparent indices for black."""
     blocks = _contiguous(blocks)
     n = int(blocks.shape[0])
     out = _out_like(blocks, (n, 8))
     err = _out_like(blocks, (n,), np.uint64) if with_error else None
-    p = _Dxt1Params(ctypes.sizeof(_Dxt1Params), int(perceptual), int(use_alpha_blocks), 0)
+    p = _Dxt1Params(ctypes.sizeof(_Dxt1Params), int(perceptual), int(use_alpha_blocks), 0, int(quality),
+                    int(grayscale), int(dxt1a), int(alpha_threshold), int(transparent_black))
     ip, mem = _ptr_mem(blocks)
     op, _ = _ptr_mem(out)
     ep = _ptr_mem(err)[0] if err is not None else None
@@ -262,19 +283,22 @@ def bytes_per_block(fmt: int) -> int:
     return 8 if fmt in (FMT_DXT1, FMT_DXT5A) else 16
 
 
-def compress_blocks(blocks, fmt: int, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES, stream=None):
-    """Batched crn_compress_block: (n, 64) RGBA8 -> (n, 8|16) DXTn blocks."""
+def compress_blocks(blocks, fmt: int, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES, stream=None,
+                    quality: int = DXT_UBER, alpha_threshold: int = 128):
+    """Batched crn_compress_block: (n, 64) RGBA8 -> (n, 8|16) DXTn blocks (crn_comp_flags `flags`,
+    crn_dxt_quality `quality`, m_dxt1a_alpha_threshold `alpha_threshold`)."""
     blocks = _contiguous(blocks)
     n = int(blocks.shape[0])
     out = _out_like(blocks, (n, bytes_per_block(fmt)))
     ip, mem = _ptr_mem(blocks)
-    _check(lib().crngpu_compress_blocks(ip, n, fmt, flags, _ptr_mem(out)[0], mem, _stream_ptr(stream)),
-           "crngpu_compress_blocks")
+    o = _BlockOptions(ctypes.sizeof(_BlockOptions), int(quality), int(alpha_threshold))
+    _check(lib().crngpu_compress_blocks_ex(ip, n, fmt, flags, ctypes.byref(o), _ptr_mem(out)[0], mem,
+                                           _stream_ptr(stream)), "crngpu_compress_blocks_ex")
     return out
 
 
 def compress_image(rgba, fmt: int = FMT_DXT1, flags: int = FLAG_PERCEPTUAL | FLAG_USE_BOTH_BLOCK_TYPES,
-                   out=None, stream=None):
+                   out=None, stream=None, quality: int = DXT_UBER, alpha_threshold: int = 128):
     """Plain DXTn encode of an (h, w, 4) RGBA8 image -> (blocks_y * blocks_x, 8|16) blocks."""
     rgba = _contiguous(rgba)
     h, w = int(rgba.shape[0]), int(rgba.shape[1])
@@ -282,8 +306,10 @@ def compress_image(rgba, fmt: int = FMT_DXT1, flags: int = FLAG_PERCEPTUAL | FLA
     if out is None:
         out = _out_like(rgba, (n, bytes_per_block(fmt)))
     ip, mem = _ptr_mem(rgba)
-    _check(lib().crngpu_compress_image(ip, w, h, 0, fmt, flags, _ptr_mem(out)[0], n * bytes_per_block(fmt), mem,
-                                       _stream_ptr(stream)), "crngpu_compress_image")
+    o = _BlockOptions(ctypes.sizeof(_BlockOptions), int(quality), int(alpha_threshold))
+    _check(lib().crngpu_compress_image_ex(ip, w, h, 0, fmt, flags, ctypes.byref(o), _ptr_mem(out)[0],
+                                          n * bytes_per_block(fmt), mem, _stream_ptr(stream)),
+           "crngpu_compress_image_ex")
     return out
 
 

@@ -81,6 +81,24 @@ struct EncodeSegment {
   uint32_t first_block, count, stride, options;
 };
 constexpr uint32_t kSegPerceptual = 1u, kSegThreeColour = 2u, kSegBothTypes = 4u, kSegCompShift = 8u;
+// DXT1 encoder options (the options word of a launch, and of a colour segment): the parameters
+// dxt_image::set_block_pixels gives dxt1_endpoint_optimizer (crnlib/crn_dxt_image.cpp:1436-1480)
+constexpr uint32_t kD1Perceptual = 1u;      // m_perceptual (never set together with kD1Gray)
+constexpr uint32_t kD1Three = 2u;           // m_use_alpha_blocks: 3-colour blocks allowed
+constexpr uint32_t kD1Gray = 4u;            // m_grayscale_sampling: luma distance
+constexpr uint32_t kD1Dxt1a = 8u;           // DXT1A: texels with alpha below the threshold are transparent
+constexpr uint32_t kD1BlackTrial = 16u;     // the transparent-black trial of try_alpha_as_black_optimization
+constexpr uint32_t kD1QualityShift = 8u;    // bits 8-10: crn_dxt_quality (0 superfast .. 4 uber)
+constexpr uint32_t kD1ThresholdShift = 16u; // bits 16-23: m_dxt1a_alpha_threshold
+// alpha segments: crn_dxt_quality in bits 12-14 (the probe grid of dxt5_endpoint_optimizer)
+constexpr uint32_t kSegAlphaQualityShift = 12u;
+constexpr uint32_t kDxtQualityUber = 4u, kDxtQualityBetter = 3u, kDxtQualityNormal = 2u;
+inline uint32_t dxt1_options(bool perceptual, bool use_alpha_blocks, uint32_t quality, bool grayscale, bool dxt1a,
+                             uint32_t alpha_threshold) {
+  return (perceptual && !grayscale ? kD1Perceptual : 0u) | (use_alpha_blocks ? kD1Three : 0u) |
+         (grayscale ? kD1Gray : 0u) | (dxt1a ? kD1Dxt1a : 0u) | ((quality & 7u) << kD1QualityShift) |
+         ((alpha_threshold & 255u) << kD1ThresholdShift);
+}
 // a run of consecutive blocks of one segment, the unit a warp takes
 struct EncodeChunk {
   uint32_t first, count, segment;
@@ -88,6 +106,17 @@ struct EncodeChunk {
 constexpr uint32_t kColourChunkBlocks = 8;  // blocks per DXT1 chunk (the encoder's blocks per warp)
 int dxt1_chunks_max_grid();
 int dxt5a_chunks_max_grid();
+// DXT1 / DXT5A block encoders on device buffers (dxt_encode.cu). launch_dxt1: opts is a
+// dxt1_options() word; d_err (optional) receives each block's error. launch_dxt1_black_trial: the
+// transparent-black trial over blocks already encoded with the same options (d_err_io their
+// errors): a block whose trial is better is rewritten in place, with its new error.
+// launch_dxt5a: quality sets the probe grid (+-16 Uber, +-8 Better, none below).
+int launch_dxt1(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
+                uint64_t* d_err, cudaStream_t s);
+int launch_dxt1_black_trial(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
+                            uint64_t* d_err_io, cudaStream_t s);
+int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint32_t quality, uint8_t* d_out,
+                 uint32_t out_stride, cudaStream_t s);
 int launch_dxt1_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,
                        const EncodeSegment* d_segs, int grid, cudaStream_t s);
 int launch_dxt5a_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,

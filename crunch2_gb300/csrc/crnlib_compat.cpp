@@ -222,14 +222,18 @@ void* compress(const crn_comp_params& p, crn_uint32& compressed_size, crn_uint32
     set_error("crn_compress: ETC and DXT3 output are not built");
     return nullptr;
   }
-  if ((p.m_flags & cCRNCompFlagDXT1AForTransparency) && p.m_format == cCRNFmtDXT1) {
-    set_error("crn_compress: DXT1A (alpha-threshold transparency) output is not built");
-    return nullptr;
-  }
   std::vector<uint8_t> images;
   if (!gather_images(p, images)) return nullptr;
   const uint32_t fmt = (uint32_t)p.m_format;
-  const uint32_t flags = p.m_flags & (CRNGPU_FLAG_PERCEPTUAL | CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES);
+  // crn_comp reads only the perceptual and block-type flags (.crn files never hold 3-colour
+  // blocks); dds_comp's plain encoder also honours DXT1A, grayscale sampling and transparent
+  // indices for black, with m_dxt_quality and m_dxt1a_alpha_threshold (dxt_image::pack_params::init,
+  // crnlib/crn_dxt_image.h:197-207)
+  const uint32_t crn_flags = p.m_flags & (CRNGPU_FLAG_PERCEPTUAL | CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES);
+  const uint32_t dds_flags =
+      p.m_flags & (CRNGPU_FLAG_PERCEPTUAL | CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES | CRNGPU_FLAG_TRANSPARENT_BLACK |
+                   CRNGPU_FLAG_DXT1A | CRNGPU_FLAG_GRAYSCALE);
+  const uint32_t flags = crn_flags;
   if (!progress(p, 0, 2)) {
     set_error("crn_compress: cancelled by the progress callback");
     return nullptr;
@@ -273,8 +277,12 @@ void* compress(const crn_comp_params& p, crn_uint32& compressed_size, crn_uint32
       data += (uint64_t)((std::max(1u, p.m_width >> l) + 3) / 4) * ((std::max(1u, p.m_height >> l) + 3) / 4) * bpb;
     data *= p.m_faces;
     file.resize((size_t)(128 + data));
-    const int64_t n = crngpu_compress_dds_clustered(images.data(), p.m_width, p.m_height, p.m_levels, p.m_faces, fmt,
-                                                    p.m_quality_level, flags, file.data() + 128, data);
+    crngpu_block_options bo;
+    bo.struct_size = sizeof(bo);
+    bo.dxt_quality = (uint32_t)p.m_dxt_quality;
+    bo.dxt1a_alpha_threshold = p.m_dxt1a_alpha_threshold;
+    const int64_t n = crngpu_compress_dds_clustered_ex(images.data(), p.m_width, p.m_height, p.m_levels, p.m_faces,
+                                                       fmt, p.m_quality_level, dds_flags, &bo, file.data() + 128, data);
     if (n < 0) return nullptr;
     dds_header(file.data(), p.m_width, p.m_height, p.m_levels, p.m_faces, p.m_format);
     quality = p.m_quality_level;
@@ -509,12 +517,14 @@ const char* crn_get_scale_mode_desc(crn_scale_mode sm) {
 }
 
 // The block compressor: one context per caller thread in the reference; here a context holds the
-// format and flags, and each call encodes its block on the GPU (no endpoint cache, so the output
-// does not depend on the blocks compressed before).
+// format, flags, dxt quality and DXT1A threshold, and each call encodes its block on the GPU (no
+// endpoint cache, so the output does not depend on the blocks compressed before). Each call is one
+// launch and one synchronisation: callers with many blocks should use crngpu_compress_blocks_ex.
 namespace {
 struct BlockCompressor {
   uint32_t magic;
   uint32_t format, flags;
+  crngpu_block_options options;
 };
 constexpr uint32_t kBlockMagic = 0x424C4B43u;  // "BLKC"
 }  // namespace
@@ -522,26 +532,33 @@ constexpr uint32_t kBlockMagic = 0x424C4B43u;  // "BLKC"
 crn_block_compressor_context_t crn_create_block_compressor(const crn_comp_params& params) {
   crngpu::clear_error();
   const crn_format fund = crnd::crnd_get_fundamental_dxt_format(params.m_format);
-  if (!format_supported(params.m_format) ||
-      ((params.m_flags & cCRNCompFlagDXT1AForTransparency) && fund == cCRNFmtDXT1)) {
-    set_error("crn_create_block_compressor: format not built");
+  if (!format_supported(params.m_format) || (uint32_t)params.m_dxt_quality > (uint32_t)cCRNDXTQualityUber ||
+      params.m_dxt1a_alpha_threshold > 255) {
+    set_error("crn_create_block_compressor: format not built or parameters out of range");
     return nullptr;
   }
   BlockCompressor* c = new (std::nothrow) BlockCompressor;
   if (!c) return nullptr;
   c->magic = kBlockMagic;
-  // dxt_image::pack_params::init takes perceptual and both-block-types from the flags; the
-  // swizzled DXT5 formats encode as plain DXT5 blocks (crnlib/crnlib.cpp:369-381)
+  // dxt_image::pack_params::init (crnlib/crn_dxt_image.h:197-207) takes the perceptual,
+  // both-block-types, transparent-black and grayscale flags, the dxt quality and the DXT1A
+  // threshold; crn_block_compressor::init encodes DXT1 as DXT1A when the DXT1A flag is set; the
+  // swizzled DXT5 formats encode as plain DXT5 blocks (crnlib/crnlib.cpp:358-381)
   c->format = (uint32_t)fund;
-  c->flags = params.m_flags & (CRNGPU_FLAG_PERCEPTUAL | CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES);
+  c->flags = params.m_flags & (CRNGPU_FLAG_PERCEPTUAL | CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES |
+                               CRNGPU_FLAG_TRANSPARENT_BLACK | CRNGPU_FLAG_GRAYSCALE);
+  if ((params.m_flags & cCRNCompFlagDXT1AForTransparency) && fund == cCRNFmtDXT1) c->flags |= CRNGPU_FLAG_DXT1A;
+  c->options.struct_size = sizeof(crngpu_block_options);
+  c->options.dxt_quality = (uint32_t)params.m_dxt_quality;
+  c->options.dxt1a_alpha_threshold = params.m_dxt1a_alpha_threshold;
   return c;
 }
 
 void crn_compress_block(crn_block_compressor_context_t pContext, const crn_uint32* pPixels, void* pDst_block) {
   BlockCompressor* c = static_cast<BlockCompressor*>(pContext);
   if (!c || c->magic != kBlockMagic || !pPixels || !pDst_block) return;
-  crngpu_compress_blocks(reinterpret_cast<const uint8_t*>(pPixels), 1, c->format, c->flags,
-                         static_cast<uint8_t*>(pDst_block), CRNGPU_MEM_HOST, nullptr);
+  crngpu_compress_blocks_ex(reinterpret_cast<const uint8_t*>(pPixels), 1, c->format, c->flags, &c->options,
+                            static_cast<uint8_t*>(pDst_block), CRNGPU_MEM_HOST, nullptr);
 }
 
 void crn_free_block_compressor(crn_block_compressor_context_t pContext) {

@@ -43,7 +43,15 @@ constexpr uint32_t kInf = 0xFFFFFFFFu;
 struct SingleColour { uint8_t m5[256][2], m6[256][2], m5_3[256][2], m6_3[256][2]; };
 __constant__ SingleColour c_sct;
 
-__constant__ int16_t c_uber_probe[15] = {0, 1, 2, 3, 5, 7, 9, 10, 13, 15, 19, 27, 43, 59, 91};
+// probe tables of optimize_endpoints per quality (crnlib/crn_dxt1.cpp:43-53): superfast and fast,
+// normal, better, uber; with their sizes and the probe spacing (:716-745)
+__constant__ int16_t c_probe[4][15] = {{0, 1, 2, 3},
+                                       {0, 1, 3, 5, 7},
+                                       {0, 1, 2, 3, 5, 9, 15, 19, 27, 43},
+                                       {0, 1, 2, 3, 5, 7, 9, 10, 13, 15, 19, 27, 43, 59, 91}};
+__constant__ int c_probe_size[4] = {4, 5, 10, 15};
+constexpr uint32_t kQSuperFast = 0, kQFast = 1, kQNormal = 2, kQBetter = 3, kQUber = 4;
+__device__ __forceinline__ int probe_table(uint32_t q) { return q <= kQFast ? 0 : (int)q - 1; }
 
 // ------------------------------------------------------------------------------------------
 // small helpers
@@ -73,6 +81,11 @@ struct Sol {
 struct State {
   Sol best, snap;  // snap: the best at the last compute_selectors() (hc path)
   int n, hc, three;
+  int only3;    // the block has transparent texels: 3-colour blocks only (first_block_type 1)
+  int fast;     // evaluate_solution_fast (below Better quality, no hc)
+  int gray;     // grayscale sampling: distances between luma values
+  int quality;  // crn_dxt_quality
+  int perceptual;
   float wr, wg;
 };
 
@@ -105,7 +118,7 @@ struct WarpShared {
   // phase-1 hand-off, one slot per block of the warp's chunk
   float p1f[kBlocksPerWarp][9];     // axis[3], low[3], high[3]
   uint32_t p1m[kBlocksPerWarp][6];  // try_median4 candidates (lo | hi << 16)
-  int p1n[kBlocksPerWarp];          // unique colour count
+  int p1n[kBlocksPerWarp];          // unique colour count (-1: the block is not tried)
   // phase-1 scratch, transposed [i][lane] so lanes never share a bank
   uint32_t t_col[16][kBlocksPerWarp];
   uint8_t t_w[16][kBlocksPerWarp];
@@ -166,10 +179,26 @@ struct FastRandom {
   }
 };
 
+// A near-black texel of try_alpha_as_black_optimization (crnlib/crn_dxt1.cpp:2009-2030): every
+// colour channel at most 4.
+__device__ __forceinline__ bool is_dark(uint32_t c) {
+  return (c & 0xFFu) <= 4u && ((c >> 8) & 0xFFu) <= 4u && ((c >> 16) & 0xFFu) <= 4u;
+}
+
+// Whether texel c is left out of the search as transparent: DXT1A texels whose alpha is below the
+// threshold, and in the transparent-black trial also the near-black texels (whose alpha the trial
+// sets to 0).
+__device__ __forceinline__ bool is_transparent(uint32_t c, uint32_t opts) {
+  if (!(opts & (kD1Dxt1a | kD1BlackTrial))) return false;
+  const uint32_t a = ((opts & kD1BlackTrial) && is_dark(c)) ? 0u : (c >> 24);
+  return a < ((opts >> kD1ThresholdShift) & 255u);
+}
+
 // Runs handle_multicolor_block up to optimize_endpoints' entry, plus try_median4's seeds.
-__device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, bool perceptual) {
+__device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, uint32_t opts) {
   const int L = slot;
-  // unique colours in first-occurrence order (compute_internal :2113-2131)
+  const bool perceptual = (opts & kD1Perceptual) != 0;
+  const uint32_t quality = (opts >> kD1QualityShift) & 7u;
   int n = 0;
   uint32_t pix[16];
   {
@@ -179,17 +208,38 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
       pix[4 * q] = v.x; pix[4 * q + 1] = v.y; pix[4 * q + 2] = v.z; pix[4 * q + 3] = v.w;
     }
   }
+  if (opts & kD1BlackTrial) {
+    // the trial runs for blocks without real transparency whose unique colours (alpha ignored)
+    // are neither free of near-black ones nor all near-black (:2005-2019)
+    int dark = 0;
+    bool has_t = false;
+    #pragma unroll 1
+    for (int p = 0; p < 16; p++) {
+      const uint32_t c = pix[p] & 0xFFFFFFu;
+      has_t |= (opts & kD1Dxt1a) && (pix[p] >> 24) < ((opts >> kD1ThresholdShift) & 255u);
+      int i = 0;
+      for (; i < n; i++) if (S.t_col[i][L] == c) break;
+      if (i == n) { S.t_col[n][L] = c; n++; dark += is_dark(c) ? 1 : 0; }
+    }
+    if (has_t || !dark || dark == n) { S.p1n[L] = -1; return; }
+    n = 0;
+  }
+  // unique colours of the opaque texels in first-occurrence order (compute_internal :2113-2131)
+  int opaque = 0;
   #pragma unroll 1
   for (int p = 0; p < 16; p++) {
+    if (is_transparent(pix[p], opts)) continue;
     const uint32_t c = pix[p] & 0xFFFFFFu;
+    opaque++;
     int i = 0;
     for (; i < n; i++) if (S.t_col[i][L] == c) break;
     if (i == n) { S.t_col[n][L] = c; S.t_w[n][L] = 1; n++; }
     else S.t_w[i][L]++;
   }
   S.p1n[L] = n;
-  if (n <= 1) return;
-  const float total = 16.0f;
+  // no opaque texel, or one colour and no transparency (compute_internal :2205-2227): no search
+  if (n == 0 || (n == 1 && opaque == 16)) return;
+  const float total = (float)opaque;  // m_total_unique_color_weight
   // perceptual weights (:1074-1108); powf restated as the correctly rounded float of pow()
   int passes = 1;
   float pw[3] = {1.0f, 1.0f, 1.0f};
@@ -337,7 +387,8 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
     S.p1f[L][3 + k] = low[k];
     S.p1f[L][6 + k] = high[k];
   }
-  // try_median4 seeds (:1181-1308)
+  // try_median4 seeds (:1181-1308), tried at Better and Uber only (:765-771)
+  if (quality < kQBetter) return;
   float means[4][3];
   if (n <= 4) {
     for (int i = 0; i < 4; i++) {
@@ -451,6 +502,17 @@ __device__ __forceinline__ float4 entry(float wr, float wg, int r, int g, int b)
   const float fr = (float)r, fg = (float)g, fb = (float)b;
   return make_float4(2.f * wr * fr, 2.f * wg * fg, 2.f * fb, wr * fr * fr + wg * fg * fg + fb * fb);
 }
+
+// color::RGB_to_Y (crnlib/crn_color.h:792-796): fixed-point luma
+__device__ __forceinline__ int luma(int r, int g, int b) { return (r * 19595 + g * 38470 + b * 7471 + 32768) >> 16; }
+
+// The same for the grayscale-sampling metric (crnlib/crn_dxt1.cpp:1342-1368): the squared luma
+// difference, with the colour held as (Y, 0, 0, Y^2).
+__device__ __forceinline__ float4 entry_m(bool gray, float wr, float wg, int r, int g, int b) {
+  if (!gray) return entry(wr, wg, r, g, b);
+  const float y = (float)luma(r, g, b);
+  return make_float4(2.f * y, 0.f, 0.f, y * y);
+}
 __device__ __forceinline__ float dist_part(const float4& x, const float4& q) {
   float t = fmaf(-x.x, q.x, q.w);
   t = fmaf(-x.y, q.y, t);
@@ -459,20 +521,54 @@ __device__ __forceinline__ float dist_part(const float4& x, const float4& q) {
 
 // Selector of unique colour i for solution s; ties go to the lowest index, which is how both
 // the uber trial loop and compute_selectors_hc (crn_dxt1.cpp:1845-1869) resolve them.
+// The selector evaluate_solution_fast (crnlib/crn_dxt1.cpp:1594-1757) gives colour c: its
+// projection onto the endpoint axis against the midpoints of the palette's projections.
+struct FastSel {
+  int dr, dg, db;     // 2 x the (weighted) axis
+  int t0, t1, t2;     // 4-colour: halfPoint, c0Point, c3Point; 3-colour: c02Point, c21Point
+  bool three;
+  __device__ void init(bool perceptual, bool alpha, int a, int r0, int g0, int b0, int r1, int g1, int b1) {
+    int vr = r1 - r0, vg = g1 - g0, vb = b1 - b0;
+    if (perceptual) { vr *= 8; vg *= 24; }
+    const int s0 = r0 * vr + g0 * vg + b0 * vb, s1 = r1 * vr + g1 * vg + b1 * vb;
+    dr = vr * 2; dg = vg * 2; db = vb * 2;
+    three = alpha;
+    if (!alpha) {
+      const int s2 = ((r0 * 2 + r1 + a) / 3) * vr + ((g0 * 2 + g1 + a) / 3) * vg + ((b0 * 2 + b1 + a) / 3) * vb;
+      const int s3 = ((r1 * 2 + r0 + a) / 3) * vr + ((g1 * 2 + g0 + a) / 3) * vg + ((b1 * 2 + b0 + a) / 3) * vb;
+      t0 = s3 + s2; t1 = s1 + s3; t2 = s2 + s0;
+    } else {
+      const int s2 = ((r0 + r1 + a) >> 1) * vr + ((g0 + g1 + a) >> 1) * vg + ((b0 + b1 + a) >> 1) * vb;
+      t0 = s0 + s2; t1 = s2 + s1;
+    }
+  }
+  __device__ __forceinline__ int pick(uint32_t c) const {
+    const int d = (int)(c & 255) * dr + (int)((c >> 8) & 255) * dg + (int)(c >> 16) * db;
+    if (!three) return d >= t0 ? (d < t1 ? 3 : 1) : (d < t2 ? 0 : 2);
+    return d < t0 ? 0 : (d < t1 ? 2 : 1);
+  }
+};
+
 __device__ __noinline__ int selector_of(const WarpShared& S, int i, const Sol& s) {
   if (s.enforce) return s.enforced;
   const float wr = S.st.wr, wg = S.st.wg;
+  const bool gray = S.st.gray != 0;
   const int r0 = exp5(s.lo >> 11), g0 = exp6((s.lo >> 5) & 63), b0 = exp5(s.lo & 31);
   const int r1 = exp5(s.hi >> 11), g1 = exp6((s.hi >> 5) & 63), b1 = exp5(s.hi & 31);
   const int a = s.alt;
+  if (S.st.fast) {
+    FastSel f;
+    f.init(S.st.perceptual != 0, s.alpha != 0, a, r0, g0, b0, r1, g1, b1);
+    return f.pick(S.uci[i]);
+  }
   float4 q[4];
-  q[0] = entry(wr, wg, r0, g0, b0);
-  q[1] = entry(wr, wg, r1, g1, b1);
+  q[0] = entry_m(gray, wr, wg, r0, g0, b0);
+  q[1] = entry_m(gray, wr, wg, r1, g1, b1);
   if (s.alpha) {
-    q[2] = entry(wr, wg, (r0 + r1 + a) >> 1, (g0 + g1 + a) >> 1, (b0 + b1 + a) >> 1);
+    q[2] = entry_m(gray, wr, wg, (r0 + r1 + a) >> 1, (g0 + g1 + a) >> 1, (b0 + b1 + a) >> 1);
   } else {
-    q[2] = entry(wr, wg, (r0 * 2 + r1 + a) / 3, (g0 * 2 + g1 + a) / 3, (b0 * 2 + b1 + a) / 3);
-    q[3] = entry(wr, wg, (r1 * 2 + r0 + a) / 3, (g1 * 2 + g0 + a) / 3, (b1 * 2 + b0 + a) / 3);
+    q[2] = entry_m(gray, wr, wg, (r0 * 2 + r1 + a) / 3, (g0 * 2 + g1 + a) / 3, (b0 * 2 + b1 + a) / 3);
+    q[3] = entry_m(gray, wr, wg, (r1 * 2 + r0 + a) / 3, (g1 * 2 + g0 + a) / 3, (b1 * 2 + b0 + a) / 3);
   }
   const float4 x = S.ucf[i];
   float bd = dist_part(x, q[0]);
@@ -604,7 +700,7 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
   const ListDesc& d = S.d;
   const uint32_t lane = lane_id();
   const int n = S.st.n;
-  const bool three = S.st.three != 0;
+  const bool three = S.st.three != 0, only3 = S.st.only3 != 0, fast = S.st.fast != 0, gray = S.st.gray != 0;
   const float wr = S.st.wr, wg = S.st.wg;
   bool any = false;
   int i0 = start;
@@ -628,32 +724,59 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
       live = live && (int)lane == __ffs(grp) - 1;
       live = live && !hset_find(S, key);
     }
-    // evaluate every lane's candidate (uber: 4- and 3-colour; hc: 4-colour), stopping early once
-    // no live lane can still beat the running best
+    // evaluate every lane's candidate (uber: 4- and 3-colour; hc: 4-colour; fast: the selector
+    // by projection, then its distance), stopping early once no live lane can still beat the
+    // running best. Blocks with transparent texels evaluate 3-colour blocks only.
     uint32_t e0 = 0, e1 = 0;
     {
       const int a = d.alt;
       const int r0 = exp5(lo >> 11), g0 = exp6((lo >> 5) & 63), b0 = exp5(lo & 31);
       const int r1 = exp5(hi >> 11), g1 = exp6((hi >> 5) & 63), b1 = exp5(hi & 31);
-      const float4 q0 = entry(wr, wg, r0, g0, b0), q1 = entry(wr, wg, r1, g1, b1);
-      const float4 q2 = entry(wr, wg, (r0 * 2 + r1 + a) / 3, (g0 * 2 + g1 + a) / 3, (b0 * 2 + b1 + a) / 3);
-      const float4 q3 = entry(wr, wg, (r1 * 2 + r0 + a) / 3, (g1 * 2 + g0 + a) / 3, (b1 * 2 + b0 + a) / 3);
-      const float4 q4 = entry(wr, wg, (r0 + r1 + a) >> 1, (g0 + g1 + a) >> 1, (b0 + b1 + a) >> 1);
+      const float4 q0 = entry_m(gray, wr, wg, r0, g0, b0), q1 = entry_m(gray, wr, wg, r1, g1, b1);
+      const float4 q2 = entry_m(gray, wr, wg, (r0 * 2 + r1 + a) / 3, (g0 * 2 + g1 + a) / 3, (b0 * 2 + b1 + a) / 3);
+      const float4 q3 = entry_m(gray, wr, wg, (r1 * 2 + r0 + a) / 3, (g1 * 2 + g0 + a) / 3, (b1 * 2 + b0 + a) / 3);
+      const float4 q4 = entry_m(gray, wr, wg, (r0 + r1 + a) >> 1, (g0 + g1 + a) >> 1, (b0 + b1 + a) >> 1);
       if (__any_sync(FULL_MASK, live)) {
         int k = 0;
-        for (; k < n; k++) {
-          const float4 x = S.ucf[k];
-          const uint32_t w = (uint32_t)S.ucw[k];
-          const float m01 = fminf(dist_part(x, q0), dist_part(x, q1));
-          e0 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, fminf(dist_part(x, q2), dist_part(x, q3)))));
-          if (three) e1 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, dist_part(x, q4))));
-          if ((k & 3) == 3 && __all_sync(FULL_MASK, !live || (three ? min(e0, e1) : e0) >= B0)) { k++; break; }
+        if (!fast) {
+          for (; k < n; k++) {
+            const float4 x = S.ucf[k];
+            const uint32_t w = (uint32_t)S.ucw[k];
+            const float m01 = fminf(dist_part(x, q0), dist_part(x, q1));
+            e0 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, fminf(dist_part(x, q2), dist_part(x, q3)))));
+            if (three) e1 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, dist_part(x, q4))));
+            if ((k & 3) == 3 &&
+                __all_sync(FULL_MASK, !live || (only3 ? e1 : (three ? min(e0, e1) : e0)) >= B0)) { k++; break; }
+          }
+        } else {
+          FastSel f4, f3;
+          const bool perc = S.st.perceptual != 0;
+          f4.init(perc, false, a, r0, g0, b0, r1, g1, b1);
+          f3.init(perc, true, a, r0, g0, b0, r1, g1, b1);
+          for (; k < n; k++) {
+            const float4 x = S.ucf[k];
+            const uint32_t c = S.uci[k];
+            const uint32_t w = (uint32_t)S.ucw[k];
+            if (!only3) {
+              const int s4 = f4.pick(c);
+              const float4 q = s4 == 0 ? q0 : s4 == 1 ? q1 : s4 == 2 ? q2 : q3;
+              e0 += w * f2u_exact(__fadd_rn(x.w, dist_part(x, q)));
+            }
+            if (three) {
+              const int s3 = f3.pick(c);
+              const float4 q = s3 == 0 ? q0 : s3 == 1 ? q1 : q4;
+              e1 += w * f2u_exact(__fadd_rn(x.w, dist_part(x, q)));
+            }
+            if ((k & 3) == 3 &&
+                __all_sync(FULL_MASK, !live || (only3 ? e1 : (three ? min(e0, e1) : e0)) >= B0)) { k++; break; }
+          }
         }
         if (live) work += (uint32_t)k;
       }
     }
-    const uint32_t err = (three && e1 < e0) ? e1 : e0;
-    const int type = (three && e1 < e0) ? 1 : 0;
+    const bool pick3 = only3 || (three && e1 < e0);
+    const uint32_t err = pick3 ? e1 : e0;
+    const int type = pick3 ? 1 : 0;
     // resolve the sequential outcome of the batch
     unsigned ok = __ballot_sync(FULL_MASK, live && err < B0);
     int last = -1, cut = 31;
@@ -688,9 +811,9 @@ __device__ __forceinline__ void set_list(WarpShared& S, int kind, int count, int
   }
 }
 
-// refine_solution(1) :525-698: least-squares endpoints from the current selectors, then the
-// 2 x 27 lattice neighbours of the two fitted endpoints.
-__device__ bool refine(WarpShared& S, uint32_t& work) {
+// refine_solution :525-698: least-squares endpoints from the current selectors; level 1 then tries
+// the 2 x 27 lattice neighbours of the two fitted endpoints, level 0 the fitted pair alone.
+__device__ bool refine(WarpShared& S, uint32_t& work, int level = 1) {
   compute_selectors(S);
   const uint32_t lane = lane_id();
   const int n = S.st.n;
@@ -727,7 +850,16 @@ __device__ bool refine(WarpShared& S, uint32_t& work) {
     const int v = __shfl_sync(FULL_MASK, mine, k);
     if (lane == 0) S.d.e[k] = v;
   }
-  set_list(S, LK_REFINE, 54, 0, 0);
+  __syncwarp();
+  if (level == 0) {
+    if (lane == 0) {
+      const uint32_t p0 = pack565(S.d.e[0], S.d.e[1], S.d.e[2]), p1 = pack565(S.d.e[3], S.d.e[4], S.d.e[5]);
+      S.cand[0] = canon_lo(p0, p1) | (canon_hi(p0, p1) << 16);
+    }
+    set_list(S, LK_TABLE, 1, 0, 0);
+  } else {
+    set_list(S, LK_REFINE, 54, 0, 0);
+  }
   __syncwarp();
   return run_list(S, 0, work) != 0;
 }
@@ -767,8 +899,9 @@ __device__ bool try_solid(WarpShared& S, uint32_t& work) {
     int cnt = 0;
     S.cand[cnt++] = solid_coords(ar, ag, ab, false);
     if (three) S.cand[cnt++] = solid_coords(ar, ag, ab, true);
+    // the other colours of the block as solid colours, at Uber only (:126-150)
     #pragma unroll 1
-    for (int i = 0; i < n; i++) {
+    for (int i = 0; i < (S.st.quality == (int)kQUber ? n : 0); i++) {
       const uint32_t c = S.uci[i];
       const int r = c & 255, g = (c >> 8) & 255, b = c >> 16;
       if (r == ar && g == ag && b == ab) continue;
@@ -961,26 +1094,36 @@ __device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
   }
 }
 
-// optimize_endpoints :703-1067 from the phase-1 projection bounds
+// optimize_endpoints :703-1067 from the phase-1 projection bounds. The quality level sets the probe
+// table, the probe spacing and the pass count (:716-745), whether try_median4 runs (Better and
+// up) and its refine level, the lattice moves (Normal and up; the +-2 moves and the per-pass
+// refine at Uber only) and the final tries (:1030-1058).
 __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
   const uint32_t lane = lane_id();
-  // try_median4: the six LBG pairs, then refine(1)
-  if (lane < 6) S.cand[lane] = S.p1m[slot][lane];
-  set_list(S, LK_TABLE, 6, 0, 0);
-  __syncwarp();
-  run_list(S, 0, work);
-  refine(S, work);
+  const uint32_t quality = (uint32_t)S.st.quality;
+  if (quality >= kQBetter) {
+    // try_median4: the six LBG pairs, then refine (level 1 at Uber, 0 at Better)
+    if (lane < 6) S.cand[lane] = S.p1m[slot][lane];
+    set_list(S, LK_TABLE, 6, 0, 0);
+    __syncwarp();
+    run_list(S, 0, work);
+    refine(S, work, quality == kQUber ? 1 : 0);
+  }
+  const int table = probe_table(quality);
+  const int probe_n = c_probe_size[table];
+  const int passes = quality == kQUber ? 4 : quality == kQSuperFast ? 1 : 2;
+  const float dist_per_trial = quality >= kQBetter ? .015625f : .027063293f;
   float sa1[3], low[3], high[3];
   const float lim[3] = {31.0f, 63.0f, 31.0f};
   for (int k = 0; k < 3; k++) {
-    sa1[k] = __fmul_rn(S.p1f[slot][k], .015625f);
+    sa1[k] = __fmul_rn(S.p1f[slot][k], dist_per_trial);
     const float l = __fmul_rn(S.p1f[slot][3 + k], lim[k]), h = __fmul_rn(S.p1f[slot][6 + k], lim[k]);
     low[k] = l < 0.0f ? 0.0f : (l > lim[k] ? lim[k] : l);
     high[k] = h < 0.0f ? 0.0f : (h > lim[k] ? lim[k] : h);
   }
   sa1[0] = __fmul_rn(sa1[0], 31.0f); sa1[1] = __fmul_rn(sa1[1], 63.0f); sa1[2] = __fmul_rn(sa1[2], 31.0f);
   #pragma unroll 1
-  for (int pass = 0; pass < 4; pass++) {
+  for (int pass = 0; pass < passes; pass++) {
     if (pass) {
       const uint32_t blo = S.st.best.lo, bhi = S.st.best.hi;
       low[0] = (float)(blo >> 11); low[1] = (float)((blo >> 5) & 63); low[2] = (float)(blo & 31);
@@ -988,12 +1131,12 @@ __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
     }
     const uint32_t prev = S.st.best.err;
     if (!prev) break;
-    // sweep both endpoints along the axis with the 15-entry uber probe table, both directions;
+    // sweep both endpoints along the axis with the quality's probe table, both directions;
     // lane k holds probe (i, s) = ((k+1)/2, (k+1)&1) in the reference's loop order
     {
       const int k = (int)lane;
       const int i = (k + 1) >> 1, s = (k + 1) & 1;
-      const float x = (float)c_uber_probe[i < 15 ? i : 14];
+      const float x = (float)c_probe[table][i < probe_n ? i : probe_n - 1];
       uint32_t pl, ph;
       {
         int v[3], w[3];
@@ -1006,7 +1149,7 @@ __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
         ph = pack565(w[0], w[1], w[2]);
       }
       const uint32_t pl2 = __shfl_up_sync(FULL_MASK, pl, 2), ph2 = __shfl_up_sync(FULL_MASK, ph, 2);
-      const bool in = k < 29;
+      const bool in = k < 2 * probe_n - 1;
       const bool rl = in && (k < 2 || pl != pl2), rh = in && (k < 2 || ph != ph2);
       const unsigned ml = __ballot_sync(FULL_MASK, rl), mh = __ballot_sync(FULL_MASK, rh);
       const unsigned below = (1u << lane) - 1u;
@@ -1021,8 +1164,8 @@ __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
     run_list(S, 0, work);
     // lattice neighbours: low endpoint (26 adjacent cells, then +-2 per axis), then high
     #pragma unroll 1
-    for (int side = 0; side < 2; side++) {
-      for (int kind = LK_NEIGH; kind <= LK_MOVE2; kind++) {
+    for (int side = 0; side < (quality >= kQNormal ? 2 : 0); side++) {
+      for (int kind = LK_NEIGH; kind <= (quality == kQUber ? LK_MOVE2 : LK_NEIGH); kind++) {
         if (lane == 0) {
           const uint32_t base = side ? S.st.best.hi : S.st.best.lo;
           S.d.base[0] = (int)(base >> 11); S.d.base[1] = (int)((base >> 5) & 63); S.d.base[2] = (int)(base & 31);
@@ -1034,14 +1177,15 @@ __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
       }
     }
     if (!S.st.best.err || (pass && S.st.best.err == prev)) break;
-    refine(S, work);
+    if (quality == kQUber) refine(S, work);
   }
-  if (S.st.best.err) {
+  if (quality < kQNormal) return;
+  if (S.st.best.err && !S.st.only3) {
     bool solid = false;
     if (all_selectors_equal(S)) solid = try_solid(S, work);
-    if (!solid) optimize_comps(S, work);
+    if (!solid && quality == kQUber) optimize_comps(S, work);
   }
-  if (S.st.best.err) try_combinatorial(S, work);
+  if (quality == kQUber && S.st.best.err) try_combinatorial(S, work);
 }
 
 // Plane tables -> per-channel lower bounds (compute_internal :2133-2203); lane c handles
@@ -1082,38 +1226,110 @@ __device__ void build_lower_bounds(WarpShared& S, int n, bool perceptual) {
   }
 }
 
-__device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, bool perceptual,
-                                 bool hc, bool use_alpha, uint8_t* __restrict__ out, uint64_t* __restrict__ err_out) {
+// Writes one finished block (endpoints as stored, the 32 selector bits). In the transparent-black
+// trial the block is written, with its error, only when the trial's error over all texels with
+// get_block_colors3's palette (crn_dxt.cpp:234-245; selector 3 is black) is below the error in
+// err_io (crn_dxt1.cpp:2043-2075); otherwise err_out (optional) receives `err`. Every lane calls it;
+// `pixel` is the lane's texel (lanes < 16).
+__device__ __forceinline__ void block_out(const WarpShared& S, uint32_t lo, uint32_t hi, uint32_t bits, uint32_t err,
+                                          uint32_t pixel, bool perceptual, bool gray, uint32_t opts,
+                                          uint8_t* __restrict__ out, uint64_t* __restrict__ err_out,
+                                          uint64_t* __restrict__ err_io) {
   const uint32_t lane = lane_id();
-  // unique colours in first-occurrence order via match_any (lanes >= 16 carry sentinels)
+  if (opts & kD1BlackTrial) {
+    uint32_t e = 0;
+    if (lane < 16) {
+      const uint32_t sel = (bits >> (2 * lane)) & 3u;
+      const int r0 = exp5(lo >> 11), g0 = exp6((lo >> 5) & 63), b0 = exp5(lo & 31);
+      const int r1 = exp5(hi >> 11), g1 = exp6((hi >> 5) & 63), b1 = exp5(hi & 31);
+      int pr = 0, pg = 0, pb = 0;
+      if (sel == 0) { pr = r0; pg = g0; pb = b0; }
+      else if (sel == 1) { pr = r1; pg = g1; pb = b1; }
+      else if (sel == 2) { pr = (r0 + r1) >> 1; pg = (g0 + g1) >> 1; pb = (b0 + b1) >> 1; }
+      const int r = (int)(pixel & 255), g = (int)((pixel >> 8) & 255), b = (int)((pixel >> 16) & 255);
+      if (gray) {
+        const int d = luma(r, g, b) - luma(pr, pg, pb);
+        e = (uint32_t)(d * d);
+      } else {
+        const int dr = r - pr, dg = g - pg, db = b - pb;
+        e = perceptual ? (uint32_t)(8 * dr * dr + 25 * dg * dg + db * db) : (uint32_t)(dr * dr + dg * dg + db * db);
+      }
+    }
+    const uint32_t terr = __reduce_add_sync(FULL_MASK, e);
+    if (lane == 0 && (uint64_t)terr < *err_io) {
+      *reinterpret_cast<uint2*>(out) = make_uint2(lo | (hi << 16), bits);
+      *err_io = terr;
+    }
+  } else if (lane == 0) {
+    *reinterpret_cast<uint2*>(out) = make_uint2(lo | (hi << 16), bits);
+    if (err_out) *err_out = err;
+  }
+  __syncwarp();
+}
+
+// One block on one warp: compute_internal (:2081-2232) from phase 1's hand-off, then
+// return_solution. opts: a dxt1_options() word. err_out (optional) receives the error.
+// In the transparent-black trial (kD1BlackTrial; err_io holds the block's error from the normal
+// encode) the block is re-encoded with its near-black texels transparent and rewritten, with its
+// error, only when the trial's error over all texels, selector 3 decoding to black, is lower
+// (:2001-2079).
+__device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, uint32_t opts,
+                                 uint8_t* __restrict__ out, uint64_t* __restrict__ err_out,
+                                 uint64_t* __restrict__ err_io) {
+  const uint32_t lane = lane_id();
+  if (S.p1n[slot] < 0) return 0;  // the trial does not apply to this block
+  const bool perceptual = (opts & kD1Perceptual) != 0, use_alpha = (opts & kD1Three) != 0;
+  const bool gray = (opts & kD1Gray) != 0;
+  const uint32_t quality = (opts >> kD1QualityShift) & 7u;
+  // unique colours of the opaque texels in first-occurrence order via match_any (transparent
+  // texels and lanes >= 16 carry sentinels)
   const uint32_t pixel = lane < 16 ? __ldg(reinterpret_cast<const uint32_t*>(px) + lane) : 0;
-  const uint32_t key = lane < 16 ? (pixel & 0xFFFFFFu) : (0x80000000u | lane);
+  const bool transparent = lane < 16 && is_transparent(pixel, opts);
+  const bool has_t = __any_sync(FULL_MASK, transparent);
+  const uint32_t key = (lane < 16 && !transparent) ? (pixel & 0xFFFFFFu) : (0x80000000u | lane);
   const unsigned match = __match_any_sync(FULL_MASK, key);
   const int leader = __ffs(match) - 1;
-  const bool is_leader = lane < 16 && leader == (int)lane;
+  const bool is_leader = lane < 16 && !transparent && leader == (int)lane;
   const unsigned lmask = __ballot_sync(FULL_MASK, is_leader);
   const int n = __popc(lmask);
   const int uidx = __popc(lmask & ((1u << leader) - 1u));
+  if (n == 0) {
+    // every texel transparent: black endpoints, all selectors 3 (:2205-2211); the search is skipped
+    block_out(S, 0u, 0u, 0xFFFFFFFFu, 0u, pixel, perceptual, gray, opts, out, err_out, err_io);
+    return 0;
+  }
   const float wr = perceptual ? 8.f : 1.f, wg = perceptual ? 25.f : 1.f;
   if (is_leader) {
     const float r = (float)(key & 255), g = (float)((key >> 8) & 255), b = (float)(key >> 16);
-    S.ucf[uidx] = make_float4(r, g, b, wr * r * r + wg * g * g + b * b);
+    if (gray) {
+      const float y = (float)luma((int)(key & 255), (int)((key >> 8) & 255), (int)(key >> 16));
+      S.ucf[uidx] = make_float4(y, 0.f, 0.f, y * y);
+    } else {
+      S.ucf[uidx] = make_float4(r, g, b, wr * r * r + wg * g * g + b * b);
+    }
     S.ucw[uidx] = __popc(match);
     S.uci[uidx] = key;
   }
   // clear the tried-set
   for (int k = lane; k < kHashSize / 4; k += 32) reinterpret_cast<uint4*>(S.hset)[k] = make_uint4(kInf, kInf, kInf, kInf);
+  // m_evaluate_hc (:2085): Uber, no 3-colour blocks, no transparency, no grayscale sampling
+  const bool hc = quality == kQUber && !use_alpha && !has_t && !gray;
   if (lane == 0) {
     Sol z;
     z.lo = z.hi = 0; z.err = kInf; z.alpha = 0; z.alt = 0; z.enforce = 0; z.enforced = 0;
     S.st.best = z; S.st.snap = z;
-    S.st.n = n; S.st.hc = hc ? 1 : 0; S.st.three = (!hc && use_alpha) ? 1 : 0; S.st.wr = wr; S.st.wg = wg;
+    S.st.n = n; S.st.hc = hc ? 1 : 0; S.st.three = (use_alpha || has_t) ? 1 : 0; S.st.wr = wr; S.st.wg = wg;
+    S.st.only3 = has_t ? 1 : 0;
+    S.st.fast = (!hc && quality < kQBetter) ? 1 : 0;
+    S.st.gray = gray ? 1 : 0;
+    S.st.quality = (int)quality;
+    S.st.perceptual = perceptual ? 1 : 0;
   }
   __syncwarp();
   build_lower_bounds(S, n, perceptual);
   __syncwarp();
   uint32_t work = 0;
-  if (n == 1) {
+  if (n == 1 && !has_t) {
     const uint32_t c = S.uci[0];
     const int r = c & 255, g = (c >> 8) & 255, b = c >> 16;
     if (lane == 0) { S.cand[0] = solid_coords(r, g, b, false); S.cand[1] = solid_coords(r, g, b, true); }
@@ -1123,21 +1339,18 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
   } else {
     optimize(S, slot, work);
   }
-  // return_solution :263-365
+  // return_solution :263-365 (transparent texels take selector 3)
   compute_selectors(S);
   const Sol best = S.st.best;
   const int my_sel = (int)lane < n ? selector_of(S, lane, sel_source(S)) : 0;
-  const int s = __shfl_sync(FULL_MASK, my_sel, lane < 16 ? uidx : 0);
+  const int s = __shfl_sync(FULL_MASK, my_sel, (lane < 16 && !transparent) ? uidx : 0);
   const bool invert = best.alpha ? best.lo > best.hi : best.lo < best.hi;
   int sel = s;
   if (invert) sel = best.alpha ? (s < 2 ? (s ^ 1) : s) : (s ^ 1);
+  if (transparent) sel = 3;
   const uint32_t bits = __reduce_or_sync(FULL_MASK, lane < 16 ? ((uint32_t)sel << (2 * lane)) : 0u);
-  if (lane == 0) {
-    const uint32_t lo = invert ? best.hi : best.lo, hi = invert ? best.lo : best.hi;
-    *reinterpret_cast<uint2*>(out) = make_uint2(lo | (hi << 16), bits);
-    if (err_out) *err_out = best.err;
-  }
-  __syncwarp();
+  const uint32_t lo = invert ? best.hi : best.lo, hi = invert ? best.lo : best.hi;
+  block_out(S, lo, hi, bits, best.err, pixel, perceptual, gray, opts, out, err_out, err_io);
   return work;
 }
 
@@ -1246,28 +1459,30 @@ struct ChunkStager {
 template <typename IssueNext>
 __device__ __forceinline__ unsigned long long dxt1_chunk(WarpShared& S, const uint8_t* __restrict__ blocks, uint32_t b0,
                                                          uint32_t bstride, uint32_t cnt, const uint8_t* staged,
-                                                         IssueNext issue_next, bool perceptual, bool hc, bool use_alpha,
+                                                         IssueNext issue_next, uint32_t opts,
                                                          uint8_t* __restrict__ out, uint32_t out_stride,
-                                                         uint64_t* __restrict__ err_out) {
+                                                         uint64_t* __restrict__ err_out,
+                                                         uint64_t* __restrict__ err_io) {
   // the chunk's blocks are b0, b0 + bstride, ...; out and err_out point at block b0's result;
   // staged holds them packed (nullptr: read them from global memory)
   const uint32_t lane = lane_id();
   unsigned long long work = 0;
   if (lane < cnt)
     phase1_block(S, lane, staged ? staged + (size_t)lane * 64 : blocks + ((size_t)b0 + (size_t)lane * bstride) * 64,
-                 perceptual);
+                 opts);
   __syncwarp();
   issue_next();
   #pragma unroll 1
   for (uint32_t k = 0; k < cnt; k++)
-    work += phase2_block(S, k, blocks + ((size_t)b0 + (size_t)k * bstride) * 64, perceptual, hc, use_alpha,
-                         out + (size_t)k * bstride * out_stride, err_out ? err_out + (size_t)k * bstride : nullptr);
+    work += phase2_block(S, k, blocks + ((size_t)b0 + (size_t)k * bstride) * 64, opts,
+                         out + (size_t)k * bstride * out_stride, err_out ? err_out + (size_t)k * bstride : nullptr,
+                         err_io ? err_io + (size_t)k * bstride : nullptr);
   return work;
 }
 
 __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
-    k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, int perceptual, int hc, int use_alpha,
-                  uint8_t* __restrict__ out, uint32_t out_stride, uint64_t* __restrict__ err_out,
+    k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, uint32_t opts, uint8_t* __restrict__ out,
+                  uint32_t out_stride, uint64_t* __restrict__ err_out, uint64_t* __restrict__ err_io,
                   unsigned long long* __restrict__ work_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpShared& S = reinterpret_cast<WarpShared*>(smem_raw)[threadIdx.x >> 5];
@@ -1292,8 +1507,8 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
         [&]() {
           if (k1 < mine) st.next(S, blocks + (size_t)first_block(k1) * 64, chunk_count(k1), nwarps);
         },
-        perceptual != 0, hc != 0, use_alpha != 0, out + (size_t)b0 * out_stride, out_stride,
-        err_out ? err_out + b0 : nullptr);
+        opts, out + (size_t)b0 * out_stride, out_stride, err_out ? err_out + b0 : nullptr,
+        err_io ? err_io + b0 : nullptr);
   }
   st.finish(S);
   if (work_out) {
@@ -1338,7 +1553,9 @@ struct Alpha5 {
 
 // One DXT5A element (dxt5_endpoint_optimizer::compute, crnlib/crn_dxt5a.cpp:40-196) of the 4x4
 // RGBA8 block px on channel comp, written as 8 bytes to o; a whole warp, lane per candidate.
-__device__ __forceinline__ void alpha_block(const uint8_t* __restrict__ px, int comp, int both, uint8_t* __restrict__ o) {
+// quality: crn_dxt_quality; the probe grid is +-16 at Uber, +-8 at Better and absent below (:105-110).
+__device__ __forceinline__ void alpha_block(const uint8_t* __restrict__ px, int comp, int both, uint32_t quality,
+                                            uint8_t* __restrict__ o) {
   const uint32_t lane = lane_id();
   const uint32_t v = lane < 16 ? __ldg(px + lane * 4 + comp) : 0x100u + lane;
   const unsigned match = __match_any_sync(FULL_MASK, v);
@@ -1401,19 +1618,20 @@ __device__ __forceinline__ void alpha_block(const uint8_t* __restrict__ px, int 
     if (valid) A.eval(l, h, err, type);
     accept_chain(valid, l, h, err, type, false);
   }
-  // +-16 probe around the running best (:98-141); the centre moves with each improvement
-  if (berr) {
-    int pos = 0, row_l = (int)first - 16;
-    const int total = 33 * 33;
+  // +-R probe around the running best (:98-141); the centre moves with each improvement
+  const int R = quality == kQUber ? 16 : 8, D = 2 * R + 1;
+  if (berr && quality >= kQBetter) {
+    int pos = 0, row_l = (int)first - R;
+    const int total = D * D;
     while (pos < total) {
       const int p = pos + (int)lane;
-      const int row0 = pos / 33;
+      const int row0 = pos / D;
       int l = 0, h = 0;
       bool valid = p < total;
       if (valid) {
-        const int r = p / 33, c = p % 33;
-        l = r == row0 ? row_l : (int)first + (r - 16);
-        h = (int)second + (c - 16);
+        const int r = p / D, c = p % D;
+        l = r == row0 ? row_l : (int)first + (r - R);
+        h = (int)second + (c - R);
         valid = l >= 0 && l <= 255 && h >= 0 && h <= 255;
       }
       uint32_t err = kInf;
@@ -1421,12 +1639,12 @@ __device__ __forceinline__ void alpha_block(const uint8_t* __restrict__ px, int 
       if (valid) A.eval(l, h, err, type);
       const int last = accept_chain(valid, l, h, err, type, true);
       const int next = last >= 0 ? pos + last + 1 : pos + 32;
-      const int nrow = next / 33;
+      const int nrow = next / D;
       // the reference fixes l when a row starts: a row begun inside this batch used the
       // centre from before the batch, unless it is the accepted candidate's own row
-      const int last_row = last >= 0 ? (pos + last) / 33 : -1;
+      const int last_row = last >= 0 ? (pos + last) / D : -1;
       if (last >= 0 && nrow == last_row) row_l = __shfl_sync(FULL_MASK, l, last);
-      else if (nrow != row0) row_l = (int)first + (nrow - 16);
+      else if (nrow != row0) row_l = (int)first + (nrow - R);
       pos = next;
     }
   }
@@ -1474,12 +1692,12 @@ __device__ __forceinline__ void alpha_block(const uint8_t* __restrict__ px, int 
 }
 
 __global__ void __launch_bounds__(128)
-    k_dxt5a_encode(const uint8_t* __restrict__ blocks, uint32_t n, int comp, int both, uint8_t* __restrict__ out,
-                   uint32_t out_stride) {
+    k_dxt5a_encode(const uint8_t* __restrict__ blocks, uint32_t n, int comp, int both, uint32_t quality,
+                   uint8_t* __restrict__ out, uint32_t out_stride) {
   const uint32_t warp_global = blockIdx.x * 4 + (threadIdx.x >> 5);
   const uint32_t nwarps = gridDim.x * 4;
   for (uint32_t bi = warp_global; bi < n; bi += nwarps)
-    alpha_block(blocks + (size_t)bi * 64, comp, both, out + (size_t)bi * out_stride);
+    alpha_block(blocks + (size_t)bi * 64, comp, both, quality, out + (size_t)bi * out_stride);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1504,7 +1722,6 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
   for (uint32_t c = warp_global; c < nchunks; c += nwarps) {
     const EncodeChunk ch = chunks[c];
     const EncodeSegment sg = segs[ch.segment];
-    const bool use_alpha = (sg.options & kSegThreeColour) != 0;
     const uint8_t* staged = st.acquire(S);
     const uint32_t nxt = c + nwarps;
     dxt1_chunk(
@@ -1515,8 +1732,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
             st.next(S, blocks + (size_t)cn.first * 64, cn.count);
           }
         },
-        (sg.options & kSegPerceptual) != 0, !use_alpha, use_alpha,
-        sg.out + (size_t)(ch.first - sg.first_block) * sg.stride, sg.stride, nullptr);
+        sg.options, sg.out + (size_t)(ch.first - sg.first_block) * sg.stride, sg.stride, nullptr, nullptr);
   }
   st.finish(S);
 }
@@ -1531,9 +1747,10 @@ __global__ void __launch_bounds__(128)
     const EncodeSegment sg = segs[ch.segment];
     const int comp = (int)((sg.options >> kSegCompShift) & 3u);
     const int both = (sg.options & kSegBothTypes) ? 1 : 0;
+    const uint32_t quality = (sg.options >> kSegAlphaQualityShift) & 7u;
     for (uint32_t k = 0; k < ch.count; k++) {
       const uint32_t b = ch.first + k;
-      alpha_block(blocks + (size_t)b * 64, comp, both, sg.out + (size_t)(b - sg.first_block) * sg.stride);
+      alpha_block(blocks + (size_t)b * 64, comp, both, quality, sg.out + (size_t)(b - sg.first_block) * sg.stride);
     }
   }
 }
@@ -1635,11 +1852,14 @@ int read_work_counter(uint64_t* value, cudaStream_t s) {
   return cuda_check(e, "read counter");
 }
 
-int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_alpha_blocks, uint8_t* d_out,
-                uint32_t out_stride, uint64_t* d_err, cudaStream_t s) {
+namespace {
+
+int launch_dxt1_kernel(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
+                       uint64_t* d_err, uint64_t* d_err_io, cudaStream_t s) {
   int rc = ensure_tables();
   if (rc != CRNGPU_OK) return rc;
   if (!n) return CRNGPU_OK;
+  if (((opts >> kD1QualityShift) & 7u) > kQUber) { set_error("bad DXT quality"); return CRNGPU_E_PARAM; }
   const uint32_t warps_needed = (n + kBlocksPerWarp - 1) / kBlocksPerWarp;
   const uint32_t ctas_needed = (warps_needed + kWarpsPerCta - 1) / kWarpsPerCta;
   unsigned long long* work = g_count ? static_cast<unsigned long long*>(g_count_buf.ptr) : nullptr;
@@ -1661,9 +1881,21 @@ int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_a
   if (per_sm < 1) per_sm = 1;
   const uint32_t full = (uint32_t)sms * (uint32_t)per_sm;
   const int grid = (int)(ctas_needed < full ? ctas_needed : full);
-  k_dxt1_encode<<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, perceptual, use_alpha_blocks ? 0 : 1,
-                                                       use_alpha_blocks ? 1 : 0, d_out, out_stride, d_err, work);
+  k_dxt1_encode<<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, d_out, out_stride, d_err, d_err_io, work);
   return cuda_check(cudaGetLastError(), "launch k_dxt1_encode");
+}
+
+}  // namespace
+
+int launch_dxt1(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
+                uint64_t* d_err, cudaStream_t s) {
+  return launch_dxt1_kernel(d_blocks, n, opts & ~kD1BlackTrial, d_out, out_stride, d_err, nullptr, s);
+}
+
+int launch_dxt1_black_trial(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
+                            uint64_t* d_err_io, cudaStream_t s) {
+  if (!d_err_io) { set_error("the transparent-black trial needs the blocks' errors"); return CRNGPU_E_PARAM; }
+  return launch_dxt1_kernel(d_blocks, n, opts | kD1BlackTrial, d_out, out_stride, nullptr, d_err_io, s);
 }
 
 int dxt1_chunks_max_grid() {
@@ -1719,11 +1951,12 @@ int stage_wait_counters(uint32_t out[2], bool reset) {
   return cuda_check(e, "read stage wait counters");
 }
 
-int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint8_t* d_out, uint32_t out_stride,
-                 cudaStream_t s) {
+int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint32_t quality, uint8_t* d_out,
+                 uint32_t out_stride, cudaStream_t s) {
   if (!n) return CRNGPU_OK;
+  if (quality > kQUber) { set_error("bad DXT quality"); return CRNGPU_E_PARAM; }
   const int grid = grid_for((const void*)k_dxt5a_encode, 128, (n + 3) / 4);
-  k_dxt5a_encode<<<grid, 128, 0, s>>>(d_blocks, n, comp, both ? 1 : 0, d_out, out_stride);
+  k_dxt5a_encode<<<grid, 128, 0, s>>>(d_blocks, n, comp, both ? 1 : 0, quality, d_out, out_stride);
   return cuda_check(cudaGetLastError(), "launch k_dxt5a_encode");
 }
 

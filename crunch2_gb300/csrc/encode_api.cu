@@ -9,12 +9,22 @@
 
 namespace crngpu {
 
-int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_alpha_blocks, uint8_t* d_out,
-                uint32_t out_stride, uint64_t* d_err, cudaStream_t s);
-int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint8_t* d_out, uint32_t out_stride,
-                 cudaStream_t s);
-
 namespace {
+
+// crngpu_block_options with their defaults (Uber, alpha threshold 128); false on a bad struct
+bool read_options(const crngpu_block_options* o, uint32_t* quality, uint32_t* threshold) {
+  *quality = kDxtQualityUber;
+  *threshold = 128;
+  if (!o) return true;
+  if (o->struct_size != sizeof(crngpu_block_options) || o->dxt_quality > kDxtQualityUber ||
+      o->dxt1a_alpha_threshold > 255) {
+    set_error("bad crngpu_block_options");
+    return false;
+  }
+  *quality = o->dxt_quality;
+  *threshold = o->dxt1a_alpha_threshold;
+  return true;
+}
 
 // Image -> 4x4 blocks with edge clamping (init_task :334-344): texel (x, y) of block (bx, by)
 // is img[min(4by+y, h-1)][min(4bx+x, w-1)]. One thread per output texel.
@@ -41,23 +51,45 @@ int bytes_per_block(uint32_t fmt) {
 }
 
 // Launches the element encoders of one format on device buffers (dxt_image element layout,
-// crnlib/crn_dxt_image.cpp:150-200: DXT5 = alpha block then colour block, DXN = X then Y).
-int encode_device(const uint8_t* d_in, uint32_t n, uint32_t fmt, uint32_t flags, uint8_t* d_out, cudaStream_t s) {
+// crnlib/crn_dxt_image.cpp:150-200: DXT5 = alpha block then colour block, DXN = X then Y) with
+// the optimizer parameters set_block_pixels derives from the pack parameters (:1436-1522): the
+// DXT5 colour element never uses 3-colour blocks, transparency or the black trial. d_err
+// (optional) receives the DXT1 errors; the black trial needs them, so it uses the per-thread
+// staging buffer when d_err is NULL.
+int encode_device(const uint8_t* d_in, uint32_t n, uint32_t fmt, uint32_t flags, uint32_t quality, uint32_t threshold,
+                  uint8_t* d_out, uint64_t* d_err, cudaStream_t s) {
   const bool perceptual = (flags & CRNGPU_FLAG_PERCEPTUAL) != 0;
   const bool both = (flags & CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES) != 0;
+  const bool gray = (flags & CRNGPU_FLAG_GRAYSCALE) != 0;
   switch (fmt) {
-    case CRNGPU_FMT_DXT1: return launch_dxt1(d_in, n, perceptual, both, d_out, 8, nullptr, s);
-    case CRNGPU_FMT_DXT5A: return launch_dxt5a(d_in, n, 3, both, d_out, 8, s);
+    case CRNGPU_FMT_DXT1: {
+      const uint32_t opts =
+          dxt1_options(perceptual, both, quality, gray, (flags & CRNGPU_FLAG_DXT1A) != 0, threshold);
+      // try_alpha_as_black_optimization runs when 3-colour blocks are allowed (crn_dxt1.cpp:2239)
+      const bool black = both && (flags & CRNGPU_FLAG_TRANSPARENT_BLACK);
+      if (black && !d_err) {
+        DevBuf& be = staging(3);
+        cudaError_t e = be.ensure((size_t)n * 8);
+        if (e != cudaSuccess) return cuda_check(e, "alloc error stage");
+        d_err = static_cast<uint64_t*>(be.ptr);
+      }
+      int rc = launch_dxt1(d_in, n, opts, d_out, 8, d_err, s);
+      if (rc == CRNGPU_OK && black) rc = launch_dxt1_black_trial(d_in, n, opts, d_out, 8, d_err, s);
+      return rc;
+    }
+    case CRNGPU_FMT_DXT5A: return launch_dxt5a(d_in, n, 3, both, quality, d_out, 8, s);
     case CRNGPU_FMT_DXN_XY:
     case CRNGPU_FMT_DXN_YX: {
       const int c0 = fmt == CRNGPU_FMT_DXN_XY ? 0 : 1;
-      int rc = launch_dxt5a(d_in, n, c0, both, d_out, 16, s);
-      if (rc == CRNGPU_OK) rc = launch_dxt5a(d_in, n, 1 - c0, both, d_out + 8, 16, s);
+      int rc = launch_dxt5a(d_in, n, c0, both, quality, d_out, 16, s);
+      if (rc == CRNGPU_OK) rc = launch_dxt5a(d_in, n, 1 - c0, both, quality, d_out + 8, 16, s);
       return rc;
     }
     default: {  // DXT5 family: alpha element, then a colour element that may not use 3-colour blocks
-      int rc = launch_dxt5a(d_in, n, 3, both, d_out, 16, s);
-      if (rc == CRNGPU_OK) rc = launch_dxt1(d_in, n, perceptual, false, d_out + 8, 16, nullptr, s);
+      int rc = launch_dxt5a(d_in, n, 3, both, quality, d_out, 16, s);
+      if (rc == CRNGPU_OK)
+        rc = launch_dxt1(d_in, n, dxt1_options(perceptual, false, quality, gray, false, threshold), d_out + 8, 16,
+                         nullptr, s);
       return rc;
     }
   }
@@ -102,16 +134,33 @@ using namespace crngpu;
 extern "C" int crngpu_dxt1_optimize_batch(const uint8_t* rgba_blocks, uint32_t n, const crngpu_dxt1_params* params,
                                           uint8_t* out_blocks, uint64_t* out_error, int mem, void* stream) {
   clear_error();
-  if (!params || params->struct_size != sizeof(crngpu_dxt1_params) || (n && (!rgba_blocks || !out_blocks))) {
+  const bool legacy = params && params->struct_size == 16;  // the four-field layout: Uber, no extras
+  if (!params || (!legacy && params->struct_size != sizeof(crngpu_dxt1_params)) ||
+      (n && (!rgba_blocks || !out_blocks))) {
     set_error("bad arguments");
     return CRNGPU_E_PARAM;
   }
+  const uint32_t quality = legacy ? kDxtQualityUber : params->dxt_quality;
+  const uint32_t threshold = legacy ? 128u : params->dxt1a_alpha_threshold;
+  if (quality > kDxtQualityUber || threshold > 255) { set_error("bad quality or alpha threshold"); return CRNGPU_E_PARAM; }
+  const bool gray = !legacy && params->grayscale_sampling, dxt1a = !legacy && params->dxt1a;
+  const bool black = !legacy && params->use_transparent_indices_for_black && params->use_alpha_blocks;
+  const uint32_t opts = dxt1_options(params->perceptual != 0, params->use_alpha_blocks != 0, quality, gray, dxt1a,
+                                     threshold);
   if (!n) return CRNGPU_OK;
   cudaStream_t s = as_stream(stream);
   return with_buffers(rgba_blocks, (size_t)n * 64, out_blocks, (size_t)n * 8, out_error, (size_t)n * 8, mem, s,
                       [&](const uint8_t* in, uint8_t* out, uint64_t* err) {
-                        return launch_dxt1(in, n, params->perceptual != 0, params->use_alpha_blocks != 0, out, 8, err,
-                                           s);
+                        uint64_t* e = err;
+                        if (black && !e) {
+                          DevBuf& be = staging(3);
+                          cudaError_t ce = be.ensure((size_t)n * 8);
+                          if (ce != cudaSuccess) return cuda_check(ce, "alloc error stage");
+                          e = static_cast<uint64_t*>(be.ptr);
+                        }
+                        int rc = launch_dxt1(in, n, opts, out, 8, e, s);
+                        if (rc == CRNGPU_OK && black) rc = launch_dxt1_black_trial(in, n, opts, out, 8, e, s);
+                        return rc;
                       });
 }
 
@@ -123,13 +172,22 @@ extern "C" int crngpu_dxt5a_optimize_batch(const uint8_t* rgba_blocks, uint32_t 
   cudaStream_t s = as_stream(stream);
   return with_buffers(rgba_blocks, (size_t)n * 64, out_blocks, (size_t)n * 8, nullptr, 0, mem, s,
                       [&](const uint8_t* in, uint8_t* out, uint64_t*) {
-                        return launch_dxt5a(in, n, (int)comp_index, use_both_block_types != 0, out, 8, s);
+                        return launch_dxt5a(in, n, (int)comp_index, use_both_block_types != 0, kDxtQualityUber, out, 8,
+                                           s);
                       });
 }
 
 extern "C" int crngpu_compress_blocks(const uint8_t* rgba_blocks, uint32_t n, uint32_t format, uint32_t flags,
                                       uint8_t* out_blocks, int mem, void* stream) {
+  return crngpu_compress_blocks_ex(rgba_blocks, n, format, flags, nullptr, out_blocks, mem, stream);
+}
+
+extern "C" int crngpu_compress_blocks_ex(const uint8_t* rgba_blocks, uint32_t n, uint32_t format, uint32_t flags,
+                                         const crngpu_block_options* options, uint8_t* out_blocks, int mem,
+                                         void* stream) {
   clear_error();
+  uint32_t quality, threshold;
+  if (!read_options(options, &quality, &threshold)) return CRNGPU_E_PARAM;
   const int bpb = bytes_per_block(format);
   if (!bpb) { set_error("unsupported format"); return CRNGPU_E_UNSUPPORTED; }
   if (n && (!rgba_blocks || !out_blocks)) { set_error("bad arguments"); return CRNGPU_E_PARAM; }
@@ -137,7 +195,7 @@ extern "C" int crngpu_compress_blocks(const uint8_t* rgba_blocks, uint32_t n, ui
   cudaStream_t s = as_stream(stream);
   const int rc = with_buffers(rgba_blocks, (size_t)n * 64, out_blocks, (size_t)n * bpb, nullptr, 0, mem, s,
                               [&](const uint8_t* in, uint8_t* out, uint64_t*) {
-                                return encode_device(in, n, format, flags, out, s);
+                                return encode_device(in, n, format, flags, quality, threshold, out, nullptr, s);
                               });
   return rc == CRNGPU_OK ? bpb : rc;
 }
@@ -145,7 +203,17 @@ extern "C" int crngpu_compress_blocks(const uint8_t* rgba_blocks, uint32_t n, ui
 extern "C" int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, uint32_t height, uint32_t pitch_bytes,
                                          uint32_t format, uint32_t flags, uint8_t* out, uint64_t out_size, int mem,
                                          void* stream) {
+  return crngpu_compress_image_ex(rgba, width, height, pitch_bytes, format, flags, nullptr, out, out_size, mem,
+                                  stream);
+}
+
+extern "C" int64_t crngpu_compress_image_ex(const uint8_t* rgba, uint32_t width, uint32_t height,
+                                            uint32_t pitch_bytes, uint32_t format, uint32_t flags,
+                                            const crngpu_block_options* options, uint8_t* out, uint64_t out_size,
+                                            int mem, void* stream) {
   clear_error();
+  uint32_t quality, threshold;
+  if (!read_options(options, &quality, &threshold)) return CRNGPU_E_PARAM;
   const int bpb = bytes_per_block(format);
   if (!bpb) { set_error("unsupported format"); return CRNGPU_E_UNSUPPORTED; }
   if (!rgba || !out || !width || !height) { set_error("bad arguments"); return CRNGPU_E_PARAM; }
@@ -182,7 +250,8 @@ extern "C" int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, ui
     set_error("device output must be 8-byte aligned");
     return CRNGPU_E_PARAM;
   }
-  int rc = encode_device(static_cast<const uint8_t*>(blocks.ptr), (uint32_t)n, format, flags, d_out, s);
+  int rc = encode_device(static_cast<const uint8_t*>(blocks.ptr), (uint32_t)n, format, flags, quality, threshold, d_out,
+                         nullptr, s);
   if (rc != CRNGPU_OK) return rc;
   if (so) {
     if ((e = cudaMemcpyAsync(out, so->ptr, need, cudaMemcpyDeviceToHost, s)) != cudaSuccess)

@@ -202,10 +202,11 @@ extern "C" crngpu_encode_batch crngpu_encode_batch_create(const crngpu_encode_it
       for (uint32_t b = 0; b < count; b += step)
         list.push_back(EncodeChunk{(uint32_t)first + b, std::min(step, count - b), sid});
     };
-    const uint32_t alpha_opts = both ? kSegBothTypes : 0u;
+    // Uber quality: colour segments carry a dxt1_options() word, alpha segments the quality bits
+    const uint32_t alpha_opts = (both ? kSegBothTypes : 0u) | (kDxtQualityUber << kSegAlphaQualityShift);
     switch (it.format) {
       case CRNGPU_FMT_DXT1:
-        add_seg(it.out, 8, (perceptual ? kSegPerceptual : 0u) | (both ? kSegThreeColour : 0u), true);
+        add_seg(it.out, 8, dxt1_options(perceptual, both, kDxtQualityUber, false, false, 128), true);
         break;
       case CRNGPU_FMT_DXT5A:
         add_seg(it.out, 8, alpha_opts | (3u << kSegCompShift), false);
@@ -219,7 +220,7 @@ extern "C" crngpu_encode_batch crngpu_encode_batch_create(const crngpu_encode_it
       }
       default:  // DXT5 family: alpha element, then a colour element without 3-colour blocks
         add_seg(it.out, 16, alpha_opts | (3u << kSegCompShift), false);
-        add_seg(it.out + 8, 16, perceptual ? kSegPerceptual : 0u, true);
+        add_seg(it.out + 8, 16, dxt1_options(perceptual, false, kDxtQualityUber, false, false, 128), true);
         break;
     }
   }

@@ -3349,11 +3349,37 @@ extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uin
                                                  uint32_t levels, uint32_t faces, uint32_t format,
                                                  uint32_t quality_level, uint32_t flags, void* out,
                                                  uint64_t out_capacity) {
+  return crngpu_compress_dds_clustered_ex(rgba_levels, width, height, levels, faces, format, quality_level, flags,
+                                          nullptr, out, out_capacity);
+}
+
+extern "C" int64_t crngpu_compress_dds_clustered_ex(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
+                                                    uint32_t levels, uint32_t faces, uint32_t format,
+                                                    uint32_t quality_level, uint32_t flags,
+                                                    const crngpu_block_options* options, void* out,
+                                                    uint64_t out_capacity) {
   using namespace crngpu;
   using namespace crngpu::hc;
   clear_error();
   if (quality_level > 255) { set_error("crngpu_compress_dds_clustered: quality above 255"); return CRNGPU_E_PARAM; }
   if (format_is_non_srgb(format)) flags &= ~CRNGPU_FLAG_PERCEPTUAL;
+  // dds_comp::compress_init (crnlib/crn_dds_comp.cpp:244-247): DXT1 becomes DXT1A when the flag
+  // is set, both block types are allowed and some source texel has alpha below 255
+  if (format == CRNGPU_FMT_DXT1 && (flags & CRNGPU_FLAG_DXT1A) && (flags & CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES) &&
+      rgba_levels) {
+    bool has_alpha = false;
+    uint64_t texels = 0;
+    for (uint32_t l = 0; l < levels; l++)
+      texels += (uint64_t)std::max(1u, width >> l) * std::max(1u, height >> l) * faces;
+    for (uint64_t t = 0; t < texels && !has_alpha; t++) has_alpha = rgba_levels[t * 4 + 3] < 255;
+    if (!has_alpha) flags &= ~CRNGPU_FLAG_DXT1A;
+  } else {
+    flags &= ~CRNGPU_FLAG_DXT1A;
+  }
+  if ((flags & CRNGPU_FLAG_DXT1A) && quality_level < 255) {
+    set_error("crngpu_compress_dds_clustered: DXT1A transparency below quality 255 (qdxt1 with alpha) is not built");
+    return CRNGPU_E_UNSUPPORTED;
+  }
   CrnSource src;
   int rc = src.prepare(rgba_levels, width, height, levels, faces, format, flags, "crngpu_compress_dds_clustered");
   if (rc != CRNGPU_OK) return rc;
@@ -3376,8 +3402,8 @@ extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uin
   if (quality_level >= 255) {
     // dds_comp at quality 255 (crnlib/crn_dds_comp.cpp:150-157): the plain encoder on every block
     // of the cooked source (as qdxt1::pack at full quality: every block its own cluster)
-    const int r = crngpu_compress_blocks(static_cast<const uint8_t*>(src.d_in.ptr), N, format, flags,
-                                         static_cast<uint8_t*>(src.d_out.ptr), CRNGPU_MEM_DEVICE, nullptr);
+    const int r = crngpu_compress_blocks_ex(static_cast<const uint8_t*>(src.d_in.ptr), N, format, flags, options,
+                                            static_cast<uint8_t*>(src.d_out.ptr), CRNGPU_MEM_DEVICE, nullptr);
     if (r < 0) return r;
   } else {
     // mipmapped_texture::qdxt_pack (crnlib/crn_mipmapped_texture.cpp:2330-2560): qdxt1 on the

@@ -29,8 +29,7 @@
 
 namespace crngpu {
 
-int launch_dxt1(const uint8_t* d_blocks, uint32_t n, bool perceptual, bool use_alpha_blocks, uint8_t* d_out,
-                uint32_t out_stride, uint64_t* d_err, cudaStream_t s);
+
 
 namespace mlp {
 
@@ -1062,7 +1061,8 @@ extern "C" int crngpu_dxt1_learned(void* h, const uint8_t* d_blocks, uint32_t n,
     if ((e = net->fb_in.ensure((size_t)cnt * 64)) != cudaSuccess) return cuda_check(e, "alloc fallback blocks");
     if ((e = net->fb_out.ensure((size_t)cnt * 8)) != cudaSuccess) return cuda_check(e, "alloc fallback out");
     k_gather_idx<<<(cnt * 4 + 255) / 256, 256, 0, s>>>(d_blocks, idx, cnt_d, static_cast<uint8_t*>(net->fb_in.ptr));
-    if ((rc = launch_dxt1(static_cast<uint8_t*>(net->fb_in.ptr), cnt, perceptual != 0, true,
+    if ((rc = launch_dxt1(static_cast<uint8_t*>(net->fb_in.ptr), cnt,
+                          dxt1_options(perceptual != 0, true, kDxtQualityUber, false, false, 128),
                           static_cast<uint8_t*>(net->fb_out.ptr), 8, nullptr, s)) != CRNGPU_OK)
       return rc;
     k_scatter_idx<<<(cnt + 255) / 256, 256, 0, s>>>(static_cast<uint8_t*>(net->fb_out.ptr), idx, cnt_d, d_out);

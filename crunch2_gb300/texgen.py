@@ -97,6 +97,16 @@ def colour_texture(w: int, h: int, seed: int, with_alpha_noise: bool = False) ->
     return img
 
 
+def dark_texture(w: int, h: int, seed: int) -> np.ndarray:
+    """colour_texture with its darker half pushed to near-black (every channel 0..3): the shadowed
+    or outlined content that DXT1's transparent-index-for-black encoding targets."""
+    img = colour_texture(w, h, seed)
+    rgb = img[:, :, :3].astype(np.int32)
+    dark = rgb.sum(2) < 3 * 112
+    img[:, :, :3] = np.where(dark[:, :, None], rgb >> 6, rgb).astype(np.uint8)
+    return img
+
+
 def normal_map(w: int, h: int, seed: int, strength: float = 4.0) -> np.ndarray:
     """RGBA8 normal map: fBm height (5 octaves, period 256) -> Sobel -> unit normal, XY in RG."""
     hgt = value_noise(w, h, 256, 5, seed, 11)

@@ -48,6 +48,18 @@ extern "C" {
 /* crn_comp_flags bits that the block encoders honour (inc/crnlib.h:132-185). */
 #define CRNGPU_FLAG_PERCEPTUAL 1u
 #define CRNGPU_FLAG_USE_BOTH_BLOCK_TYPES 8u
+#define CRNGPU_FLAG_TRANSPARENT_BLACK 16u  /* cCRNCompFlagUseTransparentIndicesForBlack (DXT1, with both
+                                              block types: try_alpha_as_black_optimization) */
+#define CRNGPU_FLAG_DXT1A 128u             /* cCRNCompFlagDXT1AForTransparency: DXT1 texels with alpha below
+                                              the threshold become transparent (selector 3) */
+#define CRNGPU_FLAG_GRAYSCALE 256u         /* cCRNCompFlagGrayscaleSampling: luma distance (DXT1 colour) */
+
+/* crn_dxt_quality (inc/crnlib.h:188-199): the search effort of the block encoders. */
+#define CRNGPU_DXT_QUALITY_SUPERFAST 0u
+#define CRNGPU_DXT_QUALITY_FAST 1u
+#define CRNGPU_DXT_QUALITY_NORMAL 2u
+#define CRNGPU_DXT_QUALITY_BETTER 3u
+#define CRNGPU_DXT_QUALITY_UBER 4u
 
 /* Library version and last-error text (thread-local). */
 CRNGPU_API const char* crngpu_version(void);
@@ -79,18 +91,32 @@ CRNGPU_API int crngpu_wait_counters(crngpu_wait_stats* out, int reset);
 CRNGPU_API int crngpu_force_wait_timeouts(int on);
 
 /* ------------------------------------------------------------------------------------------
- * Block encoders (quality: cCRNDXTQualityUber; endpoint caching is never used, so results do
- * not depend on how blocks are batched).
+ * Block encoders (every crn_dxt_quality; endpoint caching is never used, so results do not
+ * depend on how blocks are batched).
  * --------------------------------------------------------------------------------------- */
 
 /* Parameters of dxt1_endpoint_optimizer::params (crnlib/crn_dxt1.h:168-201) that apply to
- * 16-texel blocks: perceptual metric and whether 3-colour (alpha) blocks may be used. */
+ * 16-texel blocks. A caller that fills only the first four fields (struct_size 16, the layout of
+ * earlier versions) gets Uber quality without grayscale sampling, DXT1A or the black trial. */
 typedef struct crngpu_dxt1_params {
-    uint32_t struct_size;      /* sizeof(crngpu_dxt1_params) */
+    uint32_t struct_size;      /* sizeof(crngpu_dxt1_params), or 16 */
     int32_t perceptual;        /* m_perceptual */
     int32_t use_alpha_blocks;  /* m_use_alpha_blocks */
     int32_t reserved;
+    uint32_t dxt_quality;      /* m_quality: CRNGPU_DXT_QUALITY_* */
+    int32_t grayscale_sampling;            /* m_grayscale_sampling */
+    int32_t dxt1a;                         /* m_pixels_have_alpha per block, as dxt_image sets it for
+                                              DXT1A: some texel's alpha is below the threshold */
+    uint32_t dxt1a_alpha_threshold;        /* m_dxt1a_alpha_threshold (128) */
+    int32_t use_transparent_indices_for_black;  /* m_use_transparent_indices_for_black */
 } crngpu_dxt1_params;
+
+/* The crn_comp_params fields the block encoders read besides m_flags (crnlib.h:231-414). */
+typedef struct crngpu_block_options {
+    uint32_t struct_size;            /* sizeof(crngpu_block_options) */
+    uint32_t dxt_quality;            /* m_dxt_quality: CRNGPU_DXT_QUALITY_* (Uber by default) */
+    uint32_t dxt1a_alpha_threshold;  /* m_dxt1a_alpha_threshold (128 by default) */
+} crngpu_block_options;
 
 /* Batched replacement for dxt1_endpoint_optimizer::compute (crnlib/crn_dxt1.h:223,
  * crnlib/crn_dxt1.cpp:2234) plus the dxt1_block packing of dxt_image::set_block_pixels
@@ -116,6 +142,13 @@ CRNGPU_API int crngpu_dxt5a_optimize_batch(const uint8_t* rgba_blocks, uint32_t 
 CRNGPU_API int crngpu_compress_blocks(const uint8_t* rgba_blocks, uint32_t n, uint32_t format, uint32_t flags,
                            uint8_t* out_blocks, int mem, void* stream);
 
+/* The same with crn_comp_params::m_dxt_quality and m_dxt1a_alpha_threshold (options NULL: Uber,
+ * 128). Also honours CRNGPU_FLAG_GRAYSCALE, CRNGPU_FLAG_DXT1A (DXT1 only) and
+ * CRNGPU_FLAG_TRANSPARENT_BLACK (DXT1 with both block types), as crn_compress_block does. */
+CRNGPU_API int crngpu_compress_blocks_ex(const uint8_t* rgba_blocks, uint32_t n, uint32_t format, uint32_t flags,
+                                         const crngpu_block_options* options, uint8_t* out_blocks, int mem,
+                                         void* stream);
+
 /* Plain (quality 255, no clustering) DXTn encode of one RGBA8 image, the dxt_image::init path
  * (crnlib/crn_dxt_image.cpp:283-349,447-493): 4x4 blocks with edge clamping, block-row-major
  * output, row pitch = blocks_x * bytes_per_block. pitch_bytes: source row pitch (0 = width*4).
@@ -123,6 +156,12 @@ CRNGPU_API int crngpu_compress_blocks(const uint8_t* rgba_blocks, uint32_t n, ui
 CRNGPU_API int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, uint32_t height, uint32_t pitch_bytes,
                               uint32_t format, uint32_t flags, uint8_t* out, uint64_t out_size, int mem,
                               void* stream);
+
+/* crngpu_compress_image with the options of crngpu_compress_blocks_ex. */
+CRNGPU_API int64_t crngpu_compress_image_ex(const uint8_t* rgba, uint32_t width, uint32_t height,
+                                            uint32_t pitch_bytes, uint32_t format, uint32_t flags,
+                                            const crngpu_block_options* options, uint8_t* out, uint64_t out_size,
+                                            int mem, void* stream);
 
 /* ------------------------------------------------------------------------------------------
  * Clustered (CRN-style) DXT1 compression: dxt_hc::compress (crnlib/crn_dxt_hc.cpp:97-316) for
@@ -227,6 +266,19 @@ CRNGPU_API int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uin
                                                  uint32_t levels, uint32_t faces, uint32_t format,
                                                  uint32_t quality_level, uint32_t flags, void* out,
                                                  uint64_t out_capacity);
+
+/* The same with crn_comp_params::m_dxt_quality and m_dxt1a_alpha_threshold (options NULL: Uber,
+ * 128) for the plain encode at quality 255, where flags may also hold CRNGPU_FLAG_GRAYSCALE,
+ * CRNGPU_FLAG_TRANSPARENT_BLACK and CRNGPU_FLAG_DXT1A (DXT1A when both block types are allowed and
+ * some texel's alpha is below 255, dds_comp::compress_init, crnlib/crn_dds_comp.cpp:244-247).
+ * Below 255 the clusterizer's per-cluster search is Uber's at every dxt quality (the output is
+ * judged on quality, not bytes), grayscale and black trials are not used (qdxt1 has neither), and
+ * DXT1A is refused with CRNGPU_E_UNSUPPORTED. */
+CRNGPU_API int64_t crngpu_compress_dds_clustered_ex(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
+                                                    uint32_t levels, uint32_t faces, uint32_t format,
+                                                    uint32_t quality_level, uint32_t flags,
+                                                    const crngpu_block_options* options, void* out,
+                                                    uint64_t out_capacity);
 
 /* Many crn_compress calls at once (no counterpart in the reference, which compresses one texture
  * per call): `threads` host threads (0 = 4), each with its own CUDA stream and device buffers, take

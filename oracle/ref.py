@@ -33,6 +33,9 @@ def lib():
         L.ref_compress_texture.argtypes = [ctypes.c_void_p, _u32, _u32, _u32, _u32, _u32, _u32, _u32, _u32, _u32,
                                            _u32, ctypes.c_void_p, _u32]
         L.ref_compress_texture.restype = _u32
+        L.ref_compress_texture_bitrate.argtypes = [ctypes.c_void_p, _u32, _u32, _u32, _u32, _u32, ctypes.c_float, _u32,
+                                                   ctypes.POINTER(_u32), ctypes.POINTER(ctypes.c_float)]
+        L.ref_compress_texture_bitrate.restype = _u32
         L.ref_unpack_level.argtypes = [ctypes.c_void_p, _u32, _u32, ctypes.c_void_p, _u32]
         L.ref_unpack_level.restype = _u32
         L.ref_time_unpack.argtypes = [ctypes.c_void_p, _u32, _u32, ctypes.c_void_p, _u32]
@@ -192,3 +195,17 @@ def crnd_probe(crn: bytes):
     values = [int(v) for v in info[:n]]
     base = values[-2]
     return values, seg[:base].tobytes() if values[-1] else b""
+
+
+def compress_texture_bitrate(levels: list[np.ndarray], fmt: int, flags: int, target: float,
+                             helper_threads: int = 0) -> tuple[int, int, float]:
+    """crn_compress (.crn) of one face's mip chain with m_target_bitrate: (file size, chosen quality
+    level, reported bitrate)."""
+    flat = np.ascontiguousarray(np.concatenate([np.ascontiguousarray(l, dtype=np.uint8).reshape(-1) for l in levels]))
+    h, w = levels[0].shape[:2]
+    q, rate = _u32(0), ctypes.c_float(0)
+    size = lib().ref_compress_texture_bitrate(flat.ctypes.data, w, h, len(levels), fmt, flags, target, helper_threads,
+                                              ctypes.byref(q), ctypes.byref(rate))
+    if not size:
+        raise RuntimeError("reference crn_compress with a target bitrate failed")
+    return int(size), int(q.value), float(rate.value)

@@ -132,6 +132,40 @@ uint32_t ref_compress_texture(const uint8_t* rgba_levels, uint32_t width, uint32
   return size;
 }
 
+// crn_compress to .crn with m_target_bitrate set (the interpolative quality search of
+// create_compressed_texture, crnlib/crn_texture_comp.cpp:143-260): returns the file size (0 on
+// failure) and the chosen quality level and the bitrate crn_compress reports.
+uint32_t ref_compress_texture_bitrate(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels,
+                                      uint32_t fmt, uint32_t flags, float target_bitrate, uint32_t helper_threads,
+                                      uint32_t* actual_quality, float* actual_bitrate) {
+  crn_comp_params p;
+  p.m_file_type = cCRNFileTypeCRN;
+  p.m_width = width;
+  p.m_height = height;
+  p.m_levels = levels;
+  p.m_faces = 1;
+  p.m_format = static_cast<crn_format>(fmt);
+  p.m_flags = flags;
+  p.m_target_bitrate = target_bitrate;
+  p.m_num_helper_threads = helper_threads;
+  size_t ofs = 0;
+  for (uint32_t l = 0; l < levels; l++) {
+    uint32_t w = width >> l ? width >> l : 1, h = height >> l ? height >> l : 1;
+    p.m_pImages[0][l] = reinterpret_cast<const crn_uint32*>(rgba_levels + ofs);
+    ofs += (size_t)w * h * 4;
+  }
+  crn_mipmap_params mp;
+  mp.m_mode = cCRNMipModeUseSourceMips;
+  crn_uint32 size = 0, q = 0;
+  float rate = 0.0f;
+  void* data = crn_compress(p, mp, size, &q, &rate);
+  if (!data) return 0;
+  crn_free_block(data);
+  if (actual_quality) *actual_quality = q;
+  if (actual_bitrate) *actual_bitrate = rate;
+  return size;
+}
+
 // Transcodes one level of a .crn file with the reference crnd unpacker into out
 // (faces x blocks_y x row_pitch bytes, row_pitch = minimal). Returns bytes written or 0.
 uint32_t ref_unpack_level(const uint8_t* crn, uint32_t crn_size, uint32_t level, uint8_t* out, uint32_t out_cap) {

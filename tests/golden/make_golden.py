@@ -173,6 +173,8 @@ CRN_CASES = [
     ("dxt5_cube_64x32", 64, 32, "DXT5", 6, "colour_alpha", 14),
     ("dxn_xy_256", 256, 256, "DXN_XY", 1, "normal", 15),
     ("dxt5a_256", 256, 256, "DXT5A", 1, "colour_alpha", 16),
+    ("dxt5_2048", 2048, 2048, "DXT5", 1, "colour_alpha", 200),    # config 2's textures (12 levels)
+    ("dxn_xy_2048", 2048, 2048, "DXN_XY", 1, "normal", 201),
 ]
 
 
@@ -181,6 +183,8 @@ def texture_levels(w, h, content, seed, faces):
     for f in range(faces):
         if content == "normal":
             img = texgen.normal_map(w, h, seed + f)
+        elif content == "dark":
+            img = texgen.dark_texture(w, h, seed + f)
         else:
             img = texgen.colour_texture(w, h, seed + f, with_alpha_noise=(content == "colour_alpha"))
         out.append(texgen.mip_chain(img))
@@ -192,10 +196,17 @@ def level_bytes(w, h, level, bpb, faces):
     return ((w + 3) // 4) * ((h + 3) // 4) * bpb * faces
 
 
-def make_crn() -> None:
+def make_crn(only=None) -> None:
+    """The reference's .crn files of CRN_CASES (those named in `only`, if given) and the per-level
+    SHA-256 of its transcode, into crn/ and crn/manifest.json."""
     os.makedirs(os.path.join(HERE, "crn"), exist_ok=True)
     manifest = {}
+    if only:
+        with open(os.path.join(HERE, "crn", "manifest.json")) as fh:
+            manifest = json.load(fh)
     for name, w, h, fmt, faces, content, seed in CRN_CASES:
+        if only and name not in only:
+            continue
         fl = texture_levels(w, h, content, seed, faces)
         flags = (0 if content == "normal" else FLAG_PERCEPTUAL) | FLAG_HIERARCHICAL | FLAG_BOTH_BLOCK_TYPES
         crn = ref.compress_texture(fl, FMT[fmt], 0, 128, flags, DXT_UBER, 7)
@@ -349,6 +360,68 @@ COMPAT_DDS_CASES = [
     ("dds_agbr_64", 64, 64, "DXT5_AGBR", 1, "colour_alpha", 21, 255),
     ("dds_qdxt_dxt1_256", 256, 256, "DXT1", 1, "colour", 10, 128),
 ]
+# rate control: (name, size, format, content, seed, target bits per texel)
+BITRATE_CASES = [("dxt1_256_r1.2", 256, "DXT1", "colour", 31, 1.2), ("dxt1_256_r1.6", 256, "DXT1", "colour", 31, 1.6),
+                 ("dxt1_256_r2.2", 256, "DXT1", "colour", 31, 2.2), ("dxt5_128_r3.0", 128, "DXT5", "colour_alpha", 32, 3.0),
+                 ("dxt1_512_r1.0", 512, "DXT1", "colour", 33, 1.0)]
+
+
+def make_bitrate() -> None:
+    """The reference's crn_compress with m_target_bitrate on seeded mip chains: the quality level its
+    search chose and the bitrate it reports (bitrate_reference.json)."""
+    out = {}
+    for name, size, fmt, content, seed, target in BITRATE_CASES:
+        fl = texture_levels(size, size, content, seed, 1)
+        flags = FLAG_PERCEPTUAL | FLAG_HIERARCHICAL | FLAG_BOTH_BLOCK_TYPES
+        nbytes, q, rate = ref.compress_texture_bitrate(fl[0], FMT[fmt], flags, target, 7)
+        out[name] = {"size": size, "format": fmt, "content": content, "seed": seed, "target": target,
+                     "quality": q, "bitrate": rate, "bytes": nbytes}
+        print(name, out[name], flush=True)
+    with open(os.path.join(HERE, "bitrate_reference.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
+# crn_compress to .dds at quality 255 with the block encoder's other parameters: (name, w, h,
+# format, content, seed, flags, dxt quality)
+FLAG_BASE = FLAG_HIERARCHICAL | FLAG_NO_ENDPOINT_CACHING
+COMPAT_DDS_OPTION_CASES = [
+    ("dds_dxt1_fast_128", 128, 128, "DXT1", "colour", 30, FLAG_BASE | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES, 1),
+    ("dds_dxt1_normal_128", 128, 128, "DXT1", "colour", 31, FLAG_BASE | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES, 2),
+    ("dds_dxt1_superfast_uniform_64", 64, 64, "DXT1", "colour", 32, FLAG_BASE, 0),
+    ("dds_dxt5_better_128", 128, 128, "DXT5", "colour_alpha", 33, FLAG_BASE | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES, 3),
+    ("dds_dxn_fast_64", 64, 64, "DXN_XY", "normal", 34, FLAG_BASE | FLAG_BOTH_BLOCK_TYPES, 1),
+    ("dds_dxt1_gray_128", 128, 128, "DXT1", "colour", 35,
+     FLAG_BASE | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES | FLAG_GRAYSCALE, 4),
+    ("dds_dxt1a_128", 128, 128, "DXT1", "colour_alpha", 36,
+     FLAG_BASE | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES | FLAG_DXT1A, 4),
+    ("dds_dxt1a_better_64", 64, 64, "DXT1", "colour_alpha", 37,
+     FLAG_BASE | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES | FLAG_DXT1A, 3),
+    ("dds_dxt1_black_128", 128, 128, "DXT1", "dark", 38,
+     FLAG_BASE | FLAG_PERCEPTUAL | FLAG_BOTH_BLOCK_TYPES | FLAG_TRANSPARENT_BLACK, 4),
+    ("dds_dxt1_black_normal_64", 64, 64, "DXT1", "dark", 39,
+     FLAG_BASE | FLAG_BOTH_BLOCK_TYPES | FLAG_TRANSPARENT_BLACK, 2),
+]
+
+
+def make_compat_dds_options() -> None:
+    """Whole .dds files of the reference's crn_compress at quality 255 below Uber dxt quality, with
+    grayscale sampling, DXT1A and transparent indices for black: compat_reference.json "dds_opts"."""
+    path = os.path.join(HERE, "compat_reference.json")
+    with open(path) as fh:
+        out = json.load(fh)
+    out["dds_opts"] = {}
+    for name, w, h, fmt, content, seed, flags, dq in COMPAT_DDS_OPTION_CASES:
+        fl = texture_levels(w, h, content, seed, 1)
+        dds = ref.compress_texture(fl, FMT_ALL[fmt], 1, 255, flags, dq, 7)
+        out["dds_opts"][name] = {"width": w, "height": h, "format": fmt, "content": content, "seed": seed,
+                                 "flags": flags, "dxt_quality": dq, "size": len(dds), "header": dds[:128].hex(),
+                                 "sha256": sha(np.frombuffer(dds, np.uint8)),
+                                 "input_sha256": sha(np.concatenate([im.reshape(-1) for f in fl for im in f]))}
+        print(name, len(dds), flush=True)
+    with open(path, "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
 # crn_compress with crn_mipmap_params, mips generated from the top level: (name, w, h, format,
 # content, seed, file type, quality, mip mode, filter, blurriness, gamma filtering, tiled, max levels,
 # min mip size)
@@ -389,7 +462,15 @@ def make_compat() -> None:
                              "size": len(data), "sha256": sha(np.frombuffer(data, np.uint8)),
                              "header": data[:128].hex() if ft == 1 else None}
         print(name, len(data), flush=True)
-    for name in sorted(CASE[0] for CASE in CRN_CASES):
+    compat_crnd(out, sorted(CASE[0] for CASE in CRN_CASES))
+    with open(os.path.join(HERE, "compat_reference.json"), "w") as fh:
+        json.dump(out, fh, indent=1, sort_keys=True)
+
+
+def compat_crnd(out: dict, names) -> None:
+    """crn_decompress_crn_to_dds and the crnd header API of the reference on the committed .crn
+    files `names`, into out["crn_to_dds"] / out["crnd"]."""
+    for name in names:
         with open(os.path.join(HERE, "crn", name + ".crn"), "rb") as fh:
             crn = fh.read()
         dds = ref.crn_to_dds(crn)
@@ -397,8 +478,6 @@ def make_compat() -> None:
                                    "header": dds[:128].hex()}
         values, seg = ref.crnd_probe(crn)
         out["crnd"][name] = {"values": values, "segmented_sha256": sha(np.frombuffer(seg, np.uint8)) if seg else None}
-    with open(os.path.join(HERE, "compat_reference.json"), "w") as fh:
-        json.dump(out, fh, indent=1, sort_keys=True)
 
 
 # mip generation cases: (name, width, height, content, seed, filter, filter scale, sRGB, wrap, comps)
@@ -480,6 +559,18 @@ if __name__ == "__main__":
         sys.exit("oracle/_ref/libcrnref.so missing: run `make -C oracle ref` where the reference tree exists")
     if sys.argv[1:] == ["quality"]:
         make_quality()
+        make_compat_dds_options()
+        sys.exit(0)
+    if sys.argv[1:] == ["bitrate"]:
+        make_bitrate()
+        sys.exit(0)
+    if sys.argv[1:] == ["crn2048"]:
+        make_crn(only=("dxt5_2048", "dxn_xy_2048"))
+        with open(os.path.join(HERE, "compat_reference.json")) as fh:
+            compat = json.load(fh)
+        compat_crnd(compat, ("dxt5_2048", "dxn_xy_2048"))
+        with open(os.path.join(HERE, "compat_reference.json"), "w") as fh:
+            json.dump(compat, fh, indent=1, sort_keys=True)
         sys.exit(0)
     if sys.argv[1:] == ["config2"]:
         make_config2()
@@ -504,4 +595,6 @@ if __name__ == "__main__":
     make_mips()
     make_qdxt()
     make_compat()
+    make_compat_dds_options()
+    make_bitrate()
     print("golden fixtures written to", HERE)

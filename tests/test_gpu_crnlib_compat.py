@@ -46,8 +46,12 @@ def texture_levels(w, h, content, seed, faces):
     from crunch2_gb300 import texgen
     out = []
     for f in range(faces):
-        img = texgen.normal_map(w, h, seed + f) if content == "normal" else \
-            texgen.colour_texture(w, h, seed + f, with_alpha_noise=(content == "colour_alpha"))
+        if content == "normal":
+            img = texgen.normal_map(w, h, seed + f)
+        elif content == "dark":
+            img = texgen.dark_texture(w, h, seed + f)
+        else:
+            img = texgen.colour_texture(w, h, seed + f, with_alpha_noise=(content == "colour_alpha"))
         out.append(texgen.mip_chain(img))
     return out
 
@@ -101,6 +105,40 @@ def test_crn_compress_dds_matches_reference(api, name):
         import crunch2_gb300 as cg
         blocks = cg.compress_dds_clustered(fl, quality=R["quality"], flags=R["flags"] & 9, fmt=FMT[R["format"]])
         assert data[128:] == blocks.tobytes()
+
+
+@pytest.mark.parametrize("name", sorted(compat()["dds_opts"]))
+def test_crn_compress_dds_block_options_match_reference(api, name):
+    """crn_compress to .dds at quality 255 below Uber dxt quality, with grayscale sampling, DXT1A
+    transparency and transparent indices for black: the reference's whole file, byte for byte."""
+    R = compat()["dds_opts"][name]
+    fl = texture_levels(R["width"], R["height"], R["content"], R["seed"], 1)
+    assert G.sha(np.concatenate([im.reshape(-1) for f in fl for im in f])) == R["input_sha256"]
+    p, keep = params_for(fl, FMT[R["format"]], 1, 255, R["flags"])
+    p.m_dxt_quality = R["dxt_quality"]
+    data, size, q, _ = call_compress(api, p)
+    assert data is not None, name
+    assert size == R["size"] and data[:128].hex() == R["header"]
+    assert sha(data) == R["sha256"], name
+
+
+def test_block_compressor_options(api):
+    """crn_create_block_compressor honours m_dxt_quality, DXT1A, grayscale sampling and transparent
+    indices for black like the batched entry point."""
+    import crunch2_gb300 as cg
+    goldq = G.blocks_quality()
+    blocks = goldq["alpha_in"][:12]
+    for flags, dq in ((1 | 8, 1), (1 | 8 | 128, 4), (1 | 8 | 256, 3), (1 | 8 | 16, 4)):
+        p = A.CrnCompParams()
+        p.m_format, p.m_flags, p.m_width, p.m_height, p.m_dxt_quality = 0, flags, 4, 4, dq
+        ctx = api.crn_create_block_compressor(ctypes.byref(p))
+        assert ctx
+        out = np.zeros((len(blocks), 8), np.uint8)
+        for i, b in enumerate(blocks):
+            src = np.ascontiguousarray(b, dtype=np.uint8)
+            api.crn_compress_block(ctx, src.ctypes.data, out[i].ctypes.data)
+        api.crn_free_block_compressor(ctx)
+        assert np.array_equal(out, cg.compress_blocks(blocks, 0, flags, quality=dq)), (flags, dq)
 
 
 @pytest.mark.parametrize("name", sorted(compat()["mips"]))
