@@ -21,8 +21,9 @@ One JSON line on stdout (rank 0):
              the reference-encoded .crn of the same texture, q128) in one persistent decode launch
              and one expansion launch (CUDA graph); the expansion kernel's HBM roofline; the
              single-texture latency; the oracle on all host cores over the same .crn
-  roofline   the encoder kernel: ALU issue roofline (candidate x colour evaluations counted on
-             the device x lane-ops per evaluation, over the peak lane-op rate)
+  roofline   the encoder kernel: ALU issue roofline (the reference's candidate x colour evaluations
+             on this workload, counted by the oracle, x lane-ops per evaluation, over the peak
+             lane-op rate); the evaluations the device executed are reported beside them
   cpu_baseline  the oracle (CPU restatement of the reference, bit-identical outputs) on all
              host cores over a bounded sample of the same blocks
 Multi-GPU: replicas only (every rank encodes its own copy; value = all ranks' texels / max time).
@@ -93,6 +94,7 @@ def clustered_leg(cg, dev, levels, blocks, texels, steps: int) -> dict:
 
 
 QDXT_REFERENCE = os.path.join(ROOT, "tests", "golden", "qdxt_reference.json")
+ENCODE_WORK = os.path.join(ROOT, "tests", "golden", "encode_work.json")
 
 
 def qdxt_leg(cg, dev, levels, blocks, texels, steps: int) -> dict:
@@ -695,11 +697,20 @@ def main():
     sm_max = clk.get("sm_max_mhz") or peaks.get("sm_max_mhz", 2070.0)
     props = torch.cuda.get_device_properties(dev)
     peak_ops = props.multi_processor_count * 128 * sm_max * 1e6  # lane-ops/s: 4 SMSPs x 32 lanes per SM
-    achieved = evals * LANE_OPS_PER_EVAL / (kernel_ms / 1e3)
+    # algorithmic units: the reference's candidate x colour evaluations on this workload (a fixed
+    # count, tests/golden/encode_work.json); the device's own executed count is reported beside it
+    with open(ENCODE_WORK) as fh:
+        work = json.load(fh)
+    alg_evals = int(work["candidate_colour_evaluations"]) if work["blocks"] == n_blocks else evals
+    achieved = alg_evals * LANE_OPS_PER_EVAL / (kernel_ms / 1e3)
+    executed = evals * LANE_OPS_PER_EVAL / (kernel_ms / 1e3)
     roofline = {"bound": "alu", "kernel": "k_dxt1_encode", "achieved": round(achieved / 1e12, 3),
                 "peak": round(peak_ops / 1e12, 3), "unit": "Tops/s", "frac": round(achieved / peak_ops, 4),
                 "traffic": None, "peak_source": f"SMs x 128 lanes x max SM clock ({peak_kind} clock)",
-                "evals_per_launch": evals, "lane_ops_per_eval": LANE_OPS_PER_EVAL,
+                "evals_per_launch": alg_evals, "evals_source": "the reference's evaluate_solution loops on this "
+                "workload, counted by the oracle (tests/golden/encode_work.json)",
+                "evals_executed": evals, "frac_executed": round(executed / peak_ops, 4),
+                "lane_ops_per_eval": LANE_OPS_PER_EVAL,
                 "kernel_ms": round(kernel_ms, 4), "hbm_bytes_algorithmic": n_blocks * 72}
     expand["peak"] = peaks["hbm_gbs"]
     expand["frac"] = round(expand["achieved"] / peaks["hbm_gbs"], 4)

@@ -1,4 +1,4 @@
-// DXT1 / DXT5A block encoders for sm_103a, bit-exact with crnlib's uber-quality optimizers.
+// DXT1 / DXT5A block encoders for sm_103a, bit-exact with crnlib's optimizers at every quality.
 //
 // DXT1 (dxt1_endpoint_optimizer, crnlib/crn_dxt1.cpp) runs in two phases inside one kernel:
 //   phase 1, lane per block: unique colours, perceptual weighting (powf), the double-precision
@@ -13,7 +13,9 @@
 //     lane after it that beats the new best, and so on. Lists whose candidates are built from
 //     the running best (lattice neighbours) are regenerated right after each acceptance.
 //     The tried-solution hash set of the reference is not needed: a repeated candidate can
-//     never be accepted (its error was already compared against an equal or larger best).
+//     never be accepted (its error was already compared against an equal or larger best), so
+//     repeats are simply evaluated again. Colours are evaluated farthest-from-the-mean first,
+//     which makes the batch early-out fire sooner (an error sum is exact in any order).
 // Distances are exact integers computed in FP32 with the expanded square
 //   w.(x-p)^2 = w.x^2 + (w.p^2 - 2 w.p.x), all terms integers below 2^24.
 // This file must be compiled with --fmad=false: the FP32/FP64 parts restate the reference's
@@ -37,6 +39,9 @@ namespace crngpu {
 
 constexpr int kBlocksPerWarp = 8;
 constexpr int kWarpsPerCta = 4;
+// CTAs per SM the encoders are compiled for (registers: 65536 / (128 x 8) = 64 per thread; the
+// phase-1 PCA spills a little, the candidate loops do not). 8 beat 4, 5 and 6 on GB300.
+constexpr int kCtasPerSm = 8;
 constexpr uint32_t kInf = 0xFFFFFFFFu;
 
 // ryg single-colour tables (crnlib/crn_ryg_dxt.cpp:58-99): [value][0]=max, [1]=min endpoint
@@ -66,9 +71,6 @@ __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31; }
 // exact float (integer value in [0, 2^23)) -> uint via the 2^23 magic constant
 __device__ __forceinline__ uint32_t f2u_exact(float v) { return __float_as_uint(__fadd_rn(v, 8388608.0f)) - 0x4B000000u; }
 
-constexpr int kHashBits = 11;
-constexpr int kHashSize = 1 << kHashBits;
-constexpr int kHashProbe = 8;
 
 // A DXT1 solution (dxt1_endpoint_optimizer::potential_solution, crn_dxt1.h:272-311) minus its
 // selectors, which are recomputed from it when needed.
@@ -107,6 +109,10 @@ struct ListDesc {
 struct WarpShared {
   float4 ucf[16];     // r, g, b as floats, X2 = weighted |x|^2
   int ucw[16];        // weights
+  // the same colours in evaluation order (farthest from the block's mean first, by weighted
+  // distance): an error sum is exact in any order, and this order makes the early-out fire sooner
+  float4 ecf[16];
+  uint32_t ecw[16], eci[16];
   uint32_t uci[16];   // r | g << 8 | b << 16
   uint2 lbr[32], lbg[64], lbb[32];  // plane lower bounds: .x = low, .y = high
   uint16_t list[64];  // low-endpoint probes / combinatorial endpoints
@@ -114,7 +120,6 @@ struct WarpShared {
   uint32_t cand[64];  // table candidates (lo | hi << 16) / combinatorial scratch colours
   State st;
   ListDesc d;
-  __align__(16) uint32_t hset[kHashSize];  // tried-solution keys (lo | hi << 16), kInf = empty
   // phase-1 hand-off, one slot per block of the warp's chunk
   float p1f[kBlocksPerWarp][9];     // axis[3], low[3], high[3]
   uint32_t p1m[kBlocksPerWarp][6];  // try_median4 candidates (lo | hi << 16)
@@ -129,8 +134,9 @@ struct WarpShared {
   uint64_t bar;
 };
 
-// four CTAs of four warps per SM: 4 x (the CTA's warps + 1 KB reserved) within 228 KB
-static_assert(sizeof(WarpShared) * kWarpsPerCta + 1024 <= 57 * 1024, "DXT1 encoder shared memory per CTA");
+// kCtasPerSm CTAs of four warps per SM: each CTA's warps + 1 KB reserved within 228 KB
+static_assert((sizeof(WarpShared) * kWarpsPerCta + 1024) * kCtasPerSm <= 228 * 1024,
+              "DXT1 encoder shared memory per CTA");
 
 // ------------------------------------------------------------------------------------------
 // Phase 1 (one lane = one block).
@@ -195,10 +201,11 @@ __device__ __forceinline__ bool is_transparent(uint32_t c, uint32_t opts) {
 }
 
 // Runs handle_multicolor_block up to optimize_endpoints' entry, plus try_median4's seeds.
+template <bool G>
 __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, uint32_t opts) {
   const int L = slot;
   const bool perceptual = (opts & kD1Perceptual) != 0;
-  const uint32_t quality = (opts >> kD1QualityShift) & 7u;
+  const uint32_t quality = G ? (opts >> kD1QualityShift) & 7u : kQUber;
   int n = 0;
   uint32_t pix[16];
   {
@@ -208,7 +215,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
       pix[4 * q] = v.x; pix[4 * q + 1] = v.y; pix[4 * q + 2] = v.z; pix[4 * q + 3] = v.w;
     }
   }
-  if (opts & kD1BlackTrial) {
+  if (G && (opts & kD1BlackTrial)) {
     // the trial runs for blocks without real transparency whose unique colours (alpha ignored)
     // are neither free of near-black ones nor all near-black (:2005-2019)
     int dark = 0;
@@ -228,7 +235,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
   int opaque = 0;
   #pragma unroll 1
   for (int p = 0; p < 16; p++) {
-    if (is_transparent(pix[p], opts)) continue;
+    if (G && is_transparent(pix[p], opts)) continue;
     const uint32_t c = pix[p] & 0xFFFFFFu;
     opaque++;
     int i = 0;
@@ -324,7 +331,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
       if (fabs(g) > m) m = fabs(g);
       if (fabs(b) > m) m = fabs(b);
       if (m > 1e-10) {
-        m = __ddiv_rn(1.0, m);
+        m = __drcp_rn(m);  // 1.0 / m, correctly rounded
         r = __dmul_rn(r, m); g = __dmul_rn(g, m); b = __dmul_rn(b, m);
       }
       const double d0 = __dsub_rn(vf[0], r), d1 = __dsub_rn(vf[1], g), d2 = __dsub_rn(vf[2], b);
@@ -549,14 +556,15 @@ struct FastSel {
   }
 };
 
+template <bool G>
 __device__ __noinline__ int selector_of(const WarpShared& S, int i, const Sol& s) {
   if (s.enforce) return s.enforced;
   const float wr = S.st.wr, wg = S.st.wg;
-  const bool gray = S.st.gray != 0;
+  const bool gray = G && S.st.gray != 0;
   const int r0 = exp5(s.lo >> 11), g0 = exp6((s.lo >> 5) & 63), b0 = exp5(s.lo & 31);
   const int r1 = exp5(s.hi >> 11), g1 = exp6((s.hi >> 5) & 63), b1 = exp5(s.hi & 31);
   const int a = s.alt;
-  if (S.st.fast) {
+  if (G && S.st.fast) {
     FastSel f;
     f.init(S.st.perceptual != 0, s.alpha != 0, a, r0, g0, b0, r1, g1, b1);
     return f.pick(S.uci[i]);
@@ -602,30 +610,6 @@ __device__ __forceinline__ void accept(WarpShared& S, uint32_t lo, uint32_t hi, 
   __syncwarp();
 }
 
-// Tried-solution set (m_solutions_tried, crn_dxt1.cpp:1323-1330): open addressing in shared
-// memory. A hit may only be reported for a key that was really evaluated before; a miss (or a
-// full probe window) just means the candidate is evaluated again, which cannot change results.
-__device__ __forceinline__ uint32_t hslot(uint32_t key) { return (key * 0x9E3779B1u) >> (32 - kHashBits); }
-__device__ __forceinline__ bool hset_find(const WarpShared& S, uint32_t key) {
-  if (key == kInf) return false;  // the empty marker is never stored as a key
-  uint32_t h = hslot(key);
-  for (int k = 0; k < kHashProbe; k++) {
-    const uint32_t v = S.hset[(h + k) & (kHashSize - 1)];
-    if (v == key) return true;
-    if (v == kInf) return false;
-  }
-  return false;
-}
-__device__ __forceinline__ void hset_insert(WarpShared& S, uint32_t key) {
-  if (key == kInf) return;
-  uint32_t h = hslot(key);
-  for (int k = 0; k < kHashProbe; k++) {
-    uint32_t* p = &S.hset[(h + k) & (kHashSize - 1)];
-    const uint32_t old = atomicCAS(p, kInf, key);
-    if (old == kInf || old == key) return;
-  }
-}
-
 // Candidate i of the current list (descriptor in S.d); false when the reference skips it.
 __device__ __forceinline__ bool gen_candidate(const WarpShared& S, const ListDesc& d, int i, uint32_t& lo, uint32_t& hi) {
   switch (d.kind) {
@@ -635,7 +619,9 @@ __device__ __forceinline__ bool gen_candidate(const WarpShared& S, const ListDes
       return true;
     }
     case LK_PAIRS: {
-      const int a = i / d.nh, b = i - a * d.nh;
+      // i / nh through a float reciprocal: exact for i < 2^10, nh <= 31 (the fraction of
+      // (i + 0.5) / nh is at least 1 / 62 away from an integer)
+      const int a = __float2int_rz(__fmul_rn(__fadd_rn((float)i, 0.5f), __frcp_rn((float)d.nh))), b = i - a * d.nh;
       const uint32_t p0 = S.list[a], p1 = S.list2[b];
       lo = canon_lo(p0, p1); hi = canon_hi(p0, p1);
       return true;
@@ -696,11 +682,13 @@ __device__ __forceinline__ bool gen_candidate(const WarpShared& S, const ListDes
 // Runs the list described by S.d from position `start` with the reference's sequential
 // semantics; see the file comment. Returns, for stop_on_accept lists, the position of the
 // first accepted candidate (or -1); otherwise 1 if anything was accepted, else 0.
+template <bool G>
 __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
   const ListDesc& d = S.d;
   const uint32_t lane = lane_id();
   const int n = S.st.n;
-  const bool three = S.st.three != 0, only3 = S.st.only3 != 0, fast = S.st.fast != 0, gray = S.st.gray != 0;
+  const bool three = S.st.three != 0, only3 = G && S.st.only3 != 0, fast = G && S.st.fast != 0;
+  const bool gray = G && S.st.gray != 0;
   const float wr = S.st.wr, wg = S.st.wg;
   bool any = false;
   int i0 = start;
@@ -715,15 +703,13 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
       i0 += 32;
       continue;
     }
-    const uint32_t key = lo | (hi << 16);
-    if (!d.alt) {
-      // a repeated candidate can never win: keep the first copy in the batch, drop keys tried before
-      const unsigned same = __match_any_sync(FULL_MASK, key);
-      const unsigned live_mask = __ballot_sync(FULL_MASK, live);
-      const unsigned grp = same & live_mask;
-      live = live && (int)lane == __ffs(grp) - 1;
-      live = live && !hset_find(S, key);
-    }
+    // No tried-solution set (m_solutions_tried, crn_dxt1.cpp:1323-1330): a candidate evaluated
+    // before had an error at or above the best of that time, and the best only falls, so evaluating
+    // it again cannot accept it. The current best itself (once there is one; same palette
+    // rounding, endpoints not bumped apart by the equal-endpoint rule) is skipped, as its error
+    // would only reach the best at its last colour.
+    if (!d.alt && B0 != kInf && !S.st.best.alt && !S.st.best.enforce)
+      live = live && (lo | (hi << 16)) != (S.st.best.lo | (S.st.best.hi << 16));
     // evaluate every lane's candidate (uber: 4- and 3-colour; hc: 4-colour; fast: the selector
     // by projection, then its distance), stopping early once no live lane can still beat the
     // running best. Blocks with transparent texels evaluate 3-colour blocks only.
@@ -740,8 +726,8 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
         int k = 0;
         if (!fast) {
           for (; k < n; k++) {
-            const float4 x = S.ucf[k];
-            const uint32_t w = (uint32_t)S.ucw[k];
+            const float4 x = S.ecf[k];
+            const uint32_t w = S.ecw[k];
             const float m01 = fminf(dist_part(x, q0), dist_part(x, q1));
             e0 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, fminf(dist_part(x, q2), dist_part(x, q3)))));
             if (three) e1 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, dist_part(x, q4))));
@@ -754,9 +740,9 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
           f4.init(perc, false, a, r0, g0, b0, r1, g1, b1);
           f3.init(perc, true, a, r0, g0, b0, r1, g1, b1);
           for (; k < n; k++) {
-            const float4 x = S.ucf[k];
-            const uint32_t c = S.uci[k];
-            const uint32_t w = (uint32_t)S.ucw[k];
+            const float4 x = S.ecf[k];
+            const uint32_t c = S.eci[k];
+            const uint32_t w = S.ecw[k];
             if (!only3) {
               const int s4 = f4.pick(c);
               const float4 q = s4 == 0 ? q0 : s4 == 1 ? q1 : s4 == 2 ? q2 : q3;
@@ -779,21 +765,18 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
     const int type = pick3 ? 1 : 0;
     // resolve the sequential outcome of the batch
     unsigned ok = __ballot_sync(FULL_MASK, live && err < B0);
-    int last = -1, cut = 31;
+    int last = -1;
     while (ok) {
       const int j = __ffs(ok) - 1;
       accept(S, __shfl_sync(FULL_MASK, lo, j), __shfl_sync(FULL_MASK, hi, j), __shfl_sync(FULL_MASK, err, j),
              __shfl_sync(FULL_MASK, type, j), d.alt);
       any = true;
       last = j;
-      if (d.dependent) { cut = j; break; }
+      if (d.dependent) break;
       const uint32_t B = S.st.best.err;
       const unsigned after = j == 31 ? 0u : (FULL_MASK << (j + 1));
       ok = __ballot_sync(FULL_MASK, live && lb < B && err < B) & after;
     }
-    // lanes past an accepted candidate of a dependent list were generated from a stale best:
-    // only candidates up to the cut count as tried
-    if (!d.alt && live && (int)lane <= cut) hset_insert(S, key);
     __syncwarp();
     if (d.dependent && last >= 0) {
       if (d.stop_on_accept) return i0 + last;
@@ -813,13 +796,14 @@ __device__ __forceinline__ void set_list(WarpShared& S, int kind, int count, int
 
 // refine_solution :525-698: least-squares endpoints from the current selectors; level 1 then tries
 // the 2 x 27 lattice neighbours of the two fitted endpoints, level 0 the fitted pair alone.
+template <bool G>
 __device__ bool refine(WarpShared& S, uint32_t& work, int level = 1) {
   compute_selectors(S);
   const uint32_t lane = lane_id();
   const int n = S.st.n;
   int a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // ak0 ak1 ak2 at1r at1g at1b at2r at2g at2b
   if ((int)lane < n) {
-    const int step = selector_of(S, lane, sel_source(S)) ^ 1;
+    const int step = selector_of<G>(S, lane, sel_source(S)) ^ 1;
     const int w = S.ucw[lane];
     const uint32_t c = S.uci[lane];
     const int r = (c & 255) * w, g = ((c >> 8) & 255) * w, b = (c >> 16) * w;
@@ -861,13 +845,14 @@ __device__ bool refine(WarpShared& S, uint32_t& work, int level = 1) {
     set_list(S, LK_REFINE, 54, 0, 0);
   }
   __syncwarp();
-  return run_list(S, 0, work) != 0;
+  return run_list<G>(S, 0, work) != 0;
 }
 
+template <bool G>
 __device__ bool all_selectors_equal(const WarpShared& S) {
   const uint32_t lane = lane_id();
   const int n = S.st.n;
-  const int mine = (int)lane < n ? selector_of(S, lane, sel_source(S)) : -1;
+  const int mine = (int)lane < n ? selector_of<G>(S, lane, sel_source(S)) : -1;
   const int first = __shfl_sync(FULL_MASK, mine, 0);
   return __all_sync(FULL_MASK, (int)lane >= n || mine == first);
 }
@@ -881,6 +866,7 @@ __device__ __forceinline__ uint32_t solid_coords(int r, int g, int b, bool three
 }
 
 // try_average_block_as_solid :93-153
+template <bool G>
 __device__ bool try_solid(WarpShared& S, uint32_t& work) {
   const uint32_t lane = lane_id();
   const int n = S.st.n;
@@ -901,7 +887,7 @@ __device__ bool try_solid(WarpShared& S, uint32_t& work) {
     if (three) S.cand[cnt++] = solid_coords(ar, ag, ab, true);
     // the other colours of the block as solid colours, at Uber only (:126-150)
     #pragma unroll 1
-    for (int i = 0; i < (S.st.quality == (int)kQUber ? n : 0); i++) {
+    for (int i = 0; i < ((!G || S.st.quality == (int)kQUber) ? n : 0); i++) {
       const uint32_t c = S.uci[i];
       const int r = c & 255, g = (c >> 8) & 255, b = c >> 16;
       if (r == ar && g == ag && b == ab) continue;
@@ -913,17 +899,18 @@ __device__ bool try_solid(WarpShared& S, uint32_t& work) {
   __syncwarp();
   set_list(S, LK_TABLE, S.d.count, 0, 0);
   __syncwarp();
-  return run_list(S, 0, work) != 0;
+  return run_list<G>(S, 0, work) != 0;
 }
 
 // compute_endpoint_component_errors :369-413 as closed-form quadratics; fills S.d.W/WP2/WPP/rem
+template <bool G>
 __device__ void comp_errors(WarpShared& S, int comp) {
   const uint32_t lane = lane_id();
   const int n = S.st.n;
   int sel = -1;
   uint32_t p = 0, w = 0;
   if ((int)lane < n) {
-    sel = selector_of(S, lane, sel_source(S));
+    sel = selector_of<G>(S, lane, sel_source(S));
     p = (S.uci[lane] >> (8 * comp)) & 255;
     w = (uint32_t)S.ucw[lane];
   }
@@ -959,6 +946,7 @@ __device__ __forceinline__ uint32_t comp_E(const ListDesc& d, int s, uint32_t p)
 }
 
 // optimize_endpoint_comps :415-486
+template <bool G>
 __device__ void optimize_comps(WarpShared& S, uint32_t& work) {
   compute_selectors(S);
   if (S.st.best.alpha || !S.st.best.err) return;
@@ -972,7 +960,7 @@ __device__ void optimize_comps(WarpShared& S, uint32_t& work) {
     const uint32_t clo = S.st.best.lo, chi = S.st.best.hi;
     int lo_u[3] = {(int)(clo >> 11), (int)((clo >> 5) & 63), (int)(clo & 31)};
     const int hi_u[3] = {(int)(chi >> 11), (int)((chi >> 5) & 63), (int)(chi & 31)};
-    comp_errors(S, comp);
+    comp_errors<G>(S, comp);
     const int limit = comp == 1 ? 64 : 32;
     auto ex = [&](int c) { return (uint32_t)(comp == 1 ? exp6(c) : exp5(c)); };
     uint32_t best_err = comp_E(S.d, 0, ex(lo_u[comp])) + comp_E(S.d, 1, ex(hi_u[comp])) +
@@ -999,11 +987,11 @@ __device__ void optimize_comps(WarpShared& S, uint32_t& work) {
       }
       int start = 0;
       while (start < limit) {
-        const int c1 = run_list(S, start, work);
+        const int c1 = run_list<G>(S, start, work);
         if (c1 < 0) break;
         if (!S.st.best.err) return;
         compute_selectors(S);
-        comp_errors(S, comp);
+        comp_errors<G>(S, comp);
         const uint32_t p0 = (uint32_t)S.d.p0, p1 = ex(c1);
         best_err = comp_E(S.d, 0, ex(c0)) + comp_E(S.d, 1, p1) + comp_E(S.d, 2, (p0 * 2 + p1) / 3) +
                    comp_E(S.d, 3, (p0 + p1 * 2) / 3);
@@ -1019,6 +1007,7 @@ __device__ void optimize_comps(WarpShared& S, uint32_t& work) {
 
 // try_combinatorial_encoding :1886-1997: blocks of 2..4 colours that were DXT-compressed
 // before may have their original endpoints recovered by extrapolation.
+template <bool G>
 __device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
   const int n = S.st.n;
   if (n < 2 || n > 4) return;
@@ -1085,7 +1074,7 @@ __device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
         S.d.row = i;
       }
       __syncwarp();
-      run_list(S, 0, work);
+      run_list<G>(S, 0, work);
     }
     if (alt) {
       if (lane == 0 && S.st.best.err) S.st.best.err = saved;
@@ -1098,16 +1087,17 @@ __device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
 // table, the probe spacing and the pass count (:716-745), whether try_median4 runs (Better and
 // up) and its refine level, the lattice moves (Normal and up; the +-2 moves and the per-pass
 // refine at Uber only) and the final tries (:1030-1058).
+template <bool G>
 __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
   const uint32_t lane = lane_id();
-  const uint32_t quality = (uint32_t)S.st.quality;
+  const uint32_t quality = G ? (uint32_t)S.st.quality : kQUber;
   if (quality >= kQBetter) {
     // try_median4: the six LBG pairs, then refine (level 1 at Uber, 0 at Better)
     if (lane < 6) S.cand[lane] = S.p1m[slot][lane];
     set_list(S, LK_TABLE, 6, 0, 0);
     __syncwarp();
-    run_list(S, 0, work);
-    refine(S, work, quality == kQUber ? 1 : 0);
+    run_list<G>(S, 0, work);
+    refine<G>(S, work, quality == kQUber ? 1 : 0);
   }
   const int table = probe_table(quality);
   const int probe_n = c_probe_size[table];
@@ -1161,7 +1151,7 @@ __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
       }
       __syncwarp();
     }
-    run_list(S, 0, work);
+    run_list<G>(S, 0, work);
     // lattice neighbours: low endpoint (26 adjacent cells, then +-2 per axis), then high
     #pragma unroll 1
     for (int side = 0; side < (quality >= kQNormal ? 2 : 0); side++) {
@@ -1173,19 +1163,19 @@ __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
           S.d.stop_on_accept = 0; S.d.side = side;
         }
         __syncwarp();
-        run_list(S, 0, work);
+        run_list<G>(S, 0, work);
       }
     }
     if (!S.st.best.err || (pass && S.st.best.err == prev)) break;
-    if (quality == kQUber) refine(S, work);
+    if (quality == kQUber) refine<G>(S, work);
   }
   if (quality < kQNormal) return;
-  if (S.st.best.err && !S.st.only3) {
+  if (S.st.best.err && !(G && S.st.only3)) {
     bool solid = false;
-    if (all_selectors_equal(S)) solid = try_solid(S, work);
-    if (!solid && quality == kQUber) optimize_comps(S, work);
+    if (all_selectors_equal<G>(S)) solid = try_solid<G>(S, work);
+    if (!solid && quality == kQUber) optimize_comps<G>(S, work);
   }
-  if (quality == kQUber && S.st.best.err) try_combinatorial(S, work);
+  if (quality == kQUber && S.st.best.err) try_combinatorial<G>(S, work);
 }
 
 // Plane tables -> per-channel lower bounds (compute_internal :2133-2203); lane c handles
@@ -1231,12 +1221,13 @@ __device__ void build_lower_bounds(WarpShared& S, int n, bool perceptual) {
 // get_block_colors3's palette (crn_dxt.cpp:234-245; selector 3 is black) is below the error in
 // err_io (crn_dxt1.cpp:2043-2075); otherwise err_out (optional) receives `err`. Every lane calls it;
 // `pixel` is the lane's texel (lanes < 16).
+template <bool G>
 __device__ __forceinline__ void block_out(const WarpShared& S, uint32_t lo, uint32_t hi, uint32_t bits, uint32_t err,
                                           uint32_t pixel, bool perceptual, bool gray, uint32_t opts,
                                           uint8_t* __restrict__ out, uint64_t* __restrict__ err_out,
                                           uint64_t* __restrict__ err_io) {
   const uint32_t lane = lane_id();
-  if (opts & kD1BlackTrial) {
+  if (G && (opts & kD1BlackTrial)) {
     uint32_t e = 0;
     if (lane < 16) {
       const uint32_t sel = (bits >> (2 * lane)) & 3u;
@@ -1273,18 +1264,19 @@ __device__ __forceinline__ void block_out(const WarpShared& S, uint32_t lo, uint
 // encode) the block is re-encoded with its near-black texels transparent and rewritten, with its
 // error, only when the trial's error over all texels, selector 3 decoding to black, is lower
 // (:2001-2079).
+template <bool G>
 __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, uint32_t opts,
                                  uint8_t* __restrict__ out, uint64_t* __restrict__ err_out,
                                  uint64_t* __restrict__ err_io) {
   const uint32_t lane = lane_id();
-  if (S.p1n[slot] < 0) return 0;  // the trial does not apply to this block
+  if (G && S.p1n[slot] < 0) return 0;  // the trial does not apply to this block
   const bool perceptual = (opts & kD1Perceptual) != 0, use_alpha = (opts & kD1Three) != 0;
-  const bool gray = (opts & kD1Gray) != 0;
-  const uint32_t quality = (opts >> kD1QualityShift) & 7u;
+  const bool gray = G && (opts & kD1Gray) != 0;
+  const uint32_t quality = G ? (opts >> kD1QualityShift) & 7u : kQUber;
   // unique colours of the opaque texels in first-occurrence order via match_any (transparent
   // texels and lanes >= 16 carry sentinels)
   const uint32_t pixel = lane < 16 ? __ldg(reinterpret_cast<const uint32_t*>(px) + lane) : 0;
-  const bool transparent = lane < 16 && is_transparent(pixel, opts);
+  const bool transparent = G && lane < 16 && is_transparent(pixel, opts);
   const bool has_t = __any_sync(FULL_MASK, transparent);
   const uint32_t key = (lane < 16 && !transparent) ? (pixel & 0xFFFFFFu) : (0x80000000u | lane);
   const unsigned match = __match_any_sync(FULL_MASK, key);
@@ -1293,9 +1285,9 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
   const unsigned lmask = __ballot_sync(FULL_MASK, is_leader);
   const int n = __popc(lmask);
   const int uidx = __popc(lmask & ((1u << leader) - 1u));
-  if (n == 0) {
+  if (G && n == 0) {
     // every texel transparent: black endpoints, all selectors 3 (:2205-2211); the search is skipped
-    block_out(S, 0u, 0u, 0xFFFFFFFFu, 0u, pixel, perceptual, gray, opts, out, err_out, err_io);
+    block_out<G>(S, 0u, 0u, 0xFFFFFFFFu, 0u, pixel, perceptual, gray, opts, out, err_out, err_io);
     return 0;
   }
   const float wr = perceptual ? 8.f : 1.f, wg = perceptual ? 25.f : 1.f;
@@ -1310,8 +1302,35 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
     S.ucw[uidx] = __popc(match);
     S.uci[uidx] = key;
   }
-  // clear the tried-set
-  for (int k = lane; k < kHashSize / 4; k += 32) reinterpret_cast<uint4*>(S.hset)[k] = make_uint4(kInf, kInf, kInf, kInf);
+  __syncwarp();
+  {
+    // evaluation order: weight x weighted squared distance from the mean, largest first (ties by
+    // first occurrence); lane i < n places colour i at its rank
+    float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t w = 0, c = 0;
+    if ((int)lane < n) { x = S.ucf[lane]; w = (uint32_t)S.ucw[lane]; c = S.uci[lane]; }
+    const float fw = (float)w;
+    const float sw = (float)__reduce_add_sync(FULL_MASK, w);
+    float m[3];
+    {
+      float a[3] = {__fmul_rn(fw, x.x), __fmul_rn(fw, x.y), __fmul_rn(fw, x.z)};
+      for (int k = 0; k < 3; k++) {
+        for (int o = 16; o > 0; o >>= 1) a[k] = __fadd_rn(a[k], __shfl_xor_sync(FULL_MASK, a[k], o));
+        m[k] = __fdiv_rn(a[k], sw);
+      }
+    }
+    const float dr = __fsub_rn(x.x, m[0]), dg = __fsub_rn(x.y, m[1]), db = __fsub_rn(x.z, m[2]);
+    const float key = (int)lane < n ? __fmul_rn(fw, __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(wr, dr), dr),
+                                                                      __fmul_rn(__fmul_rn(wg, dg), dg)),
+                                                             __fmul_rn(db, db)))
+                                    : -1.f;
+    int rank = 0;
+    for (int j = 0; j < n; j++) {
+      const float kj = __shfl_sync(FULL_MASK, key, j);
+      rank += (kj > key || (kj == key && j < (int)lane)) ? 1 : 0;
+    }
+    if ((int)lane < n) { S.ecf[rank] = x; S.ecw[rank] = w; S.eci[rank] = c; }
+  }
   // m_evaluate_hc (:2085): Uber, no 3-colour blocks, no transparency, no grayscale sampling
   const bool hc = quality == kQUber && !use_alpha && !has_t && !gray;
   if (lane == 0) {
@@ -1335,14 +1354,14 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
     if (lane == 0) { S.cand[0] = solid_coords(r, g, b, false); S.cand[1] = solid_coords(r, g, b, true); }
     set_list(S, LK_TABLE, use_alpha ? 2 : 1, 0, 0);
     __syncwarp();
-    run_list(S, 0, work);
+    run_list<G>(S, 0, work);
   } else {
-    optimize(S, slot, work);
+    optimize<G>(S, slot, work);
   }
   // return_solution :263-365 (transparent texels take selector 3)
   compute_selectors(S);
   const Sol best = S.st.best;
-  const int my_sel = (int)lane < n ? selector_of(S, lane, sel_source(S)) : 0;
+  const int my_sel = (int)lane < n ? selector_of<G>(S, lane, sel_source(S)) : 0;
   const int s = __shfl_sync(FULL_MASK, my_sel, (lane < 16 && !transparent) ? uidx : 0);
   const bool invert = best.alpha ? best.lo > best.hi : best.lo < best.hi;
   int sel = s;
@@ -1350,7 +1369,7 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
   if (transparent) sel = 3;
   const uint32_t bits = __reduce_or_sync(FULL_MASK, lane < 16 ? ((uint32_t)sel << (2 * lane)) : 0u);
   const uint32_t lo = invert ? best.hi : best.lo, hi = invert ? best.lo : best.hi;
-  block_out(S, lo, hi, bits, best.err, pixel, perceptual, gray, opts, out, err_out, err_io);
+  block_out<G>(S, lo, hi, bits, best.err, pixel, perceptual, gray, opts, out, err_out, err_io);
   return work;
 }
 
@@ -1456,7 +1475,7 @@ struct ChunkStager {
 // out + k * out_stride (and err_out[k]). staged holds the cnt blocks (shared memory, or the
 // global blocks themselves); after phase 1 has read them, issue_next() starts the next chunk's
 // copy. Returns the candidate x colour evaluation count.
-template <typename IssueNext>
+template <bool G, typename IssueNext>
 __device__ __forceinline__ unsigned long long dxt1_chunk(WarpShared& S, const uint8_t* __restrict__ blocks, uint32_t b0,
                                                          uint32_t bstride, uint32_t cnt, const uint8_t* staged,
                                                          IssueNext issue_next, uint32_t opts,
@@ -1468,19 +1487,22 @@ __device__ __forceinline__ unsigned long long dxt1_chunk(WarpShared& S, const ui
   const uint32_t lane = lane_id();
   unsigned long long work = 0;
   if (lane < cnt)
-    phase1_block(S, lane, staged ? staged + (size_t)lane * 64 : blocks + ((size_t)b0 + (size_t)lane * bstride) * 64,
+    phase1_block<G>(S, lane, staged ? staged + (size_t)lane * 64 : blocks + ((size_t)b0 + (size_t)lane * bstride) * 64,
                  opts);
   __syncwarp();
   issue_next();
   #pragma unroll 1
   for (uint32_t k = 0; k < cnt; k++)
-    work += phase2_block(S, k, blocks + ((size_t)b0 + (size_t)k * bstride) * 64, opts,
+    work += phase2_block<G>(S, k, blocks + ((size_t)b0 + (size_t)k * bstride) * 64, opts,
                          out + (size_t)k * bstride * out_stride, err_out ? err_out + (size_t)k * bstride : nullptr,
                          err_io ? err_io + (size_t)k * bstride : nullptr);
   return work;
 }
 
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
+// G = false: Uber quality, perceptual or uniform, no grayscale sampling, transparency or black trial
+// (the default encode, compiled without the general paths); G = true: every option.
+template <bool G>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kCtasPerSm)
     k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, uint32_t opts, uint8_t* __restrict__ out,
                   uint32_t out_stride, uint64_t* __restrict__ err_out, uint64_t* __restrict__ err_io,
                   unsigned long long* __restrict__ work_out) {
@@ -1502,7 +1524,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
     const uint32_t cnt = chunk_count(k0);
     const uint8_t* staged = st.acquire(S);
     const uint32_t k1 = k0 + kBlocksPerWarp;
-    work += dxt1_chunk(
+    work += dxt1_chunk<G>(
         S, blocks, b0, nwarps, cnt, staged,
         [&]() {
           if (k1 < mine) st.next(S, blocks + (size_t)first_block(k1) * 64, chunk_count(k1), nwarps);
@@ -1707,7 +1729,7 @@ __global__ void __launch_bounds__(128)
 
 static_assert(kColourChunkBlocks <= (uint32_t)kBlocksPerWarp, "a colour chunk must fit one warp's block slots");
 
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kCtasPerSm)
     k_dxt1_encode_chunks(const uint8_t* __restrict__ blocks, const EncodeChunk* __restrict__ chunks, uint32_t nchunks,
                          const EncodeSegment* __restrict__ segs) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1724,7 +1746,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4)
     const EncodeSegment sg = segs[ch.segment];
     const uint8_t* staged = st.acquire(S);
     const uint32_t nxt = c + nwarps;
-    dxt1_chunk(
+    dxt1_chunk<false>(
         S, blocks, ch.first, 1, ch.count, staged,
         [&]() {
           if (nxt < nchunks) {
@@ -1870,18 +1892,28 @@ int launch_dxt1_kernel(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8
   {
     std::lock_guard<std::mutex> lock(device_setup_mutex());
     if (dev < 64 && !attr_done[dev]) {
-      cudaError_t ae = cudaFuncSetAttribute(k_dxt1_encode, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaError_t ae = cudaFuncSetAttribute(k_dxt1_encode<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (ae == cudaSuccess)
+        ae = cudaFuncSetAttribute(k_dxt1_encode<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (ae != cudaSuccess) return cuda_check(ae, "set smem attribute");
       attr_done[dev] = true;
     }
   }
+  // the general kernel for anything beyond the default Uber encode
+  const bool general = (opts & ~(kD1Perceptual | kD1Three | (7u << kD1QualityShift) | (255u << kD1ThresholdShift))) ||
+                       ((opts >> kD1QualityShift) & 7u) != kQUber;
+  const void* kernel = general ? (const void*)k_dxt1_encode<true> : (const void*)k_dxt1_encode<false>;
   int per_sm = 1, sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dxt1_encode, kWarpsPerCta * 32, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarpsPerCta * 32, smem);
   if (per_sm < 1) per_sm = 1;
   const uint32_t full = (uint32_t)sms * (uint32_t)per_sm;
   const int grid = (int)(ctas_needed < full ? ctas_needed : full);
-  k_dxt1_encode<<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, d_out, out_stride, d_err, d_err_io, work);
+  if (general)
+    k_dxt1_encode<true><<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, d_out, out_stride, d_err, d_err_io, work);
+  else
+    k_dxt1_encode<false><<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, d_out, out_stride, d_err, d_err_io,
+                                                               work);
   return cuda_check(cudaGetLastError(), "launch k_dxt1_encode");
 }
 

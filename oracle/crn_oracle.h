@@ -35,6 +35,12 @@ typedef struct oracle_dxt1_opts {
 int oracle_dxt1_blocks_ex(const uint8_t* blocks, uint32_t n, const oracle_dxt1_opts* o, uint8_t* out,
                           uint64_t* err, int threads);
 
+// Candidate x unique-colour evaluations (colours visited by the reference's evaluate_solution
+// loops, crn_dxt1.cpp:1370-1592, 1759-1835) of the Uber DXT1 search on n blocks: the encoder's
+// algorithmic work count.
+uint64_t oracle_dxt1_count_evaluations(const uint8_t* blocks, uint32_t n, int perceptual, int use_alpha_blocks,
+                                       int threads);
+
 // DXT5A (single channel) endpoint optimizer over 4x4 blocks
 // (dxt5_endpoint_optimizer::compute, crnlib/crn_dxt5a.cpp:40-196), uber quality.
 //   comp: channel index 0..3;  use_both_block_types: allow 6-value blocks

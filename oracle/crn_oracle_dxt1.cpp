@@ -215,6 +215,11 @@ bool Dxt1Search::evaluate(Coords c, bool alt) {
   return quality_ >= kBetter ? evaluate_uber(c, alt) : evaluate_fast(c, alt);
 }
 
+// Candidate x unique-colour evaluations of the reference's loops (the encoder's unit of
+// algorithmic work): colours visited per evaluated candidate, the larger of the two block types'
+// loops where both run. Counted per thread, summed by oracle_dxt1_count_evaluations.
+thread_local uint64_t t_evals = 0;
+
 // evaluate_solution_uber :1370-1592
 bool Dxt1Search::evaluate_uber(Coords c, bool alt) {
   const int n = (int)uc_.size();
@@ -229,9 +234,10 @@ bool Dxt1Search::evaluate_uber(Coords c, bool alt) {
   const int a = alt ? 1 : 0;
   const int first_type = have_alpha_ ? 1 : 0;
   const int last_type = (have_alpha_ || use_alpha_) ? 1 : 0;
+  int visited_max = 0;
   for (int type = first_type; type <= last_type; type++) {
     uint64_t terr = 0;
-    int ncol;
+    int ncol, visited = 0;
     if (type == 0) {
       col[2] = {(col[0].r * 2 + col[1].r + a) / 3, (col[0].g * 2 + col[1].g + a) / 3, (col[0].b * 2 + col[1].b + a) / 3};
       col[3] = {(col[1].r * 2 + col[0].r + a) / 3, (col[1].g * 2 + col[0].g + a) / 3, (col[1].b * 2 + col[0].b + a) / 3};
@@ -241,6 +247,7 @@ bool Dxt1Search::evaluate_uber(Coords c, bool alt) {
       ncol = 3;
     }
     for (int i = n - 1; i >= 0; i--) {
+      visited++;
       unsigned be = mdist(perceptual_, gray_, uc_[i], col[0]);
       int bi = 0;
       for (int k = 1; k < ncol; k++) {
@@ -251,6 +258,7 @@ bool Dxt1Search::evaluate_uber(Coords c, bool alt) {
       if (terr >= trial_.error) break;
       trial_sel_[i] = (uint8_t)bi;
     }
+    visited_max = std::max(visited_max, visited);
     if (terr < trial_.error) {
       trial_.error = terr;
       trial_.alpha_block = type != 0;
@@ -258,6 +266,7 @@ bool Dxt1Search::evaluate_uber(Coords c, bool alt) {
       trial_.alt = alt;
     }
   }
+  t_evals += (uint64_t)visited_max;
   trial_.enforce = !trial_.alpha_block && trial_.c.lo == trial_.c.hi;
   if (trial_.enforce) {
     uint8_t s;
@@ -354,6 +363,7 @@ bool Dxt1Search::evaluate_hc(Coords c, bool alt) {
   RGB c3 = {(c1.r * 2 + c0.r + a) / 3, (c1.g * 2 + c0.g + a) / 3, (c1.b * 2 + c0.b + a) / 3};
   uint64_t err = 0;
   for (size_t i = 0; i < uc_.size() && err < best_.error; i++) {
+    t_evals++;
     unsigned e01 = std::min(cdist(perceptual_, uc_[i], c0), cdist(perceptual_, uc_[i], c1));
     unsigned e23 = std::min(cdist(perceptual_, uc_[i], c2), cdist(perceptual_, uc_[i], c3));
     err += (uint64_t)std::min(e01, e23) * w_[i];
@@ -1184,6 +1194,26 @@ extern "C" int oracle_dxt1_blocks_ex(const uint8_t* blocks, uint32_t n, const or
     }
   });
   return 0;
+}
+
+// Candidate x unique-colour evaluations the reference's Uber DXT1 search makes on n blocks
+// (perceptual / 3-colour flags as oracle_dxt1_blocks): the encoder's algorithmic work count.
+extern "C" uint64_t oracle_dxt1_count_evaluations(const uint8_t* blocks, uint32_t n, int perceptual,
+                                                  int use_alpha_blocks, int threads) {
+  sct();
+  std::atomic<uint64_t> total(0);
+  parallel_for(n, threads, [&](uint32_t i0, uint32_t i1) {
+    Dxt1Search s;
+    t_evals = 0;
+    for (uint32_t i = i0; i < i1; i++) {
+      uint16_t lo, hi;
+      uint8_t sel[16];
+      uint64_t e;
+      s.run(blocks + (size_t)i * 64, 16, perceptual != 0, use_alpha_blocks != 0, lo, hi, sel, e);
+    }
+    total += t_evals;
+  });
+  return total.load();
 }
 
 extern "C" int oracle_encode_blocks(const uint8_t* blocks, uint32_t n, int fmt, int perceptual,

@@ -40,6 +40,8 @@ def lib():
         L.oracle_dxt1_blocks_ex.restype = i32
         L.oracle_dxt5a_blocks_q.argtypes = [vp, u32, i32, i32, i32, vp]
         L.oracle_dxt5a_blocks_q.restype = i32
+        L.oracle_dxt1_count_evaluations.argtypes = [vp, u32, i32, i32, i32]
+        L.oracle_dxt1_count_evaluations.restype = ctypes.c_uint64
         L.oracle_encode_blocks.argtypes = [vp, u32, i32, i32, i32, vp, i32]
         L.oracle_encode_blocks.restype = i32
         L.oracle_unpack_level.argtypes = [vp, u32, u32, vp, u32, u32]
@@ -84,6 +86,14 @@ def dxt5a_blocks(blocks: np.ndarray, comp: int, use_both_block_types: bool = Tru
                                    out.ctypes.data) != 0:
         raise ValueError("bad quality")
     return out
+
+
+def dxt1_count_evaluations(blocks: np.ndarray, perceptual: bool = True, use_alpha_blocks: bool = True,
+                           threads: int = 1) -> int:
+    """Candidate x unique-colour evaluations of the reference's Uber DXT1 search on the blocks."""
+    blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+    return int(lib().oracle_dxt1_count_evaluations(blocks.ctypes.data, blocks.shape[0], int(perceptual),
+                                                   int(use_alpha_blocks), threads))
 
 
 def encode_blocks(blocks: np.ndarray, fmt: int, perceptual: bool = True, use_both_block_types: bool = True,
