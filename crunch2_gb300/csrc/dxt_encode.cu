@@ -490,9 +490,11 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
 
 // ------------------------------------------------------------------------------------------
 // Phase 2 (one warp = one block). All search state that is uniform across the warp (running
-// best, list descriptor, candidate tables, tried-set) lives in the warp's shared memory, and a
-// single non-inlined list runner holds the one copy of the candidate evaluation loop, so the
-// hot loop stays small enough for the instruction cache.
+// best, list descriptor, candidate tables) lives in the warp's shared memory, and a single
+// non-inlined list runner holds the one copy of the candidate evaluation loop; the list setups
+// (refine, solid, per-component, combinatorial) are non-inlined too. The kernel is bound by
+// instruction fetch (the largest stall reason), so the code a block's search runs through is kept
+// small: one instance of each routine.
 
 __device__ __forceinline__ uint32_t lower_bound(const WarpShared& S, uint32_t lo, uint32_t hi) {
   // evaluate_solution's plane-table prune (crn_dxt1.cpp:1312-1322)
@@ -797,7 +799,7 @@ __device__ __forceinline__ void set_list(WarpShared& S, int kind, int count, int
 // refine_solution :525-698: least-squares endpoints from the current selectors; level 1 then tries
 // the 2 x 27 lattice neighbours of the two fitted endpoints, level 0 the fitted pair alone.
 template <bool G>
-__device__ bool refine(WarpShared& S, uint32_t& work, int level = 1) {
+__device__ __noinline__ bool refine(WarpShared& S, uint32_t& work, int level = 1) {
   compute_selectors(S);
   const uint32_t lane = lane_id();
   const int n = S.st.n;
@@ -849,7 +851,7 @@ __device__ bool refine(WarpShared& S, uint32_t& work, int level = 1) {
 }
 
 template <bool G>
-__device__ bool all_selectors_equal(const WarpShared& S) {
+__device__ __noinline__ bool all_selectors_equal(const WarpShared& S) {
   const uint32_t lane = lane_id();
   const int n = S.st.n;
   const int mine = (int)lane < n ? selector_of<G>(S, lane, sel_source(S)) : -1;
@@ -867,7 +869,7 @@ __device__ __forceinline__ uint32_t solid_coords(int r, int g, int b, bool three
 
 // try_average_block_as_solid :93-153
 template <bool G>
-__device__ bool try_solid(WarpShared& S, uint32_t& work) {
+__device__ __noinline__ bool try_solid(WarpShared& S, uint32_t& work) {
   const uint32_t lane = lane_id();
   const int n = S.st.n;
   int tr = 0, tg = 0, tb = 0;
@@ -904,7 +906,7 @@ __device__ bool try_solid(WarpShared& S, uint32_t& work) {
 
 // compute_endpoint_component_errors :369-413 as closed-form quadratics; fills S.d.W/WP2/WPP/rem
 template <bool G>
-__device__ void comp_errors(WarpShared& S, int comp) {
+__device__ __noinline__ void comp_errors(WarpShared& S, int comp) {
   const uint32_t lane = lane_id();
   const int n = S.st.n;
   int sel = -1;
@@ -947,7 +949,7 @@ __device__ __forceinline__ uint32_t comp_E(const ListDesc& d, int s, uint32_t p)
 
 // optimize_endpoint_comps :415-486
 template <bool G>
-__device__ void optimize_comps(WarpShared& S, uint32_t& work) {
+__device__ __noinline__ void optimize_comps(WarpShared& S, uint32_t& work) {
   compute_selectors(S);
   if (S.st.best.alpha || !S.st.best.err) return;
   const uint32_t blo = S.st.best.lo, bhi = S.st.best.hi;
@@ -1008,7 +1010,7 @@ __device__ void optimize_comps(WarpShared& S, uint32_t& work) {
 // try_combinatorial_encoding :1886-1997: blocks of 2..4 colours that were DXT-compressed
 // before may have their original endpoints recovered by extrapolation.
 template <bool G>
-__device__ void try_combinatorial(WarpShared& S, uint32_t& work) {
+__device__ __noinline__ void try_combinatorial(WarpShared& S, uint32_t& work) {
   const int n = S.st.n;
   if (n < 2 || n > 4) return;
   const uint32_t lane = lane_id();
