@@ -117,8 +117,11 @@ int launch_dxt1_black_trial(const uint8_t* d_blocks, uint32_t n, uint32_t opts, 
                             uint64_t* d_err_io, cudaStream_t s);
 int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint32_t quality, uint8_t* d_out,
                  uint32_t out_stride, cudaStream_t s);
+// the batched colour encode: phase 1 writes one seed record of kDxt1SeedBytes per block to
+// d_seeds (room for every gathered block of the batch), phase 2 reads them
+constexpr size_t kDxt1SeedBytes = 64;
 int launch_dxt1_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,
-                       const EncodeSegment* d_segs, int grid, cudaStream_t s);
+                       const EncodeSegment* d_segs, void* d_seeds, int grid, cudaStream_t s);
 int launch_dxt5a_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,
                         const EncodeSegment* d_segs, int grid, cudaStream_t s);
 

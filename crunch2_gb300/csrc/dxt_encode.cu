@@ -27,6 +27,7 @@
 // centre of the reference.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 #include <cstring>
@@ -105,7 +106,29 @@ struct ListDesc {
   uint32_t W[4], WP2[4], WPP[4], rem[4];
 };
 
-// Per-warp shared state: phase-1 hand-off for the warp's blocks plus phase-2 working set.
+// Phase 1's hand-off for one block, written by k_dxt1_seeds to global memory and read by the
+// search kernel (64 bytes).
+struct __align__(16) Seed {
+  float f[9];     // axis[3], low[3], high[3]
+  uint32_t m[6];  // try_median4 candidates (lo | hi << 16)
+  int n;          // unique colour count (-1: the block is not tried)
+};
+static_assert(sizeof(Seed) == kDxt1SeedBytes, "seed record size");
+
+// Per-warp shared memory of the phase-1 kernel: a lane per block, 32 blocks per warp.
+constexpr int kSeedLanes = 32;
+struct SeedShared {
+  // scratch, transposed [i][lane] so lanes never share a bank
+  uint32_t t_col[16][kSeedLanes];
+  uint8_t t_w[16][kSeedLanes];
+  float t_norm[3][16][kSeedLanes];
+  // the warp's 4x4 blocks (RGBA8, 64 bytes each), staged by bulk copies (TMA) that complete on
+  // `bar`; the next group's copies are issued once the lanes have read this one
+  __align__(16) uint8_t stage[kSeedLanes * 64];
+  uint64_t bar;
+};
+
+// Per-warp shared state of the search kernel: the block's seed and the phase-2 working set.
 struct WarpShared {
   float4 ucf[16];     // r, g, b as floats, X2 = weighted |x|^2
   int ucw[16];        // weights
@@ -120,23 +143,15 @@ struct WarpShared {
   uint32_t cand[64];  // table candidates (lo | hi << 16) / combinatorial scratch colours
   State st;
   ListDesc d;
-  // phase-1 hand-off, one slot per block of the warp's chunk
-  float p1f[kBlocksPerWarp][9];     // axis[3], low[3], high[3]
-  uint32_t p1m[kBlocksPerWarp][6];  // try_median4 candidates (lo | hi << 16)
-  int p1n[kBlocksPerWarp];          // unique colour count (-1: the block is not tried)
-  // phase-1 scratch, transposed [i][lane] so lanes never share a bank
-  uint32_t t_col[16][kBlocksPerWarp];
-  uint8_t t_w[16][kBlocksPerWarp];
-  float t_norm[3][16][kBlocksPerWarp];
-  // the chunk's 4x4 blocks (RGBA8, 64 bytes each), staged by one bulk copy (TMA) that completes
-  // on `bar`; the next chunk's copy is issued once phase 1 has read this one
-  __align__(16) uint8_t stage[kBlocksPerWarp * 64];
-  uint64_t bar;
+  Seed sd;  // the current block's phase-1 hand-off
 };
 
 // kCtasPerSm CTAs of four warps per SM: each CTA's warps + 1 KB reserved within 228 KB
 static_assert((sizeof(WarpShared) * kWarpsPerCta + 1024) * kCtasPerSm <= 228 * 1024,
               "DXT1 encoder shared memory per CTA");
+constexpr int kSeedCtasPerSm = 4;
+static_assert((sizeof(SeedShared) * kWarpsPerCta + 1024) * kSeedCtasPerSm <= 228 * 1024,
+              "DXT1 phase-1 shared memory per CTA");
 
 // ------------------------------------------------------------------------------------------
 // Phase 1 (one lane = one block).
@@ -200,21 +215,15 @@ __device__ __forceinline__ bool is_transparent(uint32_t c, uint32_t opts) {
   return a < ((opts >> kD1ThresholdShift) & 255u);
 }
 
-// Runs handle_multicolor_block up to optimize_endpoints' entry, plus try_median4's seeds.
+// Runs handle_multicolor_block up to optimize_endpoints' entry, plus try_median4's seeds, for the
+// block whose 16 texels are pix (lane `slot` of the warp); the hand-off goes to *out.
 template <bool G>
-__device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, uint32_t opts) {
+__device__ void phase1_block(SeedShared& S, int slot, const uint32_t (&pix)[16], uint32_t opts,
+                             Seed* __restrict__ out) {
   const int L = slot;
   const bool perceptual = (opts & kD1Perceptual) != 0;
   const uint32_t quality = G ? (opts >> kD1QualityShift) & 7u : kQUber;
   int n = 0;
-  uint32_t pix[16];
-  {
-    const uint4* p4 = reinterpret_cast<const uint4*>(px);  // the staged copy in shared memory
-    for (int q = 0; q < 4; q++) {
-      const uint4 v = p4[q];
-      pix[4 * q] = v.x; pix[4 * q + 1] = v.y; pix[4 * q + 2] = v.z; pix[4 * q + 3] = v.w;
-    }
-  }
   if (G && (opts & kD1BlackTrial)) {
     // the trial runs for blocks without real transparency whose unique colours (alpha ignored)
     // are neither free of near-black ones nor all near-black (:2005-2019)
@@ -228,7 +237,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
       for (; i < n; i++) if (S.t_col[i][L] == c) break;
       if (i == n) { S.t_col[n][L] = c; n++; dark += is_dark(c) ? 1 : 0; }
     }
-    if (has_t || !dark || dark == n) { S.p1n[L] = -1; return; }
+    if (has_t || !dark || dark == n) { out->n = -1; return; }
     n = 0;
   }
   // unique colours of the opaque texels in first-occurrence order (compute_internal :2113-2131)
@@ -243,7 +252,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
     if (i == n) { S.t_col[n][L] = c; S.t_w[n][L] = 1; n++; }
     else S.t_w[i][L]++;
   }
-  S.p1n[L] = n;
+  out->n = n;
   // no opaque texel, or one colour and no transparency (compute_internal :2205-2227): no search
   if (n == 0 || (n == 1 && opaque == 16)) return;
   const float total = (float)opaque;  // m_total_unique_color_weight
@@ -390,9 +399,9 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
     if (ray_unit_box(high, nd, c)) { high[0] = c[0]; high[1] = c[1]; high[2] = c[2]; }
   }
   for (int k = 0; k < 3; k++) {
-    S.p1f[L][k] = axis[k];
-    S.p1f[L][3 + k] = low[k];
-    S.p1f[L][6 + k] = high[k];
+    out->f[k] = axis[k];
+    out->f[3 + k] = low[k];
+    out->f[6 + k] = high[k];
   }
   // try_median4 seeds (:1181-1308), tried at Better and Uber only (:765-771)
   if (quality < kQBetter) return;
@@ -483,7 +492,7 @@ __device__ void phase1_block(WarpShared& S, int slot, const uint8_t* __restrict_
                   b = min(clampi(q[e][2], 0, 255), 31);
         pk[e] = pack565(r, g, b);
       }
-      S.p1m[L][slot_i++] = canon_lo(pk[0], pk[1]) | (canon_hi(pk[0], pk[1]) << 16);
+      out->m[slot_i++] = canon_lo(pk[0], pk[1]) | (canon_hi(pk[0], pk[1]) << 16);
     }
   }
 }
@@ -1090,12 +1099,12 @@ __device__ __noinline__ void try_combinatorial(WarpShared& S, uint32_t& work) {
 // up) and its refine level, the lattice moves (Normal and up; the +-2 moves and the per-pass
 // refine at Uber only) and the final tries (:1030-1058).
 template <bool G>
-__device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
+__device__ void optimize(WarpShared& S, uint32_t& work) {
   const uint32_t lane = lane_id();
   const uint32_t quality = G ? (uint32_t)S.st.quality : kQUber;
   if (quality >= kQBetter) {
     // try_median4: the six LBG pairs, then refine (level 1 at Uber, 0 at Better)
-    if (lane < 6) S.cand[lane] = S.p1m[slot][lane];
+    if (lane < 6) S.cand[lane] = S.sd.m[lane];
     set_list(S, LK_TABLE, 6, 0, 0);
     __syncwarp();
     run_list<G>(S, 0, work);
@@ -1108,8 +1117,8 @@ __device__ void optimize(WarpShared& S, int slot, uint32_t& work) {
   float sa1[3], low[3], high[3];
   const float lim[3] = {31.0f, 63.0f, 31.0f};
   for (int k = 0; k < 3; k++) {
-    sa1[k] = __fmul_rn(S.p1f[slot][k], dist_per_trial);
-    const float l = __fmul_rn(S.p1f[slot][3 + k], lim[k]), h = __fmul_rn(S.p1f[slot][6 + k], lim[k]);
+    sa1[k] = __fmul_rn(S.sd.f[k], dist_per_trial);
+    const float l = __fmul_rn(S.sd.f[3 + k], lim[k]), h = __fmul_rn(S.sd.f[6 + k], lim[k]);
     low[k] = l < 0.0f ? 0.0f : (l > lim[k] ? lim[k] : l);
     high[k] = h < 0.0f ? 0.0f : (h > lim[k] ? lim[k] : h);
   }
@@ -1267,11 +1276,11 @@ __device__ __forceinline__ void block_out(const WarpShared& S, uint32_t lo, uint
 // error, only when the trial's error over all texels, selector 3 decoding to black, is lower
 // (:2001-2079).
 template <bool G>
-__device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restrict__ px, uint32_t opts,
+__device__ uint32_t phase2_block(WarpShared& S, const uint8_t* __restrict__ px, uint32_t opts,
                                  uint8_t* __restrict__ out, uint64_t* __restrict__ err_out,
                                  uint64_t* __restrict__ err_io) {
   const uint32_t lane = lane_id();
-  if (G && S.p1n[slot] < 0) return 0;  // the trial does not apply to this block
+  if (G && S.sd.n < 0) return 0;  // the trial does not apply to this block
   const bool perceptual = (opts & kD1Perceptual) != 0, use_alpha = (opts & kD1Three) != 0;
   const bool gray = G && (opts & kD1Gray) != 0;
   const uint32_t quality = G ? (opts >> kD1QualityShift) & 7u : kQUber;
@@ -1358,7 +1367,7 @@ __device__ uint32_t phase2_block(WarpShared& S, int slot, const uint8_t* __restr
     __syncwarp();
     run_list<G>(S, 0, work);
   } else {
-    optimize<G>(S, slot, work);
+    optimize<G>(S, work);
   }
   // return_solution :263-365 (transparent texels take selector 3)
   compute_selectors(S);
@@ -1392,7 +1401,7 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-__device__ __forceinline__ void stage_init(WarpShared& S) {
+__device__ __forceinline__ void stage_init(SeedShared& S) {
   if (lane_id() == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.bar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -1400,29 +1409,28 @@ __device__ __forceinline__ void stage_init(WarpShared& S) {
   __syncwarp();
 }
 
-// lane 0: announce the byte count and start the copy of cnt blocks into S.stage: block k comes
-// from src + k * stride blocks (stride 1: one copy of the whole run; else one 64-byte copy each)
-__device__ __forceinline__ void stage_issue(WarpShared& S, const uint8_t* src, uint32_t cnt, uint32_t stride = 1) {
+// lane 0: announce the byte count and start the copies of nrun runs of consecutive blocks into
+// S.stage: run j (cnt[j] blocks from src[j]) lands at stage byte offset dst[j]. Every source is a
+// block (64-byte aligned), so addresses and sizes meet the bulk copy's 16-byte rules.
+__device__ __forceinline__ void stage_issue(SeedShared& S, int nrun, const uint8_t* const* src, const uint32_t* cnt,
+                                            const uint32_t* dst) {
   if (lane_id() == 0) {
-    const uint32_t bytes = cnt * 64u, bar = smem_u32(&S.bar), dst = smem_u32(S.stage);
+    uint32_t bytes = 0;
+    for (int j = 0; j < nrun; j++) bytes += cnt[j] * 64u;
+    const uint32_t bar = smem_u32(&S.bar), base = smem_u32(S.stage);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier generic reads of the stage
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-    if (stride == 1) {
-      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-                   "l"(src), "r"(bytes), "r"(bar)
-                   : "memory");
-    } else {
-      for (uint32_t k = 0; k < cnt; k++)
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], 64, [%2];" ::"r"(
-                         dst + 64u * k),
-                     "l"(src + (size_t)k * stride * 64), "r"(bar)
+    for (int j = 0; j < nrun; j++)
+      if (cnt[j])
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         base + dst[j]),
+                     "l"(src[j]), "r"(cnt[j] * 64u), "r"(bar)
                      : "memory");
-    }
   }
 }
 
 // every lane: wait for the copy of the given phase parity; false after `polls` polls
-__device__ __forceinline__ bool stage_poll(WarpShared& S, uint32_t parity, uint32_t polls) {
+__device__ __forceinline__ bool stage_poll(SeedShared& S, uint32_t parity, uint32_t polls) {
   const uint32_t bar = smem_u32(&S.bar);
   for (uint32_t i = 0; i < polls; i++) {
     uint32_t done;
@@ -1435,106 +1443,118 @@ __device__ __forceinline__ bool stage_poll(WarpShared& S, uint32_t parity, uint3
   return false;
 }
 
-__device__ __forceinline__ bool stage_wait(WarpShared& S, uint32_t parity) {
+__device__ __forceinline__ bool stage_wait(SeedShared& S, uint32_t parity) {
   if (stage_poll(S, parity, g_stage_wait_polls)) return true;
   if (lane_id() == 0) atomicAdd(&g_stage_timeouts, 1u);
   return false;
 }
 
-// A warp's sequence of chunks with the blocks of each staged in shared memory: the copy for chunk
-// i + 1 is issued as soon as phase 1 of chunk i has read the stage, so it overlaps phase 2.
+// A warp's sequence of block groups, each staged in shared memory: the copies for group i + 1 are
+// issued as soon as the lanes have read group i from the stage, so they overlap its phase 1.
 struct ChunkStager {
   uint32_t parity = 0;
   bool live = true;   // false after a timed-out wait: blocks are then read from global memory
   bool pending = false;
-  __device__ void start(WarpShared& S, const uint8_t* src, uint32_t cnt, uint32_t stride = 1) {
+  __device__ void start(SeedShared& S, int nrun, const uint8_t* const* src, const uint32_t* cnt, const uint32_t* dst) {
     stage_init(S);
-    stage_issue(S, src, cnt, stride);
+    stage_issue(S, nrun, src, cnt, dst);
     pending = true;
   }
-  // the staged blocks of the current chunk, or nullptr once staging was abandoned (the caller then
+  // the staged blocks of the current group, or nullptr once staging was abandoned (the caller then
   // reads the blocks from global memory)
-  __device__ const uint8_t* acquire(WarpShared& S) {
+  __device__ const uint8_t* acquire(SeedShared& S) {
     if (live && pending) {
       live = stage_wait(S, parity);
       if (live) { parity ^= 1u; pending = false; }
     }
     return live ? S.stage : nullptr;
   }
-  __device__ void next(WarpShared& S, const uint8_t* src, uint32_t cnt, uint32_t stride = 1) {
+  __device__ void next(SeedShared& S, int nrun, const uint8_t* const* src, const uint32_t* cnt, const uint32_t* dst) {
     if (!live) return;
     __syncwarp();  // every lane has read the stage
-    stage_issue(S, src, cnt, stride);
+    stage_issue(S, nrun, src, cnt, dst);
     pending = true;
   }
   // before the warp exits: a copy still in flight must land first (bounded by the drain limit)
-  __device__ void finish(WarpShared& S) {
+  __device__ void finish(SeedShared& S) {
     if (pending && !stage_poll(S, parity, kStageDrainPolls) && lane_id() == 0) atomicAdd(&g_stage_drain_failures, 1u);
   }
 };
 
-// cnt (<= kBlocksPerWarp) consecutive blocks from b0 on one warp; block k's result goes to
-// out + k * out_stride (and err_out[k]). staged holds the cnt blocks (shared memory, or the
-// global blocks themselves); after phase 1 has read them, issue_next() starts the next chunk's
-// copy. Returns the candidate x colour evaluation count.
-template <bool G, typename IssueNext>
-__device__ __forceinline__ unsigned long long dxt1_chunk(WarpShared& S, const uint8_t* __restrict__ blocks, uint32_t b0,
-                                                         uint32_t bstride, uint32_t cnt, const uint8_t* staged,
-                                                         IssueNext issue_next, uint32_t opts,
-                                                         uint8_t* __restrict__ out, uint32_t out_stride,
-                                                         uint64_t* __restrict__ err_out,
-                                                         uint64_t* __restrict__ err_io) {
-  // the chunk's blocks are b0, b0 + bstride, ...; out and err_out point at block b0's result;
-  // staged holds them packed (nullptr: read them from global memory)
-  const uint32_t lane = lane_id();
-  unsigned long long work = 0;
-  if (lane < cnt)
-    phase1_block<G>(S, lane, staged ? staged + (size_t)lane * 64 : blocks + ((size_t)b0 + (size_t)lane * bstride) * 64,
-                 opts);
-  __syncwarp();
-  issue_next();
-  #pragma unroll 1
-  for (uint32_t k = 0; k < cnt; k++)
-    work += phase2_block<G>(S, k, blocks + ((size_t)b0 + (size_t)k * bstride) * 64, opts,
-                         out + (size_t)k * bstride * out_stride, err_out ? err_out + (size_t)k * bstride : nullptr,
-                         err_io ? err_io + (size_t)k * bstride : nullptr);
-  return work;
+__device__ __forceinline__ void load_pix(const uint8_t* px, uint32_t (&pix)[16]) {
+  const uint4* p4 = reinterpret_cast<const uint4*>(px);
+  for (int q = 0; q < 4; q++) {
+    const uint4 v = p4[q];
+    pix[4 * q] = v.x; pix[4 * q + 1] = v.y; pix[4 * q + 2] = v.z; pix[4 * q + 3] = v.w;
+  }
 }
 
+// Phase 1 over n blocks: warp w takes the groups of 32 consecutive blocks g = w, w + W, ..., a lane
+// per block, each group staged by one bulk copy.
+template <bool G>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kSeedCtasPerSm)
+    k_dxt1_seeds(const uint8_t* __restrict__ blocks, uint32_t n, uint32_t opts, Seed* __restrict__ seeds) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SeedShared& S = reinterpret_cast<SeedShared*>(smem_raw)[threadIdx.x >> 5];
+  const uint32_t lane = lane_id();
+  const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  const uint32_t nwarps = gridDim.x * kWarpsPerCta;
+  const uint32_t groups = (n + kSeedLanes - 1) / kSeedLanes;
+  const uint32_t zero = 0;
+  auto run = [&](uint32_t g, const uint8_t*& src, uint32_t& cnt) {
+    src = blocks + (size_t)g * kSeedLanes * 64;
+    cnt = min((uint32_t)kSeedLanes, n - g * kSeedLanes);
+  };
+  ChunkStager st;
+  if (warp_global < groups) {
+    const uint8_t* src; uint32_t cnt;
+    run(warp_global, src, cnt);
+    st.start(S, 1, &src, &cnt, &zero);
+  }
+  for (uint32_t g = warp_global; g < groups; g += nwarps) {
+    const uint32_t b = g * kSeedLanes + lane;
+    const uint8_t* staged = st.acquire(S);
+    uint32_t pix[16];
+    if (b < n) load_pix(staged ? staged + (size_t)lane * 64 : blocks + (size_t)b * 64, pix);
+    const uint32_t gn = g + nwarps;
+    if (gn < groups) {
+      const uint8_t* src; uint32_t cnt;
+      run(gn, src, cnt);
+      st.next(S, 1, &src, &cnt, &zero);
+    }
+    if (b < n) phase1_block<G>(S, (int)lane, pix, opts, seeds + b);
+  }
+  st.finish(S);
+}
+
+// one lane per 16 bytes: the block's seed into the warp's shared memory
+__device__ __forceinline__ void load_seed(WarpShared& S, const Seed* __restrict__ seed) {
+  const uint32_t lane = lane_id();
+  if (lane < 4) reinterpret_cast<uint4*>(&S.sd)[lane] = __ldg(reinterpret_cast<const uint4*>(seed) + lane);
+  __syncwarp();
+}
+
+// Phase 2 over n blocks whose seeds k_dxt1_seeds wrote: warp w takes blocks w, w + W, w + 2W, ...
+// (every warp's count within one of the others', block costs interleaved across warps).
 // G = false: Uber quality, perceptual or uniform, no grayscale sampling, transparency or black trial
 // (the default encode, compiled without the general paths); G = true: every option.
 template <bool G>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kCtasPerSm)
-    k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, uint32_t opts, uint8_t* __restrict__ out,
-                  uint32_t out_stride, uint64_t* __restrict__ err_out, uint64_t* __restrict__ err_io,
-                  unsigned long long* __restrict__ work_out) {
+    k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, uint32_t opts, const Seed* __restrict__ seeds,
+                  uint8_t* __restrict__ out, uint32_t out_stride, uint64_t* __restrict__ err_out,
+                  uint64_t* __restrict__ err_io, unsigned long long* __restrict__ work_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpShared& S = reinterpret_cast<WarpShared*>(smem_raw)[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
   const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const uint32_t nwarps = gridDim.x * kWarpsPerCta;
-  // warp w takes blocks w, w + nwarps, w + 2 nwarps, ... (every warp's count within one of the
-  // others', block costs interleaved across warps), eight at a time
-  const uint32_t mine = warp_global < n ? (n - warp_global + nwarps - 1) / nwarps : 0;
   unsigned long long work = 0;
-  auto chunk_count = [&](uint32_t k0) { return min((uint32_t)kBlocksPerWarp, mine - k0); };
-  auto first_block = [&](uint32_t k0) { return warp_global + k0 * nwarps; };
-  ChunkStager st;
-  if (mine) st.start(S, blocks + (size_t)first_block(0) * 64, chunk_count(0), nwarps);
-  for (uint32_t k0 = 0; k0 < mine; k0 += kBlocksPerWarp) {
-    const uint32_t b0 = first_block(k0);
-    const uint32_t cnt = chunk_count(k0);
-    const uint8_t* staged = st.acquire(S);
-    const uint32_t k1 = k0 + kBlocksPerWarp;
-    work += dxt1_chunk<G>(
-        S, blocks, b0, nwarps, cnt, staged,
-        [&]() {
-          if (k1 < mine) st.next(S, blocks + (size_t)first_block(k1) * 64, chunk_count(k1), nwarps);
-        },
-        opts, out + (size_t)b0 * out_stride, out_stride, err_out ? err_out + b0 : nullptr,
-        err_io ? err_io + b0 : nullptr);
+  #pragma unroll 1
+  for (uint32_t b = warp_global; b < n; b += nwarps) {
+    load_seed(S, seeds + b);
+    work += phase2_block<G>(S, blocks + (size_t)b * 64, opts, out + (size_t)b * out_stride,
+                            err_out ? err_out + b : nullptr, err_io ? err_io + b : nullptr);
   }
-  st.finish(S);
   if (work_out) {
     for (int o = 16; o > 0; o >>= 1) work += __shfl_xor_sync(FULL_MASK, work, o);
     if (lane == 0 && work) atomicAdd(work_out, work);
@@ -1729,36 +1749,74 @@ __global__ void __launch_bounds__(128)
 // consecutive blocks of one segment (one element of one texture: its DXT1 colour, DXT5 colour or
 // alpha, a DXN channel); the segment gives the output base, stride and encoder options.
 
-static_assert(kColourChunkBlocks <= (uint32_t)kBlocksPerWarp, "a colour chunk must fit one warp's block slots");
+static_assert(kSeedLanes % kColourChunkBlocks == 0 && kSeedLanes / kColourChunkBlocks == 4,
+              "the phase-1 kernel stages four colour chunks per warp");
 
+// Phase 1 of the batched encode: warp w takes the groups of 4 consecutive chunks g = w, w + W, ...
+// (lane 8j + k: block k of chunk 4g + j), each chunk's run of blocks staged by one bulk copy; the
+// seed of block b goes to seeds[b].
+__global__ void __launch_bounds__(kWarpsPerCta * 32, kSeedCtasPerSm)
+    k_dxt1_seeds_chunks(const uint8_t* __restrict__ blocks, const EncodeChunk* __restrict__ chunks, uint32_t nchunks,
+                        const EncodeSegment* __restrict__ segs, Seed* __restrict__ seeds) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SeedShared& S = reinterpret_cast<SeedShared*>(smem_raw)[threadIdx.x >> 5];
+  const uint32_t lane = lane_id();
+  const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  const uint32_t nwarps = gridDim.x * kWarpsPerCta;
+  constexpr uint32_t kPer = kSeedLanes / kColourChunkBlocks;  // chunks per group
+  const uint32_t groups = (nchunks + kPer - 1) / kPer;
+  const uint32_t dst[kPer] = {0, 64 * kColourChunkBlocks, 128 * kColourChunkBlocks, 192 * kColourChunkBlocks};
+  auto runs = [&](uint32_t g, const uint8_t* (&src)[kPer], uint32_t (&cnt)[kPer]) {
+    for (uint32_t j = 0; j < kPer; j++) {
+      const uint32_t c = g * kPer + j;
+      const EncodeChunk ch = c < nchunks ? chunks[c] : EncodeChunk{0, 0, 0};
+      src[j] = blocks + (size_t)ch.first * 64;
+      cnt[j] = ch.count;
+    }
+  };
+  ChunkStager st;
+  if (warp_global < groups) {
+    const uint8_t* src[kPer]; uint32_t cnt[kPer];
+    runs(warp_global, src, cnt);
+    st.start(S, kPer, src, cnt, dst);
+  }
+  for (uint32_t g = warp_global; g < groups; g += nwarps) {
+    const uint32_t c = g * kPer + lane / kColourChunkBlocks, k = lane % kColourChunkBlocks;
+    const EncodeChunk ch = c < nchunks ? chunks[c] : EncodeChunk{0, 0, 0};
+    const bool mine = k < ch.count;
+    const uint8_t* staged = st.acquire(S);
+    uint32_t pix[16];
+    if (mine) load_pix(staged ? staged + (size_t)lane * 64 : blocks + ((size_t)ch.first + k) * 64, pix);
+    const uint32_t gn = g + nwarps;
+    if (gn < groups) {
+      const uint8_t* src[kPer]; uint32_t cnt[kPer];
+      runs(gn, src, cnt);
+      st.next(S, kPer, src, cnt, dst);
+    }
+    if (mine) phase1_block<false>(S, (int)lane, pix, segs[ch.segment].options, seeds + ch.first + k);
+  }
+  st.finish(S);
+}
+
+// Phase 2 of the batched encode: persistent warps walk the chunk table, a block at a time.
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kCtasPerSm)
     k_dxt1_encode_chunks(const uint8_t* __restrict__ blocks, const EncodeChunk* __restrict__ chunks, uint32_t nchunks,
-                         const EncodeSegment* __restrict__ segs) {
+                         const EncodeSegment* __restrict__ segs, const Seed* __restrict__ seeds) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpShared& S = reinterpret_cast<WarpShared*>(smem_raw)[threadIdx.x >> 5];
   const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
   const uint32_t nwarps = gridDim.x * kWarpsPerCta;
-  ChunkStager st;
-  if (warp_global < nchunks) {
-    const EncodeChunk c0 = chunks[warp_global];
-    st.start(S, blocks + (size_t)c0.first * 64, c0.count);
-  }
   for (uint32_t c = warp_global; c < nchunks; c += nwarps) {
     const EncodeChunk ch = chunks[c];
     const EncodeSegment sg = segs[ch.segment];
-    const uint8_t* staged = st.acquire(S);
-    const uint32_t nxt = c + nwarps;
-    dxt1_chunk<false>(
-        S, blocks, ch.first, 1, ch.count, staged,
-        [&]() {
-          if (nxt < nchunks) {
-            const EncodeChunk cn = chunks[nxt];
-            st.next(S, blocks + (size_t)cn.first * 64, cn.count);
-          }
-        },
-        sg.options, sg.out + (size_t)(ch.first - sg.first_block) * sg.stride, sg.stride, nullptr, nullptr);
+    #pragma unroll 1
+    for (uint32_t k = 0; k < ch.count; k++) {
+      const uint32_t b = ch.first + k;
+      load_seed(S, seeds + b);
+      phase2_block<false>(S, blocks + (size_t)b * 64, sg.options, sg.out + (size_t)(b - sg.first_block) * sg.stride,
+                          nullptr, nullptr);
+    }
   }
-  st.finish(S);
 }
 
 __global__ void __launch_bounds__(128)
@@ -1878,45 +1936,108 @@ int read_work_counter(uint64_t* value, cudaStream_t s) {
 
 namespace {
 
+// Per-device stream-ordered pool for the seed records between the two DXT1 kernels (memory is
+// kept in the pool between calls, so steady-state calls do not go to the driver).
+int seed_pool(int dev, cudaMemPool_t* out) {
+  static cudaMemPool_t pools[64] = {};
+  if (dev < 0 || dev >= 64) { set_error("device index out of range"); return CRNGPU_E_PARAM; }
+  std::lock_guard<std::mutex> lock(device_setup_mutex());
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p;
+    cudaError_t e = cudaMemPoolCreate(&p, &props);
+    if (e != cudaSuccess) return cuda_check(e, "create seed pool");
+    uint64_t keep = ~0ull;
+    if ((e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess)
+      return cuda_check(e, "seed pool attribute");
+    pools[dev] = p;
+  }
+  *out = pools[dev];
+  return CRNGPU_OK;
+}
+
+// Shared-memory attributes and resident CTAs per SM of the DXT1 kernels, set up once per device.
+struct Dxt1Launch {
+  int sms = 148, seeds_per_sm = 1, search_per_sm[2] = {1, 1};
+};
+int dxt1_launch_setup(int dev, Dxt1Launch* L) {
+  static Dxt1Launch cache[64];
+  static bool done[64] = {};
+  if (dev < 0 || dev >= 64) { set_error("device index out of range"); return CRNGPU_E_PARAM; }
+  std::lock_guard<std::mutex> lock(device_setup_mutex());
+  if (!done[dev]) {
+    Dxt1Launch c;
+    const int smem = (int)(sizeof(WarpShared) * kWarpsPerCta), seed_smem = (int)(sizeof(SeedShared) * kWarpsPerCta);
+    cudaError_t e = cudaFuncSetAttribute(k_dxt1_encode<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dxt1_encode<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_dxt1_encode_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_dxt1_seeds<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, seed_smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_dxt1_seeds<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, seed_smem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_dxt1_seeds_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, seed_smem);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&c.sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.seeds_per_sm, k_dxt1_seeds<true>, kWarpsPerCta * 32, seed_smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.search_per_sm[0], k_dxt1_encode<false>, kWarpsPerCta * 32, smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c.search_per_sm[1], k_dxt1_encode<true>, kWarpsPerCta * 32, smem);
+    if (e != cudaSuccess) return cuda_check(e, "set up the DXT1 kernels");
+    c.seeds_per_sm = c.seeds_per_sm < 1 ? 1 : c.seeds_per_sm;
+    for (int k = 0; k < 2; k++) c.search_per_sm[k] = c.search_per_sm[k] < 1 ? 1 : c.search_per_sm[k];
+    cache[dev] = c;
+    done[dev] = true;
+  }
+  *L = cache[dev];
+  return CRNGPU_OK;
+}
+
+// Phase 1 (k_dxt1_seeds) then phase 2 (k_dxt1_encode) over n blocks, their seed records in
+// stream-ordered memory from the seed pool.
 int launch_dxt1_kernel(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
                        uint64_t* d_err, uint64_t* d_err_io, cudaStream_t s) {
   int rc = ensure_tables();
   if (rc != CRNGPU_OK) return rc;
   if (!n) return CRNGPU_OK;
   if (((opts >> kD1QualityShift) & 7u) > kQUber) { set_error("bad DXT quality"); return CRNGPU_E_PARAM; }
-  const uint32_t warps_needed = (n + kBlocksPerWarp - 1) / kBlocksPerWarp;
-  const uint32_t ctas_needed = (warps_needed + kWarpsPerCta - 1) / kWarpsPerCta;
-  unsigned long long* work = g_count ? static_cast<unsigned long long*>(g_count_buf.ptr) : nullptr;
-  const size_t smem = sizeof(WarpShared) * kWarpsPerCta;
-  static bool attr_done[64] = {};
   int dev = 0;
-  cudaGetDevice(&dev);
-  {
-    std::lock_guard<std::mutex> lock(device_setup_mutex());
-    if (dev < 64 && !attr_done[dev]) {
-      cudaError_t ae = cudaFuncSetAttribute(k_dxt1_encode<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (ae == cudaSuccess)
-        ae = cudaFuncSetAttribute(k_dxt1_encode<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (ae != cudaSuccess) return cuda_check(ae, "set smem attribute");
-      attr_done[dev] = true;
-    }
-  }
-  // the general kernel for anything beyond the default Uber encode
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
+  Dxt1Launch L;
+  if ((rc = dxt1_launch_setup(dev, &L)) != CRNGPU_OK) return rc;
+  cudaMemPool_t pool;
+  if ((rc = seed_pool(dev, &pool)) != CRNGPU_OK) return rc;
+  Seed* seeds = nullptr;
+  if ((e = cudaMallocFromPoolAsync(reinterpret_cast<void**>(&seeds), (size_t)n * sizeof(Seed), pool, s)) != cudaSuccess)
+    return cuda_check(e, "allocate seed records");
+  unsigned long long* work = g_count ? static_cast<unsigned long long*>(g_count_buf.ptr) : nullptr;
+  // the general kernels for anything beyond the default Uber encode
   const bool general = (opts & ~(kD1Perceptual | kD1Three | (7u << kD1QualityShift) | (255u << kD1ThresholdShift))) ||
                        ((opts >> kD1QualityShift) & 7u) != kQUber;
-  const void* kernel = general ? (const void*)k_dxt1_encode<true> : (const void*)k_dxt1_encode<false>;
-  int per_sm = 1, sms = 148;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarpsPerCta * 32, smem);
-  if (per_sm < 1) per_sm = 1;
-  const uint32_t full = (uint32_t)sms * (uint32_t)per_sm;
-  const int grid = (int)(ctas_needed < full ? ctas_needed : full);
-  if (general)
-    k_dxt1_encode<true><<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, d_out, out_stride, d_err, d_err_io, work);
-  else
-    k_dxt1_encode<false><<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, d_out, out_stride, d_err, d_err_io,
-                                                               work);
-  return cuda_check(cudaGetLastError(), "launch k_dxt1_encode");
+  const uint32_t seed_warps = (n + kSeedLanes - 1) / kSeedLanes;
+  const uint32_t seed_full = (uint32_t)(L.sms * L.seeds_per_sm);
+  const uint32_t seed_grid = std::min<uint32_t>((seed_warps + kWarpsPerCta - 1) / kWarpsPerCta, seed_full);
+  const size_t seed_smem = sizeof(SeedShared) * kWarpsPerCta, smem = sizeof(WarpShared) * kWarpsPerCta;
+  const uint32_t full = (uint32_t)(L.sms * L.search_per_sm[general ? 1 : 0]);
+  const uint32_t grid = std::min<uint32_t>((n + kWarpsPerCta - 1) / kWarpsPerCta, full);
+  if (general) {
+    k_dxt1_seeds<true><<<seed_grid, kWarpsPerCta * 32, seed_smem, s>>>(d_blocks, n, opts, seeds);
+    k_dxt1_encode<true><<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, seeds, d_out, out_stride, d_err,
+                                                             d_err_io, work);
+  } else {
+    k_dxt1_seeds<false><<<seed_grid, kWarpsPerCta * 32, seed_smem, s>>>(d_blocks, n, opts, seeds);
+    k_dxt1_encode<false><<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, seeds, d_out, out_stride, d_err,
+                                                              d_err_io, work);
+  }
+  e = cudaGetLastError();
+  const cudaError_t fe = cudaFreeAsync(seeds, s);
+  if (e != cudaSuccess) return cuda_check(e, "launch k_dxt1_seeds / k_dxt1_encode");
+  return cuda_check(fe, "release seed records");
 }
 
 }  // namespace
@@ -1934,13 +2055,12 @@ int launch_dxt1_black_trial(const uint8_t* d_blocks, uint32_t n, uint32_t opts, 
 
 int dxt1_chunks_max_grid() {
   const size_t smem = sizeof(WarpShared) * kWarpsPerCta;
-  int dev = 0, per_sm = 1, sms = 148;
+  int dev = 0, per_sm = 1;
   cudaGetDevice(&dev);
-  if (cudaFuncSetAttribute(k_dxt1_encode_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return -1;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  Dxt1Launch L;
+  if (dxt1_launch_setup(dev, &L) != CRNGPU_OK) return -1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dxt1_encode_chunks, kWarpsPerCta * 32, smem);
-  return sms * (per_sm < 1 ? 1 : per_sm);
+  return L.sms * (per_sm < 1 ? 1 : per_sm);
 }
 
 int dxt5a_chunks_max_grid() {
@@ -1952,13 +2072,23 @@ int dxt5a_chunks_max_grid() {
 }
 
 int launch_dxt1_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,
-                       const EncodeSegment* d_segs, int grid, cudaStream_t s) {
+                       const EncodeSegment* d_segs, void* d_seeds, int grid, cudaStream_t s) {
   int rc = ensure_tables();
   if (rc != CRNGPU_OK) return rc;
   if (!nchunks) return CRNGPU_OK;
-  const size_t smem = sizeof(WarpShared) * kWarpsPerCta;
-  k_dxt1_encode_chunks<<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, d_chunks, nchunks, d_segs);
-  return cuda_check(cudaGetLastError(), "launch k_dxt1_encode_chunks");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  Dxt1Launch L;
+  if ((rc = dxt1_launch_setup(dev, &L)) != CRNGPU_OK) return rc;
+  const uint32_t groups = (nchunks + 3) / 4;
+  const uint32_t seed_grid =
+      std::min<uint32_t>((groups + kWarpsPerCta - 1) / kWarpsPerCta, (uint32_t)(L.sms * L.seeds_per_sm));
+  Seed* seeds = static_cast<Seed*>(d_seeds);
+  k_dxt1_seeds_chunks<<<seed_grid, kWarpsPerCta * 32, sizeof(SeedShared) * kWarpsPerCta, s>>>(d_blocks, d_chunks,
+                                                                                           nchunks, d_segs, seeds);
+  k_dxt1_encode_chunks<<<grid, kWarpsPerCta * 32, sizeof(WarpShared) * kWarpsPerCta, s>>>(d_blocks, d_chunks, nchunks,
+                                                                                         d_segs, seeds);
+  return cuda_check(cudaGetLastError(), "launch k_dxt1_seeds_chunks / k_dxt1_encode_chunks");
 }
 
 int launch_dxt5a_chunks(const uint8_t* d_blocks, const EncodeChunk* d_chunks, uint32_t nchunks,

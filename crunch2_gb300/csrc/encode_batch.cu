@@ -56,6 +56,7 @@ struct EncodeBatch {
   uint64_t nblocks = 0, texels = 0;
   uint32_t ntiles = 0, ncolour = 0, nalpha = 0;
   DevBuf blocks, d_tiles, d_segs, d_cchunks, d_achunks;
+  DevBuf seeds;  // the colour encoder's per-block hand-off between its two kernels
   int sms = 148, colour_max = 0, alpha_max = 0;
   int colour_grid = 0, alpha_grid = 0;  // 0 until tuned
   float colour_ms[kColourVariants] = {}, alpha_ms[kAlphaVariants] = {};
@@ -80,7 +81,8 @@ int enqueue(EncodeBatch* b, cudaStream_t s, int colour_grid, int alpha_grid) {
                                b->side);
   if (rc != CRNGPU_OK) return rc;
   if ((e = cudaEventRecord(b->join, b->side)) != cudaSuccess) return cuda_check(e, "record join");
-  rc = launch_dxt1_chunks(blk, static_cast<const EncodeChunk*>(b->d_cchunks.ptr), b->ncolour, segs, colour_grid, s);
+  rc = launch_dxt1_chunks(blk, static_cast<const EncodeChunk*>(b->d_cchunks.ptr), b->ncolour, segs, b->seeds.ptr,
+                          colour_grid, s);
   if (rc != CRNGPU_OK) return rc;
   if ((e = cudaStreamWaitEvent(s, b->join, 0)) != cudaSuccess) return cuda_check(e, "wait join");
   return CRNGPU_OK;
@@ -101,7 +103,7 @@ int autotune(EncodeBatch* b, cudaStream_t s) {
     for (int rep = 0; rep < 2; rep++) {
       cudaEventRecord(ev[0], s);
       const int r = colour ? launch_dxt1_chunks(blk, static_cast<const EncodeChunk*>(b->d_cchunks.ptr), b->ncolour,
-                                                segs, grid, s)
+                                                segs, b->seeds.ptr, grid, s)
                            : launch_dxt5a_chunks(blk, static_cast<const EncodeChunk*>(b->d_achunks.ptr), b->nalpha,
                                                  segs, grid, s);
       if (r != CRNGPU_OK) return r;
@@ -243,6 +245,7 @@ extern "C" crngpu_encode_batch crngpu_encode_batch_create(const crngpu_encode_it
       rc = cuda_check(e, what);
   };
   if (rc == CRNGPU_OK && (e = b->blocks.ensure(nblocks * 64)) != cudaSuccess) rc = cuda_check(e, "alloc blocks");
+  if (rc == CRNGPU_OK && (e = b->seeds.ensure(nblocks * kDxt1SeedBytes)) != cudaSuccess) rc = cuda_check(e, "alloc seeds");
   upload(b->d_tiles, tiles.data(), tiles.size() * sizeof(GatherTile), "upload gather tiles");
   upload(b->d_segs, segs.data(), segs.size() * sizeof(EncodeSegment), "upload segments");
   upload(b->d_cchunks, cchunks.data(), cchunks.size() * sizeof(EncodeChunk), "upload colour chunks");
