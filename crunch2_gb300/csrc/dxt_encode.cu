@@ -141,6 +141,7 @@ struct WarpShared {
   uint16_t list[64];  // low-endpoint probes / combinatorial endpoints
   uint16_t list2[32]; // high-endpoint probes
   uint32_t cand[64];  // table candidates (lo | hi << 16) / combinatorial scratch colours
+  uint2 pq[64];       // run_list's queue of unpruned candidates of a fixed list: (lo | hi << 16, bound)
   State st;
   ListDesc d;
   Seed sd;  // the current block's phase-1 hand-off
@@ -703,24 +704,67 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
   const float wr = S.st.wr, wg = S.st.wg;
   bool any = false;
   int i0 = start;
-  while (i0 < d.count) {
-    const int i = i0 + (int)lane;
-    uint32_t lo = 0, hi = 0;
-    bool valid = i < d.count && gen_candidate(S, d, i, lo, hi);
-    const uint32_t lb = valid ? lower_bound(S, lo, hi) : kInf;
+  // Lists whose candidates do not depend on the running best are compacted: the candidates that
+  // survive the plane-table prune (against the best when they are generated) queue up in list order
+  // in S.pq, and each batch evaluates 32 of them, so the colour loop runs on full warps. The prune
+  // is repeated against the best at the start of the batch; acceptances follow list order, as in
+  // the sparse form. Lists regenerated after each acceptance run sparse, 32 positions at a time.
+  const bool compact = !d.dependent;
+  int qn = 0;  // queued candidates (compact lists)
+  // No tried-solution set (m_solutions_tried, crn_dxt1.cpp:1323-1330): a candidate evaluated
+  // before had an error at or above the best of that time, and the best only falls, so evaluating
+  // it again cannot accept it. The current best itself (once there is one; same palette rounding,
+  // endpoints not bumped apart by the equal-endpoint rule) is skipped, as its error would only
+  // reach the best at its last colour.
+  auto not_best = [&](uint32_t lo, uint32_t hi) {
+    const Sol& b = S.st.best;
+    return d.alt || b.err == kInf || b.alt || b.enforce || (lo | (hi << 16)) != (b.lo | (b.hi << 16));
+  };
+  for (;;) {
+    uint32_t lo = 0, hi = 0, lb = kInf;
+    bool live;
+    int take = 32;
     const uint32_t B0 = S.st.best.err;
-    bool live = valid && lb < B0;
-    if (!__any_sync(FULL_MASK, live)) {  // the whole batch is pruned: nothing tried, nothing to insert
-      i0 += 32;
+    if (compact) {
+      while (qn < 32 && i0 < d.count) {
+        const int i = i0 + (int)lane;
+        uint32_t clo = 0, chi = 0;
+        const bool valid = i < d.count && gen_candidate(S, d, i, clo, chi);
+        const uint32_t clb = valid ? lower_bound(S, clo, chi) : kInf;
+        const bool keep = valid && clb < S.st.best.err && not_best(clo, chi);
+        const unsigned m = __ballot_sync(FULL_MASK, keep);
+        if (keep) S.pq[qn + __popc(m & ((1u << lane) - 1u))] = make_uint2(clo | (chi << 16), clb);
+        qn += __popc(m);
+        i0 += 32;
+      }
+      __syncwarp();
+      if (!qn) break;
+      take = min(qn, 32);
+      if ((int)lane < take) {
+        const uint2 v = S.pq[lane];
+        lo = v.x & 0xFFFFu; hi = v.x >> 16; lb = v.y;
+      }
+      live = (int)lane < take && lb < B0;
+    } else {
+      if (i0 >= d.count) break;
+      const int i = i0 + (int)lane;
+      const bool valid = i < d.count && gen_candidate(S, d, i, lo, hi);
+      lb = valid ? lower_bound(S, lo, hi) : kInf;
+      live = valid && lb < B0 && not_best(lo, hi);
+    }
+    if (!__any_sync(FULL_MASK, live)) {  // the whole batch is pruned: nothing to evaluate
+      if (compact) {
+        const int rest = qn - take;
+        const uint2 v = (int)lane < rest ? S.pq[take + lane] : make_uint2(0u, 0u);
+        __syncwarp();
+        if ((int)lane < rest) S.pq[lane] = v;
+        __syncwarp();
+        qn = rest;
+      } else {
+        i0 += 32;
+      }
       continue;
     }
-    // No tried-solution set (m_solutions_tried, crn_dxt1.cpp:1323-1330): a candidate evaluated
-    // before had an error at or above the best of that time, and the best only falls, so evaluating
-    // it again cannot accept it. The current best itself (once there is one; same palette
-    // rounding, endpoints not bumped apart by the equal-endpoint rule) is skipped, as its error
-    // would only reach the best at its last colour.
-    if (!d.alt && B0 != kInf && !S.st.best.alt && !S.st.best.enforce)
-      live = live && (lo | (hi << 16)) != (S.st.best.lo | (S.st.best.hi << 16));
     // evaluate every lane's candidate (uber: 4- and 3-colour; hc: 4-colour; fast: the selector
     // by projection, then its distance), stopping early once no live lane can still beat the
     // running best. Blocks with transparent texels evaluate 3-colour blocks only.
@@ -789,7 +833,14 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
       ok = __ballot_sync(FULL_MASK, live && lb < B && err < B) & after;
     }
     __syncwarp();
-    if (d.dependent && last >= 0) {
+    if (compact) {
+      const int rest = qn - take;
+      const uint2 v = (int)lane < rest ? S.pq[take + lane] : make_uint2(0u, 0u);
+      __syncwarp();
+      if ((int)lane < rest) S.pq[lane] = v;
+      __syncwarp();
+      qn = rest;
+    } else if (last >= 0) {
       if (d.stop_on_accept) return i0 + last;
       i0 += last + 1;
     } else {
