@@ -1003,9 +1003,6 @@ __device__ __noinline__ void comp_errors(WarpShared& S, int comp) {
   __syncwarp();
 }
 
-__device__ __forceinline__ uint32_t comp_E(const ListDesc& d, int s, uint32_t p) {
-  return d.W[s] * p * p - d.WP2[s] * p + d.WPP[s];
-}
 
 // optimize_endpoint_comps :415-486
 template <bool G>
@@ -1025,28 +1022,44 @@ __device__ __noinline__ void optimize_comps(WarpShared& S, uint32_t& work) {
     comp_errors<G>(S, comp);
     const int limit = comp == 1 ? 64 : 32;
     auto ex = [&](int c) { return (uint32_t)(comp == 1 ? exp6(c) : exp5(c)); };
-    uint32_t best_err = comp_E(S.d, 0, ex(lo_u[comp])) + comp_E(S.d, 1, ex(hi_u[comp])) +
-                        comp_E(S.d, 2, (uint32_t)((p0s * 2 + p1s) / 3)) + comp_E(S.d, 3, (uint32_t)((p0s + p1s * 2) / 3));
-    if (S.d.rem[0] >= best_err) continue;
+    // the component's error tables in registers (uniform across the warp)
+    uint32_t W[4], WP2[4], WPP[4], rem[4];
+    auto load_tables = [&]() {
+      for (int k = 0; k < 4; k++) { W[k] = S.d.W[k]; WP2[k] = S.d.WP2[k]; WPP[k] = S.d.WPP[k]; rem[k] = S.d.rem[k]; }
+    };
+    auto E = [&](int k, uint32_t p) { return W[k] * p * p - WP2[k] * p + WPP[k]; };
+    load_tables();
+    uint32_t best_err = E(0, ex(lo_u[comp])) + E(1, ex(hi_u[comp])) + E(2, (uint32_t)((p0s * 2 + p1s) / 3)) +
+                        E(3, (uint32_t)((p0s + p1s * 2) / 3));
+    if (rem[0] >= best_err) continue;
     #pragma unroll 1
     for (int c0 = 0; c0 < limit; c0++) {
-      uint32_t e0 = comp_E(S.d, 0, ex(c0));
-      if (e0 + S.d.rem[1] >= best_err) continue;
+      const uint32_t p0 = ex(c0);
+      uint32_t e0 = E(0, p0);
+      if (e0 + rem[1] >= best_err) continue;
+      {
+        // does any c1 pass the component-table prune for this c0 (:456-466)? lane c1 and c1 + 32;
+        // a pair passes exactly when its component error is below the best's
+        bool pass = false;
+        for (int c1 = (int)lane; c1 < limit; c1 += 32) {
+          const uint32_t p1 = ex(c1);
+          uint32_t e = e0 + E(1, p1);
+          if (e + rem[2] >= best_err) continue;
+          e += E(2, (p0 * 2 + p1) / 3);
+          if (e + rem[3] >= best_err) continue;
+          e += E(3, (p0 + p1 * 2) / 3);
+          pass |= e < best_err;
+        }
+        if (!__any_sync(FULL_MASK, pass)) continue;
+      }
       lo_u[comp] = c0;
       if (lane == 0) {
         S.d.kind = LK_COMPS; S.d.count = limit; S.d.dependent = 1; S.d.alt = 0; S.d.stop_on_accept = 1;
-        S.d.comp = comp; S.d.p0 = (int)ex(c0); S.d.e0 = e0; S.d.best_err = best_err;
+        S.d.comp = comp; S.d.p0 = (int)p0; S.d.e0 = e0; S.d.best_err = best_err;
         S.d.packed_lo = pack565(lo_u[0], lo_u[1], lo_u[2]);
         S.d.base[0] = hi_u[0]; S.d.base[1] = hi_u[1]; S.d.base[2] = hi_u[2];
       }
       __syncwarp();
-      {
-        // cheap pre-check: does any c1 pass the component-table prune for this c0?
-        uint32_t tlo, thi;
-        const bool p0ok = (int)lane < limit && gen_candidate(S, S.d, lane, tlo, thi);
-        const bool p1ok = (int)lane + 32 < limit && gen_candidate(S, S.d, lane + 32, tlo, thi);
-        if (!__any_sync(FULL_MASK, p0ok || p1ok)) continue;
-      }
       int start = 0;
       while (start < limit) {
         const int c1 = run_list<G>(S, start, work);
@@ -1054,13 +1067,13 @@ __device__ __noinline__ void optimize_comps(WarpShared& S, uint32_t& work) {
         if (!S.st.best.err) return;
         compute_selectors(S);
         comp_errors<G>(S, comp);
-        const uint32_t p0 = (uint32_t)S.d.p0, p1 = ex(c1);
-        best_err = comp_E(S.d, 0, ex(c0)) + comp_E(S.d, 1, p1) + comp_E(S.d, 2, (p0 * 2 + p1) / 3) +
-                   comp_E(S.d, 3, (p0 + p1 * 2) / 3);
-        e0 = comp_E(S.d, 0, ex(c0));
+        load_tables();
+        const uint32_t p1 = ex(c1);
+        best_err = E(0, p0) + E(1, p1) + E(2, (p0 * 2 + p1) / 3) + E(3, (p0 + p1 * 2) / 3);
+        e0 = E(0, p0);
         if (lane == 0) { S.d.e0 = e0; S.d.best_err = best_err; }
         __syncwarp();
-        if (e0 + S.d.rem[1] >= best_err) break;
+        if (e0 + rem[1] >= best_err) break;
         start = c1 + 1;
       }
     }
