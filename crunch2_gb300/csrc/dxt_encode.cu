@@ -786,7 +786,7 @@ __device__ __noinline__ int run_list(WarpShared& S, int start, uint32_t& work) {
             const float m01 = fminf(dist_part(x, q0), dist_part(x, q1));
             e0 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, fminf(dist_part(x, q2), dist_part(x, q3)))));
             if (three) e1 += w * f2u_exact(__fadd_rn(x.w, fminf(m01, dist_part(x, q4))));
-            if ((k & 3) == 3 &&
+            if ((k & 1) == 1 &&
                 __all_sync(FULL_MASK, !live || (only3 ? e1 : (three ? min(e0, e1) : e0)) >= B0)) { k++; break; }
           }
         } else {
