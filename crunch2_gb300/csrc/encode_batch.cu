@@ -47,7 +47,7 @@ int format_bpb(uint32_t fmt) {
 }
 
 constexpr uint32_t kAlphaChunkBlocks = 8;
-constexpr int kColourVariants = 4;  // colour grid: (v + 1) CTAs per SM, capped at the occupancy
+constexpr int kColourVariants = 4;  // colour grid: 2 (v + 1) CTAs per SM, capped at the occupancy
 constexpr int kAlphaVariants = 4;   // alpha grid: 2 << v CTAs per SM, capped at the occupancy
 
 struct EncodeBatch {
@@ -124,7 +124,7 @@ int autotune(EncodeBatch* b, cudaStream_t s) {
   }
   float best = 3.4e38f;
   for (int v = 0; v < kColourVariants && rc == CRNGPU_OK && b->ncolour; v++) {
-    const int grid = std::min(b->colour_max, b->sms * (v + 1));
+    const int grid = std::min(b->colour_max, b->sms * 2 * (v + 1));  // 2, 4, 6, 8 CTAs per SM
     rc = time_it(true, grid, b->colour_ms[v]);
     if (rc == CRNGPU_OK && b->colour_ms[v] < best) { best = b->colour_ms[v]; b->colour_grid = grid; }
   }
