@@ -167,6 +167,8 @@ def lib():
     L.crngpu_wait_counters.restype = i32
     L.crngpu_force_wait_timeouts.argtypes = [i32]
     L.crngpu_force_wait_timeouts.restype = i32
+    L.crngpu_set_decode_split.argtypes = [u32]
+    L.crngpu_set_decode_split.restype = i32
     _lib = L
     return L
 
@@ -199,6 +201,17 @@ def wait_counters(reset: bool = False) -> dict:
 def force_wait_timeouts(on: bool) -> None:
     """Test hook: every first bounded wait gives up at once (on) or the normal bounds apply (off)."""
     _check(lib().crngpu_force_wait_timeouts(int(on)), "crngpu_force_wait_timeouts")
+
+
+DECODE_SPLIT_DEFAULT, DECODE_LANE_ONLY, DECODE_WIDE_ONLY = 0, 0xFFFFFFFF, 1
+
+
+def set_decode_split(min_blocks: int) -> None:
+    """Which levels run on the wide (CTA-per-level) decoder and which on the lane decoder
+    (crngpu_set_decode_split): DECODE_SPLIT_DEFAULT lets each plan pick the split with the shortest
+    decode; a block count sends levels at least that large to the wide decoder; DECODE_LANE_ONLY /
+    DECODE_WIDE_ONLY force one decoder for every level. Both give the same bytes."""
+    _check(lib().crngpu_set_decode_split(int(min_blocks) & 0xFFFFFFFF), "crngpu_set_decode_split")
 
 
 def _check(rc: int, where: str) -> int:

@@ -348,6 +348,699 @@ __global__ void __launch_bounds__(kDecodeWarps * 32) k_crn_decode_textures(const
   if (err) atomicMax(status, err);
 }
 
+// ------------------------------------------------------------------------------------------
+// Large levels: k_crn_decode_wide, one CTA per level stream.
+//
+// The lane decoder above spends about 430 cycles per block on one lane, because every symbol is
+// a chain of dependent steps (bit-window refill, table lookup, shift) and a 1024 x 1024 level has
+// 65,536 blocks in one chain. This decoder keeps only the part of that chain that is truly serial
+// -- where the next chunk or block starts in the bit stream -- and makes each of its steps one
+// shared-memory load:
+//
+//  * Step tables, per bit position. For every bit position p of a window of the stream, worker
+//    warps decode, in parallel and without knowing whether a code starts at p, the code of every
+//    model the format reads at p, and compose the lengths into three "where does the next item
+//    start" tables: next0[p] (a block with no endpoint deltas: its selector code(s)), next1[p] (a
+//    block with endpoint deltas: delta code(s) then selector code(s)), nextC[p] (a 2x2 chunk pair
+//    of an even row: the reference-group code, then its two blocks, each as next0 or next1 as the
+//    group says), and the reference group g[p] decoded at p.
+//  * The chain. Lane 0 of warp 0 walks the level: on an even row it visits chunk starts
+//    (p = nextC[p], keeping g[p] for the row below), on an odd row block starts (p = next0[p] or
+//    next1[p] as the reference stored by the row above says). It records each item's bit position.
+//  * Emission. With the positions known, worker threads decode the symbols of each recorded item
+//    in parallel (one item per thread), then resolve the running endpoint indices of each row with
+//    a scan: a block with endpoint deltas adds them (mod the palette size), a "left" reference
+//    keeps the running index, an "up" reference sets it from the row above. The scan's operator
+//    (set-or-add-mod-n) is associative as long as every delta is below the palette size, which
+//    holds for every stream the reference writes (its delta models have one symbol per palette
+//    entry); a row holding a larger delta is resolved sequentially with the reference's own rule.
+//
+// Windows are kWS bits apart and kWX = kWS + kWM bits long. The chain steps in pairs and tests
+// the position of the last item it recorded once per pair, so that its loop branch never waits on
+// a load in flight: its last items in a window may start up to 2 x 144 bits (two chunk pairs) past
+// kWS, and a table entry reads at most 128 bits past its own position; the overlap kWM covers both. The CTA runs in
+// phases: in phase t the chain
+// walks window t - 1 while the workers build window t and emit the items the chain recorded in
+// phase t - 1; two table buffers and two item lists alternate. The result is bit-identical to
+// unpack_dxt1/dxt5/dxn/dxt5a (inc/crn_decomp.h:3944-4223), including the status the lane decoder
+// reports for corrupt streams.
+constexpr uint32_t kWS = 2048;                 // window stride (bits)
+constexpr uint32_t kWM = 448;                  // window overlap (bits): 2 x 144 of chain overshoot + 128 of table reach
+constexpr uint32_t kWX = kWS + kWM;            // positions per window
+constexpr uint32_t kWWords = kWX / 32 + 4;     // staged stream words per window
+constexpr uint32_t kWWorkers = 256;            // builder / emitter threads (warps 1 .. 8)
+constexpr uint32_t kWThreads = kWWorkers + 32; // + the chain warp (warp 0)
+constexpr uint32_t kWPer = (kWX + kWWorkers - 1) / kWWorkers;  // window positions per worker
+constexpr uint32_t kWMaxW = 1024;              // widest row, in blocks (4096 texels)
+constexpr uint32_t kWList = kWS + 4;           // chain items per phase, at most (positions increase; two past kWS)
+constexpr uint32_t kWBlk = kWS + 448;          // emitted blocks per phase, at most (each costs >= 1 bit)
+constexpr uint32_t kWNotDone = 0xFFFFFFFFu;
+
+// Shared-memory layout of k_crn_decode_wide (bytes), for a format reading `nm` models.
+struct WideLayout {
+  uint32_t lut, nx, gt, words, list, rb, grow, un, total;
+};
+__host__ __device__ constexpr uint32_t wide_align16(uint32_t v) { return (v + 15u) & ~15u; }
+__host__ __device__ inline WideLayout wide_layout(uint32_t nm) {
+  WideLayout L{};
+  uint32_t o = 0;
+  L.lut = o;   o += nm * (4u << kLutBits);       // first-level tables of the models read
+  L.nx = o;    o += 3u * 2u * kWX * 2u;          // next0, next1, nextC (u16) for two windows
+  L.gt = o;    o = wide_align16(o + 2u * kWX);   // reference group at each position, two windows
+  L.words = o; o += 4u * kWWords * 4u;           // staged stream words, four windows
+  L.list = o;  o += 2u * kWList * 4u;            // chain items (bit position | reference << 30), two phases
+  L.rb = o;    o += 2u * kWMaxW * 2u;            // endpoint index A and B of the row above
+  L.grow = o;  o = wide_align16(o + kWMaxW / 2); // the chain's reference groups of the current even row
+  L.un = o;                                      // union: build temporaries / emitted blocks
+  o += 7u * kWX > 2u * kWBlk * 4u ? 7u * kWX : 2u * kWBlk * 4u;
+  L.total = wide_align16(o);
+  return L;
+}
+
+// Word m of a level stream (its bytes 4m .. 4m + 3, MSB first); bytes at or past `end` read as
+// zero. `src` may have any alignment: the word is assembled from the aligned words around it, and
+// an aligned word is only read when it holds a byte of the stream. Split in a load and a finish so
+// that a caller can keep the loads in flight while it does other work.
+struct RawWord {
+  uint32_t lo, hi;
+};
+__device__ __forceinline__ RawWord stream_word_load(const uint8_t* src, uint32_t end, uint32_t m) {
+  const uint32_t at = 4u * m;
+  RawWord w{0u, 0u};
+  if (at >= end) return w;
+  const uint32_t r = (uint32_t)((uintptr_t)src & 3u);
+  const uint32_t* A = reinterpret_cast<const uint32_t*>(src - r + at);
+  w.lo = __ldg(A);
+  if (r && at + 4u - r < end) w.hi = __ldg(A + 1);
+  return w;
+}
+__device__ __forceinline__ uint32_t stream_word_finish(const uint8_t* src, uint32_t end, uint32_t m, RawWord raw) {
+  const uint32_t at = 4u * m;
+  if (at >= end) return 0u;
+  const uint32_t r = (uint32_t)((uintptr_t)src & 3u);
+  uint32_t w = __byte_perm(raw.lo, raw.hi, (r + 3u) | ((r + 2u) << 4) | ((r + 1u) << 8) | (r << 12));
+  if (at + 4u > end) w &= 0xFFFFFFFFu << (8u * (4u - (end - at)));
+  return w;
+}
+__device__ __forceinline__ uint32_t stream_word(const uint8_t* src, uint32_t end, uint32_t m) {
+  return stream_word_finish(src, end, m, stream_word_load(src, end, m));
+}
+
+// The 32 stream bits starting at window position j (the window's staged words `w`).
+__device__ __forceinline__ uint32_t window_bits(const uint32_t* w, uint32_t j) {
+  return __funnelshift_l(w[(j >> 5) + 1], w[j >> 5], j & 31u);
+}
+
+// Canonical prefix decode with the first-level table `lut` and, for codes longer than kLutBits,
+// the model's per-length bounds staged in shared memory: aux[0..4] = limit[12..16], aux[5..9] =
+// base[12..16], aux[10] = number of symbols. Codes longer than kLutBits need no loop: the length is
+// 12 plus the number of bounds at or below the bits (the bounds do not decrease with the length).
+constexpr uint32_t kAuxWords = 12;
+__device__ __forceinline__ uint32_t long_code_len(uint32_t v16, const uint32_t* aux) {
+  uint32_t l = kLutBits + 1;
+#pragma unroll
+  for (int k = 0; k < kMaxCodeLen - kLutBits; k++) l += v16 >= aux[k] ? 1u : 0u;
+  return l;  // kMaxCodeLen + 1: no such code
+}
+
+// Length of the code at the top of `v16` (16 bits, MSB first); an invalid code is kMaxCodeLen long,
+// as in decode_sym.
+__device__ __forceinline__ uint32_t code_len(uint32_t v16, const uint32_t* __restrict__ lut, const uint32_t* aux) {
+  const uint32_t e = lut[v16 >> (16 - kLutBits)];
+  const uint32_t l = min(long_code_len(v16, aux), (uint32_t)kMaxCodeLen);
+  return e != kLutLong ? e >> 16 : l;
+}
+
+// Symbol of the code at the top of `v16` and its length in `len`. Same rules as decode_sym: an
+// invalid code (or a code past the model's symbols) sets `bad`, yields symbol 0 and, when no code
+// of any length matches, is kMaxCodeLen long. `st` holds the model's sorted symbols
+// [st_base, st_base + kStaged) in shared memory; others are read from the device model.
+constexpr uint32_t kStaged = 512;
+__device__ __forceinline__ uint32_t code_sym(uint32_t v16, const uint32_t* __restrict__ lut, const uint32_t* aux,
+                                             const DevModel* __restrict__ m, const uint16_t* st, uint32_t& len,
+                                             uint32_t& bad) {
+  const uint32_t e = lut[v16 >> (16 - kLutBits)];
+  if (e != kLutLong) {
+    len = e >> 16;
+    return e & 0xFFFFu;
+  }
+  const uint32_t l = long_code_len(v16, aux);
+  if (l > (uint32_t)kMaxCodeLen) {
+    bad |= 1u;
+    len = kMaxCodeLen;
+    return 0u;
+  }
+  len = l;
+  const int idx = (int)aux[5 + l - (kLutBits + 1)] + (int)(v16 >> (16 - l));
+  if (idx < 0 || (uint32_t)idx >= aux[10]) {
+    bad |= 1u;
+    return 0u;
+  }
+  const uint32_t k = (uint32_t)idx - aux[11];
+  return k < kStaged ? (uint32_t)st[k] : (uint32_t)__ldg(&m->sorted[idx]);
+}
+
+__device__ __forceinline__ void worker_sync() { asm volatile("bar.sync 1, %0;" ::"r"(kWWorkers) : "memory"); }
+__device__ __forceinline__ bool worker_sync_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(kWWorkers)
+      : "memory");
+  return r != 0u;
+}
+
+__device__ __forceinline__ uint32_t add_mod(uint32_t x, uint32_t y, uint32_t n) { return x + y >= n ? x + y - n : x + y; }
+
+// Scan operator of the endpoint-index resolution: x -> set ? a : (x + a) mod n (b likewise).
+struct IdxOp {
+  uint32_t set, a, b;
+};
+template <bool TWO>
+__device__ __forceinline__ IdxOp idx_compose(const IdxOp& f, const IdxOp& g, uint32_t nA, uint32_t nB) {
+  if (g.set) return g;
+  return IdxOp{f.set, add_mod(f.a, g.a, nA), TWO ? add_mod(f.b, g.b, nB) : 0u};
+}
+
+// The decoder's dynamic shared memory, named at file scope so that every pointer into it is known
+// to be shared (loads and stores stay shared-window accesses after inlining).
+extern __shared__ __align__(16) uint8_t wide_smem[];
+
+// Small shared state of k_crn_decode_wide (one instance per CTA).
+struct WideShared {
+  uint32_t meta[2][3];  // per item list: count, first row, first item in that row
+  uint32_t done, carry[2], bad;
+  uint32_t scan[kWWorkers / 32][3];
+  uint32_t aux[5][kAuxWords];       // long-code bounds of the models read (slot order of the tables)
+  uint16_t sorted[5][kStaged];      // sorted symbols: the reference model's first, the others' longest
+};
+
+template <int KIND>
+__device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, uint32_t* status) {
+  constexpr bool colour = KIND == kKDxt1 || KIND == kKDxt5;
+  constexpr bool two = KIND == kKDxt5 || KIND == kKDxn;
+  constexpr bool five = KIND == kKDxt5;
+  constexpr uint32_t nm = five ? 5u : 3u;
+  uint8_t* sm = wide_smem;
+  const WideLayout Ly = wide_layout(nm);
+
+  const uint32_t tid = threadIdx.x;
+  uint32_t* luts = reinterpret_cast<uint32_t*>(sm + Ly.lut);
+  const uint32_t* lR = luts;
+  const uint32_t* lDA = luts + (1u << kLutBits);
+  const uint32_t* lSA = luts + (2u << kLutBits);
+  const uint32_t* lDB = five ? luts + (3u << kLutBits) : lDA;
+  const uint32_t* lSB = five ? luts + (4u << kLutBits) : lSA;
+  // model slots of the second endpoint / selector code (the same models as the first for DXN)
+  constexpr uint32_t sDB = five ? 3u : 1u, sSB = five ? 4u : 2u;
+  const DevModel* mR = J.models + kMRef;
+  const DevModel* mDA = J.models + (colour ? kMEp0 : kMEp1);
+  const DevModel* mSA = J.models + (colour ? kMSel0 : kMSel1);
+  const DevModel* mDB = J.models + kMEp1;
+  const DevModel* mSB = J.models + kMSel1;
+  uint16_t* nx0 = reinterpret_cast<uint16_t*>(sm + Ly.nx);
+  uint16_t* nx1 = nx0 + 2 * kWX;
+  uint16_t* nxC = nx1 + 2 * kWX;
+  uint8_t* gt = sm + Ly.gt;
+  uint32_t* words = reinterpret_cast<uint32_t*>(sm + Ly.words);
+  uint32_t* list = reinterpret_cast<uint32_t*>(sm + Ly.list);
+  uint16_t* rbA = reinterpret_cast<uint16_t*>(sm + Ly.rb);
+  uint16_t* rbB = rbA + kWMaxW;
+  uint8_t* grow = sm + Ly.grow;
+  uint8_t* un = sm + Ly.un;
+  uint8_t* lenR = un;            // build temporaries
+  uint8_t* lenDA = un + kWX;
+  uint8_t* lenSA = un + 2 * kWX;
+  uint8_t* lenDB = un + 3 * kWX;
+  uint8_t* lenSB = un + 4 * kWX;
+  uint8_t* lenSBk = un + 5 * kWX;  // selector codes of one block (two-endpoint formats)
+  uint8_t* lenEBk = un + 6 * kWX;  // endpoint codes of one block (two-endpoint formats)
+  uint32_t* bw0 = reinterpret_cast<uint32_t*>(un);  // emitted blocks: reference | delta A << 2 | selector A << 16
+  uint32_t* bw1 = bw0 + kWBlk;                      // delta B | selector B << 16
+
+  const uint32_t W = (J.bx + 1) & ~1u, H = (J.by + 1) & ~1u, W2 = W >> 1;
+  const uint32_t rows = J.faces * H;
+  const uint32_t nA = J.n_a, nB = J.n_b, nSA = J.n_sa, nSB = J.n_sb;
+
+  {  // stage the first-level tables, long-code bounds and sorted symbols; clear the running state
+    const int srcm[5] = {kMRef, colour ? kMEp0 : kMEp1, colour ? kMSel0 : kMSel1, kMEp1, kMSel1};
+    for (uint32_t t = 0; t < nm; t++) {
+      const uint4* src = reinterpret_cast<const uint4*>(J.models[srcm[t]].lut);
+      uint4* dst = reinterpret_cast<uint4*>(luts + (t << kLutBits));
+      for (uint32_t k = tid; k < (1u << kLutBits) / 4; k += blockDim.x) dst[k] = __ldg(src + k);
+    }
+    for (uint32_t x = tid; x < W; x += blockDim.x) rbA[x] = rbB[x] = 0;
+    if (tid < nm * kAuxWords) {
+      const uint32_t t = tid / kAuxWords, k = tid - t * kAuxWords;
+      const DevModel* md = J.models + srcm[t];
+      // aux[11]: sorted index of the first long code (offset of length 12 = base + first code)
+      S.aux[t][k] = k < 5 ? __ldg(&md->limit[kLutBits + 1 + k])
+                  : k < 10 ? (uint32_t)__ldg(&md->base[kLutBits + 1 + k - 5])
+                  : k == 10 ? __ldg(&md->num_syms)
+                  : t == 0 ? 0u
+                  : (uint32_t)(__ldg(&md->base[kLutBits + 1]) + (int)(__ldg(&md->limit[kLutBits]) >> (16 - kLutBits - 1)));
+    }
+    if (tid == 0) {
+      S.done = kWNotDone;
+      S.carry[0] = S.carry[1] = 0;
+      S.bad = 0;
+    }
+    // the stream words of window 0 (later windows are loaded one phase ahead)
+    for (uint32_t m = tid; m < kWWords; m += blockDim.x) words[m] = stream_word(J.src, J.src_size, m);
+  }
+  __syncthreads();
+  {
+    const int srcm[5] = {kMRef, colour ? kMEp0 : kMEp1, colour ? kMSel0 : kMSel1, kMEp1, kMSel1};
+    for (uint32_t i = tid; i < nm * kStaged; i += blockDim.x) {
+      const uint32_t t = i / kStaged, k = i - t * kStaged;
+      const uint32_t idx = S.aux[t][11] + k;
+      S.sorted[t][k] = idx < kMaxSyms ? __ldg(&J.models[srcm[t]].sorted[idx]) : (uint16_t)0;
+    }
+  }
+  __syncthreads();
+
+  uint32_t c_r = 0, c_e = 0, c_j = 0;  // the chain's row, item within the row, window position
+  uint32_t done_at = kWNotDone;
+  const bool worker = tid >= 32;
+  const uint32_t wt = tid - 32;
+  for (uint32_t t = 0;; t++) {
+    if (tid == 0 && t >= 1 && done_at == kWNotDone) {
+      // ---- the chain walks window t - 1 and records its items in list (t - 1) & 1
+      const uint32_t wb = (t - 1) & 1u;
+      const uint16_t* n0 = nx0 + wb * kWX;
+      const uint16_t* n1 = nx1 + wb * kWX;
+      const uint16_t* nC = nxC + wb * kWX;
+      const uint8_t* g = gt + wb * kWX;
+      uint32_t* L = list + wb * kWList;
+      const uint32_t a = (t - 1) * kWS;
+      S.meta[wb][1] = c_r;
+      S.meta[wb][2] = c_e;
+      // jp: position of the last item recorded, the loop test. Steps go in pairs with one test per
+      // pair, so a loop branch never waits on a table load in flight; the only dependency of a step
+      // is the table load at j. Odd-row group bytes are loaded a pair ahead.
+      uint32_t n = 0, j = c_j, jp = 0, r = c_r, e = c_e;
+      while (r < rows && jp < kWS) {
+        if (!(r & 1u)) {
+          while (e + 2 <= W2 && jp < kWS) {
+            const uint32_t j1 = nC[j];
+            const uint32_t g0 = g[j];
+            L[n] = a + j;
+            const uint32_t j2 = nC[j1];
+            const uint32_t g1 = g[j1];
+            L[n + 1] = a + j1;
+            grow[e] = (uint8_t)g0;
+            grow[e + 1] = (uint8_t)g1;
+            n += 2;
+            jp = j1;
+            j = j2;
+            e += 2;
+          }
+          if (e < W2 && jp < kWS) {
+            const uint32_t jn = nC[j];
+            grow[e] = g[j];
+            L[n++] = a + j;
+            jp = j;
+            j = jn;
+            e++;
+          }
+        } else if (e < W) {
+          uint32_t ref0 = (grow[e >> 1] >> ((e & 1u) ? 6 : 2)) & 3u;
+          while (e + 2 <= W && jp < kWS) {
+            const uint32_t e1 = e + 1, e2 = min(e + 2, W - 1);
+            const uint32_t gb1 = grow[e1 >> 1], gb2 = grow[e2 >> 1];
+            L[n] = (a + j) | (ref0 << 30);
+            const uint32_t j1 = (ref0 ? n0 : n1)[j];
+            const uint32_t ref1 = (gb1 >> ((e1 & 1u) ? 6 : 2)) & 3u;
+            L[n + 1] = (a + j1) | (ref1 << 30);
+            const uint32_t j2 = (ref1 ? n0 : n1)[j1];
+            ref0 = (gb2 >> ((e2 & 1u) ? 6 : 2)) & 3u;
+            n += 2;
+            jp = j1;
+            j = j2;
+            e += 2;
+          }
+          if (e < W && jp < kWS) {
+            L[n++] = (a + j) | (ref0 << 30);
+            jp = j;
+            j = (ref0 ? n0 : n1)[j];
+            e++;
+          }
+        }
+        if (e == ((r & 1u) ? W : W2)) {
+          e = 0;
+          r++;
+        }
+      }
+      S.meta[wb][0] = n;
+      c_r = r;
+      c_e = e;
+      c_j = j - kWS;
+      if (r >= rows) S.done = t;
+    } else if (worker) {
+      // the stream words of window t + 1, stored once this phase's emission is done
+      const uint32_t pre_m = (((t + 1) * kWS) >> 5) + wt;
+      const RawWord pre = (done_at == kWNotDone && wt < kWWords) ? stream_word_load(J.src, J.src_size, pre_m)
+                                                                  : RawWord{0u, 0u};
+      if (done_at == kWNotDone) {
+        // ---- build window t into table buffer t & 1 (its words were staged one phase ahead).
+        // Each stage issues all its loads for the thread's kWPer positions before it computes and
+        // stores, so the loads of one position never wait behind the stores of another.
+        const uint32_t wb = t & 1u;
+        const uint32_t* wd = words + (t & 3u) * kWWords;
+        uint8_t* g = gt + wb * kWX;
+        {
+          uint32_t v[kWPer], eR[kWPer], eD[kWPer], eS[kWPer], eD2[kWPer], eS2[kWPer];
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) v[q] = window_bits(wd, min(wt + q * kWWorkers, kWX - 1)) >> 16;
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) {
+            const uint32_t i = v[q] >> (16 - kLutBits);
+            eR[q] = lR[i];
+            eD[q] = lDA[i];
+            eS[q] = lSA[i];
+            if (five) {
+              eD2[q] = lDB[i];
+              eS2[q] = lSB[i];
+            }
+          }
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) {
+            const uint32_t j = wt + q * kWWorkers;
+            if (j < kWX) {
+              uint32_t sym = eR[q] & 0xFFFFu, len = eR[q] >> 16, junk = 0;
+              if (eR[q] == kLutLong) sym = code_sym(v[q], lR, S.aux[0], mR, S.sorted[0], len, junk);
+              g[j] = (uint8_t)sym;
+              lenR[j] = (uint8_t)len;
+              const uint32_t ll1 = min(long_code_len(v[q], S.aux[1]), (uint32_t)kMaxCodeLen);
+              const uint32_t ll2 = min(long_code_len(v[q], S.aux[2]), (uint32_t)kMaxCodeLen);
+              lenDA[j] = (uint8_t)(eD[q] != kLutLong ? eD[q] >> 16 : ll1);
+              lenSA[j] = (uint8_t)(eS[q] != kLutLong ? eS[q] >> 16 : ll2);
+              if (five) {
+                const uint32_t ll3 = min(long_code_len(v[q], S.aux[3]), (uint32_t)kMaxCodeLen);
+                const uint32_t ll4 = min(long_code_len(v[q], S.aux[4]), (uint32_t)kMaxCodeLen);
+                lenDB[j] = (uint8_t)(eD2[q] != kLutLong ? eD2[q] >> 16 : ll3);
+                lenSB[j] = (uint8_t)(eS2[q] != kLutLong ? eS2[q] >> 16 : ll4);
+              }
+            }
+          }
+        }
+        worker_sync();
+        const uint8_t* sbl = lenSA;  // length of a block's selector code(s) at each position
+        const uint8_t* ebl = lenDA;  // length of a block's endpoint delta code(s)
+        if (two) {
+          const uint8_t* l2D = five ? lenDB : lenDA;
+          const uint8_t* l2S = five ? lenSB : lenSA;
+          uint32_t ls[kWPer], ld[kWPer], xs[kWPer], xd[kWPer];
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) {
+            const uint32_t j = min(wt + q * kWWorkers, kWX - 1);
+            ls[q] = lenSA[j];
+            ld[q] = lenDA[j];
+          }
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) {
+            const uint32_t j = min(wt + q * kWWorkers, kWX - 1);
+            xs[q] = l2S[min(j + ls[q], kWX - 1)];
+            xd[q] = l2D[min(j + ld[q], kWX - 1)];
+          }
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) {
+            const uint32_t j = wt + q * kWWorkers;
+            if (j < kWX) {
+              lenSBk[j] = (uint8_t)(ls[q] + xs[q]);
+              lenEBk[j] = (uint8_t)(ld[q] + xd[q]);
+            }
+          }
+          worker_sync();
+          sbl = lenSBk;
+          ebl = lenEBk;
+        }
+        uint16_t* b0 = nx0 + wb * kWX;
+        uint16_t* b1 = nx1 + wb * kWX;
+        {
+          uint32_t sb[kWPer], qq[kWPer], s2[kWPer];
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) {
+            const uint32_t j = min(wt + q * kWWorkers, kWX - 1);
+            sb[q] = sbl[j];
+            qq[q] = min(j + ebl[j], kWX - 1);
+          }
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) s2[q] = sbl[qq[q]];
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) {
+            const uint32_t j = wt + q * kWWorkers;
+            if (j < kWX) {
+              b0[j] = (uint16_t)min(j + sb[q], kWX - 1);
+              b1[j] = (uint16_t)min(qq[q] + s2[q], kWX - 1);
+            }
+          }
+        }
+        worker_sync();
+        {
+          uint16_t* bc = nxC + wb * kWX;
+          uint32_t gg[kWPer], q1[kWPer];
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) {
+            const uint32_t j = min(wt + q * kWWorkers, kWX - 1);
+            gg[q] = g[j];
+            q1[q] = min(j + lenR[j], kWX - 1);
+          }
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) q1[q] = (gg[q] & 3u) ? b0[q1[q]] : b1[q1[q]];
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) q1[q] = ((gg[q] >> 4) & 3u) ? b0[q1[q]] : b1[q1[q]];
+#pragma unroll
+          for (uint32_t q = 0; q < kWPer; q++) {
+            const uint32_t j = wt + q * kWWorkers;
+            if (j < kWX) bc[j] = (uint16_t)q1[q];
+          }
+        }
+        worker_sync();  // the temporaries are dead; the emission below reuses their space
+      }
+      if (t >= 2 && (done_at == kWNotDone || t - 2 < done_at)) {
+        // ---- emit list t - 2 (buffer t & 1), decoding from window t - 2's staged words
+        const uint32_t lb = t & 1u;
+        const uint32_t* L = list + lb * kWList;
+        const uint32_t* wd = words + ((t - 2) & 3u) * kWWords;
+        const uint32_t a2 = (t - 2) * kWS;
+        const uint32_t n = S.meta[lb][0], r0 = S.meta[lb][1], e0 = S.meta[lb][2];
+        // item i -> row, item within the row, first block of the list's block array
+        const uint32_t odd0 = r0 & 1u, be0 = odd0 ? 1u : 2u;
+        const uint32_t nfirst = (odd0 ? W : W2) - e0;
+        const uint32_t n1 = odd0 ? W2 : W, be1 = odd0 ? 2u : 1u;
+        auto locate = [&](uint32_t i, uint32_t& r, uint32_t& e, uint32_t& blk) {
+          if (i < nfirst) {
+            r = r0;
+            e = e0 + i;
+            blk = i * be0;
+            return;
+          }
+          const uint32_t ip = i - nfirst, pairs = ip / (W2 + W), rem = ip - pairs * (W2 + W);
+          const uint32_t base = nfirst * be0 + pairs * 2u * W;
+          if (rem < n1) {
+            r = r0 + 1 + 2 * pairs;
+            e = rem;
+            blk = base + rem * be1;
+          } else {
+            r = r0 + 2 + 2 * pairs;
+            e = rem - n1;
+            blk = base + W + (rem - n1) * be0;
+          }
+        };
+        uint32_t bad = 0;
+        for (uint32_t i = wt; i < n; i += kWWorkers) {
+          const uint32_t ent = L[i];
+          uint32_t j = (ent & 0x3FFFFFFFu) - a2;
+          uint32_t r, e, blk;
+          locate(i, r, e, blk);
+          auto dec = [&](const uint32_t* lut, uint32_t slot, const DevModel* m) {
+            uint32_t len;
+            const uint32_t s = code_sym(window_bits(wd, j) >> 16, lut, S.aux[slot], m, S.sorted[slot], len, bad);
+            j += len;
+            return s;
+          };
+          auto block = [&](uint32_t ref, uint32_t k) {
+            uint32_t dA = 0, dB = 0;
+            if (!ref) {
+              dA = dec(lDA, 1, mDA);
+              if (two) dB = dec(lDB, sDB, mDB);
+            }
+            const uint32_t sA = dec(lSA, 2, mSA);
+            const uint32_t sB = two ? dec(lSB, sSB, mSB) : 0u;
+            bw0[k] = ref | (dA << 2) | (sA << 16);
+            if (two) bw1[k] = dB | (sB << 16);
+          };
+          if (!(r & 1u)) {
+            const uint32_t g = dec(lR, 0, mR) & 0xFFu;
+            block(g & 3u, blk);
+            block((g >> 4) & 3u, blk + 1);
+          } else {
+            block(ent >> 30, blk);
+          }
+        }
+        if (bad) atomicOr(&S.bad, 1u);
+        uint32_t total = 0;
+        if (n) {
+          uint32_t r, e, blk;
+          locate(n - 1, r, e, blk);
+          total = blk + ((r & 1u) ? 1u : 2u);
+        }
+        worker_sync();
+        // resolve the endpoint indices row segment by row segment, in stream order
+        uint32_t r = r0, x = odd0 ? e0 : 2 * e0, b = 0;
+        uint32_t badi = 0;
+        while (b < total) {
+          const uint32_t cnt = min(W - x, total - b);
+          const uint32_t f = r / H, y = r - f * H;
+          const bool vis_row = y < J.by;
+          const uint32_t per = (cnt + kWWorkers - 1) / kWWorkers;  // <= 4 (rows of at most 1024 blocks)
+          const uint32_t k0 = min(cnt, wt * per), k1 = min(cnt, k0 + per);
+          IdxOp op[4];
+          IdxOp mine{0, 0, 0};
+          bool inexact = nA == 0 || (two && nB == 0);
+#pragma unroll
+          for (uint32_t q = 0; q < 4; q++) {
+            const uint32_t k = k0 + q;
+            if (k < k1) {
+              const uint32_t w0 = bw0[b + k], ref = w0 & 3u;
+              const uint32_t dA = (w0 >> 2) & 0x3FFFu, dB = two ? (bw1[b + k] & 0xFFFFu) : 0u;
+              if (ref == 0) {
+                op[q] = IdxOp{0, dA, dB};
+                inexact |= dA >= nA || (two && dB >= nB);
+              } else if (ref == 1) {
+                op[q] = IdxOp{0, 0, 0};
+              } else {
+                op[q] = IdxOp{1, rbA[x + k], two ? (uint32_t)rbB[x + k] : 0u};
+              }
+              mine = idx_compose<two>(mine, op[q], nA, nB);
+            }
+          }
+          const uint32_t cA = S.carry[0], cB = S.carry[1];
+          if (worker_sync_or(inexact)) {
+            // a delta at or above its palette size: the reference's sequential rule, on one thread
+            if (wt == 0) {
+              uint32_t iA = cA, iB = cB;
+              for (uint32_t k = 0; k < cnt; k++) {
+                const uint32_t w0 = bw0[b + k], ref = w0 & 3u;
+                if (ref == 0) {
+                  iA += (w0 >> 2) & 0x3FFFu;
+                  if (iA >= nA) iA -= nA;
+                  if (two) {
+                    iB += bw1[b + k] & 0xFFFFu;
+                    if (iB >= nB) iB -= nB;
+                  }
+                } else if (ref >= 2) {
+                  iA = rbA[x + k];
+                  iB = rbB[x + k];
+                }
+                // the row buffer holds 16-bit indices: larger ones are corrupt in any case
+                if (iA > 0xFFFFu || iB > 0xFFFFu) badi = 1;
+                iA &= 0xFFFFu;
+                iB &= 0xFFFFu;
+                rbA[x + k] = (uint16_t)iA;
+                rbB[x + k] = (uint16_t)iB;
+                const uint32_t sA = w0 >> 16, sB = two ? bw1[b + k] >> 16 : 0u;
+                if (iA >= nA || sA >= nSA || (two && (iB >= nB || sB >= nSB))) badi = 1;
+                if (vis_row && x + k < J.bx) {
+                  const uint64_t at = ((uint64_t)f * J.by + y) * J.bx + x + k;
+                  if (two) reinterpret_cast<uint64_t*>(J.rec)[at] = (uint64_t)(iA | (sA << 16)) | ((uint64_t)(iB | (sB << 16)) << 32);
+                  else reinterpret_cast<uint32_t*>(J.rec)[at] = iA | (sA << 16);
+                }
+              }
+              S.carry[0] = iA;
+              S.carry[1] = iB;
+            }
+          } else {
+            // block-wide exclusive scan of the per-thread compositions
+            const uint32_t lane = wt & 31u, wi = wt >> 5;
+            IdxOp inc = mine;
+#pragma unroll
+            for (uint32_t d = 1; d < 32; d <<= 1) {
+              IdxOp o;
+              o.set = __shfl_up_sync(0xFFFFFFFFu, inc.set, d);
+              o.a = __shfl_up_sync(0xFFFFFFFFu, inc.a, d);
+              o.b = __shfl_up_sync(0xFFFFFFFFu, inc.b, d);
+              if (lane >= d) inc = idx_compose<two>(o, inc, nA, nB);
+            }
+            if (lane == 31) {
+              S.scan[wi][0] = inc.set;
+              S.scan[wi][1] = inc.a;
+              S.scan[wi][2] = inc.b;
+            }
+            IdxOp ex;
+            ex.set = __shfl_up_sync(0xFFFFFFFFu, inc.set, 1);
+            ex.a = __shfl_up_sync(0xFFFFFFFFu, inc.a, 1);
+            ex.b = __shfl_up_sync(0xFFFFFFFFu, inc.b, 1);
+            if (lane == 0) ex = IdxOp{0, 0, 0};
+            worker_sync();
+            IdxOp tot[kWWorkers / 32];
+#pragma unroll
+            for (uint32_t w = 0; w < kWWorkers / 32; w++) tot[w] = IdxOp{S.scan[w][0], S.scan[w][1], S.scan[w][2]};
+            IdxOp pre_op{0, 0, 0};
+#pragma unroll
+            for (uint32_t w = 0; w < kWWorkers / 32; w++)
+              if (w < wi) pre_op = idx_compose<two>(pre_op, tot[w], nA, nB);
+            pre_op = idx_compose<two>(pre_op, ex, nA, nB);
+            uint32_t iA = pre_op.set ? pre_op.a : add_mod(cA, pre_op.a, nA);
+            uint32_t iB = two ? (pre_op.set ? pre_op.b : add_mod(cB, pre_op.b, nB)) : 0u;
+#pragma unroll
+            for (uint32_t q = 0; q < 4; q++) {
+              const uint32_t k = k0 + q;
+              if (k < k1) {
+                iA = op[q].set ? op[q].a : add_mod(iA, op[q].a, nA);
+                if (two) iB = op[q].set ? op[q].b : add_mod(iB, op[q].b, nB);
+                rbA[x + k] = (uint16_t)iA;
+                if (two) rbB[x + k] = (uint16_t)iB;
+                const uint32_t w0 = bw0[b + k];
+                const uint32_t sA = w0 >> 16, sB = two ? bw1[b + k] >> 16 : 0u;
+                if (iA >= nA || sA >= nSA || (two && (iB >= nB || sB >= nSB))) badi = 1;
+                if (vis_row && x + k < J.bx) {
+                  const uint64_t at = ((uint64_t)f * J.by + y) * J.bx + x + k;
+                  if (two) reinterpret_cast<uint64_t*>(J.rec)[at] = (uint64_t)(iA | (sA << 16)) | ((uint64_t)(iB | (sB << 16)) << 32);
+                  else reinterpret_cast<uint32_t*>(J.rec)[at] = iA | (sA << 16);
+                }
+                if (k + 1 == cnt) {
+                  S.carry[0] = iA;
+                  S.carry[1] = iB;
+                }
+              }
+            }
+          }
+          worker_sync();  // row buffer and carry are complete before the next segment reads them
+          b += cnt;
+          x += cnt;
+          if (x == W) {
+            x = 0;
+            r++;
+          }
+        }
+        if (badi) atomicOr(&S.bad, 2u);
+      }
+      if (done_at == kWNotDone && wt < kWWords)
+        words[((t + 1) & 3u) * kWWords + wt] = stream_word_finish(J.src, J.src_size, pre_m, pre);
+    }
+    __syncthreads();
+    done_at = S.done;
+    if (done_at != kWNotDone && t >= done_at + 1) break;
+  }
+  if (tid == 0 && S.bad) atomicMax(status, (S.bad & 1u) ? (uint32_t)kStBadCode : (uint32_t)kStBadIndex);
+}
+
+// One CTA per large level stream (`jobs`, largest first).
+__global__ void __launch_bounds__(kWThreads) k_crn_decode_wide(const StreamJob* __restrict__ jobs,
+                                                               uint32_t* __restrict__ status) {
+  __shared__ WideShared S;
+  const StreamJob J = jobs[blockIdx.x];
+  switch (J.kind) {
+    case kKDxt1: wide_level<kKDxt1>(J, S, status); break;
+    case kKDxt5: wide_level<kKDxt5>(J, S, status); break;
+    case kKDxn: wide_level<kKDxn>(J, S, status); break;
+    default: wide_level<kKDxt5a>(J, S, status); break;
+  }
+}
+
 // Palette entry index, clamped so that records left unwritten by a stream the decoder rejected
 // as corrupt can never read outside the palette (valid records are already in range).
 __device__ __forceinline__ uint32_t clamp_idx(uint32_t i, uint32_t n) { return i < n ? i : 0u; }
@@ -785,6 +1478,9 @@ struct LevelTask {
 struct Plan {
   std::vector<uint8_t> image;
   uint32_t n_item = 0, n_stream = 0, n_expand = 0, ctas = 0;
+  uint32_t n_wide = 0;      // level streams for k_crn_decode_wide (one CTA each, largest first)
+  uint32_t wide_smem = 0;   // its dynamic shared memory (the largest format's layout)
+  size_t wide_ofs = 0;
   uint32_t rb_words = 2;    // largest row-buffer need of one texture job (words)
   uint32_t lut_words = 0;   // first-level tables staged per texture job (words)
   size_t stream_ofs = 0, expand_ofs = 0;
@@ -797,20 +1493,79 @@ uint64_t level_records(const CrnFile& F, uint32_t l) {
   return (uint64_t)F.level[l].blocks_x * F.level[l].blocks_y * F.faces;
 }
 
-// false if a texture job would not fit the decoder (more than 32 levels or rows too wide)
-bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
+// Which level streams go to k_crn_decode_wide. 0 (the default): the split that minimises the
+// plan's decode time (decide_wide); otherwise levels of at least this many blocks (all faces) go
+// to the wide decoder. Set by crngpu_set_decode_split (tests force either decoder on every level).
+std::atomic<uint32_t> g_wide_min_blocks{0};
+
+// Decode cost model, in microseconds per block for a one-endpoint format (twice that for DXT5 and
+// DXN), measured on GB300: the lane decoder's serial chain and one wide CTA's phase loop.
+constexpr double kLaneUsPerBlock = 0.20, kWideUsPerBlock = 0.05;
+constexpr uint32_t kWideMinBlocks = 256;  // smaller levels always go to the lane decoder
+
+uint64_t task_blocks(const LevelTask& t) {
+  const LevelInfo& li = t.file->level[t.level];
+  return (uint64_t)li.blocks_x * li.blocks_y * t.file->faces;
+}
+
+bool wide_eligible(const LevelTask& t) {
+  const LevelInfo& li = t.file->level[t.level];
+  // list items hold a bit position below 2^30, so the stream is below 2^27 bytes
+  return ((li.blocks_x + 1) & ~1u) <= kWMaxW && t.src_size < (1u << 27);
+}
+
+// Per task: true if it goes to the wide decoder. The lane decoder runs every stream side by side
+// and finishes with its longest stream; the wide decoder runs `wide_slots` CTAs at once and
+// finishes when its queue drains, but never before its largest level. The two run one after the
+// other on the caller's stream. With the levels sorted by cost, the first k go wide for the k that
+// minimises wide time + lane time of level k + 1.
+std::vector<bool> decide_wide(const std::vector<LevelTask>& tasks, uint32_t wide_slots) {
+  std::vector<bool> wide(tasks.size(), false);
+  const uint32_t fixed = g_wide_min_blocks.load(std::memory_order_relaxed);
+  if (fixed) {
+    for (size_t i = 0; i < tasks.size(); i++) wide[i] = wide_eligible(tasks[i]) && task_blocks(tasks[i]) >= fixed;
+    return wide;
+  }
+  std::vector<std::pair<double, size_t>> cost;  // lane cost, task
+  double lane_rest = 0;                         // longest lane stream among the ineligible ones
+  for (size_t i = 0; i < tasks.size(); i++) {
+    const double w = (tasks[i].file->kind == Kind::DXT5 || tasks[i].file->kind == Kind::DXN) ? 2.0 : 1.0;
+    const double c = (double)task_blocks(tasks[i]) * w;
+    if (wide_eligible(tasks[i]) && task_blocks(tasks[i]) >= kWideMinBlocks) cost.push_back({c, i});
+    else lane_rest = std::max(lane_rest, c * kLaneUsPerBlock);
+  }
+  std::stable_sort(cost.begin(), cost.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
+  double best = std::max(lane_rest, cost.empty() ? 0.0 : cost[0].first * kLaneUsPerBlock), sum = 0;
+  constexpr double kWideLaunchUs = 10.0;  // a second kernel launch and its fixed set-up
+  size_t best_k = 0;
+  for (size_t k = 1; k <= cost.size(); k++) {
+    sum += cost[k - 1].first * kWideUsPerBlock;
+    const double wide_t = std::max(cost[0].first * kWideUsPerBlock, sum / std::max<uint32_t>(1, wide_slots));
+    const double lane_t = std::max(lane_rest, k < cost.size() ? cost[k].first * kLaneUsPerBlock : 0.0);
+    if (wide_t + lane_t + kWideLaunchUs < best) {
+      best = wide_t + lane_t + kWideLaunchUs;
+      best_k = k;
+    }
+  }
+  for (size_t k = 0; k < best_k; k++) wide[cost[k].second] = true;
+  return wide;
+}
+
+// false if a texture job would not fit the decoder (more than 32 levels or rows too wide).
+// `wide_slots`: CTAs of k_crn_decode_wide resident at once on the device (wide_slots()).
+bool make_plan(const std::vector<LevelTask>& tasks, Plan& p, uint32_t wide_slots) {
   std::vector<TexJob> items;
   std::vector<std::vector<StreamJob>> item_streams;
+  std::vector<StreamJob> wide;
+  const std::vector<bool> to_wide = decide_wide(tasks, wide_slots);
   for (size_t i = 0; i < tasks.size();) {
     size_t k = i;
     while (k < tasks.size() && tasks[k].item == tasks[i].item) k++;
-    if (k - i > 32) return false;
     const CrnFile& F = *tasks[i].file;
     const uint32_t kind = (uint32_t)F.kind;
     const bool colour = kind == kKDxt1 || kind == kKDxt5;
     TexJob T{};
     T.models = tasks[i].models;
-    T.nlev = (uint32_t)(k - i);
     T.kind = kind;
     std::vector<StreamJob> sj;
     uint32_t rb = 0;
@@ -829,11 +1584,19 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
       j.n_b = tasks[t].pal.n_aep;
       j.n_sa = colour ? tasks[t].pal.n_csel : tasks[t].pal.n_asel;
       j.n_sb = tasks[t].pal.n_asel;
+      if (to_wide[t]) {
+        wide.push_back(j);
+        continue;
+      }
       j.rb_ofs = rb;
       rb += (li.blocks_x + 1) & ~1u;
       T.work = std::max<uint64_t>(T.work, (uint64_t)li.blocks_x * li.blocks_y * F.faces * (kind == kKDxt1 || kind == kKDxt5a ? 1 : 2));
       sj.push_back(j);
     }
+    i = k;
+    if (sj.empty()) continue;
+    if (sj.size() > 32) return false;
+    T.nlev = (uint32_t)sj.size();
     // the texture's longest streams first: the decoder gives each of the first few its own warp
     std::stable_sort(sj.begin(), sj.end(),
                      [](const StreamJob& a, const StreamJob& b) { return a.bx * a.by > b.bx * b.by; });
@@ -842,8 +1605,12 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
     p.lut_words = std::max(p.lut_words, models_used(kind) << kLutBits);
     items.push_back(T);
     item_streams.push_back(std::move(sj));
-    i = k;
   }
+  // the largest wide levels first, so the longest chains start first
+  std::stable_sort(wide.begin(), wide.end(), [](const StreamJob& a, const StreamJob& b) {
+    return (uint64_t)a.bx * a.by * a.faces * record_bytes(a.kind) > (uint64_t)b.bx * b.by * b.faces * record_bytes(b.kind);
+  });
+  for (const StreamJob& j : wide) p.wide_smem = std::max(p.wide_smem, wide_layout(models_used(j.kind)).total);
   // largest textures first: the persistent warps then finish at about the same time
   std::vector<size_t> order(items.size());
   for (size_t i = 0; i < order.size(); i++) order[i] = i;
@@ -884,11 +1651,13 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
   p.n_item = (uint32_t)it_sorted.size();
   p.n_stream = (uint32_t)sj.size();
   p.n_expand = (uint32_t)ej.size();
+  p.n_wide = (uint32_t)wide.size();
   p.ctas = (uint32_t)tiles[0].size();
   auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
   p.stream_ofs = al(sizeof(TexJob) * it_sorted.size());
   p.expand_ofs = p.stream_ofs + al(sizeof(StreamJob) * sj.size());
-  size_t end = p.expand_ofs + al(sizeof(ExpandJob) * ej.size());
+  p.wide_ofs = p.expand_ofs + al(sizeof(ExpandJob) * ej.size());
+  size_t end = p.wide_ofs + al(sizeof(StreamJob) * wide.size());
   for (int ts = 0; ts < kTileSizes; ts++) {
     p.tile_ofs[ts] = end;
     p.tile_ctas[ts] = (uint32_t)tiles[ts].size();
@@ -898,43 +1667,73 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p) {
   std::memcpy(p.image.data(), it_sorted.data(), sizeof(TexJob) * it_sorted.size());
   std::memcpy(p.image.data() + p.stream_ofs, sj.data(), sizeof(StreamJob) * sj.size());
   std::memcpy(p.image.data() + p.expand_ofs, ej.data(), sizeof(ExpandJob) * ej.size());
+  if (!wide.empty()) std::memcpy(p.image.data() + p.wide_ofs, wide.data(), sizeof(StreamJob) * wide.size());
   for (int ts = 0; ts < kTileSizes; ts++)
     std::memcpy(p.image.data() + p.tile_ofs[ts], tiles[ts].data(), sizeof(uint2) * tiles[ts].size());
   return true;
 }
 
-// Persistent decoder grid: CTAs of one warp, as many as shared memory lets reside on every SM.
-int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
-  static int sms[64] = {}, smem_sm[64] = {};
-  static bool attr_set[64] = {};
+// Per-device set-up of the transcoder kernels (shared-memory attributes) and the figures the
+// plans need: SM count, shared memory per SM, and how many wide-decoder CTAs are resident at once.
+struct DecodeDevice {
+  int sms = 0, smem_sm = 0;
+  uint32_t wide_slots = 0;
+  bool ready = false;
+};
+
+int decode_device(const DecodeDevice** out) {
+  static DecodeDevice devs[64];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_check(e, "cudaGetDevice");
   if (dev < 0 || dev >= 64) { set_error("device index out of range"); return CRNGPU_E_PARAM; }
   std::lock_guard<std::mutex> lock(device_setup_mutex());
-  if (!sms[dev]) {
-    if ((e = cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+  DecodeDevice& D = devs[dev];
+  if (!D.ready) {
+    if ((e = cudaDeviceGetAttribute(&D.sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
       return cuda_check(e, "device attribute");
-    if ((e = cudaDeviceGetAttribute(&smem_sm[dev], cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
+    if ((e = cudaDeviceGetAttribute(&D.smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess)
       return cuda_check(e, "device attribute");
-  }
-  if (!attr_set[dev]) {
     if ((e = cudaFuncSetAttribute(k_crn_decode_textures, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)kDecodeSmemMax)) != cudaSuccess)
       return cuda_check(e, "decoder shared memory attribute");
+    if ((e = cudaFuncSetAttribute(k_crn_decode_wide, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)wide_layout(5).total)) != cudaSuccess)
+      return cuda_check(e, "wide decoder shared memory attribute");
     for (int v = 0; v < kExpandVariants; v++)
       if ((kVariantStage[v] || kVariantTmaBytes[v]) &&
           (e = cudaFuncSetAttribute(kExpandKernels[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)(kVariantTmaBytes[v] + (kVariantStage[v] ? 2 * kMaxSyms * sizeof(uint32_t) : 0)))) !=
               cudaSuccess)
         return cuda_check(e, "expansion shared memory attribute");
-    attr_set[dev] = true;
+    int per_sm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_crn_decode_wide, kWThreads,
+                                                           wide_layout(3).total)) != cudaSuccess)
+      return cuda_check(e, "wide decoder occupancy");
+    D.wide_slots = (uint32_t)std::max(1, per_sm) * (uint32_t)D.sms;
+    D.ready = true;
   }
+  *out = &D;
+  return CRNGPU_OK;
+}
+
+int wide_slots(uint32_t* slots) {
+  const DecodeDevice* D = nullptr;
+  const int rc = decode_device(&D);
+  if (rc == CRNGPU_OK) *slots = D->wide_slots;
+  return rc;
+}
+
+// Persistent decoder grid: CTAs of one warp, as many as shared memory lets reside on every SM.
+int decode_grid(const Plan& p, uint32_t* grid, size_t* smem) {
+  const DecodeDevice* D = nullptr;
+  const int rc = decode_device(&D);
+  if (rc != CRNGPU_OK) return rc;
   *smem = (size_t)(p.lut_words + p.rb_words) * sizeof(uint32_t);
   // CTAs of kDecodeWarps warps: at most 2048 / (32 kDecodeWarps) per SM, fewer if shared memory binds
   const uint32_t per_sm = std::max<uint32_t>(
-      1, std::min<uint32_t>(2048 / (32 * kDecodeWarps), (uint32_t)(smem_sm[dev] / (*smem + 1024))));
-  *grid = std::max<uint32_t>(1, std::min<uint32_t>(p.n_item, per_sm * (uint32_t)sms[dev]));
+      1, std::min<uint32_t>(2048 / (32 * kDecodeWarps), (uint32_t)(D->smem_sm / (*smem + 1024))));
+  *grid = std::max<uint32_t>(1, std::min<uint32_t>(p.n_item, per_sm * (uint32_t)D->sms));
   return CRNGPU_OK;
 }
 
@@ -954,8 +1753,15 @@ int enqueue_plan(const Plan& p, const uint8_t* d_jobs, uint32_t* words, cudaStre
   const TexJob* tj = reinterpret_cast<const TexJob*>(d_jobs);
   const StreamJob* sj = reinterpret_cast<const StreamJob*>(d_jobs + p.stream_ofs);
   const ExpandJob* ej = reinterpret_cast<const ExpandJob*>(d_jobs + p.expand_ofs);
-  if (decode && p.n_item) {
+  if (decode && (p.n_item || p.n_wide)) {
     if ((e = cudaMemsetAsync(words, 0, 8, s)) != cudaSuccess) return cuda_check(e, "clear work counter");
+  }
+  if (decode && p.n_wide) {
+    const StreamJob* wj = reinterpret_cast<const StreamJob*>(d_jobs + p.wide_ofs);
+    k_crn_decode_wide<<<p.n_wide, kWThreads, p.wide_smem, s>>>(wj, words + 1);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_decode_wide");
+  }
+  if (decode && p.n_item) {
     k_crn_decode_textures<<<grid, kDecodeWarps * 32, smem, s>>>(tj, p.n_item, sj, words, p.lut_words, p.rb_words,
                                                              words + 1);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_crn_decode_textures");
@@ -994,7 +1800,10 @@ int run_levels(UnpackContext* c, std::vector<LevelTask>& tasks, cudaStream_t s) 
     ofs += (level_records(c->file, t.level) * c->rec_bytes() + 15) & ~(uint64_t)15;
   }
   Plan p;
-  if (!make_plan(tasks, p)) { set_error("too many levels in one texture job"); return CRNGPU_E_PARAM; }
+  uint32_t slots = 0;
+  int rc0 = wide_slots(&slots);
+  if (rc0 != CRNGPU_OK) return rc0;
+  if (!make_plan(tasks, p, slots)) { set_error("too many levels in one texture job"); return CRNGPU_E_PARAM; }
   if ((e = c->d_jobs.ensure(p.image.size() + 16)) != cudaSuccess) return cuda_check(e, "alloc jobs");
   if ((e = cudaMemcpyAsync(c->d_jobs.ptr, p.image.data(), p.image.size(), cudaMemcpyHostToDevice, s)) != cudaSuccess)
     return cuda_check(e, "copy jobs");
@@ -1251,7 +2060,9 @@ extern "C" crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_ba
   }
   if ((e = b->d_records.ensure(rec + 16)) != cudaSuccess) { cuda_check(e, "alloc records"); return nullptr; }
   for (LevelTask& t : tasks) t.rec = static_cast<uint8_t*>(b->d_records.ptr) + reinterpret_cast<uintptr_t>(t.rec);
-  if (!make_plan(tasks, b->plan)) { set_error("too many levels in one batch item"); return nullptr; }
+  uint32_t slots = 0;
+  if (wide_slots(&slots) != CRNGPU_OK) return nullptr;
+  if (!make_plan(tasks, b->plan, slots)) { set_error("too many levels in one batch item"); return nullptr; }
   if ((e = b->d_jobs.ensure(b->plan.image.size() + 16)) != cudaSuccess) { cuda_check(e, "alloc jobs"); return nullptr; }
   if ((e = cudaMemcpy(b->d_jobs.ptr, b->plan.image.data(), b->plan.image.size(), cudaMemcpyHostToDevice)) !=
       cudaSuccess) {
@@ -1372,6 +2183,12 @@ extern "C" int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch) {
   UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
   if (!b || b->magic != 0x42415443u) return CRNGPU_E_PARAM;
   return (int64_t)b->out_bytes;
+}
+
+extern "C" int crngpu_set_decode_split(uint32_t min_blocks) {
+  clear_error();
+  g_wide_min_blocks.store(min_blocks, std::memory_order_relaxed);
+  return CRNGPU_OK;
 }
 
 extern "C" int crngpu_unpack_batch_destroy(crngpu_unpack_batch batch) {
@@ -1513,7 +2330,9 @@ extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_si
   t.rec = base + o_rec;
   t.item = 0;
   Plan p;
-  if (!make_plan({t}, p)) { set_error("bad level"); return CRNGPU_E_PARAM; }
+  uint32_t slots = 0;
+  if ((rc = wide_slots(&slots)) != CRNGPU_OK) return rc;
+  if (!make_plan({t}, p, slots)) { set_error("bad level"); return CRNGPU_E_PARAM; }
   const size_t need = o_jobs + al(p.image.size());
   if (need > kNoAllocScratchBytes) {
     set_error("level needs " + std::to_string(need) + " bytes of scratch; the allocation-free entry point has " +

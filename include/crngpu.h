@@ -474,6 +474,20 @@ CRNGPU_API int crngpu_unpack_batch_set_variant(crngpu_unpack_batch batch, int32_
 /* Total output bytes of the batch (sum of the items' level sizes). */
 CRNGPU_API int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch);
 
+/* Which decoder runs a level's block stream (no counterpart in the reference, which has one
+ * serial decoder). The wide decoder gives one CTA to a level: per-bit-position step tables built
+ * in parallel, a serial walk of chunk and block starts at one shared-memory load per step, then
+ * parallel symbol decode and a scan of the endpoint indices. It has the lowest latency per level
+ * but does more work per block. The lane decoder runs one level stream per lane, many streams per
+ * warp: least work per block, the latency of a serial decode. Both give the same bytes.
+ * min_blocks = 0 (the default): each plan sends its largest levels to the wide decoder as long as
+ * that shortens the plan's decode (a cost model of both decoders and the device's resident wide
+ * CTAs); a single texture's large levels go wide, a batch of many textures mostly stays on the
+ * lane decoder. Otherwise levels of at least min_blocks blocks (all faces) go wide: 1 sends every
+ * level with rows of at most 1024 blocks, 0xFFFFFFFF none. Applies to plans built after the call:
+ * contexts' unpack calls and batches created afterwards. */
+CRNGPU_API int crngpu_set_decode_split(uint32_t min_blocks);
+
 CRNGPU_API int crngpu_unpack_batch_destroy(crngpu_unpack_batch batch);
 
 /* Mip generation (mipmapped_texture::generate_mipmaps, crnlib/crn_mipmapped_texture.cpp:2140-2215,

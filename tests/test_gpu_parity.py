@@ -126,6 +126,60 @@ def test_transcode_levels_bit_exact(cg, name):
             pos += info["bytes"]
 
 
+@pytest.fixture
+def decode_split(cg):
+    """Sets crngpu_set_decode_split for one test and restores the default after it."""
+    def set_split(mode):
+        cg.set_decode_split({"wide": cg.DECODE_WIDE_ONLY, "lane": cg.DECODE_LANE_ONLY}[mode])
+    yield set_split
+    cg.set_decode_split(cg.DECODE_SPLIT_DEFAULT)
+
+
+@pytest.mark.parametrize("mode", ["wide", "lane"])
+@pytest.mark.parametrize("name", sorted(G.manifest().keys()))
+def test_transcode_each_decoder_bit_exact(cg, decode_split, name, mode):
+    """Every level of every fixture through one decoder alone: the wide decoder (a CTA per level,
+    1x1 mip levels and cube faces included) or the lane decoder (a lane per level stream), against
+    the reference's per-level SHA-256, one level per call and all levels in one call."""
+    decode_split(mode)
+    m = G.manifest()[name]
+    with cg.unpack_begin(G.crn_bytes(name)) as ctx:
+        for lvl, info in enumerate(m["levels"]):
+            assert G.sha(ctx.unpack_level(lvl).reshape(-1)) == info["sha256"], (name, lvl, mode)
+        allv = ctx.unpack_levels()
+        pos = 0
+        for lvl, info in enumerate(m["levels"]):
+            assert G.sha(allv[pos:pos + info["bytes"]]) == info["sha256"], (name, lvl, mode, "all levels")
+            pos += info["bytes"]
+
+
+@pytest.mark.parametrize("name", ["dxt1_256", "dxt5_256", "dxn_xy_256", "dxt5a_256", "dxt5_cube_64x32"])
+def test_transcode_decoders_agree_on_corrupt_streams(cg, decode_split, name):
+    """Random bytes written over a level's stream: the wide and the lane decoder return the same
+    outcome -- the same error code, or the same bytes when the stream still decodes."""
+    import struct
+    crn = bytes(G.crn_bytes(name))
+    nlev = len(G.manifest()[name]["levels"])
+    ofs = [struct.unpack(">I", crn[70 + 4 * l:74 + 4 * l])[0] for l in range(nlev)] + [len(crn)]
+    rng = np.random.default_rng(11)
+    for trial in range(12):
+        lvl = trial % 2
+        bad = bytearray(crn)
+        span = ofs[lvl + 1] - ofs[lvl]
+        pos = ofs[lvl] + int(rng.integers(0, max(1, span - 16)))
+        n = int(min(32, ofs[lvl + 1] - pos))
+        bad[pos:pos + n] = rng.integers(0, 256, n, dtype=np.uint8).tobytes()
+        outcome = {}
+        for mode in ("wide", "lane"):
+            decode_split(mode)
+            with cg.unpack_begin(bytes(bad)) as ctx:
+                try:
+                    outcome[mode] = ("ok", G.sha(ctx.unpack_level(lvl).reshape(-1)))
+                except cg.CrnGpuError as e:
+                    outcome[mode] = ("error", e.code)
+        assert outcome["wide"] == outcome["lane"], (name, trial, outcome)
+
+
 @pytest.mark.parametrize("use_graph", [False, True])
 def test_transcode_batch_mixed_formats(cg, use_graph):
     """Every fixture (DXT1, DXT5, DXN, DXT5A, cube maps, NPOT) in one batch, each twice with its
