@@ -388,31 +388,35 @@ constexpr uint32_t kWS = 2048;                 // window stride (bits)
 constexpr uint32_t kWM = 448;                  // window overlap (bits): 2 x 144 of chain overshoot + 128 of table reach
 constexpr uint32_t kWX = kWS + kWM;            // positions per window
 constexpr uint32_t kWWords = kWX / 32 + 4;     // staged stream words per window
-constexpr uint32_t kWWorkers = 256;            // builder / emitter threads (warps 1 .. 8)
-constexpr uint32_t kWThreads = kWWorkers + 32; // + the chain warp (warp 0)
-constexpr uint32_t kWPer = (kWX + kWWorkers - 1) / kWWorkers;  // window positions per worker
+constexpr uint32_t kWEmitters = 128;           // emitter threads (warps 1 .. 4)
+constexpr uint32_t kWBuilders = 480;           // table-builder threads (warps 5 .. 19)
+constexpr uint32_t kWThreads = 32 + kWEmitters + kWBuilders;  // + the chain warp (warp 0)
+constexpr uint32_t kWPer = (kWX + kWBuilders - 1) / kWBuilders;  // window positions per builder
 constexpr uint32_t kWMaxW = 1024;              // widest row, in blocks (4096 texels)
 constexpr uint32_t kWList = kWS + 4;           // chain items per phase, at most (positions increase; two past kWS)
 constexpr uint32_t kWBlk = kWS + 448;          // emitted blocks per phase, at most (each costs >= 1 bit)
 constexpr uint32_t kWNotDone = 0xFFFFFFFFu;
+constexpr uint32_t kStaged = 512;        // reference model: its first sorted symbols in shared memory
+constexpr uint32_t kStagedLong = 4096;   // other models: the symbols of their codes longer than kLutBits
 
 // Shared-memory layout of k_crn_decode_wide (bytes), for a format reading `nm` models.
 struct WideLayout {
-  uint32_t lut, nx, gt, words, list, rb, grow, un, total;
+  uint32_t lut, srt, nx, gt, words, list, rb, grow, un, bw, total;
 };
 __host__ __device__ constexpr uint32_t wide_align16(uint32_t v) { return (v + 15u) & ~15u; }
 __host__ __device__ inline WideLayout wide_layout(uint32_t nm) {
   WideLayout L{};
   uint32_t o = 0;
   L.lut = o;   o += nm * (4u << kLutBits);       // first-level tables of the models read
+  L.srt = o;   o += (nm - 1) * kStagedLong * 2u;  // long-code symbols of the models after the reference
   L.nx = o;    o += 3u * 2u * kWX * 2u;          // next0, next1, nextC (u16) for two windows
   L.gt = o;    o = wide_align16(o + 2u * kWX);   // reference group at each position, two windows
   L.words = o; o += 4u * kWWords * 4u;           // staged stream words, four windows
   L.list = o;  o += 2u * kWList * 4u;            // chain items (bit position | reference << 30), two phases
   L.rb = o;    o += 2u * kWMaxW * 2u;            // endpoint index A and B of the row above
   L.grow = o;  o = wide_align16(o + kWMaxW / 2); // the chain's reference groups of the current even row
-  L.un = o;                                      // union: build temporaries / emitted blocks
-  o += 7u * kWX > 2u * kWBlk * 4u ? 7u * kWX : 2u * kWBlk * 4u;
+  L.un = o;    o = wide_align16(o + 7u * kWX);   // build temporaries (code lengths at each position)
+  L.bw = o;    o += 2u * kWBlk * 4u;             // emitted blocks of one item list
   L.total = wide_align16(o);
   return L;
 }
@@ -474,11 +478,10 @@ __device__ __forceinline__ uint32_t code_len(uint32_t v16, const uint32_t* __res
 // Symbol of the code at the top of `v16` and its length in `len`. Same rules as decode_sym: an
 // invalid code (or a code past the model's symbols) sets `bad`, yields symbol 0 and, when no code
 // of any length matches, is kMaxCodeLen long. `st` holds the model's sorted symbols
-// [st_base, st_base + kStaged) in shared memory; others are read from the device model.
-constexpr uint32_t kStaged = 512;
+// [aux[11], aux[11] + st_n) in shared memory; others are read from the device model.
 __device__ __forceinline__ uint32_t code_sym(uint32_t v16, const uint32_t* __restrict__ lut, const uint32_t* aux,
-                                             const DevModel* __restrict__ m, const uint16_t* st, uint32_t& len,
-                                             uint32_t& bad) {
+                                             const DevModel* __restrict__ m, const uint16_t* st, uint32_t st_n,
+                                             uint32_t& len, uint32_t& bad) {
   const uint32_t e = lut[v16 >> (16 - kLutBits)];
   if (e != kLutLong) {
     len = e >> 16;
@@ -497,16 +500,19 @@ __device__ __forceinline__ uint32_t code_sym(uint32_t v16, const uint32_t* __res
     return 0u;
   }
   const uint32_t k = (uint32_t)idx - aux[11];
-  return k < kStaged ? (uint32_t)st[k] : (uint32_t)__ldg(&m->sorted[idx]);
+  return k < st_n ? (uint32_t)st[k] : (uint32_t)__ldg(&m->sorted[idx]);
 }
 
-__device__ __forceinline__ void worker_sync() { asm volatile("bar.sync 1, %0;" ::"r"(kWWorkers) : "memory"); }
-__device__ __forceinline__ bool worker_sync_or(bool v) {
+// Barriers of the table builders (named barrier 1) and of the emitters (named barrier 2); the
+// other roles run on.
+__device__ __forceinline__ void builder_sync() { asm volatile("bar.sync 1, %0;" ::"r"(kWBuilders) : "memory"); }
+__device__ __forceinline__ void emitter_sync() { asm volatile("bar.sync 2, %0;" ::"r"(kWEmitters) : "memory"); }
+__device__ __forceinline__ bool emitter_sync_or(bool v) {
   uint32_t r;
   asm volatile(
-      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 1, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 2, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
       : "=r"(r)
-      : "r"((uint32_t)v), "r"(kWWorkers)
+      : "r"((uint32_t)v), "r"(kWEmitters)
       : "memory");
   return r != 0u;
 }
@@ -531,9 +537,9 @@ extern __shared__ __align__(16) uint8_t wide_smem[];
 struct WideShared {
   uint32_t meta[2][3];  // per item list: count, first row, first item in that row
   uint32_t done, carry[2], bad;
-  uint32_t scan[kWWorkers / 32][3];
   uint32_t aux[5][kAuxWords];       // long-code bounds of the models read (slot order of the tables)
-  uint16_t sorted[5][kStaged];      // sorted symbols: the reference model's first, the others' longest
+  uint32_t scan[kWEmitters / 32][3];
+  uint16_t rsorted[kStaged];        // the reference model's first sorted symbols
 };
 
 template <int KIND>
@@ -544,6 +550,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
   constexpr uint32_t nm = five ? 5u : 3u;
   uint8_t* sm = wide_smem;
   const WideLayout Ly = wide_layout(nm);
+  uint16_t* srt = reinterpret_cast<uint16_t*>(sm + Ly.srt);
 
   const uint32_t tid = threadIdx.x;
   uint32_t* luts = reinterpret_cast<uint32_t*>(sm + Ly.lut);
@@ -576,7 +583,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
   uint8_t* lenSB = un + 4 * kWX;
   uint8_t* lenSBk = un + 5 * kWX;  // selector codes of one block (two-endpoint formats)
   uint8_t* lenEBk = un + 6 * kWX;  // endpoint codes of one block (two-endpoint formats)
-  uint32_t* bw0 = reinterpret_cast<uint32_t*>(un);  // emitted blocks: reference | delta A << 2 | selector A << 16
+  uint32_t* bw0 = reinterpret_cast<uint32_t*>(sm + Ly.bw);  // emitted blocks: reference | delta A << 2 | selector A << 16
   uint32_t* bw1 = bw0 + kWBlk;                      // delta B | selector B << 16
 
   const uint32_t W = (J.bx + 1) & ~1u, H = (J.by + 1) & ~1u, W2 = W >> 1;
@@ -612,18 +619,20 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
   __syncthreads();
   {
     const int srcm[5] = {kMRef, colour ? kMEp0 : kMEp1, colour ? kMSel0 : kMSel1, kMEp1, kMSel1};
-    for (uint32_t i = tid; i < nm * kStaged; i += blockDim.x) {
-      const uint32_t t = i / kStaged, k = i - t * kStaged;
+    for (uint32_t k = tid; k < kStaged; k += blockDim.x) S.rsorted[k] = __ldg(&mR->sorted[k]);
+    for (uint32_t i = tid; i < (nm - 1) * kStagedLong; i += blockDim.x) {
+      const uint32_t t = 1 + i / kStagedLong, k = i % kStagedLong;
       const uint32_t idx = S.aux[t][11] + k;
-      S.sorted[t][k] = idx < kMaxSyms ? __ldg(&J.models[srcm[t]].sorted[idx]) : (uint16_t)0;
+      srt[i] = idx < kMaxSyms ? __ldg(&J.models[srcm[t]].sorted[idx]) : (uint16_t)0;
     }
   }
   __syncthreads();
 
   uint32_t c_r = 0, c_e = 0, c_j = 0;  // the chain's row, item within the row, window position
   uint32_t done_at = kWNotDone;
-  const bool worker = tid >= 32;
-  const uint32_t wt = tid - 32;
+  const uint32_t warp = tid >> 5, lane = tid & 31u;
+  const uint32_t wt = tid - (32 + kWEmitters);  // builder index
+  const uint32_t et = tid - 32;                 // emitter index
   for (uint32_t t = 0;; t++) {
     if (tid == 0 && t >= 1 && done_at == kWNotDone) {
       // ---- the chain walks window t - 1 and records its items in list (t - 1) & 1
@@ -697,8 +706,8 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
       c_e = e;
       c_j = j - kWS;
       if (r >= rows) S.done = t;
-    } else if (worker) {
-      // the stream words of window t + 1, stored once this phase's emission is done
+    } else if (warp >= 1 + kWEmitters / 32) {
+      // the stream words of window t + 1, stored at the end of the build
       const uint32_t pre_m = (((t + 1) * kWS) >> 5) + wt;
       const RawWord pre = (done_at == kWNotDone && wt < kWWords) ? stream_word_load(J.src, J.src_size, pre_m)
                                                                   : RawWord{0u, 0u};
@@ -712,7 +721,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
         {
           uint32_t v[kWPer], eR[kWPer], eD[kWPer], eS[kWPer], eD2[kWPer], eS2[kWPer];
 #pragma unroll
-          for (uint32_t q = 0; q < kWPer; q++) v[q] = window_bits(wd, min(wt + q * kWWorkers, kWX - 1)) >> 16;
+          for (uint32_t q = 0; q < kWPer; q++) v[q] = window_bits(wd, min(wt + q * kWBuilders, kWX - 1)) >> 16;
 #pragma unroll
           for (uint32_t q = 0; q < kWPer; q++) {
             const uint32_t i = v[q] >> (16 - kLutBits);
@@ -726,10 +735,10 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
           }
 #pragma unroll
           for (uint32_t q = 0; q < kWPer; q++) {
-            const uint32_t j = wt + q * kWWorkers;
+            const uint32_t j = wt + q * kWBuilders;
             if (j < kWX) {
               uint32_t sym = eR[q] & 0xFFFFu, len = eR[q] >> 16, junk = 0;
-              if (eR[q] == kLutLong) sym = code_sym(v[q], lR, S.aux[0], mR, S.sorted[0], len, junk);
+              if (eR[q] == kLutLong) sym = code_sym(v[q], lR, S.aux[0], mR, S.rsorted, kStaged, len, junk);
               g[j] = (uint8_t)sym;
               lenR[j] = (uint8_t)len;
               const uint32_t ll1 = min(long_code_len(v[q], S.aux[1]), (uint32_t)kMaxCodeLen);
@@ -745,7 +754,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
             }
           }
         }
-        worker_sync();
+        builder_sync();
         const uint8_t* sbl = lenSA;  // length of a block's selector code(s) at each position
         const uint8_t* ebl = lenDA;  // length of a block's endpoint delta code(s)
         if (two) {
@@ -754,25 +763,25 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
           uint32_t ls[kWPer], ld[kWPer], xs[kWPer], xd[kWPer];
 #pragma unroll
           for (uint32_t q = 0; q < kWPer; q++) {
-            const uint32_t j = min(wt + q * kWWorkers, kWX - 1);
+            const uint32_t j = min(wt + q * kWBuilders, kWX - 1);
             ls[q] = lenSA[j];
             ld[q] = lenDA[j];
           }
 #pragma unroll
           for (uint32_t q = 0; q < kWPer; q++) {
-            const uint32_t j = min(wt + q * kWWorkers, kWX - 1);
+            const uint32_t j = min(wt + q * kWBuilders, kWX - 1);
             xs[q] = l2S[min(j + ls[q], kWX - 1)];
             xd[q] = l2D[min(j + ld[q], kWX - 1)];
           }
 #pragma unroll
           for (uint32_t q = 0; q < kWPer; q++) {
-            const uint32_t j = wt + q * kWWorkers;
+            const uint32_t j = wt + q * kWBuilders;
             if (j < kWX) {
               lenSBk[j] = (uint8_t)(ls[q] + xs[q]);
               lenEBk[j] = (uint8_t)(ld[q] + xd[q]);
             }
           }
-          worker_sync();
+          builder_sync();
           sbl = lenSBk;
           ebl = lenEBk;
         }
@@ -782,7 +791,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
           uint32_t sb[kWPer], qq[kWPer], s2[kWPer];
 #pragma unroll
           for (uint32_t q = 0; q < kWPer; q++) {
-            const uint32_t j = min(wt + q * kWWorkers, kWX - 1);
+            const uint32_t j = min(wt + q * kWBuilders, kWX - 1);
             sb[q] = sbl[j];
             qq[q] = min(j + ebl[j], kWX - 1);
           }
@@ -790,20 +799,20 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
           for (uint32_t q = 0; q < kWPer; q++) s2[q] = sbl[qq[q]];
 #pragma unroll
           for (uint32_t q = 0; q < kWPer; q++) {
-            const uint32_t j = wt + q * kWWorkers;
+            const uint32_t j = wt + q * kWBuilders;
             if (j < kWX) {
               b0[j] = (uint16_t)min(j + sb[q], kWX - 1);
               b1[j] = (uint16_t)min(qq[q] + s2[q], kWX - 1);
             }
           }
         }
-        worker_sync();
+        builder_sync();
         {
           uint16_t* bc = nxC + wb * kWX;
           uint32_t gg[kWPer], q1[kWPer];
 #pragma unroll
           for (uint32_t q = 0; q < kWPer; q++) {
-            const uint32_t j = min(wt + q * kWWorkers, kWX - 1);
+            const uint32_t j = min(wt + q * kWBuilders, kWX - 1);
             gg[q] = g[j];
             q1[q] = min(j + lenR[j], kWX - 1);
           }
@@ -813,213 +822,201 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
           for (uint32_t q = 0; q < kWPer; q++) q1[q] = ((gg[q] >> 4) & 3u) ? b0[q1[q]] : b1[q1[q]];
 #pragma unroll
           for (uint32_t q = 0; q < kWPer; q++) {
-            const uint32_t j = wt + q * kWWorkers;
+            const uint32_t j = wt + q * kWBuilders;
             if (j < kWX) bc[j] = (uint16_t)q1[q];
           }
         }
-        worker_sync();  // the temporaries are dead; the emission below reuses their space
-      }
-      if (t >= 2 && (done_at == kWNotDone || t - 2 < done_at)) {
-        // ---- emit list t - 2 (buffer t & 1), decoding from window t - 2's staged words
-        const uint32_t lb = t & 1u;
-        const uint32_t* L = list + lb * kWList;
-        const uint32_t* wd = words + ((t - 2) & 3u) * kWWords;
-        const uint32_t a2 = (t - 2) * kWS;
-        const uint32_t n = S.meta[lb][0], r0 = S.meta[lb][1], e0 = S.meta[lb][2];
-        // item i -> row, item within the row, first block of the list's block array
-        const uint32_t odd0 = r0 & 1u, be0 = odd0 ? 1u : 2u;
-        const uint32_t nfirst = (odd0 ? W : W2) - e0;
-        const uint32_t n1 = odd0 ? W2 : W, be1 = odd0 ? 2u : 1u;
-        auto locate = [&](uint32_t i, uint32_t& r, uint32_t& e, uint32_t& blk) {
-          if (i < nfirst) {
-            r = r0;
-            e = e0 + i;
-            blk = i * be0;
-            return;
-          }
-          const uint32_t ip = i - nfirst, pairs = ip / (W2 + W), rem = ip - pairs * (W2 + W);
-          const uint32_t base = nfirst * be0 + pairs * 2u * W;
-          if (rem < n1) {
-            r = r0 + 1 + 2 * pairs;
-            e = rem;
-            blk = base + rem * be1;
-          } else {
-            r = r0 + 2 + 2 * pairs;
-            e = rem - n1;
-            blk = base + W + (rem - n1) * be0;
-          }
-        };
-        uint32_t bad = 0;
-        for (uint32_t i = wt; i < n; i += kWWorkers) {
-          const uint32_t ent = L[i];
-          uint32_t j = (ent & 0x3FFFFFFFu) - a2;
-          uint32_t r, e, blk;
-          locate(i, r, e, blk);
-          auto dec = [&](const uint32_t* lut, uint32_t slot, const DevModel* m) {
-            uint32_t len;
-            const uint32_t s = code_sym(window_bits(wd, j) >> 16, lut, S.aux[slot], m, S.sorted[slot], len, bad);
-            j += len;
-            return s;
-          };
-          auto block = [&](uint32_t ref, uint32_t k) {
-            uint32_t dA = 0, dB = 0;
-            if (!ref) {
-              dA = dec(lDA, 1, mDA);
-              if (two) dB = dec(lDB, sDB, mDB);
-            }
-            const uint32_t sA = dec(lSA, 2, mSA);
-            const uint32_t sB = two ? dec(lSB, sSB, mSB) : 0u;
-            bw0[k] = ref | (dA << 2) | (sA << 16);
-            if (two) bw1[k] = dB | (sB << 16);
-          };
-          if (!(r & 1u)) {
-            const uint32_t g = dec(lR, 0, mR) & 0xFFu;
-            block(g & 3u, blk);
-            block((g >> 4) & 3u, blk + 1);
-          } else {
-            block(ent >> 30, blk);
-          }
-        }
-        if (bad) atomicOr(&S.bad, 1u);
-        uint32_t total = 0;
-        if (n) {
-          uint32_t r, e, blk;
-          locate(n - 1, r, e, blk);
-          total = blk + ((r & 1u) ? 1u : 2u);
-        }
-        worker_sync();
-        // resolve the endpoint indices row segment by row segment, in stream order
-        uint32_t r = r0, x = odd0 ? e0 : 2 * e0, b = 0;
-        uint32_t badi = 0;
-        while (b < total) {
-          const uint32_t cnt = min(W - x, total - b);
-          const uint32_t f = r / H, y = r - f * H;
-          const bool vis_row = y < J.by;
-          const uint32_t per = (cnt + kWWorkers - 1) / kWWorkers;  // <= 4 (rows of at most 1024 blocks)
-          const uint32_t k0 = min(cnt, wt * per), k1 = min(cnt, k0 + per);
-          IdxOp op[4];
-          IdxOp mine{0, 0, 0};
-          bool inexact = nA == 0 || (two && nB == 0);
-#pragma unroll
-          for (uint32_t q = 0; q < 4; q++) {
-            const uint32_t k = k0 + q;
-            if (k < k1) {
-              const uint32_t w0 = bw0[b + k], ref = w0 & 3u;
-              const uint32_t dA = (w0 >> 2) & 0x3FFFu, dB = two ? (bw1[b + k] & 0xFFFFu) : 0u;
-              if (ref == 0) {
-                op[q] = IdxOp{0, dA, dB};
-                inexact |= dA >= nA || (two && dB >= nB);
-              } else if (ref == 1) {
-                op[q] = IdxOp{0, 0, 0};
-              } else {
-                op[q] = IdxOp{1, rbA[x + k], two ? (uint32_t)rbB[x + k] : 0u};
-              }
-              mine = idx_compose<two>(mine, op[q], nA, nB);
-            }
-          }
-          const uint32_t cA = S.carry[0], cB = S.carry[1];
-          if (worker_sync_or(inexact)) {
-            // a delta at or above its palette size: the reference's sequential rule, on one thread
-            if (wt == 0) {
-              uint32_t iA = cA, iB = cB;
-              for (uint32_t k = 0; k < cnt; k++) {
-                const uint32_t w0 = bw0[b + k], ref = w0 & 3u;
-                if (ref == 0) {
-                  iA += (w0 >> 2) & 0x3FFFu;
-                  if (iA >= nA) iA -= nA;
-                  if (two) {
-                    iB += bw1[b + k] & 0xFFFFu;
-                    if (iB >= nB) iB -= nB;
-                  }
-                } else if (ref >= 2) {
-                  iA = rbA[x + k];
-                  iB = rbB[x + k];
-                }
-                // the row buffer holds 16-bit indices: larger ones are corrupt in any case
-                if (iA > 0xFFFFu || iB > 0xFFFFu) badi = 1;
-                iA &= 0xFFFFu;
-                iB &= 0xFFFFu;
-                rbA[x + k] = (uint16_t)iA;
-                rbB[x + k] = (uint16_t)iB;
-                const uint32_t sA = w0 >> 16, sB = two ? bw1[b + k] >> 16 : 0u;
-                if (iA >= nA || sA >= nSA || (two && (iB >= nB || sB >= nSB))) badi = 1;
-                if (vis_row && x + k < J.bx) {
-                  const uint64_t at = ((uint64_t)f * J.by + y) * J.bx + x + k;
-                  if (two) reinterpret_cast<uint64_t*>(J.rec)[at] = (uint64_t)(iA | (sA << 16)) | ((uint64_t)(iB | (sB << 16)) << 32);
-                  else reinterpret_cast<uint32_t*>(J.rec)[at] = iA | (sA << 16);
-                }
-              }
-              S.carry[0] = iA;
-              S.carry[1] = iB;
-            }
-          } else {
-            // block-wide exclusive scan of the per-thread compositions
-            const uint32_t lane = wt & 31u, wi = wt >> 5;
-            IdxOp inc = mine;
-#pragma unroll
-            for (uint32_t d = 1; d < 32; d <<= 1) {
-              IdxOp o;
-              o.set = __shfl_up_sync(0xFFFFFFFFu, inc.set, d);
-              o.a = __shfl_up_sync(0xFFFFFFFFu, inc.a, d);
-              o.b = __shfl_up_sync(0xFFFFFFFFu, inc.b, d);
-              if (lane >= d) inc = idx_compose<two>(o, inc, nA, nB);
-            }
-            if (lane == 31) {
-              S.scan[wi][0] = inc.set;
-              S.scan[wi][1] = inc.a;
-              S.scan[wi][2] = inc.b;
-            }
-            IdxOp ex;
-            ex.set = __shfl_up_sync(0xFFFFFFFFu, inc.set, 1);
-            ex.a = __shfl_up_sync(0xFFFFFFFFu, inc.a, 1);
-            ex.b = __shfl_up_sync(0xFFFFFFFFu, inc.b, 1);
-            if (lane == 0) ex = IdxOp{0, 0, 0};
-            worker_sync();
-            IdxOp tot[kWWorkers / 32];
-#pragma unroll
-            for (uint32_t w = 0; w < kWWorkers / 32; w++) tot[w] = IdxOp{S.scan[w][0], S.scan[w][1], S.scan[w][2]};
-            IdxOp pre_op{0, 0, 0};
-#pragma unroll
-            for (uint32_t w = 0; w < kWWorkers / 32; w++)
-              if (w < wi) pre_op = idx_compose<two>(pre_op, tot[w], nA, nB);
-            pre_op = idx_compose<two>(pre_op, ex, nA, nB);
-            uint32_t iA = pre_op.set ? pre_op.a : add_mod(cA, pre_op.a, nA);
-            uint32_t iB = two ? (pre_op.set ? pre_op.b : add_mod(cB, pre_op.b, nB)) : 0u;
-#pragma unroll
-            for (uint32_t q = 0; q < 4; q++) {
-              const uint32_t k = k0 + q;
-              if (k < k1) {
-                iA = op[q].set ? op[q].a : add_mod(iA, op[q].a, nA);
-                if (two) iB = op[q].set ? op[q].b : add_mod(iB, op[q].b, nB);
-                rbA[x + k] = (uint16_t)iA;
-                if (two) rbB[x + k] = (uint16_t)iB;
-                const uint32_t w0 = bw0[b + k];
-                const uint32_t sA = w0 >> 16, sB = two ? bw1[b + k] >> 16 : 0u;
-                if (iA >= nA || sA >= nSA || (two && (iB >= nB || sB >= nSB))) badi = 1;
-                if (vis_row && x + k < J.bx) {
-                  const uint64_t at = ((uint64_t)f * J.by + y) * J.bx + x + k;
-                  if (two) reinterpret_cast<uint64_t*>(J.rec)[at] = (uint64_t)(iA | (sA << 16)) | ((uint64_t)(iB | (sB << 16)) << 32);
-                  else reinterpret_cast<uint32_t*>(J.rec)[at] = iA | (sA << 16);
-                }
-                if (k + 1 == cnt) {
-                  S.carry[0] = iA;
-                  S.carry[1] = iB;
-                }
-              }
-            }
-          }
-          worker_sync();  // row buffer and carry are complete before the next segment reads them
-          b += cnt;
-          x += cnt;
-          if (x == W) {
-            x = 0;
-            r++;
-          }
-        }
-        if (badi) atomicOr(&S.bad, 2u);
       }
       if (done_at == kWNotDone && wt < kWWords)
         words[((t + 1) & 3u) * kWWords + wt] = stream_word_finish(J.src, J.src_size, pre_m, pre);
+    } else if (warp >= 1 && t >= 2 && (done_at == kWNotDone || t - 2 < done_at)) {
+      // ---- the emitter warps: list t - 2 (buffer t & 1), decoded from window t - 2's staged
+      // words, then its endpoint indices resolved row segment by row segment
+      const uint32_t lb = t & 1u;
+      const uint32_t* L = list + lb * kWList;
+      const uint32_t* wd = words + ((t - 2) & 3u) * kWWords;
+      const uint32_t a2 = (t - 2) * kWS;
+      const uint32_t n = S.meta[lb][0], r0 = S.meta[lb][1], e0 = S.meta[lb][2];
+      // item i -> row, first block of the list's block array
+      const uint32_t odd0 = r0 & 1u, be0 = odd0 ? 1u : 2u;
+      const uint32_t nfirst = (odd0 ? W : W2) - e0;
+      const uint32_t n1 = odd0 ? W2 : W, be1 = odd0 ? 2u : 1u;
+      auto locate = [&](uint32_t i, uint32_t& r, uint32_t& blk) {
+        if (i < nfirst) {
+          r = r0;
+          blk = i * be0;
+          return;
+        }
+        const uint32_t ip = i - nfirst, pairs = ip / (W2 + W), rem = ip - pairs * (W2 + W);
+        const uint32_t base = nfirst * be0 + pairs * 2u * W;
+        if (rem < n1) {
+          r = r0 + 1 + 2 * pairs;
+          blk = base + rem * be1;
+        } else {
+          r = r0 + 2 + 2 * pairs;
+          blk = base + W + (rem - n1) * be0;
+        }
+      };
+      const uint16_t* stA = srt;
+      const uint16_t* stS = srt + kStagedLong;
+      const uint16_t* stDB = five ? srt + 2 * kStagedLong : stA;
+      const uint16_t* stSB = five ? srt + 3 * kStagedLong : stS;
+      uint32_t bad = 0;
+      for (uint32_t i = et; i < n; i += kWEmitters) {
+        const uint32_t ent = L[i];
+        uint32_t j = (ent & 0x3FFFFFFFu) - a2;
+        uint32_t r, blk;
+        locate(i, r, blk);
+        auto dec = [&](const uint32_t* lut, uint32_t slot, const DevModel* m, const uint16_t* st, uint32_t st_n) {
+          uint32_t len;
+          const uint32_t sym = code_sym(window_bits(wd, j) >> 16, lut, S.aux[slot], m, st, st_n, len, bad);
+          j += len;
+          return sym;
+        };
+        auto block = [&](uint32_t ref, uint32_t k) {
+          uint32_t dA = 0, dB = 0;
+          if (!ref) {
+            dA = dec(lDA, 1, mDA, stA, kStagedLong);
+            if (two) dB = dec(lDB, sDB, mDB, stDB, kStagedLong);
+          }
+          const uint32_t sA = dec(lSA, 2, mSA, stS, kStagedLong);
+          const uint32_t sB = two ? dec(lSB, sSB, mSB, stSB, kStagedLong) : 0u;
+          bw0[k] = ref | (dA << 2) | (sA << 16);
+          if (two) bw1[k] = dB | (sB << 16);
+        };
+        if (!(r & 1u)) {
+          const uint32_t g = dec(lR, 0, mR, S.rsorted, kStaged) & 0xFFu;
+          block(g & 3u, blk);
+          block((g >> 4) & 3u, blk + 1);
+        } else {
+          block(ent >> 30, blk);
+        }
+      }
+      if (bad) atomicOr(&S.bad, 1u);
+      uint32_t total = 0;
+      if (n) {
+        uint32_t r, blk;
+        locate(n - 1, r, blk);
+        total = blk + ((r & 1u) ? 1u : 2u);
+      }
+      emitter_sync();
+      // The scan operator per block: a block with deltas adds them (mod the palette size), a
+      // "left" reference keeps the running index, an "up" reference sets it from the row above.
+      auto block_op = [&](uint32_t b, uint32_t x, bool& inexact) -> IdxOp {
+        const uint32_t w0 = bw0[b], ref = w0 & 3u;
+        if (ref == 0) {
+          const uint32_t dA = (w0 >> 2) & 0x3FFFu, dB = two ? (bw1[b] & 0xFFFFu) : 0u;
+          inexact |= dA >= nA || (two && dB >= nB);
+          return IdxOp{0, dA, dB};
+        }
+        if (ref == 1) return IdxOp{0, 0, 0};
+        return IdxOp{1, rbA[x], two ? (uint32_t)rbB[x] : 0u};
+      };
+      uint32_t r = r0, x = odd0 ? e0 : 2 * e0, b = 0, badi = 0;
+      while (b < total) {
+        const uint32_t cnt = min(W - x, total - b);
+        const uint32_t f = r / H, y = r - f * H;
+        const bool vis_row = y < J.by;
+        const uint32_t per = (cnt + kWEmitters - 1) / kWEmitters;  // <= 8 (rows of at most 1024 blocks)
+        const uint32_t k0 = min(cnt, et * per), k1 = min(cnt, k0 + per);
+        bool inexact = nA == 0 || (two && nB == 0);
+        IdxOp mine{0, 0, 0};
+        for (uint32_t k = k0; k < k1; k++) mine = idx_compose<two>(mine, block_op(b + k, x + k, inexact), nA, nB);
+        const uint32_t cA = S.carry[0], cB = S.carry[1];
+        if (emitter_sync_or(inexact)) {
+          // a delta at or above its palette size: the reference's sequential rule, on one thread
+          if (et == 0) {
+            uint32_t iA = cA, iB = cB;
+            for (uint32_t k = 0; k < cnt; k++) {
+              const uint32_t w0 = bw0[b + k], ref = w0 & 3u;
+              if (ref == 0) {
+                iA += (w0 >> 2) & 0x3FFFu;
+                if (iA >= nA) iA -= nA;
+                if (two) {
+                  iB += bw1[b + k] & 0xFFFFu;
+                  if (iB >= nB) iB -= nB;
+                }
+              } else if (ref >= 2) {
+                iA = rbA[x + k];
+                iB = rbB[x + k];
+              }
+              // the row buffer holds 16-bit indices: larger ones are corrupt in any case
+              if (iA > 0xFFFFu || iB > 0xFFFFu) badi = 1;
+              iA &= 0xFFFFu;
+              iB &= 0xFFFFu;
+              rbA[x + k] = (uint16_t)iA;
+              rbB[x + k] = (uint16_t)iB;
+              const uint32_t sA = w0 >> 16, sB = two ? bw1[b + k] >> 16 : 0u;
+              if (iA >= nA || sA >= nSA || (two && (iB >= nB || sB >= nSB))) badi = 1;
+              if (vis_row && x + k < J.bx) {
+                const uint64_t at = ((uint64_t)f * J.by + y) * J.bx + x + k;
+                if (two) reinterpret_cast<uint64_t*>(J.rec)[at] = (uint64_t)(iA | (sA << 16)) | ((uint64_t)(iB | (sB << 16)) << 32);
+                else reinterpret_cast<uint32_t*>(J.rec)[at] = iA | (sA << 16);
+              }
+            }
+            S.carry[0] = iA;
+            S.carry[1] = iB;
+          }
+        } else {
+          // exclusive scan of the threads' compositions: warp shuffles, then the warp totals
+          const uint32_t wi = et >> 5;
+          IdxOp inc = mine;
+#pragma unroll
+          for (uint32_t d = 1; d < 32; d <<= 1) {
+            IdxOp o;
+            o.set = __shfl_up_sync(0xFFFFFFFFu, inc.set, d);
+            o.a = __shfl_up_sync(0xFFFFFFFFu, inc.a, d);
+            o.b = __shfl_up_sync(0xFFFFFFFFu, inc.b, d);
+            if (lane >= d) inc = idx_compose<two>(o, inc, nA, nB);
+          }
+          if (lane == 31) {
+            S.scan[wi][0] = inc.set;
+            S.scan[wi][1] = inc.a;
+            S.scan[wi][2] = inc.b;
+          }
+          IdxOp ex;
+          ex.set = __shfl_up_sync(0xFFFFFFFFu, inc.set, 1);
+          ex.a = __shfl_up_sync(0xFFFFFFFFu, inc.a, 1);
+          ex.b = __shfl_up_sync(0xFFFFFFFFu, inc.b, 1);
+          if (lane == 0) ex = IdxOp{0, 0, 0};
+          emitter_sync();
+          IdxOp pre_op{0, 0, 0};
+#pragma unroll
+          for (uint32_t w = 0; w < kWEmitters / 32; w++)
+            if (w < wi) pre_op = idx_compose<two>(pre_op, IdxOp{S.scan[w][0], S.scan[w][1], S.scan[w][2]}, nA, nB);
+          pre_op = idx_compose<two>(pre_op, ex, nA, nB);
+          uint32_t iA = pre_op.set ? pre_op.a : add_mod(cA, pre_op.a, nA);
+          uint32_t iB = two ? (pre_op.set ? pre_op.b : add_mod(cB, pre_op.b, nB)) : 0u;
+          bool dummy = false;
+          for (uint32_t k = k0; k < k1; k++) {
+            const IdxOp o = block_op(b + k, x + k, dummy);  // reads the row above before this thread's write
+            iA = o.set ? o.a : add_mod(iA, o.a, nA);
+            if (two) iB = o.set ? o.b : add_mod(iB, o.b, nB);
+            rbA[x + k] = (uint16_t)iA;
+            if (two) rbB[x + k] = (uint16_t)iB;
+            const uint32_t w0 = bw0[b + k];
+            const uint32_t sA = w0 >> 16, sB = two ? bw1[b + k] >> 16 : 0u;
+            if (iA >= nA || sA >= nSA || (two && (iB >= nB || sB >= nSB))) badi = 1;
+            if (vis_row && x + k < J.bx) {
+              const uint64_t at = ((uint64_t)f * J.by + y) * J.bx + x + k;
+              if (two) reinterpret_cast<uint64_t*>(J.rec)[at] = (uint64_t)(iA | (sA << 16)) | ((uint64_t)(iB | (sB << 16)) << 32);
+              else reinterpret_cast<uint32_t*>(J.rec)[at] = iA | (sA << 16);
+            }
+            if (k + 1 == cnt) {
+              S.carry[0] = iA;
+              S.carry[1] = iB;
+            }
+          }
+        }
+        emitter_sync();  // row buffer and carry are complete before the next segment reads them
+        b += cnt;
+        x += cnt;
+        if (x == W) {
+          x = 0;
+          r++;
+        }
+      }
+      if (badi) atomicOr(&S.bad, 2u);
     }
     __syncthreads();
     done_at = S.done;
@@ -1029,7 +1026,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
 }
 
 // One CTA per large level stream (`jobs`, largest first).
-__global__ void __launch_bounds__(kWThreads) k_crn_decode_wide(const StreamJob* __restrict__ jobs,
+__global__ void __launch_bounds__(kWThreads, 1) k_crn_decode_wide(const StreamJob* __restrict__ jobs,
                                                                uint32_t* __restrict__ status) {
   __shared__ WideShared S;
   const StreamJob J = jobs[blockIdx.x];
