@@ -611,6 +611,20 @@ def main():
     for _ in range(args.warmup):
         ctx0.unpack_levels(out=d_tx, stream=stream)
     single_ms = timed(lambda: ctx0.unpack_levels(out=d_tx, stream=stream), args.steps)
+    # the same texture with every level on the lane decoder (one lane per level stream)
+    cg.set_decode_split(cg.DECODE_LANE_ONLY)
+    ctx0.unpack_levels(out=d_tx, stream=stream)
+    single_lane_ms = timed(lambda: ctx0.unpack_levels(out=d_tx, stream=stream), max(3, args.steps // 4))
+    cg.set_decode_split(cg.DECODE_SPLIT_DEFAULT)
+    # the reference's own 2048x2048 DXT5 .crn (12 levels), one texture
+    with open(os.path.join(ROOT, "tests", "golden", "crn", "dxt5_2048.crn"), "rb") as fh:
+        crn5 = fh.read()
+    with cg.unpack_begin(crn5) as ctx5:
+        d5 = torch.empty(sum(ctx5.level_bytes(l) for l in range(ctx5.levels)), dtype=torch.uint8, device=dev)
+        ctx5.unpack_levels(out=d5, stream=stream)
+        single5_ms = timed(lambda: ctx5.unpack_levels(out=d5, stream=stream), max(3, args.steps // 4))
+        single5_bytes = d5.numel()
+    del d5
     ctxs = [cg.unpack_begin(crn) for _ in range(TX_BATCH)]
     outs = [torch.empty(tx_bytes, dtype=torch.uint8, device=dev) for _ in range(TX_BATCH)]
     batch = cg.UnpackBatch([(c, 0, c.levels, o) for c, o in zip(ctxs, outs)])
@@ -653,8 +667,12 @@ def main():
                          "h2d_bytes_per_step": 0, "d2h_bytes_per_step": TX_BATCH * tx_bytes,
                          "path": "crngpu_unpack_batch_launch (graph) + D2H of every level to pinned host memory"},
                  "single_texture": {"ms": round(single_ms, 4), "GB/s": round(tx_bytes / (single_ms / 1e3) / 1e9, 4),
-                                    "note": "one texture = 11 level streams on 11 lanes of one warp; the 1024x1024 "
-                                            "level is one serial prefix-code chain, so this is its latency"},
+                                    "lane_decoder_ms": round(single_lane_ms, 4),
+                                    "dxt5_2048_ms": round(single5_ms, 4),
+                                    "dxt5_2048_GB/s": round(single5_bytes / (single5_ms / 1e3) / 1e9, 4),
+                                    "path": "ctx.unpack_levels (crngpu_unpack_levels), device destination: levels of "
+                                            ">= 256 blocks on k_crn_decode_wide (a CTA per level), the rest on the "
+                                            "lane decoder; lane_decoder_ms: every level on the lane decoder"},
                  "expand_roofline": None,
                  "expand_autotune": {"variant": tune_variant, "ms_per_variant": tune_ms,
                                      "variants": "0-11: tile of 1024 << (v >> 1) blocks, DXT1 palettes staged "
@@ -722,6 +740,11 @@ def main():
         cpu = cpu_encode_baseline(blocks, texels / n_blocks)
         transcode["cpu_baseline"] = cpu_transcode_baseline(crn, tx_bytes)
         transcode["vs_cpu"] = round(transcode["value"] / transcode["cpu_baseline"]["value"], 2)
+        # one host thread transcoding the same single file (the reference's use case, one file per call)
+        from oracle import port
+        reps = 8
+        secs = port.time_unpack(crn, reps, 1)
+        transcode["single_texture"]["cpu_1_thread_ms"] = round(secs / reps * 1e3, 4)
 
     if rank == 0:
         line = {"metric": METRIC, "value": round(value, 3), "unit": "Mtexel/s", "n_gpus": world,
@@ -746,6 +769,24 @@ def main():
                 "clustered_2048": clustered_2048, "mixed_batch": mixed_batch, "mips": mips, "roofline": roofline,
                 "cpu_baseline": cpu,
                 "gpu_launches": args.steps * 1, "clocks": clk, "wall_s_timed": round(wall, 4)}
+        # compact figures of every leg, last, so that a truncated log still carries them
+        def pick(d, *keys):
+            for k in keys:
+                d = d.get(k) if isinstance(d, dict) else None
+            return d
+        line["summary"] = {
+            "encode_mtexel_s": round(value, 1), "e2e_mtexel_s": round(e2e_value, 1),
+            "encode_roofline_frac": roofline["frac"],
+            "learned_mtexel_s": pick(learned, "value"), "learned_speedup": pick(learned, "speedup_vs_plain"),
+            "learned_rmse_delta": pick(learned, "rmse_delta"),
+            "transcode_batch_gb_s": transcode["value"], "transcode_single_ms": transcode["single_texture"]["ms"],
+            "transcode_single_cpu_1_thread_ms": pick(transcode, "single_texture", "cpu_1_thread_ms"),
+            "transcode_dxt5_2048_ms": transcode["single_texture"]["dxt5_2048_ms"],
+            "expand_hbm_frac": expand["frac"],
+            "mixed_encode_mtexel_s": pick(mixed_batch, "encode", "value"),
+            "mixed_transcode_gb_s": pick(mixed_batch, "transcode", "value"),
+            "crn_encode_mtexel_s": pick(clustered, "value"),
+            "cpu_encode_mtexel_s": round(cpu["value"], 3) if cpu else None}
         print(json.dumps(line))
 
 

@@ -1497,7 +1497,7 @@ std::atomic<uint32_t> g_wide_min_blocks{0};
 
 // Decode cost model, in microseconds per block for a one-endpoint format (twice that for DXT5 and
 // DXN), measured on GB300: the lane decoder's serial chain and one wide CTA's phase loop.
-constexpr double kLaneUsPerBlock = 0.20, kWideUsPerBlock = 0.05;
+constexpr double kLaneUsPerBlock = 0.20, kWideUsPerBlock = 0.03;
 constexpr uint32_t kWideMinBlocks = 256;  // smaller levels always go to the lane decoder
 
 uint64_t task_blocks(const LevelTask& t) {
