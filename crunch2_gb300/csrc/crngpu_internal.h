@@ -113,6 +113,10 @@ int dxt5a_chunks_max_grid();
 // launch_dxt5a: quality sets the probe grid (+-16 Uber, +-8 Better, none below).
 int launch_dxt1(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
                 uint64_t* d_err, cudaStream_t s);
+// The same with the block count in device memory (*n_dev <= n_max), so that a caller need not
+// read it back before the launch; the grids are sized for n_max.
+int launch_dxt1_count(const uint8_t* d_blocks, uint32_t n_max, const uint32_t* n_dev, uint32_t opts, uint8_t* d_out,
+                      uint32_t out_stride, cudaStream_t s);
 int launch_dxt1_black_trial(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
                             uint64_t* d_err_io, cudaStream_t s);
 int launch_dxt5a(const uint8_t* d_blocks, uint32_t n, int comp, bool both, uint32_t quality, uint8_t* d_out,

@@ -1557,8 +1557,10 @@ __device__ __forceinline__ void load_pix(const uint8_t* px, uint32_t (&pix)[16])
 // per block, each group staged by one bulk copy.
 template <bool G>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kSeedCtasPerSm)
-    k_dxt1_seeds(const uint8_t* __restrict__ blocks, uint32_t n, uint32_t opts, Seed* __restrict__ seeds) {
+    k_dxt1_seeds(const uint8_t* __restrict__ blocks, uint32_t n, uint32_t opts, Seed* __restrict__ seeds,
+                 const uint32_t* __restrict__ n_dev) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (n_dev) n = min(n, *n_dev);  // a count the host does not read back: n is then only the grid's bound
   SeedShared& S = reinterpret_cast<SeedShared*>(smem_raw)[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
   const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
@@ -1606,8 +1608,10 @@ template <bool G>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kCtasPerSm)
     k_dxt1_encode(const uint8_t* __restrict__ blocks, uint32_t n, uint32_t opts, const Seed* __restrict__ seeds,
                   uint8_t* __restrict__ out, uint32_t out_stride, uint64_t* __restrict__ err_out,
-                  uint64_t* __restrict__ err_io, unsigned long long* __restrict__ work_out) {
+                  uint64_t* __restrict__ err_io, unsigned long long* __restrict__ work_out,
+                  const uint32_t* __restrict__ n_dev) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (n_dev) n = min(n, *n_dev);
   WarpShared& S = reinterpret_cast<WarpShared*>(smem_raw)[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
   const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
@@ -2063,8 +2067,9 @@ int dxt1_launch_setup(int dev, Dxt1Launch* L) {
 
 // Phase 1 (k_dxt1_seeds) then phase 2 (k_dxt1_encode) over n blocks, their seed records in
 // stream-ordered memory from the seed pool.
+// n_dev (optional): the block count in device memory, at most n; the grids are sized for n.
 int launch_dxt1_kernel(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
-                       uint64_t* d_err, uint64_t* d_err_io, cudaStream_t s) {
+                       uint64_t* d_err, uint64_t* d_err_io, cudaStream_t s, const uint32_t* n_dev = nullptr) {
   int rc = ensure_tables();
   if (rc != CRNGPU_OK) return rc;
   if (!n) return CRNGPU_OK;
@@ -2090,13 +2095,13 @@ int launch_dxt1_kernel(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8
   const uint32_t full = (uint32_t)(L.sms * L.search_per_sm[general ? 1 : 0]);
   const uint32_t grid = std::min<uint32_t>((n + kWarpsPerCta - 1) / kWarpsPerCta, full);
   if (general) {
-    k_dxt1_seeds<true><<<seed_grid, kWarpsPerCta * 32, seed_smem, s>>>(d_blocks, n, opts, seeds);
+    k_dxt1_seeds<true><<<seed_grid, kWarpsPerCta * 32, seed_smem, s>>>(d_blocks, n, opts, seeds, n_dev);
     k_dxt1_encode<true><<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, seeds, d_out, out_stride, d_err,
-                                                             d_err_io, work);
+                                                             d_err_io, work, n_dev);
   } else {
-    k_dxt1_seeds<false><<<seed_grid, kWarpsPerCta * 32, seed_smem, s>>>(d_blocks, n, opts, seeds);
+    k_dxt1_seeds<false><<<seed_grid, kWarpsPerCta * 32, seed_smem, s>>>(d_blocks, n, opts, seeds, n_dev);
     k_dxt1_encode<false><<<grid, kWarpsPerCta * 32, smem, s>>>(d_blocks, n, opts, seeds, d_out, out_stride, d_err,
-                                                              d_err_io, work);
+                                                              d_err_io, work, n_dev);
   }
   e = cudaGetLastError();
   const cudaError_t fe = cudaFreeAsync(seeds, s);
@@ -2109,6 +2114,11 @@ int launch_dxt1_kernel(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8
 int launch_dxt1(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
                 uint64_t* d_err, cudaStream_t s) {
   return launch_dxt1_kernel(d_blocks, n, opts & ~kD1BlackTrial, d_out, out_stride, d_err, nullptr, s);
+}
+
+int launch_dxt1_count(const uint8_t* d_blocks, uint32_t n_max, const uint32_t* n_dev, uint32_t opts, uint8_t* d_out,
+                      uint32_t out_stride, cudaStream_t s) {
+  return launch_dxt1_kernel(d_blocks, n_max, opts & ~kD1BlackTrial, d_out, out_stride, nullptr, nullptr, s, n_dev);
 }
 
 int launch_dxt1_black_trial(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,

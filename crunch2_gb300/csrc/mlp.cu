@@ -1050,23 +1050,27 @@ extern "C" int crngpu_dxt1_learned(void* h, const uint8_t* d_blocks, uint32_t n,
                                                       perceptual, d_out, idx, cnt_d, threshold);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_learned_refit");
   }
+  // blocks above the bound: the exact optimizer on a compacted copy, scattered back. The count
+  // stays on the device: the gather, both encoder kernels and the scatter read it there, so the
+  // call never waits for the host between the proposals and the fallback.
+  if ((e = net->fb_in.ensure((size_t)n * 64)) != cudaSuccess) return cuda_check(e, "alloc fallback blocks");
+  if ((e = net->fb_out.ensure((size_t)n * 8)) != cudaSuccess) return cuda_check(e, "alloc fallback out");
+  const uint32_t sweep = (uint32_t)std::min<uint64_t>(((uint64_t)n * 4 + 255) / 256, 8192);
+  k_gather_idx<<<sweep, 256, 0, s>>>(d_blocks, idx, cnt_d, static_cast<uint8_t*>(net->fb_in.ptr));
+  if ((rc = launch_dxt1_count(static_cast<uint8_t*>(net->fb_in.ptr), n, cnt_d,
+                              dxt1_options(perceptual != 0, true, kDxtQualityUber, false, false, 128),
+                              static_cast<uint8_t*>(net->fb_out.ptr), 8, s)) != CRNGPU_OK)
+    return rc;
+  k_scatter_idx<<<(sweep + 3) / 4, 256, 0, s>>>(static_cast<uint8_t*>(net->fb_out.ptr), idx, cnt_d, d_out);
   uint32_t cnt = 0;
-  if ((e = cudaMemcpyAsync(&cnt, cnt_d, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+  if (fallbacks && (e = cudaMemcpyAsync(&cnt, cnt_d, 4, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
     return cuda_check(e, "read fallback count");
-  if (cnt > n) { set_error("crngpu_dxt1_learned: fallback count out of range"); return CRNGPU_E_DEVICE; }
-  if (fallbacks) *fallbacks = cnt;
-  if (cnt) {
-    // blocks above the bound: the exact optimizer, on a compacted copy, scattered back
-    if ((e = net->fb_in.ensure((size_t)cnt * 64)) != cudaSuccess) return cuda_check(e, "alloc fallback blocks");
-    if ((e = net->fb_out.ensure((size_t)cnt * 8)) != cudaSuccess) return cuda_check(e, "alloc fallback out");
-    k_gather_idx<<<(cnt * 4 + 255) / 256, 256, 0, s>>>(d_blocks, idx, cnt_d, static_cast<uint8_t*>(net->fb_in.ptr));
-    if ((rc = launch_dxt1(static_cast<uint8_t*>(net->fb_in.ptr), cnt,
-                          dxt1_options(perceptual != 0, true, kDxtQualityUber, false, false, 128),
-                          static_cast<uint8_t*>(net->fb_out.ptr), 8, nullptr, s)) != CRNGPU_OK)
-      return rc;
-    k_scatter_idx<<<(cnt + 255) / 256, 256, 0, s>>>(static_cast<uint8_t*>(net->fb_out.ptr), idx, cnt_d, d_out);
-  }
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "learned encode kernels");
-  return check_flag(*net, s);
+  rc = check_flag(*net, s);  // synchronises the stream
+  if (rc != CRNGPU_OK) return rc;
+  if (fallbacks) {
+    if (cnt > n) { set_error("crngpu_dxt1_learned: fallback count out of range"); return CRNGPU_E_DEVICE; }
+    *fallbacks = cnt;
+  }
+  return CRNGPU_OK;
 }
