@@ -558,6 +558,29 @@ def main():
     chain_batch.close()
     h2d_chain, d2h_chain = int(host_chain.numel()), int(host_chain_out.numel())
 
+    # the drop-in path: crn_compress to DDS at quality 255 calls crngpu_compress_dds_clustered with
+    # the host mip chain (upload, GPU gather of every level, one encoder launch, one download)
+    host_chain_np = host_chain.numpy()
+    dds_out = np.zeros(n_blocks * 8, np.uint8)
+    L = cg.lib()
+
+    def drop_in_step():
+        rc = L.crngpu_compress_dds_clustered(host_chain_np.ctypes.data, w0, h0, len(levels), 1, cg.FMT_DXT1, 255,
+                                             cg.FLAG_PERCEPTUAL | cg.FLAG_USE_BOTH_BLOCK_TYPES,
+                                             dds_out.ctypes.data, dds_out.size)
+        if rc < 0:
+            raise cg.CrnGpuError(rc, "crngpu_compress_dds_clustered")
+
+    for _ in range(args.warmup):
+        drop_in_step()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        drop_in_step()
+    drop_in_s = max_over_ranks(world, time.perf_counter() - t0)
+    drop_in_value = world * texels * args.steps / drop_in_s / 1e6
+    drop_in_parity = bool(np.array_equal(dds_out.reshape(-1, 8), d_out.cpu().numpy()))
+
     # ---- learned endpoint proposal (shipped weights) on the same blocks, against the plain result
     from crunch2_gb300 import learned as LR
     net = LR.default_net()
@@ -761,6 +784,11 @@ def main():
                         "grid": chain_grids[0],
                         "path": "pinned host mip chain -> H2D -> crngpu_encode_batch_launch (CUDA graph) -> D2H -> "
                                 "host sync, every step; wall time"},
+                "e2e_drop_in": {"value": round(drop_in_value, 3), "unit": "Mtexel/s",
+                                "h2d_bytes_per_step": h2d_chain, "d2h_bytes_per_step": d2h_chain,
+                                "parity_vs_device_encode": drop_in_parity,
+                                "path": "crngpu_compress_dds_clustered at quality 255 (what crn_compress to DDS calls): "
+                                        "pageable host mip chain in, DDS block data out, one call per step; wall time"},
                 "e2e_per_level": {"value": round(per_level_value, 3), "unit": "Mtexel/s", "h2d_bytes_per_step": h2d,
                                   "d2h_bytes_per_step": d2h,
                                   "path": "crngpu_compress_image per level (11 calls, each synchronous), "
@@ -776,6 +804,7 @@ def main():
             return d
         line["summary"] = {
             "encode_mtexel_s": round(value, 1), "e2e_mtexel_s": round(e2e_value, 1),
+            "e2e_drop_in_mtexel_s": round(drop_in_value, 1),
             "encode_roofline_frac": roofline["frac"],
             "learned_mtexel_s": pick(learned, "value"), "learned_speedup": pick(learned, "speedup_vs_plain"),
             "learned_rmse_delta": pick(learned, "rmse_delta"),

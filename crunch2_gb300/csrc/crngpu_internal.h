@@ -15,7 +15,7 @@ namespace crngpu {
 // the conversions :1267-1311). DXT5_CCxY stores luma in alpha and the JFIF chroma (biased by 123
 // and 125, crnlib/crn_color.h:788-807) in red and green; xGxR / xGBR / AGBR move red to alpha.
 // Texels are RGBA8 with red in the lowest byte. Other formats pass through.
-inline uint32_t cook_texel(uint32_t format, uint32_t px) {
+__host__ __device__ inline uint32_t cook_texel(uint32_t format, uint32_t px) {
   const int r = (int)(px & 255u), g = (int)((px >> 8) & 255u), b = (int)((px >> 16) & 255u), a = (int)(px >> 24);
   auto pack = [](int c0, int c1, int c2, int c3) {
     return (uint32_t)c0 | ((uint32_t)c1 << 8) | ((uint32_t)c2 << 16) | ((uint32_t)c3 << 24);
@@ -113,6 +113,14 @@ int dxt5a_chunks_max_grid();
 // launch_dxt5a: quality sets the probe grid (+-16 Uber, +-8 Better, none below).
 int launch_dxt1(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
                 uint64_t* d_err, cudaStream_t s);
+// dds_comp at quality 255 for a whole texture (host RGBA8 levels, face after face, level after
+// level, tightly packed): every block of every face and level through the plain encoder, output in
+// DDS order at minimal pitch. Returns the output bytes (or the bytes needed when out is NULL or
+// too small) or a CRNGPU_E_* code. `flags` / `quality` / `threshold` as encode_device takes them.
+int64_t dds_plain_chain(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels, uint32_t faces,
+                        uint32_t format, uint32_t flags, uint32_t quality, uint32_t threshold, void* out,
+                        uint64_t out_capacity);
+
 // The same with the block count in device memory (*n_dev <= n_max), so that a caller need not
 // read it back before the launch; the grids are sized for n_max.
 int launch_dxt1_count(const uint8_t* d_blocks, uint32_t n_max, const uint32_t* n_dev, uint32_t opts, uint8_t* d_out,

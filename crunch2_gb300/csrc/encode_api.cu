@@ -3,7 +3,9 @@
 // (dxt_image::init, crnlib/crn_dxt_image.cpp:283-349,447-493).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <vector>
 
 #include "crngpu_internal.h"
 
@@ -38,6 +40,33 @@ __global__ void k_gather_blocks(const uint8_t* __restrict__ img, uint32_t w, uin
     const uint32_t x = min(bx * 4 + (tin & 3), w - 1), y = min(by * 4 + (tin >> 2), h - 1);
     const uint8_t* p = img + (uint64_t)y * pitch + (uint64_t)x * 4;
     out[t] = (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+  }
+}
+
+// Level -> 4x4 blocks as k_gather_blocks, each texel cooked for the target format (cook_texel).
+// Several images (faces and levels) in one launch: job j covers blocks [first[j], first[j + 1]).
+struct GatherImage {
+  uint64_t src;      // byte offset of the image in the uploaded chain
+  uint32_t w, h, bx;
+  uint32_t first;    // first block of the image in the output
+};
+__global__ void k_gather_chain(const uint8_t* __restrict__ chain, const GatherImage* __restrict__ imgs, uint32_t nimg,
+                               uint32_t total_blocks, uint32_t format, uint32_t* __restrict__ out) {
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (uint64_t)total_blocks * 16;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t blk = (uint32_t)(t >> 4), tin = (uint32_t)t & 15;
+    uint32_t lo = 0, hi = nimg - 1;  // the image holding block blk: the last with first <= blk
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (imgs[mid].first <= blk) lo = mid;
+      else hi = mid - 1;
+    }
+    const GatherImage im = imgs[lo];
+    const uint32_t b = blk - im.first, by = b / im.bx, bxx = b - by * im.bx;
+    const uint32_t x = min(bxx * 4 + (tin & 3), im.w - 1), y = min(by * 4 + (tin >> 2), im.h - 1);
+    const uint8_t* p = chain + im.src + ((uint64_t)y * im.w + x) * 4;
+    const uint32_t px = (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+    out[t] = cook_texel(format, px);
   }
 }
 
@@ -126,6 +155,60 @@ int with_buffers(const uint8_t* in, size_t in_bytes, uint8_t* out, size_t out_by
 }
 
 }  // namespace
+
+int64_t dds_plain_chain(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels, uint32_t faces,
+                        uint32_t format, uint32_t flags, uint32_t quality, uint32_t threshold, void* out,
+                        uint64_t out_capacity) {
+  const int bpb = bytes_per_block(format);
+  if (!bpb) { set_error("unsupported format"); return CRNGPU_E_UNSUPPORTED; }
+  if (!rgba_levels || !width || !height || width > 4096 || height > 4096 || !levels || levels > 16 ||
+      (faces != 1 && faces != 6)) {
+    set_error("dds_plain_chain: bad dimensions, level or face count");
+    return CRNGPU_E_PARAM;
+  }
+  uint32_t full = 1;
+  while ((width >> full) || (height >> full)) full++;
+  if (levels > full) { set_error("dds_plain_chain: more levels than the mip chain has"); return CRNGPU_E_PARAM; }
+  // the images in DDS order (face after face, level after level), which is also the input order
+  std::vector<GatherImage> imgs;
+  uint64_t src = 0;
+  uint32_t blocks = 0;
+  for (uint32_t f = 0; f < faces; f++)
+    for (uint32_t l = 0; l < levels; l++) {
+      const uint32_t w = std::max(1u, width >> l), h = std::max(1u, height >> l);
+      const uint32_t bx = (w + 3) / 4, by = (h + 3) / 4;
+      imgs.push_back(GatherImage{src, w, h, bx, blocks});
+      src += (uint64_t)w * h * 4;
+      blocks += bx * by;
+    }
+  const uint64_t need = (uint64_t)blocks * bpb;
+  if (!out || out_capacity < need) return (int64_t)need;
+  cudaStream_t s = nullptr;
+  cudaError_t e;
+  DevBuf& chain = staging(4);
+  DevBuf& table = staging(5);
+  DevBuf& gathered = staging(6);
+  DevBuf& encoded = staging(7);
+  if ((e = chain.ensure(src)) != cudaSuccess || (e = table.ensure(sizeof(GatherImage) * imgs.size())) != cudaSuccess ||
+      (e = gathered.ensure((size_t)blocks * 64)) != cudaSuccess || (e = encoded.ensure(need)) != cudaSuccess)
+    return cuda_check(e, "alloc chain buffers");
+  if ((e = cudaMemcpyAsync(chain.ptr, rgba_levels, src, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+      (e = cudaMemcpyAsync(table.ptr, imgs.data(), sizeof(GatherImage) * imgs.size(), cudaMemcpyHostToDevice, s)) !=
+          cudaSuccess)
+    return cuda_check(e, "upload chain");
+  const uint64_t texels = (uint64_t)blocks * 16;
+  const uint32_t grid = (uint32_t)std::min<uint64_t>((texels + 255) / 256, 65535);
+  k_gather_chain<<<grid, 256, 0, s>>>(static_cast<const uint8_t*>(chain.ptr), static_cast<const GatherImage*>(table.ptr),
+                                      (uint32_t)imgs.size(), blocks, format, static_cast<uint32_t*>(gathered.ptr));
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_gather_chain");
+  int rc = encode_device(static_cast<const uint8_t*>(gathered.ptr), blocks, format, flags, quality, threshold,
+                         static_cast<uint8_t*>(encoded.ptr), nullptr, s);
+  if (rc != CRNGPU_OK) return rc;
+  if ((e = cudaMemcpyAsync(out, encoded.ptr, need, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return cuda_check(e, "copy result");
+  return (int64_t)need;
+}
 
 }  // namespace crngpu
 

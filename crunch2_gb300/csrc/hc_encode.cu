@@ -3380,6 +3380,21 @@ extern "C" int64_t crngpu_compress_dds_clustered_ex(const uint8_t* rgba_levels, 
     set_error("crngpu_compress_dds_clustered: DXT1A transparency below quality 255 (qdxt1 with alpha) is not built");
     return CRNGPU_E_UNSUPPORTED;
   }
+  if (quality_level >= 255) {
+    // dds_comp at quality 255 (crnlib/crn_dds_comp.cpp:150-157): the plain encoder on every block
+    // of the cooked source -- uploaded once, gathered on the GPU, one encoder launch for the chain
+    uint32_t q = kDxtQualityUber, thr = 128;
+    if (options) {
+      if (options->struct_size != sizeof(crngpu_block_options) || options->dxt_quality > kDxtQualityUber ||
+          options->dxt1a_alpha_threshold > 255) {
+        set_error("bad crngpu_block_options");
+        return CRNGPU_E_PARAM;
+      }
+      q = options->dxt_quality;
+      thr = options->dxt1a_alpha_threshold;
+    }
+    return dds_plain_chain(rgba_levels, width, height, levels, faces, format, flags, q, thr, out, out_capacity);
+  }
   CrnSource src;
   int rc = src.prepare(rgba_levels, width, height, levels, faces, format, flags, "crngpu_compress_dds_clustered");
   if (rc != CRNGPU_OK) return rc;
