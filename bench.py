@@ -436,7 +436,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--skip", default="", help="comma-separated legs to leave out of the run (their keys are "
-                                               "null): clustered, clustered_2048, mixed, mips")
+                                               "null): clustered, clustered_2048, mixed, mips, config4")
     args = ap.parse_args()
     skip = set(x for x in args.skip.split(",") if x)
     args.warmup = max(args.warmup, 3)
@@ -609,6 +609,22 @@ def main():
                "path": "crngpu_dxt1_learned: fused MLP (k_mlp_infer) + refit (k_learned_refit) + exact "
                        "optimizer on fallback blocks; one host sync per call"}
     del net
+
+    # ---- config 4's evaluation: the shipped weights on 32 held-out 4096x4096 textures (a seed
+    # range the training never saw), learned vs plain encode time and RGB RMSE per texture
+    config4_eval = None
+    if "config4" not in skip:
+        r4 = LR.config4(weights=LR.WEIGHTS, eval_textures=32, eval_size=4096, threshold=LR.DEFAULT_THRESHOLD)
+        g4 = r4["learned"][0]
+        config4_eval = {"textures": r4["eval_textures"], "size": r4["eval_size"], "blocks": r4["eval_blocks"],
+                        "plain_mtexel_s": round(r4["plain_mtexel_s"], 1),
+                        "learned_mtexel_s": round(g4["learned_mtexel_s"], 1), "speedup": round(g4["speedup"], 3),
+                        "rmse_plain": round(r4["rmse_plain"], 4), "rmse_learned": round(g4["rmse_learned"], 4),
+                        "rmse_delta": round(g4["rmse_learned"] - r4["rmse_plain"], 4),
+                        "fallback_frac": round(g4["fallback_frac"], 4), "threshold": LR.DEFAULT_THRESHOLD,
+                        "path": "learned.config4(weights=shipped): per texture, crngpu_dxt1_optimize_batch and "
+                                "crngpu_dxt1_learned on device blocks, CUDA events"}
+        learned["config4_eval"] = config4_eval
 
     # ---- CRN -> DXT1 transcode: a batch of TX_BATCH textures (each its own context, i.e. its own
     # tables and palettes, holding the reference-encoded .crn of the same texture, q128, 11 levels)
@@ -808,6 +824,8 @@ def main():
             "encode_roofline_frac": roofline["frac"],
             "learned_mtexel_s": pick(learned, "value"), "learned_speedup": pick(learned, "speedup_vs_plain"),
             "learned_rmse_delta": pick(learned, "rmse_delta"),
+            "config4_learned_speedup": pick(learned, "config4_eval", "speedup"),
+            "config4_rmse_delta": pick(learned, "config4_eval", "rmse_delta"),
             "transcode_batch_gb_s": transcode["value"], "transcode_single_ms": transcode["single_texture"]["ms"],
             "transcode_single_cpu_1_thread_ms": pick(transcode, "single_texture", "cpu_1_thread_ms"),
             "transcode_dxt5_2048_ms": transcode["single_texture"]["dxt5_2048_ms"],

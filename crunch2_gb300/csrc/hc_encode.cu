@@ -3414,13 +3414,7 @@ extern "C" int64_t crngpu_compress_dds_clustered_ex(const uint8_t* rgba_levels, 
     case CRNGPU_FMT_DXN_YX: elems = {{CRNGPU_FMT_DXT5A, 1, 0}, {CRNGPU_FMT_DXT5A, 0, 8}}; break;
     default: elems = {{CRNGPU_FMT_DXT5A, 3, 0}, {CRNGPU_FMT_DXT1, 0, 8}}; break;  // the DXT5 family
   }
-  if (quality_level >= 255) {
-    // dds_comp at quality 255 (crnlib/crn_dds_comp.cpp:150-157): the plain encoder on every block
-    // of the cooked source (as qdxt1::pack at full quality: every block its own cluster)
-    const int r = crngpu_compress_blocks_ex(static_cast<const uint8_t*>(src.d_in.ptr), N, format, flags, options,
-                                            static_cast<uint8_t*>(src.d_out.ptr), CRNGPU_MEM_DEVICE, nullptr);
-    if (r < 0) return r;
-  } else {
+  {
     // mipmapped_texture::qdxt_pack (crnlib/crn_mipmapped_texture.cpp:2330-2560): qdxt1 on the
     // colour element, qdxt5 on each alpha / DXN element, each with its own tiling and codebooks;
     // element k is written to d_out + k * N * 8 and interleaved below
@@ -3479,7 +3473,7 @@ extern "C" int64_t crngpu_compress_dds_clustered_ex(const uint8_t* rgba_levels, 
   std::vector<uint8_t> dxt((size_t)N * bpb);
   if ((e = cudaMemcpy(dxt.data(), src.d_out.ptr, dxt.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
     return cuda_check(e, "copy result");
-  if (quality_level < 255 && elems.size() == 2) {  // element planes -> 16-byte blocks
+  if (elems.size() == 2) {  // element planes -> 16-byte blocks
     std::vector<uint8_t> planes(dxt);
     for (uint32_t b = 0; b < N; b++)
       for (size_t k = 0; k < 2; k++)

@@ -126,3 +126,16 @@ def test_trained_network_beats_untrained(L, trained):
           "untrained", res["untrained"])
     assert res["trained"][2] < res["untrained"][2]      # better proposals before any fallback
     assert res["trained"][1] < res["untrained"][1]      # fewer blocks need the exact optimizer
+
+
+def test_shipped_network_on_held_out_textures(L):
+    """Config 4's evaluation at a reduced size: the shipped weights on two held-out 2048 x 2048
+    textures from config 4's evaluation seed range, at config 4's fallback threshold (1.5): RGB
+    RMSE within 0.1 of the plain optimizer's, and faster than the plain optimizer. (bench.py runs
+    the full 32 x 4096^2 evaluation.)"""
+    r = L.config4(weights=L.WEIGHTS, eval_textures=2, eval_size=2048, threshold=L.DEFAULT_THRESHOLD)
+    got = r["learned"][0]
+    print({k: r[k] for k in ("plain_mtexel_s", "rmse_plain")}, got)
+    assert got["rmse_learned"] - r["rmse_plain"] <= 0.1
+    assert got["speedup"] > 2.0
+    assert 0.0 < got["fallback_frac"] < 0.25

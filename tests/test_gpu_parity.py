@@ -355,3 +355,33 @@ def test_dxt1_full_1024_mip_chain_against_oracle(cg):
         ofs += n
     frac = check_dxt1(got, ref, blocks, True)
     print(f"1024 chain: {frac:.5f} of {got.shape[0]} blocks identical to the oracle")
+
+
+def test_transcode_batch_of_own_files_matches_oracle(cg):
+    """Files this library writes (crngpu_compress_crn) in the shapes of config 3's mixed batch --
+    non-square sizes from 32 to 512, full mip chains, DXT1 / DXT5 / DXN_XY / DXT5A -- decoded in one
+    batch (the plan's split sends the larger levels to the wide decoder), every level against the
+    oracle's CPU restatement of crnd's unpacker (pinned to the reference's transcodes)."""
+    from crunch2_gb300 import texgen
+    from oracle import port
+    shapes = [(512, 256, cg.FMT_DXT1), (256, 512, cg.FMT_DXT5), (512, 512, cg.FMT_DXN_XY), (128, 32, cg.FMT_DXT1),
+              (32, 256, cg.FMT_DXT5A), (512, 128, cg.FMT_DXT5)]
+    files = []
+    for i, (w, h, fmt) in enumerate(shapes):
+        img = texgen.normal_map(w, h, 700 + i) if fmt == cg.FMT_DXN_XY else \
+            texgen.colour_texture(w, h, 700 + i, with_alpha_noise=fmt in (cg.FMT_DXT5, cg.FMT_DXT5A))
+        files.append(cg.compress_crn([texgen.mip_chain(img)], fmt=fmt, quality=128))
+    ctxs = [cg.unpack_begin(f) for f in files]
+    outs = [torch.zeros(sum(c.level_bytes(l) for l in range(c.levels)), dtype=torch.uint8, device="cuda") for c in ctxs]
+    with cg.UnpackBatch([(c, 0, c.levels, o) for c, o in zip(ctxs, outs)]) as batch:
+        batch.launch()
+        batch.status()
+    for f, c, o in zip(files, ctxs, outs):
+        host = o.cpu().numpy()
+        pos = 0
+        for lvl in range(c.levels):
+            n = c.level_bytes(lvl)
+            want = port.unpack_level(f, lvl, n)
+            assert want is not None and np.array_equal(host[pos:pos + n], want), (c.width, c.height, lvl)
+            pos += n
+        c.close()
