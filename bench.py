@@ -812,7 +812,7 @@ def main():
                 "learned": learned, "transcode": transcode, "clustered": clustered, "clustered_dds": qdxt,
                 "clustered_2048": clustered_2048, "mixed_batch": mixed_batch, "mips": mips, "roofline": roofline,
                 "cpu_baseline": cpu,
-                "gpu_launches": args.steps * 1, "clocks": clk, "wall_s_timed": round(wall, 4)}
+                "gpu_launches": args.steps * 2, "clocks": clk, "wall_s_timed": round(wall, 4)}
         # compact figures of every leg, last, so that a truncated log still carries them
         def pick(d, *keys):
             for k in keys:

@@ -1,10 +1,12 @@
 // Library-wide pieces of the C ABI: version, last-error text, device buffers.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <mutex>
 #include <string>
 
 #include "crngpu_internal.h"
+#include "host_alloc.h"
 
 namespace crngpu {
 
@@ -59,11 +61,60 @@ void DevBuf::release() {
   device = -1;
 }
 
+// Host allocation hooks of the transcoder's state (host_alloc.h). Each allocation carries a
+// 16-byte header with the hooks that made it, so it is always freed by the same allocator.
+namespace {
+struct HostHooks {
+  HostReallocFn realloc_fn = nullptr;
+  HostMsizeFn msize_fn = nullptr;
+  void* user = nullptr;
+};
+std::mutex g_host_mu;
+HostHooks g_host;
+struct alignas(16) AllocHeader {
+  HostReallocFn fn;
+  void* user;
+};
+}  // namespace
+
 // Staging buffers for host-memory calls; one set per host thread so concurrent callers on
 // different threads never share them.
 DevBuf& staging(int slot) {
   thread_local DevBuf bufs[8];
   return bufs[slot & 7];
+}
+
+void set_host_hooks(HostReallocFn realloc_fn, HostMsizeFn msize_fn, void* user) {
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  g_host = (realloc_fn && msize_fn) ? HostHooks{realloc_fn, msize_fn, user} : HostHooks{};
+}
+
+void* host_alloc(size_t bytes) {
+  HostHooks h;
+  {
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    h = g_host;
+  }
+  const size_t total = bytes + sizeof(AllocHeader);
+  void* p = nullptr;
+  if (h.realloc_fn) {
+    size_t actual = 0;
+    p = h.realloc_fn(nullptr, total, &actual, true, h.user);
+  } else {
+    p = std::malloc(total);
+  }
+  if (!p) return nullptr;
+  AllocHeader* hd = static_cast<AllocHeader*>(p);
+  hd->fn = h.realloc_fn;
+  hd->user = h.user;
+  return hd + 1;
+}
+
+void host_free(void* q) {
+  if (!q) return;
+  AllocHeader* hd = static_cast<AllocHeader*>(q) - 1;
+  if (hd->fn) hd->fn(hd, 0, nullptr, true, hd->user);
+  else std::free(hd);
 }
 
 }  // namespace crngpu

@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include "host_alloc.h"
+
 namespace crngpu {
 
 // Canonical-prefix decode table in the layout the device decoder reads (one contiguous POD
@@ -26,11 +28,11 @@ struct DevModel {
 
 // Host copy of a received model (code lengths) + the device table built from it.
 struct Model {
-  std::vector<uint8_t> sizes;
+  HVec<uint8_t> sizes;
   bool used = false;
   // host decode helpers (palettes are decoded on the host)
   uint32_t first[kMaxCodeLen + 1] = {}, count[kMaxCodeLen + 1] = {}, offset[kMaxCodeLen + 1] = {};
-  std::vector<uint16_t> sorted;
+  HVec<uint16_t> sorted;
   bool build();
   void to_device(DevModel& d) const;
 };
@@ -52,8 +54,8 @@ struct CrnFile {
   Kind kind = Kind::DXT1;
   LevelInfo level[16];
   Model ref_dm, ep_dm[2], sel_dm[2];
-  std::vector<uint32_t> colour_ep, colour_sel;
-  std::vector<uint16_t> alpha_ep, alpha_sel;  // alpha_sel: 3 uint16 per entry
+  HVec<uint32_t> colour_ep, colour_sel;
+  HVec<uint16_t> alpha_ep, alpha_sel;  // alpha_sel: 3 uint16 per entry
   std::string error;
 
   // Validates the header (crnd_get_header, inc/crn_decomp.h:2657-2670), receives the five

@@ -27,6 +27,7 @@
 
 #include "crn_file.h"
 #include "crngpu_internal.h"
+#include "host_alloc.h"
 
 namespace crngpu {
 
@@ -1375,7 +1376,7 @@ std::atomic<int> g_expand_variant[64] = {};
 // ------------------------------------------------------------------------------------------
 // Host side.
 
-struct UnpackContext {
+struct UnpackContext : HostObject {
   uint32_t magic = 0x43524E47u;
   int device = -1;
   CrnFile file;
@@ -1393,13 +1394,13 @@ bool valid_ctx(const UnpackContext* c) { return c && c->magic == 0x43524E47u; }
 
 // Palettes in the device layout, packed back to back with 16-byte alignment. `base` is the
 // device address the image will be copied to; returns the image and fills *pal.
-std::vector<uint8_t> palette_image(const CrnFile& F, uint8_t* base, DevPalettes* pal) {
+HVec<uint8_t> palette_image(const CrnFile& F, uint8_t* base, DevPalettes* pal) {
   auto al = [](size_t v) { return (v + 15) & ~(size_t)15; };
   const size_t n_cep = F.colour_ep.size(), n_csel = F.colour_sel.size();
   const size_t n_aep = F.alpha_ep.size(), n_asel = F.alpha_sel.size() / 3;
   const size_t o_csel = al(n_cep * 4), o_asel = o_csel + al(n_csel * 4), o_aep = o_asel + al(n_asel * 8);
   const size_t total = o_aep + al(n_aep * 2) + 16;
-  std::vector<uint8_t> host(total, 0);
+  HVec<uint8_t> host(total, 0);
   if (n_cep) std::memcpy(host.data(), F.colour_ep.data(), n_cep * 4);
   if (n_csel) std::memcpy(host.data() + o_csel, F.colour_sel.data(), n_csel * 4);
   for (size_t i = 0; i < n_asel; i++) {
@@ -1425,8 +1426,8 @@ size_t palette_bytes(const CrnFile& F) {
          al(F.alpha_ep.size() * 2) + 16;
 }
 
-std::vector<DevModel> model_image(const CrnFile& F) {
-  std::vector<DevModel> models(kNumModels);
+HVec<DevModel> model_image(const CrnFile& F) {
+  HVec<DevModel> models(kNumModels);
   F.ref_dm.to_device(models[kMRef]);
   F.ep_dm[0].to_device(models[kMEp0]);
   F.sel_dm[0].to_device(models[kMSel0]);
@@ -1443,13 +1444,13 @@ int upload_context(UnpackContext* c, const uint8_t* data, uint32_t size) {
   if ((e = c->d_file.ensure(size + 64)) != cudaSuccess) return cuda_check(e, "alloc file");
   if ((e = cudaMemcpy(c->d_file.ptr, data, size, cudaMemcpyHostToDevice)) != cudaSuccess)
     return cuda_check(e, "copy file");
-  std::vector<DevModel> models = model_image(F);
+  HVec<DevModel> models = model_image(F);
   if ((e = c->d_models.ensure(sizeof(DevModel) * kNumModels)) != cudaSuccess) return cuda_check(e, "alloc models");
   if ((e = cudaMemcpy(c->d_models.ptr, models.data(), sizeof(DevModel) * kNumModels, cudaMemcpyHostToDevice)) !=
       cudaSuccess)
     return cuda_check(e, "copy models");
   if ((e = c->d_pal.ensure(palette_bytes(F))) != cudaSuccess) return cuda_check(e, "alloc palettes");
-  std::vector<uint8_t> img = palette_image(F, static_cast<uint8_t*>(c->d_pal.ptr), &c->pal);
+  HVec<uint8_t> img = palette_image(F, static_cast<uint8_t*>(c->d_pal.ptr), &c->pal);
   if ((e = cudaMemcpy(c->d_pal.ptr, img.data(), img.size(), cudaMemcpyHostToDevice)) != cudaSuccess)
     return cuda_check(e, "copy palettes");
   if ((e = c->d_status.ensure(16)) != cudaSuccess) return cuda_check(e, "alloc status");
@@ -1473,7 +1474,7 @@ struct LevelTask {
 // Launch plan: jobs image [TexJob x n_item][StreamJob x n_stream][ExpandJob x n_expand],
 // built on the host. Tasks with the same `item` (consecutive) form one texture job.
 struct Plan {
-  std::vector<uint8_t> image;
+  HVec<uint8_t> image;
   uint32_t n_item = 0, n_stream = 0, n_expand = 0, ctas = 0;
   uint32_t n_wide = 0;      // level streams for k_crn_decode_wide (one CTA each, largest first)
   uint32_t wide_smem = 0;   // its dynamic shared memory (the largest format's layout)
@@ -1516,14 +1517,14 @@ bool wide_eligible(const LevelTask& t) {
 // finishes when its queue drains, but never before its largest level. The two run one after the
 // other on the caller's stream. With the levels sorted by cost, the first k go wide for the k that
 // minimises wide time + lane time of level k + 1.
-std::vector<bool> decide_wide(const std::vector<LevelTask>& tasks, uint32_t wide_slots) {
-  std::vector<bool> wide(tasks.size(), false);
+HVec<bool> decide_wide(const HVec<LevelTask>& tasks, uint32_t wide_slots) {
+  HVec<bool> wide(tasks.size(), false);
   const uint32_t fixed = g_wide_min_blocks.load(std::memory_order_relaxed);
   if (fixed) {
     for (size_t i = 0; i < tasks.size(); i++) wide[i] = wide_eligible(tasks[i]) && task_blocks(tasks[i]) >= fixed;
     return wide;
   }
-  std::vector<std::pair<double, size_t>> cost;  // lane cost, task
+  HVec<std::pair<double, size_t>> cost;  // lane cost, task
   double lane_rest = 0;                         // longest lane stream among the ineligible ones
   for (size_t i = 0; i < tasks.size(); i++) {
     const double w = (tasks[i].file->kind == Kind::DXT5 || tasks[i].file->kind == Kind::DXN) ? 2.0 : 1.0;
@@ -1550,11 +1551,11 @@ std::vector<bool> decide_wide(const std::vector<LevelTask>& tasks, uint32_t wide
 
 // false if a texture job would not fit the decoder (more than 32 levels or rows too wide).
 // `wide_slots`: CTAs of k_crn_decode_wide resident at once on the device (wide_slots()).
-bool make_plan(const std::vector<LevelTask>& tasks, Plan& p, uint32_t wide_slots) {
-  std::vector<TexJob> items;
-  std::vector<std::vector<StreamJob>> item_streams;
-  std::vector<StreamJob> wide;
-  const std::vector<bool> to_wide = decide_wide(tasks, wide_slots);
+bool make_plan(const HVec<LevelTask>& tasks, Plan& p, uint32_t wide_slots) {
+  HVec<TexJob> items;
+  HVec<HVec<StreamJob>> item_streams;
+  HVec<StreamJob> wide;
+  const HVec<bool> to_wide = decide_wide(tasks, wide_slots);
   for (size_t i = 0; i < tasks.size();) {
     size_t k = i;
     while (k < tasks.size() && tasks[k].item == tasks[i].item) k++;
@@ -1564,7 +1565,7 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p, uint32_t wide_slots
     TexJob T{};
     T.models = tasks[i].models;
     T.kind = kind;
-    std::vector<StreamJob> sj;
+    HVec<StreamJob> sj;
     uint32_t rb = 0;
     for (size_t t = i; t < k; t++) {
       const LevelInfo& li = F.level[tasks[t].level];
@@ -1609,19 +1610,19 @@ bool make_plan(const std::vector<LevelTask>& tasks, Plan& p, uint32_t wide_slots
   });
   for (const StreamJob& j : wide) p.wide_smem = std::max(p.wide_smem, wide_layout(models_used(j.kind)).total);
   // largest textures first: the persistent warps then finish at about the same time
-  std::vector<size_t> order(items.size());
+  HVec<size_t> order(items.size());
   for (size_t i = 0; i < order.size(); i++) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return items[a].work > items[b].work; });
-  std::vector<TexJob> it_sorted;
-  std::vector<StreamJob> sj;
+  HVec<TexJob> it_sorted;
+  HVec<StreamJob> sj;
   for (size_t o : order) {
     TexJob T = items[o];
     T.first = (uint32_t)sj.size();
     it_sorted.push_back(T);
     sj.insert(sj.end(), item_streams[o].begin(), item_streams[o].end());
   }
-  std::vector<ExpandJob> ej;
-  std::vector<uint2> tiles[kTileSizes];
+  HVec<ExpandJob> ej;
+  HVec<uint2> tiles[kTileSizes];
   for (const LevelTask& t : tasks) {
     const CrnFile& F = *t.file;
     const LevelInfo& li = F.level[t.level];
@@ -1785,7 +1786,7 @@ int status_to_rc(uint32_t st) {
 
 // Decodes and expands a list of levels of one context (destinations device memory), then
 // reads the status word back (synchronises `s`).
-int run_levels(UnpackContext* c, std::vector<LevelTask>& tasks, cudaStream_t s) {
+int run_levels(UnpackContext* c, HVec<LevelTask>& tasks, cudaStream_t s) {
   // one record buffer for all levels, each level's records starting on a 16-byte boundary
   uint64_t rec = 0;
   for (LevelTask& t : tasks) rec += (level_records(c->file, t.level) * c->rec_bytes() + 15) & ~(uint64_t)15;
@@ -1871,7 +1872,7 @@ int unpack_one(UnpackContext* c, const uint8_t* host_src, const uint8_t* dev_src
         if ((e = cudaMemcpyAsync(t.dst[f], dst_faces[f], face_bytes, cudaMemcpyHostToDevice, s)) != cudaSuccess)
           return cuda_check(e, "stage output");
   }
-  std::vector<LevelTask> tasks{t};
+  HVec<LevelTask> tasks{t};
   int rc = run_levels(c, tasks, s);
   if (rc != CRNGPU_OK) return rc;
   if (out_stage) {
@@ -1893,7 +1894,7 @@ uint64_t levels_bytes(const CrnFile& F, uint32_t first, uint32_t count) {
 
 // Level tasks writing levels [first, first + count) back to back at `out` (minimal pitch).
 void levels_tasks(UnpackContext* c, uint32_t first, uint32_t count, uint8_t* out, uint32_t item,
-                  std::vector<LevelTask>& tasks) {
+                  HVec<LevelTask>& tasks) {
   const CrnFile& F = c->file;
   uint64_t ofs = 0;
   for (uint32_t l = first; l < first + count; l++) {
@@ -1930,7 +1931,7 @@ int expand_wait_counters(uint32_t out[2], bool reset) {
 // A prepared batch: many levels of many contexts, decoded by one persistent launch and expanded
 // by one more. The job tables and record buffer are uploaded/allocated once at creation, so a
 // launch only enqueues a memset and two kernels (and can replay as a CUDA graph).
-struct UnpackBatch {
+struct UnpackBatch : HostObject {
   uint32_t magic = 0x42415443u;
   int device = -1;
   Plan plan;
@@ -2013,7 +2014,7 @@ extern "C" int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t firs
     if ((e = stage->ensure(total)) != cudaSuccess) return cuda_check(e, "alloc output stage");
     out = static_cast<uint8_t*>(stage->ptr);
   }
-  std::vector<LevelTask> tasks;
+  HVec<LevelTask> tasks;
   levels_tasks(c, first_level, level_count, out, 0, tasks);
   int rc = run_levels(c, tasks, s);
   if (rc != CRNGPU_OK) return rc;
@@ -2031,7 +2032,7 @@ extern "C" crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_ba
   std::unique_ptr<UnpackBatch> b(new UnpackBatch());
   cudaError_t e = cudaGetDevice(&b->device);
   if (e != cudaSuccess) { cuda_check(e, "cudaGetDevice"); return nullptr; }
-  std::vector<LevelTask> tasks;
+  HVec<LevelTask> tasks;
   uint64_t rec = 0;
   for (uint32_t i = 0; i < n; i++) {
     UnpackContext* c = reinterpret_cast<UnpackContext*>(items[i].ctx);
@@ -2312,9 +2313,9 @@ extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_si
   cudaStream_t s = as_stream(stream);
   cudaError_t e;
   // host images of the tables, palettes and launch descriptors (ordinary heap, copied below)
-  std::vector<DevModel> models = model_image(F);
+  HVec<DevModel> models = model_image(F);
   DevPalettes pal;
-  std::vector<uint8_t> pal_img = palette_image(F, base + o_pal, &pal);
+  HVec<uint8_t> pal_img = palette_image(F, base + o_pal, &pal);
   LevelTask t{};
   t.file = &F;
   t.models = reinterpret_cast<const DevModel*>(base + o_models);

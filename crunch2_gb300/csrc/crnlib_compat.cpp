@@ -26,6 +26,7 @@
 
 #include "../../include/crnlib_compat.h"
 #include "crn_file.h"
+#include "host_alloc.h"
 #include "crngpu_internal.h"
 
 namespace {
@@ -374,7 +375,7 @@ void* compress_with_mips(const crn_comp_params& cp, const crn_mipmap_params& mp,
 // ---------------------------------------------------------------------------------------------
 // Transcoder contexts
 
-struct CrndContext {
+struct CrndContext : crngpu::HostObject {
   uint32_t magic;
   crngpu_unpack_context ctx;
   const void* data;
@@ -579,7 +580,12 @@ int crn_get_version_patch() { return 0; }
 
 namespace crnd {
 
-void crnd_set_memory_callbacks(crnd_realloc_func, crnd_msize_func, void*) {}
+// The transcoder's host state (contexts, parsed files, palettes, launch plans, batches) is
+// allocated through these hooks from then on, as crnd's is (inc/crn_decomp.h:2440-2459). Device
+// memory is the CUDA runtime's; the reference has none.
+void crnd_set_memory_callbacks(crnd_realloc_func pRealloc, crnd_msize_func pMSize, void* pUser_data) {
+  crngpu::set_host_hooks(pRealloc, pMSize, pUser_data);
+}
 
 uint32 crnd_crn_format_to_fourcc(crn_format fmt) { return format_fourcc(fmt); }
 
@@ -668,7 +674,7 @@ crnd_unpack_context crnd_unpack_begin(const void* pData, uint32 data_size) {
   if (!pData || data_size < kHeaderMin) return nullptr;
   crngpu_unpack_context ctx = crngpu_unpack_begin(pData, data_size);
   if (!ctx) return nullptr;
-  CrndContext* c = new (std::nothrow) CrndContext{kCrndMagic, ctx, pData, data_size};
+  CrndContext* c = new (std::nothrow) CrndContext{{}, kCrndMagic, ctx, pData, data_size};
   if (!c) crngpu_unpack_end(ctx);
   return c;
 }

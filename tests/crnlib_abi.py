@@ -78,6 +78,8 @@ SYMBOLS = {
     "crn_compress_mips": ("_Z12crn_compressRK15crn_comp_paramsRK17crn_mipmap_paramsRjPjPf", vp, [vp, vp, vp, vp, vp]),
     "crn_free_block": ("_Z14crn_free_blockPv", None, [vp]),
     "crn_set_memory_callbacks": ("_Z24crn_set_memory_callbacksPFPvS_mPmbS_EPFmS_S_ES_", None, [REALLOC, MSIZE, vp]),
+    "crnd_set_memory_callbacks": ("_ZN4crnd25crnd_set_memory_callbacksEPFPvS0_mPmbS0_EPFmS0_S0_ES0_", None,
+                                  [REALLOC, MSIZE, vp]),
     "crn_decompress_crn_to_dds": ("_Z25crn_decompress_crn_to_ddsPKvRj", vp, [vp, vp]),
     "crn_create_block_compressor": ("_Z27crn_create_block_compressorRK15crn_comp_params", vp, [vp]),
     "crn_compress_block": ("_Z18crn_compress_blockPvPKjS_", None, [vp, vp, vp]),

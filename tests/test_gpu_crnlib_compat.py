@@ -225,6 +225,56 @@ def test_crnd_unpack_matches_golden_host_and_device(api, name):
     assert not api.crnd_unpack_level(None, None, 0, 0, 0)
 
 
+def test_crnd_memory_hooks_carry_the_transcoder_state(api):
+    """crnd_set_memory_callbacks: the transcoder's host state -- context, parsed header, models,
+    palettes, launch plans -- is allocated through the caller's hooks, as crnd's is; crnd_unpack_end
+    returns all of it, and the output does not change."""
+    name = "dxt5_256"
+    m = G.manifest()[name]
+    crn = G.crn_bytes(name)
+    live, calls = {}, {"alloc": 0, "free": 0, "bytes": 0}
+
+    @A.REALLOC
+    def realloc(ptr, size, actual, movable, user):
+        if not ptr:
+            b = ctypes.create_string_buffer(size)
+            live[ctypes.addressof(b)] = b
+            calls["alloc"] += 1
+            calls["bytes"] += size
+            if actual:
+                actual[0] = size
+            return ctypes.addressof(b)
+        if size == 0:
+            calls["free"] += 1
+            live.pop(ptr, None)
+        return None
+
+    @A.MSIZE
+    def msize(ptr, user):
+        return ctypes.sizeof(live[ptr]) if ptr in live else 0
+
+    buf = ctypes.create_string_buffer(crn, len(crn))
+    api.crnd_set_memory_callbacks(realloc, msize, None)
+    try:
+        ctx = api.crnd_unpack_begin(buf, len(crn))
+        assert ctx and calls["alloc"] > 0
+        begun = calls["alloc"]
+        bpb = G.bytes_per_block(m["format"])
+        for l, L in enumerate(m["levels"]):
+            w, h = max(1, m["width"] >> l), max(1, m["height"] >> l)
+            face_bytes = ((w + 3) // 4) * bpb * ((h + 3) // 4)
+            out = np.zeros(face_bytes, np.uint8)
+            ptrs = (ctypes.c_void_p * 6)(out.ctypes.data)
+            assert api.crnd_unpack_level(ctx, ptrs, face_bytes, 0, l)
+            assert G.sha(out) == L["sha256"], l
+        assert calls["alloc"] > begun  # each call's launch plan too
+        assert api.crnd_unpack_end(ctx)
+    finally:
+        api.crnd_set_memory_callbacks(A.REALLOC(0), A.MSIZE(0), None)
+    print(calls)
+    assert calls["alloc"] == calls["free"] and not live
+
+
 def test_crn_compress_crn_is_the_c_abi_file(api):
     import crunch2_gb300 as cg
     fl = texture_levels(128, 128, "colour", 21, 1)
