@@ -865,13 +865,30 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
       uint32_t bad = 0;
       for (uint32_t i = et; i < n; i += kWEmitters) {
         const uint32_t ent = L[i];
-        uint32_t j = (ent & 0x3FFFFFFFu) - a2;
+        const uint32_t j = (ent & 0x3FFFFFFFu) - a2;
         uint32_t r, blk;
         locate(i, r, blk);
+        // A bit reader in registers: acc holds the next `have` stream bits MSB first (17..64 of
+        // them before each decode); a chunk pair is at most 144 bits, so at most three one-word
+        // refills follow the first 64 bits. Refill k brings bits [j + 64 + 32k, + 32), which start
+        // at word wi = j / 32 + 2 + k with the item's own offset sh inside it.
+        uint32_t wi = j >> 5;
+        const uint32_t sh = j & 31u;
+        uint64_t acc = (((uint64_t)wd[wi] << 32) | wd[wi + 1]) << sh;
+        if (sh) acc |= (uint64_t)(wd[wi + 2] >> (32 - sh));
+        int have = 64;
+        wi += 2;
         auto dec = [&](const uint32_t* lut, uint32_t slot, const DevModel* m, const uint16_t* st, uint32_t st_n) {
+          if (have <= 32) {
+            const uint32_t bits = sh ? (uint32_t)(((((uint64_t)wd[wi] << 32) | wd[wi + 1]) << sh) >> 32) : wd[wi];
+            acc |= (uint64_t)bits << (32 - have);
+            have += 32;
+            wi += 1;
+          }
           uint32_t len;
-          const uint32_t sym = code_sym(window_bits(wd, j) >> 16, lut, S.aux[slot], m, st, st_n, len, bad);
-          j += len;
+          const uint32_t sym = code_sym((uint32_t)(acc >> 48), lut, S.aux[slot], m, st, st_n, len, bad);
+          acc <<= len;
+          have -= (int)len;
           return sym;
         };
         auto block = [&](uint32_t ref, uint32_t k) {
