@@ -63,6 +63,8 @@ struct GemmArgs {
   const float* bias;     // per column
   int ldc;
   uint32_t* err;         // set to 1 if an mbarrier wait timed out
+  int kslice;            // split K: CTA z covers K columns [z * kslice, (z + 1) * kslice) (0: all of K)
+  float* part;           // split K: CTA z writes its raw partial tile to part + z * M * N (row-major, N)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -92,12 +94,14 @@ __device__ __forceinline__ float gelu_grad(float x) {
 __device__ __forceinline__ float load_op(const Operand& o, int row, int k, int rows, int ks) {
   if (row >= rows || k >= ks) return 0.f;
   switch (o.kind) {
-    case OP_F32: return reinterpret_cast<const float*>(o.p)[row * o.s_row + k * o.s_k];
-    case OP_BF16: return __bfloat162float(reinterpret_cast<const __nv_bfloat16*>(o.p)[row * o.s_row + k * o.s_k]);
+    // read-only inputs of the product: non-coherent loads, which the compiler may also move ahead of
+    // the shared-memory stores of the staging loop
+    case OP_F32: return __ldg(reinterpret_cast<const float*>(o.p) + row * o.s_row + k * o.s_k);
+    case OP_BF16: return __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(o.p) + row * o.s_row + k * o.s_k));
     default: {
       const int s = o.pix_sample_is_row ? row : k, f = o.pix_sample_is_row ? k : row;
       const uint8_t* px = reinterpret_cast<const uint8_t*>(o.p);
-      return (float)px[(long long)s * 64 + (f / 3) * 4 + f % 3] * (1.0f / 255.0f);
+      return (float)__ldg(px + (long long)s * 64 + (f / 3) * 4 + f % 3) * (1.0f / 255.0f);
     }
   }
 }
@@ -119,7 +123,9 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint32_
   return done != 0;
 }
 
-// C tile (blockIdx.x: 128 rows of M, blockIdx.y: BN columns of N) = A x B^T over all of K.
+// C tile (blockIdx.x: 128 rows of M, blockIdx.y: BN columns of N) = A x B^T over all of K, or --
+// split K, for products whose M x N has few tiles but whose K is the batch -- over the slice of K
+// of blockIdx.z, written raw to g.part for k_splitk_sum.
 template <int BN>
 __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
   __shared__ __align__(1024) unsigned char sa[BM * BK * 2];
@@ -141,23 +147,33 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
   const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
   uint32_t phase = 0;
   bool ok = true;
-  const int nk = (g.K + BK - 1) / BK;
+  const int kbeg = g.kslice ? (int)blockIdx.z * g.kslice : 0;
+  const int kend = g.kslice ? min(g.K, kbeg + g.kslice) : g.K;
+  const int nk = (kend - kbeg + BK - 1) / BK;
   for (int kc = 0; kc < nk; kc++) {
-    const int k0 = kc * BK;
+    const int k0 = kbeg + kc * BK;
     // stage A (BM x BK) and B (BN x BK); the faster-varying index follows the operand's
-    // contiguous dimension so global reads coalesce
-    for (int e = tid; e < BM * BK; e += 128) {
-      int r, k;
-      if (g.a.kind != OP_PIXELS && g.a.s_row == 1) { r = e % BM; k = e / BM; } else { k = e % BK; r = e / BK; }
-      const float v = load_op(g.a, m0 + r, k0 + k, g.M, g.K);
-      *reinterpret_cast<__nv_bfloat16*>(sa + kmaj_off(r, k, BK)) = __float2bfloat16(v);
-    }
-    for (int e = tid; e < BN * BK; e += 128) {
-      int r, k;
-      if (g.b.kind != OP_PIXELS && g.b.s_row == 1) { r = e % BN; k = e / BN; } else { k = e % BK; r = e / BK; }
-      const float v = load_op(g.b, n0 + r, k0 + k, g.N, g.K);
-      *reinterpret_cast<__nv_bfloat16*>(sb + kmaj_off(r, k, BK)) = __float2bfloat16(v);
-    }
+    // contiguous dimension so global reads coalesce. Eight elements per thread at a time: their
+    // loads are all in flight before the first conversion and store.
+    auto stage = [&](const Operand& o, int rows_tile, int row0, int rows, unsigned char* dst) {
+      const bool rmaj = o.kind != OP_PIXELS && o.s_row == 1;
+      for (int e0 = tid; e0 < rows_tile * BK; e0 += 128 * 8) {
+        float v[8];
+        int rr[8], kk[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const int e = e0 + u * 128;
+          if (rmaj) { rr[u] = e % rows_tile; kk[u] = e / rows_tile; } else { kk[u] = e % BK; rr[u] = e / BK; }
+          v[u] = e < rows_tile * BK ? load_op(o, row0 + rr[u], k0 + kk[u], rows, g.K) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+          if (e0 + u * 128 < rows_tile * BK)
+            *reinterpret_cast<__nv_bfloat16*>(dst + kmaj_off(rr[u], kk[u], BK)) = __float2bfloat16(v[u]);
+      }
+    };
+    stage(g.a, BM, m0, g.M, sa);
+    stage(g.b, BN, n0, g.N, sb);
     asm volatile("fence.proxy.async.shared::cta;");  // generic-proxy smem writes -> tensor core reads
     __syncthreads();
     if (tid == 0) {
@@ -208,6 +224,10 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
           const int col = n0 + c0 + j;
           if (col >= g.N) continue;
           float v = __uint_as_float(r[j]);
+          if (g.part) {
+            g.part[((long long)blockIdx.z * g.M + row) * g.N + col] = v;
+            continue;
+          }
           const long long o = (long long)row * g.ldc + col;
           if (g.epi == EPI_STORE) {
             if (g.bias) v += g.bias[col];
@@ -229,6 +249,18 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kTmemCols));
+}
+
+// Split K: C[row, col] (+ bias) = the sum of the slices' partial tiles, in slice order.
+__global__ void k_splitk_sum(const float* __restrict__ part, int slices, int M, int N, float* __restrict__ C, int ldc,
+                             const float* __restrict__ bias) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= M * N) return;
+  const int row = i / N, col = i - row * N;
+  float v = 0.f;
+  for (int z = 0; z < slices; z++) v += part[(long long)z * M * N + i];
+  if (bias) v += bias[col];
+  C[(long long)row * ldc + col] = v;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -682,6 +714,7 @@ struct Net {
   // activations / scratch sized for the largest batch seen
   int cap = 0;
   DevBuf pre1, h1, pre2, h2, y, dy, dpre2, dpre1, dh_b, dh_b1, targets, loss, errflag;
+  DevBuf splitk;  // partial tiles of the split-K weight-gradient products
   // learned encode scratch
   DevBuf fb_idx, fb_count, fb_in, fb_out, chunk_y;
   std::vector<Param*> params() { return {&W1, &b1, &W2, &b2, &W3, &b3}; }
@@ -739,7 +772,7 @@ Operand op_pixels(const uint8_t* p, bool sample_is_row) { return Operand{p, OP_P
 // Each CTA allocates kTmemCols of the SM's 512 tensor-memory columns; an unused dynamic
 // shared-memory reservation brings every CTA to about 57 KB so at most 4 CTAs share an SM and
 // the allocations never wait on each other.
-int gemm(const GemmArgs& g, cudaStream_t s) {
+int gemm(GemmArgs g, cudaStream_t s, DevBuf* split_scratch = nullptr) {
   static bool attr_done[64] = {};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -754,14 +787,34 @@ int gemm(const GemmArgs& g, cudaStream_t s) {
     }
   }
   const unsigned gx = (g.M + BM - 1) / BM;
-  if (g.N <= 16) {
-    k_gemm_tc<16><<<dim3(gx, (g.N + 15) / 16), 128, 40 << 10, s>>>(g);
-  } else if (g.N <= 48) {
-    k_gemm_tc<48><<<dim3(gx, (g.N + 47) / 48), 128, 36 << 10, s>>>(g);
-  } else {
-    k_gemm_tc<128><<<dim3(gx, (g.N + 127) / 128), 128, 24 << 10, s>>>(g);
+  const unsigned bn = g.N <= 16 ? 16u : g.N <= 48 ? 48u : 128u;
+  const unsigned gy = (g.N + bn - 1) / bn;
+  // Products with few output tiles and a long K (the weight gradients: K is the batch) split K so
+  // that about 128 CTAs share the work; the slices are summed by k_splitk_sum in a fixed order.
+  unsigned gz = 1;
+  g.kslice = 0;
+  g.part = nullptr;
+  if (split_scratch && g.epi == EPI_STORE && g.C && !g.Cb && gx * gy < 32 && g.K >= 4 * BK) {
+    gz = std::min<unsigned>(128 / (gx * gy), (unsigned)((g.K + BK - 1) / BK));
+    const int slice = ((g.K + (int)gz - 1) / (int)gz + BK - 1) / BK * BK;
+    gz = (unsigned)((g.K + slice - 1) / slice);
+    cudaError_t e = split_scratch->ensure((size_t)gz * g.M * g.N * sizeof(float));
+    if (e != cudaSuccess) return cuda_check(e, "alloc split-K scratch");
+    g.kslice = slice;
+    g.part = static_cast<float*>(split_scratch->ptr);
   }
-  return cuda_check(cudaGetLastError(), "launch k_gemm_tc");
+  const dim3 grid(gx, gy, gz);
+  if (bn == 16) k_gemm_tc<16><<<grid, 128, 40 << 10, s>>>(g);
+  else if (bn == 48) k_gemm_tc<48><<<grid, 128, 36 << 10, s>>>(g);
+  else k_gemm_tc<128><<<grid, 128, 24 << 10, s>>>(g);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_check(e, "launch k_gemm_tc");
+  if (g.part) {
+    k_splitk_sum<<<(g.M * g.N + 255) / 256, 256, 0, s>>>(g.part, (int)gz, g.M, g.N, g.C, g.ldc, g.bias);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_check(e, "launch k_splitk_sum");
+  }
+  return CRNGPU_OK;
 }
 
 GemmArgs args(Operand a, Operand b, int M, int N, int K, int epi, float* C, __nv_bfloat16* Cb, const float* pre,
@@ -769,6 +822,8 @@ GemmArgs args(Operand a, Operand b, int M, int N, int K, int epi, float* C, __nv
   GemmArgs g;
   g.a = a; g.b = b; g.M = M; g.N = N; g.K = K; g.epi = epi; g.C = C; g.Cb = Cb; g.pre = pre; g.bias = bias; g.ldc = ldc;
   g.err = static_cast<uint32_t*>(net.errflag.ptr);
+  g.kslice = 0;
+  g.part = nullptr;
   return g;
 }
 
@@ -836,7 +891,7 @@ int backward(Net& net, const uint8_t* blocks, int B, cudaStream_t s) {
   // dW3 [16 x 256] = dY^T H2 ; db3 = colsum(dY)
   if ((rc = gemm(args(op_f32(dy, 1, kOutPad), op_bf16(static_cast<__nv_bfloat16*>(net.h2.ptr), 1, kHid), kOutPad, kHid,
                       B, EPI_STORE, static_cast<float*>(net.W3.g.ptr), nullptr, nullptr, nullptr, kHid, net),
-                 s)) != CRNGPU_OK)
+                 s, &net.splitk)) != CRNGPU_OK)
     return rc;
   k_colsum<<<1, kOutPad, 0, s>>>(dy, B, kOutPad, static_cast<float*>(net.b3.g.ptr));
   // dpre2 = (dY W3) * gelu'(pre2)
@@ -847,7 +902,7 @@ int backward(Net& net, const uint8_t* blocks, int B, cudaStream_t s) {
   // dW2 [256 x 256] = dpre2^T H1 ; db2
   if ((rc = gemm(args(op_bf16(dhb, 1, kHid), op_bf16(static_cast<__nv_bfloat16*>(net.h1.ptr), 1, kHid), kHid, kHid, B,
                       EPI_STORE, static_cast<float*>(net.W2.g.ptr), nullptr, nullptr, nullptr, kHid, net),
-                 s)) != CRNGPU_OK)
+                 s, &net.splitk)) != CRNGPU_OK)
     return rc;
   k_colsum<<<(kHid + 127) / 128, 128, 0, s>>>(dpre2, B, kHid, static_cast<float*>(net.b2.g.ptr));
   // dpre1 = (dpre2 W2) * gelu'(pre1)
@@ -858,7 +913,7 @@ int backward(Net& net, const uint8_t* blocks, int B, cudaStream_t s) {
   // dW1 [256 x 48] = dpre1^T X ; db1
   if ((rc = gemm(args(op_bf16(dhb1, 1, kHid), op_pixels(blocks, false), kHid, kIn, B, EPI_STORE,
                       static_cast<float*>(net.W1.g.ptr), nullptr, nullptr, nullptr, kIn, net),
-                 s)) != CRNGPU_OK)
+                 s, &net.splitk)) != CRNGPU_OK)
     return rc;
   k_colsum<<<(kHid + 127) / 128, 128, 0, s>>>(dpre1, B, kHid, static_cast<float*>(net.b1.g.ptr));
   return cuda_check(cudaGetLastError(), "backward kernels");
