@@ -156,6 +156,27 @@ __global__ void __launch_bounds__(128) k_gemm_tc(GemmArgs g) {
     // contiguous dimension so global reads coalesce. Eight elements per thread at a time: their
     // loads are all in flight before the first conversion and store.
     auto stage = [&](const Operand& o, int rows_tile, int row0, int rows, unsigned char* dst) {
+      if (o.kind == OP_BF16 && o.s_k == 1 && (o.s_row & 7) == 0 && ((uintptr_t)o.p & 15) == 0) {
+        // BF16 rows with K contiguous: 8 consecutive K of a row are one 16-byte segment of the
+        // K-major core-matrix layout, copied with one load and one store
+        const __nv_bfloat16* src = reinterpret_cast<const __nv_bfloat16*>(o.p);
+#pragma unroll 4
+        for (int e = tid; e < rows_tile * (BK / 8); e += 128) {
+          const int r = e / (BK / 8), kg = e - r * (BK / 8);
+          const int row = row0 + r, k = k0 + kg * 8;
+          uint4 v = make_uint4(0u, 0u, 0u, 0u);
+          if (row < rows && k + 8 <= g.K) {
+            v = __ldg(reinterpret_cast<const uint4*>(src + (long long)row * o.s_row + k));
+          } else if (row < rows) {
+            __nv_bfloat16 h[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) h[u] = k + u < g.K ? src[(long long)row * o.s_row + k + u] : __float2bfloat16(0.f);
+            v = *reinterpret_cast<const uint4*>(h);
+          }
+          *reinterpret_cast<uint4*>(dst + kmaj_off(r, kg * 8, BK)) = v;
+        }
+        return;
+      }
       const bool rmaj = o.kind != OP_PIXELS && o.s_row == 1;
       for (int e0 = tid; e0 < rows_tile * BK; e0 += 128 * 8) {
         float v[8];
