@@ -385,3 +385,21 @@ def test_transcode_batch_of_own_files_matches_oracle(cg):
             assert want is not None and np.array_equal(host[pos:pos + n], want), (c.width, c.height, lvl)
             pos += n
         c.close()
+
+
+@pytest.mark.parametrize("mode", ["wide", "lane"])
+def test_transcode_widest_rows_match_oracle(cg, decode_split, mode):
+    """The widest rows a .crn holds: a 4096 x 32 DXT1 and a 4096 x 64 DXT5 texture (rows of 1024
+    blocks, the wide decoder's largest row buffer), written by this library, every level through
+    one decoder against the oracle's crnd restatement."""
+    from crunch2_gb300 import texgen
+    from oracle import port
+    decode_split(mode)
+    for w, h, fmt, seed in ((4096, 32, cg.FMT_DXT1, 900), (4096, 64, cg.FMT_DXT5, 901)):
+        img = texgen.colour_texture(w, h, seed, with_alpha_noise=fmt == cg.FMT_DXT5)
+        crn = cg.compress_crn([texgen.mip_chain(img)], fmt=fmt, quality=96)
+        with cg.unpack_begin(crn) as ctx:
+            for lvl in range(ctx.levels):
+                n = ctx.level_bytes(lvl)
+                want = port.unpack_level(crn, lvl, n)
+                assert want is not None and np.array_equal(ctx.unpack_level(lvl).reshape(-1), want), (w, h, lvl, mode)
