@@ -389,9 +389,10 @@ constexpr uint32_t kWS = 2048;                 // window stride (bits)
 constexpr uint32_t kWM = 448;                  // window overlap (bits): 2 x 144 of chain overshoot + 128 of table reach
 constexpr uint32_t kWX = kWS + kWM;            // positions per window
 constexpr uint32_t kWWords = kWX / 32 + 4;     // staged stream words per window
-constexpr uint32_t kWEmitters = 128;           // emitter threads (warps 1 .. 4)
-constexpr uint32_t kWBuilders = 480;           // table-builder threads (warps 5 .. 19)
-constexpr uint32_t kWThreads = 32 + kWEmitters + kWBuilders;  // + the chain warp (warp 0)
+constexpr uint32_t kWEmitters = 128;           // symbol-decoder threads (warps 1 .. 4)
+constexpr uint32_t kWResolvers = 64;           // endpoint-index resolver threads (warps 5, 6)
+constexpr uint32_t kWBuilders = 416;           // table-builder threads (warps 7 .. 19)
+constexpr uint32_t kWThreads = 32 + kWEmitters + kWResolvers + kWBuilders;  // + the chain warp (warp 0)
 constexpr uint32_t kWPer = (kWX + kWBuilders - 1) / kWBuilders;  // window positions per builder
 constexpr uint32_t kWMaxW = 1024;              // widest row, in blocks (4096 texels)
 constexpr uint32_t kWList = kWS + 4;           // chain items per phase, at most (positions increase; two past kWS)
@@ -417,7 +418,7 @@ __host__ __device__ inline WideLayout wide_layout(uint32_t nm) {
   L.rb = o;    o += 2u * kWMaxW * 2u;            // endpoint index A and B of the row above
   L.grow = o;  o = wide_align16(o + kWMaxW / 2); // the chain's reference groups of the current even row
   L.un = o;    o = wide_align16(o + 7u * kWX);   // build temporaries (code lengths at each position)
-  L.bw = o;    o += 2u * kWBlk * 4u;             // emitted blocks of one item list
+  L.bw = o;    o += 2u * 2u * kWBlk * 4u;        // decoded blocks of two item lists (decoded, being resolved)
   L.total = wide_align16(o);
   return L;
 }
@@ -507,13 +508,13 @@ __device__ __forceinline__ uint32_t code_sym(uint32_t v16, const uint32_t* __res
 // Barriers of the table builders (named barrier 1) and of the emitters (named barrier 2); the
 // other roles run on.
 __device__ __forceinline__ void builder_sync() { asm volatile("bar.sync 1, %0;" ::"r"(kWBuilders) : "memory"); }
-__device__ __forceinline__ void emitter_sync() { asm volatile("bar.sync 2, %0;" ::"r"(kWEmitters) : "memory"); }
-__device__ __forceinline__ bool emitter_sync_or(bool v) {
+__device__ __forceinline__ void resolver_sync() { asm volatile("bar.sync 2, %0;" ::"r"(kWResolvers) : "memory"); }
+__device__ __forceinline__ bool resolver_sync_or(bool v) {
   uint32_t r;
   asm volatile(
       "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, 2, %2, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
       : "=r"(r)
-      : "r"((uint32_t)v), "r"(kWEmitters)
+      : "r"((uint32_t)v), "r"(kWResolvers)
       : "memory");
   return r != 0u;
 }
@@ -537,9 +538,10 @@ extern __shared__ __align__(16) uint8_t wide_smem[];
 // Small shared state of k_crn_decode_wide (one instance per CTA).
 struct WideShared {
   uint32_t meta[2][3];  // per item list: count, first row, first item in that row
+  uint32_t rmeta[2][3]; // per decoded list (for the resolvers): block count, first row, first item
   uint32_t done, carry[2], bad;
   uint32_t aux[5][kAuxWords];       // long-code bounds of the models read (slot order of the tables)
-  uint32_t scan[kWEmitters / 32][3];
+  uint32_t scan[kWResolvers / 32][3];
   uint16_t rsorted[kStaged];        // the reference model's first sorted symbols
 };
 
@@ -584,8 +586,9 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
   uint8_t* lenSB = un + 4 * kWX;
   uint8_t* lenSBk = un + 5 * kWX;  // selector codes of one block (two-endpoint formats)
   uint8_t* lenEBk = un + 6 * kWX;  // endpoint codes of one block (two-endpoint formats)
-  uint32_t* bw0 = reinterpret_cast<uint32_t*>(sm + Ly.bw);  // emitted blocks: reference | delta A << 2 | selector A << 16
-  uint32_t* bw1 = bw0 + kWBlk;                      // delta B | selector B << 16
+  // decoded blocks of list i at bwbuf + (i & 1) * 2 * kWBlk: word 0 = reference | delta A << 2 |
+  // selector A << 16, word 1 (kWBlk further) = delta B | selector B << 16
+  uint32_t* bwbuf = reinterpret_cast<uint32_t*>(sm + Ly.bw);
 
   const uint32_t W = (J.bx + 1) & ~1u, H = (J.by + 1) & ~1u, W2 = W >> 1;
   const uint32_t rows = J.faces * H;
@@ -632,8 +635,9 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
   uint32_t c_r = 0, c_e = 0, c_j = 0;  // the chain's row, item within the row, window position
   uint32_t done_at = kWNotDone;
   const uint32_t warp = tid >> 5, lane = tid & 31u;
-  const uint32_t wt = tid - (32 + kWEmitters);  // builder index
-  const uint32_t et = tid - 32;                 // emitter index
+  const uint32_t wt = tid - (32 + kWEmitters + kWResolvers);  // builder index
+  const uint32_t et = tid - 32;                               // decoder index
+  const uint32_t rt = tid - (32 + kWEmitters);                // resolver index
   for (uint32_t t = 0;; t++) {
     if (tid == 0 && t >= 1 && done_at == kWNotDone) {
       // ---- the chain walks window t - 1 and records its items in list (t - 1) & 1
@@ -707,7 +711,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
       c_e = e;
       c_j = j - kWS;
       if (r >= rows) S.done = t;
-    } else if (warp >= 1 + kWEmitters / 32) {
+    } else if (warp >= 1 + (kWEmitters + kWResolvers) / 32) {
       // the stream words of window t + 1, stored at the end of the build
       const uint32_t pre_m = (((t + 1) * kWS) >> 5) + wt;
       const RawWord pre = (done_at == kWNotDone && wt < kWWords) ? stream_word_load(J.src, J.src_size, pre_m)
@@ -830,9 +834,9 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
       }
       if (done_at == kWNotDone && wt < kWWords)
         words[((t + 1) & 3u) * kWWords + wt] = stream_word_finish(J.src, J.src_size, pre_m, pre);
-    } else if (warp >= 1 && t >= 2 && (done_at == kWNotDone || t - 2 < done_at)) {
-      // ---- the emitter warps: list t - 2 (buffer t & 1), decoded from window t - 2's staged
-      // words, then its endpoint indices resolved row segment by row segment
+    } else if (warp >= 1 && warp < 1 + kWEmitters / 32 && t >= 2 && (done_at == kWNotDone || t - 2 < done_at)) {
+      // ---- the decoder warps: list t - 2 (list buffer t & 1), decoded from window t - 2's
+      // staged words into block buffer (t - 2) & 1; the resolvers take it in the next phase
       const uint32_t lb = t & 1u;
       const uint32_t* L = list + lb * kWList;
       const uint32_t* wd = words + ((t - 2) & 3u) * kWWords;
@@ -862,6 +866,8 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
       const uint16_t* stS = srt + kStagedLong;
       const uint16_t* stDB = five ? srt + 2 * kStagedLong : stA;
       const uint16_t* stSB = five ? srt + 3 * kStagedLong : stS;
+      uint32_t* bw0 = bwbuf + ((t - 2) & 1u) * 2u * kWBlk;
+      uint32_t* bw1 = bw0 + kWBlk;
       uint32_t bad = 0;
       for (uint32_t i = et; i < n; i += kWEmitters) {
         const uint32_t ent = L[i];
@@ -911,13 +917,24 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
         }
       }
       if (bad) atomicOr(&S.bad, 1u);
-      uint32_t total = 0;
-      if (n) {
-        uint32_t r, blk;
-        locate(n - 1, r, blk);
-        total = blk + ((r & 1u) ? 1u : 2u);
+      if (et == 0) {
+        uint32_t total = 0;
+        if (n) {
+          uint32_t r, blk;
+          locate(n - 1, r, blk);
+          total = blk + ((r & 1u) ? 1u : 2u);
+        }
+        S.rmeta[(t - 2) & 1u][0] = total;
+        S.rmeta[(t - 2) & 1u][1] = r0;
+        S.rmeta[(t - 2) & 1u][2] = e0;
       }
-      emitter_sync();
+    } else if (warp >= 1 + kWEmitters / 32 && t >= 3 && (done_at == kWNotDone || t - 3 < done_at)) {
+      // ---- the resolver warps: the endpoint indices of list t - 3 (decoded in the previous
+      // phase into block buffer (t - 3) & 1), row segment by row segment, in stream order
+      const uint32_t* bw0 = bwbuf + ((t - 3) & 1u) * 2u * kWBlk;
+      const uint32_t* bw1 = bw0 + kWBlk;
+      const uint32_t total = S.rmeta[(t - 3) & 1u][0], r0 = S.rmeta[(t - 3) & 1u][1], e0 = S.rmeta[(t - 3) & 1u][2];
+      const uint32_t odd0 = r0 & 1u;
       // The scan operator per block: a block with deltas adds them (mod the palette size), a
       // "left" reference keeps the running index, an "up" reference sets it from the row above.
       auto block_op = [&](uint32_t b, uint32_t x, bool& inexact) -> IdxOp {
@@ -935,15 +952,15 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
         const uint32_t cnt = min(W - x, total - b);
         const uint32_t f = r / H, y = r - f * H;
         const bool vis_row = y < J.by;
-        const uint32_t per = (cnt + kWEmitters - 1) / kWEmitters;  // <= 8 (rows of at most 1024 blocks)
-        const uint32_t k0 = min(cnt, et * per), k1 = min(cnt, k0 + per);
+        const uint32_t per = (cnt + kWResolvers - 1) / kWResolvers;  // <= 16 (rows of at most 1024 blocks)
+        const uint32_t k0 = min(cnt, rt * per), k1 = min(cnt, k0 + per);
         bool inexact = nA == 0 || (two && nB == 0);
         IdxOp mine{0, 0, 0};
         for (uint32_t k = k0; k < k1; k++) mine = idx_compose<two>(mine, block_op(b + k, x + k, inexact), nA, nB);
         const uint32_t cA = S.carry[0], cB = S.carry[1];
-        if (emitter_sync_or(inexact)) {
+        if (resolver_sync_or(inexact)) {
           // a delta at or above its palette size: the reference's sequential rule, on one thread
-          if (et == 0) {
+          if (rt == 0) {
             uint32_t iA = cA, iB = cB;
             for (uint32_t k = 0; k < cnt; k++) {
               const uint32_t w0 = bw0[b + k], ref = w0 & 3u;
@@ -977,7 +994,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
           }
         } else {
           // exclusive scan of the threads' compositions: warp shuffles, then the warp totals
-          const uint32_t wi = et >> 5;
+          const uint32_t wi = rt >> 5;
           IdxOp inc = mine;
 #pragma unroll
           for (uint32_t d = 1; d < 32; d <<= 1) {
@@ -997,10 +1014,10 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
           ex.a = __shfl_up_sync(0xFFFFFFFFu, inc.a, 1);
           ex.b = __shfl_up_sync(0xFFFFFFFFu, inc.b, 1);
           if (lane == 0) ex = IdxOp{0, 0, 0};
-          emitter_sync();
+          resolver_sync();
           IdxOp pre_op{0, 0, 0};
 #pragma unroll
-          for (uint32_t w = 0; w < kWEmitters / 32; w++)
+          for (uint32_t w = 0; w < kWResolvers / 32; w++)
             if (w < wi) pre_op = idx_compose<two>(pre_op, IdxOp{S.scan[w][0], S.scan[w][1], S.scan[w][2]}, nA, nB);
           pre_op = idx_compose<two>(pre_op, ex, nA, nB);
           uint32_t iA = pre_op.set ? pre_op.a : add_mod(cA, pre_op.a, nA);
@@ -1026,7 +1043,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
             }
           }
         }
-        emitter_sync();  // row buffer and carry are complete before the next segment reads them
+        resolver_sync();  // row buffer and carry are complete before the next segment reads them
         b += cnt;
         x += cnt;
         if (x == W) {
@@ -1038,7 +1055,7 @@ __device__ __forceinline__ void wide_level(const StreamJob& J, WideShared& S, ui
     }
     __syncthreads();
     done_at = S.done;
-    if (done_at != kWNotDone && t >= done_at + 1) break;
+    if (done_at != kWNotDone && t >= done_at + 2) break;
   }
   if (tid == 0 && S.bad) atomicMax(status, (S.bad & 1u) ? (uint32_t)kStBadCode : (uint32_t)kStBadIndex);
 }
