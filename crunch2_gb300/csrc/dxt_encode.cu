@@ -1554,7 +1554,10 @@ __device__ __forceinline__ void load_pix(const uint8_t* px, uint32_t (&pix)[16])
 }
 
 // Phase 1 over n blocks: warp w takes the groups of 32 consecutive blocks g = w, w + W, ..., a lane
-// per block, each group staged by one bulk copy.
+// per block, each group staged by one bulk copy. Warps are ranked CTA-first (warp 0 of every CTA,
+// then warp 1, ...), and the grid has a CTA per group up to the resident limit, so a short batch
+// (the learned encoder's fallback blocks, a small mip level) puts one working warp on each SM:
+// the seeds are bound by the SM's FP64 pipe, which the warps of one CTA would share.
 template <bool G>
 __global__ void __launch_bounds__(kWarpsPerCta * 32, kSeedCtasPerSm)
     k_dxt1_seeds(const uint8_t* __restrict__ blocks, uint32_t n, uint32_t opts, Seed* __restrict__ seeds,
@@ -1563,7 +1566,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, kSeedCtasPerSm)
   if (n_dev) n = min(n, *n_dev);  // a count the host does not read back: n is then only the grid's bound
   SeedShared& S = reinterpret_cast<SeedShared*>(smem_raw)[threadIdx.x >> 5];
   const uint32_t lane = lane_id();
-  const uint32_t warp_global = blockIdx.x * kWarpsPerCta + (threadIdx.x >> 5);
+  const uint32_t warp_global = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
   const uint32_t nwarps = gridDim.x * kWarpsPerCta;
   const uint32_t groups = (n + kSeedLanes - 1) / kSeedLanes;
   const uint32_t zero = 0;
@@ -2090,7 +2093,7 @@ int launch_dxt1_kernel(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8
                        ((opts >> kD1QualityShift) & 7u) != kQUber;
   const uint32_t seed_warps = (n + kSeedLanes - 1) / kSeedLanes;
   const uint32_t seed_full = (uint32_t)(L.sms * L.seeds_per_sm);
-  const uint32_t seed_grid = std::min<uint32_t>((seed_warps + kWarpsPerCta - 1) / kWarpsPerCta, seed_full);
+  const uint32_t seed_grid = std::min<uint32_t>(seed_warps, seed_full);
   const size_t seed_smem = sizeof(SeedShared) * kWarpsPerCta, smem = sizeof(WarpShared) * kWarpsPerCta;
   const uint32_t full = (uint32_t)(L.sms * L.search_per_sm[general ? 1 : 0]);
   const uint32_t grid = std::min<uint32_t>((n + kWarpsPerCta - 1) / kWarpsPerCta, full);
