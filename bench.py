@@ -5,7 +5,8 @@ synthetic texture (value noise + 40 flat rectangles, seed 100; 11 box-filtered l
 One JSON line on stdout (rank 0):
   value      whole-job DXT1 encode Mtexel/s, inputs resident in HBM, device time of K steps
   learned    the learned-proposal encode of the same blocks (shipped weights): Mtexel/s, RGB
-             RMSE beside the plain encode's, fallback fraction
+             RMSE beside the plain encode's, fallback fraction; the fallback blocks through the
+             exact optimizer at Better quality, and at Uber (uber_fallback)
   e2e        the same encode through the C ABI from pinned host memory: every step the H2D copy
              of the mip chain, crngpu_encode_batch_launch (CUDA graph) and the D2H copy of the
              blocks, wall time; e2e_per_level the same through crngpu_compress_image per level
@@ -52,6 +53,7 @@ CRN_FIXTURE = os.path.join(ROOT, "tests", "golden", "crn", "c1_dxt1_1024.crn")
 METRIC = "DXT1 encode Mtexel/s at matched RMSE, learned vs plain; CRN→DXT1 transcode GB/s"
 L2_FLUSH_BYTES = 256 << 20
 TX_BATCH = 1024  # textures per transcode batch
+QUALITY_NAMES = ["superfast", "fast", "normal", "better", "uber"]  # crn_dxt_quality 0..4
 LANE_OPS_PER_EVAL = 27  # uber inner loop per candidate x colour: 15 FFMA, 4 FMNMX, 4 FADD, 2 IADD, 2 IMAD
 
 
@@ -585,36 +587,45 @@ def main():
     from crunch2_gb300 import learned as LR
     net = LR.default_net()
     d_learned = torch.empty_like(d_out)
-    for _ in range(args.warmup):
-        flush.fill_(1)
-        net.encode(d_blocks, threshold=LR.DEFAULT_THRESHOLD, out=d_learned, stream=stream)
-    torch.cuda.synchronize()
-    ln_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ln_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    fallbacks = 0
-    for i in range(args.steps):
-        flush.fill_(i & 0xFF)
-        ln_start[i].record(stream)
-        _, fallbacks = net.encode(d_blocks, threshold=LR.DEFAULT_THRESHOLD, out=d_learned, stream=stream)
-        ln_end[i].record(stream)
-    torch.cuda.synchronize()
-    ln_ms = sum(s.elapsed_time(e) for s, e in zip(ln_start, ln_end)) / args.steps
     rmse_plain = LR.rgb_rmse_torch(d_out, d_blocks)
-    rmse_learned = LR.rgb_rmse_torch(d_learned, d_blocks)
-    learned = {"value": round(texels / (ln_ms / 1e3) / 1e6, 3), "unit": "Mtexel/s", "ms_per_step": round(ln_ms, 4),
-               "speedup_vs_plain": round(kernel_ms / ln_ms, 3), "rmse_plain": round(rmse_plain, 4),
-               "rmse_learned": round(rmse_learned, 4), "rmse_delta": round(rmse_learned - rmse_plain, 4),
-               "fallback_frac": round(fallbacks / n_blocks, 4), "threshold": LR.DEFAULT_THRESHOLD,
-               "weights": "crunch2_gb300/weights/dxt1_endpoint_net.npz",
-               "path": "crngpu_dxt1_learned: fused MLP (k_mlp_infer) + refit (k_learned_refit) + exact "
-                       "optimizer on fallback blocks; one host sync per call"}
+
+    def learned_run(quality):
+        for _ in range(args.warmup):
+            flush.fill_(1)
+            net.encode(d_blocks, threshold=LR.DEFAULT_THRESHOLD, out=d_learned, stream=stream, fallback_quality=quality)
+        torch.cuda.synchronize()
+        ln_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ln_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        fallbacks = 0
+        for i in range(args.steps):
+            flush.fill_(i & 0xFF)
+            ln_start[i].record(stream)
+            _, fallbacks = net.encode(d_blocks, threshold=LR.DEFAULT_THRESHOLD, out=d_learned, stream=stream,
+                                      fallback_quality=quality)
+            ln_end[i].record(stream)
+        torch.cuda.synchronize()
+        ln_ms = sum(s.elapsed_time(e) for s, e in zip(ln_start, ln_end)) / args.steps
+        rmse_learned = LR.rgb_rmse_torch(d_learned, d_blocks)
+        return {"value": round(texels / (ln_ms / 1e3) / 1e6, 3), "unit": "Mtexel/s", "ms_per_step": round(ln_ms, 4),
+                "speedup_vs_plain": round(kernel_ms / ln_ms, 3), "rmse_plain": round(rmse_plain, 4),
+                "rmse_learned": round(rmse_learned, 4), "rmse_delta": round(rmse_learned - rmse_plain, 4),
+                "fallback_frac": round(fallbacks / n_blocks, 4), "threshold": LR.DEFAULT_THRESHOLD,
+                "fallback_quality": QUALITY_NAMES[quality]}
+
+    learned = learned_run(LR.DEFAULT_FALLBACK_QUALITY)
+    learned.update({"weights": "crunch2_gb300/weights/dxt1_endpoint_net.npz",
+                    "path": "crngpu_dxt1_learned_ex: fused MLP (k_mlp_infer) + refit (k_learned_refit) + exact "
+                            "optimizer on the fallback blocks at the stated crn_dxt_quality; one host sync per call"})
+    if LR.DEFAULT_FALLBACK_QUALITY != 4:
+        learned["uber_fallback"] = learned_run(4)
     del net
 
     # ---- config 4's evaluation: the shipped weights on 32 held-out 4096x4096 textures (a seed
     # range the training never saw), learned vs plain encode time and RGB RMSE per texture
     config4_eval = None
     if "config4" not in skip:
-        r4 = LR.config4(weights=LR.WEIGHTS, eval_textures=32, eval_size=4096, threshold=LR.DEFAULT_THRESHOLD)
+        r4 = LR.config4(weights=LR.WEIGHTS, eval_textures=32, eval_size=4096, threshold=LR.DEFAULT_THRESHOLD,
+                        fallback_quality=LR.DEFAULT_FALLBACK_QUALITY)
         g4 = r4["learned"][0]
         config4_eval = {"textures": r4["eval_textures"], "size": r4["eval_size"], "blocks": r4["eval_blocks"],
                         "plain_mtexel_s": round(r4["plain_mtexel_s"], 1),
@@ -622,8 +633,9 @@ def main():
                         "rmse_plain": round(r4["rmse_plain"], 4), "rmse_learned": round(g4["rmse_learned"], 4),
                         "rmse_delta": round(g4["rmse_learned"] - r4["rmse_plain"], 4),
                         "fallback_frac": round(g4["fallback_frac"], 4), "threshold": LR.DEFAULT_THRESHOLD,
+                        "fallback_quality": QUALITY_NAMES[LR.DEFAULT_FALLBACK_QUALITY],
                         "path": "learned.config4(weights=shipped): per texture, crngpu_dxt1_optimize_batch and "
-                                "crngpu_dxt1_learned on device blocks, CUDA events"}
+                                "crngpu_dxt1_learned_ex on device blocks, CUDA events"}
         learned["config4_eval"] = config4_eval
 
     # ---- CRN -> DXT1 transcode: a batch of TX_BATCH textures (each its own context, i.e. its own
@@ -824,6 +836,7 @@ def main():
             "encode_roofline_frac": roofline["frac"],
             "learned_mtexel_s": pick(learned, "value"), "learned_speedup": pick(learned, "speedup_vs_plain"),
             "learned_rmse_delta": pick(learned, "rmse_delta"),
+            "learned_uber_fallback_speedup": pick(learned, "uber_fallback", "speedup_vs_plain"),
             "config4_learned_speedup": pick(learned, "config4_eval", "speedup"),
             "config4_rmse_delta": pick(learned, "config4_eval", "rmse_delta"),
             "transcode_batch_gb_s": transcode["value"], "transcode_single_ms": transcode["single_texture"]["ms"],

@@ -1095,11 +1095,12 @@ extern "C" int crngpu_mlp_make_targets(const uint8_t* d_blocks8, const uint64_t*
 // Learned DXT1 encode of n blocks (device RGBA8 in, device dxt1 out): MLP proposal, one
 // selector refit, and the exact optimizer for blocks whose error exceeds threshold x the
 // predicted bound. *fallbacks (host, optional) receives how many blocks fell back.
-extern "C" int crngpu_dxt1_learned(void* h, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
-                                   uint8_t* d_out, uint32_t* fallbacks, void* stream) {
+extern "C" int crngpu_dxt1_learned_ex(void* h, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
+                                      uint32_t fallback_quality, uint8_t* d_out, uint32_t* fallbacks, void* stream) {
   clear_error();
   Net* net = static_cast<Net*>(h);
   if (!net || net->magic != 0x4D4C5030u || !d_blocks || !d_out) return CRNGPU_E_PARAM;
+  if (fallback_quality > kDxtQualityUber) { set_error("crngpu_dxt1_learned: bad fallback quality"); return CRNGPU_E_PARAM; }
   if (!n) return CRNGPU_OK;
   if (n > (1u << 28)) { set_error("crngpu_dxt1_learned: at most 2^28 blocks per call"); return CRNGPU_E_PARAM; }
   cudaStream_t s = as_stream(stream);
@@ -1134,7 +1135,7 @@ extern "C" int crngpu_dxt1_learned(void* h, const uint8_t* d_blocks, uint32_t n,
   const uint32_t sweep = (uint32_t)std::min<uint64_t>(((uint64_t)n * 4 + 255) / 256, 8192);
   k_gather_idx<<<sweep, 256, 0, s>>>(d_blocks, idx, cnt_d, static_cast<uint8_t*>(net->fb_in.ptr));
   if ((rc = launch_dxt1_count(static_cast<uint8_t*>(net->fb_in.ptr), n, cnt_d,
-                              dxt1_options(perceptual != 0, true, kDxtQualityUber, false, false, 128),
+                              dxt1_options(perceptual != 0, true, fallback_quality, false, false, 128),
                               static_cast<uint8_t*>(net->fb_out.ptr), 8, s)) != CRNGPU_OK)
     return rc;
   k_scatter_idx<<<(sweep + 3) / 4, 256, 0, s>>>(static_cast<uint8_t*>(net->fb_out.ptr), idx, cnt_d, d_out);
@@ -1149,4 +1150,9 @@ extern "C" int crngpu_dxt1_learned(void* h, const uint8_t* d_blocks, uint32_t n,
     *fallbacks = cnt;
   }
   return CRNGPU_OK;
+}
+
+extern "C" int crngpu_dxt1_learned(void* h, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
+                                   uint8_t* d_out, uint32_t* fallbacks, void* stream) {
+  return crngpu_dxt1_learned_ex(h, d_blocks, n, perceptual, threshold, kDxtQualityUber, d_out, fallbacks, stream);
 }

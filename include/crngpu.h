@@ -384,6 +384,11 @@ CRNGPU_API int crngpu_mlp_train_step(void* net, const uint8_t* d_blocks, const f
 CRNGPU_API int crngpu_dxt1_learned(void* net, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
                                    uint8_t* d_out, uint32_t* fallbacks, void* stream);
 
+/* The same with the exact optimizer's search effort on the fallback blocks: fallback_quality is a
+ * CRNGPU_DXT_QUALITY_* (crngpu_dxt1_learned uses CRNGPU_DXT_QUALITY_UBER). */
+CRNGPU_API int crngpu_dxt1_learned_ex(void* net, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
+                                      uint32_t fallback_quality, uint8_t* d_out, uint32_t* fallbacks, void* stream);
+
 /* ------------------------------------------------------------------------------------------
  * CRN -> DXTn transcoder (crnd::crn_unpacker, inc/crn_decomp.h:3498-4223; API inc/crn_defs.h:
  * 174-205). Supported: DXT1, DXT5 family, DXN_XY/YX, DXT5A. ETC formats: CRNGPU_E_UNSUPPORTED.

@@ -104,9 +104,29 @@ def test_zero_threshold_falls_back_to_exact_optimizer(L, trained):
     import crunch2_gb300 as cg
     net, _ = trained
     blocks = torch.from_numpy(G.c0_blocks()).cuda()
-    out, fb = net.encode(blocks, threshold=0.0)
+    out, fb = net.encode(blocks, threshold=0.0, fallback_quality=4)
     assert fb == blocks.shape[0]
     assert torch.equal(out, cg.dxt1_optimize(blocks))
+
+
+@pytest.mark.parametrize("quality", [0, 2, 3])
+def test_fallback_quality_is_the_exact_optimizer_at_that_quality(L, trained, quality):
+    import crunch2_gb300 as cg
+    net, _ = trained
+    blocks = torch.from_numpy(G.c0_blocks()).cuda()
+    out, fb = net.encode(blocks, threshold=0.0, fallback_quality=quality)
+    assert fb == blocks.shape[0]
+    assert torch.equal(out, cg.dxt1_optimize(blocks, quality=quality))
+    # crngpu_dxt1_learned is crngpu_dxt1_learned_ex with Uber fallback
+    a = torch.empty_like(out)
+    fa = L.ctypes.c_uint32(0)
+    L._check(L._bind().crngpu_dxt1_learned(net.h, blocks.data_ptr(), blocks.shape[0], 1, 1.5, a.data_ptr(),
+                                           L.ctypes.byref(fa), None), "crngpu_dxt1_learned")
+    torch.cuda.synchronize()
+    b, fb_b = net.encode(blocks, threshold=1.5, fallback_quality=4)
+    assert torch.equal(a, b) and fa.value == fb_b
+    with pytest.raises(cg.CrnGpuError):
+        net.encode(blocks, threshold=1.5, fallback_quality=5)
 
 
 def test_trained_network_beats_untrained(L, trained):
