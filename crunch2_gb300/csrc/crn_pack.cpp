@@ -20,10 +20,8 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
-#include <queue>
 #include <string>
 #include <thread>
-#include <unordered_map>
 #include <vector>
 
 #include "crn_file.h"
@@ -32,12 +30,18 @@
 namespace crngpu {
 namespace {
 
+// MSB-first bit writer. A code of up to 32 bits joins the fewer than 8 pending bits in a 64-bit
+// accumulator, whose whole bytes are then appended; bits above the pending ones are stale and
+// never read.
 class BitWriter {
  public:
-  void put(uint32_t v, uint32_t bits) {
-    for (int i = (int)bits - 1; i >= 0; i--) {
-      acc_ = (acc_ << 1) | ((v >> i) & 1u);
-      if (++n_ == 8) { out_.push_back((uint8_t)acc_); acc_ = 0; n_ = 0; }
+  void put(uint32_t v, uint32_t bits) {  // the low `bits` (<= 32) bits of v
+    if (!bits) return;
+    acc_ = (acc_ << bits) | ((uint64_t)v & ((1ull << bits) - 1ull));
+    n_ += bits;
+    while (n_ >= 8) {
+      n_ -= 8;
+      out_.push_back((uint8_t)(acc_ >> n_));
     }
   }
   std::vector<uint8_t> finish() {
@@ -48,12 +52,16 @@ class BitWriter {
 
  private:
   std::vector<uint8_t> out_;
-  uint32_t acc_ = 0;
-  int n_ = 0;
+  uint64_t acc_ = 0;
+  uint32_t n_ = 0;
 };
 
 // Huffman code lengths for a histogram, limited to `limit` bits (frequencies are halved until the
-// tree fits). Unused symbols get 0; a single used symbol gets length 1.
+// tree fits). Unused symbols get 0; a single used symbol gets length 1. The two lightest nodes
+// are merged first, ties to the lower node id (leaves 0..n-1 by symbol, then merged nodes in
+// creation order). Merged nodes are created in non-decreasing weight, so the lightest node is at
+// the front of either the (weight, symbol)-sorted leaves or the merged nodes: two queues instead
+// of a heap, with the same merges.
 std::vector<uint8_t> code_lengths(const std::vector<uint32_t>& freq_in, int limit) {
   const size_t n = freq_in.size();
   std::vector<uint8_t> len(n, 0);
@@ -63,27 +71,41 @@ std::vector<uint8_t> code_lengths(const std::vector<uint32_t>& freq_in, int limi
     if (freq[i]) { used++; last = i; }
   if (!used) return len;
   if (used == 1) { len[last] = 1; return len; }
+  std::vector<uint32_t> leaves;
+  leaves.reserve(used);
+  std::vector<uint64_t> mw(used - 1);             // merged node k: weight, parent
+  std::vector<uint32_t> parent(n + used - 1);     // by node id: leaves 0..n-1, merged n + k
+  std::vector<uint8_t> depth(used - 1);
   for (;;) {
-    // nodes: leaves 0..n-1, internal n..; (weight, id) min-heap with id tie-break for determinism
-    std::vector<int> parent(2 * n, -1);
-    using Item = std::pair<uint64_t, int>;
-    std::priority_queue<Item, std::vector<Item>, std::greater<Item>> q;
+    leaves.clear();
     for (size_t i = 0; i < n; i++)
-      if (freq[i]) q.push({freq[i], (int)i});
-    int next = (int)n;
-    while (q.size() > 1) {
-      const Item a = q.top(); q.pop();
-      const Item b = q.top(); q.pop();
-      parent[a.second] = next;
-      parent[b.second] = next;
-      q.push({a.first + b.first, next++});
+      if (freq[i]) leaves.push_back((uint32_t)i);
+    std::sort(leaves.begin(), leaves.end(),
+              [&](uint32_t a, uint32_t b) { return freq[a] != freq[b] ? freq[a] < freq[b] : a < b; });
+    size_t li = 0, mi = 0, made = 0;
+    auto take = [&]() -> std::pair<uint64_t, size_t> {  // (weight, node id) of the lighter front
+      if (li < leaves.size() && (mi == made || freq[leaves[li]] <= mw[mi])) {
+        const uint32_t s = leaves[li++];
+        return {freq[s], s};
+      }
+      const size_t k = mi++;
+      return {mw[k], n + k};
+    };
+    while (made < used - 1) {
+      const auto a = take();
+      const auto b = take();
+      parent[a.second] = (uint32_t)(n + made);
+      parent[b.second] = (uint32_t)(n + made);
+      mw[made++] = a.first + b.first;
     }
+    // depths top-down: a merged node's parent was created after it
     int maxl = 0;
-    for (size_t i = 0; i < n; i++) {
-      if (!freq[i]) continue;
-      int d = 0;
-      for (int p = (int)i; parent[p] >= 0; p = parent[p]) d++;
-      len[i] = (uint8_t)d;
+    depth[used - 2] = 0;
+    for (size_t k = used - 1; k-- > 0;)
+      if (k != used - 2) depth[k] = (uint8_t)std::min<int>(255, depth[parent[n + k] - n] + 1);
+    for (uint32_t s : leaves) {
+      const int d = depth[parent[s] - n] + 1;
+      len[s] = (uint8_t)std::min(d, 255);
       maxl = std::max(maxl, d);
     }
     if (maxl <= limit) return len;
@@ -175,31 +197,76 @@ void put_be(std::vector<uint8_t>& d, size_t at, uint32_t v, int bytes) {
   for (int i = bytes - 1; i >= 0; i--) d[at + (size_t)(bytes - 1 - i)] = (uint8_t)(v >> (8 * i));
 }
 
+// Distinct values in first-use order, found through an open-addressing table (multiplicative
+// hash, linear probing, at most half full).
 struct Palette {
-  std::vector<uint64_t> values;               // distinct values in first-use order
-  std::unordered_map<uint64_t, uint32_t> index;
+  std::vector<uint64_t> values;
+  std::vector<uint64_t> keys;
+  std::vector<uint32_t> slot;  // index into values + 1; 0 = empty
+  uint32_t shift = 64;
+  static size_t hash(uint64_t v, uint32_t shift) { return (size_t)((v * 0x9E3779B97F4A7C15ull) >> shift); }
+  void grow() {
+    const size_t size = slot.empty() ? 1024 : 2 * slot.size();
+    shift = 64;
+    for (size_t k = size; k > 1; k >>= 1) shift--;
+    keys.assign(size, 0);
+    slot.assign(size, 0);
+    for (size_t i = 0; i < values.size(); i++) {
+      size_t h = hash(values[i], shift);
+      while (slot[h]) h = (h + 1) & (size - 1);
+      keys[h] = values[i];
+      slot[h] = (uint32_t)i + 1;
+    }
+  }
+  uint64_t last_value = 0;
+  uint32_t last_index = UINT32_MAX;  // the previous add's result: neighbouring blocks often repeat
   uint32_t add(uint64_t v) {
-    auto it = index.find(v);
-    if (it != index.end()) return it->second;
-    const uint32_t i = (uint32_t)values.size();
-    index.emplace(v, i);
+    if (last_index != UINT32_MAX && v == last_value) return last_index;
+    last_value = v;
+    return last_index = insert(v);
+  }
+  uint32_t insert(uint64_t v) {
+    if (2 * (values.size() + 1) > slot.size()) grow();
+    const size_t mask = slot.size() - 1;
+    size_t h = hash(v, shift);
+    for (; slot[h]; h = (h + 1) & mask)
+      if (keys[h] == v) return slot[h] - 1;
+    keys[h] = v;
+    slot[h] = (uint32_t)values.size() + 1;
     values.push_back(v);
-    return i;
+    return (uint32_t)values.size() - 1;
   }
 };
 
-// DXT order -> linear order selectors (g_dxt1_to_linear, g_dxt5_to_linear, crnlib/crn_dxt.cpp:35-39)
+// DXT order -> linear order selectors (g_dxt1_to_linear, g_dxt5_to_linear, crnlib/crn_dxt.cpp:35-39),
+// four selectors per table lookup
+struct SelectorTables {
+  uint8_t d1[256];
+  uint16_t d5[4096];
+  SelectorTables() {
+    static const uint8_t t1[4] = {0, 3, 1, 2}, t5[8] = {0, 7, 1, 2, 3, 4, 5, 6};
+    for (uint32_t x = 0; x < 256; x++) {
+      uint32_t v = 0;
+      for (int p = 0; p < 4; p++) v |= (uint32_t)t1[(x >> (2 * p)) & 3] << (2 * p);
+      d1[x] = (uint8_t)v;
+    }
+    for (uint32_t x = 0; x < 4096; x++) {
+      uint32_t v = 0;
+      for (int p = 0; p < 4; p++) v |= (uint32_t)t5[(x >> (3 * p)) & 7] << (3 * p);
+      d5[x] = (uint16_t)v;
+    }
+  }
+};
+const SelectorTables kSelectorTables;
 uint32_t dxt1_sel_to_linear(uint32_t dxt) {
-  static const uint8_t t[4] = {0, 3, 1, 2};
-  uint32_t lin = 0;
-  for (int p = 0; p < 16; p++) lin |= (uint32_t)t[(dxt >> (2 * p)) & 3] << (2 * p);
-  return lin;
+  const uint8_t* t = kSelectorTables.d1;
+  return (uint32_t)t[dxt & 255] | ((uint32_t)t[(dxt >> 8) & 255] << 8) | ((uint32_t)t[(dxt >> 16) & 255] << 16) |
+         ((uint32_t)t[dxt >> 24] << 24);
 }
 uint64_t dxt5_sel_to_linear(uint64_t dxt) {
-  static const uint8_t t[8] = {0, 7, 1, 2, 3, 4, 5, 6};
-  uint64_t lin = 0;
-  for (int p = 0; p < 16; p++) lin |= (uint64_t)t[(dxt >> (3 * p)) & 7] << (3 * p);
-  return lin;
+  const uint16_t* t = kSelectorTables.d5;
+  return (uint64_t)t[dxt & 4095] | ((uint64_t)t[(dxt >> 12) & 4095] << 12) | ((uint64_t)t[(dxt >> 24) & 4095] << 24) |
+         ((uint64_t)t[(dxt >> 36) & 4095] << 36);
 }
 
 // ---- palettes (crn_comp::pack_color_endpoints / pack_color_selectors / pack_alpha_endpoints /
@@ -308,11 +375,17 @@ std::vector<uint8_t> pack_alpha_selectors(const std::vector<uint64_t>& values) {
 // and optimize_alpha_selectors, crnlib/crn_comp.cpp:921-975, 1236-1282): a per-field cost of the
 // XOR of corresponding 2-bit (colour) or 3-bit (alpha) selectors, costs {0, 5, 14, 10} and
 // {0, 2, 3, 3, 5, 5, 4, 4}.
-inline uint32_t colour_selector_cost(uint64_t a, uint64_t b) {
-  const uint32_t x = (uint32_t)(a ^ b);
-  const uint32_t lo = x & 0x55555555u, hi = (x >> 1) & 0x55555555u;
-  return 5u * (uint32_t)__builtin_popcount(lo & ~hi) + 14u * (uint32_t)__builtin_popcount(hi & ~lo) +
-         10u * (uint32_t)__builtin_popcount(lo & hi);
+// Colour: the 2-bit fields of the XOR, even and odd ones in separate nibbles, each nibble's cost
+// 5 b0 + 14 b1 - 9 b0 b1 (exact in modular arithmetic: every nibble ends in 0..14), then the
+// nibbles summed as bytes; plain integer operations, so the chain's scans vectorise.
+inline uint32_t colour_selector_cost(uint32_t a, uint32_t b) {
+  const uint32_t x = a ^ b;
+  const uint32_t e = x & 0x33333333u, o = (x >> 2) & 0x33333333u;
+  const uint32_t e0 = e & 0x11111111u, e1 = (e >> 1) & 0x11111111u;
+  const uint32_t o0 = o & 0x11111111u, o1 = (o >> 1) & 0x11111111u;
+  const uint32_t ce = 5u * e0 + 14u * e1 - 9u * (e0 & e1), co = 5u * o0 + 14u * o1 - 9u * (o0 & o1);
+  const uint32_t bytes = (ce & 0x0F0F0F0Fu) + ((ce >> 4) & 0x0F0F0F0Fu) + (co & 0x0F0F0F0Fu) + ((co >> 4) & 0x0F0F0F0Fu);
+  return (bytes * 0x01010101u) >> 24;
 }
 // the XOR-delta cost of four 3-bit selectors at once, {0, 2, 3, 3, 5, 5, 4, 4} per selector
 struct AlphaCost4 {
@@ -331,27 +404,38 @@ inline uint32_t alpha_selector_cost(uint64_t a, uint64_t b) {
 // Nearest-neighbour chain over payload values: starting from the entry with the smallest
 // start_cost (its distance from an all-zero entry), repeatedly take the remaining entry closest
 // (cost) to the last one taken (sort_color_endpoints / sort_alpha_endpoints / the selector
-// sorts). Returns each entry's rank.
+// sorts). Returns each entry's rank. `floor` is the least cost two distinct entries can have: a
+// scan that meets it has found its first minimum and stops there. Costs are computed a tile at a
+// time into a buffer (a loop the compiler vectorises), then the tile is searched.
 template <class T, class Start, class Cost>
-std::vector<uint32_t> nearest_chain(const std::vector<T>& payload, Start start_cost, Cost cost) {
+std::vector<uint32_t> nearest_chain(const std::vector<T>& payload, Start start_cost, Cost cost, uint32_t floor) {
   // the remaining entries' ids and payloads are kept dense, in the order a swap-with-last removal
   // leaves them, so the scan (and its first-minimum tie-break) visits them in that order
+  constexpr uint32_t kTile = 256;
   const uint32_t n = (uint32_t)payload.size();
   std::vector<uint32_t> rank(n), id(n);
   std::vector<T> val(payload);
   for (uint32_t i = 0; i < n; i++) id[i] = i;
+  uint32_t c[kTile];
   T cur{};
   for (uint32_t left = n; left; left--) {
     uint32_t best = 0, best_cost = UINT32_MAX;
-    if (left == n) {
-      for (uint32_t i = 0; i < left; i++) {
-        const uint32_t c = start_cost(val[i]);
-        if (c < best_cost) { best_cost = c; best = i; }
+    const uint32_t stop = left == n ? 0u : floor;
+    for (uint32_t t0 = 0; t0 < left && best_cost > stop; t0 += kTile) {
+      const uint32_t m = std::min(kTile, left - t0);
+      const T* v = val.data() + t0;
+      if (left == n) {
+        for (uint32_t i = 0; i < m; i++) c[i] = start_cost(v[i]);
+      } else {
+        for (uint32_t i = 0; i < m; i++) c[i] = cost(v[i], cur);
       }
-    } else {
-      for (uint32_t i = 0; i < left; i++) {
-        const uint32_t c = cost(val[i], cur);
-        if (c < best_cost) { best_cost = c; best = i; }
+      uint32_t tmin = UINT32_MAX;
+      for (uint32_t i = 0; i < m; i++) tmin = std::min(tmin, c[i]);
+      if (tmin < best_cost) {
+        uint32_t i = 0;
+        while (c[i] != tmin) i++;
+        best_cost = tmin;
+        best = t0 + i;
       }
     }
     cur = val[best];
@@ -579,7 +663,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         for (uint64_t b = lv[l].first; b < end; b++)
           for (int c = comp_lo[m]; c < comp_hi[m]; c++) {
             const uint32_t e = rank[eidx[b * ncomp + c]];
-            if (!ref[b]) h[(e + n - prev[c]) % n]++;
+            if (!ref[b]) h[e >= prev[c] ? e - prev[c] : e + n - prev[c]]++;
             prev[c] = e;
           }
       }
@@ -599,10 +683,15 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
       // selectors: nearest-neighbour chain under the XOR-delta cost
       workers.emplace_back([&, m] {
         const std::vector<uint64_t>& v = sel_pal[m]->values;
-        if (m) sel_rank[m] = nearest_chain(v, [](uint64_t a) { return alpha_selector_cost(a, 0); },
-                                           [](uint64_t a, uint64_t b) { return alpha_selector_cost(a, b); });
-        else sel_rank[m] = nearest_chain(v, [](uint64_t a) { return colour_selector_cost(a, 0); },
-                                         [](uint64_t a, uint64_t b) { return colour_selector_cost(a, b); });
+        // least cost between distinct words: one selector off by one (5 colour, 2 alpha)
+        if (m) {
+          sel_rank[m] = nearest_chain(v, [](uint64_t a) { return alpha_selector_cost(a, 0); },
+                                      [](uint64_t a, uint64_t b) { return alpha_selector_cost(a, b); }, 2u);
+        } else {
+          const std::vector<uint32_t> v32(v.begin(), v.end());
+          sel_rank[m] = nearest_chain(v32, [](uint32_t a) { return colour_selector_cost(a, 0u); },
+                                      [](uint32_t a, uint32_t b) { return colour_selector_cost(a, b); }, 5u);
+        }
       });
       workers.emplace_back([&, m, n] {
         // endpoints, unpacked to 8-bit components: colour (r, g, b) of both endpoints, or the two alphas
@@ -618,9 +707,11 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
             c[3 * e + 2] = (int32_t)((bl << 3) | (bl >> 2));
           }
         }
-        // co-occurrence of consecutive endpoints in the delta-coded blocks, both directions,
-        // sorted and run-length counted into rows
-        std::vector<uint64_t> pairs;
+        // co-occurrence of consecutive endpoints in the delta-coded blocks, both directions, as
+        // (entry << 13 | neighbour) keys (indices < kMaxSyms = 2^13), sorted by two stable
+        // counting passes over the 13-bit digits and run-length counted into rows
+        static_assert(kMaxSyms <= (1 << 13), "pair keys hold two 13-bit indices");
+        std::vector<uint32_t> pairs;
         for (uint32_t l = 0; l < levels; l++) {
           uint32_t prev[3] = {0, 0, 0};
           const uint64_t end = lv[l].first + (uint64_t)lv[l].W * lv[l].H * faces;
@@ -628,21 +719,30 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
             for (int c = comp_lo[m]; c < comp_hi[m]; c++) {
               const uint32_t e = eidx[b * ncomp + c];
               if (!ref[b] && e != prev[c]) {
-                pairs.push_back(((uint64_t)e << 32) | prev[c]);
-                pairs.push_back(((uint64_t)prev[c] << 32) | e);
+                pairs.push_back((e << 13) | prev[c]);
+                pairs.push_back((prev[c] << 13) | e);
               }
               prev[c] = e;
             }
         }
-        std::sort(pairs.begin(), pairs.end());
+        {
+          std::vector<uint32_t> sorted(pairs.size()), cnt(8193);
+          for (int shift = 0; shift <= 13; shift += 13) {
+            std::fill(cnt.begin(), cnt.end(), 0u);
+            for (uint32_t k : pairs) cnt[((k >> shift) & 8191u) + 1]++;
+            for (int i = 0; i < 8192; i++) cnt[i + 1] += cnt[i];
+            for (uint32_t k : pairs) sorted[cnt[(k >> shift) & 8191u]++] = k;
+            pairs.swap(sorted);
+          }
+        }
         Adjacency adj;
         adj.start.assign(n + 1, 0);
         adj.total.assign(n, 0);
         for (size_t k = 0; k < pairs.size();) {
           size_t r = k + 1;
           while (r < pairs.size() && pairs[r] == pairs[k]) r++;
-          const uint32_t i = (uint32_t)(pairs[k] >> 32);
-          adj.nb.push_back((uint32_t)pairs[k]);
+          const uint32_t i = pairs[k] >> 13;
+          adj.nb.push_back(pairs[k] & 8191u);
           adj.count.push_back((uint32_t)(r - k));
           adj.start[i + 1]++;
           adj.total[i] += (uint32_t)(r - k);
@@ -658,7 +758,11 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         std::vector<uint32_t> trial[4];
         uint64_t bits[4];
         std::vector<std::thread> tw;
-        tw.emplace_back([&] { trial[0] = nearest_chain(u, comps_norm, comps_dist); bits[0] = stream_bits(m, trial[0]); });
+        // least distance between distinct endpoints: one 6-bit green step (4^2) or one alpha step
+        tw.emplace_back([&] {
+          trial[0] = nearest_chain(u, comps_norm, comps_dist, m ? 1u : 16u);
+          bits[0] = stream_bits(m, trial[0]);
+        });
         for (int t = 0; t < 3; t++)
           tw.emplace_back([&, t] {
             trial[t + 1] = grow_chain(u, adj, first, (uint32_t)((float)unit * (1.0f + weights[t])), unit, m ? 0 : 3);
@@ -683,58 +787,61 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         sidx[b * ncomp + c] = sel_rank[m][sidx[b * ncomp + c]];
       }
   }
-  // block streams: the histograms first, then the coded streams
-  std::vector<uint32_t> h_ref(256, 0), h_ep[2], h_sel[2];
-  if (colour) { h_ep[0].assign(cep.values.size(), 0); h_sel[0].assign(csel.values.size(), 0); }
-  if (nalpha) { h_ep[1].assign(aep.values.size(), 0); h_sel[1].assign(asel.values.size(), 0); }
-  auto ref_at = [&](const Lv& L, uint32_t f, uint32_t y, uint32_t x) -> uint32_t {
-    return ref[L.first + ((uint64_t)f * L.H + y) * L.W + x];
-  };
-  Huff m_ref, m_ep[2], m_sel[2];
-  std::vector<std::vector<uint8_t>> level_data(levels);
-  for (int pass = 0; pass < 2; pass++) {
-    if (pass == 1) {
-      ensure_used(h_ref);
-      m_ref.build(h_ref, 16);
-      for (int m = 0; m < 2; m++) {
-        if (h_ep[m].empty()) continue;
-        ensure_used(h_ep[m]);
-        ensure_used(h_sel[m]);
-        m_ep[m].build(h_ep[m], 16);
-        m_sel[m].build(h_sel[m], 16);
-      }
-    }
-    for (uint32_t l = 0; l < levels; l++) {
-      const Lv& L = lv[l];
-      BitWriter bw;
-      uint32_t prev[3] = {0, 0, 0};
-      for (uint32_t f = 0; f < faces; f++)
-        for (uint32_t y = 0; y < L.H; y++)
-          for (uint32_t x = 0; x < L.W; x++) {
-            if (!(y & 1) && !(x & 1)) {
-              const uint32_t g = ref_at(L, f, y, x) | (ref_at(L, f, y + 1, x) << 2) | (ref_at(L, f, y, x + 1) << 4) |
-                                 (ref_at(L, f, y + 1, x + 1) << 6);
-              if (pass) m_ref.put(bw, g); else h_ref[g]++;
-            }
-            const uint64_t b = L.first + ((uint64_t)f * L.H + y) * L.W + x;
-            for (int c = 0; c < ncomp; c++) {
-              const int m = (colour && c == 0) ? 0 : 1;
-              const uint32_t e = eidx[b * ncomp + c];
-              if (ref[b] == 0) {
-                const uint32_t n = (uint32_t)(m ? aep.values.size() : cep.values.size());
-                const uint32_t d = (e + n - prev[c]) % n;
-                if (pass) m_ep[m].put(bw, d); else h_ep[m][d]++;
-              }
-              prev[c] = e;
-            }
-            for (int c = 0; c < ncomp; c++) {
-              const int m = (colour && c == 0) ? 0 : 1;
-              const uint32_t s = sidx[b * ncomp + c];
-              if (pass) m_sel[m].put(bw, s); else h_sel[m][s]++;
-            }
+  // block streams: one walk records every level's symbols (model << 16 | symbol) and counts them,
+  // then each level is coded behind the finished models. Models: 0 reference groups, 1 / 2 colour
+  // endpoint deltas / selectors, 3 / 4 alpha endpoint deltas / selectors.
+  std::vector<uint32_t> hist[5];
+  hist[0].assign(256, 0);
+  if (colour) { hist[1].assign(cep.values.size(), 0); hist[2].assign(csel.values.size(), 0); }
+  if (nalpha) { hist[3].assign(aep.values.size(), 0); hist[4].assign(asel.values.size(), 0); }
+  const uint32_t pal_n[2] = {(uint32_t)cep.values.size(), (uint32_t)aep.values.size()};
+  std::vector<std::vector<uint32_t>> level_syms(levels);
+  for (uint32_t l = 0; l < levels; l++) {
+    const Lv& L = lv[l];
+    std::vector<uint32_t>& out = level_syms[l];
+    out.reserve((size_t)L.W * L.H * faces * (2 * ncomp + 1));
+    uint32_t prev[3] = {0, 0, 0};
+    for (uint32_t f = 0; f < faces; f++)
+      for (uint32_t y = 0; y < L.H; y++) {
+        const uint64_t row = L.first + ((uint64_t)f * L.H + y) * L.W;
+        for (uint32_t x = 0; x < L.W; x++) {
+          const uint64_t b = row + x;
+          if (!(y & 1) && !(x & 1)) {
+            const uint32_t g = ref[b] | (ref[b + L.W] << 2) | (ref[b + 1] << 4) | (ref[b + L.W + 1] << 6);
+            out.push_back(g);
+            hist[0][g]++;
           }
-      if (pass) level_data[l] = bw.finish();
-    }
+          for (int c = 0; c < ncomp; c++) {
+            const int m = (colour && c == 0) ? 0 : 1;
+            const uint32_t e = eidx[b * ncomp + c];
+            if (ref[b] == 0) {
+              const uint32_t d = e >= prev[c] ? e - prev[c] : e + pal_n[m] - prev[c];
+              out.push_back(((uint32_t)(1 + 2 * m) << 16) | d);
+              hist[1 + 2 * m][d]++;
+            }
+            prev[c] = e;
+          }
+          for (int c = 0; c < ncomp; c++) {
+            const int m = (colour && c == 0) ? 0 : 1;
+            const uint32_t sel = sidx[b * ncomp + c];
+            out.push_back(((uint32_t)(2 + 2 * m) << 16) | sel);
+            hist[2 + 2 * m][sel]++;
+          }
+        }
+      }
+  }
+  Huff models[5];
+  for (int k = 0; k < 5; k++) {
+    if (hist[k].empty()) continue;
+    ensure_used(hist[k]);
+    models[k].build(hist[k], 16);
+  }
+  std::vector<std::vector<uint8_t>> level_data(levels);
+  for (uint32_t l = 0; l < levels; l++) {
+    BitWriter bw;
+    for (uint32_t v : level_syms[l]) models[v >> 16].put(bw, v & 0xFFFFu);
+    level_data[l] = bw.finish();
+    std::vector<uint32_t>().swap(level_syms[l]);
   }
   std::vector<uint8_t> pal[4];
   if (colour) {
@@ -749,9 +856,9 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
   std::vector<uint8_t> tables;
   {
     BitWriter bw;
-    send_model(bw, m_ref);
-    if (colour) { send_model(bw, m_ep[0]); send_model(bw, m_sel[0]); }
-    if (nalpha) { send_model(bw, m_ep[1]); send_model(bw, m_sel[1]); }
+    send_model(bw, models[0]);
+    if (colour) { send_model(bw, models[1]); send_model(bw, models[2]); }
+    if (nalpha) { send_model(bw, models[3]); send_model(bw, models[4]); }
     tables = bw.finish();
   }
   if (tables.size() > 0xFFFF) { set_error("crngpu_crn_pack: model tables too large"); return CRNGPU_E_PARAM; }
