@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <thread>
 #include <vector>
@@ -140,6 +141,40 @@ struct Huff {
   }
   void put(BitWriter& bw, uint32_t sym) const { bw.put(code[sym], len[sym]); }
 };
+
+// A symbol list (model << 16 | symbol) coded behind its models, MSB first, as BitWriter would
+// write it: the accumulator in locals, whole 32-bit words stored into a buffer sized for the
+// longest codes (16 bits a symbol).
+std::vector<uint8_t> code_symbols(const std::vector<uint32_t>& syms, const Huff* models, int nmodels) {
+  const uint32_t* code[8];
+  const uint8_t* len[8];
+  for (int k = 0; k < nmodels; k++) {
+    code[k] = models[k].code.data();
+    len[k] = models[k].len.data();
+  }
+  std::vector<uint8_t> out(syms.size() * 2 + 8);
+  uint8_t* p = out.data();
+  uint64_t acc = 0;
+  uint32_t n = 0;
+  for (uint32_t v : syms) {
+    const uint32_t k = v >> 16, sym = v & 0xFFFFu, l = len[k][sym];
+    acc = (acc << l) | code[k][sym];  // a canonical code of l bits is below 2^l
+    n += l;
+    if (n >= 32) {
+      n -= 32;
+      const uint32_t w = (uint32_t)(acc >> n);
+      p[0] = (uint8_t)(w >> 24); p[1] = (uint8_t)(w >> 16); p[2] = (uint8_t)(w >> 8); p[3] = (uint8_t)w;
+      p += 4;
+    }
+  }
+  while (n >= 8) {
+    n -= 8;
+    *p++ = (uint8_t)(acc >> n);
+  }
+  if (n) *p++ = (uint8_t)(acc << (8 - n));
+  out.resize((size_t)(p - out.data()));
+  return out;
+}
 
 // symbol_codec's static model transmission, the inverse of
 // decode_receive_static_data_model (inc/crn_decomp.h:3044-3123): 14-bit symbol count, the 21
@@ -478,13 +513,14 @@ std::vector<uint32_t> grow_chain(const std::vector<Comps>& u, const Adjacency& a
   // per remaining entry (dense slots, swap-with-last removal): id, accumulated co-occurrence,
   // similarity to the front and to the back of the chain, components
   const uint32_t n = (uint32_t)u.size();
-  std::vector<uint32_t> id, freq, sim_f, sim_b, row(n, 0), pos(n, UINT32_MAX), chain(2 * n + 1);
-  std::vector<int32_t> cc[6];  // components, one array each, so the distance loops vectorise
+  std::vector<uint32_t> id, freq, slot_of(n, UINT32_MAX), pos(n, UINT32_MAX), chain(2 * n + 1);
+  std::vector<uint16_t> sim_f, sim_b;
+  std::vector<int16_t> cc[6];  // components, one array each, so the distance loops vectorise
   id.reserve(n);
   for (uint32_t i = 0; i < n; i++)
     if (i != first) {
       id.push_back(i);
-      for (int k = 0; k < 6; k++) cc[k].push_back(u[i].c[k]);
+      for (int k = 0; k < 6; k++) cc[k].push_back((int16_t)u[i].c[k]);
     }
   freq.assign(id.size(), 0);
   sim_f.assign(id.size(), 0);
@@ -492,28 +528,41 @@ std::vector<uint32_t> grow_chain(const std::vector<Comps>& u, const Adjacency& a
   uint32_t lo = n, hi = n;
   chain[n] = first;
   pos[first] = n;
-  auto load = [&](uint32_t s, bool on) {
-    for (uint32_t k = adj.start[s]; k < adj.start[s + 1]; k++) row[adj.nb[k]] = on ? adj.count[k] : 0;
+  // a taken entry's co-occurrences join the accumulated counts of the entries still remaining
+  for (uint32_t i = 0; i < (uint32_t)id.size(); i++) slot_of[id[i]] = i;
+  auto take_row = [&](uint32_t s) {
+    for (uint32_t k = adj.start[s]; k < adj.start[s + 1]; k++) {
+      const uint32_t sl = slot_of[adj.nb[k]];
+      if (sl != UINT32_MAX) freq[sl] += adj.count[k];
+    }
   };
-  load(first, true);
-  uint32_t last = first;
+  take_row(first);
   Comps front = u[first], back = u[first];
   bool front_new = true, back_new = true;
   uint64_t normaliser = 0;
-  // similarity of every remaining entry to a new chain end
-  auto similarity = [&](const Comps& end, uint32_t* sim, size_t m) {
-    const int32_t e0 = end.c[0], e1 = end.c[1], e2 = end.c[2], e3 = end.c[3], e4 = end.c[4], e5 = end.c[5];
-    const int32_t *c0 = cc[0].data(), *c1 = cc[1].data(), *c2 = cc[2].data(), *c3 = cc[3].data(), *c4 = cc[4].data(),
+  // similarity of every remaining entry to a new chain end, base - min(distance, cap), in 16-bit
+  // lanes: a squared component difference (<= 255^2) is clamped to cap before the sum, so the sum
+  // (<= 6 cap) cannot wrap and its minimum with cap is min(distance, cap). Needs cap <= 10922 and
+  // base <= 65535 (the callers' units are 4000 and 1000, base at most 1.5 units).
+  const uint16_t cap16 = (uint16_t)cap, base16 = (uint16_t)base;
+  auto similarity = [&](const Comps& end, uint16_t* sim, size_t m) {
+    const int16_t e0 = (int16_t)end.c[0], e1 = (int16_t)end.c[1], e2 = (int16_t)end.c[2], e3 = (int16_t)end.c[3],
+                  e4 = (int16_t)end.c[4], e5 = (int16_t)end.c[5];
+    const int16_t *c0 = cc[0].data(), *c1 = cc[1].data(), *c2 = cc[2].data(), *c3 = cc[3].data(), *c4 = cc[4].data(),
                   *c5 = cc[5].data();
+    auto sq = [cap16](int16_t a, int16_t b) -> uint16_t {
+      const uint16_t x = (uint16_t)(a - b);
+      const uint16_t q = (uint16_t)((uint32_t)x * x);  // the square modulo 2^16: exact, at most 255^2
+      return q < cap16 ? q : cap16;
+    };
     for (size_t i = 0; i < m; i++) {
-      const int32_t d0 = c0[i] - e0, d1 = c1[i] - e1, d2 = c2[i] - e2, d3 = c3[i] - e3, d4 = c4[i] - e4, d5 = c5[i] - e5;
-      const uint32_t d = (uint32_t)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5);
-      sim[i] = base - (d < cap ? d : cap);
+      const uint16_t d = (uint16_t)(sq(c0[i], e0) + sq(c1[i], e1) + sq(c2[i], e2) + sq(c3[i], e3) + sq(c4[i], e4) +
+                                    sq(c5[i], e5));
+      sim[i] = (uint16_t)(base16 - (d < cap16 ? d : cap16));
     }
   };
   while (!id.empty()) {
     const size_t m = id.size();
-    for (size_t i = 0; i < m; i++) freq[i] += row[id[i]];
     if (front_new) similarity(front, sim_f.data(), m);
     if (back_new) similarity(back, sim_b.data(), m);
     uint64_t best_val = 0;
@@ -524,9 +573,6 @@ std::vector<uint32_t> grow_chain(const std::vector<Comps>& u, const Adjacency& a
     }
     const uint32_t s = id[best];
     const uint32_t sf = sim_f[best], sb = sim_b[best], fs = freq[best];
-    load(last, false);
-    load(s, true);
-    last = s;
     // co-occurrence of s with each half of the chain, weighted (L-1-2k) by distance k from that end
     const int64_t L = (int64_t)hi - lo + 1;
     uint64_t w_front = 0, w_back = 0;
@@ -548,6 +594,9 @@ std::vector<uint32_t> grow_chain(const std::vector<Comps>& u, const Adjacency& a
     freq[best] = freq[m - 1]; freq.pop_back();
     sim_f[best] = sim_f[m - 1]; sim_f.pop_back();
     sim_b[best] = sim_b[m - 1]; sim_b.pop_back();
+    slot_of[s] = UINT32_MAX;
+    if (best < id.size()) slot_of[id[best]] = (uint32_t)best;
+    take_row(s);
   }
   std::vector<uint32_t> rank(n);
   for (uint32_t p = lo; p <= hi; p++) rank[chain[p]] = p - lo;
@@ -603,24 +652,50 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
   Palette cep, csel, aep, asel;
   const int ncomp = (colour ? 1 : 0) + nalpha;
   std::vector<uint32_t> eidx((size_t)nblocks * ncomp), sidx((size_t)nblocks * ncomp);
-  for (uint64_t b = 0; b < nblocks; b++) {
-    const uint8_t* blk = blocks + b * bpb;
-    int c = 0;
-    if (colour) {
-      const uint8_t* cb = blk + (bpb == 16 ? 8 : 0);
-      uint32_t ep, sel;
-      std::memcpy(&ep, cb, 4);
-      std::memcpy(&sel, cb + 4, 4);
-      eidx[b * ncomp + c] = cep.add(ep);
-      sidx[b * ncomp + c] = csel.add(dxt1_sel_to_linear(sel));
-      c++;
+  // the four palettes are independent (each in its own first-use order): one thread each on large
+  // inputs
+  auto colour_endpoints = [&] {
+    for (uint64_t b = 0; b < nblocks; b++) {
+      uint32_t ep;
+      std::memcpy(&ep, blocks + b * bpb + (bpb == 16 ? 8 : 0), 4);
+      eidx[b * ncomp] = cep.add(ep);
     }
-    for (int a = 0; a < nalpha; a++, c++) {
-      const uint8_t* ab = blk + 8 * a;
-      uint64_t sel = 0;
-      for (int k = 0; k < 6; k++) sel |= (uint64_t)ab[2 + k] << (8 * k);
-      eidx[b * ncomp + c] = aep.add((uint64_t)ab[0] | ((uint64_t)ab[1] << 8));
-      sidx[b * ncomp + c] = asel.add(dxt5_sel_to_linear(sel));
+  };
+  auto colour_selectors = [&] {
+    for (uint64_t b = 0; b < nblocks; b++) {
+      uint32_t sel;
+      std::memcpy(&sel, blocks + b * bpb + (bpb == 16 ? 8 : 0) + 4, 4);
+      sidx[b * ncomp] = csel.add(dxt1_sel_to_linear(sel));
+    }
+  };
+  const int c_alpha = colour ? 1 : 0;
+  auto alpha_endpoints = [&] {
+    for (uint64_t b = 0; b < nblocks; b++)
+      for (int a = 0; a < nalpha; a++) {
+        const uint8_t* ab = blocks + b * bpb + 8 * a;
+        eidx[b * ncomp + c_alpha + a] = aep.add((uint64_t)ab[0] | ((uint64_t)ab[1] << 8));
+      }
+  };
+  auto alpha_selectors = [&] {
+    for (uint64_t b = 0; b < nblocks; b++)
+      for (int a = 0; a < nalpha; a++) {
+        const uint8_t* ab = blocks + b * bpb + 8 * a;
+        uint64_t sel = 0;
+        for (int k = 0; k < 6; k++) sel |= (uint64_t)ab[2 + k] << (8 * k);
+        sidx[b * ncomp + c_alpha + a] = asel.add(dxt5_sel_to_linear(sel));
+      }
+  };
+  {
+    std::vector<std::function<void()>> jobs;
+    if (colour) { jobs.emplace_back(colour_endpoints); jobs.emplace_back(colour_selectors); }
+    if (nalpha) { jobs.emplace_back(alpha_endpoints); jobs.emplace_back(alpha_selectors); }
+    if (nblocks < 16384) {
+      for (auto& j : jobs) j();
+    } else {
+      std::vector<std::thread> t;
+      for (size_t k = 1; k < jobs.size(); k++) t.emplace_back(jobs[k]);
+      jobs[0]();
+      for (auto& x : t) x.join();
     }
   }
   if (cep.values.size() > (size_t)kMaxSyms || csel.values.size() > (size_t)kMaxSyms ||
@@ -765,6 +840,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         });
         for (int t = 0; t < 3; t++)
           tw.emplace_back([&, t] {
+            static_assert(4000u * 3 / 2 <= 65535u && 4000u <= 10922u, "grow_chain's 16-bit similarity");
             trial[t + 1] = grow_chain(u, adj, first, (uint32_t)((float)unit * (1.0f + weights[t])), unit, m ? 0 : 3);
             bits[t + 1] = stream_bits(m, trial[t + 1]);
           });
@@ -838,9 +914,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
   }
   std::vector<std::vector<uint8_t>> level_data(levels);
   for (uint32_t l = 0; l < levels; l++) {
-    BitWriter bw;
-    for (uint32_t v : level_syms[l]) models[v >> 16].put(bw, v & 0xFFFFu);
-    level_data[l] = bw.finish();
+    level_data[l] = code_symbols(level_syms[l], models, 5);
     std::vector<uint32_t>().swap(level_syms[l]);
   }
   std::vector<uint8_t> pal[4];
