@@ -93,8 +93,8 @@ def clustered_leg(cg, dev, levels, blocks, texels, steps: int) -> dict:
             "quality": 128, "rmse": round(crn_rmse(our_crn), 4), "rmse_reference_crn": round(crn_rmse(ref_crn), 4),
             "bits_per_texel": round(len(our_crn) * 8 / texels, 4),
             "bits_per_texel_reference": round(len(ref_crn) * 8 / texels, 4),
-            "path": "crngpu_compress_crn: host RGBA8 mip chain -> crn_comp block gather (host) -> H2D -> "
-                    "clustered encode (every dxt_hc stage on the GPU) -> D2H -> .crn writer (host); wall time"}
+            "path": "crngpu_compress_crn: host RGBA8 mip chain -> H2D -> crn_comp block gather and clustered "
+                    "encode (every dxt_hc stage) on the GPU -> D2H -> .crn writer (host); wall time"}
 
 
 QDXT_REFERENCE = os.path.join(ROOT, "tests", "golden", "qdxt_reference.json")

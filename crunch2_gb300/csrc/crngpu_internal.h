@@ -113,6 +113,17 @@ int dxt5a_chunks_max_grid();
 // launch_dxt5a: quality sets the probe grid (+-16 Uber, +-8 Better, none below).
 int launch_dxt1(const uint8_t* d_blocks, uint32_t n, uint32_t opts, uint8_t* d_out, uint32_t out_stride,
                 uint64_t* d_err, cudaStream_t s);
+// One image of a host mip chain uploaded as a whole, gathered into 4x4 blocks of cooked texels
+// (cook_texel) by launch_gather_chain: the image's blocks are [first, the next image's first),
+// bx to a row, texels edge-clamped to w x h.
+struct GatherImage {
+  uint64_t src;      // byte offset of the image in the uploaded chain
+  uint32_t w, h, bx;
+  uint32_t first;    // first block of the image in the output
+};
+int launch_gather_chain(const uint8_t* d_chain, const GatherImage* d_imgs, uint32_t nimg, uint32_t blocks,
+                        uint32_t format, uint32_t* d_out, cudaStream_t s);
+
 // dds_comp at quality 255 for a whole texture (host RGBA8 levels, face after face, level after
 // level, tightly packed): every block of every face and level through the plain encoder, output in
 // DDS order at minimal pitch. Returns the output bytes (or the bytes needed when out is NULL or

@@ -45,11 +45,6 @@ __global__ void k_gather_blocks(const uint8_t* __restrict__ img, uint32_t w, uin
 
 // Level -> 4x4 blocks as k_gather_blocks, each texel cooked for the target format (cook_texel).
 // Several images (faces and levels) in one launch: job j covers blocks [first[j], first[j + 1]).
-struct GatherImage {
-  uint64_t src;      // byte offset of the image in the uploaded chain
-  uint32_t w, h, bx;
-  uint32_t first;    // first block of the image in the output
-};
 __global__ void k_gather_chain(const uint8_t* __restrict__ chain, const GatherImage* __restrict__ imgs, uint32_t nimg,
                                uint32_t total_blocks, uint32_t format, uint32_t* __restrict__ out) {
   for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < (uint64_t)total_blocks * 16;
@@ -156,6 +151,15 @@ int with_buffers(const uint8_t* in, size_t in_bytes, uint8_t* out, size_t out_by
 
 }  // namespace
 
+int launch_gather_chain(const uint8_t* d_chain, const GatherImage* d_imgs, uint32_t nimg, uint32_t blocks,
+                        uint32_t format, uint32_t* d_out, cudaStream_t s) {
+  if (!nimg || !blocks) return CRNGPU_OK;
+  const uint64_t texels = (uint64_t)blocks * 16;
+  const uint32_t grid = (uint32_t)std::min<uint64_t>((texels + 255) / 256, 65535);
+  k_gather_chain<<<grid, 256, 0, s>>>(d_chain, d_imgs, nimg, blocks, format, d_out);
+  return cuda_check(cudaGetLastError(), "launch k_gather_chain");
+}
+
 int64_t dds_plain_chain(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels, uint32_t faces,
                         uint32_t format, uint32_t flags, uint32_t quality, uint32_t threshold, void* out,
                         uint64_t out_capacity) {
@@ -196,12 +200,10 @@ int64_t dds_plain_chain(const uint8_t* rgba_levels, uint32_t width, uint32_t hei
       (e = cudaMemcpyAsync(table.ptr, imgs.data(), sizeof(GatherImage) * imgs.size(), cudaMemcpyHostToDevice, s)) !=
           cudaSuccess)
     return cuda_check(e, "upload chain");
-  const uint64_t texels = (uint64_t)blocks * 16;
-  const uint32_t grid = (uint32_t)std::min<uint64_t>((texels + 255) / 256, 65535);
-  k_gather_chain<<<grid, 256, 0, s>>>(static_cast<const uint8_t*>(chain.ptr), static_cast<const GatherImage*>(table.ptr),
-                                      (uint32_t)imgs.size(), blocks, format, static_cast<uint32_t*>(gathered.ptr));
-  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_check(e, "launch k_gather_chain");
-  int rc = encode_device(static_cast<const uint8_t*>(gathered.ptr), blocks, format, flags, quality, threshold,
+  int rc = launch_gather_chain(static_cast<const uint8_t*>(chain.ptr), static_cast<const GatherImage*>(table.ptr),
+                               (uint32_t)imgs.size(), blocks, format, static_cast<uint32_t*>(gathered.ptr), s);
+  if (rc != CRNGPU_OK) return rc;
+  rc = encode_device(static_cast<const uint8_t*>(gathered.ptr), blocks, format, flags, quality, threshold,
                          static_cast<uint8_t*>(encoded.ptr), nullptr, s);
   if (rc != CRNGPU_OK) return rc;
   if ((e = cudaMemcpyAsync(out, encoded.ptr, need, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||

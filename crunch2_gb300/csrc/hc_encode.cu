@@ -3195,18 +3195,19 @@ extern "C" int crngpu_hc_codebook_sizes(uint32_t width, uint32_t height, uint32_
 
 // crn_compress with m_file_type = cCRNFileTypeCRN and source mips (inc/crnlib.h:614,
 // crnlib/crnlib.cpp:242-267 -> crn_comp::compress_internal, crnlib/crn_comp.cpp:1515-1611):
-// crn_comp's block gather (edge clamped, levels padded to 8 texels, crn_comp.cpp:717-741), the
+// crn_comp's block gather (edge clamped, levels padded to 8 texels, crn_comp.cpp:717-741) and the
 // clustered encode on the GPU, then the .crn writer on the host.
 namespace crngpu {
 namespace {
 
 // The quality-independent part of crn_compress: the blocks of every level and face in crn_comp's
-// layout (crn_comp::alias_images / quantize_images, crnlib/crn_comp.cpp:454-463, 717-741),
-// gathered on the host with edge clamping and uploaded once; a pass per quality level then runs
-// the clustered encode and the writer.
-// per host thread: the gathered blocks and the encoded blocks on the device, kept between calls
+// layout (crn_comp::alias_images / quantize_images, crnlib/crn_comp.cpp:454-463, 717-741): the
+// host chain uploaded once and gathered on the GPU with edge clamping (k_gather_chain); a pass per
+// quality level then runs the clustered encode and the writer.
+// per host thread: the uploaded chain, the gathered blocks and the encoded blocks on the device,
+// kept between calls
 struct CrnDeviceBuffers {
-  DevBuf in, out, st, words;
+  DevBuf in, out, st, words, chain, images;
 };
 CrnDeviceBuffers& crn_buffers() {
   static thread_local std::unique_ptr<CrnDeviceBuffers> b[64];
@@ -3239,7 +3240,8 @@ struct CrnSource {
     width = w; height = h; levels = nl; faces = nf; format = fmt;
     std::memset(&P, 0, sizeof(P));
     P.struct_size = sizeof(P);
-    std::vector<uint32_t> blocks;
+    // the host chain (face after face, level after level) is uploaded as it is; the gather into
+    // crn_comp's layout (levels in order, a level's faces one after another) runs on the GPU
     std::vector<size_t> img_ofs((size_t)faces * levels);
     size_t ofs = 0;
     for (uint32_t f = 0; f < faces; f++)
@@ -3248,27 +3250,21 @@ struct CrnSource {
         ofs += (size_t)std::max(1u, width >> l) * std::max(1u, height >> l) * 4;
         texels += (uint64_t)std::max(1u, width >> l) * std::max(1u, height >> l);
       }
+    std::vector<GatherImage> imgs;
+    uint32_t nblocks = 0;
     for (uint32_t l = 0; l < levels; l++) {
       const uint32_t lw = std::max(1u, width >> l), lh = std::max(1u, height >> l);
       const uint32_t W = ((lw + 7) & ~7u) >> 2, H = ((lh + 7) & ~7u) >> 2;
-      P.levels[l].first_block = (uint32_t)(blocks.size() / 16);
+      P.levels[l].first_block = nblocks;
       P.levels[l].num_blocks = W * H * faces;
       P.levels[l].block_width = W;
       P.levels[l].weight = std::min(12.0f, powf(1.3f, (float)l));
       for (uint32_t f = 0; f < faces; f++) {
-        const uint32_t* img = reinterpret_cast<const uint32_t*>(rgba_levels + img_ofs[(size_t)f * levels + l]);
-        for (uint32_t by = 0; by < H; by++)
-          for (uint32_t bx = 0; bx < W; bx++)
-            for (uint32_t dy = 0; dy < 4; dy++)
-              for (uint32_t dx = 0; dx < 4; dx++) {
-                const uint32_t x = std::min(bx * 4 + dx, lw - 1), y = std::min(by * 4 + dy, lh - 1);
-                uint32_t px;
-                std::memcpy(&px, img + (size_t)y * lw + x, 4);
-                blocks.push_back(cook_texel(format, px));
-              }
+        imgs.push_back(GatherImage{(uint64_t)img_ofs[(size_t)f * levels + l], lw, lh, W, nblocks});
+        nblocks += W * H;
       }
     }
-    P.num_blocks = (uint32_t)(blocks.size() / 16);
+    P.num_blocks = nblocks;
     P.num_levels = levels;
     P.num_faces = faces;
     const bool colour_fmt = format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5;
@@ -3281,11 +3277,19 @@ struct CrnSource {
     P.alpha_component = opt.alpha_component;
     bpb = (format == CRNGPU_FMT_DXT1 || format == CRNGPU_FMT_DXT5A) ? 8 : 16;
     cudaError_t e;
-    if ((e = d_in.ensure(blocks.size() * 4)) != cudaSuccess || (e = d_out.ensure((size_t)P.num_blocks * bpb)) != cudaSuccess)
+    CrnDeviceBuffers& cb = crn_buffers();
+    if ((e = d_in.ensure((size_t)nblocks * 64)) != cudaSuccess ||
+        (e = d_out.ensure((size_t)P.num_blocks * bpb)) != cudaSuccess || (e = cb.chain.ensure(ofs)) != cudaSuccess ||
+        (e = cb.images.ensure(sizeof(GatherImage) * imgs.size())) != cudaSuccess)
       return cuda_check(e, "alloc blocks");
-    if ((e = cudaMemcpyAsync(d_in.ptr, blocks.data(), blocks.size() * 4, cudaMemcpyHostToDevice, stream)) != cudaSuccess)
-      return cuda_check(e, "copy blocks");
-    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_check(e, "sync");  // `blocks` is freed next
+    if ((e = cudaMemcpyAsync(cb.chain.ptr, rgba_levels, ofs, cudaMemcpyHostToDevice, stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(cb.images.ptr, imgs.data(), sizeof(GatherImage) * imgs.size(), cudaMemcpyHostToDevice,
+                             stream)) != cudaSuccess)
+      return cuda_check(e, "upload chain");
+    int rc = launch_gather_chain(static_cast<const uint8_t*>(cb.chain.ptr), static_cast<const GatherImage*>(cb.images.ptr),
+                                 (uint32_t)imgs.size(), nblocks, format, static_cast<uint32_t*>(d_in.ptr), stream);
+    if (rc != CRNGPU_OK) return rc;
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_check(e, "sync");  // `imgs` is freed next
     return CRNGPU_OK;
   }
 
