@@ -64,3 +64,69 @@ def test_pack_rejects_unclusterable_and_bad_input(cg):
     with pytest.raises(cg.CrnGpuError):
         cg.crn_pack(big, 512, 512, 1, 1, 0)
     assert cg.crn_pack(blocks, 256, 256, 1, 1, 0)[:2] == b"Hx"
+
+
+def synthetic_levels(rng, w, h, faces, bpb, colour, nalpha):
+    """Visible blocks per level and face drawn from small pools, with runs of repeated endpoints,
+    as a clustered encode leaves them."""
+    levels = []
+    l = 0
+    while True:
+        lw, lh = max(1, w >> l), max(1, h >> l)
+        by, bx = (lh + 3) // 4, (lw + 3) // 4
+        fl = []
+        for _ in range(faces):
+            n = by * bx
+            blk = np.zeros((n, bpb), np.uint8)
+            pick = rng.integers(0, 40, n)
+            runs = rng.random(n) < 0.4
+            for i in range(1, n):
+                if runs[i]:
+                    pick[i] = pick[i - 1]
+            for a in range(nalpha):
+                blk[:, 8 * a:8 * a + 2] = rng.integers(0, 256, (40, 2), dtype=np.uint8)[pick]
+                blk[:, 8 * a + 2:8 * a + 8] = rng.integers(0, 256, (25, 6), dtype=np.uint8)[rng.integers(0, 25, n)]
+            if colour:
+                c = 8 if bpb == 16 else 0
+                blk[:, c:c + 4] = rng.integers(0, 256, (40, 4), dtype=np.uint8)[pick]
+                blk[:, c + 4:c + 8] = rng.integers(0, 256, (30, 4), dtype=np.uint8)[rng.integers(0, 30, n)]
+            fl.append(blk.reshape(by, bx, bpb))
+        levels.append(fl)
+        if lw == 1 and lh == 1:
+            return levels
+        l += 1
+
+
+# (format, bytes per block, colour block, alpha blocks, width, height, faces) -> sha256 of the file.
+# The writer's bytes are pinned (the hashes are of the files the straightforward form of the
+# writer made: full chain scans, a sorted pair list, heap-built Huffman trees, a bit-at-a-time
+# writer); its restatements for speed must leave them unchanged.
+WRITER_CASES = {
+    ("DXT1", 8, True, 0, 100, 60, 1):
+        "58421731e4e3c2976369a3007a665dcd472b04a1157043bf279cafdb719832e2",
+    ("DXT1", 8, True, 0, 64, 64, 6):
+        "053ba262df93808a4b95584ad7e8b5c4483e2ced4a68875d2f775c9675bb604c",
+    ("DXT5", 16, True, 1, 256, 128, 1):
+        "9c5dd8cd4ec5cd65824df5d616a037522a99ee00a698e93c5fb86751b9add5bc",
+    ("DXN_XY", 16, False, 2, 96, 200, 1):
+        "715c9aa169dcae8d58ebb0de222cef4a672440e0fcef82d2a04e3b8e1deffe36",
+    ("DXT5A", 8, False, 1, 128, 128, 6):
+        "595c03e7c0856c7b5cb0bc4f9f336426a5686fc398c47e249a99e5a4a4926074",
+}
+
+
+@pytest.mark.parametrize("case", sorted(WRITER_CASES))
+def test_writer_bytes_are_pinned(cg, case):
+    import hashlib
+    from oracle import port
+    name, bpb, colour, nalpha, w, h, faces = case
+    rng = np.random.default_rng(1000 + sorted(WRITER_CASES).index(case))
+    levels = synthetic_levels(rng, w, h, faces, bpb, colour, nalpha)
+    blocks = cg.crn_layout_from_levels(levels, w, h, faces, bpb)
+    packed = cg.crn_pack(blocks, w, h, len(levels), faces, FMT[name])
+    for l, fl in enumerate(levels):
+        raw = port.unpack_level(packed, l, sum(x.size for x in fl))
+        assert np.array_equal(raw, np.concatenate([x.reshape(-1) for x in fl])), (case, l)
+    digest = hashlib.sha256(packed).hexdigest()
+    print(case, len(packed), digest)
+    assert digest == WRITER_CASES[case], (case, digest)
