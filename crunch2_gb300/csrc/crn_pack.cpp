@@ -485,15 +485,51 @@ std::vector<uint32_t> nearest_chain(const std::vector<T>& payload, Start start_c
 struct Comps {
   int32_t c[6];
 };
-inline uint32_t comps_dist(const Comps& a, const Comps& b) {
-  uint32_t d = 0;
-  for (int k = 0; k < 6; k++) d += (uint32_t)((a.c[k] - b.c[k]) * (a.c[k] - b.c[k]));
-  return d;
-}
-inline uint32_t comps_norm(const Comps& a) {
-  uint32_t d = 0;
-  for (int k = 0; k < 6; k++) d += (uint32_t)(a.c[k] * a.c[k]);
-  return d;
+
+// nearest_chain over endpoints, the cost the squared distance of the six components (the start
+// cost: the distance from the all-zero entry), with the components in one array each so that the
+// distance loop vectorises; the same scan order, first-minimum tie-break and stop at `floor`.
+std::vector<uint32_t> nearest_chain_comps(const std::vector<Comps>& u, uint32_t floor) {
+  constexpr uint32_t kTile = 256;
+  const uint32_t n = (uint32_t)u.size();
+  std::vector<uint32_t> rank(n), id(n);
+  std::vector<int32_t> cc[6];
+  for (int k = 0; k < 6; k++) cc[k].resize(n);
+  for (uint32_t i = 0; i < n; i++) {
+    id[i] = i;
+    for (int k = 0; k < 6; k++) cc[k][i] = u[i].c[k];
+  }
+  uint32_t c[kTile];
+  int32_t cur[6] = {0, 0, 0, 0, 0, 0};
+  for (uint32_t left = n; left; left--) {
+    uint32_t best = 0, best_cost = UINT32_MAX;
+    const uint32_t stop = left == n ? 0u : floor;
+    for (uint32_t t0 = 0; t0 < left && best_cost > stop; t0 += kTile) {
+      const uint32_t m = std::min(kTile, left - t0);
+      const int32_t *c0 = cc[0].data() + t0, *c1 = cc[1].data() + t0, *c2 = cc[2].data() + t0,
+                    *c3 = cc[3].data() + t0, *c4 = cc[4].data() + t0, *c5 = cc[5].data() + t0;
+      for (uint32_t i = 0; i < m; i++) {
+        const int32_t d0 = c0[i] - cur[0], d1 = c1[i] - cur[1], d2 = c2[i] - cur[2], d3 = c3[i] - cur[3],
+                      d4 = c4[i] - cur[4], d5 = c5[i] - cur[5];
+        c[i] = (uint32_t)(d0 * d0 + d1 * d1 + d2 * d2 + d3 * d3 + d4 * d4 + d5 * d5);
+      }
+      uint32_t tmin = UINT32_MAX;
+      for (uint32_t i = 0; i < m; i++) tmin = std::min(tmin, c[i]);
+      if (tmin < best_cost) {
+        uint32_t i = 0;
+        while (c[i] != tmin) i++;
+        best_cost = tmin;
+        best = t0 + i;
+      }
+    }
+    for (int k = 0; k < 6; k++) {
+      cur[k] = cc[k][best];
+      cc[k][best] = cc[k][left - 1];
+    }
+    rank[id[best]] = n - left;
+    id[best] = id[left - 1];
+  }
+  return rank;
 }
 
 // Symmetric counts of consecutive endpoint indices in the coded stream, as compressed rows.
@@ -648,7 +684,8 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
     lv[l] = Lv{((w + 7) & ~7u) >> 2, ((h + 7) & ~7u) >> 2, (uint32_t)nblocks};
     nblocks += (uint64_t)lv[l].W * lv[l].H * faces;
   }
-  // per block: endpoint / selector palette indices of each component (colour, alpha0, alpha1)
+  // endpoint / selector palette indices of each component (colour, alpha0, alpha1), component
+  // after component
   Palette cep, csel, aep, asel;
   const int ncomp = (colour ? 1 : 0) + nalpha;
   std::vector<uint32_t> eidx((size_t)nblocks * ncomp), sidx((size_t)nblocks * ncomp);
@@ -658,14 +695,14 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
     for (uint64_t b = 0; b < nblocks; b++) {
       uint32_t ep;
       std::memcpy(&ep, blocks + b * bpb + (bpb == 16 ? 8 : 0), 4);
-      eidx[b * ncomp] = cep.add(ep);
+      eidx[b] = cep.add(ep);
     }
   };
   auto colour_selectors = [&] {
     for (uint64_t b = 0; b < nblocks; b++) {
       uint32_t sel;
       std::memcpy(&sel, blocks + b * bpb + (bpb == 16 ? 8 : 0) + 4, 4);
-      sidx[b * ncomp] = csel.add(dxt1_sel_to_linear(sel));
+      sidx[b] = csel.add(dxt1_sel_to_linear(sel));
     }
   };
   const int c_alpha = colour ? 1 : 0;
@@ -673,7 +710,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
     for (uint64_t b = 0; b < nblocks; b++)
       for (int a = 0; a < nalpha; a++) {
         const uint8_t* ab = blocks + b * bpb + 8 * a;
-        eidx[b * ncomp + c_alpha + a] = aep.add((uint64_t)ab[0] | ((uint64_t)ab[1] << 8));
+        eidx[(size_t)(c_alpha + a) * nblocks + b] = aep.add((uint64_t)ab[0] | ((uint64_t)ab[1] << 8));
       }
   };
   auto alpha_selectors = [&] {
@@ -682,7 +719,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         const uint8_t* ab = blocks + b * bpb + 8 * a;
         uint64_t sel = 0;
         for (int k = 0; k < 6; k++) sel |= (uint64_t)ab[2 + k] << (8 * k);
-        sidx[b * ncomp + c_alpha + a] = asel.add(dxt5_sel_to_linear(sel));
+        sidx[(size_t)(c_alpha + a) * nblocks + b] = asel.add(dxt5_sel_to_linear(sel));
       }
   };
   {
@@ -714,9 +751,9 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         const uint64_t b = L.first + (uint64_t)row * L.W + x;
         bool left = row || x, top = row != 0;
         for (int c = 0; c < ncomp; c++) {
-          const uint32_t e = eidx[b * ncomp + c];
-          if (left) left = e == eidx[(b - 1) * ncomp + c];
-          if (top) top = e == eidx[(b - L.W) * ncomp + c];
+          const uint32_t e = eidx[(size_t)c * nblocks + b];
+          if (left) left = e == eidx[(size_t)c * nblocks + b - 1];
+          if (top) top = e == eidx[(size_t)c * nblocks + b - L.W];
         }
         ref[b] = left ? 1 : top ? 2 : 0;
       }
@@ -737,7 +774,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         const uint64_t end = lv[l].first + (uint64_t)lv[l].W * lv[l].H * faces;
         for (uint64_t b = lv[l].first; b < end; b++)
           for (int c = comp_lo[m]; c < comp_hi[m]; c++) {
-            const uint32_t e = rank[eidx[b * ncomp + c]];
+            const uint32_t e = rank[eidx[(size_t)c * nblocks + b]];
             if (!ref[b]) h[e >= prev[c] ? e - prev[c] : e + n - prev[c]]++;
             prev[c] = e;
           }
@@ -792,7 +829,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
           const uint64_t end = lv[l].first + (uint64_t)lv[l].W * lv[l].H * faces;
           for (uint64_t b = lv[l].first; b < end; b++)
             for (int c = comp_lo[m]; c < comp_hi[m]; c++) {
-              const uint32_t e = eidx[b * ncomp + c];
+              const uint32_t e = eidx[(size_t)c * nblocks + b];
               if (!ref[b] && e != prev[c]) {
                 pairs.push_back((e << 13) | prev[c]);
                 pairs.push_back((prev[c] << 13) | e);
@@ -835,7 +872,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         std::vector<std::thread> tw;
         // least distance between distinct endpoints: one 6-bit green step (4^2) or one alpha step
         tw.emplace_back([&] {
-          trial[0] = nearest_chain(u, comps_norm, comps_dist, m ? 1u : 16u);
+          trial[0] = nearest_chain_comps(u, m ? 1u : 16u);
           bits[0] = stream_bits(m, trial[0]);
         });
         for (int t = 0; t < 3; t++)
@@ -859,8 +896,8 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
     sel_pal[m]->values = permuted(sel_pal[m]->values, sel_rank[m]);
     for (uint64_t b = 0; b < nblocks; b++)
       for (int c = comp_lo[m]; c < comp_hi[m]; c++) {
-        eidx[b * ncomp + c] = ep_rank[m][eidx[b * ncomp + c]];
-        sidx[b * ncomp + c] = sel_rank[m][sidx[b * ncomp + c]];
+        eidx[(size_t)c * nblocks + b] = ep_rank[m][eidx[(size_t)c * nblocks + b]];
+        sidx[(size_t)c * nblocks + b] = sel_rank[m][sidx[(size_t)c * nblocks + b]];
       }
   }
   // block streams: one walk records every level's symbols (model << 16 | symbol) and counts them,
@@ -889,7 +926,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
           }
           for (int c = 0; c < ncomp; c++) {
             const int m = (colour && c == 0) ? 0 : 1;
-            const uint32_t e = eidx[b * ncomp + c];
+            const uint32_t e = eidx[(size_t)c * nblocks + b];
             if (ref[b] == 0) {
               const uint32_t d = e >= prev[c] ? e - prev[c] : e + pal_n[m] - prev[c];
               out.push_back(((uint32_t)(1 + 2 * m) << 16) | d);
@@ -899,7 +936,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
           }
           for (int c = 0; c < ncomp; c++) {
             const int m = (colour && c == 0) ? 0 : 1;
-            const uint32_t sel = sidx[b * ncomp + c];
+            const uint32_t sel = sidx[(size_t)c * nblocks + b];
             out.push_back(((uint32_t)(2 + 2 * m) << 16) | sel);
             hist[2 + 2 * m][sel]++;
           }
