@@ -28,7 +28,7 @@ from . import texgen  # noqa: F401  (seeded synthetic inputs)
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libcrngpu.so")
 
-OK, E_PARAM, E_CORRUPT, E_DEVICE, E_UNSUPPORTED = 0, -1, -2, -3, -4
+OK, E_PARAM, E_CORRUPT, E_DEVICE, E_UNSUPPORTED, E_NOMEM = 0, -1, -2, -3, -4, -5
 MEM_HOST, MEM_DEVICE = 0, 1
 FMT_DXT1, FMT_DXT5, FMT_DXN_XY, FMT_DXN_YX, FMT_DXT5A = 0, 2, 7, 8, 9
 FLAG_PERCEPTUAL, FLAG_USE_BOTH_BLOCK_TYPES = 1, 8

@@ -3,6 +3,7 @@
 
 #include <cstdlib>
 #include <mutex>
+#include <new>
 #include <string>
 
 #include "crngpu_internal.h"
@@ -21,6 +22,23 @@ std::mutex& device_setup_mutex() {
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 void clear_error() { g_last_error.clear(); }
+
+int exception_status() noexcept {
+  int rc = CRNGPU_E_DEVICE;
+  const char* msg = "internal error";
+  try {
+    throw;
+  } catch (const std::bad_alloc&) {
+    rc = CRNGPU_E_NOMEM;
+    msg = "out of host memory";
+  } catch (...) {
+  }
+  try {
+    g_last_error = msg;
+  } catch (...) {
+  }
+  return rc;
+}
 const char* last_error_cstr() { return g_last_error.c_str(); }
 
 int cuda_check(cudaError_t e, const char* what) {

@@ -652,7 +652,7 @@ std::vector<T> permuted(const std::vector<T>& v, const std::vector<uint32_t>& ra
 using namespace crngpu;
 
 extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32_t height, uint32_t levels,
-                                   uint32_t faces, uint32_t format, void* out, uint64_t out_capacity) {
+                                   uint32_t faces, uint32_t format, void* out, uint64_t out_capacity) try {
   clear_error();
   if (!blocks || !width || !height || width > 4096 || height > 4096 || !levels || levels > 16 ||
       (faces != 1 && faces != 6)) {
@@ -1012,4 +1012,6 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
   put_be(d, 4, crc16(d.data() + 6, header_size - 6), 2);
   if (out && out_capacity >= d.size()) std::memcpy(out, d.data(), d.size());
   return (int64_t)d.size();
+} catch (...) {
+  return crngpu::exception_status();
 }

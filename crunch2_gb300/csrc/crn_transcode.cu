@@ -1985,7 +1985,7 @@ struct UnpackBatch : HostObject {
 
 using namespace crngpu;
 
-extern "C" crngpu_unpack_context crngpu_unpack_begin(const void* data, uint32_t data_size) {
+extern "C" crngpu_unpack_context crngpu_unpack_begin(const void* data, uint32_t data_size) try {
   clear_error();
   if (!data) { set_error("NULL data"); return nullptr; }
   std::unique_ptr<UnpackContext> c(new UnpackContext());
@@ -1995,10 +1995,13 @@ extern "C" crngpu_unpack_context crngpu_unpack_begin(const void* data, uint32_t 
   }
   if (upload_context(c.get(), static_cast<const uint8_t*>(data), data_size) != CRNGPU_OK) return nullptr;
   return reinterpret_cast<crngpu_unpack_context>(c.release());
+} catch (...) {
+  crngpu::exception_status();
+  return nullptr;
 }
 
 extern "C" int crngpu_get_info(crngpu_unpack_context ctx, uint32_t* width, uint32_t* height, uint32_t* levels,
-                               uint32_t* faces, uint32_t* format, uint32_t* bytes_per_block) {
+                               uint32_t* faces, uint32_t* format, uint32_t* bytes_per_block) try {
   UnpackContext* c = reinterpret_cast<UnpackContext*>(ctx);
   if (!valid_ctx(c)) return CRNGPU_E_PARAM;
   if (width) *width = c->file.width;
@@ -2008,29 +2011,35 @@ extern "C" int crngpu_get_info(crngpu_unpack_context ctx, uint32_t* width, uint3
   if (format) *format = c->file.format;
   if (bytes_per_block) *bytes_per_block = c->file.bytes_per_block;
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int crngpu_unpack_level(crngpu_unpack_context ctx, void** dst_faces, uint32_t dst_size_in_bytes,
-                                   uint32_t row_pitch_in_bytes, uint32_t level_index, int mem, void* stream) {
+                                   uint32_t row_pitch_in_bytes, uint32_t level_index, int mem, void* stream) try {
   clear_error();
   return unpack_one(reinterpret_cast<UnpackContext*>(ctx), nullptr, nullptr, 0, dst_faces, dst_size_in_bytes,
                     row_pitch_in_bytes, level_index, mem, stream);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int crngpu_unpack_level_segmented(crngpu_unpack_context ctx, const void* src, uint32_t src_size_in_bytes,
                                              void** dst_faces, uint32_t dst_size_in_bytes,
                                              uint32_t row_pitch_in_bytes, uint32_t level_index, int mem,
-                                             void* stream) {
+                                             void* stream) try {
   clear_error();
   if (!src || !src_size_in_bytes) { set_error("NULL segment"); return CRNGPU_E_PARAM; }
   const uint8_t* s = static_cast<const uint8_t*>(src);
   return unpack_one(reinterpret_cast<UnpackContext*>(ctx), mem == CRNGPU_MEM_DEVICE ? nullptr : s,
                     mem == CRNGPU_MEM_DEVICE ? s : nullptr, src_size_in_bytes, dst_faces, dst_size_in_bytes,
                     row_pitch_in_bytes, level_index, mem, stream);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t first_level, uint32_t level_count,
-                                        void* dst, uint64_t dst_size, int mem, void* stream) {
+                                        void* dst, uint64_t dst_size, int mem, void* stream) try {
   clear_error();
   UnpackContext* c = reinterpret_cast<UnpackContext*>(ctx);
   if (!valid_ctx(c) || !dst || !level_count || first_level + level_count > c->file.levels || c->file.segmented) {
@@ -2058,9 +2067,11 @@ extern "C" int64_t crngpu_unpack_levels(crngpu_unpack_context ctx, uint32_t firs
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   }
   return (int64_t)total;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_batch_item* items, uint32_t n) {
+extern "C" crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_batch_item* items, uint32_t n) try {
   clear_error();
   if (!items || !n) { set_error("empty batch"); return nullptr; }
   std::unique_ptr<UnpackBatch> b(new UnpackBatch());
@@ -2107,9 +2118,12 @@ extern "C" crngpu_unpack_batch crngpu_unpack_batch_create(const crngpu_unpack_ba
   size_t smem = 0;
   if (decode_grid(b->plan, &grid, &smem) != CRNGPU_OK) return nullptr;
   return reinterpret_cast<crngpu_unpack_batch>(b.release());
+} catch (...) {
+  crngpu::exception_status();
+  return nullptr;
 }
 
-extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t flags, void* stream) {
+extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t flags, void* stream) try {
   clear_error();
   UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
   if (!b || b->magic != 0x42415443u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
@@ -2177,9 +2191,11 @@ extern "C" int crngpu_unpack_batch_launch(crngpu_unpack_batch batch, uint32_t fl
   }
   if ((e = cudaGraphLaunch(b->graph, s)) != cudaSuccess) return cuda_check(e, "graph launch");
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int crngpu_unpack_batch_set_variant(crngpu_unpack_batch batch, int32_t variant) {
+extern "C" int crngpu_unpack_batch_set_variant(crngpu_unpack_batch batch, int32_t variant) try {
   clear_error();
   UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
   if (!b || b->magic != 0x42415443u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
@@ -2190,9 +2206,11 @@ extern "C" int crngpu_unpack_batch_set_variant(crngpu_unpack_batch batch, int32_
     b->graph = nullptr;
   }
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int crngpu_unpack_batch_status(crngpu_unpack_batch batch, void* stream) {
+extern "C" int crngpu_unpack_batch_status(crngpu_unpack_batch batch, void* stream) try {
   clear_error();
   UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
   if (!b || b->magic != 0x42415443u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
@@ -2201,46 +2219,58 @@ extern "C" int crngpu_unpack_batch_status(crngpu_unpack_batch batch, void* strea
   if (e != cudaSuccess) return cuda_check(e, "read status");
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   return status_to_rc(b->words_host[1]);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int crngpu_unpack_batch_tuning(crngpu_unpack_batch batch, int32_t* variant, float* ms, uint32_t n) {
+extern "C" int crngpu_unpack_batch_tuning(crngpu_unpack_batch batch, int32_t* variant, float* ms, uint32_t n) try {
   UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
   if (!b || b->magic != 0x42415443u) return CRNGPU_E_PARAM;
   if (variant) *variant = b->variant;
   for (uint32_t i = 0; ms && i < n && i < (uint32_t)kExpandVariants; i++) ms[i] = b->variant_ms[i];
   return kExpandVariants;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch) {
+extern "C" int64_t crngpu_unpack_batch_bytes(crngpu_unpack_batch batch) try {
   UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
   if (!b || b->magic != 0x42415443u) return CRNGPU_E_PARAM;
   return (int64_t)b->out_bytes;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int crngpu_set_decode_split(uint32_t min_blocks) {
+extern "C" int crngpu_set_decode_split(uint32_t min_blocks) try {
   clear_error();
   g_wide_min_blocks.store(min_blocks, std::memory_order_relaxed);
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int crngpu_unpack_batch_destroy(crngpu_unpack_batch batch) {
+extern "C" int crngpu_unpack_batch_destroy(crngpu_unpack_batch batch) try {
   UnpackBatch* b = reinterpret_cast<UnpackBatch*>(batch);
   if (!b || b->magic != 0x42415443u) return CRNGPU_E_PARAM;
   b->magic = 0;
   delete b;
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int crngpu_unpack_end(crngpu_unpack_context ctx) {
+extern "C" int crngpu_unpack_end(crngpu_unpack_context ctx) try {
   UnpackContext* c = reinterpret_cast<UnpackContext*>(ctx);
   if (!valid_ctx(c)) return CRNGPU_E_PARAM;
   c->magic = 0;
   delete c;
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" void crngpu_crn_decompress(void* src, unsigned int src_size, void* dst, unsigned int dst_size,
-                                      unsigned int firstLevel, unsigned int levelCount) {
+                                      unsigned int firstLevel, unsigned int levelCount) try {
   (void)dst_size;  // the reference wrapper does not bound-check dst either; each level is checked below
   crngpu_unpack_context ctx = crngpu_unpack_begin(src, src_size);
   if (!ctx) return;
@@ -2259,6 +2289,8 @@ extern "C" void crngpu_crn_decompress(void* src, unsigned int src_size, void* ds
     height >>= 1;
   }
   crngpu_unpack_end(ctx);
+} catch (...) {
+  crngpu::exception_status();
 }
 
 // ------------------------------------------------------------------------------------------
@@ -2310,7 +2342,7 @@ int noalloc_scratch_ptr(unsigned char** out) {
 
 extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_size, void** dst_faces,
                                            uint32_t dst_size_in_bytes, uint32_t row_pitch_in_bytes,
-                                           uint32_t level_index, void* stream) {
+                                           uint32_t level_index, void* stream) try {
   using namespace crngpu;
   clear_error();
   if (!crn_data || !dst_faces || dst_size_in_bytes < 8) { set_error("bad arguments"); return CRNGPU_E_PARAM; }
@@ -2389,4 +2421,6 @@ extern "C" int crngpu_unpack_level_noalloc(const void* crn_data, uint32_t crn_si
   if ((e = cudaMemcpyAsync(st, words, 8, cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_check(e, "read status");
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   return status_to_rc(st[1]);
+} catch (...) {
+  return crngpu::exception_status();
 }

@@ -47,6 +47,10 @@ inline bool format_is_non_srgb(uint32_t format) {
 // Thread-local last-error text behind crngpu_last_error().
 void set_error(const std::string& msg);
 void clear_error();
+// The status of the exception being handled, for the C-ABI entry points, which let none escape:
+// CRNGPU_E_NOMEM for std::bad_alloc (host memory exhausted, or an allocation the installed memory
+// hooks refused), CRNGPU_E_DEVICE for anything else; the last-error text says which.
+int exception_status() noexcept;
 const char* last_error_cstr();
 
 // Guards every lazily filled per-device cache of the library (function attributes, symbol

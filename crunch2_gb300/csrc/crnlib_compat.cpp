@@ -433,21 +433,51 @@ void crn_set_memory_callbacks(crn_realloc_func pRealloc, crn_msize_func pMSize, 
 
 void crn_free_block(void* pBlock) { block_free(pBlock); }
 
+// No exception leaves these (the reference reports failure as NULL with a zero size): an
+// allocation that fails, or that installed memory hooks refuse, ends the call that way.
 void* crn_compress(const crn_comp_params& comp_params, crn_uint32& compressed_size, crn_uint32* pActual_quality_level,
-                   float* pActual_bitrate) {
+                   float* pActual_bitrate) try {
   return compress(comp_params, compressed_size, pActual_quality_level, pActual_bitrate);
+} catch (...) {
+  crngpu::exception_status();
+  compressed_size = 0;
+  return nullptr;
 }
 
 void* crn_compress(const crn_comp_params& comp_params, const crn_mipmap_params& mip_params, crn_uint32& compressed_size,
-                   crn_uint32* pActual_quality_level, float* pActual_bitrate) {
+                   crn_uint32* pActual_quality_level, float* pActual_bitrate) try {
   return compress_with_mips(comp_params, mip_params, compressed_size, pActual_quality_level, pActual_bitrate);
+} catch (...) {
+  crngpu::exception_status();
+  compressed_size = 0;
+  return nullptr;
 }
+
+namespace {
+void* dds_of_context(crngpu_unpack_context ctx, crn_uint32& file_size);
+}  // namespace
 
 void* crn_decompress_crn_to_dds(const void* pCRN_file_data, crn_uint32& file_size) {
   const uint32_t crn_size = file_size;
   file_size = 0;
   crngpu_unpack_context ctx = crngpu_unpack_begin(pCRN_file_data, crn_size);
   if (!ctx) return nullptr;
+  struct End {
+    crngpu_unpack_context c;
+    ~End() { crngpu_unpack_end(c); }
+  } end{ctx};
+  try {
+    return dds_of_context(ctx, file_size);
+  } catch (...) {
+    crngpu::exception_status();
+    file_size = 0;
+    return nullptr;
+  }
+}
+
+namespace {
+// the DDS file of every level of an unpack context
+void* dds_of_context(crngpu_unpack_context ctx, crn_uint32& file_size) {
   uint32_t w = 0, h = 0, levels = 0, faces = 0, fmt = 0, bpb = 0;
   crngpu_get_info(ctx, &w, &h, &levels, &faces, &fmt, &bpb);
   uint64_t data = 0;
@@ -458,7 +488,6 @@ void* crn_decompress_crn_to_dds(const void* pCRN_file_data, crn_uint32& file_siz
   // out face-major as DDS stores it
   std::vector<uint8_t> lv((size_t)data);
   const int64_t n = crngpu_unpack_levels(ctx, 0, levels, lv.data(), data, CRNGPU_MEM_HOST, nullptr);
-  crngpu_unpack_end(ctx);
   if (n < 0) return nullptr;
   uint8_t* o = out.data() + 128;
   for (uint32_t f = 0; f < faces; f++) {
@@ -473,6 +502,7 @@ void* crn_decompress_crn_to_dds(const void* pCRN_file_data, crn_uint32& file_siz
   dds_header(out.data(), w, h, levels, faces, static_cast<crn_format>(fmt));
   return to_block(out, file_size);
 }
+}  // namespace
 
 crn_uint32 crn_get_format_fourcc(crn_format fmt) { return format_fourcc(fmt); }
 crn_uint32 crn_get_format_bits_per_texel(crn_format fmt) { return format_bits_per_texel(fmt); }

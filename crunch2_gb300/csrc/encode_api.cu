@@ -217,7 +217,7 @@ int64_t dds_plain_chain(const uint8_t* rgba_levels, uint32_t width, uint32_t hei
 using namespace crngpu;
 
 extern "C" int crngpu_dxt1_optimize_batch(const uint8_t* rgba_blocks, uint32_t n, const crngpu_dxt1_params* params,
-                                          uint8_t* out_blocks, uint64_t* out_error, int mem, void* stream) {
+                                          uint8_t* out_blocks, uint64_t* out_error, int mem, void* stream) try {
   clear_error();
   const bool legacy = params && params->struct_size == 16;  // the four-field layout: Uber, no extras
   if (!params || (!legacy && params->struct_size != sizeof(crngpu_dxt1_params)) ||
@@ -247,10 +247,12 @@ extern "C" int crngpu_dxt1_optimize_batch(const uint8_t* rgba_blocks, uint32_t n
                         if (rc == CRNGPU_OK && black) rc = launch_dxt1_black_trial(in, n, opts, out, 8, e, s);
                         return rc;
                       });
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int crngpu_dxt5a_optimize_batch(const uint8_t* rgba_blocks, uint32_t n, uint32_t comp_index,
-                                           int32_t use_both_block_types, uint8_t* out_blocks, int mem, void* stream) {
+                                           int32_t use_both_block_types, uint8_t* out_blocks, int mem, void* stream) try {
   clear_error();
   if (comp_index > 3 || (n && (!rgba_blocks || !out_blocks))) { set_error("bad arguments"); return CRNGPU_E_PARAM; }
   if (!n) return CRNGPU_OK;
@@ -260,16 +262,20 @@ extern "C" int crngpu_dxt5a_optimize_batch(const uint8_t* rgba_blocks, uint32_t 
                         return launch_dxt5a(in, n, (int)comp_index, use_both_block_types != 0, kDxtQualityUber, out, 8,
                                            s);
                       });
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int crngpu_compress_blocks(const uint8_t* rgba_blocks, uint32_t n, uint32_t format, uint32_t flags,
-                                      uint8_t* out_blocks, int mem, void* stream) {
+                                      uint8_t* out_blocks, int mem, void* stream) try {
   return crngpu_compress_blocks_ex(rgba_blocks, n, format, flags, nullptr, out_blocks, mem, stream);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int crngpu_compress_blocks_ex(const uint8_t* rgba_blocks, uint32_t n, uint32_t format, uint32_t flags,
                                          const crngpu_block_options* options, uint8_t* out_blocks, int mem,
-                                         void* stream) {
+                                         void* stream) try {
   clear_error();
   uint32_t quality, threshold;
   if (!read_options(options, &quality, &threshold)) return CRNGPU_E_PARAM;
@@ -283,19 +289,23 @@ extern "C" int crngpu_compress_blocks_ex(const uint8_t* rgba_blocks, uint32_t n,
                                 return encode_device(in, n, format, flags, quality, threshold, out, nullptr, s);
                               });
   return rc == CRNGPU_OK ? bpb : rc;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int64_t crngpu_compress_image(const uint8_t* rgba, uint32_t width, uint32_t height, uint32_t pitch_bytes,
                                          uint32_t format, uint32_t flags, uint8_t* out, uint64_t out_size, int mem,
-                                         void* stream) {
+                                         void* stream) try {
   return crngpu_compress_image_ex(rgba, width, height, pitch_bytes, format, flags, nullptr, out, out_size, mem,
                                   stream);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int64_t crngpu_compress_image_ex(const uint8_t* rgba, uint32_t width, uint32_t height,
                                             uint32_t pitch_bytes, uint32_t format, uint32_t flags,
                                             const crngpu_block_options* options, uint8_t* out, uint64_t out_size,
-                                            int mem, void* stream) {
+                                            int mem, void* stream) try {
   clear_error();
   uint32_t quality, threshold;
   if (!read_options(options, &quality, &threshold)) return CRNGPU_E_PARAM;
@@ -344,4 +354,6 @@ extern "C" int64_t crngpu_compress_image_ex(const uint8_t* rgba, uint32_t width,
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   }
   return (int64_t)need;
+} catch (...) {
+  return crngpu::exception_status();
 }

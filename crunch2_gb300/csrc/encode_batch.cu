@@ -155,7 +155,7 @@ void destroy(EncodeBatch* b) {
 
 using namespace crngpu;
 
-extern "C" crngpu_encode_batch crngpu_encode_batch_create(const crngpu_encode_item* items, uint32_t n, uint32_t flags) {
+extern "C" crngpu_encode_batch crngpu_encode_batch_create(const crngpu_encode_item* items, uint32_t n, uint32_t flags) try {
   clear_error();
   if (!items || !n) { set_error("crngpu_encode_batch_create: no items"); return nullptr; }
   const bool perceptual = (flags & CRNGPU_FLAG_PERCEPTUAL) != 0;
@@ -257,9 +257,12 @@ extern "C" crngpu_encode_batch crngpu_encode_batch_create(const crngpu_encode_it
     rc = cuda_check(e, "events");
   if (rc != CRNGPU_OK) { destroy(b); return nullptr; }
   return reinterpret_cast<crngpu_encode_batch>(b);
+} catch (...) {
+  crngpu::exception_status();
+  return nullptr;
 }
 
-extern "C" int crngpu_encode_batch_launch(crngpu_encode_batch batch, uint32_t flags, void* stream) {
+extern "C" int crngpu_encode_batch_launch(crngpu_encode_batch batch, uint32_t flags, void* stream) try {
   clear_error();
   EncodeBatch* b = reinterpret_cast<EncodeBatch*>(batch);
   if (!b || b->magic != 0x454E4342u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
@@ -288,9 +291,11 @@ extern "C" int crngpu_encode_batch_launch(crngpu_encode_batch batch, uint32_t fl
   }
   if ((e = cudaGraphLaunch(b->graph, s)) != cudaSuccess) return cuda_check(e, "graph launch");
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int crngpu_encode_batch_tuning(crngpu_encode_batch batch, int32_t* grids, float* ms, uint32_t n) {
+extern "C" int crngpu_encode_batch_tuning(crngpu_encode_batch batch, int32_t* grids, float* ms, uint32_t n) try {
   clear_error();
   EncodeBatch* b = reinterpret_cast<EncodeBatch*>(batch);
   if (!b || b->magic != 0x454E4342u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
@@ -298,20 +303,26 @@ extern "C" int crngpu_encode_batch_tuning(crngpu_encode_batch batch, int32_t* gr
   for (uint32_t i = 0; ms && i < n && i < (uint32_t)(kColourVariants + kAlphaVariants); i++)
     ms[i] = i < (uint32_t)kColourVariants ? b->colour_ms[i] : b->alpha_ms[i - kColourVariants];
   return kColourVariants + kAlphaVariants;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int64_t crngpu_encode_batch_size(crngpu_encode_batch batch, uint64_t* texels) {
+extern "C" int64_t crngpu_encode_batch_size(crngpu_encode_batch batch, uint64_t* texels) try {
   clear_error();
   EncodeBatch* b = reinterpret_cast<EncodeBatch*>(batch);
   if (!b || b->magic != 0x454E4342u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
   if (texels) *texels = b->texels;
   return (int64_t)b->nblocks;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int crngpu_encode_batch_destroy(crngpu_encode_batch batch) {
+extern "C" int crngpu_encode_batch_destroy(crngpu_encode_batch batch) try {
   clear_error();
   EncodeBatch* b = reinterpret_cast<EncodeBatch*>(batch);
   if (!b || b->magic != 0x454E4342u) { set_error("bad batch"); return CRNGPU_E_PARAM; }
   destroy(b);
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }

@@ -3148,7 +3148,7 @@ bool hc_params_ok(const crngpu_hc_params* params) {
 // Clustered DXT1 encode with the colour codebooks and indices (dxt_hc::compress for cDXT1).
 extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_params* params, uint8_t* d_out,
                                        uint16_t* d_endpoint_idx, uint16_t* d_selector_idx, uint32_t* d_endpoints,
-                                       uint32_t* d_selectors, crngpu_hc_stats* stats, void* stream) {
+                                       uint32_t* d_selectors, crngpu_hc_stats* stats, void* stream) try {
   clear_error();
   if (!d_blocks || !d_out || !hc_params_ok(params)) {
     set_error("crngpu_hc_compress_dxt1: bad arguments");
@@ -3156,22 +3156,26 @@ extern "C" int crngpu_hc_compress_dxt1(const uint8_t* d_blocks, const crngpu_hc_
   }
   return hc_compress_impl(d_blocks, *params, CRNGPU_FMT_DXT1, d_out, d_endpoint_idx, d_selector_idx, d_endpoints,
                           d_selectors, stats, as_stream(stream));
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // Clustered encode of any supported format (dxt_hc::compress). See include/crngpu.h.
 extern "C" int crngpu_hc_compress(const uint8_t* d_blocks, const crngpu_hc_params* params, uint32_t format,
-                                  uint8_t* d_out, crngpu_hc_stats* stats, void* stream) {
+                                  uint8_t* d_out, crngpu_hc_stats* stats, void* stream) try {
   clear_error();
   if (!d_blocks || !d_out || !hc_params_ok(params)) {
     set_error("crngpu_hc_compress: bad arguments");
     return CRNGPU_E_PARAM;
   }
   return hc_compress_impl(d_blocks, *params, format, d_out, nullptr, nullptr, nullptr, nullptr, stats, as_stream(stream));
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // Codebook sizes of crn_comp::quantize_images (crnlib/crn_comp.cpp:541-577) for a quality level.
 extern "C" int crngpu_hc_codebook_sizes(uint32_t width, uint32_t height, uint32_t quality_level, uint32_t format,
-                                        uint32_t* sizes4) {
+                                        uint32_t* sizes4) try {
   if (!sizes4 || !width || !height) return CRNGPU_E_PARAM;
   const uint32_t kMin = 8, kMax = 8192;  // cCRNMinPaletteSize, cCRNMaxPaletteSize (inc/crnlib.h:118-119)
   uint32_t max_entries = ((width + 3) / 4) * ((height + 3) / 4);
@@ -3191,6 +3195,8 @@ extern "C" int crngpu_hc_codebook_sizes(uint32_t width, uint32_t height, uint32_
   sizes4[2] = size(24, powf(quality, 2.1f * amul));   // alpha endpoints
   sizes4[3] = size(48, powf(quality, 1.65f * amul));  // alpha selectors
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // crn_compress with m_file_type = cCRNFileTypeCRN and source mips (inc/crnlib.h:614,
@@ -3337,7 +3343,7 @@ int64_t deliver(const std::vector<uint8_t>& file, void* out, uint64_t out_capaci
 
 extern "C" int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t width, uint32_t height, uint32_t levels,
                                        uint32_t faces, uint32_t format, uint32_t quality_level, uint32_t flags,
-                                       void* out, uint64_t out_capacity) {
+                                       void* out, uint64_t out_capacity) try {
   using namespace crngpu;
   clear_error();
   if (quality_level > 255) { set_error("crngpu_compress_crn: quality above 255"); return CRNGPU_E_PARAM; }
@@ -3347,21 +3353,25 @@ extern "C" int64_t crngpu_compress_crn(const uint8_t* rgba_levels, uint32_t widt
   std::vector<uint8_t> file;
   if ((rc = src.pass(quality_level, file)) != CRNGPU_OK) return rc;
   return deliver(file, out, out_capacity);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int64_t crngpu_compress_dds_clustered(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
                                                  uint32_t levels, uint32_t faces, uint32_t format,
                                                  uint32_t quality_level, uint32_t flags, void* out,
-                                                 uint64_t out_capacity) {
+                                                 uint64_t out_capacity) try {
   return crngpu_compress_dds_clustered_ex(rgba_levels, width, height, levels, faces, format, quality_level, flags,
                                           nullptr, out, out_capacity);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int64_t crngpu_compress_dds_clustered_ex(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
                                                     uint32_t levels, uint32_t faces, uint32_t format,
                                                     uint32_t quality_level, uint32_t flags,
                                                     const crngpu_block_options* options, void* out,
-                                                    uint64_t out_capacity) {
+                                                    uint64_t out_capacity) try {
   using namespace crngpu;
   using namespace crngpu::hc;
   clear_error();
@@ -3498,9 +3508,11 @@ extern "C" int64_t crngpu_compress_dds_clustered_ex(const uint8_t* rgba_levels, 
       }
     }
   return (int64_t)need;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
-extern "C" int crngpu_compress_crn_batch(crngpu_crn_batch_item* items, uint32_t n, uint32_t threads) {
+extern "C" int crngpu_compress_crn_batch(crngpu_crn_batch_item* items, uint32_t n, uint32_t threads) try {
   using namespace crngpu;
   clear_error();
   if (!items && n) { set_error("crngpu_compress_crn_batch: no items"); return CRNGPU_E_PARAM; }
@@ -3535,6 +3547,8 @@ extern "C" int crngpu_compress_crn_batch(crngpu_crn_batch_item* items, uint32_t 
   for (auto& t : pool) t.join();
   if (failed) set_error("crngpu_compress_crn_batch: some items failed (see their result)");
   return failed ? CRNGPU_E_PARAM : CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 namespace crngpu {
@@ -3602,20 +3616,22 @@ int bitrate_search(CrnSource& src, float target_bitrate, std::vector<uint8_t>& b
 extern "C" int64_t crngpu_compress_crn_bitrate(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
                                                uint32_t levels, uint32_t faces, uint32_t format, float target_bitrate,
                                                uint32_t flags, void* out, uint64_t out_capacity,
-                                               uint32_t* quality_out, float* bitrate_out) {
+                                               uint32_t* quality_out, float* bitrate_out) try {
   if (!(target_bitrate > 0.0f)) {
     crngpu::set_error("crngpu_compress_crn_bitrate: target bitrate must be positive");
     return CRNGPU_E_PARAM;
   }
   return crngpu_compress_crn_ex(rgba_levels, width, height, levels, faces, format, 0, target_bitrate, flags, nullptr,
                                 out, out_capacity, quality_out, bitrate_out);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int64_t crngpu_compress_crn_ex(const uint8_t* rgba_levels, uint32_t width, uint32_t height,
                                           uint32_t levels, uint32_t faces, uint32_t format, uint32_t quality_level,
                                           float target_bitrate, uint32_t flags, const crngpu_crn_options* options,
                                           void* out, uint64_t out_capacity, uint32_t* quality_out,
-                                          float* bitrate_out) {
+                                          float* bitrate_out) try {
   using namespace crngpu;
   clear_error();
   if (quality_out) *quality_out = 0;
@@ -3646,4 +3662,6 @@ extern "C" int64_t crngpu_compress_crn_ex(const uint8_t* rgba_levels, uint32_t w
     if (bitrate_out) *bitrate_out = (float)file.size() * 8.0f / (float)src.texels;
   }
   return deliver(file, out, out_capacity);
+} catch (...) {
+  return crngpu::exception_status();
 }

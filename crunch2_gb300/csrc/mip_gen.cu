@@ -298,7 +298,7 @@ using namespace crngpu::mip;
 
 extern "C" int64_t crngpu_generate_mipmaps(const uint8_t* rgba, uint32_t width, uint32_t height, uint32_t levels,
                                            uint32_t filter, float filter_scale, uint32_t flags, uint8_t* out,
-                                           uint64_t out_size, int mem, void* stream) {
+                                           uint64_t out_size, int mem, void* stream) try {
   clear_error();
   if (!rgba || !out || !width || !height || width > 16384 || height > 16384 || filter > 4 || !(filter_scale > 0.0f)) {
     set_error("crngpu_generate_mipmaps: bad arguments");
@@ -410,4 +410,6 @@ extern "C" int64_t crngpu_generate_mipmaps(const uint8_t* rgba, uint32_t width, 
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_check(e, "sync");
   }
   return (int64_t)need;
+} catch (...) {
+  return crngpu::exception_status();
 }

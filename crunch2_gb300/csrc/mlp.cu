@@ -970,7 +970,7 @@ int mma_wait_counter(uint32_t* out, bool reset) {
 using namespace crngpu;
 using namespace crngpu::mlp;
 
-extern "C" void* crngpu_mlp_create(uint64_t seed) {
+extern "C" void* crngpu_mlp_create(uint64_t seed) try {
   clear_error();
   Net* net = new Net();
   cudaGetDevice(&net->device);
@@ -994,19 +994,24 @@ extern "C" void* crngpu_mlp_create(uint64_t seed) {
   }
   cudaDeviceSynchronize();
   return net;
+} catch (...) {
+  crngpu::exception_status();
+  return nullptr;
 }
 
-extern "C" int crngpu_mlp_destroy(void* h) {
+extern "C" int crngpu_mlp_destroy(void* h) try {
   Net* net = static_cast<Net*>(h);
   if (!net || net->magic != 0x4D4C5030u) return CRNGPU_E_PARAM;
   net->magic = 0;
   delete net;
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // Parameter access for checkpoints and gradient checks. which: 0 W1, 1 b1, 2 W2, 3 b2, 4 W3, 5 b3;
 // what: 0 weights, 1 gradients. count = number of floats in the buffer.
-extern "C" int crngpu_mlp_param(void* h, int which, int what, float* host, uint32_t count, int write) {
+extern "C" int crngpu_mlp_param(void* h, int which, int what, float* host, uint32_t count, int write) try {
   Net* net = static_cast<Net*>(h);
   if (!net || net->magic != 0x4D4C5030u || which < 0 || which > 5 || !host) return CRNGPU_E_PARAM;
   Param* p = net->params()[which];
@@ -1018,20 +1023,24 @@ extern "C" int crngpu_mlp_param(void* h, int which, int what, float* host, uint3
     return cuda_check(cudaMemcpy(dev, host, count * 4, cudaMemcpyHostToDevice), "write param");
   }
   return cuda_check(cudaMemcpy(host, dev, count * 4, cudaMemcpyDeviceToHost), "read param");
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // Loss of the error-bound output: tau <= 0 squared error (weight ignored); 0 < tau < 1 the
 // tau-quantile (pinball) loss scaled by `weight`.
-extern "C" int crngpu_mlp_set_bound_loss(void* h, float tau, float weight) {
+extern "C" int crngpu_mlp_set_bound_loss(void* h, float tau, float weight) try {
   Net* net = static_cast<Net*>(h);
   if (!net || net->magic != 0x4D4C5030u || !(tau < 1.f) || !(weight > 0.f)) return CRNGPU_E_PARAM;
   net->bound_tau = tau > 0.f ? tau : 0.f;
   net->bound_weight = weight;
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // Forward pass over n blocks (device RGBA8, n x 64) -> y (device, n x 16 fp32).
-extern "C" int crngpu_mlp_forward(void* h, const uint8_t* d_blocks, uint32_t n, float* d_y, void* stream) {
+extern "C" int crngpu_mlp_forward(void* h, const uint8_t* d_blocks, uint32_t n, float* d_y, void* stream) try {
   clear_error();
   Net* net = static_cast<Net*>(h);
   if (!net || net->magic != 0x4D4C5030u || !d_blocks || !d_y) return CRNGPU_E_PARAM;
@@ -1043,12 +1052,14 @@ extern "C" int crngpu_mlp_forward(void* h, const uint8_t* d_blocks, uint32_t n, 
   int rc = infer(*net, d_blocks, n, d_y, s);
   if (rc != CRNGPU_OK) return rc;
   return check_flag(*net, s);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // Gradients of the loss for n blocks and targets (device, n x 8 fp32) into the gradient buffers;
 // *loss (host) receives the loss. Does not update the weights.
 extern "C" int crngpu_mlp_gradients(void* h, const uint8_t* d_blocks, const float* d_targets, uint32_t n, float* loss,
-                                    void* stream) {
+                                    void* stream) try {
   clear_error();
   Net* net = static_cast<Net*>(h);
   if (!net || net->magic != 0x4D4C5030u || !d_blocks || !d_targets || !n) return CRNGPU_E_PARAM;
@@ -1061,11 +1072,13 @@ extern "C" int crngpu_mlp_gradients(void* h, const uint8_t* d_blocks, const floa
   if ((rc = backward(*net, d_blocks, (int)n, s)) != CRNGPU_OK) return rc;
   if (loss) cudaMemcpyAsync(loss, net->loss.ptr, 4, cudaMemcpyDeviceToHost, s);
   return check_flag(*net, s);
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // One AdamW step (betas 0.9/0.999, eps 1e-8) on a batch: forward, backward, update.
 extern "C" int crngpu_mlp_train_step(void* h, const uint8_t* d_blocks, const float* d_targets, uint32_t n, float lr,
-                                     float weight_decay, float* loss, void* stream) {
+                                     float weight_decay, float* loss, void* stream) try {
   int rc = crngpu_mlp_gradients(h, d_blocks, d_targets, n, loss, stream);
   if (rc != CRNGPU_OK) return rc;
   Net* net = static_cast<Net*>(h);
@@ -1081,22 +1094,26 @@ extern "C" int crngpu_mlp_train_step(void* h, const uint8_t* d_blocks, const flo
                                is_bias ? 0.f : weight_decay, bc1, bc2, is_bias ? 1 : p->rows_live, p->cols);
   }
   return cuda_check(cudaGetLastError(), "launch k_adamw");
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // Training targets from plain-optimizer output (device): blocks8 (n x 8) + errors (n) -> n x 8.
 extern "C" int crngpu_mlp_make_targets(const uint8_t* d_blocks8, const uint64_t* d_err, uint32_t n, float* d_targets,
-                                       void* stream) {
+                                       void* stream) try {
   if (!d_blocks8 || !d_err || !d_targets) return CRNGPU_E_PARAM;
   k_make_targets<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, as_stream(stream)>>>(d_blocks8, d_err,
                                                                                                   (int)n, d_targets);
   return cuda_check(cudaGetLastError(), "launch k_make_targets");
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 // Learned DXT1 encode of n blocks (device RGBA8 in, device dxt1 out): MLP proposal, one
 // selector refit, and the exact optimizer for blocks whose error exceeds threshold x the
 // predicted bound. *fallbacks (host, optional) receives how many blocks fell back.
 extern "C" int crngpu_dxt1_learned_ex(void* h, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
-                                      uint32_t fallback_quality, uint8_t* d_out, uint32_t* fallbacks, void* stream) {
+                                      uint32_t fallback_quality, uint8_t* d_out, uint32_t* fallbacks, void* stream) try {
   clear_error();
   Net* net = static_cast<Net*>(h);
   if (!net || net->magic != 0x4D4C5030u || !d_blocks || !d_out) return CRNGPU_E_PARAM;
@@ -1150,9 +1167,13 @@ extern "C" int crngpu_dxt1_learned_ex(void* h, const uint8_t* d_blocks, uint32_t
     *fallbacks = cnt;
   }
   return CRNGPU_OK;
+} catch (...) {
+  return crngpu::exception_status();
 }
 
 extern "C" int crngpu_dxt1_learned(void* h, const uint8_t* d_blocks, uint32_t n, int perceptual, float threshold,
-                                   uint8_t* d_out, uint32_t* fallbacks, void* stream) {
+                                   uint8_t* d_out, uint32_t* fallbacks, void* stream) try {
   return crngpu_dxt1_learned_ex(h, d_blocks, n, perceptual, threshold, kDxtQualityUber, d_out, fallbacks, stream);
+} catch (...) {
+  return crngpu::exception_status();
 }

@@ -29,6 +29,7 @@ extern "C" {
 #define CRNGPU_E_CORRUPT (-2)      /* malformed .crn data (header, tables or block stream) */
 #define CRNGPU_E_DEVICE (-3)       /* CUDA error (allocation, launch, copy) */
 #define CRNGPU_E_UNSUPPORTED (-4)  /* valid request outside this library's scope */
+#define CRNGPU_E_NOMEM (-5)        /* host memory exhausted (or refused by the installed memory hooks) */
 
 /* Memory kinds for the `mem` arguments. */
 #define CRNGPU_MEM_HOST 0

@@ -206,3 +206,52 @@ def test_emscripten_wrapper_geometry(api, name):
         w, h = m["width"] >> l, m["height"] >> l
         assert api.crn_get_uncompressed_size(crn, len(crn), l) == ((w + 3) // 4) * ((h + 3) // 4) * bpb
     assert api.crn_get_width(b"not a crn file at all, just bytes" * 4, 136) == 0
+
+
+def test_refused_allocations_end_the_call_without_leaks(api):
+    """crnd_set_memory_callbacks hooks that refuse an allocation (after 0, 1, 2, ... granted ones):
+    crnd_unpack_begin returns NULL as crnd does -- no exception crosses the C++ and C interfaces --
+    the last error names the refusal, and everything granted before it is given back. Only host
+    parsing runs before the first refusal, so no GPU work is involved."""
+    import crunch2_gb300 as cg
+    crn = G.crn_bytes("dxt5_256")
+    buf = ctypes.create_string_buffer(crn, len(crn))
+    seen_limits = 0
+    for limit in range(0, 64):
+        live, calls = {}, {"alloc": 0, "free": 0, "refused": 0}
+
+        @A.REALLOC
+        def realloc(ptr, size, actual, movable, user):
+            if not ptr:
+                if calls["alloc"] >= limit:
+                    calls["refused"] += 1
+                    return None
+                b = ctypes.create_string_buffer(size)
+                live[ctypes.addressof(b)] = b
+                calls["alloc"] += 1
+                if actual:
+                    actual[0] = size
+                return ctypes.addressof(b)
+            if size == 0:
+                calls["free"] += 1
+                live.pop(ptr, None)
+            return None
+
+        @A.MSIZE
+        def msize(ptr, user):
+            return ctypes.sizeof(live[ptr]) if ptr in live else 0
+
+        api.crnd_set_memory_callbacks(realloc, msize, None)
+        try:
+            ctx = api.crnd_unpack_begin(buf, len(crn))
+        finally:
+            api.crnd_set_memory_callbacks(A.REALLOC(0), A.MSIZE(0), None)
+        if not calls["refused"]:
+            if ctx:  # a GPU is present and the whole context fitted within the limit
+                assert api.crnd_unpack_end(ctx)
+            break  # the parse needs fewer allocations than this limit
+        seen_limits += 1
+        assert not ctx, limit
+        assert cg.last_error() == "out of host memory", (limit, cg.last_error())
+        assert calls["alloc"] == calls["free"] and not live, (limit, calls)
+    assert seen_limits >= 3  # the context, the parsed file and its tables each met a refusal
