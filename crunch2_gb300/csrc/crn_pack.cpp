@@ -18,9 +18,12 @@
 //     keeping the trial whose palette plus index stream codes in the fewest bits.
 // The order changes the file size only, never the decoded blocks.
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
+#include <exception>
 #include <functional>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -145,7 +148,8 @@ struct Huff {
 // A symbol list (model << 16 | symbol) coded behind its models, MSB first, as BitWriter would
 // write it: the accumulator in locals, whole 32-bit words stored into a buffer sized for the
 // longest codes (16 bits a symbol).
-std::vector<uint8_t> code_symbols(const std::vector<uint32_t>& syms, const Huff* models, int nmodels) {
+std::vector<uint8_t> code_symbols(const std::vector<uint32_t>& syms, const Huff* models, int nmodels,
+                                  uint64_t* bits = nullptr) {
   const uint32_t* code[8];
   const uint8_t* len[8];
   for (int k = 0; k < nmodels; k++) {
@@ -171,9 +175,69 @@ std::vector<uint8_t> code_symbols(const std::vector<uint32_t>& syms, const Huff*
     n -= 8;
     *p++ = (uint8_t)(acc >> n);
   }
+  if (bits) *bits = (uint64_t)(p - out.data()) * 8 + n;
   if (n) *p++ = (uint8_t)(acc << (8 - n));
   out.resize((size_t)(p - out.data()));
   return out;
+}
+
+// Appends `bits` bits of a zero-padded MSB-first bit string to an MSB-first stream of out_bits
+// bits (whose last byte is zero-padded as well).
+void append_bits(std::vector<uint8_t>& out, uint64_t& out_bits, const std::vector<uint8_t>& in, uint64_t bits) {
+  const size_t nin = (size_t)((bits + 7) / 8);
+  if (!nin) return;
+  const uint32_t shift = (uint32_t)(out_bits & 7);
+  out.resize((size_t)((out_bits + bits + 7) / 8) + 1);  // one byte of room for the shifted spill
+  uint8_t* o = out.data() + out_bits / 8;
+  if (!shift) {
+    std::memcpy(o, in.data(), nin);
+  } else {
+    for (size_t k = 0; k < nin; k++) {
+      o[k] |= (uint8_t)(in[k] >> shift);
+      o[k + 1] = (uint8_t)(in[k] << (8 - shift));
+    }
+  }
+  out_bits += bits;
+  out.resize((size_t)((out_bits + 7) / 8));
+}
+
+// Runs fn(job, worker) for jobs 0 .. n-1 on up to `threads` threads (worker < threads), taking
+// jobs in order as workers free up. An exception in a job is passed on to the caller once every
+// worker has stopped.
+template <class F>
+void parallel_jobs(size_t n, unsigned threads, F fn) {
+  threads = (unsigned)std::max<size_t>(1, std::min<size_t>(threads, n));
+  if (threads == 1) {
+    for (size_t j = 0; j < n; j++) fn(j, 0u);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::exception_ptr error;
+  std::mutex error_mu;
+  auto work = [&](unsigned w) {
+    try {
+      for (size_t j = next++; j < n; j = next++) fn(j, w);
+    } catch (...) {
+      std::lock_guard<std::mutex> lock(error_mu);
+      if (!error) error = std::current_exception();
+      next = n;
+    }
+  };
+  std::vector<std::thread> pool;
+  try {
+    for (unsigned w = 1; w < threads; w++) pool.emplace_back(work, w);
+  } catch (...) {  // a thread that cannot start: the others take its jobs
+  }
+  work(0);
+  for (auto& t : pool) t.join();
+  if (error) std::rethrow_exception(error);
+}
+
+// worker threads for the writer's parallel steps
+unsigned pack_threads(uint64_t nblocks) {
+  if (nblocks < 16384) return 1;
+  const unsigned hw = std::thread::hardware_concurrency();
+  return std::max(1u, std::min(hw ? hw : 4u, 16u));
 }
 
 // symbol_codec's static model transmission, the inverse of
@@ -726,14 +790,7 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
     std::vector<std::function<void()>> jobs;
     if (colour) { jobs.emplace_back(colour_endpoints); jobs.emplace_back(colour_selectors); }
     if (nalpha) { jobs.emplace_back(alpha_endpoints); jobs.emplace_back(alpha_selectors); }
-    if (nblocks < 16384) {
-      for (auto& j : jobs) j();
-    } else {
-      std::vector<std::thread> t;
-      for (size_t k = 1; k < jobs.size(); k++) t.emplace_back(jobs[k]);
-      jobs[0]();
-      for (auto& x : t) x.join();
-    }
+    parallel_jobs(jobs.size(), pack_threads(nblocks), [&](size_t j, unsigned) { jobs[j](); });
   }
   if (cep.values.size() > (size_t)kMaxSyms || csel.values.size() > (size_t)kMaxSyms ||
       aep.values.size() > (size_t)kMaxSyms || asel.values.size() > (size_t)kMaxSyms) {
@@ -744,9 +801,22 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
   // endpoint delta per component), 1 same endpoints as the previous block in decode order, 2 same
   // as the block above (the faces of a level are one tall image to the decoder's row buffer)
   std::vector<uint8_t> ref(nblocks, 0);
+  // the block streams' work units: runs of whole row pairs (a reference group covers two rows; a
+  // level's faces are one tall image, each face an even number of rows)
+  struct RowRun {
+    uint32_t level, row0, row1;
+  };
+  std::vector<RowRun> runs;
   for (uint32_t l = 0; l < levels; l++) {
-    const Lv& L = lv[l];
-    for (uint32_t row = 0; row < faces * L.H; row++)
+    const uint32_t rows = faces * lv[l].H, step = std::max(2u, (16384u / lv[l].W) & ~1u);
+    for (uint32_t r = 0; r < rows; r += step) runs.push_back(RowRun{l, r, std::min(rows, r + step)});
+  }
+  const unsigned threads = pack_threads(nblocks);
+  // the per-block passes only pay for their threads on large inputs (a 2048 x 2048 mip chain)
+  const unsigned block_threads = nblocks >= (1u << 18) ? threads : 1u;
+  parallel_jobs(runs.size(), block_threads, [&](size_t j, unsigned) {
+    const Lv& L = lv[runs[j].level];
+    for (uint32_t row = runs[j].row0; row < runs[j].row1; row++)
       for (uint32_t x = 0; x < L.W; x++) {
         const uint64_t b = L.first + (uint64_t)row * L.W + x;
         bool left = row || x, top = row != 0;
@@ -757,14 +827,14 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         }
         ref[b] = left ? 1 : top ? 2 : 0;
       }
-  }
+  });
   // palette order. Model 0 = colour (component 0 when present), model 1 = alpha (the rest).
   const int comp_lo[2] = {0, colour ? 1 : 0}, comp_hi[2] = {colour ? 1 : 0, ncomp};
   Palette* ep_pal[2] = {&cep, &aep};
   Palette* sel_pal[2] = {&csel, &asel};
   std::vector<uint32_t> ep_rank[2], sel_rank[2];
   {
-    std::vector<std::thread> workers;
+    std::vector<std::function<void()>> workers;  // per model: the selector order, the endpoint order
     // the endpoint trials of model m: coded size of the palette plus the index deltas
     auto stream_bits = [&](int m, const std::vector<uint32_t>& rank) -> uint64_t {
       const uint32_t n = (uint32_t)rank.size();
@@ -869,26 +939,23 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         const float weights[3] = {0.0f, 1.0f / 6.0f, 0.5f};
         std::vector<uint32_t> trial[4];
         uint64_t bits[4];
-        std::vector<std::thread> tw;
-        // least distance between distinct endpoints: one 6-bit green step (4^2) or one alpha step
-        tw.emplace_back([&] {
-          trial[0] = nearest_chain_comps(u, m ? 1u : 16u);
-          bits[0] = stream_bits(m, trial[0]);
+        static_assert(4000u * 3 / 2 <= 65535u && 4000u <= 10922u, "grow_chain's 16-bit similarity");
+        parallel_jobs(4, threads, [&](size_t t, unsigned) {
+          if (t == 0) {
+            // least distance between distinct endpoints: one 6-bit green step (4^2) or one alpha step
+            trial[0] = nearest_chain_comps(u, m ? 1u : 16u);
+          } else {
+            trial[t] = grow_chain(u, adj, first, (uint32_t)((float)unit * (1.0f + weights[t - 1])), unit, m ? 0 : 3);
+          }
+          bits[t] = stream_bits(m, trial[t]);
         });
-        for (int t = 0; t < 3; t++)
-          tw.emplace_back([&, t] {
-            static_assert(4000u * 3 / 2 <= 65535u && 4000u <= 10922u, "grow_chain's 16-bit similarity");
-            trial[t + 1] = grow_chain(u, adj, first, (uint32_t)((float)unit * (1.0f + weights[t])), unit, m ? 0 : 3);
-            bits[t + 1] = stream_bits(m, trial[t + 1]);
-          });
-        for (auto& w : tw) w.join();
         int best = 0;
         for (int t = 1; t < 4; t++)
           if (bits[t] < bits[best]) best = t;
         ep_rank[m] = std::move(trial[best]);
       });
     }
-    for (auto& w : workers) w.join();
+    parallel_jobs(workers.size(), threads, [&](size_t j, unsigned) { workers[j](); });
   }
   for (int m = 0; m < 2; m++) {
     if (comp_lo[m] == comp_hi[m]) continue;
@@ -900,60 +967,76 @@ extern "C" int64_t crngpu_crn_pack(const uint8_t* blocks, uint32_t width, uint32
         sidx[(size_t)c * nblocks + b] = sel_rank[m][sidx[(size_t)c * nblocks + b]];
       }
   }
-  // block streams: one walk records every level's symbols (model << 16 | symbol) and counts them,
-  // then each level is coded behind the finished models. Models: 0 reference groups, 1 / 2 colour
-  // endpoint deltas / selectors, 3 / 4 alpha endpoint deltas / selectors.
-  std::vector<uint32_t> hist[5];
-  hist[0].assign(256, 0);
-  if (colour) { hist[1].assign(cep.values.size(), 0); hist[2].assign(csel.values.size(), 0); }
-  if (nalpha) { hist[3].assign(aep.values.size(), 0); hist[4].assign(asel.values.size(), 0); }
+  // block streams: each run of rows records its symbols (model << 16 | symbol) and counts them;
+  // then every run is coded behind the finished models and a level's runs are joined. Models:
+  // 0 reference groups, 1 / 2 colour endpoint deltas / selectors, 3 / 4 alpha endpoint deltas /
+  // selectors. An endpoint delta is against the previous block of the level in decode order, so a
+  // run starts from the indices of the block before it.
+  size_t hist_size[5] = {256, 0, 0, 0, 0};
+  if (colour) { hist_size[1] = cep.values.size(); hist_size[2] = csel.values.size(); }
+  if (nalpha) { hist_size[3] = aep.values.size(); hist_size[4] = asel.values.size(); }
+  std::vector<std::vector<uint32_t>> hists((size_t)block_threads * 5);
+  for (unsigned w = 0; w < block_threads; w++)
+    for (int k = 0; k < 5; k++) hists[(size_t)w * 5 + k].assign(hist_size[k], 0);
   const uint32_t pal_n[2] = {(uint32_t)cep.values.size(), (uint32_t)aep.values.size()};
-  std::vector<std::vector<uint32_t>> level_syms(levels);
-  for (uint32_t l = 0; l < levels; l++) {
-    const Lv& L = lv[l];
-    std::vector<uint32_t>& out = level_syms[l];
-    out.reserve((size_t)L.W * L.H * faces * (2 * ncomp + 1));
+  std::vector<std::vector<uint32_t>> run_syms(runs.size());
+  parallel_jobs(runs.size(), block_threads, [&](size_t j, unsigned w) {
+    const RowRun& R = runs[j];
+    const Lv& L = lv[R.level];
+    std::vector<uint32_t>* hist = &hists[(size_t)w * 5];
+    std::vector<uint32_t>& out = run_syms[j];
+    out.reserve((size_t)L.W * (R.row1 - R.row0) * (2 * ncomp + 1));
     uint32_t prev[3] = {0, 0, 0};
-    for (uint32_t f = 0; f < faces; f++)
-      for (uint32_t y = 0; y < L.H; y++) {
-        const uint64_t row = L.first + ((uint64_t)f * L.H + y) * L.W;
-        for (uint32_t x = 0; x < L.W; x++) {
-          const uint64_t b = row + x;
-          if (!(y & 1) && !(x & 1)) {
-            const uint32_t g = ref[b] | (ref[b + L.W] << 2) | (ref[b + 1] << 4) | (ref[b + L.W + 1] << 6);
-            out.push_back(g);
-            hist[0][g]++;
+    const uint64_t start = L.first + (uint64_t)R.row0 * L.W;
+    if (R.row0)
+      for (int c = 0; c < ncomp; c++) prev[c] = eidx[(size_t)c * nblocks + start - 1];
+    for (uint32_t y = R.row0; y < R.row1; y++) {
+      const uint64_t row = L.first + (uint64_t)y * L.W;
+      for (uint32_t x = 0; x < L.W; x++) {
+        const uint64_t b = row + x;
+        if (!(y & 1) && !(x & 1)) {
+          const uint32_t g = ref[b] | (ref[b + L.W] << 2) | (ref[b + 1] << 4) | (ref[b + L.W + 1] << 6);
+          out.push_back(g);
+          hist[0][g]++;
+        }
+        for (int c = 0; c < ncomp; c++) {
+          const int m = (colour && c == 0) ? 0 : 1;
+          const uint32_t e = eidx[(size_t)c * nblocks + b];
+          if (ref[b] == 0) {
+            const uint32_t d = e >= prev[c] ? e - prev[c] : e + pal_n[m] - prev[c];
+            out.push_back(((uint32_t)(1 + 2 * m) << 16) | d);
+            hist[1 + 2 * m][d]++;
           }
-          for (int c = 0; c < ncomp; c++) {
-            const int m = (colour && c == 0) ? 0 : 1;
-            const uint32_t e = eidx[(size_t)c * nblocks + b];
-            if (ref[b] == 0) {
-              const uint32_t d = e >= prev[c] ? e - prev[c] : e + pal_n[m] - prev[c];
-              out.push_back(((uint32_t)(1 + 2 * m) << 16) | d);
-              hist[1 + 2 * m][d]++;
-            }
-            prev[c] = e;
-          }
-          for (int c = 0; c < ncomp; c++) {
-            const int m = (colour && c == 0) ? 0 : 1;
-            const uint32_t sel = sidx[(size_t)c * nblocks + b];
-            out.push_back(((uint32_t)(2 + 2 * m) << 16) | sel);
-            hist[2 + 2 * m][sel]++;
-          }
+          prev[c] = e;
+        }
+        for (int c = 0; c < ncomp; c++) {
+          const int m = (colour && c == 0) ? 0 : 1;
+          const uint32_t sel = sidx[(size_t)c * nblocks + b];
+          out.push_back(((uint32_t)(2 + 2 * m) << 16) | sel);
+          hist[2 + 2 * m][sel]++;
         }
       }
-  }
+    }
+  });
   Huff models[5];
   for (int k = 0; k < 5; k++) {
-    if (hist[k].empty()) continue;
-    ensure_used(hist[k]);
-    models[k].build(hist[k], 16);
+    if (!hist_size[k]) continue;
+    std::vector<uint32_t>& h = hists[k];
+    for (unsigned w = 1; w < block_threads; w++)
+      for (size_t i = 0; i < h.size(); i++) h[i] += hists[(size_t)w * 5 + k][i];
+    ensure_used(h);
+    models[k].build(h, 16);
   }
+  std::vector<std::vector<uint8_t>> run_code(runs.size());
+  std::vector<uint64_t> run_bits(runs.size());
+  parallel_jobs(runs.size(), block_threads, [&](size_t j, unsigned) {
+    run_code[j] = code_symbols(run_syms[j], models, 5, &run_bits[j]);
+    std::vector<uint32_t>().swap(run_syms[j]);
+  });
   std::vector<std::vector<uint8_t>> level_data(levels);
-  for (uint32_t l = 0; l < levels; l++) {
-    level_data[l] = code_symbols(level_syms[l], models, 5);
-    std::vector<uint32_t>().swap(level_syms[l]);
-  }
+  std::vector<uint64_t> level_bits(levels, 0);
+  for (size_t j = 0; j < runs.size(); j++)
+    append_bits(level_data[runs[j].level], level_bits[runs[j].level], run_code[j], run_bits[j]);
   std::vector<uint8_t> pal[4];
   if (colour) {
     pal[0] = pack_colour_endpoints(cep.values);
