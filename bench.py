@@ -56,6 +56,9 @@ METRIC = "DXT1 encode Mtexel/s at matched RMSE, learned vs plain; CRN→DXT1 tra
 L2_FLUSH_BYTES = 256 << 20
 TX_BATCH = 1024  # textures per transcode batch
 QUALITY_NAMES = ["superfast", "fast", "normal", "better", "uber"]  # crn_dxt_quality 0..4
+# DRAM bytes (read, written) per launch of the two plain-encode kernels on this workload, from one
+# ncu capture (dram__bytes_read.sum, dram__bytes_write.sum)
+DXT1_ENCODE_DRAM = {"k_dxt1_seeds": (6.28e6, 0.91e6), "k_dxt1_encode": (13.8e6, 32.7e6)}
 LANE_OPS_PER_EVAL = 27  # uber inner loop per candidate x colour: 15 FFMA, 4 FMNMX, 4 FADD, 2 IADD, 2 IMAD
 
 
@@ -777,7 +780,12 @@ def main():
     executed = evals * LANE_OPS_PER_EVAL / (kernel_ms / 1e3)
     roofline = {"bound": "alu", "kernel": "k_dxt1_encode", "achieved": round(achieved / 1e12, 3),
                 "peak": round(peak_ops / 1e12, 3), "unit": "Tops/s", "frac": round(achieved / peak_ops, 4),
-                "traffic": None, "peak_source": f"SMs x 128 lanes x max SM clock ({peak_kind} clock)",
+                "traffic": DXT1_ENCODE_DRAM["k_dxt1_encode"][0] + DXT1_ENCODE_DRAM["k_dxt1_encode"][1],
+                "traffic_detail": {"read_write_bytes_per_launch": DXT1_ENCODE_DRAM,
+                                   "source": "one ncu capture of the first timed step: dram__bytes_read.sum, "
+                                             "dram__bytes_write.sum; the writes are mostly the L2 write-back of "
+                                             "the 256 MiB flush before the step"},
+                "peak_source": f"SMs x 128 lanes x max SM clock ({peak_kind} clock)",
                 "evals_per_launch": alg_evals, "evals_source": "the reference's evaluate_solution loops on this "
                 "workload, counted by the oracle (tests/golden/encode_work.json)",
                 "evals_executed": evals, "frac_executed": round(executed / peak_ops, 4),
