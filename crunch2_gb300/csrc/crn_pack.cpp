@@ -665,13 +665,19 @@ std::vector<uint32_t> grow_chain(const std::vector<Comps>& u, const Adjacency& a
     const size_t m = id.size();
     if (front_new) similarity(front, sim_f.data(), m);
     if (back_new) similarity(back, sim_b.data(), m);
-    uint64_t best_val = 0;
-    size_t best = 0;
+    // the best entry: the highest score, the lowest id among equal scores, found as the largest key
+    // score << 13 | (8191 - id) in one pass the compiler vectorises. A score is below 2^46: a
+    // similarity below 2^16 times a co-occurrence count plus normaliser below 2^30 (at most two
+    // co-occurrences per block and component, at most 2^23 blocks of 3 components, a normaliser of
+    // at most 8 counts); ids are below kMaxSyms = 2^13.
+    const uint32_t norm = (uint32_t)normaliser;
+    uint64_t top = 0;
     for (size_t i = 0; i < m; i++) {
-      const uint64_t v = (uint64_t)std::max(sim_f[i], sim_b[i]) * ((uint64_t)freq[i] + normaliser) + 1;
-      if (v > best_val || (v == best_val && id[i] < id[best])) { best_val = v; best = i; }
+      const uint64_t score = (uint64_t)std::max(sim_f[i], sim_b[i]) * (uint32_t)(freq[i] + norm) + 1;
+      top = std::max(top, (score << 13) | (uint64_t)(8191u - id[i]));
     }
-    const uint32_t s = id[best];
+    const uint32_t s = 8191u - (uint32_t)(top & 8191u);
+    const size_t best = slot_of[s];
     const uint32_t sf = sim_f[best], sb = sim_b[best], fs = freq[best];
     // co-occurrence of s with each half of the chain, weighted (L-1-2k) by distance k from that end
     const int64_t L = (int64_t)hi - lo + 1;
