@@ -31,6 +31,23 @@ def decode_all(crn, m, port):
     return out
 
 
+# sha256 of each fixture's repacked file: the bytes the straightforward writer (full chain scans,
+# a sorted pair list, heap-built Huffman trees, a bit-at-a-time writer) made; the 2048 x 2048
+# files take the writer's threaded per-block passes.
+REPACK_SHA = {
+    "c1_dxt1_1024": "8785e5dbdbb1736bb0eb17faabd36827f7d0b106c239681165024d911f227bc4",
+    "dxn_xy_2048": "845b938e86a585d14022436505ef6569e08bdc99dc5ee44036435075b96682e8",
+    "dxn_xy_256": "dc625e843abb266b383bb951ffb09627506167f494cb68a8b749995eb17b0d52",
+    "dxt1_100x60": "7f6dc1bca24d403a43bda5b6322171cf94e13ce8db5abfe0648c82e0003c751a",
+    "dxt1_256": "4841a1c0fc306943c725e7244e69ecb6a84d22fc126db61bd708d7a19cf3186e",
+    "dxt1_cube_64": "199b6a3e9ecb619d4aee06f834f82745bb069e4541cd3c4042e503cfcc31baeb",
+    "dxt5_2048": "dbacca76cfc674157a50643a00b728d15adb87c39e9346e26ffdb651920dfb78",
+    "dxt5_256": "612bef535d8160c3cc293aa6093f1ae017d0828f606495b5bd3b00a541a5ebaa",
+    "dxt5_cube_64x32": "2c70b0ff2e7176735e7bcfab53aa69bfed9efa4582419f99fdb5c57a48da1bc3",
+    "dxt5a_256": "2cf8da5070b63919fa29e572f79cc2566633aef6dced07245d4f6fec1b2de0bc",
+}
+
+
 @pytest.mark.parametrize("name", sorted(G.manifest().keys()))
 def test_repacked_fixture_decodes_to_the_same_blocks(cg, name):
     from oracle import port, ref
@@ -49,6 +66,8 @@ def test_repacked_fixture_decodes_to_the_same_blocks(cg, name):
             assert np.array_equal(ref.unpack_level(packed, l, info["bytes"]),
                                   np.concatenate([x.reshape(-1) for x in levels[l]])), (name, l, "reference crnd")
     print(f"{name}: reference .crn {len(crn)} bytes, repacked {len(packed)} bytes")
+    import hashlib
+    assert hashlib.sha256(packed).hexdigest() == REPACK_SHA[name], name
     # palette ordering as crn_comp's: the same blocks code in about the reference's size
     assert len(packed) <= 1.01 * len(crn), (name, len(packed), len(crn))
 
