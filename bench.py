@@ -672,6 +672,29 @@ def main():
     ctx0.unpack_levels(out=d_tx, stream=stream)
     single_lane_ms = timed(lambda: ctx0.unpack_levels(out=d_tx, stream=stream), max(3, args.steps // 4))
     cg.set_decode_split(cg.DECODE_SPLIT_DEFAULT)
+    # a crnlib caller's sequence for one file: crnd_unpack_begin, crnd_unpack_level for every level
+    # in turn, crnd_unpack_end (the C ABI's calls, device destinations), wall time per file
+    lvl_views, o = [], 0
+    for lv in range(ctx0.levels):
+        nb = ctx0.level_bytes(lv)
+        lvl_views.append(d_tx[o:o + nb].view(ctx0.faces, -1))
+        o += nb
+
+    def per_level_file():
+        with cg.unpack_begin(crn) as c:
+            for lv in range(c.levels):
+                c.unpack_level(lv, out=lvl_views[lv], stream=stream)
+
+    for _ in range(args.warmup):
+        per_level_file()
+    torch.cuda.synchronize()
+    reps = max(5, args.steps)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        per_level_file()
+    torch.cuda.synchronize()
+    per_level_ms = (time.perf_counter() - t0) / reps * 1e3
+    per_level_parity = bool((d_tx.cpu().numpy() == ctx0.unpack_levels()).all())
     # the reference's own 2048x2048 DXT5 .crn (12 levels), one texture
     with open(os.path.join(ROOT, "tests", "golden", "crn", "dxt5_2048.crn"), "rb") as fh:
         crn5 = fh.read()
@@ -724,11 +747,15 @@ def main():
                          "path": "crngpu_unpack_batch_launch (graph) + D2H of every level to pinned host memory"},
                  "single_texture": {"ms": round(single_ms, 4), "GB/s": round(tx_bytes / (single_ms / 1e3) / 1e9, 4),
                                     "lane_decoder_ms": round(single_lane_ms, 4),
+                                    "per_level_calls_ms": round(per_level_ms, 4),
+                                    "per_level_calls_parity": per_level_parity,
                                     "dxt5_2048_ms": round(single5_ms, 4),
                                     "dxt5_2048_GB/s": round(single5_bytes / (single5_ms / 1e3) / 1e9, 4),
                                     "path": "ctx.unpack_levels (crngpu_unpack_levels), device destination: levels of "
                                             ">= 256 blocks on k_crn_decode_wide (a CTA per level), the rest on the "
-                                            "lane decoder; lane_decoder_ms: every level on the lane decoder"},
+                                            "lane decoder; lane_decoder_ms: every level on the lane decoder; per_level_calls_ms: "
+                                            "unpack_begin + crngpu_unpack_level per level + unpack_end, wall time "
+                                            "per file (the crnd_unpack_level pattern)"},
                  "expand_roofline": None,
                  "expand_autotune": {"variant": tune_variant, "ms_per_variant": tune_ms,
                                      "variants": "0-11: tile of 1024 << (v >> 1) blocks, DXT1 palettes staged "
@@ -851,6 +878,7 @@ def main():
             "config4_rmse_delta": pick(learned, "config4_eval", "rmse_delta"),
             "transcode_batch_gb_s": transcode["value"], "transcode_single_ms": transcode["single_texture"]["ms"],
             "transcode_single_cpu_1_thread_ms": pick(transcode, "single_texture", "cpu_1_thread_ms"),
+            "transcode_single_per_level_calls_ms": pick(transcode, "single_texture", "per_level_calls_ms"),
             "transcode_dxt5_2048_ms": transcode["single_texture"]["dxt5_2048_ms"],
             "expand_hbm_frac": expand["frac"],
             "mixed_encode_mtexel_s": pick(mixed_batch, "encode", "value"),

@@ -1417,6 +1417,10 @@ struct UnpackContext : HostObject {
   DevBuf d_file, d_models, d_pal, d_jobs, d_records, d_status;
   DevPalettes pal{};
   uint32_t status_host[2] = {0, 0};
+  // every level decoded at minimal pitch by the first unpack_level call (0: not tried yet,
+  // 1: holds every level, 2: not used for this context)
+  DevBuf d_level_cache;
+  int level_cache_state = 0;
 
   uint32_t kind() const { return (uint32_t)file.kind; }
   uint32_t rec_bytes() const { return record_bytes(kind()); }
@@ -1860,6 +1864,54 @@ LevelTask context_task(UnpackContext* c, uint32_t level) {
   return t;
 }
 
+uint64_t levels_bytes(const CrnFile& F, uint32_t first, uint32_t count);
+void levels_tasks(UnpackContext* c, uint32_t first, uint32_t count, uint8_t* out, uint32_t item,
+                  HVec<LevelTask>& tasks);
+
+// crnd_unpack_level is called a level at a time, usually for every level of a file in turn. The
+// first call on a context decodes every level in one plan into a device cache -- the levels'
+// streams decode side by side, so that costs about what the largest level alone does -- and this
+// call and the later ones copy their level out of it. A file with a level the decoder rejects
+// (the error must belong to the level asked for), or whose levels take more than
+// kLevelCacheMax bytes, is decoded a level per call instead.
+constexpr uint64_t kLevelCacheMax = 64ull << 20;
+constexpr int kNoLevelCache = 1;  // not a status: the caller decodes the level itself
+
+int cached_level(UnpackContext* c, uint32_t level, void** dst_faces, uint32_t row_pitch, int mem, cudaStream_t s) {
+  const CrnFile& F = c->file;
+  if (c->level_cache_state == 0) {
+    c->level_cache_state = 2;  // until the decode below succeeds
+    const uint64_t total = levels_bytes(F, 0, F.levels);
+    if (total > kLevelCacheMax) return kNoLevelCache;
+    if (c->d_level_cache.ensure(total) != cudaSuccess) {
+      cudaGetLastError();
+      return kNoLevelCache;
+    }
+    HVec<LevelTask> tasks;
+    levels_tasks(c, 0, F.levels, static_cast<uint8_t*>(c->d_level_cache.ptr), 0, tasks);
+    const int rc = run_levels(c, tasks, s);
+    if (rc == CRNGPU_E_DEVICE) return rc;
+    if (rc != CRNGPU_OK) {
+      clear_error();
+      return kNoLevelCache;
+    }
+    c->level_cache_state = 1;
+  }
+  if (c->level_cache_state != 1) return kNoLevelCache;
+  const LevelInfo& li = F.level[level];
+  const uint32_t minimal = li.blocks_x * F.bytes_per_block;
+  const uint64_t face_bytes = (uint64_t)minimal * li.blocks_y;
+  const uint8_t* src = static_cast<const uint8_t*>(c->d_level_cache.ptr) + levels_bytes(F, 0, level);
+  const cudaMemcpyKind kind = mem == CRNGPU_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  cudaError_t e;
+  // row padding beyond the minimal pitch keeps the caller's bytes, as the decoder leaves it
+  for (uint32_t f = 0; f < F.faces; f++)
+    if ((e = cudaMemcpy2DAsync(dst_faces[f], row_pitch, src + face_bytes * f, minimal, minimal, li.blocks_y, kind, s)) !=
+        cudaSuccess)
+      return cuda_check(e, "copy level");
+  return cuda_check(cudaStreamSynchronize(s), "sync");
+}
+
 // Shared implementation of crngpu_unpack_level / _segmented.
 int unpack_one(UnpackContext* c, const uint8_t* host_src, const uint8_t* dev_src, uint32_t src_size,
                void** dst_faces, uint32_t dst_size, uint32_t row_pitch, uint32_t level, int mem, void* stream) {
@@ -1881,6 +1933,10 @@ int unpack_one(UnpackContext* c, const uint8_t* host_src, const uint8_t* dev_src
   if (F.segmented && !dev_src && !host_src) {
     set_error("segmented file: pass the level data (crngpu_unpack_level_segmented)");
     return CRNGPU_E_PARAM;
+  }
+  if (!dev_src && !host_src) {
+    const int rc = cached_level(c, level, dst_faces, row_pitch, mem, s);
+    if (rc != kNoLevelCache) return rc;
   }
   LevelTask t = context_task(c, level);
   t.pitch = row_pitch;

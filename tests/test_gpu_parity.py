@@ -180,6 +180,33 @@ def test_transcode_decoders_agree_on_corrupt_streams(cg, decode_split, name):
         assert outcome["wide"] == outcome["lane"], (name, trial, outcome)
 
 
+@pytest.mark.parametrize("name", ["dxt1_256", "dxt5_256", "dxt5_cube_64x32"])
+def test_per_level_calls_with_a_corrupt_level(cg, name):
+    """crngpu_unpack_level decodes every level on its first call and serves later calls from
+    that decode; a level the decoder rejects must not take the others with it: with one level's
+    stream overwritten, every other level, asked for in any order, is still bit-exact."""
+    import struct
+    crn = bytearray(G.crn_bytes(name))
+    levels = G.manifest()[name]["levels"]
+    ofs = [struct.unpack(">I", bytes(crn[70 + 4 * l:74 + 4 * l]))[0] for l in range(len(levels))] + [len(crn)]
+    bad = 1
+    crn[ofs[bad]:ofs[bad + 1]] = bytes([0xFF]) * (ofs[bad + 1] - ofs[bad])
+    order = list(range(len(levels)))[::-1]
+    with cg.unpack_begin(bytes(crn)) as ctx:
+        for lvl in order:
+            if lvl == bad:
+                try:
+                    ctx.unpack_level(lvl)
+                except cg.CrnGpuError:
+                    pass
+                continue
+            assert G.sha(ctx.unpack_level(lvl).reshape(-1)) == levels[lvl]["sha256"], (name, lvl)
+    # intact file, levels in a shuffled order, twice over the same context
+    with cg.unpack_begin(G.crn_bytes(name)) as ctx:
+        for lvl in [2, 0, 1] + list(range(len(levels))):
+            assert G.sha(ctx.unpack_level(lvl).reshape(-1)) == levels[lvl]["sha256"], (name, lvl)
+
+
 @pytest.mark.parametrize("use_graph", [False, True])
 def test_transcode_batch_mixed_formats(cg, use_graph):
     """Every fixture (DXT1, DXT5, DXN, DXT5A, cube maps, NPOT) in one batch, each twice with its
