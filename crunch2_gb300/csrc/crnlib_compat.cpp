@@ -803,8 +803,9 @@ namespace {
 crnd::crn_texture_info wrapper_info(void* src, unsigned int src_size) {
   crnd::crn_texture_info ti;
   if (!crnd::crnd_get_texture_info(src, src_size, &ti)) {
-    std::memset(&ti, 0, sizeof(ti));
-    ti.m_struct_size = sizeof(ti);
+    ti.m_width = ti.m_height = ti.m_levels = ti.m_faces = ti.m_bytes_per_block = 0;
+    ti.m_userdata0 = ti.m_userdata1 = 0;
+    ti.m_format = static_cast<crn_format>(0);
   }
   return ti;
 }
